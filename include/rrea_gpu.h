@@ -1,0 +1,199 @@
+/*
+ * rrea_gpu.h — C-ABI of the GB300 kinetic step for the RREA overlay.
+ *
+ * This library replaces the per-timestep e-/e+/photon transport that the
+ * reference runs inside
+ *   void rrea::warpx::RreaParticleInteraction::Apply(WarpX&, RreaWarpXCoupling&,
+ *        rrea::RreaInteractionTables const&, int step, amrex::Real time_s,
+ *        amrex::Real dt_s)
+ * (native_amrex_rrea/warpx_overlay/Source/Rrea/RreaParticleInteraction.H:1609-1623,
+ *  body in RreaParticleInteraction.cpp:12-62).  The overlay keeps that C++
+ * signature; its body gathers the species tiles, calls rrea_gpu_apply_electrons(), and
+ * raises amrex::Abort on a non-OK status, which preserves the fail-closed
+ * contract of the reference (every guard aborts the whole step before any
+ * side effect is committed).
+ *
+ * Plain pointers and sizes only; no C++ or torch types cross this boundary.
+ * Every entry point returns an rrea_gpu_status; none aborts or traps.
+ */
+#ifndef RREA_GPU_H
+#define RREA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    RREA_GPU_OK = 0,
+    RREA_GPU_ERR_ARGUMENT = 1,        /* bad pointer, size or configuration */
+    RREA_GPU_ERR_TABLES = 2,          /* table bundle missing or violates its contract */
+    RREA_GPU_ERR_CUDA = 3,            /* a CUDA runtime call failed */
+    RREA_GPU_ERR_RANGE = 4,           /* a table query left its certified range */
+    RREA_GPU_ERR_GEOMETRY = 5,        /* a particle state outside the domain or non-finite */
+    RREA_GPU_ERR_RNG_OVERFLOW = 6,    /* packed RNG index / event ordinal overflow */
+    RREA_GPU_ERR_GUARD = 7,           /* strict optical-depth subcycle guard */
+    RREA_GPU_ERR_CAPACITY = 8,        /* an output buffer is too small for this step */
+    RREA_GPU_ERR_INVALID_STATE = 9,   /* non-finite rate, invalid hazard selection */
+    RREA_GPU_ERR_NOT_READY = 10       /* tables, field or particles not uploaded */
+} rrea_gpu_status;
+
+/* Species ordinals, as RreaSecondarySpecies
+ * (RreaParticleInteraction.H:28-32). */
+enum { RREA_SPECIES_ELECTRON = 0, RREA_SPECIES_POSITRON = 1, RREA_SPECIES_PHOTON = 2 };
+
+/*
+ * Per-run transport configuration.  Field meanings follow
+ * RreaParticleInteractionConfig (RreaParticleInteraction.H:1576-1596) and the
+ * coupling accessors LowEnergyCutoffEv / PhotonCutoffEv / RngSeed
+ * (RreaWarpXCoupling.H:240-250).  rrea_gpu_default_config() fills the
+ * reference defaults.
+ */
+typedef struct {
+    /* geometry: RZ domain [r_lo, r_hi) x [z_lo, z_hi), cells nr x nz */
+    double r_lo, r_hi, z_lo, z_hi;
+    int32_t nr, nz;
+    int32_t periodic_z;
+    int32_t strict_transport_guards;
+    /* material: uniform density ratio rho/rho_table (rho_table = 1.20479 kg/m^3) */
+    double density_ratio;
+    /* cuts; photon_cutoff_eV is forced to the tables' brems cutoff */
+    double low_energy_cutoff_eV;
+    double photon_cutoff_eV;
+    /* substep controls */
+    double max_optical_depth_per_substep;
+    uint64_t max_subcycles;
+    double max_gs_collisions_per_substep;
+    double gs_total_collision_cap;
+    double max_field_impulse_fraction;
+    double field_impulse_floor_eV;
+    uint64_t rng_seed;
+    int32_t debug_disable_hard_moller;
+    int32_t reserved0;
+} rrea_gpu_config;
+
+typedef struct rrea_gpu_ctx rrea_gpu_ctx;
+
+/* Reference defaults (RreaParticleInteraction.H:1576-1596; tracking cut 1 keV). */
+void rrea_gpu_default_config(rrea_gpu_config* cfg);
+
+/* Creates a context on the current CUDA device.  Allocates device scratch
+ * sized for `capacity` particles per species. */
+rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rrea_gpu_ctx** out);
+rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx);
+
+/* Loads transport_physics.json and its RREATBL containers
+ * (replaces RreaInteractionTables::Load, S/RreaInteractionTables.cpp:1659). */
+rrea_gpu_status rrea_gpu_load_tables(rrea_gpu_ctx* ctx, const char* transport_physics_json);
+
+/* Sets the Maxwell (scattered) field and the static ambient field on the
+ * replicated TM-RZ vectors (I/RreaMaxwellTMRZ.H:61-85): er (nr+1)*nz,
+ * ez nr*(nz+1), btheta (nr+1)*(nz+1); amb_er/amb_ez as er/ez.  Host pointers. */
+rrea_gpu_status rrea_gpu_set_field(rrea_gpu_ctx* ctx, const double* er, const double* ez,
+                                   const double* btheta, const double* amb_er,
+                                   const double* amb_ez);
+
+/*
+ * One species tile in host memory, as the overlay's WarpX tile holds it
+ * (PIdx r, z, theta, ux, uy, uz, w and the runtime rrea_prev_* components,
+ * RreaWarpXCoupling.cpp:111-149).  id > 0 marks a valid particle; the step
+ * negates the id of every particle it removes.
+ */
+typedef struct {
+    int64_t n;
+    double* r;
+    double* z;
+    double* theta;
+    double* ux;
+    double* uy;
+    double* uz;
+    double* w;
+    double* prev_r;
+    double* prev_z;
+    double* prev_theta;
+    double* prev_ux;
+    double* prev_uy;
+    double* prev_uz;
+    int64_t* id;
+    int32_t* cpu;
+} rrea_gpu_tile;
+
+/* One secondary produced by the step (RreaSecondaryParticle,
+ * RreaParticleInteraction.H:612-635), in the reference's deterministic
+ * order (parent index, then creation order within the parent). */
+typedef struct {
+    int32_t species;
+    int32_t process;
+    int32_t root_species;
+    int32_t pad;
+    int64_t parent_index;
+    uint64_t root_key;
+    uint64_t lineage;
+    double x, y, z, dir_x, dir_y, dir_z, weight, energy_eV, birth_fraction;
+} rrea_gpu_secondary;
+
+/*
+ * Drop-in for the electron phase of RreaParticleInteraction::Apply
+ * (TransportStep::ApplyElectronTransport, RreaElectronTransport.cpp:9-902):
+ * copies the tile to HBM, transports every valid electron through one outer
+ * step dt on the GPU, copies the tile back, and returns the secondaries in
+ * deterministic order.  `secondaries` may be NULL to only count them.
+ */
+rrea_gpu_status rrea_gpu_apply_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, int32_t step,
+                                         double time_s, double dt_s,
+                                         rrea_gpu_secondary* secondaries,
+                                         int64_t secondary_capacity, int64_t* n_secondaries);
+
+/* Cell-source grids (S/RreaEventAccumulator.cpp:129-164 field ids 0..4:
+ * low-energy electrons, positive ions, direct negative ions, ionization
+ * count, energy loss), each nr*nz, i + nr*j.  Accumulated since the last
+ * rrea_gpu_reset_sources(). */
+rrea_gpu_status rrea_gpu_download_sources(rrea_gpu_ctx* ctx, double* out5);
+rrea_gpu_status rrea_gpu_reset_sources(rrea_gpu_ctx* ctx);
+
+/* Per-particle diagnostics of the last electron step: substeps used,
+ * hazard draws made and terminal disposition (0 survive, 1 escape,
+ * 2 demotion, 3 zero-weight skip, -1 not transported). */
+rrea_gpu_status rrea_gpu_download_diagnostics(rrea_gpu_ctx* ctx, int64_t n, uint64_t* subcycles,
+                                              uint64_t* events, int32_t* disposition);
+
+/* Copies the last error message (NUL-terminated, truncated to size). */
+void rrea_gpu_last_error(const rrea_gpu_ctx* ctx, char* buf, size_t size);
+
+/*
+ * Resident engine mode: the electron tile stays in HBM across steps.  In this
+ * mode the captured pre-push state (rrea_prev_*) IS the current state, which
+ * is what CaptureRreaPositionsBeforePush (RreaWarpXCoupling.cpp:151-208)
+ * establishes before WarpX's own charged push, whose kick the transport step
+ * discards (RreaTransportStep.H:705-820).
+ *   stage:  host tile -> HBM (prev_* are ignored)
+ *   step:   one outer step on the resident tile, no host copies
+ *   fetch:  HBM -> host tile (r, z, theta, ux, uy, uz, id)
+ */
+rrea_gpu_status rrea_gpu_stage_electrons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile);
+rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s,
+                                                 int64_t* n_secondaries);
+rrea_gpu_status rrea_gpu_fetch_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile);
+
+/* Launch shape of the transport kernel (threads per block in {32..128}, a
+ * multiple of 32; resident blocks per SM) and whether per-particle
+ * diagnostics are written. */
+rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm,
+                                    int32_t diagnostics);
+
+/* Counts and device time of the last step: particles transported (valid on
+ * entry), secondaries produced, and the transport kernel's duration measured
+ * with CUDA events on the context stream. */
+rrea_gpu_status rrea_gpu_last_step_stats(rrea_gpu_ctx* ctx, int64_t* transported, int64_t* secondaries,
+                                         double* kernel_ms);
+
+/* The context's CUDA stream (a cudaStream_t), for timing with events. */
+rrea_gpu_status rrea_gpu_stream(rrea_gpu_ctx* ctx, void** stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RREA_GPU_H */

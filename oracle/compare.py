@@ -1,0 +1,89 @@
+"""ORACLE: test infrastructure only.
+
+Parity comparison of one GPU electron phase against the oracle on the same
+input tile.  Discrete results (dispositions, substep and hazard-draw counts,
+validity, secondary keys) must match exactly; FP64 state within 1e-12
+relative (positions with a 1e-12 x domain-size floor); cell-source grids,
+which the GPU accumulates with atomics in nondeterministic order, within
+1e-12 of each grid's largest cell.
+"""
+import numpy as np
+
+from . import oracle as _oracle
+from rrea_feedback_warpx_amrex_geant4_gb300.workloads import copy_tile
+
+RTOL = 1.0e-12
+
+
+def _close(a, b, rtol, atol):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b) <= atol + rtol * np.maximum(np.abs(a), np.abs(b))
+
+
+def run_pair(ctx, cfg, field, arr, step, dt_s):
+    """Runs GPU (apply mode) and oracle on copies of `arr`; returns both."""
+    g_arr = copy_tile(arr)
+    o_arr = copy_tile(arr)
+    ctx.reset_sources()
+    g_sec = ctx.apply_electrons(g_arr, step, dt_s)
+    n = arr["id"].shape[0]
+    g_sub, g_ev, g_disp = ctx.diagnostics(n)
+    g_cells = ctx.sources()
+    o = _oracle.electron_step(cfg, field, step, dt_s, o_arr)
+    return (g_arr, g_sec, g_sub, g_ev, g_disp, g_cells), (o_arr, o)
+
+
+def compare(cfg, gpu, orc, domain_scale):
+    """Returns a list of mismatch descriptions (empty when parity holds)."""
+    g_arr, g_sec, g_sub, g_ev, g_disp, g_cells = gpu
+    o_arr, o = orc
+    problems = []
+    if not np.array_equal(g_disp, o["disposition"]):
+        bad = np.nonzero(g_disp != o["disposition"])[0]
+        problems.append(f"disposition differs at {bad[:10].tolist()} ({len(bad)} particles)")
+    if not np.array_equal(g_sub, o["subcycles"]):
+        bad = np.nonzero(g_sub != o["subcycles"])[0]
+        problems.append(f"subcycles differ at {bad[:10].tolist()} ({len(bad)})")
+    if not np.array_equal(g_ev, o["events"]):
+        bad = np.nonzero(g_ev != o["events"])[0]
+        problems.append(f"hazard draws differ at {bad[:10].tolist()} ({len(bad)})")
+    if not np.array_equal(g_arr["id"], o_arr["id"]):
+        problems.append("validity (id sign) differs")
+    alive = (o_arr["id"] > 0) & (o["disposition"] == 0)
+    atol_pos = RTOL * domain_scale
+    for name, atol in (("z", atol_pos), ("r", atol_pos)):
+        ok = _close(g_arr[name][alive], o_arr[name][alive], RTOL, atol)
+        if not ok.all():
+            problems.append(f"{name} differs for {(~ok).sum()} survivors")
+    gx, gy = g_arr["r"] * np.cos(g_arr["theta"]), g_arr["r"] * np.sin(g_arr["theta"])
+    ox, oy = o_arr["r"] * np.cos(o_arr["theta"]), o_arr["r"] * np.sin(o_arr["theta"])
+    for name, a, b in (("x", gx, ox), ("y", gy, oy)):
+        ok = _close(a[alive], b[alive], RTOL, atol_pos * 4)
+        if not ok.all():
+            problems.append(f"{name} differs for {(~ok).sum()} survivors")
+    umag = np.sqrt(o_arr["ux"] ** 2 + o_arr["uy"] ** 2 + o_arr["uz"] ** 2)
+    moved = o["disposition"] <= 1
+    moved &= o["disposition"] >= 0
+    for name in ("ux", "uy", "uz"):
+        ok = _close(g_arr[name][moved], o_arr[name][moved], RTOL, RTOL * umag[moved])
+        if not ok.all():
+            problems.append(f"{name} differs for {(~ok).sum()} particles")
+    os_ = o["secondaries"]
+    if len(g_sec) != len(os_):
+        problems.append(f"secondary count {len(g_sec)} vs oracle {len(os_)}")
+    else:
+        for key in ("species", "process", "parent_index", "root_key", "lineage", "root_species"):
+            if not np.array_equal(g_sec[key], os_[key]):
+                problems.append(f"secondary {key} differs")
+        for key, atol in (("x", atol_pos), ("y", atol_pos), ("z", atol_pos), ("dir_x", RTOL), ("dir_y", RTOL),
+                          ("dir_z", RTOL), ("weight", 0.0), ("energy_eV", 0.0), ("birth_fraction", RTOL)):
+            ok = _close(g_sec[key], os_[key], RTOL, atol)
+            if not ok.all():
+                problems.append(f"secondary {key} differs for {(~ok).sum()}")
+    for f in range(5):
+        scale = max(np.abs(o["cells"][f]).max(), 1e-300)
+        ok = _close(g_cells[f], o["cells"][f], 0.0, RTOL * scale * 16)
+        if not ok.all():
+            problems.append(f"cell source field {f} differs in {(~ok).sum()} cells")
+    return problems

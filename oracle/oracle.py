@@ -1,0 +1,173 @@
+"""ORACLE: test infrastructure only.
+
+ctypes wrapper over oracle/liboracle.so, the CPU restatement of the
+reference kinetic step.  Used by tests/, __graft_entry__.smoke() and the CPU
+baseline leg of bench.py as the checker; the shipped GPU library never loads
+it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .build import build_oracle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+_lib = None
+
+
+class RreaGpuConfig(ctypes.Structure):
+    """Mirror of rrea_gpu_config (include/rrea_gpu.h)."""
+
+    _fields_ = [
+        ("r_lo", ctypes.c_double), ("r_hi", ctypes.c_double),
+        ("z_lo", ctypes.c_double), ("z_hi", ctypes.c_double),
+        ("nr", ctypes.c_int32), ("nz", ctypes.c_int32),
+        ("periodic_z", ctypes.c_int32), ("strict_transport_guards", ctypes.c_int32),
+        ("density_ratio", ctypes.c_double),
+        ("low_energy_cutoff_eV", ctypes.c_double), ("photon_cutoff_eV", ctypes.c_double),
+        ("max_optical_depth_per_substep", ctypes.c_double), ("max_subcycles", ctypes.c_uint64),
+        ("max_gs_collisions_per_substep", ctypes.c_double), ("gs_total_collision_cap", ctypes.c_double),
+        ("max_field_impulse_fraction", ctypes.c_double), ("field_impulse_floor_eV", ctypes.c_double),
+        ("rng_seed", ctypes.c_uint64),
+        ("debug_disable_hard_moller", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+    ]
+
+
+class RreaGpuTile(ctypes.Structure):
+    """Mirror of rrea_gpu_tile (include/rrea_gpu.h)."""
+
+    _fields_ = [("n", ctypes.c_int64)] + [
+        (name, ctypes.POINTER(ctypes.c_double))
+        for name in ("r", "z", "theta", "ux", "uy", "uz", "w",
+                     "prev_r", "prev_z", "prev_theta", "prev_ux", "prev_uy", "prev_uz")
+    ] + [("id", ctypes.POINTER(ctypes.c_int64)), ("cpu", ctypes.POINTER(ctypes.c_int32))]
+
+
+SECONDARY_DTYPE = np.dtype([
+    ("species", "<i4"), ("process", "<i4"), ("root_species", "<i4"), ("pad", "<i4"),
+    ("parent_index", "<i8"), ("root_key", "<u8"), ("lineage", "<u8"),
+    ("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("dir_x", "<f8"), ("dir_y", "<f8"), ("dir_z", "<f8"),
+    ("weight", "<f8"), ("energy_eV", "<f8"), ("birth_fraction", "<f8"),
+])
+
+TILE_FIELDS = ("r", "z", "theta", "ux", "uy", "uz", "w",
+               "prev_r", "prev_z", "prev_theta", "prev_ux", "prev_uy", "prev_uz")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle()
+        _lib = ctypes.CDLL(path)
+        d = ctypes.POINTER(ctypes.c_double)
+        _lib.oracle_load_tables.argtypes = [ctypes.c_char_p]
+        _lib.oracle_primitive.argtypes = [ctypes.c_int, d, ctypes.c_int64, d]
+        _lib.oracle_rng.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_int64,
+                                    ctypes.POINTER(ctypes.c_uint64), d]
+        _lib.oracle_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+        _lib.oracle_electron_step.argtypes = [ctypes.POINTER(RreaGpuConfig), d, d, d, d, d, ctypes.c_int32,
+                                              ctypes.c_double, ctypes.POINTER(RreaGpuTile)]
+        _lib.oracle_counts.argtypes = [ctypes.POINTER(ctypes.c_int64)] * 3
+        _lib.oracle_secondaries.argtypes = [ctypes.c_void_p]
+        _lib.oracle_sources.argtypes = [d]
+        _lib.oracle_segments.argtypes = [d]
+        _lib.oracle_diagnostics.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                                            ctypes.POINTER(ctypes.c_int32)]
+        _lib.oracle_cell_sources.argtypes = [d]
+    return _lib
+
+
+class OracleFailure(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"oracle status {code}: {message}")
+        self.code = code
+
+
+def _check(rc):
+    if rc != 0:
+        buf = ctypes.create_string_buffer(1024)
+        lib().oracle_last_error(buf, 1024)
+        raise OracleFailure(rc, buf.value.decode())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+_loaded_path = None
+
+
+def load_tables(path):
+    global _loaded_path
+    if _loaded_path == path:
+        return
+    _check(lib().oracle_load_tables(path.encode()))
+    _loaded_path = path
+
+
+def primitive(which, inputs, out_cols):
+    inputs = np.ascontiguousarray(inputs, dtype=np.float64)
+    n = inputs.shape[0]
+    out = np.zeros((n, out_cols), dtype=np.float64)
+    _check(lib().oracle_primitive(which, _dptr(inputs), n, _dptr(out)))
+    return out
+
+
+def rng(keys):
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    n = keys.shape[0]
+    counter = np.zeros(n, dtype=np.uint64)
+    uniform = np.zeros(n, dtype=np.float64)
+    lib().oracle_rng(keys.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n,
+                     counter.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _dptr(uniform))
+    return counter, uniform
+
+
+def make_tile_struct(arrays):
+    """arrays: dict of contiguous numpy arrays (TILE_FIELDS f8, id i8, cpu i4)."""
+    t = RreaGpuTile()
+    t.n = arrays["id"].shape[0]
+    for name in TILE_FIELDS:
+        setattr(t, name, _dptr(arrays[name]))
+    t.id = arrays["id"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    t.cpu = arrays["cpu"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    return t
+
+
+def electron_step(cfg, field, step, dt_s, arrays):
+    """Runs the oracle electron phase in place on `arrays` (numpy tile).
+    Returns dict with secondaries, sources, segments, diagnostics, cells."""
+    cfg = as_config(cfg)
+    t = make_tile_struct(arrays)
+    _check(lib().oracle_electron_step(ctypes.byref(cfg), _dptr(field["er"]), _dptr(field["ez"]),
+                                      _dptr(field["bt"]), _dptr(field["amb_er"]), _dptr(field["amb_ez"]),
+                                      step, dt_s, ctypes.byref(t)))
+    n_sec, n_src, n_seg = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    lib().oracle_counts(ctypes.byref(n_sec), ctypes.byref(n_src), ctypes.byref(n_seg))
+    sec = np.zeros(n_sec.value, dtype=SECONDARY_DTYPE)
+    if n_sec.value:
+        lib().oracle_secondaries(sec.ctypes.data)
+    src = np.zeros((n_src.value, 7))
+    if n_src.value:
+        lib().oracle_sources(_dptr(src))
+    seg = np.zeros((n_seg.value, 11))
+    if n_seg.value:
+        lib().oracle_segments(_dptr(seg))
+    n = t.n
+    sub = np.zeros(n, dtype=np.uint64)
+    ev = np.zeros(n, dtype=np.uint64)
+    disp = np.zeros(n, dtype=np.int32)
+    lib().oracle_diagnostics(sub.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                             ev.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                             disp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    cells = np.zeros(5 * cfg.nr * cfg.nz)
+    lib().oracle_cell_sources(_dptr(cells))
+    return {"secondaries": sec, "sources": src, "segments": seg, "subcycles": sub, "events": ev,
+            "disposition": disp, "cells": cells.reshape(5, cfg.nz, cfg.nr)}
+
+
+def as_config(cfg):
+    """Copies any rrea_gpu_config-layout ctypes structure into the oracle's."""
+    return RreaGpuConfig.from_buffer_copy(bytes(cfg))

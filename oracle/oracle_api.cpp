@@ -1,0 +1,180 @@
+// ORACLE — test infrastructure only.  C entry points of the CPU restatement
+// for ctypes (oracle/oracle.py).  Never linked into the shipped library.
+#include "oracle_core.hpp"
+
+#include <cstring>
+#include <memory>
+#include <string>
+
+namespace {
+
+std::unique_ptr<rrea_host::TableSet> g_tables;
+oracle::StepOutputs g_out;
+oracle::CellSources g_cells;
+std::string g_error;
+
+int guard(std::exception const& e)
+{
+    g_error = e.what();
+    if (auto const* oe = dynamic_cast<oracle::OracleError const*>(&e)) {
+        return oe->code;
+    }
+    return RREA_GPU_ERR_TABLES;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_load_tables(char const* path)
+{
+    try {
+        auto t = std::make_unique<rrea_host::TableSet>();
+        t->Load(path);
+        g_tables = std::move(t);
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+void oracle_last_error(char* buf, size_t size)
+{
+    if (size == 0) return;
+    std::strncpy(buf, g_error.c_str(), size - 1);
+    buf[size - 1] = '\0';
+}
+
+int oracle_primitive(int which, double const* in, int64_t n, double* out)
+{
+    if (!g_tables) return RREA_GPU_ERR_NOT_READY;
+    try {
+        return oracle::RunPrimitive(*g_tables, which, in, n, out);
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+void oracle_rng(uint64_t const* keys, int64_t n, uint64_t* counter, double* uniform)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t const* k = keys + 5 * i;
+        counter[i] = oracle::rng_counter(k[0], k[1], k[2], k[3], k[4]);
+        uniform[i] = oracle::rng_uniform(k[0], k[1], k[2], k[3], k[4]);
+    }
+}
+
+// Arena export so tests can compare the host loader against the device copy.
+int64_t oracle_arena_size() { return g_tables ? static_cast<int64_t>(g_tables->arena().size()) : 0; }
+
+int oracle_electron_step(rrea_gpu_config const* cfg, double const* er, double const* ez, double const* bt,
+                         double const* amb_er, double const* amb_ez, int32_t step, double dt_s,
+                         rrea_gpu_tile const* tile)
+{
+    if (!g_tables) return RREA_GPU_ERR_NOT_READY;
+    try {
+        oracle::FieldGrid fg;
+        fg.nr = cfg->nr;
+        fg.nz = cfg->nz;
+        fg.dr = (cfg->r_hi - cfg->r_lo) / cfg->nr;
+        fg.dz = (cfg->z_hi - cfg->z_lo) / cfg->nz;
+        fg.z_lo = cfg->z_lo;
+        std::size_t const ner = static_cast<std::size_t>(cfg->nr + 1) * cfg->nz;
+        std::size_t const nez = static_cast<std::size_t>(cfg->nr) * (cfg->nz + 1);
+        std::size_t const nbt = static_cast<std::size_t>(cfg->nr + 1) * (cfg->nz + 1);
+        fg.er.assign(er, er + ner);
+        fg.ez.assign(ez, ez + nez);
+        fg.bt.assign(bt, bt + nbt);
+        fg.amb_er.assign(amb_er, amb_er + ner);
+        fg.amb_ez.assign(amb_ez, amb_ez + nez);
+        oracle::ChargedTile t;
+        t.n = tile->n;
+        t.r = tile->r; t.z = tile->z; t.theta = tile->theta;
+        t.ux = tile->ux; t.uy = tile->uy; t.uz = tile->uz; t.w = tile->w;
+        t.prev_r = tile->prev_r; t.prev_z = tile->prev_z; t.prev_theta = tile->prev_theta;
+        t.prev_ux = tile->prev_ux; t.prev_uy = tile->prev_uy; t.prev_uz = tile->prev_uz;
+        t.id = tile->id;
+        t.cpu = tile->cpu;
+        g_out.clear();
+        oracle::ApplyElectronTransport(*g_tables, *cfg, fg, step, dt_s, t, g_out);
+        g_cells.nr = cfg->nr;
+        g_cells.nz = cfg->nz;
+        for (auto& f : g_cells.f) f.assign(static_cast<std::size_t>(cfg->nr) * cfg->nz, 0.0);
+        oracle::DepositSources(*cfg, g_out.sources, cfg->low_energy_cutoff_eV, g_cells);
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+void oracle_counts(int64_t* n_sec, int64_t* n_src, int64_t* n_seg)
+{
+    *n_sec = static_cast<int64_t>(g_out.secondaries.size());
+    *n_src = static_cast<int64_t>(g_out.sources.size());
+    *n_seg = static_cast<int64_t>(g_out.segments.size());
+}
+
+// Secondaries in the rrea_gpu_secondary layout.
+void oracle_secondaries(rrea_gpu_secondary* out)
+{
+    for (std::size_t i = 0; i < g_out.secondaries.size(); ++i) {
+        auto const& s = g_out.secondaries[i];
+        rrea_gpu_secondary& o = out[i];
+        o.species = s.species;
+        o.process = s.process;
+        o.root_species = s.root_species;
+        o.pad = 0;
+        o.parent_index = s.parent_index;
+        o.root_key = s.root_key;
+        o.lineage = s.lineage;
+        o.x = s.x; o.y = s.y; o.z = s.z;
+        o.dir_x = s.dx; o.dir_y = s.dy; o.dir_z = s.dz;
+        o.weight = s.w;
+        o.energy_eV = s.energy;
+        o.birth_fraction = s.birth;
+    }
+}
+
+// Sources as rows (kind, r, z, w, secondary_energy, energy_loss, parent).
+void oracle_sources(double* out)
+{
+    for (std::size_t i = 0; i < g_out.sources.size(); ++i) {
+        auto const& s = g_out.sources[i];
+        double* o = out + 7 * i;
+        o[0] = s.kind; o[1] = s.r; o[2] = s.z; o[3] = s.w; o[4] = s.secondary_energy; o[5] = s.energy_loss;
+        o[6] = static_cast<double>(s.parent_index);
+    }
+}
+
+// Segments as rows (kind, a0..a6, channel, faces, parent).
+void oracle_segments(double* out)
+{
+    for (std::size_t i = 0; i < g_out.segments.size(); ++i) {
+        auto const& s = g_out.segments[i];
+        double* o = out + 11 * i;
+        o[0] = s.kind;
+        for (int c = 0; c < 7; ++c) o[1 + c] = s.a[c];
+        o[8] = static_cast<double>(s.channel);
+        o[9] = s.faces;
+        o[10] = static_cast<double>(s.parent_index);
+    }
+}
+
+void oracle_diagnostics(uint64_t* subcycles, uint64_t* events, int32_t* disposition)
+{
+    for (std::size_t i = 0; i < g_out.subcycles.size(); ++i) {
+        subcycles[i] = g_out.subcycles[i];
+        events[i] = g_out.events[i];
+        disposition[i] = g_out.disposition[i];
+    }
+}
+
+void oracle_cell_sources(double* out5)
+{
+    std::size_t const n = static_cast<std::size_t>(g_cells.nr) * g_cells.nz;
+    for (int f = 0; f < 5; ++f) {
+        for (std::size_t i = 0; i < n; ++i) out5[f * n + i] = g_cells.f[f].empty() ? 0.0 : g_cells.f[f][i];
+    }
+}
+
+}  // extern "C"

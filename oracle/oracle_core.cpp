@@ -1,0 +1,1716 @@
+// ORACLE — test infrastructure only (see oracle_core.hpp).
+#include "oracle_core.hpp"
+
+#include <functional>
+#include <sstream>
+
+namespace oracle {
+
+namespace {
+
+using rrea_host::TableSet;
+
+// ======================================================================
+// Transport path: I/RreaTransportPath.H:13-73, S/RreaTransportPath.cpp:13-295
+// ======================================================================
+struct Piece {
+    double begin = 0.0, end = 0.0, length = 0.0, shift = 0.0;
+};
+
+struct Path {
+    double sx = 0, sy = 0, sz = 0, ex = 0, ey = 0, ez = 0;
+    double full = 0, in_begin = 0, in_end = 0, in_length = 0;
+    bool exits = false, periodic = false;
+    double rlo = 0, rhi = 0, zlo = 0, zhi = 0;
+    std::vector<Piece> pieces;
+
+    // S/RreaTransportPath.cpp:13-27
+    double WrapZ(double z) const
+    {
+        if (!periodic) return z;
+        double const len = zhi - zlo;
+        if (!(len > 0.0)) return z;
+        double w = std::fmod(z - zlo, len);
+        if (w < 0.0) w += len;
+        return zlo + w;
+    }
+    // S/RreaTransportPath.cpp:29-40
+    bool OutsideCertified(double r, double z) const
+    {
+        if (!std::isfinite(r) || !std::isfinite(z)) return true;
+        if (r < rlo || r >= rhi) return true;
+        return !periodic && (z < zlo || z >= zhi);
+    }
+    // S/RreaTransportPath.cpp:42-52
+    void PointAtFull(double f, double& x, double& y, double& z) const
+    {
+        f = std::max(0.0, std::min(1.0, f));
+        x = sx + f * (ex - sx);
+        y = sy + f * (ey - sy);
+        z = WrapZ(sz + f * (ez - sz));
+    }
+    // S/RreaTransportPath.cpp:54-71
+    void PointAtPiece(Piece const& p, double f, double& x, double& y, double& z) const
+    {
+        f = std::max(p.begin, std::min(p.end, f));
+        x = sx + f * (ex - sx);
+        y = sy + f * (ey - sy);
+        z = sz + f * (ez - sz) + p.shift;
+        z = std::max(zlo, std::min(zhi, z));
+    }
+};
+
+// S/RreaTransportPath.cpp:73-295
+Path ClipRz(double r0, double th0, double z0, double r1, double th1, double z1, double rlo,
+            double rhi, double zlo, double zhi, bool periodic)
+{
+    auto finite = [](double v) { return std::isfinite(v); };
+    if (!finite(r0) || !finite(th0) || !finite(z0) || !finite(r1) || !finite(th1) || !finite(z1)
+        || r0 < 0.0 || r1 < 0.0 || rlo < 0.0 || !(rlo < rhi) || !(zlo < zhi)) {
+        fail(RREA_GPU_ERR_GEOMETRY, "ClipRzTransportPath received invalid geometry or coordinates");
+    }
+    Path p;
+    p.periodic = periodic;
+    p.rlo = rlo;
+    p.rhi = rhi;
+    p.zlo = zlo;
+    p.zhi = zhi;
+    p.sx = r0 * std::cos(th0);
+    p.sy = r0 * std::sin(th0);
+    p.sz = z0;
+    p.ex = r1 * std::cos(th1);
+    p.ey = r1 * std::sin(th1);
+    p.ez = z1;
+    double const dx = p.ex - p.sx, dy = p.ey - p.sy, dz = p.ez - p.sz;
+    p.full = std::sqrt(dx * dx + dy * dy + dz * dz);
+    p.in_begin = 0.0;
+    double const scale = std::max(1.0, std::max(rhi, std::max(std::abs(zlo), std::abs(zhi))));
+    double const tol = 64.0 * kEps * scale;
+    if (r0 < rlo - tol || r0 > rhi + tol || z0 < zlo - tol || z0 > zhi + tol) {
+        fail(RREA_GPU_ERR_GEOMETRY, "previous particle position is outside the physical RZ domain");
+    }
+    double exit_fraction = 1.0;
+    auto keep = [&](double c) {
+        if (c >= 0.0 && c < exit_fraction) exit_fraction = c;
+    };
+    if (!periodic) {
+        if (dz > 0.0) keep((zhi - z0) / dz);
+        else if (dz < 0.0) keep((zlo - z0) / dz);
+    }
+    double const a = dx * dx + dy * dy;
+    if (a > 0.0) {
+        double const b = 2.0 * (p.sx * dx + p.sy * dy);
+        auto cyl = [&](double radius, bool outer) {
+            double const c = p.sx * p.sx + p.sy * p.sy - radius * radius;
+            double const disc = b * b - 4.0 * a * c;
+            if (disc < 0.0) return;
+            double const root = std::sqrt(std::max(disc, 0.0));
+            double const inv2a = 0.5 / a;
+            double const roots[2] = {(-b - root) * inv2a, (-b + root) * inv2a};
+            for (double cand : roots) {
+                if (cand <= 0.0 || cand > 1.0) continue;
+                double const deriv = 2.0 * a * cand + b;
+                bool const leaves = outer ? deriv > 0.0 : deriv < 0.0;
+                if (leaves) keep(cand);
+            }
+        };
+        cyl(rhi, true);
+        if (rlo > 0.0) cyl(rlo, false);
+    }
+    p.in_end = std::max(0.0, std::min(1.0, exit_fraction));
+    p.in_length = p.full * (p.in_end - p.in_begin);
+    p.exits = p.in_end < 1.0 - 64.0 * kEps;
+
+    std::vector<double> bp = {p.in_begin, p.in_end};
+    if (periodic && std::abs(dz) > 0.0 && p.in_end > p.in_begin) {
+        long double const lz0 = static_cast<long double>(z0);
+        long double const lz1 = lz0 + static_cast<long double>(dz) * static_cast<long double>(p.in_end);
+        long double const lzlo = static_cast<long double>(zlo);
+        long double const period = static_cast<long double>(zhi - zlo);
+        long double const low = std::min(lz0, lz1), high = std::max(lz0, lz1);
+        long double const first_ld = std::floor((low - lzlo) / period) + 1.0L;
+        long double const last_ld = std::ceil((high - lzlo) / period) - 1.0L;
+        if (last_ld - first_ld + 1.0L > 1000000.0L) {
+            fail(RREA_GPU_ERR_GEOMETRY, "periodic path crosses more than 1,000,000 seams");
+        }
+        long long const first = static_cast<long long>(first_ld);
+        long long const last = static_cast<long long>(last_ld);
+        for (long long image = first; image <= last; ++image) {
+            long double const seam = lzlo + static_cast<long double>(image) * period;
+            double const frac = static_cast<double>((seam - lz0) / static_cast<long double>(dz));
+            double const ftol = 128.0 * kEps * std::max(1.0, std::abs(frac));
+            if (frac > p.in_begin + ftol && frac < p.in_end - ftol) bp.push_back(frac);
+        }
+    }
+    std::sort(bp.begin(), bp.end());
+    bp.erase(std::unique(bp.begin(), bp.end(),
+                         [](double l, double r) {
+                             return std::abs(l - r)
+                                 <= 128.0 * kEps * std::max(1.0, std::max(std::abs(l), std::abs(r)));
+                         }),
+             bp.end());
+    double const period_m = zhi - zlo;
+    for (std::size_t i = 1; i < bp.size(); ++i) {
+        double const b0 = bp[i - 1], e0 = bp[i];
+        if (!(e0 > b0)) continue;
+        double const mid = 0.5 * (b0 + e0);
+        double const mid_z = z0 + mid * dz;
+        double shift = 0.0;
+        if (periodic) {
+            double const image = std::floor((mid_z - zlo) / period_m);
+            shift = -image * period_m;
+        }
+        p.pieces.push_back(Piece{b0, e0, p.full * (e0 - b0), shift});
+    }
+    return p;
+}
+
+// ======================================================================
+// Tables: S/RreaInteractionTables.cpp
+// ======================================================================
+struct Tables {
+    TableSet const& t;
+    RreaArenaIndex const& ix;
+    explicit Tables(TableSet const& ts) : t(ts), ix(ts.index()) {}
+
+    // RreaInteractionTable::Interpolate, S/RreaInteractionTables.cpp:1580-1630
+    double interpolate(int which, double q) const
+    {
+        RreaTable1DIndex const& h = ix.hot[which];
+        double const* x = t.at(h.x);
+        double const* y = t.at(h.y);
+        double const* lx = t.at(h.lx);
+        double const* ly = t.at(h.ly);
+        int const n = h.n;
+        if (!std::isfinite(q) || q < x[0] || q > x[n - 1]) {
+            std::ostringstream m;
+            m.precision(17);
+            m << "interaction table " << which << " query " << q << " eV outside certified range";
+            fail(RREA_GPU_ERR_RANGE, m.str());
+        }
+        double const* up = std::lower_bound(x, x + n, q);
+        if (up == x) return y[0];
+        if (up == x + n) return y[n - 1];
+        int const hi = static_cast<int>(up - x);
+        int const lo = hi - 1;
+        if (x[hi] == q) return y[hi];
+        if (h.mode == RREA_INTERP_LINEAR) {
+            double const tt = (q - x[lo]) / (x[hi] - x[lo]);
+            return y[lo] + tt * (y[hi] - y[lo]);
+        }
+        double const tt = (std::log(q) - lx[lo]) / (lx[hi] - lx[lo]);
+        bool const pos = y[lo] > 0.0 && y[hi] > 0.0;
+        if (h.mode == RREA_INTERP_LOGX_LINEAR || (h.mode == RREA_INTERP_LOGLOG_ZERO_THRESHOLD && !pos)) {
+            return y[lo] + tt * (y[hi] - y[lo]);
+        }
+        if (!pos) fail(RREA_GPU_ERR_INVALID_STATE, "loglog_linear requires positive bracket");
+        return std::exp(ly[lo] + tt * (ly[hi] - ly[lo]));
+    }
+
+    // S/RreaInteractionTables.cpp:624-648
+    static double semilogx(double const* x, double const* lx, double const* y, int n, double q)
+    {
+        if (n < 2) return n ? y[0] : 0.0;
+        if (!std::isfinite(q) || q < x[0] || q > x[n - 1]) {
+            fail(RREA_GPU_ERR_RANGE, "elastic-table query outside its inclusive energy range");
+        }
+        if (q == x[0]) return y[0];
+        if (q == x[n - 1]) return y[n - 1];
+        double const* up = std::lower_bound(x, x + n, q);
+        int const hi = static_cast<int>(up - x);
+        int const lo = hi - 1;
+        if (x[hi] == q) return y[hi];
+        double const tt = (std::log(q) - lx[lo]) / (lx[hi] - lx[lo]);
+        return y[lo] + tt * (y[hi] - y[lo]);
+    }
+
+    static double mfp_from_inverse(double inv)
+    {
+        // S/RreaInteractionTables.cpp:110-119
+        if (!std::isfinite(inv) || inv < 0.0) {
+            fail(RREA_GPU_ERR_INVALID_STATE, "process inverse length must be finite and nonnegative");
+        }
+        return inv > 0.0 ? 1.0 / inv : 1.0e99;
+    }
+
+    void require_charged(double e) const
+    {
+        // S/RreaInteractionTables.cpp:2241-2264
+        if (!std::isfinite(e) || !(e >= ix.charged_min_eV && e <= ix.charged_max_eV)) {
+            std::ostringstream m;
+            m.precision(17);
+            m << "schema-6 charged sampler energy " << e << " eV outside the certified range";
+            fail(RREA_GPU_ERR_RANGE, m.str());
+        }
+    }
+
+    // :2382-2392, :2655-2664
+    double ElectronCollisionLoss(double e, double dr) const { return interpolate(RREA_T_E_COLLISION, e) * dr; }
+    double ElectronSoftRadiativeDrag(double e, double dr) const { return interpolate(RREA_T_E_SOFT_RAD, e) * dr; }
+    // :2394-2412
+    double ElectronHardMollerMeanFreePath(double e, double dr) const
+    {
+        double const inv = interpolate(RREA_T_E_HARD_MOLLER, e);
+        if (ix.hard_moller_threshold_eV > 0.0 && e <= 2.0 * ix.hard_moller_threshold_eV) return 1.0e99;
+        return mfp_from_inverse(inv * dr);
+    }
+    // :2666-2676
+    double ElectronBremsstrahlungMeanFreePath(double e, double dr) const
+    {
+        return mfp_from_inverse(interpolate(RREA_T_E_TRACKED_BREMS, e) * dr);
+    }
+    // :2414-2440
+    double ElectronHardMollerEnergyLoss(double e, double dr) const
+    {
+        RreaTable1DIndex const& h = ix.hot[RREA_T_E_HARD_MOLLER];
+        double const inv = interpolate(RREA_T_E_HARD_MOLLER, e);
+        if (!(inv > 0.0)) return 0.0;
+        double const mean = semilogx(t.at(h.x), t.at(h.lx), t.at(ix.hard_moller_mean_secondary), h.n, e);
+        if (!(mean > 0.0)) return 0.0;
+        return mean * inv * dr;
+    }
+    // :1071-1110
+    double mean_conditional(int which, double e) const
+    {
+        RreaCondCdfIndex const& ci = ix.cdf[which];
+        double const* prim = t.at(ci.primary);
+        double const* start = t.at(ci.start);
+        double const* u = t.at(ci.u);
+        double const* v = t.at(ci.v);
+        auto group_mean = [&](int g) {
+            int const b = static_cast<int>(start[g]), en = static_cast<int>(start[g + 1]);
+            double mean = u[b] * v[b];
+            for (int i = b + 1; i < en; ++i) mean += 0.5 * (v[i - 1] + v[i]) * (u[i] - u[i - 1]);
+            mean += (1.0 - u[en - 1]) * v[en - 1];
+            return mean;
+        };
+        if (e < prim[0] || e > prim[ci.ng - 1]) {
+            fail(RREA_GPU_ERR_RANGE, "conditional-CDF mean query outside its range");
+        }
+        double const* up = std::lower_bound(prim, prim + ci.ng, e);
+        if (up == prim) return group_mean(0);
+        if (up == prim + ci.ng) return group_mean(ci.ng - 1);
+        int const hi = static_cast<int>(up - prim);
+        if (prim[hi] == e) return group_mean(hi);
+        int const lo = hi - 1;
+        double const y0 = group_mean(lo), y1 = group_mean(hi);
+        double const tt = (std::log(e) - std::log(prim[lo])) / (std::log(prim[hi]) - std::log(prim[lo]));
+        return y0 > 0.0 && y1 > 0.0 ? std::exp(std::log(y0) + tt * (std::log(y1) - std::log(y0)))
+                                    : y0 + tt * (y1 - y0);
+    }
+    // :2678-2696
+    double ElectronTrackedBremsEnergyLoss(double e, double dr) const
+    {
+        double const inv = interpolate(RREA_T_E_TRACKED_BREMS, e) * dr;
+        if (!(inv > 0.0)) return 0.0;
+        return inv * mean_conditional(RREA_C_BREMS_E, e);
+    }
+    // :2298-2324 (only the two rates the channel gates read)
+    void ElectronGateRates(double e, double& moller_inv, double& brems_inv) const
+    {
+        if (!(e >= ix.charged_min_eV && e <= ix.charged_max_eV)) {
+            fail(RREA_GPU_ERR_RANGE, "schema-6 electron energy outside the certified range");
+        }
+        interpolate(RREA_T_E_COLLISION, e);
+        interpolate(RREA_T_E_SOFT_RAD, e);
+        moller_inv = interpolate(RREA_T_E_HARD_MOLLER, e);
+        brems_inv = interpolate(RREA_T_E_TRACKED_BREMS, e);
+        interpolate(RREA_T_E_ELASTIC_TRANSPORT, e);
+    }
+    // :2477-2502
+    double ElasticMeanFreePath(int species, double e, double dr) const
+    {
+        RreaElasticIndex const& el = ix.elastic[species];
+        return semilogx(t.at(el.x), t.at(el.lx), t.at(el.mfp), el.n, e) / dr;
+    }
+    double ScreeningEta(int species, double e) const
+    {
+        RreaElasticIndex const& el = ix.elastic[species];
+        return semilogx(t.at(el.x), t.at(el.lx), t.at(el.eta), el.n, e);
+    }
+    // :807-827
+    static void log_bracket(double const* g, int n, double q, int& i, double& frac)
+    {
+        int const last = n - 1;
+        if (!std::isfinite(q) || q < g[0] || q > g[last]) {
+            fail(RREA_GPU_ERR_RANGE, "elastic-angle query outside its tabulated range");
+        }
+        if (q == g[0]) { i = 0; frac = 0.0; return; }
+        if (q == g[last]) { i = last - 1; frac = 1.0; return; }
+        int lo = 0, hi = last;
+        while (hi - lo > 1) {
+            int const m = (lo + hi) / 2;
+            if (g[m] <= q) lo = m; else hi = m;
+        }
+        i = lo;
+        double const llo = std::log(g[lo]), lhi = std::log(g[hi]);
+        if (lhi == llo) { frac = (q == g[lo]) ? 0.0 : 1.0; return; }
+        frac = (std::log(q) - llo) / (lhi - llo);
+    }
+    // :831-891
+    double sample_gs_angle(RreaAngleIndex const& a, double e, double n, double u) const
+    {
+        int const np = a.np, nu = a.nu;
+        int ie = 0, ip = 0;
+        double te = 0.0, tn = 0.0;
+        log_bracket(t.at(a.e), a.ne, e, ie, te);
+        log_bracket(t.at(a.p), a.np, n, ip, tn);
+        double const* omc = t.at(a.omc);
+        double const* cu = t.at(a.u);
+        auto cos_at_node = [&](int iu) {
+            auto val = [&](int ei, int pi) { return omc[(static_cast<std::size_t>(ei) * np + pi) * nu + iu]; };
+            double const la = std::log(val(ie, ip));
+            double const lb = std::log(val(ie + 1, ip));
+            double const lc = std::log(val(ie, ip + 1));
+            double const ld = std::log(val(ie + 1, ip + 1));
+            double const lxx = (1 - te) * (1 - tn) * la + te * (1 - tn) * lb + (1 - te) * tn * lc + te * tn * ld;
+            return 1.0 - std::exp(lxx);
+        };
+        auto omc_at = [&](int iu) { return std::max(1.0 - cos_at_node(iu), std::numeric_limits<double>::min()); };
+        int const first = 1, last = nu - 2;
+        double one_minus_cos;
+        if (last <= first) {
+            one_minus_cos = omc_at(first);
+        } else if (u <= cu[first]) {
+            double const d1 = omc_at(first), d2 = omc_at(first + 1);
+            double const u1 = cu[first], u2 = cu[first + 1];
+            double const slope = std::log(d2 / d1) / std::log(u2 / u1);
+            double const ueff = std::max(u, u1 * 1.0e-6);
+            one_minus_cos = d1 * std::exp(slope * std::log(ueff / u1));
+        } else if (u >= cu[last]) {
+            one_minus_cos = omc_at(last);
+        } else {
+            int lo = first, hi = last;
+            while (hi - lo > 1) {
+                int const m = (lo + hi) / 2;
+                if (cu[m] <= u) lo = m; else hi = m;
+            }
+            double const d0 = omc_at(lo), d1 = omc_at(hi);
+            double const fu = std::log(u / cu[lo]) / std::log(cu[hi] / cu[lo]);
+            one_minus_cos = d0 * std::exp(fu * std::log(d1 / d0));
+        }
+        double const c = 1.0 - std::min(2.0, one_minus_cos);
+        return std::min(1.0, std::max(-1.0, c));
+    }
+    // :2504-2544
+    double SampleGsCosTheta(int species, double e, double n, double u) const
+    {
+        require_charged(e);
+        if (!std::isfinite(u) || u < 0.0 || u > 1.0) fail(RREA_GPU_ERR_INVALID_STATE, "GS cdf query not in [0,1]");
+        bool const use_gs = e <= ix.gs_wentzel_transition_eV;
+        RreaAngleIndex const& a = use_gs ? ix.gs[species] : ix.wentzel[species];
+        double const* eg = t.at(a.e);
+        if (e < eg[0] || e > eg[a.ne - 1]) fail(RREA_GPU_ERR_RANGE, "GS energy outside the model branch");
+        if (!std::isfinite(n) || n < ix.gs_few_collision_threshold) {
+            fail(RREA_GPU_ERR_INVALID_STATE, "GS path n below the multiple-scattering branch");
+        }
+        if (n >= ix.gs_isotropic_above_n) return 2.0 * u - 1.0;
+        return sample_gs_angle(a, e, n, u);
+    }
+    // :2546-2560
+    double SampleSingleElasticCosTheta(int species, double e, double cdf_u) const
+    {
+        require_charged(e);
+        double const eta = ScreeningEta(species, e);
+        double const u = std::min(std::max(cdf_u, 0.0), 1.0 - 1.0e-15);
+        return 1.0 - 2.0 * eta * u / (1.0 + eta - u);
+    }
+    // :2584-2653
+    double SampleMollerSecondaryEnergy(double e, double u) const
+    {
+        require_charged(e);
+        return rrea_host::HostSampleConditional(t, RREA_C_MOLLER, e, u, true);
+    }
+    // :2698-2712
+    double SampleBremsstrahlungPhotonEnergy(double e, double u) const
+    {
+        require_charged(e);
+        return rrea_host::HostSampleConditional(t, RREA_C_BREMS_E, e, u, false);
+    }
+    // :2714-2760
+    double SampleBremsstrahlungCosTheta(double e, double cdf_u) const
+    {
+        require_charged(e);
+        cdf_u = std::max(0.0, std::min(1.0, cdf_u));
+        if (cdf_u == 0.0) return 1.0;
+        if (cdf_u == 1.0) return -1.0;
+        double constexpr a = 0.625;
+        auto g2 = [](double x) {
+            if (x < 1.0e-3) {
+                return x * x * (0.5 + x * (-1.0 / 3.0 + x * (1.0 / 8.0 + x * (-1.0 / 30.0 + x * (1.0 / 144.0)))));
+            }
+            return -std::expm1(-x) - x * std::exp(-x);
+        };
+        auto mix = [&](double uu) { return 0.25 * g2(a * uu) + 0.75 * g2(3.0 * a * uu); };
+        double const umax = 2.0 * (1.0 + e / kMeC2);
+        double const target = cdf_u * mix(umax);
+        double lo = 0.0, hi = umax;
+        for (int it = 0; it < 60; ++it) {
+            double const mid = 0.5 * (lo + hi);
+            if (mix(mid) < target) lo = mid; else hi = mid;
+        }
+        double const f = 0.5 * (lo + hi) / umax;
+        return 1.0 - 2.0 * f * f;
+    }
+};
+
+// ======================================================================
+// Kinematics: O/RreaChargedInterleave.H, I/RreaLorentzPush.H,
+// I/RreaSeedSchedule.H:31-43, O/RreaParticleInteraction.H:92-105, 1494-1506
+// ======================================================================
+double proper_velocity_from_kinetic(double k)
+{
+    if (k <= 0.0) return 0.0;
+    double const g = 1.0 + k / kMeC2;
+    return kC * std::sqrt(std::max(g * g - 1.0, 0.0));
+}
+double kinetic_from_proper_velocity(double ux, double uy, double uz)
+{
+    double const u2 = ux * ux + uy * uy + uz * uz;
+    double const g = std::sqrt(1.0 + u2 / (kC * kC));
+    return u2 * kMeC2 / ((kC * kC) * (g + 1.0));
+}
+double charged_speed(double k)
+{
+    if (!std::isfinite(k) || k < 0.0) return std::numeric_limits<double>::quiet_NaN();
+    double const g = 1.0 + k / kMeC2;
+    double const b2 = std::max(0.0, 1.0 - 1.0 / (g * g));
+    return kC * std::sqrt(b2);
+}
+void normalize(double& x, double& y, double& z)
+{
+    double const n = std::sqrt(x * x + y * y + z * z);
+    if (n <= 0.0) { x = 0.0; y = 0.0; z = 1.0; return; }
+    x /= n; y /= n; z /= n;
+}
+void transverse_basis(double dx, double dy, double dz, double& b1x, double& b1y, double& b1z, double& b2x,
+                      double& b2y, double& b2z)
+{
+    normalize(dx, dy, dz);
+    double rx = 0.0, ry = 0.0, rz = 1.0;
+    if (std::abs(dz) > 0.9) { rx = 1.0; rz = 0.0; }
+    b1x = ry * dz - rz * dy;
+    b1y = rz * dx - rx * dz;
+    b1z = rx * dy - ry * dx;
+    normalize(b1x, b1y, b1z);
+    b2x = dy * b1z - dz * b1y;
+    b2y = dz * b1x - dx * b1z;
+    b2z = dx * b1y - dy * b1x;
+    normalize(b2x, b2y, b2z);
+}
+void cone_direction(double ax, double ay, double az, double cos_t, double u_phi, double& ox, double& oy,
+                    double& oz)
+{
+    normalize(ax, ay, az);
+    double b1x, b1y, b1z, b2x, b2y, b2z;
+    transverse_basis(ax, ay, az, b1x, b1y, b1z, b2x, b2y, b2z);
+    cos_t = std::min(1.0, std::max(-1.0, cos_t));
+    double const sin_t = std::sqrt(std::max(0.0, 1.0 - cos_t * cos_t));
+    double const phi = kTwoPi * u_phi;
+    double const cp = std::cos(phi), sp = std::sin(phi);
+    ox = ax * cos_t + sin_t * (cp * b1x + sp * b2x);
+    oy = ay * cos_t + sin_t * (cp * b1y + sp * b2y);
+    oz = az * cos_t + sin_t * (cp * b1z + sp * b2z);
+    normalize(ox, oy, oz);
+}
+int poisson_capped(double mean, double u, int kmax)
+{
+    if (mean <= 0.0) return 0;
+    double p = std::exp(-mean);
+    double cum = p;
+    int k = 0;
+    while (u > cum && k < kmax) {
+        ++k;
+        p *= mean / static_cast<double>(k);
+        cum += p;
+    }
+    return k;
+}
+double unit_cycle(double u)
+{
+    u -= std::floor(u);
+    return u < 0.0 ? u + 1.0 : u;
+}
+double moller_secondary_cos(double kp, double ks)
+{
+    kp = std::max(kp, 0.0);
+    ks = std::max(ks, 0.0);
+    if (kp <= 0.0 || ks <= 0.0) return 1.0;
+    double const v = ks * (kp + 2.0 * kMeC2) / (kp * (ks + 2.0 * kMeC2));
+    return std::sqrt(std::min(1.0, std::max(0.0, v)));
+}
+double moller_primary_cos(double kp, double ks)
+{
+    double const scat = std::max(0.0, kp - ks);
+    if (kp <= 0.0 || scat <= 0.0) return 1.0;
+    double const v = scat * (kp + 2.0 * kMeC2) / (kp * (scat + 2.0 * kMeC2));
+    return std::sqrt(std::min(1.0, std::max(0.0, v)));
+}
+void moller_lab_directions(double px, double py, double pz, double kp, double ks, double u_az, double& opx,
+                           double& opy, double& opz, double& osx, double& osy, double& osz)
+{
+    normalize(px, py, pz);
+    u_az = unit_cycle(u_az);
+    cone_direction(px, py, pz, moller_secondary_cos(kp, ks), u_az, osx, osy, osz);
+    cone_direction(px, py, pz, moller_primary_cos(kp, ks), unit_cycle(u_az + 0.5), opx, opy, opz);
+}
+void photon_recoil(double k0, double eg, double gx, double gy, double gz, double& cx, double& cy, double& cz)
+{
+    eg = std::max(eg, 0.0);
+    if (k0 <= 0.0 || eg <= 0.0) return;
+    normalize(cx, cy, cz);
+    normalize(gx, gy, gz);
+    double const p0 = std::sqrt(std::max(0.0, k0 * (k0 + 2.0 * kMeC2)));
+    double const px = p0 * cx - eg * gx, py = p0 * cy - eg * gy, pz = p0 * cz - eg * gz;
+    double const n = std::sqrt(px * px + py * py + pz * pz);
+    if (n > 0.0) {
+        cx = px / n; cy = py / n; cz = pz / n;
+        normalize(cx, cy, cz);
+    }
+}
+
+struct FieldRange {
+    double work = 0, ex = 0, ey = 0, ez = 0, bx = 0, by = 0, bz = 0, length = 0;
+};
+
+// O/RreaChargedInterleave.H:100-138 + I/RreaLorentzPush.H:21-46
+void half_kick(FieldRange const& f, double half_dt, double q, double& k, double& dx, double& dy, double& dz)
+{
+    double const umag = proper_velocity_from_kinetic(k);
+    double const s = q * (kC * kC / kMeC2) * half_dt;
+    double const uxm = umag * dx + s * f.ex;
+    double const uym = umag * dy + s * f.ey;
+    double const uzm = umag * dz + s * f.ez;
+    double const gamma = std::sqrt(1.0 + (uxm * uxm + uym * uym + uzm * uzm) / (kC * kC));
+    double const tx = s * f.bx / (2.0 * gamma), ty = s * f.by / (2.0 * gamma), tz = s * f.bz / (2.0 * gamma);
+    double const t2 = tx * tx + ty * ty + tz * tz;
+    double const sx = 2.0 * tx / (1.0 + t2), sy = 2.0 * ty / (1.0 + t2), sz = 2.0 * tz / (1.0 + t2);
+    double const ppx = uxm + uym * tz - uzm * ty;
+    double const ppy = uym + uzm * tx - uxm * tz;
+    double const ppz = uzm + uxm * ty - uym * tx;
+    double const ux = uxm + ppy * sz - ppz * sy;
+    double const uy = uym + ppz * sx - ppx * sz;
+    double const uz = uzm + ppx * sy - ppy * sx;
+    double const norm = std::sqrt(ux * ux + uy * uy + uz * uz);
+    if (norm > 0.0 && std::isfinite(norm)) {
+        dx = ux / norm; dy = uy / norm; dz = uz / norm;
+    }
+    k = std::max(0.0, k + 0.5 * f.work);
+}
+
+// ======================================================================
+// Field gather: S/RreaAmrexAdvance.cpp:511-579, I/RreaFieldGatherStencil.H
+// ======================================================================
+struct Gather {
+    FieldGrid const& fg;
+    rrea_gpu_config const& cfg;
+    double cell_er(int i, int j) const
+    {
+        std::size_t const lo = static_cast<std::size_t>(i) + static_cast<std::size_t>(fg.nr + 1) * j;
+        std::size_t const hi = static_cast<std::size_t>(i + 1) + static_cast<std::size_t>(fg.nr + 1) * j;
+        return 0.5 * ((fg.er[lo] + fg.amb_er[lo]) + (fg.er[hi] + fg.amb_er[hi]));
+    }
+    double cell_ez(int i, int j) const
+    {
+        std::size_t const lo = static_cast<std::size_t>(i) + static_cast<std::size_t>(fg.nr) * j;
+        std::size_t const hi = static_cast<std::size_t>(i) + static_cast<std::size_t>(fg.nr) * (j + 1);
+        return 0.5 * ((fg.ez[lo] + fg.amb_ez[lo]) + (fg.ez[hi] + fg.amb_ez[hi]));
+    }
+    double bt(int i, int j) const
+    {
+        return fg.bt[static_cast<std::size_t>(i) + static_cast<std::size_t>(fg.nr + 1) * j];
+    }
+    void at(double r, double z, double& er, double& ez, double& bth) const
+    {
+        bool const periodic = cfg.periodic_z != 0;
+        double const fx = (r - cfg.r_lo) / fg.dr + 0.0 - 0.5;
+        double const fz = (z - cfg.z_lo) / fg.dz + 0.0 - 0.5;
+        int const ir0 = static_cast<int>(std::floor(fx));
+        int const iz0 = static_cast<int>(std::floor(fz));
+        double const tx = fx - static_cast<double>(ir0);
+        double const tz = fz - static_cast<double>(iz0);
+        int const i0 = std::max(0, std::min(fg.nr - 1, ir0));
+        int const i1 = std::max(0, std::min(fg.nr - 1, ir0 + 1));
+        int j0 = periodic ? iz0 : std::max(0, std::min(fg.nz - 1, iz0));
+        int j1 = periodic ? iz0 + 1 : std::max(0, std::min(fg.nz - 1, iz0 + 1));
+        if (periodic) {
+            j0 = (j0 + fg.nz) % fg.nz;
+            j1 = (j1 + fg.nz) % fg.nz;
+        }
+        auto bil = [&](double f00, double f01, double f10, double f11) {
+            return (1.0 - tx) * ((1.0 - tz) * f00 + tz * f01) + tx * ((1.0 - tz) * f10 + tz * f11);
+        };
+        double const first_center = cfg.r_lo + 0.5 * fg.dr;
+        double const axis = r >= first_center ? 1.0 : std::max(0.0, (r - cfg.r_lo) / (0.5 * fg.dr));
+        er = bil(cell_er(i0, j0), cell_er(i0, j1), cell_er(i1, j0), cell_er(i1, j1)) * axis;
+        ez = bil(cell_ez(i0, j0), cell_ez(i0, j1), cell_ez(i1, j0), cell_ez(i1, j1));
+        // MaxwellBthetaAt, S/RreaAmrexAdvance.cpp:511-530
+        if (r <= 0.0) {
+            bth = 0.0;
+        } else {
+            double const fr = std::clamp(r / fg.dr, 0.0, static_cast<double>(fg.nr));
+            double const fzz = std::clamp((z - fg.z_lo) / fg.dz, 0.0, static_cast<double>(fg.nz));
+            int const a0 = std::min(static_cast<int>(std::floor(fr)), fg.nr - 1);
+            int const b0 = std::min(static_cast<int>(std::floor(fzz)), fg.nz - 1);
+            double const tr = fr - a0, tzz = fzz - b0;
+            bth = (1.0 - tr) * ((1.0 - tzz) * bt(a0, b0) + tzz * bt(a0, b0 + 1))
+                + tr * ((1.0 - tzz) * bt(a0 + 1, b0) + tzz * bt(a0 + 1, b0 + 1));
+        }
+    }
+};
+
+// O/RreaPathFieldWork.H:57-150 with I/RreaGaussLegendre8.H:24-60
+FieldRange path_field_work(Gather const& g, Path const& path, double q, double begin, double end)
+{
+    FieldRange res;
+    if (!(path.full > 0.0)) return res;
+    begin = std::max(path.in_begin, begin);
+    end = std::min(path.in_end, end);
+    if (!(end > begin)) return res;
+    double const pdx = (path.ex - path.sx) / path.full;
+    double const pdy = (path.ey - path.sy) / path.full;
+    double const pdz = (path.ez - path.sz) / path.full;
+    static long double const kGl2 = 0.577350269189625764509148780501957L;
+    for (Piece const& piece : path.pieces) {
+        double const pb = std::max(begin, piece.begin);
+        double const pe = std::min(end, piece.end);
+        if (!(pe > pb)) continue;
+        auto node = [&](double f, std::array<double, 7>& o) {
+            double x, y, z;
+            path.PointAtPiece(piece, f, x, y, z);
+            double const r = std::hypot(x, y);
+            double rad = 0.0, rc = 1.0, rs = 0.0;
+            if (r > 0.0) {
+                rad = (pdx * x + pdy * y) / r;
+                rc = x / r;
+                rs = y / r;
+            }
+            double er, ez, bth;
+            g.at(r, z, er, ez, bth);
+            double const work = q * (er * rad + ez * pdz) * 1.0;
+            if (!std::isfinite(work) || !std::isfinite(er) || !std::isfinite(ez) || !std::isfinite(bth)) {
+                fail(RREA_GPU_ERR_INVALID_STATE, "substep field-impulse gather is non-finite");
+            }
+            o = {work, er * rc, er * rs, ez, -bth * rs, bth * rc, 0.0};
+        };
+        double const mid = 0.5 * (pb + pe);
+        double const half = 0.5 * (pe - pb);
+        double const off = half * static_cast<double>(kGl2);
+        std::array<double, 7> below, above;
+        node(mid - off, below);
+        node(mid + off, above);
+        std::array<double, 7> integ;
+        for (int c = 0; c < 7; ++c) integ[c] = half * (below[c] + above[c]);
+        res.work += path.full * integ[0];
+        res.ex += path.full * integ[1];
+        res.ey += path.full * integ[2];
+        res.ez += path.full * integ[3];
+        res.bx += path.full * integ[4];
+        res.by += path.full * integ[5];
+        res.bz += path.full * integ[6];
+        res.length += path.full * (pe - pb);
+    }
+    if (res.length > 0.0) {
+        res.ex /= res.length; res.ey /= res.length; res.ez /= res.length;
+        res.bx /= res.length; res.by /= res.length; res.bz /= res.length;
+    }
+    return res;
+}
+
+// ======================================================================
+// Material path: O/RreaMaterialPath.H (uniform density profile)
+// ======================================================================
+struct Interval {
+    double begin = 0, end = 0, length = 0, density = 1.0;
+};
+double positive_or(double v, double fb) { return v > 0.0 ? v : fb; }
+
+// :87-114 with TransportDensityRatioAtZ = the uniform configured ratio
+std::vector<Interval> build_intervals(Path const& path, double density_ratio, double fallback)
+{
+    std::vector<Interval> out;
+    for (Piece const& piece : path.pieces) {
+        if (!(piece.length > 0.0)) continue;
+        // integrate_density_piece_m (:60-85): midpoint rule
+        double dl = 0.0;
+        {
+            double const b = std::max(piece.begin, piece.begin);
+            double const e = std::min(piece.end, piece.end);
+            if (e > b && path.full > 0.0) {
+                double x, y, z;
+                path.PointAtPiece(piece, 0.5 * (b + e), x, y, z);
+                dl = path.full * (e - b) * positive_or(density_ratio, fallback);
+            }
+        }
+        Interval iv;
+        iv.begin = piece.begin;
+        iv.end = piece.end;
+        iv.length = piece.length;
+        iv.density = positive_or(dl / piece.length, fallback);
+        out.push_back(iv);
+    }
+    return out;
+}
+// :117-136
+double density_path(std::vector<Interval> const& iv, Path const& path, double b, double e)
+{
+    b = std::max(path.in_begin, b);
+    e = std::min(path.in_end, e);
+    if (!(e > b)) return 0.0;
+    double s = 0.0;
+    for (Interval const& i : iv) {
+        double const bb = std::max(b, i.begin), ee = std::min(e, i.end);
+        if (ee > bb) s += path.full * (ee - bb) * i.density;
+    }
+    return s;
+}
+// :142-170
+double fraction_at_density_path(std::vector<Interval> const& iv, Path const& path, double b, double e,
+                                double target)
+{
+    b = std::max(path.in_begin, b);
+    e = std::min(path.in_end, e);
+    if (!std::isfinite(target) || target < 0.0) fail(RREA_GPU_ERR_INVALID_STATE, "sampled density path invalid");
+    double rem = target;
+    for (Interval const& i : iv) {
+        double const bb = std::max(b, i.begin), ee = std::min(e, i.end);
+        if (!(ee > bb) || !(i.density > 0.0)) continue;
+        double const c = path.full * (ee - bb) * i.density;
+        if (rem <= c) return bb + rem / (path.full * i.density);
+        rem -= c;
+    }
+    return e;
+}
+// :175-199
+double max_uniform_slice(std::vector<Interval> const& iv, Path const& path, uint64_t n)
+{
+    if (n == 0) fail(RREA_GPU_ERR_INVALID_STATE, "zero subcycles");
+    double const span = path.in_end - path.in_begin;
+    double const d = static_cast<double>(n);
+    double m = 0.0;
+    for (uint64_t i = 0; i < n; ++i) {
+        m = std::max(m, density_path(iv, path, path.in_begin + static_cast<double>(i) / d * span,
+                                     path.in_begin + static_cast<double>(i + 1U) / d * span));
+    }
+    return m;
+}
+// :213-222
+double frozen_rate(double v)
+{
+    if (!std::isfinite(v) || v < 0.0) fail(RREA_GPU_ERR_INVALID_STATE, "frozen material-path rate invalid");
+    return v;
+}
+
+// ======================================================================
+// Substep sizing: O/RreaTransportStep.H:104-184
+// ======================================================================
+uint64_t driver_count(double amount, double per)
+{
+    return static_cast<uint64_t>(std::max(1.0, std::ceil(amount / per)));
+}
+uint64_t selected_material_subcycles(double max_tau, std::vector<Interval> const& iv, Path const& path,
+                                     rrea_gpu_config const& cfg, bool& viol, double total_stp)
+{
+    double const target = cfg.max_optical_depth_per_substep;
+    if (!(target > 0.0) || cfg.max_subcycles == 0) fail(RREA_GPU_ERR_ARGUMENT, "invalid subcycle controls");
+    uint64_t const cap = cfg.max_subcycles;
+    uint64_t const req = static_cast<uint64_t>(std::max(1.0, std::ceil(max_tau / target)));
+    viol = req > cap;
+    uint64_t sub = std::min(req, cap);
+    for (;;) {
+        double const maximum = total_stp * max_uniform_slice(iv, path, sub);
+        double const tol = 64.0 * kEps * std::max(1.0, target);
+        if (maximum <= target + tol) return sub;
+        if (sub >= cap) { viol = true; return sub; }
+        long double const est = std::ceil(static_cast<long double>(sub) * static_cast<long double>(maximum / target));
+        uint64_t next = sub + 1U;
+        if (est >= static_cast<long double>(cap)) next = cap;
+        else if (est > static_cast<long double>(next)) next = static_cast<uint64_t>(est);
+        sub = std::min(next, cap);
+    }
+}
+
+// ======================================================================
+// Continuous drag: O/RreaParticleInteraction.H:203-265,
+// O/RreaChargedInterleave.H:157-292
+// ======================================================================
+struct Limit {
+    double end = 0.0;
+    bool reaches = false;
+    bool valid = false;
+};
+template <typename F>
+Limit limit_at_cutoff(double b, double e, double k, double cut, F&& loss_to)
+{
+    Limit r{b, false, false};
+    if (!std::isfinite(b) || !std::isfinite(e) || !std::isfinite(k) || !std::isfinite(cut) || !(e >= b)
+        || !(k >= cut) || !(cut >= 0.0)) {
+        return r;
+    }
+    if (e == b) {
+        r.valid = true;
+        r.reaches = k == cut;
+        return r;
+    }
+    double const to_cut = k - cut;
+    double const req = loss_to(e);
+    if (!std::isfinite(req) || req < 0.0) return r;
+    r.valid = true;
+    if (req < to_cut) { r.end = e; return r; }
+    r.reaches = true;
+    if (to_cut == 0.0) return r;
+    double lo = b, hi = e;
+    for (int it = 0; it < 56; ++it) {
+        double const mid = 0.5 * (lo + hi);
+        double const l = loss_to(mid);
+        if (!std::isfinite(l) || l < 0.0) {
+            r.valid = false;
+            r.reaches = false;
+            r.end = b;
+            return r;
+        }
+        if (l < to_cut) lo = mid; else hi = mid;
+    }
+    r.end = 0.5 * (lo + hi);
+    return r;
+}
+
+struct DragPlan {
+    double end = 0.0;
+    bool applied = false, limit_valid = true, reaches = false;
+    double drag = 0, collision = 0, soft = 0, hard = 0, raw_collision = 0, collision_stp = 0;
+};
+
+template <typename DP>
+DragPlan plan_drag(double b, double e, double k, double stop_e, double cut, DP&& dpath, double stp_col,
+                   double stp_soft, double stp_hard)
+{
+    DragPlan p;
+    p.end = b;
+    if (!(e > b) || !(k > 0.0) || stop_e < cut) return p;
+    p.collision_stp = stp_col;
+    double const total = stp_col + stp_soft;
+    Limit const lim = limit_at_cutoff(b, e, k, cut, [&](double re) { return total * dpath(b, re); });
+    if (!lim.valid) { p.limit_valid = false; return p; }
+    p.applied = true;
+    p.reaches = lim.reaches;
+    p.end = lim.end;
+    double const path_m = dpath(b, p.end);
+    p.raw_collision = stp_col * path_m;
+    double const raw_soft = stp_soft * path_m;
+    double const avail = std::max(0.0, k - cut);
+    p.drag = lim.reaches ? avail : std::min(p.raw_collision + raw_soft, avail);
+    p.collision = std::min(p.raw_collision, p.drag);
+    p.soft = std::max(0.0, p.drag - p.collision);
+    p.hard = std::min(stp_hard * path_m, avail);
+    return p;
+}
+
+// ======================================================================
+// Competing hazard: O/RreaParticleInteraction.H:1402-1492
+// ======================================================================
+struct Selection {
+    bool valid = false, event = false;
+    int channel = -1;
+    double sampled = 0.0, total = 0.0;
+};
+Selection select_hazard(std::array<double, 3> const& taus, int count, double u1, double u2)
+{
+    Selection r;
+    if (count < 1 || count > 3 || !std::isfinite(u1) || !std::isfinite(u2)) return r;
+    for (int i = 0; i < count; ++i) {
+        double const t = taus[static_cast<std::size_t>(i)];
+        if (!std::isfinite(t) || t < 0.0) return r;
+        r.total += t;
+    }
+    r.valid = std::isfinite(r.total);
+    if (!r.valid) return r;
+    u1 = std::max(0.0, std::min(1.0, u1));
+    r.sampled = -std::log(std::max(1.0e-30, 1.0 - u1));
+    if (!(r.sampled < r.total)) return r;
+    r.event = true;
+    u2 = std::max(0.0, std::min(1.0, u2));
+    double const target = u2 * r.total;
+    double cum = 0.0;
+    int last_open = -1;
+    for (int i = 0; i < count; ++i) {
+        double const t = taus[static_cast<std::size_t>(i)];
+        if (t > 0.0) last_open = i;
+        cum += t;
+        if (target < cum) { r.channel = i; return r; }
+    }
+    r.channel = last_open;
+    r.valid = r.channel >= 0;
+    r.event = r.valid;
+    return r;
+}
+
+// ======================================================================
+// Terminal / boundary helpers: O/RreaParticleInteraction.H:267-540
+// ======================================================================
+bool half_open_rz(double r, double z, double rlo, double rhi, double zlo, double zhi)
+{
+    return std::isfinite(r) && std::isfinite(z) && rhi > rlo && zhi > zlo && r >= rlo && r < rhi && z >= zlo
+        && z < zhi;
+}
+bool cartesian_half_open(double x, double y, double z, double rlo, double rhi, double zlo, double zhi)
+{
+    if (!std::isfinite(x) || !std::isfinite(y)) return false;
+    return half_open_rz(std::hypot(x, y), z, rlo, rhi, zlo, zhi);
+}
+bool advance_running(Path const& path, double f, double rlo, double rhi, double zlo, double zhi, double& rx,
+                     double& ry, double& rz)
+{
+    double x, y, z;
+    path.PointAtFull(f, x, y, z);
+    double const wz = path.WrapZ(z);
+    if (!cartesian_half_open(x, y, wz, rlo, rhi, zlo, zhi)) return false;
+    rx = x;
+    ry = y;
+    rz = wz;
+    return true;
+}
+struct EscapePolicy {
+    bool escapes = false, invalidate = false;
+};
+EscapePolicy clipped_escape_policy(Path const& path, double er, double ez)
+{
+    EscapePolicy p;
+    if (!std::isfinite(er) || !std::isfinite(ez)) {
+        p.escapes = true;
+        p.invalidate = true;
+        return p;
+    }
+    double const cz = path.WrapZ(ez);
+    bool const outside = path.OutsideCertified(er, cz);
+    bool const strictly = er < path.rlo || er > path.rhi || (!path.periodic && (ez < path.zlo || ez > path.zhi));
+    p.escapes = path.exits || outside;
+    p.invalidate = p.escapes && !strictly;
+    if (p.escapes) p.invalidate = true;  // clipped policy: RREA owns every escape
+    return p;
+}
+struct Crossing {
+    bool valid = false;
+    double sr = 0, sz = 0, cr = 0, cz = 0;
+    uint32_t faces = 0;
+};
+Crossing boundary_crossing(Path const& path)
+{
+    Crossing r;
+    double cx, cy;
+    path.PointAtFull(path.in_end, cx, cy, r.cz);
+    r.cz = path.WrapZ(r.cz);
+    r.cr = std::hypot(cx, cy);
+    r.sr = std::hypot(path.sx, path.sy);
+    r.sz = path.WrapZ(path.sz);
+    double const scale = std::max(1.0, std::max(path.rhi, std::max(std::abs(path.zlo), std::abs(path.zhi))));
+    double const tol = 512.0 * kEps * scale;
+    bool const on_r = std::abs(r.cr - path.rhi) <= tol;
+    bool const on_zlo = !path.periodic && std::abs(r.cz - path.zlo) <= tol;
+    bool const on_zhi = !path.periodic && std::abs(r.cz - path.zhi) <= tol;
+    double const dx = path.ex - path.sx, dy = path.ey - path.sy, dz = path.ez - path.sz;
+    double const outward = cx * dx + cy * dy;
+    // I/RreaSegmentDepositionRZ.H face bits: r_hi = 1, z_lo = 2, z_hi = 4
+    if (on_r && outward > -tol * scale) { r.faces |= 1u; r.cr = path.rhi; }
+    if (on_zlo && dz < 0.0) { r.faces |= 2u; r.cz = path.zlo; }
+    if (on_zhi && dz > 0.0) { r.faces |= 4u; r.cz = path.zhi; }
+    if (r.faces == 0u) {
+        if (on_r) { r.faces |= 1u; r.cr = path.rhi; }
+        if (on_zhi) { r.faces |= 4u; r.cz = path.zhi; }
+    }
+    r.valid = r.faces != 0u && std::isfinite(r.sr) && std::isfinite(r.sz) && std::isfinite(r.cr)
+        && std::isfinite(r.cz);
+    return r;
+}
+
+}  // namespace
+
+// ======================================================================
+// Electron phase: O/RreaElectronTransport.cpp:9-902 (+ O/RreaTransportStep.H
+// prologue/escape/writeback :720-905)
+// ======================================================================
+void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, FieldGrid const& field, int step,
+                            double dt_s, ChargedTile& tile, StepOutputs& out)
+{
+    Tables const tables(ts);
+    Gather const gather{field, cfg};
+    double const rlo = cfg.r_lo, rhi = cfg.r_hi, zlo = cfg.z_lo, zhi = cfg.z_hi;
+    bool const periodic = cfg.periodic_z != 0;
+    double const cutoff = cfg.low_energy_cutoff_eV;
+    double const photon_cut = cfg.photon_cutoff_eV;
+    double const hm_thr = ts.index().hard_moller_threshold_eV;
+    bool const hm_enabled = cfg.debug_disable_hard_moller == 0;
+    // RreaParticleInteraction.cpp:33-35 (uniform density: profile ratio = configured ratio)
+    double const density_ratio = positive_or(cfg.density_ratio, 1.0);
+    uint64_t const seed = cfg.rng_seed;
+    uint64_t const step_key = static_cast<uint64_t>(std::max(step, 0));
+    double const w_air = ts.index().w_air_eV_per_pair;
+
+    out.subcycles.assign(static_cast<std::size_t>(tile.n), 0);
+    out.events.assign(static_cast<std::size_t>(tile.n), 0);
+    out.disposition.assign(static_cast<std::size_t>(tile.n), -1);
+    std::vector<uint64_t>& out_subcycles = out.subcycles;
+    std::vector<uint64_t>& out_events = out.events;
+    std::vector<int32_t>& out_disposition = out.disposition;
+
+    // OpenMP over 64-particle chunks, schedule(dynamic,1), per-chunk logs
+    // merged in chunk order (O/RreaElectronTransport.cpp:42-58, 892-897).
+    constexpr int64_t kChunk = 64;
+    int64_t const n_chunks = (tile.n + kChunk - 1) / kChunk;
+    std::vector<StepOutputs> chunk_out(static_cast<std::size_t>(n_chunks));
+    std::vector<int> chunk_err(static_cast<std::size_t>(n_chunks), 0);
+    std::vector<std::string> chunk_msg(static_cast<std::size_t>(n_chunks));
+#pragma omp parallel for schedule(dynamic, 1) if (n_chunks > 1)
+    for (int64_t chunk = 0; chunk < n_chunks; ++chunk) {
+      StepOutputs& cout = chunk_out[static_cast<std::size_t>(chunk)];
+      try {
+      int64_t const ip_end = std::min(tile.n, (chunk + 1) * kChunk);
+      for (int64_t ip = chunk * kChunk; ip < ip_end; ++ip) {
+        if (!(tile.id[ip] > 0)) continue;
+        std::size_t const sp = static_cast<std::size_t>(ip);
+        uint64_t lineage = 0;  // TransportSideEffects::spawn_transient_lineage (O/RreaTransportLog.H:179)
+        int current_process = 0;
+        // ---- BeginRunningChargedParticle (O/RreaTransportStep.H:720-820)
+        uint64_t const key = static_cast<uint64_t>(std::llabs(tile.id[ip]))
+            ^ (static_cast<uint64_t>(tile.cpu ? tile.cpu[ip] : 0) << 40);
+        double const weight = tile.w[ip];
+        if (weight <= 0.0) {
+            tile.id[ip] = -tile.id[ip];
+            out_disposition[sp] = 3;
+            continue;
+        }
+        if (tile.prev_r[ip] > rhi + 1.0e-9 * rhi) {
+            fail(RREA_GPU_ERR_GEOMETRY, "RREA electron survived outside the domain");
+        }
+        double dx = tile.prev_ux[ip], dy = tile.prev_uy[ip], dz = tile.prev_uz[ip];
+        double k = kinetic_from_proper_velocity(dx, dy, dz);
+        normalize(dx, dy, dz);
+        double const seed_r = tile.prev_r[ip], seed_th = tile.prev_theta[ip];
+        double run_x = seed_r * std::cos(seed_th);
+        double run_y = seed_r * std::sin(seed_th);
+        double run_z = tile.prev_z[ip];
+        double const r_particle = seed_r, z_particle = run_z;
+
+        auto build_chord = [&](double req_dt, Path& path) -> bool {
+            // O/RreaParticleInteraction.H:110-161
+            if (!std::isfinite(req_dt) || !std::isfinite(dt_s) || !(req_dt >= 0.0) || !(dt_s > 0.0)) return false;
+            double const speed = charged_speed(k);
+            double const dn = std::sqrt(dx * dx + dy * dy + dz * dz);
+            if (!std::isfinite(speed) || !std::isfinite(dn) || !(dn > 0.0)) return false;
+            double const sc = speed * req_dt / dn;
+            double const exx = run_x + sc * dx, eyy = run_y + sc * dy, ezz = run_z + sc * dz;
+            path = ClipRz(std::hypot(run_x, run_y), std::atan2(run_y, run_x), run_z, std::hypot(exx, eyy),
+                          std::atan2(eyy, exx), ezz, rlo, rhi, zlo, zhi, periodic);
+            return std::isfinite(path.full) && path.in_begin == 0.0;
+        };
+
+        Path driver;
+        bool const driver_valid = build_chord(dt_s, driver);
+        EscapePolicy escape = clipped_escape_policy(driver, std::hypot(driver.ex, driver.ey), driver.ez);
+        double const ds = driver_valid ? driver.in_length : 0.0;
+        std::vector<Interval> const driver_iv = build_intervals(driver, density_ratio, density_ratio);
+        double const driver_span = std::max(driver.in_end, 1.0e-6);
+        double const field_work = path_field_work(gather, driver, -1.0, 0.0, 1.0).work / driver_span;
+
+        double const chord_dpath = density_path(driver_iv, driver, driver.in_begin, driver.in_end);
+        double transported_dpath = 0.0, transported_len = 0.0;
+        double particle_density = ds > 0.0 ? chord_dpath / ds : positive_or(density_ratio, density_ratio);
+        Path path = driver;
+        std::vector<Interval> iv = driver_iv;
+
+        auto push_source = [&](int kind, double r, double z, double w, double sec, double loss) {
+            cout.sources.push_back(Source{kind, r, z, w, sec, loss, ip});
+        };
+        auto push_segment = [&](int kind, std::array<double, 7> const& a, uint64_t ch, uint32_t faces) {
+            Segment s;
+            s.kind = kind;
+            for (int c = 0; c < 7; ++c) s.a[c] = a[c];
+            s.channel = ch;
+            s.faces = faces;
+            s.parent_index = ip;
+            cout.segments.push_back(s);
+        };
+        auto add_secondary = [&](int species, double x, double y, double z, double sx, double sy, double sz,
+                                 double e, double birth) {
+            Secondary s;
+            s.species = species;
+            s.process = current_process;
+            s.x = x; s.y = y; s.z = z;
+            s.dx = sx; s.dy = sy; s.dz = sz;
+            s.w = weight;
+            s.energy = e;
+            s.birth = birth;
+            s.root_key = key;
+            s.lineage = lineage++;
+            s.root_species = 0;
+            s.parent_index = ip;
+            cout.secondaries.push_back(s);
+        };
+        // TransportStep::deposit_local_energy_as_ion_pairs (O/RreaTransportStep.H:530-561)
+        auto deposit_local = [&](double r, double z, double w, double e) {
+            if (w <= 0.0 || e <= 0.0) return;
+            double const pw = w * e / std::max(w_air, 1.0);
+            if (pw <= 0.0) return;
+            push_source(0, r, z, pw, 0.0, w_air);
+        };
+        // CommitChargedEscape (O/RreaTransportStep.H:829-863)
+        auto commit_escape = [&]() {
+            double const u = proper_velocity_from_kinetic(k);
+            tile.ux[ip] = u * dx;
+            tile.uy[ip] = u * dy;
+            tile.uz[ip] = u * dz;
+            Crossing const c = boundary_crossing(path);
+            push_segment(1, {r_particle, z_particle, c.sr, c.sz, c.cr, c.cz, -weight}, 1u, c.faces);
+            if (escape.invalidate) tile.id[ip] = -tile.id[ip];
+            out_disposition[sp] = 1;
+        };
+        auto demote = [&](double r, double z) {
+            // O/RreaElectronTransport.cpp:151-174 and :856-879
+            current_process = 12;  // LowEnergyDemotion
+            push_source(1, r, z, weight, 0.0, 0.0);
+            deposit_local(r, z, weight, k);
+            push_segment(0, {r_particle, z_particle, r, z, -weight, 0.0, 0.0}, 2u, 0u);
+            tile.id[ip] = -tile.id[ip];
+            out_disposition[sp] = 2;
+        };
+
+        // :129-175
+        bool const below = k < cutoff;
+        int const initial = escape.escapes ? 1 : (below ? 2 : 0);
+        if (initial == 1 && below) { commit_escape(); continue; }
+        if (initial == 2) { demote(r_particle, z_particle); continue; }
+        if (ds <= 0.0) {
+            if (escape.escapes) commit_escape();
+            else out_disposition[sp] = 0;
+            continue;
+        }
+        if (driver_iv.empty()) fail(RREA_GPU_ERR_INVALID_STATE, "positive length but no material segments");
+
+        // competing STP rates (O/RreaChargedFinalStates.H:107-152)
+        auto competing = [&](double e) {
+            std::array<double, 3> s{};
+            bool const m_open = hm_enabled && hm_thr > 0.0 && e > 2.0 * hm_thr;
+            if (m_open) {
+                double const mfp = tables.ElectronHardMollerMeanFreePath(e, 1.0);
+                s[0] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+            } else {
+                s[0] = frozen_rate(0.0);
+            }
+            bool const b_open = std::isfinite(e) && std::isfinite(photon_cut) && e > photon_cut;
+            if (b_open) {
+                double const mfp = tables.ElectronBremsstrahlungMeanFreePath(e, 1.0);
+                s[1] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+            } else {
+                s[1] = frozen_rate(0.0);
+            }
+            s[2] = 0.0;
+            return s;
+        };
+        // RreaChargedChannelOpenAt (O/RreaChargedFinalStates.H:56-96)
+        auto channel_open = [&](int ch, double e) {
+            double mi, bi;
+            tables.ElectronGateRates(e, mi, bi);
+            if (ch == 0) return hm_enabled && (hm_thr > 0.0 && e > 2.0 * hm_thr) && mi > 0.0;
+            if (ch == 1) return (std::isfinite(e) && std::isfinite(photon_cut) && e > photon_cut) && bi > 0.0;
+            return false;
+        };
+
+        std::array<double, 3> const init = competing(k);
+        double const driver_dpath = chord_dpath / driver_span;
+        bool viol = false;
+        uint64_t subcycles = selected_material_subcycles((init[0] * driver_dpath) + (init[1] * driver_dpath),
+                                                         driver_iv, driver, cfg, viol, init[0] + init[1]);
+        {
+            double const gs_n = frozen_rate([&] {
+                double const mfp = tables.ElasticMeanFreePath(0, k, 1.0);
+                return mfp > 0.0 ? 1.0 / mfp : 0.0;
+            }()) * driver_dpath;
+            double const ke = std::max(k, cutoff);
+            double const drag_est = (ke > 0.0 ? tables.ElectronCollisionLoss(ke, 1.0)
+                                                    + tables.ElectronSoftRadiativeDrag(ke, 1.0)
+                                              : 0.0)
+                * driver_dpath;
+            double const impulse = std::max(cfg.max_field_impulse_fraction * k,
+                                            std::max(cfg.field_impulse_floor_eV, 1.0));
+            uint64_t const gsd = driver_count(std::min(gs_n, cfg.gs_total_collision_cap),
+                                              std::max(cfg.max_gs_collisions_per_substep, 1.0));
+            uint64_t const imd = driver_count(std::abs(field_work) + drag_est, impulse);
+            subcycles = std::min<uint64_t>(std::max({subcycles, gsd, imd}), cfg.max_subcycles);
+        }
+        if (cfg.strict_transport_guards && viol) {
+            fail(RREA_GPU_ERR_GUARD, "strict transport guard: optical-depth subcycle cap exceeded");
+        }
+        out_subcycles[sp] = subcycles;
+
+        bool exited = false;
+        uint64_t completed = 0;
+        bool terminated_mid = false;
+        double mid_r = r_particle, mid_z = z_particle;
+        double const sub_dt = dt_s / static_cast<double>(subcycles);
+        FieldRange sub_field;
+        double sub_dt_eff = 0.0;
+        uint64_t events = 0;
+
+        auto elapsed_at = [&](double f) {
+            double const within = std::min(1.0, std::max(0.0, f));
+            return std::min(1.0, (static_cast<double>(completed) + within) / static_cast<double>(subcycles));
+        };
+        auto mark_stopped = [&](double f) {
+            if (path.exits && f >= path.in_end) { exited = true; return; }
+            double x, y, z;
+            path.PointAtFull(f, x, y, z);
+            double const r = std::hypot(x, y);
+            if (!cartesian_half_open(x, y, z, rlo, rhi, zlo, zhi)) { exited = true; return; }
+            mid_z = z;
+            mid_r = r;
+            terminated_mid = true;
+        };
+        // apply_electron_continuous_segment (:294-400)
+        auto continuous = [&](double b, double e, double stop_e) -> Limit {
+            auto dp = [&](double bb, double ee) { return density_path(iv, path, bb, ee); };
+            double sc = 0, ss = 0, sh = 0;
+            bool const need = (e > b) && (k > 0.0) && !(stop_e < cutoff);
+            if (need) {
+                sc = frozen_rate(tables.ElectronCollisionLoss(stop_e, 1.0));
+                ss = frozen_rate(tables.ElectronSoftRadiativeDrag(stop_e, 1.0));
+                sh = (hm_enabled && hm_thr > 0.0 && stop_e > 2.0 * hm_thr)
+                    ? frozen_rate(tables.ElectronHardMollerEnergyLoss(stop_e, 1.0))
+                    : 0.0;
+            }
+            DragPlan const plan = plan_drag(b, e, k, stop_e, cutoff, dp, sc, ss, sh);
+            if (!plan.limit_valid) fail(RREA_GPU_ERR_INVALID_STATE, "continuous stopping has no monotone cutoff point");
+            if (!plan.applied) return Limit{b, false, true};
+            // RreaPartitionContinuousIonPairs (O/RreaChargedInterleave.H:157-196)
+            if (plan.collision > 0.0 && plan.raw_collision > 0.0) {
+                for (Interval const& i : iv) {
+                    double const bb = std::max(b, i.begin), ee = std::min(plan.end, i.end);
+                    if (!(ee > bb)) continue;
+                    double const raw = path.full * (ee - bb) * i.density * plan.collision_stp;
+                    double const loss = plan.collision * raw / plan.raw_collision;
+                    double const pw = weight * loss / std::max(w_air, 1.0);
+                    if (!(pw > 0.0)) continue;
+                    double x, y, z;
+                    path.PointAtFull(0.5 * (bb + ee), x, y, z);
+                    push_source(0, std::hypot(x, y), z, pw, 0.5 * cutoff, w_air);
+                }
+            }
+            k = std::max(0.0, k - plan.drag);
+            if (plan.reaches) k = cutoff;
+            return Limit{plan.end, plan.reaches, true};
+        };
+
+        // RreaRunChargedSubstepInterleave (O/RreaChargedInterleave.H:693-732)
+        for (uint64_t sub = 0; sub < subcycles; ++sub) {
+            if (k < cutoff) break;
+            double sb = 0.0, se = 0.0;
+            // build_substep (:535-598)
+            {
+                Path np;
+                if (!build_chord(sub_dt, np)) break;
+                path = np;
+                if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
+                    exited = path.exits;
+                    break;
+                }
+                iv = build_intervals(path, density_ratio, density_ratio);
+                if (iv.empty()) fail(RREA_GPU_ERR_INVALID_STATE, "microchord with no material intervals");
+                for (Interval const& i : iv) {
+                    transported_dpath += i.length * i.density;
+                    transported_len += i.length;
+                }
+                sb = path.in_begin;
+                se = path.in_end;
+                sub_field = path_field_work(gather, path, -1.0, sb, se);
+                sub_dt_eff = sub_dt * (se - sb);
+                half_kick(sub_field, 0.5 * sub_dt_eff, -1.0, k, dx, dy, dz);
+                if (k < cutoff) { mark_stopped(sb); break; }
+            }
+            // run_events: RreaRunChargedEventInterleave (:546-664)
+            {
+                std::array<double, 3> stp{};
+                uint64_t rng_index = 0;
+                double ex = 0, ey = 0, ez = 0, er = 0;
+                double rem = sb;
+                uint64_t ordinal = 0;
+                while (rem < se && k >= cutoff) {
+                    if (ordinal >= kEventCap) fail(RREA_GPU_ERR_RNG_OVERFLOW, "electron event ordinal overflow");
+                    double const frozen = k;
+                    stp = competing(frozen);
+                    double const seg_dp = density_path(iv, path, rem, se);
+                    std::array<double, 3> const taus = {stp[0] * seg_dp, stp[1] * seg_dp, 0.0};
+                    if (!try_live_hazard_index(0, sub, ordinal, rng_index)) {
+                        fail(RREA_GPU_ERR_RNG_OVERFLOW, "electron repeated-hazard RNG index overflow");
+                    }
+                    ++events;
+                    uint64_t const od_ch = ordinal == 0 ? kElectronCompetingOpticalDepth : kElectronContinuationOpticalDepth;
+                    uint64_t const cc_ch = ordinal == 0 ? kElectronCompetingChannel : kElectronContinuationChannel;
+                    double const u1 = rng_uniform(seed, key, step_key, rng_index, od_ch);
+                    double const u2 = rng_uniform(seed, key, step_key, rng_index, cc_ch);
+                    Selection const sel = select_hazard(taus, 2, u1, u2);
+                    double ev_frac = 0.0;
+                    bool split_valid = false;
+                    if (sel.valid && sel.event) {
+                        ev_frac = fraction_at_density_path(iv, path, rem, se, sel.sampled / (stp[0] + stp[1]));
+                        split_valid = std::isfinite(rem) && std::isfinite(ev_frac) && std::isfinite(se) && (se > rem)
+                            && !(ev_frac < rem) && !(ev_frac > se);
+                    }
+                    if (!sel.valid) fail(RREA_GPU_ERR_INVALID_STATE, "electron competing-hazard selection invalid");
+                    if (!sel.event) {
+                        Limit const l = continuous(rem, se, frozen);
+                        if (l.reaches) mark_stopped(l.end);
+                        break;
+                    }
+                    if (!split_valid) fail(RREA_GPU_ERR_INVALID_STATE, "sampled event depth outside its subcycle");
+                    path.PointAtFull(ev_frac, ex, ey, ez);
+                    er = std::hypot(ex, ey);
+                    Limit const l = continuous(rem, ev_frac, frozen);
+                    if (l.reaches) { mark_stopped(l.end); break; }
+                    bool const open_ev = k >= cutoff && channel_open(sel.channel, k);
+                    if (!open_ev) {
+                        bool const open_fr = frozen >= cutoff && channel_open(sel.channel, frozen);
+                        if (!open_fr) fail(RREA_GPU_ERR_INVALID_STATE, "selected channel closed before its event depth");
+                        rem = ev_frac;
+                        ++ordinal;
+                        continue;
+                    }
+                    double const birth = elapsed_at(ev_frac);
+                    if (sel.channel == 0) {
+                        // RreaApplyHardMollerFinalState (O/RreaChargedFinalStates.H:164-225)
+                        double const kb = k;
+                        double sec = tables.SampleMollerSecondaryEnergy(
+                            kb, rng_uniform(seed, key, step_key, rng_index, kHardMollerEnergy));
+                        sec = std::max(hm_thr, std::min(sec, 0.5 * kb));
+                        double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
+                        moller_lab_directions(dx, dy, dz, kb, sec,
+                                              rng_uniform(seed, key, step_key, rng_index, kHardMollerAzimuth), pdx,
+                                              pdy, pdz, sdx, sdy, sdz);
+                        k = std::max(0.0, kb - sec);
+                        dx = pdx; dy = pdy; dz = pdz;
+                        current_process = 2;  // HardMoller
+                        add_secondary(0, ex, ey, ez, sdx, sdy, sdz, sec, birth);
+                        push_source(0, er, ez, weight, sec, sec);
+                    } else if (sel.channel == 1) {
+                        // RreaApplyBremsFinalState (O/RreaChargedFinalStates.H:329-394)
+                        double const kb = k;
+                        double const eu = rng_uniform(seed, key, step_key, rng_index, kBremsEnergy);
+                        double const sampled = tables.SampleBremsstrahlungPhotonEnergy(kb, eu);
+                        // RreaClassifyBremsEnergyDisposition (O/RreaParticleInteraction.H:1552-1574)
+                        double const eg = std::min(std::max(sampled, 0.0), std::max(kb, 0.0));
+                        double const after = std::max(0.0, std::max(kb, 0.0) - eg);
+                        bool const tracked = std::isfinite(photon_cut) && photon_cut >= 0.0 && eg >= photon_cut;
+                        double gx = dx, gy = dy, gz = dz;
+                        double const ct = tables.SampleBremsstrahlungCosTheta(
+                            kb, rng_uniform(seed, key, step_key, rng_index, kBremsAngle));
+                        cone_direction(dx, dy, dz, ct, rng_uniform(seed, key, step_key, rng_index, kBremsAzimuth), gx,
+                                       gy, gz);
+                        photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
+                        k = after;
+                        current_process = 4;  // Bremsstrahlung
+                        if (tracked) {
+                            add_secondary(2, ex, ey, ez, gx, gy, gz, eg, birth);
+                        } else if (eg > 0.0) {
+                            deposit_local(er, ez, weight, eg);
+                        }
+                    }
+                    if (k <= cutoff) { mark_stopped(ev_frac); break; }
+                    rem = ev_frac;
+                    ++ordinal;
+                }
+            }
+            if (terminated_mid) break;
+            // finish_interleaved_substep (:502-524)
+            {
+                bool stop = false;
+                if (k >= cutoff) {
+                    // apply_gs_elastic_scatter (O/RreaTransportStep.H:371-423)
+                    double const mfp = tables.ElasticMeanFreePath(0, k, 1.0);
+                    double const gs_n = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0) * density_path(iv, path, sb, se);
+                    if (gs_n > 0.0) {
+                        auto gkey = [&](uint64_t ch, uint64_t inner) {
+                            return rng_uniform(seed, key, step_key, (sub << 8) | inner, ch);
+                        };
+                        auto deflect = [&](double ct, double uphi) {
+                            double nx, ny, nz;
+                            cone_direction(dx, dy, dz, ct, uphi, nx, ny, nz);
+                            dx = nx; dy = ny; dz = nz;
+                        };
+                        double const few = ts.index().gs_few_collision_threshold;
+                        if (gs_n < few) {
+                            int const cap = static_cast<int>(std::ceil(3.0 * few));
+                            if (cap >= 255) fail(RREA_GPU_ERR_INVALID_STATE, "GS few-collision cap too large");
+                            int const cnt = poisson_capped(gs_n, gkey(kElectronGsFewCount, 0), cap);
+                            for (int q = 0; q < cnt; ++q) {
+                                double const ct = tables.SampleSingleElasticCosTheta(
+                                    0, k, gkey(kElectronGsFewScatter, static_cast<uint64_t>(q + 1)));
+                                deflect(ct, gkey(kElectronGsFewAzimuth, static_cast<uint64_t>(q + 1)));
+                            }
+                        } else {
+                            double const ct = tables.SampleGsCosTheta(0, k, gs_n, gkey(kElectronGsAngle, 0));
+                            deflect(ct, gkey(kElectronGsAzimuth, 0));
+                        }
+                    }
+                }
+                half_kick(sub_field, 0.5 * sub_dt_eff, -1.0, k, dx, dy, dz);
+                if (k < cutoff) { mark_stopped(se); stop = true; }
+                if (stop) break;
+            }
+            if (!advance_running(path, se, rlo, rhi, zlo, zhi, run_x, run_y, run_z)) { exited = true; break; }
+            if (path.exits) { exited = true; break; }
+            completed = sub + 1U;
+        }
+        out_events[sp] = events;
+        if (exited) {
+            escape = clipped_escape_policy(path, std::hypot(path.ex, path.ey), path.ez);
+        }
+        if (transported_len > 0.0) particle_density = transported_dpath / transported_len;
+        double const end_r = std::hypot(run_x, run_y);
+        double fer, fez, fbt;
+        gather.at(end_r, run_z, fer, fez, fbt);
+        // electron_ensemble_mean_drag_ev_per_m (O/RreaTransportStep.H:226-247)
+        double threshold = 0.0;
+        {
+            double const ke = std::max(k, cutoff);
+            if (ke > 0.0 && particle_density > 0.0) {
+                double const hard = hm_enabled ? tables.ElectronHardMollerEnergyLoss(ke, particle_density) : 0.0;
+                threshold = (tables.ElectronCollisionLoss(ke, particle_density)
+                             + tables.ElectronSoftRadiativeDrag(ke, particle_density))
+                    + hard + tables.ElectronTrackedBremsEnergyLoss(ke, particle_density);
+            }
+        }
+        // RreaEvaluateElectronStatePolicy (O/RreaParticleInteraction.H:1302-1317)
+        bool const below_cut = k < cutoff;
+        bool const nonrunaway = hm_thr > 0.0 && k <= hm_thr && std::hypot(fer, fez) <= threshold;
+        int disp;
+        if (exited) disp = 1;
+        else if (terminated_mid) disp = 2;
+        else disp = (below_cut || nonrunaway) ? 2 : 0;
+        if (disp == 1) { commit_escape(); continue; }
+        if (disp == 2) {
+            double const dr_ = terminated_mid ? mid_r : end_r;
+            double const dz_ = terminated_mid ? mid_z : run_z;
+            demote(dr_, dz_);
+            continue;
+        }
+        // CommitSurvivorChargedWriteback (O/RreaTransportStep.H:874-905)
+        double const um = proper_velocity_from_kinetic(k);
+        tile.ux[ip] = um * dx;
+        tile.uy[ip] = um * dy;
+        tile.uz[ip] = um * dz;
+        tile.r[ip] = end_r;
+        tile.theta[ip] = std::atan2(run_y, run_x);
+        tile.z[ip] = run_z;
+        push_segment(0, {r_particle, z_particle, end_r, run_z, -weight, 0.0, 0.0}, 0u, 0u);
+        out_disposition[sp] = 0;
+      }
+      } catch (OracleError const& e) {
+        chunk_err[static_cast<std::size_t>(chunk)] = e.code;
+        chunk_msg[static_cast<std::size_t>(chunk)] = e.what();
+      }
+    }
+    for (int64_t chunk = 0; chunk < n_chunks; ++chunk) {
+        if (chunk_err[static_cast<std::size_t>(chunk)] != 0) {
+            fail(chunk_err[static_cast<std::size_t>(chunk)], chunk_msg[static_cast<std::size_t>(chunk)]);
+        }
+    }
+    for (auto& c : chunk_out) {
+        out.secondaries.insert(out.secondaries.end(), c.secondaries.begin(), c.secondaries.end());
+        out.sources.insert(out.sources.end(), c.sources.begin(), c.sources.end());
+        out.segments.insert(out.segments.end(), c.segments.begin(), c.segments.end());
+    }
+}
+
+// Primitive-level entry points, one row of inputs per call, matching the
+// golden fixtures written by oracle/ref_golden.cpp.
+int RunPrimitive(TableSet const& ts, int which, double const* in, int64_t n, double* out)
+{
+    Tables const t(ts);
+    for (int64_t i = 0; i < n; ++i) {
+        switch (which) {
+        case 1: {  // (table, e) -> value
+            double const* a = in + 2 * i;
+            out[i] = t.interpolate(static_cast<int>(a[0]), a[1]);
+            break;
+        }
+        case 2: {  // (e, dr) -> 10 accessors
+            double const* a = in + 2 * i;
+            double* o = out + 10 * i;
+            double const e = a[0], dr = a[1];
+            o[0] = t.ElectronCollisionLoss(e, dr);
+            o[1] = t.ElectronSoftRadiativeDrag(e, dr);
+            o[2] = t.ElectronHardMollerMeanFreePath(e, dr);
+            o[3] = t.ElectronBremsstrahlungMeanFreePath(e, dr);
+            o[4] = t.ElectronHardMollerEnergyLoss(e, dr);
+            o[5] = t.ElectronTrackedBremsEnergyLoss(e, dr);
+            o[6] = t.ElasticMeanFreePath(0, e, dr);
+            o[7] = t.ScreeningEta(0, e);
+            o[8] = t.ElasticMeanFreePath(1, e, dr);
+            o[9] = t.ScreeningEta(1, e);
+            break;
+        }
+        case 3: {
+            double const* a = in + 4 * i;
+            out[i] = t.SampleGsCosTheta(static_cast<int>(a[0]), a[1], a[2], a[3]);
+            break;
+        }
+        case 4: {
+            double const* a = in + 3 * i;
+            out[i] = t.SampleSingleElasticCosTheta(static_cast<int>(a[0]), a[1], a[2]);
+            break;
+        }
+        case 5: out[i] = t.SampleMollerSecondaryEnergy(in[2 * i], in[2 * i + 1]); break;
+        case 6: out[i] = t.SampleBremsstrahlungPhotonEnergy(in[2 * i], in[2 * i + 1]); break;
+        case 7: out[i] = t.SampleBremsstrahlungCosTheta(in[2 * i], in[2 * i + 1]); break;
+        case 8: {
+            double const* a = in + 13 * i;
+            FieldRange f;
+            f.work = a[0]; f.ex = a[1]; f.ey = a[2]; f.ez = a[3]; f.bx = a[4]; f.by = a[5]; f.bz = a[6];
+            double k = a[9], dx = a[10], dy = a[11], dz = a[12];
+            half_kick(f, a[7], a[8], k, dx, dy, dz);
+            double* o = out + 4 * i;
+            o[0] = k; o[1] = dx; o[2] = dy; o[3] = dz;
+            break;
+        }
+        case 9: {
+            double const* a = in + 5 * i;
+            double* o = out + 3 * i;
+            cone_direction(a[0], a[1], a[2], a[3], a[4], o[0], o[1], o[2]);
+            break;
+        }
+        case 10: {
+            double const* a = in + 6 * i;
+            double* o = out + 6 * i;
+            moller_lab_directions(a[0], a[1], a[2], a[3], a[4], a[5], o[0], o[1], o[2], o[3], o[4], o[5]);
+            break;
+        }
+        case 11: {
+            double const* a = in + 8 * i;
+            double* o = out + 3 * i;
+            o[0] = a[5]; o[1] = a[6]; o[2] = a[7];
+            photon_recoil(a[0], a[1], a[2], a[3], a[4], o[0], o[1], o[2]);
+            break;
+        }
+        case 12: out[i] = poisson_capped(in[2 * i], in[2 * i + 1], 30); break;
+        case 13: {
+            double const* a = in + 6 * i;
+            std::array<double, 3> taus = {a[0], a[1], a[2]};
+            Selection const s = select_hazard(taus, static_cast<int>(a[3]), a[4], a[5]);
+            double* o = out + 5 * i;
+            o[0] = s.valid; o[1] = s.event; o[2] = s.channel; o[3] = s.sampled; o[4] = s.total;
+            break;
+        }
+        case 14: {
+            double const* a = in + 10 * i;
+            double const len = a[8], rho = a[9];
+            DragPlan const p = plan_drag(a[0], a[1], a[2], a[3], a[4],
+                                         [&](double bb, double ee) { return len * (ee - bb) * rho; }, a[5], a[6],
+                                         a[7]);
+            double* o = out + 9 * i;
+            o[0] = p.end; o[1] = p.applied; o[2] = p.limit_valid; o[3] = p.reaches; o[4] = p.drag;
+            o[5] = p.collision; o[6] = p.soft; o[7] = p.hard; o[8] = p.raw_collision;
+            break;
+        }
+        case 15: {
+            double const* a = in + 9 * i;
+            double* o = out + 17 * i;
+            double const x = a[0], y = a[1], z = a[2], dx = a[3], dy = a[4], dz = a[5], k = a[6], dt = a[7];
+            bool const periodic = a[8] != 0.0;
+            // RreaBuildRunningChargedChord, O/RreaParticleInteraction.H:110-161
+            bool valid = false;
+            Path p;
+            double const speed = charged_speed(k);
+            double const dn = std::sqrt(dx * dx + dy * dy + dz * dz);
+            if (std::isfinite(speed) && std::isfinite(dn) && dn > 0.0) {
+                double const sc = speed * dt / dn;
+                double const ex = x + sc * dx, ey = y + sc * dy, ez = z + sc * dz;
+                p = ClipRz(std::hypot(x, y), std::atan2(y, x), z, std::hypot(ex, ey), std::atan2(ey, ex), ez, 0.0,
+                           50.0, 0.0, 500.0, periodic);
+                valid = std::isfinite(p.full) && p.in_begin == 0.0;
+            }
+            double const np = static_cast<double>(p.pieces.size());
+            o[0] = valid; o[1] = p.sx; o[2] = p.sy; o[3] = p.sz; o[4] = p.ex; o[5] = p.ey; o[6] = p.ez;
+            o[7] = p.full; o[8] = p.in_end; o[9] = p.in_length; o[10] = p.exits; o[11] = np;
+            o[12] = np > 0 ? p.pieces[0].begin : -1.0;
+            o[13] = np > 0 ? p.pieces[0].end : -1.0;
+            o[14] = np > 0 ? p.pieces[0].shift : 0.0;
+            o[15] = np > 0 ? p.pieces.back().begin : -1.0;
+            o[16] = np > 0 ? p.pieces.back().shift : 0.0;
+            break;
+        }
+        default:
+            fail(RREA_GPU_ERR_ARGUMENT, "unknown primitive");
+        }
+    }
+    return 0;
+}
+
+// O/RreaCouplingSources.cpp:435-512 + S/RreaEventAccumulator.cpp:129-164, 386-502
+void DepositSources(rrea_gpu_config const& cfg, std::vector<Source> const& sources, double cutoff,
+                    CellSources& cells)
+{
+    int const nr = cells.nr, nz = cells.nz;
+    for (auto& f : cells.f) {
+        if (f.size() != static_cast<std::size_t>(nr) * nz) f.assign(static_cast<std::size_t>(nr) * nz, 0.0);
+    }
+    double const dr = (cfg.r_hi - cfg.r_lo) / nr, dz = (cfg.z_hi - cfg.z_lo) / nz;
+    bool const periodic = cfg.periodic_z != 0;
+    auto add = [&](int field, double r, double z, double value) {
+        if (!std::isfinite(value) || value == 0.0) return;
+        double zz = z;
+        if (periodic) {
+            double const len = cfg.z_hi - cfg.z_lo;
+            double s = std::fmod(zz - cfg.z_lo, len);
+            if (s < 0.0) s += len;
+            zz = cfg.z_lo + s;
+        }
+        int const ic = static_cast<int>(std::floor((r - cfg.r_lo) / dr));
+        int const jc = static_cast<int>(std::floor((zz - cfg.z_lo) / dz));
+        if (ic < 0 || ic >= nr || jc < 0 || jc >= nz) return;
+        double const rc = (r - cfg.r_lo) / dr + 0.0 - 0.5;
+        int const i0 = static_cast<int>(std::floor(rc));
+        double const wr1 = rc - i0, wr0 = 1.0 - wr1;
+        double const zc = (zz - cfg.z_lo) / dz + 0.0 - 0.5;
+        int const j0 = static_cast<int>(std::floor(zc));
+        double const wz1 = zc - j0, wz0 = 1.0 - wz1;
+        for (int a = 0; a < 2; ++a) {
+            double const wz = a == 0 ? wz0 : wz1;
+            if (wz == 0.0) continue;
+            int j = j0 + a;
+            if (j < 0 || j > nz - 1) {
+                if (periodic) { j = ((j % nz) + nz) % nz; } else { continue; }
+            }
+            for (int b = 0; b < 2; ++b) {
+                double const wr = b == 0 ? wr0 : wr1;
+                double const v = value * wr * wz;
+                if (v == 0.0) continue;
+                int i = i0 + b;
+                if (i < 0 || i > nr - 1) {
+                    if (i == -1 && cfg.r_lo == 0.0) i = 0; else continue;
+                }
+                if (!std::isfinite(v) || v == 0.0) continue;
+                cells.f[field][static_cast<std::size_t>(i) + static_cast<std::size_t>(nr) * j] += v;
+            }
+        }
+    };
+    for (Source const& s : sources) {
+        if (s.w <= 0.0) continue;
+        if (s.kind == 0) {
+            // AccumulateIonizationEvent
+            add(1, s.r, s.z, s.w);
+            if (s.secondary_energy < cutoff) add(0, s.r, s.z, s.w);
+            add(3, s.r, s.z, s.w);
+            add(4, s.r, s.z, std::max(s.w, 0.0) * std::max(s.energy_loss, 0.0));
+        } else if (s.kind == 1) {
+            // AccumulateLowEnergyElectron
+            add(0, s.r, s.z, s.w);
+            add(3, s.r, s.z, s.w);
+            add(4, s.r, s.z, std::max(s.w, 0.0) * std::max(std::max(s.energy_loss, 0.0), 0.0));
+        } else {
+            // AccumulatePositiveIonSourceOnly
+            add(1, s.r, s.z, s.w);
+            add(3, s.r, s.z, s.w);
+            add(4, s.r, s.z, std::max(s.w, 0.0) * std::max(s.energy_loss, 0.0));
+        }
+    }
+}
+
+}  // namespace oracle

@@ -1,0 +1,187 @@
+// ORACLE — test infrastructure only.  A scalar CPU restatement of the
+// reference's per-timestep kinetic step (RREA overlay,
+// native_amrex_rrea/warpx_overlay/Source/Rrea/ and native_amrex_rrea/src/),
+// used by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the
+// checker.  The shipped GPU path never calls into this directory.
+//
+// Every function cites the reference file:line it restates.  Shorthand:
+//   O/ = native_amrex_rrea/warpx_overlay/Source/Rrea/
+//   S/ = native_amrex_rrea/src/
+//   I/ = native_amrex_rrea/include/rrea/
+#pragma once
+
+#include "../rrea_feedback_warpx_amrex_geant4_gb300/csrc/host/table_set.hpp"
+#include "../include/rrea_gpu.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <limits>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace oracle {
+
+constexpr double kMeC2 = 510998.95000;          // I/RreaConstants.H:9
+constexpr double kC = 299792458.0;              // I/RreaConstants.H:10
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr double kEps = std::numeric_limits<double>::epsilon();
+
+struct OracleError : std::runtime_error {
+    int code;
+    OracleError(int c, std::string const& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] inline void fail(int code, std::string const& msg) { throw OracleError(code, msg); }
+
+// ---------------------------------------------------------------- RNG
+// O/RreaRng.cpp:9-44
+inline uint64_t splitmix64(uint64_t v)
+{
+    v += 0x9e3779b97f4a7c15ULL;
+    v = (v ^ (v >> 30U)) * 0xbf58476d1ce4e5b9ULL;
+    v = (v ^ (v >> 27U)) * 0x94d049bb133111ebULL;
+    return v ^ (v >> 31U);
+}
+inline uint64_t rng_counter(uint64_t seed, uint64_t pid, uint64_t step, uint64_t idx, uint64_t ch)
+{
+    uint64_t s = splitmix64(seed);
+    s ^= splitmix64(pid + 0x100000001b3ULL);
+    s ^= splitmix64(step + 0x9e3779b97f4a7c15ULL);
+    s ^= splitmix64(idx + 0xbf58476d1ce4e5b9ULL);
+    s ^= splitmix64(ch + 0x94d049bb133111ebULL);
+    return splitmix64(s);
+}
+inline double rng_uniform(uint64_t seed, uint64_t pid, uint64_t step, uint64_t idx, uint64_t ch)
+{
+    return (static_cast<double>(rng_counter(seed, pid, step, idx, ch) >> 12U) + 0.5) * 0x1.0p-52;
+}
+
+// O/RreaRng.H:17-97 channel ids used by the transport phases.
+enum Channel : uint64_t {
+    kHardMollerEnergy = 22, kHardMollerAzimuth = 23,
+    kBremsEnergy = 42, kBremsAngle = 43, kBremsAzimuth = 44,
+    kElectronGsAngle = 89, kElectronGsAzimuth = 90, kElectronGsFewCount = 91,
+    kElectronGsFewScatter = 92, kElectronGsFewAzimuth = 93,
+    kElectronCompetingOpticalDepth = 107, kElectronCompetingChannel = 108,
+    kElectronContinuationOpticalDepth = 124, kElectronContinuationChannel = 125,
+};
+
+// O/RreaParticleInteraction.H:642-710
+constexpr uint64_t kLineageCap = uint64_t{1} << 14;
+constexpr uint64_t kSegmentCap = uint64_t{1} << 14;
+constexpr uint64_t kEventCap = uint64_t{1} << 13;
+constexpr uint64_t kInnerCap = uint64_t{1} << 8;
+inline bool try_pack_transient(bool newborn, uint64_t species, uint64_t lineage, uint64_t segment,
+                               uint64_t ordinal, uint64_t inner, uint64_t& out)
+{
+    if (species >= 3U || lineage >= kLineageCap || segment >= kSegmentCap || ordinal >= kEventCap
+        || inner >= kInnerCap) {
+        return false;
+    }
+    out = (static_cast<uint64_t>(newborn) << 51) | (species << 49) | (lineage << 35) | (segment << 21)
+        | (ordinal << 8) | inner;
+    return true;
+}
+inline bool try_live_hazard_index(uint64_t species, uint64_t segment, uint64_t ordinal, uint64_t& out)
+{
+    if (species >= 3U) return false;
+    if (ordinal == 0U) {
+        if (segment >= kSegmentCap) return false;
+        out = segment;
+        return true;
+    }
+    return try_pack_transient(false, species, 1U, segment, ordinal, 0U, out);
+}
+
+// ---------------------------------------------------------------- output records
+struct Secondary {
+    int species;  // 0 e-, 1 e+, 2 photon  (O/RreaParticleInteraction.H:28-32)
+    int process;  // RreaSecondaryProcess ordinal
+    double x, y, z, dx, dy, dz, w, energy, birth;
+    uint64_t root_key, lineage;
+    int root_species;
+    int64_t parent_index;
+};
+
+struct Source {
+    int kind;  // 0 ionization event, 1 low-energy electron, 2 positive ion only
+    double r, z, w, secondary_energy, energy_loss;
+    int64_t parent_index;
+};
+
+struct Segment {
+    int kind;  // 0 net chord, 1 escape
+    double a[7];
+    uint64_t channel;
+    uint32_t faces;
+    int64_t parent_index;
+};
+
+struct StepOutputs {
+    std::vector<Secondary> secondaries;
+    std::vector<Source> sources;
+    std::vector<Segment> segments;
+    // per-particle diagnostics for parity: substeps used, events drawn
+    std::vector<uint64_t> subcycles;
+    std::vector<uint64_t> events;
+    std::vector<int32_t> disposition;  // 0 survive, 1 escape, 2 demote, 3 skip (w<=0), -1 invalid input
+    void clear()
+    {
+        secondaries.clear();
+        sources.clear();
+        segments.clear();
+        subcycles.clear();
+        events.clear();
+        disposition.clear();
+    }
+};
+
+// Charged tile view (O/RreaTransportStep.H:454-468): current state written
+// back, prev_* read as the authoritative pre-push state.
+struct ChargedTile {
+    int64_t n = 0;
+    double* r = nullptr;
+    double* z = nullptr;
+    double* theta = nullptr;
+    double* ux = nullptr;
+    double* uy = nullptr;
+    double* uz = nullptr;
+    double const* w = nullptr;
+    double const* prev_r = nullptr;
+    double const* prev_z = nullptr;
+    double const* prev_theta = nullptr;
+    double const* prev_ux = nullptr;
+    double const* prev_uy = nullptr;
+    double const* prev_uz = nullptr;
+    int64_t* id = nullptr;  // > 0 valid; the step negates invalidated ids
+    int32_t const* cpu = nullptr;
+};
+
+struct FieldGrid {
+    int nr = 0, nz = 0;
+    double dr = 0.0, dz = 0.0, z_lo = 0.0;
+    std::vector<double> er, ez, bt, amb_er, amb_ez;
+};
+
+struct CellSources {
+    int nr = 0, nz = 0;
+    std::vector<double> f[5];  // low e-, positive ion, direct negative ion, ionization count, energy loss
+};
+
+// Runs the electron phase of one step (O/RreaElectronTransport.cpp:9-902)
+// over one tile.  Throws OracleError on any fail-closed guard.
+void ApplyElectronTransport(rrea_host::TableSet const& tables, rrea_gpu_config const& cfg,
+                            FieldGrid const& field, int step, double dt_s, ChargedTile& tile,
+                            StepOutputs& out);
+
+// Primitive-level evaluation for fixture comparisons (ids listed in oracle_core.cpp).
+int RunPrimitive(rrea_host::TableSet const& tables, int which, double const* in, int64_t n, double* out);
+
+// O/RreaCouplingSources.cpp:435-512 + S/RreaEventAccumulator.cpp:386-502
+void DepositSources(rrea_gpu_config const& cfg, std::vector<Source> const& sources,
+                    double low_energy_cutoff_eV, CellSources& cells);
+
+}  // namespace oracle

@@ -1,0 +1,334 @@
+// Golden-vector generator built from the REFERENCE's own sources (compiled
+// in place under the reference checkout against oracle/ref_shim) by
+// oracle/Makefile.ref into oracle/_ref/ref_golden.  It evaluates the
+// reference's primitives on seeded inputs and writes inputs and outputs as
+// .npy fixtures under tests/golden/.  Those fixtures pin the oracle
+// restatement (oracle/oracle_core.cpp) and the device kernels to the
+// reference's arithmetic.  Test infrastructure only.
+#include "RreaChargedInterleave.H"
+#include "RreaParticleInteraction.H"
+#include "RreaRng.H"
+#include "rrea/RreaInteractionTables.H"
+#include "rrea/RreaSeedSchedule.H"
+#include "rrea/RreaTransportPath.H"
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+std::string g_outdir;
+
+struct Gen {
+    uint64_t s;
+    explicit Gen(uint64_t seed) : s(seed) {}
+    uint64_t next()
+    {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        return z ^ (z >> 31);
+    }
+    double uni() { return (static_cast<double>(next() >> 11) + 0.5) * 0x1.0p-53; }
+    double logu(double lo, double hi) { return std::exp(std::log(lo) + uni() * (std::log(hi) - std::log(lo))); }
+};
+
+void write_npy(std::string const& name, char const* descr, std::size_t rows, std::size_t cols,
+               void const* data, std::size_t item)
+{
+    std::string path = g_outdir + "/" + name + ".npy";
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) throw std::runtime_error("cannot write " + path);
+    char header[256];
+    int const hl = std::snprintf(header, sizeof(header),
+                                 "{'descr': '%s', 'fortran_order': False, 'shape': (%zu, %zu), }", descr, rows, cols);
+    std::string h(header, static_cast<std::size_t>(hl));
+    std::size_t total = 10 + h.size() + 1;
+    std::size_t pad = (64 - total % 64) % 64;
+    h.append(pad, ' ');
+    h.push_back('\n');
+    unsigned char magic[8] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0};
+    std::fwrite(magic, 1, 8, f);
+    uint16_t const len = static_cast<uint16_t>(h.size());
+    std::fwrite(&len, 2, 1, f);
+    std::fwrite(h.data(), 1, h.size(), f);
+    std::fwrite(data, item, rows * cols, f);
+    std::fclose(f);
+}
+void write_f8(std::string const& name, std::size_t cols, std::vector<double> const& v)
+{
+    write_npy(name, "<f8", v.size() / cols, cols, v.data(), 8);
+}
+void write_u8(std::string const& name, std::size_t cols, std::vector<uint64_t> const& v)
+{
+    write_npy(name, "<u8", v.size() / cols, cols, v.data(), 8);
+}
+
+// Energies that exercise node-exact, ulp-adjacent, threshold and random queries.
+std::vector<double> charged_energies(Gen& g, rrea::RreaInteractionTables const& t, int n_random)
+{
+    std::vector<double> e;
+    double const special[] = {1.0e3, 1.0e4, 5.0e4, 1.0e5, 7.2e6, 1.0e8, 1.0e10};
+    for (double s : special) {
+        e.push_back(s);
+        if (s > 1.0e3) e.push_back(std::nextafter(s, 0.0));
+        if (s < 1.0e10) e.push_back(std::nextafter(s, 1.0e11));
+    }
+    e.push_back(2.0 * t.HardMollerSecondaryThresholdEv());
+    e.push_back(std::nextafter(2.0 * t.HardMollerSecondaryThresholdEv(), 1.0e11));
+    for (int i = 0; i < n_random; ++i) e.push_back(g.logu(1.0e3, 1.0e10));
+    return e;
+}
+
+}  // namespace
+
+int main(int argc, char** argv)
+{
+    if (argc < 3) {
+        std::fprintf(stderr, "usage: ref_golden <transport_physics.json> <outdir>\n");
+        return 2;
+    }
+    g_outdir = argv[2];
+    try {
+        rrea::RreaInteractionTables tables;
+        tables.Load(argv[1]);
+        Gen g(20261203ULL);
+
+        // ---- RNG: O/RreaRng.cpp
+        {
+            std::vector<uint64_t> rows;
+            for (int i = 0; i < 2048; ++i) {
+                rrea::warpx::RreaRngKey k{g.next(), g.next() >> (i % 40), g.next() % 100000, g.next() >> 12,
+                                          g.next() % 140};
+                rows.insert(rows.end(), {k.seed, k.particle_id, k.step, k.interaction_index, k.channel_id,
+                                         rrea::warpx::RreaRng::Counter(k)});
+                double const u = rrea::warpx::RreaRng::Uniform01(k);
+                uint64_t ub;
+                std::memcpy(&ub, &u, 8);
+                rows.push_back(ub);
+            }
+            write_u8("ref_rng", 7, rows);
+        }
+
+        // ---- hot 1-D tables: RreaInteractionTable::Interpolate via ProbeTableValue
+        {
+            char const* names[15] = {
+                "electron_collision_stopping_air", "electron_soft_radiative_stopping_air",
+                "electron_hard_moller_inverse_length_air", "electron_tracked_brems_inverse_length_air",
+                "electron_elastic_transport_inverse_length_air", "positron_collision_stopping_air",
+                "positron_soft_radiative_stopping_air", "positron_hard_bhabha_inverse_length_air",
+                "positron_tracked_brems_inverse_length_air", "positron_elastic_transport_inverse_length_air",
+                "positron_annihilation_inverse_length_air", "photon_compton_inverse_length_air",
+                "photon_photoelectric_inverse_length_air", "photon_pair_nuclear_inverse_length_air",
+                "photon_pair_triplet_inverse_length_air"};
+            std::vector<double> rows;
+            for (int t = 0; t < 15; ++t) {
+                bool const photon = t >= 11;
+                double const lo = photon ? 1.0e3 : 1.0e3, hi = photon ? 1.0e11 : 1.0e10;
+                std::vector<double> es;
+                if (photon) {
+                    for (int i = 0; i < 400; ++i) es.push_back(g.logu(lo, hi));
+                    double const edges[] = {1.0e3, 1.0e11, 1022000.0, 1021997.9, 2043995.8};
+                    for (double x : edges) es.push_back(x);
+                } else {
+                    es = charged_energies(g, tables, 400);
+                }
+                for (double e : es) {
+                    if (e < lo || e > hi) continue;
+                    rows.insert(rows.end(), {static_cast<double>(t), e, tables.ProbeTableValue(names[t], e)});
+                }
+            }
+            write_f8("ref_interp", 3, rows);
+        }
+
+        // ---- electron accessors used by the transport loop
+        {
+            std::vector<double> rows;
+            for (double e : charged_energies(g, tables, 1500)) {
+                double const dr = (g.uni() < 0.5) ? 1.0 : 0.5 + 1.5 * g.uni();
+                rows.insert(rows.end(),
+                            {e, dr, tables.ElectronCollisionLoss(e, dr), tables.ElectronSoftRadiativeDrag(e, dr),
+                             tables.ElectronHardMollerMeanFreePath(e, dr),
+                             tables.ElectronBremsstrahlungMeanFreePath(e, dr),
+                             tables.ElectronHardMollerEnergyLoss(e, dr), tables.ElectronTrackedBremsEnergyLoss(e, dr),
+                             tables.ElasticMeanFreePath(false, e, dr), tables.ScreeningEta(false, e),
+                             tables.ElasticMeanFreePath(true, e, dr), tables.ScreeningEta(true, e)});
+            }
+            write_f8("ref_electron_accessors", 12, rows);
+        }
+
+        // ---- samplers
+        {
+            std::vector<double> gs;
+            for (int i = 0; i < 3000; ++i) {
+                int const sp = i % 2;
+                double const e = (i % 7 == 0) ? g.logu(5.0e7, 1.0e10) : g.logu(1.0e3, 1.0e10);
+                double const n = (i % 11 == 0) ? g.logu(1.0e5, 1.0e7) : g.logu(10.0, 1.0e5);
+                double const u = (i % 13 == 0) ? g.uni() * 1.0e-4 : g.uni();
+                gs.insert(gs.end(), {static_cast<double>(sp), e, n, u,
+                                     tables.SampleGsCosTheta(sp == 1, e, n, u)});
+            }
+            write_f8("ref_gs_angle", 5, gs);
+
+            std::vector<double> single;
+            for (int i = 0; i < 1000; ++i) {
+                int const sp = i % 2;
+                double const e = g.logu(1.0e3, 1.0e10), u = g.uni();
+                single.insert(single.end(), {static_cast<double>(sp), e, u,
+                                             tables.SampleSingleElasticCosTheta(sp == 1, e, u)});
+            }
+            write_f8("ref_single_elastic", 4, single);
+
+            std::vector<double> moller, brems, tsai;
+            for (int i = 0; i < 3000; ++i) {
+                double const em = (i % 17 == 0) ? std::nextafter(1.0e5, 1.0e11) : g.logu(1.000001e5, 1.0e10);
+                double const u = (i % 19 == 0) ? (i % 38 == 0 ? 0.0 : 1.0) : g.uni();
+                moller.insert(moller.end(), {em, u, tables.SampleMollerSecondaryEnergy(em, u)});
+                double const eb = g.logu(5.0001e4, 1.0e10);
+                brems.insert(brems.end(), {eb, u, tables.SampleBremsstrahlungPhotonEnergy(eb, u)});
+                double const et = g.logu(1.0e3, 1.0e10);
+                tsai.insert(tsai.end(), {et, u, tables.SampleBremsstrahlungCosTheta(et, u)});
+            }
+            write_f8("ref_moller_energy", 3, moller);
+            write_f8("ref_brems_energy", 3, brems);
+            write_f8("ref_brems_angle", 3, tsai);
+        }
+
+        // ---- kinematics: O/RreaChargedInterleave.H, I/RreaLorentzPush.H
+        {
+            using namespace rrea::warpx;
+            std::vector<double> kick;
+            for (int i = 0; i < 2000; ++i) {
+                RreaPathFieldSubRange f;
+                f.work_eV = (g.uni() - 0.5) * 2.0e5;
+                f.avg_ex_v_per_m = (g.uni() - 0.5) * 1.0e6;
+                f.avg_ey_v_per_m = (g.uni() - 0.5) * 1.0e6;
+                f.avg_ez_v_per_m = (g.uni() - 0.5) * 1.0e6;
+                double const bs = (i % 3 == 0) ? 0.0 : 1.0e-3;
+                f.avg_bx_t = (g.uni() - 0.5) * bs;
+                f.avg_by_t = (g.uni() - 0.5) * bs;
+                f.avg_bz_t = (g.uni() - 0.5) * bs;
+                double const half_dt = g.logu(1.0e-13, 1.0e-9);
+                double const q = (i % 2) ? 1.0 : -1.0;
+                double k = g.logu(1.0e3, 1.0e9);
+                double dx = g.uni() - 0.5, dy = g.uni() - 0.5, dz = g.uni() - 0.5;
+                RreaNormalizeDirection(dx, dy, dz);
+                std::vector<double> in = {f.work_eV, f.avg_ex_v_per_m, f.avg_ey_v_per_m, f.avg_ez_v_per_m,
+                                          f.avg_bx_t, f.avg_by_t, f.avg_bz_t, half_dt, q, k, dx, dy, dz};
+                (void)RreaApplyChargedFieldHalfKick(f, half_dt, q, k, dx, dy, dz);
+                kick.insert(kick.end(), in.begin(), in.end());
+                kick.insert(kick.end(), {k, dx, dy, dz});
+            }
+            write_f8("ref_half_kick", 17, kick);
+
+            std::vector<double> cone, mol, rec, poi;
+            for (int i = 0; i < 2000; ++i) {
+                double ax = g.uni() - 0.5, ay = g.uni() - 0.5, az = (i % 5 == 0) ? 0.95 : g.uni() - 0.5;
+                double const ct = 2.0 * g.uni() - 1.0, uphi = g.uni();
+                double ox, oy, oz;
+                RreaSampleConeDirection(ax, ay, az, ct, uphi, ox, oy, oz);
+                cone.insert(cone.end(), {ax, ay, az, ct, uphi, ox, oy, oz});
+
+                double const kp = g.logu(1.0e5, 1.0e9), ks = kp * 0.5 * g.uni(), ua = g.uni();
+                double p1, p2, p3, s1, s2, s3;
+                RreaSampleMollerLabDirections(ax, ay, az, kp, ks, ua, p1, p2, p3, s1, s2, s3);
+                mol.insert(mol.end(), {ax, ay, az, kp, ks, ua, p1, p2, p3, s1, s2, s3});
+
+                double cx = ax, cy = ay, cz = az;
+                RreaNormalizeDirection(cx, cy, cz);
+                double const k0 = g.logu(5.0e4, 1.0e9), eg = k0 * g.uni();
+                double gx = g.uni() - 0.5, gy = g.uni() - 0.5, gz = g.uni() - 0.5;
+                std::vector<double> in = {k0, eg, gx, gy, gz, cx, cy, cz};
+                RreaApplyPhotonRecoilToChargedDirection(k0, eg, gx, gy, gz, cx, cy, cz);
+                rec.insert(rec.end(), in.begin(), in.end());
+                rec.insert(rec.end(), {cx, cy, cz});
+
+                double const mean = 10.0 * g.uni(), up = g.uni();
+                poi.insert(poi.end(), {mean, up, static_cast<double>(RreaPoissonSampleCapped(mean, up, 30))});
+            }
+            write_f8("ref_cone", 8, cone);
+            write_f8("ref_moller_dirs", 12, mol);
+            write_f8("ref_photon_recoil", 11, rec);
+            write_f8("ref_poisson", 3, poi);
+
+            std::vector<double> haz;
+            for (int i = 0; i < 2000; ++i) {
+                std::array<double, 3> taus = {g.uni() * 0.05, (i % 4 == 0) ? 0.0 : g.uni() * 0.05,
+                                              (i % 3 == 0) ? g.uni() * 0.01 : 0.0};
+                int const cnt = 2 + (i % 2);
+                double const u1 = (i % 50 == 0) ? 0.999999 : g.uni(), u2 = (i % 37 == 0) ? 1.0 : g.uni();
+                auto const s = RreaSelectCompetingHazard(taus, cnt, u1, u2);
+                haz.insert(haz.end(), {taus[0], taus[1], taus[2], static_cast<double>(cnt), u1, u2,
+                                       static_cast<double>(s.valid), static_cast<double>(s.event),
+                                       static_cast<double>(s.channel), s.sampled_optical_depth,
+                                       s.total_optical_depth});
+            }
+            write_f8("ref_hazard", 11, haz);
+
+            std::vector<double> drag;
+            for (int i = 0; i < 2000; ++i) {
+                double const b = 0.3 * g.uni(), e = b + (1.0 - b) * g.uni();
+                double const cut = 1.0e4, k = cut + g.logu(1.0, 1.0e7);
+                double const stop = (i % 9 == 0) ? 0.5 * cut : k;
+                double const col = g.logu(1.0e2, 1.0e6), soft = (i % 2) ? 0.0 : g.logu(1.0, 1.0e4),
+                             hard = g.logu(1.0, 1.0e3);
+                double const len = g.logu(1.0e-3, 100.0), rho = 0.5 + g.uni();
+                auto plan = RreaPlanContinuousDragSegment(
+                    b, e, k, stop, cut, [&](double bb, double ee) { return len * (ee - bb) * rho; },
+                    [&] { return RreaFrozenStoppingPowers{col, soft, hard}; });
+                drag.insert(drag.end(), {b, e, k, stop, cut, col, soft, hard, len, rho, plan.effective_end_fraction,
+                                         static_cast<double>(plan.applied), static_cast<double>(plan.limit_valid),
+                                         static_cast<double>(plan.reaches_cutoff), plan.drag_loss_eV,
+                                         plan.collision_loss_eV, plan.soft_radiative_loss_eV,
+                                         plan.hard_transfer_loss_eV, plan.raw_collision_loss_eV});
+            }
+            write_f8("ref_drag_plan", 19, drag);
+
+            std::vector<double> chord;
+            for (int i = 0; i < 3000; ++i) {
+                double const rhi = 50.0, zlo = 0.0, zhi = 500.0;
+                double r = (i % 6 == 0) ? 0.0 : rhi * g.uni();
+                if (i % 10 == 1) r = rhi * (1.0 - 1.0e-7 * g.uni());
+                double const th = 2.0 * 3.141592653589793 * g.uni() - 3.141592653589793;
+                double z = zlo + (zhi - zlo) * g.uni();
+                if (i % 10 == 2) z = zhi - 0.05 * g.uni();
+                if (i % 10 == 3) z = zlo + 0.05 * g.uni();
+                RreaRunningChargedState st;
+                st.x_m = r * std::cos(th);
+                st.y_m = r * std::sin(th);
+                st.z_m = z;
+                st.dir_x = g.uni() - 0.5;
+                st.dir_y = g.uni() - 0.5;
+                st.dir_z = g.uni() - 0.5;
+                st.kinetic_energy_eV = g.logu(1.0e3, 1.0e10);
+                double const dt = (i % 4 == 0) ? 5.0e-10 : g.logu(1.0e-12, 1.0e-6);
+                bool const periodic = (i % 8 == 7);
+                auto const ch = RreaBuildRunningChargedChord(st, dt, 5.0e-10, 0.0, rhi, zlo, zhi, periodic);
+                auto const& p = ch.path;
+                double const np = static_cast<double>(p.in_domain_pieces.size());
+                double const p0b = np > 0 ? p.in_domain_pieces[0].begin_fraction : -1.0;
+                double const p0e = np > 0 ? p.in_domain_pieces[0].end_fraction : -1.0;
+                double const p0s = np > 0 ? p.in_domain_pieces[0].wrapped_z_shift_m : 0.0;
+                double const plb = np > 0 ? p.in_domain_pieces.back().begin_fraction : -1.0;
+                double const pls = np > 0 ? p.in_domain_pieces.back().wrapped_z_shift_m : 0.0;
+                chord.insert(chord.end(),
+                             {st.x_m, st.y_m, st.z_m, st.dir_x, st.dir_y, st.dir_z, st.kinetic_energy_eV, dt,
+                              static_cast<double>(periodic), static_cast<double>(ch.valid), p.start_x_m, p.start_y_m,
+                              p.start_z_m, p.end_x_m, p.end_y_m, p.end_z_m, p.full_length_m,
+                              p.in_domain_end_fraction, p.in_domain_length_m, static_cast<double>(p.exits_domain), np,
+                              p0b, p0e, p0s, plb, pls});
+            }
+            write_f8("ref_chord", 26, chord);
+        }
+        std::printf("golden fixtures written to %s\n", g_outdir.c_str());
+    } catch (std::exception const& e) {
+        std::fprintf(stderr, "ref_golden failed: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}

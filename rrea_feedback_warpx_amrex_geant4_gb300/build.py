@@ -1,0 +1,77 @@
+"""Builds the GB300 kinetic-step library in-tree:
+rrea_feedback_warpx_amrex_geant4_gb300/lib/librrea_gpu.so (sm_103a only).
+
+FMA contraction is disabled (--fmad=false) so device arithmetic rounds like
+the reference's x86-64 host build; transcendental calls are the only
+remaining source of last-ulp differences.
+"""
+import os
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+LIBDIR = os.path.join(PKG, "lib")
+LIB = os.path.join(LIBDIR, "librrea_gpu.so")
+
+SOURCES = [
+    os.path.join(CSRC, "rrea_capi.cu"),
+    os.path.join(CSRC, "rrea_kernels.cu"),
+    os.path.join(CSRC, "host", "table_set.cpp"),
+]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    cand = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    return cand if os.path.exists(cand) else "nvcc"
+
+
+def _deps():
+    out = []
+    for d, _, files in os.walk(CSRC):
+        out += [os.path.join(d, f) for f in files if f.endswith((".cu", ".cuh", ".h", ".hpp", ".cpp"))]
+    out.append(os.path.join(ROOT, "include", "rrea_gpu.h"))
+    return out
+
+
+def build(force=False, verbose=False):
+    if not force and os.path.exists(LIB):
+        t = os.path.getmtime(LIB)
+        if all(os.path.getmtime(d) <= t for d in _deps()):
+            return LIB
+    os.makedirs(LIBDIR, exist_ok=True)
+    objdir = os.path.join(PKG, "_build")
+    os.makedirs(objdir, exist_ok=True)
+    nvcc = _nvcc()
+    common = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
+              "-I", CSRC, "-I", os.path.join(ROOT, "include")] + ARCH
+    if verbose:
+        common += ["-Xptxas", "-v"]
+    objs = []
+    procs = []
+    for src in SOURCES:
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
+        cmd = [nvcc, "-c", src, "-o", obj] + common
+        if src.endswith(".cpp"):
+            cmd = [nvcc, "-x", "cu", "-c", src, "-o", obj] + common
+        procs.append((subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT), cmd))
+        objs.append(obj)
+    failed = False
+    for p, cmd in procs:
+        out, _ = p.communicate()
+        if out and (verbose or p.returncode):
+            sys.stdout.write(out.decode(errors="replace"))
+        if p.returncode != 0:
+            failed = True
+    if failed:
+        raise RuntimeError("nvcc compilation failed")
+    tmp = LIB + ".tmp"
+    subprocess.check_call([nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lz", "-lcudart"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose="-v" in sys.argv))

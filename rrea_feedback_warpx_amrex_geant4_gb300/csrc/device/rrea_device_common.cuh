@@ -1,0 +1,387 @@
+// Device-side primitives of the RREA kinetic step: counter RNG, constants,
+// error reporting, and the table queries over the schema-6 arena.
+//
+// Each function restates the reference primitive cited beside it; the
+// arithmetic is kept operation-for-operation so that, compiled without FMA
+// contraction, results agree with the reference to the last ulp except where
+// the device libm (log/exp/sin/cos/atan2/hypot) rounds differently from the
+// host libm.
+#pragma once
+
+#include "../rrea_arena.h"
+#include "../../../include/rrea_gpu.h"
+
+#include <stdint.h>
+
+namespace rrea_dev {
+
+constexpr double kMeC2 = 510998.95000;   // I/RreaConstants.H:9
+constexpr double kC = 299792458.0;       // I/RreaConstants.H:10
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr double kEps = 2.220446049250313080847263336181640625e-16;
+constexpr double kDblMin = 2.2250738585072013830902327173324040642192159804623318306e-308;
+constexpr double kGl2Node = 0.577350269189625764509148780501957;  // I/RreaGaussLegendre8.H:22
+
+// Everything a kernel needs that does not change within a step.
+struct StepConstants {
+    rrea_gpu_config cfg;
+    RreaArenaIndex tix;
+    double dr, dz;
+    double hm_threshold_eV;
+    double photon_cutoff_eV;
+    double density_ratio;
+    uint64_t step_key;
+    double dt_s;
+    int32_t hm_enabled;
+    int32_t pad;
+};
+
+// Per-thread error latch.  Device code never traps: a failing guard records
+// its status here and the particle loop unwinds; the kernel then publishes
+// the first failure to the global status word.
+struct Err {
+    int code = 0;
+    __device__ __forceinline__ void set(int c)
+    {
+        if (code == 0) code = c;
+    }
+};
+
+// ------------------------------------------------------------------ RNG
+// O/RreaRng.cpp:9-44 (counter_splitmix64_v1)
+__device__ __forceinline__ uint64_t splitmix64(uint64_t v)
+{
+    v += 0x9e3779b97f4a7c15ULL;
+    v = (v ^ (v >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    v = (v ^ (v >> 27)) * 0x94d049bb133111ebULL;
+    return v ^ (v >> 31);
+}
+
+// The seed/particle/step words are fixed for a particle-step: fold them once.
+struct RngStream {
+    uint64_t folded;  // splitmix(seed) ^ splitmix(pid+c1) ^ splitmix(step+c2)
+    __device__ __forceinline__ void init(uint64_t seed, uint64_t pid, uint64_t step)
+    {
+        folded = splitmix64(seed) ^ splitmix64(pid + 0x100000001b3ULL) ^ splitmix64(step + 0x9e3779b97f4a7c15ULL);
+    }
+    __device__ __forceinline__ uint64_t counter(uint64_t idx, uint64_t ch) const
+    {
+        uint64_t s = folded;
+        s ^= splitmix64(idx + 0xbf58476d1ce4e5b9ULL);
+        s ^= splitmix64(ch + 0x94d049bb133111ebULL);
+        return splitmix64(s);
+    }
+    __device__ __forceinline__ double uniform(uint64_t idx, uint64_t ch) const
+    {
+        return (__ull2double_rn(counter(idx, ch) >> 12) + 0.5) * 0x1.0p-52;
+    }
+};
+
+// O/RreaRng.H:17-97
+enum : uint64_t {
+    kChHardMollerEnergy = 22, kChHardMollerAzimuth = 23,
+    kChBremsEnergy = 42, kChBremsAngle = 43, kChBremsAzimuth = 44,
+    kChElectronGsAngle = 89, kChElectronGsAzimuth = 90, kChElectronGsFewCount = 91,
+    kChElectronGsFewScatter = 92, kChElectronGsFewAzimuth = 93,
+    kChElectronCompetingOpticalDepth = 107, kChElectronCompetingChannel = 108,
+    kChElectronContinuationOpticalDepth = 124, kChElectronContinuationChannel = 125,
+};
+
+// O/RreaParticleInteraction.H:642-710
+constexpr uint64_t kSegmentCap = uint64_t{1} << 14;
+constexpr uint64_t kEventCap = uint64_t{1} << 13;
+__device__ __forceinline__ bool live_hazard_index(uint64_t species, uint64_t segment, uint64_t ordinal,
+                                                  uint64_t& out)
+{
+    if (segment >= kSegmentCap) return false;
+    if (ordinal == 0U) {
+        out = segment;
+        return true;
+    }
+    if (ordinal >= kEventCap) return false;
+    out = (uint64_t{0} << 51) | (species << 49) | (uint64_t{1} << 35) | (segment << 21) | (ordinal << 8);
+    return true;
+}
+
+// ------------------------------------------------------------------ tables
+// First index i in [0, n) with x[i] >= q (std::lower_bound), n if none.
+__device__ __forceinline__ int lower_bound(const double* __restrict__ x, int n, double q)
+{
+    int lo = 0, count = n;
+    while (count > 0) {
+        int const step = count >> 1;
+        int const mid = lo + step;
+        if (__ldg(x + mid) < q) {
+            lo = mid + 1;
+            count -= step + 1;
+        } else {
+            count = step;
+        }
+    }
+    return lo;
+}
+
+// Bracket of one query on a hot-table grid, shared by every table that uses
+// the same grid (RreaInteractionTable::Interpolate's lower_bound and
+// node-exact tests, S/RreaInteractionTables.cpp:1598-1609).
+struct Bracket {
+    int kind;   // 0 front, 1 back, 2 exact node hi, 3 interior (lo = hi-1)
+    int hi;
+    double t;   // log-space fraction (valid when kind == 3)
+};
+
+__device__ __forceinline__ bool bracket_hot(const double* __restrict__ arena, RreaTable1DIndex const& h,
+                                            double q, Bracket& b, Err& err)
+{
+    const double* x = arena + h.x;
+    int const n = h.n;
+    if (!isfinite(q) || q < __ldg(x) || q > __ldg(x + n - 1)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return false;
+    }
+    int const up = lower_bound(x, n, q);
+    if (up == 0) { b.kind = 0; b.hi = 0; b.t = 0.0; return true; }
+    if (up == n) { b.kind = 1; b.hi = n - 1; b.t = 0.0; return true; }
+    b.hi = up;
+    if (__ldg(x + up) == q) { b.kind = 2; b.t = 0.0; return true; }
+    b.kind = 3;
+    const double* lx = arena + h.lx;
+    if (h.mode == RREA_INTERP_LINEAR) {
+        b.t = (q - __ldg(x + up - 1)) / (__ldg(x + up) - __ldg(x + up - 1));
+    } else {
+        b.t = (log(q) - __ldg(lx + up - 1)) / (__ldg(lx + up) - __ldg(lx + up - 1));
+    }
+    return true;
+}
+
+// Value of one hot table at a prepared bracket
+// (S/RreaInteractionTables.cpp:1599-1629).
+__device__ __forceinline__ double eval_hot(const double* __restrict__ arena, RreaTable1DIndex const& h,
+                                           Bracket const& b, Err& err)
+{
+    const double* y = arena + h.y;
+    if (b.kind == 0) return __ldg(y);
+    if (b.kind == 1) return __ldg(y + h.n - 1);
+    if (b.kind == 2) return __ldg(y + b.hi);
+    double const ylo = __ldg(y + b.hi - 1), yhi = __ldg(y + b.hi);
+    if (h.mode == RREA_INTERP_LINEAR) return ylo + b.t * (yhi - ylo);
+    bool const pos = ylo > 0.0 && yhi > 0.0;
+    if (h.mode == RREA_INTERP_LOGX_LINEAR || (h.mode == RREA_INTERP_LOGLOG_ZERO_THRESHOLD && !pos)) {
+        return ylo + b.t * (yhi - ylo);
+    }
+    if (!pos) {
+        err.set(RREA_GPU_ERR_INVALID_STATE);
+        return 0.0;
+    }
+    const double* ly = arena + h.ly;
+    double const llo = __ldg(ly + b.hi - 1), lhi = __ldg(ly + b.hi);
+    return exp(llo + b.t * (lhi - llo));
+}
+
+__device__ __forceinline__ double interpolate(const double* __restrict__ arena, RreaTable1DIndex const& h, double q,
+                                              Err& err)
+{
+    Bracket b;
+    if (!bracket_hot(arena, h, q, b, err)) return 0.0;
+    return eval_hot(arena, h, b, err);
+}
+
+// S/RreaInteractionTables.cpp:624-648 (interp_semilogx_strict)
+__device__ __forceinline__ double semilogx(const double* __restrict__ x, const double* __restrict__ lx,
+                                           const double* __restrict__ y, int n, double q, Err& err)
+{
+    if (!isfinite(q) || q < __ldg(x) || q > __ldg(x + n - 1)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return 0.0;
+    }
+    if (q == __ldg(x)) return __ldg(y);
+    if (q == __ldg(x + n - 1)) return __ldg(y + n - 1);
+    int const hi = lower_bound(x, n, q);
+    if (__ldg(x + hi) == q) return __ldg(y + hi);
+    int const lo = hi - 1;
+    double const t = (log(q) - __ldg(lx + lo)) / (__ldg(lx + hi) - __ldg(lx + lo));
+    return __ldg(y + lo) + t * (__ldg(y + hi) - __ldg(y + lo));
+}
+
+// S/RreaInteractionTables.cpp:110-119
+__device__ __forceinline__ double mfp_from_inverse(double inv, Err& err)
+{
+    if (!isfinite(inv) || inv < 0.0) {
+        err.set(RREA_GPU_ERR_INVALID_STATE);
+        return 1.0e99;
+    }
+    return inv > 0.0 ? 1.0 / inv : 1.0e99;
+}
+
+// O/RreaMaterialPath.H:213-222
+__device__ __forceinline__ double frozen_rate(double v, Err& err)
+{
+    if (!isfinite(v) || v < 0.0) {
+        err.set(RREA_GPU_ERR_INVALID_STATE);
+        return 0.0;
+    }
+    return v;
+}
+
+__device__ __forceinline__ bool charged_in_range(RreaArenaIndex const& ix, double e)
+{
+    return isfinite(e) && e >= ix.charged_min_eV && e <= ix.charged_max_eV;
+}
+
+// Conditional inverse-CDF sampling: S/RreaInteractionTables.cpp:995-1069;
+// `moller` selects the Moller variant (:2584-2653) that log-interpolates
+// between groups without the positivity test.
+__device__ __forceinline__ double sample_conditional(const double* __restrict__ arena, RreaCondCdfIndex const& ci,
+                                                     double e, double cdf_u, bool moller, Err& err)
+{
+    const double* prim = arena + ci.primary;
+    const double* lprim = arena + ci.lprimary;
+    const double* start = arena + ci.start;
+    const double* u = arena + ci.u;
+    const double* v = arena + ci.v;
+    cdf_u = fmax(0.0, fmin(1.0, cdf_u));
+    int const ng = ci.ng;
+    if (!isfinite(e) || e < __ldg(prim) || e > __ldg(prim + ng - 1)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return 0.0;
+    }
+    auto sample_group = [&](int g) {
+        int const b = static_cast<int>(__ldg(start + g));
+        int const en = static_cast<int>(__ldg(start + g + 1));
+        int const up = b + lower_bound(u + b, en - b, cdf_u);
+        if (up == b) return __ldg(v + b);
+        if (up == en) return __ldg(v + en - 1);
+        int const lo = up - 1;
+        double const denom = __ldg(u + up) - __ldg(u + lo);
+        double const t = denom > 0.0 ? (cdf_u - __ldg(u + lo)) / denom : 0.0;
+        return __ldg(v + lo) + t * (__ldg(v + up) - __ldg(v + lo));
+    };
+    int const up = lower_bound(prim, ng, e);
+    if (up == 0) return sample_group(0);
+    if (up == ng) return sample_group(ng - 1);
+    if (__ldg(prim + up) == e) return sample_group(up);
+    int const lo = up - 1;
+    double const y0 = sample_group(lo);
+    double const y1 = sample_group(up);
+    double const t = (log(e) - __ldg(lprim + lo)) / (__ldg(lprim + up) - __ldg(lprim + lo));
+    if (moller || (y0 > 0.0 && y1 > 0.0)) {
+        return exp(log(y0) + t * (log(y1) - log(y0)));
+    }
+    return y0 + t * (y1 - y0);
+}
+
+// S/RreaInteractionTables.cpp:1071-1110 (group means are per-group constants;
+// they are accumulated here in the reference's order).
+__device__ __forceinline__ double group_mean(const double* __restrict__ arena, RreaCondCdfIndex const& ci, int g)
+{
+    const double* start = arena + ci.start;
+    const double* u = arena + ci.u;
+    const double* v = arena + ci.v;
+    int const b = static_cast<int>(__ldg(start + g)), en = static_cast<int>(__ldg(start + g + 1));
+    double mean = __ldg(u + b) * __ldg(v + b);
+    for (int i = b + 1; i < en; ++i) {
+        mean += 0.5 * (__ldg(v + i - 1) + __ldg(v + i)) * (__ldg(u + i) - __ldg(u + i - 1));
+    }
+    mean += (1.0 - __ldg(u + en - 1)) * __ldg(v + en - 1);
+    return mean;
+}
+
+__device__ __forceinline__ double mean_conditional(const double* __restrict__ arena, RreaCondCdfIndex const& ci,
+                                                   double e, Err& err)
+{
+    const double* prim = arena + ci.primary;
+    const double* lprim = arena + ci.lprimary;
+    int const ng = ci.ng;
+    if (e < __ldg(prim) || e > __ldg(prim + ng - 1)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return 0.0;
+    }
+    int const up = lower_bound(prim, ng, e);
+    if (up == 0) return group_mean(arena, ci, 0);
+    if (up == ng) return group_mean(arena, ci, ng - 1);
+    if (__ldg(prim + up) == e) return group_mean(arena, ci, up);
+    int const lo = up - 1;
+    double const y0 = group_mean(arena, ci, lo), y1 = group_mean(arena, ci, up);
+    double const t = (log(e) - __ldg(lprim + lo)) / (__ldg(lprim + up) - __ldg(lprim + lo));
+    return y0 > 0.0 && y1 > 0.0 ? exp(log(y0) + t * (log(y1) - log(y0))) : y0 + t * (y1 - y0);
+}
+
+// S/RreaInteractionTables.cpp:807-827
+__device__ __forceinline__ void log_bracket(const double* __restrict__ g, const double* __restrict__ lg, int n,
+                                            double q, int& i, double& frac, Err& err)
+{
+    int const last = n - 1;
+    if (!isfinite(q) || q < __ldg(g) || q > __ldg(g + last)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        i = 0;
+        frac = 0.0;
+        return;
+    }
+    if (q == __ldg(g)) { i = 0; frac = 0.0; return; }
+    if (q == __ldg(g + last)) { i = last - 1; frac = 1.0; return; }
+    int lo = 0, hi = last;
+    while (hi - lo > 1) {
+        int const m = (lo + hi) / 2;
+        if (__ldg(g + m) <= q) lo = m; else hi = m;
+    }
+    i = lo;
+    double const llo = __ldg(lg + lo), lhi = __ldg(lg + hi);
+    if (lhi == llo) {
+        frac = (q == __ldg(g + lo)) ? 0.0 : 1.0;
+        return;
+    }
+    frac = (log(q) - llo) / (lhi - llo);
+}
+
+// S/RreaInteractionTables.cpp:831-891 (node logs read precomputed)
+__device__ __forceinline__ double sample_gs_angle(const double* __restrict__ arena, RreaAngleIndex const& a,
+                                                  double e, double n, double u, Err& err)
+{
+    int const np = a.np, nu = a.nu;
+    int ie = 0, ip = 0;
+    double te = 0.0, tn = 0.0;
+    log_bracket(arena + a.e, arena + a.le, a.ne, e, ie, te, err);
+    log_bracket(arena + a.p, arena + a.lp, a.np, n, ip, tn, err);
+    if (err.code) return 1.0;
+    const double* lomc = arena + a.lomc;
+    const double* cu = arena + a.u;
+    const double* lur = arena + a.lur;
+    size_t const b00 = (static_cast<size_t>(ie) * np + ip) * nu;
+    size_t const b10 = (static_cast<size_t>(ie + 1) * np + ip) * nu;
+    size_t const b01 = (static_cast<size_t>(ie) * np + ip + 1) * nu;
+    size_t const b11 = (static_cast<size_t>(ie + 1) * np + ip + 1) * nu;
+    double const w00 = (1 - te) * (1 - tn), w10 = te * (1 - tn), w01 = (1 - te) * tn, w11 = te * tn;
+    auto omc_at = [&](int iu) {
+        double const lxx = w00 * __ldg(lomc + b00 + iu) + w10 * __ldg(lomc + b10 + iu)
+            + w01 * __ldg(lomc + b01 + iu) + w11 * __ldg(lomc + b11 + iu);
+        double const cos_node = 1.0 - exp(lxx);
+        return fmax(1.0 - cos_node, kDblMin);
+    };
+    int const first = 1, last = nu - 2;
+    double one_minus_cos;
+    if (last <= first) {
+        one_minus_cos = omc_at(first);
+    } else if (u <= __ldg(cu + first)) {
+        double const d1 = omc_at(first), d2 = omc_at(first + 1);
+        double const u1 = __ldg(cu + first);
+        double const slope = log(d2 / d1) / __ldg(lur + first);
+        double const ueff = fmax(u, u1 * 1.0e-6);
+        one_minus_cos = d1 * exp(slope * log(ueff / u1));
+    } else if (u >= __ldg(cu + last)) {
+        one_minus_cos = omc_at(last);
+    } else {
+        int lo = first, hi = last;
+        while (hi - lo > 1) {
+            int const m = (lo + hi) / 2;
+            if (__ldg(cu + m) <= u) lo = m; else hi = m;
+        }
+        double const d0 = omc_at(lo), d1 = omc_at(hi);
+        // hi == lo + 1 here, so the denominator is the precomputed node ratio log.
+        double const fu = log(u / __ldg(cu + lo)) / __ldg(lur + lo);
+        one_minus_cos = d0 * exp(fu * log(d1 / d0));
+    }
+    double const c = 1.0 - fmin(2.0, one_minus_cos);
+    return fmin(1.0, fmax(-1.0, c));
+}
+
+}  // namespace rrea_dev

@@ -1,0 +1,601 @@
+// Device transport geometry and kinematics: chord construction and RZ
+// clipping, material path, path field work, half kick, cone sampling and
+// the competing-hazard selection.  Register-resident, fixed-capacity
+// structures replace the reference's heap vectors; the arithmetic follows the
+// cited reference primitives operation for operation.
+#pragma once
+
+#include "rrea_device_common.cuh"
+
+namespace rrea_dev {
+
+// I/RreaTransportPath.H:13-73
+struct Piece {
+    double begin, end, length, shift;
+};
+
+struct Path {
+    double sx, sy, sz, ex, ey, ez;
+    double full, in_begin, in_end, in_length;
+    bool exits;
+    int npieces;
+    Piece pieces[RREA_ARENA_MAX_PIECES];
+};
+
+struct Geom {
+    double rlo, rhi, zlo, zhi;
+    bool periodic;
+};
+
+// S/RreaTransportPath.cpp:13-27
+__device__ __forceinline__ double wrap_z(Geom const& g, double z)
+{
+    if (!g.periodic) return z;
+    double const len = g.zhi - g.zlo;
+    if (!(len > 0.0)) return z;
+    double w = fmod(z - g.zlo, len);
+    if (w < 0.0) w += len;
+    return g.zlo + w;
+}
+// S/RreaTransportPath.cpp:42-52
+__device__ __forceinline__ void point_at_full(Path const& p, Geom const& g, double f, double& x, double& y, double& z)
+{
+    f = fmax(0.0, fmin(1.0, f));
+    x = p.sx + f * (p.ex - p.sx);
+    y = p.sy + f * (p.ey - p.sy);
+    z = wrap_z(g, p.sz + f * (p.ez - p.sz));
+}
+// S/RreaTransportPath.cpp:54-71
+__device__ __forceinline__ void point_at_piece(Path const& p, Geom const& g, Piece const& pc, double f, double& x,
+                                               double& y, double& z)
+{
+    f = fmax(pc.begin, fmin(pc.end, f));
+    x = p.sx + f * (p.ex - p.sx);
+    y = p.sy + f * (p.ey - p.sy);
+    z = p.sz + f * (p.ez - p.sz) + pc.shift;
+    z = fmax(g.zlo, fmin(g.zhi, z));
+}
+// S/RreaTransportPath.cpp:29-40
+__device__ __forceinline__ bool outside_certified(Geom const& g, double r, double z)
+{
+    if (!isfinite(r) || !isfinite(z)) return true;
+    if (r < g.rlo || r >= g.rhi) return true;
+    return !g.periodic && (z < g.zlo || z >= g.zhi);
+}
+
+// S/RreaTransportPath.cpp:73-295.  Periodic seams use double arithmetic where
+// the host reference uses long double.
+__device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double r1, double th1, double z1,
+                                        Geom const& g, Path& p, Err& err)
+{
+    if (!isfinite(r0) || !isfinite(th0) || !isfinite(z0) || !isfinite(r1) || !isfinite(th1) || !isfinite(z1)
+        || r0 < 0.0 || r1 < 0.0) {
+        err.set(RREA_GPU_ERR_GEOMETRY);
+        p.npieces = 0;
+        p.full = 0.0;
+        p.in_begin = p.in_end = p.in_length = 0.0;
+        p.exits = false;
+        return;
+    }
+    double s0, c0, s1, c1;
+    sincos(th0, &s0, &c0);
+    sincos(th1, &s1, &c1);
+    p.sx = r0 * c0;
+    p.sy = r0 * s0;
+    p.sz = z0;
+    p.ex = r1 * c1;
+    p.ey = r1 * s1;
+    p.ez = z1;
+    double const dx = p.ex - p.sx, dy = p.ey - p.sy, dz = p.ez - p.sz;
+    p.full = sqrt(dx * dx + dy * dy + dz * dz);
+    p.in_begin = 0.0;
+    double const scale = fmax(1.0, fmax(g.rhi, fmax(fabs(g.zlo), fabs(g.zhi))));
+    double const tol = 64.0 * kEps * scale;
+    if (r0 < g.rlo - tol || r0 > g.rhi + tol || z0 < g.zlo - tol || z0 > g.zhi + tol) {
+        err.set(RREA_GPU_ERR_GEOMETRY);
+    }
+    double exit_fraction = 1.0;
+    if (!g.periodic) {
+        if (dz > 0.0) {
+            double const c = (g.zhi - z0) / dz;
+            if (c >= 0.0 && c < exit_fraction) exit_fraction = c;
+        } else if (dz < 0.0) {
+            double const c = (g.zlo - z0) / dz;
+            if (c >= 0.0 && c < exit_fraction) exit_fraction = c;
+        }
+    }
+    double const a = dx * dx + dy * dy;
+    if (a > 0.0) {
+        double const b = 2.0 * (p.sx * dx + p.sy * dy);
+        for (int cyl = 0; cyl < 2; ++cyl) {
+            bool const outer = cyl == 0;
+            double const radius = outer ? g.rhi : g.rlo;
+            if (!outer && !(g.rlo > 0.0)) break;
+            double const c = p.sx * p.sx + p.sy * p.sy - radius * radius;
+            double const disc = b * b - 4.0 * a * c;
+            if (disc < 0.0) continue;
+            double const root = sqrt(fmax(disc, 0.0));
+            double const inv2a = 0.5 / a;
+            double const roots[2] = {(-b - root) * inv2a, (-b + root) * inv2a};
+            for (int q = 0; q < 2; ++q) {
+                double const cand = roots[q];
+                if (cand <= 0.0 || cand > 1.0) continue;
+                double const deriv = 2.0 * a * cand + b;
+                bool const leaves = outer ? deriv > 0.0 : deriv < 0.0;
+                if (leaves && cand >= 0.0 && cand < exit_fraction) exit_fraction = cand;
+            }
+        }
+    }
+    p.in_end = fmax(0.0, fmin(1.0, exit_fraction));
+    p.in_length = p.full * (p.in_end - p.in_begin);
+    p.exits = p.in_end < 1.0 - 64.0 * kEps;
+
+    // Breakpoints: [in_begin, seams..., in_end], sorted and deduplicated.
+    double bp[RREA_ARENA_MAX_PIECES + 1];
+    int nb = 0;
+    bp[nb++] = p.in_begin;
+    if (g.periodic && fabs(dz) > 0.0 && p.in_end > p.in_begin) {
+        double const zend = z0 + dz * p.in_end;
+        double const period = g.zhi - g.zlo;
+        double const low = fmin(z0, zend), high = fmax(z0, zend);
+        double const first = floor((low - g.zlo) / period) + 1.0;
+        double const last = ceil((high - g.zlo) / period) - 1.0;
+        for (double image = first; image <= last; image += 1.0) {
+            double const seam = g.zlo + image * period;
+            double const frac = (seam - z0) / dz;
+            double const ftol = 128.0 * kEps * fmax(1.0, fabs(frac));
+            if (frac > p.in_begin + ftol && frac < p.in_end - ftol) {
+                if (nb >= RREA_ARENA_MAX_PIECES) {
+                    err.set(RREA_GPU_ERR_CAPACITY);
+                    break;
+                }
+                bp[nb++] = frac;
+            }
+        }
+    }
+    bp[nb++] = p.in_end;
+    // insertion sort (tiny)
+    for (int i = 1; i < nb; ++i) {
+        double const v = bp[i];
+        int j = i - 1;
+        while (j >= 0 && bp[j] > v) {
+            bp[j + 1] = bp[j];
+            --j;
+        }
+        bp[j + 1] = v;
+    }
+    // std::unique with a relative tolerance
+    int nu = 0;
+    for (int i = 0; i < nb; ++i) {
+        if (nu > 0) {
+            double const l = bp[nu - 1], r = bp[i];
+            if (fabs(l - r) <= 128.0 * kEps * fmax(1.0, fmax(fabs(l), fabs(r)))) continue;
+        }
+        bp[nu++] = bp[i];
+    }
+    double const period_m = g.zhi - g.zlo;
+    p.npieces = 0;
+    for (int i = 1; i < nu; ++i) {
+        double const b0 = bp[i - 1], e0 = bp[i];
+        if (!(e0 > b0)) continue;
+        double shift = 0.0;
+        if (g.periodic) {
+            double const mid = 0.5 * (b0 + e0);
+            double const mid_z = z0 + mid * dz;
+            double const image = floor((mid_z - g.zlo) / period_m);
+            shift = -image * period_m;
+        }
+        p.pieces[p.npieces++] = Piece{b0, e0, p.full * (e0 - b0), shift};
+    }
+}
+
+// ------------------------------------------------------------ kinematics
+// I/RreaSeedSchedule.H:31-43
+__device__ __forceinline__ double proper_velocity_from_kinetic(double k)
+{
+    if (k <= 0.0) return 0.0;
+    double const gm = 1.0 + k / kMeC2;
+    return kC * sqrt(fmax(gm * gm - 1.0, 0.0));
+}
+// O/RreaParticleInteraction.H:1494-1506
+__device__ __forceinline__ double kinetic_from_proper_velocity(double ux, double uy, double uz)
+{
+    double const u2 = ux * ux + uy * uy + uz * uz;
+    double const gm = sqrt(1.0 + u2 / (kC * kC));
+    return u2 * kMeC2 / ((kC * kC) * (gm + 1.0));
+}
+// O/RreaParticleInteraction.H:92-105
+__device__ __forceinline__ double charged_speed(double k)
+{
+    if (!isfinite(k) || k < 0.0) return __longlong_as_double(0x7ff8000000000000LL);
+    double const gm = 1.0 + k / kMeC2;
+    double const b2 = fmax(0.0, 1.0 - 1.0 / (gm * gm));
+    return kC * sqrt(b2);
+}
+// O/RreaChargedInterleave.H:294-307
+__device__ __forceinline__ void normalize(double& x, double& y, double& z)
+{
+    double const n = sqrt(x * x + y * y + z * z);
+    if (n <= 0.0) {
+        x = 0.0; y = 0.0; z = 1.0;
+        return;
+    }
+    x /= n; y /= n; z /= n;
+}
+// O/RreaChargedInterleave.H:309-364
+__device__ __forceinline__ void cone_direction(double ax, double ay, double az, double cos_t, double u_phi,
+                                               double& ox, double& oy, double& oz)
+{
+    normalize(ax, ay, az);
+    double dx = ax, dy = ay, dz = az;
+    normalize(dx, dy, dz);
+    double rx = 0.0, ry = 0.0, rz = 1.0;
+    if (fabs(dz) > 0.9) { rx = 1.0; rz = 0.0; }
+    double b1x = ry * dz - rz * dy, b1y = rz * dx - rx * dz, b1z = rx * dy - ry * dx;
+    normalize(b1x, b1y, b1z);
+    double b2x = dy * b1z - dz * b1y, b2y = dz * b1x - dx * b1z, b2z = dx * b1y - dy * b1x;
+    normalize(b2x, b2y, b2z);
+    cos_t = fmin(1.0, fmax(-1.0, cos_t));
+    double const sin_t = sqrt(fmax(0.0, 1.0 - cos_t * cos_t));
+    double const phi = kTwoPi * u_phi;
+    double sp, cp;
+    sincos(phi, &sp, &cp);
+    ox = ax * cos_t + sin_t * (cp * b1x + sp * b2x);
+    oy = ay * cos_t + sin_t * (cp * b1y + sp * b2y);
+    oz = az * cos_t + sin_t * (cp * b1z + sp * b2z);
+    normalize(ox, oy, oz);
+}
+// O/RreaChargedInterleave.H:371-389
+__device__ __forceinline__ int poisson_capped(double mean, double u, int kmax)
+{
+    if (mean <= 0.0) return 0;
+    double p = exp(-mean);
+    double cum = p;
+    int k = 0;
+    while (u > cum && k < kmax) {
+        ++k;
+        p *= mean / static_cast<double>(k);
+        cum += p;
+    }
+    return k;
+}
+__device__ __forceinline__ double unit_cycle(double u)
+{
+    u -= floor(u);
+    return u < 0.0 ? u + 1.0 : u;
+}
+// O/RreaChargedInterleave.H:391-463
+__device__ __forceinline__ double moller_cos(double kp, double ks_or_scat)
+{
+    double const v = ks_or_scat * (kp + 2.0 * kMeC2) / (kp * (ks_or_scat + 2.0 * kMeC2));
+    return sqrt(fmin(1.0, fmax(0.0, v)));
+}
+__device__ __forceinline__ void moller_lab_directions(double px, double py, double pz, double kp, double ks,
+                                                      double u_az, double& opx, double& opy, double& opz,
+                                                      double& osx, double& osy, double& osz)
+{
+    normalize(px, py, pz);
+    u_az = unit_cycle(u_az);
+    double cs;
+    {
+        double const a = fmax(kp, 0.0), b = fmax(ks, 0.0);
+        cs = (a <= 0.0 || b <= 0.0) ? 1.0 : moller_cos(a, b);
+    }
+    double cpm;
+    {
+        double const scat = fmax(0.0, kp - ks);
+        cpm = (kp <= 0.0 || scat <= 0.0) ? 1.0 : moller_cos(kp, scat);
+    }
+    cone_direction(px, py, pz, cs, u_az, osx, osy, osz);
+    cone_direction(px, py, pz, cpm, unit_cycle(u_az + 0.5), opx, opy, opz);
+}
+// O/RreaChargedInterleave.H:465-496
+__device__ __forceinline__ void photon_recoil(double k0, double eg, double gx, double gy, double gz, double& cx,
+                                              double& cy, double& cz)
+{
+    eg = fmax(eg, 0.0);
+    if (k0 <= 0.0 || eg <= 0.0) return;
+    normalize(cx, cy, cz);
+    normalize(gx, gy, gz);
+    double const p0 = sqrt(fmax(0.0, k0 * (k0 + 2.0 * kMeC2)));
+    double const px = p0 * cx - eg * gx, py = p0 * cy - eg * gy, pz = p0 * cz - eg * gz;
+    double const n = sqrt(px * px + py * py + pz * pz);
+    if (n > 0.0) {
+        cx = px / n; cy = py / n; cz = pz / n;
+        normalize(cx, cy, cz);
+    }
+}
+
+struct FieldRange {
+    double work, ex, ey, ez, bx, by, bz, length;
+};
+
+// O/RreaChargedInterleave.H:100-138 with the Boris rotation of
+// I/RreaLorentzPush.H:21-46
+__device__ __forceinline__ void half_kick(FieldRange const& f, double half_dt, double q, double& k, double& dx,
+                                          double& dy, double& dz)
+{
+    double const umag = proper_velocity_from_kinetic(k);
+    double const s = q * (kC * kC / kMeC2) * half_dt;
+    double const uxm = umag * dx + s * f.ex;
+    double const uym = umag * dy + s * f.ey;
+    double const uzm = umag * dz + s * f.ez;
+    double const gamma = sqrt(1.0 + (uxm * uxm + uym * uym + uzm * uzm) / (kC * kC));
+    double const tx = s * f.bx / (2.0 * gamma), ty = s * f.by / (2.0 * gamma), tz = s * f.bz / (2.0 * gamma);
+    double const t2 = tx * tx + ty * ty + tz * tz;
+    double const sx = 2.0 * tx / (1.0 + t2), sy = 2.0 * ty / (1.0 + t2), sz = 2.0 * tz / (1.0 + t2);
+    double const ppx = uxm + uym * tz - uzm * ty;
+    double const ppy = uym + uzm * tx - uxm * tz;
+    double const ppz = uzm + uxm * ty - uym * tx;
+    double const ux = uxm + ppy * sz - ppz * sy;
+    double const uy = uym + ppz * sx - ppx * sz;
+    double const uz = uzm + ppx * sy - ppy * sx;
+    double const norm = sqrt(ux * ux + uy * uy + uz * uz);
+    if (norm > 0.0 && isfinite(norm)) {
+        dx = ux / norm; dy = uy / norm; dz = uz / norm;
+    }
+    k = fmax(0.0, k + 0.5 * f.work);
+}
+
+// ------------------------------------------------------------ field gather
+// Cell-centred total field (Maxwell + ambient face averages, computed once
+// per step by a prep kernel exactly as S/RreaAmrexAdvance.cpp:556-565 forms
+// them) and the corner Btheta of the replicated Maxwell vectors.
+struct FieldView {
+    const double* __restrict__ cell_er;  // nr*nz, i + nr*j
+    const double* __restrict__ cell_ez;  // nr*nz
+    const double* __restrict__ bt;       // (nr+1)*(nz+1), i + (nr+1)*j
+    int nr, nz;
+    double dr, dz, r_lo, z_lo;
+    bool periodic;
+    bool has_b;
+};
+
+// S/RreaAmrexAdvance.cpp:532-579 with I/RreaFieldGatherStencil.H:49-133 and
+// MaxwellBthetaAt :511-530
+__device__ __forceinline__ void gather(FieldView const& fv, double r, double z, double& er, double& ez, double& bth)
+{
+    double const fx = (r - fv.r_lo) / fv.dr + 0.0 - 0.5;
+    double const fz = (z - fv.z_lo) / fv.dz + 0.0 - 0.5;
+    double const flx = floor(fx), flz = floor(fz);
+    int const ir0 = static_cast<int>(flx);
+    int const iz0 = static_cast<int>(flz);
+    double const tx = fx - static_cast<double>(ir0);
+    double const tz = fz - static_cast<double>(iz0);
+    int const i0 = max(0, min(fv.nr - 1, ir0));
+    int const i1 = max(0, min(fv.nr - 1, ir0 + 1));
+    int j0, j1;
+    if (fv.periodic) {
+        j0 = (iz0 + fv.nz) % fv.nz;
+        j1 = (iz0 + 1 + fv.nz) % fv.nz;
+    } else {
+        j0 = max(0, min(fv.nz - 1, iz0));
+        j1 = max(0, min(fv.nz - 1, iz0 + 1));
+    }
+    size_t const r0 = static_cast<size_t>(fv.nr) * j0, r1 = static_cast<size_t>(fv.nr) * j1;
+    double const e00 = __ldg(fv.cell_er + i0 + r0), e01 = __ldg(fv.cell_er + i0 + r1);
+    double const e10 = __ldg(fv.cell_er + i1 + r0), e11 = __ldg(fv.cell_er + i1 + r1);
+    double const z00 = __ldg(fv.cell_ez + i0 + r0), z01 = __ldg(fv.cell_ez + i0 + r1);
+    double const z10 = __ldg(fv.cell_ez + i1 + r0), z11 = __ldg(fv.cell_ez + i1 + r1);
+    double const first_center = fv.r_lo + 0.5 * fv.dr;
+    double const axis = r >= first_center ? 1.0 : fmax(0.0, (r - fv.r_lo) / (0.5 * fv.dr));
+    er = ((1.0 - tx) * ((1.0 - tz) * e00 + tz * e01) + tx * ((1.0 - tz) * e10 + tz * e11)) * axis;
+    ez = (1.0 - tx) * ((1.0 - tz) * z00 + tz * z01) + tx * ((1.0 - tz) * z10 + tz * z11);
+    if (!fv.has_b || r <= 0.0) {
+        bth = 0.0;
+        if (!fv.has_b && r > 0.0) bth = 0.0;
+        return;
+    }
+    double const fr = fmin(fmax(r / fv.dr, 0.0), static_cast<double>(fv.nr));
+    double const fzz = fmin(fmax((z - fv.z_lo) / fv.dz, 0.0), static_cast<double>(fv.nz));
+    int const a0 = min(static_cast<int>(floor(fr)), fv.nr - 1);
+    int const b0 = min(static_cast<int>(floor(fzz)), fv.nz - 1);
+    double const tr = fr - a0, tzz = fzz - b0;
+    size_t const w = static_cast<size_t>(fv.nr + 1);
+    bth = (1.0 - tr) * ((1.0 - tzz) * __ldg(fv.bt + a0 + w * b0) + tzz * __ldg(fv.bt + a0 + w * (b0 + 1)))
+        + tr * ((1.0 - tzz) * __ldg(fv.bt + a0 + 1 + w * b0) + tzz * __ldg(fv.bt + a0 + 1 + w * (b0 + 1)));
+}
+
+// O/RreaPathFieldWork.H:57-150 with the two-node rule of
+// I/RreaGaussLegendre8.H:24-60
+__device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom const& g, Path const& p, double q,
+                                                      double begin, double end, Err& err)
+{
+    FieldRange res{0, 0, 0, 0, 0, 0, 0, 0};
+    if (!(p.full > 0.0)) return res;
+    begin = fmax(p.in_begin, begin);
+    end = fmin(p.in_end, end);
+    if (!(end > begin)) return res;
+    double const pdx = (p.ex - p.sx) / p.full;
+    double const pdy = (p.ey - p.sy) / p.full;
+    double const pdz = (p.ez - p.sz) / p.full;
+    for (int ip = 0; ip < p.npieces; ++ip) {
+        Piece const& pc = p.pieces[ip];
+        double const pb = fmax(begin, pc.begin);
+        double const pe = fmin(end, pc.end);
+        if (!(pe > pb)) continue;
+        double const mid = 0.5 * (pb + pe);
+        double const half = 0.5 * (pe - pb);
+        double const off = half * kGl2Node;
+        double acc[7];
+#pragma unroll
+        for (int node = 0; node < 2; ++node) {
+            double const f = node == 0 ? mid - off : mid + off;
+            double x, y, z;
+            point_at_piece(p, g, pc, f, x, y, z);
+            double const r = hypot(x, y);
+            double rad = 0.0, rc = 1.0, rs = 0.0;
+            if (r > 0.0) {
+                rad = (pdx * x + pdy * y) / r;
+                rc = x / r;
+                rs = y / r;
+            }
+            double er, ez, bth;
+            gather(fv, r, z, er, ez, bth);
+            double const work = q * (er * rad + ez * pdz) * 1.0;
+            if (!isfinite(work) || !isfinite(er) || !isfinite(ez) || !isfinite(bth)) {
+                err.set(RREA_GPU_ERR_INVALID_STATE);
+            }
+            double const v[7] = {work, er * rc, er * rs, ez, -bth * rs, bth * rc, 0.0};
+            if (node == 0) {
+#pragma unroll
+                for (int c = 0; c < 7; ++c) acc[c] = v[c];
+            } else {
+#pragma unroll
+                for (int c = 0; c < 7; ++c) acc[c] = half * (acc[c] + v[c]);
+            }
+        }
+        res.work += p.full * acc[0];
+        res.ex += p.full * acc[1];
+        res.ey += p.full * acc[2];
+        res.ez += p.full * acc[3];
+        res.bx += p.full * acc[4];
+        res.by += p.full * acc[5];
+        res.bz += p.full * acc[6];
+        res.length += p.full * (pe - pb);
+    }
+    if (res.length > 0.0) {
+        res.ex /= res.length; res.ey /= res.length; res.ez /= res.length;
+        res.bx /= res.length; res.by /= res.length; res.bz /= res.length;
+    }
+    return res;
+}
+
+// ------------------------------------------------------------ material path
+// O/RreaMaterialPath.H:47-199 for a uniform density ratio: one interval per
+// in-domain piece.
+struct Intervals {
+    int n;
+    double begin[RREA_ARENA_MAX_PIECES], end[RREA_ARENA_MAX_PIECES], length[RREA_ARENA_MAX_PIECES],
+        density[RREA_ARENA_MAX_PIECES];
+};
+
+__device__ __forceinline__ double positive_or(double v, double fb) { return v > 0.0 ? v : fb; }
+
+// :60-114
+__device__ __forceinline__ void build_intervals(Path const& p, double rho, Intervals& iv)
+{
+    iv.n = 0;
+    for (int i = 0; i < p.npieces; ++i) {
+        Piece const& pc = p.pieces[i];
+        if (!(pc.length > 0.0)) continue;
+        double dl = 0.0;
+        if (pc.end > pc.begin && p.full > 0.0) dl = p.full * (pc.end - pc.begin) * positive_or(rho, rho);
+        iv.begin[iv.n] = pc.begin;
+        iv.end[iv.n] = pc.end;
+        iv.length[iv.n] = pc.length;
+        iv.density[iv.n] = positive_or(dl / pc.length, rho);
+        ++iv.n;
+    }
+}
+// :117-136
+__device__ __forceinline__ double density_path(Intervals const& iv, Path const& p, double b, double e)
+{
+    b = fmax(p.in_begin, b);
+    e = fmin(p.in_end, e);
+    if (!(e > b)) return 0.0;
+    double s = 0.0;
+    for (int i = 0; i < iv.n; ++i) {
+        double const bb = fmax(b, iv.begin[i]), ee = fmin(e, iv.end[i]);
+        if (ee > bb) s += p.full * (ee - bb) * iv.density[i];
+    }
+    return s;
+}
+// :142-170
+__device__ __forceinline__ double fraction_at_density_path(Intervals const& iv, Path const& p, double b, double e,
+                                                           double target, Err& err)
+{
+    b = fmax(p.in_begin, b);
+    e = fmin(p.in_end, e);
+    if (!isfinite(target) || target < 0.0) {
+        err.set(RREA_GPU_ERR_INVALID_STATE);
+        return e;
+    }
+    double rem = target;
+    for (int i = 0; i < iv.n; ++i) {
+        double const bb = fmax(b, iv.begin[i]), ee = fmin(e, iv.end[i]);
+        if (!(ee > bb) || !(iv.density[i] > 0.0)) continue;
+        double const c = p.full * (ee - bb) * iv.density[i];
+        if (rem <= c) return bb + rem / (p.full * iv.density[i]);
+        rem -= c;
+    }
+    return e;
+}
+// :175-199
+__device__ __forceinline__ double max_uniform_slice(Intervals const& iv, Path const& p, uint64_t n)
+{
+    double const span = p.in_end - p.in_begin;
+    double const d = static_cast<double>(n);
+    double m = 0.0;
+    for (uint64_t i = 0; i < n; ++i) {
+        m = fmax(m, density_path(iv, p, p.in_begin + static_cast<double>(i) / d * span,
+                                 p.in_begin + static_cast<double>(i + 1U) / d * span));
+    }
+    return m;
+}
+
+// ------------------------------------------------------------ hazards
+// O/RreaParticleInteraction.H:1402-1454
+struct Selection {
+    bool valid, event;
+    int channel;
+    double sampled, total;
+};
+__device__ __forceinline__ Selection select_hazard(double t0, double t1, double t2, int count, double u1, double u2)
+{
+    Selection r{false, false, -1, 0.0, 0.0};
+    double const taus[3] = {t0, t1, t2};
+    if (count < 1 || count > 3 || !isfinite(u1) || !isfinite(u2)) return r;
+    for (int i = 0; i < count; ++i) {
+        if (!isfinite(taus[i]) || taus[i] < 0.0) return r;
+        r.total += taus[i];
+    }
+    r.valid = isfinite(r.total);
+    if (!r.valid) return r;
+    u1 = fmax(0.0, fmin(1.0, u1));
+    r.sampled = -log(fmax(1.0e-30, 1.0 - u1));
+    if (!(r.sampled < r.total)) return r;
+    r.event = true;
+    u2 = fmax(0.0, fmin(1.0, u2));
+    double const target = u2 * r.total;
+    double cum = 0.0;
+    int last_open = -1;
+    for (int i = 0; i < count; ++i) {
+        if (taus[i] > 0.0) last_open = i;
+        cum += taus[i];
+        if (target < cum) {
+            r.channel = i;
+            return r;
+        }
+    }
+    r.channel = last_open;
+    r.valid = r.channel >= 0;
+    r.event = r.valid;
+    return r;
+}
+
+// ------------------------------------------------------------ terminal helpers
+// O/RreaParticleInteraction.H:318-354
+__device__ __forceinline__ bool cartesian_half_open(Geom const& g, double x, double y, double z)
+{
+    if (!isfinite(x) || !isfinite(y)) return false;
+    double const r = hypot(x, y);
+    return isfinite(r) && isfinite(z) && g.rhi > g.rlo && g.zhi > g.zlo && r >= g.rlo && r < g.rhi && z >= g.zlo
+        && z < g.zhi;
+}
+// O/RreaParticleInteraction.H:409-452 (clipped policy: RREA owns every escape)
+__device__ __forceinline__ void clipped_escape_policy(Path const& p, Geom const& g, double er, double ez,
+                                                      bool& escapes, bool& invalidate)
+{
+    if (!isfinite(er) || !isfinite(ez)) {
+        escapes = true;
+        invalidate = true;
+        return;
+    }
+    double const cz = wrap_z(g, ez);
+    bool const outside = outside_certified(g, er, cz);
+    escapes = p.exits || outside;
+    invalidate = escapes;
+}
+
+}  // namespace rrea_dev

@@ -1,0 +1,809 @@
+// One electron through one outer step on one GPU thread: the body of the
+// reference's electron loop (O/RreaElectronTransport.cpp:59-889, with the
+// shared prologue/escape/writeback of O/RreaTransportStep.H:720-905 and the
+// substep/event interleave of O/RreaChargedInterleave.H:546-732).
+//
+// The reference threads a transaction log through lambdas; here every side
+// effect goes straight to its device sink:
+//   * secondaries  -> append buffer with (parent index, lineage) keys, ordered
+//                     after the kernel into the reference's chunk order;
+//   * cell sources -> FP64 atomics into the five cell-source grids with the
+//                     order-1 CIC stencil of S/RreaEventAccumulator.cpp:386-502;
+//   * tallies      -> not kept (diagnostic ledger only).
+#pragma once
+
+#include "rrea_device_path.cuh"
+
+namespace rrea_dev {
+
+struct ElectronArgs {
+    int64_t n;
+    // The current and prev_* arrays may alias (resident engine mode, where
+    // the captured pre-push state IS the current state): no __restrict__.
+    double* r;
+    double* z;
+    double* theta;
+    double* ux;
+    double* uy;
+    double* uz;
+    const double* __restrict__ w;
+    const double* prev_r;
+    const double* prev_z;
+    const double* prev_theta;
+    const double* prev_ux;
+    const double* prev_uy;
+    const double* prev_uz;
+    int64_t* __restrict__ id;
+    const int32_t* __restrict__ cpu;
+    // secondaries (unordered append) and per-parent counts for the ordering pass
+    rrea_gpu_secondary* __restrict__ sec;
+    unsigned long long* __restrict__ sec_count;
+    int64_t sec_capacity;
+    uint32_t* __restrict__ sec_per_parent;
+    // cell sources: 5 grids of nr*nz
+    double* __restrict__ cells;
+    // optional per-particle diagnostics (may be null)
+    uint64_t* __restrict__ diag_subcycles;
+    uint64_t* __restrict__ diag_events;
+    int32_t* __restrict__ diag_disposition;
+    // status: first failing code and particle
+    int* __restrict__ status;
+    long long* __restrict__ fail_index;
+    // particles transported this step (id > 0 on entry)
+    unsigned long long* __restrict__ transported;
+    const double* __restrict__ arena;
+    FieldView fv;
+};
+
+// Order-1 cell deposit (S/RreaEventAccumulator.cpp:386-502, field ids of
+// :129-164) for the uniform RZ grid with r_lo on the axis.
+__device__ __forceinline__ void add_to_field(StepConstants const& C, double* __restrict__ cells, int field,
+                                             double r, double z, double value)
+{
+    if (!isfinite(value) || value == 0.0) return;
+    rrea_gpu_config const& cfg = C.cfg;
+    int const nr = cfg.nr, nz = cfg.nz;
+    double zz = z;
+    if (cfg.periodic_z) {
+        double const len = cfg.z_hi - cfg.z_lo;
+        double s = fmod(zz - cfg.z_lo, len);
+        if (s < 0.0) s += len;
+        zz = cfg.z_lo + s;
+    }
+    int const ic = static_cast<int>(floor((r - cfg.r_lo) / C.dr));
+    int const jc = static_cast<int>(floor((zz - cfg.z_lo) / C.dz));
+    if (ic < 0 || ic >= nr || jc < 0 || jc >= nz) return;
+    double const rc = (r - cfg.r_lo) / C.dr + 0.0 - 0.5;
+    int const i0 = static_cast<int>(floor(rc));
+    double const wr1 = rc - i0, wr0 = 1.0 - wr1;
+    double const zc = (zz - cfg.z_lo) / C.dz + 0.0 - 0.5;
+    int const j0 = static_cast<int>(floor(zc));
+    double const wz1 = zc - j0, wz0 = 1.0 - wz1;
+    double* grid = cells + static_cast<size_t>(field) * nr * nz;
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        double const wz = a == 0 ? wz0 : wz1;
+        if (wz == 0.0) continue;
+        int j = j0 + a;
+        if (j < 0 || j > nz - 1) {
+            if (cfg.periodic_z) j = ((j % nz) + nz) % nz;
+            else continue;
+        }
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            double const wr = b == 0 ? wr0 : wr1;
+            double const v = value * wr * wz;
+            if (v == 0.0) continue;
+            int i = i0 + b;
+            if (i < 0 || i > nr - 1) {
+                if (i == -1 && cfg.r_lo == 0.0) i = 0;
+                else continue;
+            }
+            if (!isfinite(v)) continue;
+            atomicAdd(grid + i + static_cast<size_t>(nr) * j, v);
+        }
+    }
+}
+
+// O/RreaCouplingSources.cpp:435-512
+__device__ __forceinline__ void deposit_source(StepConstants const& C, double* __restrict__ cells, int kind,
+                                               double r, double z, double w, double sec_e, double loss)
+{
+    if (w <= 0.0) return;
+    if (kind == 0) {  // AccumulateIonizationEvent
+        add_to_field(C, cells, 1, r, z, w);
+        if (sec_e < C.cfg.low_energy_cutoff_eV) add_to_field(C, cells, 0, r, z, w);
+        add_to_field(C, cells, 3, r, z, w);
+        add_to_field(C, cells, 4, r, z, fmax(w, 0.0) * fmax(loss, 0.0));
+    } else if (kind == 1) {  // AccumulateLowEnergyElectron
+        add_to_field(C, cells, 0, r, z, w);
+        add_to_field(C, cells, 3, r, z, w);
+        add_to_field(C, cells, 4, r, z, fmax(w, 0.0) * fmax(fmax(loss, 0.0), 0.0));
+    } else {  // AccumulatePositiveIonSourceOnly
+        add_to_field(C, cells, 1, r, z, w);
+        add_to_field(C, cells, 3, r, z, w);
+        add_to_field(C, cells, 4, r, z, fmax(w, 0.0) * fmax(loss, 0.0));
+    }
+}
+
+struct ElectronState {
+    double k, dx, dy, dz;
+    double run_x, run_y, run_z;
+};
+
+// Electron transport coefficients needed by the loop, all on one bracket of
+// the shared 2856-row grid when the bundle provides one.
+struct ElectronRates {
+    double collision, soft, moller_inv, brems_inv;
+};
+
+__device__ __forceinline__ void electron_rates(StepConstants const& C, const double* __restrict__ arena, double e,
+                                               ElectronRates& out, Err& err)
+{
+    RreaArenaIndex const& ix = C.tix;
+    if (ix.electron_grid_shared) {
+        Bracket b;
+        if (!bracket_hot(arena, ix.hot[RREA_T_E_COLLISION], e, b, err)) return;
+        out.collision = eval_hot(arena, ix.hot[RREA_T_E_COLLISION], b, err);
+        out.soft = eval_hot(arena, ix.hot[RREA_T_E_SOFT_RAD], b, err);
+        out.moller_inv = eval_hot(arena, ix.hot[RREA_T_E_HARD_MOLLER], b, err);
+        out.brems_inv = eval_hot(arena, ix.hot[RREA_T_E_TRACKED_BREMS], b, err);
+    } else {
+        out.collision = interpolate(arena, ix.hot[RREA_T_E_COLLISION], e, err);
+        out.soft = interpolate(arena, ix.hot[RREA_T_E_SOFT_RAD], e, err);
+        out.moller_inv = interpolate(arena, ix.hot[RREA_T_E_HARD_MOLLER], e, err);
+        out.brems_inv = interpolate(arena, ix.hot[RREA_T_E_TRACKED_BREMS], e, err);
+    }
+}
+
+// Competing STP rates, O/RreaChargedFinalStates.H:107-152 with the accessors
+// ElectronHardMollerMeanFreePath / ElectronBremsstrahlungMeanFreePath
+// (S/RreaInteractionTables.cpp:2394-2412, 2666-2676).
+__device__ __forceinline__ void competing_rates(StepConstants const& C, const double* __restrict__ arena, double e,
+                                                double& s0, double& s1, Err& err)
+{
+    double const thr = C.hm_threshold_eV;
+    bool const m_open = C.hm_enabled && thr > 0.0 && e > 2.0 * thr;
+    bool const b_open = isfinite(e) && isfinite(C.photon_cutoff_eV) && e > C.photon_cutoff_eV;
+    s0 = 0.0;
+    s1 = 0.0;
+    if (m_open || b_open) {
+        ElectronRates rt;
+        electron_rates(C, arena, e, rt, err);
+        if (err.code) return;
+        if (m_open) {
+            double const mfp = (thr > 0.0 && e <= 2.0 * thr) ? 1.0e99 : mfp_from_inverse(rt.moller_inv * 1.0, err);
+            s0 = mfp > 0.0 ? 1.0 / mfp : 0.0;
+        }
+        if (b_open) {
+            double const mfp = mfp_from_inverse(rt.brems_inv * 1.0, err);
+            s1 = mfp > 0.0 ? 1.0 / mfp : 0.0;
+        }
+    }
+    s0 = frozen_rate(s0, err);
+    s1 = frozen_rate(s1, err);
+}
+
+// S/RreaInteractionTables.cpp:2414-2440
+__device__ __forceinline__ double hard_moller_energy_loss(StepConstants const& C, const double* __restrict__ arena,
+                                                          double e, double dr, Err& err)
+{
+    RreaTable1DIndex const& h = C.tix.hot[RREA_T_E_HARD_MOLLER];
+    double const inv = interpolate(arena, h, e, err);
+    if (!(inv > 0.0)) return 0.0;
+    double const mean = semilogx(arena + h.x, arena + h.lx, arena + C.tix.hard_moller_mean_secondary, h.n, e, err);
+    if (!(mean > 0.0)) return 0.0;
+    return mean * inv * dr;
+}
+
+// S/RreaInteractionTables.cpp:2477-2493
+__device__ __forceinline__ double elastic_inverse_stp(StepConstants const& C, const double* __restrict__ arena,
+                                                      double e, Err& err)
+{
+    RreaElasticIndex const& el = C.tix.elastic[0];
+    double const mfp = semilogx(arena + el.x, arena + el.lx, arena + el.mfp, el.n, e, err) / 1.0;
+    return frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0, err);
+}
+
+// S/RreaInteractionTables.cpp:2504-2560
+__device__ __forceinline__ double sample_gs_cos(StepConstants const& C, const double* __restrict__ arena, double e,
+                                                double n, double u, Err& err)
+{
+    RreaArenaIndex const& ix = C.tix;
+    if (!charged_in_range(ix, e)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return 1.0;
+    }
+    if (!isfinite(u) || u < 0.0 || u > 1.0) {
+        err.set(RREA_GPU_ERR_INVALID_STATE);
+        return 1.0;
+    }
+    bool const use_gs = e <= ix.gs_wentzel_transition_eV;
+    RreaAngleIndex const& a = use_gs ? ix.gs[0] : ix.wentzel[0];
+    if (e < __ldg(arena + a.e) || e > __ldg(arena + a.e + a.ne - 1)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return 1.0;
+    }
+    if (!isfinite(n) || n < ix.gs_few_collision_threshold) {
+        err.set(RREA_GPU_ERR_INVALID_STATE);
+        return 1.0;
+    }
+    if (n >= ix.gs_isotropic_above_n) return 2.0 * u - 1.0;
+    return sample_gs_angle(arena, a, e, n, u, err);
+}
+__device__ __forceinline__ double sample_single_elastic_cos(StepConstants const& C, const double* __restrict__ arena,
+                                                            double e, double cdf_u, Err& err)
+{
+    if (!charged_in_range(C.tix, e)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return 1.0;
+    }
+    RreaElasticIndex const& el = C.tix.elastic[0];
+    double const eta = semilogx(arena + el.x, arena + el.lx, arena + el.eta, el.n, e, err);
+    double const u = fmin(fmax(cdf_u, 0.0), 1.0 - 1.0e-15);
+    return 1.0 - 2.0 * eta * u / (1.0 + eta - u);
+}
+// S/RreaInteractionTables.cpp:2714-2760
+__device__ __forceinline__ double tsai_g2(double x)
+{
+    if (x < 1.0e-3) {
+        return x * x * (0.5 + x * (-1.0 / 3.0 + x * (1.0 / 8.0 + x * (-1.0 / 30.0 + x * (1.0 / 144.0)))));
+    }
+    return -expm1(-x) - x * exp(-x);
+}
+__device__ __forceinline__ double sample_brems_cos(StepConstants const& C, double e, double cdf_u, Err& err)
+{
+    if (!charged_in_range(C.tix, e)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return 1.0;
+    }
+    cdf_u = fmax(0.0, fmin(1.0, cdf_u));
+    if (cdf_u == 0.0) return 1.0;
+    if (cdf_u == 1.0) return -1.0;
+    double constexpr a = 0.625;
+    double const umax = 2.0 * (1.0 + e / kMeC2);
+    double const target = cdf_u * (0.25 * tsai_g2(a * umax) + 0.75 * tsai_g2(3.0 * a * umax));
+    double lo = 0.0, hi = umax;
+    for (int it = 0; it < 60; ++it) {
+        double const mid = 0.5 * (lo + hi);
+        double const m = 0.25 * tsai_g2(a * mid) + 0.75 * tsai_g2(3.0 * a * mid);
+        if (m < target) lo = mid; else hi = mid;
+    }
+    double const f = 0.5 * (lo + hi) / umax;
+    return 1.0 - 2.0 * f * f;
+}
+
+__device__ __forceinline__ void record_failure(ElectronArgs const& A, int code, int64_t ip)
+{
+    if (atomicCAS(A.status, 0, code) == 0) {
+        *A.fail_index = static_cast<long long>(ip);
+    }
+}
+
+// Returns the disposition (0 survive, 1 escape, 2 demotion, 3 zero weight).
+__device__ __forceinline__ int transport_electron(StepConstants const& C, ElectronArgs const& A, int64_t ip,
+                                                  uint64_t& subcycles_out, uint64_t& events_out,
+                                                  uint32_t& lineage, Err& err)
+{
+    const double* __restrict__ arena = A.arena;
+    rrea_gpu_config const& cfg = C.cfg;
+    Geom const g{cfg.r_lo, cfg.r_hi, cfg.z_lo, cfg.z_hi, cfg.periodic_z != 0};
+    double const cutoff = cfg.low_energy_cutoff_eV;
+    double const rho = C.density_ratio;
+    double const w_air = C.tix.w_air_eV_per_pair;
+    double const hm_thr = C.hm_threshold_eV;
+    double const dt_s = C.dt_s;
+
+    // ---- prologue, O/RreaTransportStep.H:730-819
+    uint64_t const key = static_cast<uint64_t>(llabs(A.id[ip])) ^ (static_cast<uint64_t>(A.cpu ? A.cpu[ip] : 0) << 40);
+    double const weight = A.w[ip];
+    if (weight <= 0.0) {
+        A.id[ip] = -A.id[ip];
+        return 3;
+    }
+    double const prev_r = A.prev_r[ip];
+    if (prev_r > cfg.r_hi + 1.0e-9 * cfg.r_hi) {
+        err.set(RREA_GPU_ERR_GEOMETRY);
+        return -1;
+    }
+    RngStream rng;
+    rng.init(cfg.rng_seed, key, C.step_key);
+    double dx = A.prev_ux[ip], dy = A.prev_uy[ip], dz = A.prev_uz[ip];
+    double k = kinetic_from_proper_velocity(dx, dy, dz);
+    normalize(dx, dy, dz);
+    double const seed_th = A.prev_theta[ip];
+    double sth, cth;
+    sincos(seed_th, &sth, &cth);
+    double run_x = prev_r * cth;
+    double run_y = prev_r * sth;
+    double run_z = A.prev_z[ip];
+    double const r_particle = prev_r, z_particle = run_z;
+
+    auto build_chord = [&](double req_dt, Path& path) -> bool {
+        // O/RreaParticleInteraction.H:110-161
+        if (!isfinite(req_dt) || !(req_dt >= 0.0)) return false;
+        double const speed = charged_speed(k);
+        double const dn = sqrt(dx * dx + dy * dy + dz * dz);
+        if (!isfinite(speed) || !isfinite(dn) || !(dn > 0.0)) return false;
+        double const sc = speed * req_dt / dn;
+        double const exx = run_x + sc * dx, eyy = run_y + sc * dy, ezz = run_z + sc * dz;
+        clip_rz(hypot(run_x, run_y), atan2(run_y, run_x), run_z, hypot(exx, eyy), atan2(eyy, exx), ezz, g, path,
+                err);
+        return isfinite(path.full) && path.in_begin == 0.0;
+    };
+    auto add_secondary = [&](int species, int process, double x, double y, double z, double sx, double sy, double sz,
+                             double e, double birth) {
+        unsigned long long const slot = atomicAdd(A.sec_count, 1ULL);
+        if (slot < static_cast<unsigned long long>(A.sec_capacity)) {
+            rrea_gpu_secondary s;
+            s.species = species;
+            s.process = process;
+            s.root_species = 0;
+            s.pad = 0;
+            s.parent_index = ip;
+            s.root_key = key;
+            s.lineage = lineage;
+            s.x = x; s.y = y; s.z = z;
+            s.dir_x = sx; s.dir_y = sy; s.dir_z = sz;
+            s.weight = weight;
+            s.energy_eV = e;
+            s.birth_fraction = birth;
+            A.sec[slot] = s;
+        } else {
+            err.set(RREA_GPU_ERR_CAPACITY);
+        }
+        ++lineage;
+    };
+    auto deposit_local = [&](double r, double z, double e) {
+        // O/RreaTransportStep.H:530-561
+        if (weight <= 0.0 || e <= 0.0) return;
+        double const pw = weight * e / fmax(w_air, 1.0);
+        if (pw <= 0.0) return;
+        deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
+    };
+    auto finish = [&](int disp) { return disp; };
+
+    Path path;
+    bool const driver_valid = build_chord(dt_s, path);
+    if (err.code) return finish(-1);
+    bool esc, esc_inv;
+    clipped_escape_policy(path, g, hypot(path.ex, path.ey), path.ez, esc, esc_inv);
+    double const ds = driver_valid ? path.in_length : 0.0;
+    Intervals iv;
+    build_intervals(path, rho, iv);
+    double const driver_span = fmax(path.in_end, 1.0e-6);
+    FieldRange const dfw = path_field_work(A.fv, g, path, -1.0, 0.0, 1.0, err);
+    double const field_work = dfw.work / driver_span;
+    double const chord_dpath = density_path(iv, path, path.in_begin, path.in_end);
+    double transported_dpath = 0.0, transported_len = 0.0;
+    double particle_density = ds > 0.0 ? chord_dpath / ds : positive_or(rho, rho);
+
+    auto commit_escape = [&]() {
+        // O/RreaTransportStep.H:829-863 (the escape deposit is applied by the
+        // current-deposition pass, not here)
+        double const u = proper_velocity_from_kinetic(k);
+        A.ux[ip] = u * dx;
+        A.uy[ip] = u * dy;
+        A.uz[ip] = u * dz;
+        if (esc_inv) A.id[ip] = -A.id[ip];
+        return finish(1);
+    };
+    auto demote = [&](double r, double z) {
+        // O/RreaElectronTransport.cpp:151-174, 856-879
+        deposit_source(C, A.cells, 1, r, z, weight, 0.0, 0.0);
+        deposit_local(r, z, k);
+        A.id[ip] = -A.id[ip];
+        return finish(2);
+    };
+
+    bool const below = k < cutoff;
+    if (esc && below) return commit_escape();
+    if (!esc && below) return demote(r_particle, z_particle);
+    if (ds <= 0.0) {
+        if (esc) return commit_escape();
+        return finish(0);
+    }
+    if (iv.n == 0) {
+        err.set(RREA_GPU_ERR_INVALID_STATE);
+        return finish(-1);
+    }
+
+    // ---- substep count, O/RreaElectronTransport.cpp:187-279
+    uint64_t subcycles;
+    {
+        double s0, s1;
+        competing_rates(C, arena, k, s0, s1, err);
+        double const driver_dpath = chord_dpath / driver_span;
+        double const target = cfg.max_optical_depth_per_substep;
+        uint64_t const cap = cfg.max_subcycles;
+        double const max_tau = (s0 * driver_dpath) + (s1 * driver_dpath);
+        double const total_stp = s0 + s1;
+        uint64_t const req = static_cast<uint64_t>(fmax(1.0, ceil(max_tau / target)));
+        bool viol = req > cap;
+        uint64_t sub = req < cap ? req : cap;
+        // selected_material_subcycles, O/RreaTransportStep.H:148-184
+        for (int guard = 0; guard < 64; ++guard) {
+            double const maximum = total_stp * max_uniform_slice(iv, path, sub);
+            double const tol = 64.0 * kEps * fmax(1.0, target);
+            if (maximum <= target + tol) break;
+            if (sub >= cap) {
+                viol = true;
+                break;
+            }
+            double const est = ceil(static_cast<double>(sub) * (maximum / target));
+            uint64_t next = sub + 1U;
+            if (est >= static_cast<double>(cap)) next = cap;
+            else if (est > static_cast<double>(next)) next = static_cast<uint64_t>(est);
+            sub = next < cap ? next : cap;
+        }
+        double const gs_n = elastic_inverse_stp(C, arena, k, err) * driver_dpath;
+        double const ke = fmax(k, cutoff);
+        double drag_est = 0.0;
+        if (ke > 0.0) {
+            ElectronRates rt;
+            electron_rates(C, arena, ke, rt, err);
+            drag_est = (rt.collision * 1.0 + rt.soft * 1.0) * driver_dpath;
+        }
+        double const impulse = fmax(cfg.max_field_impulse_fraction * k, fmax(cfg.field_impulse_floor_eV, 1.0));
+        uint64_t const gsd = static_cast<uint64_t>(
+            fmax(1.0, ceil(fmin(gs_n, cfg.gs_total_collision_cap) / fmax(cfg.max_gs_collisions_per_substep, 1.0))));
+        uint64_t const imd = static_cast<uint64_t>(fmax(1.0, ceil((fabs(field_work) + drag_est) / impulse)));
+        uint64_t m = sub;
+        if (gsd > m) m = gsd;
+        if (imd > m) m = imd;
+        subcycles = m < cap ? m : cap;
+        if (cfg.strict_transport_guards && viol) err.set(RREA_GPU_ERR_GUARD);
+        if (err.code) return finish(-1);
+    }
+    subcycles_out = subcycles;
+
+    bool exited = false;
+    uint64_t completed = 0;
+    bool terminated_mid = false;
+    double mid_r = r_particle, mid_z = z_particle;
+    double const sub_dt = dt_s / static_cast<double>(subcycles);
+    FieldRange sub_field{0, 0, 0, 0, 0, 0, 0, 0};
+    double sub_dt_eff = 0.0;
+    uint64_t events = 0;
+
+    auto mark_stopped = [&](double f) {
+        if (path.exits && f >= path.in_end) {
+            exited = true;
+            return;
+        }
+        double x, y, z;
+        point_at_full(path, g, f, x, y, z);
+        if (!cartesian_half_open(g, x, y, z)) {
+            exited = true;
+            return;
+        }
+        mid_z = z;
+        mid_r = hypot(x, y);
+        terminated_mid = true;
+    };
+    // O/RreaElectronTransport.cpp:294-400 with RreaPlanContinuousDragSegment
+    // (O/RreaChargedInterleave.H:239-292) and the cutoff limiter
+    // (O/RreaParticleInteraction.H:203-265).  Returns true when the drag
+    // reached the cutoff; `end_out` is the effective end fraction.
+    auto continuous = [&](double b, double e, double stop_e, double& end_out) -> bool {
+        end_out = b;
+        if (!(e > b) || !(k > 0.0) || stop_e < cutoff) return false;
+        ElectronRates rt;
+        electron_rates(C, arena, stop_e, rt, err);
+        double const sc = frozen_rate(rt.collision * 1.0, err);
+        double const ss = frozen_rate(rt.soft * 1.0, err);
+        double const sh = (C.hm_enabled && hm_thr > 0.0 && stop_e > 2.0 * hm_thr)
+            ? frozen_rate(hard_moller_energy_loss(C, arena, stop_e, 1.0, err), err)
+            : 0.0;
+        if (err.code) return false;
+        double const total = sc + ss;
+        // limiter
+        double eff = b;
+        bool reaches = false;
+        bool valid = false;
+        if (isfinite(b) && isfinite(e) && isfinite(k) && isfinite(cutoff) && e >= b && k >= cutoff && cutoff >= 0.0) {
+            double const to_cut = k - cutoff;
+            double const req = total * density_path(iv, path, b, e);
+            if (isfinite(req) && req >= 0.0) {
+                valid = true;
+                if (req < to_cut) {
+                    eff = e;
+                } else {
+                    reaches = true;
+                    if (to_cut != 0.0) {
+                        double lo = b, hi = e;
+                        for (int it = 0; it < 56; ++it) {
+                            double const mid = 0.5 * (lo + hi);
+                            double const l = total * density_path(iv, path, b, mid);
+                            if (!isfinite(l) || l < 0.0) {
+                                valid = false;
+                                break;
+                            }
+                            if (l < to_cut) lo = mid; else hi = mid;
+                        }
+                        eff = valid ? 0.5 * (lo + hi) : b;
+                        if (!valid) reaches = false;
+                    }
+                }
+            }
+        }
+        if (!valid) {
+            err.set(RREA_GPU_ERR_INVALID_STATE);
+            return false;
+        }
+        double const path_m = density_path(iv, path, b, eff);
+        double const raw_col = sc * path_m;
+        double const raw_soft = ss * path_m;
+        double const avail = fmax(0.0, k - cutoff);
+        double const drag = reaches ? avail : fmin(raw_col + raw_soft, avail);
+        double const col = fmin(raw_col, drag);
+        (void)sh;
+        // ion pairs, O/RreaChargedInterleave.H:157-196
+        if (col > 0.0 && raw_col > 0.0) {
+            for (int i = 0; i < iv.n; ++i) {
+                double const bb = fmax(b, iv.begin[i]), ee = fmin(eff, iv.end[i]);
+                if (!(ee > bb)) continue;
+                double const raw = path.full * (ee - bb) * iv.density[i] * sc;
+                double const loss = col * raw / raw_col;
+                double const pw = weight * loss / fmax(w_air, 1.0);
+                if (!(pw > 0.0)) continue;
+                double x, y, z;
+                point_at_full(path, g, 0.5 * (bb + ee), x, y, z);
+                deposit_source(C, A.cells, 0, hypot(x, y), z, pw, 0.5 * cutoff, w_air);
+            }
+        }
+        k = fmax(0.0, k - drag);
+        if (reaches) k = cutoff;
+        end_out = eff;
+        return reaches;
+    };
+    auto channel_open = [&](int ch, double e) -> bool {
+        // O/RreaChargedFinalStates.H:56-96
+        if (!charged_in_range(C.tix, e)) {
+            err.set(RREA_GPU_ERR_RANGE);
+            return false;
+        }
+        ElectronRates rt;
+        electron_rates(C, arena, e, rt, err);
+        if (ch == 0) return C.hm_enabled && (hm_thr > 0.0 && e > 2.0 * hm_thr) && rt.moller_inv > 0.0;
+        if (ch == 1) return (isfinite(e) && isfinite(C.photon_cutoff_eV) && e > C.photon_cutoff_eV) && rt.brems_inv > 0.0;
+        return false;
+    };
+
+    // ---- substep interleave, O/RreaChargedInterleave.H:693-732
+    for (uint64_t sub = 0; sub < subcycles; ++sub) {
+        if (k < cutoff) break;
+        double sb, se;
+        {
+            Path np;
+            if (!build_chord(sub_dt, np)) break;
+            path = np;
+            if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
+                exited = path.exits;
+                break;
+            }
+            build_intervals(path, rho, iv);
+            if (iv.n == 0) {
+                err.set(RREA_GPU_ERR_INVALID_STATE);
+                break;
+            }
+            for (int i = 0; i < iv.n; ++i) {
+                transported_dpath += iv.length[i] * iv.density[i];
+                transported_len += iv.length[i];
+            }
+            sb = path.in_begin;
+            se = path.in_end;
+            sub_field = path_field_work(A.fv, g, path, -1.0, sb, se, err);
+            sub_dt_eff = sub_dt * (se - sb);
+            half_kick(sub_field, 0.5 * sub_dt_eff, -1.0, k, dx, dy, dz);
+            if (k < cutoff) {
+                mark_stopped(sb);
+                break;
+            }
+        }
+        // ---- event interleave, O/RreaChargedInterleave.H:546-664
+        {
+            double rem = sb;
+            uint64_t ordinal = 0;
+            while (rem < se && k >= cutoff) {
+                if (err.code) break;
+                if (ordinal >= kEventCap) {
+                    err.set(RREA_GPU_ERR_RNG_OVERFLOW);
+                    break;
+                }
+                double const frozen = k;
+                double s0, s1;
+                competing_rates(C, arena, frozen, s0, s1, err);
+                double const seg_dp = density_path(iv, path, rem, se);
+                double const t0 = s0 * seg_dp, t1 = s1 * seg_dp;
+                uint64_t rng_index;
+                if (!live_hazard_index(0, sub, ordinal, rng_index)) {
+                    err.set(RREA_GPU_ERR_RNG_OVERFLOW);
+                    break;
+                }
+                ++events;
+                double const u1 = rng.uniform(rng_index, ordinal == 0 ? kChElectronCompetingOpticalDepth
+                                                                      : kChElectronContinuationOpticalDepth);
+                double const u2 = rng.uniform(rng_index, ordinal == 0 ? kChElectronCompetingChannel
+                                                                      : kChElectronContinuationChannel);
+                Selection const selv = select_hazard(t0, t1, 0.0, 2, u1, u2);
+                if (!selv.valid) {
+                    err.set(RREA_GPU_ERR_INVALID_STATE);
+                    break;
+                }
+                if (!selv.event) {
+                    double eff;
+                    if (continuous(rem, se, frozen, eff)) mark_stopped(eff);
+                    break;
+                }
+                double const ev = fraction_at_density_path(iv, path, rem, se, selv.sampled / (s0 + s1), err);
+                if (!(isfinite(rem) && isfinite(ev) && isfinite(se) && se > rem && !(ev < rem) && !(ev > se))) {
+                    err.set(RREA_GPU_ERR_INVALID_STATE);
+                    break;
+                }
+                double ex, ey, ez;
+                point_at_full(path, g, ev, ex, ey, ez);
+                double const er = hypot(ex, ey);
+                {
+                    double eff;
+                    if (continuous(rem, ev, frozen, eff)) {
+                        mark_stopped(eff);
+                        break;
+                    }
+                }
+                bool const open_ev = k >= cutoff && channel_open(selv.channel, k);
+                if (!open_ev) {
+                    bool const open_fr = frozen >= cutoff && channel_open(selv.channel, frozen);
+                    if (!open_fr) {
+                        err.set(RREA_GPU_ERR_INVALID_STATE);
+                        break;
+                    }
+                    rem = ev;
+                    ++ordinal;
+                    continue;
+                }
+                double const within = fmin(1.0, fmax(0.0, ev));
+                double const birth = fmin(1.0, (static_cast<double>(completed) + within) / static_cast<double>(subcycles));
+                if (selv.channel == 0) {
+                    // RreaApplyHardMollerFinalState, O/RreaChargedFinalStates.H:164-225
+                    double const kb = k;
+                    if (!charged_in_range(C.tix, kb)) {
+                        err.set(RREA_GPU_ERR_RANGE);
+                        break;
+                    }
+                    double sec = sample_conditional(arena, C.tix.cdf[RREA_C_MOLLER], kb,
+                                                    rng.uniform(rng_index, kChHardMollerEnergy), true, err);
+                    sec = fmax(hm_thr, fmin(sec, 0.5 * kb));
+                    double pdx, pdy, pdz, sdx, sdy, sdz;
+                    moller_lab_directions(dx, dy, dz, kb, sec, rng.uniform(rng_index, kChHardMollerAzimuth), pdx, pdy,
+                                          pdz, sdx, sdy, sdz);
+                    k = fmax(0.0, kb - sec);
+                    dx = pdx; dy = pdy; dz = pdz;
+                    add_secondary(0, 2, ex, ey, ez, sdx, sdy, sdz, sec, birth);
+                    deposit_source(C, A.cells, 0, er, ez, weight, sec, sec);
+                } else if (selv.channel == 1) {
+                    // RreaApplyBremsFinalState, O/RreaChargedFinalStates.H:329-394
+                    double const kb = k;
+                    if (!charged_in_range(C.tix, kb)) {
+                        err.set(RREA_GPU_ERR_RANGE);
+                        break;
+                    }
+                    double const sampled = sample_conditional(arena, C.tix.cdf[RREA_C_BREMS_E], kb,
+                                                              rng.uniform(rng_index, kChBremsEnergy), false, err);
+                    double const eg = fmin(fmax(sampled, 0.0), fmax(kb, 0.0));
+                    double const after = fmax(0.0, fmax(kb, 0.0) - eg);
+                    bool const tracked = isfinite(C.photon_cutoff_eV) && C.photon_cutoff_eV >= 0.0 && eg >= C.photon_cutoff_eV;
+                    double const ct = sample_brems_cos(C, kb, rng.uniform(rng_index, kChBremsAngle), err);
+                    double gx, gy, gz;
+                    cone_direction(dx, dy, dz, ct, rng.uniform(rng_index, kChBremsAzimuth), gx, gy, gz);
+                    photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
+                    k = after;
+                    if (tracked) {
+                        add_secondary(2, 4, ex, ey, ez, gx, gy, gz, eg, birth);
+                    } else if (eg > 0.0) {
+                        deposit_local(er, ez, eg);
+                    }
+                }
+                if (k <= cutoff) {
+                    mark_stopped(ev);
+                    break;
+                }
+                rem = ev;
+                ++ordinal;
+            }
+        }
+        if (err.code) break;
+        if (terminated_mid) break;
+        // ---- finish_interleaved_substep, O/RreaElectronTransport.cpp:502-524
+        if (k >= cutoff) {
+            // apply_gs_elastic_scatter, O/RreaTransportStep.H:371-423
+            double const gs_n = elastic_inverse_stp(C, arena, k, err) * density_path(iv, path, sb, se);
+            if (gs_n > 0.0) {
+                double const few = C.tix.gs_few_collision_threshold;
+                if (gs_n < few) {
+                    int const cap = static_cast<int>(ceil(3.0 * few));
+                    if (cap >= 255) {
+                        err.set(RREA_GPU_ERR_INVALID_STATE);
+                        break;
+                    }
+                    int const cnt = poisson_capped(gs_n, rng.uniform((sub << 8) | 0, kChElectronGsFewCount), cap);
+                    for (int q = 0; q < cnt; ++q) {
+                        uint64_t const inner = static_cast<uint64_t>(q + 1);
+                        double const ct = sample_single_elastic_cos(
+                            C, arena, k, rng.uniform((sub << 8) | inner, kChElectronGsFewScatter), err);
+                        double nx, ny, nz;
+                        cone_direction(dx, dy, dz, ct, rng.uniform((sub << 8) | inner, kChElectronGsFewAzimuth), nx,
+                                       ny, nz);
+                        dx = nx; dy = ny; dz = nz;
+                    }
+                } else {
+                    double const ct = sample_gs_cos(C, arena, k, gs_n, rng.uniform(sub << 8, kChElectronGsAngle), err);
+                    double nx, ny, nz;
+                    cone_direction(dx, dy, dz, ct, rng.uniform(sub << 8, kChElectronGsAzimuth), nx, ny, nz);
+                    dx = nx; dy = ny; dz = nz;
+                }
+            }
+        }
+        half_kick(sub_field, 0.5 * sub_dt_eff, -1.0, k, dx, dy, dz);
+        if (k < cutoff) {
+            mark_stopped(se);
+            break;
+        }
+        {
+            // RreaAdvanceRunningChargedPosition, O/RreaParticleInteraction.H:368-392
+            double x, y, z;
+            point_at_full(path, g, se, x, y, z);
+            double const wz = wrap_z(g, z);
+            if (!cartesian_half_open(g, x, y, wz)) {
+                exited = true;
+                break;
+            }
+            run_x = x;
+            run_y = y;
+            run_z = wz;
+        }
+        if (path.exits) {
+            exited = true;
+            break;
+        }
+        completed = sub + 1U;
+    }
+    events_out = events;
+    if (err.code) return finish(-1);
+    if (exited) clipped_escape_policy(path, g, hypot(path.ex, path.ey), path.ez, esc, esc_inv);
+    if (transported_len > 0.0) particle_density = transported_dpath / transported_len;
+    double const end_r = hypot(run_x, run_y);
+    double fer, fez, fbt;
+    gather(A.fv, end_r, run_z, fer, fez, fbt);
+    // electron_ensemble_mean_drag_ev_per_m, O/RreaTransportStep.H:226-247
+    double threshold = 0.0;
+    {
+        double const ke = fmax(k, cutoff);
+        if (ke > 0.0 && particle_density > 0.0) {
+            ElectronRates rt;
+            electron_rates(C, arena, ke, rt, err);
+            double const hard = C.hm_enabled ? hard_moller_energy_loss(C, arena, ke, particle_density, err) : 0.0;
+            double tracked = 0.0;
+            double const inv = rt.brems_inv * particle_density;
+            if (inv > 0.0) tracked = inv * mean_conditional(arena, C.tix.cdf[RREA_C_BREMS_E], ke, err);
+            threshold = (rt.collision * particle_density + rt.soft * particle_density) + hard + tracked;
+        }
+    }
+    if (err.code) return finish(-1);
+    bool const below_cut = k < cutoff;
+    bool const nonrunaway = hm_thr > 0.0 && k <= hm_thr && hypot(fer, fez) <= threshold;
+    if (exited) return commit_escape();
+    if (terminated_mid) return demote(mid_r, mid_z);
+    if (below_cut || nonrunaway) return demote(end_r, run_z);
+    // CommitSurvivorChargedWriteback, O/RreaTransportStep.H:874-905
+    double const um = proper_velocity_from_kinetic(k);
+    A.ux[ip] = um * dx;
+    A.uy[ip] = um * dy;
+    A.uz[ip] = um * dz;
+    A.r[ip] = end_r;
+    A.theta[ip] = atan2(run_y, run_x);
+    A.z[ip] = run_z;
+    return finish(0);
+}
+
+}  // namespace rrea_dev

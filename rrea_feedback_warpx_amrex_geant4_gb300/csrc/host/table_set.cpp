@@ -1,0 +1,481 @@
+#include "table_set.hpp"
+
+#include "json_lite.hpp"
+#include "rreatbl.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace rrea_host {
+
+namespace {
+
+std::string read_text(std::string const& path)
+{
+    std::ifstream in(path, std::ios::binary);
+    if (!in) {
+        throw std::runtime_error("cannot open " + path);
+    }
+    std::ostringstream s;
+    s << in.rdbuf();
+    return s.str();
+}
+
+std::string dir_of(std::string const& path)
+{
+    std::size_t const slash = path.find_last_of('/');
+    return slash == std::string::npos ? std::string(".") : path.substr(0, slash);
+}
+
+struct Table1D {
+    std::string interpolation;
+    std::vector<double> x, y;
+};
+
+struct CondGroups {
+    std::vector<double> primary;
+    std::vector<std::vector<double>> u, v;
+};
+
+struct Angle {
+    std::vector<double> e, p, u, omc;
+};
+
+// Conditional CDF rows grouped by consecutive primary energy
+// (RreaInteractionTables.cpp:576-616) with the monotonicity contract of
+// ValidateRreaConditionalCdfGroups (:1527-1578).
+CondGroups group_conditional(std::vector<double> const& primaries,
+                             std::vector<double> const& cdfs,
+                             std::vector<double> const& values,
+                             std::string const& label)
+{
+    CondGroups g;
+    for (std::size_t i = 0; i < primaries.size(); ++i) {
+        double const p = primaries[i];
+        if (!(p > 0.0) || !(cdfs[i] >= 0.0 && cdfs[i] <= 1.0) || !(values[i] >= 0.0)) {
+            throw std::runtime_error("conditional CDF row invalid: " + label);
+        }
+        if (g.primary.empty() || g.primary.back() != p) {
+            if (!g.primary.empty() && p <= g.primary.back()) {
+                throw std::runtime_error("conditional CDF groups not increasing: " + label);
+            }
+            g.primary.push_back(p);
+            g.u.emplace_back();
+            g.v.emplace_back();
+        }
+        if (!g.u.back().empty() && cdfs[i] <= g.u.back().back()) {
+            throw std::runtime_error("conditional CDF u not increasing: " + label);
+        }
+        g.u.back().push_back(cdfs[i]);
+        g.v.back().push_back(values[i]);
+    }
+    if (g.primary.size() < 2) {
+        throw std::runtime_error("conditional CDF needs >= 2 groups: " + label);
+    }
+    for (std::size_t k = 0; k < g.primary.size(); ++k) {
+        if (g.u[k].size() < 2 || g.u[k].front() != 0.0 || g.u[k].back() != 1.0) {
+            throw std::runtime_error("conditional CDF group endpoints must be 0 and 1: " + label);
+        }
+        for (std::size_t n = 1; n < g.v[k].size(); ++n) {
+            if (g.v[k][n] < g.v[k][n - 1]) {
+                throw std::runtime_error("conditional CDF values not monotone: " + label);
+            }
+        }
+    }
+    return g;
+}
+
+// (energy, path) grouping of a GS/Wentzel inverse-CDF table
+// (RreaInteractionTables.cpp:687-772).
+Angle load_angle(std::string const& path)
+{
+    auto const c = ReadRreaTableContainer(path);
+    auto const energies = c.column("primary_energy_eV");
+    auto const paths = c.column("path_over_elastic_mfp");
+    auto const us = c.column("cdf");
+    auto const xs = c.column("one_minus_cos_theta");
+    std::map<double, std::map<double, std::vector<std::pair<double, double>>>> by_ep;
+    for (std::size_t i = 0; i < energies.size(); ++i) {
+        by_ep[energies[i]][paths[i]].emplace_back(us[i], xs[i]);
+    }
+    Angle a;
+    for (auto const& ep : by_ep) a.e.push_back(ep.first);
+    for (auto const& pp : by_ep.begin()->second) a.p.push_back(pp.first);
+    for (auto const& up : by_ep.begin()->second.begin()->second) a.u.push_back(up.first);
+    std::size_t const ne = a.e.size(), np = a.p.size(), nu = a.u.size();
+    if (ne < 2 || np < 2 || nu < 2) {
+        throw std::runtime_error("angle table too small: " + path);
+    }
+    a.omc.assign(ne * np * nu, 1.0);
+    for (std::size_t ie = 0; ie < ne; ++ie) {
+        auto const& pm = by_ep.at(a.e[ie]);
+        if (pm.size() != np) throw std::runtime_error("angle path count varies: " + path);
+        for (std::size_t ip = 0; ip < np; ++ip) {
+            auto const& v = pm.at(a.p[ip]);
+            if (v.size() != nu) throw std::runtime_error("angle u count varies: " + path);
+            for (std::size_t iu = 0; iu < nu; ++iu) {
+                if (v[iu].first != a.u[iu]) throw std::runtime_error("angle u grid differs: " + path);
+                double const x = v[iu].second;
+                if (!(x > 0.0) || x > 2.0) throw std::runtime_error("angle omc out of (0,2]: " + path);
+                if (iu > 0 && x > v[iu - 1].second) throw std::runtime_error("angle omc not monotone: " + path);
+                a.omc[(ie * np + ip) * nu + iu] = x;
+            }
+        }
+    }
+    return a;
+}
+
+}  // namespace
+
+int64_t TableSet::push(std::vector<double> const& values)
+{
+    int64_t const off = static_cast<int64_t>(m_arena.size());
+    m_arena.insert(m_arena.end(), values.begin(), values.end());
+    // Keep every array 32-byte aligned in the arena.
+    while (m_arena.size() % 4 != 0) {
+        m_arena.push_back(0.0);
+    }
+    return off;
+}
+
+int64_t TableSet::push_logs(std::vector<double> const& values, bool zero_for_nonpositive)
+{
+    std::vector<double> logs(values.size());
+    for (std::size_t i = 0; i < values.size(); ++i) {
+        logs[i] = (values[i] > 0.0 || !zero_for_nonpositive) ? std::log(values[i]) : 0.0;
+    }
+    return push(logs);
+}
+
+void TableSet::Load(std::string const& config_path)
+{
+    m_loaded = false;
+    m_arena.clear();
+    m_index = RreaArenaIndex{};
+    std::string const dir = dir_of(config_path);
+    JsonValue const cfg = ParseJson(read_text(config_path));
+    if (cfg.str("schema_version") != "6") {
+        throw std::runtime_error("only production schema 6 is supported");
+    }
+    JsonValue const& scattering = cfg.at("elastic_scattering_model");
+    double const transition = scattering.num_or("transition_energy_eV", -1.0);
+    double const few = scattering.num_or("few_collision_threshold_n", -1.0);
+    double const iso = scattering.num_or("isotropic_above_path_n", -1.0);
+    if (!(transition > 0.0) || !(few > 0.0) || !(iso > few)) {
+        throw std::runtime_error("invalid elastic_scattering_model thresholds");
+    }
+    if (cfg.str_or("transport_model", "") != "rrea_mc_pic_v6_geant4_10_7_4p04") {
+        throw std::runtime_error("unexpected transport_model");
+    }
+
+    static char const* const hot_names[RREA_T_COUNT] = {
+        "electron_collision_stopping_air",
+        "electron_soft_radiative_stopping_air",
+        "electron_hard_moller_inverse_length_air",
+        "electron_tracked_brems_inverse_length_air",
+        "electron_elastic_transport_inverse_length_air",
+        "positron_collision_stopping_air",
+        "positron_soft_radiative_stopping_air",
+        "positron_hard_bhabha_inverse_length_air",
+        "positron_tracked_brems_inverse_length_air",
+        "positron_elastic_transport_inverse_length_air",
+        "positron_annihilation_inverse_length_air",
+        "photon_compton_inverse_length_air",
+        "photon_photoelectric_inverse_length_air",
+        "photon_pair_nuclear_inverse_length_air",
+        "photon_pair_triplet_inverse_length_air",
+    };
+    static char const* const cdf_names[RREA_C_COUNT] = {
+        "electron_moller_secondary_cdf_air",
+        "positron_hard_bhabha_secondary_cdf_air",
+        "brems_photon_energy_cdf_air",
+        "positron_brems_photon_energy_cdf_air",
+    };
+
+    std::map<std::string, Table1D> tables;
+    std::map<std::string, CondGroups> cdfs;
+    std::map<std::string, Angle> angles;
+    std::map<std::string, std::vector<std::vector<double>>> elastic;  // x, mfp, eta, transport
+
+    JsonValue const& list = cfg.at("tables");
+    for (auto const& obj : list.items) {
+        std::string const name = obj.str("name");
+        std::string const kind = obj.str_or("table_kind", "");
+        std::string const path = dir + "/" + obj.str("path");
+        if (kind == "gs_angle_cdf_2d" || kind == "wentzel_vi_angle_cdf_2d") {
+            angles[name] = load_angle(path);
+            continue;
+        }
+        if (name == "electron_elastic_mfp_air" || name == "positron_elastic_mfp_air") {
+            auto const c = ReadRreaTableContainer(path);
+            std::vector<std::vector<double>> cols = {
+                c.column("primary_energy_eV"), c.column("elastic_mfp_m_stp"),
+                c.column("screening_eta"), c.column("transport_mfp_m_stp")};
+            for (std::size_t i = 0; i < cols[0].size(); ++i) {
+                if (!(cols[0][i] > 0.0) || !(cols[1][i] > 0.0) || !(cols[2][i] > 0.0)
+                    || (i > 0 && !(cols[0][i] > cols[0][i - 1]))) {
+                    throw std::runtime_error("elastic parameter table invalid: " + name);
+                }
+            }
+            elastic[name] = std::move(cols);
+            continue;
+        }
+        if (kind == "conditional_cdf") {
+            std::string value_column = obj.str_or("value_column", "");
+            if (value_column.empty()) value_column = obj.str("primary_value_column");
+            auto const c = ReadRreaTableContainer(path);
+            cdfs[name] = group_conditional(c.column("primary_energy_eV"), c.column("cdf_u"),
+                                           c.column(value_column), name);
+            continue;
+        }
+        if (kind == "photoelectric_subshell_cdf") {
+            continue;  // photon final states load this separately
+        }
+        std::string x_column = obj.str_or("x_column", "energy_eV");
+        std::string value_column = obj.str_or("value_column", "");
+        if (value_column.empty()) value_column = obj.str("primary_value_column");
+        std::string interpolation = obj.str_or("interpolation", "loglog_linear");
+        if (obj.str_or("extrapolation", "forbidden") != "forbidden") {
+            throw std::runtime_error("table extrapolation must be forbidden: " + name);
+        }
+        bool const allow_dup = obj.bool_or("allow_duplicate_x", false);
+        auto const c = ReadRreaTableContainer(path);
+        Table1D t;
+        t.interpolation = interpolation;
+        t.x = c.column(x_column);
+        t.y = c.column(value_column);
+        if (t.x.size() != t.y.size() || t.x.size() < 2) {
+            throw std::runtime_error("table column sizes invalid: " + name);
+        }
+        for (std::size_t i = 0; i < t.x.size(); ++i) {
+            if (!(t.x[i] > 0.0) || t.y[i] < 0.0
+                || (interpolation == "loglog_linear" && !(t.y[i] > 0.0))) {
+                throw std::runtime_error("table values invalid: " + name);
+            }
+            if (i > 0 && (t.x[i] < t.x[i - 1] || (!allow_dup && t.x[i] == t.x[i - 1]))) {
+                throw std::runtime_error("table energy grid not increasing: " + name);
+            }
+        }
+        tables[name] = std::move(t);
+    }
+
+    auto const charged = cfg.at("charged_energy_range_eV");
+    auto const photon = cfg.at("photon_energy_range_eV");
+    m_index.charged_min_eV = charged.items.at(0).num();
+    m_index.charged_max_eV = charged.items.at(1).num();
+    m_index.photon_min_eV = photon.items.at(0).num();
+    m_index.photon_max_eV = photon.items.at(1).num();
+    m_index.hard_moller_threshold_eV = cfg.num_or("hard_moller_secondary_threshold_eV", 0.0);
+    m_index.brems_absolute_cutoff_eV = cfg.num_or("brems_absolute_cutoff_eV", 0.0);
+    m_index.reference_density_kg_m3 = cfg.num_or("reference_density_kg_m3", -1.0);
+    m_index.gs_few_collision_threshold = few;
+    m_index.gs_isotropic_above_n = iso;
+    m_index.gs_wentzel_transition_eV = transition;
+    m_index.w_air_eV_per_pair = 33.97;  // ICRU Report 31 W value for air
+    if (!(m_index.hard_moller_threshold_eV > 0.0) || !(m_index.brems_absolute_cutoff_eV > 0.0)
+        || !(m_index.reference_density_kg_m3 > 0.0)) {
+        throw std::runtime_error("schema-6 thresholds or reference density invalid");
+    }
+
+    // Hot 1-D tables.  Tables sharing a bit-identical energy grid share one
+    // arena copy of it (and of its logs).
+    std::vector<std::pair<std::vector<double> const*, std::pair<int64_t, int64_t>>> grids;
+    for (int t = 0; t < RREA_T_COUNT; ++t) {
+        auto const it = tables.find(hot_names[t]);
+        if (it == tables.end()) {
+            throw std::runtime_error(std::string("missing required table ") + hot_names[t]);
+        }
+        Table1D const& tab = it->second;
+        RreaTable1DIndex& h = m_index.hot[t];
+        h.n = static_cast<int32_t>(tab.x.size());
+        if (tab.interpolation == "loglog_linear") h.mode = RREA_INTERP_LOGLOG;
+        else if (tab.interpolation == "loglog_positive_with_zero_threshold") h.mode = RREA_INTERP_LOGLOG_ZERO_THRESHOLD;
+        else if (tab.interpolation == "logx_linear") h.mode = RREA_INTERP_LOGX_LINEAR;
+        else if (tab.interpolation == "linear") h.mode = RREA_INTERP_LINEAR;
+        else throw std::runtime_error("unsupported interpolation " + tab.interpolation);
+        bool reused = false;
+        for (auto const& g : grids) {
+            if (*g.first == tab.x) {
+                h.x = g.second.first;
+                h.lx = g.second.second;
+                reused = true;
+                break;
+            }
+        }
+        if (!reused) {
+            h.x = push(tab.x);
+            h.lx = push_logs(tab.x, false);
+            grids.push_back({&tab.x, {h.x, h.lx}});
+        }
+        h.y = push(tab.y);
+        h.ly = push_logs(tab.y, true);
+    }
+    auto shared = [&](int first, int last) {
+        for (int t = first + 1; t <= last; ++t) {
+            if (m_index.hot[t].x != m_index.hot[first].x) return 0;
+        }
+        return 1;
+    };
+    m_index.electron_grid_shared = shared(RREA_T_E_COLLISION, RREA_T_E_ELASTIC_TRANSPORT);
+    m_index.positron_grid_shared = shared(RREA_T_P_COLLISION, RREA_T_P_ANNIHILATION);
+    m_index.photon_grid_shared = shared(RREA_T_PH_COMPTON, RREA_T_PH_PAIR_TRIPLET);
+    // Certified-range coverage (RreaInteractionTables.cpp:1979-2017).
+    for (int t = 0; t < RREA_T_COUNT; ++t) {
+        RreaTable1DIndex const& h = m_index.hot[t];
+        double const lo = (t >= RREA_T_PH_COMPTON) ? m_index.photon_min_eV : m_index.charged_min_eV;
+        double const hi = (t >= RREA_T_PH_COMPTON) ? m_index.photon_max_eV : m_index.charged_max_eV;
+        if (m_arena[h.x] != lo || m_arena[h.x + h.n - 1] != hi) {
+            throw std::runtime_error(std::string("table does not cover certified range: ") + hot_names[t]);
+        }
+    }
+
+    for (int c = 0; c < RREA_C_COUNT; ++c) {
+        auto const it = cdfs.find(cdf_names[c]);
+        if (it == cdfs.end()) {
+            throw std::runtime_error(std::string("missing conditional CDF ") + cdf_names[c]);
+        }
+        CondGroups const& g = it->second;
+        RreaCondCdfIndex& ci = m_index.cdf[c];
+        ci.ng = static_cast<int32_t>(g.primary.size());
+        ci.primary = push(g.primary);
+        ci.lprimary = push_logs(g.primary, false);
+        std::vector<double> start(g.primary.size() + 1, 0.0), u, v;
+        for (std::size_t k = 0; k < g.primary.size(); ++k) {
+            start[k] = static_cast<double>(u.size());
+            u.insert(u.end(), g.u[k].begin(), g.u[k].end());
+            v.insert(v.end(), g.v[k].begin(), g.v[k].end());
+        }
+        start.back() = static_cast<double>(u.size());
+        ci.total = static_cast<int32_t>(u.size());
+        ci.start = push(start);
+        ci.u = push(u);
+        ci.v = push(v);
+    }
+
+    for (int s = 0; s < 2; ++s) {
+        auto const it = elastic.find(s == 0 ? "electron_elastic_mfp_air" : "positron_elastic_mfp_air");
+        if (it == elastic.end()) throw std::runtime_error("missing elastic parameter table");
+        auto const& cols = it->second;
+        if (cols[0].front() != 1.0e3 || cols[0].back() != 1.0e10) {
+            throw std::runtime_error("elastic parameter table must cover 1 keV - 10 GeV");
+        }
+        RreaElasticIndex& e = m_index.elastic[s];
+        e.n = static_cast<int32_t>(cols[0].size());
+        e.x = push(cols[0]);
+        e.lx = push_logs(cols[0], false);
+        e.mfp = push(cols[1]);
+        e.eta = push(cols[2]);
+    }
+
+    auto put_angle = [&](RreaAngleIndex& ai, char const* name, double lo, double hi) {
+        auto const it = angles.find(name);
+        if (it == angles.end()) throw std::runtime_error(std::string("missing angle table ") + name);
+        Angle const& a = it->second;
+        if (a.e.front() != lo || a.e.back() != hi || a.p.front() > few || a.p.back() < iso) {
+            throw std::runtime_error(std::string("angle table coverage invalid: ") + name);
+        }
+        ai.ne = static_cast<int32_t>(a.e.size());
+        ai.np = static_cast<int32_t>(a.p.size());
+        ai.nu = static_cast<int32_t>(a.u.size());
+        ai.e = push(a.e);
+        ai.le = push_logs(a.e, false);
+        ai.p = push(a.p);
+        ai.lp = push_logs(a.p, false);
+        ai.u = push(a.u);
+        std::vector<double> lur(a.u.size(), 0.0);
+        for (std::size_t i = 0; i + 1 < a.u.size(); ++i) {
+            lur[i] = (a.u[i] > 0.0) ? std::log(a.u[i + 1] / a.u[i]) : 0.0;
+        }
+        ai.lur = push(lur);
+        ai.omc = push(a.omc);
+        ai.lomc = push_logs(a.omc, false);
+    };
+    put_angle(m_index.gs[0], "electron_gs_angle_cdf_air", m_index.charged_min_eV, transition);
+    put_angle(m_index.gs[1], "positron_gs_angle_cdf_air", m_index.charged_min_eV, transition);
+    put_angle(m_index.wentzel[0], "electron_wentzel_vi_angle_cdf_air", transition, m_index.charged_max_eV);
+    put_angle(m_index.wentzel[1], "positron_wentzel_vi_angle_cdf_air", transition, m_index.charged_max_eV);
+
+    // Mean hard-Moller delta-ray energy per event on the rate grid: midpoint
+    // quadrature of the secondary sampler over 4096 uniform nodes, only where
+    // the rate is positive (RreaInteractionTables.cpp:2146-2179).
+    {
+        RreaTable1DIndex const& rate = m_index.hot[RREA_T_E_HARD_MOLLER];
+        RreaCondCdfIndex const& mc = m_index.cdf[RREA_C_MOLLER];
+        std::vector<double> mean(static_cast<std::size_t>(rate.n), 0.0);
+        int const samples = 4096;
+        for (int i = 0; i < rate.n; ++i) {
+            double const e = m_arena[rate.x + i];
+            if (!(m_arena[rate.y + i] > 0.0)) {
+                continue;
+            }
+            if (e < m_arena[mc.primary] || e > m_arena[mc.primary + mc.ng - 1]) {
+                throw std::runtime_error("hard-Moller rate positive outside the Moller CDF range");
+            }
+            double acc = 0.0;
+            for (int s = 0; s < samples; ++s) {
+                acc += HostSampleConditional(*this, RREA_C_MOLLER, e,
+                                             (static_cast<double>(s) + 0.5) / samples, true);
+            }
+            mean[static_cast<std::size_t>(i)] = acc / static_cast<double>(samples);
+        }
+        m_index.hard_moller_mean_secondary = push(mean);
+    }
+    m_index.total_doubles = static_cast<int64_t>(m_arena.size());
+    m_loaded = true;
+}
+
+// Conditional inverse-CDF sampling (RreaInteractionTables.cpp:995-1069 and the
+// Moller variant :2584-2653, which always log-interpolates between groups).
+double HostSampleConditional(TableSet const& tables, int which, double primary_eV,
+                             double cdf_u, bool moller_always_log)
+{
+    RreaCondCdfIndex const& ci = tables.index().cdf[which];
+    double const* prim = tables.at(ci.primary);
+    double const* start = tables.at(ci.start);
+    double const* u = tables.at(ci.u);
+    double const* v = tables.at(ci.v);
+    cdf_u = std::max(0.0, std::min(1.0, cdf_u));
+    auto sample_group = [&](int g) {
+        int const b = static_cast<int>(start[g]);
+        int const e = static_cast<int>(start[g + 1]);
+        double const* ub = u + b;
+        double const* up = std::lower_bound(ub, u + e, cdf_u);
+        if (up == ub) return v[b];
+        if (up == u + e) return v[e - 1];
+        int const hi = static_cast<int>(up - u);
+        int const lo = hi - 1;
+        double const denom = u[hi] - u[lo];
+        double const t = denom > 0.0 ? (cdf_u - u[lo]) / denom : 0.0;
+        return v[lo] + t * (v[hi] - v[lo]);
+    };
+    if (!std::isfinite(primary_eV) || primary_eV < prim[0] || primary_eV > prim[ci.ng - 1]) {
+        throw std::runtime_error("conditional CDF primary energy outside range");
+    }
+    if (!moller_always_log) {
+        if (primary_eV == prim[0]) return sample_group(0);
+        if (primary_eV == prim[ci.ng - 1]) return sample_group(ci.ng - 1);
+    }
+    double const* up = std::lower_bound(prim, prim + ci.ng, primary_eV);
+    if (up == prim) return sample_group(0);
+    if (up == prim + ci.ng) return sample_group(ci.ng - 1);
+    int const hi = static_cast<int>(up - prim);
+    int const lo = hi - 1;
+    if (prim[hi] == primary_eV) return sample_group(hi);
+    double const y0 = sample_group(lo);
+    double const y1 = sample_group(hi);
+    double const t = (std::log(primary_eV) - std::log(prim[lo]))
+        / (std::log(prim[hi]) - std::log(prim[lo]));
+    if (moller_always_log || (y0 > 0.0 && y1 > 0.0)) {
+        return std::exp(std::log(y0) + t * (std::log(y1) - std::log(y0)));
+    }
+    return y0 + t * (y1 - y0);
+}
+
+}  // namespace rrea_host

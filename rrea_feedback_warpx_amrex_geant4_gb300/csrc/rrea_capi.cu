@@ -1,0 +1,590 @@
+// C-ABI of the GB300 kinetic step (include/rrea_gpu.h).  Host C++ around the
+// kernels in rrea_kernels.cu: owns the device arena, field vectors, the
+// resident species tile and every per-step buffer.  All device memory is
+// allocated at create/load time; a step allocates nothing.
+#include "../../include/rrea_gpu.h"
+
+#include "device/rrea_electron.cuh"
+#include "host/table_set.hpp"
+#include "rrea_kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+namespace {
+
+constexpr int kTileDoubles = 13;
+
+}  // namespace
+
+struct rrea_gpu_ctx {
+    rrea_gpu_config cfg{};
+    int64_t capacity = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+
+    rrea_host::TableSet tables;
+    bool tables_loaded = false;
+    double* d_arena = nullptr;
+
+    double* d_er = nullptr;
+    double* d_ez = nullptr;
+    double* d_bt = nullptr;
+    double* d_amb_er = nullptr;
+    double* d_amb_ez = nullptr;
+    double* d_cell_er = nullptr;
+    double* d_cell_ez = nullptr;
+    bool field_set = false;
+    bool has_b = false;
+
+    double* d_tile[kTileDoubles] = {};
+    int64_t* d_id = nullptr;
+    int32_t* d_cpu = nullptr;
+    int64_t staged_n = 0;
+
+    rrea_gpu_secondary* d_sec_unordered = nullptr;
+    rrea_gpu_secondary* d_sec_ordered = nullptr;
+    int64_t sec_capacity = 0;
+    unsigned long long* d_sec_count = nullptr;
+    uint32_t* d_sec_per_parent = nullptr;
+    int64_t* d_offsets = nullptr;
+    int64_t* d_scan_scratch = nullptr;
+    double* d_cells = nullptr;
+    uint64_t* d_diag_sub = nullptr;
+    uint64_t* d_diag_ev = nullptr;
+    int32_t* d_diag_disp = nullptr;
+    int* d_status = nullptr;
+    long long* d_fail_index = nullptr;
+    unsigned long long* d_transported = nullptr;
+    cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev_stop = nullptr;
+    float last_kernel_ms = 0.0f;
+    int64_t last_transported = 0;
+    int64_t last_secondaries = 0;
+    int launch_threads = 128;
+    int launch_blocks_per_sm = 8;
+    bool diagnostics = true;
+
+    std::string last_error;
+};
+
+namespace {
+
+rrea_gpu_status fail(rrea_gpu_ctx* ctx, rrea_gpu_status code, std::string const& msg)
+{
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+rrea_gpu_status cuda_fail(rrea_gpu_ctx* ctx, cudaError_t e, char const* where)
+{
+    return fail(ctx, RREA_GPU_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define RREA_CUDA(ctx, call)                                  \
+    do {                                                      \
+        cudaError_t const _e = (call);                        \
+        if (_e != cudaSuccess) return cuda_fail(ctx, _e, #call); \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count)
+{
+    return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T) > 0 ? count * sizeof(T) : sizeof(T));
+}
+
+void dfree(void* p)
+{
+    if (p) cudaFree(p);
+}
+
+bool config_valid(rrea_gpu_config const& c, std::string& why)
+{
+    if (!(std::isfinite(c.r_lo) && std::isfinite(c.r_hi) && std::isfinite(c.z_lo) && std::isfinite(c.z_hi))
+        || !(c.r_lo >= 0.0) || !(c.r_hi > c.r_lo) || !(c.z_hi > c.z_lo)) {
+        why = "invalid RZ domain";
+        return false;
+    }
+    if (c.r_lo != 0.0) {
+        why = "the RZ domain must start on the axis (r_lo = 0)";
+        return false;
+    }
+    if (c.nr < 1 || c.nz < 1) {
+        why = "field grid must have at least one cell per direction";
+        return false;
+    }
+    if (!(c.max_optical_depth_per_substep > 0.0) || !std::isfinite(c.max_optical_depth_per_substep)
+        || c.max_subcycles == 0 || c.max_subcycles >= (uint64_t{1} << 14)) {
+        why = "invalid subcycle controls (max_subcycles must be in [1, 16383])";
+        return false;
+    }
+    if (!(c.low_energy_cutoff_eV > 0.0) || !std::isfinite(c.low_energy_cutoff_eV)) {
+        why = "low_energy_cutoff_eV must be finite and positive";
+        return false;
+    }
+    if (!(c.max_gs_collisions_per_substep > 0.0) || !(c.gs_total_collision_cap > 0.0)
+        || !(c.max_field_impulse_fraction > 0.0) || !(c.field_impulse_floor_eV >= 0.0)) {
+        why = "invalid substep driver controls";
+        return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rrea_gpu_default_config(rrea_gpu_config* cfg)
+{
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->r_lo = 0.0;
+    cfg->r_hi = 50.0;
+    cfg->z_lo = 0.0;
+    cfg->z_hi = 500.0;
+    cfg->nr = 32;
+    cfg->nz = 256;
+    cfg->periodic_z = 0;
+    cfg->strict_transport_guards = 1;
+    cfg->density_ratio = 1.0;
+    cfg->low_energy_cutoff_eV = 1.0e3;
+    cfg->photon_cutoff_eV = 5.0e4;
+    cfg->max_optical_depth_per_substep = 0.05;
+    cfg->max_subcycles = 256;
+    cfg->max_gs_collisions_per_substep = 32.0;
+    cfg->gs_total_collision_cap = 1024.0;
+    cfg->max_field_impulse_fraction = 0.1;
+    cfg->field_impulse_floor_eV = 1.0e4;
+    cfg->rng_seed = 0;
+    cfg->debug_disable_hard_moller = 0;
+}
+
+rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rrea_gpu_ctx** out)
+{
+    if (!cfg || !out || capacity < 1) return RREA_GPU_ERR_ARGUMENT;
+    *out = nullptr;
+    std::string why;
+    if (!config_valid(*cfg, why)) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_ctx* ctx = new (std::nothrow) rrea_gpu_ctx();
+    if (!ctx) return RREA_GPU_ERR_CAPACITY;
+    ctx->cfg = *cfg;
+    ctx->capacity = capacity;
+    auto bail = [&](rrea_gpu_status s) {
+        rrea_gpu_destroy(ctx);
+        return s;
+    };
+    if (cudaGetDevice(&ctx->device) != cudaSuccess) return bail(RREA_GPU_ERR_CUDA);
+    if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess) {
+        return bail(RREA_GPU_ERR_CUDA);
+    }
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RREA_GPU_ERR_CUDA);
+    size_t const n = static_cast<size_t>(capacity);
+    size_t const ner = static_cast<size_t>(cfg->nr + 1) * cfg->nz;
+    size_t const nez = static_cast<size_t>(cfg->nr) * (cfg->nz + 1);
+    size_t const nbt = static_cast<size_t>(cfg->nr + 1) * (cfg->nz + 1);
+    size_t const ncell = static_cast<size_t>(cfg->nr) * cfg->nz;
+    bool ok = dalloc(&ctx->d_er, ner) == cudaSuccess && dalloc(&ctx->d_ez, nez) == cudaSuccess
+        && dalloc(&ctx->d_bt, nbt) == cudaSuccess && dalloc(&ctx->d_amb_er, ner) == cudaSuccess
+        && dalloc(&ctx->d_amb_ez, nez) == cudaSuccess && dalloc(&ctx->d_cell_er, ncell) == cudaSuccess
+        && dalloc(&ctx->d_cell_ez, ncell) == cudaSuccess && dalloc(&ctx->d_cells, 5 * ncell) == cudaSuccess;
+    for (int f = 0; ok && f < kTileDoubles; ++f) ok = dalloc(&ctx->d_tile[f], n) == cudaSuccess;
+    ctx->sec_capacity = 2 * capacity + 4096;
+    size_t const nsec = static_cast<size_t>(ctx->sec_capacity);
+    ok = ok && dalloc(&ctx->d_id, n) == cudaSuccess && dalloc(&ctx->d_cpu, n) == cudaSuccess
+        && dalloc(&ctx->d_sec_unordered, nsec) == cudaSuccess && dalloc(&ctx->d_sec_ordered, nsec) == cudaSuccess
+        && dalloc(&ctx->d_sec_count, 1) == cudaSuccess && dalloc(&ctx->d_sec_per_parent, n) == cudaSuccess
+        && dalloc(&ctx->d_offsets, n) == cudaSuccess
+        && dalloc(&ctx->d_scan_scratch, static_cast<size_t>(rrea_launch::scan_scratch_elems(capacity))) == cudaSuccess
+        && dalloc(&ctx->d_diag_sub, n) == cudaSuccess && dalloc(&ctx->d_diag_ev, n) == cudaSuccess
+        && dalloc(&ctx->d_diag_disp, n) == cudaSuccess && dalloc(&ctx->d_status, 1) == cudaSuccess
+        && dalloc(&ctx->d_fail_index, 1) == cudaSuccess && dalloc(&ctx->d_transported, 1) == cudaSuccess
+        && cudaEventCreate(&ctx->ev_start) == cudaSuccess && cudaEventCreate(&ctx->ev_stop) == cudaSuccess;
+    if (!ok) return bail(RREA_GPU_ERR_CUDA);
+    if (cudaMemsetAsync(ctx->d_cells, 0, 5 * ncell * sizeof(double), ctx->stream) != cudaSuccess) {
+        return bail(RREA_GPU_ERR_CUDA);
+    }
+    *out = ctx;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
+{
+    if (!ctx) return RREA_GPU_OK;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    dfree(ctx->d_arena);
+    dfree(ctx->d_er);
+    dfree(ctx->d_ez);
+    dfree(ctx->d_bt);
+    dfree(ctx->d_amb_er);
+    dfree(ctx->d_amb_ez);
+    dfree(ctx->d_cell_er);
+    dfree(ctx->d_cell_ez);
+    for (auto* p : ctx->d_tile) dfree(p);
+    dfree(ctx->d_id);
+    dfree(ctx->d_cpu);
+    dfree(ctx->d_sec_unordered);
+    dfree(ctx->d_sec_ordered);
+    dfree(ctx->d_sec_count);
+    dfree(ctx->d_sec_per_parent);
+    dfree(ctx->d_offsets);
+    dfree(ctx->d_scan_scratch);
+    dfree(ctx->d_cells);
+    dfree(ctx->d_diag_sub);
+    dfree(ctx->d_diag_ev);
+    dfree(ctx->d_diag_disp);
+    dfree(ctx->d_status);
+    dfree(ctx->d_fail_index);
+    dfree(ctx->d_transported);
+    if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+    if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_load_tables(rrea_gpu_ctx* ctx, const char* path)
+{
+    if (!ctx || !path) return RREA_GPU_ERR_ARGUMENT;
+    try {
+        ctx->tables.Load(path);
+    } catch (std::exception const& e) {
+        ctx->tables_loaded = false;
+        return fail(ctx, RREA_GPU_ERR_TABLES, e.what());
+    }
+    // The photon cutoff is the bundle's brems cutoff; a differing configured
+    // value is refused (RreaCouplingConfig.cpp:1334-1342).
+    double const brems_cut = ctx->tables.index().brems_absolute_cutoff_eV;
+    if (std::isfinite(ctx->cfg.photon_cutoff_eV) && ctx->cfg.photon_cutoff_eV != brems_cut) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "photon_cutoff_eV does not match the tables' brems_absolute_cutoff_eV");
+    }
+    ctx->cfg.photon_cutoff_eV = brems_cut;
+    double const hm = ctx->tables.index().hard_moller_threshold_eV;
+    if (!(hm > ctx->cfg.low_energy_cutoff_eV)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "hard-Moller threshold must exceed the tracking cutoff");
+    }
+    if (ctx->cfg.low_energy_cutoff_eV < ctx->tables.index().charged_min_eV) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "tracking cutoff below the certified charged range");
+    }
+    auto const& arena = ctx->tables.arena();
+    dfree(ctx->d_arena);
+    ctx->d_arena = nullptr;
+    RREA_CUDA(ctx, dalloc(&ctx->d_arena, arena.size()));
+    RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_arena, arena.data(), arena.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->tables_loaded = true;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_set_field(rrea_gpu_ctx* ctx, const double* er, const double* ez, const double* bt,
+                                   const double* amb_er, const double* amb_ez)
+{
+    if (!ctx || !er || !ez || !bt || !amb_er || !amb_ez) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_config const& c = ctx->cfg;
+    size_t const ner = static_cast<size_t>(c.nr + 1) * c.nz;
+    size_t const nez = static_cast<size_t>(c.nr) * (c.nz + 1);
+    size_t const nbt = static_cast<size_t>(c.nr + 1) * (c.nz + 1);
+    bool any_b = false;
+    for (size_t i = 0; i < nbt; ++i) {
+        if (bt[i] != 0.0) {
+            any_b = true;
+            break;
+        }
+    }
+    RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_er, er, ner * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_ez, ez, nez * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_bt, bt, nbt * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_amb_er, amb_er, ner * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_amb_ez, amb_ez, nez * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    RREA_CUDA(ctx, rrea_launch::field_prep(c.nr, c.nz, ctx->d_er, ctx->d_ez, ctx->d_amb_er, ctx->d_amb_ez,
+                                           ctx->d_cell_er, ctx->d_cell_ez, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->has_b = any_b;
+    ctx->field_set = true;
+    return RREA_GPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+rrea_gpu_status stage_tile(rrea_gpu_ctx* ctx, rrea_gpu_tile const* t)
+{
+    if (t->n > ctx->capacity) return fail(ctx, RREA_GPU_ERR_CAPACITY, "tile larger than the context capacity");
+    double* const host[kTileDoubles] = {t->r, t->z, t->theta, t->ux, t->uy, t->uz, t->w,
+                                        t->prev_r, t->prev_z, t->prev_theta, t->prev_ux, t->prev_uy, t->prev_uz};
+    size_t const bytes = static_cast<size_t>(t->n) * sizeof(double);
+    for (int f = 0; f < kTileDoubles; ++f) {
+        if (!host[f]) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "null tile component");
+        if (t->n) RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_tile[f], host[f], bytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if (!t->id) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "null tile id");
+    if (t->n) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_id, t->id, static_cast<size_t>(t->n) * sizeof(int64_t),
+                                       cudaMemcpyHostToDevice, ctx->stream));
+        if (t->cpu) {
+            RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_cpu, t->cpu, static_cast<size_t>(t->n) * sizeof(int32_t),
+                                           cudaMemcpyHostToDevice, ctx->stream));
+        } else {
+            RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_cpu, 0, static_cast<size_t>(t->n) * sizeof(int32_t), ctx->stream));
+        }
+    }
+    ctx->staged_n = t->n;
+    return RREA_GPU_OK;
+}
+
+// Launches the electron phase on the staged device tile.  `aliased` runs the
+// resident engine mode: the captured pre-push state is the current state.
+rrea_gpu_status launch_electrons(rrea_gpu_ctx* ctx, int32_t step, double dt_s, bool aliased)
+{
+    if (!ctx->tables_loaded || !ctx->field_set) {
+        return fail(ctx, RREA_GPU_ERR_NOT_READY, "tables and field must be set before a step");
+    }
+    if (!(dt_s > 0.0) || !std::isfinite(dt_s)) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "dt must be finite and positive");
+    rrea_gpu_config const& c = ctx->cfg;
+    rrea_dev::StepConstants sc{};
+    sc.cfg = c;
+    sc.tix = ctx->tables.index();
+    sc.dr = (c.r_hi - c.r_lo) / c.nr;
+    sc.dz = (c.z_hi - c.z_lo) / c.nz;
+    sc.hm_threshold_eV = sc.tix.hard_moller_threshold_eV;
+    sc.photon_cutoff_eV = c.photon_cutoff_eV;
+    // RreaParticleInteraction.cpp:33-35 with a uniform density ratio
+    sc.density_ratio = c.density_ratio > 0.0 ? c.density_ratio : 1.0;
+    sc.step_key = static_cast<uint64_t>(step > 0 ? step : 0);
+    sc.dt_s = dt_s;
+    sc.hm_enabled = c.debug_disable_hard_moller ? 0 : 1;
+    RREA_CUDA(ctx, rrea_launch::set_step_constants(sc, ctx->stream));
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_sec_count, 0, sizeof(unsigned long long), ctx->stream));
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_transported, 0, sizeof(unsigned long long), ctx->stream));
+
+    rrea_dev::ElectronArgs a{};
+    a.n = ctx->staged_n;
+    double** t = ctx->d_tile;
+    a.r = t[0]; a.z = t[1]; a.theta = t[2]; a.ux = t[3]; a.uy = t[4]; a.uz = t[5]; a.w = t[6];
+    if (aliased) {
+        a.prev_r = t[0]; a.prev_z = t[1]; a.prev_theta = t[2]; a.prev_ux = t[3]; a.prev_uy = t[4]; a.prev_uz = t[5];
+    } else {
+        a.prev_r = t[7]; a.prev_z = t[8]; a.prev_theta = t[9]; a.prev_ux = t[10]; a.prev_uy = t[11]; a.prev_uz = t[12];
+    }
+    a.id = ctx->d_id;
+    a.cpu = ctx->d_cpu;
+    a.sec = ctx->d_sec_unordered;
+    a.sec_count = ctx->d_sec_count;
+    a.sec_capacity = ctx->sec_capacity;
+    a.sec_per_parent = ctx->d_sec_per_parent;
+    a.cells = ctx->d_cells;
+    a.diag_subcycles = ctx->diagnostics ? ctx->d_diag_sub : nullptr;
+    a.diag_events = ctx->diagnostics ? ctx->d_diag_ev : nullptr;
+    a.diag_disposition = ctx->diagnostics ? ctx->d_diag_disp : nullptr;
+    a.status = ctx->d_status;
+    a.fail_index = ctx->d_fail_index;
+    a.transported = ctx->d_transported;
+    a.arena = ctx->d_arena;
+    a.fv.cell_er = ctx->d_cell_er;
+    a.fv.cell_ez = ctx->d_cell_ez;
+    a.fv.bt = ctx->d_bt;
+    a.fv.nr = c.nr;
+    a.fv.nz = c.nz;
+    a.fv.dr = sc.dr;
+    a.fv.dz = sc.dz;
+    a.fv.r_lo = c.r_lo;
+    a.fv.z_lo = c.z_lo;
+    a.fv.periodic = c.periodic_z != 0;
+    a.fv.has_b = ctx->has_b;
+    if (a.n > 0) {
+        int64_t const want = (a.n + ctx->launch_threads - 1) / ctx->launch_threads;
+        int64_t const cap = static_cast<int64_t>(ctx->num_sms) * ctx->launch_blocks_per_sm;
+        int const blocks = static_cast<int>(want < cap ? want : cap);
+        RREA_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+        RREA_CUDA(ctx, rrea_launch::electron_step(a, blocks > 0 ? blocks : 1, ctx->launch_threads, ctx->stream));
+        RREA_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+    }
+    unsigned long long count = 0;
+    unsigned long long transported = 0;
+    int status = 0;
+    long long fail_index = -1;
+    RREA_CUDA(ctx, cudaMemcpyAsync(&count, ctx->d_sec_count, sizeof(count), cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(&status, ctx->d_status, sizeof(status), cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(&fail_index, ctx->d_fail_index, sizeof(fail_index), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(&transported, ctx->d_transported, sizeof(transported), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->last_transported = static_cast<int64_t>(transported);
+    ctx->last_kernel_ms = 0.0f;
+    if (a.n > 0) RREA_CUDA(ctx, cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev_start, ctx->ev_stop));
+    if (status != 0) {
+        return fail(ctx, static_cast<rrea_gpu_status>(status),
+                    "electron transport guard failed (status " + std::to_string(status) + ") at particle "
+                        + std::to_string(fail_index));
+    }
+    if (count > static_cast<unsigned long long>(ctx->sec_capacity)) {
+        return fail(ctx, RREA_GPU_ERR_CAPACITY, "secondary buffer overflow");
+    }
+    ctx->last_secondaries = static_cast<int64_t>(count);
+    RREA_CUDA(ctx, rrea_launch::order_secondaries(ctx->d_sec_per_parent, a.n, ctx->d_offsets, ctx->d_scan_scratch,
+                                                  ctx->d_sec_unordered, ctx->last_secondaries, ctx->d_sec_ordered,
+                                                  ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status unstage_tile(rrea_gpu_ctx* ctx, rrea_gpu_tile* t)
+{
+    double* const host[6] = {t->r, t->z, t->theta, t->ux, t->uy, t->uz};
+    size_t const bytes = static_cast<size_t>(t->n) * sizeof(double);
+    if (t->n) {
+        for (int f = 0; f < 6; ++f) {
+            RREA_CUDA(ctx, cudaMemcpyAsync(host[f], ctx->d_tile[f], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        RREA_CUDA(ctx, cudaMemcpyAsync(t->id, ctx->d_id, static_cast<size_t>(t->n) * sizeof(int64_t),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    return RREA_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rrea_gpu_status rrea_gpu_apply_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, int32_t step, double time_s,
+                                         double dt_s, rrea_gpu_secondary* secondaries, int64_t secondary_capacity,
+                                         int64_t* n_secondaries)
+{
+    (void)time_s;
+    if (!ctx || !tile || tile->n < 0) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_status s = stage_tile(ctx, tile);
+    if (s != RREA_GPU_OK) return s;
+    s = launch_electrons(ctx, step, dt_s, /*aliased=*/false);
+    if (s != RREA_GPU_OK) return s;
+    if (n_secondaries) *n_secondaries = ctx->last_secondaries;
+    if (secondaries && ctx->last_secondaries > secondary_capacity) {
+        return fail(ctx, RREA_GPU_ERR_CAPACITY, "caller secondary buffer too small");
+    }
+    s = unstage_tile(ctx, tile);
+    if (s != RREA_GPU_OK) return s;
+    if (secondaries && ctx->last_secondaries > 0) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(secondaries, ctx->d_sec_ordered,
+                                       static_cast<size_t>(ctx->last_secondaries) * sizeof(rrea_gpu_secondary),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_download_sources(rrea_gpu_ctx* ctx, double* out5)
+{
+    if (!ctx || !out5) return RREA_GPU_ERR_ARGUMENT;
+    size_t const n = static_cast<size_t>(ctx->cfg.nr) * ctx->cfg.nz * 5;
+    RREA_CUDA(ctx, cudaMemcpyAsync(out5, ctx->d_cells, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_reset_sources(rrea_gpu_ctx* ctx)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    size_t const n = static_cast<size_t>(ctx->cfg.nr) * ctx->cfg.nz * 5;
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_cells, 0, n * sizeof(double), ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_download_diagnostics(rrea_gpu_ctx* ctx, int64_t n, uint64_t* subcycles, uint64_t* events,
+                                              int32_t* disposition)
+{
+    if (!ctx || n < 0 || n > ctx->capacity) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->diagnostics) return fail(ctx, RREA_GPU_ERR_NOT_READY, "diagnostics are disabled");
+    if (n == 0) return RREA_GPU_OK;
+    if (subcycles) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(subcycles, ctx->d_diag_sub, n * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    }
+    if (events) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(events, ctx->d_diag_ev, n * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    }
+    if (disposition) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(disposition, ctx->d_diag_disp, n * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+void rrea_gpu_last_error(const rrea_gpu_ctx* ctx, char* buf, size_t size)
+{
+    if (!buf || size == 0) return;
+    std::string const& m = ctx ? ctx->last_error : std::string("no context");
+    std::strncpy(buf, m.c_str(), size - 1);
+    buf[size - 1] = '\0';
+}
+
+// ---- resident engine mode (inputs already in HBM) --------------------------
+
+rrea_gpu_status rrea_gpu_stage_electrons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile)
+{
+    if (!ctx || !tile || tile->n < 0) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_status const s = stage_tile(ctx, tile);
+    if (s != RREA_GPU_OK) return s;
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t* n_secondaries)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_status const s = launch_electrons(ctx, step, dt_s, /*aliased=*/true);
+    if (s != RREA_GPU_OK) return s;
+    if (n_secondaries) *n_secondaries = ctx->last_secondaries;
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fetch_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile)
+{
+    if (!ctx || !tile || tile->n != ctx->staged_n) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_status const s = unstage_tile(ctx, tile);
+    if (s != RREA_GPU_OK) return s;
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm,
+                                    int32_t diagnostics)
+{
+    if (!ctx || threads_per_block < 32 || threads_per_block > 128 || (threads_per_block % 32) != 0 || blocks_per_sm < 1
+        || blocks_per_sm > 64) {
+        return RREA_GPU_ERR_ARGUMENT;
+    }
+    ctx->launch_threads = threads_per_block;
+    ctx->launch_blocks_per_sm = blocks_per_sm;
+    ctx->diagnostics = diagnostics != 0;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_last_step_stats(rrea_gpu_ctx* ctx, int64_t* transported, int64_t* secondaries,
+                                         double* kernel_ms)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    if (transported) *transported = ctx->last_transported;
+    if (secondaries) *secondaries = ctx->last_secondaries;
+    if (kernel_ms) *kernel_ms = static_cast<double>(ctx->last_kernel_ms);
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_stream(rrea_gpu_ctx* ctx, void** stream)
+{
+    if (!ctx || !stream) return RREA_GPU_ERR_ARGUMENT;
+    *stream = ctx->stream;
+    return RREA_GPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,253 @@
+"""Python host side of the GB300 kinetic step: a thin ctypes binding over the
+C-ABI in include/rrea_gpu.h (lib/librrea_gpu.so).
+
+The names mirror the reference overlay: ``RreaParticleInteraction.Apply``
+runs the per-timestep transport of one electron tile the way
+``rrea::warpx::RreaParticleInteraction::Apply`` does
+(native_amrex_rrea/warpx_overlay/Source/Rrea/RreaParticleInteraction.H:1609-1623),
+and every non-OK status raises, as the reference aborts.  There is no CPU
+fallback: a missing library raises at load.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import DEFAULT_TABLES, PACKAGE_DIR
+
+LIB_PATH = os.path.join(PACKAGE_DIR, "lib", "librrea_gpu.so")
+
+STATUS_NAMES = {
+    0: "OK", 1: "ERR_ARGUMENT", 2: "ERR_TABLES", 3: "ERR_CUDA", 4: "ERR_RANGE", 5: "ERR_GEOMETRY",
+    6: "ERR_RNG_OVERFLOW", 7: "ERR_GUARD", 8: "ERR_CAPACITY", 9: "ERR_INVALID_STATE", 10: "ERR_NOT_READY",
+}
+
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+class RreaGpuConfig(ctypes.Structure):
+    """rrea_gpu_config (include/rrea_gpu.h)."""
+
+    _fields_ = [
+        ("r_lo", ctypes.c_double), ("r_hi", ctypes.c_double),
+        ("z_lo", ctypes.c_double), ("z_hi", ctypes.c_double),
+        ("nr", ctypes.c_int32), ("nz", ctypes.c_int32),
+        ("periodic_z", ctypes.c_int32), ("strict_transport_guards", ctypes.c_int32),
+        ("density_ratio", ctypes.c_double),
+        ("low_energy_cutoff_eV", ctypes.c_double), ("photon_cutoff_eV", ctypes.c_double),
+        ("max_optical_depth_per_substep", ctypes.c_double), ("max_subcycles", ctypes.c_uint64),
+        ("max_gs_collisions_per_substep", ctypes.c_double), ("gs_total_collision_cap", ctypes.c_double),
+        ("max_field_impulse_fraction", ctypes.c_double), ("field_impulse_floor_eV", ctypes.c_double),
+        ("rng_seed", ctypes.c_uint64),
+        ("debug_disable_hard_moller", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+    ]
+
+
+class RreaGpuTile(ctypes.Structure):
+    """rrea_gpu_tile (include/rrea_gpu.h)."""
+
+    _fields_ = [("n", ctypes.c_int64)] + [
+        (name, _D) for name in ("r", "z", "theta", "ux", "uy", "uz", "w",
+                                "prev_r", "prev_z", "prev_theta", "prev_ux", "prev_uy", "prev_uz")
+    ] + [("id", ctypes.POINTER(ctypes.c_int64)), ("cpu", ctypes.POINTER(ctypes.c_int32))]
+
+
+TILE_FIELDS = ("r", "z", "theta", "ux", "uy", "uz", "w",
+               "prev_r", "prev_z", "prev_theta", "prev_ux", "prev_uy", "prev_uz")
+
+SECONDARY_DTYPE = np.dtype([
+    ("species", "<i4"), ("process", "<i4"), ("root_species", "<i4"), ("pad", "<i4"),
+    ("parent_index", "<i8"), ("root_key", "<u8"), ("lineage", "<u8"),
+    ("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("dir_x", "<f8"), ("dir_y", "<f8"), ("dir_z", "<f8"),
+    ("weight", "<f8"), ("energy_eV", "<f8"), ("birth_fraction", "<f8"),
+])
+
+# Every entry point include/rrea_gpu.h declares.
+EXPORTED_SYMBOLS = (
+    "rrea_gpu_default_config", "rrea_gpu_create", "rrea_gpu_destroy", "rrea_gpu_load_tables",
+    "rrea_gpu_set_field", "rrea_gpu_apply_electrons", "rrea_gpu_download_sources", "rrea_gpu_reset_sources",
+    "rrea_gpu_download_diagnostics", "rrea_gpu_last_error", "rrea_gpu_stage_electrons",
+    "rrea_gpu_step_electrons_resident", "rrea_gpu_fetch_electrons", "rrea_gpu_set_launch", "rrea_gpu_stream",
+    "rrea_gpu_last_step_stats",
+)
+
+_lib = None
+
+
+class RreaGpuError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"rrea_gpu status {status} ({STATUS_NAMES.get(status, '?')}): {message}")
+        self.status = status
+
+
+def load_library(path=LIB_PATH):
+    """Loads the in-tree CUDA library; raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run __graft_entry__.build() (no CPU fallback exists)")
+    lib = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    lib.rrea_gpu_default_config.argtypes = [ctypes.POINTER(RreaGpuConfig)]
+    lib.rrea_gpu_default_config.restype = None
+    lib.rrea_gpu_create.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_int64, ctypes.POINTER(vp)]
+    lib.rrea_gpu_destroy.argtypes = [vp]
+    lib.rrea_gpu_load_tables.argtypes = [vp, ctypes.c_char_p]
+    lib.rrea_gpu_set_field.argtypes = [vp, _D, _D, _D, _D, _D]
+    lib.rrea_gpu_apply_electrons.argtypes = [vp, ctypes.POINTER(RreaGpuTile), ctypes.c_int32, ctypes.c_double,
+                                             ctypes.c_double, vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    lib.rrea_gpu_download_sources.argtypes = [vp, _D]
+    lib.rrea_gpu_reset_sources.argtypes = [vp]
+    lib.rrea_gpu_download_diagnostics.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64),
+                                                  ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int32)]
+    lib.rrea_gpu_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    lib.rrea_gpu_last_error.restype = None
+    lib.rrea_gpu_stage_electrons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
+    lib.rrea_gpu_step_electrons_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_double,
+                                                     ctypes.POINTER(ctypes.c_int64)]
+    lib.rrea_gpu_fetch_electrons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
+    lib.rrea_gpu_set_launch.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+    lib.rrea_gpu_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    lib.rrea_gpu_last_step_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                             ctypes.POINTER(ctypes.c_double)]
+    for name in EXPORTED_SYMBOLS:
+        fn = getattr(lib, name)
+        if fn.restype is not None and name not in ("rrea_gpu_default_config", "rrea_gpu_last_error"):
+            fn.restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def default_config(**overrides):
+    cfg = RreaGpuConfig()
+    load_library().rrea_gpu_default_config(ctypes.byref(cfg))
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def tile_struct(arrays):
+    """Builds an rrea_gpu_tile over a dict of contiguous numpy arrays."""
+    t = RreaGpuTile()
+    t.n = int(arrays["id"].shape[0])
+    for name in TILE_FIELDS:
+        a = arrays[name]
+        assert a.dtype == np.float64 and a.flags.c_contiguous, name
+        setattr(t, name, a.ctypes.data_as(_D))
+    t.id = arrays["id"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    t.cpu = arrays["cpu"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    return t
+
+
+class RreaGpuContext:
+    """Owns one rrea_gpu_ctx (device arena, field, resident tile, buffers)."""
+
+    def __init__(self, config, capacity):
+        self.lib = load_library()
+        self.config = config
+        self.capacity = int(capacity)
+        handle = ctypes.c_void_p()
+        self._check(self.lib.rrea_gpu_create(ctypes.byref(config), self.capacity, ctypes.byref(handle)), None)
+        self.handle = handle
+
+    def _check(self, status, handle="self"):
+        if status != 0:
+            msg = ""
+            if handle is not None and getattr(self, "handle", None) is not None:
+                buf = ctypes.create_string_buffer(2048)
+                self.lib.rrea_gpu_last_error(self.handle, buf, 2048)
+                msg = buf.value.decode(errors="replace")
+            raise RreaGpuError(status, msg)
+
+    def close(self):
+        if getattr(self, "handle", None) is not None:
+            self.lib.rrea_gpu_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load_tables(self, path=DEFAULT_TABLES):
+        self._check(self.lib.rrea_gpu_load_tables(self.handle, path.encode()))
+
+    def set_field(self, er, ez, bt, amb_er, amb_ez):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (er, ez, bt, amb_er, amb_ez)]
+        self._check(self.lib.rrea_gpu_set_field(self.handle, *[a.ctypes.data_as(_D) for a in arrs]))
+
+    def set_launch(self, threads_per_block=128, blocks_per_sm=8, diagnostics=True):
+        self._check(self.lib.rrea_gpu_set_launch(self.handle, threads_per_block, blocks_per_sm, int(diagnostics)))
+
+    def apply_electrons(self, arrays, step, dt_s, time_s=0.0, want_secondaries=True):
+        """Drop-in electron phase on host arrays (modified in place).
+        Returns the ordered secondaries as a structured array."""
+        t = tile_struct(arrays)
+        n_sec = ctypes.c_int64()
+        cap = 2 * self.capacity + 4096
+        buf = np.zeros(cap if want_secondaries else 0, dtype=SECONDARY_DTYPE)
+        ptr = ctypes.c_void_p(buf.ctypes.data) if want_secondaries else None
+        self._check(self.lib.rrea_gpu_apply_electrons(self.handle, ctypes.byref(t), int(step), float(time_s),
+                                                      float(dt_s), ptr, cap, ctypes.byref(n_sec)))
+        return buf[: n_sec.value] if want_secondaries else n_sec.value
+
+    def stage_electrons(self, arrays):
+        self._check(self.lib.rrea_gpu_stage_electrons(self.handle, ctypes.byref(tile_struct(arrays))))
+
+    def step_electrons_resident(self, step, dt_s):
+        n_sec = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_step_electrons_resident(self.handle, int(step), float(dt_s),
+                                                              ctypes.byref(n_sec)))
+        return n_sec.value
+
+    def fetch_electrons(self, arrays):
+        self._check(self.lib.rrea_gpu_fetch_electrons(self.handle, ctypes.byref(tile_struct(arrays))))
+
+    def sources(self):
+        c = self.config
+        out = np.zeros(5 * c.nr * c.nz)
+        self._check(self.lib.rrea_gpu_download_sources(self.handle, out.ctypes.data_as(_D)))
+        return out.reshape(5, c.nz, c.nr)
+
+    def reset_sources(self):
+        self._check(self.lib.rrea_gpu_reset_sources(self.handle))
+
+    def diagnostics(self, n):
+        sub = np.zeros(n, dtype=np.uint64)
+        ev = np.zeros(n, dtype=np.uint64)
+        disp = np.zeros(n, dtype=np.int32)
+        self._check(self.lib.rrea_gpu_download_diagnostics(
+            self.handle, n, sub.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+            ev.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), disp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+        return sub, ev, disp
+
+    def last_step_stats(self):
+        """(particles transported, secondaries, transport-kernel ms) of the last step."""
+        t, s, ms = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+        self._check(self.lib.rrea_gpu_last_step_stats(self.handle, ctypes.byref(t), ctypes.byref(s), ctypes.byref(ms)))
+        return t.value, s.value, ms.value
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        self._check(self.lib.rrea_gpu_stream(self.handle, ctypes.byref(s)))
+        return s.value
+
+
+class RreaParticleInteraction:
+    """Host mirror of rrea::warpx::RreaParticleInteraction: construct with the
+    transport configuration, then Apply(tile, step, time_s, dt_s) once per
+    step.  Raises RreaGpuError where the reference calls amrex::Abort."""
+
+    def __init__(self, config, capacity, tables=DEFAULT_TABLES, field=None):
+        self.ctx = RreaGpuContext(config, capacity)
+        self.ctx.load_tables(tables)
+        if field is not None:
+            self.ctx.set_field(**field)
+
+    def SetField(self, er, ez, bt, amb_er, amb_ez):
+        self.ctx.set_field(er, ez, bt, amb_er, amb_ez)
+
+    def Apply(self, electrons, step, time_s, dt_s):
+        return self.ctx.apply_electrons(electrons, step, dt_s, time_s=time_s)

@@ -1,0 +1,62 @@
+"""CPU-side checks of the shipped library: it builds for sm_103a, loads
+without a GPU, and exports every entry point include/rrea_gpu.h declares.
+No compute call is made here."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from rrea_feedback_warpx_amrex_geant4_gb300 import build, gpu
+    build.build()
+    return gpu
+
+
+def declared_entry_points():
+    text = open(os.path.join(ROOT, "include", "rrea_gpu.h")).read()
+    return sorted(set(re.findall(r"\b(rrea_gpu_[a-z_]+)\s*\(", text)))
+
+
+def test_header_declares_expected_symbols(gpu):
+    assert set(declared_entry_points()) == set(gpu.EXPORTED_SYMBOLS)
+
+
+def test_library_exports_every_declared_symbol(gpu):
+    lib = ctypes.CDLL(gpu.LIB_PATH)
+    for name in declared_entry_points():
+        assert hasattr(lib, name), name
+
+
+def test_default_config_matches_reference_defaults(gpu):
+    cfg = gpu.default_config()
+    # RreaParticleInteractionConfig defaults (RreaParticleInteraction.H:1576-1596)
+    assert cfg.max_optical_depth_per_substep == 0.05
+    assert cfg.max_subcycles == 256
+    assert cfg.strict_transport_guards == 1
+    assert cfg.max_gs_collisions_per_substep == 32.0
+    assert cfg.gs_total_collision_cap == 1024.0
+    assert cfg.max_field_impulse_fraction == 0.1
+    assert cfg.field_impulse_floor_eV == 1.0e4
+    assert cfg.density_ratio == 1.0
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    from rrea_feedback_warpx_amrex_geant4_gb300 import gpu
+    with pytest.raises(RuntimeError):
+        gpu._lib_saved = gpu._lib
+        try:
+            gpu._lib = None
+            gpu.load_library(str(tmp_path / "absent.so"))
+        finally:
+            gpu._lib = gpu._lib_saved
+
+
+def test_structure_layouts_match_header(gpu):
+    from oracle import oracle as o
+    assert ctypes.sizeof(gpu.RreaGpuConfig) == ctypes.sizeof(o.RreaGpuConfig) == 136
+    assert gpu.SECONDARY_DTYPE.itemsize == 4 * 4 + 8 * 3 + 8 * 9

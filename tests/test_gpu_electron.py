@@ -1,0 +1,120 @@
+"""GPU electron phase vs the oracle on identical inputs (config-0 and
+config-1 shaped tiles), through the C-ABI drop-in entry point.
+
+Tolerances: dispositions, substep counts, hazard-draw counts, validity and
+secondary keys bit-exact; FP64 state within 1e-12 relative (positions with a
+1e-12 x domain floor); atomically accumulated cell sources within 1.6e-11 of
+each grid's largest cell."""
+import numpy as np
+import pytest
+
+from conftest import TABLES
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mods():
+    from rrea_feedback_warpx_amrex_geant4_gb300 import build, gpu, workloads
+    from oracle import compare, oracle
+    build.build()
+    oracle.load_tables(TABLES)
+    return gpu, workloads, oracle, compare
+
+
+def _ctx(gpu, workloads, case, n):
+    cfg = workloads.make_config(gpu, case)
+    ctx = gpu.RreaGpuContext(cfg, n)
+    ctx.load_tables(TABLES)
+    field = workloads.make_field(case)
+    ctx.set_field(**field)
+    return cfg, ctx, field
+
+
+@pytest.mark.parametrize("case,n,steps", [("uniform_c0", 512, 3), ("scaleup_c1", 2048, 2)])
+def test_electron_step_parity(mods, case, n, steps):
+    gpu, workloads, oracle, compare = mods
+    cfg, ctx, field = _ctx(gpu, workloads, case, n)
+    arr = workloads.make_electrons(case, n, seed=7)
+    scale = max(cfg.r_hi, cfg.z_hi)
+    for step in range(steps):
+        g, o = compare.run_pair(ctx, cfg, field, arr, step, 5.0e-10)
+        problems = compare.compare(cfg, g, o, scale)
+        assert not problems, f"step {step}: " + "; ".join(problems)
+        # next step starts from the oracle's state (no error accumulation)
+        arr = o[0]
+        workloads.capture_prev(arr)
+    ctx.close()
+
+
+def test_resident_mode_matches_apply_mode(mods):
+    gpu, workloads, oracle, compare = mods
+    cfg, ctx, field = _ctx(gpu, workloads, "scaleup_c1", 4096)
+    arr = workloads.make_electrons("scaleup_c1", 4096, seed=11)
+    a = workloads.copy_tile(arr)
+    n_apply = len(ctx.apply_electrons(a, 5, 5.0e-10))
+    b = workloads.copy_tile(arr)
+    ctx.stage_electrons(b)
+    n_res = ctx.step_electrons_resident(5, 5.0e-10)
+    ctx.fetch_electrons(b)
+    assert n_apply == n_res
+    for f in ("r", "z", "theta", "ux", "uy", "uz", "id"):
+        np.testing.assert_array_equal(a[f], b[f])
+    ctx.close()
+
+
+def test_zero_weight_and_invalid_particles(mods):
+    gpu, workloads, oracle, compare = mods
+    cfg, ctx, field = _ctx(gpu, workloads, "uniform_c0", 64)
+    arr = workloads.make_electrons("uniform_c0", 64, seed=3)
+    arr["w"][::4] = 0.0
+    arr["id"][1::8] *= -1
+    g, o = compare.run_pair(ctx, cfg, field, arr, 0, 5.0e-10)
+    assert not compare.compare(cfg, g, o, 500.0)
+    assert (g[4][::4][arr["id"][::4] > 0] == 3).all()
+    ctx.close()
+
+
+def test_below_cutoff_electrons_demote(mods):
+    gpu, workloads, oracle, compare = mods
+    cfg, ctx, field = _ctx(gpu, workloads, "uniform_c0", 32)
+    arr = workloads.make_electrons("uniform_c0", 32, seed=3)
+    k = np.full(32, 5.0e3)
+    u = workloads.proper_velocity(k)
+    for f in ("uz", "prev_uz"):
+        arr[f][:] = u
+    arr["z"][:] = arr["prev_z"][:] = 100.0
+    g, o = compare.run_pair(ctx, cfg, field, arr, 0, 5.0e-10)
+    assert not compare.compare(cfg, g, o, 500.0)
+    assert (g[4] == 2).all()
+    cells = g[5]
+    assert cells[0].sum() > 0.0  # low-energy electron sources were booked
+    ctx.close()
+
+
+def test_escape_through_upper_face(mods):
+    gpu, workloads, oracle, compare = mods
+    cfg, ctx, field = _ctx(gpu, workloads, "uniform_c0", 32)
+    arr = workloads.make_electrons("uniform_c0", 32, seed=3)
+    arr["z"][:] = arr["prev_z"][:] = 500.0 - 0.01
+    g, o = compare.run_pair(ctx, cfg, field, arr, 0, 5.0e-10)
+    assert not compare.compare(cfg, g, o, 500.0)
+    assert (g[4] == 1).all()
+    assert (g[0]["id"] < 0).all()
+    ctx.close()
+
+
+def test_out_of_domain_state_fails_closed(mods):
+    gpu, workloads, oracle, compare = mods
+    cfg, ctx, field = _ctx(gpu, workloads, "uniform_c0", 8)
+    arr = workloads.make_electrons("uniform_c0", 8, seed=3)
+    arr["prev_r"][3] = 60.0
+    with pytest.raises(gpu.RreaGpuError) as e:
+        ctx.apply_electrons(arr, 0, 5.0e-10)
+    assert e.value.status == 5
+    with pytest.raises(oracle.OracleFailure):
+        oracle.electron_step(cfg, field, 0, 5.0e-10, workloads.copy_tile(arr))
+    # the context stays usable after a failed step
+    ok = workloads.make_electrons("uniform_c0", 8, seed=4)
+    ctx.apply_electrons(ok, 0, 5.0e-10)
+    ctx.close()
