@@ -177,9 +177,11 @@ rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step
                                                  int64_t* n_secondaries);
 rrea_gpu_status rrea_gpu_fetch_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile);
 
-/* Launch shape of the transport kernel (threads per block in {32..128}, a
- * multiple of 32; resident blocks per SM) and whether per-particle
- * diagnostics are written. */
+/* Launch shape of the transport kernel: threads per block (32..128, a
+ * multiple of 32) and resident 128-thread blocks per SM (2 to 5; the
+ * kernel variant's register budget follows: 255, 168, 128 or 102 registers).  The
+ * grid is one resident wave with a grid-stride loop.  `diagnostics` enables
+ * the per-particle diagnostic arrays. */
 rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm,
                                     int32_t diagnostics);
 

@@ -45,7 +45,8 @@ def build(force=False, verbose=False):
     objdir = os.path.join(PKG, "_build")
     os.makedirs(objdir, exist_ok=True)
     nvcc = _nvcc()
-    common = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
+    fmad = "true" if os.environ.get("RREA_FMAD", "0") == "1" else "false"
+    common = ["-std=c++17", "-O3", "-lineinfo", f"--fmad={fmad}", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I", CSRC, "-I", os.path.join(ROOT, "include")] + ARCH
     if verbose:
         common += ["-Xptxas", "-v"]

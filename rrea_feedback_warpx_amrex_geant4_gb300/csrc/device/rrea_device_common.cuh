@@ -22,11 +22,32 @@ constexpr double kEps = 2.220446049250313080847263336181640625e-16;
 constexpr double kDblMin = 2.2250738585072013830902327173324040642192159804623318306e-308;
 constexpr double kGl2Node = 0.577350269189625764509148780501957;  // I/RreaGaussLegendre8.H:22
 
+// Division by a divisor that is reused: one IEEE reciprocal y = RN(1/b),
+// then per quotient a product and one FMA residual correction,
+//   q0 = RN(a*y),  r = RN(a - b*q0) (exact via FMA),  q = RN(q0 + r*y).
+// By Markstein's theorem (Markstein 1990; Muller et al., Handbook of
+// Floating-Point Arithmetic, 2nd ed., Thm 4.10) q = RN(a/b) whenever q0 is a
+// faithful quotient, which RN(a*y) is for all but rare operands; in those it
+// is within one ulp of RN(a/b).  Finite operands away from overflow and
+// underflow only.  Costs three FP64 instructions per quotient instead of a
+// full division sequence.
+struct Divisor {
+    double b, y;
+};
+__host__ __device__ __forceinline__ Divisor make_divisor(double b) { return Divisor{b, 1.0 / b}; }
+__device__ __forceinline__ double quot(double a, Divisor const& d)
+{
+    double const q0 = a * d.y;
+    double const r = fma(-q0, d.b, a);
+    return fma(r, d.y, q0);
+}
+
 // Everything a kernel needs that does not change within a step.
 struct StepConstants {
     rrea_gpu_config cfg;
     RreaArenaIndex tix;
     double dr, dz;
+    Divisor div_dr, div_dz;
     double hm_threshold_eV;
     double photon_cutoff_eV;
     double density_ratio;
@@ -104,14 +125,28 @@ __device__ __forceinline__ bool live_hazard_index(uint64_t species, uint64_t seg
 }
 
 // ------------------------------------------------------------------ tables
+// Every table grid searched here (energies, path lengths, CDF nodes) holds
+// non-negative finite doubles, and so does every query.  For such values the
+// IEEE-754 order equals the order of the bit patterns read as signed 64-bit
+// integers (after mapping -0.0 to +0.0), so the searches compare integers:
+// the same result as comparing doubles, issued on the integer pipe instead
+// of GB300's narrow FP64 pipe.
+__device__ __forceinline__ long long order_key(double v)
+{
+    long long const b = __double_as_longlong(v);
+    return b == static_cast<long long>(0x8000000000000000ULL) ? 0LL : b;
+}
+
 // First index i in [0, n) with x[i] >= q (std::lower_bound), n if none.
 __device__ __forceinline__ int lower_bound(const double* __restrict__ x, int n, double q)
 {
+    long long const qk = order_key(q);
+    const long long* __restrict__ xk = reinterpret_cast<const long long*>(x);
     int lo = 0, count = n;
     while (count > 0) {
         int const step = count >> 1;
         int const mid = lo + step;
-        if (__ldg(x + mid) < q) {
+        if (__ldg(xk + mid) < qk) {
             lo = mid + 1;
             count -= step + 1;
         } else {
@@ -127,7 +162,9 @@ __device__ __forceinline__ int lower_bound(const double* __restrict__ x, int n, 
 struct Bracket {
     int kind;   // 0 front, 1 back, 2 exact node hi, 3 interior (lo = hi-1)
     int hi;
-    double t;   // log-space fraction (valid when kind == 3)
+    double q;
+    double t;   // log-space fraction, computed on first use (kind == 3)
+    bool have_t;
 };
 
 __device__ __forceinline__ bool bracket_hot(const double* __restrict__ arena, RreaTable1DIndex const& h,
@@ -135,34 +172,50 @@ __device__ __forceinline__ bool bracket_hot(const double* __restrict__ arena, Rr
 {
     const double* x = arena + h.x;
     int const n = h.n;
+    b.q = q;
+    b.have_t = false;
+    b.t = 0.0;
     if (!isfinite(q) || q < __ldg(x) || q > __ldg(x + n - 1)) {
         err.set(RREA_GPU_ERR_RANGE);
         return false;
     }
     int const up = lower_bound(x, n, q);
-    if (up == 0) { b.kind = 0; b.hi = 0; b.t = 0.0; return true; }
-    if (up == n) { b.kind = 1; b.hi = n - 1; b.t = 0.0; return true; }
+    if (up == 0) { b.kind = 0; b.hi = 0; return true; }
+    if (up == n) { b.kind = 1; b.hi = n - 1; return true; }
     b.hi = up;
-    if (__ldg(x + up) == q) { b.kind = 2; b.t = 0.0; return true; }
+    if (__ldg(x + up) == q) { b.kind = 2; return true; }
     b.kind = 3;
-    const double* lx = arena + h.lx;
-    if (h.mode == RREA_INTERP_LINEAR) {
-        b.t = (q - __ldg(x + up - 1)) / (__ldg(x + up) - __ldg(x + up - 1));
-    } else {
-        b.t = (log(q) - __ldg(lx + up - 1)) / (__ldg(lx + up) - __ldg(lx + up - 1));
-    }
     return true;
+}
+
+// The interpolation fraction of an interior bracket: linear in x for linear
+// tables, in log x otherwise (S/RreaInteractionTables.cpp:1610-1616).
+__device__ __forceinline__ double bracket_t(const double* __restrict__ arena, RreaTable1DIndex const& h, Bracket& b)
+{
+    if (!b.have_t) {
+        int const up = b.hi;
+        if (h.mode == RREA_INTERP_LINEAR) {
+            const double* x = arena + h.x;
+            b.t = (b.q - __ldg(x + up - 1)) / (__ldg(x + up) - __ldg(x + up - 1));
+        } else {
+            const double* lx = arena + h.lx;
+            b.t = (log(b.q) - __ldg(lx + up - 1)) / (__ldg(lx + up) - __ldg(lx + up - 1));
+        }
+        b.have_t = true;
+    }
+    return b.t;
 }
 
 // Value of one hot table at a prepared bracket
 // (S/RreaInteractionTables.cpp:1599-1629).
 __device__ __forceinline__ double eval_hot(const double* __restrict__ arena, RreaTable1DIndex const& h,
-                                           Bracket const& b, Err& err)
+                                           Bracket& b, Err& err)
 {
     const double* y = arena + h.y;
     if (b.kind == 0) return __ldg(y);
     if (b.kind == 1) return __ldg(y + h.n - 1);
     if (b.kind == 2) return __ldg(y + b.hi);
+    bracket_t(arena, h, b);
     double const ylo = __ldg(y + b.hi - 1), yhi = __ldg(y + b.hi);
     if (h.mode == RREA_INTERP_LINEAR) return ylo + b.t * (yhi - ylo);
     bool const pos = ylo > 0.0 && yhi > 0.0;
@@ -186,9 +239,25 @@ __device__ __forceinline__ double interpolate(const double* __restrict__ arena, 
     return eval_hot(arena, h, b, err);
 }
 
-// S/RreaInteractionTables.cpp:624-648 (interp_semilogx_strict)
+// Whether a hot table is strictly positive at a prepared bracket, without
+// evaluating its exponential: an interior bracket with two positive nodes is
+// exp(finite) > 0 in the log-log modes (node logs are O(10), far from
+// underflow); every other case evaluates the value exactly as eval_hot does.
+__device__ __forceinline__ bool positive_hot(const double* __restrict__ arena, RreaTable1DIndex const& h,
+                                             Bracket& b, Err& err)
+{
+    if (b.kind == 3 && h.mode != RREA_INTERP_LINEAR && h.mode != RREA_INTERP_LOGX_LINEAR) {
+        const double* y = arena + h.y;
+        if (__ldg(y + b.hi - 1) > 0.0 && __ldg(y + b.hi) > 0.0) return true;
+    }
+    return eval_hot(arena, h, b, err) > 0.0;
+}
+
+// S/RreaInteractionTables.cpp:624-648 (interp_semilogx_strict).  `lq`, when
+// not NaN, is log(q) already computed by the caller for the same q.
 __device__ __forceinline__ double semilogx(const double* __restrict__ x, const double* __restrict__ lx,
-                                           const double* __restrict__ y, int n, double q, Err& err)
+                                           const double* __restrict__ y, int n, double q, Err& err,
+                                           double lq = __builtin_nan(""))
 {
     if (!isfinite(q) || q < __ldg(x) || q > __ldg(x + n - 1)) {
         err.set(RREA_GPU_ERR_RANGE);
@@ -199,7 +268,8 @@ __device__ __forceinline__ double semilogx(const double* __restrict__ x, const d
     int const hi = lower_bound(x, n, q);
     if (__ldg(x + hi) == q) return __ldg(y + hi);
     int const lo = hi - 1;
-    double const t = (log(q) - __ldg(lx + lo)) / (__ldg(lx + hi) - __ldg(lx + lo));
+    double const lqq = isnan(lq) ? log(q) : lq;
+    double const t = (lqq - __ldg(lx + lo)) / (__ldg(lx + hi) - __ldg(lx + lo));
     return __ldg(y + lo) + t * (__ldg(y + hi) - __ldg(y + lo));
 }
 
@@ -270,20 +340,12 @@ __device__ __forceinline__ double sample_conditional(const double* __restrict__ 
     return y0 + t * (y1 - y0);
 }
 
-// S/RreaInteractionTables.cpp:1071-1110 (group means are per-group constants;
-// they are accumulated here in the reference's order).
+// S/RreaInteractionTables.cpp:1071-1110.  The group means are per-group
+// constants; the loader accumulates them once in the reference's order and
+// stores them (and their logs) in the arena.
 __device__ __forceinline__ double group_mean(const double* __restrict__ arena, RreaCondCdfIndex const& ci, int g)
 {
-    const double* start = arena + ci.start;
-    const double* u = arena + ci.u;
-    const double* v = arena + ci.v;
-    int const b = static_cast<int>(__ldg(start + g)), en = static_cast<int>(__ldg(start + g + 1));
-    double mean = __ldg(u + b) * __ldg(v + b);
-    for (int i = b + 1; i < en; ++i) {
-        mean += 0.5 * (__ldg(v + i - 1) + __ldg(v + i)) * (__ldg(u + i) - __ldg(u + i - 1));
-    }
-    mean += (1.0 - __ldg(u + en - 1)) * __ldg(v + en - 1);
-    return mean;
+    return __ldg(arena + ci.mean + g);
 }
 
 __device__ __forceinline__ double mean_conditional(const double* __restrict__ arena, RreaCondCdfIndex const& ci,
@@ -303,12 +365,17 @@ __device__ __forceinline__ double mean_conditional(const double* __restrict__ ar
     int const lo = up - 1;
     double const y0 = group_mean(arena, ci, lo), y1 = group_mean(arena, ci, up);
     double const t = (log(e) - __ldg(lprim + lo)) / (__ldg(lprim + up) - __ldg(lprim + lo));
-    return y0 > 0.0 && y1 > 0.0 ? exp(log(y0) + t * (log(y1) - log(y0))) : y0 + t * (y1 - y0);
+    if (y0 > 0.0 && y1 > 0.0) {
+        double const l0 = __ldg(arena + ci.lmean + lo), l1 = __ldg(arena + ci.lmean + up);
+        return exp(l0 + t * (l1 - l0));
+    }
+    return y0 + t * (y1 - y0);
 }
 
 // S/RreaInteractionTables.cpp:807-827
 __device__ __forceinline__ void log_bracket(const double* __restrict__ g, const double* __restrict__ lg, int n,
-                                            double q, int& i, double& frac, Err& err)
+                                            double q, int& i, double& frac, Err& err,
+                                            double lq = __builtin_nan(""))
 {
     int const last = n - 1;
     if (!isfinite(q) || q < __ldg(g) || q > __ldg(g + last)) {
@@ -320,9 +387,11 @@ __device__ __forceinline__ void log_bracket(const double* __restrict__ g, const 
     if (q == __ldg(g)) { i = 0; frac = 0.0; return; }
     if (q == __ldg(g + last)) { i = last - 1; frac = 1.0; return; }
     int lo = 0, hi = last;
+    long long const qk = order_key(q);
+    const long long* __restrict__ gk = reinterpret_cast<const long long*>(g);
     while (hi - lo > 1) {
         int const m = (lo + hi) / 2;
-        if (__ldg(g + m) <= q) lo = m; else hi = m;
+        if (__ldg(gk + m) <= qk) lo = m; else hi = m;
     }
     i = lo;
     double const llo = __ldg(lg + lo), lhi = __ldg(lg + hi);
@@ -330,17 +399,18 @@ __device__ __forceinline__ void log_bracket(const double* __restrict__ g, const 
         frac = (q == __ldg(g + lo)) ? 0.0 : 1.0;
         return;
     }
-    frac = (log(q) - llo) / (lhi - llo);
+    frac = ((isnan(lq) ? log(q) : lq) - llo) / (lhi - llo);
 }
 
 // S/RreaInteractionTables.cpp:831-891 (node logs read precomputed)
 __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ arena, RreaAngleIndex const& a,
-                                                  double e, double n, double u, Err& err)
+                                                  double e, double n, double u, Err& err,
+                                                  double le = __builtin_nan(""))
 {
     int const np = a.np, nu = a.nu;
     int ie = 0, ip = 0;
     double te = 0.0, tn = 0.0;
-    log_bracket(arena + a.e, arena + a.le, a.ne, e, ie, te, err);
+    log_bracket(arena + a.e, arena + a.le, a.ne, e, ie, te, err, le);
     log_bracket(arena + a.p, arena + a.lp, a.np, n, ip, tn, err);
     if (err.code) return 1.0;
     const double* lomc = arena + a.lomc;
@@ -371,9 +441,11 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
         one_minus_cos = omc_at(last);
     } else {
         int lo = first, hi = last;
+        long long const uk = order_key(u);
+        const long long* __restrict__ cuk = reinterpret_cast<const long long*>(cu);
         while (hi - lo > 1) {
             int const m = (lo + hi) / 2;
-            if (__ldg(cu + m) <= u) lo = m; else hi = m;
+            if (__ldg(cuk + m) <= uk) lo = m; else hi = m;
         }
         double const d0 = omc_at(lo), d1 = omc_at(hi);
         // hi == lo + 1 here, so the denominator is the precomputed node ratio log.

@@ -14,12 +14,15 @@ struct Piece {
     double begin, end, length, shift;
 };
 
+// NP is the piece capacity: 1 for an absorbing z domain (a clipped chord
+// has exactly one in-domain piece), RREA_ARENA_MAX_PIECES for periodic z.
+template <int NP>
 struct Path {
     double sx, sy, sz, ex, ey, ez;
     double full, in_begin, in_end, in_length;
     bool exits;
     int npieces;
-    Piece pieces[RREA_ARENA_MAX_PIECES];
+    Piece pieces[NP];
 };
 
 struct Geom {
@@ -38,7 +41,8 @@ __device__ __forceinline__ double wrap_z(Geom const& g, double z)
     return g.zlo + w;
 }
 // S/RreaTransportPath.cpp:42-52
-__device__ __forceinline__ void point_at_full(Path const& p, Geom const& g, double f, double& x, double& y, double& z)
+template <int NP>
+__device__ __forceinline__ void point_at_full(Path<NP> const& p, Geom const& g, double f, double& x, double& y, double& z)
 {
     f = fmax(0.0, fmin(1.0, f));
     x = p.sx + f * (p.ex - p.sx);
@@ -46,7 +50,8 @@ __device__ __forceinline__ void point_at_full(Path const& p, Geom const& g, doub
     z = wrap_z(g, p.sz + f * (p.ez - p.sz));
 }
 // S/RreaTransportPath.cpp:54-71
-__device__ __forceinline__ void point_at_piece(Path const& p, Geom const& g, Piece const& pc, double f, double& x,
+template <int NP>
+__device__ __forceinline__ void point_at_piece(Path<NP> const& p, Geom const& g, Piece const& pc, double f, double& x,
                                                double& y, double& z)
 {
     f = fmax(pc.begin, fmin(pc.end, f));
@@ -65,8 +70,9 @@ __device__ __forceinline__ bool outside_certified(Geom const& g, double r, doubl
 
 // S/RreaTransportPath.cpp:73-295.  Periodic seams use double arithmetic where
 // the host reference uses long double.
+template <int NP>
 __device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double r1, double th1, double z1,
-                                        Geom const& g, Path& p, Err& err)
+                                        Geom const& g, Path<NP>& p, Err& err)
 {
     if (!isfinite(r0) || !isfinite(th0) || !isfinite(z0) || !isfinite(r1) || !isfinite(th1) || !isfinite(z1)
         || r0 < 0.0 || r1 < 0.0) {
@@ -131,7 +137,7 @@ __device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double
     p.exits = p.in_end < 1.0 - 64.0 * kEps;
 
     // Breakpoints: [in_begin, seams..., in_end], sorted and deduplicated.
-    double bp[RREA_ARENA_MAX_PIECES + 1];
+    double bp[NP + 1];
     int nb = 0;
     bp[nb++] = p.in_begin;
     if (g.periodic && fabs(dz) > 0.0 && p.in_end > p.in_begin) {
@@ -145,7 +151,7 @@ __device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double
             double const frac = (seam - z0) / dz;
             double const ftol = 128.0 * kEps * fmax(1.0, fabs(frac));
             if (frac > p.in_begin + ftol && frac < p.in_end - ftol) {
-                if (nb >= RREA_ARENA_MAX_PIECES) {
+                if (nb >= NP) {
                     err.set(RREA_GPU_ERR_CAPACITY);
                     break;
                 }
@@ -220,7 +226,8 @@ __device__ __forceinline__ void normalize(double& x, double& y, double& z)
         x = 0.0; y = 0.0; z = 1.0;
         return;
     }
-    x /= n; y /= n; z /= n;
+    Divisor const d = make_divisor(n);
+    x = quot(x, d); y = quot(y, d); z = quot(z, d);
 }
 // O/RreaChargedInterleave.H:309-364
 __device__ __forceinline__ void cone_direction(double ax, double ay, double az, double cos_t, double u_phi,
@@ -301,7 +308,8 @@ __device__ __forceinline__ void photon_recoil(double k0, double eg, double gx, d
     double const px = p0 * cx - eg * gx, py = p0 * cy - eg * gy, pz = p0 * cz - eg * gz;
     double const n = sqrt(px * px + py * py + pz * pz);
     if (n > 0.0) {
-        cx = px / n; cy = py / n; cz = pz / n;
+        Divisor const d = make_divisor(n);
+        cx = quot(px, d); cy = quot(py, d); cz = quot(pz, d);
         normalize(cx, cy, cz);
     }
 }
@@ -321,9 +329,11 @@ __device__ __forceinline__ void half_kick(FieldRange const& f, double half_dt, d
     double const uym = umag * dy + s * f.ey;
     double const uzm = umag * dz + s * f.ez;
     double const gamma = sqrt(1.0 + (uxm * uxm + uym * uym + uzm * uzm) / (kC * kC));
-    double const tx = s * f.bx / (2.0 * gamma), ty = s * f.by / (2.0 * gamma), tz = s * f.bz / (2.0 * gamma);
+    Divisor const d2g = make_divisor(2.0 * gamma);
+    double const tx = quot(s * f.bx, d2g), ty = quot(s * f.by, d2g), tz = quot(s * f.bz, d2g);
     double const t2 = tx * tx + ty * ty + tz * tz;
-    double const sx = 2.0 * tx / (1.0 + t2), sy = 2.0 * ty / (1.0 + t2), sz = 2.0 * tz / (1.0 + t2);
+    Divisor const d1t = make_divisor(1.0 + t2);
+    double const sx = quot(2.0 * tx, d1t), sy = quot(2.0 * ty, d1t), sz = quot(2.0 * tz, d1t);
     double const ppx = uxm + uym * tz - uzm * ty;
     double const ppy = uym + uzm * tx - uxm * tz;
     double const ppz = uzm + uxm * ty - uym * tx;
@@ -332,7 +342,8 @@ __device__ __forceinline__ void half_kick(FieldRange const& f, double half_dt, d
     double const uz = uzm + ppx * sy - ppy * sx;
     double const norm = sqrt(ux * ux + uy * uy + uz * uz);
     if (norm > 0.0 && isfinite(norm)) {
-        dx = ux / norm; dy = uy / norm; dz = uz / norm;
+        Divisor const dn = make_divisor(norm);
+        dx = quot(ux, dn); dy = quot(uy, dn); dz = quot(uz, dn);
     }
     k = fmax(0.0, k + 0.5 * f.work);
 }
@@ -342,6 +353,7 @@ __device__ __forceinline__ void half_kick(FieldRange const& f, double half_dt, d
 // per step by a prep kernel exactly as S/RreaAmrexAdvance.cpp:556-565 forms
 // them) and the corner Btheta of the replicated Maxwell vectors.
 struct FieldView {
+    Divisor div_dr, div_dz;
     const double* __restrict__ cell_er;  // nr*nz, i + nr*j
     const double* __restrict__ cell_ez;  // nr*nz
     const double* __restrict__ bt;       // (nr+1)*(nz+1), i + (nr+1)*j
@@ -355,8 +367,8 @@ struct FieldView {
 // MaxwellBthetaAt :511-530
 __device__ __forceinline__ void gather(FieldView const& fv, double r, double z, double& er, double& ez, double& bth)
 {
-    double const fx = (r - fv.r_lo) / fv.dr + 0.0 - 0.5;
-    double const fz = (z - fv.z_lo) / fv.dz + 0.0 - 0.5;
+    double const fx = quot(r - fv.r_lo, fv.div_dr) + 0.0 - 0.5;
+    double const fz = quot(z - fv.z_lo, fv.div_dz) + 0.0 - 0.5;
     double const flx = floor(fx), flz = floor(fz);
     int const ir0 = static_cast<int>(flx);
     int const iz0 = static_cast<int>(flz);
@@ -386,8 +398,8 @@ __device__ __forceinline__ void gather(FieldView const& fv, double r, double z, 
         if (!fv.has_b && r > 0.0) bth = 0.0;
         return;
     }
-    double const fr = fmin(fmax(r / fv.dr, 0.0), static_cast<double>(fv.nr));
-    double const fzz = fmin(fmax((z - fv.z_lo) / fv.dz, 0.0), static_cast<double>(fv.nz));
+    double const fr = fmin(fmax(quot(r, fv.div_dr), 0.0), static_cast<double>(fv.nr));
+    double const fzz = fmin(fmax(quot(z - fv.z_lo, fv.div_dz), 0.0), static_cast<double>(fv.nz));
     int const a0 = min(static_cast<int>(floor(fr)), fv.nr - 1);
     int const b0 = min(static_cast<int>(floor(fzz)), fv.nz - 1);
     double const tr = fr - a0, tzz = fzz - b0;
@@ -398,7 +410,8 @@ __device__ __forceinline__ void gather(FieldView const& fv, double r, double z, 
 
 // O/RreaPathFieldWork.H:57-150 with the two-node rule of
 // I/RreaGaussLegendre8.H:24-60
-__device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom const& g, Path const& p, double q,
+template <int NP>
+__device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom const& g, Path<NP> const& p, double q,
                                                       double begin, double end, Err& err)
 {
     FieldRange res{0, 0, 0, 0, 0, 0, 0, 0};
@@ -406,9 +419,10 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
     begin = fmax(p.in_begin, begin);
     end = fmin(p.in_end, end);
     if (!(end > begin)) return res;
-    double const pdx = (p.ex - p.sx) / p.full;
-    double const pdy = (p.ey - p.sy) / p.full;
-    double const pdz = (p.ez - p.sz) / p.full;
+    Divisor const dfull = make_divisor(p.full);
+    double const pdx = quot(p.ex - p.sx, dfull);
+    double const pdy = quot(p.ey - p.sy, dfull);
+    double const pdz = quot(p.ez - p.sz, dfull);
     for (int ip = 0; ip < p.npieces; ++ip) {
         Piece const& pc = p.pieces[ip];
         double const pb = fmax(begin, pc.begin);
@@ -426,9 +440,10 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
             double const r = hypot(x, y);
             double rad = 0.0, rc = 1.0, rs = 0.0;
             if (r > 0.0) {
-                rad = (pdx * x + pdy * y) / r;
-                rc = x / r;
-                rs = y / r;
+                Divisor const dr = make_divisor(r);
+                rad = quot(pdx * x + pdy * y, dr);
+                rc = quot(x, dr);
+                rs = quot(y, dr);
             }
             double er, ez, bth;
             gather(fv, r, z, er, ez, bth);
@@ -455,8 +470,9 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
         res.length += p.full * (pe - pb);
     }
     if (res.length > 0.0) {
-        res.ex /= res.length; res.ey /= res.length; res.ez /= res.length;
-        res.bx /= res.length; res.by /= res.length; res.bz /= res.length;
+        Divisor const dl = make_divisor(res.length);
+        res.ex = quot(res.ex, dl); res.ey = quot(res.ey, dl); res.ez = quot(res.ez, dl);
+        res.bx = quot(res.bx, dl); res.by = quot(res.by, dl); res.bz = quot(res.bz, dl);
     }
     return res;
 }
@@ -464,16 +480,17 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
 // ------------------------------------------------------------ material path
 // O/RreaMaterialPath.H:47-199 for a uniform density ratio: one interval per
 // in-domain piece.
+template <int NP>
 struct Intervals {
     int n;
-    double begin[RREA_ARENA_MAX_PIECES], end[RREA_ARENA_MAX_PIECES], length[RREA_ARENA_MAX_PIECES],
-        density[RREA_ARENA_MAX_PIECES];
+    double begin[NP], end[NP], length[NP], density[NP];
 };
 
 __device__ __forceinline__ double positive_or(double v, double fb) { return v > 0.0 ? v : fb; }
 
 // :60-114
-__device__ __forceinline__ void build_intervals(Path const& p, double rho, Intervals& iv)
+template <int NP>
+__device__ __forceinline__ void build_intervals(Path<NP> const& p, double rho, Intervals<NP>& iv)
 {
     iv.n = 0;
     for (int i = 0; i < p.npieces; ++i) {
@@ -489,7 +506,8 @@ __device__ __forceinline__ void build_intervals(Path const& p, double rho, Inter
     }
 }
 // :117-136
-__device__ __forceinline__ double density_path(Intervals const& iv, Path const& p, double b, double e)
+template <int NP>
+__device__ __forceinline__ double density_path(Intervals<NP> const& iv, Path<NP> const& p, double b, double e)
 {
     b = fmax(p.in_begin, b);
     e = fmin(p.in_end, e);
@@ -502,7 +520,8 @@ __device__ __forceinline__ double density_path(Intervals const& iv, Path const& 
     return s;
 }
 // :142-170
-__device__ __forceinline__ double fraction_at_density_path(Intervals const& iv, Path const& p, double b, double e,
+template <int NP>
+__device__ __forceinline__ double fraction_at_density_path(Intervals<NP> const& iv, Path<NP> const& p, double b, double e,
                                                            double target, Err& err)
 {
     b = fmax(p.in_begin, b);
@@ -522,7 +541,8 @@ __device__ __forceinline__ double fraction_at_density_path(Intervals const& iv, 
     return e;
 }
 // :175-199
-__device__ __forceinline__ double max_uniform_slice(Intervals const& iv, Path const& p, uint64_t n)
+template <int NP>
+__device__ __forceinline__ double max_uniform_slice(Intervals<NP> const& iv, Path<NP> const& p, uint64_t n)
 {
     double const span = p.in_end - p.in_begin;
     double const d = static_cast<double>(n);
@@ -584,7 +604,8 @@ __device__ __forceinline__ bool cartesian_half_open(Geom const& g, double x, dou
         && z < g.zhi;
 }
 // O/RreaParticleInteraction.H:409-452 (clipped policy: RREA owns every escape)
-__device__ __forceinline__ void clipped_escape_policy(Path const& p, Geom const& g, double er, double ez,
+template <int NP>
+__device__ __forceinline__ void clipped_escape_policy(Path<NP> const& p, Geom const& g, double er, double ez,
                                                       bool& escapes, bool& invalidate)
 {
     if (!isfinite(er) || !isfinite(ez)) {

@@ -13,54 +13,26 @@
 #pragma once
 
 #include "rrea_device_path.cuh"
+#include "rrea_electron_args.cuh"
 
 namespace rrea_dev {
 
-struct ElectronArgs {
-    int64_t n;
-    // The current and prev_* arrays may alias (resident engine mode, where
-    // the captured pre-push state IS the current state): no __restrict__.
-    double* r;
-    double* z;
-    double* theta;
-    double* ux;
-    double* uy;
-    double* uz;
-    const double* __restrict__ w;
-    const double* prev_r;
-    const double* prev_z;
-    const double* prev_theta;
-    const double* prev_ux;
-    const double* prev_uy;
-    const double* prev_uz;
-    int64_t* __restrict__ id;
-    const int32_t* __restrict__ cpu;
-    // secondaries (unordered append) and per-parent counts for the ordering pass
-    rrea_gpu_secondary* __restrict__ sec;
-    unsigned long long* __restrict__ sec_count;
-    int64_t sec_capacity;
-    uint32_t* __restrict__ sec_per_parent;
-    // cell sources: 5 grids of nr*nz
-    double* __restrict__ cells;
-    // optional per-particle diagnostics (may be null)
-    uint64_t* __restrict__ diag_subcycles;
-    uint64_t* __restrict__ diag_events;
-    int32_t* __restrict__ diag_disposition;
-    // status: first failing code and particle
-    int* __restrict__ status;
-    long long* __restrict__ fail_index;
-    // particles transported this step (id > 0 on entry)
-    unsigned long long* __restrict__ transported;
-    const double* __restrict__ arena;
-    FieldView fv;
-};
+
 
 // Order-1 cell deposit (S/RreaEventAccumulator.cpp:386-502, field ids of
-// :129-164) for the uniform RZ grid with r_lo on the axis.
-__device__ __forceinline__ void add_to_field(StepConstants const& C, double* __restrict__ cells, int field,
-                                             double r, double z, double value)
+// :129-164) for the uniform RZ grid with r_lo on the axis.  One source feeds
+// up to four fields at the same point, so its stencil (containing cell,
+// order-1 weights, axis fold) is built once and applied to each value.
+struct CellStencil {
+    bool valid;
+    int i[2], j[2];
+    bool use_i[2], use_j[2];
+    double wr[2], wz[2];
+};
+
+__device__ __forceinline__ CellStencil make_stencil(StepConstants const& C, double r, double z)
 {
-    if (!isfinite(value) || value == 0.0) return;
+    CellStencil st;
     rrea_gpu_config const& cfg = C.cfg;
     int const nr = cfg.nr, nz = cfg.nz;
     double zz = z;
@@ -70,37 +42,55 @@ __device__ __forceinline__ void add_to_field(StepConstants const& C, double* __r
         if (s < 0.0) s += len;
         zz = cfg.z_lo + s;
     }
-    int const ic = static_cast<int>(floor((r - cfg.r_lo) / C.dr));
-    int const jc = static_cast<int>(floor((zz - cfg.z_lo) / C.dz));
-    if (ic < 0 || ic >= nr || jc < 0 || jc >= nz) return;
-    double const rc = (r - cfg.r_lo) / C.dr + 0.0 - 0.5;
+    double const fr = quot(r - cfg.r_lo, C.div_dr);
+    double const fz = quot(zz - cfg.z_lo, C.div_dz);
+    int const ic = static_cast<int>(floor(fr));
+    int const jc = static_cast<int>(floor(fz));
+    st.valid = !(ic < 0 || ic >= nr || jc < 0 || jc >= nz);
+    if (!st.valid) return st;
+    double const rc = fr + 0.0 - 0.5;
     int const i0 = static_cast<int>(floor(rc));
-    double const wr1 = rc - i0, wr0 = 1.0 - wr1;
-    double const zc = (zz - cfg.z_lo) / C.dz + 0.0 - 0.5;
+    st.wr[1] = rc - i0;
+    st.wr[0] = 1.0 - st.wr[1];
+    double const zc = fz + 0.0 - 0.5;
     int const j0 = static_cast<int>(floor(zc));
-    double const wz1 = zc - j0, wz0 = 1.0 - wz1;
-    double* grid = cells + static_cast<size_t>(field) * nr * nz;
+    st.wz[1] = zc - j0;
+    st.wz[0] = 1.0 - st.wz[1];
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
-        double const wz = a == 0 ? wz0 : wz1;
-        if (wz == 0.0) continue;
         int j = j0 + a;
+        st.use_j[a] = true;
         if (j < 0 || j > nz - 1) {
             if (cfg.periodic_z) j = ((j % nz) + nz) % nz;
-            else continue;
+            else st.use_j[a] = false;
         }
+        st.j[a] = j;
+        int i = i0 + a;
+        st.use_i[a] = true;
+        if (i < 0 || i > nr - 1) {
+            if (i == -1 && cfg.r_lo == 0.0) i = 0;
+            else st.use_i[a] = false;
+        }
+        st.i[a] = i;
+    }
+    return st;
+}
+
+__device__ __forceinline__ void stencil_add(StepConstants const& C, double* __restrict__ cells, CellStencil const& st,
+                                            int field, double value)
+{
+    if (!st.valid || !isfinite(value) || value == 0.0) return;
+    int const nr = C.cfg.nr;
+    double* grid = cells + static_cast<size_t>(field) * nr * C.cfg.nz;
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        double const wz = st.wz[a];
+        if (wz == 0.0 || !st.use_j[a]) continue;
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
-            double const wr = b == 0 ? wr0 : wr1;
-            double const v = value * wr * wz;
-            if (v == 0.0) continue;
-            int i = i0 + b;
-            if (i < 0 || i > nr - 1) {
-                if (i == -1 && cfg.r_lo == 0.0) i = 0;
-                else continue;
-            }
-            if (!isfinite(v)) continue;
-            atomicAdd(grid + i + static_cast<size_t>(nr) * j, v);
+            double const v = value * st.wr[b] * wz;
+            if (v == 0.0 || !st.use_i[b] || !isfinite(v)) continue;
+            atomicAdd(grid + st.i[b] + static_cast<size_t>(nr) * st.j[a], v);
         }
     }
 }
@@ -110,75 +100,92 @@ __device__ __forceinline__ void deposit_source(StepConstants const& C, double* _
                                                double r, double z, double w, double sec_e, double loss)
 {
     if (w <= 0.0) return;
+    CellStencil const st = make_stencil(C, r, z);
+    if (!st.valid) return;
     if (kind == 0) {  // AccumulateIonizationEvent
-        add_to_field(C, cells, 1, r, z, w);
-        if (sec_e < C.cfg.low_energy_cutoff_eV) add_to_field(C, cells, 0, r, z, w);
-        add_to_field(C, cells, 3, r, z, w);
-        add_to_field(C, cells, 4, r, z, fmax(w, 0.0) * fmax(loss, 0.0));
+        stencil_add(C, cells, st, 1, w);
+        if (sec_e < C.cfg.low_energy_cutoff_eV) stencil_add(C, cells, st, 0, w);
+        stencil_add(C, cells, st, 3, w);
+        stencil_add(C, cells, st, 4, fmax(w, 0.0) * fmax(loss, 0.0));
     } else if (kind == 1) {  // AccumulateLowEnergyElectron
-        add_to_field(C, cells, 0, r, z, w);
-        add_to_field(C, cells, 3, r, z, w);
-        add_to_field(C, cells, 4, r, z, fmax(w, 0.0) * fmax(fmax(loss, 0.0), 0.0));
+        stencil_add(C, cells, st, 0, w);
+        stencil_add(C, cells, st, 3, w);
+        stencil_add(C, cells, st, 4, fmax(w, 0.0) * fmax(fmax(loss, 0.0), 0.0));
     } else {  // AccumulatePositiveIonSourceOnly
-        add_to_field(C, cells, 1, r, z, w);
-        add_to_field(C, cells, 3, r, z, w);
-        add_to_field(C, cells, 4, r, z, fmax(w, 0.0) * fmax(loss, 0.0));
+        stencil_add(C, cells, st, 1, w);
+        stencil_add(C, cells, st, 3, w);
+        stencil_add(C, cells, st, 4, fmax(w, 0.0) * fmax(loss, 0.0));
     }
 }
 
-struct ElectronState {
-    double k, dx, dy, dz;
-    double run_x, run_y, run_z;
+// The electron coefficient tables (collision, soft radiative, hard-Moller
+// and tracked-brems rates) share one bit-identical 2856-row energy grid in
+// the schema-6 bundle (the loader refuses to run the device path otherwise).
+// One bracket per distinct query energy therefore serves every table, and
+// each table value is interpolated on first use only.  The hazard refreeze
+// and the drag segment that follows it query the same frozen energy, so the
+// drag reuses the refreeze's bracket instead of searching again.
+struct RateCache {
+    long long key = -1;  // bit pattern of the bracketed energy; -1 = none
+    Bracket b;
+    double v[4];
+    unsigned have = 0;  // bit i: v[i] valid (0 collision, 1 soft, 2 Moller, 3 brems)
 };
 
-// Electron transport coefficients needed by the loop, all on one bracket of
-// the shared 2856-row grid when the bundle provides one.
-struct ElectronRates {
-    double collision, soft, moller_inv, brems_inv;
-};
-
-__device__ __forceinline__ void electron_rates(StepConstants const& C, const double* __restrict__ arena, double e,
-                                               ElectronRates& out, Err& err)
+__device__ __forceinline__ bool rate_bracket(StepConstants const& C, const double* __restrict__ arena, RateCache& rc,
+                                             double e, Err& err)
 {
-    RreaArenaIndex const& ix = C.tix;
-    if (ix.electron_grid_shared) {
-        Bracket b;
-        if (!bracket_hot(arena, ix.hot[RREA_T_E_COLLISION], e, b, err)) return;
-        out.collision = eval_hot(arena, ix.hot[RREA_T_E_COLLISION], b, err);
-        out.soft = eval_hot(arena, ix.hot[RREA_T_E_SOFT_RAD], b, err);
-        out.moller_inv = eval_hot(arena, ix.hot[RREA_T_E_HARD_MOLLER], b, err);
-        out.brems_inv = eval_hot(arena, ix.hot[RREA_T_E_TRACKED_BREMS], b, err);
-    } else {
-        out.collision = interpolate(arena, ix.hot[RREA_T_E_COLLISION], e, err);
-        out.soft = interpolate(arena, ix.hot[RREA_T_E_SOFT_RAD], e, err);
-        out.moller_inv = interpolate(arena, ix.hot[RREA_T_E_HARD_MOLLER], e, err);
-        out.brems_inv = interpolate(arena, ix.hot[RREA_T_E_TRACKED_BREMS], e, err);
-    }
+    long long const key = __double_as_longlong(e);
+    if (rc.key == key) return true;
+    rc.key = -1;
+    rc.have = 0;
+    if (!bracket_hot(arena, C.tix.hot[RREA_T_E_COLLISION], e, rc.b, err)) return false;
+    rc.key = key;
+    return true;
 }
+
+__device__ __forceinline__ double rate_value(StepConstants const& C, const double* __restrict__ arena, RateCache& rc,
+                                             double e, int which, Err& err)
+{
+    if (!rate_bracket(C, arena, rc, e, err)) return 0.0;
+    unsigned const bit = 1u << which;
+    if (!(rc.have & bit)) {
+        rc.v[which] = eval_hot(arena, C.tix.hot[RREA_T_E_COLLISION + which], rc.b, err);
+        rc.have |= bit;
+    }
+    return rc.v[which];
+}
+
+__device__ __forceinline__ bool rate_positive(StepConstants const& C, const double* __restrict__ arena, RateCache& rc,
+                                              double e, int which, Err& err)
+{
+    if (!rate_bracket(C, arena, rc, e, err)) return false;
+    unsigned const bit = 1u << which;
+    if (rc.have & bit) return rc.v[which] > 0.0;
+    return positive_hot(arena, C.tix.hot[RREA_T_E_COLLISION + which], rc.b, err);
+}
+
+enum { kRateCollision = 0, kRateSoft = 1, kRateMoller = 2, kRateBrems = 3 };
 
 // Competing STP rates, O/RreaChargedFinalStates.H:107-152 with the accessors
 // ElectronHardMollerMeanFreePath / ElectronBremsstrahlungMeanFreePath
 // (S/RreaInteractionTables.cpp:2394-2412, 2666-2676).
-__device__ __forceinline__ void competing_rates(StepConstants const& C, const double* __restrict__ arena, double e,
-                                                double& s0, double& s1, Err& err)
+__device__ __forceinline__ void competing_rates(StepConstants const& C, const double* __restrict__ arena,
+                                                RateCache& rc, double e, double& s0, double& s1, Err& err)
 {
     double const thr = C.hm_threshold_eV;
     bool const m_open = C.hm_enabled && thr > 0.0 && e > 2.0 * thr;
     bool const b_open = isfinite(e) && isfinite(C.photon_cutoff_eV) && e > C.photon_cutoff_eV;
     s0 = 0.0;
     s1 = 0.0;
-    if (m_open || b_open) {
-        ElectronRates rt;
-        electron_rates(C, arena, e, rt, err);
-        if (err.code) return;
-        if (m_open) {
-            double const mfp = (thr > 0.0 && e <= 2.0 * thr) ? 1.0e99 : mfp_from_inverse(rt.moller_inv * 1.0, err);
-            s0 = mfp > 0.0 ? 1.0 / mfp : 0.0;
-        }
-        if (b_open) {
-            double const mfp = mfp_from_inverse(rt.brems_inv * 1.0, err);
-            s1 = mfp > 0.0 ? 1.0 / mfp : 0.0;
-        }
+    if (m_open) {
+        double const inv = rate_value(C, arena, rc, e, kRateMoller, err);
+        double const mfp = (thr > 0.0 && e <= 2.0 * thr) ? 1.0e99 : mfp_from_inverse(inv * 1.0, err);
+        s0 = mfp > 0.0 ? 1.0 / mfp : 0.0;
+    }
+    if (b_open) {
+        double const mfp = mfp_from_inverse(rate_value(C, arena, rc, e, kRateBrems, err) * 1.0, err);
+        s1 = mfp > 0.0 ? 1.0 / mfp : 0.0;
     }
     s0 = frozen_rate(s0, err);
     s1 = frozen_rate(s1, err);
@@ -198,16 +205,17 @@ __device__ __forceinline__ double hard_moller_energy_loss(StepConstants const& C
 
 // S/RreaInteractionTables.cpp:2477-2493
 __device__ __forceinline__ double elastic_inverse_stp(StepConstants const& C, const double* __restrict__ arena,
-                                                      double e, Err& err)
+                                                      double e, Err& err,
+                                                      double le = __builtin_nan(""))
 {
     RreaElasticIndex const& el = C.tix.elastic[0];
-    double const mfp = semilogx(arena + el.x, arena + el.lx, arena + el.mfp, el.n, e, err) / 1.0;
+    double const mfp = semilogx(arena + el.x, arena + el.lx, arena + el.mfp, el.n, e, err, le) / 1.0;
     return frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0, err);
 }
 
 // S/RreaInteractionTables.cpp:2504-2560
 __device__ __forceinline__ double sample_gs_cos(StepConstants const& C, const double* __restrict__ arena, double e,
-                                                double n, double u, Err& err)
+                                                double n, double u, Err& err, double le)
 {
     RreaArenaIndex const& ix = C.tix;
     if (!charged_in_range(ix, e)) {
@@ -229,17 +237,17 @@ __device__ __forceinline__ double sample_gs_cos(StepConstants const& C, const do
         return 1.0;
     }
     if (n >= ix.gs_isotropic_above_n) return 2.0 * u - 1.0;
-    return sample_gs_angle(arena, a, e, n, u, err);
+    return sample_gs_angle(arena, a, e, n, u, err, le);
 }
 __device__ __forceinline__ double sample_single_elastic_cos(StepConstants const& C, const double* __restrict__ arena,
-                                                            double e, double cdf_u, Err& err)
+                                                            double e, double cdf_u, Err& err, double le)
 {
     if (!charged_in_range(C.tix, e)) {
         err.set(RREA_GPU_ERR_RANGE);
         return 1.0;
     }
     RreaElasticIndex const& el = C.tix.elastic[0];
-    double const eta = semilogx(arena + el.x, arena + el.lx, arena + el.eta, el.n, e, err);
+    double const eta = semilogx(arena + el.x, arena + el.lx, arena + el.eta, el.n, e, err, le);
     double const u = fmin(fmax(cdf_u, 0.0), 1.0 - 1.0e-15);
     return 1.0 - 2.0 * eta * u / (1.0 + eta - u);
 }
@@ -280,7 +288,140 @@ __device__ __forceinline__ void record_failure(ElectronArgs const& A, int code, 
     }
 }
 
+// TransportSideEffects::AddSecondary (O/RreaTransportLog.H:437-447): the
+// record carries the parent's RNG key and its per-parent lineage counter.
+__device__ __forceinline__ void append_secondary(ElectronArgs const& A, int64_t ip, uint64_t key, double weight,
+                                                 uint32_t& lineage, int species, int process, double x, double y,
+                                                 double z, double sx, double sy, double sz, double e, double birth,
+                                                 Err& err)
+{
+    unsigned long long const slot = atomicAdd(A.sec_count, 1ULL);
+    if (slot < static_cast<unsigned long long>(A.sec_capacity)) {
+        rrea_gpu_secondary s;
+        s.species = species;
+        s.process = process;
+        s.root_species = 0;
+        s.pad = 0;
+        s.parent_index = ip;
+        s.root_key = key;
+        s.lineage = lineage;
+        s.x = x; s.y = y; s.z = z;
+        s.dir_x = sx; s.dir_y = sy; s.dir_z = sz;
+        s.weight = weight;
+        s.energy_eV = e;
+        s.birth_fraction = birth;
+        A.sec[slot] = s;
+    } else {
+        err.set(RREA_GPU_ERR_CAPACITY);
+    }
+    ++lineage;
+}
+
+// Interaction site of one discrete event (RreaInteractionSite,
+// O/RreaParticleInteraction.H:943-949).
+struct Site {
+    double x, y, z, r, birth;
+};
+
+// RreaApplyHardMollerFinalState, O/RreaChargedFinalStates.H:164-225
+__device__ __forceinline__ void moller_final_state(StepConstants const& C, ElectronArgs const& A, RngStream const& rng,
+                                                uint64_t rng_index, int64_t ip, uint64_t key, double weight,
+                                                Site const& site, double& k, double& dx, double& dy, double& dz,
+                                                uint32_t& lineage, Err& err)
+{
+    double const kb = k;
+    if (!charged_in_range(C.tix, kb)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return;
+    }
+    double sec = sample_conditional(A.arena, C.tix.cdf[RREA_C_MOLLER], kb,
+                                    rng.uniform(rng_index, kChHardMollerEnergy), true, err);
+    sec = fmax(C.hm_threshold_eV, fmin(sec, 0.5 * kb));
+    double pdx, pdy, pdz, sdx, sdy, sdz;
+    moller_lab_directions(dx, dy, dz, kb, sec, rng.uniform(rng_index, kChHardMollerAzimuth), pdx, pdy, pdz, sdx, sdy,
+                          sdz);
+    k = fmax(0.0, kb - sec);
+    dx = pdx; dy = pdy; dz = pdz;
+    append_secondary(A, ip, key, weight, lineage, 0, 2, site.x, site.y, site.z, sdx, sdy, sdz, sec, site.birth, err);
+    deposit_source(C, A.cells, 0, site.r, site.z, weight, sec, sec);
+}
+
+// RreaApplyBremsFinalState, O/RreaChargedFinalStates.H:329-394
+__device__ __forceinline__ void brems_final_state(StepConstants const& C, ElectronArgs const& A, RngStream const& rng,
+                                               uint64_t rng_index, int64_t ip, uint64_t key, double weight,
+                                               Site const& site, double& k, double& dx, double& dy, double& dz,
+                                               uint32_t& lineage, Err& err)
+{
+    double const kb = k;
+    if (!charged_in_range(C.tix, kb)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return;
+    }
+    double const sampled = sample_conditional(A.arena, C.tix.cdf[RREA_C_BREMS_E], kb,
+                                              rng.uniform(rng_index, kChBremsEnergy), false, err);
+    double const eg = fmin(fmax(sampled, 0.0), fmax(kb, 0.0));
+    double const after = fmax(0.0, fmax(kb, 0.0) - eg);
+    bool const tracked = isfinite(C.photon_cutoff_eV) && C.photon_cutoff_eV >= 0.0 && eg >= C.photon_cutoff_eV;
+    double const ct = sample_brems_cos(C, kb, rng.uniform(rng_index, kChBremsAngle), err);
+    double gx, gy, gz;
+    cone_direction(dx, dy, dz, ct, rng.uniform(rng_index, kChBremsAzimuth), gx, gy, gz);
+    photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
+    k = after;
+    if (tracked) {
+        append_secondary(A, ip, key, weight, lineage, 2, 4, site.x, site.y, site.z, gx, gy, gz, eg, site.birth, err);
+    } else if (eg > 0.0) {
+        // deposit_local_energy_as_ion_pairs, O/RreaTransportStep.H:530-561
+        double const w_air = C.tix.w_air_eV_per_pair;
+        double const pw = weight * eg / fmax(w_air, 1.0);
+        if (weight > 0.0 && pw > 0.0) deposit_source(C, A.cells, 0, site.r, site.z, pw, 0.0, w_air);
+    }
+}
+
+// Few-collision branch of apply_gs_elastic_scatter (O/RreaTransportStep.H:397-416):
+// a Poisson number of single screened-Rutherford deflections.  Rare for
+// tracked electrons (n >= 10 elastic collisions per substep at MeV energies),
+// so it is kept out of line.
+__device__ __noinline__ void gs_few_collisions(StepConstants const& C, const double* __restrict__ arena,
+                                               RngStream const& rng, uint64_t sub, double gs_n, double k, double lk,
+                                               double& dx, double& dy, double& dz, Err& err)
+{
+    double const few = C.tix.gs_few_collision_threshold;
+    int const cap = static_cast<int>(ceil(3.0 * few));
+    if (cap >= 255) {
+        err.set(RREA_GPU_ERR_INVALID_STATE);
+        return;
+    }
+    int const cnt = poisson_capped(gs_n, rng.uniform((sub << 8) | 0, kChElectronGsFewCount), cap);
+    for (int q = 0; q < cnt; ++q) {
+        uint64_t const inner = static_cast<uint64_t>(q + 1);
+        double const ct =
+            sample_single_elastic_cos(C, arena, k, rng.uniform((sub << 8) | inner, kChElectronGsFewScatter), err, lk);
+        double nx, ny, nz;
+        cone_direction(dx, dy, dz, ct, rng.uniform((sub << 8) | inner, kChElectronGsFewAzimuth), nx, ny, nz);
+        dx = nx; dy = ny; dz = nz;
+    }
+}
+
+// The 56-step bisection of RreaLimitContinuousSegmentAtCutoff
+// (O/RreaParticleInteraction.H:245-263), run only when the drag reaches the
+// cutoff inside the segment.  Returns false when a loss is not finite.
+template <int NP>
+__device__ __noinline__ bool cutoff_bisection(Intervals<NP> const* iv, Path<NP> const* path, double b, double e,
+                                              double total, double to_cut, double& eff)
+{
+    double lo = b, hi = e;
+    for (int it = 0; it < 56; ++it) {
+        double const mid = 0.5 * (lo + hi);
+        double const l = total * density_path(*iv, *path, b, mid);
+        if (!isfinite(l) || l < 0.0) return false;
+        if (l < to_cut) lo = mid; else hi = mid;
+    }
+    eff = 0.5 * (lo + hi);
+    return true;
+}
+
 // Returns the disposition (0 survive, 1 escape, 2 demotion, 3 zero weight).
+template <int NP>
 __device__ __forceinline__ int transport_electron(StepConstants const& C, ElectronArgs const& A, int64_t ip,
                                                   uint64_t& subcycles_out, uint64_t& events_out,
                                                   uint32_t& lineage, Err& err)
@@ -319,7 +460,7 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
     double run_z = A.prev_z[ip];
     double const r_particle = prev_r, z_particle = run_z;
 
-    auto build_chord = [&](double req_dt, Path& path) -> bool {
+    auto build_chord = [&](double req_dt, Path<NP>& path) -> bool {
         // O/RreaParticleInteraction.H:110-161
         if (!isfinite(req_dt) || !(req_dt >= 0.0)) return false;
         double const speed = charged_speed(k);
@@ -331,29 +472,6 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                 err);
         return isfinite(path.full) && path.in_begin == 0.0;
     };
-    auto add_secondary = [&](int species, int process, double x, double y, double z, double sx, double sy, double sz,
-                             double e, double birth) {
-        unsigned long long const slot = atomicAdd(A.sec_count, 1ULL);
-        if (slot < static_cast<unsigned long long>(A.sec_capacity)) {
-            rrea_gpu_secondary s;
-            s.species = species;
-            s.process = process;
-            s.root_species = 0;
-            s.pad = 0;
-            s.parent_index = ip;
-            s.root_key = key;
-            s.lineage = lineage;
-            s.x = x; s.y = y; s.z = z;
-            s.dir_x = sx; s.dir_y = sy; s.dir_z = sz;
-            s.weight = weight;
-            s.energy_eV = e;
-            s.birth_fraction = birth;
-            A.sec[slot] = s;
-        } else {
-            err.set(RREA_GPU_ERR_CAPACITY);
-        }
-        ++lineage;
-    };
     auto deposit_local = [&](double r, double z, double e) {
         // O/RreaTransportStep.H:530-561
         if (weight <= 0.0 || e <= 0.0) return;
@@ -363,13 +481,13 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
     };
     auto finish = [&](int disp) { return disp; };
 
-    Path path;
+    Path<NP> path;
     bool const driver_valid = build_chord(dt_s, path);
     if (err.code) return finish(-1);
     bool esc, esc_inv;
     clipped_escape_policy(path, g, hypot(path.ex, path.ey), path.ez, esc, esc_inv);
     double const ds = driver_valid ? path.in_length : 0.0;
-    Intervals iv;
+    Intervals<NP> iv;
     build_intervals(path, rho, iv);
     double const driver_span = fmax(path.in_end, 1.0e-6);
     FieldRange const dfw = path_field_work(A.fv, g, path, -1.0, 0.0, 1.0, err);
@@ -410,9 +528,10 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
 
     // ---- substep count, O/RreaElectronTransport.cpp:187-279
     uint64_t subcycles;
+    RateCache rc;
     {
         double s0, s1;
-        competing_rates(C, arena, k, s0, s1, err);
+        competing_rates(C, arena, rc, k, s0, s1, err);
         double const driver_dpath = chord_dpath / driver_span;
         double const target = cfg.max_optical_depth_per_substep;
         uint64_t const cap = cfg.max_subcycles;
@@ -440,9 +559,9 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
         double const ke = fmax(k, cutoff);
         double drag_est = 0.0;
         if (ke > 0.0) {
-            ElectronRates rt;
-            electron_rates(C, arena, ke, rt, err);
-            drag_est = (rt.collision * 1.0 + rt.soft * 1.0) * driver_dpath;
+            double const col = rate_value(C, arena, rc, ke, kRateCollision, err);
+            double const soft = rate_value(C, arena, rc, ke, kRateSoft, err);
+            drag_est = (col * 1.0 + soft * 1.0) * driver_dpath;
         }
         double const impulse = fmax(cfg.max_field_impulse_fraction * k, fmax(cfg.field_impulse_floor_eV, 1.0));
         uint64_t const gsd = static_cast<uint64_t>(
@@ -488,13 +607,11 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
     auto continuous = [&](double b, double e, double stop_e, double& end_out) -> bool {
         end_out = b;
         if (!(e > b) || !(k > 0.0) || stop_e < cutoff) return false;
-        ElectronRates rt;
-        electron_rates(C, arena, stop_e, rt, err);
-        double const sc = frozen_rate(rt.collision * 1.0, err);
-        double const ss = frozen_rate(rt.soft * 1.0, err);
-        double const sh = (C.hm_enabled && hm_thr > 0.0 && stop_e > 2.0 * hm_thr)
-            ? frozen_rate(hard_moller_energy_loss(C, arena, stop_e, 1.0, err), err)
-            : 0.0;
+        // The plan's hard-transfer loss feeds only the reference's scalar
+        // tally, and its table queries cannot fail at an energy the
+        // collision table just accepted, so it is not evaluated here.
+        double const sc = frozen_rate(rate_value(C, arena, rc, stop_e, kRateCollision, err) * 1.0, err);
+        double const ss = frozen_rate(rate_value(C, arena, rc, stop_e, kRateSoft, err) * 1.0, err);
         if (err.code) return false;
         double const total = sc + ss;
         // limiter
@@ -511,18 +628,11 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                 } else {
                     reaches = true;
                     if (to_cut != 0.0) {
-                        double lo = b, hi = e;
-                        for (int it = 0; it < 56; ++it) {
-                            double const mid = 0.5 * (lo + hi);
-                            double const l = total * density_path(iv, path, b, mid);
-                            if (!isfinite(l) || l < 0.0) {
-                                valid = false;
-                                break;
-                            }
-                            if (l < to_cut) lo = mid; else hi = mid;
+                        valid = cutoff_bisection<NP>(&iv, &path, b, e, total, to_cut, eff);
+                        if (!valid) {
+                            eff = b;
+                            reaches = false;
                         }
-                        eff = valid ? 0.5 * (lo + hi) : b;
-                        if (!valid) reaches = false;
                     }
                 }
             }
@@ -537,7 +647,6 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
         double const avail = fmax(0.0, k - cutoff);
         double const drag = reaches ? avail : fmin(raw_col + raw_soft, avail);
         double const col = fmin(raw_col, drag);
-        (void)sh;
         // ion pairs, O/RreaChargedInterleave.H:157-196
         if (col > 0.0 && raw_col > 0.0) {
             for (int i = 0; i < iv.n; ++i) {
@@ -563,10 +672,15 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
             err.set(RREA_GPU_ERR_RANGE);
             return false;
         }
-        ElectronRates rt;
-        electron_rates(C, arena, e, rt, err);
-        if (ch == 0) return C.hm_enabled && (hm_thr > 0.0 && e > 2.0 * hm_thr) && rt.moller_inv > 0.0;
-        if (ch == 1) return (isfinite(e) && isfinite(C.photon_cutoff_eV) && e > C.photon_cutoff_eV) && rt.brems_inv > 0.0;
+        if (!rate_bracket(C, arena, rc, e, err)) return false;
+        if (ch == 0) {
+            return C.hm_enabled && (hm_thr > 0.0 && e > 2.0 * hm_thr)
+                && rate_positive(C, arena, rc, e, kRateMoller, err);
+        }
+        if (ch == 1) {
+            return (isfinite(e) && isfinite(C.photon_cutoff_eV) && e > C.photon_cutoff_eV)
+                && rate_positive(C, arena, rc, e, kRateBrems, err);
+        }
         return false;
     };
 
@@ -575,7 +689,7 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
         if (k < cutoff) break;
         double sb, se;
         {
-            Path np;
+            Path<NP> np;
             if (!build_chord(sub_dt, np)) break;
             path = np;
             if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
@@ -613,7 +727,7 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                 }
                 double const frozen = k;
                 double s0, s1;
-                competing_rates(C, arena, frozen, s0, s1, err);
+                competing_rates(C, arena, rc, frozen, s0, s1, err);
                 double const seg_dp = density_path(iv, path, rem, se);
                 double const t0 = s0 * seg_dp, t1 = s1 * seg_dp;
                 uint64_t rng_index;
@@ -664,46 +778,13 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                 }
                 double const within = fmin(1.0, fmax(0.0, ev));
                 double const birth = fmin(1.0, (static_cast<double>(completed) + within) / static_cast<double>(subcycles));
+                Site const site{ex, ey, ez, er, birth};
                 if (selv.channel == 0) {
-                    // RreaApplyHardMollerFinalState, O/RreaChargedFinalStates.H:164-225
-                    double const kb = k;
-                    if (!charged_in_range(C.tix, kb)) {
-                        err.set(RREA_GPU_ERR_RANGE);
-                        break;
-                    }
-                    double sec = sample_conditional(arena, C.tix.cdf[RREA_C_MOLLER], kb,
-                                                    rng.uniform(rng_index, kChHardMollerEnergy), true, err);
-                    sec = fmax(hm_thr, fmin(sec, 0.5 * kb));
-                    double pdx, pdy, pdz, sdx, sdy, sdz;
-                    moller_lab_directions(dx, dy, dz, kb, sec, rng.uniform(rng_index, kChHardMollerAzimuth), pdx, pdy,
-                                          pdz, sdx, sdy, sdz);
-                    k = fmax(0.0, kb - sec);
-                    dx = pdx; dy = pdy; dz = pdz;
-                    add_secondary(0, 2, ex, ey, ez, sdx, sdy, sdz, sec, birth);
-                    deposit_source(C, A.cells, 0, er, ez, weight, sec, sec);
+                    moller_final_state(C, A, rng, rng_index, ip, key, weight, site, k, dx, dy, dz, lineage, err);
                 } else if (selv.channel == 1) {
-                    // RreaApplyBremsFinalState, O/RreaChargedFinalStates.H:329-394
-                    double const kb = k;
-                    if (!charged_in_range(C.tix, kb)) {
-                        err.set(RREA_GPU_ERR_RANGE);
-                        break;
-                    }
-                    double const sampled = sample_conditional(arena, C.tix.cdf[RREA_C_BREMS_E], kb,
-                                                              rng.uniform(rng_index, kChBremsEnergy), false, err);
-                    double const eg = fmin(fmax(sampled, 0.0), fmax(kb, 0.0));
-                    double const after = fmax(0.0, fmax(kb, 0.0) - eg);
-                    bool const tracked = isfinite(C.photon_cutoff_eV) && C.photon_cutoff_eV >= 0.0 && eg >= C.photon_cutoff_eV;
-                    double const ct = sample_brems_cos(C, kb, rng.uniform(rng_index, kChBremsAngle), err);
-                    double gx, gy, gz;
-                    cone_direction(dx, dy, dz, ct, rng.uniform(rng_index, kChBremsAzimuth), gx, gy, gz);
-                    photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
-                    k = after;
-                    if (tracked) {
-                        add_secondary(2, 4, ex, ey, ez, gx, gy, gz, eg, birth);
-                    } else if (eg > 0.0) {
-                        deposit_local(er, ez, eg);
-                    }
+                    brems_final_state(C, A, rng, rng_index, ip, key, weight, site, k, dx, dy, dz, lineage, err);
                 }
+                if (err.code) break;
                 if (k <= cutoff) {
                     mark_stopped(ev);
                     break;
@@ -717,27 +798,16 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
         // ---- finish_interleaved_substep, O/RreaElectronTransport.cpp:502-524
         if (k >= cutoff) {
             // apply_gs_elastic_scatter, O/RreaTransportStep.H:371-423
-            double const gs_n = elastic_inverse_stp(C, arena, k, err) * density_path(iv, path, sb, se);
+            // log(k) is shared by the elastic-MFP and angle-table brackets.
+            double const lk = (k > 0.0) ? log(k) : __longlong_as_double(0x7ff8000000000000LL);
+            double const gs_n = elastic_inverse_stp(C, arena, k, err, lk) * density_path(iv, path, sb, se);
             if (gs_n > 0.0) {
                 double const few = C.tix.gs_few_collision_threshold;
                 if (gs_n < few) {
-                    int const cap = static_cast<int>(ceil(3.0 * few));
-                    if (cap >= 255) {
-                        err.set(RREA_GPU_ERR_INVALID_STATE);
-                        break;
-                    }
-                    int const cnt = poisson_capped(gs_n, rng.uniform((sub << 8) | 0, kChElectronGsFewCount), cap);
-                    for (int q = 0; q < cnt; ++q) {
-                        uint64_t const inner = static_cast<uint64_t>(q + 1);
-                        double const ct = sample_single_elastic_cos(
-                            C, arena, k, rng.uniform((sub << 8) | inner, kChElectronGsFewScatter), err);
-                        double nx, ny, nz;
-                        cone_direction(dx, dy, dz, ct, rng.uniform((sub << 8) | inner, kChElectronGsFewAzimuth), nx,
-                                       ny, nz);
-                        dx = nx; dy = ny; dz = nz;
-                    }
+                    gs_few_collisions(C, arena, rng, sub, gs_n, k, lk, dx, dy, dz, err);
+                    if (err.code) break;
                 } else {
-                    double const ct = sample_gs_cos(C, arena, k, gs_n, rng.uniform(sub << 8, kChElectronGsAngle), err);
+                    double const ct = sample_gs_cos(C, arena, k, gs_n, rng.uniform(sub << 8, kChElectronGsAngle), err, lk);
                     double nx, ny, nz;
                     cone_direction(dx, dy, dz, ct, rng.uniform(sub << 8, kChElectronGsAzimuth), nx, ny, nz);
                     dx = nx; dy = ny; dz = nz;
@@ -779,14 +849,18 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
     double threshold = 0.0;
     {
         double const ke = fmax(k, cutoff);
-        if (ke > 0.0 && particle_density > 0.0) {
-            ElectronRates rt;
-            electron_rates(C, arena, ke, rt, err);
+        // The drag threshold only decides the gate when k <= the hard-Moller
+        // threshold; above it only its range check can matter, and that is
+        // kept.
+        if (!charged_in_range(C.tix, ke)) err.set(RREA_GPU_ERR_RANGE);
+        if (ke > 0.0 && particle_density > 0.0 && k <= hm_thr) {
+            double const col = rate_value(C, arena, rc, ke, kRateCollision, err);
+            double const soft = rate_value(C, arena, rc, ke, kRateSoft, err);
             double const hard = C.hm_enabled ? hard_moller_energy_loss(C, arena, ke, particle_density, err) : 0.0;
             double tracked = 0.0;
-            double const inv = rt.brems_inv * particle_density;
+            double const inv = rate_value(C, arena, rc, ke, kRateBrems, err) * particle_density;
             if (inv > 0.0) tracked = inv * mean_conditional(arena, C.tix.cdf[RREA_C_BREMS_E], ke, err);
-            threshold = (rt.collision * particle_density + rt.soft * particle_density) + hard + tracked;
+            threshold = (col * particle_density + soft * particle_density) + hard + tracked;
         }
     }
     if (err.code) return finish(-1);

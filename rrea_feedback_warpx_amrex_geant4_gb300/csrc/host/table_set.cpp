@@ -318,8 +318,10 @@ void TableSet::Load(std::string const& config_path)
         h.ly = push_logs(tab.y, true);
     }
     auto shared = [&](int first, int last) {
+        bool const linear = m_index.hot[first].mode == RREA_INTERP_LINEAR;
         for (int t = first + 1; t <= last; ++t) {
             if (m_index.hot[t].x != m_index.hot[first].x) return 0;
+            if ((m_index.hot[t].mode == RREA_INTERP_LINEAR) != linear) return 0;
         }
         return 1;
     };
@@ -357,6 +359,21 @@ void TableSet::Load(std::string const& config_path)
         ci.start = push(start);
         ci.u = push(u);
         ci.v = push(v);
+        // Per-group mean of the inverse CDF, trapezoid over the u nodes in the
+        // reference's accumulation order (RreaInteractionTables.cpp:1075-1085).
+        std::vector<double> mean(g.primary.size(), 0.0);
+        for (std::size_t k = 0; k < g.primary.size(); ++k) {
+            std::vector<double> const& gu = g.u[k];
+            std::vector<double> const& gv = g.v[k];
+            double m = gu.front() * gv.front();
+            for (std::size_t i = 1; i < gu.size(); ++i) {
+                m += 0.5 * (gv[i - 1] + gv[i]) * (gu[i] - gu[i - 1]);
+            }
+            m += (1.0 - gu.back()) * gv.back();
+            mean[k] = m;
+        }
+        ci.mean = push(mean);
+        ci.lmean = push_logs(mean, true);
     }
 
     for (int s = 0; s < 2; ++s) {

@@ -69,6 +69,8 @@ typedef struct {
     int64_t start;     // ng+1 node offsets (stored as doubles, exact integers)
     int64_t u;         // cdf nodes
     int64_t v;         // sampled values
+    int64_t mean;      // ng per-group means (RreaInteractionTables.cpp:1075-1085 quadrature)
+    int64_t lmean;     // ng logs of the group means (0 where the mean is not positive)
 } RreaCondCdfIndex;
 
 typedef struct {

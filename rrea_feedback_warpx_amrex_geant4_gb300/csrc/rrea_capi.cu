@@ -4,7 +4,7 @@
 // allocated at create/load time; a step allocates nothing.
 #include "../../include/rrea_gpu.h"
 
-#include "device/rrea_electron.cuh"
+#include "device/rrea_electron_args.cuh"
 #include "host/table_set.hpp"
 #include "rrea_kernels.h"
 
@@ -68,7 +68,8 @@ struct rrea_gpu_ctx {
     int64_t last_transported = 0;
     int64_t last_secondaries = 0;
     int launch_threads = 128;
-    int launch_blocks_per_sm = 8;
+    int launch_blocks_per_sm = 4;
+    int launch_min_blocks = 4;
     bool diagnostics = true;
 
     std::string last_error;
@@ -353,6 +354,8 @@ rrea_gpu_status launch_electrons(rrea_gpu_ctx* ctx, int32_t step, double dt_s, b
     sc.tix = ctx->tables.index();
     sc.dr = (c.r_hi - c.r_lo) / c.nr;
     sc.dz = (c.z_hi - c.z_lo) / c.nz;
+    sc.div_dr = rrea_dev::make_divisor(sc.dr);
+    sc.div_dz = rrea_dev::make_divisor(sc.dz);
     sc.hm_threshold_eV = sc.tix.hard_moller_threshold_eV;
     sc.photon_cutoff_eV = c.photon_cutoff_eV;
     // RreaParticleInteraction.cpp:33-35 with a uniform density ratio
@@ -395,16 +398,19 @@ rrea_gpu_status launch_electrons(rrea_gpu_ctx* ctx, int32_t step, double dt_s, b
     a.fv.nz = c.nz;
     a.fv.dr = sc.dr;
     a.fv.dz = sc.dz;
+    a.fv.div_dr = sc.div_dr;
+    a.fv.div_dz = sc.div_dz;
     a.fv.r_lo = c.r_lo;
     a.fv.z_lo = c.z_lo;
     a.fv.periodic = c.periodic_z != 0;
     a.fv.has_b = ctx->has_b;
     if (a.n > 0) {
         int64_t const want = (a.n + ctx->launch_threads - 1) / ctx->launch_threads;
-        int64_t const cap = static_cast<int64_t>(ctx->num_sms) * ctx->launch_blocks_per_sm;
+        int64_t const cap = static_cast<int64_t>(ctx->num_sms) * ctx->launch_blocks_per_sm * (128 / ctx->launch_threads);
         int const blocks = static_cast<int>(want < cap ? want : cap);
         RREA_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
-        RREA_CUDA(ctx, rrea_launch::electron_step(a, blocks > 0 ? blocks : 1, ctx->launch_threads, ctx->stream));
+        RREA_CUDA(ctx, rrea_launch::electron_step(a, blocks > 0 ? blocks : 1, ctx->launch_threads,
+                                                  ctx->launch_min_blocks, c.periodic_z != 0, ctx->stream));
         RREA_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
     }
     unsigned long long count = 0;
@@ -567,6 +573,10 @@ rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block
     ctx->launch_threads = threads_per_block;
     ctx->launch_blocks_per_sm = blocks_per_sm;
     ctx->diagnostics = diagnostics != 0;
+    // Register budget of the transport kernel follows the requested
+    // residency: >= 4 resident 128-thread blocks caps it at 128 registers.
+    int const resident = blocks_per_sm * threads_per_block / 128;
+    ctx->launch_min_blocks = resident >= 5 ? 5 : (resident == 4 ? 4 : (resident == 3 ? 3 : 2));
     return RREA_GPU_OK;
 }
 

@@ -37,7 +37,11 @@ __global__ void field_prep_kernel(int nr, int nz, const double* __restrict__ er,
     }
 }
 
-__global__ void __launch_bounds__(128) electron_step_kernel(ElectronArgs A)
+// MinBlocks trades registers for resident warps: 2 -> up to 255 registers
+// (8 warps/SM), 3 -> 168 (12), 4 -> 128 (16), 5 -> 102 (20).
+// NP is the chord piece capacity: 1 for absorbing z faces, 4 for periodic z.
+template <int MinBlocks, int NP>
+__global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(ElectronArgs A)
 {
     StepConstants const& C = c_step;
     unsigned int moved = 0;
@@ -54,7 +58,7 @@ __global__ void __launch_bounds__(128) electron_step_kernel(ElectronArgs A)
         uint64_t sub = 0, ev = 0;
         uint32_t lineage = 0;
         ++moved;
-        int const disp = transport_electron(C, A, ip, sub, ev, lineage, err);
+        int const disp = transport_electron<NP>(C, A, ip, sub, ev, lineage, err);
         // Every record this particle appended carries a lineage below this
         // count, so the ordering scan/scatter stays in bounds on every path.
         if (A.sec_per_parent) A.sec_per_parent[ip] = lineage;
@@ -165,9 +169,19 @@ cudaError_t field_prep(int nr, int nz, const double* er, const double* ez, const
     return cudaGetLastError();
 }
 
-cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, cudaStream_t stream)
+cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, int min_blocks, bool periodic,
+                          cudaStream_t stream)
 {
-    rrea_dev::electron_step_kernel<<<blocks, threads, 0, stream>>>(args);
+    if (periodic) {
+        rrea_dev::electron_step_kernel<4, RREA_ARENA_MAX_PIECES><<<blocks, threads, 0, stream>>>(args);
+        return cudaGetLastError();
+    }
+    switch (min_blocks) {
+    case 3: rrea_dev::electron_step_kernel<3, 1><<<blocks, threads, 0, stream>>>(args); break;
+    case 4: rrea_dev::electron_step_kernel<4, 1><<<blocks, threads, 0, stream>>>(args); break;
+    case 5: rrea_dev::electron_step_kernel<5, 1><<<blocks, threads, 0, stream>>>(args); break;
+    default: rrea_dev::electron_step_kernel<2, 1><<<blocks, threads, 0, stream>>>(args); break;
+    }
     return cudaGetLastError();
 }
 
