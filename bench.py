@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=32768)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--threads", type=int, default=128)
-    p.add_argument("--blocks-per-sm", type=int, default=4)
+    p.add_argument("--blocks-per-sm", type=int, default=5)
     return p.parse_args()
 
 

@@ -8,7 +8,8 @@
  *        amrex::Real dt_s)
  * (native_amrex_rrea/warpx_overlay/Source/Rrea/RreaParticleInteraction.H:1609-1623,
  *  body in RreaParticleInteraction.cpp:12-62).  The overlay keeps that C++
- * signature; its body gathers the species tiles, calls rrea_gpu_apply_electrons(), and
+ * signature; its body gathers the species tiles, calls rrea_gpu_apply_electrons()
+ * and rrea_gpu_apply_photons(), and
  * raises amrex::Abort on a non-OK status, which preserves the fail-closed
  * contract of the reference (every guard aborts the whole step before any
  * side effect is committed).
@@ -177,9 +178,38 @@ rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step
                                                  int64_t* n_secondaries);
 rrea_gpu_status rrea_gpu_fetch_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile);
 
+/*
+ * Drop-in for the photon phase of RreaParticleInteraction::Apply
+ * (TransportStep::ApplyPhotonTransport, RreaPhotonTransport.cpp:9-461, final
+ * states RreaPhotonFinalStates.H:56-365).  The tile's (r, theta, z) is the
+ * end point of WarpX's straight photon push and prev_* its captured start;
+ * (ux, uy, uz) is the photon momentum in eV.  Each photon flies its chord,
+ * interacts at most once per chord (Compton continues along the new
+ * direction for the rest of the chord), and the absorbed or escaped ones
+ * get a negated id.  Secondaries come back in deterministic order with
+ * root_species = RREA_SPECIES_PHOTON.  Diagnostics: subcycles 0, events =
+ * hazard draws, disposition 0 survive, 1 escape, 2 absorbed.
+ */
+rrea_gpu_status rrea_gpu_apply_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, int32_t step,
+                                       double time_s, double dt_s,
+                                       rrea_gpu_secondary* secondaries,
+                                       int64_t secondary_capacity, int64_t* n_secondaries);
+
+/*
+ * Resident photon mode: the staged tile holds photons at their start point.
+ * The step pushes each photon straight by c*dt along its momentum (the
+ * WarpX photon pusher, x += c dt u/|u| in Cartesian coordinates) and then
+ * runs the photon phase on that chord, all on the device.  stage/fetch move
+ * the tile as for electrons.
+ */
+rrea_gpu_status rrea_gpu_stage_photons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile);
+rrea_gpu_status rrea_gpu_step_photons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s,
+                                               int64_t* n_secondaries);
+rrea_gpu_status rrea_gpu_fetch_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile);
+
 /* Launch shape of the transport kernel: threads per block (32..128, a
- * multiple of 32) and resident 128-thread blocks per SM (2 to 5; the
- * kernel variant's register budget follows: 255, 168, 128 or 102 registers).  The
+ * multiple of 32) and resident 128-thread blocks per SM (2 to 8; the
+ * kernel variant's register budget follows: 255, 168, 128, 102, 85 or 64).  The
  * grid is one resident wave with a grid-stride loop.  `diagnostics` enables
  * the per-particle diagnostic arrays. */
 rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm,

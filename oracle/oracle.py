@@ -69,6 +69,8 @@ def lib():
         _lib.oracle_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         _lib.oracle_electron_step.argtypes = [ctypes.POINTER(RreaGpuConfig), d, d, d, d, d, ctypes.c_int32,
                                               ctypes.c_double, ctypes.POINTER(RreaGpuTile)]
+        _lib.oracle_photon_step.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_int32, ctypes.c_double,
+                                            ctypes.POINTER(RreaGpuTile)]
         _lib.oracle_counts.argtypes = [ctypes.POINTER(ctypes.c_int64)] * 3
         _lib.oracle_secondaries.argtypes = [ctypes.c_void_p]
         _lib.oracle_sources.argtypes = [d]
@@ -144,6 +146,19 @@ def electron_step(cfg, field, step, dt_s, arrays):
     _check(lib().oracle_electron_step(ctypes.byref(cfg), _dptr(field["er"]), _dptr(field["ez"]),
                                       _dptr(field["bt"]), _dptr(field["amb_er"]), _dptr(field["amb_ez"]),
                                       step, dt_s, ctypes.byref(t)))
+    return _collect(cfg, t)
+
+
+def photon_step(cfg, step, dt_s, arrays):
+    """Runs the oracle photon phase in place on `arrays` (photon tile: prev_*
+    is the captured start, r/theta/z the straight-push endpoint)."""
+    cfg = as_config(cfg)
+    t = make_tile_struct(arrays)
+    _check(lib().oracle_photon_step(ctypes.byref(cfg), step, dt_s, ctypes.byref(t)))
+    return _collect(cfg, t)
+
+
+def _collect(cfg, t):
     n_sec, n_src, n_seg = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
     lib().oracle_counts(ctypes.byref(n_sec), ctypes.byref(n_src), ctypes.byref(n_seg))
     sec = np.zeros(n_sec.value, dtype=SECONDARY_DTYPE)

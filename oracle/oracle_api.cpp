@@ -107,6 +107,30 @@ int oracle_electron_step(rrea_gpu_config const* cfg, double const* er, double co
     }
 }
 
+int oracle_photon_step(rrea_gpu_config const* cfg, int32_t step, double dt_s, rrea_gpu_tile const* tile)
+{
+    if (!g_tables) return RREA_GPU_ERR_NOT_READY;
+    try {
+        oracle::ChargedTile t;
+        t.n = tile->n;
+        t.r = tile->r; t.z = tile->z; t.theta = tile->theta;
+        t.ux = tile->ux; t.uy = tile->uy; t.uz = tile->uz; t.w = tile->w;
+        t.prev_r = tile->prev_r; t.prev_z = tile->prev_z; t.prev_theta = tile->prev_theta;
+        t.prev_ux = tile->prev_ux; t.prev_uy = tile->prev_uy; t.prev_uz = tile->prev_uz;
+        t.id = tile->id;
+        t.cpu = tile->cpu;
+        g_out.clear();
+        oracle::ApplyPhotonTransport(*g_tables, *cfg, step, dt_s, t, g_out);
+        g_cells.nr = cfg->nr;
+        g_cells.nz = cfg->nz;
+        for (auto& f : g_cells.f) f.assign(static_cast<std::size_t>(cfg->nr) * cfg->nz, 0.0);
+        oracle::DepositSources(*cfg, g_out.sources, cfg->low_energy_cutoff_eV, g_cells);
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
 void oracle_counts(int64_t* n_sec, int64_t* n_src, int64_t* n_seg)
 {
     *n_sec = static_cast<int64_t>(g_out.secondaries.size());

@@ -1,6 +1,7 @@
 // ORACLE — test infrastructure only (see oracle_core.hpp).
 #include "oracle_core.hpp"
 
+#include <cstring>
 #include <functional>
 #include <sstream>
 
@@ -1023,6 +1024,364 @@ Crossing boundary_crossing(Path const& path)
     return r;
 }
 
+// ======================================================================
+// Photon samplers: S/RreaInteractionTables.cpp:2272-2296, 2762-3127,
+// 1374-1525, 3208-3253, 63-108; I/RreaUniformStream.H:21-53
+// ======================================================================
+struct UniformStream {
+    uint64_t state;
+    static uint64_t sm(uint64_t x)
+    {
+        x += 0x9E3779B97F4A7C15ULL;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+        return x ^ (x >> 31);
+    }
+    UniformStream(double u1, double u2)
+    {
+        uint64_t b1, b2;
+        std::memcpy(&b1, &u1, 8);
+        std::memcpy(&b2, &u2, 8);
+        uint64_t const h2 = sm(b2);
+        state = sm(b1) ^ ((h2 << 32) | (h2 >> 32));
+    }
+    double next()
+    {
+        state += 0x9E3779B97F4A7C15ULL;
+        uint64_t z = state;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z = z ^ (z >> 31);
+        return static_cast<double>(z >> 11) * (1.0 / 9007199254740992.0);
+    }
+};
+
+double clamp_unit(double v)
+{
+    if (!std::isfinite(v)) return 0.5;
+    return std::max(0.0, std::min(1.0, v));
+}
+double wrap_unit(double v)
+{
+    if (!std::isfinite(v)) return 0.0;
+    v = v - std::floor(v);
+    if (v < 0.0) v += 1.0;
+    return v;
+}
+
+struct PhotonRates {
+    double compton, pe, nuclear, triplet;
+    double total() const { return compton + pe + nuclear + triplet; }
+};
+PhotonRates photon_rates(Tables const& t, double e, double dr)
+{
+    if (!(e >= t.ix.photon_min_eV && e <= t.ix.photon_max_eV)) {
+        fail(RREA_GPU_ERR_RANGE, "schema-6 photon energy outside the certified range");
+    }
+    return PhotonRates{t.interpolate(RREA_T_PH_COMPTON, e) * dr, t.interpolate(RREA_T_PH_PHOTOELECTRIC, e) * dr,
+                       t.interpolate(RREA_T_PH_PAIR_NUCLEAR, e) * dr, t.interpolate(RREA_T_PH_PAIR_TRIPLET, e) * dr};
+}
+void require_photon(Tables const& t, double e)
+{
+    if (!std::isfinite(e) || !(e >= t.ix.photon_min_eV && e <= t.ix.photon_max_eV)) {
+        fail(RREA_GPU_ERR_RANGE, "schema-6 photon sampler energy outside the certified range");
+    }
+}
+// :2778-2804; 0 Compton, 1 photoelectric, 2 pair nuclear, 3 pair triplet
+int sample_photon_channel(Tables const& t, double e, double u)
+{
+    require_photon(t, e);
+    u = std::max(0.0, std::min(1.0, u));
+    PhotonRates const r = photon_rates(t, e, 1.0);
+    double const total = r.total();
+    if (!(total > 0.0) || !std::isfinite(total)) fail(RREA_GPU_ERR_INVALID_STATE, "photon rates sum to zero");
+    double const target = u * total;
+    if (target < r.compton) return 0;
+    if (target < r.compton + r.pe) return 1;
+    if (target < r.compton + r.pe + r.nuclear) return 2;
+    return 3;
+}
+struct ComptonState {
+    double recoil, scattered, cos_theta;
+};
+// :2806-2871
+ComptonState sample_klein_nishina(Tables const& t, double e, double draw_mu, double draw_accept)
+{
+    require_photon(t, e);
+    if (e <= 0.0) fail(RREA_GPU_ERR_INVALID_STATE, "Compton sampler requires positive energy");
+    draw_mu = std::max(0.0, std::min(1.0, draw_mu));
+    draw_accept = std::max(0.0, std::min(1.0, draw_accept));
+    UniformStream stream(draw_mu, draw_accept);
+    double const alpha = e / kMeC2;
+    double const eps0 = 1.0 / (1.0 + 2.0 * alpha);
+    double const eps0sq = eps0 * eps0;
+    double const a1 = -std::log(eps0);
+    double const a2 = 0.5 * (1.0 - eps0sq);
+    double epsilon = eps0, onecost = 0.0;
+    for (int iter = 0; iter < 128; ++iter) {
+        double const u1 = iter == 0 ? draw_mu : stream.next();
+        double const u2 = iter == 0 ? draw_accept : stream.next();
+        double epsilonsq;
+        if (a1 > (a1 + a2) * u1) {
+            epsilon = std::exp(-a1 * u2);
+            epsilonsq = epsilon * epsilon;
+        } else {
+            epsilonsq = eps0sq + (1.0 - eps0sq) * u2;
+            epsilon = std::sqrt(epsilonsq);
+        }
+        onecost = (1.0 - epsilon) / (epsilon * alpha);
+        double const sint2 = onecost * (2.0 - onecost);
+        double const greject = 1.0 - epsilon * sint2 / (1.0 + epsilonsq);
+        if (greject >= stream.next()) break;
+    }
+    double mu = 1.0 - onecost;
+    mu = std::max(-1.0, std::min(1.0, mu));
+    ComptonState st;
+    st.scattered = std::max(0.0, epsilon * e);
+    st.recoil = std::max(0.0, e - st.scattered);
+    st.cos_theta = mu;
+    return st;
+}
+// :2878-2941 -> (photoelectron energy, binding energy)
+void sample_photoelectric(Tables const& t, double e, double u, double& electron, double& binding)
+{
+    require_photon(t, e);
+    RreaPhotoelectricIndex const& pi = t.ix.pe;
+    double const* prim = t.t.at(pi.primary);
+    double const* start = t.t.at(pi.start);
+    double const* cu = t.t.at(pi.u);
+    double const* bind = t.t.at(pi.binding);
+    if (e < prim[0] || e > prim[pi.ng - 1]) fail(RREA_GPU_ERR_RANGE, "photoelectric primary out of range");
+    u = std::max(0.0, std::min(1.0, u));
+    double const* up = std::lower_bound(prim, prim + pi.ng, e);
+    int g;
+    if (up == prim) g = 0;
+    else if (up == prim + pi.ng) g = pi.ng - 1;
+    else if (*up == e) g = static_cast<int>(up - prim);
+    else g = static_cast<int>(up - prim) - 1;
+    int const b = static_cast<int>(start[g]), en = static_cast<int>(start[g + 1]);
+    double const* row = std::lower_bound(cu + b, cu + en, u);
+    int const r = row == cu + en ? en - 1 : static_cast<int>(row - cu);
+    if (bind[r] > e) fail(RREA_GPU_ERR_INVALID_STATE, "photoelectric binding exceeds photon energy");
+    binding = bind[r];
+    electron = std::max(0.0, e - bind[r]);
+}
+// :2949-3044 (long double as in the reference)
+double sample_photoelectron_cos(Tables const& t, double k, double draw)
+{
+    if (!(k == 0.0)) t.require_charged(k);
+    long double const u = static_cast<long double>(clamp_unit(draw));
+    if (u <= 0.0L) return -1.0;
+    if (u >= 1.0L) return 1.0;
+    long double const gamma = 1.0L + static_cast<long double>(k) / static_cast<long double>(kMeC2);
+    long double const inv_g2 = 1.0L / (gamma * gamma);
+    long double const beta = std::sqrt(std::max(0.0L, 1.0L - inv_g2));
+    if (beta < 1.0e-4L) {
+        long double lo = -1.0L, hi = 1.0L;
+        for (int it = 0; it < 96; ++it) {
+            long double const mid = 0.5L * (lo + hi);
+            if (mid == lo || mid == hi) break;
+            long double const cdf = (2.0L + mid * (3.0L - mid * mid)) / 4.0L;
+            if (cdf < u) lo = mid; else hi = mid;
+        }
+        return static_cast<double>(0.5L * (lo + hi));
+    }
+    long double const b = 0.5L * gamma * (gamma - 1.0L) * (gamma - 2.0L);
+    long double const c = -inv_g2;
+    long double const t_lo = inv_g2 / (1.0L + beta);
+    long double const t_hi = 1.0L + beta;
+    auto prim = [c, b](long double x) {
+        return -c / (3.0L * x * x * x) - (2.0L + b * c) / (2.0L * x * x) - (2.0L * b - 1.0L) / x - b * std::log(x);
+    };
+    long double const f_lo = prim(t_lo), f_hi = prim(t_hi);
+    long double const total = f_hi - f_lo;
+    if (!(total > 0.0L) || !std::isfinite(total)) fail(RREA_GPU_ERR_INVALID_STATE, "Sauter-Gavrila normalization");
+    long double const target = (1.0L - u) * f_hi + u * f_lo;
+    long double lo = t_lo, hi = t_hi;
+    for (int it = 0; it < 128; ++it) {
+        long double const mid = 0.5L * (lo + hi);
+        if (mid == lo || mid == hi) break;
+        if (prim(mid) < target) lo = mid; else hi = mid;
+    }
+    long double const tt = 0.5L * (lo + hi);
+    return static_cast<double>(std::max(-1.0L, std::min(1.0L, (1.0L - tt) / beta)));
+}
+struct PairState {
+    bool valid = false;
+    double e_electron = 0, e_positron = 0, e_recoil = 0, local = 0;
+    double edir[3] = {0, 0, 1}, pdir[3] = {0, 0, 1}, rdir[3] = {0, 0, 1};
+    bool recoil = false;
+};
+void normalize_local(double& x, double& y, double& z)
+{
+    double const n = std::sqrt(x * x + y * y + z * z);
+    if (n <= 0.0 || !std::isfinite(n)) { x = 0.0; y = 0.0; z = 1.0; return; }
+    x /= n; y /= n; z /= n;
+}
+// :3053-3127 with BuildRreaPairEmpiricalFinalState :1384-1525; channel 2 nuclear, 3 triplet
+PairState sample_pair(Tables const& t, double e, int channel, double d_inv, double d_polar, double d_azim)
+{
+    require_photon(t, e);
+    PairState st;
+    bool const triplet = channel == 3;
+    double const threshold = triplet ? 4.0 * kMeC2 : 2.0 * kMeC2;
+    if (!(std::isfinite(e) && e > threshold)) return st;
+    RreaPairBankIndex const& pb = t.ix.pair[triplet ? 1 : 0];
+    double const* prim = t.t.at(pb.primary);
+    double const* start = t.t.at(pb.start);
+    int sel = 0;
+    if (e >= prim[pb.nb - 1]) {
+        sel = pb.nb - 1;
+    } else if (e > prim[0]) {
+        double const* up = std::lower_bound(prim, prim + pb.nb, e);
+        int const hi = static_cast<int>(up - prim);
+        if (prim[hi] == e) {
+            sel = hi;
+        } else {
+            int const lo = hi - 1;
+            double const tt = (std::log(e) - std::log(prim[lo])) / (std::log(prim[hi]) - std::log(prim[lo]));
+            sel = clamp_unit(d_polar) < tt ? hi : lo;
+        }
+    }
+    std::size_t const b0 = static_cast<std::size_t>(start[sel]);
+    std::size_t const size = static_cast<std::size_t>(start[sel + 1]) - b0;
+    std::size_t const idx = std::min(size - 1, static_cast<std::size_t>(clamp_unit(d_inv) * static_cast<double>(size)));
+    double const* rec = t.t.at(pb.records) + (b0 + idx) * RREA_PAIR_RECORD_DOUBLES;
+    int const count = static_cast<int>(rec[0]);
+    int es = -1, ps = -1, rs = -1;
+    for (int slot = 0; slot < count; ++slot) {
+        int const pdg = static_cast<int>(rec[1 + slot]);
+        if (pdg == -11) ps = slot;
+        else if (pdg == 11) { if (es < 0) es = slot; else rs = slot; }
+    }
+    if (es < 0 || ps < 0 || (triplet && rs < 0)) fail(RREA_GPU_ERR_INVALID_STATE, "pair record topology");
+    double const avail = e - 2.0 * kMeC2;
+    double const rot = kTwoPi * clamp_unit(d_azim);
+    double const cr = std::cos(rot), sr = std::sin(rot);
+    auto rotated = [&](int slot, double* d) {
+        double const px = rec[7 + 3 * slot], py = rec[8 + 3 * slot], pz = rec[9 + 3 * slot];
+        d[0] = cr * px - sr * py;
+        d[1] = sr * px + cr * py;
+        d[2] = pz;
+        normalize_local(d[0], d[1], d[2]);
+    };
+    st.valid = true;
+    st.e_electron = avail * rec[4 + es];
+    st.e_positron = avail * rec[4 + ps];
+    rotated(es, st.edir);
+    rotated(ps, st.pdir);
+    if (triplet) {
+        st.recoil = true;
+        st.e_recoil = avail * rec[4 + rs];
+        rotated(rs, st.rdir);
+    }
+    double const tol = 64.0 * kEps * std::max(1.0, avail);
+    auto sum = [&]() { return st.e_electron + st.e_positron + st.e_recoil; };
+    double expl = sum();
+    if (!std::isfinite(expl) || st.e_electron < 0.0 || st.e_positron < 0.0 || st.e_recoil < 0.0) {
+        fail(RREA_GPU_ERR_INVALID_STATE, "pair record negative energy");
+    }
+    if (expl > avail) {
+        if (expl - avail > tol) fail(RREA_GPU_ERR_INVALID_STATE, "pair record closure");
+        double const scale = avail / expl;
+        st.e_electron *= scale; st.e_positron *= scale; st.e_recoil *= scale;
+        expl = sum();
+    }
+    st.local = avail - expl;
+    auto reduce_largest = [&](double corr) {
+        double* es_[3] = {&st.e_electron, &st.e_positron, &st.e_recoil};
+        double** largest = std::max_element(es_, es_ + 3, [](double const* a, double const* b) { return *a < *b; });
+        if (**largest < corr) fail(RREA_GPU_ERR_INVALID_STATE, "pair closure correction");
+        **largest -= corr;
+    };
+    if (st.local < 0.0) {
+        double const corr = -st.local;
+        if (corr > tol) fail(RREA_GPU_ERR_INVALID_STATE, "pair negative remainder");
+        reduce_largest(corr);
+        st.local = 0.0;
+    }
+    double accounted = sum() + st.local;
+    double resid = avail - accounted;
+    if (std::abs(resid) > tol) fail(RREA_GPU_ERR_INVALID_STATE, "pair closure residual");
+    if (resid >= 0.0) st.local += resid;
+    else if (st.local >= -resid) st.local += resid;
+    else reduce_largest(-resid);
+    accounted = sum() + st.local;
+    if (st.e_electron < 0.0 || st.e_positron < 0.0 || st.e_recoil < 0.0 || st.local < 0.0
+        || std::abs(avail - accounted) > tol) {
+        fail(RREA_GPU_ERR_INVALID_STATE, "pair nonnegative closure");
+    }
+    return st;
+}
+// O/RreaChargedInterleave.H:498-517
+void rotate_to_axis(double ax, double ay, double az, double lx, double ly, double lz, double& ox, double& oy,
+                    double& oz)
+{
+    normalize(ax, ay, az);
+    normalize(lx, ly, lz);
+    double b1x, b1y, b1z, b2x, b2y, b2z;
+    transverse_basis(ax, ay, az, b1x, b1y, b1z, b2x, b2y, b2z);
+    ox = lx * b1x + ly * b2x + lz * ax;
+    oy = lx * b1y + ly * b2y + lz * ay;
+    oz = lx * b1z + ly * b2z + lz * az;
+    normalize(ox, oy, oz);
+}
+struct AnnihilationState {
+    double e1 = 0, e2 = 0, cos1 = 1, azim = 0;
+    bool valid = false, at_rest = false;
+};
+// :63-108
+double annihilation_fraction(double gamma, double draw)
+{
+    if (gamma <= 1.0 + 1.0e-12) return 0.5;
+    double const bcm = std::sqrt(std::max(0.0, (gamma - 1.0) / (gamma + 1.0)));
+    double const emin = 0.5 * (1.0 - bcm), emax = 0.5 * (1.0 + bcm);
+    double const u = clamp_unit(draw);
+    double const gp1 = gamma + 1.0;
+    double const a = 1.0 + 2.0 * gamma / (gp1 * gp1);
+    auto F = [a, gp1](double x) { return a * std::log(x) - x + 1.0 / (gp1 * gp1 * x); };
+    double const flo = F(emin), fhi = F(emax);
+    double const span = fhi - flo;
+    if (!(span > 0.0)) return 0.5;
+    double const target = flo + u * span;
+    double lo = emin, hi = emax;
+    for (int it = 0; it < 64; ++it) {
+        double const mid = 0.5 * (lo + hi);
+        if (F(mid) < target) lo = mid; else hi = mid;
+    }
+    return std::max(emin, std::min(emax, 0.5 * (lo + hi)));
+}
+// :3208-3253
+AnnihilationState sample_annihilation(Tables const& t, double k, double d_energy, double d_azim)
+{
+    if (!(k == 0.0)) t.require_charged(k);
+    AnnihilationState st;
+    k = std::max(0.0, k);
+    double const gamma = 1.0 + k / kMeC2;
+    double const total = 2.0 * kMeC2 + k;
+    if (gamma <= 1.0 + 1.0e-10) {
+        st.e1 = kMeC2;
+        st.e2 = kMeC2;
+        st.cos1 = 2.0 * clamp_unit(d_energy) - 1.0;
+        st.azim = wrap_unit(d_azim);
+        st.valid = true;
+        st.at_rest = true;
+        return st;
+    }
+    double const beta = std::sqrt(std::max(0.0, 1.0 - 1.0 / (gamma * gamma)));
+    double const eps = annihilation_fraction(gamma, d_energy);
+    st.e1 = eps * total;
+    st.e2 = std::max(0.0, total - st.e1);
+    if (st.e1 <= 0.0 || st.e2 <= 0.0) return st;
+    double const denom = eps * gamma * beta;
+    if (denom <= 0.0) return st;
+    st.cos1 = std::max(-1.0, std::min(1.0, (eps * (gamma + 1.0) - 1.0) / denom));
+    st.azim = wrap_unit(d_azim);
+    st.valid = true;
+    st.at_rest = false;
+    return st;
+}
+
 }  // namespace
 
 // ======================================================================
@@ -1519,6 +1878,273 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
     }
 }
 
+// ======================================================================
+// Photon phase: O/RreaPhotonTransport.cpp:9-461 with the final states of
+// O/RreaPhotonFinalStates.H:56-365 and TransportStep::spawn_positron_annihilation
+// (O/RreaTransportStep.H:563-702).  The photon tile's current (r, theta, z)
+// is WarpX's straight push endpoint; prev_* is the captured start.
+// ======================================================================
+void ApplyPhotonTransport(TableSet const& ts, rrea_gpu_config const& cfg, int step, double dt_s, ChargedTile& tile,
+                          StepOutputs& out)
+{
+    Tables const tables(ts);
+    double const rlo = cfg.r_lo, rhi = cfg.r_hi, zlo = cfg.z_lo, zhi = cfg.z_hi;
+    bool const periodic = cfg.periodic_z != 0;
+    double const cutoff = cfg.low_energy_cutoff_eV;
+    double const photon_cut = cfg.photon_cutoff_eV;
+    double const density_ratio = positive_or(cfg.density_ratio, 1.0);
+    uint64_t const seed = cfg.rng_seed;
+    uint64_t const step_key = static_cast<uint64_t>(std::max(step, 0));
+    double const w_air = ts.index().w_air_eV_per_pair;
+
+    out.subcycles.assign(static_cast<std::size_t>(tile.n), 0);
+    out.events.assign(static_cast<std::size_t>(tile.n), 0);
+    out.disposition.assign(static_cast<std::size_t>(tile.n), -1);
+    std::vector<uint64_t>& out_events = out.events;
+    std::vector<int32_t>& out_disposition = out.disposition;
+
+    constexpr int64_t kChunk = 64;
+    int64_t const n_chunks = (tile.n + kChunk - 1) / kChunk;
+    std::vector<StepOutputs> chunk_out(static_cast<std::size_t>(n_chunks));
+    std::vector<int> chunk_err(static_cast<std::size_t>(n_chunks), 0);
+    std::vector<std::string> chunk_msg(static_cast<std::size_t>(n_chunks));
+#pragma omp parallel for schedule(dynamic, 1) if (n_chunks > 1)
+    for (int64_t chunk = 0; chunk < n_chunks; ++chunk) {
+      StepOutputs& cout = chunk_out[static_cast<std::size_t>(chunk)];
+      try {
+      int64_t const ip_end = std::min(tile.n, (chunk + 1) * kChunk);
+      for (int64_t ip = chunk * kChunk; ip < ip_end; ++ip) {
+        if (!(tile.id[ip] > 0)) continue;
+        std::size_t const sp = static_cast<std::size_t>(ip);
+        uint64_t const key = static_cast<uint64_t>(std::llabs(tile.id[ip]))
+            ^ (static_cast<uint64_t>(tile.cpu ? tile.cpu[ip] : 0) << 40);
+        uint64_t lineage = 0;
+        int current_process = 0;
+        double const weight = tile.w[ip];
+        double energy = std::sqrt(tile.ux[ip] * tile.ux[ip] + tile.uy[ip] * tile.uy[ip] + tile.uz[ip] * tile.uz[ip]);
+        double dx = tile.ux[ip], dy = tile.uy[ip], dz = tile.uz[ip];
+        normalize(dx, dy, dz);
+        if (tile.prev_r[ip] > rhi + 1.0e-9 * rhi || tile.prev_z[ip] < zlo - 1.0e-9
+            || tile.prev_z[ip] > zhi + 1.0e-9 * zhi) {
+            fail(RREA_GPU_ERR_GEOMETRY, "RREA photon survived outside the domain");
+        }
+        Path path = ClipRz(tile.prev_r[ip], tile.prev_theta[ip], tile.prev_z[ip], tile.r[ip], tile.theta[ip],
+                           tile.z[ip], rlo, rhi, zlo, zhi, periodic);
+        uint64_t ordinal = 0;
+        double elapsed_start = 0.0;
+        auto push_source = [&](int kind, double r, double z, double w, double sec, double loss) {
+            cout.sources.push_back(Source{kind, r, z, w, sec, loss, ip});
+        };
+        auto deposit_local_at = [&](double r, double z, double w, double e) {
+            if (w <= 0.0 || e <= 0.0) return;
+            double const pw = w * e / std::max(w_air, 1.0);
+            if (pw <= 0.0) return;
+            push_source(0, r, z, pw, 0.0, w_air);
+        };
+        auto add_secondary = [&](int species, double x, double y, double z, double sx, double sy, double sz, double e,
+                                 double birth) {
+            Secondary s2;
+            s2.species = species;
+            s2.process = current_process;
+            s2.x = x; s2.y = y; s2.z = z;
+            s2.dx = sx; s2.dy = sy; s2.dz = sz;
+            s2.w = weight;
+            s2.energy = e;
+            s2.birth = birth;
+            s2.root_key = key;
+            s2.lineage = lineage++;
+            s2.root_species = 2;
+            s2.parent_index = ip;
+            cout.secondaries.push_back(s2);
+        };
+        int disp = 0;
+        for (;;) {
+            if (ordinal >= kEventCap) fail(RREA_GPU_ERR_RNG_OVERFLOW, "photon event ordinal overflow");
+            EscapePolicy const esc = clipped_escape_policy(path, std::hypot(path.ex, path.ey), path.ez);
+            double const ds = path.in_length;
+            std::vector<Interval> const iv = build_intervals(path, density_ratio, density_ratio);
+            double const chord_dpath = density_path(iv, path, path.in_begin, path.in_end);
+            if (weight <= 0.0 || energy < photon_cut) {
+                double x, y, z;
+                path.PointAtFull(path.in_begin, x, y, z);
+                current_process = 12;
+                deposit_local_at(std::hypot(x, y), z, std::max(weight, 0.0), energy);
+                tile.id[ip] = -tile.id[ip];
+                disp = 2;
+                break;
+            }
+            auto commit_no_event = [&]() {
+                double x, y, z;
+                path.PointAtFull(path.in_end, x, y, z);
+                tile.r[ip] = std::hypot(x, y);
+                tile.theta[ip] = std::atan2(y, x);
+                tile.z[ip] = path.WrapZ(z);
+                if (!esc.escapes) return 0;
+                if (esc.invalidate) tile.id[ip] = -tile.id[ip];
+                return 1;
+            };
+            if (ds <= 0.0) {
+                disp = commit_no_event();
+                break;
+            }
+            PhotonRates const rates = photon_rates(tables, energy, 1.0);
+            double const mfp = Tables::mfp_from_inverse(rates.total());
+            double const tau = chord_dpath / mfp;
+            uint64_t idx;
+            if (!try_live_hazard_index(2, 0, ordinal, idx)) fail(RREA_GPU_ERR_RNG_OVERFLOW, "photon RNG index");
+            out_events[sp] += 1;
+            double const u_int = rng_uniform(seed, key, step_key, idx, ordinal == 0 ? 51 : 128);
+            Selection const sel = select_hazard({tau, 0.0, 0.0}, 1, u_int, 0.0);
+            if (!sel.valid || !sel.event) {
+                if (!sel.valid) fail(RREA_GPU_ERR_INVALID_STATE, "photon hazard selection invalid");
+                disp = commit_no_event();
+                break;
+            }
+            double const f = fraction_at_density_path(iv, path, path.in_begin, path.in_end, sel.sampled * mfp);
+            if (!(std::isfinite(f) && f >= path.in_begin && f <= path.in_end && path.in_end > path.in_begin)) {
+                fail(RREA_GPU_ERR_INVALID_STATE, "photon event depth outside its chord");
+            }
+            double const dist = path.full * (f - path.in_begin);
+            double px, py, pz;
+            path.PointAtFull(f, px, py, pz);
+            double const remaining = std::max(0.0, path.full - dist);
+            double const birth =
+                std::min(1.0, elapsed_start + dist / std::max(kC * dt_s, std::numeric_limits<double>::min()));
+            double const pr = std::hypot(px, py);
+            int const channel = sample_photon_channel(
+                tables, energy, rng_uniform(seed, key, step_key, idx, ordinal == 0 ? 52 : 129));
+            auto R = [&](uint64_t ch) { return rng_uniform(seed, key, step_key, idx, ch); };
+            bool repeat = false;
+            Path next;
+            if (channel == 0) {
+                // RreaApplyComptonFinalState, O/RreaPhotonFinalStates.H:56-147
+                current_process = 5;
+                double const inc = energy;
+                ComptonState const cs = sample_klein_nishina(tables, inc, R(53), R(54));
+                double sx, sy, sz;
+                cone_direction(dx, dy, dz, cs.cos_theta, R(58), sx, sy, sz);
+                double rx = inc * dx - cs.scattered * sx, ry = inc * dy - cs.scattered * sy,
+                       rz = inc * dz - cs.scattered * sz;
+                normalize(rx, ry, rz);
+                if (cs.recoil >= cutoff) {
+                    add_secondary(0, px, py, pz, rx, ry, rz, cs.recoil, birth);
+                    push_source(0, pr, pz, weight, cs.recoil, cs.recoil);
+                } else {
+                    push_source(0, pr, pz, weight, cs.recoil, 0.0);
+                    deposit_local_at(pr, pz, weight, cs.recoil);
+                }
+                energy = cs.scattered;
+                if (energy < photon_cut) {
+                    deposit_local_at(pr, pz, weight, energy);
+                    tile.id[ip] = -tile.id[ip];
+                    disp = 2;
+                } else {
+                    dx = sx; dy = sy; dz = sz;
+                    tile.ux[ip] = energy * dx;
+                    tile.uy[ip] = energy * dy;
+                    tile.uz[ip] = energy * dz;
+                    double const xt = px + dx * remaining, yt = py + dy * remaining, zt = pz + dz * remaining;
+                    next = ClipRz(pr, std::atan2(py, px), pz, std::hypot(xt, yt), std::atan2(yt, xt), zt, rlo, rhi, zlo,
+                                  zhi, periodic);
+                    double nx, ny, nz;
+                    next.PointAtFull(next.in_end, nx, ny, nz);
+                    tile.r[ip] = std::hypot(nx, ny);
+                    tile.theta[ip] = std::atan2(ny, nx);
+                    tile.z[ip] = next.WrapZ(nz);
+                    repeat = remaining > 0.0;
+                    disp = 0;
+                }
+            } else if (channel == 1) {
+                // RreaApplyPhotoelectricFinalState, O/RreaPhotonFinalStates.H:160-224
+                current_process = 6;
+                double pe_e, bind;
+                sample_photoelectric(tables, energy, R(55), pe_e, bind);
+                double const ee = std::min(pe_e, energy);
+                if (ee >= cutoff) {
+                    double ex, ey, ez;
+                    cone_direction(dx, dy, dz, sample_photoelectron_cos(tables, ee, R(60)), R(65), ex, ey, ez);
+                    add_secondary(0, px, py, pz, ex, ey, ez, ee, birth);
+                    push_source(0, pr, pz, weight, ee, ee);
+                } else {
+                    push_source(0, pr, pz, weight, ee, 0.0);
+                    deposit_local_at(pr, pz, weight, ee);
+                }
+                if (bind > 0.0) deposit_local_at(pr, pz, weight, bind);
+                tile.id[ip] = -tile.id[ip];
+                disp = 2;
+            } else {
+                // RreaApplyPairFinalState, O/RreaPhotonFinalStates.H:239-365
+                bool const triplet = channel == 3;
+                current_process = triplet ? 8 : 7;
+                PairState const ps = sample_pair(tables, energy, channel, R(66), R(57), R(59));
+                if (!ps.valid) fail(RREA_GPU_ERR_INVALID_STATE, "pair channel without phase space");
+                double edx, edy, edz, pdx, pdy, pdz;
+                rotate_to_axis(dx, dy, dz, ps.edir[0], ps.edir[1], ps.edir[2], edx, edy, edz);
+                rotate_to_axis(dx, dy, dz, ps.pdir[0], ps.pdir[1], ps.pdir[2], pdx, pdy, pdz);
+                if (ps.e_electron >= cutoff) {
+                    add_secondary(0, px, py, pz, edx, edy, edz, ps.e_electron, birth);
+                } else {
+                    push_source(1, pr, pz, weight, 0.0, 0.0);
+                    deposit_local_at(pr, pz, weight, ps.e_electron);
+                }
+                if (ps.e_positron >= cutoff) {
+                    add_secondary(1, px, py, pz, pdx, pdy, pdz, ps.e_positron, birth);
+                } else {
+                    // spawn_positron_annihilation at rest, O/RreaTransportStep.H:563-702
+                    double ax = pdx, ay = pdy, az = pdz;
+                    normalize(ax, ay, az);
+                    AnnihilationState const an = sample_annihilation(tables, 0.0, R(80), R(81));
+                    double g1x, g1y, g1z;
+                    cone_direction(ax, ay, az, an.cos1, an.azim, g1x, g1y, g1z);
+                    double const e1 = std::max(an.e1, 0.0), e2 = std::max(an.e2, 0.0);
+                    double g2x = -g1x, g2y = -g1y, g2z = -g1z;
+                    double local = 0.0;
+                    // the annihilation photons join the pair's transaction group
+                    if (e1 >= photon_cut) add_secondary(2, px, py, pz, g1x, g1y, g1z, e1, birth);
+                    else local += e1;
+                    if (e2 >= photon_cut) add_secondary(2, px, py, pz, g2x, g2y, g2z, e2, birth);
+                    else local += e2;
+                    if (ps.e_positron > 0.0) deposit_local_at(pr, pz, weight, ps.e_positron);
+                    if (local > 0.0) deposit_local_at(pr, pz, weight, local);
+                    push_source(2, pr, pz, weight, 0.0, 0.0);
+                }
+                if (ps.recoil) {
+                    double rdx, rdy, rdz;
+                    rotate_to_axis(dx, dy, dz, ps.rdir[0], ps.rdir[1], ps.rdir[2], rdx, rdy, rdz);
+                    if (ps.e_recoil >= cutoff) add_secondary(0, px, py, pz, rdx, rdy, rdz, ps.e_recoil, birth);
+                    push_source(0, pr, pz, weight, ps.e_recoil, 0.0);
+                    if (ps.e_recoil < cutoff) deposit_local_at(pr, pz, weight, ps.e_recoil);
+                }
+                if (ps.local > 0.0) deposit_local_at(pr, pz, weight, ps.local);
+                tile.id[ip] = -tile.id[ip];
+                disp = 2;
+            }
+            if (repeat) {
+                path = next;
+                elapsed_start = birth;
+                ++ordinal;
+                continue;
+            }
+            break;
+        }
+        out_disposition[sp] = disp;
+      }
+      } catch (OracleError const& e) {
+        chunk_err[static_cast<std::size_t>(chunk)] = e.code;
+        chunk_msg[static_cast<std::size_t>(chunk)] = e.what();
+      }
+    }
+    for (int64_t chunk = 0; chunk < n_chunks; ++chunk) {
+        if (chunk_err[static_cast<std::size_t>(chunk)] != 0) {
+            fail(chunk_err[static_cast<std::size_t>(chunk)], chunk_msg[static_cast<std::size_t>(chunk)]);
+        }
+    }
+    for (auto& c : chunk_out) {
+        out.secondaries.insert(out.secondaries.end(), c.secondaries.begin(), c.secondaries.end());
+        out.sources.insert(out.sources.end(), c.sources.begin(), c.sources.end());
+    }
+}
+
 // Primitive-level entry points, one row of inputs per call, matching the
 // golden fixtures written by oracle/ref_golden.cpp.
 int RunPrimitive(TableSet const& ts, int which, double const* in, int64_t n, double* out)
@@ -1634,6 +2260,33 @@ int RunPrimitive(TableSet const& ts, int which, double const* in, int64_t n, dou
             o[14] = np > 0 ? p.pieces[0].shift : 0.0;
             o[15] = np > 0 ? p.pieces.back().begin : -1.0;
             o[16] = np > 0 ? p.pieces.back().shift : 0.0;
+            break;
+        }
+        case 16: out[i] = sample_photon_channel(t, in[2 * i], in[2 * i + 1]); break;
+        case 17: {  // (e, draw_mu, draw_accept) -> recoil, scattered, cos
+            double const* a = in + 3 * i;
+            ComptonState const c = sample_klein_nishina(t, a[0], a[1], a[2]);
+            out[3 * i] = c.recoil; out[3 * i + 1] = c.scattered; out[3 * i + 2] = c.cos_theta;
+            break;
+        }
+        case 18: {  // (e, u) -> electron, binding
+            sample_photoelectric(t, in[2 * i], in[2 * i + 1], out[2 * i], out[2 * i + 1]);
+            break;
+        }
+        case 19: out[i] = sample_photoelectron_cos(t, in[2 * i], in[2 * i + 1]); break;
+        case 20: {  // (e, channel, inv, polar, azim) -> valid, ee, ep, er, local, 9 dirs
+            double const* a = in + 5 * i;
+            PairState const p = sample_pair(t, a[0], static_cast<int>(a[1]), a[2], a[3], a[4]);
+            double* o = out + 14 * i;
+            o[0] = p.valid; o[1] = p.e_electron; o[2] = p.e_positron; o[3] = p.e_recoil; o[4] = p.local;
+            for (int c = 0; c < 3; ++c) { o[5 + c] = p.edir[c]; o[8 + c] = p.pdir[c]; o[11 + c] = p.rdir[c]; }
+            break;
+        }
+        case 21: {  // (k, d_energy, d_azim) -> e1, e2, cos1, azim, valid, at_rest
+            double const* a = in + 3 * i;
+            AnnihilationState const an = sample_annihilation(t, a[0], a[1], a[2]);
+            double* o = out + 6 * i;
+            o[0] = an.e1; o[1] = an.e2; o[2] = an.cos1; o[3] = an.azim; o[4] = an.valid; o[5] = an.at_rest;
             break;
         }
         default:

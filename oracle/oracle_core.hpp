@@ -177,6 +177,11 @@ void ApplyElectronTransport(rrea_host::TableSet const& tables, rrea_gpu_config c
                             FieldGrid const& field, int step, double dt_s, ChargedTile& tile,
                             StepOutputs& out);
 
+// Photon phase of one step (O/RreaPhotonTransport.cpp:9-461) over one tile:
+// prev_* is the captured start, (r, theta, z) the straight-push endpoint.
+void ApplyPhotonTransport(rrea_host::TableSet const& tables, rrea_gpu_config const& cfg, int step, double dt_s,
+                          ChargedTile& tile, StepOutputs& out);
+
 // Primitive-level evaluation for fixture comparisons (ids listed in oracle_core.cpp).
 int RunPrimitive(rrea_host::TableSet const& tables, int which, double const* in, int64_t n, double* out);
 

@@ -325,6 +325,46 @@ int main(int argc, char** argv)
             }
             write_f8("ref_chord", 26, chord);
         }
+        // ---- photon samplers: S/RreaInteractionTables.cpp:2778-3253
+        {
+            std::vector<double> chan, kn, pe, pec, pair, ann;
+            for (int i = 0; i < 3000; ++i) {
+                double const e = (i % 10 == 0) ? g.logu(1.0e3, 2.0e4) : g.logu(1.0e3, 1.0e11);
+                double const u = g.uni();
+                chan.insert(chan.end(), {e, u, static_cast<double>(static_cast<int>(tables.SamplePhotonChannel(e, u)))});
+                double const ek = g.logu(5.0e4, 1.0e9), u1 = g.uni(), u2 = g.uni();
+                auto const c = tables.SampleComptonKleinNishinaFinalState(ek, u1, u2);
+                kn.insert(kn.end(), {ek, u1, u2, c.recoil_electron_energy_eV, c.scattered_photon_energy_eV, c.cos_theta});
+                double const ep = (i % 7 == 0) ? g.logu(1.0e3, 5.0e3) : g.logu(1.0e3, 1.0e11);
+                auto const p = tables.SamplePhotoelectricFinalState(ep, u);
+                pe.insert(pe.end(), {ep, u, p.photoelectron_energy_eV, p.binding_energy_eV});
+                double const kk = (i % 13 == 0) ? g.logu(1.0e3, 1.2e3) : g.logu(1.0e3, 1.0e10);
+                double const up = (i % 29 == 0) ? 0.0 : g.uni();
+                pec.insert(pec.end(), {kk, up, tables.SamplePhotoelectronCosTheta(kk, up)});
+                double const eg = (i % 9 == 0) ? g.logu(1.0e6, 3.0e6) : g.logu(2.1e6, 1.0e11);
+                int const ch = (i % 2 == 0) ? 2 : 3;
+                double const d1 = g.uni(), d2 = g.uni(), d3 = g.uni();
+                auto const pr = tables.SamplePairFinalState(eg, static_cast<rrea::RreaPhotonChannel>(ch), d1, d2, d3,
+                                                            0.5, 0.5);
+                pair.insert(pair.end(), {eg, static_cast<double>(ch), d1, d2, d3, static_cast<double>(pr.valid),
+                                         pr.electron_energy_eV, pr.positron_energy_eV, pr.recoil_electron_energy_eV,
+                                         pr.local_deposit_energy_eV, pr.electron_dir_x, pr.electron_dir_y,
+                                         pr.electron_dir_z, pr.positron_dir_x, pr.positron_dir_y, pr.positron_dir_z,
+                                         pr.recoil_dir_x, pr.recoil_dir_y, pr.recoil_dir_z});
+                double const ka = (i % 5 == 0) ? 0.0 : g.logu(1.0e3, 1.0e9);
+                double const a1 = g.uni(), a2 = g.uni() * 3.0 - 1.0;
+                auto const an = tables.SamplePositronAnnihilationFinalState(ka, a1, a2);
+                ann.insert(ann.end(), {ka, a1, a2, an.photon1_energy_eV, an.photon2_energy_eV, an.photon1_cos_theta,
+                                       an.photon1_azimuth_u, static_cast<double>(an.valid),
+                                       static_cast<double>(an.at_rest)});
+            }
+            write_f8("ref_photon_channel", 3, chan);
+            write_f8("ref_klein_nishina", 6, kn);
+            write_f8("ref_photoelectric", 4, pe);
+            write_f8("ref_photoelectron_cos", 3, pec);
+            write_f8("ref_pair", 19, pair);
+            write_f8("ref_annihilation", 9, ann);
+        }
         std::printf("golden fixtures written to %s\n", g_outdir.c_str());
     } catch (std::exception const& e) {
         std::fprintf(stderr, "ref_golden failed: %s\n", e.what());

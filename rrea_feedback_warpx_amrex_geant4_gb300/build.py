@@ -18,6 +18,7 @@ LIB = os.path.join(LIBDIR, "librrea_gpu.so")
 SOURCES = [
     os.path.join(CSRC, "rrea_capi.cu"),
     os.path.join(CSRC, "rrea_kernels.cu"),
+    os.path.join(CSRC, "rrea_photon_kernels.cu"),
     os.path.join(CSRC, "host", "table_set.cpp"),
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -12,111 +12,11 @@
 //   * tallies      -> not kept (diagnostic ledger only).
 #pragma once
 
-#include "rrea_device_path.cuh"
-#include "rrea_electron_args.cuh"
+#include "rrea_sinks.cuh"
 
 namespace rrea_dev {
 
 
-
-// Order-1 cell deposit (S/RreaEventAccumulator.cpp:386-502, field ids of
-// :129-164) for the uniform RZ grid with r_lo on the axis.  One source feeds
-// up to four fields at the same point, so its stencil (containing cell,
-// order-1 weights, axis fold) is built once and applied to each value.
-struct CellStencil {
-    bool valid;
-    int i[2], j[2];
-    bool use_i[2], use_j[2];
-    double wr[2], wz[2];
-};
-
-__device__ __forceinline__ CellStencil make_stencil(StepConstants const& C, double r, double z)
-{
-    CellStencil st;
-    rrea_gpu_config const& cfg = C.cfg;
-    int const nr = cfg.nr, nz = cfg.nz;
-    double zz = z;
-    if (cfg.periodic_z) {
-        double const len = cfg.z_hi - cfg.z_lo;
-        double s = fmod(zz - cfg.z_lo, len);
-        if (s < 0.0) s += len;
-        zz = cfg.z_lo + s;
-    }
-    double const fr = quot(r - cfg.r_lo, C.div_dr);
-    double const fz = quot(zz - cfg.z_lo, C.div_dz);
-    int const ic = static_cast<int>(floor(fr));
-    int const jc = static_cast<int>(floor(fz));
-    st.valid = !(ic < 0 || ic >= nr || jc < 0 || jc >= nz);
-    if (!st.valid) return st;
-    double const rc = fr + 0.0 - 0.5;
-    int const i0 = static_cast<int>(floor(rc));
-    st.wr[1] = rc - i0;
-    st.wr[0] = 1.0 - st.wr[1];
-    double const zc = fz + 0.0 - 0.5;
-    int const j0 = static_cast<int>(floor(zc));
-    st.wz[1] = zc - j0;
-    st.wz[0] = 1.0 - st.wz[1];
-#pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        int j = j0 + a;
-        st.use_j[a] = true;
-        if (j < 0 || j > nz - 1) {
-            if (cfg.periodic_z) j = ((j % nz) + nz) % nz;
-            else st.use_j[a] = false;
-        }
-        st.j[a] = j;
-        int i = i0 + a;
-        st.use_i[a] = true;
-        if (i < 0 || i > nr - 1) {
-            if (i == -1 && cfg.r_lo == 0.0) i = 0;
-            else st.use_i[a] = false;
-        }
-        st.i[a] = i;
-    }
-    return st;
-}
-
-__device__ __forceinline__ void stencil_add(StepConstants const& C, double* __restrict__ cells, CellStencil const& st,
-                                            int field, double value)
-{
-    if (!st.valid || !isfinite(value) || value == 0.0) return;
-    int const nr = C.cfg.nr;
-    double* grid = cells + static_cast<size_t>(field) * nr * C.cfg.nz;
-#pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        double const wz = st.wz[a];
-        if (wz == 0.0 || !st.use_j[a]) continue;
-#pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            double const v = value * st.wr[b] * wz;
-            if (v == 0.0 || !st.use_i[b] || !isfinite(v)) continue;
-            atomicAdd(grid + st.i[b] + static_cast<size_t>(nr) * st.j[a], v);
-        }
-    }
-}
-
-// O/RreaCouplingSources.cpp:435-512
-__device__ __forceinline__ void deposit_source(StepConstants const& C, double* __restrict__ cells, int kind,
-                                               double r, double z, double w, double sec_e, double loss)
-{
-    if (w <= 0.0) return;
-    CellStencil const st = make_stencil(C, r, z);
-    if (!st.valid) return;
-    if (kind == 0) {  // AccumulateIonizationEvent
-        stencil_add(C, cells, st, 1, w);
-        if (sec_e < C.cfg.low_energy_cutoff_eV) stencil_add(C, cells, st, 0, w);
-        stencil_add(C, cells, st, 3, w);
-        stencil_add(C, cells, st, 4, fmax(w, 0.0) * fmax(loss, 0.0));
-    } else if (kind == 1) {  // AccumulateLowEnergyElectron
-        stencil_add(C, cells, st, 0, w);
-        stencil_add(C, cells, st, 3, w);
-        stencil_add(C, cells, st, 4, fmax(w, 0.0) * fmax(fmax(loss, 0.0), 0.0));
-    } else {  // AccumulatePositiveIonSourceOnly
-        stencil_add(C, cells, st, 1, w);
-        stencil_add(C, cells, st, 3, w);
-        stencil_add(C, cells, st, 4, fmax(w, 0.0) * fmax(loss, 0.0));
-    }
-}
 
 // The electron coefficient tables (collision, soft radiative, hard-Moller
 // and tracked-brems rates) share one bit-identical 2856-row energy grid in
@@ -279,42 +179,6 @@ __device__ __forceinline__ double sample_brems_cos(StepConstants const& C, doubl
     }
     double const f = 0.5 * (lo + hi) / umax;
     return 1.0 - 2.0 * f * f;
-}
-
-__device__ __forceinline__ void record_failure(ElectronArgs const& A, int code, int64_t ip)
-{
-    if (atomicCAS(A.status, 0, code) == 0) {
-        *A.fail_index = static_cast<long long>(ip);
-    }
-}
-
-// TransportSideEffects::AddSecondary (O/RreaTransportLog.H:437-447): the
-// record carries the parent's RNG key and its per-parent lineage counter.
-__device__ __forceinline__ void append_secondary(ElectronArgs const& A, int64_t ip, uint64_t key, double weight,
-                                                 uint32_t& lineage, int species, int process, double x, double y,
-                                                 double z, double sx, double sy, double sz, double e, double birth,
-                                                 Err& err)
-{
-    unsigned long long const slot = atomicAdd(A.sec_count, 1ULL);
-    if (slot < static_cast<unsigned long long>(A.sec_capacity)) {
-        rrea_gpu_secondary s;
-        s.species = species;
-        s.process = process;
-        s.root_species = 0;
-        s.pad = 0;
-        s.parent_index = ip;
-        s.root_key = key;
-        s.lineage = lineage;
-        s.x = x; s.y = y; s.z = z;
-        s.dir_x = sx; s.dir_y = sy; s.dir_z = sz;
-        s.weight = weight;
-        s.energy_eV = e;
-        s.birth_fraction = birth;
-        A.sec[slot] = s;
-    } else {
-        err.set(RREA_GPU_ERR_CAPACITY);
-    }
-    ++lineage;
 }
 
 // Interaction site of one discrete event (RreaInteractionSite,

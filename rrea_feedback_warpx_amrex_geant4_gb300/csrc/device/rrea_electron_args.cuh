@@ -1,5 +1,6 @@
-// Arguments of the electron transport kernel: the species tile (SoA in
-// HBM), the per-step output sinks and the field view.  Shared by the kernel
+// Arguments of the species transport kernels (electron and photon phases):
+// the species tile (SoA in HBM), the per-step output sinks and the field
+// view (unused by the photon phase).  Shared by the kernel
 // translation unit and the host-side launcher.
 #pragma once
 
@@ -44,6 +45,9 @@ struct ElectronArgs {
     unsigned long long* __restrict__ transported;
     const double* __restrict__ arena;
     FieldView fv;
+    // photon phase only: 1 = push each photon straight by c*dt from its
+    // current state before transporting the chord (resident mode)
+    int32_t straight_push;
 };
 
 }  // namespace rrea_dev

@@ -13,6 +13,8 @@
 #include <utility>
 #include <vector>
 
+#include <cstdint>
+
 namespace rrea_host {
 
 namespace {
@@ -199,6 +201,8 @@ void TableSet::Load(std::string const& config_path)
         "positron_brems_photon_energy_cdf_air",
     };
 
+    std::vector<double> pe_primary, pe_prob_sum;
+    std::vector<std::vector<double>> pe_rows_u, pe_rows_b;
     std::map<std::string, Table1D> tables;
     std::map<std::string, CondGroups> cdfs;
     std::map<std::string, Angle> angles;
@@ -236,7 +240,46 @@ void TableSet::Load(std::string const& config_path)
             continue;
         }
         if (kind == "photoelectric_subshell_cdf") {
-            continue;  // photon final states load this separately
+            // S/RreaInteractionTables.cpp:893-987
+            auto const c = ReadRreaTableContainer(path);
+            auto const prim = c.column("primary_energy_eV");
+            auto const cdf = c.column("cdf_u");
+            auto const prob = c.column("subshell_probability");
+            auto const bind = c.column("binding_energy_eV");
+            auto const relax = c.column("relaxation_energy_eV");
+            pe_primary.clear();
+            pe_rows_u.clear();
+            pe_rows_b.clear();
+            for (std::size_t i = 0; i < prim.size(); ++i) {
+                if (!(prim[i] > 0.0) || bind[i] < 0.0 || relax[i] < 0.0
+                    || relax[i] > bind[i] * (1.0 + 1.0e-9) || bind[i] > prim[i] || cdf[i] < 0.0 || cdf[i] > 1.0
+                    || prob[i] < 0.0) {
+                    throw std::runtime_error("invalid photoelectric subshell row");
+                }
+                bool const reset = !pe_primary.empty() && pe_primary.back() == prim[i] && !pe_rows_u.back().empty()
+                    && cdf[i] <= pe_rows_u.back().back();
+                if (pe_primary.empty() || pe_primary.back() != prim[i] || reset) {
+                    if (!pe_primary.empty() && prim[i] < pe_primary.back()) {
+                        throw std::runtime_error("photoelectric groups must be nondecreasing");
+                    }
+                    pe_primary.push_back(prim[i]);
+                    pe_rows_u.emplace_back();
+                    pe_rows_b.emplace_back();
+                    pe_prob_sum.push_back(0.0);
+                }
+                if (!pe_rows_u.back().empty() && cdf[i] <= pe_rows_u.back().back()) {
+                    throw std::runtime_error("photoelectric CDF not increasing within a group");
+                }
+                pe_rows_u.back().push_back(cdf[i]);
+                pe_rows_b.back().push_back(bind[i]);
+                pe_prob_sum.back() += prob[i];
+            }
+            for (std::size_t g = 0; g < pe_primary.size(); ++g) {
+                if (std::abs(pe_rows_u[g].back() - 1.0) > 1.0e-12 || std::abs(pe_prob_sum[g] - 1.0) > 1.0e-10) {
+                    throw std::runtime_error("photoelectric subshell group does not close at 1");
+                }
+            }
+            continue;
         }
         std::string x_column = obj.str_or("x_column", "energy_eV");
         std::string value_column = obj.str_or("value_column", "");
@@ -444,8 +487,165 @@ void TableSet::Load(std::string const& config_path)
         }
         m_index.hard_moller_mean_secondary = push(mean);
     }
+    // Photoelectric subshell CDF.
+    {
+        if (pe_primary.size() < 2 || pe_primary.front() != m_index.photon_min_eV
+            || pe_primary.back() != m_index.photon_max_eV) {
+            throw std::runtime_error("photoelectric subshell CDF must cover the photon range");
+        }
+        RreaPhotoelectricIndex& pi = m_index.pe;
+        pi.ng = static_cast<int32_t>(pe_primary.size());
+        pi.primary = push(pe_primary);
+        std::vector<double> start(pe_primary.size() + 1), u, b;
+        for (std::size_t g = 0; g < pe_primary.size(); ++g) {
+            start[g] = static_cast<double>(u.size());
+            u.insert(u.end(), pe_rows_u[g].begin(), pe_rows_u[g].end());
+            b.insert(b.end(), pe_rows_b[g].begin(), pe_rows_b[g].end());
+        }
+        start.back() = static_cast<double>(u.size());
+        pi.total = static_cast<int32_t>(u.size());
+        pi.start = push(start);
+        pi.u = push(u);
+        pi.binding = push(b);
+    }
+    LoadPairBank(dir + "/final_state/pair_final_state_samples_air.bin.rtb",
+                 dir + "/final_state/pair_final_state_samples_air.index.json");
     m_index.total_doubles = static_cast<int64_t>(m_arena.size());
     m_loaded = true;
+}
+
+// Training split of the correlated pair bank with its record contract
+// (S/RreaInteractionTables.cpp:1123-1370).
+void TableSet::LoadPairBank(std::string const& bin_path, std::string const& index_path)
+{
+    auto const bank = ReadRreaTableContainer(bin_path);
+    if (bank.header.str_or("kind", "") != "records" || bank.header.str_or("record_bytes", "") != "144") {
+        throw std::runtime_error("pair final-state container is not a 144-byte record set");
+    }
+    auto const target_z = bank.column("target_Z");
+    auto const channel_code = bank.column("channel_code");
+    auto const lepton_count = bank.column("lepton_count");
+    auto const flags = bank.column("flags");
+    auto const primary = bank.column("primary_energy_eV");
+    auto const recoil = bank.column("local_recoil_fraction");
+    std::vector<double> pdg[3], reserved[3], frac[3], dxs[3], dys[3], dzs[3];
+    for (int slot = 0; slot < 3; ++slot) {
+        std::string const p = "p" + std::to_string(slot) + "_";
+        pdg[slot] = bank.column(p + "pdg");
+        reserved[slot] = bank.column(p + "reserved");
+        frac[slot] = bank.column(p + "kinetic_fraction");
+        dxs[slot] = bank.column(p + "dir_x");
+        dys[slot] = bank.column(p + "dir_y");
+        dzs[slot] = bank.column(p + "dir_z");
+    }
+    std::size_t const rows = bank.rows();
+    JsonValue const index = ParseJson(read_text(index_path));
+    if (JsonValue const* failures = index.find("failures")) {
+        if (!failures->items.empty()) throw std::runtime_error("pair index reports producer failures");
+    }
+    struct Block {
+        int channel;
+        double energy;
+        std::size_t offset, count;
+    };
+    std::vector<Block> blocks;
+    std::vector<std::pair<std::size_t, std::size_t>> ranges;
+    for (auto const& b : index.at("blocks").items) {
+        std::string const split = b.str("split");
+        std::string const ch = b.str("channel");
+        int const channel = ch == "nuclear" ? 0 : (ch == "triplet" ? 1 : -1);
+        if (channel < 0) throw std::runtime_error("unknown pair channel " + ch);
+        double const energy = b.at("primary_energy_eV").num();
+        std::size_t const byte_offset = static_cast<std::size_t>(b.at("byte_offset").num());
+        std::size_t const offset = static_cast<std::size_t>(b.at("record_offset").num());
+        std::size_t const count = static_cast<std::size_t>(b.at("count").num());
+        if (!(energy > 0.0) || offset > rows || count > rows - offset || byte_offset != 64 + offset * 144) {
+            throw std::runtime_error("pair index block has invalid offset/count");
+        }
+        if (count > 0) ranges.emplace_back(offset, offset + count);
+        if (split != "training") {
+            if (split != "holdout") throw std::runtime_error("pair split must be training or holdout");
+            continue;
+        }
+        if (count == 0) continue;
+        if (count < 4096) throw std::runtime_error("pair training block has fewer than 4096 records");
+        blocks.push_back(Block{channel, energy, offset, count});
+    }
+    std::sort(ranges.begin(), ranges.end());
+    std::size_t next = 0;
+    for (auto const& r : ranges) {
+        if (r.first != next) throw std::runtime_error("pair index blocks overlap or leave a gap");
+        next = r.second;
+    }
+    if (next != rows) throw std::runtime_error("pair index does not cover the bank");
+    std::stable_sort(blocks.begin(), blocks.end(), [](Block const& a, Block const& b) {
+        return a.channel != b.channel ? a.channel < b.channel : a.energy < b.energy;
+    });
+    double const closure_tol = 64.0 * 2.220446049250313080847263336181640625e-16;
+    for (int channel = 0; channel < 2; ++channel) {
+        std::vector<double> energies, starts, recs;
+        double last = 0.0;
+        for (Block const& b : blocks) {
+            if (b.channel != channel) continue;
+            if (!(b.energy > last)) throw std::runtime_error("pair training energies not increasing");
+            last = b.energy;
+            energies.push_back(b.energy);
+            starts.push_back(static_cast<double>(recs.size() / RREA_PAIR_RECORD_DOUBLES));
+            int const expect = channel == 1 ? 3 : 2;
+            for (std::size_t i = 0; i < b.count; ++i) {
+                std::size_t const row = b.offset + i;
+                int const z = static_cast<int>(std::llround(target_z[row]));
+                auto const code = static_cast<uint32_t>(std::llround(channel_code[row]));
+                int const count = static_cast<int>(std::llround(lepton_count[row]));
+                auto const fl = static_cast<uint32_t>(std::llround(flags[row]));
+                int const rec_channel = code == 1u ? 0 : (code == 2u ? 1 : -1);
+                if ((z != 6 && z != 7 && z != 8 && z != 18) || (fl & 1u) == 0u || (fl & ~3u) != 0u
+                    || rec_channel != channel || count != expect
+                    || std::abs(primary[row] - b.energy) > 1.0e-12 * b.energy || recoil[row] < 0.0
+                    || recoil[row] > 1.0) {
+                    throw std::runtime_error("pair final-state record metadata is invalid");
+                }
+                double fsum = recoil[row];
+                int ne = 0, np = 0;
+                for (int slot = 0; slot < 3; ++slot) {
+                    if (std::llround(reserved[slot][row]) != 0) throw std::runtime_error("pair reserved word set");
+                    if (slot < expect) {
+                        double const n = std::sqrt(dxs[slot][row] * dxs[slot][row] + dys[slot][row] * dys[slot][row]
+                                                   + dzs[slot][row] * dzs[slot][row]);
+                        if (frac[slot][row] < 0.0 || std::abs(n - 1.0) > 1.0e-8) {
+                            throw std::runtime_error("pair particle record invalid");
+                        }
+                        fsum += frac[slot][row];
+                        long const pd = std::llround(pdg[slot][row]);
+                        ne += pd == 11 ? 1 : 0;
+                        np += pd == -11 ? 1 : 0;
+                    } else if (std::llround(pdg[slot][row]) != 0 || frac[slot][row] != 0.0 || dxs[slot][row] != 0.0
+                               || dys[slot][row] != 0.0 || dzs[slot][row] != 0.0) {
+                        throw std::runtime_error("pair unused slot not zero");
+                    }
+                }
+                if (ne != expect - 1 || np != 1 || std::abs(fsum - 1.0) > closure_tol) {
+                    throw std::runtime_error("pair record topology/closure invalid");
+                }
+                recs.push_back(static_cast<double>(count));
+                for (int slot = 0; slot < 3; ++slot) recs.push_back(static_cast<double>(std::llround(pdg[slot][row])));
+                for (int slot = 0; slot < 3; ++slot) recs.push_back(frac[slot][row]);
+                for (int slot = 0; slot < 3; ++slot) {
+                    recs.push_back(dxs[slot][row]);
+                    recs.push_back(dys[slot][row]);
+                    recs.push_back(dzs[slot][row]);
+                }
+            }
+        }
+        if (energies.size() < 2 || last < 1.0e11) throw std::runtime_error("pair training blocks do not cover 100 GeV");
+        starts.push_back(static_cast<double>(recs.size() / RREA_PAIR_RECORD_DOUBLES));
+        RreaPairBankIndex& pb = m_index.pair[channel];
+        pb.nb = static_cast<int32_t>(energies.size());
+        pb.primary = push(energies);
+        pb.lprimary = push_logs(energies, false);
+        pb.start = push(starts);
+        pb.records = push(recs);
+    }
 }
 
 // Conditional inverse-CDF sampling (RreaInteractionTables.cpp:995-1069 and the

@@ -34,6 +34,7 @@ public:
     double const* at(int64_t offset) const { return m_arena.data() + offset; }
 
 private:
+    void LoadPairBank(std::string const& bin_path, std::string const& index_path);
     int64_t push(std::vector<double> const& values);
     int64_t push_logs(std::vector<double> const& values, bool zero_for_nonpositive);
 

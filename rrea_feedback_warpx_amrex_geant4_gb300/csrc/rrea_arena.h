@@ -92,6 +92,33 @@ typedef struct {
     int64_t lomc;       // log(one_minus_cos)
 } RreaAngleIndex;
 
+// Photoelectric subshell CDF (S/RreaInteractionTables.cpp:893-987): groups
+// of (cdf_u, binding energy) rows per primary energy; duplicated edge
+// energies appear as two consecutive groups.
+typedef struct {
+    int32_t ng;
+    int32_t total;
+    int64_t primary;   // ng
+    int64_t start;     // ng+1 row offsets (exact integers)
+    int64_t u;         // rows: cumulative subshell probability
+    int64_t binding;   // rows: binding energy [eV]
+} RreaPhotoelectricIndex;
+
+// Correlated pair final-state bank, training split only
+// (S/RreaInteractionTables.cpp:1187-1370): blocks sorted by primary energy,
+// each a run of 16-double records
+//   [lepton_count, pdg0, pdg1, pdg2, frac0, frac1, frac2,
+//    dx0, dy0, dz0, dx1, dy1, dz1, dx2, dy2, dz2].
+#define RREA_PAIR_RECORD_DOUBLES 16
+typedef struct {
+    int32_t nb;
+    int32_t pad;
+    int64_t primary;   // nb block energies
+    int64_t lprimary;  // nb logs
+    int64_t start;     // nb+1 record offsets (exact integers)
+    int64_t records;   // records * RREA_PAIR_RECORD_DOUBLES
+} RreaPairBankIndex;
+
 typedef struct {
     RreaTable1DIndex hot[RREA_T_COUNT];
     RreaCondCdfIndex cdf[RREA_C_COUNT];
@@ -99,6 +126,8 @@ typedef struct {
     RreaAngleIndex gs[2];              // option4 GS, E <= transition
     RreaAngleIndex wentzel[2];         // WentzelVI, E > transition
     int64_t hard_moller_mean_secondary;  // on the hard-Moller rate grid
+    RreaPhotoelectricIndex pe;
+    RreaPairBankIndex pair[2];         // 0 nuclear, 1 triplet
     int64_t total_doubles;
     double charged_min_eV, charged_max_eV;
     double photon_min_eV, photon_max_eV;

@@ -68,8 +68,8 @@ struct rrea_gpu_ctx {
     int64_t last_transported = 0;
     int64_t last_secondaries = 0;
     int launch_threads = 128;
-    int launch_blocks_per_sm = 4;
-    int launch_min_blocks = 4;
+    int launch_blocks_per_sm = 5;
+    int launch_min_blocks = 5;
     bool diagnostics = true;
 
     std::string last_error;
@@ -340,9 +340,11 @@ rrea_gpu_status stage_tile(rrea_gpu_ctx* ctx, rrea_gpu_tile const* t)
     return RREA_GPU_OK;
 }
 
-// Launches the electron phase on the staged device tile.  `aliased` runs the
-// resident engine mode: the captured pre-push state is the current state.
-rrea_gpu_status launch_electrons(rrea_gpu_ctx* ctx, int32_t step, double dt_s, bool aliased)
+// Launches one species phase (RREA_SPECIES_ELECTRON or RREA_SPECIES_PHOTON)
+// on the staged device tile.  `aliased` runs the resident engine mode: the
+// captured pre-push state is the current state (for photons the kernel then
+// performs the straight push itself).
+rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, double dt_s, bool aliased)
 {
     if (!ctx->tables_loaded || !ctx->field_set) {
         return fail(ctx, RREA_GPU_ERR_NOT_READY, "tables and field must be set before a step");
@@ -404,13 +406,19 @@ rrea_gpu_status launch_electrons(rrea_gpu_ctx* ctx, int32_t step, double dt_s, b
     a.fv.z_lo = c.z_lo;
     a.fv.periodic = c.periodic_z != 0;
     a.fv.has_b = ctx->has_b;
+    a.straight_push = (species == RREA_SPECIES_PHOTON && aliased) ? 1 : 0;
     if (a.n > 0) {
         int64_t const want = (a.n + ctx->launch_threads - 1) / ctx->launch_threads;
         int64_t const cap = static_cast<int64_t>(ctx->num_sms) * ctx->launch_blocks_per_sm * (128 / ctx->launch_threads);
         int const blocks = static_cast<int>(want < cap ? want : cap);
         RREA_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
-        RREA_CUDA(ctx, rrea_launch::electron_step(a, blocks > 0 ? blocks : 1, ctx->launch_threads,
-                                                  ctx->launch_min_blocks, c.periodic_z != 0, ctx->stream));
+        if (species == RREA_SPECIES_PHOTON) {
+            RREA_CUDA(ctx, rrea_launch::photon_step(sc, a, blocks > 0 ? blocks : 1, ctx->launch_threads,
+                                                    c.periodic_z != 0, ctx->stream));
+        } else {
+            RREA_CUDA(ctx, rrea_launch::electron_step(a, blocks > 0 ? blocks : 1, ctx->launch_threads,
+                                                      ctx->launch_min_blocks, c.periodic_z != 0, ctx->stream));
+        }
         RREA_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
     }
     unsigned long long count = 0;
@@ -429,7 +437,8 @@ rrea_gpu_status launch_electrons(rrea_gpu_ctx* ctx, int32_t step, double dt_s, b
     if (a.n > 0) RREA_CUDA(ctx, cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev_start, ctx->ev_stop));
     if (status != 0) {
         return fail(ctx, static_cast<rrea_gpu_status>(status),
-                    "electron transport guard failed (status " + std::to_string(status) + ") at particle "
+                    std::string(species == RREA_SPECIES_PHOTON ? "photon" : "electron")
+                        + " transport guard failed (status " + std::to_string(status) + ") at particle "
                         + std::to_string(fail_index));
     }
     if (count > static_cast<unsigned long long>(ctx->sec_capacity)) {
@@ -456,19 +465,13 @@ rrea_gpu_status unstage_tile(rrea_gpu_ctx* ctx, rrea_gpu_tile* t)
     return RREA_GPU_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-rrea_gpu_status rrea_gpu_apply_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, int32_t step, double time_s,
-                                         double dt_s, rrea_gpu_secondary* secondaries, int64_t secondary_capacity,
-                                         int64_t* n_secondaries)
+rrea_gpu_status apply_phase(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile* tile, int32_t step, double dt_s,
+                            rrea_gpu_secondary* secondaries, int64_t secondary_capacity, int64_t* n_secondaries)
 {
-    (void)time_s;
     if (!ctx || !tile || tile->n < 0) return RREA_GPU_ERR_ARGUMENT;
     rrea_gpu_status s = stage_tile(ctx, tile);
     if (s != RREA_GPU_OK) return s;
-    s = launch_electrons(ctx, step, dt_s, /*aliased=*/false);
+    s = launch_phase(ctx, species, step, dt_s, /*aliased=*/false);
     if (s != RREA_GPU_OK) return s;
     if (n_secondaries) *n_secondaries = ctx->last_secondaries;
     if (secondaries && ctx->last_secondaries > secondary_capacity) {
@@ -483,6 +486,36 @@ rrea_gpu_status rrea_gpu_apply_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile,
     }
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RREA_GPU_OK;
+}
+
+rrea_gpu_status step_resident(rrea_gpu_ctx* ctx, int species, int32_t step, double dt_s, int64_t* n_secondaries)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_status const s = launch_phase(ctx, species, step, dt_s, /*aliased=*/true);
+    if (s != RREA_GPU_OK) return s;
+    if (n_secondaries) *n_secondaries = ctx->last_secondaries;
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rrea_gpu_status rrea_gpu_apply_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, int32_t step, double time_s,
+                                         double dt_s, rrea_gpu_secondary* secondaries, int64_t secondary_capacity,
+                                         int64_t* n_secondaries)
+{
+    (void)time_s;
+    return apply_phase(ctx, RREA_SPECIES_ELECTRON, tile, step, dt_s, secondaries, secondary_capacity, n_secondaries);
+}
+
+rrea_gpu_status rrea_gpu_apply_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, int32_t step, double time_s,
+                                       double dt_s, rrea_gpu_secondary* secondaries, int64_t secondary_capacity,
+                                       int64_t* n_secondaries)
+{
+    (void)time_s;
+    return apply_phase(ctx, RREA_SPECIES_PHOTON, tile, step, dt_s, secondaries, secondary_capacity, n_secondaries);
 }
 
 rrea_gpu_status rrea_gpu_download_sources(rrea_gpu_ctx* ctx, double* out5)
@@ -546,12 +579,7 @@ rrea_gpu_status rrea_gpu_stage_electrons(rrea_gpu_ctx* ctx, const rrea_gpu_tile*
 
 rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t* n_secondaries)
 {
-    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
-    rrea_gpu_status const s = launch_electrons(ctx, step, dt_s, /*aliased=*/true);
-    if (s != RREA_GPU_OK) return s;
-    if (n_secondaries) *n_secondaries = ctx->last_secondaries;
-    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return RREA_GPU_OK;
+    return step_resident(ctx, RREA_SPECIES_ELECTRON, step, dt_s, n_secondaries);
 }
 
 rrea_gpu_status rrea_gpu_fetch_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile)
@@ -561,6 +589,21 @@ rrea_gpu_status rrea_gpu_fetch_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile)
     if (s != RREA_GPU_OK) return s;
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_stage_photons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile)
+{
+    return rrea_gpu_stage_electrons(ctx, tile);
+}
+
+rrea_gpu_status rrea_gpu_step_photons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t* n_secondaries)
+{
+    return step_resident(ctx, RREA_SPECIES_PHOTON, step, dt_s, n_secondaries);
+}
+
+rrea_gpu_status rrea_gpu_fetch_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile)
+{
+    return rrea_gpu_fetch_electrons(ctx, tile);
 }
 
 rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm,
@@ -576,7 +619,7 @@ rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block
     // Register budget of the transport kernel follows the requested
     // residency: >= 4 resident 128-thread blocks caps it at 128 registers.
     int const resident = blocks_per_sm * threads_per_block / 128;
-    ctx->launch_min_blocks = resident >= 5 ? 5 : (resident == 4 ? 4 : (resident == 3 ? 3 : 2));
+    ctx->launch_min_blocks = resident >= 8 ? 8 : (resident >= 6 ? 6 : (resident < 2 ? 2 : resident));
     return RREA_GPU_OK;
 }
 

@@ -38,7 +38,8 @@ __global__ void field_prep_kernel(int nr, int nz, const double* __restrict__ er,
 }
 
 // MinBlocks trades registers for resident warps: 2 -> up to 255 registers
-// (8 warps/SM), 3 -> 168 (12), 4 -> 128 (16), 5 -> 102 (20).
+// (8 warps/SM), 3 -> 168 (12), 4 -> 128 (16), 5 -> 102 (20), 6 -> 85 (24),
+// 8 -> 64 (32).
 // NP is the chord piece capacity: 1 for absorbing z faces, 4 for periodic z.
 template <int MinBlocks, int NP>
 __global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(ElectronArgs A)
@@ -180,6 +181,8 @@ cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
     case 3: rrea_dev::electron_step_kernel<3, 1><<<blocks, threads, 0, stream>>>(args); break;
     case 4: rrea_dev::electron_step_kernel<4, 1><<<blocks, threads, 0, stream>>>(args); break;
     case 5: rrea_dev::electron_step_kernel<5, 1><<<blocks, threads, 0, stream>>>(args); break;
+    case 6: rrea_dev::electron_step_kernel<6, 1><<<blocks, threads, 0, stream>>>(args); break;
+    case 8: rrea_dev::electron_step_kernel<8, 1><<<blocks, threads, 0, stream>>>(args); break;
     default: rrea_dev::electron_step_kernel<2, 1><<<blocks, threads, 0, stream>>>(args); break;
     }
     return cudaGetLastError();

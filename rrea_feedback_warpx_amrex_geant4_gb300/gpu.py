@@ -68,7 +68,8 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_set_field", "rrea_gpu_apply_electrons", "rrea_gpu_download_sources", "rrea_gpu_reset_sources",
     "rrea_gpu_download_diagnostics", "rrea_gpu_last_error", "rrea_gpu_stage_electrons",
     "rrea_gpu_step_electrons_resident", "rrea_gpu_fetch_electrons", "rrea_gpu_set_launch", "rrea_gpu_stream",
-    "rrea_gpu_last_step_stats",
+    "rrea_gpu_last_step_stats", "rrea_gpu_apply_photons", "rrea_gpu_stage_photons",
+    "rrea_gpu_step_photons_resident", "rrea_gpu_fetch_photons",
 )
 
 _lib = None
@@ -97,6 +98,11 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_set_field.argtypes = [vp, _D, _D, _D, _D, _D]
     lib.rrea_gpu_apply_electrons.argtypes = [vp, ctypes.POINTER(RreaGpuTile), ctypes.c_int32, ctypes.c_double,
                                              ctypes.c_double, vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    lib.rrea_gpu_apply_photons.argtypes = lib.rrea_gpu_apply_electrons.argtypes
+    lib.rrea_gpu_stage_photons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
+    lib.rrea_gpu_step_photons_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_double,
+                                                   ctypes.POINTER(ctypes.c_int64)]
+    lib.rrea_gpu_fetch_photons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
     lib.rrea_gpu_download_sources.argtypes = [vp, _D]
     lib.rrea_gpu_reset_sources.argtypes = [vp]
     lib.rrea_gpu_download_diagnostics.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64),
@@ -181,17 +187,37 @@ class RreaGpuContext:
     def set_launch(self, threads_per_block=128, blocks_per_sm=8, diagnostics=True):
         self._check(self.lib.rrea_gpu_set_launch(self.handle, threads_per_block, blocks_per_sm, int(diagnostics)))
 
-    def apply_electrons(self, arrays, step, dt_s, time_s=0.0, want_secondaries=True):
-        """Drop-in electron phase on host arrays (modified in place).
-        Returns the ordered secondaries as a structured array."""
+    def _apply(self, fn, arrays, step, dt_s, time_s, want_secondaries):
         t = tile_struct(arrays)
         n_sec = ctypes.c_int64()
         cap = 2 * self.capacity + 4096
         buf = np.zeros(cap if want_secondaries else 0, dtype=SECONDARY_DTYPE)
         ptr = ctypes.c_void_p(buf.ctypes.data) if want_secondaries else None
-        self._check(self.lib.rrea_gpu_apply_electrons(self.handle, ctypes.byref(t), int(step), float(time_s),
-                                                      float(dt_s), ptr, cap, ctypes.byref(n_sec)))
+        self._check(fn(self.handle, ctypes.byref(t), int(step), float(time_s), float(dt_s), ptr, cap,
+                       ctypes.byref(n_sec)))
         return buf[: n_sec.value] if want_secondaries else n_sec.value
+
+    def apply_electrons(self, arrays, step, dt_s, time_s=0.0, want_secondaries=True):
+        """Drop-in electron phase on host arrays (modified in place).
+        Returns the ordered secondaries as a structured array."""
+        return self._apply(self.lib.rrea_gpu_apply_electrons, arrays, step, dt_s, time_s, want_secondaries)
+
+    def apply_photons(self, arrays, step, dt_s, time_s=0.0, want_secondaries=True):
+        """Drop-in photon phase on host arrays (modified in place): (r, theta,
+        z) is the pushed end point, prev_* the start, u the momentum in eV."""
+        return self._apply(self.lib.rrea_gpu_apply_photons, arrays, step, dt_s, time_s, want_secondaries)
+
+    def stage_photons(self, arrays):
+        self._check(self.lib.rrea_gpu_stage_photons(self.handle, ctypes.byref(tile_struct(arrays))))
+
+    def step_photons_resident(self, step, dt_s):
+        n_sec = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_step_photons_resident(self.handle, int(step), float(dt_s),
+                                                            ctypes.byref(n_sec)))
+        return n_sec.value
+
+    def fetch_photons(self, arrays):
+        self._check(self.lib.rrea_gpu_fetch_photons(self.handle, ctypes.byref(tile_struct(arrays))))
 
     def stage_electrons(self, arrays):
         self._check(self.lib.rrea_gpu_stage_electrons(self.handle, ctypes.byref(tile_struct(arrays))))
@@ -249,5 +275,14 @@ class RreaParticleInteraction:
     def SetField(self, er, ez, bt, amb_er, amb_ez):
         self.ctx.set_field(er, ez, bt, amb_er, amb_ez)
 
-    def Apply(self, electrons, step, time_s, dt_s):
-        return self.ctx.apply_electrons(electrons, step, dt_s, time_s=time_s)
+    def Apply(self, electrons, step, time_s, dt_s, photons=None):
+        """Electron phase, then photon phase (the reference's order,
+        RreaParticleInteraction.cpp:54-57).  Returns the ordered secondaries
+        of each phase: (electron_secondaries, photon_secondaries or None)."""
+        if not dt_s > 0.0:
+            return None, None
+        sec_e = self.ctx.apply_electrons(electrons, step, dt_s, time_s=time_s)
+        sec_g = None
+        if photons is not None:
+            sec_g = self.ctx.apply_photons(photons, step, dt_s, time_s=time_s)
+        return sec_e, sec_g

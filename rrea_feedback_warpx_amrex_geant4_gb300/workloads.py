@@ -27,10 +27,12 @@ def kinetic_energy(ux, uy, uz):
 
 
 CASES = {
-    # configs[0]: 1e4 seeds at 7.2 MeV from r=0, z=0; 400 kV/m; 32x256 over 50 m x 500 m
+    # reference CPU case: 1e4 seeds at 7.2 MeV from r=0, z=0; 400 kV/m;
+    # 32x256 cells over 50 m x 500 m
     "uniform_c0": dict(r_hi=50.0, z_hi=500.0, nr=32, nz=256, field_v_per_m=4.0e5, seeds=10_000),
-    # configs[1]: 1e5 seeds log-uniform 1-20 MeV, isotropic in the -E hemisphere,
-    # uniform in a 5 m x 10 m disk; 500 kV/m; 256x2048 over 200 m x 2 km
+    # scale-up case: 1e5 seeds log-uniform 1-20 MeV, isotropic in the -E
+    # hemisphere, uniform in a 5 m x 10 m disk; 500 kV/m; 256x2048 cells over
+    # 200 m x 2 km
     "scaleup_c1": dict(r_hi=200.0, z_hi=2000.0, nr=256, nz=2048, field_v_per_m=5.0e5, seeds=100_000),
 }
 
@@ -85,6 +87,44 @@ def make_electrons(case, n, seed=12345):
         arr[f] = np.ascontiguousarray(arr[f], dtype=np.float64)
         arr["prev_" + f] = arr[f].copy()
     return arr
+
+
+def make_photons(case, n, dt_s, seed=4321, e_lo=5.0e4, e_hi=1.0e9):
+    """Photon tile (host SoA): energies log-uniform in [e_lo, e_hi] eV,
+    isotropic directions, starts spread over the inner domain; prev_* holds
+    the start and (r, theta, z) the straight-push end point after dt_s."""
+    rng = np.random.default_rng(seed)
+    p = CASES[case]
+    e = np.exp(rng.uniform(np.log(e_lo), np.log(e_hi), n))
+    r = 0.5 * p["r_hi"] * np.sqrt(rng.uniform(0.0, 1.0, n))
+    theta = rng.uniform(-np.pi, np.pi, n)
+    z = rng.uniform(0.1 * p["z_hi"], 0.9 * p["z_hi"], n)
+    mu = rng.uniform(-1.0, 1.0, n)
+    phi = rng.uniform(0.0, 2.0 * np.pi, n)
+    s = np.sqrt(1.0 - mu * mu)
+    arr = {
+        "r": r.copy(), "z": z.copy(), "theta": theta.copy(),
+        "ux": e * s * np.cos(phi), "uy": e * s * np.sin(phi), "uz": e * mu,
+        "w": np.ones(n),
+        "id": np.arange(1, n + 1, dtype=np.int64), "cpu": np.zeros(n, dtype=np.int32),
+    }
+    for f in ("r", "z", "theta", "ux", "uy", "uz"):
+        arr[f] = np.ascontiguousarray(arr[f], dtype=np.float64)
+        arr["prev_" + f] = arr[f].copy()
+    push_photons(arr, dt_s)
+    return arr
+
+
+def push_photons(arr, dt_s):
+    """WarpX's straight photon push from prev_* (x += c dt u/|u| on the
+    Cartesian image of the RZ point) into (r, theta, z)."""
+    e = np.sqrt(arr["ux"] ** 2 + arr["uy"] ** 2 + arr["uz"] ** 2)
+    f = np.where(e > 0.0, C_LIGHT * dt_s / np.where(e > 0.0, e, 1.0), 0.0)
+    x = arr["prev_r"] * np.cos(arr["prev_theta"]) + arr["ux"] * f
+    y = arr["prev_r"] * np.sin(arr["prev_theta"]) + arr["uy"] * f
+    arr["z"][:] = arr["prev_z"] + arr["uz"] * f
+    arr["r"][:] = np.hypot(x, y)
+    arr["theta"][:] = np.arctan2(y, x)
 
 
 def capture_prev(arr):
