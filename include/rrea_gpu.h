@@ -224,6 +224,57 @@ rrea_gpu_status rrea_gpu_last_step_stats(rrea_gpu_ctx* ctx, int64_t* transported
 /* The context's CUDA stream (a cudaStream_t), for timing with events. */
 rrea_gpu_status rrea_gpu_stream(rrea_gpu_ctx* ctx, void** stream);
 
+/*
+ * Allocation-free secondary ordering.  NO COUNTERPART IN THE REFERENCE: the
+ * reference orders secondaries on the host inside its transport step; this
+ * entry point exists for device-side integrations.
+ *
+ * Puts `n_secondaries` records from d_unordered into d_ordered in the
+ * deterministic order of rrea_gpu_apply_electrons / rrea_gpu_apply_photons
+ * (parent index, then lineage): record s goes to
+ * (sum of d_counts[0 .. s.parent_index-1]) + s.lineage.
+ *
+ * Who needs it: a caller that owns every device buffer through its own
+ * arena or fixed memory budget (for example a PIC code whose particle and
+ * field arena already holds the GPU's memory) and therefore must not have a
+ * library call cudaMalloc or cudaFree in the middle of its step - those
+ * calls would bypass the arena's accounting, and cudaFree synchronizes the
+ * whole device.  This function calls no allocating routine: its scratch
+ * (per-parent offsets, scan block sums, an error word; about 2 MiB) is a
+ * fixed device array inside this library, sized for at most
+ * RREA_GPU_NOALLOC_MAX_PARENTS parents per call.
+ *
+ * Arguments (all device pointers in the current device's memory):
+ *   d_counts      n_parents uint32 counts: records per parent
+ *   d_unordered   n_secondaries records; each (parent_index, lineage) pair
+ *                 must appear once, with lineage < d_counts[parent_index]
+ *   d_ordered     n_secondaries records of output; must not overlap
+ *                 d_unordered; needs no initialisation
+ *   stream        a cudaStream_t, or NULL for the legacy default stream
+ *   message       optional host buffer for an error description
+ * Nothing the caller passes needs to start at zero; the internal error word
+ * is cleared by each call before use.
+ *
+ * Returns RREA_GPU_ERR_CAPACITY (with a message) when n_parents exceeds
+ * RREA_GPU_NOALLOC_MAX_PARENTS, RREA_GPU_ERR_ARGUMENT for negative sizes,
+ * null or overlapping buffers, and RREA_GPU_ERR_INVALID_STATE when the
+ * records are inconsistent with the counts (such records are skipped, no
+ * out-of-range write happens).  The call blocks until the pass on `stream`
+ * has finished.
+ *
+ * The first call on each device looks up the scratch address once
+ * (cudaGetSymbolAddress, with that device current); if stream capture is
+ * used anywhere in the process, make that first call before capture starts.
+ * All calls on one device share the one scratch array: calls that overlap in
+ * time (from two host threads, or on two streams) race on it and must be
+ * serialised by the caller.
+ */
+#define RREA_GPU_NOALLOC_MAX_PARENTS (1 << 18)
+rrea_gpu_status rrea_gpu_order_secondaries_noalloc(const uint32_t* d_counts, int64_t n_parents,
+                                                   const rrea_gpu_secondary* d_unordered,
+                                                   int64_t n_secondaries, rrea_gpu_secondary* d_ordered,
+                                                   void* stream, char* message, size_t message_size);
+
 #ifdef __cplusplus
 }
 #endif

@@ -190,6 +190,19 @@ cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
 
 int64_t scan_scratch_elems(int64_t n) { return (n + rrea_dev::kScanBlock - 1) / rrea_dev::kScanBlock + 1; }
 
+cudaError_t exclusive_scan_counts(const uint32_t* counts, int64_t n, int64_t* offsets, int64_t* block_scratch,
+                                  cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    int64_t const nblocks = (n + rrea_dev::kScanBlock - 1) / rrea_dev::kScanBlock;
+    rrea_dev::scan_block_sums<<<static_cast<unsigned>(nblocks), rrea_dev::kScanBlock, 0, stream>>>(counts, n,
+                                                                                                  block_scratch);
+    rrea_dev::scan_block_offsets<<<1, rrea_dev::kScanBlock, 0, stream>>>(block_scratch, nblocks);
+    rrea_dev::scan_apply<<<static_cast<unsigned>(nblocks), rrea_dev::kScanBlock, 0, stream>>>(counts, n, block_scratch,
+                                                                                             offsets);
+    return cudaGetLastError();
+}
+
 cudaError_t order_secondaries(const uint32_t* counts, int64_t n, int64_t* offsets, int64_t* block_scratch,
                               const rrea_gpu_secondary* unordered, int64_t count, rrea_gpu_secondary* ordered,
                               cudaStream_t stream)

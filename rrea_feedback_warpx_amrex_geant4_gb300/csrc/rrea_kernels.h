@@ -20,6 +20,10 @@ cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
 cudaError_t photon_step(rrea_dev::StepConstants const& sc, rrea_dev::ElectronArgs const& args, int blocks, int threads,
                         bool periodic, cudaStream_t stream);
 int64_t scan_scratch_elems(int64_t n);
+// Exclusive scan of per-parent counts into offsets (block_scratch holds
+// scan_scratch_elems(n) elements); the first half of order_secondaries.
+cudaError_t exclusive_scan_counts(const uint32_t* counts, int64_t n, int64_t* offsets, int64_t* block_scratch,
+                                  cudaStream_t stream);
 cudaError_t order_secondaries(const uint32_t* counts, int64_t n, int64_t* offsets, int64_t* block_scratch,
                               const rrea_gpu_secondary* unordered, int64_t count, rrea_gpu_secondary* ordered,
                               cudaStream_t stream);

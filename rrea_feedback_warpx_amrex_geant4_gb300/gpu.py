@@ -69,8 +69,9 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_download_diagnostics", "rrea_gpu_last_error", "rrea_gpu_stage_electrons",
     "rrea_gpu_step_electrons_resident", "rrea_gpu_fetch_electrons", "rrea_gpu_set_launch", "rrea_gpu_stream",
     "rrea_gpu_last_step_stats", "rrea_gpu_apply_photons", "rrea_gpu_stage_photons",
-    "rrea_gpu_step_photons_resident", "rrea_gpu_fetch_photons",
+    "rrea_gpu_step_photons_resident", "rrea_gpu_fetch_photons", "rrea_gpu_order_secondaries_noalloc",
 )
+NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 
 _lib = None
 
@@ -103,6 +104,8 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_step_photons_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_double,
                                                    ctypes.POINTER(ctypes.c_int64)]
     lib.rrea_gpu_fetch_photons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
+    lib.rrea_gpu_order_secondaries_noalloc.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp,
+                                                       ctypes.c_char_p, ctypes.c_size_t]
     lib.rrea_gpu_download_sources.argtypes = [vp, _D]
     lib.rrea_gpu_reset_sources.argtypes = [vp]
     lib.rrea_gpu_download_diagnostics.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64),
@@ -259,6 +262,16 @@ class RreaGpuContext:
         s = ctypes.c_void_p()
         self._check(self.lib.rrea_gpu_stream(self.handle, ctypes.byref(s)))
         return s.value
+
+
+def order_secondaries_noalloc(d_counts, n_parents, d_unordered, n_secondaries, d_ordered, stream=None):
+    """rrea_gpu_order_secondaries_noalloc on device addresses (ints);
+    returns (status, message)."""
+    buf = ctypes.create_string_buffer(512)
+    st = load_library().rrea_gpu_order_secondaries_noalloc(
+        ctypes.c_void_p(d_counts), int(n_parents), ctypes.c_void_p(d_unordered), int(n_secondaries),
+        ctypes.c_void_p(d_ordered), ctypes.c_void_p(stream), buf, 512)
+    return st, buf.value.decode(errors="replace")
 
 
 class RreaParticleInteraction:

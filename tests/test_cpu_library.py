@@ -60,3 +60,14 @@ def test_structure_layouts_match_header(gpu):
     from oracle import oracle as o
     assert ctypes.sizeof(gpu.RreaGpuConfig) == ctypes.sizeof(o.RreaGpuConfig) == 136
     assert gpu.SECONDARY_DTYPE.itemsize == 4 * 4 + 8 * 3 + 8 * 9
+
+
+def test_noalloc_source_calls_no_allocator():
+    """The allocation-free ordering entry point keeps its scratch in a
+    file-scope device array and never calls an allocating routine."""
+    src = open(os.path.join(ROOT, "rrea_feedback_warpx_amrex_geant4_gb300", "csrc", "rrea_noalloc.cu")).read()
+    code = "\n".join(line.split("//")[0] for line in src.splitlines())
+    for banned in ("cudaMalloc", "cudaFree", "cudaHostAlloc", "cudaMallocAsync", "malloc(", "new ", "torch"):
+        assert banned not in code, banned
+    assert "static __device__ __align__(256)" in code
+    assert "cudaGetSymbolAddress" in code
