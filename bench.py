@@ -1,19 +1,21 @@
 #!/usr/bin/env python3
 """Throughput of the GB300 kinetic step: particle-steps/s on one GB300.
 
-Workload (configs[1] shape, "Plain GPU scale-up"): a population of electrons
-drawn from that case's seed distribution (K log-uniform 1-20 MeV, isotropic
-in the -E hemisphere, uniform in a 5 m x 10 m disk), air at 1.225 kg/m^3,
-uniform E_z = -500 kV/m, 256 x 2048 grid over 200 m x 2 km, dt = 0.5 ns,
-10 keV tracking cut.  One step = one outer dt of the electron transport
-phase over the whole resident population.  Synthetic seeds; no dataset.
+Workload: the plain GPU scale-up case.  Electrons drawn from its seed
+distribution (K log-uniform 1-20 MeV, isotropic in the -E hemisphere,
+uniform in a 5 m x 10 m disk) plus a photon population (E log-uniform
+50 keV-20 MeV, +z hemisphere, same disk), air at 1.225 kg/m^3, uniform
+E_z = -500 kV/m, 256 x 2048 grid over 200 m x 2 km, dt = 0.5 ns, 10 keV
+tracking cut.  One step = one outer dt of the electron phase and then the
+photon phase (the reference's phase order) over both resident populations.
+Synthetic seeds; no dataset.
 
-  value       particle-steps/s with the tile resident in HBM (device-timed)
-  e2e         the same through the drop-in C-ABI entry point with host
-              buffers: H2D of the tile, the step, D2H of tile + secondaries
-  roofline    transport kernel vs measured HBM bandwidth (112 B algorithmic
-              traffic per particle-step: read r,z,theta,ux,uy,uz,w,id, write
-              r,z,theta,ux,uy,uz)
+  value       particle-steps/s with the tiles resident in HBM (device-timed)
+  e2e         the same through the drop-in C-ABI entry points with host
+              buffers: H2D of the tiles, the step, D2H of tiles + secondaries
+  roofline    electron transport kernel (the dominant one) vs measured HBM
+              bandwidth (112 B algorithmic traffic per particle-step: read
+              r,z,theta,ux,uy,uz,w,id, write r,z,theta,ux,uy,uz)
   cpu_baseline the oracle (CPU restatement, all host threads) on a bounded
               sample of the same workload
 
@@ -36,7 +38,8 @@ sys.path.insert(0, ROOT)
 CASE = "scaleup_c1"
 DT_S = 5.0e-10
 BYTES_PER_PARTICLE_STEP = 112
-METRIC = "particle-steps/s (electron transport phase, configs[1] workload)"
+PHOTON_FRACTION = 0.5  # photons per electron in the resident populations
+METRIC = "particle-steps/s on 1 GB300 (plain kinetic step: electron + photon phases)"
 
 
 def parse():
@@ -49,7 +52,7 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=32768)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--threads", type=int, default=128)
-    p.add_argument("--blocks-per-sm", type=int, default=5)
+    p.add_argument("--blocks-per-sm", type=int, default=16)
     return p.parse_args()
 
 
@@ -136,19 +139,46 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.samples)}
 
 
+def make_photons(n, seed):
+    from rrea_feedback_warpx_amrex_geant4_gb300 import workloads
+
+    rng = np.random.default_rng(seed)
+    e = np.exp(rng.uniform(np.log(5.0e4), np.log(2.0e7), n))
+    r = 5.0 * np.sqrt(rng.uniform(0.0, 1.0, n))
+    theta = rng.uniform(-np.pi, np.pi, n)
+    z = rng.uniform(0.0, 10.0, n)
+    mu = rng.uniform(0.0, 1.0, n)
+    phi = rng.uniform(0.0, 2.0 * np.pi, n)
+    sn = np.sqrt(1.0 - mu * mu)
+    arr = {"r": r, "z": z, "theta": theta, "ux": e * sn * np.cos(phi), "uy": e * sn * np.sin(phi), "uz": e * mu,
+           "w": np.ones(n), "id": np.arange(1, n + 1, dtype=np.int64), "cpu": np.zeros(n, dtype=np.int32)}
+    for f in ("r", "z", "theta", "ux", "uy", "uz"):
+        arr[f] = np.ascontiguousarray(arr[f], dtype=np.float64)
+        arr["prev_" + f] = arr[f].copy()
+    workloads.push_photons(arr, DT_S)
+    return arr
+
+
 def cpu_oracle_rate(cfg, field, n, seed, steps=1):
-    """Oracle particle-steps/s on n electrons for `steps` steps (all threads)."""
+    """Oracle particle-steps/s on n electrons and PHOTON_FRACTION*n photons
+    for `steps` steps (all threads)."""
     from oracle import oracle
     from rrea_feedback_warpx_amrex_geant4_gb300 import DEFAULT_TABLES, workloads
 
-    oracle.load_tables(DEFAULT_TABLES)
+    if not getattr(cpu_oracle_rate, "_loaded", False):
+        oracle.load_tables(DEFAULT_TABLES)
+        cpu_oracle_rate._loaded = True
     arr = workloads.make_electrons(CASE, n, seed=seed)
+    pho = make_photons(int(n * PHOTON_FRACTION), seed + 1)
     moved = 0
     t0 = time.perf_counter()
     for s in range(steps):
-        moved += int((arr["id"] > 0).sum())
+        moved += int((arr["id"] > 0).sum()) + int((pho["id"] > 0).sum())
         oracle.electron_step(cfg, field, s, DT_S, arr)
+        oracle.photon_step(cfg, s, DT_S, pho)
         workloads.capture_prev(arr)
+        workloads.capture_prev(pho)
+        workloads.push_photons(pho, DT_S)
     dt = time.perf_counter() - t0
     return moved / dt, moved, dt
 
@@ -175,11 +205,13 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * total_t / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (configs[1] seed distribution)",
-        "config": {"workload": f"{CASE}: electron phase, {args.cpu_sample} electrons per timed step",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (scale-up case seed distribution)",
+        "config": {"workload": f"{CASE}: electron + photon phases, {args.cpu_sample} electrons and "
+                               f"{int(args.cpu_sample * PHOTON_FRACTION)} photons per timed step",
                    "grid": "256x2048", "dt_s": DT_S},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.cpu_sample} electrons x {args.steps} steps, OpenMP chunks of 64"},
+                         "sample": f"{args.cpu_sample} e- + {int(args.cpu_sample * PHOTON_FRACTION)} photons x "
+                                   f"{args.steps} steps, OpenMP chunks of 64"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -204,6 +236,7 @@ def run_gb300(args, rank, world, local):
         torch.cuda.synchronize()
 
     n = args.population
+    n_g = int(n * PHOTON_FRACTION)
     cfg = workloads.make_config(gpu, CASE)
     ctx = gpu.RreaGpuContext(cfg, n)
     ctx.load_tables(DEFAULT_TABLES)
@@ -211,21 +244,34 @@ def run_gb300(args, rank, world, local):
     ctx.set_field(**field)
     ctx.set_launch(args.threads, args.blocks_per_sm, diagnostics=False)
     arr = workloads.make_electrons(CASE, n, seed=777 + rank)
+    pho = make_photons(n_g, seed=778 + rank)
+    for f in ("r", "z", "theta"):
+        pho[f][:] = pho["prev_" + f]  # the resident photon step pushes by itself
     ctx.stage_electrons(arr)
+    ctx.stage_photons(pho)
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
+    def one_step(step):
+        ne = ctx.step_electrons_resident(step, DT_S)
+        te, _, kme = ctx.last_step_stats()
+        ng = ctx.step_photons_resident(step, DT_S)
+        tg, _, kmg = ctx.last_step_stats()
+        return te, tg, kme, kmg, ne, ng
+
     step = 0
     for _ in range(args.warmup):
-        ctx.step_electrons_resident(step, DT_S)
+        one_step(step)
         step += 1
     barrier()
 
     clocks = ClockSampler(local)
     clocks.start()
     total_ms = 0.0
-    kernel_ms = 0.0
-    moved = 0
+    kernel_ms_e = 0.0
+    kernel_ms_g = 0.0
+    moved_e = 0
+    moved_g = 0
     launches = 0
     secondaries = 0
     for _ in range(args.steps):
@@ -234,21 +280,24 @@ def run_gb300(args, rank, world, local):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        nsec = ctx.step_electrons_resident(step, DT_S)
+        te, tg, kme, kmg, ne, ng = one_step(step)
         e1.record(stream)
         e1.synchronize()
         total_ms += e0.elapsed_time(e1)
-        t, s, kms = ctx.last_step_stats()
-        kernel_ms += kms
-        moved += t
-        secondaries += nsec
-        launches += 1 + 3 + (1 if nsec > 0 else 0)
+        kernel_ms_e += kme
+        kernel_ms_g += kmg
+        moved_e += te
+        moved_g += tg
+        secondaries += ne + ng
+        # per phase: transport kernel, 3 scan kernels, scatter when anything was appended
+        launches += (1 + 3 + (1 if ne > 0 else 0)) + (1 + 3 + (1 if ng > 0 else 0))
         step += 1
     barrier()
     clocks.stop()
 
     # max over ranks of the device time; total work summed
-    t_local = torch.tensor([total_ms, float(moved), kernel_ms], dtype=torch.float64, device="cuda")
+    moved = moved_e + moved_g
+    t_local = torch.tensor([total_ms, float(moved)], dtype=torch.float64, device="cuda")
     if dist is not None:
         tmax = t_local.clone()
         dist.all_reduce(tmax[0:1], op=dist.ReduceOp.MAX)
@@ -259,37 +308,47 @@ def run_gb300(args, rank, world, local):
     value = moved_all / (total_ms_max / 1000.0)
 
     # ---- e2e through the drop-in C-ABI (host buffers, copies in the timed region)
-    ctx2_n = n
-    pinned = {}
-    for k, v in workloads.make_electrons(CASE, ctx2_n, seed=4242 + rank).items():
-        tt = torch.from_numpy(v).pin_memory()
-        pinned[k] = tt.numpy()
+    def pinned_tile(src):
+        out = {}
+        for k, v in src.items():
+            out[k] = torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy()
+        return out
+
+    pe = pinned_tile(workloads.make_electrons(CASE, n, seed=4242 + rank))
     for f in ("r", "z", "theta", "ux", "uy", "uz"):
-        pinned["prev_" + f] = pinned[f]  # the captured state is the current state
+        pe["prev_" + f] = pe[f]  # the captured state is the current state
+    pg = pinned_tile(make_photons(n_g, seed=4243 + rank))
     e2e_moved = 0
     e2e_t = 0.0
     sec_bytes = 0
-    ctx.apply_electrons(pinned, step, DT_S, want_secondaries=True)  # warm
+    ctx.apply_electrons(pe, step, DT_S, want_secondaries=True)  # warm
+    ctx.apply_photons(pg, step, DT_S, want_secondaries=True)
     step += 1
     barrier()
     for _ in range(args.e2e_steps):
-        live = int((pinned["id"] > 0).sum())
+        # photons: the host captures the start and pushes (WarpX's part of the step)
+        for f in ("r", "z", "theta", "ux", "uy", "uz"):
+            np.copyto(pg["prev_" + f], pg[f])
+        workloads.push_photons(pg, DT_S)
+        live = int((pe["id"] > 0).sum()) + int((pg["id"] > 0).sum())
         t0 = time.perf_counter()
-        sec = ctx.apply_electrons(pinned, step, DT_S, want_secondaries=True)
+        sec_e = ctx.apply_electrons(pe, step, DT_S, want_secondaries=True)
+        sec_g = ctx.apply_photons(pg, step, DT_S, want_secondaries=True)
         e2e_t += time.perf_counter() - t0
         e2e_moved += live
-        sec_bytes += len(sec) * gpu.SECONDARY_DTYPE.itemsize
+        sec_bytes += (len(sec_e) + len(sec_g)) * gpu.SECONDARY_DTYPE.itemsize
         step += 1
     e2e_value = e2e_moved / e2e_t
-    h2d = ctx2_n * (13 * 8 + 8 + 4)
-    d2h = ctx2_n * (6 * 8 + 8) + sec_bytes // max(args.e2e_steps, 1)
+    h2d = (n + n_g) * (13 * 8 + 8 + 4)
+    d2h = (n + n_g) * (6 * 8 + 8) + sec_bytes // max(args.e2e_steps, 1)
 
     if rank == 0:
         peak, peak_kind = read_peaks()
-        achieved = (moved * BYTES_PER_PARTICLE_STEP) / (kernel_ms / 1000.0) / 1.0e9 if kernel_ms > 0 else 0.0
+        achieved = (moved_e * BYTES_PER_PARTICLE_STEP) / (kernel_ms_e / 1000.0) / 1.0e9 if kernel_ms_e > 0 else 0.0
+        achieved_g = (moved_g * BYTES_PER_PARTICLE_STEP) / (kernel_ms_g / 1000.0) / 1.0e9 if kernel_ms_g > 0 else 0.0
         traffic_pps = read_traffic_per_particle_step()
         launches_per_step = launches / max(args.steps, 1)
-        traffic = traffic_pps * (moved / max(args.steps, 1)) if traffic_pps else None
+        traffic = traffic_pps * (moved_e / max(args.steps, 1)) if traffic_pps else None
         cores = os.cpu_count() or 1
         cpu_n = min(args.cpu_sample, 16384)
         cpu_rate, cpu_moved, cpu_t = cpu_oracle_rate(cfg, field, cpu_n, seed=31337)
@@ -297,22 +356,27 @@ def run_gb300(args, rank, world, local):
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (configs[1] seed distribution, seeded numpy PRNG)",
-            "config": {"workload": f"{CASE}: electron transport phase over a resident population of {n} e- "
-                                   f"per GPU (configs[1] seeds/geometry/field), dt 0.5 ns",
-                       "grid": "256x2048", "population_per_gpu": n, "dt_s": DT_S,
+            "data": "synthetic (scale-up case seed distribution, seeded numpy PRNG)",
+            "config": {"workload": f"{CASE}: electron + photon phases over resident populations of {n} e- and "
+                                   f"{n_g} photons per GPU (256x2048 cells over 200 m x 2 km, uniform "
+                                   f"E_z = -500 kV/m), dt 0.5 ns",
+                       "grid": "256x2048", "population_per_gpu": {"electrons": n, "photons": n_g}, "dt_s": DT_S,
                        "l2": "flushed between timed steps (256 MiB write)",
                        "parallelism": f"dp{world} (independent particle shards)"},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
-                    "path": "rrea_gpu_apply_electrons (pinned host tile -> HBM -> host)"},
+                    "path": "rrea_gpu_apply_electrons + rrea_gpu_apply_photons (pinned host tiles -> HBM -> host)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic, "kernel": "electron_step_kernel",
                          "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
-                         "kernel_ms_per_step": kernel_ms / args.steps},
+                         "kernel_ms_per_step": kernel_ms_e / args.steps,
+                         "photon_kernel": {"kernel": "photon_step_kernel", "achieved": achieved_g,
+                                           "frac": achieved_g / peak, "kernel_ms_per_step": kernel_ms_g / args.steps}},
+            "phases": {"electron_steps": moved_e, "photon_steps": moved_g},
             "cpu_baseline": {"value": cpu_rate, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{cpu_n} electrons x 1 step of the same workload, OpenMP chunks of 64"},
+                             "sample": f"{cpu_n} e- + {int(cpu_n * PHOTON_FRACTION)} photons x 1 step of the "
+                                       f"same workload, OpenMP chunks of 64"},
             "gpu_launches": launches,
             "gpu_launches_per_step": launches_per_step,
             "secondaries_per_step": secondaries / max(args.steps, 1),

@@ -196,7 +196,9 @@ rrea_gpu_status rrea_gpu_apply_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, i
                                        int64_t secondary_capacity, int64_t* n_secondaries);
 
 /*
- * Resident photon mode: the staged tile holds photons at their start point.
+ * Resident photon mode: the context keeps one resident tile per species, so
+ * the photon tile stays in HBM next to the electron tile.  The staged photon
+ * tile holds photons at their start point.
  * The step pushes each photon straight by c*dt along its momentum (the
  * WarpX photon pusher, x += c dt u/|u| in Cartesian coordinates) and then
  * runs the photon phase on that chord, all on the device.  stage/fetch move
@@ -207,11 +209,12 @@ rrea_gpu_status rrea_gpu_step_photons_resident(rrea_gpu_ctx* ctx, int32_t step, 
                                                int64_t* n_secondaries);
 rrea_gpu_status rrea_gpu_fetch_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile);
 
-/* Launch shape of the transport kernel: threads per block (32..128, a
- * multiple of 32) and resident 128-thread blocks per SM (2 to 8; the
- * kernel variant's register budget follows: 255, 168, 128, 102, 85 or 64).  The
- * grid is one resident wave with a grid-stride loop.  `diagnostics` enables
- * the per-particle diagnostic arrays. */
+/* Launch shape of the transport kernels: threads per block (32..128, a
+ * multiple of 32) and resident 128-thread blocks per SM (1 to 64; the
+ * electron kernel variant follows the residency: 2, 4, 8, 12 or 16 blocks
+ * with 255, 128, 64, 40 or 32 registers per thread; default 16, the full
+ * 64 warps per SM).  The grid is one resident wave with a grid-stride loop.
+ * `diagnostics` enables the per-particle diagnostic arrays. */
 rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm,
                                     int32_t diagnostics);
 

@@ -136,6 +136,19 @@ __device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double
     p.in_length = p.full * (p.in_end - p.in_begin);
     p.exits = p.in_end < 1.0 - 64.0 * kEps;
 
+    if constexpr (NP == 1) {
+        // Absorbing z: no seams, so the breakpoints are [in_begin, in_end]
+        // (already sorted); deduplication drops the piece when the two are
+        // within the tolerance.  Static indices keep the path in registers.
+        double const l = p.in_begin, r = p.in_end;
+        bool const dup = fabs(l - r) <= 128.0 * kEps * fmax(1.0, fmax(fabs(l), fabs(r)));
+        p.npieces = 0;
+        if (!dup && r > l) {
+            p.pieces[0] = Piece{l, r, p.full * (r - l), 0.0};
+            p.npieces = 1;
+        }
+        return;
+    }
     // Breakpoints: [in_begin, seams..., in_end], sorted and deduplicated.
     double bp[NP + 1];
     int nb = 0;
@@ -423,7 +436,9 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
     double const pdx = quot(p.ex - p.sx, dfull);
     double const pdy = quot(p.ey - p.sy, dfull);
     double const pdz = quot(p.ez - p.sz, dfull);
-    for (int ip = 0; ip < p.npieces; ++ip) {
+#pragma unroll
+    for (int ip = 0; ip < NP; ++ip) {
+        if (ip >= p.npieces) break;
         Piece const& pc = p.pieces[ip];
         double const pb = fmax(begin, pc.begin);
         double const pe = fmin(end, pc.end);
@@ -493,6 +508,18 @@ template <int NP>
 __device__ __forceinline__ void build_intervals(Path<NP> const& p, double rho, Intervals<NP>& iv)
 {
     iv.n = 0;
+    if constexpr (NP == 1) {
+        Piece const& pc = p.pieces[0];
+        if (p.npieces < 1 || !(pc.length > 0.0)) return;
+        double dl = 0.0;
+        if (pc.end > pc.begin && p.full > 0.0) dl = p.full * (pc.end - pc.begin) * positive_or(rho, rho);
+        iv.begin[0] = pc.begin;
+        iv.end[0] = pc.end;
+        iv.length[0] = pc.length;
+        iv.density[0] = positive_or(dl / pc.length, rho);
+        iv.n = 1;
+        return;
+    }
     for (int i = 0; i < p.npieces; ++i) {
         Piece const& pc = p.pieces[i];
         if (!(pc.length > 0.0)) continue;
@@ -513,7 +540,9 @@ __device__ __forceinline__ double density_path(Intervals<NP> const& iv, Path<NP>
     e = fmin(p.in_end, e);
     if (!(e > b)) return 0.0;
     double s = 0.0;
-    for (int i = 0; i < iv.n; ++i) {
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        if (i >= iv.n) break;
         double const bb = fmax(b, iv.begin[i]), ee = fmin(e, iv.end[i]);
         if (ee > bb) s += p.full * (ee - bb) * iv.density[i];
     }
@@ -531,7 +560,9 @@ __device__ __forceinline__ double fraction_at_density_path(Intervals<NP> const& 
         return e;
     }
     double rem = target;
-    for (int i = 0; i < iv.n; ++i) {
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        if (i >= iv.n) break;
         double const bb = fmax(b, iv.begin[i]), ee = fmin(e, iv.end[i]);
         if (!(ee > bb) || !(iv.density[i] > 0.0)) continue;
         double const c = p.full * (ee - bb) * iv.density[i];
@@ -566,7 +597,9 @@ __device__ __forceinline__ Selection select_hazard(double t0, double t1, double 
     Selection r{false, false, -1, 0.0, 0.0};
     double const taus[3] = {t0, t1, t2};
     if (count < 1 || count > 3 || !isfinite(u1) || !isfinite(u2)) return r;
-    for (int i = 0; i < count; ++i) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (i >= count) break;
         if (!isfinite(taus[i]) || taus[i] < 0.0) return r;
         r.total += taus[i];
     }
@@ -580,7 +613,9 @@ __device__ __forceinline__ Selection select_hazard(double t0, double t1, double 
     double const target = u2 * r.total;
     double cum = 0.0;
     int last_open = -1;
-    for (int i = 0; i < count; ++i) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (i >= count) break;
         if (taus[i] > 0.0) last_open = i;
         cum += taus[i];
         if (target < cum) {

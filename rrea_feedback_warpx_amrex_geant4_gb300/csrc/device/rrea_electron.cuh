@@ -16,6 +16,10 @@
 
 namespace rrea_dev {
 
+// Per-step constants of the electron phase.  Defined in this header, which
+// only the electron kernel's translation unit (rrea_kernels.cu) includes.
+__constant__ StepConstants c_step;
+
 
 
 // The electron coefficient tables (collision, soft radiative, hard-Moller
@@ -241,20 +245,27 @@ __device__ __forceinline__ void brems_final_state(StepConstants const& C, Electr
     }
 }
 
+// The out-of-line helpers below take every argument by value and return
+// their results by value: a reference or pointer to a caller variable would
+// pin that variable to the thread's stack for the whole transport loop.
+
+struct Dir3 {
+    double x, y, z;
+    int err;
+};
+
 // Few-collision branch of apply_gs_elastic_scatter (O/RreaTransportStep.H:397-416):
 // a Poisson number of single screened-Rutherford deflections.  Rare for
 // tracked electrons (n >= 10 elastic collisions per substep at MeV energies),
 // so it is kept out of line.
-__device__ __noinline__ void gs_few_collisions(StepConstants const& C, const double* __restrict__ arena,
-                                               RngStream const& rng, uint64_t sub, double gs_n, double k, double lk,
-                                               double& dx, double& dy, double& dz, Err& err)
+__device__ __noinline__ Dir3 gs_few_collisions(const double* __restrict__ arena, RngStream rng, uint64_t sub,
+                                               double gs_n, double k, double lk, double dx, double dy, double dz)
 {
+    StepConstants const& C = c_step;
+    Err err;
     double const few = C.tix.gs_few_collision_threshold;
     int const cap = static_cast<int>(ceil(3.0 * few));
-    if (cap >= 255) {
-        err.set(RREA_GPU_ERR_INVALID_STATE);
-        return;
-    }
+    if (cap >= 255) return Dir3{dx, dy, dz, RREA_GPU_ERR_INVALID_STATE};
     int const cnt = poisson_capped(gs_n, rng.uniform((sub << 8) | 0, kChElectronGsFewCount), cap);
     for (int q = 0; q < cnt; ++q) {
         uint64_t const inner = static_cast<uint64_t>(q + 1);
@@ -264,24 +275,24 @@ __device__ __noinline__ void gs_few_collisions(StepConstants const& C, const dou
         cone_direction(dx, dy, dz, ct, rng.uniform((sub << 8) | inner, kChElectronGsFewAzimuth), nx, ny, nz);
         dx = nx; dy = ny; dz = nz;
     }
+    return Dir3{dx, dy, dz, err.code};
 }
 
 // The 56-step bisection of RreaLimitContinuousSegmentAtCutoff
 // (O/RreaParticleInteraction.H:245-263), run only when the drag reaches the
-// cutoff inside the segment.  Returns false when a loss is not finite.
+// cutoff inside the segment.  Returns NaN when a loss is not finite.
 template <int NP>
-__device__ __noinline__ bool cutoff_bisection(Intervals<NP> const* iv, Path<NP> const* path, double b, double e,
-                                              double total, double to_cut, double& eff)
+__device__ __noinline__ double cutoff_bisection(Intervals<NP> iv, Path<NP> path, double b, double e, double total,
+                                                double to_cut)
 {
     double lo = b, hi = e;
     for (int it = 0; it < 56; ++it) {
         double const mid = 0.5 * (lo + hi);
-        double const l = total * density_path(*iv, *path, b, mid);
-        if (!isfinite(l) || l < 0.0) return false;
+        double const l = total * density_path(iv, path, b, mid);
+        if (!isfinite(l) || l < 0.0) return __longlong_as_double(0x7ff8000000000000LL);
         if (l < to_cut) lo = mid; else hi = mid;
     }
-    eff = 0.5 * (lo + hi);
-    return true;
+    return 0.5 * (lo + hi);
 }
 
 // Returns the disposition (0 survive, 1 escape, 2 demotion, 3 zero weight).
@@ -492,7 +503,8 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                 } else {
                     reaches = true;
                     if (to_cut != 0.0) {
-                        valid = cutoff_bisection<NP>(&iv, &path, b, e, total, to_cut, eff);
+                        eff = cutoff_bisection<NP>(iv, path, b, e, total, to_cut);
+                        valid = !isnan(eff);
                         if (!valid) {
                             eff = b;
                             reaches = false;
@@ -513,7 +525,9 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
         double const col = fmin(raw_col, drag);
         // ion pairs, O/RreaChargedInterleave.H:157-196
         if (col > 0.0 && raw_col > 0.0) {
-            for (int i = 0; i < iv.n; ++i) {
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                if (i >= iv.n) break;
                 double const bb = fmax(b, iv.begin[i]), ee = fmin(eff, iv.end[i]);
                 if (!(ee > bb)) continue;
                 double const raw = path.full * (ee - bb) * iv.density[i] * sc;
@@ -565,7 +579,9 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                 err.set(RREA_GPU_ERR_INVALID_STATE);
                 break;
             }
-            for (int i = 0; i < iv.n; ++i) {
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                if (i >= iv.n) break;
                 transported_dpath += iv.length[i] * iv.density[i];
                 transported_len += iv.length[i];
             }
@@ -668,7 +684,9 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
             if (gs_n > 0.0) {
                 double const few = C.tix.gs_few_collision_threshold;
                 if (gs_n < few) {
-                    gs_few_collisions(C, arena, rng, sub, gs_n, k, lk, dx, dy, dz, err);
+                    Dir3 const d3 = gs_few_collisions(arena, rng, sub, gs_n, k, lk, dx, dy, dz);
+                    dx = d3.x; dy = d3.y; dz = d3.z;
+                    if (d3.err) err.set(d3.err);
                     if (err.code) break;
                 } else {
                     double const ct = sample_gs_cos(C, arena, k, gs_n, rng.uniform(sub << 8, kChElectronGsAngle), err, lk);

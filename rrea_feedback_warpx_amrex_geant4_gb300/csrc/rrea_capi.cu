@@ -1,6 +1,7 @@
 // C-ABI of the GB300 kinetic step (include/rrea_gpu.h).  Host C++ around the
-// kernels in rrea_kernels.cu: owns the device arena, field vectors, the
-// resident species tile and every per-step buffer.  All device memory is
+// kernels in rrea_kernels.cu and rrea_photon_kernels.cu: owns the device
+// arena, field vectors, one resident tile per species and every per-step
+// buffer.  All device memory is
 // allocated at create/load time; a step allocates nothing.
 #include "../../include/rrea_gpu.h"
 
@@ -19,6 +20,16 @@
 namespace {
 
 constexpr int kTileDoubles = 13;
+constexpr int kSpecies = 3;
+
+// Device SoA of one species: r, z, theta, ux, uy, uz, w, prev_r, prev_z,
+// prev_theta, prev_ux, prev_uy, prev_uz, then id and cpu.
+struct SpeciesTile {
+    double* d[kTileDoubles] = {};
+    int64_t* id = nullptr;
+    int32_t* cpu = nullptr;
+    int64_t n = 0;
+};
 
 }  // namespace
 
@@ -43,10 +54,8 @@ struct rrea_gpu_ctx {
     bool field_set = false;
     bool has_b = false;
 
-    double* d_tile[kTileDoubles] = {};
-    int64_t* d_id = nullptr;
-    int32_t* d_cpu = nullptr;
-    int64_t staged_n = 0;
+    // one resident SoA tile per species (RREA_SPECIES_ELECTRON/POSITRON/PHOTON)
+    SpeciesTile tiles[kSpecies];
 
     rrea_gpu_secondary* d_sec_unordered = nullptr;
     rrea_gpu_secondary* d_sec_ordered = nullptr;
@@ -68,8 +77,8 @@ struct rrea_gpu_ctx {
     int64_t last_transported = 0;
     int64_t last_secondaries = 0;
     int launch_threads = 128;
-    int launch_blocks_per_sm = 5;
-    int launch_min_blocks = 5;
+    int launch_blocks_per_sm = 16;
+    int launch_min_blocks = 16;
     bool diagnostics = true;
 
     std::string last_error;
@@ -194,11 +203,14 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         && dalloc(&ctx->d_bt, nbt) == cudaSuccess && dalloc(&ctx->d_amb_er, ner) == cudaSuccess
         && dalloc(&ctx->d_amb_ez, nez) == cudaSuccess && dalloc(&ctx->d_cell_er, ncell) == cudaSuccess
         && dalloc(&ctx->d_cell_ez, ncell) == cudaSuccess && dalloc(&ctx->d_cells, 5 * ncell) == cudaSuccess;
-    for (int f = 0; ok && f < kTileDoubles; ++f) ok = dalloc(&ctx->d_tile[f], n) == cudaSuccess;
+    for (int sp = 0; ok && sp < kSpecies; ++sp) {
+        SpeciesTile& st = ctx->tiles[sp];
+        for (int f = 0; ok && f < kTileDoubles; ++f) ok = dalloc(&st.d[f], n) == cudaSuccess;
+        ok = ok && dalloc(&st.id, n) == cudaSuccess && dalloc(&st.cpu, n) == cudaSuccess;
+    }
     ctx->sec_capacity = 2 * capacity + 4096;
     size_t const nsec = static_cast<size_t>(ctx->sec_capacity);
-    ok = ok && dalloc(&ctx->d_id, n) == cudaSuccess && dalloc(&ctx->d_cpu, n) == cudaSuccess
-        && dalloc(&ctx->d_sec_unordered, nsec) == cudaSuccess && dalloc(&ctx->d_sec_ordered, nsec) == cudaSuccess
+    ok = ok && dalloc(&ctx->d_sec_unordered, nsec) == cudaSuccess && dalloc(&ctx->d_sec_ordered, nsec) == cudaSuccess
         && dalloc(&ctx->d_sec_count, 1) == cudaSuccess && dalloc(&ctx->d_sec_per_parent, n) == cudaSuccess
         && dalloc(&ctx->d_offsets, n) == cudaSuccess
         && dalloc(&ctx->d_scan_scratch, static_cast<size_t>(rrea_launch::scan_scratch_elems(capacity))) == cudaSuccess
@@ -226,9 +238,11 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     dfree(ctx->d_amb_ez);
     dfree(ctx->d_cell_er);
     dfree(ctx->d_cell_ez);
-    for (auto* p : ctx->d_tile) dfree(p);
-    dfree(ctx->d_id);
-    dfree(ctx->d_cpu);
+    for (auto& st : ctx->tiles) {
+        for (auto* p : st.d) dfree(p);
+        dfree(st.id);
+        dfree(st.cpu);
+    }
     dfree(ctx->d_sec_unordered);
     dfree(ctx->d_sec_ordered);
     dfree(ctx->d_sec_count);
@@ -315,28 +329,29 @@ rrea_gpu_status rrea_gpu_set_field(rrea_gpu_ctx* ctx, const double* er, const do
 
 namespace {
 
-rrea_gpu_status stage_tile(rrea_gpu_ctx* ctx, rrea_gpu_tile const* t)
+rrea_gpu_status stage_tile(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile const* t)
 {
+    SpeciesTile& st = ctx->tiles[species];
     if (t->n > ctx->capacity) return fail(ctx, RREA_GPU_ERR_CAPACITY, "tile larger than the context capacity");
     double* const host[kTileDoubles] = {t->r, t->z, t->theta, t->ux, t->uy, t->uz, t->w,
                                         t->prev_r, t->prev_z, t->prev_theta, t->prev_ux, t->prev_uy, t->prev_uz};
     size_t const bytes = static_cast<size_t>(t->n) * sizeof(double);
     for (int f = 0; f < kTileDoubles; ++f) {
         if (!host[f]) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "null tile component");
-        if (t->n) RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_tile[f], host[f], bytes, cudaMemcpyHostToDevice, ctx->stream));
+        if (t->n) RREA_CUDA(ctx, cudaMemcpyAsync(st.d[f], host[f], bytes, cudaMemcpyHostToDevice, ctx->stream));
     }
     if (!t->id) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "null tile id");
     if (t->n) {
-        RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_id, t->id, static_cast<size_t>(t->n) * sizeof(int64_t),
+        RREA_CUDA(ctx, cudaMemcpyAsync(st.id, t->id, static_cast<size_t>(t->n) * sizeof(int64_t),
                                        cudaMemcpyHostToDevice, ctx->stream));
         if (t->cpu) {
-            RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_cpu, t->cpu, static_cast<size_t>(t->n) * sizeof(int32_t),
+            RREA_CUDA(ctx, cudaMemcpyAsync(st.cpu, t->cpu, static_cast<size_t>(t->n) * sizeof(int32_t),
                                            cudaMemcpyHostToDevice, ctx->stream));
         } else {
-            RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_cpu, 0, static_cast<size_t>(t->n) * sizeof(int32_t), ctx->stream));
+            RREA_CUDA(ctx, cudaMemsetAsync(st.cpu, 0, static_cast<size_t>(t->n) * sizeof(int32_t), ctx->stream));
         }
     }
-    ctx->staged_n = t->n;
+    st.n = t->n;
     return RREA_GPU_OK;
 }
 
@@ -371,16 +386,17 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_transported, 0, sizeof(unsigned long long), ctx->stream));
 
     rrea_dev::ElectronArgs a{};
-    a.n = ctx->staged_n;
-    double** t = ctx->d_tile;
+    SpeciesTile& st = ctx->tiles[species];
+    a.n = st.n;
+    double** t = st.d;
     a.r = t[0]; a.z = t[1]; a.theta = t[2]; a.ux = t[3]; a.uy = t[4]; a.uz = t[5]; a.w = t[6];
     if (aliased) {
         a.prev_r = t[0]; a.prev_z = t[1]; a.prev_theta = t[2]; a.prev_ux = t[3]; a.prev_uy = t[4]; a.prev_uz = t[5];
     } else {
         a.prev_r = t[7]; a.prev_z = t[8]; a.prev_theta = t[9]; a.prev_ux = t[10]; a.prev_uy = t[11]; a.prev_uz = t[12];
     }
-    a.id = ctx->d_id;
-    a.cpu = ctx->d_cpu;
+    a.id = st.id;
+    a.cpu = st.cpu;
     a.sec = ctx->d_sec_unordered;
     a.sec_count = ctx->d_sec_count;
     a.sec_capacity = ctx->sec_capacity;
@@ -451,15 +467,16 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     return RREA_GPU_OK;
 }
 
-rrea_gpu_status unstage_tile(rrea_gpu_ctx* ctx, rrea_gpu_tile* t)
+rrea_gpu_status unstage_tile(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile* t)
 {
+    SpeciesTile& st = ctx->tiles[species];
     double* const host[6] = {t->r, t->z, t->theta, t->ux, t->uy, t->uz};
     size_t const bytes = static_cast<size_t>(t->n) * sizeof(double);
     if (t->n) {
         for (int f = 0; f < 6; ++f) {
-            RREA_CUDA(ctx, cudaMemcpyAsync(host[f], ctx->d_tile[f], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+            RREA_CUDA(ctx, cudaMemcpyAsync(host[f], st.d[f], bytes, cudaMemcpyDeviceToHost, ctx->stream));
         }
-        RREA_CUDA(ctx, cudaMemcpyAsync(t->id, ctx->d_id, static_cast<size_t>(t->n) * sizeof(int64_t),
+        RREA_CUDA(ctx, cudaMemcpyAsync(t->id, st.id, static_cast<size_t>(t->n) * sizeof(int64_t),
                                        cudaMemcpyDeviceToHost, ctx->stream));
     }
     return RREA_GPU_OK;
@@ -469,7 +486,7 @@ rrea_gpu_status apply_phase(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile* tile,
                             rrea_gpu_secondary* secondaries, int64_t secondary_capacity, int64_t* n_secondaries)
 {
     if (!ctx || !tile || tile->n < 0) return RREA_GPU_ERR_ARGUMENT;
-    rrea_gpu_status s = stage_tile(ctx, tile);
+    rrea_gpu_status s = stage_tile(ctx, species, tile);
     if (s != RREA_GPU_OK) return s;
     s = launch_phase(ctx, species, step, dt_s, /*aliased=*/false);
     if (s != RREA_GPU_OK) return s;
@@ -477,13 +494,31 @@ rrea_gpu_status apply_phase(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile* tile,
     if (secondaries && ctx->last_secondaries > secondary_capacity) {
         return fail(ctx, RREA_GPU_ERR_CAPACITY, "caller secondary buffer too small");
     }
-    s = unstage_tile(ctx, tile);
+    s = unstage_tile(ctx, species, tile);
     if (s != RREA_GPU_OK) return s;
     if (secondaries && ctx->last_secondaries > 0) {
         RREA_CUDA(ctx, cudaMemcpyAsync(secondaries, ctx->d_sec_ordered,
                                        static_cast<size_t>(ctx->last_secondaries) * sizeof(rrea_gpu_secondary),
                                        cudaMemcpyDeviceToHost, ctx->stream));
     }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status stage_species(rrea_gpu_ctx* ctx, int species, const rrea_gpu_tile* tile)
+{
+    if (!ctx || !tile || tile->n < 0) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_status const s = stage_tile(ctx, species, tile);
+    if (s != RREA_GPU_OK) return s;
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status fetch_species(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile* tile)
+{
+    if (!ctx || !tile || tile->n != ctx->tiles[species].n) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_status const s = unstage_tile(ctx, species, tile);
+    if (s != RREA_GPU_OK) return s;
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RREA_GPU_OK;
 }
@@ -570,11 +605,7 @@ void rrea_gpu_last_error(const rrea_gpu_ctx* ctx, char* buf, size_t size)
 
 rrea_gpu_status rrea_gpu_stage_electrons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile)
 {
-    if (!ctx || !tile || tile->n < 0) return RREA_GPU_ERR_ARGUMENT;
-    rrea_gpu_status const s = stage_tile(ctx, tile);
-    if (s != RREA_GPU_OK) return s;
-    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return RREA_GPU_OK;
+    return stage_species(ctx, RREA_SPECIES_ELECTRON, tile);
 }
 
 rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t* n_secondaries)
@@ -584,16 +615,12 @@ rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step
 
 rrea_gpu_status rrea_gpu_fetch_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile)
 {
-    if (!ctx || !tile || tile->n != ctx->staged_n) return RREA_GPU_ERR_ARGUMENT;
-    rrea_gpu_status const s = unstage_tile(ctx, tile);
-    if (s != RREA_GPU_OK) return s;
-    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return RREA_GPU_OK;
+    return fetch_species(ctx, RREA_SPECIES_ELECTRON, tile);
 }
 
 rrea_gpu_status rrea_gpu_stage_photons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile)
 {
-    return rrea_gpu_stage_electrons(ctx, tile);
+    return stage_species(ctx, RREA_SPECIES_PHOTON, tile);
 }
 
 rrea_gpu_status rrea_gpu_step_photons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t* n_secondaries)
@@ -603,7 +630,7 @@ rrea_gpu_status rrea_gpu_step_photons_resident(rrea_gpu_ctx* ctx, int32_t step, 
 
 rrea_gpu_status rrea_gpu_fetch_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile)
 {
-    return rrea_gpu_fetch_electrons(ctx, tile);
+    return fetch_species(ctx, RREA_SPECIES_PHOTON, tile);
 }
 
 rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm,
@@ -616,10 +643,10 @@ rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block
     ctx->launch_threads = threads_per_block;
     ctx->launch_blocks_per_sm = blocks_per_sm;
     ctx->diagnostics = diagnostics != 0;
-    // Register budget of the transport kernel follows the requested
-    // residency: >= 4 resident 128-thread blocks caps it at 128 registers.
+    // Register budget of the electron kernel follows the requested
+    // residency (16 resident 128-thread blocks: 32 registers).
     int const resident = blocks_per_sm * threads_per_block / 128;
-    ctx->launch_min_blocks = resident >= 8 ? 8 : (resident >= 6 ? 6 : (resident < 2 ? 2 : resident));
+    ctx->launch_min_blocks = resident >= 16 ? 16 : resident >= 12 ? 12 : resident >= 8 ? 8 : resident >= 4 ? 4 : 2;
     return RREA_GPU_OK;
 }
 

@@ -13,8 +13,6 @@
 
 namespace rrea_dev {
 
-__constant__ StepConstants c_step;
-
 __global__ void field_prep_kernel(int nr, int nz, const double* __restrict__ er, const double* __restrict__ ez,
                                   const double* __restrict__ amb_er, const double* __restrict__ amb_ez,
                                   double* __restrict__ cell_er, double* __restrict__ cell_ez)
@@ -38,8 +36,9 @@ __global__ void field_prep_kernel(int nr, int nz, const double* __restrict__ er,
 }
 
 // MinBlocks trades registers for resident warps: 2 -> up to 255 registers
-// (8 warps/SM), 3 -> 168 (12), 4 -> 128 (16), 5 -> 102 (20), 6 -> 85 (24),
-// 8 -> 64 (32).
+// (8 warps/SM), 4 -> 128 (16), 8 -> 64 (32), 12 -> 40 (48), 16 -> 32 (64).
+// The transport loop is latency-bound (instruction fetch and dependent
+// FP64 chains), so full residency wins despite the spills it forces.
 // NP is the chord piece capacity: 1 for absorbing z faces, 4 for periodic z.
 template <int MinBlocks, int NP>
 __global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(ElectronArgs A)
@@ -174,15 +173,14 @@ cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
                           cudaStream_t stream)
 {
     if (periodic) {
-        rrea_dev::electron_step_kernel<4, RREA_ARENA_MAX_PIECES><<<blocks, threads, 0, stream>>>(args);
+        rrea_dev::electron_step_kernel<16, RREA_ARENA_MAX_PIECES><<<blocks, threads, 0, stream>>>(args);
         return cudaGetLastError();
     }
     switch (min_blocks) {
-    case 3: rrea_dev::electron_step_kernel<3, 1><<<blocks, threads, 0, stream>>>(args); break;
     case 4: rrea_dev::electron_step_kernel<4, 1><<<blocks, threads, 0, stream>>>(args); break;
-    case 5: rrea_dev::electron_step_kernel<5, 1><<<blocks, threads, 0, stream>>>(args); break;
-    case 6: rrea_dev::electron_step_kernel<6, 1><<<blocks, threads, 0, stream>>>(args); break;
     case 8: rrea_dev::electron_step_kernel<8, 1><<<blocks, threads, 0, stream>>>(args); break;
+    case 12: rrea_dev::electron_step_kernel<12, 1><<<blocks, threads, 0, stream>>>(args); break;
+    case 16: rrea_dev::electron_step_kernel<16, 1><<<blocks, threads, 0, stream>>>(args); break;
     default: rrea_dev::electron_step_kernel<2, 1><<<blocks, threads, 0, stream>>>(args); break;
     }
     return cudaGetLastError();

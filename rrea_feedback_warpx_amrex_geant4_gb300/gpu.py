@@ -187,7 +187,7 @@ class RreaGpuContext:
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (er, ez, bt, amb_er, amb_ez)]
         self._check(self.lib.rrea_gpu_set_field(self.handle, *[a.ctypes.data_as(_D) for a in arrs]))
 
-    def set_launch(self, threads_per_block=128, blocks_per_sm=8, diagnostics=True):
+    def set_launch(self, threads_per_block=128, blocks_per_sm=16, diagnostics=True):
         self._check(self.lib.rrea_gpu_set_launch(self.handle, threads_per_block, blocks_per_sm, int(diagnostics)))
 
     def _apply(self, fn, arrays, step, dt_s, time_s, want_secondaries):
