@@ -8,8 +8,9 @@
  *        amrex::Real dt_s)
  * (native_amrex_rrea/warpx_overlay/Source/Rrea/RreaParticleInteraction.H:1609-1623,
  *  body in RreaParticleInteraction.cpp:12-62).  The overlay keeps that C++
- * signature; its body gathers the species tiles, calls rrea_gpu_apply_electrons()
- * and rrea_gpu_apply_photons(), and
+ * signature; its body gathers the species tiles, calls rrea_gpu_apply_electrons(),
+ * rrea_gpu_apply_photons() and rrea_gpu_apply_positrons() (the reference's
+ * phase order), and
  * raises amrex::Abort on a non-OK status, which preserves the fail-closed
  * contract of the reference (every guard aborts the whole step before any
  * side effect is committed).
@@ -177,6 +178,27 @@ rrea_gpu_status rrea_gpu_stage_electrons(rrea_gpu_ctx* ctx, const rrea_gpu_tile*
 rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s,
                                                  int64_t* n_secondaries);
 rrea_gpu_status rrea_gpu_fetch_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile);
+
+/*
+ * Drop-in for the positron phase of RreaParticleInteraction::Apply
+ * (TransportStep::ApplyPositronTransport, RreaPositronTransport.cpp:9-878):
+ * the electron engine with charge +1, the Bhabha / brems / in-flight
+ * annihilation channels (RreaChargedFinalStates.H:226-394,
+ * RreaTransportStep.H:563-702) and at-rest annihilation below the cutoff.
+ * Tile, secondaries and diagnostics as for electrons; disposition 2 means
+ * annihilated; secondaries carry root_species = RREA_SPECIES_POSITRON.
+ */
+rrea_gpu_status rrea_gpu_apply_positrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, int32_t step,
+                                         double time_s, double dt_s,
+                                         rrea_gpu_secondary* secondaries,
+                                         int64_t secondary_capacity, int64_t* n_secondaries);
+
+/* Resident positron mode: as the resident electron mode, on the context's
+ * positron tile. */
+rrea_gpu_status rrea_gpu_stage_positrons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile);
+rrea_gpu_status rrea_gpu_step_positrons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s,
+                                                 int64_t* n_secondaries);
+rrea_gpu_status rrea_gpu_fetch_positrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile);
 
 /*
  * Drop-in for the photon phase of RreaParticleInteraction::Apply

@@ -27,7 +27,7 @@ def build_oracle(force=False):
     return LIB
 
 
-def build_reference_checker(reference="/root/reference"):
+def build_reference_golden(reference="/root/reference"):
     """Builds oracle/_ref/ref_golden from the reference's own sources when the
     reference checkout is present (never on the GPU host)."""
     if not os.path.isdir(os.path.join(reference, "native_amrex_rrea")):

@@ -2,8 +2,8 @@
 
 ctypes wrapper over oracle/liboracle.so, the CPU restatement of the
 reference kinetic step.  Used by tests/, __graft_entry__.smoke() and the CPU
-baseline leg of bench.py as the checker; the shipped GPU library never loads
-it.
+baseline leg of bench.py to check and time the GPU path; the shipped GPU
+library never loads it.
 """
 import ctypes
 import os
@@ -69,6 +69,7 @@ def lib():
         _lib.oracle_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         _lib.oracle_electron_step.argtypes = [ctypes.POINTER(RreaGpuConfig), d, d, d, d, d, ctypes.c_int32,
                                               ctypes.c_double, ctypes.POINTER(RreaGpuTile)]
+        _lib.oracle_positron_step.argtypes = _lib.oracle_electron_step.argtypes
         _lib.oracle_photon_step.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_int32, ctypes.c_double,
                                             ctypes.POINTER(RreaGpuTile)]
         _lib.oracle_counts.argtypes = [ctypes.POINTER(ctypes.c_int64)] * 3
@@ -144,6 +145,16 @@ def electron_step(cfg, field, step, dt_s, arrays):
     cfg = as_config(cfg)
     t = make_tile_struct(arrays)
     _check(lib().oracle_electron_step(ctypes.byref(cfg), _dptr(field["er"]), _dptr(field["ez"]),
+                                      _dptr(field["bt"]), _dptr(field["amb_er"]), _dptr(field["amb_ez"]),
+                                      step, dt_s, ctypes.byref(t)))
+    return _collect(cfg, t)
+
+
+def positron_step(cfg, field, step, dt_s, arrays):
+    """Runs the oracle positron phase in place on `arrays` (numpy tile)."""
+    cfg = as_config(cfg)
+    t = make_tile_struct(arrays)
+    _check(lib().oracle_positron_step(ctypes.byref(cfg), _dptr(field["er"]), _dptr(field["ez"]),
                                       _dptr(field["bt"]), _dptr(field["amb_er"]), _dptr(field["amb_ez"]),
                                       step, dt_s, ctypes.byref(t)))
     return _collect(cfg, t)

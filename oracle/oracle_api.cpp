@@ -67,9 +67,25 @@ void oracle_rng(uint64_t const* keys, int64_t n, uint64_t* counter, double* unif
 // Arena export so tests can compare the host loader against the device copy.
 int64_t oracle_arena_size() { return g_tables ? static_cast<int64_t>(g_tables->arena().size()) : 0; }
 
+int charged_step(bool positron, rrea_gpu_config const* cfg, double const* er, double const* ez, double const* bt,
+                 double const* amb_er, double const* amb_ez, int32_t step, double dt_s, rrea_gpu_tile const* tile);
+
 int oracle_electron_step(rrea_gpu_config const* cfg, double const* er, double const* ez, double const* bt,
                          double const* amb_er, double const* amb_ez, int32_t step, double dt_s,
                          rrea_gpu_tile const* tile)
+{
+    return charged_step(false, cfg, er, ez, bt, amb_er, amb_ez, step, dt_s, tile);
+}
+
+int oracle_positron_step(rrea_gpu_config const* cfg, double const* er, double const* ez, double const* bt,
+                         double const* amb_er, double const* amb_ez, int32_t step, double dt_s,
+                         rrea_gpu_tile const* tile)
+{
+    return charged_step(true, cfg, er, ez, bt, amb_er, amb_ez, step, dt_s, tile);
+}
+
+int charged_step(bool positron, rrea_gpu_config const* cfg, double const* er, double const* ez, double const* bt,
+                 double const* amb_er, double const* amb_ez, int32_t step, double dt_s, rrea_gpu_tile const* tile)
 {
     if (!g_tables) return RREA_GPU_ERR_NOT_READY;
     try {
@@ -96,7 +112,11 @@ int oracle_electron_step(rrea_gpu_config const* cfg, double const* er, double co
         t.id = tile->id;
         t.cpu = tile->cpu;
         g_out.clear();
-        oracle::ApplyElectronTransport(*g_tables, *cfg, fg, step, dt_s, t, g_out);
+        if (positron) {
+            oracle::ApplyPositronTransport(*g_tables, *cfg, fg, step, dt_s, t, g_out);
+        } else {
+            oracle::ApplyElectronTransport(*g_tables, *cfg, fg, step, dt_s, t, g_out);
+        }
         g_cells.nr = cfg->nr;
         g_cells.nz = cfg->nz;
         for (auto& f : g_cells.f) f.assign(static_cast<std::size_t>(cfg->nr) * cfg->nz, 0.0);

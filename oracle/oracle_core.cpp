@@ -255,6 +255,36 @@ struct Tables {
         if (ix.hard_moller_threshold_eV > 0.0 && e <= 2.0 * ix.hard_moller_threshold_eV) return 1.0e99;
         return mfp_from_inverse(inv * dr);
     }
+    // :3129-3178, 3196-3206
+    double PositronCollisionLoss(double e, double dr) const { return interpolate(RREA_T_P_COLLISION, e) * dr; }
+    double PositronSoftRadiativeDrag(double e, double dr) const { return interpolate(RREA_T_P_SOFT_RAD, e) * dr; }
+    double PositronBremsstrahlungMeanFreePath(double e, double dr) const
+    {
+        return mfp_from_inverse(interpolate(RREA_T_P_TRACKED_BREMS, e) * dr);
+    }
+    double PositronHardBhabhaMeanFreePath(double e, double dr) const
+    {
+        double const inv = interpolate(RREA_T_P_HARD_BHABHA, e);
+        if (ix.hard_moller_threshold_eV > 0.0 && e <= ix.hard_moller_threshold_eV) return 1.0e99;
+        return mfp_from_inverse(inv * dr);
+    }
+    double PositronAnnihilationMeanFreePath(double e, double dr) const
+    {
+        return mfp_from_inverse(interpolate(RREA_T_P_ANNIHILATION, e) * dr);
+    }
+    // :2325-2353 (the three rates the positron channel gates read)
+    void PositronGateRates(double e, double& bhabha_inv, double& brems_inv, double& annihilation_inv) const
+    {
+        if (!(e >= ix.charged_min_eV && e <= ix.charged_max_eV)) {
+            fail(RREA_GPU_ERR_RANGE, "schema-6 positron energy outside the certified range");
+        }
+        interpolate(RREA_T_P_COLLISION, e);
+        interpolate(RREA_T_P_SOFT_RAD, e);
+        bhabha_inv = interpolate(RREA_T_P_HARD_BHABHA, e);
+        brems_inv = interpolate(RREA_T_P_TRACKED_BREMS, e);
+        interpolate(RREA_T_P_ELASTIC_TRANSPORT, e);
+        annihilation_inv = interpolate(RREA_T_P_ANNIHILATION, e);
+    }
     // :2666-2676
     double ElectronBremsstrahlungMeanFreePath(double e, double dr) const
     {
@@ -427,6 +457,17 @@ struct Tables {
     {
         require_charged(e);
         return rrea_host::HostSampleConditional(t, RREA_C_BREMS_E, e, u, false);
+    }
+    // :3180-3194 and :2562-2575 (general sampler, log interpolation between groups)
+    double SamplePositronBhabhaSecondaryEnergy(double e, double u) const
+    {
+        require_charged(e);
+        return rrea_host::HostSampleConditional(t, RREA_C_BHABHA, e, u, false);
+    }
+    double SamplePositronBremsstrahlungPhotonEnergy(double e, double u) const
+    {
+        require_charged(e);
+        return rrea_host::HostSampleConditional(t, RREA_C_BREMS_P, e, u, false);
     }
     // :2714-2760
     double SampleBremsstrahlungCosTheta(double e, double cdf_u) const
@@ -1879,6 +1920,527 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
 }
 
 // ======================================================================
+// Positron phase: O/RreaPositronTransport.cpp:9-878 with the Bhabha and
+// brems final states of O/RreaChargedFinalStates.H:226-394 and
+// TransportStep::spawn_positron_annihilation (O/RreaTransportStep.H:563-702).
+// ======================================================================
+namespace {
+
+// spawn_positron_annihilation (O/RreaTransportStep.H:563-702).  `emit` and
+// `deposit` are the caller's secondary and ion-pair sinks.
+template <typename Emit, typename Deposit, typename Source>
+void spawn_annihilation(Tables const& tables, double photon_cut, double x, double y, double z, double r,
+                        double zs, double ax, double ay, double az, double w, double k, bool at_rest,
+                        double d_energy, double d_azim, double birth, Emit&& emit, Deposit&& deposit,
+                        Source&& source)
+{
+    if (w <= 0.0) return;
+    normalize(ax, ay, az);
+    double const ka = at_rest ? 0.0 : std::max(k, 0.0);
+    AnnihilationState const an = sample_annihilation(tables, ka, d_energy, d_azim);
+    double g1x, g1y, g1z;
+    cone_direction(ax, ay, az, an.cos1, an.azim, g1x, g1y, g1z);
+    double const e1 = std::max(an.e1, 0.0), e2 = std::max(an.e2, 0.0);
+    double g2x = -g1x, g2y = -g1y, g2z = -g1z;
+    if (!an.at_rest && e2 > 0.0) {
+        double const p = std::sqrt(std::max(0.0, ka * (ka + 2.0 * kMeC2)));
+        g2x = (p * ax - e1 * g1x) / e2;
+        g2y = (p * ay - e1 * g1y) / e2;
+        g2z = (p * az - e1 * g1z) / e2;
+        normalize(g2x, g2y, g2z);
+    }
+    double local = 0.0;
+    if (e1 >= photon_cut) emit(x, y, z, g1x, g1y, g1z, e1, birth);
+    else local += e1;
+    if (e2 >= photon_cut) emit(x, y, z, g2x, g2y, g2z, e2, birth);
+    else local += e2;
+    if (at_rest && k > 0.0) deposit(r, zs, w, k);
+    if (local > 0.0) deposit(r, zs, w, local);
+    source(r, zs, w);
+}
+
+}  // namespace
+
+void ApplyPositronTransport(TableSet const& ts, rrea_gpu_config const& cfg, FieldGrid const& field, int step,
+                            double dt_s, ChargedTile& tile, StepOutputs& out)
+{
+    Tables const tables(ts);
+    Gather const gather{field, cfg};
+    double const rlo = cfg.r_lo, rhi = cfg.r_hi, zlo = cfg.z_lo, zhi = cfg.z_hi;
+    bool const periodic = cfg.periodic_z != 0;
+    double const cutoff = cfg.low_energy_cutoff_eV;
+    double const photon_cut = cfg.photon_cutoff_eV;
+    double const hm_thr = ts.index().hard_moller_threshold_eV;
+    double const density_ratio = positive_or(cfg.density_ratio, 1.0);
+    uint64_t const seed = cfg.rng_seed;
+    uint64_t const step_key = static_cast<uint64_t>(std::max(step, 0));
+    double const w_air = ts.index().w_air_eV_per_pair;
+
+    out.subcycles.assign(static_cast<std::size_t>(tile.n), 0);
+    out.events.assign(static_cast<std::size_t>(tile.n), 0);
+    out.disposition.assign(static_cast<std::size_t>(tile.n), -1);
+
+    constexpr int64_t kChunk = 64;
+    int64_t const n_chunks = (tile.n + kChunk - 1) / kChunk;
+    std::vector<StepOutputs> chunk_out(static_cast<std::size_t>(n_chunks));
+    std::vector<int> chunk_err(static_cast<std::size_t>(n_chunks), 0);
+    std::vector<std::string> chunk_msg(static_cast<std::size_t>(n_chunks));
+#pragma omp parallel for schedule(dynamic, 1) if (n_chunks > 1)
+    for (int64_t chunk = 0; chunk < n_chunks; ++chunk) {
+      StepOutputs& cout = chunk_out[static_cast<std::size_t>(chunk)];
+      try {
+      int64_t const ip_end = std::min(tile.n, (chunk + 1) * kChunk);
+      for (int64_t ip = chunk * kChunk; ip < ip_end; ++ip) {
+        if (!(tile.id[ip] > 0)) continue;
+        std::size_t const sp = static_cast<std::size_t>(ip);
+        uint64_t lineage = 0;
+        int current_process = 0;
+        // ---- BeginRunningChargedParticle (O/RreaTransportStep.H:720-820), charge +1
+        uint64_t const key = static_cast<uint64_t>(std::llabs(tile.id[ip]))
+            ^ (static_cast<uint64_t>(tile.cpu ? tile.cpu[ip] : 0) << 40);
+        double const weight = tile.w[ip];
+        if (weight <= 0.0) {
+            tile.id[ip] = -tile.id[ip];
+            out.disposition[sp] = 3;
+            continue;
+        }
+        if (tile.prev_r[ip] > rhi + 1.0e-9 * rhi) {
+            fail(RREA_GPU_ERR_GEOMETRY, "RREA positron survived outside the domain");
+        }
+        double dx = tile.prev_ux[ip], dy = tile.prev_uy[ip], dz = tile.prev_uz[ip];
+        double k = kinetic_from_proper_velocity(dx, dy, dz);
+        normalize(dx, dy, dz);
+        double const seed_r = tile.prev_r[ip], seed_th = tile.prev_theta[ip];
+        double run_x = seed_r * std::cos(seed_th);
+        double run_y = seed_r * std::sin(seed_th);
+        double run_z = tile.prev_z[ip];
+        double const x_particle = run_x, y_particle = run_y;
+        double const r_particle = seed_r, z_particle = run_z;
+
+        auto build_chord = [&](double req_dt, Path& path) -> bool {
+            // O/RreaParticleInteraction.H:110-161
+            if (!std::isfinite(req_dt) || !std::isfinite(dt_s) || !(req_dt >= 0.0) || !(dt_s > 0.0)) return false;
+            double const speed = charged_speed(k);
+            double const dn = std::sqrt(dx * dx + dy * dy + dz * dz);
+            if (!std::isfinite(speed) || !std::isfinite(dn) || !(dn > 0.0)) return false;
+            double const sc = speed * req_dt / dn;
+            double const exx = run_x + sc * dx, eyy = run_y + sc * dy, ezz = run_z + sc * dz;
+            path = ClipRz(std::hypot(run_x, run_y), std::atan2(run_y, run_x), run_z, std::hypot(exx, eyy),
+                          std::atan2(eyy, exx), ezz, rlo, rhi, zlo, zhi, periodic);
+            return std::isfinite(path.full) && path.in_begin == 0.0;
+        };
+
+        Path driver;
+        bool const driver_valid = build_chord(dt_s, driver);
+        EscapePolicy escape = clipped_escape_policy(driver, std::hypot(driver.ex, driver.ey), driver.ez);
+        double const ds = driver_valid ? driver.in_length : 0.0;
+        std::vector<Interval> const driver_iv = build_intervals(driver, density_ratio, density_ratio);
+        double const driver_span = std::max(driver.in_end, 1.0e-6);
+        double const field_work = path_field_work(gather, driver, 1.0, 0.0, 1.0).work / driver_span;
+        Path path = driver;
+        std::vector<Interval> iv = driver_iv;
+
+        auto push_source = [&](int kind, double r, double z, double w, double sec, double loss) {
+            cout.sources.push_back(Source{kind, r, z, w, sec, loss, ip});
+        };
+        auto push_segment = [&](int kind, std::array<double, 7> const& a, uint64_t ch, uint32_t faces) {
+            Segment sg;
+            sg.kind = kind;
+            for (int c = 0; c < 7; ++c) sg.a[c] = a[c];
+            sg.channel = ch;
+            sg.faces = faces;
+            sg.parent_index = ip;
+            cout.segments.push_back(sg);
+        };
+        auto add_secondary = [&](int species, double x, double y, double z, double sx, double sy, double sz,
+                                 double e, double birth) {
+            Secondary s2;
+            s2.species = species;
+            s2.process = current_process;
+            s2.x = x; s2.y = y; s2.z = z;
+            s2.dx = sx; s2.dy = sy; s2.dz = sz;
+            s2.w = weight;
+            s2.energy = e;
+            s2.birth = birth;
+            s2.root_key = key;
+            s2.lineage = lineage++;
+            s2.root_species = 1;
+            s2.parent_index = ip;
+            cout.secondaries.push_back(s2);
+        };
+        auto deposit_local = [&](double r, double z, double w, double e) {
+            if (w <= 0.0 || e <= 0.0) return;
+            double const pw = w * e / std::max(w_air, 1.0);
+            if (pw <= 0.0) return;
+            push_source(0, r, z, pw, 0.0, w_air);
+        };
+        auto annihilate = [&](double x, double y, double z, double r, double w, double ke, bool at_rest,
+                              uint64_t idx, double birth) {
+            current_process = 9;  // PositronAnnihilation
+            spawn_annihilation(
+                tables, photon_cut, x, y, z, r, z, dx, dy, dz, w, ke, at_rest,
+                rng_uniform(seed, key, step_key, idx, kAnnihilationPolar),
+                rng_uniform(seed, key, step_key, idx, kAnnihilationAzimuth), birth,
+                [&](double px, double py, double pz, double gx, double gy, double gz, double e, double b) {
+                    add_secondary(2, px, py, pz, gx, gy, gz, e, b);
+                },
+                deposit_local, [&](double rr, double zz, double ww) { push_source(2, rr, zz, ww, 0.0, 0.0); });
+        };
+        // CommitChargedEscape (O/RreaTransportStep.H:829-863), mesh weight +w
+        auto commit_escape = [&]() {
+            double const u = proper_velocity_from_kinetic(k);
+            tile.ux[ip] = u * dx;
+            tile.uy[ip] = u * dy;
+            tile.uz[ip] = u * dz;
+            Crossing const c = boundary_crossing(path);
+            push_segment(1, {r_particle, z_particle, c.sr, c.sz, c.cr, c.cz, weight}, 1u, c.faces);
+            if (escape.invalidate) tile.id[ip] = -tile.id[ip];
+            out.disposition[sp] = 1;
+        };
+
+        // :112-160
+        bool const below = k < cutoff;
+        if (escape.escapes && below) { commit_escape(); continue; }
+        if (!escape.escapes && below) {
+            annihilate(x_particle, y_particle, z_particle, r_particle, weight, k, true, 0, 1.0);
+            push_segment(0, {r_particle, z_particle, r_particle, z_particle, weight, 0.0, 0.0}, 4u, 0u);
+            tile.id[ip] = -tile.id[ip];
+            out.disposition[sp] = 2;
+            continue;
+        }
+        if (ds <= 0.0) {
+            if (escape.escapes) commit_escape();
+            else out.disposition[sp] = 0;
+            continue;
+        }
+        if (driver_iv.empty()) fail(RREA_GPU_ERR_INVALID_STATE, "positron path has positive length but no material");
+
+        // RreaChargedCompetingStpRates(is_positron) (O/RreaChargedFinalStates.H:107-152)
+        auto competing = [&](double e) {
+            std::array<double, 3> s{};
+            bool const b_open = !(hm_thr > 0.0 && e <= hm_thr);
+            if (b_open) {
+                double const mfp = tables.PositronHardBhabhaMeanFreePath(e, 1.0);
+                s[0] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+            } else {
+                s[0] = frozen_rate(0.0);
+            }
+            if (e > photon_cut) {
+                double const mfp = tables.PositronBremsstrahlungMeanFreePath(e, 1.0);
+                s[1] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+            } else {
+                s[1] = frozen_rate(0.0);
+            }
+            double const mfp = tables.PositronAnnihilationMeanFreePath(e, 1.0);
+            s[2] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+            return s;
+        };
+        // RreaChargedChannelOpenAt(is_positron) (O/RreaChargedFinalStates.H:56-81)
+        auto channel_open = [&](int ch, double e) {
+            double bi, ri, ai;
+            tables.PositronGateRates(e, bi, ri, ai);
+            if (ch == 0) return !(hm_thr > 0.0 && e <= hm_thr) && bi > 0.0;
+            if (ch == 1) return e > photon_cut && ri > 0.0;
+            if (ch == 2) return ai > 0.0;
+            return false;
+        };
+
+        std::array<double, 3> const init = competing(k);
+        double const init_total = init[0] + init[1] + init[2];
+        double const driver_dpath = density_path(driver_iv, driver, driver.in_begin, driver.in_end) / driver_span;
+        bool viol = false;
+        uint64_t subcycles =
+            selected_material_subcycles(init_total * driver_dpath, driver_iv, driver, cfg, viol, init_total);
+        {
+            double const gs_n = frozen_rate([&] {
+                double const mfp = tables.ElasticMeanFreePath(1, k, 1.0);
+                return mfp > 0.0 ? 1.0 / mfp : 0.0;
+            }()) * driver_dpath;
+            double const drag_est = tables.PositronCollisionLoss(std::max(k, cutoff), 1.0) * driver_dpath;
+            double const impulse = std::max(cfg.max_field_impulse_fraction * k,
+                                            std::max(cfg.field_impulse_floor_eV, 1.0));
+            uint64_t const gsd = driver_count(std::min(gs_n, cfg.gs_total_collision_cap),
+                                              std::max(cfg.max_gs_collisions_per_substep, 1.0));
+            uint64_t const imd = driver_count(std::abs(field_work) + drag_est, impulse);
+            subcycles = std::min<uint64_t>(std::max({subcycles, gsd, imd}), cfg.max_subcycles);
+        }
+        if (cfg.strict_transport_guards && viol) {
+            fail(RREA_GPU_ERR_GUARD, "strict transport guard: optical-depth subcycle cap exceeded");
+        }
+        out.subcycles[sp] = subcycles;
+
+        bool exited = false;
+        bool annihilated = false;
+        uint64_t completed = 0;
+        bool stopped = false;
+        double stop_x = x_particle, stop_y = y_particle, stop_z = z_particle, stop_r = r_particle;
+        double stop_elapsed = 1.0;
+        double const sub_dt = dt_s / static_cast<double>(subcycles);
+        FieldRange sub_field;
+        double sub_dt_eff = 0.0;
+        uint64_t events = 0;
+
+        auto elapsed_at = [&](double f) {
+            double const within = std::min(1.0, std::max(0.0, f));
+            return std::min(1.0, (static_cast<double>(completed) + within) / static_cast<double>(subcycles));
+        };
+        auto mark_stopped = [&](double f) {
+            if (path.exits && f >= path.in_end) { exited = true; return; }
+            double x, y, z;
+            path.PointAtFull(f, x, y, z);
+            if (!cartesian_half_open(x, y, z, rlo, rhi, zlo, zhi)) { exited = true; return; }
+            stop_x = x;
+            stop_y = y;
+            stop_z = z;
+            stop_r = std::hypot(x, y);
+            stop_elapsed = elapsed_at(f);
+            stopped = true;
+        };
+        // apply_positron_continuous_segment (:268-365)
+        auto continuous = [&](double b, double e, double stop_e) -> Limit {
+            auto dp = [&](double bb, double ee) { return density_path(iv, path, bb, ee); };
+            double sc = 0, ss = 0;
+            bool const need = (e > b) && (k > 0.0) && !(stop_e < cutoff);
+            if (need) {
+                sc = frozen_rate(tables.PositronCollisionLoss(stop_e, 1.0));
+                ss = frozen_rate(tables.PositronSoftRadiativeDrag(stop_e, 1.0));
+            }
+            DragPlan const plan = plan_drag(b, e, k, stop_e, cutoff, dp, sc, ss, 0.0);
+            if (!plan.limit_valid) fail(RREA_GPU_ERR_INVALID_STATE, "positron stopping has no monotone cutoff point");
+            if (!plan.applied) return Limit{b, false, true};
+            k = std::max(0.0, k - plan.drag);
+            if (plan.reaches) k = cutoff;
+            if (plan.collision > 0.0 && plan.raw_collision > 0.0) {
+                for (Interval const& i : iv) {
+                    double const bb = std::max(b, i.begin), ee = std::min(plan.end, i.end);
+                    if (!(ee > bb)) continue;
+                    double const raw = path.full * (ee - bb) * i.density * plan.collision_stp;
+                    double const loss = plan.collision * raw / plan.raw_collision;
+                    double const pw = weight * loss / std::max(w_air, 1.0);
+                    if (!(pw > 0.0)) continue;
+                    double x, y, z;
+                    path.PointAtFull(0.5 * (bb + ee), x, y, z);
+                    push_source(0, std::hypot(x, y), z, pw, 0.0, w_air);
+                }
+            }
+            return Limit{plan.end, plan.reaches, true};
+        };
+
+        for (uint64_t sub = 0; sub < subcycles; ++sub) {
+            if (k < cutoff) break;
+            double sb = 0.0, se = 0.0;
+            {
+                Path np;
+                if (!build_chord(sub_dt, np)) break;
+                path = np;
+                if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
+                    exited = path.exits;
+                    break;
+                }
+                iv = build_intervals(path, density_ratio, density_ratio);
+                if (iv.empty()) fail(RREA_GPU_ERR_INVALID_STATE, "positron microchord with no material intervals");
+                sb = path.in_begin;
+                se = path.in_end;
+                sub_field = path_field_work(gather, path, 1.0, sb, se);
+                sub_dt_eff = sub_dt * (se - sb);
+                half_kick(sub_field, 0.5 * sub_dt_eff, 1.0, k, dx, dy, dz);
+                if (k < cutoff) { mark_stopped(sb); break; }
+            }
+            {
+                std::array<double, 3> stp{};
+                uint64_t rng_index = 0;
+                double ex = 0, ey = 0, ez = 0, er = 0;
+                double rem = sb;
+                uint64_t ordinal = 0;
+                while (rem < se && k >= cutoff) {
+                    if (ordinal >= kEventCap) fail(RREA_GPU_ERR_RNG_OVERFLOW, "positron event ordinal overflow");
+                    double const frozen = k;
+                    stp = competing(frozen);
+                    double const total_stp = stp[0] + stp[1] + stp[2];
+                    double const seg_dp = density_path(iv, path, rem, se);
+                    std::array<double, 3> const taus = {stp[0] * seg_dp, stp[1] * seg_dp, stp[2] * seg_dp};
+                    if (!try_live_hazard_index(1, sub, ordinal, rng_index)) {
+                        fail(RREA_GPU_ERR_RNG_OVERFLOW, "positron repeated-hazard RNG index overflow");
+                    }
+                    ++events;
+                    uint64_t const od_ch =
+                        ordinal == 0 ? kPositronCompetingOpticalDepth : kPositronContinuationOpticalDepth;
+                    uint64_t const cc_ch = ordinal == 0 ? kPositronCompetingChannel : kPositronContinuationChannel;
+                    double const u1 = rng_uniform(seed, key, step_key, rng_index, od_ch);
+                    double const u2 = rng_uniform(seed, key, step_key, rng_index, cc_ch);
+                    Selection const sel = select_hazard(taus, 3, u1, u2);
+                    double ev_frac = 0.0;
+                    bool split_valid = false;
+                    if (sel.valid && sel.event) {
+                        ev_frac = fraction_at_density_path(iv, path, rem, se, sel.sampled / total_stp);
+                        split_valid = std::isfinite(rem) && std::isfinite(ev_frac) && std::isfinite(se) && (se > rem)
+                            && !(ev_frac < rem) && !(ev_frac > se);
+                    }
+                    if (!sel.valid) fail(RREA_GPU_ERR_INVALID_STATE, "positron competing-hazard selection invalid");
+                    if (!sel.event) {
+                        Limit const l = continuous(rem, se, frozen);
+                        if (l.reaches) mark_stopped(l.end);
+                        break;
+                    }
+                    if (!split_valid) fail(RREA_GPU_ERR_INVALID_STATE, "sampled event depth outside its subcycle");
+                    path.PointAtFull(ev_frac, ex, ey, ez);
+                    er = std::hypot(ex, ey);
+                    Limit const l = continuous(rem, ev_frac, frozen);
+                    if (l.reaches) { mark_stopped(l.end); break; }
+                    bool const open_ev = k >= cutoff && channel_open(sel.channel, k);
+                    if (!open_ev) {
+                        bool const open_fr = frozen >= cutoff && channel_open(sel.channel, frozen);
+                        if (!open_fr) fail(RREA_GPU_ERR_INVALID_STATE, "selected channel closed before its event depth");
+                        rem = ev_frac;
+                        ++ordinal;
+                        continue;
+                    }
+                    double const birth = elapsed_at(ev_frac);
+                    if (sel.channel == 0) {
+                        // RreaApplyBhabhaFinalState (O/RreaChargedFinalStates.H:238-288)
+                        double const kb = k;
+                        double const sec = std::min(
+                            tables.SamplePositronBhabhaSecondaryEnergy(
+                                kb, rng_uniform(seed, key, step_key, rng_index, kPositronBhabhaEnergy)),
+                            std::max(0.0, kb));
+                        if (sec > 0.0 && !(hm_thr > 0.0 && sec < hm_thr)) {
+                            double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
+                            moller_lab_directions(dx, dy, dz, kb, sec,
+                                                  rng_uniform(seed, key, step_key, rng_index, kPositronBhabhaAzimuth),
+                                                  pdx, pdy, pdz, sdx, sdy, sdz);
+                            k = std::max(0.0, kb - sec);
+                            dx = pdx; dy = pdy; dz = pdz;
+                            current_process = 3;  // HardBhabha
+                            add_secondary(0, ex, ey, ez, sdx, sdy, sdz, sec, birth);
+                            push_source(2, er, ez, weight, 0.0, sec);
+                        }
+                    } else if (sel.channel == 1) {
+                        // RreaApplyBremsFinalState, positron CDF (O/RreaChargedFinalStates.H:329-394)
+                        double const kb = k;
+                        double const eu = rng_uniform(seed, key, step_key, rng_index, kPositronBremsEnergy);
+                        double const sampled = tables.SamplePositronBremsstrahlungPhotonEnergy(kb, eu);
+                        double const eg = std::min(std::max(sampled, 0.0), std::max(kb, 0.0));
+                        double const after = std::max(0.0, std::max(kb, 0.0) - eg);
+                        bool const tracked = std::isfinite(photon_cut) && photon_cut >= 0.0 && eg >= photon_cut;
+                        double gx = dx, gy = dy, gz = dz;
+                        double const ct = tables.SampleBremsstrahlungCosTheta(
+                            kb, rng_uniform(seed, key, step_key, rng_index, kPositronBremsAngle));
+                        cone_direction(dx, dy, dz, ct,
+                                       rng_uniform(seed, key, step_key, rng_index, kPositronBremsAzimuth), gx, gy, gz);
+                        photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
+                        k = after;
+                        current_process = 4;  // Bremsstrahlung
+                        if (tracked) {
+                            add_secondary(2, ex, ey, ez, gx, gy, gz, eg, birth);
+                        } else if (eg > 0.0) {
+                            deposit_local(er, ez, weight, eg);
+                        }
+                    } else {
+                        // in-flight annihilation (:700-727)
+                        annihilate(ex, ey, ez, er, weight, k, false, rng_index, birth);
+                        push_segment(0, {r_particle, z_particle, er, ez, weight, 0.0, 0.0}, 4u, 0u);
+                        annihilated = true;
+                        break;
+                    }
+                    if (k <= cutoff) { mark_stopped(ev_frac); break; }
+                    rem = ev_frac;
+                    ++ordinal;
+                }
+            }
+            if (stopped || annihilated) break;
+            // finish_interleaved_substep (:478-499)
+            {
+                if (k >= cutoff) {
+                    double const mfp = tables.ElasticMeanFreePath(1, k, 1.0);
+                    double const gs_n = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0) * density_path(iv, path, sb, se);
+                    if (gs_n > 0.0) {
+                        auto gkey = [&](uint64_t ch, uint64_t inner) {
+                            return rng_uniform(seed, key, step_key, (sub << 8) | inner, ch);
+                        };
+                        auto deflect = [&](double ct, double uphi) {
+                            double nx, ny, nz;
+                            cone_direction(dx, dy, dz, ct, uphi, nx, ny, nz);
+                            dx = nx; dy = ny; dz = nz;
+                        };
+                        double const few = ts.index().gs_few_collision_threshold;
+                        if (gs_n < few) {
+                            int const cap = static_cast<int>(std::ceil(3.0 * few));
+                            if (cap >= 255) fail(RREA_GPU_ERR_INVALID_STATE, "GS few-collision cap too large");
+                            int const cnt = poisson_capped(gs_n, gkey(kPositronGsFewCount, 0), cap);
+                            for (int q = 0; q < cnt; ++q) {
+                                double const ct = tables.SampleSingleElasticCosTheta(
+                                    1, k, gkey(kPositronGsFewScatter, static_cast<uint64_t>(q + 1)));
+                                deflect(ct, gkey(kPositronGsFewAzimuth, static_cast<uint64_t>(q + 1)));
+                            }
+                        } else {
+                            double const ct = tables.SampleGsCosTheta(1, k, gs_n, gkey(kPositronGsAngle, 0));
+                            deflect(ct, gkey(kPositronGsAzimuth, 0));
+                        }
+                    }
+                }
+                half_kick(sub_field, 0.5 * sub_dt_eff, 1.0, k, dx, dy, dz);
+                if (k < cutoff) { mark_stopped(se); break; }
+            }
+            if (!advance_running(path, se, rlo, rhi, zlo, zhi, run_x, run_y, run_z)) { exited = true; break; }
+            if (path.exits) { exited = true; break; }
+            completed = sub + 1U;
+        }
+        out.events[sp] = events;
+        if (exited) {
+            escape = clipped_escape_policy(path, std::hypot(path.ex, path.ey), path.ez);
+        }
+        if (annihilated) {
+            tile.id[ip] = -tile.id[ip];
+            out.disposition[sp] = 2;
+            continue;
+        }
+        // RreaResolveChargedTransportTerminal (O/RreaParticleInteraction.H:292-312)
+        int disp;
+        if (exited) disp = 1;
+        else if (stopped) disp = 2;
+        else disp = k < cutoff ? 2 : 0;
+        if (disp == 1) { commit_escape(); continue; }
+        if (disp == 2) {
+            double const ax = stopped ? stop_x : run_x;
+            double const ay = stopped ? stop_y : run_y;
+            double const az = stopped ? stop_z : run_z;
+            double const ar = stopped ? stop_r : std::hypot(run_x, run_y);
+            annihilate(ax, ay, az, ar, weight, k, true, subcycles, stopped ? stop_elapsed : 1.0);
+            push_segment(0, {r_particle, z_particle, ar, az, weight, 0.0, 0.0}, 4u, 0u);
+            tile.id[ip] = -tile.id[ip];
+            out.disposition[sp] = 2;
+            continue;
+        }
+        // CommitSurvivorChargedWriteback (O/RreaTransportStep.H:874-905)
+        double const end_r = std::hypot(run_x, run_y);
+        double const um = proper_velocity_from_kinetic(k);
+        tile.ux[ip] = um * dx;
+        tile.uy[ip] = um * dy;
+        tile.uz[ip] = um * dz;
+        tile.r[ip] = end_r;
+        tile.theta[ip] = std::atan2(run_y, run_x);
+        tile.z[ip] = run_z;
+        push_segment(0, {r_particle, z_particle, end_r, run_z, weight, 0.0, 0.0}, 0u, 0u);
+        out.disposition[sp] = 0;
+      }
+      } catch (OracleError const& e) {
+        chunk_err[static_cast<std::size_t>(chunk)] = e.code;
+        chunk_msg[static_cast<std::size_t>(chunk)] = e.what();
+      }
+    }
+    for (int64_t chunk = 0; chunk < n_chunks; ++chunk) {
+        if (chunk_err[static_cast<std::size_t>(chunk)] != 0) {
+            fail(chunk_err[static_cast<std::size_t>(chunk)], chunk_msg[static_cast<std::size_t>(chunk)]);
+        }
+    }
+    for (auto& c : chunk_out) {
+        out.secondaries.insert(out.secondaries.end(), c.secondaries.begin(), c.secondaries.end());
+        out.sources.insert(out.sources.end(), c.sources.begin(), c.sources.end());
+        out.segments.insert(out.segments.end(), c.segments.begin(), c.segments.end());
+    }
+}
+
+// ======================================================================
 // Photon phase: O/RreaPhotonTransport.cpp:9-461 with the final states of
 // O/RreaPhotonFinalStates.H:56-365 and TransportStep::spawn_positron_annihilation
 // (O/RreaTransportStep.H:563-702).  The photon tile's current (r, theta, z)
@@ -2289,6 +2851,18 @@ int RunPrimitive(TableSet const& ts, int which, double const* in, int64_t n, dou
             o[0] = an.e1; o[1] = an.e2; o[2] = an.cos1; o[3] = an.azim; o[4] = an.valid; o[5] = an.at_rest;
             break;
         }
+        case 22: {  // (e, dr) -> positron collision, soft, Bhabha MFP, brems MFP, annihilation MFP
+            double const e = in[2 * i], dr = in[2 * i + 1];
+            double* o = out + 5 * i;
+            o[0] = t.PositronCollisionLoss(e, dr);
+            o[1] = t.PositronSoftRadiativeDrag(e, dr);
+            o[2] = t.PositronHardBhabhaMeanFreePath(e, dr);
+            o[3] = t.PositronBremsstrahlungMeanFreePath(e, dr);
+            o[4] = t.PositronAnnihilationMeanFreePath(e, dr);
+            break;
+        }
+        case 23: out[i] = t.SamplePositronBhabhaSecondaryEnergy(in[2 * i], in[2 * i + 1]); break;
+        case 24: out[i] = t.SamplePositronBremsstrahlungPhotonEnergy(in[2 * i], in[2 * i + 1]); break;
         default:
             fail(RREA_GPU_ERR_ARGUMENT, "unknown primitive");
         }

@@ -1,8 +1,8 @@
 // ORACLE — test infrastructure only.  A scalar CPU restatement of the
 // reference's per-timestep kinetic step (RREA overlay,
 // native_amrex_rrea/warpx_overlay/Source/Rrea/ and native_amrex_rrea/src/),
-// used by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the
-// checker.  The shipped GPU path never calls into this directory.
+// used by tests/, __graft_entry__.smoke() and bench.py's CPU baseline to
+// check the GPU path.  The shipped GPU path never calls into this directory.
 //
 // Every function cites the reference file:line it restates.  Shorthand:
 //   O/ = native_amrex_rrea/warpx_overlay/Source/Rrea/
@@ -67,6 +67,13 @@ enum Channel : uint64_t {
     kElectronGsFewScatter = 92, kElectronGsFewAzimuth = 93,
     kElectronCompetingOpticalDepth = 107, kElectronCompetingChannel = 108,
     kElectronContinuationOpticalDepth = 124, kElectronContinuationChannel = 125,
+    kPositronBhabhaEnergy = 74, kPositronBremsEnergy = 76, kPositronBremsAngle = 77, kPositronBremsAzimuth = 78,
+    kAnnihilationPolar = 80, kAnnihilationAzimuth = 81,
+    kPositronGsAngle = 94, kPositronGsAzimuth = 95, kPositronGsFewCount = 96, kPositronGsFewScatter = 97,
+    kPositronGsFewAzimuth = 98,
+    kPositronCompetingOpticalDepth = 109, kPositronCompetingChannel = 110,
+    kPositronContinuationOpticalDepth = 126, kPositronContinuationChannel = 127,
+    kPositronBhabhaAzimuth = 130,
 };
 
 // O/RreaParticleInteraction.H:642-710
@@ -174,6 +181,12 @@ struct CellSources {
 // Runs the electron phase of one step (O/RreaElectronTransport.cpp:9-902)
 // over one tile.  Throws OracleError on any fail-closed guard.
 void ApplyElectronTransport(rrea_host::TableSet const& tables, rrea_gpu_config const& cfg,
+                            FieldGrid const& field, int step, double dt_s, ChargedTile& tile,
+                            StepOutputs& out);
+
+// Positron phase of one step (O/RreaPositronTransport.cpp:9-878) over one
+// tile.  Dispositions: 0 survive, 1 escape, 2 annihilated, 3 zero weight.
+void ApplyPositronTransport(rrea_host::TableSet const& tables, rrea_gpu_config const& cfg,
                             FieldGrid const& field, int step, double dt_s, ChargedTile& tile,
                             StepOutputs& out);
 

@@ -325,6 +325,37 @@ int main(int argc, char** argv)
             }
             write_f8("ref_chord", 26, chord);
         }
+        // ---- positron accessors and samplers: S/RreaInteractionTables.cpp:2325-2353,
+        //      3129-3206, 2562-2575
+        {
+            std::vector<double> acc, bha, pbr;
+            for (double e : charged_energies(g, tables, 1500)) {
+                double const dr = (g.uni() < 0.5) ? 1.0 : 0.5 + 1.5 * g.uni();
+                acc.insert(acc.end(), {e, dr, tables.PositronCollisionLoss(e, dr), tables.PositronSoftRadiativeDrag(e, dr),
+                                       tables.PositronHardBhabhaMeanFreePath(e, dr),
+                                       tables.PositronBremsstrahlungMeanFreePath(e, dr),
+                                       tables.PositronAnnihilationMeanFreePath(e, dr)});
+                // the conditional CDFs start near the 50 keV production
+                // threshold; queries below a CDF's first group abort there
+                // (the shim turns that into an exception) and are skipped
+                double const u = g.uni();
+                double const v = (g.uni() < 0.05) ? 0.0 : g.uni();
+                try {
+                    double const b = tables.SamplePositronBhabhaSecondaryEnergy(e, u);
+                    bha.insert(bha.end(), {e, u, b});
+                } catch (std::exception const&) {
+                }
+                try {
+                    double const b = tables.SamplePositronBremsstrahlungPhotonEnergy(e, v);
+                    pbr.insert(pbr.end(), {e, v, b});
+                } catch (std::exception const&) {
+                }
+            }
+            write_f8("ref_positron_accessors", 7, acc);
+            write_f8("ref_bhabha_energy", 3, bha);
+            write_f8("ref_positron_brems_energy", 3, pbr);
+        }
+
         // ---- photon samplers: S/RreaInteractionTables.cpp:2778-3253
         {
             std::vector<double> chan, kn, pe, pec, pair, ann;

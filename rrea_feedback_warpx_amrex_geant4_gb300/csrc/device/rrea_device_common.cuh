@@ -106,6 +106,13 @@ enum : uint64_t {
     kChElectronGsFewScatter = 92, kChElectronGsFewAzimuth = 93,
     kChElectronCompetingOpticalDepth = 107, kChElectronCompetingChannel = 108,
     kChElectronContinuationOpticalDepth = 124, kChElectronContinuationChannel = 125,
+    kChPositronBhabhaEnergy = 74, kChPositronBremsEnergy = 76, kChPositronBremsAngle = 77,
+    kChPositronBremsAzimuth = 78, kChPositronAnnihilationPolar = 80, kChPositronAnnihilationAzimuth = 81,
+    kChPositronGsAngle = 94, kChPositronGsAzimuth = 95, kChPositronGsFewCount = 96, kChPositronGsFewScatter = 97,
+    kChPositronGsFewAzimuth = 98,
+    kChPositronCompetingOpticalDepth = 109, kChPositronCompetingChannel = 110,
+    kChPositronContinuationOpticalDepth = 126, kChPositronContinuationChannel = 127,
+    kChPositronBhabhaAzimuth = 130,
 };
 
 // O/RreaParticleInteraction.H:642-710

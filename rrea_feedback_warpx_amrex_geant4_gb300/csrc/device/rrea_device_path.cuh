@@ -518,18 +518,18 @@ __device__ __forceinline__ void build_intervals(Path<NP> const& p, double rho, I
         iv.length[0] = pc.length;
         iv.density[0] = positive_or(dl / pc.length, rho);
         iv.n = 1;
-        return;
-    }
-    for (int i = 0; i < p.npieces; ++i) {
-        Piece const& pc = p.pieces[i];
-        if (!(pc.length > 0.0)) continue;
-        double dl = 0.0;
-        if (pc.end > pc.begin && p.full > 0.0) dl = p.full * (pc.end - pc.begin) * positive_or(rho, rho);
-        iv.begin[iv.n] = pc.begin;
-        iv.end[iv.n] = pc.end;
-        iv.length[iv.n] = pc.length;
-        iv.density[iv.n] = positive_or(dl / pc.length, rho);
-        ++iv.n;
+    } else {
+        for (int i = 0; i < p.npieces; ++i) {
+            Piece const& pc = p.pieces[i];
+            if (!(pc.length > 0.0)) continue;
+            double dl = 0.0;
+            if (pc.end > pc.begin && p.full > 0.0) dl = p.full * (pc.end - pc.begin) * positive_or(rho, rho);
+            iv.begin[iv.n] = pc.begin;
+            iv.end[iv.n] = pc.end;
+            iv.length[iv.n] = pc.length;
+            iv.density[iv.n] = positive_or(dl / pc.length, rho);
+            ++iv.n;
+        }
     }
 }
 // :117-136

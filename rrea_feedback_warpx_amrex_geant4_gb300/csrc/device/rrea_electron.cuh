@@ -29,47 +29,49 @@ __constant__ StepConstants c_step;
 // each table value is interpolated on first use only.  The hazard refreeze
 // and the drag segment that follows it query the same frozen energy, so the
 // drag reuses the refreeze's bracket instead of searching again.
+// The positron tables likewise share one grid among themselves; the cache is
+// used with the base table RREA_T_E_COLLISION or RREA_T_P_COLLISION.
 struct RateCache {
     long long key = -1;  // bit pattern of the bracketed energy; -1 = none
     Bracket b;
-    double v[4];
-    unsigned have = 0;  // bit i: v[i] valid (0 collision, 1 soft, 2 Moller, 3 brems)
+    double v[6];
+    unsigned have = 0;  // bit i: v[i] valid (0 collision, 1 soft, 2 hard, 3 brems, 5 annihilation)
 };
 
 __device__ __forceinline__ bool rate_bracket(StepConstants const& C, const double* __restrict__ arena, RateCache& rc,
-                                             double e, Err& err)
+                                             double e, Err& err, int base = RREA_T_E_COLLISION)
 {
     long long const key = __double_as_longlong(e);
     if (rc.key == key) return true;
     rc.key = -1;
     rc.have = 0;
-    if (!bracket_hot(arena, C.tix.hot[RREA_T_E_COLLISION], e, rc.b, err)) return false;
+    if (!bracket_hot(arena, C.tix.hot[base], e, rc.b, err)) return false;
     rc.key = key;
     return true;
 }
 
 __device__ __forceinline__ double rate_value(StepConstants const& C, const double* __restrict__ arena, RateCache& rc,
-                                             double e, int which, Err& err)
+                                             double e, int which, Err& err, int base = RREA_T_E_COLLISION)
 {
-    if (!rate_bracket(C, arena, rc, e, err)) return 0.0;
+    if (!rate_bracket(C, arena, rc, e, err, base)) return 0.0;
     unsigned const bit = 1u << which;
     if (!(rc.have & bit)) {
-        rc.v[which] = eval_hot(arena, C.tix.hot[RREA_T_E_COLLISION + which], rc.b, err);
+        rc.v[which] = eval_hot(arena, C.tix.hot[base + which], rc.b, err);
         rc.have |= bit;
     }
     return rc.v[which];
 }
 
 __device__ __forceinline__ bool rate_positive(StepConstants const& C, const double* __restrict__ arena, RateCache& rc,
-                                              double e, int which, Err& err)
+                                              double e, int which, Err& err, int base = RREA_T_E_COLLISION)
 {
-    if (!rate_bracket(C, arena, rc, e, err)) return false;
+    if (!rate_bracket(C, arena, rc, e, err, base)) return false;
     unsigned const bit = 1u << which;
     if (rc.have & bit) return rc.v[which] > 0.0;
-    return positive_hot(arena, C.tix.hot[RREA_T_E_COLLISION + which], rc.b, err);
+    return positive_hot(arena, C.tix.hot[base + which], rc.b, err);
 }
 
-enum { kRateCollision = 0, kRateSoft = 1, kRateMoller = 2, kRateBrems = 3 };
+enum { kRateCollision = 0, kRateSoft = 1, kRateMoller = 2, kRateBhabha = 2, kRateBrems = 3, kRateAnnihilation = 5 };
 
 // Competing STP rates, O/RreaChargedFinalStates.H:107-152 with the accessors
 // ElectronHardMollerMeanFreePath / ElectronBremsstrahlungMeanFreePath
@@ -95,6 +97,36 @@ __device__ __forceinline__ void competing_rates(StepConstants const& C, const do
     s1 = frozen_rate(s1, err);
 }
 
+// Positron competing STP rates, O/RreaChargedFinalStates.H:121-140 with the
+// accessors PositronHardBhabhaMeanFreePath, PositronBremsstrahlungMeanFreePath
+// and PositronAnnihilationMeanFreePath (S/RreaInteractionTables.cpp:3141-3206):
+// Bhabha opens above the production threshold, brems above the photon cut,
+// annihilation at every energy.
+__device__ __forceinline__ void competing_rates_positron(StepConstants const& C, const double* __restrict__ arena,
+                                                         RateCache& rc, double e, double& s0, double& s1, double& s2,
+                                                         Err& err)
+{
+    double const thr = C.hm_threshold_eV;
+    s0 = 0.0;
+    s1 = 0.0;
+    if (!(thr > 0.0 && e <= thr)) {
+        double const mfp = mfp_from_inverse(rate_value(C, arena, rc, e, kRateBhabha, err, RREA_T_P_COLLISION) * 1.0,
+                                            err);
+        s0 = mfp > 0.0 ? 1.0 / mfp : 0.0;
+    }
+    if (e > C.photon_cutoff_eV) {
+        double const mfp = mfp_from_inverse(rate_value(C, arena, rc, e, kRateBrems, err, RREA_T_P_COLLISION) * 1.0,
+                                            err);
+        s1 = mfp > 0.0 ? 1.0 / mfp : 0.0;
+    }
+    double const mfp2 =
+        mfp_from_inverse(rate_value(C, arena, rc, e, kRateAnnihilation, err, RREA_T_P_COLLISION) * 1.0, err);
+    s2 = mfp2 > 0.0 ? 1.0 / mfp2 : 0.0;
+    s0 = frozen_rate(s0, err);
+    s1 = frozen_rate(s1, err);
+    s2 = frozen_rate(s2, err);
+}
+
 // S/RreaInteractionTables.cpp:2414-2440
 __device__ __forceinline__ double hard_moller_energy_loss(StepConstants const& C, const double* __restrict__ arena,
                                                           double e, double dr, Err& err)
@@ -110,16 +142,16 @@ __device__ __forceinline__ double hard_moller_energy_loss(StepConstants const& C
 // S/RreaInteractionTables.cpp:2477-2493
 __device__ __forceinline__ double elastic_inverse_stp(StepConstants const& C, const double* __restrict__ arena,
                                                       double e, Err& err,
-                                                      double le = __builtin_nan(""))
+                                                      double le = __builtin_nan(""), int species = 0)
 {
-    RreaElasticIndex const& el = C.tix.elastic[0];
+    RreaElasticIndex const& el = C.tix.elastic[species];
     double const mfp = semilogx(arena + el.x, arena + el.lx, arena + el.mfp, el.n, e, err, le) / 1.0;
     return frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0, err);
 }
 
 // S/RreaInteractionTables.cpp:2504-2560
 __device__ __forceinline__ double sample_gs_cos(StepConstants const& C, const double* __restrict__ arena, double e,
-                                                double n, double u, Err& err, double le)
+                                                double n, double u, Err& err, double le, int species = 0)
 {
     RreaArenaIndex const& ix = C.tix;
     if (!charged_in_range(ix, e)) {
@@ -131,7 +163,7 @@ __device__ __forceinline__ double sample_gs_cos(StepConstants const& C, const do
         return 1.0;
     }
     bool const use_gs = e <= ix.gs_wentzel_transition_eV;
-    RreaAngleIndex const& a = use_gs ? ix.gs[0] : ix.wentzel[0];
+    RreaAngleIndex const& a = use_gs ? ix.gs[species] : ix.wentzel[species];
     if (e < __ldg(arena + a.e) || e > __ldg(arena + a.e + a.ne - 1)) {
         err.set(RREA_GPU_ERR_RANGE);
         return 1.0;
@@ -144,13 +176,14 @@ __device__ __forceinline__ double sample_gs_cos(StepConstants const& C, const do
     return sample_gs_angle(arena, a, e, n, u, err, le);
 }
 __device__ __forceinline__ double sample_single_elastic_cos(StepConstants const& C, const double* __restrict__ arena,
-                                                            double e, double cdf_u, Err& err, double le)
+                                                            double e, double cdf_u, Err& err, double le,
+                                                            int species = 0)
 {
     if (!charged_in_range(C.tix, e)) {
         err.set(RREA_GPU_ERR_RANGE);
         return 1.0;
     }
-    RreaElasticIndex const& el = C.tix.elastic[0];
+    RreaElasticIndex const& el = C.tix.elastic[species];
     double const eta = semilogx(arena + el.x, arena + el.lx, arena + el.eta, el.n, e, err, le);
     double const u = fmin(fmax(cdf_u, 0.0), 1.0 - 1.0e-15);
     return 1.0 - 2.0 * eta * u / (1.0 + eta - u);
@@ -214,7 +247,9 @@ __device__ __forceinline__ void moller_final_state(StepConstants const& C, Elect
     deposit_source(C, A.cells, 0, site.r, site.z, weight, sec, sec);
 }
 
-// RreaApplyBremsFinalState, O/RreaChargedFinalStates.H:329-394
+// RreaApplyBremsFinalState, O/RreaChargedFinalStates.H:329-394; POS selects
+// the positron photon-energy CDF and RNG channels.
+template <bool POS = false>
 __device__ __forceinline__ void brems_final_state(StepConstants const& C, ElectronArgs const& A, RngStream const& rng,
                                                uint64_t rng_index, int64_t ip, uint64_t key, double weight,
                                                Site const& site, double& k, double& dx, double& dy, double& dz,
@@ -225,18 +260,21 @@ __device__ __forceinline__ void brems_final_state(StepConstants const& C, Electr
         err.set(RREA_GPU_ERR_RANGE);
         return;
     }
-    double const sampled = sample_conditional(A.arena, C.tix.cdf[RREA_C_BREMS_E], kb,
-                                              rng.uniform(rng_index, kChBremsEnergy), false, err);
+    double const sampled = sample_conditional(A.arena, C.tix.cdf[POS ? RREA_C_BREMS_P : RREA_C_BREMS_E], kb,
+                                              rng.uniform(rng_index, POS ? kChPositronBremsEnergy : kChBremsEnergy),
+                                              false, err);
     double const eg = fmin(fmax(sampled, 0.0), fmax(kb, 0.0));
     double const after = fmax(0.0, fmax(kb, 0.0) - eg);
     bool const tracked = isfinite(C.photon_cutoff_eV) && C.photon_cutoff_eV >= 0.0 && eg >= C.photon_cutoff_eV;
-    double const ct = sample_brems_cos(C, kb, rng.uniform(rng_index, kChBremsAngle), err);
+    double const ct = sample_brems_cos(C, kb, rng.uniform(rng_index, POS ? kChPositronBremsAngle : kChBremsAngle), err);
     double gx, gy, gz;
-    cone_direction(dx, dy, dz, ct, rng.uniform(rng_index, kChBremsAzimuth), gx, gy, gz);
+    cone_direction(dx, dy, dz, ct, rng.uniform(rng_index, POS ? kChPositronBremsAzimuth : kChBremsAzimuth), gx, gy,
+                   gz);
     photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
     k = after;
     if (tracked) {
-        append_secondary(A, ip, key, weight, lineage, 2, 4, site.x, site.y, site.z, gx, gy, gz, eg, site.birth, err);
+        append_secondary(A, ip, key, weight, lineage, 2, 4, site.x, site.y, site.z, gx, gy, gz, eg, site.birth, err,
+                         POS ? 1 : 0);
     } else if (eg > 0.0) {
         // deposit_local_energy_as_ion_pairs, O/RreaTransportStep.H:530-561
         double const w_air = C.tix.w_air_eV_per_pair;
@@ -254,25 +292,156 @@ struct Dir3 {
     int err;
 };
 
+// RreaApplyBhabhaFinalState, O/RreaChargedFinalStates.H:238-288: a
+// secondary below the production threshold discards this event only.
+__device__ __forceinline__ void bhabha_final_state(StepConstants const& C, ElectronArgs const& A, RngStream const& rng,
+                                                   uint64_t rng_index, int64_t ip, uint64_t key, double weight,
+                                                   Site const& site, double& k, double& dx, double& dy, double& dz,
+                                                   uint32_t& lineage, Err& err)
+{
+    double const kb = k;
+    if (!charged_in_range(C.tix, kb)) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return;
+    }
+    double const sec = fmin(sample_conditional(A.arena, C.tix.cdf[RREA_C_BHABHA], kb,
+                                               rng.uniform(rng_index, kChPositronBhabhaEnergy), false, err),
+                            fmax(0.0, kb));
+    double const thr = C.hm_threshold_eV;
+    if (!(sec > 0.0) || (thr > 0.0 && sec < thr)) return;
+    double pdx, pdy, pdz, sdx, sdy, sdz;
+    moller_lab_directions(dx, dy, dz, kb, sec, rng.uniform(rng_index, kChPositronBhabhaAzimuth), pdx, pdy, pdz, sdx,
+                          sdy, sdz);
+    k = fmax(0.0, kb - sec);
+    dx = pdx; dy = pdy; dz = pdz;
+    append_secondary(A, ip, key, weight, lineage, 0, 3, site.x, site.y, site.z, sdx, sdy, sdz, sec, site.birth, err, 1);
+    deposit_source(C, A.cells, 2, site.r, site.z, weight, 0.0, sec);
+}
+
+// sample_annihilation_photon_energy_fraction (S/RreaInteractionTables.cpp:63-108):
+// Heitler two-photon spectrum by 64-step bisection of its primitive.
+__device__ __forceinline__ double annihilation_fraction(double gamma, double draw)
+{
+    if (gamma <= 1.0 + 1.0e-12) return 0.5;
+    double const bcm = sqrt(fmax(0.0, (gamma - 1.0) / (gamma + 1.0)));
+    double const emin = 0.5 * (1.0 - bcm), emax = 0.5 * (1.0 + bcm);
+    double const u = isfinite(draw) ? fmax(0.0, fmin(1.0, draw)) : 0.5;
+    double const gp1 = gamma + 1.0;
+    double const a = 1.0 + 2.0 * gamma / (gp1 * gp1);
+    double const c = gp1 * gp1;
+    double const flo = a * log(emin) - emin + 1.0 / (c * emin);
+    double const fhi = a * log(emax) - emax + 1.0 / (c * emax);
+    double const span = fhi - flo;
+    if (!(span > 0.0)) return 0.5;
+    double const target = flo + u * span;
+    double lo = emin, hi = emax;
+    for (int it = 0; it < 64; ++it) {
+        double const mid = 0.5 * (lo + hi);
+        if (a * log(mid) - mid + 1.0 / (c * mid) < target) lo = mid; else hi = mid;
+    }
+    return fmax(emin, fmin(emax, 0.5 * (lo + hi)));
+}
+
+// TransportStep::spawn_positron_annihilation (O/RreaTransportStep.H:563-702)
+// with SamplePositronAnnihilationFinalState (S/RreaInteractionTables.cpp:
+// 3208-3253): two photons, momentum-balanced in flight, back to back at rest;
+// a below-cutoff positron first thermalizes its kinetic energy as ion pairs.
+// Returns the parent's lineage count after the appended photons.  Taken out
+// of line with every argument by value (it runs at most once per positron).
+__device__ __noinline__ uint32_t spawn_annihilation(ElectronArgs A, RngStream rng, uint64_t idx, int64_t ip,
+                                                    uint64_t key, double weight, uint32_t lineage, double x, double y,
+                                                    double z, double r, double ax, double ay, double az, double k,
+                                                    bool at_rest, double birth)
+{
+    StepConstants const& C = c_step;
+    Err err;
+    if (weight <= 0.0) return lineage;
+    normalize(ax, ay, az);
+    double const ka = at_rest ? 0.0 : fmax(k, 0.0);
+    if (!(ka == 0.0) && !charged_in_range(C.tix, ka)) {
+        record_failure(A, RREA_GPU_ERR_RANGE, ip);
+        return lineage;
+    }
+    double const d_e = rng.uniform(idx, kChPositronAnnihilationPolar);
+    double const d_a = rng.uniform(idx, kChPositronAnnihilationAzimuth);
+    double const gamma = 1.0 + ka / kMeC2;
+    double const total = 2.0 * kMeC2 + ka;
+    double e1 = 0.0, e2 = 0.0, cos1 = 1.0, azim = 0.0;
+    bool rest = false;
+    if (gamma <= 1.0 + 1.0e-10) {
+        e1 = kMeC2;
+        e2 = kMeC2;
+        cos1 = 2.0 * (isfinite(d_e) ? fmax(0.0, fmin(1.0, d_e)) : 0.5) - 1.0;
+        azim = isfinite(d_a) ? d_a - floor(d_a) : 0.0;
+        if (azim < 0.0) azim += 1.0;
+        rest = true;
+    } else {
+        double const beta = sqrt(fmax(0.0, 1.0 - 1.0 / (gamma * gamma)));
+        double const eps = annihilation_fraction(gamma, d_e);
+        e1 = eps * total;
+        e2 = fmax(0.0, total - e1);
+        double const denom = eps * gamma * beta;
+        if (e1 > 0.0 && e2 > 0.0 && denom > 0.0) {
+            cos1 = fmax(-1.0, fmin(1.0, (eps * (gamma + 1.0) - 1.0) / denom));
+            azim = isfinite(d_a) ? d_a - floor(d_a) : 0.0;
+            if (azim < 0.0) azim += 1.0;
+        }
+    }
+    double g1x, g1y, g1z;
+    cone_direction(ax, ay, az, cos1, azim, g1x, g1y, g1z);
+    e1 = fmax(e1, 0.0);
+    e2 = fmax(e2, 0.0);
+    double g2x = -g1x, g2y = -g1y, g2z = -g1z;
+    if (!rest && e2 > 0.0) {
+        double const p = sqrt(fmax(0.0, ka * (ka + 2.0 * kMeC2)));
+        g2x = (p * ax - e1 * g1x) / e2;
+        g2y = (p * ay - e1 * g1y) / e2;
+        g2z = (p * az - e1 * g1z) / e2;
+        normalize(g2x, g2y, g2z);
+    }
+    double local = 0.0;
+    double const cut = C.photon_cutoff_eV;
+    double const w_air = C.tix.w_air_eV_per_pair;
+    if (e1 >= cut) append_secondary(A, ip, key, weight, lineage, 2, 9, x, y, z, g1x, g1y, g1z, e1, birth, err, 1);
+    else local += e1;
+    if (e2 >= cut) append_secondary(A, ip, key, weight, lineage, 2, 9, x, y, z, g2x, g2y, g2z, e2, birth, err, 1);
+    else local += e2;
+    if (at_rest && k > 0.0) {
+        double const pw = weight * k / fmax(w_air, 1.0);
+        if (pw > 0.0) deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
+    }
+    if (local > 0.0) {
+        double const pw = weight * local / fmax(w_air, 1.0);
+        if (pw > 0.0) deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
+    }
+    deposit_source(C, A.cells, 2, r, z, weight, 0.0, 0.0);
+    if (err.code) record_failure(A, err.code, ip);
+    return lineage;
+}
+
 // Few-collision branch of apply_gs_elastic_scatter (O/RreaTransportStep.H:397-416):
 // a Poisson number of single screened-Rutherford deflections.  Rare for
 // tracked electrons (n >= 10 elastic collisions per substep at MeV energies),
 // so it is kept out of line.
 __device__ __noinline__ Dir3 gs_few_collisions(const double* __restrict__ arena, RngStream rng, uint64_t sub,
-                                               double gs_n, double k, double lk, double dx, double dy, double dz)
+                                               double gs_n, double k, double lk, double dx, double dy, double dz,
+                                               int species)
 {
+    uint64_t const ch_count = species ? kChPositronGsFewCount : kChElectronGsFewCount;
+    uint64_t const ch_scatter = species ? kChPositronGsFewScatter : kChElectronGsFewScatter;
+    uint64_t const ch_azimuth = species ? kChPositronGsFewAzimuth : kChElectronGsFewAzimuth;
     StepConstants const& C = c_step;
     Err err;
     double const few = C.tix.gs_few_collision_threshold;
     int const cap = static_cast<int>(ceil(3.0 * few));
     if (cap >= 255) return Dir3{dx, dy, dz, RREA_GPU_ERR_INVALID_STATE};
-    int const cnt = poisson_capped(gs_n, rng.uniform((sub << 8) | 0, kChElectronGsFewCount), cap);
+    int const cnt = poisson_capped(gs_n, rng.uniform((sub << 8) | 0, ch_count), cap);
     for (int q = 0; q < cnt; ++q) {
         uint64_t const inner = static_cast<uint64_t>(q + 1);
         double const ct =
-            sample_single_elastic_cos(C, arena, k, rng.uniform((sub << 8) | inner, kChElectronGsFewScatter), err, lk);
+            sample_single_elastic_cos(C, arena, k, rng.uniform((sub << 8) | inner, ch_scatter), err, lk, species);
         double nx, ny, nz;
-        cone_direction(dx, dy, dz, ct, rng.uniform((sub << 8) | inner, kChElectronGsFewAzimuth), nx, ny, nz);
+        cone_direction(dx, dy, dz, ct, rng.uniform((sub << 8) | inner, ch_azimuth), nx, ny, nz);
         dx = nx; dy = ny; dz = nz;
     }
     return Dir3{dx, dy, dz, err.code};
@@ -295,12 +464,21 @@ __device__ __noinline__ double cutoff_bisection(Intervals<NP> iv, Path<NP> path,
     return 0.5 * (lo + hi);
 }
 
-// Returns the disposition (0 survive, 1 escape, 2 demotion, 3 zero weight).
-template <int NP>
-__device__ __forceinline__ int transport_electron(StepConstants const& C, ElectronArgs const& A, int64_t ip,
-                                                  uint64_t& subcycles_out, uint64_t& events_out,
-                                                  uint32_t& lineage, Err& err)
+// One charged particle through one outer step.  POS = false is the electron
+// loop (O/RreaElectronTransport.cpp); POS = true the positron loop
+// (O/RreaPositronTransport.cpp:9-878), which shares the substep and event
+// engine and differs in charge, channels (Bhabha, brems, annihilation), drag
+// tables, GS tables and RNG channels, and ends below the cutoff in at-rest
+// annihilation instead of demotion.  Returns the disposition (0 survive,
+// 1 escape, 2 demotion / annihilation, 3 zero weight, -1 error).
+template <int NP, bool POS = false>
+__device__ __forceinline__ int transport_charged(StepConstants const& C, ElectronArgs const& A, int64_t ip,
+                                                 uint64_t& subcycles_out, uint64_t& events_out,
+                                                 uint32_t& lineage, Err& err)
 {
+    constexpr double q = POS ? 1.0 : -1.0;
+    constexpr int species = POS ? 1 : 0;
+    constexpr int rate_base = POS ? RREA_T_P_COLLISION : RREA_T_E_COLLISION;
     const double* __restrict__ arena = A.arena;
     rrea_gpu_config const& cfg = C.cfg;
     Geom const g{cfg.r_lo, cfg.r_hi, cfg.z_lo, cfg.z_hi, cfg.periodic_z != 0};
@@ -334,6 +512,7 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
     double run_y = prev_r * sth;
     double run_z = A.prev_z[ip];
     double const r_particle = prev_r, z_particle = run_z;
+    double const x_particle = run_x, y_particle = run_y;
 
     auto build_chord = [&](double req_dt, Path<NP>& path) -> bool {
         // O/RreaParticleInteraction.H:110-161
@@ -365,7 +544,7 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
     Intervals<NP> iv;
     build_intervals(path, rho, iv);
     double const driver_span = fmax(path.in_end, 1.0e-6);
-    FieldRange const dfw = path_field_work(A.fv, g, path, -1.0, 0.0, 1.0, err);
+    FieldRange const dfw = path_field_work(A.fv, g, path, q, 0.0, 1.0, err);
     double const field_work = dfw.work / driver_span;
     double const chord_dpath = density_path(iv, path, path.in_begin, path.in_end);
     double transported_dpath = 0.0, transported_len = 0.0;
@@ -388,10 +567,19 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
         A.id[ip] = -A.id[ip];
         return finish(2);
     };
+    auto annihilate = [&](double x, double y, double z, double r, uint64_t idx, double birth) {
+        // at-rest annihilation, O/RreaPositronTransport.cpp:131-160, 793-845
+        lineage = spawn_annihilation(A, rng, idx, ip, key, weight, lineage, x, y, z, r, dx, dy, dz, k, true, birth);
+        A.id[ip] = -A.id[ip];
+        return finish(2);
+    };
 
     bool const below = k < cutoff;
     if (esc && below) return commit_escape();
-    if (!esc && below) return demote(r_particle, z_particle);
+    if (!esc && below) {
+        if constexpr (POS) return annihilate(x_particle, y_particle, z_particle, r_particle, 0, 1.0);
+        else return demote(r_particle, z_particle);
+    }
     if (ds <= 0.0) {
         if (esc) return commit_escape();
         return finish(0);
@@ -405,13 +593,21 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
     uint64_t subcycles;
     RateCache rc;
     {
-        double s0, s1;
-        competing_rates(C, arena, rc, k, s0, s1, err);
+        double s0, s1, s2 = 0.0;
+        if constexpr (POS) competing_rates_positron(C, arena, rc, k, s0, s1, s2, err);
+        else competing_rates(C, arena, rc, k, s0, s1, err);
         double const driver_dpath = chord_dpath / driver_span;
         double const target = cfg.max_optical_depth_per_substep;
         uint64_t const cap = cfg.max_subcycles;
-        double const max_tau = (s0 * driver_dpath) + (s1 * driver_dpath);
-        double const total_stp = s0 + s1;
+        double max_tau, total_stp;
+        if constexpr (POS) {
+            // O/RreaPositronTransport.cpp:168-185: the summed rate times the path
+            total_stp = (s0 + s1) + s2;
+            max_tau = total_stp * driver_dpath;
+        } else {
+            max_tau = (s0 * driver_dpath) + (s1 * driver_dpath);
+            total_stp = s0 + s1;
+        }
         uint64_t const req = static_cast<uint64_t>(fmax(1.0, ceil(max_tau / target)));
         bool viol = req > cap;
         uint64_t sub = req < cap ? req : cap;
@@ -430,10 +626,13 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
             else if (est > static_cast<double>(next)) next = static_cast<uint64_t>(est);
             sub = next < cap ? next : cap;
         }
-        double const gs_n = elastic_inverse_stp(C, arena, k, err) * driver_dpath;
+        double const gs_n = elastic_inverse_stp(C, arena, k, err, __builtin_nan(""), species) * driver_dpath;
         double const ke = fmax(k, cutoff);
         double drag_est = 0.0;
-        if (ke > 0.0) {
+        if constexpr (POS) {
+            // collision stopping only (O/RreaPositronTransport.cpp:195-201)
+            drag_est = rate_value(C, arena, rc, ke, kRateCollision, err, rate_base) * 1.0 * driver_dpath;
+        } else if (ke > 0.0) {
             double const col = rate_value(C, arena, rc, ke, kRateCollision, err);
             double const soft = rate_value(C, arena, rc, ke, kRateSoft, err);
             drag_est = (col * 1.0 + soft * 1.0) * driver_dpath;
@@ -454,7 +653,9 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
     bool exited = false;
     uint64_t completed = 0;
     bool terminated_mid = false;
+    bool annihilated = false;
     double mid_r = r_particle, mid_z = z_particle;
+    double mid_x = x_particle, mid_y = y_particle, mid_elapsed = 1.0;
     double const sub_dt = dt_s / static_cast<double>(subcycles);
     FieldRange sub_field{0, 0, 0, 0, 0, 0, 0, 0};
     double sub_dt_eff = 0.0;
@@ -473,6 +674,13 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
         }
         mid_z = z;
         mid_r = hypot(x, y);
+        if constexpr (POS) {
+            // stop point and elapsed fraction for the at-rest annihilation
+            mid_x = x;
+            mid_y = y;
+            double const within = fmin(1.0, fmax(0.0, f));
+            mid_elapsed = fmin(1.0, (static_cast<double>(completed) + within) / static_cast<double>(subcycles));
+        }
         terminated_mid = true;
     };
     // O/RreaElectronTransport.cpp:294-400 with RreaPlanContinuousDragSegment
@@ -485,8 +693,8 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
         // The plan's hard-transfer loss feeds only the reference's scalar
         // tally, and its table queries cannot fail at an energy the
         // collision table just accepted, so it is not evaluated here.
-        double const sc = frozen_rate(rate_value(C, arena, rc, stop_e, kRateCollision, err) * 1.0, err);
-        double const ss = frozen_rate(rate_value(C, arena, rc, stop_e, kRateSoft, err) * 1.0, err);
+        double const sc = frozen_rate(rate_value(C, arena, rc, stop_e, kRateCollision, err, rate_base) * 1.0, err);
+        double const ss = frozen_rate(rate_value(C, arena, rc, stop_e, kRateSoft, err, rate_base) * 1.0, err);
         if (err.code) return false;
         double const total = sc + ss;
         // limiter
@@ -536,7 +744,7 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                 if (!(pw > 0.0)) continue;
                 double x, y, z;
                 point_at_full(path, g, 0.5 * (bb + ee), x, y, z);
-                deposit_source(C, A.cells, 0, hypot(x, y), z, pw, 0.5 * cutoff, w_air);
+                deposit_source(C, A.cells, 0, hypot(x, y), z, pw, POS ? 0.0 : 0.5 * cutoff, w_air);
             }
         }
         k = fmax(0.0, k - drag);
@@ -548,6 +756,15 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
         // O/RreaChargedFinalStates.H:56-96
         if (!charged_in_range(C.tix, e)) {
             err.set(RREA_GPU_ERR_RANGE);
+            return false;
+        }
+        if constexpr (POS) {
+            if (!rate_bracket(C, arena, rc, e, err, rate_base)) return false;
+            if (ch == 0) {
+                return !(hm_thr > 0.0 && e <= hm_thr) && rate_positive(C, arena, rc, e, kRateBhabha, err, rate_base);
+            }
+            if (ch == 1) return e > C.photon_cutoff_eV && rate_positive(C, arena, rc, e, kRateBrems, err, rate_base);
+            if (ch == 2) return rate_positive(C, arena, rc, e, kRateAnnihilation, err, rate_base);
             return false;
         }
         if (!rate_bracket(C, arena, rc, e, err)) return false;
@@ -587,9 +804,9 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
             }
             sb = path.in_begin;
             se = path.in_end;
-            sub_field = path_field_work(A.fv, g, path, -1.0, sb, se, err);
+            sub_field = path_field_work(A.fv, g, path, q, sb, se, err);
             sub_dt_eff = sub_dt * (se - sb);
-            half_kick(sub_field, 0.5 * sub_dt_eff, -1.0, k, dx, dy, dz);
+            half_kick(sub_field, 0.5 * sub_dt_eff, q, k, dx, dy, dz);
             if (k < cutoff) {
                 mark_stopped(sb);
                 break;
@@ -606,21 +823,28 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                     break;
                 }
                 double const frozen = k;
-                double s0, s1;
-                competing_rates(C, arena, rc, frozen, s0, s1, err);
+                double s0, s1, s2 = 0.0;
+                if constexpr (POS) competing_rates_positron(C, arena, rc, frozen, s0, s1, s2, err);
+                else competing_rates(C, arena, rc, frozen, s0, s1, err);
                 double const seg_dp = density_path(iv, path, rem, se);
-                double const t0 = s0 * seg_dp, t1 = s1 * seg_dp;
+                double const t0 = s0 * seg_dp, t1 = s1 * seg_dp, t2 = s2 * seg_dp;
                 uint64_t rng_index;
-                if (!live_hazard_index(0, sub, ordinal, rng_index)) {
+                if (!live_hazard_index(species, sub, ordinal, rng_index)) {
                     err.set(RREA_GPU_ERR_RNG_OVERFLOW);
                     break;
                 }
                 ++events;
-                double const u1 = rng.uniform(rng_index, ordinal == 0 ? kChElectronCompetingOpticalDepth
-                                                                      : kChElectronContinuationOpticalDepth);
-                double const u2 = rng.uniform(rng_index, ordinal == 0 ? kChElectronCompetingChannel
-                                                                      : kChElectronContinuationChannel);
-                Selection const selv = select_hazard(t0, t1, 0.0, 2, u1, u2);
+                uint64_t const ch_depth = POS ? (ordinal == 0 ? kChPositronCompetingOpticalDepth
+                                                              : kChPositronContinuationOpticalDepth)
+                                              : (ordinal == 0 ? kChElectronCompetingOpticalDepth
+                                                              : kChElectronContinuationOpticalDepth);
+                uint64_t const ch_channel = POS ? (ordinal == 0 ? kChPositronCompetingChannel
+                                                                : kChPositronContinuationChannel)
+                                                : (ordinal == 0 ? kChElectronCompetingChannel
+                                                                : kChElectronContinuationChannel);
+                double const u1 = rng.uniform(rng_index, ch_depth);
+                double const u2 = rng.uniform(rng_index, ch_channel);
+                Selection const selv = select_hazard(t0, t1, t2, POS ? 3 : 2, u1, u2);
                 if (!selv.valid) {
                     err.set(RREA_GPU_ERR_INVALID_STATE);
                     break;
@@ -630,7 +854,8 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                     if (continuous(rem, se, frozen, eff)) mark_stopped(eff);
                     break;
                 }
-                double const ev = fraction_at_density_path(iv, path, rem, se, selv.sampled / (s0 + s1), err);
+                double const ev = fraction_at_density_path(iv, path, rem, se,
+                                                           selv.sampled / (POS ? (s0 + s1) + s2 : s0 + s1), err);
                 if (!(isfinite(rem) && isfinite(ev) && isfinite(se) && se > rem && !(ev < rem) && !(ev > se))) {
                     err.set(RREA_GPU_ERR_INVALID_STATE);
                     break;
@@ -659,10 +884,25 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
                 double const within = fmin(1.0, fmax(0.0, ev));
                 double const birth = fmin(1.0, (static_cast<double>(completed) + within) / static_cast<double>(subcycles));
                 Site const site{ex, ey, ez, er, birth};
-                if (selv.channel == 0) {
-                    moller_final_state(C, A, rng, rng_index, ip, key, weight, site, k, dx, dy, dz, lineage, err);
-                } else if (selv.channel == 1) {
-                    brems_final_state(C, A, rng, rng_index, ip, key, weight, site, k, dx, dy, dz, lineage, err);
+                if constexpr (POS) {
+                    if (selv.channel == 0) {
+                        bhabha_final_state(C, A, rng, rng_index, ip, key, weight, site, k, dx, dy, dz, lineage, err);
+                    } else if (selv.channel == 1) {
+                        brems_final_state<true>(C, A, rng, rng_index, ip, key, weight, site, k, dx, dy, dz, lineage,
+                                                err);
+                    } else {
+                        // in-flight annihilation, O/RreaPositronTransport.cpp:700-727
+                        lineage = spawn_annihilation(A, rng, rng_index, ip, key, weight, lineage, ex, ey, ez, er, dx,
+                                                     dy, dz, k, false, birth);
+                        annihilated = true;
+                        break;
+                    }
+                } else {
+                    if (selv.channel == 0) {
+                        moller_final_state(C, A, rng, rng_index, ip, key, weight, site, k, dx, dy, dz, lineage, err);
+                    } else if (selv.channel == 1) {
+                        brems_final_state(C, A, rng, rng_index, ip, key, weight, site, k, dx, dy, dz, lineage, err);
+                    }
                 }
                 if (err.code) break;
                 if (k <= cutoff) {
@@ -674,29 +914,32 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
             }
         }
         if (err.code) break;
-        if (terminated_mid) break;
+        if (terminated_mid || annihilated) break;
         // ---- finish_interleaved_substep, O/RreaElectronTransport.cpp:502-524
         if (k >= cutoff) {
             // apply_gs_elastic_scatter, O/RreaTransportStep.H:371-423
             // log(k) is shared by the elastic-MFP and angle-table brackets.
             double const lk = (k > 0.0) ? log(k) : __longlong_as_double(0x7ff8000000000000LL);
-            double const gs_n = elastic_inverse_stp(C, arena, k, err, lk) * density_path(iv, path, sb, se);
+            double const gs_n = elastic_inverse_stp(C, arena, k, err, lk, species) * density_path(iv, path, sb, se);
             if (gs_n > 0.0) {
                 double const few = C.tix.gs_few_collision_threshold;
                 if (gs_n < few) {
-                    Dir3 const d3 = gs_few_collisions(arena, rng, sub, gs_n, k, lk, dx, dy, dz);
+                    Dir3 const d3 = gs_few_collisions(arena, rng, sub, gs_n, k, lk, dx, dy, dz, species);
                     dx = d3.x; dy = d3.y; dz = d3.z;
                     if (d3.err) err.set(d3.err);
                     if (err.code) break;
                 } else {
-                    double const ct = sample_gs_cos(C, arena, k, gs_n, rng.uniform(sub << 8, kChElectronGsAngle), err, lk);
+                    double const ct = sample_gs_cos(C, arena, k, gs_n,
+                                                    rng.uniform(sub << 8, POS ? kChPositronGsAngle : kChElectronGsAngle),
+                                                    err, lk, species);
                     double nx, ny, nz;
-                    cone_direction(dx, dy, dz, ct, rng.uniform(sub << 8, kChElectronGsAzimuth), nx, ny, nz);
+                    cone_direction(dx, dy, dz, ct, rng.uniform(sub << 8, POS ? kChPositronGsAzimuth : kChElectronGsAzimuth),
+                                   nx, ny, nz);
                     dx = nx; dy = ny; dz = nz;
                 }
             }
         }
-        half_kick(sub_field, 0.5 * sub_dt_eff, -1.0, k, dx, dy, dz);
+        half_kick(sub_field, 0.5 * sub_dt_eff, q, k, dx, dy, dz);
         if (k < cutoff) {
             mark_stopped(se);
             break;
@@ -723,6 +966,24 @@ __device__ __forceinline__ int transport_electron(StepConstants const& C, Electr
     events_out = events;
     if (err.code) return finish(-1);
     if (exited) clipped_escape_policy(path, g, hypot(path.ex, path.ey), path.ez, esc, esc_inv);
+    if constexpr (POS) {
+        // O/RreaPositronTransport.cpp:764-870
+        if (annihilated) {
+            A.id[ip] = -A.id[ip];
+            return finish(2);
+        }
+        if (exited) return commit_escape();
+        if (terminated_mid) return annihilate(mid_x, mid_y, mid_z, mid_r, subcycles, mid_elapsed);
+        if (k < cutoff) return annihilate(run_x, run_y, run_z, hypot(run_x, run_y), subcycles, 1.0);
+        double const um = proper_velocity_from_kinetic(k);
+        A.ux[ip] = um * dx;
+        A.uy[ip] = um * dy;
+        A.uz[ip] = um * dz;
+        A.r[ip] = hypot(run_x, run_y);
+        A.theta[ip] = atan2(run_y, run_x);
+        A.z[ip] = run_z;
+        return finish(0);
+    }
     if (transported_len > 0.0) particle_density = transported_dpath / transported_len;
     double const end_r = hypot(run_x, run_y);
     double fer, fez, fbt;

@@ -286,6 +286,12 @@ rrea_gpu_status rrea_gpu_load_tables(rrea_gpu_ctx* ctx, const char* path)
     if (ctx->cfg.low_energy_cutoff_eV < ctx->tables.index().charged_min_eV) {
         return fail(ctx, RREA_GPU_ERR_ARGUMENT, "tracking cutoff below the certified charged range");
     }
+    // The charged kernels bracket each energy once per species and evaluate
+    // every coefficient table at that bracket.
+    if (!ctx->tables.index().electron_grid_shared || !ctx->tables.index().positron_grid_shared) {
+        return fail(ctx, RREA_GPU_ERR_TABLES,
+                    "the electron (positron) coefficient tables must share one energy grid");
+    }
     auto const& arena = ctx->tables.arena();
     dfree(ctx->d_arena);
     ctx->d_arena = nullptr;
@@ -431,6 +437,9 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
         if (species == RREA_SPECIES_PHOTON) {
             RREA_CUDA(ctx, rrea_launch::photon_step(sc, a, blocks > 0 ? blocks : 1, ctx->launch_threads,
                                                     c.periodic_z != 0, ctx->stream));
+        } else if (species == RREA_SPECIES_POSITRON) {
+            RREA_CUDA(ctx, rrea_launch::positron_step(a, blocks > 0 ? blocks : 1, ctx->launch_threads,
+                                                      c.periodic_z != 0, ctx->stream));
         } else {
             RREA_CUDA(ctx, rrea_launch::electron_step(a, blocks > 0 ? blocks : 1, ctx->launch_threads,
                                                       ctx->launch_min_blocks, c.periodic_z != 0, ctx->stream));
@@ -453,7 +462,8 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     if (a.n > 0) RREA_CUDA(ctx, cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev_start, ctx->ev_stop));
     if (status != 0) {
         return fail(ctx, static_cast<rrea_gpu_status>(status),
-                    std::string(species == RREA_SPECIES_PHOTON ? "photon" : "electron")
+                    std::string(species == RREA_SPECIES_PHOTON ? "photon"
+                                : species == RREA_SPECIES_POSITRON ? "positron" : "electron")
                         + " transport guard failed (status " + std::to_string(status) + ") at particle "
                         + std::to_string(fail_index));
     }
@@ -545,6 +555,14 @@ rrea_gpu_status rrea_gpu_apply_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile,
     return apply_phase(ctx, RREA_SPECIES_ELECTRON, tile, step, dt_s, secondaries, secondary_capacity, n_secondaries);
 }
 
+rrea_gpu_status rrea_gpu_apply_positrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, int32_t step, double time_s,
+                                         double dt_s, rrea_gpu_secondary* secondaries, int64_t secondary_capacity,
+                                         int64_t* n_secondaries)
+{
+    (void)time_s;
+    return apply_phase(ctx, RREA_SPECIES_POSITRON, tile, step, dt_s, secondaries, secondary_capacity, n_secondaries);
+}
+
 rrea_gpu_status rrea_gpu_apply_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile, int32_t step, double time_s,
                                        double dt_s, rrea_gpu_secondary* secondaries, int64_t secondary_capacity,
                                        int64_t* n_secondaries)
@@ -616,6 +634,21 @@ rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step
 rrea_gpu_status rrea_gpu_fetch_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile)
 {
     return fetch_species(ctx, RREA_SPECIES_ELECTRON, tile);
+}
+
+rrea_gpu_status rrea_gpu_stage_positrons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile)
+{
+    return stage_species(ctx, RREA_SPECIES_POSITRON, tile);
+}
+
+rrea_gpu_status rrea_gpu_step_positrons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t* n_secondaries)
+{
+    return step_resident(ctx, RREA_SPECIES_POSITRON, step, dt_s, n_secondaries);
+}
+
+rrea_gpu_status rrea_gpu_fetch_positrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile)
+{
+    return fetch_species(ctx, RREA_SPECIES_POSITRON, tile);
 }
 
 rrea_gpu_status rrea_gpu_stage_photons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile)

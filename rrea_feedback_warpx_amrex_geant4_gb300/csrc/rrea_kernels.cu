@@ -3,6 +3,7 @@
 //   field_prep_kernel     cell-centred total field (Maxwell + ambient face
 //                         averages), once per step
 //   electron_step_kernel  one thread per electron, full outer step
+//   positron_step_kernel  one thread per positron, full outer step
 //   scan / scatter        orders the appended secondaries into the reference's
 //                         deterministic order (parent index, then lineage)
 #include "rrea_kernels.h"
@@ -40,8 +41,9 @@ __global__ void field_prep_kernel(int nr, int nz, const double* __restrict__ er,
 // The transport loop is latency-bound (instruction fetch and dependent
 // FP64 chains), so full residency wins despite the spills it forces.
 // NP is the chord piece capacity: 1 for absorbing z faces, 4 for periodic z.
-template <int MinBlocks, int NP>
-__global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(ElectronArgs A)
+// Grid-stride body shared by the electron and positron kernels.
+template <int NP, bool POS>
+__device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
 {
     StepConstants const& C = c_step;
     unsigned int moved = 0;
@@ -58,7 +60,7 @@ __global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(ElectronA
         uint64_t sub = 0, ev = 0;
         uint32_t lineage = 0;
         ++moved;
-        int const disp = transport_electron<NP>(C, A, ip, sub, ev, lineage, err);
+        int const disp = transport_charged<NP, POS>(C, A, ip, sub, ev, lineage, err);
         // Every record this particle appended carries a lineage below this
         // count, so the ordering scan/scatter stays in bounds on every path.
         if (A.sec_per_parent) A.sec_per_parent[ip] = lineage;
@@ -70,6 +72,18 @@ __global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(ElectronA
     // warp-aggregated count of transported particles
     unsigned int const warp_total = __reduce_add_sync(0xffffffffu, moved);
     if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(A.transported, static_cast<unsigned long long>(warp_total));
+}
+
+template <int MinBlocks, int NP>
+__global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(ElectronArgs A)
+{
+    charged_step_body<NP, false>(A);
+}
+
+template <int MinBlocks, int NP>
+__global__ void __launch_bounds__(128, MinBlocks) positron_step_kernel(ElectronArgs A)
+{
+    charged_step_body<NP, true>(A);
 }
 
 // Exclusive scan of per-parent secondary counts (uint32 -> int64 offsets),
@@ -182,6 +196,17 @@ cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
     case 12: rrea_dev::electron_step_kernel<12, 1><<<blocks, threads, 0, stream>>>(args); break;
     case 16: rrea_dev::electron_step_kernel<16, 1><<<blocks, threads, 0, stream>>>(args); break;
     default: rrea_dev::electron_step_kernel<2, 1><<<blocks, threads, 0, stream>>>(args); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, bool periodic,
+                          cudaStream_t stream)
+{
+    if (periodic) {
+        rrea_dev::positron_step_kernel<16, RREA_ARENA_MAX_PIECES><<<blocks, threads, 0, stream>>>(args);
+    } else {
+        rrea_dev::positron_step_kernel<16, 1><<<blocks, threads, 0, stream>>>(args);
     }
     return cudaGetLastError();
 }

@@ -16,6 +16,8 @@ cudaError_t field_prep(int nr, int nz, const double* er, const double* ez, const
                        double* cell_er, double* cell_ez, cudaStream_t stream);
 cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, int min_blocks, bool periodic,
                           cudaStream_t stream);
+cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, bool periodic,
+                          cudaStream_t stream);
 // Photon phase (rrea_photon_kernels.cu); copies `sc` to its own constant bank.
 cudaError_t photon_step(rrea_dev::StepConstants const& sc, rrea_dev::ElectronArgs const& args, int blocks, int threads,
                         bool periodic, cudaStream_t stream);

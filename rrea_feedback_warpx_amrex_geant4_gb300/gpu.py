@@ -70,6 +70,8 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_step_electrons_resident", "rrea_gpu_fetch_electrons", "rrea_gpu_set_launch", "rrea_gpu_stream",
     "rrea_gpu_last_step_stats", "rrea_gpu_apply_photons", "rrea_gpu_stage_photons",
     "rrea_gpu_step_photons_resident", "rrea_gpu_fetch_photons", "rrea_gpu_order_secondaries_noalloc",
+    "rrea_gpu_apply_positrons", "rrea_gpu_stage_positrons", "rrea_gpu_step_positrons_resident",
+    "rrea_gpu_fetch_positrons",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 
@@ -100,6 +102,11 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_apply_electrons.argtypes = [vp, ctypes.POINTER(RreaGpuTile), ctypes.c_int32, ctypes.c_double,
                                              ctypes.c_double, vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
     lib.rrea_gpu_apply_photons.argtypes = lib.rrea_gpu_apply_electrons.argtypes
+    lib.rrea_gpu_apply_positrons.argtypes = lib.rrea_gpu_apply_electrons.argtypes
+    lib.rrea_gpu_stage_positrons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
+    lib.rrea_gpu_step_positrons_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_double,
+                                                     ctypes.POINTER(ctypes.c_int64)]
+    lib.rrea_gpu_fetch_positrons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
     lib.rrea_gpu_stage_photons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
     lib.rrea_gpu_step_photons_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_double,
                                                    ctypes.POINTER(ctypes.c_int64)]
@@ -205,6 +212,22 @@ class RreaGpuContext:
         Returns the ordered secondaries as a structured array."""
         return self._apply(self.lib.rrea_gpu_apply_electrons, arrays, step, dt_s, time_s, want_secondaries)
 
+    def apply_positrons(self, arrays, step, dt_s, time_s=0.0, want_secondaries=True):
+        """Drop-in positron phase on host arrays (modified in place)."""
+        return self._apply(self.lib.rrea_gpu_apply_positrons, arrays, step, dt_s, time_s, want_secondaries)
+
+    def stage_positrons(self, arrays):
+        self._check(self.lib.rrea_gpu_stage_positrons(self.handle, ctypes.byref(tile_struct(arrays))))
+
+    def step_positrons_resident(self, step, dt_s):
+        n_sec = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_step_positrons_resident(self.handle, int(step), float(dt_s),
+                                                              ctypes.byref(n_sec)))
+        return n_sec.value
+
+    def fetch_positrons(self, arrays):
+        self._check(self.lib.rrea_gpu_fetch_positrons(self.handle, ctypes.byref(tile_struct(arrays))))
+
     def apply_photons(self, arrays, step, dt_s, time_s=0.0, want_secondaries=True):
         """Drop-in photon phase on host arrays (modified in place): (r, theta,
         z) is the pushed end point, prev_* the start, u the momentum in eV."""
@@ -288,14 +311,13 @@ class RreaParticleInteraction:
     def SetField(self, er, ez, bt, amb_er, amb_ez):
         self.ctx.set_field(er, ez, bt, amb_er, amb_ez)
 
-    def Apply(self, electrons, step, time_s, dt_s, photons=None):
-        """Electron phase, then photon phase (the reference's order,
-        RreaParticleInteraction.cpp:54-57).  Returns the ordered secondaries
-        of each phase: (electron_secondaries, photon_secondaries or None)."""
+    def Apply(self, electrons, step, time_s, dt_s, photons=None, positrons=None):
+        """Electron, photon and positron phases in the reference's order
+        (RreaParticleInteraction.cpp:54-57).  Returns the ordered secondaries
+        of each phase (None for a species not given)."""
         if not dt_s > 0.0:
-            return None, None
+            return None, None, None
         sec_e = self.ctx.apply_electrons(electrons, step, dt_s, time_s=time_s)
-        sec_g = None
-        if photons is not None:
-            sec_g = self.ctx.apply_photons(photons, step, dt_s, time_s=time_s)
-        return sec_e, sec_g
+        sec_g = self.ctx.apply_photons(photons, step, dt_s, time_s=time_s) if photons is not None else None
+        sec_p = self.ctx.apply_positrons(positrons, step, dt_s, time_s=time_s) if positrons is not None else None
+        return sec_e, sec_g, sec_p

@@ -53,6 +53,9 @@ def test_rng_fixture(oracle_mod):
     ("ref_poisson", 12, 2, 1),
     ("ref_hazard", 13, 6, 5),
     ("ref_drag_plan", 14, 10, 9),
+    ("ref_positron_accessors", 22, 2, 5),
+    ("ref_bhabha_energy", 23, 2, 1),
+    ("ref_positron_brems_energy", 24, 2, 1),
     ("ref_photon_channel", 16, 2, 1),
     ("ref_klein_nishina", 17, 3, 3),
     ("ref_photoelectric", 18, 2, 2),
