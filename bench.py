@@ -253,6 +253,7 @@ def run_gb300(args, rank, world, local):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def one_step(step):
+        ctx.reset_current()  # the net-chord current is per step (ResetNetChordStep)
         ne = ctx.step_electrons_resident(step, DT_S)
         te, _, kme = ctx.last_step_stats()
         ng = ctx.step_photons_resident(step, DT_S)
@@ -289,8 +290,9 @@ def run_gb300(args, rank, world, local):
         moved_e += te
         moved_g += tg
         secondaries += ne + ng
-        # per phase: transport kernel, 3 scan kernels, scatter when anything was appended
-        launches += (1 + 3 + (1 if ne > 0 else 0)) + (1 + 3 + (1 if ng > 0 else 0))
+        # electron phase: transport, current deposition, 3 scan kernels, scatter when
+        # anything was appended; photon phase: transport, 3 scan kernels, scatter
+        launches += (2 + 3 + (1 if ne > 0 else 0)) + (1 + 3 + (1 if ng > 0 else 0))
         step += 1
     barrier()
     clocks.stop()

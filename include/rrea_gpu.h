@@ -155,6 +155,29 @@ rrea_gpu_status rrea_gpu_apply_electrons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile,
 rrea_gpu_status rrea_gpu_download_sources(rrea_gpu_ctx* ctx, double* out5);
 rrea_gpu_status rrea_gpu_reset_sources(rrea_gpu_ctx* ctx);
 
+/*
+ * Net-chord current of the charged phases (RREA J deposition,
+ * RreaWarpXCoupling.cpp:417-544 with RreaSegmentDepositionRZ.H): each
+ * transported electron or positron deposits its committed chord (captured
+ * start -> end point, stop point or annihilation point), and each escape its
+ * chord to the exact face crossing plus the boundary-cloud closure, as
+ * charge-conserving (Umeda zigzag) index-space fluxes on the coupling's padded
+ * grid (nr + 2 cells in r; nz + 4 in z, two pad cells below and above).  The
+ * grid accumulates over the phases run since the last reset; the reference
+ * resets it once per step (ResetNetChordStep).  Only for a non-periodic z
+ * domain (the reference refuses periodic z here); otherwise these calls return
+ * RREA_GPU_ERR_ARGUMENT.
+ *   download_current:        physical face current densities [A/m^2],
+ *                            Jr (nr+1)*nz and Jz nr*(nz+1), index i + stride*j
+ *                            (ConvertPaddedIndexCurrentToPhysicalRZ).
+ *   download_current_index:  the padded grids themselves: rho (nr+2)*(nz+4),
+ *                            Jr (nr+3)*(nz+4), Jz (nr+2)*(nz+5), in units of
+ *                            weight * index / s (for continuity checks).
+ */
+rrea_gpu_status rrea_gpu_reset_current(rrea_gpu_ctx* ctx);
+rrea_gpu_status rrea_gpu_download_current(rrea_gpu_ctx* ctx, double* jr, double* jz);
+rrea_gpu_status rrea_gpu_download_current_index(rrea_gpu_ctx* ctx, double* rho, double* jr, double* jz);
+
 /* Per-particle diagnostics of the last electron step: substeps used,
  * hazard draws made and terminal disposition (0 survive, 1 escape,
  * 2 demotion, 3 zero-weight skip, -1 not transported). */

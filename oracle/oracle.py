@@ -70,6 +70,8 @@ def lib():
         _lib.oracle_electron_step.argtypes = [ctypes.POINTER(RreaGpuConfig), d, d, d, d, d, ctypes.c_int32,
                                               ctypes.c_double, ctypes.POINTER(RreaGpuTile)]
         _lib.oracle_positron_step.argtypes = _lib.oracle_electron_step.argtypes
+        _lib.oracle_deposit_segments.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_double, d, ctypes.c_int64,
+                                                 d, d, d, d, d]
         _lib.oracle_photon_step.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_int32, ctypes.c_double,
                                             ctypes.POINTER(RreaGpuTile)]
         _lib.oracle_counts.argtypes = [ctypes.POINTER(ctypes.c_int64)] * 3
@@ -158,6 +160,35 @@ def positron_step(cfg, field, step, dt_s, arrays):
                                       _dptr(field["bt"]), _dptr(field["amb_er"]), _dptr(field["amb_ez"]),
                                       step, dt_s, ctypes.byref(t)))
     return _collect(cfg, t)
+
+
+def netchord_shapes(cfg):
+    """Shapes (rows, cols) of the padded rho/Jr/Jz and physical Jr/Jz grids."""
+    nr, nz = cfg.nr + 2, cfg.nz + 4
+    return {"rho": (nz, nr), "jr": (nz, nr + 1), "jz": (nz + 1, nr),
+            "jr_phys": (cfg.nz, cfg.nr + 1), "jz_phys": (cfg.nz + 1, cfg.nr)}
+
+
+def deposit_segments(cfg, dt_s, rows):
+    """Net-chord current of segment rows (kind, a0..a6, faces) on cfg's padded
+    grid; returns dict of rho, jr, jz (padded index space) and jr_phys, jz_phys."""
+    cfg = as_config(cfg)
+    rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 9)
+    shapes = netchord_shapes(cfg)
+    out = {k: np.zeros(v) for k, v in shapes.items()}
+    _check(lib().oracle_deposit_segments(ctypes.byref(cfg), dt_s, _dptr(rows), rows.shape[0], _dptr(out["rho"]),
+                                         _dptr(out["jr"]), _dptr(out["jz"]), _dptr(out["jr_phys"]),
+                                         _dptr(out["jz_phys"])))
+    return out
+
+
+def segment_rows(result):
+    """Segment rows (kind, a0..a6, faces) from a step result's segments."""
+    seg = result["segments"]
+    rows = np.zeros((seg.shape[0], 9))
+    rows[:, :8] = seg[:, :8]
+    rows[:, 8] = seg[:, 9]
+    return rows
 
 
 def photon_step(cfg, step, dt_s, arrays):

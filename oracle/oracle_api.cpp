@@ -151,6 +151,42 @@ int oracle_photon_step(rrea_gpu_config const* cfg, int32_t step, double dt_s, rr
     }
 }
 
+// Net-chord current of `n` segment rows (kind, a0..a6, faces) on the padded
+// grid of `cfg` (O/RreaWarpXCoupling.cpp:417-544): padded index-space rho,
+// Jr, Jz and the physical current densities.
+int oracle_deposit_segments(rrea_gpu_config const* cfg, double dt_s, double const* rows, int64_t n, double* rho,
+                            double* jr, double* jz, double* jr_phys, double* jz_phys)
+{
+    try {
+        if (cfg->periodic_z) {
+            throw oracle::OracleError(RREA_GPU_ERR_ARGUMENT, "net-chord current needs a non-periodic z domain");
+        }
+        oracle::NetChordGrid g;
+        g.Reset(*cfg);
+        std::vector<oracle::Segment> segs(static_cast<std::size_t>(n));
+        for (int64_t i = 0; i < n; ++i) {
+            double const* r = rows + 9 * i;
+            oracle::Segment& s = segs[static_cast<std::size_t>(i)];
+            s.kind = static_cast<int>(r[0]);
+            for (int c = 0; c < 7; ++c) s.a[c] = r[1 + c];
+            s.channel = 0;
+            s.faces = static_cast<uint32_t>(r[8]);
+            s.parent_index = i;
+        }
+        oracle::DepositNetChords(g, dt_s, segs);
+        std::vector<double> jrp, jzp;
+        oracle::ConvertNetChordCurrent(g, jrp, jzp);
+        std::copy(g.rho.begin(), g.rho.end(), rho);
+        std::copy(g.jr.begin(), g.jr.end(), jr);
+        std::copy(g.jz.begin(), g.jz.end(), jz);
+        std::copy(jrp.begin(), jrp.end(), jr_phys);
+        std::copy(jzp.begin(), jzp.end(), jz_phys);
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
 void oracle_counts(int64_t* n_sec, int64_t* n_src, int64_t* n_seg)
 {
     *n_sec = static_cast<int64_t>(g_out.secondaries.size());

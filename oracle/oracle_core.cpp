@@ -1560,6 +1560,8 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
             tile.uy[ip] = u * dy;
             tile.uz[ip] = u * dz;
             Crossing const c = boundary_crossing(path);
+            // TransportSideEffects::AccumulateChargedEscape (O/RreaTransportLog.H:573-584)
+            if (!c.valid) fail(RREA_GPU_ERR_GEOMETRY, "charged escape has no certified absorbing-face crossing");
             push_segment(1, {r_particle, z_particle, c.sr, c.sz, c.cr, c.cz, -weight}, 1u, c.faces);
             if (escape.invalidate) tile.id[ip] = -tile.id[ip];
             out_disposition[sp] = 1;
@@ -2093,6 +2095,8 @@ void ApplyPositronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
             tile.uy[ip] = u * dy;
             tile.uz[ip] = u * dz;
             Crossing const c = boundary_crossing(path);
+            // TransportSideEffects::AccumulateChargedEscape (O/RreaTransportLog.H:573-584)
+            if (!c.valid) fail(RREA_GPU_ERR_GEOMETRY, "charged escape has no certified absorbing-face crossing");
             push_segment(1, {r_particle, z_particle, c.sr, c.sz, c.cr, c.cz, weight}, 1u, c.faces);
             if (escape.invalidate) tile.id[ip] = -tile.id[ip];
             out.disposition[sp] = 1;
@@ -2868,6 +2872,238 @@ int RunPrimitive(TableSet const& ts, int which, double const* in, int64_t n, dou
         }
     }
     return 0;
+}
+
+// ======================================================================
+// Net-chord current: I/RreaSegmentDepositionRZ.H:64-458 and the coupling's
+// padded grid (O/RreaWarpXCoupling.cpp:417-544)
+// ======================================================================
+void NetChordGrid::Reset(rrea_gpu_config const& cfg)
+{
+    int constexpr pad = 2;
+    phys_nr = cfg.nr;
+    phys_nz = cfg.nz;
+    phys_z_begin = pad;
+    nr = cfg.nr + pad;
+    nz = cfg.nz + 2 * pad;
+    dr = (cfg.r_hi - cfg.r_lo) / cfg.nr;
+    dz = (cfg.z_hi - cfg.z_lo) / cfg.nz;
+    r_lo = cfg.r_lo;
+    z_lo = cfg.z_lo - pad * dz;
+    rho.assign(static_cast<std::size_t>(nr) * nz, 0.0);
+    jr.assign(static_cast<std::size_t>(nr + 1) * nz, 0.0);
+    jz.assign(static_cast<std::size_t>(nr) * (nz + 1), 0.0);
+}
+
+namespace {
+
+// :67-90
+void cic_charge(NetChordGrid& g, double q, double r, double z)
+{
+    double const xr = (r - g.r_lo) / g.dr - 0.5;
+    double const xz = (z - g.z_lo) / g.dz - 0.5;
+    int const i0 = static_cast<int>(std::floor(xr));
+    int const j0 = static_cast<int>(std::floor(xz));
+    double const fr = xr - i0, fz = xz - j0;
+    double const wr[2] = {1.0 - fr, fr};
+    double const wz[2] = {1.0 - fz, fz};
+    for (int a = 0; a < 2; ++a) {
+        for (int b = 0; b < 2; ++b) {
+            int i = i0 + a, j = j0 + b;
+            if (i < 0) i = -1 - i;
+            if (i >= g.nr) i = g.nr - 1;
+            if (j < 0) j = 0;
+            if (j >= g.nz) j = g.nz - 1;
+            g.rho[static_cast<std::size_t>(i) + static_cast<std::size_t>(g.nr) * j] += q * wr[a] * wz[b];
+        }
+    }
+}
+
+// :96-150: index-space fluxes of one in-cell piece, midpoint transverse weights
+void deposit_piece(NetChordGrid& g, double q_over_dt, double xr0, double xz0, double xr1, double xz1)
+{
+    double fr_flux = q_over_dt * (xr1 - xr0);
+    double const fz_flux = q_over_dt * (xz1 - xz0);
+    double const mr = 0.5 * (xr0 + xr1), mz = 0.5 * (xz0 + xz1);
+    {
+        int const jf = static_cast<int>(std::floor(mz));
+        double const fz = mz - jf;
+        int const fi = static_cast<int>(std::floor(mr)) + 1;
+        if (fi <= 0) fr_flux = 0.0;
+        for (int b = 0; b < 2; ++b) {
+            int j = jf + b;
+            if (j < 0) j = 0;
+            if (j >= g.nz) j = g.nz - 1;
+            int i = fi;
+            if (i <= 0) continue;
+            if (i > g.nr) i = g.nr;
+            g.jr[static_cast<std::size_t>(i) + static_cast<std::size_t>(g.nr + 1) * j] +=
+                fr_flux * (b == 0 ? 1.0 - fz : fz);
+        }
+    }
+    {
+        int const ifc = static_cast<int>(std::floor(mr));
+        double const fr = mr - ifc;
+        int const fj = static_cast<int>(std::floor(mz)) + 1;
+        for (int a = 0; a < 2; ++a) {
+            int i = ifc + a;
+            if (i < 0) i = -1 - i;
+            if (i >= g.nr) i = g.nr - 1;
+            int j = fj;
+            if (j < 0) j = 0;
+            if (j > g.nz) j = g.nz;
+            g.jz[static_cast<std::size_t>(i) + static_cast<std::size_t>(g.nr) * j] +=
+                fz_flux * (a == 0 ? 1.0 - fr : fr);
+        }
+    }
+}
+
+// :152-189: split at CIC cell boundaries in both directions, then deposit
+void deposit_segment(NetChordGrid& g, double q, double dt, double r0, double z0, double r1, double z1)
+{
+    double const q_over_dt = q / dt;
+    double const xr0 = (r0 - g.r_lo) / g.dr - 0.5, xz0 = (z0 - g.z_lo) / g.dz - 0.5;
+    double const xr1 = (r1 - g.r_lo) / g.dr - 0.5, xz1 = (z1 - g.z_lo) / g.dz - 0.5;
+    std::vector<double> cuts{0.0, 1.0};
+    auto add = [&cuts](double a, double b) {
+        if (a == b) return;
+        double const lo = std::min(a, b), hi = std::max(a, b);
+        for (double k = std::ceil(lo); k <= std::floor(hi); ++k) {
+            double const t = (k - a) / (b - a);
+            if (t > 0.0 && t < 1.0) cuts.push_back(t);
+        }
+    };
+    add(xr0, xr1);
+    add(xz0, xz1);
+    std::sort(cuts.begin(), cuts.end());
+    for (std::size_t p = 0; p + 1 < cuts.size(); ++p) {
+        double const s0 = cuts[p], s1 = cuts[p + 1];
+        if (s1 <= s0) continue;
+        deposit_piece(g, q_over_dt, xr0 + s0 * (xr1 - xr0), xz0 + s0 * (xz1 - xz0), xr0 + s1 * (xr1 - xr0),
+                      xz0 + s1 * (xz1 - xz0));
+    }
+}
+
+// :229-397
+bool deposit_escape(NetChordGrid& g, double q, double dt, double sr0, double sz0, double fr0, double fz0, double cr,
+                    double cz, uint32_t faces)
+{
+    uint32_t constexpr known = 1u | 2u | 4u;
+    if (!(dt > 0.0) || !std::isfinite(q) || !std::isfinite(dt) || !std::isfinite(sr0) || !std::isfinite(sz0)
+        || !std::isfinite(fr0) || !std::isfinite(fz0) || !std::isfinite(cr) || !std::isfinite(cz)
+        || g.phys_nr <= 0 || g.phys_nr >= g.nr || g.phys_nz <= 0 || g.phys_z_begin <= 0
+        || g.phys_z_begin + g.phys_nz >= g.nz || faces == 0u || (faces & ~known) != 0u
+        || ((faces & 2u) && (faces & 4u))) {
+        return false;
+    }
+    if (faces & 1u) cr = g.r_lo + g.phys_nr * g.dr;
+    if (faces & 2u) cz = g.z_lo + g.phys_z_begin * g.dz;
+    else if (faces & 4u) cz = g.z_lo + (g.phys_z_begin + g.phys_nz) * g.dz;
+    struct Move {
+        std::size_t from, to, face;
+        double charge;
+        bool radial;
+        int orient;
+    };
+    std::vector<Move> moves;
+    double const xr = (cr - g.r_lo) / g.dr - 0.5;
+    double const xz = (cz - g.z_lo) / g.dz - 0.5;
+    int const i0 = static_cast<int>(std::floor(xr));
+    int const j0 = static_cast<int>(std::floor(xz));
+    double const fr = xr - i0, fz = xz - j0;
+    double const wr[2] = {1.0 - fr, fr};
+    double const wz[2] = {1.0 - fz, fz};
+    for (int a = 0; a < 2; ++a) {
+        for (int b = 0; b < 2; ++b) {
+            int i = i0 + a;
+            int const j = j0 + b;
+            if (i < 0) i = -1 - i;
+            if (i < 0 || i >= g.nr || j < 0 || j >= g.nz) return false;
+            bool const physical = i < g.phys_nr && j >= g.phys_z_begin && j < g.phys_z_begin + g.phys_nz;
+            if (!physical) continue;
+            uint32_t cand[3];
+            int nc = 0;
+            if ((faces & 1u) && i == g.phys_nr - 1) cand[nc++] = 1u;
+            if ((faces & 2u) && j == g.phys_z_begin) cand[nc++] = 2u;
+            if ((faces & 4u) && j == g.phys_z_begin + g.phys_nz - 1) cand[nc++] = 4u;
+            if (nc == 0) return false;
+            double const share = q * wr[a] * wz[b] / nc;
+            std::size_t const from = static_cast<std::size_t>(i) + static_cast<std::size_t>(g.nr) * j;
+            for (int c = 0; c < nc; ++c) {
+                if (cand[c] == 1u) {
+                    moves.push_back(Move{from, static_cast<std::size_t>(i + 1) + static_cast<std::size_t>(g.nr) * j,
+                                         static_cast<std::size_t>(g.phys_nr) + static_cast<std::size_t>(g.nr + 1) * j,
+                                         share, true, 1});
+                } else {
+                    int const face_j = cand[c] == 2u ? g.phys_z_begin : g.phys_z_begin + g.phys_nz;
+                    int const to_j = cand[c] == 2u ? j - 1 : j + 1;
+                    moves.push_back(Move{from, static_cast<std::size_t>(i) + static_cast<std::size_t>(g.nr) * to_j,
+                                         static_cast<std::size_t>(i) + static_cast<std::size_t>(g.nr) * face_j, share,
+                                         false, cand[c] == 2u ? -1 : 1});
+                }
+            }
+        }
+    }
+    if (moves.empty()) return false;
+    cic_charge(g, -q, sr0, sz0);
+    cic_charge(g, q, cr, cz);
+    deposit_segment(g, q, dt, sr0, sz0, fr0, fz0);
+    deposit_segment(g, q, dt, fr0, fz0, cr, cz);
+    for (Move const& m : moves) {
+        double const flux = m.orient * m.charge / dt;
+        if (m.radial) g.jr[m.face] += flux;
+        else g.jz[m.face] += flux;
+        g.rho[m.from] -= m.charge;
+        g.rho[m.to] += m.charge;
+    }
+    return true;
+}
+
+}  // namespace
+
+// O/RreaWarpXCoupling.cpp:446-544 (AccumulateChargedSegment / AccumulateChargedEscape)
+void DepositNetChords(NetChordGrid& g, double dt_s, std::vector<Segment> const& segments)
+{
+    for (Segment const& s : segments) {
+        if (s.kind == 0) {
+            double const q = s.a[4];
+            if (q == 0.0) continue;
+            deposit_segment(g, q, dt_s, s.a[0], s.a[1], s.a[2], s.a[3]);
+        } else {
+            double const q = s.a[6];
+            if (q == 0.0) continue;
+            if (!deposit_escape(g, q, dt_s, s.a[0], s.a[1], s.a[2], s.a[3], s.a[4], s.a[5], s.faces)) {
+                fail(RREA_GPU_ERR_GEOMETRY, "charged escape could not close its exact boundary CIC cloud");
+            }
+        }
+    }
+}
+
+void ConvertNetChordCurrent(NetChordGrid const& g, std::vector<double>& jr_phys, std::vector<double>& jz_phys)
+{
+    double constexpr pi = 3.14159265358979323846;
+    double constexpr qe = 1.602176634e-19;
+    int const nr = g.phys_nr, nz = g.phys_nz, pad = g.phys_z_begin;
+    jr_phys.assign(static_cast<std::size_t>(nr + 1) * nz, 0.0);
+    jz_phys.assign(static_cast<std::size_t>(nr) * (nz + 1), 0.0);
+    for (int j = pad; j < pad + nz; ++j) {
+        for (int i = 0; i <= nr; ++i) {
+            double const flux = g.jr[static_cast<std::size_t>(i) + static_cast<std::size_t>(g.nr + 1) * j];
+            double const rf = i * g.dr;
+            if (flux == 0.0 || rf <= 0.0) continue;
+            jr_phys[static_cast<std::size_t>(i) + static_cast<std::size_t>(nr + 1) * (j - pad)] +=
+                qe * flux / (2.0 * pi * rf * g.dz);
+        }
+    }
+    for (int j = pad; j <= pad + nz; ++j) {
+        for (int i = 0; i < nr; ++i) {
+            double const flux = g.jz[static_cast<std::size_t>(i) + static_cast<std::size_t>(g.nr) * j];
+            if (flux == 0.0) continue;
+            double const rlo = i * g.dr, rhi = (i + 1) * g.dr;
+            jz_phys[static_cast<std::size_t>(i) + static_cast<std::size_t>(nr) * (j - pad)] +=
+                qe * flux / (pi * (rhi * rhi - rlo * rlo));
+        }
+    }
 }
 
 // O/RreaCouplingSources.cpp:435-512 + S/RreaEventAccumulator.cpp:129-164, 386-502

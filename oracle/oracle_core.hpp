@@ -195,6 +195,26 @@ void ApplyPositronTransport(rrea_host::TableSet const& tables, rrea_gpu_config c
 void ApplyPhotonTransport(rrea_host::TableSet const& tables, rrea_gpu_config const& cfg, int step, double dt_s,
                           ChargedTile& tile, StepOutputs& out);
 
+// Padded net-chord grid of the coupling (O/RreaWarpXCoupling.cpp:417-444):
+// nr + 2 cells in r, nz + 4 in z (two pad cells below and above).
+struct NetChordGrid {
+    int nr = 0, nz = 0;          // padded sizes
+    int phys_nr = 0, phys_z_begin = 0, phys_nz = 0;
+    double dr = 0.0, dz = 0.0, r_lo = 0.0, z_lo = 0.0;
+    std::vector<double> rho, jr, jz;  // rho nr*nz; jr (nr+1)*nz; jz nr*(nz+1)
+    void Reset(rrea_gpu_config const& cfg);
+};
+
+// Replays the step's charged segments into the grid: DepositSegmentRZ for a
+// net chord and DepositEscapingSegmentRZ for an escape
+// (I/RreaSegmentDepositionRZ.H:96-397).  Throws on an escape whose boundary
+// cloud cannot be closed.
+void DepositNetChords(NetChordGrid& g, double dt_s, std::vector<Segment> const& segments);
+
+// ConvertPaddedIndexCurrentToPhysicalRZ (I/RreaSegmentDepositionRZ.H:399-458)
+// with the coupling's charge per index flux (the elementary charge).
+void ConvertNetChordCurrent(NetChordGrid const& g, std::vector<double>& jr_phys, std::vector<double>& jz_phys);
+
 // Primitive-level evaluation for fixture comparisons (ids listed in oracle_core.cpp).
 int RunPrimitive(rrea_host::TableSet const& tables, int which, double const* in, int64_t n, double* out);
 

@@ -9,7 +9,9 @@
 #include "RreaParticleInteraction.H"
 #include "RreaRng.H"
 #include "rrea/RreaInteractionTables.H"
+#include "rrea/RreaConstants.H"
 #include "rrea/RreaSeedSchedule.H"
+#include "rrea/RreaSegmentDepositionRZ.H"
 #include "rrea/RreaTransportPath.H"
 
 #include <cmath>
@@ -354,6 +356,63 @@ int main(int argc, char** argv)
             write_f8("ref_positron_accessors", 7, acc);
             write_f8("ref_bhabha_energy", 3, bha);
             write_f8("ref_positron_brems_energy", 3, pbr);
+        }
+
+        // ---- net-chord current: I/RreaSegmentDepositionRZ.H on the coupling's padded grid
+        //      (8 x 12 physical cells of 0.75 m x 1.25 m, two pad cells; O/RreaWarpXCoupling.cpp:417-444)
+        {
+            rrea::SegmentGridRZ grid;
+            int const pnr = 8, pnz = 12, pad = 2;
+            grid.nr = pnr + pad;
+            grid.nz = pnz + 2 * pad;
+            grid.dr = 0.75;
+            grid.dz = 1.25;
+            grid.r_lo = 0.0;
+            grid.z_lo = -pad * grid.dz;
+            grid.resize();
+            double const dt = 3.7e-10;
+            double const rhi = pnr * grid.dr, zhi = pnz * grid.dz;
+            std::vector<double> segs;  // kind, a0..a6, faces
+            for (int i = 0; i < 400; ++i) {
+                double const q = (g.uni() < 0.5 ? -1.0 : 1.0) * (0.5 + 1.5 * g.uni());
+                double const r0 = (i % 17 == 0) ? 0.2 * grid.dr * g.uni() : rhi * g.uni() * 0.999;
+                double const z0 = zhi * g.uni() * 0.999;
+                double const len = 2.0 * grid.dr * g.uni();
+                double const th = 6.283185307179586 * g.uni();
+                double r1 = std::abs(r0 + len * std::cos(th));
+                double z1 = z0 + len * std::sin(th);
+                r1 = std::min(r1, rhi * 0.999);
+                z1 = std::min(std::max(z1, 0.0), zhi * 0.999);
+                rrea::DepositSegmentRZ(grid, q, dt, r0, z0, r1, z1);
+                segs.insert(segs.end(), {0.0, r0, z0, r1, z1, q, 0.0, 0.0, 0.0});
+            }
+            for (int i = 0; i < 150; ++i) {
+                double const q = (g.uni() < 0.5 ? -1.0 : 1.0) * (0.5 + 1.5 * g.uni());
+                int const face = i % 3;  // 0 r_hi, 1 z_lo, 2 z_hi
+                double cr, cz;
+                std::uint32_t bits;
+                if (face == 0) { cr = rhi; cz = zhi * (0.05 + 0.9 * g.uni()); bits = rrea::kEscapeFaceRHi; }
+                else if (face == 1) { cr = rhi * 0.95 * g.uni(); cz = 0.0; bits = rrea::kEscapeFaceZLo; }
+                else { cr = rhi * 0.95 * g.uni(); cz = zhi; bits = rrea::kEscapeFaceZHi; }
+                double const fr0 = std::min(std::abs(cr - (face == 0 ? 0.4 : 0.3 * (g.uni() - 0.5))), rhi * 0.999);
+                double const fz0 = std::min(std::max(cz + (face == 1 ? 0.4 : face == 2 ? -0.4 : 0.3 * (g.uni() - 0.5)),
+                                                     0.0), zhi * 0.999);
+                double const sr0 = std::min(std::abs(fr0 - 0.8 * (g.uni() - 0.5)), rhi * 0.999);
+                double const sz0 = std::min(std::max(fz0 - 0.8 * (g.uni() - 0.5), 0.0), zhi * 0.999);
+                auto const res = rrea::DepositEscapingSegmentRZ(grid, q, dt, sr0, sz0, fr0, fz0, cr, cz, pnr, pad, pnz,
+                                                                bits);
+                if (!res.valid) continue;
+                segs.insert(segs.end(), {1.0, sr0, sz0, fr0, fz0, cr, cz, q, static_cast<double>(bits)});
+            }
+            std::vector<double> jr_phys, jz_phys;
+            rrea::ConvertPaddedIndexCurrentToPhysicalRZ(pnr, pnz, grid.dr, grid.dz, pad, rrea::qe, grid.jr, grid.jz,
+                                                        jr_phys, jz_phys);
+            write_f8("ref_netchord_segments", 9, segs);
+            write_f8("ref_netchord_rho", 1, grid.rho);
+            write_f8("ref_netchord_jr", 1, grid.jr);
+            write_f8("ref_netchord_jz", 1, grid.jz);
+            write_f8("ref_netchord_jr_phys", 1, jr_phys);
+            write_f8("ref_netchord_jz_phys", 1, jz_phys);
         }
 
         // ---- photon samplers: S/RreaInteractionTables.cpp:2778-3253

@@ -638,6 +638,38 @@ __device__ __forceinline__ bool cartesian_half_open(Geom const& g, double x, dou
     return isfinite(r) && isfinite(z) && g.rhi > g.rlo && g.zhi > g.zlo && r >= g.rlo && r < g.rhi && z >= g.zlo
         && z < g.zhi;
 }
+// RreaChargedBoundaryCrossingForPath (O/RreaParticleInteraction.H:468-540):
+// the exact absorbing-face point of the final microchord and the crossed
+// faces (bits 1 r_hi, 2 z_lo, 4 z_hi).  Returns false when no face is
+// certified.
+template <int NP>
+__device__ __forceinline__ bool charged_crossing(Path<NP> const& p, Geom const& g, double& sr, double& sz, double& cr,
+                                                 double& cz, uint32_t& faces)
+{
+    double cx, cy;
+    point_at_full(p, g, p.in_end, cx, cy, cz);
+    cz = wrap_z(g, cz);
+    cr = hypot(cx, cy);
+    sr = hypot(p.sx, p.sy);
+    sz = wrap_z(g, p.sz);
+    double const scale = fmax(1.0, fmax(g.rhi, fmax(fabs(g.zlo), fabs(g.zhi))));
+    double const tol = 512.0 * kEps * scale;
+    bool const on_r = fabs(cr - g.rhi) <= tol;
+    bool const on_zlo = !g.periodic && fabs(cz - g.zlo) <= tol;
+    bool const on_zhi = !g.periodic && fabs(cz - g.zhi) <= tol;
+    double const dx = p.ex - p.sx, dy = p.ey - p.sy, dz = p.ez - p.sz;
+    double const outward = cx * dx + cy * dy;
+    faces = 0u;
+    if (on_r && outward > -tol * scale) { faces |= 1u; cr = g.rhi; }
+    if (on_zlo && dz < 0.0) { faces |= 2u; cz = g.zlo; }
+    if (on_zhi && dz > 0.0) { faces |= 4u; cz = g.zhi; }
+    if (faces == 0u) {
+        if (on_r) { faces |= 1u; cr = g.rhi; }
+        if (on_zhi) { faces |= 4u; cz = g.zhi; }
+    }
+    return faces != 0u && isfinite(sr) && isfinite(sz) && isfinite(cr) && isfinite(cz);
+}
+
 // O/RreaParticleInteraction.H:409-452 (clipped policy: RREA owns every escape)
 template <int NP>
 __device__ __forceinline__ void clipped_escape_policy(Path<NP> const& p, Geom const& g, double er, double ez,

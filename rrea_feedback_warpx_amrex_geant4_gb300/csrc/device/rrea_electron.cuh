@@ -550,18 +550,51 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     double transported_dpath = 0.0, transported_len = 0.0;
     double particle_density = ds > 0.0 ? chord_dpath / ds : positive_or(rho, rho);
 
+    // net chord from the captured start (AccumulateChargedSegment), signed
+    // with the species charge; deposited by the current pass after the kernel
+    auto put_segment = [&](double r1, double z1) {
+        if (!A.segments) return;
+        SegmentRec& s = A.segments[ip];
+        s.a[0] = r_particle;
+        s.a[1] = z_particle;
+        s.a[2] = r1;
+        s.a[3] = z1;
+        s.a[4] = q * weight;
+        s.faces = 0u;
+        s.kind = 1;
+    };
     auto commit_escape = [&]() {
-        // O/RreaTransportStep.H:829-863 (the escape deposit is applied by the
-        // current-deposition pass, not here)
+        // O/RreaTransportStep.H:829-863: the escape deposit closes on the
+        // exact face crossing of the final microchord
         double const u = proper_velocity_from_kinetic(k);
         A.ux[ip] = u * dx;
         A.uy[ip] = u * dy;
         A.uz[ip] = u * dz;
+        double sr, sz, cr, cz;
+        uint32_t faces;
+        if (!charged_crossing(path, g, sr, sz, cr, cz, faces)) {
+            // O/RreaTransportLog.H:581-584
+            err.set(RREA_GPU_ERR_GEOMETRY);
+            return finish(-1);
+        }
+        if (A.segments) {
+            SegmentRec& s = A.segments[ip];
+            s.a[0] = r_particle;
+            s.a[1] = z_particle;
+            s.a[2] = sr;
+            s.a[3] = sz;
+            s.a[4] = cr;
+            s.a[5] = cz;
+            s.a[6] = q * weight;
+            s.faces = faces;
+            s.kind = 2;
+        }
         if (esc_inv) A.id[ip] = -A.id[ip];
         return finish(1);
     };
     auto demote = [&](double r, double z) {
         // O/RreaElectronTransport.cpp:151-174, 856-879
+        put_segment(r, z);
         deposit_source(C, A.cells, 1, r, z, weight, 0.0, 0.0);
         deposit_local(r, z, k);
         A.id[ip] = -A.id[ip];
@@ -569,6 +602,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     };
     auto annihilate = [&](double x, double y, double z, double r, uint64_t idx, double birth) {
         // at-rest annihilation, O/RreaPositronTransport.cpp:131-160, 793-845
+        put_segment(r, z);
         lineage = spawn_annihilation(A, rng, idx, ip, key, weight, lineage, x, y, z, r, dx, dy, dz, k, true, birth);
         A.id[ip] = -A.id[ip];
         return finish(2);
@@ -892,6 +926,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                                                 err);
                     } else {
                         // in-flight annihilation, O/RreaPositronTransport.cpp:700-727
+                        put_segment(er, ez);
                         lineage = spawn_annihilation(A, rng, rng_index, ip, key, weight, lineage, ex, ey, ez, er, dx,
                                                      dy, dz, k, false, birth);
                         annihilated = true;
@@ -982,6 +1017,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         A.r[ip] = hypot(run_x, run_y);
         A.theta[ip] = atan2(run_y, run_x);
         A.z[ip] = run_z;
+        put_segment(A.r[ip], run_z);
         return finish(0);
     }
     if (transported_len > 0.0) particle_density = transported_dpath / transported_len;
@@ -1020,6 +1056,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     A.r[ip] = end_r;
     A.theta[ip] = atan2(run_y, run_x);
     A.z[ip] = run_z;
+    put_segment(end_r, run_z);
     return finish(0);
 }
 

@@ -8,6 +8,28 @@
 
 namespace rrea_dev {
 
+// One charged particle's net-chord record for the current deposition
+// (TransportSideEffects::AccumulateChargedSegment / AccumulateChargedEscape,
+// O/RreaTransportLog.H:556-599).  kind 0: nothing to deposit; 1: segment
+// (a0..a4 = r0, z0, r1, z1, signed weight); 2: escape (a0..a6 = trajectory
+// start r, z, final microchord start r, z, crossing r, z, signed weight).
+struct SegmentRec {
+    double a[7];
+    int32_t kind;
+    uint32_t faces;
+};
+
+// The coupling's padded net-chord grid (O/RreaWarpXCoupling.cpp:417-444):
+// rho nr*nz, jr (nr+1)*nz, jz nr*(nz+1), index-space fluxes.
+struct NetGrid {
+    int nr, nz;                           // padded cells
+    int phys_nr, phys_z_begin, phys_nz;   // physical block inside the padding
+    double dr, dz, r_lo, z_lo;            // z_lo of the padded grid
+    double* rho;
+    double* jr;
+    double* jz;
+};
+
 struct ElectronArgs {
     int64_t n;
     // The current and prev_* arrays may alias (resident engine mode, where
@@ -48,6 +70,8 @@ struct ElectronArgs {
     // photon phase only: 1 = push each photon straight by c*dt from its
     // current state before transporting the chord (resident mode)
     int32_t straight_push;
+    // charged phases: one net-chord record per tile slot (may be null)
+    SegmentRec* __restrict__ segments;
 };
 
 }  // namespace rrea_dev

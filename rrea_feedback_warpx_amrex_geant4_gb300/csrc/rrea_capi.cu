@@ -65,6 +65,13 @@ struct rrea_gpu_ctx {
     int64_t* d_offsets = nullptr;
     int64_t* d_scan_scratch = nullptr;
     double* d_cells = nullptr;
+    // net-chord current (non-periodic z only): one record per tile slot and
+    // the padded index-space grid plus the physical face currents
+    rrea_dev::SegmentRec* d_seg = nullptr;
+    rrea_dev::NetGrid net{};
+    bool netchord = false;
+    double* d_jr_phys = nullptr;
+    double* d_jz_phys = nullptr;
     uint64_t* d_diag_sub = nullptr;
     uint64_t* d_diag_ev = nullptr;
     int32_t* d_diag_disp = nullptr;
@@ -208,6 +215,29 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         for (int f = 0; ok && f < kTileDoubles; ++f) ok = dalloc(&st.d[f], n) == cudaSuccess;
         ok = ok && dalloc(&st.id, n) == cudaSuccess && dalloc(&st.cpu, n) == cudaSuccess;
     }
+    ctx->netchord = cfg->periodic_z == 0;
+    {
+        // O/RreaWarpXCoupling.cpp:417-444: two pad cells beyond r_hi, below z_lo and above z_hi
+        int constexpr pad = 2;
+        rrea_dev::NetGrid& g = ctx->net;
+        g.phys_nr = cfg->nr;
+        g.phys_nz = cfg->nz;
+        g.phys_z_begin = pad;
+        g.nr = cfg->nr + pad;
+        g.nz = cfg->nz + 2 * pad;
+        g.dr = (cfg->r_hi - cfg->r_lo) / cfg->nr;
+        g.dz = (cfg->z_hi - cfg->z_lo) / cfg->nz;
+        g.r_lo = cfg->r_lo;
+        g.z_lo = cfg->z_lo - pad * g.dz;
+        if (ctx->netchord) {
+            ok = ok && dalloc(&ctx->d_seg, n) == cudaSuccess
+                && dalloc(&g.rho, static_cast<size_t>(g.nr) * g.nz) == cudaSuccess
+                && dalloc(&g.jr, static_cast<size_t>(g.nr + 1) * g.nz) == cudaSuccess
+                && dalloc(&g.jz, static_cast<size_t>(g.nr) * (g.nz + 1)) == cudaSuccess
+                && dalloc(&ctx->d_jr_phys, static_cast<size_t>(cfg->nr + 1) * cfg->nz) == cudaSuccess
+                && dalloc(&ctx->d_jz_phys, static_cast<size_t>(cfg->nr) * (cfg->nz + 1)) == cudaSuccess;
+        }
+    }
     ctx->sec_capacity = 2 * capacity + 4096;
     size_t const nsec = static_cast<size_t>(ctx->sec_capacity);
     ok = ok && dalloc(&ctx->d_sec_unordered, nsec) == cudaSuccess && dalloc(&ctx->d_sec_ordered, nsec) == cudaSuccess
@@ -222,6 +252,7 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
     if (cudaMemsetAsync(ctx->d_cells, 0, 5 * ncell * sizeof(double), ctx->stream) != cudaSuccess) {
         return bail(RREA_GPU_ERR_CUDA);
     }
+    if (ctx->netchord && rrea_gpu_reset_current(ctx) != RREA_GPU_OK) return bail(RREA_GPU_ERR_CUDA);
     *out = ctx;
     return RREA_GPU_OK;
 }
@@ -250,6 +281,12 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     dfree(ctx->d_offsets);
     dfree(ctx->d_scan_scratch);
     dfree(ctx->d_cells);
+    dfree(ctx->d_seg);
+    dfree(ctx->net.rho);
+    dfree(ctx->net.jr);
+    dfree(ctx->net.jz);
+    dfree(ctx->d_jr_phys);
+    dfree(ctx->d_jz_phys);
     dfree(ctx->d_diag_sub);
     dfree(ctx->d_diag_ev);
     dfree(ctx->d_diag_disp);
@@ -429,6 +466,7 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     a.fv.periodic = c.periodic_z != 0;
     a.fv.has_b = ctx->has_b;
     a.straight_push = (species == RREA_SPECIES_PHOTON && aliased) ? 1 : 0;
+    a.segments = (species != RREA_SPECIES_PHOTON && ctx->netchord) ? ctx->d_seg : nullptr;
     if (a.n > 0) {
         int64_t const want = (a.n + ctx->launch_threads - 1) / ctx->launch_threads;
         int64_t const cap = static_cast<int64_t>(ctx->num_sms) * ctx->launch_blocks_per_sm * (128 / ctx->launch_threads);
@@ -445,6 +483,10 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
                                                       ctx->launch_min_blocks, c.periodic_z != 0, ctx->stream));
         }
         RREA_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+        if (a.segments) {
+            RREA_CUDA(ctx, rrea_launch::netchord_deposit(a.segments, a.n, ctx->net, dt_s, ctx->d_status,
+                                                         ctx->d_fail_index, ctx->num_sms * 8, ctx->stream));
+        }
     }
     unsigned long long count = 0;
     unsigned long long transported = 0;
@@ -585,6 +627,47 @@ rrea_gpu_status rrea_gpu_reset_sources(rrea_gpu_ctx* ctx)
     if (!ctx) return RREA_GPU_ERR_ARGUMENT;
     size_t const n = static_cast<size_t>(ctx->cfg.nr) * ctx->cfg.nz * 5;
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_cells, 0, n * sizeof(double), ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_reset_current(rrea_gpu_ctx* ctx)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->netchord) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "net-chord current needs a non-periodic z domain");
+    rrea_dev::NetGrid const& g = ctx->net;
+    RREA_CUDA(ctx, cudaMemsetAsync(g.rho, 0, static_cast<size_t>(g.nr) * g.nz * sizeof(double), ctx->stream));
+    RREA_CUDA(ctx, cudaMemsetAsync(g.jr, 0, static_cast<size_t>(g.nr + 1) * g.nz * sizeof(double), ctx->stream));
+    RREA_CUDA(ctx, cudaMemsetAsync(g.jz, 0, static_cast<size_t>(g.nr) * (g.nz + 1) * sizeof(double), ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_download_current(rrea_gpu_ctx* ctx, double* jr, double* jz)
+{
+    if (!ctx || !jr || !jz) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->netchord) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "net-chord current needs a non-periodic z domain");
+    rrea_gpu_config const& c = ctx->cfg;
+    RREA_CUDA(ctx, rrea_launch::netchord_convert(ctx->net, ctx->d_jr_phys, ctx->d_jz_phys, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(jr, ctx->d_jr_phys, static_cast<size_t>(c.nr + 1) * c.nz * sizeof(double),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(jz, ctx->d_jz_phys, static_cast<size_t>(c.nr) * (c.nz + 1) * sizeof(double),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_download_current_index(rrea_gpu_ctx* ctx, double* rho, double* jr, double* jz)
+{
+    if (!ctx || !rho || !jr || !jz) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->netchord) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "net-chord current needs a non-periodic z domain");
+    rrea_dev::NetGrid const& g = ctx->net;
+    RREA_CUDA(ctx, cudaMemcpyAsync(rho, g.rho, static_cast<size_t>(g.nr) * g.nz * sizeof(double),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(jr, g.jr, static_cast<size_t>(g.nr + 1) * g.nz * sizeof(double),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(jz, g.jz, static_cast<size_t>(g.nr) * (g.nz + 1) * sizeof(double),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RREA_GPU_OK;
 }

@@ -50,6 +50,7 @@ __device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
     for (int64_t ip = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; ip < A.n;
          ip += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         if (!(A.id[ip] > 0)) {
+            if (A.segments) A.segments[ip].kind = 0;
             if (A.sec_per_parent) A.sec_per_parent[ip] = 0;
             if (A.diag_disposition) A.diag_disposition[ip] = -1;
             if (A.diag_subcycles) A.diag_subcycles[ip] = 0;
@@ -60,6 +61,7 @@ __device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
         uint64_t sub = 0, ev = 0;
         uint32_t lineage = 0;
         ++moved;
+        if (A.segments) A.segments[ip].kind = 0;
         int const disp = transport_charged<NP, POS>(C, A, ip, sub, ev, lineage, err);
         // Every record this particle appended carries a lineage below this
         // count, so the ordering scan/scatter stays in bounds on every path.

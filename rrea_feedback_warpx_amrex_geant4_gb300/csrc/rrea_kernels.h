@@ -7,6 +7,8 @@
 
 namespace rrea_dev {
 struct ElectronArgs;
+struct SegmentRec;
+struct NetGrid;
 }
 
 namespace rrea_launch {
@@ -21,6 +23,11 @@ cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
 // Photon phase (rrea_photon_kernels.cu); copies `sc` to its own constant bank.
 cudaError_t photon_step(rrea_dev::StepConstants const& sc, rrea_dev::ElectronArgs const& args, int blocks, int threads,
                         bool periodic, cudaStream_t stream);
+// Net-chord current (rrea_deposit.cu): replay the segment records of one
+// charged phase into the padded grid; convert the grid to physical J.
+cudaError_t netchord_deposit(rrea_dev::SegmentRec const* seg, int64_t n, rrea_dev::NetGrid const& g, double dt,
+                             int* status, long long* fail_index, int blocks, cudaStream_t stream);
+cudaError_t netchord_convert(rrea_dev::NetGrid const& g, double* jr_phys, double* jz_phys, cudaStream_t stream);
 int64_t scan_scratch_elems(int64_t n);
 // Exclusive scan of per-parent counts into offsets (block_scratch holds
 // scan_scratch_elems(n) elements); the first half of order_secondaries.

@@ -71,7 +71,8 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_last_step_stats", "rrea_gpu_apply_photons", "rrea_gpu_stage_photons",
     "rrea_gpu_step_photons_resident", "rrea_gpu_fetch_photons", "rrea_gpu_order_secondaries_noalloc",
     "rrea_gpu_apply_positrons", "rrea_gpu_stage_positrons", "rrea_gpu_step_positrons_resident",
-    "rrea_gpu_fetch_positrons",
+    "rrea_gpu_fetch_positrons", "rrea_gpu_reset_current", "rrea_gpu_download_current",
+    "rrea_gpu_download_current_index",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 
@@ -113,6 +114,9 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_fetch_photons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
     lib.rrea_gpu_order_secondaries_noalloc.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp,
                                                        ctypes.c_char_p, ctypes.c_size_t]
+    lib.rrea_gpu_reset_current.argtypes = [vp]
+    lib.rrea_gpu_download_current.argtypes = [vp, _D, _D]
+    lib.rrea_gpu_download_current_index.argtypes = [vp, _D, _D, _D]
     lib.rrea_gpu_download_sources.argtypes = [vp, _D]
     lib.rrea_gpu_reset_sources.argtypes = [vp]
     lib.rrea_gpu_download_diagnostics.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64),
@@ -265,6 +269,27 @@ class RreaGpuContext:
 
     def reset_sources(self):
         self._check(self.lib.rrea_gpu_reset_sources(self.handle))
+
+    def reset_current(self):
+        self._check(self.lib.rrea_gpu_reset_current(self.handle))
+
+    def current(self):
+        """Physical face current densities (Jr (nz, nr+1), Jz (nz+1, nr)) in A/m^2."""
+        c = self.config
+        jr = np.zeros((c.nz, c.nr + 1))
+        jz = np.zeros((c.nz + 1, c.nr))
+        self._check(self.lib.rrea_gpu_download_current(self.handle, jr.ctypes.data_as(_D), jz.ctypes.data_as(_D)))
+        return jr, jz
+
+    def current_index(self):
+        """Padded index-space grids: rho (nz+4, nr+2), jr (nz+4, nr+3), jz (nz+5, nr+2)."""
+        c = self.config
+        rho = np.zeros((c.nz + 4, c.nr + 2))
+        jr = np.zeros((c.nz + 4, c.nr + 3))
+        jz = np.zeros((c.nz + 5, c.nr + 2))
+        self._check(self.lib.rrea_gpu_download_current_index(self.handle, rho.ctypes.data_as(_D),
+                                                             jr.ctypes.data_as(_D), jz.ctypes.data_as(_D)))
+        return {"rho": rho, "jr": jr, "jz": jz}
 
     def diagnostics(self, n):
         sub = np.zeros(n, dtype=np.uint64)

@@ -84,3 +84,45 @@ def test_photoelectron_cos_matches_reference(oracle_mod):
     g = load("ref_photoelectron_cos")
     out = oracle_mod.primitive(19, g[:, :2], 1)[:, 0]
     np.testing.assert_allclose(out, g[:, 2], rtol=0, atol=4e-16)
+
+
+def test_netchord_deposition_matches_reference(oracle_mod):
+    """Net-chord Umeda deposition and escape boundary closure
+    (I/RreaSegmentDepositionRZ.H) on the coupling's padded grid: 8 x 12
+    physical cells of 0.75 m x 1.25 m with two pad cells."""
+    cfg = oracle_mod.RreaGpuConfig()
+    cfg.r_lo, cfg.r_hi, cfg.z_lo, cfg.z_hi, cfg.nr, cfg.nz = 0.0, 6.0, 0.0, 15.0, 8, 12
+    segs = load("ref_netchord_segments")
+    assert (segs[:, 0] == 1).sum() > 50
+    out = oracle_mod.deposit_segments(cfg, 3.7e-10, segs)
+    for key in ("rho", "jr", "jz", "jr_phys", "jz_phys"):
+        np.testing.assert_array_equal(out[key].ravel(), load("ref_netchord_" + key)[:, 0])
+
+
+def test_netchord_continuity_identity(oracle_mod):
+    """Cellwise RZ continuity on the padded index grid: the CIC charge change
+    of a segment equals minus its index-space current divergence times dt."""
+    cfg = oracle_mod.RreaGpuConfig()
+    cfg.r_lo, cfg.r_hi, cfg.z_lo, cfg.z_hi, cfg.nr, cfg.nz = 0.0, 6.0, 0.0, 15.0, 8, 12
+    rng = np.random.default_rng(3)
+    dt = 1.0e-9
+    for _ in range(50):
+        r0, z0 = rng.uniform(0.0, 5.5), rng.uniform(1.0, 14.0)
+        r1, z1 = abs(r0 + rng.uniform(-1.5, 1.5)), z0 + rng.uniform(-1.5, 1.5)
+        q = rng.uniform(-2.0, 2.0)
+        # an escape row with zero charge deposits nothing; use CIC through two segments of opposite sign
+        rows = np.array([[0, r0, z0, r1, z1, q, 0, 0, 0]])
+        out = oracle_mod.deposit_segments(cfg, dt, rows)
+        rho = np.zeros((16, 10))
+        for (r, z, s) in ((r0, z0, -q), (r1, z1, q)):
+            xr, xz = r / 0.75 - 0.5, (z + 2.5) / 1.25 - 0.5
+            i0, j0 = int(np.floor(xr)), int(np.floor(xz))
+            fr, fz = xr - i0, xz - j0
+            for a, wr in ((0, 1 - fr), (1, fr)):
+                for b, wz in ((0, 1 - fz), (1, fz)):
+                    i, j = i0 + a, j0 + b
+                    if i < 0:
+                        i = -1 - i
+                    rho[j, i] += s * wr * wz
+        div = (out["jr"][:, 1:] - out["jr"][:, :-1]) + (out["jz"][1:, :] - out["jz"][:-1, :])
+        np.testing.assert_allclose(rho + dt * div, 0.0, atol=1e-13 * abs(q))
