@@ -178,6 +178,21 @@ rrea_gpu_status rrea_gpu_reset_current(rrea_gpu_ctx* ctx);
 rrea_gpu_status rrea_gpu_download_current(rrea_gpu_ctx* ctx, double* jr, double* jz);
 rrea_gpu_status rrea_gpu_download_current_index(rrea_gpu_ctx* ctx, double* rho, double* jr, double* jz);
 
+/*
+ * Field update kept on the device (RreaAmrexAdvance::AdvanceOneStep's Maxwell
+ * part, S/RreaAmrexAdvance.cpp:593-800, with the leapfrog of
+ * RreaMaxwellTMRZ.H:147-228): the accumulated net-chord current is converted
+ * to physical Jr/Jz and drives `substeps` equal leapfrog substeps of the
+ * scattered TM field (B restaggered by (dt - dt_sub)/2 before and after,
+ * first-order Silver-Mueller on the open faces).  The carrier-fluid current
+ * and conductivity are not included (no fluid model in this library).  The
+ * cell fields the transport gathers are refreshed afterwards.  Refuses a
+ * step violating c dt sqrt(dr^-2 + dz^-2) < 1, and periodic z.
+ */
+rrea_gpu_status rrea_gpu_advance_field(rrea_gpu_ctx* ctx, double dt_s, int32_t substeps);
+/* Copies the scattered field vectors (layouts as rrea_gpu_set_field). */
+rrea_gpu_status rrea_gpu_download_field(rrea_gpu_ctx* ctx, double* er, double* ez, double* btheta);
+
 /* Per-particle diagnostics of the last electron step: substeps used,
  * hazard draws made and terminal disposition (0 survive, 1 escape,
  * 2 demotion, 3 zero-weight skip, -1 not transported). */

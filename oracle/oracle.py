@@ -70,6 +70,8 @@ def lib():
         _lib.oracle_electron_step.argtypes = [ctypes.POINTER(RreaGpuConfig), d, d, d, d, d, ctypes.c_int32,
                                               ctypes.c_double, ctypes.POINTER(RreaGpuTile)]
         _lib.oracle_positron_step.argtypes = _lib.oracle_electron_step.argtypes
+        _lib.oracle_advance_maxwell.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_int, d, d, d, d, d]
         _lib.oracle_deposit_segments.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_double, d, ctypes.c_int64,
                                                  d, d, d, d, d]
         _lib.oracle_photon_step.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_int32, ctypes.c_double,
@@ -189,6 +191,15 @@ def segment_rows(result):
     rows[:, :8] = seg[:, :8]
     rows[:, 8] = seg[:, 9]
     return rows
+
+
+def advance_maxwell(nr, nz, dr, dz, dt_s, substeps, er, ez, bt, jr, jz):
+    """Maxwell TM-RZ field step (no fluid) on copies of er, ez, bt; returns them."""
+    er, ez, bt = (np.array(a, dtype=np.float64).ravel().copy() for a in (er, ez, bt))
+    jr, jz = (np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (jr, jz))
+    _check(lib().oracle_advance_maxwell(nr, nz, dr, dz, dt_s, substeps, _dptr(er), _dptr(ez), _dptr(bt), _dptr(jr),
+                                        _dptr(jz)))
+    return er, ez, bt
 
 
 def photon_step(cfg, step, dt_s, arrays):

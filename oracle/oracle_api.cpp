@@ -187,6 +187,33 @@ int oracle_deposit_segments(rrea_gpu_config const* cfg, double dt_s, double cons
     }
 }
 
+// Maxwell field step in place on (er, ez, bt) with face current (jr, jz).
+int oracle_advance_maxwell(int nr, int nz, double dr, double dz, double dt_s, int substeps, double* er, double* ez,
+                           double* bt, double const* jr, double const* jz)
+{
+    try {
+        oracle::MaxwellField f;
+        f.nr = nr;
+        f.nz = nz;
+        f.dr = dr;
+        f.dz = dz;
+        std::size_t const ner = static_cast<std::size_t>(nr + 1) * nz;
+        std::size_t const nez = static_cast<std::size_t>(nr) * (nz + 1);
+        std::size_t const nbt = static_cast<std::size_t>(nr + 1) * (nz + 1);
+        f.er.assign(er, er + ner);
+        f.ez.assign(ez, ez + nez);
+        f.bt.assign(bt, bt + nbt);
+        std::vector<double> const vjr(jr, jr + ner), vjz(jz, jz + nez);
+        oracle::AdvanceMaxwell(f, dt_s, substeps, vjr, vjz);
+        std::copy(f.er.begin(), f.er.end(), er);
+        std::copy(f.ez.begin(), f.ez.end(), ez);
+        std::copy(f.bt.begin(), f.bt.end(), bt);
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
 void oracle_counts(int64_t* n_sec, int64_t* n_src, int64_t* n_seg)
 {
     *n_sec = static_cast<int64_t>(g_out.secondaries.size());

@@ -3106,6 +3106,89 @@ void ConvertNetChordCurrent(NetChordGrid const& g, std::vector<double>& jr_phys,
     }
 }
 
+// ======================================================================
+// Maxwell TM-RZ: I/RreaMaxwellTMRZ.H:147-228 composed as
+// S/RreaAmrexAdvance.cpp:690-780 (no fluid)
+// ======================================================================
+namespace {
+
+constexpr double kEps0 = 8.8541878128e-12;
+constexpr double kMu0 = 1.25663706212e-6;
+
+inline std::size_t er_at(MaxwellField const& f, int i, int j)
+{
+    return static_cast<std::size_t>(i) + static_cast<std::size_t>(f.nr + 1) * j;
+}
+inline std::size_t ez_at(MaxwellField const& f, int i, int j)
+{
+    return static_cast<std::size_t>(i) + static_cast<std::size_t>(f.nr) * j;
+}
+
+// :143-154, dBtheta/dt = dEz/dr - dEr/dz at interior corners
+void advance_b(MaxwellField& f, double dt)
+{
+    for (int j = 1; j < f.nz; ++j) {
+        for (int i = 1; i < f.nr; ++i) {
+            f.bt[er_at(f, i, j)] += dt * ((f.ez[ez_at(f, i, j)] - f.ez[ez_at(f, i - 1, j)]) / f.dr
+                                         - (f.er[er_at(f, i, j)] - f.er[er_at(f, i, j - 1)]) / f.dz);
+        }
+    }
+}
+// :156-175, first-order Silver-Mueller on the outer r and both z faces
+void silver_mueller(MaxwellField& f)
+{
+    for (int j = 0; j <= f.nz; ++j) f.bt[er_at(f, f.nr, j)] = -f.ez[ez_at(f, f.nr - 1, j)] / kC;
+    for (int i = 1; i <= f.nr; ++i) {
+        f.bt[er_at(f, i, 0)] = -f.er[er_at(f, i, 0)] / kC;
+        f.bt[er_at(f, i, f.nz)] = f.er[er_at(f, i, f.nz - 1)] / kC;
+    }
+    for (int j = 0; j <= f.nz; ++j) f.bt[er_at(f, 0, j)] = 0.0;
+}
+// :177-214 with no conductivity and no ambient term
+void advance_e(MaxwellField& f, double dt, std::vector<double> const& jr, std::vector<double> const& jz)
+{
+    double const c2dt = dt / (kEps0 * kMu0);
+    for (int j = 0; j < f.nz; ++j) {
+        for (int i = 1; i <= f.nr; ++i) {
+            std::size_t const face = er_at(f, i, j);
+            double const a = 0.0 * dt / (2.0 * kEps0);
+            double drive = -c2dt * (f.bt[er_at(f, i, j + 1)] - f.bt[er_at(f, i, j)]) / f.dz;
+            drive -= dt / kEps0 * jr[face];
+            f.er[face] = ((1.0 - a) * f.er[face] + drive) / (1.0 + a);
+        }
+        f.er[er_at(f, 0, j)] = 0.0;
+    }
+    for (int j = 0; j <= f.nz; ++j) {
+        for (int i = 0; i < f.nr; ++i) {
+            std::size_t const face = ez_at(f, i, j);
+            double const a = 0.0 * dt / (2.0 * kEps0);
+            double drive = c2dt * ((i + 1) * f.bt[er_at(f, i + 1, j)] - i * f.bt[er_at(f, i, j)]) / ((i + 0.5) * f.dr);
+            drive -= dt / kEps0 * jz[face];
+            f.ez[face] = ((1.0 - a) * f.ez[face] + drive) / (1.0 + a);
+        }
+    }
+}
+
+}  // namespace
+
+void AdvanceMaxwell(MaxwellField& f, double dt_s, int substeps, std::vector<double> const& jr,
+                    std::vector<double> const& jz)
+{
+    if (!std::isfinite(dt_s) || dt_s <= 0.0 || substeps < 1) fail(RREA_GPU_ERR_ARGUMENT, "invalid field step");
+    double const cfl = kC * dt_s * std::sqrt(1.0 / (f.dr * f.dr) + 1.0 / (f.dz * f.dz));
+    if (!std::isfinite(cfl) || !(cfl < 1.0)) fail(RREA_GPU_ERR_ARGUMENT, "Maxwell TM violates the Yee CFL condition");
+    double const dts = dt_s / static_cast<double>(substeps);
+    double const restagger = 0.5 * (dt_s - dts);
+    advance_b(f, restagger);
+    for (int k = 0; k < substeps; ++k) {
+        advance_b(f, dts);
+        silver_mueller(f);
+        advance_e(f, dts, jr, jz);
+    }
+    advance_b(f, -restagger);
+    silver_mueller(f);
+}
+
 // O/RreaCouplingSources.cpp:435-512 + S/RreaEventAccumulator.cpp:129-164, 386-502
 void DepositSources(rrea_gpu_config const& cfg, std::vector<Source> const& sources, double cutoff,
                     CellSources& cells)

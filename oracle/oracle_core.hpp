@@ -215,6 +215,21 @@ void DepositNetChords(NetChordGrid& g, double dt_s, std::vector<Segment> const& 
 // with the coupling's charge per index flux (the elementary charge).
 void ConvertNetChordCurrent(NetChordGrid const& g, std::vector<double>& jr_phys, std::vector<double>& jz_phys);
 
+// Maxwell TM-RZ field on the replicated vectors (I/RreaMaxwellTMRZ.H:61-85):
+// er (nr+1)*nz, ez nr*(nz+1), bt (nr+1)*(nz+1).
+struct MaxwellField {
+    int nr = 0, nz = 0;
+    double dr = 0.0, dz = 0.0;
+    std::vector<double> er, ez, bt;
+};
+
+// One outer field step with the face current (jr, jz) held over `substeps`
+// equal material substeps: the Maxwell part of RreaAmrexAdvance::AdvanceOneStep
+// (S/RreaAmrexAdvance.cpp:593-800) with no fluid current or conductivity.
+// Throws on a CFL violation.
+void AdvanceMaxwell(MaxwellField& f, double dt_s, int substeps, std::vector<double> const& jr,
+                    std::vector<double> const& jz);
+
 // Primitive-level evaluation for fixture comparisons (ids listed in oracle_core.cpp).
 int RunPrimitive(rrea_host::TableSet const& tables, int which, double const* in, int64_t n, double* out);
 

@@ -10,6 +10,7 @@
 #include "RreaRng.H"
 #include "rrea/RreaInteractionTables.H"
 #include "rrea/RreaConstants.H"
+#include "rrea/RreaMaxwellTMRZ.H"
 #include "rrea/RreaSeedSchedule.H"
 #include "rrea/RreaSegmentDepositionRZ.H"
 #include "rrea/RreaTransportPath.H"
@@ -413,6 +414,54 @@ int main(int argc, char** argv)
             write_f8("ref_netchord_jz", 1, grid.jz);
             write_f8("ref_netchord_jr_phys", 1, jr_phys);
             write_f8("ref_netchord_jz_phys", 1, jz_phys);
+        }
+
+        // ---- Maxwell TM-RZ leapfrog with a fixed face current (I/RreaMaxwellTMRZ.H:147-228),
+        //      composed as S/RreaAmrexAdvance.cpp:690-780 with no fluid: restagger B by
+        //      (dt - dt_sub)/2, `sub` x (B, Silver-Mueller, E), restagger back, Silver-Mueller
+        {
+            rrea::MaxwellTMRZ f;
+            f.nr = 12;
+            f.nz = 20;
+            f.dr = 0.75;
+            f.dz = 1.25;
+            f.z_lo = 0.0;
+            f.resize();
+            for (auto& v : f.er) v = 1.0e4 * (2.0 * g.uni() - 1.0);
+            for (auto& v : f.ez) v = 1.0e4 * (2.0 * g.uni() - 1.0);
+            for (auto& v : f.btheta) v = 3.0e-5 * (2.0 * g.uni() - 1.0);
+            for (int j = 0; j <= f.nz; ++j) f.Bt(0, j) = 0.0;
+            for (int j = 0; j < f.nz; ++j) f.Er(0, j) = 0.0;
+            std::vector<double> jr(f.er.size()), jz(f.ez.size());
+            for (auto& v : jr) v = 2.0e-3 * (2.0 * g.uni() - 1.0);
+            for (auto& v : jz) v = 2.0e-3 * (2.0 * g.uni() - 1.0);
+            std::vector<double> init;
+            init.insert(init.end(), f.er.begin(), f.er.end());
+            init.insert(init.end(), f.ez.begin(), f.ez.end());
+            init.insert(init.end(), f.btheta.begin(), f.btheta.end());
+            init.insert(init.end(), jr.begin(), jr.end());
+            init.insert(init.end(), jz.begin(), jz.end());
+            double const dt = 0.9 / (rrea::kMaxwellC * std::sqrt(1.0 / (f.dr * f.dr) + 1.0 / (f.dz * f.dz)));
+            int const sub = 3;
+            double const dts = dt / sub;
+            double const restagger = 0.5 * (dt - dts);
+            std::vector<double> out;
+            for (int step = 0; step < 4; ++step) {
+                rrea::MaxwellAdvanceB(f, restagger);
+                for (int k = 0; k < sub; ++k) {
+                    rrea::MaxwellAdvanceB(f, dts);
+                    rrea::MaxwellSilverMueller(f);
+                    rrea::MaxwellAdvanceE(f, dts, nullptr, nullptr, &jr, &jz, nullptr, nullptr);
+                }
+                rrea::MaxwellAdvanceB(f, -restagger);
+                rrea::MaxwellSilverMueller(f);
+            }
+            out.insert(out.end(), f.er.begin(), f.er.end());
+            out.insert(out.end(), f.ez.begin(), f.ez.end());
+            out.insert(out.end(), f.btheta.begin(), f.btheta.end());
+            write_f8("ref_maxwell_init", 1, init);
+            write_f8("ref_maxwell_out", 1, out);
+            write_f8("ref_maxwell_dt", 1, std::vector<double>{dt});
         }
 
         // ---- photon samplers: S/RreaInteractionTables.cpp:2778-3253

@@ -672,6 +672,42 @@ rrea_gpu_status rrea_gpu_download_current_index(rrea_gpu_ctx* ctx, double* rho, 
     return RREA_GPU_OK;
 }
 
+rrea_gpu_status rrea_gpu_advance_field(rrea_gpu_ctx* ctx, double dt_s, int32_t substeps)
+{
+    if (!ctx || !(dt_s > 0.0) || !std::isfinite(dt_s) || substeps < 1) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->field_set) return fail(ctx, RREA_GPU_ERR_NOT_READY, "the field must be set before it is advanced");
+    if (!ctx->netchord) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "the field update needs a non-periodic z domain");
+    rrea_gpu_config const& c = ctx->cfg;
+    rrea_dev::NetGrid const& g = ctx->net;
+    double const cfl = 299792458.0 * dt_s * std::sqrt(1.0 / (g.dr * g.dr) + 1.0 / (g.dz * g.dz));
+    if (!std::isfinite(cfl) || !(cfl < 1.0)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "Maxwell TM violates the Yee CFL condition c dt sqrt(dr^-2+dz^-2) < 1");
+    }
+    RREA_CUDA(ctx, rrea_launch::netchord_convert(g, ctx->d_jr_phys, ctx->d_jz_phys, ctx->stream));
+    RREA_CUDA(ctx, rrea_launch::maxwell_step(c.nr, c.nz, g.dr, g.dz, dt_s, substeps, ctx->d_er, ctx->d_ez, ctx->d_bt,
+                                             ctx->d_jr_phys, ctx->d_jz_phys, ctx->stream));
+    RREA_CUDA(ctx, rrea_launch::field_prep(c.nr, c.nz, ctx->d_er, ctx->d_ez, ctx->d_amb_er, ctx->d_amb_ez,
+                                           ctx->d_cell_er, ctx->d_cell_ez, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->has_b = true;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_download_field(rrea_gpu_ctx* ctx, double* er, double* ez, double* bt)
+{
+    if (!ctx || !er || !ez || !bt) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->field_set) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no field has been set");
+    rrea_gpu_config const& c = ctx->cfg;
+    size_t const ner = static_cast<size_t>(c.nr + 1) * c.nz;
+    size_t const nez = static_cast<size_t>(c.nr) * (c.nz + 1);
+    size_t const nbt = static_cast<size_t>(c.nr + 1) * (c.nz + 1);
+    RREA_CUDA(ctx, cudaMemcpyAsync(er, ctx->d_er, ner * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(ez, ctx->d_ez, nez * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(bt, ctx->d_bt, nbt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
 rrea_gpu_status rrea_gpu_download_diagnostics(rrea_gpu_ctx* ctx, int64_t n, uint64_t* subcycles, uint64_t* events,
                                               int32_t* disposition)
 {

@@ -28,6 +28,9 @@ cudaError_t photon_step(rrea_dev::StepConstants const& sc, rrea_dev::ElectronArg
 cudaError_t netchord_deposit(rrea_dev::SegmentRec const* seg, int64_t n, rrea_dev::NetGrid const& g, double dt,
                              int* status, long long* fail_index, int blocks, cudaStream_t stream);
 cudaError_t netchord_convert(rrea_dev::NetGrid const& g, double* jr_phys, double* jz_phys, cudaStream_t stream);
+// Maxwell TM-RZ step with a fixed face current (rrea_field.cu).
+cudaError_t maxwell_step(int nr, int nz, double dr, double dz, double dt, int substeps, double* er, double* ez,
+                         double* bt, const double* jr, const double* jz, cudaStream_t stream);
 int64_t scan_scratch_elems(int64_t n);
 // Exclusive scan of per-parent counts into offsets (block_scratch holds
 // scan_scratch_elems(n) elements); the first half of order_secondaries.

@@ -72,7 +72,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_step_photons_resident", "rrea_gpu_fetch_photons", "rrea_gpu_order_secondaries_noalloc",
     "rrea_gpu_apply_positrons", "rrea_gpu_stage_positrons", "rrea_gpu_step_positrons_resident",
     "rrea_gpu_fetch_positrons", "rrea_gpu_reset_current", "rrea_gpu_download_current",
-    "rrea_gpu_download_current_index",
+    "rrea_gpu_download_current_index", "rrea_gpu_advance_field", "rrea_gpu_download_field",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 
@@ -114,6 +114,8 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_fetch_photons.argtypes = [vp, ctypes.POINTER(RreaGpuTile)]
     lib.rrea_gpu_order_secondaries_noalloc.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp,
                                                        ctypes.c_char_p, ctypes.c_size_t]
+    lib.rrea_gpu_advance_field.argtypes = [vp, ctypes.c_double, ctypes.c_int32]
+    lib.rrea_gpu_download_field.argtypes = [vp, _D, _D, _D]
     lib.rrea_gpu_reset_current.argtypes = [vp]
     lib.rrea_gpu_download_current.argtypes = [vp, _D, _D]
     lib.rrea_gpu_download_current_index.argtypes = [vp, _D, _D, _D]
@@ -269,6 +271,19 @@ class RreaGpuContext:
 
     def reset_sources(self):
         self._check(self.lib.rrea_gpu_reset_sources(self.handle))
+
+    def advance_field(self, dt_s, substeps=1):
+        self._check(self.lib.rrea_gpu_advance_field(self.handle, float(dt_s), int(substeps)))
+
+    def field(self):
+        """Scattered field vectors (er, ez, bt), flat, layouts as set_field."""
+        c = self.config
+        er = np.zeros((c.nr + 1) * c.nz)
+        ez = np.zeros(c.nr * (c.nz + 1))
+        bt = np.zeros((c.nr + 1) * (c.nz + 1))
+        self._check(self.lib.rrea_gpu_download_field(self.handle, er.ctypes.data_as(_D), ez.ctypes.data_as(_D),
+                                                     bt.ctypes.data_as(_D)))
+        return er, ez, bt
 
     def reset_current(self):
         self._check(self.lib.rrea_gpu_reset_current(self.handle))

@@ -126,3 +126,17 @@ def test_netchord_continuity_identity(oracle_mod):
                     rho[j, i] += s * wr * wz
         div = (out["jr"][:, 1:] - out["jr"][:, :-1]) + (out["jz"][1:, :] - out["jz"][:-1, :])
         np.testing.assert_allclose(rho + dt * div, 0.0, atol=1e-13 * abs(q))
+
+
+def test_maxwell_step_matches_reference(oracle_mod):
+    """Maxwell TM-RZ leapfrog (I/RreaMaxwellTMRZ.H) over four outer steps of
+    three material substeps with a fixed face current, 12 x 20 cells."""
+    nr, nz, dr, dz = 12, 20, 0.75, 1.25
+    init = load("ref_maxwell_init")[:, 0]
+    ner, nez, nbt = (nr + 1) * nz, nr * (nz + 1), (nr + 1) * (nz + 1)
+    er, ez, bt = init[:ner], init[ner:ner + nez], init[ner + nez:ner + nez + nbt]
+    jr, jz = init[ner + nez + nbt:2 * ner + nez + nbt], init[2 * ner + nez + nbt:]
+    dt = load("ref_maxwell_dt")[0, 0]
+    for _ in range(4):
+        er, ez, bt = oracle_mod.advance_maxwell(nr, nz, dr, dz, dt, 3, er, ez, bt, jr, jz)
+    np.testing.assert_array_equal(np.concatenate([er, ez, bt]), load("ref_maxwell_out")[:, 0])
