@@ -193,6 +193,22 @@ rrea_gpu_status rrea_gpu_advance_field(rrea_gpu_ctx* ctx, double dt_s, int32_t s
 /* Copies the scattered field vectors (layouts as rrea_gpu_set_field). */
 rrea_gpu_status rrea_gpu_download_field(rrea_gpu_ctx* ctx, double* er, double* ez, double* btheta);
 
+/*
+ * Population ceiling (RreaWarpXCoupling::EnforcePopulationCeiling,
+ * RreaCouplingPopulation.cpp:100-146).  count_live counts the valid
+ * (id > 0) particles of the context's resident tile of `species`.
+ * population_projection is RreaStrictPopulationProjection
+ * (RreaParticleInteraction.H:1257-1275): survivors = current - removals,
+ * projected = survivors + insertions (saturating at UINT64_MAX on overflow);
+ * RREA_GPU_OK when projected <= ceiling (< ceiling with reject_equality),
+ * RREA_GPU_ERR_CAPACITY otherwise or when removals > current, where the
+ * reference aborts.  A ceiling of 0 means "no ceiling" in the reference and
+ * is the caller's to skip.  No context is needed for the projection.
+ */
+rrea_gpu_status rrea_gpu_count_live(rrea_gpu_ctx* ctx, int32_t species, int64_t* live);
+rrea_gpu_status rrea_gpu_population_projection(uint64_t current, uint64_t removals, uint64_t insertions,
+                                               uint64_t ceiling, int32_t reject_equality, uint64_t* projected);
+
 /* Per-particle diagnostics of the last electron step: substeps used,
  * hazard draws made and terminal disposition (0 survive, 1 escape,
  * 2 demotion, 3 zero-weight skip, -1 not transported). */

@@ -708,6 +708,41 @@ rrea_gpu_status rrea_gpu_download_field(rrea_gpu_ctx* ctx, double* er, double* e
     return RREA_GPU_OK;
 }
 
+rrea_gpu_status rrea_gpu_count_live(rrea_gpu_ctx* ctx, int32_t species, int64_t* live)
+{
+    if (!ctx || !live || species < 0 || species >= kSpecies) return RREA_GPU_ERR_ARGUMENT;
+    SpeciesTile const& st = ctx->tiles[species];
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_transported, 0, sizeof(unsigned long long), ctx->stream));
+    RREA_CUDA(ctx, rrea_launch::count_live(st.id, st.n, ctx->d_transported, ctx->num_sms * 4, ctx->stream));
+    unsigned long long count = 0;
+    RREA_CUDA(ctx, cudaMemcpyAsync(&count, ctx->d_transported, sizeof(count), cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *live = static_cast<int64_t>(count);
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_population_projection(uint64_t current, uint64_t removals, uint64_t insertions,
+                                               uint64_t ceiling, int32_t reject_equality, uint64_t* projected)
+{
+    // RreaStrictPopulationProjection (O/RreaParticleInteraction.H:1257-1275)
+    uint64_t p = 0;
+    bool fits;
+    if (removals > current) {
+        fits = false;
+    } else {
+        uint64_t const survivors = current - removals;
+        if (insertions > UINT64_MAX - survivors) {
+            p = UINT64_MAX;
+            fits = false;
+        } else {
+            p = survivors + insertions;
+            fits = reject_equality ? p < ceiling : p <= ceiling;
+        }
+    }
+    if (projected) *projected = p;
+    return fits ? RREA_GPU_OK : RREA_GPU_ERR_CAPACITY;
+}
+
 rrea_gpu_status rrea_gpu_download_diagnostics(rrea_gpu_ctx* ctx, int64_t n, uint64_t* subcycles, uint64_t* events,
                                               int32_t* disposition)
 {

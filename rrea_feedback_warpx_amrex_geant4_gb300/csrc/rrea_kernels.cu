@@ -88,6 +88,18 @@ __global__ void __launch_bounds__(128, MinBlocks) positron_step_kernel(ElectronA
     charged_step_body<NP, true>(A);
 }
 
+// Live (id > 0) particles of a tile, warp-aggregated.
+__global__ void count_live_kernel(const int64_t* __restrict__ id, int64_t n, unsigned long long* __restrict__ out)
+{
+    unsigned int live = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        live += id[i] > 0 ? 1u : 0u;
+    }
+    unsigned int const warp_total = __reduce_add_sync(0xffffffffu, live);
+    if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(out, static_cast<unsigned long long>(warp_total));
+}
+
 // Exclusive scan of per-parent secondary counts (uint32 -> int64 offsets),
 // three passes: block sums, scan of block sums, block-local scan + offset.
 constexpr int kScanBlock = 1024;
@@ -210,6 +222,13 @@ cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
     } else {
         rrea_dev::positron_step_kernel<16, 1><<<blocks, threads, 0, stream>>>(args);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t count_live(const int64_t* id, int64_t n, unsigned long long* out, int blocks, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    rrea_dev::count_live_kernel<<<blocks, 256, 0, stream>>>(id, n, out);
     return cudaGetLastError();
 }
 

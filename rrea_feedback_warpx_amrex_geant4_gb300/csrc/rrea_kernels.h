@@ -31,6 +31,7 @@ cudaError_t netchord_convert(rrea_dev::NetGrid const& g, double* jr_phys, double
 // Maxwell TM-RZ step with a fixed face current (rrea_field.cu).
 cudaError_t maxwell_step(int nr, int nz, double dr, double dz, double dt, int substeps, double* er, double* ez,
                          double* bt, const double* jr, const double* jz, cudaStream_t stream);
+cudaError_t count_live(const int64_t* id, int64_t n, unsigned long long* out, int blocks, cudaStream_t stream);
 int64_t scan_scratch_elems(int64_t n);
 // Exclusive scan of per-parent counts into offsets (block_scratch holds
 // scan_scratch_elems(n) elements); the first half of order_secondaries.

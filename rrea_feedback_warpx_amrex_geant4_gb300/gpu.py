@@ -73,8 +73,10 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_apply_positrons", "rrea_gpu_stage_positrons", "rrea_gpu_step_positrons_resident",
     "rrea_gpu_fetch_positrons", "rrea_gpu_reset_current", "rrea_gpu_download_current",
     "rrea_gpu_download_current_index", "rrea_gpu_advance_field", "rrea_gpu_download_field",
+    "rrea_gpu_count_live", "rrea_gpu_population_projection",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
+SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
 
 _lib = None
 
@@ -115,6 +117,9 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_order_secondaries_noalloc.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp,
                                                        ctypes.c_char_p, ctypes.c_size_t]
     lib.rrea_gpu_advance_field.argtypes = [vp, ctypes.c_double, ctypes.c_int32]
+    lib.rrea_gpu_count_live.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
+    lib.rrea_gpu_population_projection.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                                   ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)]
     lib.rrea_gpu_download_field.argtypes = [vp, _D, _D, _D]
     lib.rrea_gpu_reset_current.argtypes = [vp]
     lib.rrea_gpu_download_current.argtypes = [vp, _D, _D]
@@ -272,6 +277,11 @@ class RreaGpuContext:
     def reset_sources(self):
         self._check(self.lib.rrea_gpu_reset_sources(self.handle))
 
+    def count_live(self, species):
+        live = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_count_live(self.handle, int(species), ctypes.byref(live)))
+        return live.value
+
     def advance_field(self, dt_s, substeps=1):
         self._check(self.lib.rrea_gpu_advance_field(self.handle, float(dt_s), int(substeps)))
 
@@ -325,6 +335,14 @@ class RreaGpuContext:
         s = ctypes.c_void_p()
         self._check(self.lib.rrea_gpu_stream(self.handle, ctypes.byref(s)))
         return s.value
+
+
+def population_projection(current, removals, insertions, ceiling, reject_equality=False):
+    """RreaStrictPopulationProjection: (fits, projected)."""
+    projected = ctypes.c_uint64()
+    status = load_library().rrea_gpu_population_projection(int(current), int(removals), int(insertions), int(ceiling),
+                                                           int(bool(reject_equality)), ctypes.byref(projected))
+    return status == 0, projected.value
 
 
 def order_secondaries_noalloc(d_counts, n_parents, d_unordered, n_secondaries, d_ordered, stream=None):

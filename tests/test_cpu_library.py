@@ -71,3 +71,17 @@ def test_noalloc_source_calls_no_allocator():
         assert banned not in code, banned
     assert "static __device__ __align__(256)" in code
     assert "cudaGetSymbolAddress" in code
+
+
+
+def test_population_projection_matches_reference_rule(gpu):
+    """RreaStrictPopulationProjection (O/RreaParticleInteraction.H:1257-1275);
+    host-only, no GPU call."""
+    P = gpu.population_projection
+    assert P(100, 10, 50, 140) == (True, 140)          # inclusive ceiling
+    assert P(100, 10, 50, 140, True) == (False, 140)   # equality rejected
+    assert P(100, 10, 51, 140) == (False, 141)
+    assert P(5, 6, 0, 10)[0] is False                   # removals > current
+    big = 2 ** 64 - 1
+    assert P(big, 0, 1, big) == (False, big)            # saturates on overflow
+    assert P(0, 0, 0, 0) == (True, 0)

@@ -120,3 +120,19 @@ def test_out_of_domain_state_fails_closed(mods):
     ok = workloads.make_electrons("uniform_c0", 8, seed=4)
     ctx.apply_electrons(ok, 0, 5.0e-10)
     ctx.close()
+
+
+def test_count_live_matches_fetched_tile(mods):
+    gpu, workloads, oracle, compare = mods
+    cfg, ctx, field = _ctx(gpu, workloads, "uniform_c0", 2048)
+    arr = workloads.make_electrons("uniform_c0", 2048, seed=9)
+    arr["id"][::7] *= -1
+    arr["z"][:100] = arr["prev_z"][:100] = 500.0 - 0.01   # these escape
+    ctx.stage_electrons(arr)
+    assert ctx.count_live(gpu.SPECIES_ELECTRON) == int((arr["id"] > 0).sum())
+    ctx.step_electrons_resident(0, 5.0e-10)
+    ctx.fetch_electrons(arr)
+    assert ctx.count_live(gpu.SPECIES_ELECTRON) == int((arr["id"] > 0).sum())
+    fits, projected = gpu.population_projection(ctx.count_live(gpu.SPECIES_ELECTRON), 0, 10, 2048)
+    assert fits and projected == int((arr["id"] > 0).sum()) + 10
+    ctx.close()
