@@ -209,6 +209,38 @@ rrea_gpu_status rrea_gpu_count_live(rrea_gpu_ctx* ctx, int32_t species, int64_t*
 rrea_gpu_status rrea_gpu_population_projection(uint64_t current, uint64_t removals, uint64_t insertions,
                                                uint64_t ceiling, int32_t reject_equality, uint64_t* projected);
 
+/*
+ * Transient FIFO of DrainAndCommitSecondaries (RreaSecondaryCommit.cpp:9-638,
+ * residual advance RreaNewbornAdvance.cpp:20-996).  Every pending secondary
+ * born at elapsed fraction b < 1 is flown through the remaining (1 - b) dt of
+ * the step on its root particle's RNG streams (Newborn* channels 112-123);
+ * its children join the FIFO behind every queued item (a breadth-first walk)
+ * with a lineage from the per-root counter; the survivors come back in FIFO
+ * order with birth_fraction 1, ready for the overlay's AddNParticles.  The
+ * residual flights deposit into the context's cell sources and net-chord
+ * current.  Birth payloads are checked first (RREA_GPU_ERR_ARGUMENT: unknown
+ * species, non-finite fields, weight <= 0, birth outside [0, 1], lineage at
+ * the 2^14 capacity) and survivors last (RREA_GPU_ERR_INVALID_STATE), where
+ * the reference aborts the transaction.
+ *   drain_secondaries: host records in (the Apply secondaries of every phase,
+ *                      in phase order), host survivors out.  Discards the
+ *                      resident queue.
+ *   drain_resident:    drains the queue that the rrea_gpu_step_*_resident
+ *                      calls filled since the last drain; survivors stay in
+ *                      HBM until fetch_survivors.
+ *   pending_secondaries: size of the resident queue; discard != 0 empties it.
+ *   last_drain_stats:  FIFO items advanced and survivors of the last drain.
+ */
+rrea_gpu_status rrea_gpu_drain_secondaries(rrea_gpu_ctx* ctx, const rrea_gpu_secondary* pending,
+                                           int64_t n_pending, int32_t step, double dt_s,
+                                           rrea_gpu_secondary* survivors, int64_t survivor_capacity,
+                                           int64_t* n_survivors);
+rrea_gpu_status rrea_gpu_drain_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t* n_survivors);
+rrea_gpu_status rrea_gpu_fetch_survivors(rrea_gpu_ctx* ctx, rrea_gpu_secondary* survivors, int64_t capacity,
+                                         int64_t* n_survivors);
+rrea_gpu_status rrea_gpu_pending_secondaries(rrea_gpu_ctx* ctx, int64_t* n_pending, int32_t discard);
+rrea_gpu_status rrea_gpu_last_drain_stats(rrea_gpu_ctx* ctx, int64_t* fifo_items, int64_t* survivors);
+
 /* Per-particle diagnostics of the last electron step: substeps used,
  * hazard draws made and terminal disposition (0 survive, 1 escape,
  * 2 demotion, 3 zero-weight skip, -1 not transported). */
@@ -225,7 +257,8 @@ void rrea_gpu_last_error(const rrea_gpu_ctx* ctx, char* buf, size_t size);
  * establishes before WarpX's own charged push, whose kick the transport step
  * discards (RreaTransportStep.H:705-820).
  *   stage:  host tile -> HBM (prev_* are ignored)
- *   step:   one outer step on the resident tile, no host copies
+ *   step:   one outer step on the resident tile, no host copies; its ordered
+ *           secondaries join the resident drain queue
  *   fetch:  HBM -> host tile (r, z, theta, ux, uy, uz, id)
  */
 rrea_gpu_status rrea_gpu_stage_electrons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile);

@@ -72,6 +72,9 @@ def lib():
         _lib.oracle_positron_step.argtypes = _lib.oracle_electron_step.argtypes
         _lib.oracle_advance_maxwell.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                                 ctypes.c_double, ctypes.c_int, d, d, d, d, d]
+        _lib.oracle_drain.argtypes = [ctypes.POINTER(RreaGpuConfig), d, d, d, d, d, ctypes.c_int32, ctypes.c_double,
+                                      ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+        _lib.oracle_survivors.argtypes = [ctypes.c_void_p]
         _lib.oracle_deposit_segments.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_double, d, ctypes.c_int64,
                                                  d, d, d, d, d]
         _lib.oracle_photon_step.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_int32, ctypes.c_double,
@@ -200,6 +203,26 @@ def advance_maxwell(nr, nz, dr, dz, dt_s, substeps, er, ez, bt, jr, jz):
     _check(lib().oracle_advance_maxwell(nr, nz, dr, dz, dt_s, substeps, _dptr(er), _dptr(ez), _dptr(bt), _dptr(jr),
                                         _dptr(jz)))
     return er, ez, bt
+
+
+def drain(cfg, field, step, dt_s, initial):
+    """DrainAndCommitSecondaries over the structured array `initial`
+    (SECONDARY_DTYPE, in the phases' order).  Returns dict with the final
+    survivors (FIFO order), the newborns' sources, segments and cell grids."""
+    cfg = as_config(cfg)
+    initial = np.ascontiguousarray(initial, dtype=SECONDARY_DTYPE)
+    n_surv = ctypes.c_int64()
+    _check(lib().oracle_drain(ctypes.byref(cfg), _dptr(field["er"]), _dptr(field["ez"]), _dptr(field["bt"]),
+                              _dptr(field["amb_er"]), _dptr(field["amb_ez"]), step, dt_s,
+                              ctypes.c_void_p(initial.ctypes.data), initial.shape[0], ctypes.byref(n_surv)))
+    surv = np.zeros(n_surv.value, dtype=SECONDARY_DTYPE)
+    if n_surv.value:
+        lib().oracle_survivors(ctypes.c_void_p(surv.ctypes.data))
+    t = RreaGpuTile()
+    t.n = 0
+    res = _collect(cfg, t)
+    res["survivors"] = surv
+    return res
 
 
 def photon_step(cfg, step, dt_s, arrays):

@@ -214,6 +214,82 @@ int oracle_advance_maxwell(int nr, int nz, double dr, double dz, double dt_s, in
     }
 }
 
+namespace {
+std::vector<oracle::Secondary> g_survivors;
+}
+
+// DrainAndCommitSecondaries over `n` initial secondaries (rrea_gpu_secondary
+// records in the phases' order): survivors are kept for oracle_survivors, the
+// newborns' sources, segments and cell grids replace the step outputs.
+int oracle_drain(rrea_gpu_config const* cfg, double const* er, double const* ez, double const* bt,
+                 double const* amb_er, double const* amb_ez, int32_t step, double dt_s,
+                 rrea_gpu_secondary const* initial, int64_t n, int64_t* n_survivors)
+{
+    if (!g_tables) return RREA_GPU_ERR_NOT_READY;
+    try {
+        oracle::FieldGrid fg;
+        fg.nr = cfg->nr;
+        fg.nz = cfg->nz;
+        fg.dr = (cfg->r_hi - cfg->r_lo) / cfg->nr;
+        fg.dz = (cfg->z_hi - cfg->z_lo) / cfg->nz;
+        fg.z_lo = cfg->z_lo;
+        std::size_t const ner = static_cast<std::size_t>(cfg->nr + 1) * cfg->nz;
+        std::size_t const nez = static_cast<std::size_t>(cfg->nr) * (cfg->nz + 1);
+        std::size_t const nbt = static_cast<std::size_t>(cfg->nr + 1) * (cfg->nz + 1);
+        fg.er.assign(er, er + ner);
+        fg.ez.assign(ez, ez + nez);
+        fg.bt.assign(bt, bt + nbt);
+        fg.amb_er.assign(amb_er, amb_er + ner);
+        fg.amb_ez.assign(amb_ez, amb_ez + nez);
+        std::vector<oracle::Secondary> init(static_cast<std::size_t>(n));
+        for (int64_t i = 0; i < n; ++i) {
+            rrea_gpu_secondary const& r = initial[i];
+            oracle::Secondary& s = init[static_cast<std::size_t>(i)];
+            s.species = r.species;
+            s.process = r.process;
+            s.root_species = r.root_species;
+            s.parent_index = r.parent_index;
+            s.root_key = r.root_key;
+            s.lineage = r.lineage;
+            s.x = r.x; s.y = r.y; s.z = r.z;
+            s.dx = r.dir_x; s.dy = r.dir_y; s.dz = r.dir_z;
+            s.w = r.weight;
+            s.energy = r.energy_eV;
+            s.birth = r.birth_fraction;
+        }
+        g_out.clear();
+        oracle::DrainSecondaries(*g_tables, *cfg, fg, step, dt_s, init, g_survivors, g_out);
+        g_cells.nr = cfg->nr;
+        g_cells.nz = cfg->nz;
+        for (auto& f : g_cells.f) f.assign(static_cast<std::size_t>(cfg->nr) * cfg->nz, 0.0);
+        oracle::DepositSources(*cfg, g_out.sources, cfg->low_energy_cutoff_eV, g_cells);
+        *n_survivors = static_cast<int64_t>(g_survivors.size());
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+void oracle_survivors(rrea_gpu_secondary* out)
+{
+    for (std::size_t i = 0; i < g_survivors.size(); ++i) {
+        auto const& s = g_survivors[i];
+        rrea_gpu_secondary& o = out[i];
+        o.species = s.species;
+        o.process = s.process;
+        o.root_species = s.root_species;
+        o.pad = 0;
+        o.parent_index = s.parent_index;
+        o.root_key = s.root_key;
+        o.lineage = s.lineage;
+        o.x = s.x; o.y = s.y; o.z = s.z;
+        o.dir_x = s.dx; o.dir_y = s.dy; o.dir_z = s.dz;
+        o.weight = s.w;
+        o.energy_eV = s.energy;
+        o.birth_fraction = s.birth;
+    }
+}
+
 void oracle_counts(int64_t* n_sec, int64_t* n_src, int64_t* n_seg)
 {
     *n_sec = static_cast<int64_t>(g_out.secondaries.size());

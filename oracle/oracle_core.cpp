@@ -1,6 +1,8 @@
 // ORACLE — test infrastructure only (see oracle_core.hpp).
 #include "oracle_core.hpp"
 
+#include <map>
+
 #include <cstring>
 #include <functional>
 #include <sstream>
@@ -2441,6 +2443,816 @@ void ApplyPositronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
         out.secondaries.insert(out.secondaries.end(), c.secondaries.begin(), c.secondaries.end());
         out.sources.insert(out.sources.end(), c.sources.begin(), c.sources.end());
         out.segments.insert(out.segments.end(), c.segments.begin(), c.segments.end());
+    }
+}
+
+// ======================================================================
+// Newborn FIFO: O/RreaSecondaryCommit.cpp:9-638 and
+// O/RreaNewbornAdvance.cpp:20-996
+// ======================================================================
+namespace {
+
+// Everything one newborn advance produces besides its own survival.
+struct NewbornEffects {
+    std::vector<Secondary> children;  // root and lineage are assigned at the FIFO merge
+    std::vector<Source> sources;
+    std::vector<Segment> segments;
+};
+
+struct NewbornContext {
+    Tables const& tables;
+    TableSet const& ts;
+    rrea_gpu_config const& cfg;
+    Gather const& gather;
+    int step;
+    double dt_s;
+};
+
+// RreaNewbornResidualFraction / RreaNewbornElapsedStepFraction (O/RreaParticleInteraction.H:171-197)
+double newborn_residual(double birth) { return std::min(1.0, std::max(0.0, 1.0 - birth)); }
+double newborn_elapsed(double birth, double residual, uint64_t completed, uint64_t substeps, double f)
+{
+    double const within = std::min(1.0, std::max(0.0, f));
+    double const consumed = (static_cast<double>(completed) + within) / static_cast<double>(substeps);
+    return std::min(1.0, birth + residual * consumed);
+}
+
+// TransportStep::NewbornFinalPoint (O/RreaNewbornAdvance.cpp:20-48)
+bool newborn_final_point(Path const& path, double fraction, rrea_gpu_config const& cfg, double& x, double& y,
+                         double& z)
+{
+    double const span = fraction - path.in_begin;
+    double pullback = 1.0e-9;
+    for (int attempt = 0; attempt < 5; ++attempt) {
+        double const trial =
+            attempt == 0 ? fraction : std::max(path.in_begin, fraction - pullback * std::max(span, 1.0e-12));
+        path.PointAtFull(trial, x, y, z);
+        if (cartesian_half_open(x, y, path.WrapZ(z), cfg.r_lo, cfg.r_hi, cfg.z_lo, cfg.z_hi)) {
+            z = path.WrapZ(z);
+            return true;
+        }
+        if (attempt > 0) pullback *= 100.0;
+    }
+    return false;
+}
+
+// RreaEvaluateElectronStatePolicy with electron_ensemble_mean_drag_ev_per_m
+// (O/RreaParticleInteraction.H:1279-1317, O/RreaTransportStep.H:226-247)
+bool electron_demotes_at(NewbornContext const& c, double x, double y, double z, double e)
+{
+    double const cut = c.cfg.low_energy_cutoff_eV;
+    double const thr = c.ts.index().hard_moller_threshold_eV;
+    double fer, fez, fbt;
+    c.gather.at(std::hypot(x, y), z, fer, fez, fbt);
+    double const rho = positive_or(positive_or(c.cfg.density_ratio, 1.0), 1.0);
+    double const ke = std::max(e, cut);
+    double drag = 0.0;
+    if (ke > 0.0 && rho > 0.0) {
+        double const hard = c.cfg.debug_disable_hard_moller == 0 ? c.tables.ElectronHardMollerEnergyLoss(ke, rho) : 0.0;
+        drag = (c.tables.ElectronCollisionLoss(ke, rho) + c.tables.ElectronSoftRadiativeDrag(ke, rho)) + hard
+            + c.tables.ElectronTrackedBremsEnergyLoss(ke, rho);
+    }
+    bool const below = e < cut;
+    bool const nonrunaway = thr > 0.0 && e <= thr && std::hypot(fer, fez) <= drag;
+    return below || nonrunaway;
+}
+
+uint64_t pack_newborn(Secondary const& p, uint64_t segment, uint64_t ordinal, uint64_t inner)
+{
+    uint64_t v = 0;
+    if (!try_pack_transient(true, static_cast<uint64_t>(p.root_species), p.lineage, segment, ordinal, inner, v)) {
+        fail(RREA_GPU_ERR_RNG_OVERFLOW, "newborn RNG index overflow");
+    }
+    return v;
+}
+
+// TransportStep::AdvanceChargedNewborn (O/RreaNewbornAdvance.cpp:50-777)
+bool advance_charged_newborn(NewbornContext const& c, Secondary& p, NewbornEffects& fx)
+{
+    Tables const& tables = c.tables;
+    rrea_gpu_config const& cfg = c.cfg;
+    bool const pos = p.species == 1;
+    double const q = pos ? 1.0 : -1.0;
+    int const sp = pos ? 1 : 0;
+    double const rlo = cfg.r_lo, rhi = cfg.r_hi, zlo = cfg.z_lo, zhi = cfg.z_hi;
+    bool const periodic = cfg.periodic_z != 0;
+    double const cut = cfg.low_energy_cutoff_eV;
+    double const photon_cut = cfg.photon_cutoff_eV;
+    double const thr = c.ts.index().hard_moller_threshold_eV;
+    bool const hm_enabled = cfg.debug_disable_hard_moller == 0;
+    double const rho = positive_or(cfg.density_ratio, 1.0);
+    double const w_air = c.ts.index().w_air_eV_per_pair;
+    uint64_t const seed = cfg.rng_seed, key = p.root_key;
+    uint64_t const step_key = static_cast<uint64_t>(std::max(c.step, 0));
+    double const w = p.w;
+    double const birth_r = std::hypot(p.x, p.y), birth_z = p.z;
+    double const residual = newborn_residual(p.birth);
+    double k = p.energy;
+    int current_process = 0;
+    if (!cartesian_half_open(p.x, p.y, p.z, rlo, rhi, zlo, zhi)) {
+        fail(RREA_GPU_ERR_GEOMETRY, "charged transient born outside the half-open domain");
+    }
+    double dx = p.dx, dy = p.dy, dz = p.dz;
+    normalize(dx, dy, dz);
+    auto add_child = [&](int species, double x, double y, double z, double sx, double sy, double sz, double e,
+                         double birth) {
+        Secondary ch{};
+        ch.species = species;
+        ch.process = current_process;
+        ch.x = x; ch.y = y; ch.z = z;
+        ch.dx = sx; ch.dy = sy; ch.dz = sz;
+        ch.w = w;
+        ch.energy = e;
+        ch.birth = birth;
+        fx.children.push_back(ch);
+    };
+    auto push_source = [&](int kind, double r, double z, double ww, double sec, double loss) {
+        fx.sources.push_back(Source{kind, r, z, ww, sec, loss, -1});
+    };
+    auto deposit_local = [&](double r, double z, double ww, double e) {
+        if (ww <= 0.0 || e <= 0.0) return;
+        double const pw = ww * e / std::max(w_air, 1.0);
+        if (pw <= 0.0) return;
+        push_source(0, r, z, pw, 0.0, w_air);
+    };
+    auto push_segment = [&](double r1, double z1) {
+        Segment sg{};
+        sg.kind = 0;
+        sg.a[0] = birth_r; sg.a[1] = birth_z; sg.a[2] = r1; sg.a[3] = z1; sg.a[4] = q * w;
+        sg.channel = 8u;
+        sg.parent_index = -1;
+        fx.segments.push_back(sg);
+    };
+    auto push_escape = [&](Path const& path) {
+        Crossing const cr = boundary_crossing(path);
+        if (!cr.valid) fail(RREA_GPU_ERR_GEOMETRY, "charged escape has no certified absorbing-face crossing");
+        Segment sg{};
+        sg.kind = 1;
+        sg.a[0] = birth_r; sg.a[1] = birth_z; sg.a[2] = cr.sr; sg.a[3] = cr.sz; sg.a[4] = cr.cr; sg.a[5] = cr.cz;
+        sg.a[6] = q * w;
+        sg.channel = 8u | 1u;
+        sg.faces = cr.faces;
+        sg.parent_index = -1;
+        fx.segments.push_back(sg);
+    };
+    auto annihilate = [&](double x, double y, double z, double r, double ke, bool at_rest, uint64_t idx,
+                          double birth) {
+        current_process = 9;
+        spawn_annihilation(
+            tables, photon_cut, x, y, z, r, z, dx, dy, dz, w, ke, at_rest,
+            rng_uniform(seed, key, step_key, idx, kAnnihilationPolar),
+            rng_uniform(seed, key, step_key, idx, kAnnihilationAzimuth), birth,
+            [&](double px, double py, double pz, double gx, double gy, double gz, double e, double b) {
+                add_child(2, px, py, pz, gx, gy, gz, e, b);
+            },
+            deposit_local, [&](double rr, double zz, double ww) { push_source(2, rr, zz, ww, 0.0, 0.0); });
+    };
+    // birth state policy (:99-138): no net chord for a birth demotion
+    bool const demote_at_birth = pos ? k < cut : electron_demotes_at(c, p.x, p.y, p.z, k);
+    if (demote_at_birth) {
+        double const rb = std::hypot(p.x, p.y);
+        if (pos) {
+            annihilate(p.x, p.y, p.z, rb, k, true, pack_newborn(p, 0, 0, 0), p.birth);
+        } else {
+            current_process = 12;
+            push_source(1, rb, p.z, w, 0.0, 0.0);
+            deposit_local(rb, p.z, w, k);
+        }
+        return false;
+    }
+    if (!(residual > 0.0)) return true;
+    double const u = proper_velocity_from_kinetic(k);
+    double const gam = std::sqrt(1.0 + u * u / (kC * kC));
+    double const residual_dt = c.dt_s * residual;
+    double const chord = (u / gam) * residual_dt;
+    if (!(chord > 0.0)) return k >= cut;
+    double const ex = p.x + chord * dx, ey = p.y + chord * dy, ez = p.z + chord * dz;
+    Path const driver = ClipRz(std::hypot(p.x, p.y), std::atan2(p.y, p.x), p.z, std::hypot(ex, ey), std::atan2(ey, ex),
+                               ez, rlo, rhi, zlo, zhi, periodic);
+    if (!(driver.full > 0.0) || !(driver.in_length > 0.0)) {
+        if (driver.exits) {
+            push_escape(driver);
+            return false;
+        }
+        return true;
+    }
+    std::vector<Interval> const driver_iv = build_intervals(driver, rho, rho);
+    if (driver_iv.empty()) fail(RREA_GPU_ERR_INVALID_STATE, "charged transient path has no material intervals");
+    auto require_certified = [&]() {
+        if (!std::isfinite(k) || !(k >= c.ts.index().charged_min_eV && k <= c.ts.index().charged_max_eV)) {
+            fail(RREA_GPU_ERR_RANGE, "newborn charged energy left the certified range");
+        }
+    };
+    double const driver_dpath = density_path(driver_iv, driver, driver.in_begin, driver.in_end);
+    double const gs_total = frozen_rate([&] {
+        double const mfp = tables.ElasticMeanFreePath(sp, k, 1.0);
+        return mfp > 0.0 ? 1.0 / mfp : 0.0;
+    }()) * driver_dpath;
+    double drag_est;
+    if (pos) {
+        drag_est = tables.PositronCollisionLoss(k, 1.0) * driver_dpath;
+    } else {
+        drag_est = (k > 0.0 ? tables.ElectronCollisionLoss(k, 1.0) + tables.ElectronSoftRadiativeDrag(k, 1.0) : 0.0)
+            * driver_dpath;
+    }
+    double const work = path_field_work(c.gather, driver, q, 0.0, 1.0).work;
+    double const impulse = std::max(cfg.max_field_impulse_fraction * k, std::max(cfg.field_impulse_floor_eV, 1.0));
+    double const span = std::max(driver.in_end, 1.0e-6);
+    uint64_t const substeps = std::min<uint64_t>(
+        std::max(driver_count(std::min(gs_total / span, cfg.gs_total_collision_cap),
+                              std::max(cfg.max_gs_collisions_per_substep, 1.0)),
+                 driver_count((std::abs(work) + drag_est) / span, impulse)),
+        cfg.max_subcycles);
+    if (substeps >= kSegmentCap) fail(RREA_GPU_ERR_RNG_OVERFLOW, "newborn substep count outside the RNG budget");
+
+    auto competing = [&](double e) {
+        std::array<double, 3> st{};
+        if (pos) {
+            if (!(thr > 0.0 && e <= thr)) {
+                double const mfp = tables.PositronHardBhabhaMeanFreePath(e, 1.0);
+                st[0] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+            }
+            if (e > photon_cut) {
+                double const mfp = tables.PositronBremsstrahlungMeanFreePath(e, 1.0);
+                st[1] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+            }
+            double const mfp = tables.PositronAnnihilationMeanFreePath(e, 1.0);
+            st[2] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+        } else {
+            if (hm_enabled && thr > 0.0 && e > 2.0 * thr) {
+                double const mfp = tables.ElectronHardMollerMeanFreePath(e, 1.0);
+                st[0] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+            }
+            if (std::isfinite(e) && std::isfinite(photon_cut) && e > photon_cut) {
+                double const mfp = tables.ElectronBremsstrahlungMeanFreePath(e, 1.0);
+                st[1] = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0);
+            }
+        }
+        return st;
+    };
+    auto channel_open = [&](int ch, double e) {
+        if (pos) {
+            double bi, ri, ai;
+            tables.PositronGateRates(e, bi, ri, ai);
+            if (ch == 0) return !(thr > 0.0 && e <= thr) && bi > 0.0;
+            if (ch == 1) return e > photon_cut && ri > 0.0;
+            if (ch == 2) return ai > 0.0;
+            return false;
+        }
+        double mi, bi;
+        tables.ElectronGateRates(e, mi, bi);
+        if (ch == 0) return hm_enabled && (thr > 0.0 && e > 2.0 * thr) && mi > 0.0;
+        if (ch == 1) return (std::isfinite(e) && std::isfinite(photon_cut) && e > photon_cut) && bi > 0.0;
+        return false;
+    };
+
+    double run_x = p.x, run_y = p.y, run_z = p.z;
+    double const sub_dt = residual_dt / static_cast<double>(substeps);
+    double final_fraction = 0.0;
+    bool terminal_interaction = false, terminal_at_point = false, exited = false;
+    uint64_t completed = 0;
+    Path path = driver;
+    std::vector<Interval> iv = driver_iv;
+    FieldRange sub_field;
+    double sub_dt_eff = 0.0;
+    auto elapsed_at = [&](double f) { return newborn_elapsed(p.birth, residual, completed, substeps, f); };
+    // apply_newborn_drag (:260-360): the live drag module; an ion-pair source
+    // that rounds off the half-open domain falls back to the birth position
+    auto continuous = [&](double b, double e, double stop_e) -> Limit {
+        auto dp = [&](double bb, double ee) { return density_path(iv, path, bb, ee); };
+        double sc = 0, ss = 0;
+        bool const need = (e > b) && (k > 0.0) && !(stop_e < cut);
+        if (need) {
+            sc = frozen_rate(pos ? tables.PositronCollisionLoss(stop_e, 1.0) : tables.ElectronCollisionLoss(stop_e, 1.0));
+            ss = frozen_rate(pos ? tables.PositronSoftRadiativeDrag(stop_e, 1.0)
+                                 : tables.ElectronSoftRadiativeDrag(stop_e, 1.0));
+        }
+        DragPlan const plan = plan_drag(b, e, k, stop_e, cut, dp, sc, ss, 0.0);
+        if (!plan.limit_valid) fail(RREA_GPU_ERR_INVALID_STATE, "newborn stopping has no monotone cutoff point");
+        if (!plan.applied) return Limit{b, false, true};
+        if (plan.collision > 0.0 && plan.raw_collision > 0.0) {
+            for (Interval const& i : iv) {
+                double const bb = std::max(b, i.begin), ee = std::min(plan.end, i.end);
+                if (!(ee > bb)) continue;
+                double const raw = path.full * (ee - bb) * i.density * plan.collision_stp;
+                double const loss = plan.collision * raw / plan.raw_collision;
+                double const pw = w * loss / std::max(w_air, 1.0);
+                if (!(pw > 0.0)) continue;
+                double x, y, z;
+                path.PointAtFull(0.5 * (bb + ee), x, y, z);
+                double sr = std::hypot(x, y), sz = path.WrapZ(z);
+                if (!(std::isfinite(sr) && std::isfinite(sz) && sr >= rlo && sr < rhi && sz >= zlo && sz < zhi)) {
+                    sr = std::hypot(p.x, p.y);
+                    sz = p.z;
+                }
+                push_source(0, sr, sz, pw, pos ? 0.0 : 0.5 * cut, w_air);
+            }
+        }
+        k = std::max(0.0, k - plan.drag);
+        if (plan.reaches) k = cut;
+        return Limit{plan.end, plan.reaches, true};
+    };
+    auto build_chord = [&](Path& out) -> bool {
+        // RreaBuildRunningChargedChord with the residual dt as the step bound
+        if (!std::isfinite(sub_dt) || !std::isfinite(residual_dt) || !(sub_dt >= 0.0) || !(residual_dt > 0.0)) {
+            return false;
+        }
+        double const speed = charged_speed(k);
+        double const dn = std::sqrt(dx * dx + dy * dy + dz * dz);
+        if (!std::isfinite(speed) || !std::isfinite(dn) || !(dn > 0.0)) return false;
+        double const sc = speed * sub_dt / dn;
+        double const exx = run_x + sc * dx, eyy = run_y + sc * dy, ezz = run_z + sc * dz;
+        out = ClipRz(std::hypot(run_x, run_y), std::atan2(run_y, run_x), run_z, std::hypot(exx, eyy),
+                     std::atan2(eyy, exx), ezz, rlo, rhi, zlo, zhi, periodic);
+        return std::isfinite(out.full) && out.in_begin == 0.0;
+    };
+
+    for (uint64_t sub = 0; sub < substeps; ++sub) {
+        if (k < cut) break;
+        double sb = 0.0, se = 0.0;
+        {
+            Path np;
+            if (!build_chord(np)) break;
+            path = np;
+            if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
+                exited = path.exits;
+                final_fraction = 0.0;
+                break;
+            }
+            iv = build_intervals(path, rho, rho);
+            if (iv.empty()) fail(RREA_GPU_ERR_INVALID_STATE, "transient microchord has no material intervals");
+            sb = path.in_begin;
+            se = path.in_end;
+            final_fraction = se;
+            sub_field = path_field_work(c.gather, path, q, sb, se);
+            sub_dt_eff = sub_dt * (se - sb);
+            half_kick(sub_field, 0.5 * sub_dt_eff, q, k, dx, dy, dz);
+            if (k < cut) {
+                final_fraction = sb;
+                terminal_at_point = true;
+                break;
+            }
+            require_certified();
+        }
+        {
+            double rem = sb;
+            uint64_t ordinal = 0;
+            while (rem < se && k >= cut) {
+                if (ordinal >= kEventCap) fail(RREA_GPU_ERR_RNG_OVERFLOW, "newborn event ordinal overflow");
+                double const frozen = k;
+                std::array<double, 3> const st = competing(frozen);
+                double const total_stp = st[0] + st[1] + st[2];
+                double const seg_dp = density_path(iv, path, rem, se);
+                std::array<double, 3> const taus = {st[0] * seg_dp, st[1] * seg_dp, st[2] * seg_dp};
+                uint64_t const idx = pack_newborn(p, sub, ordinal, 0);
+                double const u1 = rng_uniform(seed, key, step_key, idx, kNewbornCompetingOpticalDepth);
+                double const u2 = rng_uniform(seed, key, step_key, idx, kNewbornCompetingChannel);
+                Selection const sel = select_hazard(taus, pos ? 3 : 2, u1, u2);
+                double ev = 0.0;
+                bool split_valid = false;
+                if (sel.valid && sel.event) {
+                    ev = fraction_at_density_path(iv, path, rem, se, sel.sampled / total_stp);
+                    split_valid = std::isfinite(rem) && std::isfinite(ev) && std::isfinite(se) && (se > rem)
+                        && !(ev < rem) && !(ev > se);
+                }
+                if (!sel.valid) fail(RREA_GPU_ERR_INVALID_STATE, "newborn competing-hazard selection invalid");
+                if (!sel.event) {
+                    Limit const l = continuous(rem, se, frozen);
+                    if (l.reaches) {
+                        final_fraction = l.end;
+                        terminal_at_point = true;
+                    }
+                    break;
+                }
+                if (!split_valid) fail(RREA_GPU_ERR_INVALID_STATE, "newborn event depth outside its substep");
+                double ex2, ey2, ez2;
+                path.PointAtFull(ev, ex2, ey2, ez2);
+                double const er2 = std::hypot(ex2, ey2);
+                ez2 = path.WrapZ(ez2);
+                double const ev_elapsed = elapsed_at(ev);
+                Limit const l = continuous(rem, ev, frozen);
+                if (l.reaches) {
+                    final_fraction = l.end;
+                    terminal_at_point = true;
+                    break;
+                }
+                bool const open_ev = k >= cut && channel_open(sel.channel, k);
+                if (!open_ev) {
+                    bool const open_fr = frozen >= cut && channel_open(sel.channel, frozen);
+                    if (!open_fr) fail(RREA_GPU_ERR_INVALID_STATE, "selected channel closed before its event depth");
+                    rem = ev;
+                    ++ordinal;
+                    continue;
+                }
+                auto R = [&](uint64_t ch) { return rng_uniform(seed, key, step_key, idx, ch); };
+                if (sel.channel == 0 && !pos) {
+                    double const kb = k;
+                    double sec = tables.SampleMollerSecondaryEnergy(kb, R(kHardMollerEnergy));
+                    sec = std::max(thr, std::min(sec, 0.5 * kb));
+                    double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
+                    moller_lab_directions(dx, dy, dz, kb, sec, R(kHardMollerAzimuth), pdx, pdy, pdz, sdx, sdy, sdz);
+                    k = std::max(0.0, kb - sec);
+                    dx = pdx; dy = pdy; dz = pdz;
+                    current_process = 2;
+                    add_child(0, ex2, ey2, ez2, sdx, sdy, sdz, sec, ev_elapsed);
+                    push_source(0, er2, ez2, w, sec, sec);
+                } else if (sel.channel == 0) {
+                    double const kb = k;
+                    double const sec =
+                        std::min(tables.SamplePositronBhabhaSecondaryEnergy(kb, R(kPositronBhabhaEnergy)),
+                                 std::max(0.0, kb));
+                    if (sec > 0.0 && !(thr > 0.0 && sec < thr)) {
+                        double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
+                        moller_lab_directions(dx, dy, dz, kb, sec, R(kPositronBhabhaAzimuth), pdx, pdy, pdz, sdx,
+                                              sdy, sdz);
+                        k = std::max(0.0, kb - sec);
+                        dx = pdx; dy = pdy; dz = pdz;
+                        current_process = 3;
+                        add_child(0, ex2, ey2, ez2, sdx, sdy, sdz, sec, ev_elapsed);
+                        push_source(2, er2, ez2, w, 0.0, sec);
+                    }
+                } else if (sel.channel == 1) {
+                    double const kb = k;
+                    double const sampled = pos
+                        ? tables.SamplePositronBremsstrahlungPhotonEnergy(kb, R(kPositronBremsEnergy))
+                        : tables.SampleBremsstrahlungPhotonEnergy(kb, R(kBremsEnergy));
+                    double const eg = std::min(std::max(sampled, 0.0), std::max(kb, 0.0));
+                    double const after = std::max(0.0, std::max(kb, 0.0) - eg);
+                    bool const tracked = std::isfinite(photon_cut) && photon_cut >= 0.0 && eg >= photon_cut;
+                    double gx = dx, gy = dy, gz = dz;
+                    double const ct = tables.SampleBremsstrahlungCosTheta(kb, R(pos ? kPositronBremsAngle : kBremsAngle));
+                    cone_direction(dx, dy, dz, ct, R(pos ? kPositronBremsAzimuth : kBremsAzimuth), gx, gy, gz);
+                    photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
+                    k = after;
+                    current_process = 4;
+                    if (tracked) add_child(2, ex2, ey2, ez2, gx, gy, gz, eg, ev_elapsed);
+                    else if (eg > 0.0) deposit_local(er2, ez2, w, eg);
+                } else {
+                    annihilate(ex2, ey2, ez2, er2, k, false, idx, ev_elapsed);
+                    push_segment(er2, ez2);
+                    terminal_interaction = true;
+                    final_fraction = ev;
+                    break;
+                }
+                if (k <= cut) {
+                    final_fraction = ev;
+                    terminal_at_point = true;
+                    break;
+                }
+                rem = ev;
+                ++ordinal;
+            }
+        }
+        if (terminal_interaction || terminal_at_point) break;
+        {
+            if (k >= cut) {
+                double const mfp = tables.ElasticMeanFreePath(sp, k, 1.0);
+                double const gs_n = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0) * density_path(iv, path, sb, se);
+                if (gs_n > 0.0) {
+                    auto gkey = [&](uint64_t ch, uint64_t inner) {
+                        return rng_uniform(seed, key, step_key, pack_newborn(p, sub, 0, inner), ch);
+                    };
+                    auto deflect = [&](double ct, double uphi) {
+                        double nx, ny, nz;
+                        cone_direction(dx, dy, dz, ct, uphi, nx, ny, nz);
+                        dx = nx; dy = ny; dz = nz;
+                    };
+                    double const few = c.ts.index().gs_few_collision_threshold;
+                    if (gs_n < few) {
+                        int const cap = static_cast<int>(std::ceil(3.0 * few));
+                        if (cap >= 255) fail(RREA_GPU_ERR_INVALID_STATE, "GS few-collision cap too large");
+                        int const cnt =
+                            poisson_capped(gs_n, gkey(pos ? kNewbornPositronGsFewCount : kNewbornElectronGsFewCount, 0),
+                                           cap);
+                        for (int qq = 0; qq < cnt; ++qq) {
+                            uint64_t const inner = static_cast<uint64_t>(qq + 1);
+                            double const ct = tables.SampleSingleElasticCosTheta(
+                                sp, k, gkey(pos ? kNewbornPositronGsFewScatter : kNewbornElectronGsFewScatter, inner));
+                            deflect(ct, gkey(pos ? kNewbornPositronGsFewAzimuth : kNewbornElectronGsFewAzimuth, inner));
+                        }
+                    } else {
+                        double const ct = tables.SampleGsCosTheta(
+                            sp, k, gs_n, gkey(pos ? kNewbornPositronGsAngle : kNewbornElectronGsAngle, 0));
+                        deflect(ct, gkey(pos ? kNewbornPositronGsAzimuth : kNewbornElectronGsAzimuth, 0));
+                    }
+                }
+            }
+            half_kick(sub_field, 0.5 * sub_dt_eff, q, k, dx, dy, dz);
+            if (k < cut) {
+                final_fraction = se;
+                terminal_at_point = true;
+                break;
+            }
+            require_certified();
+        }
+        if (!advance_running(path, se, rlo, rhi, zlo, zhi, run_x, run_y, run_z)) {
+            exited = true;
+            break;
+        }
+        if (path.exits) {
+            exited = true;
+            break;
+        }
+        completed = sub + 1U;
+    }
+    if (terminal_interaction) return false;
+    double fx_, fy_, fz_;
+    if (!newborn_final_point(path, final_fraction, cfg, fx_, fy_, fz_)) {
+        fail(RREA_GPU_ERR_GEOMETRY, "newborn charged transport could not place its final point");
+    }
+    double const final_r = std::hypot(fx_, fy_);
+    double const final_elapsed = elapsed_at(final_fraction);
+    bool const demote = pos ? k < cut : electron_demotes_at(c, fx_, fy_, fz_, k);
+    if (terminal_at_point || demote) {
+        if (pos) {
+            annihilate(fx_, fy_, fz_, final_r, k, true, pack_newborn(p, std::min<uint64_t>(substeps, kSegmentCap - 1), 0, 0),
+                       final_elapsed);
+        } else {
+            current_process = 12;
+            push_source(1, final_r, fz_, w, 0.0, 0.0);
+            deposit_local(final_r, fz_, w, k);
+        }
+        push_segment(final_r, fz_);
+        return false;
+    }
+    if (exited) {
+        push_escape(path);
+        return false;
+    }
+    p.x = fx_; p.y = fy_; p.z = fz_;
+    p.dx = dx; p.dy = dy; p.dz = dz;
+    p.energy = k;
+    p.birth = 1.0;
+    push_segment(final_r, fz_);
+    return true;
+}
+
+// TransportStep::AdvancePhotonNewborn (O/RreaNewbornAdvance.cpp:779-996)
+bool advance_photon_newborn(NewbornContext const& c, Secondary& p, NewbornEffects& fx)
+{
+    Tables const& tables = c.tables;
+    rrea_gpu_config const& cfg = c.cfg;
+    double const rlo = cfg.r_lo, rhi = cfg.r_hi, zlo = cfg.z_lo, zhi = cfg.z_hi;
+    bool const periodic = cfg.periodic_z != 0;
+    double const cut = cfg.low_energy_cutoff_eV;
+    double const photon_cut = cfg.photon_cutoff_eV;
+    double const rho = positive_or(cfg.density_ratio, 1.0);
+    double const w_air = c.ts.index().w_air_eV_per_pair;
+    uint64_t const seed = cfg.rng_seed, key = p.root_key;
+    uint64_t const step_key = static_cast<uint64_t>(std::max(c.step, 0));
+    double const w = p.w;
+    int current_process = 0;
+    double const residual = newborn_residual(p.birth);
+    if (!(residual > 0.0)) return p.energy >= photon_cut;
+    if (!cartesian_half_open(p.x, p.y, p.z, rlo, rhi, zlo, zhi)) {
+        fail(RREA_GPU_ERR_GEOMETRY, "photon transient born outside the half-open domain");
+    }
+    double dx = p.dx, dy = p.dy, dz = p.dz;
+    normalize(dx, dy, dz);
+    double energy = p.energy;
+    auto add_child = [&](int species, double x, double y, double z, double sx, double sy, double sz, double e,
+                         double birth) {
+        Secondary ch{};
+        ch.species = species;
+        ch.process = current_process;
+        ch.x = x; ch.y = y; ch.z = z;
+        ch.dx = sx; ch.dy = sy; ch.dz = sz;
+        ch.w = w;
+        ch.energy = e;
+        ch.birth = birth;
+        fx.children.push_back(ch);
+    };
+    auto push_source = [&](int kind, double r, double z, double ww, double sec, double loss) {
+        fx.sources.push_back(Source{kind, r, z, ww, sec, loss, -1});
+    };
+    auto deposit_local = [&](double r, double z, double ww, double e) {
+        if (ww <= 0.0 || e <= 0.0) return;
+        double const pw = ww * e / std::max(w_air, 1.0);
+        if (pw <= 0.0) return;
+        push_source(0, r, z, pw, 0.0, w_air);
+    };
+    if (energy < photon_cut) {
+        current_process = 12;
+        deposit_local(std::hypot(p.x, p.y), p.z, w, energy);
+        return false;
+    }
+    double const chord = kC * c.dt_s * residual;
+    double const ex = p.x + chord * dx, ey = p.y + chord * dy, ez = p.z + chord * dz;
+    Path path = ClipRz(std::hypot(p.x, p.y), std::atan2(p.y, p.x), p.z, std::hypot(ex, ey), std::atan2(ey, ex), ez, rlo,
+                       rhi, zlo, zhi, periodic);
+    if (!(path.full > 0.0) || !(path.in_length > 0.0)) return !path.exits;
+    double elapsed_start = p.birth;
+    uint64_t ordinal = 0;
+    for (;;) {
+        uint64_t const idx = pack_newborn(p, 0, ordinal, 0);
+        std::vector<Interval> const iv = build_intervals(path, rho, rho);
+        PhotonRates const rates = photon_rates(tables, energy, 1.0);
+        double const mfp = Tables::mfp_from_inverse(rates.total());
+        double const tau = density_path(iv, path, path.in_begin, path.in_end) / mfp;
+        auto R = [&](uint64_t ch) { return rng_uniform(seed, key, step_key, idx, ch); };
+        Selection const sel = select_hazard({tau, 0.0, 0.0}, 1, R(kNewbornCompetingOpticalDepth), 0.0);
+        if (!sel.valid) fail(RREA_GPU_ERR_INVALID_STATE, "newborn photon hazard selection invalid");
+        if (!sel.event) {
+            double fx_, fy_, fz_;
+            if (!newborn_final_point(path, path.in_end, cfg, fx_, fy_, fz_)) {
+                fail(RREA_GPU_ERR_GEOMETRY, "newborn photon could not place its final point");
+            }
+            if (path.exits) return false;
+            p.x = fx_; p.y = fy_; p.z = fz_;
+            p.dx = dx; p.dy = dy; p.dz = dz;
+            p.energy = energy;
+            p.birth = 1.0;
+            return true;
+        }
+        double const f = fraction_at_density_path(iv, path, path.in_begin, path.in_end, sel.sampled * mfp);
+        if (!(std::isfinite(f) && f >= path.in_begin && f <= path.in_end && path.in_end > path.in_begin)) {
+            fail(RREA_GPU_ERR_INVALID_STATE, "newborn photon event depth outside its chord");
+        }
+        double const dist = path.full * (f - path.in_begin);
+        double const remaining = std::max(0.0, path.full - dist);
+        double px, py, pz;
+        path.PointAtFull(f, px, py, pz);
+        double const pr = std::hypot(px, py);
+        pz = path.WrapZ(pz);
+        double const birth =
+            std::min(1.0, elapsed_start + dist / std::max(kC * c.dt_s, std::numeric_limits<double>::min()));
+        int const channel = sample_photon_channel(tables, energy, R(kNewbornCompetingChannel));
+        if (channel == 0) {
+            current_process = 5;
+            double const inc = energy;
+            ComptonState const cs = sample_klein_nishina(tables, inc, R(53), R(54));
+            double sx, sy, sz;
+            cone_direction(dx, dy, dz, cs.cos_theta, R(58), sx, sy, sz);
+            double rx = inc * dx - cs.scattered * sx, ry = inc * dy - cs.scattered * sy, rz = inc * dz - cs.scattered * sz;
+            normalize(rx, ry, rz);
+            if (cs.recoil >= cut) {
+                add_child(0, px, py, pz, rx, ry, rz, cs.recoil, birth);
+                push_source(0, pr, pz, w, cs.recoil, cs.recoil);
+            } else {
+                push_source(0, pr, pz, w, cs.recoil, 0.0);
+                deposit_local(pr, pz, w, cs.recoil);
+            }
+            energy = cs.scattered;
+            if (energy < photon_cut) {
+                deposit_local(pr, pz, w, energy);
+                return false;
+            }
+            dx = sx; dy = sy; dz = sz;
+            if (!(remaining > 0.0)) {
+                p.x = px; p.y = py; p.z = pz;
+                p.dx = dx; p.dy = dy; p.dz = dz;
+                p.energy = energy;
+                p.birth = 1.0;
+                return true;
+            }
+            double const tx = px + remaining * dx, ty = py + remaining * dy, tz = pz + remaining * dz;
+            path = ClipRz(pr, std::atan2(py, px), pz, std::hypot(tx, ty), std::atan2(ty, tx), tz, rlo, rhi, zlo, zhi,
+                          periodic);
+            elapsed_start = birth;
+            ++ordinal;
+            continue;
+        }
+        if (channel == 1) {
+            current_process = 6;
+            double pe_e, bind;
+            sample_photoelectric(tables, energy, R(55), pe_e, bind);
+            double const ee = std::min(pe_e, energy);
+            if (ee >= cut) {
+                double sx, sy, sz;
+                cone_direction(dx, dy, dz, sample_photoelectron_cos(tables, ee, R(60)), R(65), sx, sy, sz);
+                add_child(0, px, py, pz, sx, sy, sz, ee, birth);
+                push_source(0, pr, pz, w, ee, ee);
+            } else {
+                push_source(0, pr, pz, w, ee, 0.0);
+                deposit_local(pr, pz, w, ee);
+            }
+            if (bind > 0.0) deposit_local(pr, pz, w, bind);
+            return false;
+        }
+        bool const triplet = channel == 3;
+        current_process = triplet ? 8 : 7;
+        PairState const ps = sample_pair(tables, energy, channel, R(66), R(57), R(59));
+        if (!ps.valid) fail(RREA_GPU_ERR_INVALID_STATE, "pair channel without phase space");
+        double edx, edy, edz, pdx, pdy, pdz;
+        rotate_to_axis(dx, dy, dz, ps.edir[0], ps.edir[1], ps.edir[2], edx, edy, edz);
+        rotate_to_axis(dx, dy, dz, ps.pdir[0], ps.pdir[1], ps.pdir[2], pdx, pdy, pdz);
+        if (ps.e_electron >= cut) {
+            add_child(0, px, py, pz, edx, edy, edz, ps.e_electron, birth);
+        } else {
+            push_source(1, pr, pz, w, 0.0, 0.0);
+            deposit_local(pr, pz, w, ps.e_electron);
+        }
+        if (ps.e_positron >= cut) {
+            add_child(1, px, py, pz, pdx, pdy, pdz, ps.e_positron, birth);
+        } else {
+            spawn_annihilation(
+                tables, photon_cut, px, py, pz, pr, pz, pdx, pdy, pdz, w, ps.e_positron, true, R(80), R(81), birth,
+                [&](double qx, double qy, double qz, double gx, double gy, double gz, double e, double b) {
+                    add_child(2, qx, qy, qz, gx, gy, gz, e, b);
+                },
+                deposit_local, [&](double rr, double zz, double ww) { push_source(2, rr, zz, ww, 0.0, 0.0); });
+        }
+        if (ps.recoil) {
+            double rdx, rdy, rdz;
+            rotate_to_axis(dx, dy, dz, ps.rdir[0], ps.rdir[1], ps.rdir[2], rdx, rdy, rdz);
+            if (ps.e_recoil >= cut) add_child(0, px, py, pz, rdx, rdy, rdz, ps.e_recoil, birth);
+            push_source(0, pr, pz, w, ps.e_recoil, 0.0);
+            if (ps.e_recoil < cut) deposit_local(pr, pz, w, ps.e_recoil);
+        }
+        if (ps.local > 0.0) deposit_local(pr, pz, w, ps.local);
+        return false;
+    }
+}
+
+}  // namespace
+
+void DrainSecondaries(TableSet const& ts, rrea_gpu_config const& cfg, FieldGrid const& field, int step, double dt_s,
+                      std::vector<Secondary> const& initial, std::vector<Secondary>& survivors, StepOutputs& out)
+{
+    Tables const tables(ts);
+    Gather const gather{field, cfg};
+    NewbornContext const c{tables, ts, cfg, gather, step, dt_s};
+    // birth payloads entering the FIFO (O/RreaSecondaryCommit.cpp:337-373)
+    for (Secondary const& s : initial) {
+        bool const known = s.species >= 0 && s.species <= 2 && s.root_species >= 0 && s.root_species <= 2;
+        bool const finite = std::isfinite(s.x) && std::isfinite(s.y) && std::isfinite(s.z) && std::isfinite(s.dx)
+            && std::isfinite(s.dy) && std::isfinite(s.dz) && std::isfinite(s.w) && std::isfinite(s.energy)
+            && std::isfinite(s.birth);
+        bool const energy_ok = s.species == 2 ? s.energy > 0.0 : s.energy >= 0.0;
+        if (!known || !finite || !(s.w > 0.0) || !energy_ok || s.birth < 0.0 || s.birth > 1.0
+            || s.lineage >= kLineageCap) {
+            fail(RREA_GPU_ERR_ARGUMENT, "transient FIFO received an invalid birth payload");
+        }
+    }
+    std::vector<Secondary> work(initial.begin(), initial.end());
+    std::map<std::pair<uint64_t, int>, uint64_t> next_lineage;
+    for (Secondary const& s : work) {
+        uint64_t& nx = next_lineage[{s.root_key, s.root_species}];
+        nx = std::max(nx, s.lineage + 1U);
+    }
+    survivors.clear();
+    constexpr std::size_t kBatch = 1024;
+    for (std::size_t cursor = 0; cursor < work.size();) {
+        std::size_t const count = std::min(kBatch, work.size() - cursor);
+        std::vector<NewbornEffects> fx(count);
+        std::vector<char> alive(count, 1);
+        std::vector<int> err(count, 0);
+        std::vector<std::string> msg(count);
+#pragma omp parallel for schedule(dynamic, 1) if (count > 1)
+        for (long o = 0; o < static_cast<long>(count); ++o) {
+            std::size_t const i = static_cast<std::size_t>(o);
+            try {
+                Secondary& s = work[cursor + i];
+                double const e = s.energy;
+                bool const certified = s.species == 2
+                    ? (std::isfinite(e) && e >= ts.index().photon_min_eV && e <= ts.index().photon_max_eV)
+                    : (std::isfinite(e) && e >= ts.index().charged_min_eV && e <= ts.index().charged_max_eV);
+                if (!certified) fail(RREA_GPU_ERR_RANGE, "transient FIFO particle outside its certified energy range");
+                if (s.birth < 1.0) {
+                    alive[i] = s.species == 2 ? advance_photon_newborn(c, s, fx[i]) : advance_charged_newborn(c, s, fx[i]);
+                }
+            } catch (OracleError const& e) {
+                err[i] = e.code;
+                msg[i] = e.what();
+            }
+        }
+        for (std::size_t i = 0; i < count; ++i) {
+            if (err[i] != 0) fail(err[i], msg[i]);
+        }
+        for (std::size_t i = 0; i < count; ++i) {
+            Secondary const parent = work[cursor + i];
+            for (Secondary ch : fx[i].children) {
+                ch.root_key = parent.root_key;
+                ch.root_species = parent.root_species;
+                ch.parent_index = parent.parent_index;
+                uint64_t& nx = next_lineage[{ch.root_key, ch.root_species}];
+                if (nx >= kLineageCap) fail(RREA_GPU_ERR_RNG_OVERFLOW, "transient FIFO lineage overflow");
+                ch.lineage = nx++;
+                work.push_back(ch);
+            }
+            out.sources.insert(out.sources.end(), fx[i].sources.begin(), fx[i].sources.end());
+            out.segments.insert(out.segments.end(), fx[i].segments.begin(), fx[i].segments.end());
+            if (alive[i]) {
+                Secondary s = work[cursor + i];
+                s.birth = 1.0;
+                survivors.push_back(s);
+            }
+        }
+        cursor += count;
+    }
+    // final survivors at their transported endpoint (O/RreaSecondaryCommit.cpp:480-515)
+    for (Secondary const& s : survivors) {
+        bool const finite = std::isfinite(s.x) && std::isfinite(s.y) && std::isfinite(s.z) && std::isfinite(s.dx)
+            && std::isfinite(s.dy) && std::isfinite(s.dz) && std::isfinite(s.w) && std::isfinite(s.energy);
+        bool const photon = s.species == 2;
+        bool const energy_ok = photon ? s.energy > 0.0 : s.energy >= cfg.low_energy_cutoff_eV;
+        bool const certified = photon
+            ? (s.energy >= ts.index().photon_min_eV && s.energy <= ts.index().photon_max_eV)
+            : (s.energy >= ts.index().charged_min_eV && s.energy <= ts.index().charged_max_eV);
+        if (!finite || !(s.w > 0.0) || !energy_ok || !certified
+            || !cartesian_half_open(s.x, s.y, s.z, cfg.r_lo, cfg.r_hi, cfg.z_lo, cfg.z_hi)) {
+            fail(RREA_GPU_ERR_INVALID_STATE, "transient work graph contains invalid final survivors");
+        }
     }
 }
 

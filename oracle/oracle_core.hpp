@@ -74,6 +74,11 @@ enum Channel : uint64_t {
     kPositronCompetingOpticalDepth = 109, kPositronCompetingChannel = 110,
     kPositronContinuationOpticalDepth = 126, kPositronContinuationChannel = 127,
     kPositronBhabhaAzimuth = 130,
+    kNewbornElectronGsAngle = 112, kNewbornElectronGsAzimuth = 113, kNewbornElectronGsFewCount = 114,
+    kNewbornElectronGsFewScatter = 115, kNewbornElectronGsFewAzimuth = 116,
+    kNewbornPositronGsAngle = 117, kNewbornPositronGsAzimuth = 118, kNewbornPositronGsFewCount = 119,
+    kNewbornPositronGsFewScatter = 120, kNewbornPositronGsFewAzimuth = 121,
+    kNewbornCompetingOpticalDepth = 122, kNewbornCompetingChannel = 123,
 };
 
 // O/RreaParticleInteraction.H:642-710
@@ -189,6 +194,17 @@ void ApplyElectronTransport(rrea_host::TableSet const& tables, rrea_gpu_config c
 void ApplyPositronTransport(rrea_host::TableSet const& tables, rrea_gpu_config const& cfg,
                             FieldGrid const& field, int step, double dt_s, ChargedTile& tile,
                             StepOutputs& out);
+
+// DrainAndCommitSecondaries (O/RreaSecondaryCommit.cpp:9-638): the step's
+// secondaries (`initial`, in the phases' group order: electron, photon,
+// positron) are advanced FIFO through the rest of the step by
+// AdvanceChargedNewborn / AdvancePhotonNewborn (O/RreaNewbornAdvance.cpp);
+// children join the FIFO with lineages allocated per root.  `survivors` gets
+// the final survivors in FIFO order (birth fraction 1); `out` gets the
+// newborns' sources and charged segments.
+void DrainSecondaries(rrea_host::TableSet const& tables, rrea_gpu_config const& cfg, FieldGrid const& field,
+                      int step, double dt_s, std::vector<Secondary> const& initial, std::vector<Secondary>& survivors,
+                      StepOutputs& out);
 
 // Photon phase of one step (O/RreaPhotonTransport.cpp:9-461) over one tile:
 // prev_* is the captured start, (r, theta, z) the straight-push endpoint.

@@ -117,6 +117,7 @@ enum : uint64_t {
 
 // O/RreaParticleInteraction.H:642-710
 constexpr uint64_t kSegmentCap = uint64_t{1} << 14;
+constexpr uint64_t kLineageCap = uint64_t{1} << 14;  // kRreaTransientLineageCapacity
 constexpr uint64_t kEventCap = uint64_t{1} << 13;
 __device__ __forceinline__ bool live_hazard_index(uint64_t species, uint64_t segment, uint64_t ordinal,
                                                   uint64_t& out)

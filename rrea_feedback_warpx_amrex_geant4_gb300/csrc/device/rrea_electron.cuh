@@ -16,9 +16,9 @@
 
 namespace rrea_dev {
 
-// Per-step constants of the electron phase.  Defined in this header, which
-// only the electron kernel's translation unit (rrea_kernels.cu) includes.
-__constant__ StepConstants c_step;
+// Per-step constants of the charged phases.  Internal to each translation
+// unit that includes this header (each sets its own copy before launching).
+static __constant__ StepConstants c_step;
 
 
 
@@ -348,7 +348,7 @@ __device__ __forceinline__ double annihilation_fraction(double gamma, double dra
 // a below-cutoff positron first thermalizes its kinetic energy as ion pairs.
 // Returns the parent's lineage count after the appended photons.  Taken out
 // of line with every argument by value (it runs at most once per positron).
-__device__ __noinline__ uint32_t spawn_annihilation(ElectronArgs A, RngStream rng, uint64_t idx, int64_t ip,
+static __device__ __noinline__ uint32_t spawn_annihilation(ElectronArgs A, RngStream rng, uint64_t idx, int64_t ip,
                                                     uint64_t key, double weight, uint32_t lineage, double x, double y,
                                                     double z, double r, double ax, double ay, double az, double k,
                                                     bool at_rest, double birth)
@@ -423,7 +423,7 @@ __device__ __noinline__ uint32_t spawn_annihilation(ElectronArgs A, RngStream rn
 // a Poisson number of single screened-Rutherford deflections.  Rare for
 // tracked electrons (n >= 10 elastic collisions per substep at MeV energies),
 // so it is kept out of line.
-__device__ __noinline__ Dir3 gs_few_collisions(const double* __restrict__ arena, RngStream rng, uint64_t sub,
+static __device__ __noinline__ Dir3 gs_few_collisions(const double* __restrict__ arena, RngStream rng, uint64_t sub,
                                                double gs_n, double k, double lk, double dx, double dy, double dz,
                                                int species)
 {

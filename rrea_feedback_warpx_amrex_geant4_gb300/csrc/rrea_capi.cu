@@ -1,8 +1,9 @@
 // C-ABI of the GB300 kinetic step (include/rrea_gpu.h).  Host C++ around the
-// kernels in rrea_kernels.cu and rrea_photon_kernels.cu: owns the device
-// arena, field vectors, one resident tile per species and every per-step
-// buffer.  All device memory is
-// allocated at create/load time; a step allocates nothing.
+// kernels in rrea_kernels.cu, rrea_photon_kernels.cu and rrea_newborn.cu:
+// owns the device arena, field vectors, one resident tile per species and
+// every per-step buffer.  The buffers of a species phase are allocated at
+// create/load time, so a phase allocates nothing; only the secondary FIFO
+// of the drain grows on demand.
 #include "../../include/rrea_gpu.h"
 
 #include "device/rrea_electron_args.cuh"
@@ -11,11 +12,14 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
+#include <vector>
 
 namespace {
 
@@ -29,6 +33,20 @@ struct SpeciesTile {
     int64_t* id = nullptr;
     int32_t* cpu = nullptr;
     int64_t n = 0;
+};
+
+// A transient root: the RNG key and species of the live particle whose
+// streams a FIFO item draws from.
+struct RootKey {
+    uint64_t key;
+    int32_t species;
+    bool operator==(RootKey const& o) const { return key == o.key && species == o.species; }
+};
+struct RootHash {
+    size_t operator()(RootKey const& r) const
+    {
+        return static_cast<size_t>(r.key * 0x9e3779b97f4a7c15ULL) ^ static_cast<size_t>(r.species);
+    }
 };
 
 }  // namespace
@@ -78,6 +96,19 @@ struct rrea_gpu_ctx {
     int* d_status = nullptr;
     long long* d_fail_index = nullptr;
     unsigned long long* d_transported = nullptr;
+    // transient FIFO of DrainAndCommitSecondaries: the resident phases queue
+    // their ordered secondaries in d_fifo[0, fifo_pending); a drain advances
+    // the FIFO chunk by chunk and leaves the survivors in d_surv[0, n_surv)
+    rrea_gpu_secondary* d_fifo = nullptr;
+    int64_t fifo_cap = 0;
+    int64_t fifo_pending = 0;
+    rrea_gpu_secondary* d_surv = nullptr;
+    int64_t surv_cap = 0;
+    int64_t n_surv = 0;
+    uint32_t* d_alive = nullptr;
+    uint64_t* d_child_lineage = nullptr;
+    unsigned long long* d_invalid = nullptr;
+    int64_t last_drain_items = 0;
     cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev_stop = nullptr;
     float last_kernel_ms = 0.0f;
@@ -247,6 +278,8 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         && dalloc(&ctx->d_diag_sub, n) == cudaSuccess && dalloc(&ctx->d_diag_ev, n) == cudaSuccess
         && dalloc(&ctx->d_diag_disp, n) == cudaSuccess && dalloc(&ctx->d_status, 1) == cudaSuccess
         && dalloc(&ctx->d_fail_index, 1) == cudaSuccess && dalloc(&ctx->d_transported, 1) == cudaSuccess
+        && dalloc(&ctx->d_alive, n) == cudaSuccess && dalloc(&ctx->d_child_lineage, nsec) == cudaSuccess
+        && dalloc(&ctx->d_invalid, 1) == cudaSuccess
         && cudaEventCreate(&ctx->ev_start) == cudaSuccess && cudaEventCreate(&ctx->ev_stop) == cudaSuccess;
     if (!ok) return bail(RREA_GPU_ERR_CUDA);
     if (cudaMemsetAsync(ctx->d_cells, 0, 5 * ncell * sizeof(double), ctx->stream) != cudaSuccess) {
@@ -293,6 +326,11 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     dfree(ctx->d_status);
     dfree(ctx->d_fail_index);
     dfree(ctx->d_transported);
+    dfree(ctx->d_fifo);
+    dfree(ctx->d_surv);
+    dfree(ctx->d_alive);
+    dfree(ctx->d_child_lineage);
+    dfree(ctx->d_invalid);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -398,16 +436,9 @@ rrea_gpu_status stage_tile(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile const* 
     return RREA_GPU_OK;
 }
 
-// Launches one species phase (RREA_SPECIES_ELECTRON or RREA_SPECIES_PHOTON)
-// on the staged device tile.  `aliased` runs the resident engine mode: the
-// captured pre-push state is the current state (for photons the kernel then
-// performs the straight push itself).
-rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, double dt_s, bool aliased)
+// Per-step constants of every transport kernel.
+rrea_dev::StepConstants step_constants(rrea_gpu_ctx const* ctx, int32_t step, double dt_s)
 {
-    if (!ctx->tables_loaded || !ctx->field_set) {
-        return fail(ctx, RREA_GPU_ERR_NOT_READY, "tables and field must be set before a step");
-    }
-    if (!(dt_s > 0.0) || !std::isfinite(dt_s)) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "dt must be finite and positive");
     rrea_gpu_config const& c = ctx->cfg;
     rrea_dev::StepConstants sc{};
     sc.cfg = c;
@@ -423,23 +454,14 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     sc.step_key = static_cast<uint64_t>(step > 0 ? step : 0);
     sc.dt_s = dt_s;
     sc.hm_enabled = c.debug_disable_hard_moller ? 0 : 1;
-    RREA_CUDA(ctx, rrea_launch::set_step_constants(sc, ctx->stream));
-    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_sec_count, 0, sizeof(unsigned long long), ctx->stream));
-    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
-    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_transported, 0, sizeof(unsigned long long), ctx->stream));
+    return sc;
+}
 
+// The sinks, tables and field view every transport kernel shares.
+rrea_dev::ElectronArgs sink_args(rrea_gpu_ctx* ctx, rrea_dev::StepConstants const& sc)
+{
+    rrea_gpu_config const& c = ctx->cfg;
     rrea_dev::ElectronArgs a{};
-    SpeciesTile& st = ctx->tiles[species];
-    a.n = st.n;
-    double** t = st.d;
-    a.r = t[0]; a.z = t[1]; a.theta = t[2]; a.ux = t[3]; a.uy = t[4]; a.uz = t[5]; a.w = t[6];
-    if (aliased) {
-        a.prev_r = t[0]; a.prev_z = t[1]; a.prev_theta = t[2]; a.prev_ux = t[3]; a.prev_uy = t[4]; a.prev_uz = t[5];
-    } else {
-        a.prev_r = t[7]; a.prev_z = t[8]; a.prev_theta = t[9]; a.prev_ux = t[10]; a.prev_uy = t[11]; a.prev_uz = t[12];
-    }
-    a.id = st.id;
-    a.cpu = st.cpu;
     a.sec = ctx->d_sec_unordered;
     a.sec_count = ctx->d_sec_count;
     a.sec_capacity = ctx->sec_capacity;
@@ -465,6 +487,38 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     a.fv.z_lo = c.z_lo;
     a.fv.periodic = c.periodic_z != 0;
     a.fv.has_b = ctx->has_b;
+    return a;
+}
+
+// Launches one species phase (electron, positron or photon) on the staged
+// device tile.  `aliased` runs the resident engine mode: the captured
+// pre-push state is the current state (for photons the kernel then performs
+// the straight push itself).
+rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, double dt_s, bool aliased)
+{
+    if (!ctx->tables_loaded || !ctx->field_set) {
+        return fail(ctx, RREA_GPU_ERR_NOT_READY, "tables and field must be set before a step");
+    }
+    if (!(dt_s > 0.0) || !std::isfinite(dt_s)) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "dt must be finite and positive");
+    rrea_gpu_config const& c = ctx->cfg;
+    rrea_dev::StepConstants const sc = step_constants(ctx, step, dt_s);
+    RREA_CUDA(ctx, rrea_launch::set_step_constants(sc, ctx->stream));
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_sec_count, 0, sizeof(unsigned long long), ctx->stream));
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_transported, 0, sizeof(unsigned long long), ctx->stream));
+
+    rrea_dev::ElectronArgs a = sink_args(ctx, sc);
+    SpeciesTile& st = ctx->tiles[species];
+    a.n = st.n;
+    double** t = st.d;
+    a.r = t[0]; a.z = t[1]; a.theta = t[2]; a.ux = t[3]; a.uy = t[4]; a.uz = t[5]; a.w = t[6];
+    if (aliased) {
+        a.prev_r = t[0]; a.prev_z = t[1]; a.prev_theta = t[2]; a.prev_ux = t[3]; a.prev_uy = t[4]; a.prev_uz = t[5];
+    } else {
+        a.prev_r = t[7]; a.prev_z = t[8]; a.prev_theta = t[9]; a.prev_ux = t[10]; a.prev_uy = t[11]; a.prev_uz = t[12];
+    }
+    a.id = st.id;
+    a.cpu = st.cpu;
     a.straight_push = (species == RREA_SPECIES_PHOTON && aliased) ? 1 : 0;
     a.segments = (species != RREA_SPECIES_PHOTON && ctx->netchord) ? ctx->d_seg : nullptr;
     if (a.n > 0) {
@@ -575,14 +629,212 @@ rrea_gpu_status fetch_species(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile* til
     return RREA_GPU_OK;
 }
 
+// Makes `buf` hold at least `need` records with the `keep` records that
+// started at `from` moved to its front.  Reallocates (synchronizing the
+// stream) only when the buffer is too small or the records must move.
+rrea_gpu_status grow_records(rrea_gpu_ctx* ctx, rrea_gpu_secondary*& buf, int64_t& cap, int64_t need, int64_t from,
+                             int64_t keep)
+{
+    if (need <= cap && from == 0) return RREA_GPU_OK;
+    int64_t const target = need > cap ? std::max<int64_t>(need, std::max<int64_t>(2 * cap, 4096)) : cap;
+    rrea_gpu_secondary* nb = nullptr;
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    RREA_CUDA(ctx, dalloc(&nb, static_cast<size_t>(target)));
+    if (keep > 0) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(nb, buf + from, static_cast<size_t>(keep) * sizeof(rrea_gpu_secondary),
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+        RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    dfree(buf);
+    buf = nb;
+    cap = target;
+    return RREA_GPU_OK;
+}
+
+// Appends the last phase's ordered secondaries to the pending FIFO.
+rrea_gpu_status queue_secondaries(rrea_gpu_ctx* ctx)
+{
+    int64_t const n = ctx->last_secondaries;
+    if (n <= 0) return RREA_GPU_OK;
+    rrea_gpu_status const s =
+        grow_records(ctx, ctx->d_fifo, ctx->fifo_cap, ctx->fifo_pending + n, 0, ctx->fifo_pending);
+    if (s != RREA_GPU_OK) return s;
+    RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_fifo + ctx->fifo_pending, ctx->d_sec_ordered,
+                                   static_cast<size_t>(n) * sizeof(rrea_gpu_secondary), cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
+    ctx->fifo_pending += n;
+    return RREA_GPU_OK;
+}
+
 rrea_gpu_status step_resident(rrea_gpu_ctx* ctx, int species, int32_t step, double dt_s, int64_t* n_secondaries)
 {
     if (!ctx) return RREA_GPU_ERR_ARGUMENT;
-    rrea_gpu_status const s = launch_phase(ctx, species, step, dt_s, /*aliased=*/true);
+    rrea_gpu_status s = launch_phase(ctx, species, step, dt_s, /*aliased=*/true);
     if (s != RREA_GPU_OK) return s;
     if (n_secondaries) *n_secondaries = ctx->last_secondaries;
+    s = queue_secondaries(ctx);
+    if (s != RREA_GPU_OK) return s;
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RREA_GPU_OK;
+}
+
+// DrainAndCommitSecondaries' transient FIFO (O/RreaSecondaryCommit.cpp:331-474)
+// over d_fifo[0, n_initial).  The FIFO is a breadth-first walk: the children
+// of a chunk are appended behind every item already queued, so advancing it
+// chunk by chunk (at most `capacity` items, one thread each) and merging each
+// chunk's children in item order reproduces the reference's batch-of-1024
+// order exactly.  Lineages of the children come from one counter per root
+// (RNG key, root species), seeded by the initial items and kept here on the
+// host: a child's root is its item's root, so only the per-item child counts
+// cross to the host.
+rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t n_initial)
+{
+    if (!ctx->tables_loaded || !ctx->field_set) {
+        return fail(ctx, RREA_GPU_ERR_NOT_READY, "tables and field must be set before a drain");
+    }
+    if (!(dt_s > 0.0) || !std::isfinite(dt_s)) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "dt must be finite and positive");
+    rrea_gpu_config const& c = ctx->cfg;
+    rrea_dev::StepConstants const sc = step_constants(ctx, step, dt_s);
+    ctx->n_surv = 0;
+    ctx->last_drain_items = 0;
+    RREA_CUDA(ctx, rrea_launch::newborn_constants(sc, ctx->stream));
+    auto check_payloads = [&](rrea_gpu_secondary const* items, int64_t n, int mode) -> rrea_gpu_status {
+        unsigned long long invalid = 0;
+        long long first = INT64_MAX;
+        RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_invalid, 0, sizeof(unsigned long long), ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_fail_index, &first, sizeof(first), cudaMemcpyHostToDevice, ctx->stream));
+        RREA_CUDA(ctx, rrea_launch::validate_fifo(items, n, mode, ctx->d_invalid, ctx->d_fail_index, ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(&invalid, ctx->d_invalid, sizeof(invalid), cudaMemcpyDeviceToHost, ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(&first, ctx->d_fail_index, sizeof(first), cudaMemcpyDeviceToHost, ctx->stream));
+        RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (invalid == 0) return RREA_GPU_OK;
+        return fail(ctx, mode == 0 ? RREA_GPU_ERR_ARGUMENT : RREA_GPU_ERR_INVALID_STATE,
+                    std::string(mode == 0 ? "transient FIFO received an invalid birth payload"
+                                          : "transient work graph contains invalid final survivors")
+                        + " (" + std::to_string(invalid) + " records, first at " + std::to_string(first) + ")");
+    };
+    rrea_gpu_status s = check_payloads(ctx->d_fifo, n_initial, 0);
+    if (s != RREA_GPU_OK) return s;
+
+    // roots[k] is the root of FIFO item root_base + k (FIFO indices count
+    // every item merged since the drain began)
+    std::vector<RootKey> roots(static_cast<size_t>(n_initial));
+    std::unordered_map<RootKey, uint64_t, RootHash> next_lineage;
+    {
+        std::vector<rrea_gpu_secondary> init(static_cast<size_t>(n_initial));
+        if (n_initial > 0) {
+            RREA_CUDA(ctx, cudaMemcpyAsync(init.data(), ctx->d_fifo,
+                                           static_cast<size_t>(n_initial) * sizeof(rrea_gpu_secondary),
+                                           cudaMemcpyDeviceToHost, ctx->stream));
+            RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        }
+        for (size_t i = 0; i < init.size(); ++i) {
+            RootKey const r{init[i].root_key, init[i].root_species};
+            roots[i] = r;
+            uint64_t& nx = next_lineage[r];
+            nx = std::max<uint64_t>(nx, init[i].lineage + 1U);
+        }
+    }
+    std::vector<uint32_t> counts;
+    std::vector<uint64_t> lineage;
+    int64_t cursor = 0, tail = n_initial;
+    size_t root_base = 0;
+    while (cursor < tail) {
+        int64_t const chunk = std::min<int64_t>(tail - cursor, ctx->capacity);
+        RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_sec_count, 0, sizeof(unsigned long long), ctx->stream));
+        RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+        rrea_dev::ElectronArgs a = sink_args(ctx, sc);
+        a.diag_subcycles = nullptr;
+        a.diag_events = nullptr;
+        a.diag_disposition = nullptr;
+        a.segments = ctx->netchord ? ctx->d_seg : nullptr;
+        rrea_gpu_secondary* const items = ctx->d_fifo + cursor;
+        RREA_CUDA(ctx, rrea_launch::newborn_step(a, items, chunk, ctx->d_alive, ctx->num_sms * 8, c.periodic_z != 0,
+                                                 ctx->stream));
+        if (a.segments) {
+            RREA_CUDA(ctx, rrea_launch::netchord_deposit(a.segments, chunk, ctx->net, dt_s, ctx->d_status,
+                                                         ctx->d_fail_index, ctx->num_sms * 8, ctx->stream));
+        }
+        unsigned long long count = 0;
+        int status = 0;
+        long long fail_index = -1;
+        int64_t last_offset = 0;
+        uint32_t last_alive = 0;
+        RREA_CUDA(ctx, rrea_launch::exclusive_scan_counts(ctx->d_alive, chunk, ctx->d_offsets, ctx->d_scan_scratch,
+                                                          ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(&count, ctx->d_sec_count, sizeof(count), cudaMemcpyDeviceToHost, ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(&status, ctx->d_status, sizeof(status), cudaMemcpyDeviceToHost, ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(&fail_index, ctx->d_fail_index, sizeof(fail_index), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(&last_offset, ctx->d_offsets + (chunk - 1), sizeof(last_offset),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(&last_alive, ctx->d_alive + (chunk - 1), sizeof(last_alive),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+        counts.resize(static_cast<size_t>(chunk));
+        RREA_CUDA(ctx, cudaMemcpyAsync(counts.data(), ctx->d_sec_per_parent, static_cast<size_t>(chunk) * sizeof(uint32_t),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+        RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (status != 0) {
+            return fail(ctx, static_cast<rrea_gpu_status>(status),
+                        "newborn transport guard failed (status " + std::to_string(status) + ") at FIFO item "
+                            + std::to_string(cursor + fail_index));
+        }
+        if (count > static_cast<unsigned long long>(ctx->sec_capacity)) {
+            return fail(ctx, RREA_GPU_ERR_CAPACITY, "newborn child buffer overflow");
+        }
+        // survivors of the chunk, in FIFO order
+        int64_t const survivors = last_offset + static_cast<int64_t>(last_alive);
+        s = grow_records(ctx, ctx->d_surv, ctx->surv_cap, ctx->n_surv + survivors, 0, ctx->n_surv);
+        if (s != RREA_GPU_OK) return s;
+        RREA_CUDA(ctx, rrea_launch::compact_survivors(items, ctx->d_alive, ctx->d_offsets, chunk,
+                                                      ctx->d_surv + ctx->n_surv, ctx->stream));
+        ctx->n_surv += survivors;
+        // children: lineage per root in merge order, then appended behind the tail
+        int64_t const n_children = static_cast<int64_t>(count);
+        if (n_children > 0) {
+            lineage.resize(static_cast<size_t>(n_children));
+            size_t j = 0;
+            for (int64_t i = 0; i < chunk; ++i) {
+                uint32_t const ci = counts[static_cast<size_t>(i)];
+                if (ci == 0) continue;
+                RootKey const r = roots[static_cast<size_t>(ctx->last_drain_items) - root_base + static_cast<size_t>(i)];
+                uint64_t& nx = next_lineage[r];
+                for (uint32_t t = 0; t < ci; ++t) {
+                    if (nx >= rrea_dev::kLineageCap || j >= lineage.size()) {
+                        return fail(ctx, RREA_GPU_ERR_RNG_OVERFLOW, "transient FIFO lineage overflow");
+                    }
+                    lineage[j++] = nx++;
+                    roots.push_back(r);
+                }
+            }
+            if (j != lineage.size()) return fail(ctx, RREA_GPU_ERR_INVALID_STATE, "newborn child count mismatch");
+            RREA_CUDA(ctx, rrea_launch::order_secondaries(ctx->d_sec_per_parent, chunk, ctx->d_offsets,
+                                                          ctx->d_scan_scratch, ctx->d_sec_unordered, n_children,
+                                                          ctx->d_sec_ordered, ctx->stream));
+            RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_child_lineage, lineage.data(),
+                                           static_cast<size_t>(n_children) * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                           ctx->stream));
+            // make room behind the tail; items before the cursor are no longer needed
+            if (tail + n_children > ctx->fifo_cap) {
+                s = grow_records(ctx, ctx->d_fifo, ctx->fifo_cap, tail - cursor + n_children, cursor, tail - cursor);
+                if (s != RREA_GPU_OK) return s;
+                tail -= cursor;
+                cursor = 0;
+            }
+            RREA_CUDA(ctx, rrea_launch::adopt_children(ctx->d_sec_ordered, n_children, ctx->d_fifo + cursor,
+                                                       ctx->d_child_lineage, ctx->d_fifo + tail, ctx->stream));
+            tail += n_children;
+        }
+        ctx->last_drain_items += chunk;
+        cursor += chunk;
+        // roots of merged items are no longer needed
+        size_t const done = static_cast<size_t>(ctx->last_drain_items) - root_base;
+        if (done > (1u << 20) && done * 2 > roots.size()) {
+            roots.erase(roots.begin(), roots.begin() + static_cast<std::ptrdiff_t>(done));
+            root_base += done;
+        }
+    }
+    return check_payloads(ctx->d_surv, ctx->n_surv, 1);
 }
 
 }  // namespace
@@ -705,6 +957,75 @@ rrea_gpu_status rrea_gpu_download_field(rrea_gpu_ctx* ctx, double* er, double* e
     RREA_CUDA(ctx, cudaMemcpyAsync(ez, ctx->d_ez, nez * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     RREA_CUDA(ctx, cudaMemcpyAsync(bt, ctx->d_bt, nbt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_drain_secondaries(rrea_gpu_ctx* ctx, const rrea_gpu_secondary* pending, int64_t n_pending,
+                                           int32_t step, double dt_s, rrea_gpu_secondary* survivors,
+                                           int64_t survivor_capacity, int64_t* n_survivors)
+{
+    if (!ctx || n_pending < 0 || (n_pending > 0 && !pending) || survivor_capacity < 0) return RREA_GPU_ERR_ARGUMENT;
+    ctx->fifo_pending = 0;
+    rrea_gpu_status s = grow_records(ctx, ctx->d_fifo, ctx->fifo_cap, n_pending, 0, 0);
+    if (s != RREA_GPU_OK) return s;
+    if (n_pending > 0) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_fifo, pending, static_cast<size_t>(n_pending) * sizeof(rrea_gpu_secondary),
+                                       cudaMemcpyHostToDevice, ctx->stream));
+    }
+    s = drain_fifo(ctx, step, dt_s, n_pending);
+    if (s != RREA_GPU_OK) return s;
+    if (n_survivors) *n_survivors = ctx->n_surv;
+    if (survivors && ctx->n_surv > survivor_capacity) {
+        return fail(ctx, RREA_GPU_ERR_CAPACITY, "caller survivor buffer too small");
+    }
+    if (survivors && ctx->n_surv > 0) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(survivors, ctx->d_surv, static_cast<size_t>(ctx->n_surv) * sizeof(rrea_gpu_secondary),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_drain_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t* n_survivors)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    int64_t const n = ctx->fifo_pending;
+    // the queued records are consumed whether or not the drain succeeds
+    ctx->fifo_pending = 0;
+    rrea_gpu_status const s = drain_fifo(ctx, step, dt_s, n);
+    if (s != RREA_GPU_OK) return s;
+    if (n_survivors) *n_survivors = ctx->n_surv;
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fetch_survivors(rrea_gpu_ctx* ctx, rrea_gpu_secondary* survivors, int64_t capacity,
+                                         int64_t* n_survivors)
+{
+    if (!ctx || capacity < 0 || (capacity > 0 && !survivors)) return RREA_GPU_ERR_ARGUMENT;
+    if (n_survivors) *n_survivors = ctx->n_surv;
+    if (ctx->n_surv > capacity) return fail(ctx, RREA_GPU_ERR_CAPACITY, "caller survivor buffer too small");
+    if (ctx->n_surv > 0) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(survivors, ctx->d_surv, static_cast<size_t>(ctx->n_surv) * sizeof(rrea_gpu_secondary),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_pending_secondaries(rrea_gpu_ctx* ctx, int64_t* n_pending, int32_t discard)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    if (n_pending) *n_pending = ctx->fifo_pending;
+    if (discard) ctx->fifo_pending = 0;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_last_drain_stats(rrea_gpu_ctx* ctx, int64_t* fifo_items, int64_t* survivors)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    if (fifo_items) *fifo_items = ctx->last_drain_items;
+    if (survivors) *survivors = ctx->n_surv;
     return RREA_GPU_OK;
 }
 

@@ -31,6 +31,19 @@ cudaError_t netchord_convert(rrea_dev::NetGrid const& g, double* jr_phys, double
 // Maxwell TM-RZ step with a fixed face current (rrea_field.cu).
 cudaError_t maxwell_step(int nr, int nz, double dr, double dz, double dt, int substeps, double* er, double* ez,
                          double* bt, const double* jr, const double* jz, cudaStream_t stream);
+// Transient FIFO of the secondaries (rrea_newborn.cu): its own constant
+// bank, payload checks (mode 0 birth payloads, 1 final survivors), the
+// residual advance of one chunk of FIFO items, survivor compaction, and the
+// adoption of the chunk's ordered children into the FIFO tail.
+cudaError_t newborn_constants(rrea_dev::StepConstants const& sc, cudaStream_t stream);
+cudaError_t validate_fifo(const rrea_gpu_secondary* items, int64_t n, int mode, unsigned long long* invalid,
+                          long long* first, cudaStream_t stream);
+cudaError_t newborn_step(rrea_dev::ElectronArgs const& args, rrea_gpu_secondary* items, int64_t n, uint32_t* alive,
+                         int max_blocks, bool periodic, cudaStream_t stream);
+cudaError_t compact_survivors(const rrea_gpu_secondary* items, const uint32_t* alive, const int64_t* offsets,
+                              int64_t n, rrea_gpu_secondary* out, cudaStream_t stream);
+cudaError_t adopt_children(const rrea_gpu_secondary* ordered, int64_t n, const rrea_gpu_secondary* items,
+                           const uint64_t* lineage, rrea_gpu_secondary* out, cudaStream_t stream);
 cudaError_t count_live(const int64_t* id, int64_t n, unsigned long long* out, int blocks, cudaStream_t stream);
 int64_t scan_scratch_elems(int64_t n);
 // Exclusive scan of per-parent counts into offsets (block_scratch holds

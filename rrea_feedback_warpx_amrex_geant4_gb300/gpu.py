@@ -73,7 +73,9 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_apply_positrons", "rrea_gpu_stage_positrons", "rrea_gpu_step_positrons_resident",
     "rrea_gpu_fetch_positrons", "rrea_gpu_reset_current", "rrea_gpu_download_current",
     "rrea_gpu_download_current_index", "rrea_gpu_advance_field", "rrea_gpu_download_field",
-    "rrea_gpu_count_live", "rrea_gpu_population_projection",
+    "rrea_gpu_count_live", "rrea_gpu_population_projection", "rrea_gpu_drain_secondaries",
+    "rrea_gpu_drain_resident", "rrea_gpu_fetch_survivors", "rrea_gpu_pending_secondaries",
+    "rrea_gpu_last_drain_stats",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -121,6 +123,13 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_population_projection.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
                                                    ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)]
     lib.rrea_gpu_download_field.argtypes = [vp, _D, _D, _D]
+    _i64p = ctypes.POINTER(ctypes.c_int64)
+    lib.rrea_gpu_drain_secondaries.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, vp,
+                                               ctypes.c_int64, _i64p]
+    lib.rrea_gpu_drain_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_double, _i64p]
+    lib.rrea_gpu_fetch_survivors.argtypes = [vp, vp, ctypes.c_int64, _i64p]
+    lib.rrea_gpu_pending_secondaries.argtypes = [vp, _i64p, ctypes.c_int32]
+    lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
     lib.rrea_gpu_reset_current.argtypes = [vp]
     lib.rrea_gpu_download_current.argtypes = [vp, _D, _D]
     lib.rrea_gpu_download_current_index.argtypes = [vp, _D, _D, _D]
@@ -277,6 +286,42 @@ class RreaGpuContext:
     def reset_sources(self):
         self._check(self.lib.rrea_gpu_reset_sources(self.handle))
 
+    def drain_secondaries(self, pending, step, dt_s):
+        """DrainAndCommitSecondaries' transient FIFO over host records (a
+        SECONDARY_DTYPE array in phase order); returns the survivors in FIFO
+        order.  Discards the resident queue."""
+        pending = np.ascontiguousarray(pending, dtype=SECONDARY_DTYPE)
+        n = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_drain_secondaries(
+            self.handle, ctypes.c_void_p(pending.ctypes.data) if len(pending) else None, len(pending), int(step),
+            float(dt_s), None, 0, ctypes.byref(n)))
+        return self.fetch_survivors(n.value)
+
+    def drain_resident(self, step, dt_s):
+        """Drains the queue the resident phases filled; returns the survivor count."""
+        n = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_drain_resident(self.handle, int(step), float(dt_s), ctypes.byref(n)))
+        return n.value
+
+    def fetch_survivors(self, n=None):
+        if n is None:
+            n = self.last_drain_stats()[1]
+        out = np.zeros(int(n), dtype=SECONDARY_DTYPE)
+        got = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_fetch_survivors(self.handle, ctypes.c_void_p(out.ctypes.data) if n else None,
+                                                      int(n), ctypes.byref(got)))
+        return out[: got.value]
+
+    def pending_secondaries(self, discard=False):
+        n = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_pending_secondaries(self.handle, ctypes.byref(n), int(bool(discard))))
+        return n.value
+
+    def last_drain_stats(self):
+        items, surv = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_last_drain_stats(self.handle, ctypes.byref(items), ctypes.byref(surv)))
+        return items.value, surv.value
+
     def count_live(self, species):
         live = ctypes.c_int64()
         self._check(self.lib.rrea_gpu_count_live(self.handle, int(species), ctypes.byref(live)))
@@ -379,3 +424,9 @@ class RreaParticleInteraction:
         sec_g = self.ctx.apply_photons(photons, step, dt_s, time_s=time_s) if photons is not None else None
         sec_p = self.ctx.apply_positrons(positrons, step, dt_s, time_s=time_s) if positrons is not None else None
         return sec_e, sec_g, sec_p
+
+    def DrainAndCommitSecondaries(self, pending, step, dt_s):
+        """The transient FIFO of RreaSecondaryCommit.cpp:331-474 over the
+        secondaries Apply returned (concatenated in phase order); returns the
+        survivors that the overlay inserts, in FIFO order."""
+        return self.ctx.drain_secondaries(pending, step, dt_s)
