@@ -153,7 +153,8 @@ def test_resident_queue_drain_matches_oracle(mods):
     device; drain_resident consumes that queue."""
     gpu, workloads, oracle, compare = mods
     case, n, dt_s, step = "scaleup_c1", 2048, 1.0e-7, 2
-    cfg, ctx, field = _setup(gpu, workloads, case, n)
+    # 30 m chords make several secondaries per electron: room for 2 x 8192 + 4096
+    cfg, ctx, field = _setup(gpu, workloads, case, 4 * n)
     arr = workloads.make_electrons(case, n, seed=9)
     o_phase = oracle.electron_step(cfg, field, step, dt_s, workloads.copy_tile(arr))
     ctx.stage_electrons(workloads.copy_tile(arr))
