@@ -1,18 +1,25 @@
 #!/usr/bin/env python3
 """Throughput of the GB300 kinetic step: particle-steps/s on one GB300.
 
-Workload: the plain GPU scale-up case.  Electrons drawn from its seed
-distribution (K log-uniform 1-20 MeV, isotropic in the -E hemisphere,
-uniform in a 5 m x 10 m disk) plus a photon population (E log-uniform
-50 keV-20 MeV, +z hemisphere, same disk), air at 1.225 kg/m^3, uniform
-E_z = -500 kV/m, 256 x 2048 grid over 200 m x 2 km, dt = 0.5 ns, 10 keV
-tracking cut.  One step = one outer dt of the electron phase and then the
-photon phase (the reference's phase order) over both resident populations.
-Synthetic seeds; no dataset.
+Workload: the plain GPU scale-up case with its self-consistent field.
+Electrons drawn from its seed distribution (K log-uniform 1-20 MeV,
+isotropic in the -E hemisphere, uniform in a 5 m x 10 m disk), a photon
+population (E log-uniform 50 keV-20 MeV, +z hemisphere, same disk; half as
+many) and a positron population (the electron distribution; 1/16 as many),
+air at 1.225 kg/m^3, initial uniform E_z = -500 kV/m, 256 x 2048 grid over
+200 m x 2 km, dt = 0.5 ns, 10 keV tracking cut.  One step is the whole
+kinetic step in the reference's order: the electron, photon and positron
+phases over the resident populations, the transient FIFO that flies every
+secondary through the rest of its step (newborn residual legs), the
+net-chord current of all charged flights, and the Maxwell TM-RZ field update
+driven by it.  A particle-step is one live macroparticle advanced through
+one dt, its newborn residual legs included.  Synthetic seeds; no dataset.
 
   value       particle-steps/s with the tiles resident in HBM (device-timed)
   e2e         the same through the drop-in C-ABI entry points with host
-              buffers: H2D of the tiles, the step, D2H of tiles + secondaries
+              buffers: H2D of the tiles, the three phases, H2D of their
+              secondaries into the drain, D2H of tiles, secondaries and
+              survivors
   roofline    electron transport kernel (the dominant one) vs measured HBM
               bandwidth (112 B algorithmic traffic per particle-step: read
               r,z,theta,ux,uy,uz,w,id, write r,z,theta,ux,uy,uz)
@@ -39,7 +46,10 @@ CASE = "scaleup_c1"
 DT_S = 5.0e-10
 BYTES_PER_PARTICLE_STEP = 112
 PHOTON_FRACTION = 0.5  # photons per electron in the resident populations
-METRIC = "particle-steps/s on 1 GB300 (plain kinetic step: electron + photon phases)"
+POSITRON_FRACTION = 0.0625  # positrons per electron
+FIELD_SUBSTEPS = 2  # material substeps of the Maxwell update
+METRIC = ("particle-steps/s on 1 GB300 (plain kinetic step: electron, photon and positron phases, "
+          "newborn FIFO, net-chord current and field update)")
 
 
 def parse():
@@ -49,7 +59,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--population", type=int, default=1 << 21)
-    p.add_argument("--cpu-sample", type=int, default=32768)
+    p.add_argument("--cpu-sample", type=int, default=131072)
+    p.add_argument("--cpu-baseline-sample", type=int, default=1 << 19)
+    p.add_argument("--cpu-baseline-steps", type=int, default=4)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--threads", type=int, default=128)
     p.add_argument("--blocks-per-sm", type=int, default=16)
@@ -159,28 +171,53 @@ def make_photons(n, seed):
     return arr
 
 
+def cpu_populations(n, seed):
+    """Electron, photon and positron tiles of the workload (n electrons)."""
+    from rrea_feedback_warpx_amrex_geant4_gb300 import workloads
+
+    arr = workloads.make_electrons(CASE, n, seed=seed)
+    pho = make_photons(int(n * PHOTON_FRACTION), seed + 1)
+    pos = workloads.make_electrons(CASE, max(1, int(n * POSITRON_FRACTION)), seed=seed + 2)
+    return arr, pho, pos
+
+
 def cpu_oracle_rate(cfg, field, n, seed, steps=1):
-    """Oracle particle-steps/s on n electrons and PHOTON_FRACTION*n photons
-    for `steps` steps (all threads)."""
+    """Oracle particle-steps/s of the whole kinetic step (three phases, FIFO
+    drain, net-chord current, field update) on n electrons, the photon and
+    positron fractions, for `steps` steps (all threads)."""
     from oracle import oracle
     from rrea_feedback_warpx_amrex_geant4_gb300 import DEFAULT_TABLES, workloads
 
     if not getattr(cpu_oracle_rate, "_loaded", False):
         oracle.load_tables(DEFAULT_TABLES)
         cpu_oracle_rate._loaded = True
-    arr = workloads.make_electrons(CASE, n, seed=seed)
-    pho = make_photons(int(n * PHOTON_FRACTION), seed + 1)
+    arr, pho, pos = cpu_populations(n, seed)
+    fld = {k: np.array(v, dtype=np.float64) for k, v in field.items()}
+    dr = (cfg.r_hi - cfg.r_lo) / cfg.nr
+    dz = (cfg.z_hi - cfg.z_lo) / cfg.nz
     moved = 0
     t0 = time.perf_counter()
     for s in range(steps):
-        moved += int((arr["id"] > 0).sum()) + int((pho["id"] > 0).sum())
-        oracle.electron_step(cfg, field, s, DT_S, arr)
-        oracle.photon_step(cfg, s, DT_S, pho)
-        workloads.capture_prev(arr)
-        workloads.capture_prev(pho)
+        moved += int((arr["id"] > 0).sum()) + int((pho["id"] > 0).sum()) + int((pos["id"] > 0).sum())
+        oe = oracle.electron_step(cfg, fld, s, DT_S, arr)
+        og = oracle.photon_step(cfg, s, DT_S, pho)
+        op = oracle.positron_step(cfg, fld, s, DT_S, pos)
+        pending = np.concatenate([oe["secondaries"], og["secondaries"], op["secondaries"]])
+        od = oracle.drain(cfg, fld, s, DT_S, pending)
+        rows = np.concatenate([oracle.segment_rows(r) for r in (oe, op, od)])
+        cur = oracle.deposit_segments(cfg, DT_S, rows)
+        fld["er"], fld["ez"], fld["bt"] = oracle.advance_maxwell(cfg.nr, cfg.nz, dr, dz, DT_S, FIELD_SUBSTEPS,
+                                                                 fld["er"], fld["ez"], fld["bt"], cur["jr_phys"],
+                                                                 cur["jz_phys"])
+        for t in (arr, pho, pos):
+            workloads.capture_prev(t)
         workloads.push_photons(pho, DT_S)
     dt = time.perf_counter() - t0
     return moved / dt, moved, dt
+
+
+def population_text(n):
+    return (f"{n} e-, {int(n * PHOTON_FRACTION)} photons, {max(1, int(n * POSITRON_FRACTION))} e+")
 
 
 def run_reference(args, rank, world):
@@ -206,12 +243,12 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * total_t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (scale-up case seed distribution)",
-        "config": {"workload": f"{CASE}: electron + photon phases, {args.cpu_sample} electrons and "
-                               f"{int(args.cpu_sample * PHOTON_FRACTION)} photons per timed step",
-                   "grid": "256x2048", "dt_s": DT_S},
+        "config": {"workload": f"{CASE}: whole kinetic step (three phases, newborn FIFO, net-chord current, "
+                               f"field update), {population_text(args.cpu_sample)} per timed step",
+                   "grid": "256x2048", "dt_s": DT_S, "field_substeps": FIELD_SUBSTEPS},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.cpu_sample} e- + {int(args.cpu_sample * PHOTON_FRACTION)} photons x "
-                                   f"{args.steps} steps, OpenMP chunks of 64"},
+                         "sample": f"{population_text(args.cpu_sample)} x {args.steps} steps (a fresh draw of the "
+                                   f"workload each step), OpenMP chunks of 64"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -237,6 +274,7 @@ def run_gb300(args, rank, world, local):
 
     n = args.population
     n_g = int(n * PHOTON_FRACTION)
+    n_p = max(1, int(n * POSITRON_FRACTION))
     cfg = workloads.make_config(gpu, CASE)
     ctx = gpu.RreaGpuContext(cfg, n)
     ctx.load_tables(DEFAULT_TABLES)
@@ -247,8 +285,10 @@ def run_gb300(args, rank, world, local):
     pho = make_photons(n_g, seed=778 + rank)
     for f in ("r", "z", "theta"):
         pho[f][:] = pho["prev_" + f]  # the resident photon step pushes by itself
+    pos = workloads.make_electrons(CASE, n_p, seed=779 + rank)
     ctx.stage_electrons(arr)
     ctx.stage_photons(pho)
+    ctx.stage_positrons(pos)
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -258,7 +298,13 @@ def run_gb300(args, rank, world, local):
         te, _, kme = ctx.last_step_stats()
         ng = ctx.step_photons_resident(step, DT_S)
         tg, _, kmg = ctx.last_step_stats()
-        return te, tg, kme, kmg, ne, ng
+        npos = ctx.step_positrons_resident(step, DT_S)
+        tp, _, kmp = ctx.last_step_stats()
+        ctx.drain_resident(step, DT_S)  # newborn residual legs of every secondary
+        items, surv = ctx.last_drain_stats()
+        ctx.advance_field(DT_S, FIELD_SUBSTEPS)  # Maxwell TM-RZ with this step's J
+        return {"te": te, "tg": tg, "tp": tp, "kme": kme, "kmg": kmg, "kmp": kmp,
+                "secondaries": ne + ng + npos, "fifo_items": items, "survivors": surv}
 
     step = 0
     for _ in range(args.warmup):
@@ -269,36 +315,30 @@ def run_gb300(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     total_ms = 0.0
-    kernel_ms_e = 0.0
-    kernel_ms_g = 0.0
-    moved_e = 0
-    moved_g = 0
+    acc = {k: 0 for k in ("te", "tg", "tp", "kme", "kmg", "kmp", "secondaries", "fifo_items", "survivors")}
     launches = 0
-    secondaries = 0
     for _ in range(args.steps):
         flush.zero_()  # L2 flush between timed steps (256 MiB write)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        l0 = gpu.kernel_launches()
         e0.record(stream)
-        te, tg, kme, kmg, ne, ng = one_step(step)
+        r = one_step(step)
         e1.record(stream)
         e1.synchronize()
+        launches += gpu.kernel_launches() - l0  # this library's kernels only
         total_ms += e0.elapsed_time(e1)
-        kernel_ms_e += kme
-        kernel_ms_g += kmg
-        moved_e += te
-        moved_g += tg
-        secondaries += ne + ng
-        # electron phase: transport, current deposition, 3 scan kernels, scatter when
-        # anything was appended; photon phase: transport, 3 scan kernels, scatter
-        launches += (2 + 3 + (1 if ne > 0 else 0)) + (1 + 3 + (1 if ng > 0 else 0))
+        for k in acc:
+            acc[k] += r[k]
         step += 1
     barrier()
     clocks.stop()
+    moved_e, moved_g, moved_p = acc["te"], acc["tg"], acc["tp"]
+    kernel_ms_e, kernel_ms_g, kernel_ms_p = acc["kme"], acc["kmg"], acc["kmp"]
 
     # max over ranks of the device time; total work summed
-    moved = moved_e + moved_g
+    moved = moved_e + moved_g + moved_p
     t_local = torch.tensor([total_ms, float(moved)], dtype=torch.float64, device="cuda")
     if dist is not None:
         tmax = t_local.clone()
@@ -320,11 +360,29 @@ def run_gb300(args, rank, world, local):
     for f in ("r", "z", "theta", "ux", "uy", "uz"):
         pe["prev_" + f] = pe[f]  # the captured state is the current state
     pg = pinned_tile(make_photons(n_g, seed=4243 + rank))
+    pp = pinned_tile(workloads.make_electrons(CASE, n_p, seed=4244 + rank))
+    for f in ("r", "z", "theta", "ux", "uy", "uz"):
+        pp["prev_" + f] = pp[f]
+    rec = gpu.SECONDARY_DTYPE.itemsize
+
+    def e2e_step(step):
+        """The overlay's step through the drop-in entry points: Apply's three
+        phases on host tiles, then DrainAndCommitSecondaries on their host
+        secondaries, then the field update."""
+        ctx.reset_current()
+        sec_e = ctx.apply_electrons(pe, step, DT_S, want_secondaries=True)
+        sec_g = ctx.apply_photons(pg, step, DT_S, want_secondaries=True)
+        sec_p = ctx.apply_positrons(pp, step, DT_S, want_secondaries=True)
+        pending = np.concatenate([sec_e, sec_g, sec_p])
+        surv = ctx.drain_secondaries(pending, step, DT_S)
+        ctx.advance_field(DT_S, FIELD_SUBSTEPS)
+        return len(pending), len(surv)
+
     e2e_moved = 0
     e2e_t = 0.0
     sec_bytes = 0
-    ctx.apply_electrons(pe, step, DT_S, want_secondaries=True)  # warm
-    ctx.apply_photons(pg, step, DT_S, want_secondaries=True)
+    surv_bytes = 0
+    e2e_step(step)  # warm
     step += 1
     barrier()
     for _ in range(args.e2e_steps):
@@ -332,56 +390,70 @@ def run_gb300(args, rank, world, local):
         for f in ("r", "z", "theta", "ux", "uy", "uz"):
             np.copyto(pg["prev_" + f], pg[f])
         workloads.push_photons(pg, DT_S)
-        live = int((pe["id"] > 0).sum()) + int((pg["id"] > 0).sum())
+        live = int((pe["id"] > 0).sum()) + int((pg["id"] > 0).sum()) + int((pp["id"] > 0).sum())
         t0 = time.perf_counter()
-        sec_e = ctx.apply_electrons(pe, step, DT_S, want_secondaries=True)
-        sec_g = ctx.apply_photons(pg, step, DT_S, want_secondaries=True)
+        n_pending, n_surv = e2e_step(step)
         e2e_t += time.perf_counter() - t0
         e2e_moved += live
-        sec_bytes += (len(sec_e) + len(sec_g)) * gpu.SECONDARY_DTYPE.itemsize
+        sec_bytes += n_pending * rec
+        surv_bytes += n_surv * rec
         step += 1
     e2e_value = e2e_moved / e2e_t
-    h2d = (n + n_g) * (13 * 8 + 8 + 4)
-    d2h = (n + n_g) * (6 * 8 + 8) + sec_bytes // max(args.e2e_steps, 1)
+    k = max(args.e2e_steps, 1)
+    h2d = (n + n_g + n_p) * (13 * 8 + 8 + 4) + sec_bytes // k
+    d2h = (n + n_g + n_p) * (6 * 8 + 8) + sec_bytes // k + surv_bytes // k
 
     if rank == 0:
         peak, peak_kind = read_peaks()
         achieved = (moved_e * BYTES_PER_PARTICLE_STEP) / (kernel_ms_e / 1000.0) / 1.0e9 if kernel_ms_e > 0 else 0.0
         achieved_g = (moved_g * BYTES_PER_PARTICLE_STEP) / (kernel_ms_g / 1000.0) / 1.0e9 if kernel_ms_g > 0 else 0.0
+        achieved_p = (moved_p * BYTES_PER_PARTICLE_STEP) / (kernel_ms_p / 1000.0) / 1.0e9 if kernel_ms_p > 0 else 0.0
         traffic_pps = read_traffic_per_particle_step()
         launches_per_step = launches / max(args.steps, 1)
         traffic = traffic_pps * (moved_e / max(args.steps, 1)) if traffic_pps else None
         cores = os.cpu_count() or 1
-        cpu_n = min(args.cpu_sample, 16384)
-        cpu_rate, cpu_moved, cpu_t = cpu_oracle_rate(cfg, field, cpu_n, seed=31337)
+        cpu_n = args.cpu_baseline_sample
+        cpu_rate, cpu_moved, cpu_t = cpu_oracle_rate(cfg, field, cpu_n, seed=31337, steps=args.cpu_baseline_steps)
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (scale-up case seed distribution, seeded numpy PRNG)",
-            "config": {"workload": f"{CASE}: electron + photon phases over resident populations of {n} e- and "
-                                   f"{n_g} photons per GPU (256x2048 cells over 200 m x 2 km, uniform "
-                                   f"E_z = -500 kV/m), dt 0.5 ns",
-                       "grid": "256x2048", "population_per_gpu": {"electrons": n, "photons": n_g}, "dt_s": DT_S,
+            "config": {"workload": f"{CASE}: whole kinetic step (electron, photon, positron phases, newborn "
+                                   f"FIFO, net-chord current, field update) over resident populations of "
+                                   f"{population_text(n)} per GPU (256x2048 cells over 200 m x 2 km, initial "
+                                   f"uniform E_z = -500 kV/m), dt 0.5 ns",
+                       "grid": "256x2048",
+                       "population_per_gpu": {"electrons": n, "photons": n_g, "positrons": n_p},
+                       "dt_s": DT_S, "field_substeps": FIELD_SUBSTEPS,
                        "l2": "flushed between timed steps (256 MiB write)",
                        "parallelism": f"dp{world} (independent particle shards)"},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
-                    "path": "rrea_gpu_apply_electrons + rrea_gpu_apply_photons (pinned host tiles -> HBM -> host)"},
+                    "path": "rrea_gpu_apply_electrons/_photons/_positrons (pinned host tiles -> HBM -> host), "
+                            "rrea_gpu_drain_secondaries (host records in, survivors out), "
+                            "rrea_gpu_advance_field"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic, "kernel": "electron_step_kernel",
                          "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
                          "kernel_ms_per_step": kernel_ms_e / args.steps,
                          "photon_kernel": {"kernel": "photon_step_kernel", "achieved": achieved_g,
-                                           "frac": achieved_g / peak, "kernel_ms_per_step": kernel_ms_g / args.steps}},
-            "phases": {"electron_steps": moved_e, "photon_steps": moved_g},
+                                           "frac": achieved_g / peak, "kernel_ms_per_step": kernel_ms_g / args.steps},
+                         "positron_kernel": {"kernel": "positron_step_kernel", "achieved": achieved_p,
+                                             "frac": achieved_p / peak,
+                                             "kernel_ms_per_step": kernel_ms_p / args.steps}},
+            "phases": {"electron_steps": moved_e, "photon_steps": moved_g, "positron_steps": moved_p,
+                       "secondaries_per_step": acc["secondaries"] / args.steps,
+                       "fifo_items_per_step": acc["fifo_items"] / args.steps,
+                       "survivors_per_step": acc["survivors"] / args.steps,
+                       "transport_kernels_ms_per_step": (kernel_ms_e + kernel_ms_g + kernel_ms_p) / args.steps},
             "cpu_baseline": {"value": cpu_rate, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{cpu_n} e- + {int(cpu_n * PHOTON_FRACTION)} photons x 1 step of the "
-                                       f"same workload, OpenMP chunks of 64"},
+                             "sample": f"{population_text(cpu_n)} x {args.cpu_baseline_steps} steps of the same "
+                                       f"whole kinetic step ({cpu_moved} particle-steps in {cpu_t:.1f} s), "
+                                       f"OpenMP chunks of 64"},
             "gpu_launches": launches,
             "gpu_launches_per_step": launches_per_step,
-            "secondaries_per_step": secondaries / max(args.steps, 1),
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -247,6 +247,10 @@ rrea_gpu_status rrea_gpu_last_drain_stats(rrea_gpu_ctx* ctx, int64_t* fifo_items
 rrea_gpu_status rrea_gpu_download_diagnostics(rrea_gpu_ctx* ctx, int64_t n, uint64_t* subcycles,
                                               uint64_t* events, int32_t* disposition);
 
+/* Kernels this library has launched in this process (all contexts), for
+ * launch accounting around a timed region.  NO COUNTERPART IN THE REFERENCE. */
+rrea_gpu_status rrea_gpu_kernel_launches(uint64_t* count);
+
 /* Copies the last error message (NUL-terminated, truncated to size). */
 void rrea_gpu_last_error(const rrea_gpu_ctx* ctx, char* buf, size_t size);
 

@@ -72,6 +72,34 @@ struct ElectronArgs {
     int32_t straight_push;
     // charged phases: one net-chord record per tile slot (may be null)
     SegmentRec* __restrict__ segments;
+    // dynamic scheduling: warps take the next 32 particles from this counter
+    // (zeroed before the launch); null = static grid-stride assignment
+    unsigned long long* __restrict__ work;
 };
+
+// Visits every particle index of [0, n) once.  With a work counter each warp
+// claims the next 32 indices when it is done with its previous ones, so a
+// slow particle does not hold up the ones a static assignment would have
+// queued behind it on the same thread.
+template <class F>
+__device__ __forceinline__ void for_each_particle(int64_t n, unsigned long long* work, F&& f)
+{
+    if (work) {
+        int const lane = threadIdx.x & 31;
+        for (;;) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(work, 32ULL);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= static_cast<unsigned long long>(n)) break;
+            int64_t const ip = static_cast<int64_t>(base) + lane;
+            if (ip < n) f(ip);
+        }
+    } else {
+        for (int64_t ip = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; ip < n;
+             ip += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+            f(ip);
+        }
+    }
+}
 
 }  // namespace rrea_dev

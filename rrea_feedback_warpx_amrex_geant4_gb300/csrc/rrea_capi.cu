@@ -18,7 +18,6 @@
 #include <new>
 #include <stdexcept>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 namespace {
@@ -35,18 +34,48 @@ struct SpeciesTile {
     int64_t n = 0;
 };
 
-// A transient root: the RNG key and species of the live particle whose
-// streams a FIFO item draws from.
-struct RootKey {
-    uint64_t key;
-    int32_t species;
-    bool operator==(RootKey const& o) const { return key == o.key && species == o.species; }
-};
-struct RootHash {
-    size_t operator()(RootKey const& r) const
+// Dense slots for the transient roots (the RNG key and species of the live
+// particle whose streams a FIFO item draws from): an open-addressing table
+// filled once per drain from the initial items; children inherit their
+// item's slot, so no lookup happens after the start.
+class RootSlots {
+public:
+    explicit RootSlots(size_t expected)
     {
-        return static_cast<size_t>(r.key * 0x9e3779b97f4a7c15ULL) ^ static_cast<size_t>(r.species);
+        size_t cap = 16;
+        while (cap < 2 * expected) cap <<= 1;
+        keys_.assign(cap, 0);
+        species_.assign(cap, -1);
+        slots_.assign(cap, 0);
+        mask_ = cap - 1;
     }
+    // slot of (key, species); `fresh` is the slot a new root receives
+    uint32_t find_or_insert(uint64_t key, int32_t species, uint32_t fresh, bool& inserted)
+    {
+        uint64_t h = key ^ (static_cast<uint64_t>(static_cast<uint32_t>(species)) << 61);
+        h ^= h >> 33;
+        h *= 0xff51afd7ed558ccdULL;
+        h ^= h >> 33;
+        for (size_t i = static_cast<size_t>(h) & mask_;; i = (i + 1) & mask_) {
+            if (species_[i] < 0) {
+                keys_[i] = key;
+                species_[i] = species;
+                slots_[i] = fresh;
+                inserted = true;
+                return fresh;
+            }
+            if (keys_[i] == key && species_[i] == species) {
+                inserted = false;
+                return slots_[i];
+            }
+        }
+    }
+
+private:
+    std::vector<uint64_t> keys_;
+    std::vector<int32_t> species_;
+    std::vector<uint32_t> slots_;
+    size_t mask_ = 0;
 };
 
 }  // namespace
@@ -96,6 +125,7 @@ struct rrea_gpu_ctx {
     int* d_status = nullptr;
     long long* d_fail_index = nullptr;
     unsigned long long* d_transported = nullptr;
+    unsigned long long* d_work = nullptr;  // dynamic scheduling counter of the phase kernels
     // transient FIFO of DrainAndCommitSecondaries: the resident phases queue
     // their ordered secondaries in d_fifo[0, fifo_pending); a drain advances
     // the FIFO chunk by chunk and leaves the survivors in d_surv[0, n_surv)
@@ -279,7 +309,7 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         && dalloc(&ctx->d_diag_disp, n) == cudaSuccess && dalloc(&ctx->d_status, 1) == cudaSuccess
         && dalloc(&ctx->d_fail_index, 1) == cudaSuccess && dalloc(&ctx->d_transported, 1) == cudaSuccess
         && dalloc(&ctx->d_alive, n) == cudaSuccess && dalloc(&ctx->d_child_lineage, nsec) == cudaSuccess
-        && dalloc(&ctx->d_invalid, 1) == cudaSuccess
+        && dalloc(&ctx->d_invalid, 1) == cudaSuccess && dalloc(&ctx->d_work, 1) == cudaSuccess
         && cudaEventCreate(&ctx->ev_start) == cudaSuccess && cudaEventCreate(&ctx->ev_stop) == cudaSuccess;
     if (!ok) return bail(RREA_GPU_ERR_CUDA);
     if (cudaMemsetAsync(ctx->d_cells, 0, 5 * ncell * sizeof(double), ctx->stream) != cudaSuccess) {
@@ -331,6 +361,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     dfree(ctx->d_alive);
     dfree(ctx->d_child_lineage);
     dfree(ctx->d_invalid);
+    dfree(ctx->d_work);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -519,6 +550,10 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     }
     a.id = st.id;
     a.cpu = st.cpu;
+#ifndef RREA_STATIC_SCHEDULE
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long), ctx->stream));
+    a.work = ctx->d_work;
+#endif
     a.straight_push = (species == RREA_SPECIES_PHOTON && aliased) ? 1 : 0;
     a.segments = (species != RREA_SPECIES_PHOTON && ctx->netchord) ? ctx->d_seg : nullptr;
     if (a.n > 0) {
@@ -716,10 +751,11 @@ rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t
     rrea_gpu_status s = check_payloads(ctx->d_fifo, n_initial, 0);
     if (s != RREA_GPU_OK) return s;
 
-    // roots[k] is the root of FIFO item root_base + k (FIFO indices count
-    // every item merged since the drain began)
-    std::vector<RootKey> roots(static_cast<size_t>(n_initial));
-    std::unordered_map<RootKey, uint64_t, RootHash> next_lineage;
+    // slot[k] is the root slot of FIFO item root_base + k (FIFO indices
+    // count every item merged since the drain began); next[s] is the next
+    // free lineage of slot s
+    std::vector<uint32_t> slot(static_cast<size_t>(n_initial));
+    std::vector<uint64_t> next;
     {
         std::vector<rrea_gpu_secondary> init(static_cast<size_t>(n_initial));
         if (n_initial > 0) {
@@ -728,11 +764,21 @@ rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t
                                            cudaMemcpyDeviceToHost, ctx->stream));
             RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         }
+        RootSlots table(init.size());
         for (size_t i = 0; i < init.size(); ++i) {
-            RootKey const r{init[i].root_key, init[i].root_species};
-            roots[i] = r;
-            uint64_t& nx = next_lineage[r];
-            nx = std::max<uint64_t>(nx, init[i].lineage + 1U);
+            // the records of one parent are adjacent: reuse the previous slot
+            uint32_t s;
+            if (i > 0 && init[i].root_key == init[i - 1].root_key
+                && init[i].root_species == init[i - 1].root_species) {
+                s = slot[i - 1];
+            } else {
+                bool inserted = false;
+                s = table.find_or_insert(init[i].root_key, init[i].root_species, static_cast<uint32_t>(next.size()),
+                                         inserted);
+                if (inserted) next.push_back(0);
+            }
+            slot[i] = s;
+            next[s] = std::max<uint64_t>(next[s], init[i].lineage + 1U);
         }
     }
     std::vector<uint32_t> counts;
@@ -797,14 +843,14 @@ rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t
             for (int64_t i = 0; i < chunk; ++i) {
                 uint32_t const ci = counts[static_cast<size_t>(i)];
                 if (ci == 0) continue;
-                RootKey const r = roots[static_cast<size_t>(ctx->last_drain_items) - root_base + static_cast<size_t>(i)];
-                uint64_t& nx = next_lineage[r];
+                uint32_t const s = slot[static_cast<size_t>(ctx->last_drain_items) - root_base + static_cast<size_t>(i)];
+                uint64_t& nx = next[s];
                 for (uint32_t t = 0; t < ci; ++t) {
                     if (nx >= rrea_dev::kLineageCap || j >= lineage.size()) {
                         return fail(ctx, RREA_GPU_ERR_RNG_OVERFLOW, "transient FIFO lineage overflow");
                     }
                     lineage[j++] = nx++;
-                    roots.push_back(r);
+                    slot.push_back(s);
                 }
             }
             if (j != lineage.size()) return fail(ctx, RREA_GPU_ERR_INVALID_STATE, "newborn child count mismatch");
@@ -827,10 +873,10 @@ rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t
         }
         ctx->last_drain_items += chunk;
         cursor += chunk;
-        // roots of merged items are no longer needed
+        // slots of merged items are no longer needed
         size_t const done = static_cast<size_t>(ctx->last_drain_items) - root_base;
-        if (done > (1u << 20) && done * 2 > roots.size()) {
-            roots.erase(roots.begin(), roots.begin() + static_cast<std::ptrdiff_t>(done));
+        if (done > (1u << 20) && done * 2 > slot.size()) {
+            slot.erase(slot.begin(), slot.begin() + static_cast<std::ptrdiff_t>(done));
             root_base += done;
         }
     }
@@ -1026,6 +1072,13 @@ rrea_gpu_status rrea_gpu_last_drain_stats(rrea_gpu_ctx* ctx, int64_t* fifo_items
     if (!ctx) return RREA_GPU_ERR_ARGUMENT;
     if (fifo_items) *fifo_items = ctx->last_drain_items;
     if (survivors) *survivors = ctx->n_surv;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_kernel_launches(uint64_t* count)
+{
+    if (!count) return RREA_GPU_ERR_ARGUMENT;
+    *count = rrea_launch::launches_noted();
     return RREA_GPU_OK;
 }
 

@@ -295,6 +295,7 @@ cudaError_t netchord_deposit(rrea_dev::SegmentRec const* seg, int64_t n, rrea_de
                              int* status, long long* fail_index, int blocks, cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
+    note_launch();
     rrea_dev::netchord_deposit_kernel<<<blocks, 256, 0, stream>>>(seg, n, g, dt, status, fail_index);
     return cudaGetLastError();
 }
@@ -303,6 +304,7 @@ cudaError_t netchord_convert(rrea_dev::NetGrid const& g, double* jr_phys, double
 {
     int64_t const total = static_cast<int64_t>(g.phys_nr + 1) * g.phys_nz + static_cast<int64_t>(g.phys_nr) * (g.phys_nz + 1);
     int const blocks = static_cast<int>((total + 255) / 256);
+    note_launch();
     rrea_dev::netchord_convert_kernel<<<blocks > 0 ? blocks : 1, 256, 0, stream>>>(g, jr_phys, jz_phys);
     return cudaGetLastError();
 }

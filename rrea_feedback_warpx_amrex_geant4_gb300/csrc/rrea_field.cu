@@ -113,13 +113,25 @@ cudaError_t maxwell_step(int nr, int nz, double dr, double dz, double dt, int su
     int const nb_s = blocks_for(static_cast<int64_t>(nr + 1) * (nz + 1));
     int const nb_e = blocks_for(static_cast<int64_t>(nr + 1) * nz + static_cast<int64_t>(nr) * (nz + 1));
     bool const interior = nr > 1 && nz > 1;
-    if (interior) advance_b_kernel<<<nb_b, 256, 0, stream>>>(nr, nz, dr, dz, restagger, er, ez, bt);
+    if (interior) {
+        note_launch();
+        advance_b_kernel<<<nb_b, 256, 0, stream>>>(nr, nz, dr, dz, restagger, er, ez, bt);
+    }
     for (int k = 0; k < substeps; ++k) {
-        if (interior) advance_b_kernel<<<nb_b, 256, 0, stream>>>(nr, nz, dr, dz, dts, er, ez, bt);
+        if (interior) {
+            note_launch();
+            advance_b_kernel<<<nb_b, 256, 0, stream>>>(nr, nz, dr, dz, dts, er, ez, bt);
+        }
+        note_launch();
         silver_mueller_kernel<<<nb_s, 256, 0, stream>>>(nr, nz, er, ez, bt);
+        note_launch();
         advance_e_kernel<<<nb_e, 256, 0, stream>>>(nr, nz, dr, dz, dts, bt, jr, jz, er, ez);
     }
-    if (interior) advance_b_kernel<<<nb_b, 256, 0, stream>>>(nr, nz, dr, dz, -restagger, er, ez, bt);
+    if (interior) {
+        note_launch();
+        advance_b_kernel<<<nb_b, 256, 0, stream>>>(nr, nz, dr, dz, -restagger, er, ez, bt);
+    }
+    note_launch();
     silver_mueller_kernel<<<nb_s, 256, 0, stream>>>(nr, nz, er, ez, bt);
     return cudaGetLastError();
 }

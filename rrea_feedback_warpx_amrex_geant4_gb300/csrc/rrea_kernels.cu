@@ -8,6 +8,8 @@
 //                         deterministic order (parent index, then lineage)
 #include "rrea_kernels.h"
 
+#include <atomic>
+
 #include "device/rrea_electron.cuh"
 
 #include <cuda_runtime.h>
@@ -47,15 +49,14 @@ __device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
 {
     StepConstants const& C = c_step;
     unsigned int moved = 0;
-    for (int64_t ip = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; ip < A.n;
-         ip += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    for_each_particle(A.n, A.work, [&](int64_t ip) {
         if (!(A.id[ip] > 0)) {
             if (A.segments) A.segments[ip].kind = 0;
             if (A.sec_per_parent) A.sec_per_parent[ip] = 0;
             if (A.diag_disposition) A.diag_disposition[ip] = -1;
             if (A.diag_subcycles) A.diag_subcycles[ip] = 0;
             if (A.diag_events) A.diag_events[ip] = 0;
-            continue;
+            return;
         }
         Err err;
         uint64_t sub = 0, ev = 0;
@@ -70,7 +71,7 @@ __device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
         if (A.diag_disposition) A.diag_disposition[ip] = disp;
         if (A.diag_subcycles) A.diag_subcycles[ip] = sub;
         if (A.diag_events) A.diag_events[ip] = ev;
-    }
+    });
     // warp-aggregated count of transported particles
     unsigned int const warp_total = __reduce_add_sync(0xffffffffu, moved);
     if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(A.transported, static_cast<unsigned long long>(warp_total));
@@ -181,6 +182,14 @@ __global__ void scatter_secondaries(const rrea_gpu_secondary* __restrict__ in, i
 
 namespace rrea_launch {
 
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launches_noted() { return g_launches.load(std::memory_order_relaxed); }
+
+
 cudaError_t set_step_constants(rrea_dev::StepConstants const& c, cudaStream_t stream)
 {
     return cudaMemcpyToSymbolAsync(rrea_dev::c_step, &c, sizeof(c), 0, cudaMemcpyHostToDevice, stream);
@@ -192,6 +201,7 @@ cudaError_t field_prep(int nr, int nz, const double* er, const double* ez, const
     int64_t const total = static_cast<int64_t>(nr) * nz;
     int const threads = 256;
     int const blocks = static_cast<int>((total + threads - 1) / threads);
+    note_launch();
     rrea_dev::field_prep_kernel<<<blocks > 0 ? blocks : 1, threads, 0, stream>>>(nr, nz, er, ez, amb_er, amb_ez,
                                                                                   cell_er, cell_ez);
     return cudaGetLastError();
@@ -200,6 +210,7 @@ cudaError_t field_prep(int nr, int nz, const double* er, const double* ez, const
 cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, int min_blocks, bool periodic,
                           cudaStream_t stream)
 {
+    note_launch();
     if (periodic) {
         rrea_dev::electron_step_kernel<16, RREA_ARENA_MAX_PIECES><<<blocks, threads, 0, stream>>>(args);
         return cudaGetLastError();
@@ -217,6 +228,7 @@ cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
 cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, bool periodic,
                           cudaStream_t stream)
 {
+    note_launch();
     if (periodic) {
         rrea_dev::positron_step_kernel<16, RREA_ARENA_MAX_PIECES><<<blocks, threads, 0, stream>>>(args);
     } else {
@@ -228,6 +240,7 @@ cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
 cudaError_t count_live(const int64_t* id, int64_t n, unsigned long long* out, int blocks, cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
+    note_launch();
     rrea_dev::count_live_kernel<<<blocks, 256, 0, stream>>>(id, n, out);
     return cudaGetLastError();
 }
@@ -238,6 +251,7 @@ cudaError_t exclusive_scan_counts(const uint32_t* counts, int64_t n, int64_t* of
                                   cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
+    for (int k = 0; k < 3; ++k) note_launch();
     int64_t const nblocks = (n + rrea_dev::kScanBlock - 1) / rrea_dev::kScanBlock;
     rrea_dev::scan_block_sums<<<static_cast<unsigned>(nblocks), rrea_dev::kScanBlock, 0, stream>>>(counts, n,
                                                                                                   block_scratch);
@@ -252,13 +266,10 @@ cudaError_t order_secondaries(const uint32_t* counts, int64_t n, int64_t* offset
                               cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
-    int64_t const nblocks = (n + rrea_dev::kScanBlock - 1) / rrea_dev::kScanBlock;
-    rrea_dev::scan_block_sums<<<static_cast<unsigned>(nblocks), rrea_dev::kScanBlock, 0, stream>>>(counts, n,
-                                                                                                  block_scratch);
-    rrea_dev::scan_block_offsets<<<1, rrea_dev::kScanBlock, 0, stream>>>(block_scratch, nblocks);
-    rrea_dev::scan_apply<<<static_cast<unsigned>(nblocks), rrea_dev::kScanBlock, 0, stream>>>(counts, n, block_scratch,
-                                                                                             offsets);
+    cudaError_t const e = exclusive_scan_counts(counts, n, offsets, block_scratch, stream);
+    if (e != cudaSuccess) return e;
     if (count > 0) {
+        note_launch();
         int const threads = 256;
         int64_t const blocks = (count + threads - 1) / threads;
         rrea_dev::scatter_secondaries<<<static_cast<unsigned>(blocks < 65535 ? blocks : 65535), threads, 0, stream>>>(

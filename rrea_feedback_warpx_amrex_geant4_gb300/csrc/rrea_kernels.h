@@ -13,6 +13,11 @@ struct NetGrid;
 
 namespace rrea_launch {
 
+// Every kernel launch of the library is noted here (a process-wide atomic
+// counter), so the count rrea_gpu_kernel_launches reports is exact.
+void note_launch();
+unsigned long long launches_noted();
+
 cudaError_t set_step_constants(rrea_dev::StepConstants const& c, cudaStream_t stream);
 cudaError_t field_prep(int nr, int nz, const double* er, const double* ez, const double* amb_er, const double* amb_ez,
                        double* cell_er, double* cell_ez, cudaStream_t stream);

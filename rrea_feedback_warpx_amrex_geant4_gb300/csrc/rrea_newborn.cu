@@ -10,10 +10,17 @@
 namespace rrea_dev {
 namespace {
 
+// Resident blocks of 128 threads per SM the newborn kernels are compiled
+// for.  A drain holds few items, each a long dependent chain, so the goal is
+// one wave with the fewest spills, not full residency.
+#ifndef RREA_NEWBORN_MIN_BLOCKS
+#define RREA_NEWBORN_MIN_BLOCKS 8
+#endif
+
 // SPECIES 1 positron, 2 photon, 0 every other species id (the reference
 // advances anything that is not a photon or a positron as an electron).
 template <int NP, int SPECIES>
-__global__ void __launch_bounds__(128) newborn_kernel(ElectronArgs A, rrea_gpu_secondary* __restrict__ items,
+__global__ void __launch_bounds__(128, RREA_NEWBORN_MIN_BLOCKS) newborn_kernel(ElectronArgs A, rrea_gpu_secondary* __restrict__ items,
                                                       int64_t n, uint32_t* __restrict__ alive)
 {
     StepConstants const& C = c_step;
@@ -135,6 +142,7 @@ cudaError_t validate_fifo(const rrea_gpu_secondary* items, int64_t n, int mode, 
                           long long* first, cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
+    note_launch();
     rrea_dev::validate_fifo_kernel<<<rrea_dev::grid_for(n, 65535), 128, 0, stream>>>(items, n, mode, invalid, first);
     return cudaGetLastError();
 }
@@ -145,6 +153,7 @@ cudaError_t newborn_step(rrea_dev::ElectronArgs const& args, rrea_gpu_secondary*
     using namespace rrea_dev;
     if (n <= 0) return cudaSuccess;
     int const blocks = grid_for(n, max_blocks);
+    for (int k = 0; k < 3; ++k) note_launch();
     if (periodic) {
         newborn_kernel<4, 0><<<blocks, 128, 0, stream>>>(args, items, n, alive);
         newborn_kernel<4, 1><<<blocks, 128, 0, stream>>>(args, items, n, alive);
@@ -161,6 +170,7 @@ cudaError_t compact_survivors(const rrea_gpu_secondary* items, const uint32_t* a
                               int64_t n, rrea_gpu_secondary* out, cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
+    note_launch();
     rrea_dev::compact_survivors_kernel<<<rrea_dev::grid_for(n, 65535), 128, 0, stream>>>(items, alive, offsets, n,
                                                                                           out);
     return cudaGetLastError();
@@ -170,6 +180,7 @@ cudaError_t adopt_children(const rrea_gpu_secondary* ordered, int64_t n, const r
                            const uint64_t* lineage, rrea_gpu_secondary* out, cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
+    note_launch();
     rrea_dev::adopt_children_kernel<<<rrea_dev::grid_for(n, 65535), 128, 0, stream>>>(ordered, n, items, lineage,
                                                                                        out);
     return cudaGetLastError();

@@ -148,6 +148,7 @@ extern "C" rrea_gpu_status rrea_gpu_order_secondaries_noalloc(const uint32_t* d_
         int64_t blocks = (n_secondaries + threads - 1) / threads;
         if (blocks < 1) blocks = 1;
         if (blocks > 65535) blocks = 65535;
+        rrea_launch::note_launch();
         scatter_checked_kernel<<<static_cast<unsigned>(blocks), threads, 0, s>>>(
             d_unordered, n_secondaries, d_counts, n_parents, offsets, d_ordered, err_word);
         e = cudaGetLastError();

@@ -16,14 +16,13 @@ __global__ void __launch_bounds__(128, 2) photon_step_kernel(ElectronArgs A)
 {
     StepConstants const& C = c_step_photon;
     unsigned int moved = 0;
-    for (int64_t ip = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; ip < A.n;
-         ip += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    for_each_particle(A.n, A.work, [&](int64_t ip) {
         if (!(A.id[ip] > 0)) {
             if (A.sec_per_parent) A.sec_per_parent[ip] = 0;
             if (A.diag_disposition) A.diag_disposition[ip] = -1;
             if (A.diag_subcycles) A.diag_subcycles[ip] = 0;
             if (A.diag_events) A.diag_events[ip] = 0;
-            continue;
+            return;
         }
         Err err;
         uint64_t ev = 0;
@@ -36,7 +35,7 @@ __global__ void __launch_bounds__(128, 2) photon_step_kernel(ElectronArgs A)
         if (A.diag_disposition) A.diag_disposition[ip] = disp;
         if (A.diag_subcycles) A.diag_subcycles[ip] = 0;
         if (A.diag_events) A.diag_events[ip] = ev;
-    }
+    });
     unsigned int const warp_total = __reduce_add_sync(0xffffffffu, moved);
     if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(A.transported, static_cast<unsigned long long>(warp_total));
 }
@@ -51,6 +50,7 @@ cudaError_t photon_step(rrea_dev::StepConstants const& sc, rrea_dev::ElectronArg
     cudaError_t const e = cudaMemcpyToSymbolAsync(rrea_dev::c_step_photon, &sc, sizeof(sc), 0, cudaMemcpyHostToDevice,
                                                   stream);
     if (e != cudaSuccess) return e;
+    rrea_launch::note_launch();
     if (periodic) {
         rrea_dev::photon_step_kernel<RREA_ARENA_MAX_PIECES><<<blocks, threads, 0, stream>>>(args);
     } else {

@@ -75,7 +75,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_download_current_index", "rrea_gpu_advance_field", "rrea_gpu_download_field",
     "rrea_gpu_count_live", "rrea_gpu_population_projection", "rrea_gpu_drain_secondaries",
     "rrea_gpu_drain_resident", "rrea_gpu_fetch_survivors", "rrea_gpu_pending_secondaries",
-    "rrea_gpu_last_drain_stats",
+    "rrea_gpu_last_drain_stats", "rrea_gpu_kernel_launches",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -130,6 +130,7 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_fetch_survivors.argtypes = [vp, vp, ctypes.c_int64, _i64p]
     lib.rrea_gpu_pending_secondaries.argtypes = [vp, _i64p, ctypes.c_int32]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
+    lib.rrea_gpu_kernel_launches.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
     lib.rrea_gpu_reset_current.argtypes = [vp]
     lib.rrea_gpu_download_current.argtypes = [vp, _D, _D]
     lib.rrea_gpu_download_current_index.argtypes = [vp, _D, _D, _D]
@@ -153,6 +154,15 @@ def load_library(path=LIB_PATH):
             fn.restype = ctypes.c_int
     _lib = lib
     return lib
+
+
+def kernel_launches():
+    """Kernels the library has launched in this process."""
+    n = ctypes.c_uint64()
+    status = load_library().rrea_gpu_kernel_launches(ctypes.byref(n))
+    if status != 0:
+        raise RreaGpuError(status, "kernel launch count")
+    return n.value
 
 
 def default_config(**overrides):
