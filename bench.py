@@ -257,7 +257,7 @@ def run_reference(args, rank, world):
 def run_gb300(args, rank, world, local):
     import torch
 
-    from rrea_feedback_warpx_amrex_geant4_gb300 import DEFAULT_TABLES, gpu, workloads
+    from rrea_feedback_warpx_amrex_geant4_gb300 import DEFAULT_TABLES, distributed, gpu, workloads
 
     torch.cuda.set_device(local)
     dist = None
@@ -302,7 +302,8 @@ def run_gb300(args, rank, world, local):
         tp, _, kmp = ctx.last_step_stats()
         ctx.drain_resident(step, DT_S)  # newborn residual legs of every secondary
         items, surv = ctx.last_drain_stats()
-        ctx.advance_field(DT_S, FIELD_SUBSTEPS)  # Maxwell TM-RZ with this step's J
+        # Maxwell TM-RZ with this step's J, summed over the ranks' shards
+        distributed.exchange_current_and_advance(ctx, dist, DT_S, FIELD_SUBSTEPS)
         return {"te": te, "tg": tg, "tp": tp, "kme": kme, "kmg": kmg, "kmp": kmp,
                 "secondaries": ne + ng + npos, "fifo_items": items, "survivors": surv}
 
@@ -339,14 +340,7 @@ def run_gb300(args, rank, world, local):
 
     # max over ranks of the device time; total work summed
     moved = moved_e + moved_g + moved_p
-    t_local = torch.tensor([total_ms, float(moved)], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        tmax = t_local.clone()
-        dist.all_reduce(tmax[0:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(tmax[1:2], op=dist.ReduceOp.SUM)
-        t_local = tmax
-    total_ms_max = float(t_local[0])
-    moved_all = float(t_local[1])
+    total_ms_max, moved_all = distributed.reduce_step_time(total_ms, moved, dist, "cuda")
     value = moved_all / (total_ms_max / 1000.0)
 
     # ---- e2e through the drop-in C-ABI (host buffers, copies in the timed region)
@@ -375,7 +369,7 @@ def run_gb300(args, rank, world, local):
         sec_p = ctx.apply_positrons(pp, step, DT_S, want_secondaries=True)
         pending = np.concatenate([sec_e, sec_g, sec_p])
         surv = ctx.drain_secondaries(pending, step, DT_S)
-        ctx.advance_field(DT_S, FIELD_SUBSTEPS)
+        distributed.exchange_current_and_advance(ctx, dist, DT_S, FIELD_SUBSTEPS)
         return len(pending), len(surv)
 
     e2e_moved = 0
@@ -432,7 +426,7 @@ def run_gb300(args, rank, world, local):
                     "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
                     "path": "rrea_gpu_apply_electrons/_photons/_positrons (pinned host tiles -> HBM -> host), "
                             "rrea_gpu_drain_secondaries (host records in, survivors out), "
-                            "rrea_gpu_advance_field"},
+                            "rrea_gpu_current_device + rrea_gpu_advance_field_from_current"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic, "kernel": "electron_step_kernel",

@@ -194,6 +194,20 @@ rrea_gpu_status rrea_gpu_advance_field(rrea_gpu_ctx* ctx, double dt_s, int32_t s
 rrea_gpu_status rrea_gpu_download_field(rrea_gpu_ctx* ctx, double* er, double* ez, double* btheta);
 
 /*
+ * The field update of a sharded run, in two halves around the caller's
+ * allreduce of the face current (the only exchange of the path;
+ * RreaWarpXCoupling.cpp:715-717, RreaAmrexAdvance.cpp:870-871).
+ * current_device converts the step's net-chord current to the physical
+ * face currents and returns their device vectors on the context's device
+ * (Jr: (nr+1)*nz doubles, Jz: nr*(nz+1), layouts as download_current); the
+ * caller sums them across ranks in place.  advance_field_from_current then
+ * runs the Maxwell update of advance_field on those vectors as they stand.
+ * advance_field is current_device followed by advance_field_from_current.
+ */
+rrea_gpu_status rrea_gpu_current_device(rrea_gpu_ctx* ctx, double** d_jr, double** d_jz);
+rrea_gpu_status rrea_gpu_advance_field_from_current(rrea_gpu_ctx* ctx, double dt_s, int32_t substeps);
+
+/*
  * Population ceiling (RreaWarpXCoupling::EnforcePopulationCeiling,
  * RreaCouplingPopulation.cpp:100-146).  count_live counts the valid
  * (id > 0) particles of the context's resident tile of `species`.

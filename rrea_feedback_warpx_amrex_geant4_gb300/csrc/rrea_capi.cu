@@ -970,7 +970,25 @@ rrea_gpu_status rrea_gpu_download_current_index(rrea_gpu_ctx* ctx, double* rho, 
     return RREA_GPU_OK;
 }
 
+rrea_gpu_status rrea_gpu_current_device(rrea_gpu_ctx* ctx, double** d_jr, double** d_jz)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->netchord) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "the net-chord current needs a non-periodic z domain");
+    RREA_CUDA(ctx, rrea_launch::netchord_convert(ctx->net, ctx->d_jr_phys, ctx->d_jz_phys, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (d_jr) *d_jr = ctx->d_jr_phys;
+    if (d_jz) *d_jz = ctx->d_jz_phys;
+    return RREA_GPU_OK;
+}
+
 rrea_gpu_status rrea_gpu_advance_field(rrea_gpu_ctx* ctx, double dt_s, int32_t substeps)
+{
+    rrea_gpu_status const s = rrea_gpu_current_device(ctx, nullptr, nullptr);
+    if (s != RREA_GPU_OK) return s;
+    return rrea_gpu_advance_field_from_current(ctx, dt_s, substeps);
+}
+
+rrea_gpu_status rrea_gpu_advance_field_from_current(rrea_gpu_ctx* ctx, double dt_s, int32_t substeps)
 {
     if (!ctx || !(dt_s > 0.0) || !std::isfinite(dt_s) || substeps < 1) return RREA_GPU_ERR_ARGUMENT;
     if (!ctx->field_set) return fail(ctx, RREA_GPU_ERR_NOT_READY, "the field must be set before it is advanced");
@@ -981,7 +999,6 @@ rrea_gpu_status rrea_gpu_advance_field(rrea_gpu_ctx* ctx, double dt_s, int32_t s
     if (!std::isfinite(cfl) || !(cfl < 1.0)) {
         return fail(ctx, RREA_GPU_ERR_ARGUMENT, "Maxwell TM violates the Yee CFL condition c dt sqrt(dr^-2+dz^-2) < 1");
     }
-    RREA_CUDA(ctx, rrea_launch::netchord_convert(g, ctx->d_jr_phys, ctx->d_jz_phys, ctx->stream));
     RREA_CUDA(ctx, rrea_launch::maxwell_step(c.nr, c.nz, g.dr, g.dz, dt_s, substeps, ctx->d_er, ctx->d_ez, ctx->d_bt,
                                              ctx->d_jr_phys, ctx->d_jz_phys, ctx->stream));
     RREA_CUDA(ctx, rrea_launch::field_prep(c.nr, c.nz, ctx->d_er, ctx->d_ez, ctx->d_amb_er, ctx->d_amb_ez,

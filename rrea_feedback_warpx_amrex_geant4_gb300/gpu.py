@@ -75,7 +75,8 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_download_current_index", "rrea_gpu_advance_field", "rrea_gpu_download_field",
     "rrea_gpu_count_live", "rrea_gpu_population_projection", "rrea_gpu_drain_secondaries",
     "rrea_gpu_drain_resident", "rrea_gpu_fetch_survivors", "rrea_gpu_pending_secondaries",
-    "rrea_gpu_last_drain_stats", "rrea_gpu_kernel_launches",
+    "rrea_gpu_last_drain_stats", "rrea_gpu_kernel_launches", "rrea_gpu_current_device",
+    "rrea_gpu_advance_field_from_current",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -131,6 +132,8 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_pending_secondaries.argtypes = [vp, _i64p, ctypes.c_int32]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
     lib.rrea_gpu_kernel_launches.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
+    lib.rrea_gpu_current_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    lib.rrea_gpu_advance_field_from_current.argtypes = [vp, ctypes.c_double, ctypes.c_int32]
     lib.rrea_gpu_reset_current.argtypes = [vp]
     lib.rrea_gpu_download_current.argtypes = [vp, _D, _D]
     lib.rrea_gpu_download_current_index.argtypes = [vp, _D, _D, _D]
@@ -339,6 +342,17 @@ class RreaGpuContext:
 
     def advance_field(self, dt_s, substeps=1):
         self._check(self.lib.rrea_gpu_advance_field(self.handle, float(dt_s), int(substeps)))
+
+    def current_device(self):
+        """Converts the step's current and returns the device addresses and
+        lengths of the physical face currents: ((jr_ptr, n_jr), (jz_ptr, n_jz))."""
+        jr, jz = ctypes.c_void_p(), ctypes.c_void_p()
+        self._check(self.lib.rrea_gpu_current_device(self.handle, ctypes.byref(jr), ctypes.byref(jz)))
+        c = self.config
+        return (jr.value, (c.nr + 1) * c.nz), (jz.value, c.nr * (c.nz + 1))
+
+    def advance_field_from_current(self, dt_s, substeps=1):
+        self._check(self.lib.rrea_gpu_advance_field_from_current(self.handle, float(dt_s), int(substeps)))
 
     def field(self):
         """Scattered field vectors (er, ez, bt), flat, layouts as set_field."""

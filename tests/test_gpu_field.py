@@ -69,3 +69,39 @@ def test_field_step_refuses_cfl_violation(mods):
     assert e.value.status == 1
     ctx.advance_field(5.0e-10, 1)
     ctx.close()
+
+
+def test_split_field_update_with_scaled_current(mods):
+    """The sharded-run halves (rrea_gpu_current_device, then
+    rrea_gpu_advance_field_from_current) on the device vectors viewed by torch:
+    doubling the current in place, as an allreduce over two identical ranks
+    would, gives the field of the doubled current."""
+    import torch
+
+    from rrea_feedback_warpx_amrex_geant4_gb300 import distributed
+
+    gpu, workloads, oracle = mods
+    case, n, substeps, dt = "uniform_c0", 4096, 2, 5.0e-10
+    cfg = workloads.make_config(gpu, case)
+    ctx = gpu.RreaGpuContext(cfg, n)
+    ctx.load_tables(TABLES)
+    ctx.set_field(**workloads.make_field(case))
+    ctx.reset_current()
+    ctx.apply_electrons(workloads.make_electrons(case, n, seed=5), 0, dt)
+    jr, jz = ctx.current()
+    (jr_ptr, n_jr), (jz_ptr, n_jz) = ctx.current_device()
+    vr, vz = distributed.device_view(jr_ptr, n_jr), distributed.device_view(jz_ptr, n_jz)
+    np.testing.assert_array_equal(vr.cpu().numpy(), jr.ravel())
+    np.testing.assert_array_equal(vz.cpu().numpy(), jz.ravel())
+    vr.mul_(2.0)
+    vz.mul_(2.0)
+    torch.cuda.synchronize()
+    before = ctx.field()
+    ctx.advance_field_from_current(dt, substeps)
+    after = ctx.field()
+    ref = oracle.advance_maxwell(cfg.nr, cfg.nz, cfg.r_hi / cfg.nr, cfg.z_hi / cfg.nz, dt, substeps, *before,
+                                 2.0 * jr.ravel(), 2.0 * jz.ravel())
+    for name, g, o in zip(("er", "ez", "bt"), after, ref):
+        scale = max(np.abs(o).max(), 1e-300)
+        np.testing.assert_allclose(g, o, rtol=0, atol=1e-12 * scale, err_msg=name)
+    ctx.close()
