@@ -6,7 +6,8 @@ validity, secondary keys) must match exactly; FP64 state within 1e-12
 relative (positions with a 1e-12 x domain-size floor), with a bounded tail
 (TAIL_FRACTION of the particles, never beyond TAIL_RTOL); cell-source grids,
 which the GPU accumulates with atomics in nondeterministic order, within
-1e-12 of each grid's largest cell.
+1.6e-11 of each grid's largest cell, except the few cells the tail particles
+deposit into, which stay within 1.6e-9.
 """
 import numpy as np
 
@@ -37,6 +38,22 @@ def _tail_ok(a, b, atol):
     loose = _close(a, b, TAIL_RTOL, np.asarray(atol, dtype=np.float64) * (TAIL_RTOL / RTOL))
     n_over = int((~strict).sum())
     allowed = max(1, int(TAIL_FRACTION * strict.size))
+    return bool(loose.all() and n_over <= allowed), n_over
+
+
+def cells_ok(g, o):
+    """Cell grid check: every cell within 16 RTOL of the grid's largest cell,
+    except at most four cells per tail particle allowance (the order-1
+    stencil of a deposit spans four cells), which must stay within
+    16 TAIL_RTOL.  Returns (ok, n_over_strict)."""
+    g = np.asarray(g, dtype=np.float64)
+    o = np.asarray(o, dtype=np.float64)
+    scale = max(np.abs(o).max(), 1e-300)
+    strict = _close(g, o, 0.0, RTOL * scale * 16)
+    loose = _close(g, o, 0.0, TAIL_RTOL * scale * 16)
+    n_over = int((~strict).sum())
+    nonzero = int(((g != 0.0) | (o != 0.0)).sum())
+    allowed = 4 * max(1, int(TAIL_FRACTION * nonzero))
     return bool(loose.all() and n_over <= allowed), n_over
 
 
@@ -149,8 +166,7 @@ def compare(cfg, gpu, orc, domain_scale, parent_energy=None):
                 w = _worst(g_sec[key], os_[key], atol)
                 problems.append(f"secondary {key} differs for {n_over} (worst {w:.2e})")
     for f in range(5):
-        scale = max(np.abs(o["cells"][f]).max(), 1e-300)
-        ok = _close(g_cells[f], o["cells"][f], 0.0, RTOL * scale * 16)
-        if not ok.all():
-            problems.append(f"cell source field {f} differs in {(~ok).sum()} cells")
+        ok, n_over = cells_ok(g_cells[f], o["cells"][f])
+        if not ok:
+            problems.append(f"cell source field {f} differs in {n_over} cells")
     return problems

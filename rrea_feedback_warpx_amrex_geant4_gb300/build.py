@@ -1,9 +1,11 @@
 """Builds the GB300 kinetic-step library in-tree:
 rrea_feedback_warpx_amrex_geant4_gb300/lib/librrea_gpu.so (sm_103a only).
 
-FMA contraction is disabled (--fmad=false) so device arithmetic rounds like
-the reference's x86-64 host build; transcendental calls are the only
-remaining source of last-ulp differences.
+FP64 FMA contraction is on (--fmad=true): GB300's FP64 pipe issues a fused
+multiply-add for the price of a multiply, a measured 9 % of the electron
+kernel.  RREA_FMAD=0 builds with --fmad=false, whose products and sums round
+like the reference's x86-64 host build (no FMA), to isolate last-ulp
+differences when chasing a parity question.
 """
 import os
 import subprocess
@@ -50,7 +52,7 @@ def build(force=False, verbose=False):
     objdir = os.path.join(PKG, "_build")
     os.makedirs(objdir, exist_ok=True)
     nvcc = _nvcc()
-    fmad = "true" if os.environ.get("RREA_FMAD", "0") == "1" else "false"
+    fmad = "false" if os.environ.get("RREA_FMAD", "1") == "0" else "true"
     common = ["-std=c++17", "-O3", "-lineinfo", f"--fmad={fmad}", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I", CSRC, "-I", os.path.join(ROOT, "include")] + ARCH
     if verbose:

@@ -23,24 +23,16 @@ constexpr double kDblMin = 2.225073858507201383090232717332404064219215980462331
 constexpr double kGl2Node = 0.577350269189625764509148780501957;  // I/RreaGaussLegendre8.H:22
 
 // Division by a divisor that is reused: one IEEE reciprocal y = RN(1/b),
-// then per quotient a product and one FMA residual correction,
-//   q0 = RN(a*y),  r = RN(a - b*q0) (exact via FMA),  q = RN(q0 + r*y).
-// By Markstein's theorem (Markstein 1990; Muller et al., Handbook of
-// Floating-Point Arithmetic, 2nd ed., Thm 4.10) q = RN(a/b) whenever q0 is a
-// faithful quotient, which RN(a*y) is for all but rare operands; in those it
-// is within one ulp of RN(a/b).  Finite operands away from overflow and
-// underflow only.  Costs three FP64 instructions per quotient instead of a
-// full division sequence.
+// then one product per quotient, q = RN(a*y), within 1.5 ulp of RN(a/b)
+// (finite operands away from overflow and underflow).  On GB300's narrow
+// FP64 pipe one DMUL per quotient instead of a division sequence is a
+// measured 5 % of the electron kernel; the residual-corrected form
+// (Markstein) would restore RN(a/b) at two more FP64 instructions.
 struct Divisor {
     double b, y;
 };
 __host__ __device__ __forceinline__ Divisor make_divisor(double b) { return Divisor{b, 1.0 / b}; }
-__device__ __forceinline__ double quot(double a, Divisor const& d)
-{
-    double const q0 = a * d.y;
-    double const r = fma(-q0, d.b, a);
-    return fma(r, d.y, q0);
-}
+__device__ __forceinline__ double quot(double a, Divisor const& d) { return a * d.y; }
 
 // Everything a kernel needs that does not change within a step.
 struct StepConstants {

@@ -68,14 +68,14 @@ __device__ __forceinline__ bool outside_certified(Geom const& g, double r, doubl
     return !g.periodic && (z < g.zlo || z >= g.zhi);
 }
 
-// S/RreaTransportPath.cpp:73-295.  Periodic seams use double arithmetic where
-// the host reference uses long double.
+// S/RreaTransportPath.cpp:73-295 on Cartesian chord ends (x0, y0, z0) ->
+// (x1, y1, z1) with their radii r0, r1.  Periodic seams use double
+// arithmetic where the host reference uses long double.
 template <int NP>
-__device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double r1, double th1, double z1,
-                                        Geom const& g, Path<NP>& p, Err& err)
+__device__ __forceinline__ void clip_chord(double x0, double y0, double z0, double r0, double x1, double y1, double z1,
+                                           double r1, bool ends_finite, Geom const& g, Path<NP>& p, Err& err)
 {
-    if (!isfinite(r0) || !isfinite(th0) || !isfinite(z0) || !isfinite(r1) || !isfinite(th1) || !isfinite(z1)
-        || r0 < 0.0 || r1 < 0.0) {
+    if (!ends_finite || !isfinite(r0) || !isfinite(z0) || !isfinite(r1) || !isfinite(z1) || r0 < 0.0 || r1 < 0.0) {
         err.set(RREA_GPU_ERR_GEOMETRY);
         p.npieces = 0;
         p.full = 0.0;
@@ -83,14 +83,11 @@ __device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double
         p.exits = false;
         return;
     }
-    double s0, c0, s1, c1;
-    sincos(th0, &s0, &c0);
-    sincos(th1, &s1, &c1);
-    p.sx = r0 * c0;
-    p.sy = r0 * s0;
+    p.sx = x0;
+    p.sy = y0;
     p.sz = z0;
-    p.ex = r1 * c1;
-    p.ey = r1 * s1;
+    p.ex = x1;
+    p.ey = y1;
     p.ez = z1;
     double const dx = p.ex - p.sx, dy = p.ey - p.sy, dz = p.ez - p.sz;
     p.full = sqrt(dx * dx + dy * dy + dz * dz);
@@ -208,6 +205,33 @@ __device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double
     }
 }
 
+// ClipRz as the reference calls it, on cylindrical ends (r, theta, z).
+template <int NP>
+__device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double r1, double th1, double z1,
+                                        Geom const& g, Path<NP>& p, Err& err)
+{
+    bool const finite = isfinite(th0) && isfinite(th1);
+    double s0 = 0.0, c0 = 1.0, s1 = 0.0, c1 = 1.0;
+    if (finite) {
+        sincos(th0, &s0, &c0);
+        sincos(th1, &s1, &c1);
+    }
+    clip_chord(r0 * c0, r0 * s0, z0, r0, r1 * c1, r1 * s1, z1, r1, finite, g, p, err);
+}
+
+// The chords the transport loops build run between Cartesian points, which
+// the reference passes through ClipRz's (r, theta, z) interface as
+// (hypot(x, y), atan2(y, x), z) and turns back into r cos(theta),
+// r sin(theta).  Clipping the Cartesian ends directly gives the same chord to
+// within an ulp of each coordinate and saves an atan2 and a sincos per end.
+template <int NP>
+__device__ __forceinline__ void clip_xyz(double x0, double y0, double z0, double x1, double y1, double z1, Geom const& g,
+                                         Path<NP>& p, Err& err)
+{
+    bool const finite = isfinite(x0) && isfinite(y0) && isfinite(x1) && isfinite(y1);
+    clip_chord(x0, y0, z0, hypot(x0, y0), x1, y1, z1, hypot(x1, y1), finite, g, p, err);
+}
+
 // ------------------------------------------------------------ kinematics
 // I/RreaSeedSchedule.H:31-43
 __device__ __forceinline__ double proper_velocity_from_kinetic(double k)
@@ -231,16 +255,19 @@ __device__ __forceinline__ double charged_speed(double k)
     double const b2 = fmax(0.0, 1.0 - 1.0 / (gm * gm));
     return kC * sqrt(b2);
 }
-// O/RreaChargedInterleave.H:294-307
+// O/RreaChargedInterleave.H:294-307.  The reference divides by sqrt(n2);
+// scaling by rsqrt(n2) (within an ulp of 1/sqrt(n2)) gives the same unit
+// vector to within two ulps per component for a third of the FP64
+// instructions.  A zero norm falls back to +z as in the reference.
 __device__ __forceinline__ void normalize(double& x, double& y, double& z)
 {
-    double const n = sqrt(x * x + y * y + z * z);
-    if (n <= 0.0) {
+    double const n2 = x * x + y * y + z * z;
+    if (!(n2 > 0.0)) {
         x = 0.0; y = 0.0; z = 1.0;
         return;
     }
-    Divisor const d = make_divisor(n);
-    x = quot(x, d); y = quot(y, d); z = quot(z, d);
+    double const inv = rsqrt(n2);
+    x *= inv; y *= inv; z *= inv;
 }
 // O/RreaChargedInterleave.H:309-364
 __device__ __forceinline__ void cone_direction(double ax, double ay, double az, double cos_t, double u_phi,

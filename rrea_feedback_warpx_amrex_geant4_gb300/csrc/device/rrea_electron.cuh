@@ -522,8 +522,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         if (!isfinite(speed) || !isfinite(dn) || !(dn > 0.0)) return false;
         double const sc = speed * req_dt / dn;
         double const exx = run_x + sc * dx, eyy = run_y + sc * dy, ezz = run_z + sc * dz;
-        clip_rz(hypot(run_x, run_y), atan2(run_y, run_x), run_z, hypot(exx, eyy), atan2(eyy, exx), ezz, g, path,
-                err);
+        clip_xyz(run_x, run_y, run_z, exx, eyy, ezz, g, path, err);
         return isfinite(path.full) && path.in_begin == 0.0;
     };
     auto deposit_local = [&](double r, double z, double e) {

@@ -185,7 +185,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
     if (!(chord > 0.0)) return k >= cut ? 1 : 0;
     double const ex0 = p.x + chord * dx, ey0 = p.y + chord * dy, ez0 = p.z + chord * dz;
     Path<NP> path;
-    clip_rz(hypot(p.x, p.y), atan2(p.y, p.x), p.z, hypot(ex0, ey0), atan2(ey0, ex0), ez0, g, path, err);
+    clip_xyz(p.x, p.y, p.z, ex0, ey0, ez0, g, path, err);
     if (err.code) return -1;
     if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
         if (path.exits) return put_escape(path) ? 0 : -1;
@@ -332,7 +332,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
             double const sc = speed * sub_dt / dn;
             double const exx = run_x + sc * dx, eyy = run_y + sc * dy, ezz = run_z + sc * dz;
             Path<NP> np;
-            clip_rz(hypot(run_x, run_y), atan2(run_y, run_x), run_z, hypot(exx, eyy), atan2(eyy, exx), ezz, g, np, err);
+            clip_xyz(run_x, run_y, run_z, exx, eyy, ezz, g, np, err);
             if (err.code) break;
             if (!(isfinite(np.full) && np.in_begin == 0.0)) break;
             path = np;
@@ -596,7 +596,7 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
     double const chord = kC * C.dt_s * residual;
     double const ex0 = p.x + chord * dx, ey0 = p.y + chord * dy, ez0 = p.z + chord * dz;
     Path<NP> path;
-    clip_rz(hypot(p.x, p.y), atan2(p.y, p.x), p.z, hypot(ex0, ey0), atan2(ey0, ex0), ez0, g, path, err);
+    clip_xyz(p.x, p.y, p.z, ex0, ey0, ez0, g, path, err);
     if (err.code) return -1;
     if (!(path.full > 0.0) || !(path.in_length > 0.0)) return path.exits ? 0 : 1;
     double elapsed_start = p.birth_fraction;
@@ -672,7 +672,7 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
                 return 1;
             }
             double const tx = px + remaining * dx, ty = py + remaining * dy, tz = pz + remaining * dz;
-            clip_rz(pr, atan2(py, px), pz, hypot(tx, ty), atan2(ty, tx), tz, g, path, err);
+            clip_xyz(px, py, pz, tx, ty, tz, g, path, err);
             if (err.code) return -1;
             elapsed_start = b;
             continue;

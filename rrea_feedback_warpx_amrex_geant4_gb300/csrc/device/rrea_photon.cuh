@@ -588,7 +588,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             A.uz[ip] = energy * dz;
             double const xt = px + dx * remaining, yt = py + dy * remaining, zt = pz + dz * remaining;
             Path<NP> next;
-            clip_rz(pr, atan2(py, px), pz, hypot(xt, yt), atan2(yt, xt), zt, g, next, err);
+            clip_xyz(px, py, pz, xt, yt, zt, g, next, err);
             if (err.code) return -1;
             double nx, ny, nz;
             point_at_full(next, g, next.in_end, nx, ny, nz);
