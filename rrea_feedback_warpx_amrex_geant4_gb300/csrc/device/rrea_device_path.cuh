@@ -269,19 +269,23 @@ __device__ __forceinline__ void normalize(double& x, double& y, double& z)
     double const inv = rsqrt(n2);
     x *= inv; y *= inv; z *= inv;
 }
-// O/RreaChargedInterleave.H:309-364
+// O/RreaChargedInterleave.H:309-364.  The reference normalises five times:
+// the axis, a copy of it, the first and second basis vectors and the
+// result.  The copy of a unit axis, the cross product of two orthonormal
+// vectors and the rotated unit vector are already unit to within a few ulps,
+// so only the axis and the first basis vector are normalised here; the
+// direction differs from the reference's by ulps (and is renormalised by the
+// next half kick).
 __device__ __forceinline__ void cone_direction(double ax, double ay, double az, double cos_t, double u_phi,
                                                double& ox, double& oy, double& oz)
 {
     normalize(ax, ay, az);
-    double dx = ax, dy = ay, dz = az;
-    normalize(dx, dy, dz);
+    double const dx = ax, dy = ay, dz = az;
     double rx = 0.0, ry = 0.0, rz = 1.0;
     if (fabs(dz) > 0.9) { rx = 1.0; rz = 0.0; }
     double b1x = ry * dz - rz * dy, b1y = rz * dx - rx * dz, b1z = rx * dy - ry * dx;
     normalize(b1x, b1y, b1z);
-    double b2x = dy * b1z - dz * b1y, b2y = dz * b1x - dx * b1z, b2z = dx * b1y - dy * b1x;
-    normalize(b2x, b2y, b2z);
+    double const b2x = dy * b1z - dz * b1y, b2y = dz * b1x - dx * b1z, b2z = dx * b1y - dy * b1x;
     cos_t = fmin(1.0, fmax(-1.0, cos_t));
     double const sin_t = sqrt(fmax(0.0, 1.0 - cos_t * cos_t));
     double const phi = kTwoPi * u_phi;
@@ -290,7 +294,6 @@ __device__ __forceinline__ void cone_direction(double ax, double ay, double az, 
     ox = ax * cos_t + sin_t * (cp * b1x + sp * b2x);
     oy = ay * cos_t + sin_t * (cp * b1y + sp * b2y);
     oz = az * cos_t + sin_t * (cp * b1z + sp * b2z);
-    normalize(ox, oy, oz);
 }
 // O/RreaChargedInterleave.H:371-389
 __device__ __forceinline__ int poisson_capped(double mean, double u, int kmax)

@@ -474,7 +474,7 @@ __device__ __noinline__ double cutoff_bisection(Intervals<NP> iv, Path<NP> path,
 template <int NP, bool POS = false>
 __device__ __forceinline__ int transport_charged(StepConstants const& C, ElectronArgs const& A, int64_t ip,
                                                  uint64_t& subcycles_out, uint64_t& events_out,
-                                                 uint32_t& lineage, Err& err)
+                                                 uint32_t& lineage, IonPairCache& ion_pairs, Err& err)
 {
     constexpr double q = POS ? 1.0 : -1.0;
     constexpr int species = POS ? 1 : 0;
@@ -777,7 +777,8 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                 if (!(pw > 0.0)) continue;
                 double x, y, z;
                 point_at_full(path, g, 0.5 * (bb + ee), x, y, z);
-                deposit_source(C, A.cells, 0, hypot(x, y), z, pw, POS ? 0.0 : 0.5 * cutoff, w_air);
+                // deposit_source(kind 0, sec POS ? 0 : cutoff/2, loss w_air) through the cache
+                ion_pairs.add(C, A.cells, hypot(x, y), z, pw);
             }
         }
         k = fmax(0.0, k - drag);

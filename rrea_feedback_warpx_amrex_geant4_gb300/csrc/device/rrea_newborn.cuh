@@ -95,7 +95,7 @@ __device__ __forceinline__ bool newborn_electron_demotes(StepConstants const& C,
 // 0 when it ended, -1 on error.
 template <int NP, bool POS>
 __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs const& A, int64_t item,
-                                       rrea_gpu_secondary& p, uint32_t& lineage, Err& err)
+                                       rrea_gpu_secondary& p, uint32_t& lineage, IonPairCache& ion_pairs, Err& err)
 {
     const double* __restrict__ arena = A.arena;
     rrea_gpu_config const& cfg = C.cfg;
@@ -289,7 +289,8 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
                         sr = hypot(p.x, p.y);
                         sz = p.z;
                     }
-                    deposit_source(C, A.cells, 0, sr, sz, pw, POS ? 0.0 : 0.5 * cut, w_air);
+                    // deposit_source(kind 0, sec POS ? 0 : cut/2, loss w_air) through the cache
+                    ion_pairs.add(C, A.cells, sr, sz, pw);
                 }
             }
         }

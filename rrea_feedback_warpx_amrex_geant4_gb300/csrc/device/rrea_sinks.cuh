@@ -107,6 +107,86 @@ __device__ __forceinline__ void deposit_source(StepConstants const& C, double* _
     }
 }
 
+// Per-particle accumulator of the ion-pair sources of the continuous drag
+// (AccumulateIonizationEvent with a fixed secondary energy and loss = W_air).
+// The substeps of one particle almost always deposit into the same four
+// cells, so their order-1 weights are summed per cell and written with one
+// atomic per cell and field when the stencil moves or the particle is done,
+// instead of sixteen atomics per substep into a few hot cells.  Only the
+// order of the additions differs from depositing each source at once (the
+// atomics already make that order arbitrary).
+struct IonPairCache {
+    int i[2], j[2];
+    bool use_i[2], use_j[2];
+    bool live;
+    double acc[2][2];  // sum of w * wr[b] * wz[a] per stencil cell
+    double sec_e, loss;
+
+    __device__ __forceinline__ void init(double sec, double loss_per_pair)
+    {
+        live = false;
+        sec_e = sec;
+        loss = loss_per_pair;
+    }
+    __device__ __forceinline__ void flush(StepConstants const& C, double* __restrict__ cells)
+    {
+        if (!live) return;
+        live = false;
+        int const nr = C.cfg.nr;
+        size_t const plane = static_cast<size_t>(nr) * C.cfg.nz;
+        bool const low = sec_e < C.cfg.low_energy_cutoff_eV;
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+            if (!use_j[a]) continue;
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                double const v = acc[a][b];
+                if (v == 0.0 || !use_i[b] || !isfinite(v)) continue;
+                double* cell = cells + i[b] + static_cast<size_t>(nr) * j[a];
+                atomicAdd(cell + plane * 1, v);
+                if (low) atomicAdd(cell, v);
+                atomicAdd(cell + plane * 3, v);
+                double const l = v * fmax(loss, 0.0);
+                if (l != 0.0 && isfinite(l)) atomicAdd(cell + plane * 4, l);
+            }
+        }
+    }
+    // deposit_source(C, cells, 0, r, z, w, sec_e, loss) for w > 0
+    __device__ __forceinline__ void add(StepConstants const& C, double* __restrict__ cells, double r, double z, double w)
+    {
+        CellStencil const st = make_stencil(C, r, z);
+        if (!st.valid) return;
+        bool const same = live && st.i[0] == i[0] && st.i[1] == i[1] && st.j[0] == j[0] && st.j[1] == j[1]
+            && st.use_i[0] == use_i[0] && st.use_i[1] == use_i[1] && st.use_j[0] == use_j[0]
+            && st.use_j[1] == use_j[1];
+        if (!same) {
+            flush(C, cells);
+            live = true;
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                i[q] = st.i[q];
+                j[q] = st.j[q];
+                use_i[q] = st.use_i[q];
+                use_j[q] = st.use_j[q];
+                acc[q][0] = 0.0;
+                acc[q][1] = 0.0;
+            }
+        }
+        double const wv = fmax(w, 0.0);
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+            double const wz = st.wz[a];
+            if (wz == 0.0 || !st.use_j[a]) continue;
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                double const v = wv * st.wr[b] * wz;
+                if (v == 0.0 || !st.use_i[b] || !isfinite(v)) continue;
+                acc[a][b] += v;
+            }
+        }
+    }
+};
+
 __device__ __forceinline__ void record_failure(ElectronArgs const& A, int code, int64_t ip)
 {
     if (atomicCAS(A.status, 0, code) == 0) {

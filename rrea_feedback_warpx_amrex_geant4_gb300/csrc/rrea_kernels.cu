@@ -63,7 +63,10 @@ __device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
         uint32_t lineage = 0;
         ++moved;
         if (A.segments) A.segments[ip].kind = 0;
-        int const disp = transport_charged<NP, POS>(C, A, ip, sub, ev, lineage, err);
+        IonPairCache ion_pairs;
+        ion_pairs.init(POS ? 0.0 : 0.5 * C.cfg.low_energy_cutoff_eV, C.tix.w_air_eV_per_pair);
+        int const disp = transport_charged<NP, POS>(C, A, ip, sub, ev, lineage, ion_pairs, err);
+        ion_pairs.flush(C, A.cells);
         // Every record this particle appended carries a lineage below this
         // count, so the ordering scan/scatter stays in bounds on every path.
         if (A.sec_per_parent) A.sec_per_parent[ip] = lineage;

@@ -41,8 +41,14 @@ __global__ void __launch_bounds__(128, RREA_NEWBORN_MIN_BLOCKS) newborn_kernel(E
         if (!certified) {
             err.set(RREA_GPU_ERR_RANGE);
         } else if (p.birth_fraction < 1.0) {
-            if constexpr (SPECIES == 2) res = advance_photon_newborn<NP>(C, A, ip, p, lineage, err);
-            else res = advance_charged_newborn<NP, SPECIES == 1>(C, A, ip, p, lineage, err);
+            if constexpr (SPECIES == 2) {
+                res = advance_photon_newborn<NP>(C, A, ip, p, lineage, err);
+            } else {
+                IonPairCache ion_pairs;
+                ion_pairs.init(SPECIES == 1 ? 0.0 : 0.5 * C.cfg.low_energy_cutoff_eV, C.tix.w_air_eV_per_pair);
+                res = advance_charged_newborn<NP, SPECIES == 1>(C, A, ip, p, lineage, ion_pairs, err);
+                ion_pairs.flush(C, A.cells);
+            }
         }
         // every child carries a local index below this count
         A.sec_per_parent[ip] = lineage;
