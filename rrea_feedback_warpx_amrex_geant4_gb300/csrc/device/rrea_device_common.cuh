@@ -16,6 +16,7 @@
 namespace rrea_dev {
 
 constexpr double kMeC2 = 510998.95000;   // I/RreaConstants.H:9
+constexpr double kInvMeC2 = 1.0 / kMeC2;  // k / mc^2 as a product: within an ulp of the quotient
 constexpr double kC = 299792458.0;       // I/RreaConstants.H:10
 constexpr double kTwoPi = 6.283185307179586476925286766559;
 constexpr double kEps = 2.220446049250313080847263336181640625e-16;
@@ -281,6 +282,21 @@ __device__ __forceinline__ double mfp_from_inverse(double inv, Err& err)
         return 1.0e99;
     }
     return inv > 0.0 ? 1.0 / inv : 1.0e99;
+}
+
+// The rate 1/MFP of an inverse-MFP table value as the reference forms it,
+// 1 / mfp_from_inverse(inv): 1e-99 for a zero value (the 1e99 m MFP), and
+// for a normal positive value 1 / (1 / inv), which is inv to within an ulp;
+// returning inv saves two FP64 division sequences per rate.
+__device__ __forceinline__ double rate_from_inverse(double inv, Err& err)
+{
+    if (!isfinite(inv) || inv < 0.0) {
+        err.set(RREA_GPU_ERR_INVALID_STATE);
+        return 1.0e-99;
+    }
+    if (inv == 0.0) return 1.0e-99;
+    if (inv < kDblMin) return 1.0 / (1.0 / inv);  // subnormal: 1/inv may overflow
+    return inv;
 }
 
 // O/RreaMaterialPath.H:213-222

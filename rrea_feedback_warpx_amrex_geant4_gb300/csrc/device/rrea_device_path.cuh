@@ -237,7 +237,7 @@ __device__ __forceinline__ void clip_xyz(double x0, double y0, double z0, double
 __device__ __forceinline__ double proper_velocity_from_kinetic(double k)
 {
     if (k <= 0.0) return 0.0;
-    double const gm = 1.0 + k / kMeC2;
+    double const gm = 1.0 + k * kInvMeC2;
     return kC * sqrt(fmax(gm * gm - 1.0, 0.0));
 }
 // O/RreaParticleInteraction.H:1494-1506
@@ -251,7 +251,7 @@ __device__ __forceinline__ double kinetic_from_proper_velocity(double ux, double
 __device__ __forceinline__ double charged_speed(double k)
 {
     if (!isfinite(k) || k < 0.0) return __longlong_as_double(0x7ff8000000000000LL);
-    double const gm = 1.0 + k / kMeC2;
+    double const gm = 1.0 + k * kInvMeC2;
     double const b2 = fmax(0.0, 1.0 - 1.0 / (gm * gm));
     return kC * sqrt(b2);
 }

@@ -86,12 +86,10 @@ __device__ __forceinline__ void competing_rates(StepConstants const& C, const do
     s1 = 0.0;
     if (m_open) {
         double const inv = rate_value(C, arena, rc, e, kRateMoller, err);
-        double const mfp = (thr > 0.0 && e <= 2.0 * thr) ? 1.0e99 : mfp_from_inverse(inv * 1.0, err);
-        s0 = mfp > 0.0 ? 1.0 / mfp : 0.0;
+        s0 = (thr > 0.0 && e <= 2.0 * thr) ? 1.0e-99 : rate_from_inverse(inv * 1.0, err);
     }
     if (b_open) {
-        double const mfp = mfp_from_inverse(rate_value(C, arena, rc, e, kRateBrems, err) * 1.0, err);
-        s1 = mfp > 0.0 ? 1.0 / mfp : 0.0;
+        s1 = rate_from_inverse(rate_value(C, arena, rc, e, kRateBrems, err) * 1.0, err);
     }
     s0 = frozen_rate(s0, err);
     s1 = frozen_rate(s1, err);
@@ -110,18 +108,12 @@ __device__ __forceinline__ void competing_rates_positron(StepConstants const& C,
     s0 = 0.0;
     s1 = 0.0;
     if (!(thr > 0.0 && e <= thr)) {
-        double const mfp = mfp_from_inverse(rate_value(C, arena, rc, e, kRateBhabha, err, RREA_T_P_COLLISION) * 1.0,
-                                            err);
-        s0 = mfp > 0.0 ? 1.0 / mfp : 0.0;
+        s0 = rate_from_inverse(rate_value(C, arena, rc, e, kRateBhabha, err, RREA_T_P_COLLISION) * 1.0, err);
     }
     if (e > C.photon_cutoff_eV) {
-        double const mfp = mfp_from_inverse(rate_value(C, arena, rc, e, kRateBrems, err, RREA_T_P_COLLISION) * 1.0,
-                                            err);
-        s1 = mfp > 0.0 ? 1.0 / mfp : 0.0;
+        s1 = rate_from_inverse(rate_value(C, arena, rc, e, kRateBrems, err, RREA_T_P_COLLISION) * 1.0, err);
     }
-    double const mfp2 =
-        mfp_from_inverse(rate_value(C, arena, rc, e, kRateAnnihilation, err, RREA_T_P_COLLISION) * 1.0, err);
-    s2 = mfp2 > 0.0 ? 1.0 / mfp2 : 0.0;
+    s2 = rate_from_inverse(rate_value(C, arena, rc, e, kRateAnnihilation, err, RREA_T_P_COLLISION) * 1.0, err);
     s0 = frozen_rate(s0, err);
     s1 = frozen_rate(s1, err);
     s2 = frozen_rate(s2, err);
