@@ -10,6 +10,7 @@
 
 #include "../rrea_arena.h"
 #include "../../../include/rrea_gpu.h"
+#include "rrea_fastmath.cuh"
 
 #include <stdint.h>
 
@@ -200,7 +201,7 @@ __device__ __forceinline__ double bracket_t(const double* __restrict__ arena, Rr
             b.t = (b.q - __ldg(x + up - 1)) / (__ldg(x + up) - __ldg(x + up - 1));
         } else {
             const double* lx = arena + h.lx;
-            b.t = (log(b.q) - __ldg(lx + up - 1)) / (__ldg(lx + up) - __ldg(lx + up - 1));
+            b.t = (flog(arena, b.q) - __ldg(lx + up - 1)) / (__ldg(lx + up) - __ldg(lx + up - 1));
         }
         b.have_t = true;
     }
@@ -427,7 +428,7 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
     int ie = 0, ip = 0;
     double te = 0.0, tn = 0.0;
     log_bracket(arena + a.e, arena + a.le, a.ne, e, ie, te, err, le);
-    log_bracket(arena + a.p, arena + a.lp, a.np, n, ip, tn, err);
+    log_bracket(arena + a.p, arena + a.lp, a.np, n, ip, tn, err, flog(arena, n));
     if (err.code) return 1.0;
     const double* lomc = arena + a.lomc;
     const double* cu = arena + a.u;
@@ -450,9 +451,9 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
     } else if (u <= __ldg(cu + first)) {
         double const d1 = omc_at(first), d2 = omc_at(first + 1);
         double const u1 = __ldg(cu + first);
-        double const slope = log(d2 / d1) / __ldg(lur + first);
+        double const slope = flog(arena, d2 / d1) / __ldg(lur + first);
         double const ueff = fmax(u, u1 * 1.0e-6);
-        one_minus_cos = d1 * exp(slope * log(ueff / u1));
+        one_minus_cos = d1 * exp(slope * flog(arena, ueff / u1));
     } else if (u >= __ldg(cu + last)) {
         one_minus_cos = omc_at(last);
     } else {
@@ -465,8 +466,8 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
         }
         double const d0 = omc_at(lo), d1 = omc_at(hi);
         // hi == lo + 1 here, so the denominator is the precomputed node ratio log.
-        double const fu = log(u / __ldg(cu + lo)) / __ldg(lur + lo);
-        one_minus_cos = d0 * exp(fu * log(d1 / d0));
+        double const fu = flog(arena, u / __ldg(cu + lo)) / __ldg(lur + lo);
+        one_minus_cos = d0 * exp(fu * flog(arena, d1 / d0));
     }
     double const c = 1.0 - fmin(2.0, one_minus_cos);
     return fmin(1.0, fmax(-1.0, c));

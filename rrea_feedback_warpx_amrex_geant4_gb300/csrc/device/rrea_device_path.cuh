@@ -622,7 +622,8 @@ struct Selection {
     int channel;
     double sampled, total;
 };
-__device__ __forceinline__ Selection select_hazard(double t0, double t1, double t2, int count, double u1, double u2)
+__device__ __forceinline__ Selection select_hazard(const double* __restrict__ arena, double t0, double t1, double t2,
+                                                  int count, double u1, double u2)
 {
     Selection r{false, false, -1, 0.0, 0.0};
     double const taus[3] = {t0, t1, t2};
@@ -636,7 +637,7 @@ __device__ __forceinline__ Selection select_hazard(double t0, double t1, double 
     r.valid = isfinite(r.total);
     if (!r.valid) return r;
     u1 = fmax(0.0, fmin(1.0, u1));
-    r.sampled = -log(fmax(1.0e-30, 1.0 - u1));
+    r.sampled = -flog(arena, fmax(1.0e-30, 1.0 - u1));
     if (!(r.sampled < r.total)) return r;
     r.event = true;
     u2 = fmax(0.0, fmin(1.0, u2));

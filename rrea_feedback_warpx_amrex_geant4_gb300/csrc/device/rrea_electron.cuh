@@ -870,7 +870,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                                                                 : kChElectronContinuationChannel);
                 double const u1 = rng.uniform(rng_index, ch_depth);
                 double const u2 = rng.uniform(rng_index, ch_channel);
-                Selection const selv = select_hazard(t0, t1, t2, POS ? 3 : 2, u1, u2);
+                Selection const selv = select_hazard(arena, t0, t1, t2, POS ? 3 : 2, u1, u2);
                 if (!selv.valid) {
                     err.set(RREA_GPU_ERR_INVALID_STATE);
                     break;
@@ -946,7 +946,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         if (k >= cutoff) {
             // apply_gs_elastic_scatter, O/RreaTransportStep.H:371-423
             // log(k) is shared by the elastic-MFP and angle-table brackets.
-            double const lk = (k > 0.0) ? log(k) : __longlong_as_double(0x7ff8000000000000LL);
+            double const lk = (k > 0.0) ? flog(arena, k) : __longlong_as_double(0x7ff8000000000000LL);
             double const gs_n = elastic_inverse_stp(C, arena, k, err, lk, species) * density_path(iv, path, sb, se);
             if (gs_n > 0.0) {
                 double const few = C.tix.gs_few_collision_threshold;

@@ -380,7 +380,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
                 if (err.code) break;
                 double const u1 = rng.uniform(idx, kChNewbornCompetingOpticalDepth);
                 double const u2 = rng.uniform(idx, kChNewbornCompetingChannel);
-                Selection const selv = select_hazard(s0 * seg_dp, s1 * seg_dp, s2 * seg_dp, POS ? 3 : 2, u1, u2);
+                Selection const selv = select_hazard(arena, s0 * seg_dp, s1 * seg_dp, s2 * seg_dp, POS ? 3 : 2, u1, u2);
                 if (!selv.valid) {
                     err.set(RREA_GPU_ERR_INVALID_STATE);
                     break;
@@ -453,7 +453,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
         }
         if (err.code || terminal_interaction || terminal_at_point) break;
         if (k >= cut) {
-            double const lk = (k > 0.0) ? log(k) : __longlong_as_double(0x7ff8000000000000LL);
+            double const lk = (k > 0.0) ? flog(arena, k) : __longlong_as_double(0x7ff8000000000000LL);
             double const gs_n = elastic_inverse_stp(C, arena, k, err, lk, species) * density_path(iv, path, sb, se);
             if (gs_n > 0.0) {
                 double const few = C.tix.gs_few_collision_threshold;
@@ -613,7 +613,8 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
         if (!photon_rates(C, arena, energy, rates, err)) return -1;
         double const mfp = mfp_from_inverse(rates.total(), err);
         double const tau = density_path(iv, path, path.in_begin, path.in_end) / mfp;
-        Selection const sel = select_hazard(tau, 0.0, 0.0, 1, rng.uniform(idx, kChNewbornCompetingOpticalDepth), 0.0);
+        Selection const sel =
+            select_hazard(arena, tau, 0.0, 0.0, 1, rng.uniform(idx, kChNewbornCompetingOpticalDepth), 0.0);
         if (!sel.valid) {
             err.set(RREA_GPU_ERR_INVALID_STATE);
             return -1;

@@ -538,7 +538,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
         ++events_out;
         double const u_int =
             rng.uniform(idx, ordinal == 0 ? kChPhotonOpticalDepth : kChPhotonContinuationOpticalDepth);
-        Selection const sel = select_hazard(tau, 0.0, 0.0, 1, u_int, 0.0);
+        Selection const sel = select_hazard(arena, tau, 0.0, 0.0, 1, u_int, 0.0);
         if (!sel.valid) {
             err.set(RREA_GPU_ERR_INVALID_STATE);
             return -1;

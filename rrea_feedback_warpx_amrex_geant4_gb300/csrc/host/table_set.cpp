@@ -161,6 +161,24 @@ void TableSet::Load(std::string const& config_path)
     m_loaded = false;
     m_arena.clear();
     m_index = RreaArenaIndex{};
+    {
+        // Table of the device logarithm, first in the arena (rrea_arena.h):
+        // 1/F and log F split into two doubles, from long double arithmetic.
+        std::vector<double> t(3 * RREA_ARENA_LOG_TABLE_ROWS);
+        for (int j = 0; j < RREA_ARENA_LOG_TABLE_ROWS; ++j) {
+            long double const F = 1.0L + static_cast<long double>(j) / 256.0L;
+            long double const L = std::log(F);
+            double const hi = static_cast<double>(L);
+            t[3 * j] = static_cast<double>(1.0L / F);
+            t[3 * j + 1] = hi;
+            t[3 * j + 2] = static_cast<double>(L - static_cast<long double>(hi));
+        }
+        // F = 2: exactly the ln 2 split of the device code, so log(x) for x
+        // just below 1 cancels e ln2 + log F exactly
+        t[3 * 256 + 1] = 6.93147180559945286227e-01;
+        t[3 * 256 + 2] = 2.31904681384629955842e-17;
+        if (push(t) != RREA_ARENA_LOG_TABLE) throw std::logic_error("log table must open the arena");
+    }
     std::string const dir = dir_of(config_path);
     JsonValue const cfg = ParseJson(read_text(config_path));
     if (cfg.str("schema_version") != "6") {

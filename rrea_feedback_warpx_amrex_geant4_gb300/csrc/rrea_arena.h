@@ -16,6 +16,12 @@
 
 #define RREA_ARENA_MAX_PIECES 4
 
+// The arena opens with the table of the table-driven logarithm
+// (device/rrea_fastmath.cuh): for j = 0..256, F = 1 + j/256, three doubles
+// {RN(1/F), RN(log F), RN(log F - RN(log F))}.
+#define RREA_ARENA_LOG_TABLE 0
+#define RREA_ARENA_LOG_TABLE_ROWS 257
+
 enum RreaInterpMode {
     RREA_INTERP_LOGLOG = 0,
     RREA_INTERP_LOGLOG_ZERO_THRESHOLD = 1,

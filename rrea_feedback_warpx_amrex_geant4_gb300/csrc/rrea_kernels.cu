@@ -92,6 +92,17 @@ __global__ void __launch_bounds__(128, MinBlocks) positron_step_kernel(ElectronA
     charged_step_body<NP, true>(A);
 }
 
+// The table-driven log next to the CUDA log, for the accuracy test.
+__global__ void eval_log_kernel(const double* __restrict__ arena, const double* __restrict__ x, int64_t n,
+                                double* __restrict__ fast, double* __restrict__ libm)
+{
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        fast[i] = flog(arena, x[i]);
+        libm[i] = log(x[i]);
+    }
+}
+
 // Live (id > 0) particles of a tile, warp-aggregated.
 __global__ void count_live_kernel(const int64_t* __restrict__ id, int64_t n, unsigned long long* __restrict__ out)
 {
@@ -237,6 +248,15 @@ cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
     } else {
         rrea_dev::positron_step_kernel<16, 1><<<blocks, threads, 0, stream>>>(args);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t eval_log(const double* arena, const double* x, int64_t n, double* fast, double* libm, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    note_launch();
+    int64_t const b = (n + 255) / 256;
+    rrea_dev::eval_log_kernel<<<static_cast<unsigned>(b < 4096 ? b : 4096), 256, 0, stream>>>(arena, x, n, fast, libm);
     return cudaGetLastError();
 }
 

@@ -136,3 +136,38 @@ def test_count_live_matches_fetched_tile(mods):
     fits, projected = gpu.population_projection(ctx.count_live(gpu.SPECIES_ELECTRON), 0, 10, 2048)
     assert fits and projected == int((arr["id"] > 0).sum()) + 10
     ctx.close()
+
+
+def test_table_driven_log_accuracy(mods):
+    """The device's table-driven logarithm (Tang's method) against the
+    correctly rounded host log: within 2 ulps over normal positive doubles
+    from 1e-300 to 1e300, around 1, and at the table points; special inputs
+    go to the CUDA log."""
+    gpu, workloads, oracle, compare = mods
+    cfg, ctx, field = _ctx(gpu, workloads, "uniform_c0", 16)
+    rng = np.random.default_rng(2)
+    x = np.concatenate([
+        10.0 ** rng.uniform(-300, 300, 400000),
+        1.0 + rng.uniform(-1e-3, 1e-3, 200000),
+        1.0 + rng.uniform(-1e-12, 1e-12, 50000),
+        np.nextafter(1.0, 0.0) - np.arange(1000) * 2.0 ** -53,
+        1.0 + np.arange(257) / 256.0,
+        (1.0 + np.arange(257) / 256.0) * 2.0 ** rng.integers(-60, 60, 257),
+        rng.uniform(1e3, 1e10, 200000),
+        rng.uniform(0.0, 1.0, 200000),
+    ])
+    x = x[(x > 0.0) & np.isfinite(x) & (x >= np.finfo(np.float64).tiny)]
+    fast, libm = ctx.selftest_log(x)
+    ref = np.log(x.astype(np.longdouble))  # extended or quad precision
+
+    def ulps(a):
+        d = np.abs(a.astype(np.longdouble) - ref)
+        return (d / np.spacing(np.abs(ref.astype(np.float64)))).astype(np.float64)
+
+    assert ulps(fast).max() <= 2.0, ulps(fast).max()
+    assert ulps(libm).max() <= 1.5
+    special = np.array([0.0, -1.0, np.inf, np.nan, 5e-324, 1e-310])
+    f2, l2 = ctx.selftest_log(special)
+    np.testing.assert_array_equal(np.isnan(f2), np.isnan(l2))
+    np.testing.assert_array_equal(f2[~np.isnan(f2)], l2[~np.isnan(l2)])
+    ctx.close()
