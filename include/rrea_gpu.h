@@ -261,11 +261,12 @@ rrea_gpu_status rrea_gpu_last_drain_stats(rrea_gpu_ctx* ctx, int64_t* fifo_items
 rrea_gpu_status rrea_gpu_download_diagnostics(rrea_gpu_ctx* ctx, int64_t n, uint64_t* subcycles,
                                               uint64_t* events, int32_t* disposition);
 
-/* Accuracy check of the device's table-driven logarithm: for the n host
- * values x, writes the table-driven log and the CUDA log computed on the
- * device.  Needs loaded tables (the table opens the arena).  NO COUNTERPART
- * IN THE REFERENCE. */
-rrea_gpu_status rrea_gpu_selftest_log(rrea_gpu_ctx* ctx, const double* x, int64_t n, double* fast, double* libm);
+/* Accuracy check of the device's table-driven logarithm (which = 0) and
+ * exponential (which = 1): for the n host values x, writes the table-driven
+ * result and the CUDA function's, both computed on the device.  Needs loaded
+ * tables (the math tables open the arena).  NO COUNTERPART IN THE REFERENCE. */
+rrea_gpu_status rrea_gpu_selftest_math(rrea_gpu_ctx* ctx, int32_t which, const double* x, int64_t n, double* fast,
+                                       double* libm);
 
 /* Kernels this library has launched in this process (all contexts), for
  * launch accounting around a timed region.  NO COUNTERPART IN THE REFERENCE. */

@@ -230,7 +230,7 @@ __device__ __forceinline__ double eval_hot(const double* __restrict__ arena, Rre
     }
     const double* ly = arena + h.ly;
     double const llo = __ldg(ly + b.hi - 1), lhi = __ldg(ly + b.hi);
-    return exp(llo + b.t * (lhi - llo));
+    return fexp(arena, llo + b.t * (lhi - llo));
 }
 
 __device__ __forceinline__ double interpolate(const double* __restrict__ arena, RreaTable1DIndex const& h, double q,
@@ -441,7 +441,7 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
     auto omc_at = [&](int iu) {
         double const lxx = w00 * __ldg(lomc + b00 + iu) + w10 * __ldg(lomc + b10 + iu)
             + w01 * __ldg(lomc + b01 + iu) + w11 * __ldg(lomc + b11 + iu);
-        double const cos_node = 1.0 - exp(lxx);
+        double const cos_node = 1.0 - fexp(arena, lxx);
         return fmax(1.0 - cos_node, kDblMin);
     };
     int const first = 1, last = nu - 2;
@@ -453,7 +453,7 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
         double const u1 = __ldg(cu + first);
         double const slope = flog(arena, d2 / d1) / __ldg(lur + first);
         double const ueff = fmax(u, u1 * 1.0e-6);
-        one_minus_cos = d1 * exp(slope * flog(arena, ueff / u1));
+        one_minus_cos = d1 * fexp(arena, slope * flog(arena, ueff / u1));
     } else if (u >= __ldg(cu + last)) {
         one_minus_cos = omc_at(last);
     } else {
@@ -467,7 +467,7 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
         double const d0 = omc_at(lo), d1 = omc_at(hi);
         // hi == lo + 1 here, so the denominator is the precomputed node ratio log.
         double const fu = flog(arena, u / __ldg(cu + lo)) / __ldg(lur + lo);
-        one_minus_cos = d0 * exp(fu * flog(arena, d1 / d0));
+        one_minus_cos = d0 * fexp(arena, fu * flog(arena, d1 / d0));
     }
     double const c = 1.0 - fmin(2.0, one_minus_cos);
     return fmin(1.0, fmax(-1.0, c));

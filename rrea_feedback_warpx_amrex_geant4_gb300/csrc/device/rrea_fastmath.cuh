@@ -1,4 +1,4 @@
-// Table-driven natural logarithm for the transport loops.
+// Table-driven natural logarithm and exponential for the transport loops.
 //
 // GB300 issues two FP64 FMAs per clock per SM, and the library logarithm is
 // one of the largest FP64 consumers of a substep (table brackets, the GS
@@ -45,6 +45,34 @@ __device__ __forceinline__ double flog(const double* __restrict__ arena, double 
     double const hi = fma(de, kLn2Hi, __ldg(t + 1));
     double const lo = fma(de, kLn2Lo, __ldg(t + 2)) + p;
     return hi + lo;
+}
+
+// Table-driven exponential after P. T. P. Tang, "Table-driven implementation
+// of the exponential function in IEEE floating-point arithmetic", ACM TOMS
+// 15(2), 1989: k = rint(x 128/ln2), x = k ln2/128 + r with |r| <= ln2/256
+// (r from the split of ln2/128, two FMAs), exp x = 2^(k div 128) *
+// 2^((k mod 128)/128) * exp(r), expm1(r) by its Taylor series through r^5
+// (first omitted term below 2^-62).  2^(j/128) comes from the table as two
+// doubles.  Within two ulps of the correctly rounded exponential for
+// |x| < 700; larger, infinite and NaN arguments go to the CUDA exp.
+constexpr double kInvLn2x128 = 1.84664965233787316142e+02;  // RN(128 / ln 2)
+constexpr double kLn2by128Hi = 5.41521234812457272982e-03;  // RN(ln 2 / 128)
+constexpr double kLn2by128Lo = 1.81175532331742157843e-19;  // RN(ln 2 / 128 - kLn2by128Hi)
+
+__device__ __forceinline__ double fexp(const double* __restrict__ arena, double x)
+{
+    if (!(fabs(x) < 700.0)) return exp(x);
+    double const kf = rint(x * kInvLn2x128);
+    int const k = static_cast<int>(kf);
+    double r = fma(-kf, kLn2by128Hi, x);
+    r = fma(-kf, kLn2by128Lo, r);
+    double const q = fma(r, fma(r, fma(r, 1.0 / 120.0, 1.0 / 24.0), 1.0 / 6.0), 0.5);
+    double const p = fma(r * r, q, r);  // expm1(r)
+    const double* t = arena + RREA_ARENA_EXP_TABLE + 2 * (k & 127);
+    double const th = __ldg(t);
+    double const v = th + fma(th, p, __ldg(t + 1));
+    // 2^(k >> 7): |k| < 129,300, so the exponent stays in the normal range
+    return v * __longlong_as_double(static_cast<long long>((k >> 7) + 1023) << 52);
 }
 
 }  // namespace rrea_dev

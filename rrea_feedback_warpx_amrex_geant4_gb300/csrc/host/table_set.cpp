@@ -178,6 +178,14 @@ void TableSet::Load(std::string const& config_path)
         t[3 * 256 + 1] = 6.93147180559945286227e-01;
         t[3 * 256 + 2] = 2.31904681384629955842e-17;
         if (push(t) != RREA_ARENA_LOG_TABLE) throw std::logic_error("log table must open the arena");
+        std::vector<double> x(2 * RREA_ARENA_EXP_TABLE_ROWS);
+        for (int j = 0; j < RREA_ARENA_EXP_TABLE_ROWS; ++j) {
+            long double const T = std::exp2(static_cast<long double>(j) / 128.0L);
+            double const hi = static_cast<double>(T);
+            x[2 * j] = hi;
+            x[2 * j + 1] = static_cast<double>(T - static_cast<long double>(hi));
+        }
+        if (push(x) != RREA_ARENA_EXP_TABLE) throw std::logic_error("exp table must follow the log table");
     }
     std::string const dir = dir_of(config_path);
     JsonValue const cfg = ParseJson(read_text(config_path));

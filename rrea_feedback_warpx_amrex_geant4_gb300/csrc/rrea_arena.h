@@ -21,6 +21,11 @@
 // {RN(1/F), RN(log F), RN(log F - RN(log F))}.
 #define RREA_ARENA_LOG_TABLE 0
 #define RREA_ARENA_LOG_TABLE_ROWS 257
+// Then the table of the table-driven exponential: for j = 0..127, two
+// doubles {RN(2^(j/128)), RN(2^(j/128) - RN(2^(j/128)))}, at the next
+// 32-byte boundary.
+#define RREA_ARENA_EXP_TABLE 772
+#define RREA_ARENA_EXP_TABLE_ROWS 128
 
 enum RreaInterpMode {
     RREA_INTERP_LOGLOG = 0,

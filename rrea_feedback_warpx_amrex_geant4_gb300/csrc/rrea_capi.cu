@@ -1092,22 +1092,23 @@ rrea_gpu_status rrea_gpu_last_drain_stats(rrea_gpu_ctx* ctx, int64_t* fifo_items
     return RREA_GPU_OK;
 }
 
-rrea_gpu_status rrea_gpu_selftest_log(rrea_gpu_ctx* ctx, const double* x, int64_t n, double* fast, double* libm)
+rrea_gpu_status rrea_gpu_selftest_math(rrea_gpu_ctx* ctx, int32_t which, const double* x, int64_t n, double* fast,
+                                      double* libm)
 {
-    if (!ctx || n < 0 || (n > 0 && (!x || !fast || !libm))) return RREA_GPU_ERR_ARGUMENT;
-    if (!ctx->tables_loaded) return fail(ctx, RREA_GPU_ERR_NOT_READY, "the log table is part of the loaded arena");
+    if (!ctx || n < 0 || (n > 0 && (!x || !fast || !libm)) || which < 0 || which > 1) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->tables_loaded) return fail(ctx, RREA_GPU_ERR_NOT_READY, "the math tables are part of the loaded arena");
     if (n == 0) return RREA_GPU_OK;
     double* d = nullptr;
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     RREA_CUDA(ctx, dalloc(&d, static_cast<size_t>(3 * n)));
     size_t const bytes = static_cast<size_t>(n) * sizeof(double);
     cudaError_t e = cudaMemcpyAsync(d, x, bytes, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = rrea_launch::eval_log(ctx->d_arena, d, n, d + n, d + 2 * n, ctx->stream);
+    if (e == cudaSuccess) e = rrea_launch::eval_math(ctx->d_arena, which, d, n, d + n, d + 2 * n, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fast, d + n, bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(libm, d + 2 * n, bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     dfree(d);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "selftest_log");
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "selftest_math");
     return RREA_GPU_OK;
 }
 

@@ -92,14 +92,15 @@ __global__ void __launch_bounds__(128, MinBlocks) positron_step_kernel(ElectronA
     charged_step_body<NP, true>(A);
 }
 
-// The table-driven log next to the CUDA log, for the accuracy test.
-__global__ void eval_log_kernel(const double* __restrict__ arena, const double* __restrict__ x, int64_t n,
-                                double* __restrict__ fast, double* __restrict__ libm)
+// The table-driven log (which 0) or exp (which 1) next to the CUDA
+// function, for the accuracy test.
+__global__ void eval_math_kernel(const double* __restrict__ arena, int which, const double* __restrict__ x,
+                                 int64_t n, double* __restrict__ fast, double* __restrict__ libm)
 {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        fast[i] = flog(arena, x[i]);
-        libm[i] = log(x[i]);
+        fast[i] = which == 0 ? flog(arena, x[i]) : fexp(arena, x[i]);
+        libm[i] = which == 0 ? log(x[i]) : exp(x[i]);
     }
 }
 
@@ -251,12 +252,14 @@ cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
     return cudaGetLastError();
 }
 
-cudaError_t eval_log(const double* arena, const double* x, int64_t n, double* fast, double* libm, cudaStream_t stream)
+cudaError_t eval_math(const double* arena, int which, const double* x, int64_t n, double* fast, double* libm,
+                      cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
     note_launch();
     int64_t const b = (n + 255) / 256;
-    rrea_dev::eval_log_kernel<<<static_cast<unsigned>(b < 4096 ? b : 4096), 256, 0, stream>>>(arena, x, n, fast, libm);
+    rrea_dev::eval_math_kernel<<<static_cast<unsigned>(b < 4096 ? b : 4096), 256, 0, stream>>>(arena, which, x, n,
+                                                                                                fast, libm);
     return cudaGetLastError();
 }
 

@@ -49,7 +49,8 @@ cudaError_t compact_survivors(const rrea_gpu_secondary* items, const uint32_t* a
                               int64_t n, rrea_gpu_secondary* out, cudaStream_t stream);
 cudaError_t adopt_children(const rrea_gpu_secondary* ordered, int64_t n, const rrea_gpu_secondary* items,
                            const uint64_t* lineage, rrea_gpu_secondary* out, cudaStream_t stream);
-cudaError_t eval_log(const double* arena, const double* x, int64_t n, double* fast, double* libm, cudaStream_t stream);
+cudaError_t eval_math(const double* arena, int which, const double* x, int64_t n, double* fast, double* libm,
+                      cudaStream_t stream);
 cudaError_t count_live(const int64_t* id, int64_t n, unsigned long long* out, int blocks, cudaStream_t stream);
 int64_t scan_scratch_elems(int64_t n);
 // Exclusive scan of per-parent counts into offsets (block_scratch holds

@@ -76,7 +76,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_count_live", "rrea_gpu_population_projection", "rrea_gpu_drain_secondaries",
     "rrea_gpu_drain_resident", "rrea_gpu_fetch_survivors", "rrea_gpu_pending_secondaries",
     "rrea_gpu_last_drain_stats", "rrea_gpu_kernel_launches", "rrea_gpu_current_device",
-    "rrea_gpu_advance_field_from_current", "rrea_gpu_selftest_log",
+    "rrea_gpu_advance_field_from_current", "rrea_gpu_selftest_math",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -134,7 +134,7 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_kernel_launches.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
     lib.rrea_gpu_current_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
     lib.rrea_gpu_advance_field_from_current.argtypes = [vp, ctypes.c_double, ctypes.c_int32]
-    lib.rrea_gpu_selftest_log.argtypes = [vp, _D, ctypes.c_int64, _D, _D]
+    lib.rrea_gpu_selftest_math.argtypes = [vp, ctypes.c_int32, _D, ctypes.c_int64, _D, _D]
     lib.rrea_gpu_reset_current.argtypes = [vp]
     lib.rrea_gpu_download_current.argtypes = [vp, _D, _D]
     lib.rrea_gpu_download_current_index.argtypes = [vp, _D, _D, _D]
@@ -336,12 +336,12 @@ class RreaGpuContext:
         self._check(self.lib.rrea_gpu_last_drain_stats(self.handle, ctypes.byref(items), ctypes.byref(surv)))
         return items.value, surv.value
 
-    def selftest_log(self, x):
-        """(table-driven log, CUDA log) of x evaluated on the device."""
+    def selftest_math(self, which, x):
+        """(table-driven, CUDA) log (which 0) or exp (which 1) of x on the device."""
         x = np.ascontiguousarray(x, dtype=np.float64)
         fast, libm = np.zeros_like(x), np.zeros_like(x)
-        self._check(self.lib.rrea_gpu_selftest_log(self.handle, x.ctypes.data_as(_D), x.size, fast.ctypes.data_as(_D),
-                                                   libm.ctypes.data_as(_D)))
+        self._check(self.lib.rrea_gpu_selftest_math(self.handle, int(which), x.ctypes.data_as(_D), x.size,
+                                                    fast.ctypes.data_as(_D), libm.ctypes.data_as(_D)))
         return fast, libm
 
     def count_live(self, species):

@@ -157,7 +157,7 @@ def test_table_driven_log_accuracy(mods):
         rng.uniform(0.0, 1.0, 200000),
     ])
     x = x[(x > 0.0) & np.isfinite(x) & (x >= np.finfo(np.float64).tiny)]
-    fast, libm = ctx.selftest_log(x)
+    fast, libm = ctx.selftest_math(0, x)
     ref = np.log(x.astype(np.longdouble))  # extended or quad precision
 
     def ulps(a):
@@ -167,7 +167,39 @@ def test_table_driven_log_accuracy(mods):
     assert ulps(fast).max() <= 2.0, ulps(fast).max()
     assert ulps(libm).max() <= 1.5
     special = np.array([0.0, -1.0, np.inf, np.nan, 5e-324, 1e-310])
-    f2, l2 = ctx.selftest_log(special)
+    f2, l2 = ctx.selftest_math(0, special)
+    np.testing.assert_array_equal(np.isnan(f2), np.isnan(l2))
+    np.testing.assert_array_equal(f2[~np.isnan(f2)], l2[~np.isnan(l2)])
+    ctx.close()
+
+
+def test_table_driven_exp_accuracy(mods):
+    """The device's table-driven exponential (Tang's method) against the
+    correctly rounded host exp: within 2 ulps over |x| < 700, small
+    arguments and the table points; larger and special arguments go to the
+    CUDA exp."""
+    gpu, workloads, oracle, compare = mods
+    cfg, ctx, field = _ctx(gpu, workloads, "uniform_c0", 16)
+    rng = np.random.default_rng(3)
+    ln2 = np.log(2.0)
+    x = np.concatenate([
+        rng.uniform(-699.0, 699.0, 400000),
+        rng.uniform(-1e-3, 1e-3, 200000),
+        rng.uniform(-1e-12, 1e-12, 50000),
+        np.arange(-128 * 20, 128 * 20) * ln2 / 128.0,
+        rng.uniform(-50.0, 5.0, 200000),
+    ])
+    fast, libm = ctx.selftest_math(1, x)
+    ref = np.exp(x.astype(np.longdouble))
+
+    def ulps(a):
+        d = np.abs(a.astype(np.longdouble) - ref)
+        return (d / np.spacing(np.abs(ref.astype(np.float64)))).astype(np.float64)
+
+    assert ulps(fast).max() <= 2.0, ulps(fast).max()
+    assert ulps(libm).max() <= 1.5
+    special = np.array([700.0, -700.0, 710.0, -746.0, np.inf, -np.inf, np.nan])
+    f2, l2 = ctx.selftest_math(1, special)
     np.testing.assert_array_equal(np.isnan(f2), np.isnan(l2))
     np.testing.assert_array_equal(f2[~np.isnan(f2)], l2[~np.isnan(l2)])
     ctx.close()
