@@ -229,7 +229,7 @@ __device__ __forceinline__ void clip_xyz(double x0, double y0, double z0, double
                                          Path<NP>& p, Err& err)
 {
     bool const finite = isfinite(x0) && isfinite(y0) && isfinite(x1) && isfinite(y1);
-    clip_chord(x0, y0, z0, hypot(x0, y0), x1, y1, z1, hypot(x1, y1), finite, g, p, err);
+    clip_chord(x0, y0, z0, rz_radius(x0, y0), x1, y1, z1, rz_radius(x1, y1), finite, g, p, err);
 }
 
 // ------------------------------------------------------------ kinematics
@@ -482,13 +482,16 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
             double const f = node == 0 ? mid - off : mid + off;
             double x, y, z;
             point_at_piece(p, g, pc, f, x, y, z);
-            double const r = hypot(x, y);
-            double rad = 0.0, rc = 1.0, rs = 0.0;
-            if (r > 0.0) {
-                Divisor const dr = make_divisor(r);
-                rad = quot(pdx * x + pdy * y, dr);
-                rc = quot(x, dr);
-                rs = quot(y, dr);
+            // r and the radial unit vector from one rsqrt of r^2 (within two
+            // ulps of hypot and of the quotients by it)
+            double const r2 = fma(x, x, y * y);
+            double r = 0.0, rad = 0.0, rc = 1.0, rs = 0.0;
+            if (r2 > 0.0) {
+                double const inv = rsqrt(r2);
+                r = r2 * inv;
+                rad = (pdx * x + pdy * y) * inv;
+                rc = x * inv;
+                rs = y * inv;
             }
             double er, ez, bth;
             gather(fv, r, z, er, ez, bth);
@@ -665,7 +668,7 @@ __device__ __forceinline__ Selection select_hazard(const double* __restrict__ ar
 __device__ __forceinline__ bool cartesian_half_open(Geom const& g, double x, double y, double z)
 {
     if (!isfinite(x) || !isfinite(y)) return false;
-    double const r = hypot(x, y);
+    double const r = rz_radius(x, y);
     return isfinite(r) && isfinite(z) && g.rhi > g.rlo && g.zhi > g.zlo && r >= g.rlo && r < g.rhi && z >= g.zlo
         && z < g.zhi;
 }
@@ -680,8 +683,8 @@ __device__ __forceinline__ bool charged_crossing(Path<NP> const& p, Geom const& 
     double cx, cy;
     point_at_full(p, g, p.in_end, cx, cy, cz);
     cz = wrap_z(g, cz);
-    cr = hypot(cx, cy);
-    sr = hypot(p.sx, p.sy);
+    cr = rz_radius(cx, cy);
+    sr = rz_radius(p.sx, p.sy);
     sz = wrap_z(g, p.sz);
     double const scale = fmax(1.0, fmax(g.rhi, fmax(fabs(g.zlo), fabs(g.zhi))));
     double const tol = 512.0 * kEps * scale;

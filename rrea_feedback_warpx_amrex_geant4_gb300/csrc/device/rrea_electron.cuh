@@ -530,7 +530,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     bool const driver_valid = build_chord(dt_s, path);
     if (err.code) return finish(-1);
     bool esc, esc_inv;
-    clipped_escape_policy(path, g, hypot(path.ex, path.ey), path.ez, esc, esc_inv);
+    clipped_escape_policy(path, g, rz_radius(path.ex, path.ey), path.ez, esc, esc_inv);
     double const ds = driver_valid ? path.in_length : 0.0;
     Intervals<NP> iv;
     build_intervals(path, rho, iv);
@@ -698,7 +698,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
             return;
         }
         mid_z = z;
-        mid_r = hypot(x, y);
+        mid_r = rz_radius(x, y);
         if constexpr (POS) {
             // stop point and elapsed fraction for the at-rest annihilation
             mid_x = x;
@@ -770,7 +770,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                 double x, y, z;
                 point_at_full(path, g, 0.5 * (bb + ee), x, y, z);
                 // deposit_source(kind 0, sec POS ? 0 : cutoff/2, loss w_air) through the cache
-                ion_pairs.add(C, A.cells, hypot(x, y), z, pw);
+                ion_pairs.add(C, A.cells, rz_radius(x, y), z, pw);
             }
         }
         k = fmax(0.0, k - drag);
@@ -888,7 +888,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                 }
                 double ex, ey, ez;
                 point_at_full(path, g, ev, ex, ey, ez);
-                double const er = hypot(ex, ey);
+                double const er = rz_radius(ex, ey);
                 {
                     double eff;
                     if (continuous(rem, ev, frozen, eff)) {
@@ -992,7 +992,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     }
     events_out = events;
     if (err.code) return finish(-1);
-    if (exited) clipped_escape_policy(path, g, hypot(path.ex, path.ey), path.ez, esc, esc_inv);
+    if (exited) clipped_escape_policy(path, g, rz_radius(path.ex, path.ey), path.ez, esc, esc_inv);
     if constexpr (POS) {
         // O/RreaPositronTransport.cpp:764-870
         if (annihilated) {
@@ -1001,19 +1001,19 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         }
         if (exited) return commit_escape();
         if (terminated_mid) return annihilate(mid_x, mid_y, mid_z, mid_r, subcycles, mid_elapsed);
-        if (k < cutoff) return annihilate(run_x, run_y, run_z, hypot(run_x, run_y), subcycles, 1.0);
+        if (k < cutoff) return annihilate(run_x, run_y, run_z, rz_radius(run_x, run_y), subcycles, 1.0);
         double const um = proper_velocity_from_kinetic(k);
         A.ux[ip] = um * dx;
         A.uy[ip] = um * dy;
         A.uz[ip] = um * dz;
-        A.r[ip] = hypot(run_x, run_y);
+        A.r[ip] = rz_radius(run_x, run_y);
         A.theta[ip] = atan2(run_y, run_x);
         A.z[ip] = run_z;
         put_segment(A.r[ip], run_z);
         return finish(0);
     }
     if (transported_len > 0.0) particle_density = transported_dpath / transported_len;
-    double const end_r = hypot(run_x, run_y);
+    double const end_r = rz_radius(run_x, run_y);
     double fer, fez, fbt;
     gather(A.fv, end_r, run_z, fer, fez, fbt);
     // electron_ensemble_mean_drag_ev_per_m, O/RreaTransportStep.H:226-247
@@ -1036,7 +1036,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     }
     if (err.code) return finish(-1);
     bool const below_cut = k < cutoff;
-    bool const nonrunaway = hm_thr > 0.0 && k <= hm_thr && hypot(fer, fez) <= threshold;
+    bool const nonrunaway = hm_thr > 0.0 && k <= hm_thr && rz_radius(fer, fez) <= threshold;
     if (exited) return commit_escape();
     if (terminated_mid) return demote(mid_r, mid_z);
     if (below_cut || nonrunaway) return demote(end_r, run_z);

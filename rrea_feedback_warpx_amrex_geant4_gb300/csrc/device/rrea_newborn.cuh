@@ -72,7 +72,7 @@ __device__ __forceinline__ bool newborn_electron_demotes(StepConstants const& C,
     double const cut = C.cfg.low_energy_cutoff_eV;
     double const thr = C.hm_threshold_eV;
     double fer, fez, fbt;
-    gather(A.fv, hypot(x, y), z, fer, fez, fbt);
+    gather(A.fv, rz_radius(x, y), z, fer, fez, fbt);
     double const rho = positive_or(C.density_ratio, 1.0);
     double const ke = fmax(e, cut);
     if (!charged_in_range(C.tix, ke)) err.set(RREA_GPU_ERR_RANGE);
@@ -87,7 +87,7 @@ __device__ __forceinline__ bool newborn_electron_demotes(StepConstants const& C,
         if (inv > 0.0) tracked = inv * mean_conditional(A.arena, C.tix.cdf[RREA_C_BREMS_E], ke, err);
         drag = (col * rho + soft * rho) + hard + tracked;
     }
-    return e < cut || (thr > 0.0 && e <= thr && hypot(fer, fez) <= drag);
+    return e < cut || (thr > 0.0 && e <= thr && rz_radius(fer, fez) <= drag);
 }
 
 // TransportStep::AdvanceChargedNewborn (O/RreaNewbornAdvance.cpp:50-777).
@@ -112,7 +112,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
     uint64_t const root_sp = static_cast<uint64_t>(p.root_species);
     uint64_t const nb_lineage = p.lineage;
     double const birth = p.birth_fraction;
-    double const birth_r = hypot(p.x, p.y), birth_z = p.z;
+    double const birth_r = rz_radius(p.x, p.y), birth_z = p.z;
     double const residual = fmin(1.0, fmax(0.0, 1.0 - birth));
     double k = p.energy_eV;
     RngStream rng;
@@ -166,7 +166,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
         POS ? k < cut : newborn_electron_demotes(C, A, rc, p.x, p.y, p.z, k, err);
     if (err.code) return -1;
     if (demote_at_birth) {
-        double const rb = hypot(p.x, p.y);
+        double const rb = rz_radius(p.x, p.y);
         if constexpr (POS) {
             uint64_t const idx = pack(0, 0, 0);
             if (err.code) return -1;
@@ -283,10 +283,10 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
                 if (pw > 0.0) {
                     double x, y, z;
                     point_at_full(path, g, 0.5 * (bb + ee), x, y, z);
-                    double sr = hypot(x, y), sz = z;
+                    double sr = rz_radius(x, y), sz = z;
                     // a source that rounds off the half-open domain falls back to the birth point
                     if (!(isfinite(sr) && isfinite(sz) && sr >= g.rlo && sr < g.rhi && sz >= g.zlo && sz < g.zhi)) {
-                        sr = hypot(p.x, p.y);
+                        sr = rz_radius(p.x, p.y);
                         sz = p.z;
                     }
                     // deposit_source(kind 0, sec POS ? 0 : cut/2, loss w_air) through the cache
@@ -400,7 +400,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
                 }
                 double ex, ey, ez;
                 point_at_full(path, g, ev, ex, ey, ez);
-                double const er = hypot(ex, ey);
+                double const er = rz_radius(ex, ey);
                 double const ev_elapsed = elapsed_at(ev);
                 {
                     double eff;
@@ -525,7 +525,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
         err.set(RREA_GPU_ERR_GEOMETRY);
         return -1;
     }
-    double const final_r = hypot(fx, fy);
+    double const final_r = rz_radius(fx, fy);
     double const final_elapsed = elapsed_at(final_fraction);
     bool const demote = POS ? k < cut : newborn_electron_demotes(C, A, rc, fx, fy, fz, k, err);
     if (err.code) return -1;
@@ -591,7 +591,7 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
         append_secondary(A, item, key, w, lineage, sp, process, x, y, z, sx, sy, sz, e, b, err, p.root_species);
     };
     if (energy < photon_cut) {
-        deposit_local(hypot(p.x, p.y), p.z, energy);
+        deposit_local(rz_radius(p.x, p.y), p.z, energy);
         return 0;
     }
     double const chord = kC * C.dt_s * residual;
@@ -641,7 +641,7 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
         double const remaining = fmax(0.0, path.full - dist);
         double px, py, pz;
         point_at_full(path, g, f, px, py, pz);
-        double const pr = hypot(px, py);
+        double const pr = rz_radius(px, py);
         double const b = fmin(1.0, elapsed_start + dist / fmax(kC * C.dt_s, kDblMin));
         int const channel = sample_photon_channel(rates, rng.uniform(idx, kChNewbornCompetingChannel), err);
         if (err.code) return -1;

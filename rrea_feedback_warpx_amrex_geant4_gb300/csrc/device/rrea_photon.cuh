@@ -470,7 +470,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
         sincos(pth0, &s0, &c0);
         double const x1 = pr0 * c0 + ux * f, y1 = pr0 * s0 + uy * f;
         z1 = pz0 + uz * f;
-        r1 = hypot(x1, y1);
+        r1 = rz_radius(x1, y1);
         th1 = atan2(y1, x1);
     } else {
         r1 = A.r[ip];
@@ -502,7 +502,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             return -1;
         }
         bool esc, esc_inv;
-        clipped_escape_policy(path, g, hypot(path.ex, path.ey), path.ez, esc, esc_inv);
+        clipped_escape_policy(path, g, rz_radius(path.ex, path.ey), path.ez, esc, esc_inv);
         double const ds = path.in_length;
         Intervals<NP> iv;
         build_intervals(path, rho, iv);
@@ -511,14 +511,14 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             double x, y, z;
             point_at_full(path, g, path.in_begin, x, y, z);
             process = 12;
-            deposit_local_at(hypot(x, y), z, fmax(weight, 0.0), energy);
+            deposit_local_at(rz_radius(x, y), z, fmax(weight, 0.0), energy);
             A.id[ip] = -A.id[ip];
             return 2;
         }
         auto commit_no_event = [&]() {
             double x, y, z;
             point_at_full(path, g, path.in_end, x, y, z);
-            A.r[ip] = hypot(x, y);
+            A.r[ip] = rz_radius(x, y);
             A.theta[ip] = atan2(y, x);
             A.z[ip] = wrap_z(g, z);
             if (!esc) return 0;
@@ -554,7 +554,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
         point_at_full(path, g, f, px, py, pz);
         double const remaining = fmax(0.0, path.full - dist);
         double const birth = fmin(1.0, elapsed_start + dist / fmax(kC * dt_s, kDblMin));
-        double const pr = hypot(px, py);
+        double const pr = rz_radius(px, py);
         int const channel = sample_photon_channel(
             rates, rng.uniform(idx, ordinal == 0 ? kChPhotonChannel : kChPhotonContinuationChannel), err);
         if (err.code) return -1;
@@ -592,7 +592,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             if (err.code) return -1;
             double nx, ny, nz;
             point_at_full(next, g, next.in_end, nx, ny, nz);
-            A.r[ip] = hypot(nx, ny);
+            A.r[ip] = rz_radius(nx, ny);
             A.theta[ip] = atan2(ny, nx);
             A.z[ip] = wrap_z(g, nz);
             if (!(remaining > 0.0)) return 0;
