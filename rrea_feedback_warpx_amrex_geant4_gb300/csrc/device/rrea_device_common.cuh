@@ -202,12 +202,11 @@ __device__ __forceinline__ double bracket_t(const double* __restrict__ arena, Rr
 {
     if (!b.have_t) {
         int const up = b.hi;
+        // the node spacing's reciprocal is stored (rrea_arena.h)
         if (h.mode == RREA_INTERP_LINEAR) {
-            const double* x = arena + h.x;
-            b.t = (b.q - __ldg(x + up - 1)) / (__ldg(x + up) - __ldg(x + up - 1));
+            b.t = (b.q - __ldg(arena + h.x + up - 1)) * __ldg(arena + h.ix + up);
         } else {
-            const double* lx = arena + h.lx;
-            b.t = (flog(arena, b.q) - __ldg(lx + up - 1)) / (__ldg(lx + up) - __ldg(lx + up - 1));
+            b.t = (flog(arena, b.q) - __ldg(arena + h.lx + up - 1)) * __ldg(arena + h.ilx + up);
         }
         b.have_t = true;
     }
@@ -263,9 +262,10 @@ __device__ __forceinline__ bool positive_hot(const double* __restrict__ arena, R
 
 // S/RreaInteractionTables.cpp:624-648 (interp_semilogx_strict).  `lq`, when
 // not NaN, is log(q) already computed by the caller for the same q.
+// `ilx` holds the reciprocal log spacings of the grid.
 __device__ __forceinline__ double semilogx(const double* __restrict__ x, const double* __restrict__ lx,
-                                           const double* __restrict__ y, int n, double q, Err& err,
-                                           double lq = __builtin_nan(""))
+                                           const double* __restrict__ ilx, const double* __restrict__ y, int n,
+                                           double q, Err& err, double lq = __builtin_nan(""))
 {
     if (!isfinite(q) || q < __ldg(x) || q > __ldg(x + n - 1)) {
         err.set(RREA_GPU_ERR_RANGE);
@@ -277,7 +277,7 @@ __device__ __forceinline__ double semilogx(const double* __restrict__ x, const d
     if (__ldg(x + hi) == q) return __ldg(y + hi);
     int const lo = hi - 1;
     double const lqq = isnan(lq) ? log(q) : lq;
-    double const t = (lqq - __ldg(lx + lo)) / (__ldg(lx + hi) - __ldg(lx + lo));
+    double const t = (lqq - __ldg(lx + lo)) * __ldg(ilx + hi);
     return __ldg(y + lo) + t * (__ldg(y + hi) - __ldg(y + lo));
 }
 
@@ -396,9 +396,10 @@ __device__ __forceinline__ double mean_conditional(const double* __restrict__ ar
 }
 
 // S/RreaInteractionTables.cpp:807-827
-__device__ __forceinline__ void log_bracket(const double* __restrict__ g, const double* __restrict__ lg, int n,
-                                            double q, int& i, double& frac, Err& err,
-                                            double lq = __builtin_nan(""))
+// `ilg` holds the reciprocal log spacings of the grid.
+__device__ __forceinline__ void log_bracket(const double* __restrict__ g, const double* __restrict__ lg,
+                                            const double* __restrict__ ilg, int n, double q, int& i, double& frac,
+                                            Err& err, double lq = __builtin_nan(""))
 {
     int const last = n - 1;
     if (!isfinite(q) || q < __ldg(g) || q > __ldg(g + last)) {
@@ -422,7 +423,7 @@ __device__ __forceinline__ void log_bracket(const double* __restrict__ g, const 
         frac = (q == __ldg(g + lo)) ? 0.0 : 1.0;
         return;
     }
-    frac = ((isnan(lq) ? log(q) : lq) - llo) / (lhi - llo);
+    frac = ((isnan(lq) ? log(q) : lq) - llo) * __ldg(ilg + hi);
 }
 
 // S/RreaInteractionTables.cpp:831-891 (node logs read precomputed)
@@ -433,12 +434,24 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
     int const np = a.np, nu = a.nu;
     int ie = 0, ip = 0;
     double te = 0.0, tn = 0.0;
-    log_bracket(arena + a.e, arena + a.le, a.ne, e, ie, te, err, le);
-    log_bracket(arena + a.p, arena + a.lp, a.np, n, ip, tn, err, flog(arena, n));
+    log_bracket(arena + a.e, arena + a.le, arena + a.ile, a.ne, e, ie, te, err, le);
+    log_bracket(arena + a.p, arena + a.lp, arena + a.ilp, a.np, n, ip, tn, err, flog(arena, n));
     if (err.code) return 1.0;
     const double* lomc = arena + a.lomc;
     const double* cu = arena + a.u;
     const double* lur = arena + a.lur;
+    const double* ilur = arena + a.ilur;
+    const double* icu = arena + a.iu;
+    // x / lur[k] and x / u[k] as products with the stored reciprocals; a
+    // zero node (reciprocal stored as 0) keeps the reference's division
+    auto by_lur = [&](double x, int k) {
+        double const r = __ldg(ilur + k);
+        return r != 0.0 ? x * r : x / __ldg(lur + k);
+    };
+    auto by_u = [&](double x, int k) {
+        double const r = __ldg(icu + k);
+        return r != 0.0 ? x * r : x / __ldg(cu + k);
+    };
     size_t const b00 = (static_cast<size_t>(ie) * np + ip) * nu;
     size_t const b10 = (static_cast<size_t>(ie + 1) * np + ip) * nu;
     size_t const b01 = (static_cast<size_t>(ie) * np + ip + 1) * nu;
@@ -457,9 +470,9 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
     } else if (u <= __ldg(cu + first)) {
         double const d1 = omc_at(first), d2 = omc_at(first + 1);
         double const u1 = __ldg(cu + first);
-        double const slope = flog(arena, d2 / d1) / __ldg(lur + first);
+        double const slope = by_lur(flog(arena, d2 / d1), first);
         double const ueff = fmax(u, u1 * 1.0e-6);
-        one_minus_cos = d1 * fexp(arena, slope * flog(arena, ueff / u1));
+        one_minus_cos = d1 * fexp(arena, slope * flog(arena, by_u(ueff, first)));
     } else if (u >= __ldg(cu + last)) {
         one_minus_cos = omc_at(last);
     } else {
@@ -472,7 +485,7 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
         }
         double const d0 = omc_at(lo), d1 = omc_at(hi);
         // hi == lo + 1 here, so the denominator is the precomputed node ratio log.
-        double const fu = flog(arena, u / __ldg(cu + lo)) / __ldg(lur + lo);
+        double const fu = by_lur(flog(arena, by_u(u, lo)), lo);
         one_minus_cos = d0 * fexp(arena, fu * flog(arena, d1 / d0));
     }
     double const c = 1.0 - fmin(2.0, one_minus_cos);

@@ -126,7 +126,8 @@ __device__ __forceinline__ double hard_moller_energy_loss(StepConstants const& C
     RreaTable1DIndex const& h = C.tix.hot[RREA_T_E_HARD_MOLLER];
     double const inv = interpolate(arena, h, e, err);
     if (!(inv > 0.0)) return 0.0;
-    double const mean = semilogx(arena + h.x, arena + h.lx, arena + C.tix.hard_moller_mean_secondary, h.n, e, err);
+    double const mean =
+        semilogx(arena + h.x, arena + h.lx, arena + h.ilx, arena + C.tix.hard_moller_mean_secondary, h.n, e, err);
     if (!(mean > 0.0)) return 0.0;
     return mean * inv * dr;
 }
@@ -137,7 +138,7 @@ __device__ __forceinline__ double elastic_inverse_stp(StepConstants const& C, co
                                                       double le = __builtin_nan(""), int species = 0)
 {
     RreaElasticIndex const& el = C.tix.elastic[species];
-    double const mfp = semilogx(arena + el.x, arena + el.lx, arena + el.mfp, el.n, e, err, le) / 1.0;
+    double const mfp = semilogx(arena + el.x, arena + el.lx, arena + el.ilx, arena + el.mfp, el.n, e, err, le) / 1.0;
     return frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0, err);
 }
 
@@ -176,7 +177,7 @@ __device__ __forceinline__ double sample_single_elastic_cos(StepConstants const&
         return 1.0;
     }
     RreaElasticIndex const& el = C.tix.elastic[species];
-    double const eta = semilogx(arena + el.x, arena + el.lx, arena + el.eta, el.n, e, err, le);
+    double const eta = semilogx(arena + el.x, arena + el.lx, arena + el.ilx, arena + el.eta, el.n, e, err, le);
     double const u = fmin(fmax(cdf_u, 0.0), 1.0 - 1.0e-15);
     return 1.0 - 2.0 * eta * u / (1.0 + eta - u);
 }
@@ -477,6 +478,8 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     double const cutoff = cfg.low_energy_cutoff_eV;
     double const rho = C.density_ratio;
     double const w_air = C.tix.w_air_eV_per_pair;
+    // ion pairs per eV of drag loss, a product per substep instead of a division
+    double const inv_pair_energy = 1.0 / fmax(w_air, 1.0);
     double const hm_thr = C.hm_threshold_eV;
     double const dt_s = C.dt_s;
 
@@ -765,7 +768,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                 if (!(ee > bb)) continue;
                 double const raw = path.full * (ee - bb) * iv.density[i] * sc;
                 double const loss = col * raw / raw_col;
-                double const pw = weight * loss / fmax(w_air, 1.0);
+                double const pw = weight * loss * inv_pair_energy;
                 if (!(pw > 0.0)) continue;
                 double x, y, z;
                 point_at_full(path, g, 0.5 * (bb + ee), x, y, z);

@@ -156,6 +156,23 @@ int64_t TableSet::push_logs(std::vector<double> const& values, bool zero_for_non
     return push(logs);
 }
 
+int64_t TableSet::push_inverse_spacing(int64_t off, int n)
+{
+    std::vector<double> inv(static_cast<std::size_t>(n), 0.0);
+    for (int i = 1; i < n; ++i) {
+        double const d = m_arena[static_cast<std::size_t>(off + i)] - m_arena[static_cast<std::size_t>(off + i - 1)];
+        inv[static_cast<std::size_t>(i)] = d != 0.0 ? 1.0 / d : 0.0;
+    }
+    return push(inv);
+}
+
+int64_t TableSet::push_reciprocals(std::vector<double> const& values)
+{
+    std::vector<double> inv(values.size(), 0.0);
+    for (std::size_t i = 0; i < values.size(); ++i) inv[i] = values[i] != 0.0 ? 1.0 / values[i] : 0.0;
+    return push(inv);
+}
+
 void TableSet::Load(std::string const& config_path)
 {
     m_loaded = false;
@@ -383,6 +400,8 @@ void TableSet::Load(std::string const& config_path)
             h.lx = push_logs(tab.x, false);
             grids.push_back({&tab.x, {h.x, h.lx}});
         }
+        h.ix = push_inverse_spacing(h.x, h.n);
+        h.ilx = push_inverse_spacing(h.lx, h.n);
         h.y = push(tab.y);
         h.ly = push_logs(tab.y, true);
     }
@@ -458,6 +477,7 @@ void TableSet::Load(std::string const& config_path)
         e.lx = push_logs(cols[0], false);
         e.mfp = push(cols[1]);
         e.eta = push(cols[2]);
+        e.ilx = push_inverse_spacing(e.lx, e.n);
     }
 
     auto put_angle = [&](RreaAngleIndex& ai, char const* name, double lo, double hi) {
@@ -482,6 +502,10 @@ void TableSet::Load(std::string const& config_path)
         ai.lur = push(lur);
         ai.omc = push(a.omc);
         ai.lomc = push_logs(a.omc, false);
+        ai.ile = push_inverse_spacing(ai.le, ai.ne);
+        ai.ilp = push_inverse_spacing(ai.lp, ai.np);
+        ai.ilur = push_reciprocals(lur);
+        ai.iu = push_reciprocals(a.u);
     };
     put_angle(m_index.gs[0], "electron_gs_angle_cdf_air", m_index.charged_min_eV, transition);
     put_angle(m_index.gs[1], "positron_gs_angle_cdf_air", m_index.charged_min_eV, transition);

@@ -37,6 +37,11 @@ private:
     void LoadPairBank(std::string const& bin_path, std::string const& index_path);
     int64_t push(std::vector<double> const& values);
     int64_t push_logs(std::vector<double> const& values, bool zero_for_nonpositive);
+    // 1 / (a[i] - a[i-1]) for the arena array at `off` of `n` doubles (0 at i = 0
+    // and where two nodes coincide)
+    int64_t push_inverse_spacing(int64_t off, int n);
+    // 1 / v[i] (0 where v[i] = 0)
+    int64_t push_reciprocals(std::vector<double> const& values);
 
     bool m_loaded = false;
     std::vector<double> m_arena;

@@ -3,6 +3,11 @@
 // index is plain data so the same struct is filled by the host loader and
 // read by device code from __constant__ memory.
 //
+// The interpolation denominators (node spacings, the CDF node ratios and
+// nodes the GS inversion divides by) are stored as reciprocals, so a query
+// multiplies instead of running an FP64 division sequence; the quotient is
+// then within 1.5 ulp of the reference's.
+//
 // Every logarithm the reference takes of a TABLE NODE at query time
 // (node energies, node values, GS one-minus-cos nodes, CDF u-node ratios) is
 // precomputed here once with the host libm.  The reference computes exactly
@@ -70,6 +75,8 @@ typedef struct {
     int64_t lx;     // log(energy nodes)
     int64_t y;      // values
     int64_t ly;     // log(values), 0 where value <= 0
+    int64_t ix;     // 1 / (x[i] - x[i-1]) at i >= 1 (0 at i = 0)
+    int64_t ilx;    // 1 / (lx[i] - lx[i-1]) at i >= 1 (0 at i = 0)
 } RreaTable1DIndex;
 
 typedef struct {
@@ -91,6 +98,7 @@ typedef struct {
     int64_t lx;    // log energies
     int64_t mfp;   // elastic collision MFP at STP [m]
     int64_t eta;   // screening eta
+    int64_t ilx;   // 1 / (lx[i] - lx[i-1]) at i >= 1
 } RreaElasticIndex;
 
 typedef struct {
@@ -101,6 +109,9 @@ typedef struct {
     int64_t lur;        // log(u[i+1]/u[i]) for i in [0, nu-1)
     int64_t omc;        // one_minus_cos, (ie*np+ip)*nu+iu
     int64_t lomc;       // log(one_minus_cos)
+    int64_t ile, ilp;   // 1 / (le[i] - le[i-1]), 1 / (lp[i] - lp[i-1]) at i >= 1
+    int64_t ilur;       // 1 / lur[i] (0 where lur[i] = 0)
+    int64_t iu;         // 1 / u[i] (0 where u[i] = 0)
 } RreaAngleIndex;
 
 // Photoelectric subshell CDF (S/RreaInteractionTables.cpp:893-987): groups
