@@ -38,16 +38,23 @@ struct SpeciesTile {
 // particle whose streams a FIFO item draws from): an open-addressing table
 // filled once per drain from the initial items; children inherit their
 // item's slot, so no lookup happens after the start.
+// The table lives in the context across drains; an epoch stamp marks the
+// entries of the current drain, so starting a drain clears nothing.
 class RootSlots {
 public:
-    explicit RootSlots(size_t expected)
+    void reset(size_t expected)
     {
         size_t cap = 16;
         while (cap < 2 * expected) cap <<= 1;
-        keys_.assign(cap, 0);
-        species_.assign(cap, -1);
-        slots_.assign(cap, 0);
-        mask_ = cap - 1;
+        if (cap > keys_.size()) {
+            keys_.assign(cap, 0);
+            species_.assign(cap, 0);
+            slots_.assign(cap, 0);
+            stamp_.assign(cap, 0);
+            epoch_ = 0;
+        }
+        mask_ = keys_.size() - 1;
+        ++epoch_;
     }
     // slot of (key, species); `fresh` is the slot a new root receives
     uint32_t find_or_insert(uint64_t key, int32_t species, uint32_t fresh, bool& inserted)
@@ -57,10 +64,11 @@ public:
         h *= 0xff51afd7ed558ccdULL;
         h ^= h >> 33;
         for (size_t i = static_cast<size_t>(h) & mask_;; i = (i + 1) & mask_) {
-            if (species_[i] < 0) {
+            if (stamp_[i] != epoch_) {
                 keys_[i] = key;
                 species_[i] = species;
                 slots_[i] = fresh;
+                stamp_[i] = epoch_;
                 inserted = true;
                 return fresh;
             }
@@ -75,6 +83,8 @@ private:
     std::vector<uint64_t> keys_;
     std::vector<int32_t> species_;
     std::vector<uint32_t> slots_;
+    std::vector<uint64_t> stamp_;
+    uint64_t epoch_ = 0;
     size_t mask_ = 0;
 };
 
@@ -138,6 +148,12 @@ struct rrea_gpu_ctx {
     uint32_t* d_alive = nullptr;
     uint64_t* d_child_lineage = nullptr;
     unsigned long long* d_invalid = nullptr;
+    // roots of the initial FIFO items (16 B each) on the device and in pinned
+    // host memory, grown with the FIFO
+    unsigned long long* d_roots = nullptr;
+    unsigned long long* h_roots = nullptr;
+    int64_t roots_cap = 0;
+    RootSlots root_slots;
     int64_t last_drain_items = 0;
     cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev_stop = nullptr;
@@ -361,6 +377,8 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     dfree(ctx->d_alive);
     dfree(ctx->d_child_lineage);
     dfree(ctx->d_invalid);
+    dfree(ctx->d_roots);
+    if (ctx->h_roots) cudaFreeHost(ctx->h_roots);
     dfree(ctx->d_work);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
@@ -757,28 +775,44 @@ rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t
     std::vector<uint32_t> slot(static_cast<size_t>(n_initial));
     std::vector<uint64_t> next;
     {
-        std::vector<rrea_gpu_secondary> init(static_cast<size_t>(n_initial));
+        if (n_initial > ctx->roots_cap) {
+            RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            dfree(ctx->d_roots);
+            if (ctx->h_roots) cudaFreeHost(ctx->h_roots);
+            ctx->d_roots = nullptr;
+            ctx->h_roots = nullptr;
+            ctx->roots_cap = 0;
+            int64_t const cap = std::max<int64_t>(n_initial, 2 * ctx->roots_cap);
+            RREA_CUDA(ctx, dalloc(&ctx->d_roots, static_cast<size_t>(2 * cap)));
+            RREA_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&ctx->h_roots),
+                                          static_cast<size_t>(2 * cap) * sizeof(unsigned long long)));
+            ctx->roots_cap = cap;
+        }
         if (n_initial > 0) {
-            RREA_CUDA(ctx, cudaMemcpyAsync(init.data(), ctx->d_fifo,
-                                           static_cast<size_t>(n_initial) * sizeof(rrea_gpu_secondary),
+            RREA_CUDA(ctx, rrea_launch::gather_roots(ctx->d_fifo, n_initial, ctx->d_roots, ctx->stream));
+            RREA_CUDA(ctx, cudaMemcpyAsync(ctx->h_roots, ctx->d_roots,
+                                           static_cast<size_t>(2 * n_initial) * sizeof(unsigned long long),
                                            cudaMemcpyDeviceToHost, ctx->stream));
             RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         }
-        RootSlots table(init.size());
-        for (size_t i = 0; i < init.size(); ++i) {
+        unsigned long long const* roots = ctx->h_roots;
+        RootSlots& table = ctx->root_slots;
+        table.reset(static_cast<size_t>(n_initial));
+        for (int64_t i = 0; i < n_initial; ++i) {
+            uint64_t const key = roots[2 * i];
+            int32_t const species = static_cast<int32_t>(roots[2 * i + 1] >> 32);
+            uint64_t const lin = roots[2 * i + 1] & 0xffffffffULL;
             // the records of one parent are adjacent: reuse the previous slot
             uint32_t s;
-            if (i > 0 && init[i].root_key == init[i - 1].root_key
-                && init[i].root_species == init[i - 1].root_species) {
-                s = slot[i - 1];
+            if (i > 0 && roots[2 * i] == roots[2 * i - 2] && (roots[2 * i + 1] >> 32) == (roots[2 * i - 1] >> 32)) {
+                s = slot[static_cast<size_t>(i - 1)];
             } else {
                 bool inserted = false;
-                s = table.find_or_insert(init[i].root_key, init[i].root_species, static_cast<uint32_t>(next.size()),
-                                         inserted);
+                s = table.find_or_insert(key, species, static_cast<uint32_t>(next.size()), inserted);
                 if (inserted) next.push_back(0);
             }
-            slot[i] = s;
-            next[s] = std::max<uint64_t>(next[s], init[i].lineage + 1U);
+            slot[static_cast<size_t>(i)] = s;
+            next[s] = std::max<uint64_t>(next[s], lin + 1U);
         }
     }
     std::vector<uint32_t> counts;

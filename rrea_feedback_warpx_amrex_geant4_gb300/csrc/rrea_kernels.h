@@ -45,6 +45,7 @@ cudaError_t validate_fifo(const rrea_gpu_secondary* items, int64_t n, int mode, 
                           long long* first, cudaStream_t stream);
 cudaError_t newborn_step(rrea_dev::ElectronArgs const& args, rrea_gpu_secondary* items, int64_t n, uint32_t* alive,
                          int max_blocks, bool periodic, cudaStream_t stream);
+cudaError_t gather_roots(const rrea_gpu_secondary* items, int64_t n, unsigned long long* out, cudaStream_t stream);
 cudaError_t compact_survivors(const rrea_gpu_secondary* items, const uint32_t* alive, const int64_t* offsets,
                               int64_t n, rrea_gpu_secondary* out, cudaStream_t stream);
 cudaError_t adopt_children(const rrea_gpu_secondary* ordered, int64_t n, const rrea_gpu_secondary* items,

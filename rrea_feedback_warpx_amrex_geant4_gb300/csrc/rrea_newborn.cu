@@ -128,6 +128,19 @@ __global__ void validate_fifo_kernel(const rrea_gpu_secondary* __restrict__ item
     }
 }
 
+// The roots and lineages of the initial FIFO items, 16 B per item
+// (root key; root species << 32 | lineage), for the host's lineage counters.
+__global__ void gather_roots_kernel(const rrea_gpu_secondary* __restrict__ items, int64_t n,
+                                    unsigned long long* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        out[2 * i] = items[i].root_key;
+        out[2 * i + 1] = (static_cast<unsigned long long>(static_cast<uint32_t>(items[i].root_species)) << 32)
+            | static_cast<uint32_t>(items[i].lineage);
+    }
+}
+
 int grid_for(int64_t n, int cap)
 {
     int64_t const b = (n + 127) / 128;
@@ -169,6 +182,14 @@ cudaError_t newborn_step(rrea_dev::ElectronArgs const& args, rrea_gpu_secondary*
         newborn_kernel<1, 1><<<blocks, 128, 0, stream>>>(args, items, n, alive);
         newborn_kernel<1, 2><<<blocks, 128, 0, stream>>>(args, items, n, alive);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t gather_roots(const rrea_gpu_secondary* items, int64_t n, unsigned long long* out, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    note_launch();
+    rrea_dev::gather_roots_kernel<<<rrea_dev::grid_for(n, 65535), 128, 0, stream>>>(items, n, out);
     return cudaGetLastError();
 }
 
