@@ -767,7 +767,9 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                 double const bb = fmax(b, iv.begin[i]), ee = fmin(eff, iv.end[i]);
                 if (!(ee > bb)) continue;
                 double const raw = path.full * (ee - bb) * iv.density[i] * sc;
-                double const loss = col * raw / raw_col;
+                // with one interval raw is raw_col (the same products), and
+                // col * raw / raw_col is col to within an ulp
+                double const loss = NP == 1 ? col : col * raw / raw_col;
                 double const pw = weight * loss * inv_pair_energy;
                 if (!(pw > 0.0)) continue;
                 double x, y, z;

@@ -14,10 +14,37 @@ namespace rrea_dev {
 // order-1 weights, axis fold) is built once and applied to each value.
 struct CellStencil {
     bool valid;
+    int i0, j0;  // lower-left stencil cell before folding
     int i[2], j[2];
     bool use_i[2], use_j[2];
     double wr[2], wz[2];
 };
+
+// Cells of the order-1 stencil with lower-left cell (i0, j0): the radial
+// fold onto the axis cell and the periodic z wrap, or a dropped row/column.
+__device__ __forceinline__ void stencil_cells(StepConstants const& C, int i0, int j0, int i[2], int j[2], bool use_i[2],
+                                              bool use_j[2])
+{
+    rrea_gpu_config const& cfg = C.cfg;
+    int const nr = cfg.nr, nz = cfg.nz;
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        int jj = j0 + a;
+        use_j[a] = true;
+        if (jj < 0 || jj > nz - 1) {
+            if (cfg.periodic_z) jj = ((jj % nz) + nz) % nz;
+            else use_j[a] = false;
+        }
+        j[a] = jj;
+        int ii = i0 + a;
+        use_i[a] = true;
+        if (ii < 0 || ii > nr - 1) {
+            if (ii == -1 && cfg.r_lo == 0.0) ii = 0;
+            else use_i[a] = false;
+        }
+        i[a] = ii;
+    }
+}
 
 __device__ __forceinline__ CellStencil make_stencil(StepConstants const& C, double r, double z)
 {
@@ -45,23 +72,9 @@ __device__ __forceinline__ CellStencil make_stencil(StepConstants const& C, doub
     int const j0 = static_cast<int>(floor(zc));
     st.wz[1] = zc - j0;
     st.wz[0] = 1.0 - st.wz[1];
-#pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        int j = j0 + a;
-        st.use_j[a] = true;
-        if (j < 0 || j > nz - 1) {
-            if (cfg.periodic_z) j = ((j % nz) + nz) % nz;
-            else st.use_j[a] = false;
-        }
-        st.j[a] = j;
-        int i = i0 + a;
-        st.use_i[a] = true;
-        if (i < 0 || i > nr - 1) {
-            if (i == -1 && cfg.r_lo == 0.0) i = 0;
-            else st.use_i[a] = false;
-        }
-        st.i[a] = i;
-    }
+    st.i0 = i0;
+    st.j0 = j0;
+    stencil_cells(C, i0, j0, st.i, st.j, st.use_i, st.use_j);
     return st;
 }
 
@@ -114,24 +127,38 @@ __device__ __forceinline__ void deposit_source(StepConstants const& C, double* _
 // atomic per cell and field when the stencil moves or the particle is done,
 // instead of sixteen atomics per substep into a few hot cells.  Only the
 // order of the additions differs from depositing each source at once (the
-// atomics already make that order arbitrary).
+// atomics already make that order arbitrary).  The running sums sit in a
+// per-thread shared-memory slot: the transport state around them lives in
+// local memory that misses L1, and the slot is touched every substep.  The
+// stencil is named by its lower-left cell (i0, j0) packed in one word; the
+// folded cells and their use flags follow from it (stencil_cells).
+struct IonPairSlot {
+    long long key;  // (j0 << 32) | (i0 & 0xffffffff); kIonPairEmpty = none
+    double acc[4];  // sum of w * wr[b] * wz[a] at acc[2 * a + b]
+};
+constexpr long long kIonPairEmpty = static_cast<long long>(0x8000000000000000ULL);
+
+
 struct IonPairCache {
-    int i[2], j[2];
-    bool use_i[2], use_j[2];
-    bool live;
-    double acc[2][2];  // sum of w * wr[b] * wz[a] per stencil cell
+    IonPairSlot* slot;
     double sec_e, loss;
 
-    __device__ __forceinline__ void init(double sec, double loss_per_pair)
+    __device__ __forceinline__ void init(IonPairSlot* s, double sec, double loss_per_pair)
     {
-        live = false;
+        slot = s;
+        slot->key = kIonPairEmpty;
         sec_e = sec;
         loss = loss_per_pair;
     }
     __device__ __forceinline__ void flush(StepConstants const& C, double* __restrict__ cells)
     {
-        if (!live) return;
-        live = false;
+        long long const key = slot->key;
+        if (key == kIonPairEmpty) return;
+        slot->key = kIonPairEmpty;
+        int i[2], j[2];
+        bool use_i[2], use_j[2];
+        stencil_cells(C, static_cast<int>(static_cast<unsigned int>(key & 0xffffffffLL)), static_cast<int>(key >> 32), i,
+                      j, use_i, use_j);
         int const nr = C.cfg.nr;
         size_t const plane = static_cast<size_t>(nr) * C.cfg.nz;
         bool const low = sec_e < C.cfg.low_energy_cutoff_eV;
@@ -140,7 +167,7 @@ struct IonPairCache {
             if (!use_j[a]) continue;
 #pragma unroll
             for (int b = 0; b < 2; ++b) {
-                double const v = acc[a][b];
+                double const v = slot->acc[2 * a + b];
                 if (v == 0.0 || !use_i[b] || !isfinite(v)) continue;
                 double* cell = cells + i[b] + static_cast<size_t>(nr) * j[a];
                 atomicAdd(cell + plane * 1, v);
@@ -156,21 +183,12 @@ struct IonPairCache {
     {
         CellStencil const st = make_stencil(C, r, z);
         if (!st.valid) return;
-        bool const same = live && st.i[0] == i[0] && st.i[1] == i[1] && st.j[0] == j[0] && st.j[1] == j[1]
-            && st.use_i[0] == use_i[0] && st.use_i[1] == use_i[1] && st.use_j[0] == use_j[0]
-            && st.use_j[1] == use_j[1];
-        if (!same) {
+        long long const key = (static_cast<long long>(st.j0) << 32) | static_cast<unsigned int>(st.i0);
+        if (slot->key != key) {
             flush(C, cells);
-            live = true;
+            slot->key = key;
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                i[q] = st.i[q];
-                j[q] = st.j[q];
-                use_i[q] = st.use_i[q];
-                use_j[q] = st.use_j[q];
-                acc[q][0] = 0.0;
-                acc[q][1] = 0.0;
-            }
+            for (int q = 0; q < 4; ++q) slot->acc[q] = 0.0;
         }
         double const wv = fmax(w, 0.0);
 #pragma unroll
@@ -181,7 +199,7 @@ struct IonPairCache {
             for (int b = 0; b < 2; ++b) {
                 double const v = wv * st.wr[b] * wz;
                 if (v == 0.0 || !st.use_i[b] || !isfinite(v)) continue;
-                acc[a][b] += v;
+                slot->acc[2 * a + b] += v;
             }
         }
     }

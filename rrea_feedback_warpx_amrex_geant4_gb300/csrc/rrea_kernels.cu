@@ -48,6 +48,9 @@ template <int NP, bool POS>
 __device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
 {
     StepConstants const& C = c_step;
+    // one ion-pair slot per thread (the kernels launch at most 128 threads per block)
+    __shared__ IonPairSlot ion_slots[128];
+    IonPairSlot* const my_slot = ion_slots + threadIdx.x;
     unsigned int moved = 0;
     for_each_particle(A.n, A.work, [&](int64_t ip) {
         if (!(A.id[ip] > 0)) {
@@ -64,7 +67,7 @@ __device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
         ++moved;
         if (A.segments) A.segments[ip].kind = 0;
         IonPairCache ion_pairs;
-        ion_pairs.init(POS ? 0.0 : 0.5 * C.cfg.low_energy_cutoff_eV, C.tix.w_air_eV_per_pair);
+        ion_pairs.init(my_slot, POS ? 0.0 : 0.5 * C.cfg.low_energy_cutoff_eV, C.tix.w_air_eV_per_pair);
         int const disp = transport_charged<NP, POS>(C, A, ip, sub, ev, lineage, ion_pairs, err);
         ion_pairs.flush(C, A.cells);
         // Every record this particle appended carries a lineage below this

@@ -24,6 +24,7 @@ __global__ void __launch_bounds__(128, RREA_NEWBORN_MIN_BLOCKS) newborn_kernel(E
                                                       int64_t n, uint32_t* __restrict__ alive)
 {
     StepConstants const& C = c_step;
+    __shared__ IonPairSlot ion_slots[128];  // one per thread; launched with 128 threads
     for (int64_t ip = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; ip < n;
          ip += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         int const raw = items[ip].species;
@@ -45,7 +46,8 @@ __global__ void __launch_bounds__(128, RREA_NEWBORN_MIN_BLOCKS) newborn_kernel(E
                 res = advance_photon_newborn<NP>(C, A, ip, p, lineage, err);
             } else {
                 IonPairCache ion_pairs;
-                ion_pairs.init(SPECIES == 1 ? 0.0 : 0.5 * C.cfg.low_energy_cutoff_eV, C.tix.w_air_eV_per_pair);
+                ion_pairs.init(ion_slots + threadIdx.x, SPECIES == 1 ? 0.0 : 0.5 * C.cfg.low_energy_cutoff_eV,
+                               C.tix.w_air_eV_per_pair);
                 res = advance_charged_newborn<NP, SPECIES == 1>(C, A, ip, p, lineage, ion_pairs, err);
                 ion_pairs.flush(C, A.cells);
             }
