@@ -95,6 +95,10 @@ struct rrea_gpu_ctx {
     int64_t capacity = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // side streams and events that let the drain's species kernels overlap
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[2] = {nullptr, nullptr};
     int num_sms = 0;
 
     rrea_host::TableSet tables;
@@ -278,6 +282,13 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         return bail(RREA_GPU_ERR_CUDA);
     }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RREA_GPU_ERR_CUDA);
+    for (int k = 0; k < 2; ++k) {
+        if (cudaStreamCreateWithFlags(&ctx->side[k], cudaStreamNonBlocking) != cudaSuccess
+            || cudaEventCreateWithFlags(&ctx->join_ev[k], cudaEventDisableTiming) != cudaSuccess) {
+            return bail(RREA_GPU_ERR_CUDA);
+        }
+    }
+    if (cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bail(RREA_GPU_ERR_CUDA);
     size_t const n = static_cast<size_t>(capacity);
     size_t const ner = static_cast<size_t>(cfg->nr + 1) * cfg->nz;
     size_t const nez = static_cast<size_t>(cfg->nr) * (cfg->nz + 1);
@@ -383,6 +394,14 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    for (int k = 0; k < 2; ++k) {
+        if (ctx->side[k]) {
+            cudaStreamSynchronize(ctx->side[k]);
+            cudaStreamDestroy(ctx->side[k]);
+        }
+        if (ctx->join_ev[k]) cudaEventDestroy(ctx->join_ev[k]);
+    }
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
     delete ctx;
     return RREA_GPU_OK;
 }
@@ -830,7 +849,7 @@ rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t
         a.segments = ctx->netchord ? ctx->d_seg : nullptr;
         rrea_gpu_secondary* const items = ctx->d_fifo + cursor;
         RREA_CUDA(ctx, rrea_launch::newborn_step(a, items, chunk, ctx->d_alive, ctx->num_sms * 8, c.periodic_z != 0,
-                                                 ctx->stream));
+                                                 ctx->stream, ctx->side, ctx->fork_ev, ctx->join_ev));
         if (a.segments) {
             RREA_CUDA(ctx, rrea_launch::netchord_deposit(a.segments, chunk, ctx->net, dt_s, ctx->d_status,
                                                          ctx->d_fail_index, ctx->num_sms * 8, ctx->stream));

@@ -43,8 +43,11 @@ cudaError_t maxwell_step(int nr, int nz, double dr, double dz, double dt, int su
 cudaError_t newborn_constants(rrea_dev::StepConstants const& sc, cudaStream_t stream);
 cudaError_t validate_fifo(const rrea_gpu_secondary* items, int64_t n, int mode, unsigned long long* invalid,
                           long long* first, cudaStream_t stream);
+// The positron and photon kernels run on side[0] and side[1] (joined back
+// into `stream`) when the side streams and events are given.
 cudaError_t newborn_step(rrea_dev::ElectronArgs const& args, rrea_gpu_secondary* items, int64_t n, uint32_t* alive,
-                         int max_blocks, bool periodic, cudaStream_t stream);
+                         int max_blocks, bool periodic, cudaStream_t stream, cudaStream_t const side[2],
+                         cudaEvent_t fork, cudaEvent_t const join[2]);
 cudaError_t gather_roots(const rrea_gpu_secondary* items, int64_t n, unsigned long long* out, cudaStream_t stream);
 cudaError_t compact_survivors(const rrea_gpu_secondary* items, const uint32_t* alive, const int64_t* offsets,
                               int64_t n, rrea_gpu_secondary* out, cudaStream_t stream);

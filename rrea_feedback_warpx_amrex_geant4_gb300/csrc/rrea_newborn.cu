@@ -169,22 +169,42 @@ cudaError_t validate_fifo(const rrea_gpu_secondary* items, int64_t n, int mode, 
 }
 
 cudaError_t newborn_step(rrea_dev::ElectronArgs const& args, rrea_gpu_secondary* items, int64_t n, uint32_t* alive,
-                         int max_blocks, bool periodic, cudaStream_t stream)
+                         int max_blocks, bool periodic, cudaStream_t stream, cudaStream_t const side[2],
+                         cudaEvent_t fork, cudaEvent_t const join[2])
 {
     using namespace rrea_dev;
     if (n <= 0) return cudaSuccess;
     int const blocks = grid_for(n, max_blocks);
     for (int k = 0; k < 3; ++k) note_launch();
+    // The species kernels touch disjoint items, so the positron and photon
+    // ones run beside the electron one; each is a short wave whose length is
+    // its longest item, and side by side their latencies overlap.
+    cudaStream_t s1 = stream, s2 = stream;
+    if (side && fork && join) {
+        cudaError_t e = cudaEventRecord(fork, stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side[0], fork, 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side[1], fork, 0);
+        if (e != cudaSuccess) return e;
+        s1 = side[0];
+        s2 = side[1];
+    }
     if (periodic) {
         newborn_kernel<4, 0><<<blocks, 128, 0, stream>>>(args, items, n, alive);
-        newborn_kernel<4, 1><<<blocks, 128, 0, stream>>>(args, items, n, alive);
-        newborn_kernel<4, 2><<<blocks, 128, 0, stream>>>(args, items, n, alive);
+        newborn_kernel<4, 1><<<blocks, 128, 0, s1>>>(args, items, n, alive);
+        newborn_kernel<4, 2><<<blocks, 128, 0, s2>>>(args, items, n, alive);
     } else {
         newborn_kernel<1, 0><<<blocks, 128, 0, stream>>>(args, items, n, alive);
-        newborn_kernel<1, 1><<<blocks, 128, 0, stream>>>(args, items, n, alive);
-        newborn_kernel<1, 2><<<blocks, 128, 0, stream>>>(args, items, n, alive);
+        newborn_kernel<1, 1><<<blocks, 128, 0, s1>>>(args, items, n, alive);
+        newborn_kernel<1, 2><<<blocks, 128, 0, s2>>>(args, items, n, alive);
     }
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && s1 != stream) {
+        e = cudaEventRecord(join[0], s1);
+        if (e == cudaSuccess) e = cudaEventRecord(join[1], s2);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, join[0], 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, join[1], 0);
+    }
+    return e;
 }
 
 cudaError_t gather_roots(const rrea_gpu_secondary* items, int64_t n, unsigned long long* out, cudaStream_t stream)

@@ -85,3 +85,18 @@ def test_population_projection_matches_reference_rule(gpu):
     big = 2 ** 64 - 1
     assert P(big, 0, 1, big) == (False, big)            # saturates on overflow
     assert P(0, 0, 0, 0) == (True, 0)
+
+
+def test_library_leaves_no_internal_symbol_undefined(gpu):
+    """Every launcher and kernel the library calls is defined in it: an
+    internal symbol left undefined would only surface when the library is
+    loaded on the GPU machine."""
+    import shutil
+    import subprocess
+
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm is not available")
+    out = subprocess.run([nm, "-D", "--undefined-only", gpu.LIB_PATH], capture_output=True, text=True, check=True)
+    internal = [line for line in out.stdout.splitlines() if "rrea" in line]
+    assert not internal, internal
