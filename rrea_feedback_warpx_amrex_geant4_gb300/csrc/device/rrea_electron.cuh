@@ -238,6 +238,13 @@ __device__ __forceinline__ void moller_final_state(StepConstants const& C, Elect
     dx = pdx; dy = pdy; dz = pdz;
     append_secondary(A, ip, key, weight, lineage, 0, 2, site.x, site.y, site.z, sdx, sdy, sdz, sec, site.birth, err);
     deposit_source(C, A.cells, 0, site.r, site.z, weight, sec, sec);
+    // closure of the HardMoller group (O/RreaChargedFinalStates.H:211-224)
+    double const cut = C.cfg.low_energy_cutoff_eV;
+    GroupClosure gc;
+    gc.begin(-1.0, kMeC2, weight, kb, k, true);
+    gc.secondary(-1.0, kMeC2, weight, sec);
+    gc.ionization(weight, sec, cut);
+    if (!gc.valid(cut)) err.set(RREA_GPU_ERR_INVALID_STATE);
 }
 
 // RreaApplyBremsFinalState, O/RreaChargedFinalStates.H:329-394; POS selects
@@ -274,6 +281,13 @@ __device__ __forceinline__ void brems_final_state(StepConstants const& C, Electr
         double const pw = weight * eg / fmax(w_air, 1.0);
         if (weight > 0.0 && pw > 0.0) deposit_source(C, A.cells, 0, site.r, site.z, pw, 0.0, w_air);
     }
+    // closure of the Bremsstrahlung group (O/RreaChargedFinalStates.H:377-393)
+    double const cut = C.cfg.low_energy_cutoff_eV;
+    GroupClosure gc;
+    gc.begin(POS ? 1.0 : -1.0, kMeC2, weight, kb, after, true);
+    if (tracked) gc.secondary(0.0, 0.0, weight, eg);
+    else if (eg > 0.0) gc.local(weight, eg, C.tix.w_air_eV_per_pair, cut);
+    if (!gc.valid(cut)) err.set(RREA_GPU_ERR_INVALID_STATE);
 }
 
 // The out-of-line helpers below take every argument by value and return
@@ -309,6 +323,13 @@ __device__ __forceinline__ void bhabha_final_state(StepConstants const& C, Elect
     dx = pdx; dy = pdy; dz = pdz;
     append_secondary(A, ip, key, weight, lineage, 0, 3, site.x, site.y, site.z, sdx, sdy, sdz, sec, site.birth, err, 1);
     deposit_source(C, A.cells, 2, site.r, site.z, weight, 0.0, sec);
+    // closure of the HardBhabha group (O/RreaChargedFinalStates.H:281-294)
+    double const cut = C.cfg.low_energy_cutoff_eV;
+    GroupClosure gc;
+    gc.begin(1.0, kMeC2, weight, kb, k, true);
+    gc.secondary(-1.0, kMeC2, weight, sec);
+    gc.positive_ion(weight);
+    if (!gc.valid(cut)) err.set(RREA_GPU_ERR_INVALID_STATE);
 }
 
 // sample_annihilation_photon_energy_fraction (S/RreaInteractionTables.cpp:63-108):
@@ -408,6 +429,18 @@ static __device__ __noinline__ uint32_t spawn_annihilation(ElectronArgs A, RngSt
         if (pw > 0.0) deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
     }
     deposit_source(C, A.cells, 2, r, z, weight, 0.0, 0.0);
+    {
+        // closure of the PositronAnnihilation group (O/RreaPositronTransport.cpp:136-162, 710-735)
+        double const ecut = C.cfg.low_energy_cutoff_eV;
+        GroupClosure gc;
+        gc.begin(1.0, kMeC2, weight, fmax(k, 0.0), 0.0, false);
+        if (e1 >= cut) gc.secondary(0.0, 0.0, weight, e1);
+        if (e2 >= cut) gc.secondary(0.0, 0.0, weight, e2);
+        if (at_rest && k > 0.0) gc.local(weight, k, w_air, ecut);
+        gc.local(weight, local, w_air, ecut);
+        gc.positive_ion(weight);
+        if (!gc.valid(ecut)) err.set(RREA_GPU_ERR_INVALID_STATE);
+    }
     if (err.code) record_failure(A, err.code, ip);
     return lineage;
 }

@@ -661,6 +661,20 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
                 deposit_local(pr, pz, cs.recoil);
             }
             energy = cs.scattered;
+            {
+                // closure of the Compton group
+                bool const survives = energy >= photon_cut;
+                GroupClosure gc;
+                gc.begin(0.0, 0.0, w, inc, survives ? energy : 0.0, survives);
+                if (cs.recoil >= cut) gc.secondary(-1.0, kMeC2, w, cs.recoil);
+                gc.ionization(w, cs.recoil, cut);
+                if (cs.recoil < cut) gc.local(w, cs.recoil, w_air, cut);
+                if (!survives) gc.local(w, energy, w_air, cut);
+                if (!gc.valid(cut)) {
+                    err.set(RREA_GPU_ERR_INVALID_STATE);
+                    return -1;
+                }
+            }
             if (energy < photon_cut) {
                 deposit_local(pr, pz, energy);
                 return 0;
@@ -699,6 +713,16 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
                 deposit_local(pr, pz, ee);
             }
             if (bind > 0.0) deposit_local(pr, pz, bind);
+            GroupClosure gc;  // closure of the Photoelectric group
+            gc.begin(0.0, 0.0, w, energy, 0.0, false);
+            if (ee >= cut) gc.secondary(-1.0, kMeC2, w, ee);
+            gc.ionization(w, ee, cut);
+            if (ee < cut) gc.local(w, ee, w_air, cut);
+            if (bind > 0.0) gc.local(w, bind, w_air, cut);
+            if (!gc.valid(cut)) {
+                err.set(RREA_GPU_ERR_INVALID_STATE);
+                return -1;
+            }
             return 0;
         }
         bool const triplet = channel == 3;
@@ -734,6 +758,10 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
             if (ps.e_recoil < cut) deposit_local(pr, pz, ps.e_recoil);
         }
         if (ps.local > 0.0) deposit_local(pr, pz, ps.local);
+        if (!pair_closure_valid(ps, w, energy, cut, photon_cut, w_air)) {
+            err.set(RREA_GPU_ERR_INVALID_STATE);
+            return -1;
+        }
         return 0;
     }
 }

@@ -293,6 +293,41 @@ __device__ __forceinline__ double* pair_largest(PairState& st)
     if (st.e_recoil > *l) l = &st.e_recoil;
     return l;
 }
+// Closure of the PairNuclear / PairTriplet group (O/RreaPhotonFinalStates.H:278-364):
+// a sub-cutoff positron annihilates at rest into two m_e c^2 photons beside a
+// positive ion, inside the same group.
+__device__ __forceinline__ bool pair_closure_valid(PairState const& ps, double w, double e_photon, double cutoff,
+                                                   double photon_cut, double w_air)
+{
+    GroupClosure gc;
+    gc.begin(0.0, 0.0, w, e_photon, 0.0, false);
+    if (ps.e_electron >= cutoff) {
+        gc.secondary(-1.0, kMeC2, w, ps.e_electron);
+    } else {
+        gc.low_energy_electron(w);
+        gc.local(w, ps.e_electron, w_air, cutoff);
+    }
+    if (ps.e_positron >= cutoff) {
+        gc.secondary(1.0, kMeC2, w, ps.e_positron);
+    } else {
+        double local = 0.0;
+        for (int q = 0; q < 2; ++q) {
+            if (kMeC2 >= photon_cut) gc.secondary(0.0, 0.0, w, kMeC2);
+            else local += kMeC2;
+        }
+        if (ps.e_positron > 0.0) gc.local(w, ps.e_positron, w_air, cutoff);
+        gc.local(w, local, w_air, cutoff);
+        gc.positive_ion(w);
+    }
+    if (ps.recoil) {
+        if (ps.e_recoil >= cutoff) gc.secondary(-1.0, kMeC2, w, ps.e_recoil);
+        gc.ionization(w, ps.e_recoil, cutoff);
+        if (ps.e_recoil < cutoff) gc.local(w, ps.e_recoil, w_air, cutoff);
+    }
+    if (ps.local > 0.0) gc.local(w, ps.local, w_air, cutoff);
+    return gc.valid(cutoff);
+}
+
 __device__ __forceinline__ void sample_pair(StepConstants const& C, const double* __restrict__ arena, double e,
                                             int channel, double d_inv, double d_polar, double d_azim, PairState& st,
                                             Err& err)
@@ -577,6 +612,20 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
                 deposit_local_at(pr, pz, weight, cs.recoil);
             }
             energy = cs.scattered;
+            {
+                // closure of the Compton group (O/RreaPhotonFinalStates.H:92-142)
+                bool const survives = energy >= photon_cut;
+                GroupClosure gc;
+                gc.begin(0.0, 0.0, weight, inc, survives ? energy : 0.0, survives);
+                if (cs.recoil >= cutoff) gc.secondary(-1.0, kMeC2, weight, cs.recoil);
+                gc.ionization(weight, cs.recoil, cutoff);
+                if (cs.recoil < cutoff) gc.local(weight, cs.recoil, w_air, cutoff);
+                if (!survives) gc.local(weight, energy, w_air, cutoff);
+                if (!gc.valid(cutoff)) {
+                    err.set(RREA_GPU_ERR_INVALID_STATE);
+                    return -1;
+                }
+            }
             if (energy < photon_cut) {
                 deposit_local_at(pr, pz, weight, energy);
                 A.id[ip] = -A.id[ip];
@@ -627,6 +676,19 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
                 deposit_local_at(pr, pz, weight, ee);
             }
             if (bind > 0.0) deposit_local_at(pr, pz, weight, bind);
+            {
+                // closure of the Photoelectric group (O/RreaPhotonFinalStates.H:181-223)
+                GroupClosure gc;
+                gc.begin(0.0, 0.0, weight, energy, 0.0, false);
+                if (ee >= cutoff) gc.secondary(-1.0, kMeC2, weight, ee);
+                gc.ionization(weight, ee, cutoff);
+                if (ee < cutoff) gc.local(weight, ee, w_air, cutoff);
+                if (bind > 0.0) gc.local(weight, bind, w_air, cutoff);
+                if (!gc.valid(cutoff)) {
+                    err.set(RREA_GPU_ERR_INVALID_STATE);
+                    return -1;
+                }
+            }
             A.id[ip] = -A.id[ip];
             return 2;
         }
@@ -681,6 +743,10 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             if (ps.e_recoil < cutoff) deposit_local_at(pr, pz, weight, ps.e_recoil);
         }
         if (ps.local > 0.0) deposit_local_at(pr, pz, weight, ps.local);
+        if (!pair_closure_valid(ps, weight, energy, cutoff, photon_cut, w_air)) {
+            err.set(RREA_GPU_ERR_INVALID_STATE);
+            return -1;
+        }
         A.id[ip] = -A.id[ip];
         return 2;
     }

@@ -205,6 +205,86 @@ struct IonPairCache {
     }
 };
 
+// Conservation closure of one interaction group,
+// RreaValidateSecondaryGroupConservation (O/RreaParticleInteraction.H:1099-1251):
+// rest-mass-inclusive energy and charge in (the parent before the event and
+// the neutral target electron of every ionization or positive-ion source)
+// against out (the surviving parent, the secondaries, the local
+// recoil/binding/sub-cutoff energy, the ions and low-energy electrons of the
+// sources), within 64 eps of the larger side.  The ion pairs of a local
+// deposit (ionization sources below the cutoff) add the same rest energy and
+// charge to both sides and only widen the tolerance, as in the reference.
+struct GroupClosure {
+    double in_e, out_e, in_q, out_q, thru_q;
+    bool finite;
+
+    __device__ __forceinline__ void begin(double q_parent, double rest_parent, double w, double e_before, double e_after,
+                                          bool survives)
+    {
+        finite = isfinite(w) && isfinite(e_before) && isfinite(e_after) && w > 0.0 && e_before >= 0.0 && e_after >= 0.0;
+        in_q = q_parent * w;
+        out_q = survives ? in_q : 0.0;
+        in_e = w * (e_before + rest_parent);
+        out_e = survives ? w * (e_after + rest_parent) : 0.0;
+        thru_q = fabs(in_q) + fabs(out_q);
+    }
+    __device__ __forceinline__ void secondary(double q, double rest, double w, double e)
+    {
+        finite = finite && isfinite(w) && isfinite(e) && w > 0.0 && e >= 0.0;
+        out_q += q * w;
+        thru_q += fabs(q * w);
+        out_e += w * (e + rest);
+    }
+    // AccumulateIonizationEvent with event weight w and secondary energy sec_e
+    __device__ __forceinline__ void ionization(double w, double sec_e, double cutoff)
+    {
+        finite = finite && isfinite(w) && isfinite(sec_e) && w > 0.0;
+        in_e += w * kMeC2;
+        out_q += w;
+        thru_q += w;
+        if (sec_e < cutoff) {
+            out_q -= w;
+            thru_q += w;
+            out_e += w * kMeC2;
+        }
+    }
+    // AccumulatePositiveIonSourceOnly with event weight w
+    __device__ __forceinline__ void positive_ion(double w)
+    {
+        finite = finite && isfinite(w) && w > 0.0;
+        in_e += w * kMeC2;
+        out_q += w;
+        thru_q += w;
+    }
+    // AccumulateLowEnergyElectron with event weight w
+    __device__ __forceinline__ void low_energy_electron(double w)
+    {
+        finite = finite && isfinite(w) && w > 0.0;
+        out_q -= w;
+        thru_q += w;
+        out_e += w * kMeC2;
+    }
+    // deposit_local_energy_as_ion_pairs: the local energy and its pairs
+    __device__ __forceinline__ void local(double w, double e, double w_air, double cutoff)
+    {
+        if (w <= 0.0 || e <= 0.0) return;
+        out_e += w * e;
+        finite = finite && isfinite(e);
+        double const pw = w * e / fmax(w_air, 1.0);
+        if (pw > 0.0) ionization(pw, 0.0, cutoff);
+    }
+    __device__ __forceinline__ bool valid(double cutoff) const
+    {
+        if (!(finite && isfinite(cutoff) && cutoff > 0.0 && isfinite(in_e) && isfinite(out_e) && isfinite(in_q)
+              && isfinite(out_q))) {
+            return false;
+        }
+        double const tol_q = 64.0 * kEps * fmax(1.0, thru_q);
+        double const tol_e = 64.0 * kEps * fmax(1.0, fmax(fabs(in_e), fabs(out_e)));
+        return fabs(out_q - in_q) <= tol_q && fabs(out_e - in_e) <= tol_e;
+    }
+};
+
 __device__ __forceinline__ void record_failure(ElectronArgs const& A, int code, int64_t ip)
 {
     if (atomicCAS(A.status, 0, code) == 0) {
