@@ -75,6 +75,10 @@ struct ElectronArgs {
     // dynamic scheduling: warps take the next 32 particles from this counter
     // (zeroed before the launch); null = static grid-stride assignment
     unsigned long long* __restrict__ work;
+    // tile index of element 0 of every per-particle array above: a launch
+    // over one chunk of a tile passes offset arrays and the chunk's start,
+    // so parent indices and failure indices stay tile indices
+    int64_t index_base;
 };
 
 // Visits every particle index of [0, n) once.  With a work counter each warp

@@ -288,7 +288,7 @@ struct GroupClosure {
 __device__ __forceinline__ void record_failure(ElectronArgs const& A, int code, int64_t ip)
 {
     if (atomicCAS(A.status, 0, code) == 0) {
-        *A.fail_index = static_cast<long long>(ip);
+        *A.fail_index = static_cast<long long>(A.index_base + ip);
     }
 }
 
@@ -306,7 +306,7 @@ __device__ __forceinline__ void append_secondary(ElectronArgs const& A, int64_t 
         s.process = process;
         s.root_species = root_species;
         s.pad = 0;
-        s.parent_index = ip;
+        s.parent_index = A.index_base + ip;
         s.root_key = key;
         s.lineage = lineage;
         s.x = x; s.y = y; s.z = z;

@@ -24,6 +24,10 @@ namespace {
 
 constexpr int kTileDoubles = 13;
 constexpr int kSpecies = 3;
+// Chunks of a drop-in phase call whose upload overlaps the compute of the
+// chunks before it, and the tile size from which that pays.
+constexpr int kPhaseChunks = 4;
+constexpr int64_t kPipelineMinParticles = 1 << 18;
 
 // Device SoA of one species: r, z, theta, ux, uy, uz, w, prev_r, prev_z,
 // prev_theta, prev_ux, prev_uy, prev_uz, then id and cpu.
@@ -139,7 +143,11 @@ struct rrea_gpu_ctx {
     int* d_status = nullptr;
     long long* d_fail_index = nullptr;
     unsigned long long* d_transported = nullptr;
-    unsigned long long* d_work = nullptr;  // dynamic scheduling counter of the phase kernels
+    unsigned long long* d_work = nullptr;  // dynamic scheduling counters of the phase kernels, one per chunk
+    // a drop-in phase call uploads its host tile in chunks on side[0] while
+    // the kernels of earlier chunks run on `stream` and side[1]
+    cudaEvent_t chunk_up[kPhaseChunks] = {};
+    cudaEvent_t chunk_done[kPhaseChunks] = {};
     // transient FIFO of DrainAndCommitSecondaries: the resident phases queue
     // their ordered secondaries in d_fifo[0, fifo_pending); a drain advances
     // the FIFO chunk by chunk and leaves the survivors in d_surv[0, n_surv)
@@ -289,6 +297,12 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         }
     }
     if (cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bail(RREA_GPU_ERR_CUDA);
+    for (int k = 0; k < kPhaseChunks; ++k) {
+        if (cudaEventCreateWithFlags(&ctx->chunk_up[k], cudaEventDisableTiming) != cudaSuccess
+            || cudaEventCreateWithFlags(&ctx->chunk_done[k], cudaEventDisableTiming) != cudaSuccess) {
+            return bail(RREA_GPU_ERR_CUDA);
+        }
+    }
     size_t const n = static_cast<size_t>(capacity);
     size_t const ner = static_cast<size_t>(cfg->nr + 1) * cfg->nz;
     size_t const nez = static_cast<size_t>(cfg->nr) * (cfg->nz + 1);
@@ -336,7 +350,7 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         && dalloc(&ctx->d_diag_disp, n) == cudaSuccess && dalloc(&ctx->d_status, 1) == cudaSuccess
         && dalloc(&ctx->d_fail_index, 1) == cudaSuccess && dalloc(&ctx->d_transported, 1) == cudaSuccess
         && dalloc(&ctx->d_alive, n) == cudaSuccess && dalloc(&ctx->d_child_lineage, nsec) == cudaSuccess
-        && dalloc(&ctx->d_invalid, 1) == cudaSuccess && dalloc(&ctx->d_work, 1) == cudaSuccess
+        && dalloc(&ctx->d_invalid, 1) == cudaSuccess && dalloc(&ctx->d_work, kPhaseChunks) == cudaSuccess
         && cudaEventCreate(&ctx->ev_start) == cudaSuccess && cudaEventCreate(&ctx->ev_stop) == cudaSuccess;
     if (!ok) return bail(RREA_GPU_ERR_CUDA);
     if (cudaMemsetAsync(ctx->d_cells, 0, 5 * ncell * sizeof(double), ctx->stream) != cudaSuccess) {
@@ -402,6 +416,10 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
         if (ctx->join_ev[k]) cudaEventDestroy(ctx->join_ev[k]);
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    for (int k = 0; k < kPhaseChunks; ++k) {
+        if (ctx->chunk_up[k]) cudaEventDestroy(ctx->chunk_up[k]);
+        if (ctx->chunk_done[k]) cudaEventDestroy(ctx->chunk_done[k]);
+    }
     delete ctx;
     return RREA_GPU_OK;
 }
@@ -477,6 +495,19 @@ rrea_gpu_status rrea_gpu_set_field(rrea_gpu_ctx* ctx, const double* er, const do
 }  // extern "C"
 
 namespace {
+
+// The pointer and size checks of a host tile, before any copy.
+rrea_gpu_status check_tile(rrea_gpu_ctx* ctx, rrea_gpu_tile const* t)
+{
+    if (t->n > ctx->capacity) return fail(ctx, RREA_GPU_ERR_CAPACITY, "tile larger than the context capacity");
+    double* const host[kTileDoubles] = {t->r, t->z, t->theta, t->ux, t->uy, t->uz, t->w,
+                                        t->prev_r, t->prev_z, t->prev_theta, t->prev_ux, t->prev_uy, t->prev_uz};
+    for (int f = 0; f < kTileDoubles; ++f) {
+        if (!host[f]) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "null tile component");
+    }
+    if (!t->id) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "null tile id");
+    return RREA_GPU_OK;
+}
 
 rrea_gpu_status stage_tile(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile const* t)
 {
@@ -558,11 +589,37 @@ rrea_dev::ElectronArgs sink_args(rrea_gpu_ctx* ctx, rrea_dev::StepConstants cons
     return a;
 }
 
-// Launches one species phase (electron, positron or photon) on the staged
-// device tile.  `aliased` runs the resident engine mode: the captured
-// pre-push state is the current state (for photons the kernel then performs
-// the straight push itself).
-rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, double dt_s, bool aliased)
+// Uploads tile elements [off, off + len) of every column on `s`.
+rrea_gpu_status upload_range(rrea_gpu_ctx* ctx, SpeciesTile& st, rrea_gpu_tile const* t, int64_t off, int64_t len,
+                             cudaStream_t s)
+{
+    if (len <= 0) return RREA_GPU_OK;
+    double* const host[kTileDoubles] = {t->r, t->z, t->theta, t->ux, t->uy, t->uz, t->w,
+                                        t->prev_r, t->prev_z, t->prev_theta, t->prev_ux, t->prev_uy, t->prev_uz};
+    size_t const bytes = static_cast<size_t>(len) * sizeof(double);
+    for (int f = 0; f < kTileDoubles; ++f) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(st.d[f] + off, host[f] + off, bytes, cudaMemcpyHostToDevice, s));
+    }
+    RREA_CUDA(ctx, cudaMemcpyAsync(st.id + off, t->id + off, static_cast<size_t>(len) * sizeof(int64_t),
+                                   cudaMemcpyHostToDevice, s));
+    if (t->cpu) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(st.cpu + off, t->cpu + off, static_cast<size_t>(len) * sizeof(int32_t),
+                                       cudaMemcpyHostToDevice, s));
+    } else {
+        RREA_CUDA(ctx, cudaMemsetAsync(st.cpu + off, 0, static_cast<size_t>(len) * sizeof(int32_t), s));
+    }
+    return RREA_GPU_OK;
+}
+
+// Launches one species phase (electron, positron or photon) on the device
+// tile.  `aliased` runs the resident engine mode: the captured pre-push
+// state is the current state (for photons the kernel then performs the
+// straight push itself).  With a host tile (the drop-in calls) the upload
+// is part of the launch: a large tile goes up in kPhaseChunks chunks on a
+// side stream, and the kernel of each chunk starts as soon as its chunk has
+// landed, on alternating streams so a chunk's tail overlaps the next one.
+rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, double dt_s, bool aliased,
+                             rrea_gpu_tile const* host = nullptr)
 {
     if (!ctx->tables_loaded || !ctx->field_set) {
         return fail(ctx, RREA_GPU_ERR_NOT_READY, "tables and field must be set before a step");
@@ -571,12 +628,14 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     rrea_gpu_config const& c = ctx->cfg;
     rrea_dev::StepConstants const sc = step_constants(ctx, step, dt_s);
     RREA_CUDA(ctx, rrea_launch::set_step_constants(sc, ctx->stream));
+    if (species == RREA_SPECIES_PHOTON) RREA_CUDA(ctx, rrea_launch::photon_constants(sc, ctx->stream));
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_sec_count, 0, sizeof(unsigned long long), ctx->stream));
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_transported, 0, sizeof(unsigned long long), ctx->stream));
 
     rrea_dev::ElectronArgs a = sink_args(ctx, sc);
     SpeciesTile& st = ctx->tiles[species];
+    if (host) st.n = host->n;
     a.n = st.n;
     double** t = st.d;
     a.r = t[0]; a.z = t[1]; a.theta = t[2]; a.ux = t[3]; a.uy = t[4]; a.uz = t[5]; a.w = t[6];
@@ -587,28 +646,71 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     }
     a.id = st.id;
     a.cpu = st.cpu;
-#ifndef RREA_STATIC_SCHEDULE
-    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long), ctx->stream));
-    a.work = ctx->d_work;
-#endif
     a.straight_push = (species == RREA_SPECIES_PHOTON && aliased) ? 1 : 0;
     a.segments = (species != RREA_SPECIES_PHOTON && ctx->netchord) ? ctx->d_seg : nullptr;
-    if (a.n > 0) {
-        int64_t const want = (a.n + ctx->launch_threads - 1) / ctx->launch_threads;
+    // The charged kernels are long against their upload, so chunking hides
+    // the upload for the price of three extra kernel tails; the photon
+    // kernel is short and loses more to the tails than it gains.
+    int const chunks =
+        (host && species != RREA_SPECIES_PHOTON && a.n >= kPipelineMinParticles) ? kPhaseChunks : 1;
+#ifndef RREA_STATIC_SCHEDULE
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long) * chunks, ctx->stream));
+#endif
+    RREA_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+    if (host && chunks == 1) {
+        rrea_gpu_status const s = upload_range(ctx, st, host, 0, a.n, ctx->stream);
+        if (s != RREA_GPU_OK) return s;
+    }
+    if (chunks > 1) {
+        RREA_CUDA(ctx, cudaStreamWaitEvent(ctx->side[0], ctx->ev_start, 0));
+        RREA_CUDA(ctx, cudaStreamWaitEvent(ctx->side[1], ctx->ev_start, 0));
+    }
+    for (int k = 0; k < chunks && a.n > 0; ++k) {
+        int64_t const off = a.n * k / chunks;
+        int64_t const len = a.n * (k + 1) / chunks - off;
+        cudaStream_t const cs = (k % 2 == 0) ? ctx->stream : ctx->side[1];
+        if (chunks > 1) {
+            rrea_gpu_status const s = upload_range(ctx, st, host, off, len, ctx->side[0]);
+            if (s != RREA_GPU_OK) return s;
+            RREA_CUDA(ctx, cudaEventRecord(ctx->chunk_up[k], ctx->side[0]));
+            RREA_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->chunk_up[k], 0));
+        }
+        rrea_dev::ElectronArgs b = a;
+        b.n = len;
+        b.index_base = off;
+        b.r += off; b.z += off; b.theta += off; b.ux += off; b.uy += off; b.uz += off; b.w += off;
+        b.prev_r += off; b.prev_z += off; b.prev_theta += off; b.prev_ux += off; b.prev_uy += off; b.prev_uz += off;
+        b.id += off;
+        b.cpu += off;
+        b.sec_per_parent += off;
+        if (b.segments) b.segments += off;
+        if (b.diag_subcycles) b.diag_subcycles += off;
+        if (b.diag_events) b.diag_events += off;
+        if (b.diag_disposition) b.diag_disposition += off;
+#ifndef RREA_STATIC_SCHEDULE
+        b.work = ctx->d_work + k;
+#endif
+        int64_t const want = (len + ctx->launch_threads - 1) / ctx->launch_threads;
         int64_t const cap = static_cast<int64_t>(ctx->num_sms) * ctx->launch_blocks_per_sm * (128 / ctx->launch_threads);
         int const blocks = static_cast<int>(want < cap ? want : cap);
-        RREA_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
         if (species == RREA_SPECIES_PHOTON) {
-            RREA_CUDA(ctx, rrea_launch::photon_step(sc, a, blocks > 0 ? blocks : 1, ctx->launch_threads,
-                                                    c.periodic_z != 0, ctx->stream));
+            RREA_CUDA(ctx, rrea_launch::photon_step(b, blocks > 0 ? blocks : 1, ctx->launch_threads, c.periodic_z != 0,
+                                                    cs));
         } else if (species == RREA_SPECIES_POSITRON) {
-            RREA_CUDA(ctx, rrea_launch::positron_step(a, blocks > 0 ? blocks : 1, ctx->launch_threads,
-                                                      c.periodic_z != 0, ctx->stream));
+            RREA_CUDA(ctx, rrea_launch::positron_step(b, blocks > 0 ? blocks : 1, ctx->launch_threads,
+                                                      c.periodic_z != 0, cs));
         } else {
-            RREA_CUDA(ctx, rrea_launch::electron_step(a, blocks > 0 ? blocks : 1, ctx->launch_threads,
-                                                      ctx->launch_min_blocks, c.periodic_z != 0, ctx->stream));
+            RREA_CUDA(ctx, rrea_launch::electron_step(b, blocks > 0 ? blocks : 1, ctx->launch_threads,
+                                                      ctx->launch_min_blocks, c.periodic_z != 0, cs));
         }
-        RREA_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+        if (chunks > 1) RREA_CUDA(ctx, cudaEventRecord(ctx->chunk_done[k], cs));
+    }
+    if (chunks > 1) {
+        RREA_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->chunk_done[chunks - 1], 0));
+        RREA_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->chunk_done[chunks - 2], 0));
+    }
+    RREA_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+    if (a.n > 0) {
         if (a.segments) {
             RREA_CUDA(ctx, rrea_launch::netchord_deposit(a.segments, a.n, ctx->net, dt_s, ctx->d_status,
                                                          ctx->d_fail_index, ctx->num_sms * 8, ctx->stream));
@@ -664,9 +766,9 @@ rrea_gpu_status apply_phase(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile* tile,
                             rrea_gpu_secondary* secondaries, int64_t secondary_capacity, int64_t* n_secondaries)
 {
     if (!ctx || !tile || tile->n < 0) return RREA_GPU_ERR_ARGUMENT;
-    rrea_gpu_status s = stage_tile(ctx, species, tile);
+    rrea_gpu_status s = check_tile(ctx, tile);
     if (s != RREA_GPU_OK) return s;
-    s = launch_phase(ctx, species, step, dt_s, /*aliased=*/false);
+    s = launch_phase(ctx, species, step, dt_s, /*aliased=*/false, tile);
     if (s != RREA_GPU_OK) return s;
     if (n_secondaries) *n_secondaries = ctx->last_secondaries;
     if (secondaries && ctx->last_secondaries > secondary_capacity) {

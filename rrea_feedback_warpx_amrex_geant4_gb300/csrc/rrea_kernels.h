@@ -25,9 +25,10 @@ cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
                           cudaStream_t stream);
 cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, bool periodic,
                           cudaStream_t stream);
-// Photon phase (rrea_photon_kernels.cu); copies `sc` to its own constant bank.
-cudaError_t photon_step(rrea_dev::StepConstants const& sc, rrea_dev::ElectronArgs const& args, int blocks, int threads,
-                        bool periodic, cudaStream_t stream);
+// Photon phase (rrea_photon_kernels.cu): its own constant bank, set once
+// per phase before its launches.
+cudaError_t photon_constants(rrea_dev::StepConstants const& sc, cudaStream_t stream);
+cudaError_t photon_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, bool periodic, cudaStream_t stream);
 // Net-chord current (rrea_deposit.cu): replay the segment records of one
 // charged phase into the padded grid; convert the grid to physical J.
 cudaError_t netchord_deposit(rrea_dev::SegmentRec const* seg, int64_t n, rrea_dev::NetGrid const& g, double dt,

@@ -44,12 +44,13 @@ __global__ void __launch_bounds__(128, 2) photon_step_kernel(ElectronArgs A)
 
 namespace rrea_launch {
 
-cudaError_t photon_step(rrea_dev::StepConstants const& sc, rrea_dev::ElectronArgs const& args, int blocks, int threads,
-                        bool periodic, cudaStream_t stream)
+cudaError_t photon_constants(rrea_dev::StepConstants const& sc, cudaStream_t stream)
 {
-    cudaError_t const e = cudaMemcpyToSymbolAsync(rrea_dev::c_step_photon, &sc, sizeof(sc), 0, cudaMemcpyHostToDevice,
-                                                  stream);
-    if (e != cudaSuccess) return e;
+    return cudaMemcpyToSymbolAsync(rrea_dev::c_step_photon, &sc, sizeof(sc), 0, cudaMemcpyHostToDevice, stream);
+}
+
+cudaError_t photon_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, bool periodic, cudaStream_t stream)
+{
     rrea_launch::note_launch();
     if (periodic) {
         rrea_dev::photon_step_kernel<RREA_ARENA_MAX_PIECES><<<blocks, threads, 0, stream>>>(args);

@@ -203,3 +203,47 @@ def test_table_driven_exp_accuracy(mods):
     np.testing.assert_array_equal(np.isnan(f2), np.isnan(l2))
     np.testing.assert_array_equal(f2[~np.isnan(f2)], l2[~np.isnan(l2)])
     ctx.close()
+
+
+def test_chunked_drop_in_call_matches_resident_launch(mods):
+    """A drop-in call on a tile of 2^18 or more particles uploads it in
+    chunks whose kernels overlap the upload; its results equal one launch
+    over the staged tile: the same state bit for bit, the same ordered
+    secondaries and diagnostics."""
+    gpu, workloads, oracle, compare = mods
+    n = (1 << 18) + 4099
+    cfg, ctx, field = _ctx(gpu, workloads, "scaleup_c1", n)
+    arr = workloads.make_electrons("scaleup_c1", n, seed=21)
+    arr["w"][::97] = 0.0
+    arr["id"][5::113] *= -1
+    a = workloads.copy_tile(arr)
+    sec_a = ctx.apply_electrons(a, 4, 5.0e-10)
+    diag_a = ctx.diagnostics(n)
+    b = workloads.copy_tile(arr)
+    ctx.stage_electrons(b)
+    n_b = ctx.step_electrons_resident(4, 5.0e-10)
+    diag_b = ctx.diagnostics(n)
+    ctx.fetch_electrons(b)
+    assert len(sec_a) == n_b > 0
+    for f in ("r", "z", "theta", "ux", "uy", "uz", "id"):
+        np.testing.assert_array_equal(a[f], b[f], err_msg=f)
+    for x, y in zip(diag_a, diag_b):
+        np.testing.assert_array_equal(x, y)
+    ctx.pending_secondaries(discard=True)
+    ctx.close()
+
+
+def test_chunked_drop_in_positrons_match_oracle(mods):
+    """The chunked drop-in call of the positron phase (2^18 + 777 e+) against
+    the oracle, parent indices of the secondaries included."""
+    gpu, workloads, oracle, compare = mods
+    n = (1 << 18) + 777
+    cfg, ctx, field = _ctx(gpu, workloads, "scaleup_c1", n)
+    arr = workloads.make_electrons("scaleup_c1", n, seed=31)
+    g, o = compare.run_pair(ctx, cfg, field, arr, 2, 5.0e-10, species="positron")
+    # annihilation photons share the parent's total energy (kinetic + 2 m c^2)
+    e0 = workloads.kinetic_energy(arr["prev_ux"], arr["prev_uy"], arr["prev_uz"]) + 2.0 * 510998.95
+    problems = compare.compare(cfg, g, o, max(cfg.r_hi, cfg.z_hi), parent_energy=e0)
+    assert not problems, "; ".join(problems)
+    assert len(o[1]["secondaries"]) > 0 and o[1]["secondaries"]["parent_index"].max() >= (1 << 18)
+    ctx.close()
