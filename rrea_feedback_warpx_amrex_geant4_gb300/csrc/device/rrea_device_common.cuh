@@ -24,6 +24,35 @@ constexpr double kEps = 2.220446049250313080847263336181640625e-16;
 constexpr double kDblMin = 2.2250738585072013830902327173324040642192159804623318306e-308;
 constexpr double kGl2Node = 0.577350269189625764509148780501957;  // I/RreaGaussLegendre8.H:22
 
+// IEEE classification and comparisons with zero from the bit pattern.  On
+// GB300 every FP64 compare (DSETP, isfinite, isnan) takes a slot of the
+// narrow FP64 pipe, as much as an FMA; these integer forms give the same
+// answer for every input, NaN and signed zero included, on the integer pipe.
+__device__ __forceinline__ unsigned long long dbits(double x)
+{
+    return static_cast<unsigned long long>(__double_as_longlong(x));
+}
+__device__ __forceinline__ bool finite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
+__device__ __forceinline__ bool nan_bits(double x) { return (dbits(x) << 1) > 0xffe0000000000000ull; }
+__device__ __forceinline__ bool gt0(double x) { return dbits(x) - 1ull < 0x7ff0000000000000ull; }
+__device__ __forceinline__ bool ge0(double x)
+{
+    unsigned long long const b = dbits(x);
+    return b <= 0x7ff0000000000000ull || b == 0x8000000000000000ull;
+}
+__device__ __forceinline__ bool lt0(double x) { return dbits(x) - 0x8000000000000001ull < 0x7ff0000000000000ull; }
+__device__ __forceinline__ bool le0(double x)
+{
+    unsigned long long const b = dbits(x);
+    return b - 0x8000000000000000ull <= 0x7ff0000000000000ull || b == 0ull;
+}
+__device__ __forceinline__ bool eq0(double x) { return (dbits(x) << 1) == 0ull; }
+__device__ __forceinline__ bool ne0(double x) { return (dbits(x) << 1) != 0ull; }
+// fmax(x, 0.0) and fmin(x, 0.0) (a NaN operand gives the zero, as fmax and
+// fmin return the other operand) with the comparison on the integer pipe.
+__device__ __forceinline__ double max0(double x) { return gt0(x) ? x : 0.0; }
+__device__ __forceinline__ double min0(double x) { return lt0(x) ? x : 0.0; }
+
 // Division by a divisor that is reused: one IEEE reciprocal y = RN(1/b),
 // then one product per quotient, q = RN(a*y), within 1.5 ulp of RN(a/b)
 // (finite operands away from overflow and underflow).  On GB300's narrow
@@ -183,7 +212,7 @@ __device__ __forceinline__ bool bracket_hot(const double* __restrict__ arena, Rr
     b.q = q;
     b.have_t = false;
     b.t = 0.0;
-    if (!isfinite(q) || q < __ldg(x) || q > __ldg(x + n - 1)) {
+    if (!finite_bits(q) || q < __ldg(x) || q > __ldg(x + n - 1)) {
         err.set(RREA_GPU_ERR_RANGE);
         return false;
     }
@@ -225,7 +254,7 @@ __device__ __forceinline__ double eval_hot(const double* __restrict__ arena, Rre
     bracket_t(arena, h, b);
     double const ylo = __ldg(y + b.hi - 1), yhi = __ldg(y + b.hi);
     if (h.mode == RREA_INTERP_LINEAR) return ylo + b.t * (yhi - ylo);
-    bool const pos = ylo > 0.0 && yhi > 0.0;
+    bool const pos = gt0(ylo) && gt0(yhi);
     if (h.mode == RREA_INTERP_LOGX_LINEAR || (h.mode == RREA_INTERP_LOGLOG_ZERO_THRESHOLD && !pos)) {
         return ylo + b.t * (yhi - ylo);
     }
@@ -267,7 +296,7 @@ __device__ __forceinline__ double semilogx(const double* __restrict__ x, const d
                                            const double* __restrict__ ilx, const double* __restrict__ y, int n,
                                            double q, Err& err, double lq = __builtin_nan(""))
 {
-    if (!isfinite(q) || q < __ldg(x) || q > __ldg(x + n - 1)) {
+    if (!finite_bits(q) || q < __ldg(x) || q > __ldg(x + n - 1)) {
         err.set(RREA_GPU_ERR_RANGE);
         return 0.0;
     }
@@ -276,7 +305,7 @@ __device__ __forceinline__ double semilogx(const double* __restrict__ x, const d
     int const hi = lower_bound(x, n, q);
     if (__ldg(x + hi) == q) return __ldg(y + hi);
     int const lo = hi - 1;
-    double const lqq = isnan(lq) ? log(q) : lq;
+    double const lqq = nan_bits(lq) ? log(q) : lq;
     double const t = (lqq - __ldg(lx + lo)) * __ldg(ilx + hi);
     return __ldg(y + lo) + t * (__ldg(y + hi) - __ldg(y + lo));
 }
@@ -284,11 +313,11 @@ __device__ __forceinline__ double semilogx(const double* __restrict__ x, const d
 // S/RreaInteractionTables.cpp:110-119
 __device__ __forceinline__ double mfp_from_inverse(double inv, Err& err)
 {
-    if (!isfinite(inv) || inv < 0.0) {
+    if (!finite_bits(inv) || lt0(inv)) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return 1.0e99;
     }
-    return inv > 0.0 ? 1.0 / inv : 1.0e99;
+    return gt0(inv) ? 1.0 / inv : 1.0e99;
 }
 
 // The rate 1/MFP of an inverse-MFP table value as the reference forms it,
@@ -297,11 +326,11 @@ __device__ __forceinline__ double mfp_from_inverse(double inv, Err& err)
 // returning inv saves two FP64 division sequences per rate.
 __device__ __forceinline__ double rate_from_inverse(double inv, Err& err)
 {
-    if (!isfinite(inv) || inv < 0.0) {
+    if (!finite_bits(inv) || lt0(inv)) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return 1.0e-99;
     }
-    if (inv == 0.0) return 1.0e-99;
+    if (eq0(inv)) return 1.0e-99;
     if (inv < kDblMin) return 1.0 / (1.0 / inv);  // subnormal: 1/inv may overflow
     return inv;
 }
@@ -309,7 +338,7 @@ __device__ __forceinline__ double rate_from_inverse(double inv, Err& err)
 // O/RreaMaterialPath.H:213-222
 __device__ __forceinline__ double frozen_rate(double v, Err& err)
 {
-    if (!isfinite(v) || v < 0.0) {
+    if (!finite_bits(v) || lt0(v)) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return 0.0;
     }
@@ -318,7 +347,7 @@ __device__ __forceinline__ double frozen_rate(double v, Err& err)
 
 __device__ __forceinline__ bool charged_in_range(RreaArenaIndex const& ix, double e)
 {
-    return isfinite(e) && e >= ix.charged_min_eV && e <= ix.charged_max_eV;
+    return finite_bits(e) && e >= ix.charged_min_eV && e <= ix.charged_max_eV;
 }
 
 // Conditional inverse-CDF sampling: S/RreaInteractionTables.cpp:995-1069;
@@ -332,9 +361,9 @@ __device__ __forceinline__ double sample_conditional(const double* __restrict__ 
     const double* start = arena + ci.start;
     const double* u = arena + ci.u;
     const double* v = arena + ci.v;
-    cdf_u = fmax(0.0, fmin(1.0, cdf_u));
+    cdf_u = max0(fmin(1.0, cdf_u));
     int const ng = ci.ng;
-    if (!isfinite(e) || e < __ldg(prim) || e > __ldg(prim + ng - 1)) {
+    if (!finite_bits(e) || e < __ldg(prim) || e > __ldg(prim + ng - 1)) {
         err.set(RREA_GPU_ERR_RANGE);
         return 0.0;
     }
@@ -346,7 +375,7 @@ __device__ __forceinline__ double sample_conditional(const double* __restrict__ 
         if (up == en) return __ldg(v + en - 1);
         int const lo = up - 1;
         double const denom = __ldg(u + up) - __ldg(u + lo);
-        double const t = denom > 0.0 ? (cdf_u - __ldg(u + lo)) / denom : 0.0;
+        double const t = gt0(denom) ? (cdf_u - __ldg(u + lo)) / denom : 0.0;
         return __ldg(v + lo) + t * (__ldg(v + up) - __ldg(v + lo));
     };
     int const up = lower_bound(prim, ng, e);
@@ -357,7 +386,7 @@ __device__ __forceinline__ double sample_conditional(const double* __restrict__ 
     double const y0 = sample_group(lo);
     double const y1 = sample_group(up);
     double const t = (log(e) - __ldg(lprim + lo)) / (__ldg(lprim + up) - __ldg(lprim + lo));
-    if (moller || (y0 > 0.0 && y1 > 0.0)) {
+    if (moller || (gt0(y0) && gt0(y1))) {
         return exp(log(y0) + t * (log(y1) - log(y0)));
     }
     return y0 + t * (y1 - y0);
@@ -388,7 +417,7 @@ __device__ __forceinline__ double mean_conditional(const double* __restrict__ ar
     int const lo = up - 1;
     double const y0 = group_mean(arena, ci, lo), y1 = group_mean(arena, ci, up);
     double const t = (log(e) - __ldg(lprim + lo)) / (__ldg(lprim + up) - __ldg(lprim + lo));
-    if (y0 > 0.0 && y1 > 0.0) {
+    if (gt0(y0) && gt0(y1)) {
         double const l0 = __ldg(arena + ci.lmean + lo), l1 = __ldg(arena + ci.lmean + up);
         return exp(l0 + t * (l1 - l0));
     }
@@ -402,7 +431,7 @@ __device__ __forceinline__ void log_bracket(const double* __restrict__ g, const 
                                             Err& err, double lq = __builtin_nan(""))
 {
     int const last = n - 1;
-    if (!isfinite(q) || q < __ldg(g) || q > __ldg(g + last)) {
+    if (!finite_bits(q) || q < __ldg(g) || q > __ldg(g + last)) {
         err.set(RREA_GPU_ERR_RANGE);
         i = 0;
         frac = 0.0;
@@ -423,7 +452,7 @@ __device__ __forceinline__ void log_bracket(const double* __restrict__ g, const 
         frac = (q == __ldg(g + lo)) ? 0.0 : 1.0;
         return;
     }
-    frac = ((isnan(lq) ? log(q) : lq) - llo) * __ldg(ilg + hi);
+    frac = ((nan_bits(lq) ? log(q) : lq) - llo) * __ldg(ilg + hi);
 }
 
 // S/RreaInteractionTables.cpp:831-891 (node logs read precomputed)
@@ -446,11 +475,11 @@ __device__ __forceinline__ double sample_gs_angle(const double* __restrict__ are
     // zero node (reciprocal stored as 0) keeps the reference's division
     auto by_lur = [&](double x, int k) {
         double const r = __ldg(ilur + k);
-        return r != 0.0 ? x * r : x / __ldg(lur + k);
+        return ne0(r) ? x * r : x / __ldg(lur + k);
     };
     auto by_u = [&](double x, int k) {
         double const r = __ldg(icu + k);
-        return r != 0.0 ? x * r : x / __ldg(cu + k);
+        return ne0(r) ? x * r : x / __ldg(cu + k);
     };
     size_t const b00 = (static_cast<size_t>(ie) * np + ip) * nu;
     size_t const b10 = (static_cast<size_t>(ie + 1) * np + ip) * nu;

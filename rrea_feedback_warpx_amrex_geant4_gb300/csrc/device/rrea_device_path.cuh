@@ -35,16 +35,16 @@ __device__ __forceinline__ double wrap_z(Geom const& g, double z)
 {
     if (!g.periodic) return z;
     double const len = g.zhi - g.zlo;
-    if (!(len > 0.0)) return z;
+    if (!(gt0(len))) return z;
     double w = fmod(z - g.zlo, len);
-    if (w < 0.0) w += len;
+    if (lt0(w)) w += len;
     return g.zlo + w;
 }
 // S/RreaTransportPath.cpp:42-52
 template <int NP>
 __device__ __forceinline__ void point_at_full(Path<NP> const& p, Geom const& g, double f, double& x, double& y, double& z)
 {
-    f = fmax(0.0, fmin(1.0, f));
+    f = max0(fmin(1.0, f));
     x = p.sx + f * (p.ex - p.sx);
     y = p.sy + f * (p.ey - p.sy);
     z = wrap_z(g, p.sz + f * (p.ez - p.sz));
@@ -63,7 +63,7 @@ __device__ __forceinline__ void point_at_piece(Path<NP> const& p, Geom const& g,
 // S/RreaTransportPath.cpp:29-40
 __device__ __forceinline__ bool outside_certified(Geom const& g, double r, double z)
 {
-    if (!isfinite(r) || !isfinite(z)) return true;
+    if (!finite_bits(r) || !finite_bits(z)) return true;
     if (r < g.rlo || r >= g.rhi) return true;
     return !g.periodic && (z < g.zlo || z >= g.zhi);
 }
@@ -75,7 +75,7 @@ template <int NP>
 __device__ __forceinline__ void clip_chord(double x0, double y0, double z0, double r0, double x1, double y1, double z1,
                                            double r1, bool ends_finite, Geom const& g, Path<NP>& p, Err& err)
 {
-    if (!ends_finite || !isfinite(r0) || !isfinite(z0) || !isfinite(r1) || !isfinite(z1) || r0 < 0.0 || r1 < 0.0) {
+    if (!ends_finite || !finite_bits(r0) || !finite_bits(z0) || !finite_bits(r1) || !finite_bits(z1) || lt0(r0) || lt0(r1)) {
         err.set(RREA_GPU_ERR_GEOMETRY);
         p.npieces = 0;
         p.full = 0.0;
@@ -99,37 +99,37 @@ __device__ __forceinline__ void clip_chord(double x0, double y0, double z0, doub
     }
     double exit_fraction = 1.0;
     if (!g.periodic) {
-        if (dz > 0.0) {
+        if (gt0(dz)) {
             double const c = (g.zhi - z0) / dz;
-            if (c >= 0.0 && c < exit_fraction) exit_fraction = c;
-        } else if (dz < 0.0) {
+            if (ge0(c) && c < exit_fraction) exit_fraction = c;
+        } else if (lt0(dz)) {
             double const c = (g.zlo - z0) / dz;
-            if (c >= 0.0 && c < exit_fraction) exit_fraction = c;
+            if (ge0(c) && c < exit_fraction) exit_fraction = c;
         }
     }
     double const a = dx * dx + dy * dy;
-    if (a > 0.0) {
+    if (gt0(a)) {
         double const b = 2.0 * (p.sx * dx + p.sy * dy);
         for (int cyl = 0; cyl < 2; ++cyl) {
             bool const outer = cyl == 0;
             double const radius = outer ? g.rhi : g.rlo;
-            if (!outer && !(g.rlo > 0.0)) break;
+            if (!outer && !(gt0(g.rlo))) break;
             double const c = p.sx * p.sx + p.sy * p.sy - radius * radius;
             double const disc = b * b - 4.0 * a * c;
-            if (disc < 0.0) continue;
-            double const root = sqrt(fmax(disc, 0.0));
+            if (lt0(disc)) continue;
+            double const root = sqrt(max0(disc));
             double const inv2a = 0.5 / a;
             double const roots[2] = {(-b - root) * inv2a, (-b + root) * inv2a};
             for (int q = 0; q < 2; ++q) {
                 double const cand = roots[q];
-                if (cand <= 0.0 || cand > 1.0) continue;
+                if (le0(cand) || cand > 1.0) continue;
                 double const deriv = 2.0 * a * cand + b;
-                bool const leaves = outer ? deriv > 0.0 : deriv < 0.0;
-                if (leaves && cand >= 0.0 && cand < exit_fraction) exit_fraction = cand;
+                bool const leaves = outer ? gt0(deriv) : deriv < 0.0;
+                if (leaves && ge0(cand) && cand < exit_fraction) exit_fraction = cand;
             }
         }
     }
-    p.in_end = fmax(0.0, fmin(1.0, exit_fraction));
+    p.in_end = max0(fmin(1.0, exit_fraction));
     p.in_length = p.full * (p.in_end - p.in_begin);
     p.exits = p.in_end < 1.0 - 64.0 * kEps;
 
@@ -210,7 +210,7 @@ template <int NP>
 __device__ __forceinline__ void clip_rz(double r0, double th0, double z0, double r1, double th1, double z1,
                                         Geom const& g, Path<NP>& p, Err& err)
 {
-    bool const finite = isfinite(th0) && isfinite(th1);
+    bool const finite = finite_bits(th0) && finite_bits(th1);
     double s0 = 0.0, c0 = 1.0, s1 = 0.0, c1 = 1.0;
     if (finite) {
         sincos(th0, &s0, &c0);
@@ -228,7 +228,7 @@ template <int NP>
 __device__ __forceinline__ void clip_xyz(double x0, double y0, double z0, double x1, double y1, double z1, Geom const& g,
                                          Path<NP>& p, Err& err)
 {
-    bool const finite = isfinite(x0) && isfinite(y0) && isfinite(x1) && isfinite(y1);
+    bool const finite = finite_bits(x0) && finite_bits(y0) && finite_bits(x1) && finite_bits(y1);
     clip_chord(x0, y0, z0, rz_radius(x0, y0), x1, y1, z1, rz_radius(x1, y1), finite, g, p, err);
 }
 
@@ -236,9 +236,9 @@ __device__ __forceinline__ void clip_xyz(double x0, double y0, double z0, double
 // I/RreaSeedSchedule.H:31-43
 __device__ __forceinline__ double proper_velocity_from_kinetic(double k)
 {
-    if (k <= 0.0) return 0.0;
+    if (le0(k)) return 0.0;
     double const gm = 1.0 + k * kInvMeC2;
-    return kC * sqrt(fmax(gm * gm - 1.0, 0.0));
+    return kC * sqrt(max0(gm * gm - 1.0));
 }
 // O/RreaParticleInteraction.H:1494-1506
 __device__ __forceinline__ double kinetic_from_proper_velocity(double ux, double uy, double uz)
@@ -250,9 +250,9 @@ __device__ __forceinline__ double kinetic_from_proper_velocity(double ux, double
 // O/RreaParticleInteraction.H:92-105
 __device__ __forceinline__ double charged_speed(double k)
 {
-    if (!isfinite(k) || k < 0.0) return __longlong_as_double(0x7ff8000000000000LL);
+    if (!finite_bits(k) || lt0(k)) return __longlong_as_double(0x7ff8000000000000LL);
     double const gm = 1.0 + k * kInvMeC2;
-    double const b2 = fmax(0.0, 1.0 - 1.0 / (gm * gm));
+    double const b2 = max0(1.0 - 1.0 / (gm * gm));
     return kC * sqrt(b2);
 }
 // O/RreaChargedInterleave.H:294-307.  The reference divides by sqrt(n2);
@@ -262,7 +262,7 @@ __device__ __forceinline__ double charged_speed(double k)
 __device__ __forceinline__ void normalize(double& x, double& y, double& z)
 {
     double const n2 = x * x + y * y + z * z;
-    if (!(n2 > 0.0)) {
+    if (!(gt0(n2))) {
         x = 0.0; y = 0.0; z = 1.0;
         return;
     }
@@ -287,7 +287,7 @@ __device__ __forceinline__ void cone_direction(double ax, double ay, double az, 
     normalize(b1x, b1y, b1z);
     double const b2x = dy * b1z - dz * b1y, b2y = dz * b1x - dx * b1z, b2z = dx * b1y - dy * b1x;
     cos_t = fmin(1.0, fmax(-1.0, cos_t));
-    double const sin_t = sqrt(fmax(0.0, 1.0 - cos_t * cos_t));
+    double const sin_t = sqrt(max0(1.0 - cos_t * cos_t));
     double const phi = kTwoPi * u_phi;
     double sp, cp;
     sincos(phi, &sp, &cp);
@@ -298,7 +298,7 @@ __device__ __forceinline__ void cone_direction(double ax, double ay, double az, 
 // O/RreaChargedInterleave.H:371-389
 __device__ __forceinline__ int poisson_capped(double mean, double u, int kmax)
 {
-    if (mean <= 0.0) return 0;
+    if (le0(mean)) return 0;
     double p = exp(-mean);
     double cum = p;
     int k = 0;
@@ -312,13 +312,13 @@ __device__ __forceinline__ int poisson_capped(double mean, double u, int kmax)
 __device__ __forceinline__ double unit_cycle(double u)
 {
     u -= floor(u);
-    return u < 0.0 ? u + 1.0 : u;
+    return lt0(u) ? u + 1.0 : u;
 }
 // O/RreaChargedInterleave.H:391-463
 __device__ __forceinline__ double moller_cos(double kp, double ks_or_scat)
 {
     double const v = ks_or_scat * (kp + 2.0 * kMeC2) / (kp * (ks_or_scat + 2.0 * kMeC2));
-    return sqrt(fmin(1.0, fmax(0.0, v)));
+    return sqrt(fmin(1.0, max0(v)));
 }
 __device__ __forceinline__ void moller_lab_directions(double px, double py, double pz, double kp, double ks,
                                                       double u_az, double& opx, double& opy, double& opz,
@@ -328,13 +328,13 @@ __device__ __forceinline__ void moller_lab_directions(double px, double py, doub
     u_az = unit_cycle(u_az);
     double cs;
     {
-        double const a = fmax(kp, 0.0), b = fmax(ks, 0.0);
-        cs = (a <= 0.0 || b <= 0.0) ? 1.0 : moller_cos(a, b);
+        double const a = max0(kp), b = max0(ks);
+        cs = (le0(a) || le0(b)) ? 1.0 : moller_cos(a, b);
     }
     double cpm;
     {
-        double const scat = fmax(0.0, kp - ks);
-        cpm = (kp <= 0.0 || scat <= 0.0) ? 1.0 : moller_cos(kp, scat);
+        double const scat = max0(kp - ks);
+        cpm = (le0(kp) || le0(scat)) ? 1.0 : moller_cos(kp, scat);
     }
     cone_direction(px, py, pz, cs, u_az, osx, osy, osz);
     cone_direction(px, py, pz, cpm, unit_cycle(u_az + 0.5), opx, opy, opz);
@@ -343,14 +343,14 @@ __device__ __forceinline__ void moller_lab_directions(double px, double py, doub
 __device__ __forceinline__ void photon_recoil(double k0, double eg, double gx, double gy, double gz, double& cx,
                                               double& cy, double& cz)
 {
-    eg = fmax(eg, 0.0);
-    if (k0 <= 0.0 || eg <= 0.0) return;
+    eg = max0(eg);
+    if (le0(k0) || le0(eg)) return;
     normalize(cx, cy, cz);
     normalize(gx, gy, gz);
-    double const p0 = sqrt(fmax(0.0, k0 * (k0 + 2.0 * kMeC2)));
+    double const p0 = sqrt(max0(k0 * (k0 + 2.0 * kMeC2)));
     double const px = p0 * cx - eg * gx, py = p0 * cy - eg * gy, pz = p0 * cz - eg * gz;
     double const n = sqrt(px * px + py * py + pz * pz);
-    if (n > 0.0) {
+    if (gt0(n)) {
         Divisor const d = make_divisor(n);
         cx = quot(px, d); cy = quot(py, d); cz = quot(pz, d);
         normalize(cx, cy, cz);
@@ -384,11 +384,11 @@ __device__ __forceinline__ void half_kick(FieldRange const& f, double half_dt, d
     double const uy = uym + ppz * sx - ppx * sz;
     double const uz = uzm + ppx * sy - ppy * sx;
     double const norm = sqrt(ux * ux + uy * uy + uz * uz);
-    if (norm > 0.0 && isfinite(norm)) {
+    if (gt0(norm) && finite_bits(norm)) {
         Divisor const dn = make_divisor(norm);
         dx = quot(ux, dn); dy = quot(uy, dn); dz = quot(uz, dn);
     }
-    k = fmax(0.0, k + 0.5 * f.work);
+    k = max0(k + 0.5 * f.work);
 }
 
 // ------------------------------------------------------------ field gather
@@ -433,16 +433,16 @@ __device__ __forceinline__ void gather(FieldView const& fv, double r, double z, 
     double const z00 = __ldg(fv.cell_ez + i0 + r0), z01 = __ldg(fv.cell_ez + i0 + r1);
     double const z10 = __ldg(fv.cell_ez + i1 + r0), z11 = __ldg(fv.cell_ez + i1 + r1);
     double const first_center = fv.r_lo + 0.5 * fv.dr;
-    double const axis = r >= first_center ? 1.0 : fmax(0.0, (r - fv.r_lo) / (0.5 * fv.dr));
+    double const axis = r >= first_center ? 1.0 : max0((r - fv.r_lo) / (0.5 * fv.dr));
     er = ((1.0 - tx) * ((1.0 - tz) * e00 + tz * e01) + tx * ((1.0 - tz) * e10 + tz * e11)) * axis;
     ez = (1.0 - tx) * ((1.0 - tz) * z00 + tz * z01) + tx * ((1.0 - tz) * z10 + tz * z11);
-    if (!fv.has_b || r <= 0.0) {
+    if (!fv.has_b || le0(r)) {
         bth = 0.0;
-        if (!fv.has_b && r > 0.0) bth = 0.0;
+        if (!fv.has_b && gt0(r)) bth = 0.0;
         return;
     }
-    double const fr = fmin(fmax(quot(r, fv.div_dr), 0.0), static_cast<double>(fv.nr));
-    double const fzz = fmin(fmax(quot(z - fv.z_lo, fv.div_dz), 0.0), static_cast<double>(fv.nz));
+    double const fr = fmin(max0(quot(r, fv.div_dr)), static_cast<double>(fv.nr));
+    double const fzz = fmin(max0(quot(z - fv.z_lo, fv.div_dz)), static_cast<double>(fv.nz));
     int const a0 = min(static_cast<int>(floor(fr)), fv.nr - 1);
     int const b0 = min(static_cast<int>(floor(fzz)), fv.nz - 1);
     double const tr = fr - a0, tzz = fzz - b0;
@@ -458,7 +458,7 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
                                                       double begin, double end, Err& err)
 {
     FieldRange res{0, 0, 0, 0, 0, 0, 0, 0};
-    if (!(p.full > 0.0)) return res;
+    if (!(gt0(p.full))) return res;
     begin = fmax(p.in_begin, begin);
     end = fmin(p.in_end, end);
     if (!(end > begin)) return res;
@@ -486,7 +486,7 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
             // ulps of hypot and of the quotients by it)
             double const r2 = fma(x, x, y * y);
             double r = 0.0, rad = 0.0, rc = 1.0, rs = 0.0;
-            if (r2 > 0.0) {
+            if (gt0(r2)) {
                 double const inv = rsqrt(r2);
                 r = r2 * inv;
                 rad = (pdx * x + pdy * y) * inv;
@@ -496,7 +496,7 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
             double er, ez, bth;
             gather(fv, r, z, er, ez, bth);
             double const work = q * (er * rad + ez * pdz) * 1.0;
-            if (!isfinite(work) || !isfinite(er) || !isfinite(ez) || !isfinite(bth)) {
+            if (!finite_bits(work) || !finite_bits(er) || !finite_bits(ez) || !finite_bits(bth)) {
                 err.set(RREA_GPU_ERR_INVALID_STATE);
             }
             double const v[7] = {work, er * rc, er * rs, ez, -bth * rs, bth * rc, 0.0};
@@ -517,7 +517,7 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
         res.bz += p.full * acc[6];
         res.length += p.full * (pe - pb);
     }
-    if (res.length > 0.0) {
+    if (gt0(res.length)) {
         Divisor const dl = make_divisor(res.length);
         res.ex = quot(res.ex, dl); res.ey = quot(res.ey, dl); res.ez = quot(res.ez, dl);
         res.bx = quot(res.bx, dl); res.by = quot(res.by, dl); res.bz = quot(res.bz, dl);
@@ -534,7 +534,7 @@ struct Intervals {
     double begin[NP], end[NP], length[NP], density[NP];
 };
 
-__device__ __forceinline__ double positive_or(double v, double fb) { return v > 0.0 ? v : fb; }
+__device__ __forceinline__ double positive_or(double v, double fb) { return gt0(v) ? v : fb; }
 
 // :60-114
 template <int NP>
@@ -543,9 +543,9 @@ __device__ __forceinline__ void build_intervals(Path<NP> const& p, double rho, I
     iv.n = 0;
     if constexpr (NP == 1) {
         Piece const& pc = p.pieces[0];
-        if (p.npieces < 1 || !(pc.length > 0.0)) return;
+        if (p.npieces < 1 || !(gt0(pc.length))) return;
         double dl = 0.0;
-        if (pc.end > pc.begin && p.full > 0.0) dl = p.full * (pc.end - pc.begin) * positive_or(rho, rho);
+        if (pc.end > pc.begin && gt0(p.full)) dl = p.full * (pc.end - pc.begin) * positive_or(rho, rho);
         iv.begin[0] = pc.begin;
         iv.end[0] = pc.end;
         iv.length[0] = pc.length;
@@ -554,9 +554,9 @@ __device__ __forceinline__ void build_intervals(Path<NP> const& p, double rho, I
     } else {
         for (int i = 0; i < p.npieces; ++i) {
             Piece const& pc = p.pieces[i];
-            if (!(pc.length > 0.0)) continue;
+            if (!(gt0(pc.length))) continue;
             double dl = 0.0;
-            if (pc.end > pc.begin && p.full > 0.0) dl = p.full * (pc.end - pc.begin) * positive_or(rho, rho);
+            if (pc.end > pc.begin && gt0(p.full)) dl = p.full * (pc.end - pc.begin) * positive_or(rho, rho);
             iv.begin[iv.n] = pc.begin;
             iv.end[iv.n] = pc.end;
             iv.length[iv.n] = pc.length;
@@ -588,7 +588,7 @@ __device__ __forceinline__ double fraction_at_density_path(Intervals<NP> const& 
 {
     b = fmax(p.in_begin, b);
     e = fmin(p.in_end, e);
-    if (!isfinite(target) || target < 0.0) {
+    if (!finite_bits(target) || lt0(target)) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return e;
     }
@@ -597,7 +597,7 @@ __device__ __forceinline__ double fraction_at_density_path(Intervals<NP> const& 
     for (int i = 0; i < NP; ++i) {
         if (i >= iv.n) break;
         double const bb = fmax(b, iv.begin[i]), ee = fmin(e, iv.end[i]);
-        if (!(ee > bb) || !(iv.density[i] > 0.0)) continue;
+        if (!(ee > bb) || !(gt0(iv.density[i]))) continue;
         double const c = p.full * (ee - bb) * iv.density[i];
         if (rem <= c) return bb + rem / (p.full * iv.density[i]);
         rem -= c;
@@ -630,27 +630,27 @@ __device__ __forceinline__ Selection select_hazard(const double* __restrict__ ar
 {
     Selection r{false, false, -1, 0.0, 0.0};
     double const taus[3] = {t0, t1, t2};
-    if (count < 1 || count > 3 || !isfinite(u1) || !isfinite(u2)) return r;
+    if (count < 1 || count > 3 || !finite_bits(u1) || !finite_bits(u2)) return r;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         if (i >= count) break;
-        if (!isfinite(taus[i]) || taus[i] < 0.0) return r;
+        if (!finite_bits(taus[i]) || lt0(taus[i])) return r;
         r.total += taus[i];
     }
-    r.valid = isfinite(r.total);
+    r.valid = finite_bits(r.total);
     if (!r.valid) return r;
-    u1 = fmax(0.0, fmin(1.0, u1));
+    u1 = max0(fmin(1.0, u1));
     r.sampled = -flog(arena, fmax(1.0e-30, 1.0 - u1));
     if (!(r.sampled < r.total)) return r;
     r.event = true;
-    u2 = fmax(0.0, fmin(1.0, u2));
+    u2 = max0(fmin(1.0, u2));
     double const target = u2 * r.total;
     double cum = 0.0;
     int last_open = -1;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         if (i >= count) break;
-        if (taus[i] > 0.0) last_open = i;
+        if (gt0(taus[i])) last_open = i;
         cum += taus[i];
         if (target < cum) {
             r.channel = i;
@@ -667,9 +667,9 @@ __device__ __forceinline__ Selection select_hazard(const double* __restrict__ ar
 // O/RreaParticleInteraction.H:318-354
 __device__ __forceinline__ bool cartesian_half_open(Geom const& g, double x, double y, double z)
 {
-    if (!isfinite(x) || !isfinite(y)) return false;
+    if (!finite_bits(x) || !finite_bits(y)) return false;
     double const r = rz_radius(x, y);
-    return isfinite(r) && isfinite(z) && g.rhi > g.rlo && g.zhi > g.zlo && r >= g.rlo && r < g.rhi && z >= g.zlo
+    return finite_bits(r) && finite_bits(z) && g.rhi > g.rlo && g.zhi > g.zlo && r >= g.rlo && r < g.rhi && z >= g.zlo
         && z < g.zhi;
 }
 // RreaChargedBoundaryCrossingForPath (O/RreaParticleInteraction.H:468-540):
@@ -695,13 +695,13 @@ __device__ __forceinline__ bool charged_crossing(Path<NP> const& p, Geom const& 
     double const outward = cx * dx + cy * dy;
     faces = 0u;
     if (on_r && outward > -tol * scale) { faces |= 1u; cr = g.rhi; }
-    if (on_zlo && dz < 0.0) { faces |= 2u; cz = g.zlo; }
-    if (on_zhi && dz > 0.0) { faces |= 4u; cz = g.zhi; }
+    if (on_zlo && lt0(dz)) { faces |= 2u; cz = g.zlo; }
+    if (on_zhi && gt0(dz)) { faces |= 4u; cz = g.zhi; }
     if (faces == 0u) {
         if (on_r) { faces |= 1u; cr = g.rhi; }
         if (on_zhi) { faces |= 4u; cz = g.zhi; }
     }
-    return faces != 0u && isfinite(sr) && isfinite(sz) && isfinite(cr) && isfinite(cz);
+    return faces != 0u && finite_bits(sr) && finite_bits(sz) && finite_bits(cr) && finite_bits(cz);
 }
 
 // O/RreaParticleInteraction.H:409-452 (clipped policy: RREA owns every escape)
@@ -709,7 +709,7 @@ template <int NP>
 __device__ __forceinline__ void clipped_escape_policy(Path<NP> const& p, Geom const& g, double er, double ez,
                                                       bool& escapes, bool& invalidate)
 {
-    if (!isfinite(er) || !isfinite(ez)) {
+    if (!finite_bits(er) || !finite_bits(ez)) {
         escapes = true;
         invalidate = true;
         return;

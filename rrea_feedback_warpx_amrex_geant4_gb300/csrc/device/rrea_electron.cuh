@@ -67,7 +67,7 @@ __device__ __forceinline__ bool rate_positive(StepConstants const& C, const doub
 {
     if (!rate_bracket(C, arena, rc, e, err, base)) return false;
     unsigned const bit = 1u << which;
-    if (rc.have & bit) return rc.v[which] > 0.0;
+    if (rc.have & bit) return gt0(rc.v[which]);
     return positive_hot(arena, C.tix.hot[base + which], rc.b, err);
 }
 
@@ -80,13 +80,13 @@ __device__ __forceinline__ void competing_rates(StepConstants const& C, const do
                                                 RateCache& rc, double e, double& s0, double& s1, Err& err)
 {
     double const thr = C.hm_threshold_eV;
-    bool const m_open = C.hm_enabled && thr > 0.0 && e > 2.0 * thr;
-    bool const b_open = isfinite(e) && isfinite(C.photon_cutoff_eV) && e > C.photon_cutoff_eV;
+    bool const m_open = C.hm_enabled && gt0(thr) && e > 2.0 * thr;
+    bool const b_open = finite_bits(e) && finite_bits(C.photon_cutoff_eV) && e > C.photon_cutoff_eV;
     s0 = 0.0;
     s1 = 0.0;
     if (m_open) {
         double const inv = rate_value(C, arena, rc, e, kRateMoller, err);
-        s0 = (thr > 0.0 && e <= 2.0 * thr) ? 1.0e-99 : rate_from_inverse(inv * 1.0, err);
+        s0 = (gt0(thr) && e <= 2.0 * thr) ? 1.0e-99 : rate_from_inverse(inv * 1.0, err);
     }
     if (b_open) {
         s1 = rate_from_inverse(rate_value(C, arena, rc, e, kRateBrems, err) * 1.0, err);
@@ -107,7 +107,7 @@ __device__ __forceinline__ void competing_rates_positron(StepConstants const& C,
     double const thr = C.hm_threshold_eV;
     s0 = 0.0;
     s1 = 0.0;
-    if (!(thr > 0.0 && e <= thr)) {
+    if (!(gt0(thr) && e <= thr)) {
         s0 = rate_from_inverse(rate_value(C, arena, rc, e, kRateBhabha, err, RREA_T_P_COLLISION) * 1.0, err);
     }
     if (e > C.photon_cutoff_eV) {
@@ -125,10 +125,10 @@ __device__ __forceinline__ double hard_moller_energy_loss(StepConstants const& C
 {
     RreaTable1DIndex const& h = C.tix.hot[RREA_T_E_HARD_MOLLER];
     double const inv = interpolate(arena, h, e, err);
-    if (!(inv > 0.0)) return 0.0;
+    if (!(gt0(inv))) return 0.0;
     double const mean =
         semilogx(arena + h.x, arena + h.lx, arena + h.ilx, arena + C.tix.hard_moller_mean_secondary, h.n, e, err);
-    if (!(mean > 0.0)) return 0.0;
+    if (!(gt0(mean))) return 0.0;
     return mean * inv * dr;
 }
 
@@ -139,7 +139,7 @@ __device__ __forceinline__ double elastic_inverse_stp(StepConstants const& C, co
 {
     RreaElasticIndex const& el = C.tix.elastic[species];
     double const mfp = semilogx(arena + el.x, arena + el.lx, arena + el.ilx, arena + el.mfp, el.n, e, err, le) / 1.0;
-    return frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0, err);
+    return frozen_rate(gt0(mfp) ? 1.0 / mfp : 0.0, err);
 }
 
 // S/RreaInteractionTables.cpp:2504-2560
@@ -151,7 +151,7 @@ __device__ __forceinline__ double sample_gs_cos(StepConstants const& C, const do
         err.set(RREA_GPU_ERR_RANGE);
         return 1.0;
     }
-    if (!isfinite(u) || u < 0.0 || u > 1.0) {
+    if (!finite_bits(u) || lt0(u) || u > 1.0) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return 1.0;
     }
@@ -161,7 +161,7 @@ __device__ __forceinline__ double sample_gs_cos(StepConstants const& C, const do
         err.set(RREA_GPU_ERR_RANGE);
         return 1.0;
     }
-    if (!isfinite(n) || n < ix.gs_few_collision_threshold) {
+    if (!finite_bits(n) || n < ix.gs_few_collision_threshold) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return 1.0;
     }
@@ -178,7 +178,7 @@ __device__ __forceinline__ double sample_single_elastic_cos(StepConstants const&
     }
     RreaElasticIndex const& el = C.tix.elastic[species];
     double const eta = semilogx(arena + el.x, arena + el.lx, arena + el.ilx, arena + el.eta, el.n, e, err, le);
-    double const u = fmin(fmax(cdf_u, 0.0), 1.0 - 1.0e-15);
+    double const u = fmin(max0(cdf_u), 1.0 - 1.0e-15);
     return 1.0 - 2.0 * eta * u / (1.0 + eta - u);
 }
 // S/RreaInteractionTables.cpp:2714-2760
@@ -195,8 +195,8 @@ __device__ __forceinline__ double sample_brems_cos(StepConstants const& C, doubl
         err.set(RREA_GPU_ERR_RANGE);
         return 1.0;
     }
-    cdf_u = fmax(0.0, fmin(1.0, cdf_u));
-    if (cdf_u == 0.0) return 1.0;
+    cdf_u = max0(fmin(1.0, cdf_u));
+    if (eq0(cdf_u)) return 1.0;
     if (cdf_u == 1.0) return -1.0;
     double constexpr a = 0.625;
     double const umax = 2.0 * (1.0 + e / kMeC2);
@@ -234,7 +234,7 @@ __device__ __forceinline__ void moller_final_state(StepConstants const& C, Elect
     double pdx, pdy, pdz, sdx, sdy, sdz;
     moller_lab_directions(dx, dy, dz, kb, sec, rng.uniform(rng_index, kChHardMollerAzimuth), pdx, pdy, pdz, sdx, sdy,
                           sdz);
-    k = fmax(0.0, kb - sec);
+    k = max0(kb - sec);
     dx = pdx; dy = pdy; dz = pdz;
     append_secondary(A, ip, key, weight, lineage, 0, 2, site.x, site.y, site.z, sdx, sdy, sdz, sec, site.birth, err);
     deposit_source(C, A.cells, 0, site.r, site.z, weight, sec, sec);
@@ -263,9 +263,9 @@ __device__ __forceinline__ void brems_final_state(StepConstants const& C, Electr
     double const sampled = sample_conditional(A.arena, C.tix.cdf[POS ? RREA_C_BREMS_P : RREA_C_BREMS_E], kb,
                                               rng.uniform(rng_index, POS ? kChPositronBremsEnergy : kChBremsEnergy),
                                               false, err);
-    double const eg = fmin(fmax(sampled, 0.0), fmax(kb, 0.0));
-    double const after = fmax(0.0, fmax(kb, 0.0) - eg);
-    bool const tracked = isfinite(C.photon_cutoff_eV) && C.photon_cutoff_eV >= 0.0 && eg >= C.photon_cutoff_eV;
+    double const eg = fmin(max0(sampled), max0(kb));
+    double const after = max0(fmax(kb, 0.0) - eg);
+    bool const tracked = finite_bits(C.photon_cutoff_eV) && ge0(C.photon_cutoff_eV) && eg >= C.photon_cutoff_eV;
     double const ct = sample_brems_cos(C, kb, rng.uniform(rng_index, POS ? kChPositronBremsAngle : kChBremsAngle), err);
     double gx, gy, gz;
     cone_direction(dx, dy, dz, ct, rng.uniform(rng_index, POS ? kChPositronBremsAzimuth : kChBremsAzimuth), gx, gy,
@@ -275,18 +275,18 @@ __device__ __forceinline__ void brems_final_state(StepConstants const& C, Electr
     if (tracked) {
         append_secondary(A, ip, key, weight, lineage, 2, 4, site.x, site.y, site.z, gx, gy, gz, eg, site.birth, err,
                          POS ? 1 : 0);
-    } else if (eg > 0.0) {
+    } else if (gt0(eg)) {
         // deposit_local_energy_as_ion_pairs, O/RreaTransportStep.H:530-561
         double const w_air = C.tix.w_air_eV_per_pair;
         double const pw = weight * eg / fmax(w_air, 1.0);
-        if (weight > 0.0 && pw > 0.0) deposit_source(C, A.cells, 0, site.r, site.z, pw, 0.0, w_air);
+        if (gt0(weight) && gt0(pw)) deposit_source(C, A.cells, 0, site.r, site.z, pw, 0.0, w_air);
     }
     // closure of the Bremsstrahlung group (O/RreaChargedFinalStates.H:377-393)
     double const cut = C.cfg.low_energy_cutoff_eV;
     GroupClosure gc;
     gc.begin(POS ? 1.0 : -1.0, kMeC2, weight, kb, after, true);
     if (tracked) gc.secondary(0.0, 0.0, weight, eg);
-    else if (eg > 0.0) gc.local(weight, eg, C.tix.w_air_eV_per_pair, cut);
+    else if (gt0(eg)) gc.local(weight, eg, C.tix.w_air_eV_per_pair, cut);
     if (!gc.valid(cut)) err.set(RREA_GPU_ERR_INVALID_STATE);
 }
 
@@ -313,13 +313,13 @@ __device__ __forceinline__ void bhabha_final_state(StepConstants const& C, Elect
     }
     double const sec = fmin(sample_conditional(A.arena, C.tix.cdf[RREA_C_BHABHA], kb,
                                                rng.uniform(rng_index, kChPositronBhabhaEnergy), false, err),
-                            fmax(0.0, kb));
+                            max0(kb));
     double const thr = C.hm_threshold_eV;
-    if (!(sec > 0.0) || (thr > 0.0 && sec < thr)) return;
+    if (!(gt0(sec)) || (gt0(thr) && sec < thr)) return;
     double pdx, pdy, pdz, sdx, sdy, sdz;
     moller_lab_directions(dx, dy, dz, kb, sec, rng.uniform(rng_index, kChPositronBhabhaAzimuth), pdx, pdy, pdz, sdx,
                           sdy, sdz);
-    k = fmax(0.0, kb - sec);
+    k = max0(kb - sec);
     dx = pdx; dy = pdy; dz = pdz;
     append_secondary(A, ip, key, weight, lineage, 0, 3, site.x, site.y, site.z, sdx, sdy, sdz, sec, site.birth, err, 1);
     deposit_source(C, A.cells, 2, site.r, site.z, weight, 0.0, sec);
@@ -337,16 +337,16 @@ __device__ __forceinline__ void bhabha_final_state(StepConstants const& C, Elect
 __device__ __forceinline__ double annihilation_fraction(double gamma, double draw)
 {
     if (gamma <= 1.0 + 1.0e-12) return 0.5;
-    double const bcm = sqrt(fmax(0.0, (gamma - 1.0) / (gamma + 1.0)));
+    double const bcm = sqrt(max0((gamma - 1.0) / (gamma + 1.0)));
     double const emin = 0.5 * (1.0 - bcm), emax = 0.5 * (1.0 + bcm);
-    double const u = isfinite(draw) ? fmax(0.0, fmin(1.0, draw)) : 0.5;
+    double const u = finite_bits(draw) ? max0(fmin(1.0, draw)) : 0.5;
     double const gp1 = gamma + 1.0;
     double const a = 1.0 + 2.0 * gamma / (gp1 * gp1);
     double const c = gp1 * gp1;
     double const flo = a * log(emin) - emin + 1.0 / (c * emin);
     double const fhi = a * log(emax) - emax + 1.0 / (c * emax);
     double const span = fhi - flo;
-    if (!(span > 0.0)) return 0.5;
+    if (!(gt0(span))) return 0.5;
     double const target = flo + u * span;
     double lo = emin, hi = emax;
     for (int it = 0; it < 64; ++it) {
@@ -369,10 +369,10 @@ static __device__ __noinline__ uint32_t spawn_annihilation(ElectronArgs A, RngSt
 {
     StepConstants const& C = c_step;
     Err err;
-    if (weight <= 0.0) return lineage;
+    if (le0(weight)) return lineage;
     normalize(ax, ay, az);
-    double const ka = at_rest ? 0.0 : fmax(k, 0.0);
-    if (!(ka == 0.0) && !charged_in_range(C.tix, ka)) {
+    double const ka = at_rest ? 0.0 : max0(k);
+    if (!(eq0(ka)) && !charged_in_range(C.tix, ka)) {
         record_failure(A, RREA_GPU_ERR_RANGE, ip);
         return lineage;
     }
@@ -385,29 +385,29 @@ static __device__ __noinline__ uint32_t spawn_annihilation(ElectronArgs A, RngSt
     if (gamma <= 1.0 + 1.0e-10) {
         e1 = kMeC2;
         e2 = kMeC2;
-        cos1 = 2.0 * (isfinite(d_e) ? fmax(0.0, fmin(1.0, d_e)) : 0.5) - 1.0;
-        azim = isfinite(d_a) ? d_a - floor(d_a) : 0.0;
-        if (azim < 0.0) azim += 1.0;
+        cos1 = 2.0 * (finite_bits(d_e) ? max0(fmin(1.0, d_e)) : 0.5) - 1.0;
+        azim = finite_bits(d_a) ? d_a - floor(d_a) : 0.0;
+        if (lt0(azim)) azim += 1.0;
         rest = true;
     } else {
-        double const beta = sqrt(fmax(0.0, 1.0 - 1.0 / (gamma * gamma)));
+        double const beta = sqrt(max0(1.0 - 1.0 / (gamma * gamma)));
         double const eps = annihilation_fraction(gamma, d_e);
         e1 = eps * total;
-        e2 = fmax(0.0, total - e1);
+        e2 = max0(total - e1);
         double const denom = eps * gamma * beta;
-        if (e1 > 0.0 && e2 > 0.0 && denom > 0.0) {
+        if (gt0(e1) && gt0(e2) && gt0(denom)) {
             cos1 = fmax(-1.0, fmin(1.0, (eps * (gamma + 1.0) - 1.0) / denom));
-            azim = isfinite(d_a) ? d_a - floor(d_a) : 0.0;
-            if (azim < 0.0) azim += 1.0;
+            azim = finite_bits(d_a) ? d_a - floor(d_a) : 0.0;
+            if (lt0(azim)) azim += 1.0;
         }
     }
     double g1x, g1y, g1z;
     cone_direction(ax, ay, az, cos1, azim, g1x, g1y, g1z);
-    e1 = fmax(e1, 0.0);
-    e2 = fmax(e2, 0.0);
+    e1 = max0(e1);
+    e2 = max0(e2);
     double g2x = -g1x, g2y = -g1y, g2z = -g1z;
-    if (!rest && e2 > 0.0) {
-        double const p = sqrt(fmax(0.0, ka * (ka + 2.0 * kMeC2)));
+    if (!rest && gt0(e2)) {
+        double const p = sqrt(max0(ka * (ka + 2.0 * kMeC2)));
         g2x = (p * ax - e1 * g1x) / e2;
         g2y = (p * ay - e1 * g1y) / e2;
         g2z = (p * az - e1 * g1z) / e2;
@@ -420,23 +420,23 @@ static __device__ __noinline__ uint32_t spawn_annihilation(ElectronArgs A, RngSt
     else local += e1;
     if (e2 >= cut) append_secondary(A, ip, key, weight, lineage, 2, 9, x, y, z, g2x, g2y, g2z, e2, birth, err, 1);
     else local += e2;
-    if (at_rest && k > 0.0) {
+    if (at_rest && gt0(k)) {
         double const pw = weight * k / fmax(w_air, 1.0);
-        if (pw > 0.0) deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
+        if (gt0(pw)) deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
     }
-    if (local > 0.0) {
+    if (gt0(local)) {
         double const pw = weight * local / fmax(w_air, 1.0);
-        if (pw > 0.0) deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
+        if (gt0(pw)) deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
     }
     deposit_source(C, A.cells, 2, r, z, weight, 0.0, 0.0);
     {
         // closure of the PositronAnnihilation group (O/RreaPositronTransport.cpp:136-162, 710-735)
         double const ecut = C.cfg.low_energy_cutoff_eV;
         GroupClosure gc;
-        gc.begin(1.0, kMeC2, weight, fmax(k, 0.0), 0.0, false);
+        gc.begin(1.0, kMeC2, weight, max0(k), 0.0, false);
         if (e1 >= cut) gc.secondary(0.0, 0.0, weight, e1);
         if (e2 >= cut) gc.secondary(0.0, 0.0, weight, e2);
-        if (at_rest && k > 0.0) gc.local(weight, k, w_air, ecut);
+        if (at_rest && gt0(k)) gc.local(weight, k, w_air, ecut);
         gc.local(weight, local, w_air, ecut);
         gc.positive_ion(weight);
         if (!gc.valid(ecut)) err.set(RREA_GPU_ERR_INVALID_STATE);
@@ -484,7 +484,7 @@ __device__ __noinline__ double cutoff_bisection(Intervals<NP> iv, Path<NP> path,
     for (int it = 0; it < 56; ++it) {
         double const mid = 0.5 * (lo + hi);
         double const l = total * density_path(iv, path, b, mid);
-        if (!isfinite(l) || l < 0.0) return __longlong_as_double(0x7ff8000000000000LL);
+        if (!finite_bits(l) || lt0(l)) return __longlong_as_double(0x7ff8000000000000LL);
         if (l < to_cut) lo = mid; else hi = mid;
     }
     return 0.5 * (lo + hi);
@@ -519,7 +519,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     // ---- prologue, O/RreaTransportStep.H:730-819
     uint64_t const key = static_cast<uint64_t>(llabs(A.id[ip])) ^ (static_cast<uint64_t>(A.cpu ? A.cpu[ip] : 0) << 40);
     double const weight = A.w[ip];
-    if (weight <= 0.0) {
+    if (le0(weight)) {
         A.id[ip] = -A.id[ip];
         return 3;
     }
@@ -544,20 +544,20 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
 
     auto build_chord = [&](double req_dt, Path<NP>& path) -> bool {
         // O/RreaParticleInteraction.H:110-161
-        if (!isfinite(req_dt) || !(req_dt >= 0.0)) return false;
+        if (!finite_bits(req_dt) || !(ge0(req_dt))) return false;
         double const speed = charged_speed(k);
         double const dn = sqrt(dx * dx + dy * dy + dz * dz);
-        if (!isfinite(speed) || !isfinite(dn) || !(dn > 0.0)) return false;
+        if (!finite_bits(speed) || !finite_bits(dn) || !(gt0(dn))) return false;
         double const sc = speed * req_dt / dn;
         double const exx = run_x + sc * dx, eyy = run_y + sc * dy, ezz = run_z + sc * dz;
         clip_xyz(run_x, run_y, run_z, exx, eyy, ezz, g, path, err);
-        return isfinite(path.full) && path.in_begin == 0.0;
+        return finite_bits(path.full) && eq0(path.in_begin);
     };
     auto deposit_local = [&](double r, double z, double e) {
         // O/RreaTransportStep.H:530-561
-        if (weight <= 0.0 || e <= 0.0) return;
+        if (le0(weight) || le0(e)) return;
         double const pw = weight * e / fmax(w_air, 1.0);
-        if (pw <= 0.0) return;
+        if (le0(pw)) return;
         deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
     };
     auto finish = [&](int disp) { return disp; };
@@ -575,7 +575,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     double const field_work = dfw.work / driver_span;
     double const chord_dpath = density_path(iv, path, path.in_begin, path.in_end);
     double transported_dpath = 0.0, transported_len = 0.0;
-    double particle_density = ds > 0.0 ? chord_dpath / ds : positive_or(rho, rho);
+    double particle_density = gt0(ds) ? chord_dpath / ds : positive_or(rho, rho);
 
     // net chord from the captured start (AccumulateChargedSegment), signed
     // with the species charge; deposited by the current pass after the kernel
@@ -641,7 +641,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         if constexpr (POS) return annihilate(x_particle, y_particle, z_particle, r_particle, 0, 1.0);
         else return demote(r_particle, z_particle);
     }
-    if (ds <= 0.0) {
+    if (le0(ds)) {
         if (esc) return commit_escape();
         return finish(0);
     }
@@ -693,7 +693,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         if constexpr (POS) {
             // collision stopping only (O/RreaPositronTransport.cpp:195-201)
             drag_est = rate_value(C, arena, rc, ke, kRateCollision, err, rate_base) * 1.0 * driver_dpath;
-        } else if (ke > 0.0) {
+        } else if (gt0(ke)) {
             double const col = rate_value(C, arena, rc, ke, kRateCollision, err);
             double const soft = rate_value(C, arena, rc, ke, kRateSoft, err);
             drag_est = (col * 1.0 + soft * 1.0) * driver_dpath;
@@ -739,7 +739,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
             // stop point and elapsed fraction for the at-rest annihilation
             mid_x = x;
             mid_y = y;
-            double const within = fmin(1.0, fmax(0.0, f));
+            double const within = fmin(1.0, max0(f));
             mid_elapsed = fmin(1.0, (static_cast<double>(completed) + within) / static_cast<double>(subcycles));
         }
         terminated_mid = true;
@@ -750,7 +750,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     // reached the cutoff; `end_out` is the effective end fraction.
     auto continuous = [&](double b, double e, double stop_e, double& end_out) -> bool {
         end_out = b;
-        if (!(e > b) || !(k > 0.0) || stop_e < cutoff) return false;
+        if (!(e > b) || !(gt0(k)) || stop_e < cutoff) return false;
         // The plan's hard-transfer loss feeds only the reference's scalar
         // tally, and its table queries cannot fail at an energy the
         // collision table just accepted, so it is not evaluated here.
@@ -762,18 +762,18 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         double eff = b;
         bool reaches = false;
         bool valid = false;
-        if (isfinite(b) && isfinite(e) && isfinite(k) && isfinite(cutoff) && e >= b && k >= cutoff && cutoff >= 0.0) {
+        if (finite_bits(b) && finite_bits(e) && finite_bits(k) && finite_bits(cutoff) && e >= b && k >= cutoff && ge0(cutoff)) {
             double const to_cut = k - cutoff;
             double const req = total * density_path(iv, path, b, e);
-            if (isfinite(req) && req >= 0.0) {
+            if (finite_bits(req) && ge0(req)) {
                 valid = true;
                 if (req < to_cut) {
                     eff = e;
                 } else {
                     reaches = true;
-                    if (to_cut != 0.0) {
+                    if (ne0(to_cut)) {
                         eff = cutoff_bisection<NP>(iv, path, b, e, total, to_cut);
-                        valid = !isnan(eff);
+                        valid = !nan_bits(eff);
                         if (!valid) {
                             eff = b;
                             reaches = false;
@@ -789,11 +789,11 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         double const path_m = density_path(iv, path, b, eff);
         double const raw_col = sc * path_m;
         double const raw_soft = ss * path_m;
-        double const avail = fmax(0.0, k - cutoff);
+        double const avail = max0(k - cutoff);
         double const drag = reaches ? avail : fmin(raw_col + raw_soft, avail);
         double const col = fmin(raw_col, drag);
         // ion pairs, O/RreaChargedInterleave.H:157-196
-        if (col > 0.0 && raw_col > 0.0) {
+        if (gt0(col) && gt0(raw_col)) {
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
                 if (i >= iv.n) break;
@@ -804,14 +804,14 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                 // col * raw / raw_col is col to within an ulp
                 double const loss = NP == 1 ? col : col * raw / raw_col;
                 double const pw = weight * loss * inv_pair_energy;
-                if (!(pw > 0.0)) continue;
+                if (!(gt0(pw))) continue;
                 double x, y, z;
                 point_at_full(path, g, 0.5 * (bb + ee), x, y, z);
                 // deposit_source(kind 0, sec POS ? 0 : cutoff/2, loss w_air) through the cache
                 ion_pairs.add(C, A.cells, rz_radius(x, y), z, pw);
             }
         }
-        k = fmax(0.0, k - drag);
+        k = max0(k - drag);
         if (reaches) k = cutoff;
         end_out = eff;
         return reaches;
@@ -825,7 +825,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         if constexpr (POS) {
             if (!rate_bracket(C, arena, rc, e, err, rate_base)) return false;
             if (ch == 0) {
-                return !(hm_thr > 0.0 && e <= hm_thr) && rate_positive(C, arena, rc, e, kRateBhabha, err, rate_base);
+                return !(gt0(hm_thr) && e <= hm_thr) && rate_positive(C, arena, rc, e, kRateBhabha, err, rate_base);
             }
             if (ch == 1) return e > C.photon_cutoff_eV && rate_positive(C, arena, rc, e, kRateBrems, err, rate_base);
             if (ch == 2) return rate_positive(C, arena, rc, e, kRateAnnihilation, err, rate_base);
@@ -833,11 +833,11 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         }
         if (!rate_bracket(C, arena, rc, e, err)) return false;
         if (ch == 0) {
-            return C.hm_enabled && (hm_thr > 0.0 && e > 2.0 * hm_thr)
+            return C.hm_enabled && (gt0(hm_thr) && e > 2.0 * hm_thr)
                 && rate_positive(C, arena, rc, e, kRateMoller, err);
         }
         if (ch == 1) {
-            return (isfinite(e) && isfinite(C.photon_cutoff_eV) && e > C.photon_cutoff_eV)
+            return (finite_bits(e) && finite_bits(C.photon_cutoff_eV) && e > C.photon_cutoff_eV)
                 && rate_positive(C, arena, rc, e, kRateBrems, err);
         }
         return false;
@@ -851,7 +851,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
             Path<NP> np;
             if (!build_chord(sub_dt, np)) break;
             path = np;
-            if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
+            if (!(gt0(path.full)) || !(gt0(path.in_length))) {
                 exited = path.exits;
                 break;
             }
@@ -920,7 +920,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                 }
                 double const ev = fraction_at_density_path(iv, path, rem, se,
                                                            selv.sampled / (POS ? (s0 + s1) + s2 : s0 + s1), err);
-                if (!(isfinite(rem) && isfinite(ev) && isfinite(se) && se > rem && !(ev < rem) && !(ev > se))) {
+                if (!(finite_bits(rem) && finite_bits(ev) && finite_bits(se) && se > rem && !(ev < rem) && !(ev > se))) {
                     err.set(RREA_GPU_ERR_INVALID_STATE);
                     break;
                 }
@@ -945,7 +945,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                     ++ordinal;
                     continue;
                 }
-                double const within = fmin(1.0, fmax(0.0, ev));
+                double const within = fmin(1.0, max0(ev));
                 double const birth = fmin(1.0, (static_cast<double>(completed) + within) / static_cast<double>(subcycles));
                 Site const site{ex, ey, ez, er, birth};
                 if constexpr (POS) {
@@ -984,9 +984,9 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         if (k >= cutoff) {
             // apply_gs_elastic_scatter, O/RreaTransportStep.H:371-423
             // log(k) is shared by the elastic-MFP and angle-table brackets.
-            double const lk = (k > 0.0) ? flog(arena, k) : __longlong_as_double(0x7ff8000000000000LL);
+            double const lk = (gt0(k)) ? flog(arena, k) : __longlong_as_double(0x7ff8000000000000LL);
             double const gs_n = elastic_inverse_stp(C, arena, k, err, lk, species) * density_path(iv, path, sb, se);
-            if (gs_n > 0.0) {
+            if (gt0(gs_n)) {
                 double const few = C.tix.gs_few_collision_threshold;
                 if (gs_n < few) {
                     Dir3 const d3 = gs_few_collisions(arena, rng, sub, gs_n, k, lk, dx, dy, dz, species);
@@ -1050,7 +1050,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         put_segment(A.r[ip], run_z);
         return finish(0);
     }
-    if (transported_len > 0.0) particle_density = transported_dpath / transported_len;
+    if (gt0(transported_len)) particle_density = transported_dpath / transported_len;
     double const end_r = rz_radius(run_x, run_y);
     double fer, fez, fbt;
     gather(A.fv, end_r, run_z, fer, fez, fbt);
@@ -1062,19 +1062,19 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
         // threshold; above it only its range check can matter, and that is
         // kept.
         if (!charged_in_range(C.tix, ke)) err.set(RREA_GPU_ERR_RANGE);
-        if (ke > 0.0 && particle_density > 0.0 && k <= hm_thr) {
+        if (gt0(ke) && gt0(particle_density) && k <= hm_thr) {
             double const col = rate_value(C, arena, rc, ke, kRateCollision, err);
             double const soft = rate_value(C, arena, rc, ke, kRateSoft, err);
             double const hard = C.hm_enabled ? hard_moller_energy_loss(C, arena, ke, particle_density, err) : 0.0;
             double tracked = 0.0;
             double const inv = rate_value(C, arena, rc, ke, kRateBrems, err) * particle_density;
-            if (inv > 0.0) tracked = inv * mean_conditional(arena, C.tix.cdf[RREA_C_BREMS_E], ke, err);
+            if (gt0(inv)) tracked = inv * mean_conditional(arena, C.tix.cdf[RREA_C_BREMS_E], ke, err);
             threshold = (col * particle_density + soft * particle_density) + hard + tracked;
         }
     }
     if (err.code) return finish(-1);
     bool const below_cut = k < cutoff;
-    bool const nonrunaway = hm_thr > 0.0 && k <= hm_thr && rz_radius(fer, fez) <= threshold;
+    bool const nonrunaway = gt0(hm_thr) && k <= hm_thr && rz_radius(fer, fez) <= threshold;
     if (exited) return commit_escape();
     if (terminated_mid) return demote(mid_r, mid_z);
     if (below_cut || nonrunaway) return demote(end_r, run_z);

@@ -78,16 +78,16 @@ __device__ __forceinline__ bool newborn_electron_demotes(StepConstants const& C,
     if (!charged_in_range(C.tix, ke)) err.set(RREA_GPU_ERR_RANGE);
     double drag = 0.0;
     // the drag only decides the gate at or below the hard-Moller threshold
-    if (ke > 0.0 && rho > 0.0 && e <= thr) {
+    if (gt0(ke) && gt0(rho) && e <= thr) {
         double const col = rate_value(C, A.arena, rc, ke, kRateCollision, err);
         double const soft = rate_value(C, A.arena, rc, ke, kRateSoft, err);
         double const hard = C.hm_enabled ? hard_moller_energy_loss(C, A.arena, ke, rho, err) : 0.0;
         double tracked = 0.0;
         double const inv = rate_value(C, A.arena, rc, ke, kRateBrems, err) * rho;
-        if (inv > 0.0) tracked = inv * mean_conditional(A.arena, C.tix.cdf[RREA_C_BREMS_E], ke, err);
+        if (gt0(inv)) tracked = inv * mean_conditional(A.arena, C.tix.cdf[RREA_C_BREMS_E], ke, err);
         drag = (col * rho + soft * rho) + hard + tracked;
     }
-    return e < cut || (thr > 0.0 && e <= thr && rz_radius(fer, fez) <= drag);
+    return e < cut || (gt0(thr) && e <= thr && rz_radius(fer, fez) <= drag);
 }
 
 // TransportStep::AdvanceChargedNewborn (O/RreaNewbornAdvance.cpp:50-777).
@@ -113,7 +113,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
     uint64_t const nb_lineage = p.lineage;
     double const birth = p.birth_fraction;
     double const birth_r = rz_radius(p.x, p.y), birth_z = p.z;
-    double const residual = fmin(1.0, fmax(0.0, 1.0 - birth));
+    double const residual = fmin(1.0, max0(1.0 - birth));
     double k = p.energy_eV;
     RngStream rng;
     rng.init(cfg.rng_seed, key, C.step_key);
@@ -130,9 +130,9 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
         return v;
     };
     auto deposit_local = [&](double r, double z, double e) {
-        if (w <= 0.0 || e <= 0.0) return;
+        if (le0(w) || le0(e)) return;
         double const pw = w * e / fmax(w_air, 1.0);
-        if (pw <= 0.0) return;
+        if (le0(pw)) return;
         deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
     };
     auto put_segment = [&](double r1, double z1) {
@@ -177,17 +177,17 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
         }
         return 0;
     }
-    if (!(residual > 0.0)) return 1;
+    if (!(gt0(residual))) return 1;
     double const u = proper_velocity_from_kinetic(k);
     double const gam = sqrt(1.0 + u * u / (kC * kC));
     double const residual_dt = C.dt_s * residual;
     double const chord = (u / gam) * residual_dt;
-    if (!(chord > 0.0)) return k >= cut ? 1 : 0;
+    if (!(gt0(chord))) return k >= cut ? 1 : 0;
     double const ex0 = p.x + chord * dx, ey0 = p.y + chord * dy, ez0 = p.z + chord * dz;
     Path<NP> path;
     clip_xyz(p.x, p.y, p.z, ex0, ey0, ez0, g, path, err);
     if (err.code) return -1;
-    if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
+    if (!(gt0(path.full)) || !(gt0(path.in_length))) {
         if (path.exits) return put_escape(path) ? 0 : -1;
         return 1;
     }
@@ -203,7 +203,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
     if constexpr (POS) {
         drag_est = rate_value(C, arena, rc, k, kRateCollision, err, rate_base) * 1.0 * driver_dpath;
     } else {
-        drag_est = (k > 0.0 ? rate_value(C, arena, rc, k, kRateCollision, err) * 1.0
+        drag_est = (gt0(k) ? rate_value(C, arena, rc, k, kRateCollision, err) * 1.0
                                   + rate_value(C, arena, rc, k, kRateSoft, err) * 1.0
                             : 0.0)
             * driver_dpath;
@@ -227,7 +227,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
     FieldRange sub_field{0, 0, 0, 0, 0, 0, 0, 0};
     double sub_dt_eff = 0.0;
     auto elapsed_at = [&](double f) {
-        double const within = fmin(1.0, fmax(0.0, f));
+        double const within = fmin(1.0, max0(f));
         double const consumed = (static_cast<double>(completed) + within) / static_cast<double>(substeps);
         return fmin(1.0, birth + residual * consumed);
     };
@@ -237,25 +237,25 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
     // apply_newborn_drag (:260-360)
     auto continuous = [&](double b, double e, double stop_e, double& end_out) -> bool {
         end_out = b;
-        if (!(e > b) || !(k > 0.0) || stop_e < cut) return false;
+        if (!(e > b) || !(gt0(k)) || stop_e < cut) return false;
         double const sc = frozen_rate(rate_value(C, arena, rc, stop_e, kRateCollision, err, rate_base) * 1.0, err);
         double const ss = frozen_rate(rate_value(C, arena, rc, stop_e, kRateSoft, err, rate_base) * 1.0, err);
         if (err.code) return false;
         double const total = sc + ss;
         double eff = b;
         bool reaches = false, valid = false;
-        if (isfinite(b) && isfinite(e) && isfinite(k) && isfinite(cut) && e >= b && k >= cut && cut >= 0.0) {
+        if (finite_bits(b) && finite_bits(e) && finite_bits(k) && finite_bits(cut) && e >= b && k >= cut && ge0(cut)) {
             double const to_cut = k - cut;
             double const req = total * density_path(iv, path, b, e);
-            if (isfinite(req) && req >= 0.0) {
+            if (finite_bits(req) && ge0(req)) {
                 valid = true;
                 if (req < to_cut) {
                     eff = e;
                 } else {
                     reaches = true;
-                    if (to_cut != 0.0) {
+                    if (ne0(to_cut)) {
                         eff = cutoff_bisection<NP>(iv, path, b, e, total, to_cut);
-                        valid = !isnan(eff);
+                        valid = !nan_bits(eff);
                         if (!valid) {
                             eff = b;
                             reaches = false;
@@ -271,21 +271,21 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
         double const path_m = density_path(iv, path, b, eff);
         double const raw_col = sc * path_m;
         double const raw_soft = ss * path_m;
-        double const avail = fmax(0.0, k - cut);
+        double const avail = max0(k - cut);
         double const drag = reaches ? avail : fmin(raw_col + raw_soft, avail);
         double const col = fmin(raw_col, drag);
-        for (int t = 0; col > 0.0 && raw_col > 0.0 && t < iv.n; ++t) {
+        for (int t = 0; col > 0.0 && gt0(raw_col) && t < iv.n; ++t) {
             double const bb = fmax(b, iv.begin[t]), ee = fmin(eff, iv.end[t]);
             if (ee > bb) {
                 double const raw = path.full * (ee - bb) * iv.density[t] * sc;
                 double const loss = col * raw / raw_col;
                 double const pw = w * loss / fmax(w_air, 1.0);
-                if (pw > 0.0) {
+                if (gt0(pw)) {
                     double x, y, z;
                     point_at_full(path, g, 0.5 * (bb + ee), x, y, z);
                     double sr = rz_radius(x, y), sz = z;
                     // a source that rounds off the half-open domain falls back to the birth point
-                    if (!(isfinite(sr) && isfinite(sz) && sr >= g.rlo && sr < g.rhi && sz >= g.zlo && sz < g.zhi)) {
+                    if (!(finite_bits(sr) && finite_bits(sz) && sr >= g.rlo && sr < g.rhi && sz >= g.zlo && sz < g.zhi)) {
                         sr = rz_radius(p.x, p.y);
                         sz = p.z;
                     }
@@ -294,7 +294,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
                 }
             }
         }
-        k = fmax(0.0, k - drag);
+        k = max0(k - drag);
         if (reaches) k = cut;
         end_out = eff;
         return reaches;
@@ -306,16 +306,16 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
         }
         if (!rate_bracket(C, arena, rc, e, err, rate_base)) return false;
         if constexpr (POS) {
-            if (ch == 0) return !(thr > 0.0 && e <= thr) && rate_positive(C, arena, rc, e, kRateBhabha, err, rate_base);
+            if (ch == 0) return !(gt0(thr) && e <= thr) && rate_positive(C, arena, rc, e, kRateBhabha, err, rate_base);
             if (ch == 1) return e > C.photon_cutoff_eV && rate_positive(C, arena, rc, e, kRateBrems, err, rate_base);
             if (ch == 2) return rate_positive(C, arena, rc, e, kRateAnnihilation, err, rate_base);
             return false;
         } else {
             if (ch == 0) {
-                return C.hm_enabled && (thr > 0.0 && e > 2.0 * thr) && rate_positive(C, arena, rc, e, kRateMoller, err);
+                return C.hm_enabled && (gt0(thr) && e > 2.0 * thr) && rate_positive(C, arena, rc, e, kRateMoller, err);
             }
             if (ch == 1) {
-                return (isfinite(e) && isfinite(C.photon_cutoff_eV) && e > C.photon_cutoff_eV)
+                return (finite_bits(e) && finite_bits(C.photon_cutoff_eV) && e > C.photon_cutoff_eV)
                     && rate_positive(C, arena, rc, e, kRateBrems, err);
             }
             return false;
@@ -329,15 +329,15 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
             // RreaBuildRunningChargedChord with the residual dt as the step bound
             double const speed = charged_speed(k);
             double const dn = sqrt(dx * dx + dy * dy + dz * dz);
-            if (!isfinite(sub_dt) || !(sub_dt >= 0.0) || !isfinite(speed) || !isfinite(dn) || !(dn > 0.0)) break;
+            if (!finite_bits(sub_dt) || !(ge0(sub_dt)) || !finite_bits(speed) || !finite_bits(dn) || !(gt0(dn))) break;
             double const sc = speed * sub_dt / dn;
             double const exx = run_x + sc * dx, eyy = run_y + sc * dy, ezz = run_z + sc * dz;
             Path<NP> np;
             clip_xyz(run_x, run_y, run_z, exx, eyy, ezz, g, np, err);
             if (err.code) break;
-            if (!(isfinite(np.full) && np.in_begin == 0.0)) break;
+            if (!(finite_bits(np.full) && eq0(np.in_begin))) break;
             path = np;
-            if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
+            if (!(gt0(path.full)) || !(gt0(path.in_length))) {
                 exited = path.exits;
                 final_fraction = 0.0;
                 break;
@@ -394,7 +394,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
                     break;
                 }
                 double const ev = fraction_at_density_path(iv, path, rem, se, selv.sampled / total_stp, err);
-                if (!(isfinite(rem) && isfinite(ev) && isfinite(se) && se > rem && !(ev < rem) && !(ev > se))) {
+                if (!(finite_bits(rem) && finite_bits(ev) && finite_bits(se) && se > rem && !(ev < rem) && !(ev > se))) {
                     err.set(RREA_GPU_ERR_INVALID_STATE);
                     break;
                 }
@@ -453,9 +453,9 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
         }
         if (err.code || terminal_interaction || terminal_at_point) break;
         if (k >= cut) {
-            double const lk = (k > 0.0) ? flog(arena, k) : __longlong_as_double(0x7ff8000000000000LL);
+            double const lk = (gt0(k)) ? flog(arena, k) : __longlong_as_double(0x7ff8000000000000LL);
             double const gs_n = elastic_inverse_stp(C, arena, k, err, lk, species) * density_path(iv, path, sb, se);
-            if (gs_n > 0.0) {
+            if (gt0(gs_n)) {
                 double const few = C.tix.gs_few_collision_threshold;
                 if (gs_n < few) {
                     int const cap = static_cast<int>(ceil(3.0 * few));
@@ -569,8 +569,8 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
     double const w_air = C.tix.w_air_eV_per_pair;
     double const w = p.weight;
     uint64_t const key = p.root_key;
-    double const residual = fmin(1.0, fmax(0.0, 1.0 - p.birth_fraction));
-    if (!(residual > 0.0)) return p.energy_eV >= photon_cut ? 1 : 0;
+    double const residual = fmin(1.0, max0(1.0 - p.birth_fraction));
+    if (!(gt0(residual))) return p.energy_eV >= photon_cut ? 1 : 0;
     if (!in_half_open(g, p.x, p.y, p.z)) {
         err.set(RREA_GPU_ERR_GEOMETRY);
         return -1;
@@ -581,9 +581,9 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
     normalize(dx, dy, dz);
     double energy = p.energy_eV;
     auto deposit_local = [&](double r, double z, double e) {
-        if (w <= 0.0 || e <= 0.0) return;
+        if (le0(w) || le0(e)) return;
         double const pw = w * e / fmax(w_air, 1.0);
-        if (pw <= 0.0) return;
+        if (le0(pw)) return;
         deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
     };
     auto child = [&](int sp, int process, double x, double y, double z, double sx, double sy, double sz, double e,
@@ -599,7 +599,7 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
     Path<NP> path;
     clip_xyz(p.x, p.y, p.z, ex0, ey0, ez0, g, path, err);
     if (err.code) return -1;
-    if (!(path.full > 0.0) || !(path.in_length > 0.0)) return path.exits ? 0 : 1;
+    if (!(gt0(path.full)) || !(gt0(path.in_length))) return path.exits ? 0 : 1;
     double elapsed_start = p.birth_fraction;
     for (uint64_t ordinal = 0;; ++ordinal) {
         uint64_t idx;
@@ -633,12 +633,12 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
             return 1;
         }
         double const f = fraction_at_density_path(iv, path, path.in_begin, path.in_end, sel.sampled * mfp, err);
-        if (!(isfinite(f) && f >= path.in_begin && f <= path.in_end && path.in_end > path.in_begin)) {
+        if (!(finite_bits(f) && f >= path.in_begin && f <= path.in_end && path.in_end > path.in_begin)) {
             err.set(RREA_GPU_ERR_INVALID_STATE);
             return -1;
         }
         double const dist = path.full * (f - path.in_begin);
-        double const remaining = fmax(0.0, path.full - dist);
+        double const remaining = max0(path.full - dist);
         double px, py, pz;
         point_at_full(path, g, f, px, py, pz);
         double const pr = rz_radius(px, py);
@@ -680,7 +680,7 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
                 return 0;
             }
             dx = sx; dy = sy; dz = sz;
-            if (!(remaining > 0.0)) {
+            if (!(gt0(remaining))) {
                 p.x = px; p.y = py; p.z = pz;
                 p.dir_x = dx; p.dir_y = dy; p.dir_z = dz;
                 p.energy_eV = energy;
@@ -712,13 +712,13 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
                 deposit_source(C, A.cells, 0, pr, pz, w, ee, 0.0);
                 deposit_local(pr, pz, ee);
             }
-            if (bind > 0.0) deposit_local(pr, pz, bind);
+            if (gt0(bind)) deposit_local(pr, pz, bind);
             GroupClosure gc;  // closure of the Photoelectric group
             gc.begin(0.0, 0.0, w, energy, 0.0, false);
             if (ee >= cut) gc.secondary(-1.0, kMeC2, w, ee);
             gc.ionization(w, ee, cut);
             if (ee < cut) gc.local(w, ee, w_air, cut);
-            if (bind > 0.0) gc.local(w, bind, w_air, cut);
+            if (gt0(bind)) gc.local(w, bind, w_air, cut);
             if (!gc.valid(cut)) {
                 err.set(RREA_GPU_ERR_INVALID_STATE);
                 return -1;
@@ -757,7 +757,7 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
             deposit_source(C, A.cells, 0, pr, pz, w, ps.e_recoil, 0.0);
             if (ps.e_recoil < cut) deposit_local(pr, pz, ps.e_recoil);
         }
-        if (ps.local > 0.0) deposit_local(pr, pz, ps.local);
+        if (gt0(ps.local)) deposit_local(pr, pz, ps.local);
         if (!pair_closure_valid(ps, w, energy, cut, photon_cut, w_air)) {
             err.set(RREA_GPU_ERR_INVALID_STATE);
             return -1;

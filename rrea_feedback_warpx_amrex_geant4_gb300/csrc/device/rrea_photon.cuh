@@ -49,14 +49,14 @@ struct UniformStream {
 // S/RreaInteractionTables.cpp:40-61
 __device__ __forceinline__ double clamp_unit(double v)
 {
-    if (!isfinite(v)) return 0.5;
-    return fmax(0.0, fmin(1.0, v));
+    if (!finite_bits(v)) return 0.5;
+    return max0(fmin(1.0, v));
 }
 __device__ __forceinline__ double wrap_unit(double v)
 {
-    if (!isfinite(v)) return 0.0;
+    if (!finite_bits(v)) return 0.0;
     v = v - floor(v);
-    if (v < 0.0) v += 1.0;
+    if (lt0(v)) v += 1.0;
     return v;
 }
 
@@ -97,9 +97,9 @@ __device__ __forceinline__ bool photon_rates(StepConstants const& C, const doubl
 // 2 pair (nuclear), 3 pair (triplet).
 __device__ __forceinline__ int sample_photon_channel(PhotonRates const& r, double u, Err& err)
 {
-    u = fmax(0.0, fmin(1.0, u));
+    u = max0(fmin(1.0, u));
     double const total = r.total();
-    if (!(total > 0.0) || !isfinite(total)) {
+    if (!(gt0(total)) || !finite_bits(total)) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return 0;
     }
@@ -118,8 +118,8 @@ struct ComptonState {
 };
 __device__ __forceinline__ ComptonState sample_klein_nishina(double e, double draw_mu, double draw_accept)
 {
-    draw_mu = fmax(0.0, fmin(1.0, draw_mu));
-    draw_accept = fmax(0.0, fmin(1.0, draw_accept));
+    draw_mu = max0(fmin(1.0, draw_mu));
+    draw_accept = max0(fmin(1.0, draw_accept));
     UniformStream stream(draw_mu, draw_accept);
     double const alpha = e / kMeC2;
     double const eps0 = 1.0 / (1.0 + 2.0 * alpha);
@@ -144,8 +144,8 @@ __device__ __forceinline__ ComptonState sample_klein_nishina(double e, double dr
         if (greject >= stream.next()) break;
     }
     ComptonState st;
-    st.scattered = fmax(0.0, epsilon * e);
-    st.recoil = fmax(0.0, e - st.scattered);
+    st.scattered = max0(epsilon * e);
+    st.recoil = max0(e - st.scattered);
     st.cos_theta = fmax(-1.0, fmin(1.0, 1.0 - onecost));
     return st;
 }
@@ -168,7 +168,7 @@ __device__ __forceinline__ void sample_photoelectric(StepConstants const& C, con
         err.set(RREA_GPU_ERR_RANGE);
         return;
     }
-    u = fmax(0.0, fmin(1.0, u));
+    u = max0(fmin(1.0, u));
     int const up = lower_bound(prim, pi.ng, e);
     int g;
     if (up == 0) g = 0;
@@ -184,7 +184,7 @@ __device__ __forceinline__ void sample_photoelectric(StepConstants const& C, con
         return;
     }
     binding = bnd;
-    electron = fmax(0.0, e - bnd);
+    electron = max0(e - bnd);
 }
 
 // SamplePhotoelectronCosTheta, S/RreaInteractionTables.cpp:2949-3044:
@@ -211,12 +211,12 @@ __device__ __forceinline__ dd sg_prim_dd(dd b, dd c, dd twopbc, dd twobm1, doubl
 static __device__ __noinline__ double sample_photoelectron_cos(double k, double draw)
 {
     double const u = clamp_unit(draw);
-    if (u <= 0.0) return -1.0;
+    if (le0(u)) return -1.0;
     if (u >= 1.0) return 1.0;
     dd const gamma = dd_add(dd_from(1.0), dd_div(dd_from(k), dd_from(kMeC2)));
     dd const inv_g2 = dd_div(dd_from(1.0), dd_mul(gamma, gamma));
     dd const one_m = dd_sub(dd_from(1.0), inv_g2);
-    dd const beta = one_m.hi > 0.0 ? dd_sqrt(one_m) : dd_from(0.0);
+    dd const beta = gt0(one_m.hi) ? dd_sqrt(one_m) : dd_from(0.0);
     if (beta.hi < 1.0e-4) {
         // non-relativistic limit: CDF (2 + m(3 - m^2))/4 in m = cos(theta)
         double lo = -1.0, hi = 1.0;
@@ -239,7 +239,7 @@ static __device__ __noinline__ double sample_photoelectron_cos(double k, double 
     dd const f_lo = sg_prim_dd(b, c, twopbc, twobm1, t_lo.hi);
     dd const f_hi = sg_prim_dd(b, c, twopbc, twobm1, t_hi.hi);
     dd const total = dd_sub(f_hi, f_lo);
-    if (!(total.hi > 0.0) || !isfinite(total.hi)) return __longlong_as_double(0x7ff8000000000000LL);
+    if (!(gt0(total.hi)) || !finite_bits(total.hi)) return __longlong_as_double(0x7ff8000000000000LL);
     dd const target = dd_add(dd_mul(two_sum(1.0, -u), f_hi), dd_mul_d(f_lo, u));
     double const bd = b.hi, cd = c.hi, pbd = twopbc.hi, bm1d = twobm1.hi, tgt = target.hi;
     double lo = t_lo.hi, hi = t_hi.hi;
@@ -280,7 +280,7 @@ struct PairState {
 __device__ __forceinline__ void normalize_local(double& x, double& y, double& z)
 {
     double const n = sqrt(x * x + y * y + z * z);
-    if (n <= 0.0 || !isfinite(n)) {
+    if (le0(n) || !finite_bits(n)) {
         x = 0.0; y = 0.0; z = 1.0;
         return;
     }
@@ -315,7 +315,7 @@ __device__ __forceinline__ bool pair_closure_valid(PairState const& ps, double w
             if (kMeC2 >= photon_cut) gc.secondary(0.0, 0.0, w, kMeC2);
             else local += kMeC2;
         }
-        if (ps.e_positron > 0.0) gc.local(w, ps.e_positron, w_air, cutoff);
+        if (gt0(ps.e_positron)) gc.local(w, ps.e_positron, w_air, cutoff);
         gc.local(w, local, w_air, cutoff);
         gc.positive_ion(w);
     }
@@ -324,7 +324,7 @@ __device__ __forceinline__ bool pair_closure_valid(PairState const& ps, double w
         gc.ionization(w, ps.e_recoil, cutoff);
         if (ps.e_recoil < cutoff) gc.local(w, ps.e_recoil, w_air, cutoff);
     }
-    if (ps.local > 0.0) gc.local(w, ps.local, w_air, cutoff);
+    if (gt0(ps.local)) gc.local(w, ps.local, w_air, cutoff);
     return gc.valid(cutoff);
 }
 
@@ -338,7 +338,7 @@ __device__ __forceinline__ void sample_pair(StepConstants const& C, const double
     for (int c = 0; c < 3; ++c) { st.edir[c] = st.pdir[c] = st.rdir[c] = c == 2 ? 1.0 : 0.0; }
     bool const triplet = channel == 3;
     double const threshold = triplet ? 4.0 * kMeC2 : 2.0 * kMeC2;
-    if (!(isfinite(e) && e > threshold)) return;
+    if (!(finite_bits(e) && e > threshold)) return;
     RreaPairBankIndex const& pb = C.tix.pair[triplet ? 1 : 0];
     const double* prim = arena + pb.primary;
     const double* start = arena + pb.start;
@@ -396,7 +396,7 @@ __device__ __forceinline__ void sample_pair(StepConstants const& C, const double
     }
     double const tol = 64.0 * kEps * fmax(1.0, avail);
     double expl = st.e_electron + st.e_positron + st.e_recoil;
-    if (!isfinite(expl) || st.e_electron < 0.0 || st.e_positron < 0.0 || st.e_recoil < 0.0) {
+    if (!finite_bits(expl) || lt0(st.e_electron) || lt0(st.e_positron) || lt0(st.e_recoil)) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return;
     }
@@ -410,7 +410,7 @@ __device__ __forceinline__ void sample_pair(StepConstants const& C, const double
         expl = st.e_electron + st.e_positron + st.e_recoil;
     }
     st.local = avail - expl;
-    if (st.local < 0.0) {
+    if (lt0(st.local)) {
         double const corr = -st.local;
         double* l = pair_largest(st);
         if (corr > tol || *l < corr) {
@@ -426,7 +426,7 @@ __device__ __forceinline__ void sample_pair(StepConstants const& C, const double
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return;
     }
-    if (resid >= 0.0) {
+    if (ge0(resid)) {
         st.local += resid;
     } else if (st.local >= -resid) {
         st.local += resid;
@@ -439,7 +439,7 @@ __device__ __forceinline__ void sample_pair(StepConstants const& C, const double
         *l -= -resid;
     }
     accounted = st.e_electron + st.e_positron + st.e_recoil + st.local;
-    if (st.e_electron < 0.0 || st.e_positron < 0.0 || st.e_recoil < 0.0 || st.local < 0.0
+    if (lt0(st.e_electron) || lt0(st.e_positron) || lt0(st.e_recoil) || lt0(st.local)
         || fabs(avail - accounted) > tol) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
     }
@@ -500,7 +500,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
     if (A.straight_push) {
         // WarpX's photon push (x += c dt u/|u|) on the Cartesian image of the
         // RZ start point; the tile arrays alias prev_* in this mode.
-        double const f = energy > 0.0 ? kC * dt_s / energy : 0.0;
+        double const f = gt0(energy) ? kC * dt_s / energy : 0.0;
         double s0, c0;
         sincos(pth0, &s0, &c0);
         double const x1 = pr0 * c0 + ux * f, y1 = pr0 * s0 + uy * f;
@@ -519,9 +519,9 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
     int process = 0;
     auto deposit_local_at = [&](double r, double z, double w, double e) {
         // O/RreaTransportStep.H:530-561
-        if (w <= 0.0 || e <= 0.0) return;
+        if (le0(w) || le0(e)) return;
         double const pw = w * e / fmax(w_air, 1.0);
-        if (pw <= 0.0) return;
+        if (le0(pw)) return;
         deposit_source(C, A.cells, 0, r, z, pw, 0.0, w_air);
     };
     auto add_secondary = [&](int species, double x, double y, double z, double sx, double sy, double sz, double e,
@@ -542,11 +542,11 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
         Intervals<NP> iv;
         build_intervals(path, rho, iv);
         double const chord_dpath = density_path(iv, path, path.in_begin, path.in_end);
-        if (weight <= 0.0 || energy < photon_cut) {
+        if (le0(weight) || energy < photon_cut) {
             double x, y, z;
             point_at_full(path, g, path.in_begin, x, y, z);
             process = 12;
-            deposit_local_at(rz_radius(x, y), z, fmax(weight, 0.0), energy);
+            deposit_local_at(rz_radius(x, y), z, max0(weight), energy);
             A.id[ip] = -A.id[ip];
             return 2;
         }
@@ -560,7 +560,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             if (esc_inv) A.id[ip] = -A.id[ip];
             return 1;
         };
-        if (ds <= 0.0) return commit_no_event();
+        if (le0(ds)) return commit_no_event();
         PhotonRates rates;
         if (!photon_rates(C, arena, energy, rates, err)) return -1;
         double const mfp = mfp_from_inverse(rates.total(), err);
@@ -580,14 +580,14 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
         }
         if (!sel.event) return commit_no_event();
         double const f = fraction_at_density_path(iv, path, path.in_begin, path.in_end, sel.sampled * mfp, err);
-        if (!(isfinite(f) && f >= path.in_begin && f <= path.in_end && path.in_end > path.in_begin)) {
+        if (!(finite_bits(f) && f >= path.in_begin && f <= path.in_end && path.in_end > path.in_begin)) {
             err.set(RREA_GPU_ERR_INVALID_STATE);
             return -1;
         }
         double const dist = path.full * (f - path.in_begin);
         double px, py, pz;
         point_at_full(path, g, f, px, py, pz);
-        double const remaining = fmax(0.0, path.full - dist);
+        double const remaining = max0(path.full - dist);
         double const birth = fmin(1.0, elapsed_start + dist / fmax(kC * dt_s, kDblMin));
         double const pr = rz_radius(px, py);
         int const channel = sample_photon_channel(
@@ -644,7 +644,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             A.r[ip] = rz_radius(nx, ny);
             A.theta[ip] = atan2(ny, nx);
             A.z[ip] = wrap_z(g, nz);
-            if (!(remaining > 0.0)) return 0;
+            if (!(gt0(remaining))) return 0;
             path = next;
             elapsed_start = birth;
             ++ordinal;
@@ -663,7 +663,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
                     return -1;
                 }
                 double const cth = sample_photoelectron_cos(ee, rng.uniform(idx, kChPhotoelectronCos));
-                if (!isfinite(cth)) {
+                if (!finite_bits(cth)) {
                     err.set(RREA_GPU_ERR_INVALID_STATE);
                     return -1;
                 }
@@ -675,7 +675,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
                 deposit_source(C, A.cells, 0, pr, pz, weight, ee, 0.0);
                 deposit_local_at(pr, pz, weight, ee);
             }
-            if (bind > 0.0) deposit_local_at(pr, pz, weight, bind);
+            if (gt0(bind)) deposit_local_at(pr, pz, weight, bind);
             {
                 // closure of the Photoelectric group (O/RreaPhotonFinalStates.H:181-223)
                 GroupClosure gc;
@@ -683,7 +683,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
                 if (ee >= cutoff) gc.secondary(-1.0, kMeC2, weight, ee);
                 gc.ionization(weight, ee, cutoff);
                 if (ee < cutoff) gc.local(weight, ee, w_air, cutoff);
-                if (bind > 0.0) gc.local(weight, bind, w_air, cutoff);
+                if (gt0(bind)) gc.local(weight, bind, w_air, cutoff);
                 if (!gc.valid(cutoff)) {
                     err.set(RREA_GPU_ERR_INVALID_STATE);
                     return -1;
@@ -731,8 +731,8 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             else local += e1;
             if (e2 >= photon_cut) add_secondary(2, px, py, pz, -g1x, -g1y, -g1z, e2, birth);
             else local += e2;
-            if (ps.e_positron > 0.0) deposit_local_at(pr, pz, weight, ps.e_positron);
-            if (local > 0.0) deposit_local_at(pr, pz, weight, local);
+            if (gt0(ps.e_positron)) deposit_local_at(pr, pz, weight, ps.e_positron);
+            if (gt0(local)) deposit_local_at(pr, pz, weight, local);
             deposit_source(C, A.cells, 2, pr, pz, weight, 0.0, 0.0);
         }
         if (ps.recoil) {
@@ -742,7 +742,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             deposit_source(C, A.cells, 0, pr, pz, weight, ps.e_recoil, 0.0);
             if (ps.e_recoil < cutoff) deposit_local_at(pr, pz, weight, ps.e_recoil);
         }
-        if (ps.local > 0.0) deposit_local_at(pr, pz, weight, ps.local);
+        if (gt0(ps.local)) deposit_local_at(pr, pz, weight, ps.local);
         if (!pair_closure_valid(ps, weight, energy, cutoff, photon_cut, w_air)) {
             err.set(RREA_GPU_ERR_INVALID_STATE);
             return -1;

@@ -39,7 +39,7 @@ __device__ __forceinline__ void stencil_cells(StepConstants const& C, int i0, in
         int ii = i0 + a;
         use_i[a] = true;
         if (ii < 0 || ii > nr - 1) {
-            if (ii == -1 && cfg.r_lo == 0.0) ii = 0;
+            if (ii == -1 && eq0(cfg.r_lo)) ii = 0;
             else use_i[a] = false;
         }
         i[a] = ii;
@@ -55,7 +55,7 @@ __device__ __forceinline__ CellStencil make_stencil(StepConstants const& C, doub
     if (cfg.periodic_z) {
         double const len = cfg.z_hi - cfg.z_lo;
         double s = fmod(zz - cfg.z_lo, len);
-        if (s < 0.0) s += len;
+        if (lt0(s)) s += len;
         zz = cfg.z_lo + s;
     }
     double const fr = quot(r - cfg.r_lo, C.div_dr);
@@ -81,17 +81,17 @@ __device__ __forceinline__ CellStencil make_stencil(StepConstants const& C, doub
 __device__ __forceinline__ void stencil_add(StepConstants const& C, double* __restrict__ cells, CellStencil const& st,
                                             int field, double value)
 {
-    if (!st.valid || !isfinite(value) || value == 0.0) return;
+    if (!st.valid || !finite_bits(value) || eq0(value)) return;
     int const nr = C.cfg.nr;
     double* grid = cells + static_cast<size_t>(field) * nr * C.cfg.nz;
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
         double const wz = st.wz[a];
-        if (wz == 0.0 || !st.use_j[a]) continue;
+        if (eq0(wz) || !st.use_j[a]) continue;
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
             double const v = value * st.wr[b] * wz;
-            if (v == 0.0 || !st.use_i[b] || !isfinite(v)) continue;
+            if (eq0(v) || !st.use_i[b] || !finite_bits(v)) continue;
             atomicAdd(grid + st.i[b] + static_cast<size_t>(nr) * st.j[a], v);
         }
     }
@@ -101,22 +101,22 @@ __device__ __forceinline__ void stencil_add(StepConstants const& C, double* __re
 __device__ __forceinline__ void deposit_source(StepConstants const& C, double* __restrict__ cells, int kind,
                                                double r, double z, double w, double sec_e, double loss)
 {
-    if (w <= 0.0) return;
+    if (le0(w)) return;
     CellStencil const st = make_stencil(C, r, z);
     if (!st.valid) return;
     if (kind == 0) {  // AccumulateIonizationEvent
         stencil_add(C, cells, st, 1, w);
         if (sec_e < C.cfg.low_energy_cutoff_eV) stencil_add(C, cells, st, 0, w);
         stencil_add(C, cells, st, 3, w);
-        stencil_add(C, cells, st, 4, fmax(w, 0.0) * fmax(loss, 0.0));
+        stencil_add(C, cells, st, 4, max0(w) * max0(loss));
     } else if (kind == 1) {  // AccumulateLowEnergyElectron
         stencil_add(C, cells, st, 0, w);
         stencil_add(C, cells, st, 3, w);
-        stencil_add(C, cells, st, 4, fmax(w, 0.0) * fmax(fmax(loss, 0.0), 0.0));
+        stencil_add(C, cells, st, 4, max0(w) * max0(fmax(loss, 0.0)));
     } else {  // AccumulatePositiveIonSourceOnly
         stencil_add(C, cells, st, 1, w);
         stencil_add(C, cells, st, 3, w);
-        stencil_add(C, cells, st, 4, fmax(w, 0.0) * fmax(loss, 0.0));
+        stencil_add(C, cells, st, 4, max0(w) * max0(loss));
     }
 }
 
@@ -168,13 +168,13 @@ struct IonPairCache {
 #pragma unroll
             for (int b = 0; b < 2; ++b) {
                 double const v = slot->acc[2 * a + b];
-                if (v == 0.0 || !use_i[b] || !isfinite(v)) continue;
+                if (eq0(v) || !use_i[b] || !finite_bits(v)) continue;
                 double* cell = cells + i[b] + static_cast<size_t>(nr) * j[a];
                 atomicAdd(cell + plane * 1, v);
                 if (low) atomicAdd(cell, v);
                 atomicAdd(cell + plane * 3, v);
-                double const l = v * fmax(loss, 0.0);
-                if (l != 0.0 && isfinite(l)) atomicAdd(cell + plane * 4, l);
+                double const l = v * max0(loss);
+                if (ne0(l) && finite_bits(l)) atomicAdd(cell + plane * 4, l);
             }
         }
     }
@@ -190,15 +190,15 @@ struct IonPairCache {
 #pragma unroll
             for (int q = 0; q < 4; ++q) slot->acc[q] = 0.0;
         }
-        double const wv = fmax(w, 0.0);
+        double const wv = max0(w);
 #pragma unroll
         for (int a = 0; a < 2; ++a) {
             double const wz = st.wz[a];
-            if (wz == 0.0 || !st.use_j[a]) continue;
+            if (eq0(wz) || !st.use_j[a]) continue;
 #pragma unroll
             for (int b = 0; b < 2; ++b) {
                 double const v = wv * st.wr[b] * wz;
-                if (v == 0.0 || !st.use_i[b] || !isfinite(v)) continue;
+                if (eq0(v) || !st.use_i[b] || !finite_bits(v)) continue;
                 slot->acc[2 * a + b] += v;
             }
         }
@@ -221,7 +221,7 @@ struct GroupClosure {
     __device__ __forceinline__ void begin(double q_parent, double rest_parent, double w, double e_before, double e_after,
                                           bool survives)
     {
-        finite = isfinite(w) && isfinite(e_before) && isfinite(e_after) && w > 0.0 && e_before >= 0.0 && e_after >= 0.0;
+        finite = finite_bits(w) && finite_bits(e_before) && finite_bits(e_after) && gt0(w) && ge0(e_before) && ge0(e_after);
         in_q = q_parent * w;
         out_q = survives ? in_q : 0.0;
         in_e = w * (e_before + rest_parent);
@@ -230,7 +230,7 @@ struct GroupClosure {
     }
     __device__ __forceinline__ void secondary(double q, double rest, double w, double e)
     {
-        finite = finite && isfinite(w) && isfinite(e) && w > 0.0 && e >= 0.0;
+        finite = finite && finite_bits(w) && finite_bits(e) && gt0(w) && ge0(e);
         out_q += q * w;
         thru_q += fabs(q * w);
         out_e += w * (e + rest);
@@ -238,7 +238,7 @@ struct GroupClosure {
     // AccumulateIonizationEvent with event weight w and secondary energy sec_e
     __device__ __forceinline__ void ionization(double w, double sec_e, double cutoff)
     {
-        finite = finite && isfinite(w) && isfinite(sec_e) && w > 0.0;
+        finite = finite && finite_bits(w) && finite_bits(sec_e) && gt0(w);
         in_e += w * kMeC2;
         out_q += w;
         thru_q += w;
@@ -251,7 +251,7 @@ struct GroupClosure {
     // AccumulatePositiveIonSourceOnly with event weight w
     __device__ __forceinline__ void positive_ion(double w)
     {
-        finite = finite && isfinite(w) && w > 0.0;
+        finite = finite && finite_bits(w) && gt0(w);
         in_e += w * kMeC2;
         out_q += w;
         thru_q += w;
@@ -259,7 +259,7 @@ struct GroupClosure {
     // AccumulateLowEnergyElectron with event weight w
     __device__ __forceinline__ void low_energy_electron(double w)
     {
-        finite = finite && isfinite(w) && w > 0.0;
+        finite = finite && finite_bits(w) && gt0(w);
         out_q -= w;
         thru_q += w;
         out_e += w * kMeC2;
@@ -267,16 +267,16 @@ struct GroupClosure {
     // deposit_local_energy_as_ion_pairs: the local energy and its pairs
     __device__ __forceinline__ void local(double w, double e, double w_air, double cutoff)
     {
-        if (w <= 0.0 || e <= 0.0) return;
+        if (le0(w) || le0(e)) return;
         out_e += w * e;
-        finite = finite && isfinite(e);
+        finite = finite && finite_bits(e);
         double const pw = w * e / fmax(w_air, 1.0);
-        if (pw > 0.0) ionization(pw, 0.0, cutoff);
+        if (gt0(pw)) ionization(pw, 0.0, cutoff);
     }
     __device__ __forceinline__ bool valid(double cutoff) const
     {
-        if (!(finite && isfinite(cutoff) && cutoff > 0.0 && isfinite(in_e) && isfinite(out_e) && isfinite(in_q)
-              && isfinite(out_q))) {
+        if (!(finite && finite_bits(cutoff) && gt0(cutoff) && finite_bits(in_e) && finite_bits(out_e) && finite_bits(in_q)
+              && finite_bits(out_q))) {
             return false;
         }
         double const tol_q = 64.0 * kEps * fmax(1.0, thru_q);
