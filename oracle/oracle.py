@@ -86,6 +86,8 @@ def lib():
         _lib.oracle_diagnostics.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                                             ctypes.POINTER(ctypes.c_int32)]
         _lib.oracle_cell_sources.argtypes = [d]
+        _lib.oracle_set_density_profile.argtypes = [d, d, ctypes.c_int64, ctypes.c_double, ctypes.c_double]
+        _lib.oracle_density_query.argtypes = [ctypes.c_int, d, ctypes.c_int64, ctypes.c_double, d]
     return _lib
 
 
@@ -115,6 +117,37 @@ def load_tables(path):
         return
     _check(lib().oracle_load_tables(path.encode()))
     _loaded_path = path
+
+
+def set_density_profile(altitude_m=None, density_kg_m3=None, altitude_msl_at_z0_m=0.0,
+                        reference_density_kg_m3=0.0):
+    """Binds the altitude density profile (TransportDensityRatioAtZ with
+    rrea.air_density_model=altitude_profile); no arrays unbinds it."""
+    if altitude_m is None:
+        alt = dens = np.zeros(0)
+    else:
+        alt = np.ascontiguousarray(altitude_m, dtype=np.float64)
+        dens = np.ascontiguousarray(density_kg_m3, dtype=np.float64)
+        if alt.shape != dens.shape:
+            raise ValueError("altitude and density columns differ in length")
+    _check(lib().oracle_set_density_profile(_dptr(alt), _dptr(dens), alt.shape[0], altitude_msl_at_z0_m,
+                                            reference_density_kg_m3))
+
+
+def profile_density(altitude_m):
+    """The bound profile's density (kg/m^3) at each altitude."""
+    a = np.ascontiguousarray(altitude_m, dtype=np.float64)
+    out = np.zeros_like(a)
+    _check(lib().oracle_density_query(0, _dptr(a), a.shape[0], 0.0, _dptr(out)))
+    return out
+
+
+def density_ratio_at_z(z_m, uniform_ratio):
+    """TransportDensityRatioAtZ at each axial position."""
+    z = np.ascontiguousarray(z_m, dtype=np.float64)
+    out = np.zeros_like(z)
+    _check(lib().oracle_density_query(1, _dptr(z), z.shape[0], uniform_ratio, _dptr(out)))
+    return out
 
 
 def primitive(which, inputs, out_cols):

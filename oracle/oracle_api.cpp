@@ -65,6 +65,40 @@ void oracle_rng(uint64_t const* keys, int64_t n, uint64_t* counter, double* unif
 }
 
 // Arena export so tests can compare the host loader against the device copy.
+// Binds the altitude density profile (n == 0 unbinds it).
+int oracle_set_density_profile(double const* altitude_m, double const* density_kg_m3, int64_t n,
+                               double altitude_msl_at_z0_m, double reference_density_kg_m3)
+{
+    try {
+        oracle::DensityProfile p;
+        if (n > 0) {
+            p.altitude_m.assign(altitude_m, altitude_m + n);
+            p.density_kg_m3.assign(density_kg_m3, density_kg_m3 + n);
+        }
+        p.altitude_msl_at_z0_m = altitude_msl_at_z0_m;
+        p.reference_density_kg_m3 = reference_density_kg_m3;
+        oracle::SetDensityProfile(std::move(p));
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+// out[i] = the bound profile's density at altitude_m[i] (mode 0) or the
+// transport density ratio at axial position z = altitude_m[i] (mode 1).
+int oracle_density_query(int mode, double const* in, int64_t n, double uniform_ratio, double* out)
+{
+    try {
+        for (int64_t i = 0; i < n; ++i) {
+            out[i] = mode == 0 ? oracle::BoundDensityProfile().interpolate(in[i])
+                               : oracle::DensityRatioAtZ(uniform_ratio, in[i]);
+        }
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
 int64_t oracle_arena_size() { return g_tables ? static_cast<int64_t>(g_tables->arena().size()) : 0; }
 
 int charged_step(bool positron, rrea_gpu_config const* cfg, double const* er, double const* ez, double const* bt,

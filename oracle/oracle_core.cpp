@@ -762,14 +762,86 @@ FieldRange path_field_work(Gather const& g, Path const& path, double q, double b
 }
 
 // ======================================================================
-// Material path: O/RreaMaterialPath.H (uniform density profile)
+// Material path: O/RreaMaterialPath.H, with the density ratio of
+// TransportDensityRatioAtZ (uniform or altitude profile)
 // ======================================================================
 struct Interval {
     double begin = 0, end = 0, length = 0, density = 1.0;
 };
 double positive_or(double v, double fb) { return v > 0.0 ? v : fb; }
 
-// :87-114 with TransportDensityRatioAtZ = the uniform configured ratio
+}  // namespace
+
+namespace {
+DensityProfile g_profile;
+}
+
+// RreaAltitudeProfile::Interpolate, S/RreaAltitudeProfile.cpp:125-147
+double DensityProfile::interpolate(double altitude) const
+{
+    if (!enabled()) fail(RREA_GPU_ERR_NOT_READY, "altitude profile was not loaded");
+    if (altitude < altitude_m.front() || altitude > altitude_m.back() || std::isnan(altitude)) {
+        fail(RREA_GPU_ERR_RANGE, "altitude " + std::to_string(altitude) + " m is outside the profile range");
+    }
+    auto const upper = std::upper_bound(altitude_m.begin(), altitude_m.end(), altitude);
+    if (upper == altitude_m.begin()) return density_kg_m3.front();
+    if (upper == altitude_m.end()) return density_kg_m3.back();
+    std::size_t const hi = static_cast<std::size_t>(upper - altitude_m.begin());
+    std::size_t const lo = hi - 1;
+    double const span = altitude_m[hi] - altitude_m[lo];
+    double const t = span > 0.0 ? (altitude - altitude_m[lo]) / span : 0.0;
+    return (1.0 - t) * density_kg_m3[lo] + t * density_kg_m3[hi];
+}
+
+// RreaAltitudeProfile::LoadCsv's checks (S/RreaAltitudeProfile.cpp:97-117,
+// density column loaded with require_positive) and the reference density
+// the ratio is taken against (O/RreaWarpXCoupling.cpp:88-93).
+void SetDensityProfile(DensityProfile p)
+{
+    if (p.altitude_m.empty() && p.density_kg_m3.empty()) {
+        g_profile = DensityProfile{};
+        return;
+    }
+    if (p.altitude_m.size() != p.density_kg_m3.size() || p.altitude_m.size() < 2) {
+        fail(RREA_GPU_ERR_ARGUMENT, "altitude profile needs at least two rows");
+    }
+    for (std::size_t i = 0; i < p.altitude_m.size(); ++i) {
+        if (!std::isfinite(p.altitude_m[i]) || !std::isfinite(p.density_kg_m3[i])) {
+            fail(RREA_GPU_ERR_ARGUMENT, "altitude profile values must be finite");
+        }
+        if (i > 0 && p.altitude_m[i] <= p.altitude_m[i - 1]) {
+            fail(RREA_GPU_ERR_ARGUMENT, "altitude profile altitudes must be strictly increasing");
+        }
+        if (!(p.density_kg_m3[i] > 0.0)) {
+            fail(RREA_GPU_ERR_ARGUMENT, "altitude profile requires strictly positive densities");
+        }
+    }
+    if (!(p.reference_density_kg_m3 > 0.0) || !std::isfinite(p.reference_density_kg_m3)
+        || !std::isfinite(p.altitude_msl_at_z0_m)) {
+        fail(RREA_GPU_ERR_ARGUMENT, "altitude profile needs a positive reference density and a finite datum");
+    }
+    g_profile = std::move(p);
+}
+
+DensityProfile const& BoundDensityProfile() { return g_profile; }
+
+// O/RreaWarpXCoupling.cpp:79-95 (ProfileAltitudeMslAtZ, :67-71)
+double DensityRatioAtZ(double uniform_ratio, double z_m)
+{
+    if (!g_profile.enabled()) return uniform_ratio;
+    return g_profile.interpolate(g_profile.altitude_msl_at_z0_m + z_m) / g_profile.reference_density_kg_m3;
+}
+
+double StepDensityRatio(rrea_gpu_config const& cfg)
+{
+    return positive_or(DensityRatioAtZ(cfg.density_ratio, 0.5 * (cfg.z_lo + cfg.z_hi)),
+                       positive_or(cfg.density_ratio, 1.0));
+}
+
+namespace {
+
+// :87-114; `density_ratio` is the ratio without a profile and `fallback`
+// the step's ratio
 std::vector<Interval> build_intervals(Path const& path, double density_ratio, double fallback)
 {
     std::vector<Interval> out;
@@ -783,7 +855,7 @@ std::vector<Interval> build_intervals(Path const& path, double density_ratio, do
             if (e > b && path.full > 0.0) {
                 double x, y, z;
                 path.PointAtPiece(piece, 0.5 * (b + e), x, y, z);
-                dl = path.full * (e - b) * positive_or(density_ratio, fallback);
+                dl = path.full * (e - b) * positive_or(DensityRatioAtZ(density_ratio, z), fallback);
             }
         }
         Interval iv;
@@ -1442,8 +1514,8 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
     double const photon_cut = cfg.photon_cutoff_eV;
     double const hm_thr = ts.index().hard_moller_threshold_eV;
     bool const hm_enabled = cfg.debug_disable_hard_moller == 0;
-    // RreaParticleInteraction.cpp:33-35 (uniform density: profile ratio = configured ratio)
-    double const density_ratio = positive_or(cfg.density_ratio, 1.0);
+    // RreaParticleInteraction.cpp:27-35
+    double const density_ratio = StepDensityRatio(cfg);
     uint64_t const seed = cfg.rng_seed;
     uint64_t const step_key = static_cast<uint64_t>(std::max(step, 0));
     double const w_air = ts.index().w_air_eV_per_pair;
@@ -1516,7 +1588,8 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
 
         double const chord_dpath = density_path(driver_iv, driver, driver.in_begin, driver.in_end);
         double transported_dpath = 0.0, transported_len = 0.0;
-        double particle_density = ds > 0.0 ? chord_dpath / ds : positive_or(density_ratio, density_ratio);
+        double particle_density =
+            ds > 0.0 ? chord_dpath / ds : positive_or(DensityRatioAtZ(cfg.density_ratio, z_particle), density_ratio);
         Path path = driver;
         std::vector<Interval> iv = driver_iv;
 
@@ -1975,7 +2048,7 @@ void ApplyPositronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
     double const cutoff = cfg.low_energy_cutoff_eV;
     double const photon_cut = cfg.photon_cutoff_eV;
     double const hm_thr = ts.index().hard_moller_threshold_eV;
-    double const density_ratio = positive_or(cfg.density_ratio, 1.0);
+    double const density_ratio = StepDensityRatio(cfg);
     uint64_t const seed = cfg.rng_seed;
     uint64_t const step_key = static_cast<uint64_t>(std::max(step, 0));
     double const w_air = ts.index().w_air_eV_per_pair;
@@ -2504,7 +2577,7 @@ bool electron_demotes_at(NewbornContext const& c, double x, double y, double z, 
     double const thr = c.ts.index().hard_moller_threshold_eV;
     double fer, fez, fbt;
     c.gather.at(std::hypot(x, y), z, fer, fez, fbt);
-    double const rho = positive_or(positive_or(c.cfg.density_ratio, 1.0), 1.0);
+    double const rho = positive_or(DensityRatioAtZ(c.cfg.density_ratio, z), 1.0);
     double const ke = std::max(e, cut);
     double drag = 0.0;
     if (ke > 0.0 && rho > 0.0) {
@@ -2540,7 +2613,7 @@ bool advance_charged_newborn(NewbornContext const& c, Secondary& p, NewbornEffec
     double const photon_cut = cfg.photon_cutoff_eV;
     double const thr = c.ts.index().hard_moller_threshold_eV;
     bool const hm_enabled = cfg.debug_disable_hard_moller == 0;
-    double const rho = positive_or(cfg.density_ratio, 1.0);
+    double const rho = StepDensityRatio(cfg);
     double const w_air = c.ts.index().w_air_eV_per_pair;
     uint64_t const seed = cfg.rng_seed, key = p.root_key;
     uint64_t const step_key = static_cast<uint64_t>(std::max(c.step, 0));
@@ -2996,7 +3069,7 @@ bool advance_photon_newborn(NewbornContext const& c, Secondary& p, NewbornEffect
     bool const periodic = cfg.periodic_z != 0;
     double const cut = cfg.low_energy_cutoff_eV;
     double const photon_cut = cfg.photon_cutoff_eV;
-    double const rho = positive_or(cfg.density_ratio, 1.0);
+    double const rho = StepDensityRatio(cfg);
     double const w_air = c.ts.index().w_air_eV_per_pair;
     uint64_t const seed = cfg.rng_seed, key = p.root_key;
     uint64_t const step_key = static_cast<uint64_t>(std::max(c.step, 0));
@@ -3270,7 +3343,7 @@ void ApplyPhotonTransport(TableSet const& ts, rrea_gpu_config const& cfg, int st
     bool const periodic = cfg.periodic_z != 0;
     double const cutoff = cfg.low_energy_cutoff_eV;
     double const photon_cut = cfg.photon_cutoff_eV;
-    double const density_ratio = positive_or(cfg.density_ratio, 1.0);
+    double const density_ratio = StepDensityRatio(cfg);
     uint64_t const seed = cfg.rng_seed;
     uint64_t const step_key = static_cast<uint64_t>(std::max(step, 0));
     double const w_air = ts.index().w_air_eV_per_pair;

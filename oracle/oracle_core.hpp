@@ -246,6 +246,28 @@ struct MaxwellField {
 void AdvanceMaxwell(MaxwellField& f, double dt_s, int substeps, std::vector<double> const& jr,
                     std::vector<double> const& jz);
 
+// Transport density ratio at an axial position, TransportDensityRatioAtZ
+// (O/RreaWarpXCoupling.cpp:79-95): the configured uniform ratio, or, with an
+// altitude profile bound (rrea.air_density_model=altitude_profile), the
+// profile density at altitude_msl_at_z0 + z over the tables' reference
+// density.  The profile interpolates linearly between strictly increasing
+// altitude nodes and fails outside them (S/RreaAltitudeProfile.cpp:125-147).
+struct DensityProfile {
+    std::vector<double> altitude_m, density_kg_m3;
+    double altitude_msl_at_z0_m = 0.0;
+    double reference_density_kg_m3 = 0.0;
+    bool enabled() const { return !altitude_m.empty(); }
+    double interpolate(double altitude_m) const;
+};
+// Binds (or, with no nodes, unbinds) the profile; validates it as
+// RreaAltitudeProfile::LoadCsv does (S/RreaAltitudeProfile.cpp:97-117).
+void SetDensityProfile(DensityProfile p);
+DensityProfile const& BoundDensityProfile();
+double DensityRatioAtZ(double uniform_ratio, double z_m);
+// The step's fallback ratio: the ratio at the domain's axial centre, else
+// the configured ratio, else 1 (O/RreaParticleInteraction.cpp:27-35).
+double StepDensityRatio(rrea_gpu_config const& cfg);
+
 // Primitive-level evaluation for fixture comparisons (ids listed in oracle_core.cpp).
 int RunPrimitive(rrea_host::TableSet const& tables, int which, double const* in, int64_t n, double* out);
 

@@ -8,6 +8,7 @@
 #include "RreaChargedInterleave.H"
 #include "RreaParticleInteraction.H"
 #include "RreaRng.H"
+#include "rrea/RreaAltitudeProfile.H"
 #include "rrea/RreaInteractionTables.H"
 #include "rrea/RreaConstants.H"
 #include "rrea/RreaMaxwellTMRZ.H"
@@ -19,6 +20,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -503,6 +505,40 @@ int main(int argc, char** argv)
             write_f8("ref_photoelectron_cos", 3, pec);
             write_f8("ref_pair", 19, pair);
             write_f8("ref_annihilation", 9, ann);
+        }
+        // ---- altitude density profile: S/RreaAltitudeProfile.cpp (LoadCsv and
+        // Interpolate), on a synthetic exponential atmosphere written as CSV
+        // with the NRLMSISE column names and units (km, g/cm^3)
+        {
+            std::string const csv = g_outdir + "/ref_altitude_profile_input.csv";
+            {
+                std::ofstream f(csv);
+                f << "model,altitude_km_MSL,mass_density_g_cm3\n";
+                char line[128];
+                for (int i = 0; i <= 160; ++i) {
+                    double const km = 6.0 + 0.05 * i;
+                    std::snprintf(line, sizeof line, "synthetic,%.17g,%.17g\n", km, 1.225e-3 * std::exp(-km / 7.2));
+                    f << line;
+                }
+            }
+            rrea::RreaAltitudeProfile prof;
+            prof.LoadCsv(csv, "altitude_km_MSL", "mass_density_g_cm3", 1000.0, 1000.0, true);
+            std::remove(csv.c_str());
+            std::vector<double> nodes, rows;
+            for (int i = 0; i <= 160; ++i) {
+                double const a = (6.0 + 0.05 * i) * 1000.0;
+                nodes.insert(nodes.end(), {a, prof.Interpolate(a)});
+            }
+            for (int i = 0; i < 4096; ++i) {
+                double a = 6000.0 + 8000.0 * g.uni();
+                if (i < 161) a = (6.0 + 0.05 * i) * 1000.0;                       // every node
+                else if (i < 321) a = (6.0 + 0.05 * (i - 161) + 0.025) * 1000.0;  // every midpoint
+                if (i == 321) a = prof.MinAltitudeM();
+                if (i == 322) a = prof.MaxAltitudeM();
+                rows.insert(rows.end(), {a, prof.Interpolate(a)});
+            }
+            write_f8("ref_altitude_profile_nodes", 2, nodes);
+            write_f8("ref_altitude_profile", 2, rows);
         }
         std::printf("golden fixtures written to %s\n", g_outdir.c_str());
     } catch (std::exception const& e) {

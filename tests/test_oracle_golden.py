@@ -140,3 +140,37 @@ def test_maxwell_step_matches_reference(oracle_mod):
     for _ in range(4):
         er, ez, bt = oracle_mod.advance_maxwell(nr, nz, dr, dz, dt, 3, er, ez, bt, jr, jz)
     np.testing.assert_array_equal(np.concatenate([er, ez, bt]), load("ref_maxwell_out")[:, 0])
+
+
+def test_altitude_profile_matches_reference(oracle_mod):
+    """RreaAltitudeProfile::LoadCsv + Interpolate (S/RreaAltitudeProfile.cpp)
+    on a synthetic exponential atmosphere: nodes, midpoints, both ends and
+    random altitudes, bit-exact; the transport ratio is the density over the
+    tables' reference density at altitude_msl_at_z0 + z."""
+    nodes = load("ref_altitude_profile_nodes")
+    rows = load("ref_altitude_profile")
+    oracle_mod.set_density_profile(nodes[:, 0], nodes[:, 1], 6000.0, 1.20479)
+    try:
+        got = oracle_mod.profile_density(rows[:, 0])
+        np.testing.assert_array_equal(got, rows[:, 1])
+        ratio = oracle_mod.density_ratio_at_z(rows[:, 0] - 6000.0, 0.5)
+        np.testing.assert_array_equal(ratio, rows[:, 1] / 1.20479)
+        for bad in (5999.0, 14000.5, np.nan):
+            with pytest.raises(oracle_mod.OracleFailure) as e:
+                oracle_mod.profile_density(np.array([bad]))
+            assert e.value.code == 4  # RREA_GPU_ERR_RANGE
+    finally:
+        oracle_mod.set_density_profile()
+    np.testing.assert_array_equal(oracle_mod.density_ratio_at_z(np.array([0.0, 1.0e3]), 0.5), [0.5, 0.5])
+
+
+@pytest.mark.parametrize("alt,dens", [
+    ([0.0], [1.0]),                      # fewer than two rows
+    ([0.0, 0.0], [1.0, 1.0]),            # not strictly increasing
+    ([0.0, 1.0], [1.0, 0.0]),            # non-positive density
+    ([0.0, 1.0], [1.0, np.nan]),         # non-finite
+])
+def test_altitude_profile_rejects_invalid_tables(oracle_mod, alt, dens):
+    with pytest.raises(oracle_mod.OracleFailure) as e:
+        oracle_mod.set_density_profile(np.array(alt), np.array(dens), 0.0, 1.2)
+    assert e.value.code == 1  # RREA_GPU_ERR_ARGUMENT
