@@ -90,6 +90,25 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx);
  * (replaces RreaInteractionTables::Load, S/RreaInteractionTables.cpp:1659). */
 rrea_gpu_status rrea_gpu_load_tables(rrea_gpu_ctx* ctx, const char* transport_physics_json);
 
+/* Binds an altitude density profile to the transport
+ * (rrea.air_density_model=altitude_profile; replaces the profile half of
+ * RreaWarpXCoupling::TransportDensityRatioAtZ, O/RreaWarpXCoupling.cpp:79-95,
+ * and RreaAltitudeProfile, S/RreaAltitudeProfile.cpp:37-147).  The density
+ * ratio at axial position z is Interpolate(altitude_msl_at_z0_m + z) /
+ * reference_density_kg_m3, linear between the n nodes; every material
+ * interval takes it at its piece midpoint (O/RreaMaterialPath.H:60-114).
+ * Altitudes strictly increasing, densities strictly positive and finite,
+ * n >= 2, reference density positive (RREA_GPU_ERR_ARGUMENT otherwise); the
+ * domain's axial centre, where each step takes its fallback ratio
+ * (O/RreaParticleInteraction.cpp:27-35), must lie inside the profile
+ * (RREA_GPU_ERR_RANGE).  A transport query outside the profile fails the
+ * step with RREA_GPU_ERR_RANGE, as the reference throws.  n == 0 restores the
+ * configured uniform ratio.  Host pointers, copied. */
+rrea_gpu_status rrea_gpu_set_density_profile(rrea_gpu_ctx* ctx, const double* altitude_m,
+                                             const double* density_kg_m3, int64_t n,
+                                             double altitude_msl_at_z0_m,
+                                             double reference_density_kg_m3);
+
 /* Sets the Maxwell (scattered) field and the static ambient field on the
  * replicated TM-RZ vectors (I/RreaMaxwellTMRZ.H:61-85): er (nr+1)*nz,
  * ez nr*(nz+1), btheta (nr+1)*(nz+1); amb_er/amb_ez as er/ez.  Host pointers. */

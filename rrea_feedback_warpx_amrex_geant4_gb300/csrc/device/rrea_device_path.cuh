@@ -526,8 +526,8 @@ __device__ __forceinline__ FieldRange path_field_work(FieldView const& fv, Geom 
 }
 
 // ------------------------------------------------------------ material path
-// O/RreaMaterialPath.H:47-199 for a uniform density ratio: one interval per
-// in-domain piece.
+// O/RreaMaterialPath.H:47-199: one interval per in-domain piece, with the
+// piece's density ratio taken at its midpoint.
 template <int NP>
 struct Intervals {
     int n;
@@ -535,6 +535,57 @@ struct Intervals {
 };
 
 __device__ __forceinline__ double positive_or(double v, double fb) { return gt0(v) ? v : fb; }
+
+// The altitude density profile bound to the context
+// (rrea.air_density_model=altitude_profile); n == 0 is the uniform ratio.
+struct DensityProfile {
+    const double* alt;  // n strictly increasing altitudes above mean sea level (m)
+    const double* val;  // n densities (kg/m^3), strictly positive
+    int n;
+    double alt0;        // altitude of z = 0 (ProfileAltitudeMslAtZ, O/RreaWarpXCoupling.cpp:67-71)
+    double ref;         // the tables' reference density (kg/m^3)
+};
+
+// TransportDensityRatioAtZ (O/RreaWarpXCoupling.cpp:79-95) with
+// RreaAltitudeProfile::Interpolate (S/RreaAltitudeProfile.cpp:125-147): the
+// uniform ratio without a profile; with one, the density interpolated
+// linearly at alt0 + z over the reference density.  An altitude outside the
+// profile fails the step (the reference throws).  The interpolation is
+// evaluated without contraction so it rounds as the reference does.
+__device__ __forceinline__ double density_ratio_at_z(DensityProfile const& d, double uniform, double z, Err& err)
+{
+    if (d.n == 0) return uniform;
+    double const a = d.alt0 + z;
+    if (!(a >= __ldg(d.alt) && a <= __ldg(d.alt + d.n - 1))) {
+        err.set(RREA_GPU_ERR_RANGE);
+        return uniform;
+    }
+    // std::upper_bound: the first node above a
+    long long const ak = order_key(a);
+    const long long* __restrict__ xk = reinterpret_cast<const long long*>(d.alt);
+    int up = 0, count = d.n;
+    while (count > 0) {
+        int const step = count >> 1;
+        if (__ldg(xk + up + step) <= ak) {
+            up += step + 1;
+            count -= step + 1;
+        } else {
+            count = step;
+        }
+    }
+    double v;
+    if (up == 0) {
+        v = __ldg(d.val);
+    } else if (up == d.n) {
+        v = __ldg(d.val + d.n - 1);
+    } else {
+        int const lo = up - 1;
+        double const span = __ldg(d.alt + up) - __ldg(d.alt + lo);
+        double const t = gt0(span) ? (a - __ldg(d.alt + lo)) / span : 0.0;
+        v = __dadd_rn(__dmul_rn(1.0 - t, __ldg(d.val + lo)), __dmul_rn(t, __ldg(d.val + up)));
+    }
+    return v / d.ref;
+}
 
 // :60-114
 template <int NP>
@@ -564,6 +615,40 @@ __device__ __forceinline__ void build_intervals(Path<NP> const& p, double rho, I
             ++iv.n;
         }
     }
+}
+// :60-114 with the density profile: each piece's ratio at its midpoint
+// (integrate_density_piece_m's midpoint rule); `rho` is the step's ratio,
+// the fallback of a non-positive value.
+// Kept out of line: the uniform-density transport never calls it, and its
+// code stays out of the transport loop.
+template <int NP>
+__device__ __noinline__ void build_intervals_profile(Path<NP> const& p, Geom const& g, DensityProfile const& dp,
+                                                     double rho, Intervals<NP>& iv, Err& err)
+{
+    iv.n = 0;
+#pragma unroll 1
+    for (int i = 0; i < p.npieces; ++i) {
+        Piece const& pc = p.pieces[i];
+        if (!(gt0(pc.length))) continue;
+        double dl = 0.0;
+        if (pc.end > pc.begin && gt0(p.full)) {
+            double x, y, z;
+            point_at_piece(p, g, pc, 0.5 * (pc.begin + pc.end), x, y, z);
+            dl = p.full * (pc.end - pc.begin) * positive_or(density_ratio_at_z(dp, rho, z, err), rho);
+        }
+        iv.begin[iv.n] = pc.begin;
+        iv.end[iv.n] = pc.end;
+        iv.length[iv.n] = pc.length;
+        iv.density[iv.n] = positive_or(dl / pc.length, rho);
+        ++iv.n;
+    }
+}
+template <int NP>
+__device__ __forceinline__ void build_intervals(Path<NP> const& p, Geom const& g, DensityProfile const& dp,
+                                                double rho, Intervals<NP>& iv, Err& err)
+{
+    if (dp.n == 0) build_intervals(p, rho, iv);
+    else build_intervals_profile(p, g, dp, rho, iv, err);
 }
 // :117-136
 template <int NP>

@@ -569,13 +569,14 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     clipped_escape_policy(path, g, rz_radius(path.ex, path.ey), path.ez, esc, esc_inv);
     double const ds = driver_valid ? path.in_length : 0.0;
     Intervals<NP> iv;
-    build_intervals(path, rho, iv);
+    build_intervals(path, g, A.prof, rho, iv, err);
     double const driver_span = fmax(path.in_end, 1.0e-6);
     FieldRange const dfw = path_field_work(A.fv, g, path, q, 0.0, 1.0, err);
     double const field_work = dfw.work / driver_span;
     double const chord_dpath = density_path(iv, path, path.in_begin, path.in_end);
     double transported_dpath = 0.0, transported_len = 0.0;
-    double particle_density = gt0(ds) ? chord_dpath / ds : positive_or(rho, rho);
+    double particle_density =
+        gt0(ds) ? chord_dpath / ds : positive_or(density_ratio_at_z(A.prof, C.cfg.density_ratio, z_particle, err), rho);
 
     // net chord from the captured start (AccumulateChargedSegment), signed
     // with the species charge; deposited by the current pass after the kernel
@@ -855,7 +856,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                 exited = path.exits;
                 break;
             }
-            build_intervals(path, rho, iv);
+            build_intervals(path, g, A.prof, rho, iv, err);
             if (iv.n == 0) {
                 err.set(RREA_GPU_ERR_INVALID_STATE);
                 break;

@@ -56,6 +56,8 @@ struct ElectronArgs {
     uint32_t* __restrict__ sec_per_parent;
     // cell sources: 5 grids of nr*nz
     double* __restrict__ cells;
+    // altitude density profile (prof.n == 0: uniform density ratio)
+    DensityProfile prof;
     // optional per-particle diagnostics (may be null)
     uint64_t* __restrict__ diag_subcycles;
     uint64_t* __restrict__ diag_events;

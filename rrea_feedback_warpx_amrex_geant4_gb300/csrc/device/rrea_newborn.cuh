@@ -73,7 +73,7 @@ __device__ __forceinline__ bool newborn_electron_demotes(StepConstants const& C,
     double const thr = C.hm_threshold_eV;
     double fer, fez, fbt;
     gather(A.fv, rz_radius(x, y), z, fer, fez, fbt);
-    double const rho = positive_or(C.density_ratio, 1.0);
+    double const rho = positive_or(density_ratio_at_z(A.prof, C.cfg.density_ratio, z, err), 1.0);
     double const ke = fmax(e, cut);
     if (!charged_in_range(C.tix, ke)) err.set(RREA_GPU_ERR_RANGE);
     double drag = 0.0;
@@ -192,7 +192,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
         return 1;
     }
     Intervals<NP> iv;
-    build_intervals(path, rho, iv);
+    build_intervals(path, g, A.prof, rho, iv, err);
     if (iv.n == 0) {
         err.set(RREA_GPU_ERR_INVALID_STATE);
         return -1;
@@ -342,7 +342,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
                 final_fraction = 0.0;
                 break;
             }
-            build_intervals(path, rho, iv);
+            build_intervals(path, g, A.prof, rho, iv, err);
             if (iv.n == 0) {
                 err.set(RREA_GPU_ERR_INVALID_STATE);
                 break;
@@ -608,7 +608,7 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
             return -1;
         }
         Intervals<NP> iv;
-        build_intervals(path, rho, iv);
+        build_intervals(path, g, A.prof, rho, iv, err);
         PhotonRates rates;
         if (!photon_rates(C, arena, energy, rates, err)) return -1;
         double const mfp = mfp_from_inverse(rates.total(), err);

@@ -540,7 +540,7 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
         clipped_escape_policy(path, g, rz_radius(path.ex, path.ey), path.ez, esc, esc_inv);
         double const ds = path.in_length;
         Intervals<NP> iv;
-        build_intervals(path, rho, iv);
+        build_intervals(path, g, A.prof, rho, iv, err);
         double const chord_dpath = density_path(iv, path, path.in_begin, path.in_end);
         if (le0(weight) || energy < photon_cut) {
             double x, y, z;

@@ -119,6 +119,12 @@ struct rrea_gpu_ctx {
     bool field_set = false;
     bool has_b = false;
 
+    // altitude density profile: n altitudes then n densities on the device
+    double* d_profile = nullptr;
+    int profile_n = 0;
+    double profile_alt0 = 0.0, profile_ref = 0.0;
+    double profile_step_ratio = 1.0;  // the ratio at the domain's axial centre
+
     // one resident SoA tile per species (RREA_SPECIES_ELECTRON/POSITRON/PHOTON)
     SpeciesTile tiles[kSpecies];
 
@@ -378,6 +384,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
         dfree(st.id);
         dfree(st.cpu);
     }
+    dfree(ctx->d_profile);
     dfree(ctx->d_sec_unordered);
     dfree(ctx->d_sec_ordered);
     dfree(ctx->d_sec_count);
@@ -492,6 +499,70 @@ rrea_gpu_status rrea_gpu_set_field(rrea_gpu_ctx* ctx, const double* er, const do
     return RREA_GPU_OK;
 }
 
+rrea_gpu_status rrea_gpu_set_density_profile(rrea_gpu_ctx* ctx, const double* altitude_m, const double* density_kg_m3,
+                                             int64_t n, double altitude_msl_at_z0_m, double reference_density_kg_m3)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    if (n == 0) {
+        ctx->profile_n = 0;
+        return RREA_GPU_OK;
+    }
+    // RreaAltitudeProfile::LoadCsv (S/RreaAltitudeProfile.cpp:97-117) and the
+    // reference density the ratio is taken against (O/RreaWarpXCoupling.cpp:88-93)
+    if (!altitude_m || !density_kg_m3 || n < 2 || n > (int64_t{1} << 24)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "altitude profile needs at least two rows");
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        if (!std::isfinite(altitude_m[i]) || !std::isfinite(density_kg_m3[i])) {
+            return fail(ctx, RREA_GPU_ERR_ARGUMENT, "altitude profile values must be finite");
+        }
+        if (i > 0 && !(altitude_m[i] > altitude_m[i - 1])) {
+            return fail(ctx, RREA_GPU_ERR_ARGUMENT, "altitude profile altitudes must be strictly increasing");
+        }
+        if (!(density_kg_m3[i] > 0.0)) {
+            return fail(ctx, RREA_GPU_ERR_ARGUMENT, "altitude profile requires strictly positive densities");
+        }
+    }
+    if (!(reference_density_kg_m3 > 0.0) || !std::isfinite(reference_density_kg_m3) ||
+        !std::isfinite(altitude_msl_at_z0_m)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "altitude profile needs a positive reference density and a finite datum");
+    }
+    // every step asks for the ratio at the domain's axial centre
+    // (O/RreaParticleInteraction.cpp:27-35): it must lie inside the profile
+    double const a = altitude_msl_at_z0_m + 0.5 * (ctx->cfg.z_lo + ctx->cfg.z_hi);
+    if (!(a >= altitude_m[0] && a <= altitude_m[n - 1])) {
+        return fail(ctx, RREA_GPU_ERR_RANGE, "the domain's axial centre lies outside the altitude profile");
+    }
+    int64_t const up = std::upper_bound(altitude_m, altitude_m + n, a) - altitude_m;
+    double v;
+    if (up == 0) {
+        v = density_kg_m3[0];
+    } else if (up == n) {
+        v = density_kg_m3[n - 1];
+    } else {
+        double const span = altitude_m[up] - altitude_m[up - 1];
+        double const t = span > 0.0 ? (a - altitude_m[up - 1]) / span : 0.0;
+        v = (1.0 - t) * density_kg_m3[up - 1] + t * density_kg_m3[up];
+    }
+    double* d = nullptr;
+    if (cudaMalloc(&d, static_cast<size_t>(2 * n) * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, RREA_GPU_ERR_CUDA, "altitude profile allocation failed");
+    }
+    RREA_CUDA(ctx, cudaMemcpyAsync(d, altitude_m, static_cast<size_t>(n) * sizeof(double), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(d + n, density_kg_m3, static_cast<size_t>(n) * sizeof(double),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    dfree(ctx->d_profile);
+    ctx->d_profile = d;
+    ctx->profile_n = static_cast<int>(n);
+    ctx->profile_alt0 = altitude_msl_at_z0_m;
+    ctx->profile_ref = reference_density_kg_m3;
+    ctx->profile_step_ratio = v / reference_density_kg_m3;
+    return RREA_GPU_OK;
+}
+
 }  // extern "C"
 
 namespace {
@@ -549,7 +620,11 @@ rrea_dev::StepConstants step_constants(rrea_gpu_ctx const* ctx, int32_t step, do
     sc.hm_threshold_eV = sc.tix.hard_moller_threshold_eV;
     sc.photon_cutoff_eV = c.photon_cutoff_eV;
     // RreaParticleInteraction.cpp:33-35 with a uniform density ratio
-    sc.density_ratio = c.density_ratio > 0.0 ? c.density_ratio : 1.0;
+    // O/RreaParticleInteraction.cpp:27-35: the ratio at the domain's axial
+    // centre, else the configured ratio, else 1
+    double const configured = c.density_ratio > 0.0 ? c.density_ratio : 1.0;
+    sc.density_ratio = ctx->profile_n > 0 ? (ctx->profile_step_ratio > 0.0 ? ctx->profile_step_ratio : configured)
+                                          : configured;
     sc.step_key = static_cast<uint64_t>(step > 0 ? step : 0);
     sc.dt_s = dt_s;
     sc.hm_enabled = c.debug_disable_hard_moller ? 0 : 1;
@@ -566,6 +641,11 @@ rrea_dev::ElectronArgs sink_args(rrea_gpu_ctx* ctx, rrea_dev::StepConstants cons
     a.sec_capacity = ctx->sec_capacity;
     a.sec_per_parent = ctx->d_sec_per_parent;
     a.cells = ctx->d_cells;
+    a.prof.n = ctx->profile_n;
+    a.prof.alt = ctx->profile_n ? ctx->d_profile : nullptr;
+    a.prof.val = ctx->profile_n ? ctx->d_profile + ctx->profile_n : nullptr;
+    a.prof.alt0 = ctx->profile_alt0;
+    a.prof.ref = ctx->profile_ref;
     a.diag_subcycles = ctx->diagnostics ? ctx->d_diag_sub : nullptr;
     a.diag_events = ctx->diagnostics ? ctx->d_diag_ev : nullptr;
     a.diag_disposition = ctx->diagnostics ? ctx->d_diag_disp : nullptr;

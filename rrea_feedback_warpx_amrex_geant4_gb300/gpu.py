@@ -76,7 +76,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_count_live", "rrea_gpu_population_projection", "rrea_gpu_drain_secondaries",
     "rrea_gpu_drain_resident", "rrea_gpu_fetch_survivors", "rrea_gpu_pending_secondaries",
     "rrea_gpu_last_drain_stats", "rrea_gpu_kernel_launches", "rrea_gpu_current_device",
-    "rrea_gpu_advance_field_from_current", "rrea_gpu_selftest_math",
+    "rrea_gpu_advance_field_from_current", "rrea_gpu_selftest_math", "rrea_gpu_set_density_profile",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -105,6 +105,7 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_destroy.argtypes = [vp]
     lib.rrea_gpu_load_tables.argtypes = [vp, ctypes.c_char_p]
     lib.rrea_gpu_set_field.argtypes = [vp, _D, _D, _D, _D, _D]
+    lib.rrea_gpu_set_density_profile.argtypes = [vp, _D, _D, ctypes.c_int64, ctypes.c_double, ctypes.c_double]
     lib.rrea_gpu_apply_electrons.argtypes = [vp, ctypes.POINTER(RreaGpuTile), ctypes.c_int32, ctypes.c_double,
                                              ctypes.c_double, vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
     lib.rrea_gpu_apply_photons.argtypes = lib.rrea_gpu_apply_electrons.argtypes
@@ -227,6 +228,23 @@ class RreaGpuContext:
     def set_field(self, er, ez, bt, amb_er, amb_ez):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (er, ez, bt, amb_er, amb_ez)]
         self._check(self.lib.rrea_gpu_set_field(self.handle, *[a.ctypes.data_as(_D) for a in arrs]))
+
+    def set_density_profile(self, altitude_m=None, density_kg_m3=None, altitude_msl_at_z0_m=0.0,
+                            reference_density_kg_m3=0.0):
+        """Binds the altitude density profile (rrea.air_density_model=
+        altitude_profile): the transport density ratio at z is the profile
+        density at altitude_msl_at_z0_m + z over reference_density_kg_m3.
+        No arrays restores the configured uniform ratio."""
+        if altitude_m is None:
+            self._check(self.lib.rrea_gpu_set_density_profile(self.handle, None, None, 0, 0.0, 0.0))
+            return
+        alt = np.ascontiguousarray(altitude_m, dtype=np.float64)
+        dens = np.ascontiguousarray(density_kg_m3, dtype=np.float64)
+        if alt.shape != dens.shape:
+            raise ValueError("altitude and density columns differ in length")
+        self._check(self.lib.rrea_gpu_set_density_profile(self.handle, alt.ctypes.data_as(_D), dens.ctypes.data_as(_D),
+                                                          alt.shape[0], altitude_msl_at_z0_m,
+                                                          reference_density_kg_m3))
 
     def set_launch(self, threads_per_block=128, blocks_per_sm=16, diagnostics=True):
         self._check(self.lib.rrea_gpu_set_launch(self.handle, threads_per_block, blocks_per_sm, int(diagnostics)))
