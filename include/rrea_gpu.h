@@ -242,6 +242,31 @@ rrea_gpu_status rrea_gpu_count_live(rrea_gpu_ctx* ctx, int32_t species, int64_t*
 rrea_gpu_status rrea_gpu_population_projection(uint64_t current, uint64_t removals, uint64_t insertions,
                                                uint64_t ceiling, int32_t reject_equality, uint64_t* projected);
 
+/* Commits the survivors of the last resident drain (rrea_gpu_drain_resident)
+ * into the resident species tiles: the particle-creation half of
+ * DrainAndCommitSecondaries (RreaWarpXCoupling::CommitLocalParticleBatch,
+ * O/RreaCouplingSources.cpp:240-330, with the captured pre-push state of
+ * append_rrea_previous_position_attributes, :28-100).  Each record becomes a
+ * particle at (hypot(x, y), z, atan2(y, x)) with, for e-/e+, the proper
+ * velocity of its kinetic energy along its direction and, for photons, the
+ * momentum E along it; records with weight <= 0 (and photons with E <= 0)
+ * are dropped as there.  Particles are appended in FIFO order with ids
+ * continuing after the largest id staged for the species (AMReX's NextID is
+ * in the absent AMReX sources: this is the library's rule).  committed[3]
+ * (may be null) receives the counts per species (RREA_SPECIES_* order).
+ * RREA_GPU_ERR_CAPACITY, with no tile changed, when a tile would exceed the
+ * context capacity. */
+rrea_gpu_status rrea_gpu_commit_survivors_resident(rrea_gpu_ctx* ctx, int64_t* committed);
+
+/* Removes the invalid particles (id <= 0: escaped, demoted, annihilated)
+ * from a resident species tile, keeping the order of the valid ones, as
+ * WarpX's removal of invalid particles does between steps.  n_live (may be
+ * null) receives the new tile size. */
+rrea_gpu_status rrea_gpu_compact_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t* n_live);
+
+/* Number of particles (valid or not) in a resident species tile. */
+rrea_gpu_status rrea_gpu_resident_count(rrea_gpu_ctx* ctx, int32_t species, int64_t* n);
+
 /*
  * Transient FIFO of DrainAndCommitSecondaries (RreaSecondaryCommit.cpp:9-638,
  * residual advance RreaNewbornAdvance.cpp:20-996).  Every pending secondary
@@ -303,7 +328,8 @@ void rrea_gpu_last_error(const rrea_gpu_ctx* ctx, char* buf, size_t size);
  *   stage:  host tile -> HBM (prev_* are ignored)
  *   step:   one outer step on the resident tile, no host copies; its ordered
  *           secondaries join the resident drain queue
- *   fetch:  HBM -> host tile (r, z, theta, ux, uy, uz, id)
+ *   fetch:  HBM -> host tile (r, z, theta, ux, uy, uz, w, id, cpu; tile->n must equal
+ *           rrea_gpu_resident_count, which committed survivors and compaction change)
  */
 rrea_gpu_status rrea_gpu_stage_electrons(rrea_gpu_ctx* ctx, const rrea_gpu_tile* tile);
 rrea_gpu_status rrea_gpu_step_electrons_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s,

@@ -295,3 +295,45 @@ def _collect(cfg, t):
 def as_config(cfg):
     """Copies any rrea_gpu_config-layout ctypes structure into the oracle's."""
     return RreaGpuConfig.from_buffer_copy(bytes(cfg))
+
+
+ME_C2_EV = 510998.95000   # I/RreaConstants.H:9
+C_M_PER_S = 299792458.0   # I/RreaConstants.H:10
+
+
+def commit_survivors(recs, species, first_id):
+    """Particles the overlay creates from surviving FIFO records of one
+    species (RreaWarpXCoupling::CommitLocalParticleBatch,
+    O/RreaCouplingSources.cpp:240-330; the captured pre-push state of
+    append_rrea_previous_position_attributes, :28-100): records with weight
+    <= 0 (photons also with energy <= 0) are dropped; e-/e+ get the proper
+    velocity of their kinetic energy (RreaElectronProperVelocityFromKineticEv,
+    I/RreaSeedSchedule.H:31-43) along the direction, photons the momentum E
+    along it; ids continue from first_id in FIFO order.  Returns a dict of
+    columns r, z, theta, ux, uy, uz, w, id."""
+    recs = recs[recs["species"] == species]
+    keep = recs["weight"] > 0.0
+    if species == 2:
+        keep &= recs["energy_eV"] > 0.0
+    r = recs[keep]
+    d = np.stack([r["dir_x"], r["dir_y"], r["dir_z"]], axis=1)
+    norm = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+    e = r["energy_eV"]
+    u = d.copy()
+    with np.errstate(divide="ignore", invalid="ignore"):
+        if species == 2:
+            scale = np.where(norm > 0.0, e / np.where(norm > 0.0, norm, 1.0), e)
+            u = d * scale[:, None]
+            u[:, 2] = np.where(norm > 0.0, d[:, 2] * scale, e)
+        else:
+            gamma = 1.0 + e / ME_C2_EV
+            umag = C_M_PER_S * np.sqrt(np.maximum(gamma * gamma - 1.0, 0.0))
+            pos = e > 0.0
+            nz = norm > 0.0
+            for k in range(3):
+                scaled = np.where(nz, umag * d[:, k] / np.where(nz, norm, 1.0), umag if k == 2 else 0.0)
+                u[:, k] = np.where(pos, scaled, d[:, k])
+    return {"r": np.hypot(r["x"], r["y"]), "z": r["z"].copy(), "theta": np.arctan2(r["y"], r["x"]),
+            "ux": u[:, 0], "uy": u[:, 1], "uz": u[:, 2], "w": r["weight"].copy(),
+            "id": first_id + np.arange(len(r), dtype=np.int64)}
+

@@ -18,6 +18,7 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -163,6 +164,15 @@ struct rrea_gpu_ctx {
     rrea_gpu_secondary* d_surv = nullptr;
     int64_t surv_cap = 0;
     int64_t n_surv = 0;
+    // resident commit: the next id per species and the rank scratch of the
+    // survivor list; the spare tile the compaction writes into
+    int64_t next_id[kSpecies] = {1, 1, 1};
+    uint32_t* d_commit_flags = nullptr;
+    int64_t* d_commit_offsets = nullptr;
+    int64_t* d_commit_scan = nullptr;
+    int64_t commit_cap = 0;
+    SpeciesTile spare;
+    bool spare_ready = false;
     uint32_t* d_alive = nullptr;
     uint64_t* d_child_lineage = nullptr;
     unsigned long long* d_invalid = nullptr;
@@ -406,6 +416,14 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     dfree(ctx->d_transported);
     dfree(ctx->d_fifo);
     dfree(ctx->d_surv);
+    dfree(ctx->d_commit_flags);
+    dfree(ctx->d_commit_offsets);
+    dfree(ctx->d_commit_scan);
+    if (ctx->spare_ready) {
+        for (int f = 0; f < kTileDoubles; ++f) dfree(ctx->spare.d[f]);
+        dfree(ctx->spare.id);
+        dfree(ctx->spare.cpu);
+    }
     dfree(ctx->d_alive);
     dfree(ctx->d_child_lineage);
     dfree(ctx->d_invalid);
@@ -870,8 +888,24 @@ rrea_gpu_status stage_species(rrea_gpu_ctx* ctx, int species, const rrea_gpu_til
     if (!ctx || !tile || tile->n < 0) return RREA_GPU_ERR_ARGUMENT;
     rrea_gpu_status const s = stage_tile(ctx, species, tile);
     if (s != RREA_GPU_OK) return s;
+    // ids committed later continue after the largest staged id
+    int64_t top = 0;
+    for (int64_t i = 0; i < tile->n; ++i) {
+        int64_t const a = tile->id[i] < 0 ? -tile->id[i] : tile->id[i];
+        top = a > top ? a : top;
+    }
+    ctx->next_id[species] = top + 1;
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RREA_GPU_OK;
+}
+
+rrea_dev::TileColumns columns(SpeciesTile const& st)
+{
+    rrea_dev::TileColumns t{};
+    for (int f = 0; f < kTileDoubles; ++f) t.d[f] = st.d[f];
+    t.id = st.id;
+    t.cpu = st.cpu;
+    return t;
 }
 
 rrea_gpu_status fetch_species(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile* tile)
@@ -879,6 +913,17 @@ rrea_gpu_status fetch_species(rrea_gpu_ctx* ctx, int species, rrea_gpu_tile* til
     if (!ctx || !tile || tile->n != ctx->tiles[species].n) return RREA_GPU_ERR_ARGUMENT;
     rrea_gpu_status const s = unstage_tile(ctx, species, tile);
     if (s != RREA_GPU_OK) return s;
+    // a resident tile also gains particles (committed survivors): their
+    // weights and cpu words come back too
+    SpeciesTile const& st = ctx->tiles[species];
+    if (tile->n && tile->w) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(tile->w, st.d[6], static_cast<size_t>(tile->n) * sizeof(double),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (tile->n && tile->cpu) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(tile->cpu, st.cpu, static_cast<size_t>(tile->n) * sizeof(int32_t),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RREA_GPU_OK;
 }
@@ -1308,6 +1353,115 @@ rrea_gpu_status rrea_gpu_fetch_survivors(rrea_gpu_ctx* ctx, rrea_gpu_secondary* 
                                        cudaMemcpyDeviceToHost, ctx->stream));
     }
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_commit_survivors_resident(rrea_gpu_ctx* ctx, int64_t* committed)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    int64_t added[kSpecies] = {0, 0, 0};
+    int64_t const n = ctx->n_surv;
+    if (n > 0) {
+        if (n > ctx->commit_cap) {
+            dfree(ctx->d_commit_flags);
+            dfree(ctx->d_commit_offsets);
+            dfree(ctx->d_commit_scan);
+            ctx->d_commit_flags = nullptr;
+            ctx->d_commit_offsets = nullptr;
+            ctx->d_commit_scan = nullptr;
+            ctx->commit_cap = 0;
+            int64_t const cap = n + n / 2 + 1024;
+            if (dalloc(&ctx->d_commit_flags, static_cast<size_t>(cap)) != cudaSuccess
+                || dalloc(&ctx->d_commit_offsets, static_cast<size_t>(cap)) != cudaSuccess
+                || dalloc(&ctx->d_commit_scan, static_cast<size_t>(rrea_launch::scan_scratch_elems(cap))) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(ctx, RREA_GPU_ERR_CUDA, "commit scratch allocation failed");
+            }
+            ctx->commit_cap = cap;
+        }
+        // all three species are ranked before any tile changes, so a full
+        // tile leaves every tile as it was
+        for (int species = 0; species < kSpecies; ++species) {
+            RREA_CUDA(ctx, rrea_launch::commit_rank(ctx->d_surv, n, species, ctx->d_commit_flags,
+                                                    ctx->d_commit_offsets, ctx->d_commit_scan, ctx->stream));
+            int64_t last_off = 0;
+            uint32_t last_flag = 0;
+            RREA_CUDA(ctx, cudaMemcpyAsync(&last_off, ctx->d_commit_offsets + n - 1, sizeof(last_off),
+                                           cudaMemcpyDeviceToHost, ctx->stream));
+            RREA_CUDA(ctx, cudaMemcpyAsync(&last_flag, ctx->d_commit_flags + n - 1, sizeof(last_flag),
+                                           cudaMemcpyDeviceToHost, ctx->stream));
+            RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            added[species] = last_off + last_flag;
+            if (ctx->tiles[species].n + added[species] > ctx->capacity) {
+                return fail(ctx, RREA_GPU_ERR_CAPACITY, "committed survivors exceed the resident tile capacity");
+            }
+        }
+        for (int species = 0; species < kSpecies; ++species) {
+            if (added[species] == 0) continue;
+            SpeciesTile& st = ctx->tiles[species];
+            RREA_CUDA(ctx, rrea_launch::commit_rank(ctx->d_surv, n, species, ctx->d_commit_flags,
+                                                    ctx->d_commit_offsets, ctx->d_commit_scan, ctx->stream));
+            RREA_CUDA(ctx, rrea_launch::commit_scatter(ctx->d_surv, n, species, ctx->d_commit_offsets, columns(st),
+                                                       st.n, ctx->next_id[species], ctx->stream));
+            st.n += added[species];
+            ctx->next_id[species] += added[species];
+        }
+        RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        ctx->n_surv = 0;
+    }
+    if (committed) {
+        for (int species = 0; species < kSpecies; ++species) committed[species] = added[species];
+    }
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_compact_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t* n_live)
+{
+    if (!ctx || species < 0 || species >= kSpecies) return RREA_GPU_ERR_ARGUMENT;
+    SpeciesTile& st = ctx->tiles[species];
+    int64_t const n = st.n;
+    if (n > 0) {
+        if (!ctx->spare_ready) {
+            size_t const cap = static_cast<size_t>(ctx->capacity);
+            bool ok = true;
+            for (int f = 0; f < kTileDoubles; ++f) ok = ok && dalloc(&ctx->spare.d[f], cap) == cudaSuccess;
+            ok = ok && dalloc(&ctx->spare.id, cap) == cudaSuccess && dalloc(&ctx->spare.cpu, cap) == cudaSuccess;
+            if (!ok) {
+                cudaGetLastError();
+                for (int f = 0; f < kTileDoubles; ++f) {
+                    dfree(ctx->spare.d[f]);
+                    ctx->spare.d[f] = nullptr;
+                }
+                dfree(ctx->spare.id);
+                dfree(ctx->spare.cpu);
+                ctx->spare.id = nullptr;
+                ctx->spare.cpu = nullptr;
+                return fail(ctx, RREA_GPU_ERR_CUDA, "compaction tile allocation failed");
+            }
+            ctx->spare_ready = true;
+        }
+        RREA_CUDA(ctx, rrea_launch::compact_tile(columns(st), n, ctx->d_sec_per_parent, ctx->d_offsets,
+                                                 ctx->d_scan_scratch, columns(ctx->spare), ctx->stream));
+        int64_t last_off = 0;
+        uint32_t last_flag = 0;
+        RREA_CUDA(ctx, cudaMemcpyAsync(&last_off, ctx->d_offsets + n - 1, sizeof(last_off), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(&last_flag, ctx->d_sec_per_parent + n - 1, sizeof(last_flag),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+        RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int f = 0; f < kTileDoubles; ++f) std::swap(st.d[f], ctx->spare.d[f]);
+        std::swap(st.id, ctx->spare.id);
+        std::swap(st.cpu, ctx->spare.cpu);
+        st.n = last_off + last_flag;
+    }
+    if (n_live) *n_live = st.n;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_resident_count(rrea_gpu_ctx* ctx, int32_t species, int64_t* n)
+{
+    if (!ctx || !n || species < 0 || species >= kSpecies) return RREA_GPU_ERR_ARGUMENT;
+    *n = ctx->tiles[species].n;
     return RREA_GPU_OK;
 }
 

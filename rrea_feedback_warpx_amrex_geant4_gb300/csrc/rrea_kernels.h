@@ -9,6 +9,15 @@ namespace rrea_dev {
 struct ElectronArgs;
 struct SegmentRec;
 struct NetGrid;
+
+// Device columns of one species tile: r, z, theta, ux, uy, uz, w and the
+// captured prev_r, prev_z, prev_theta, prev_ux, prev_uy, prev_uz; id; cpu.
+constexpr int kTileColumns = 13;
+struct TileColumns {
+    double* d[kTileColumns];
+    int64_t* id;
+    int32_t* cpu;
+};
 }
 
 namespace rrea_launch {
@@ -65,5 +74,18 @@ cudaError_t exclusive_scan_counts(const uint32_t* counts, int64_t n, int64_t* of
 cudaError_t order_secondaries(const uint32_t* counts, int64_t n, int64_t* offsets, int64_t* block_scratch,
                               const rrea_gpu_secondary* unordered, int64_t count, rrea_gpu_secondary* ordered,
                               cudaStream_t stream);
+
+// Resident commit of the drain survivors of one species (rrea_commit.cu):
+// commit_rank flags the records the species accepts and scans them
+// (offsets[n-1] + flags[n-1] accepted); commit_scatter writes them to tile
+// rows base + rank with ids first_id + rank.
+cudaError_t commit_rank(const rrea_gpu_secondary* surv, int64_t n, int species, uint32_t* flags, int64_t* offsets,
+                        int64_t* scan_scratch, cudaStream_t stream);
+cudaError_t commit_scatter(const rrea_gpu_secondary* surv, int64_t n, int species, const int64_t* offsets,
+                           rrea_dev::TileColumns const& tile, int64_t base, int64_t first_id, cudaStream_t stream);
+// Stable compaction of the valid (id > 0) rows of src into dst; offsets[n-1]
+// + flags[n-1] is the new row count.
+cudaError_t compact_tile(rrea_dev::TileColumns const& src, int64_t n, uint32_t* flags, int64_t* offsets,
+                         int64_t* scan_scratch, rrea_dev::TileColumns const& dst, cudaStream_t stream);
 
 }  // namespace rrea_launch

@@ -77,6 +77,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_drain_resident", "rrea_gpu_fetch_survivors", "rrea_gpu_pending_secondaries",
     "rrea_gpu_last_drain_stats", "rrea_gpu_kernel_launches", "rrea_gpu_current_device",
     "rrea_gpu_advance_field_from_current", "rrea_gpu_selftest_math", "rrea_gpu_set_density_profile",
+    "rrea_gpu_commit_survivors_resident", "rrea_gpu_compact_resident", "rrea_gpu_resident_count",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -131,6 +132,9 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_drain_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_double, _i64p]
     lib.rrea_gpu_fetch_survivors.argtypes = [vp, vp, ctypes.c_int64, _i64p]
     lib.rrea_gpu_pending_secondaries.argtypes = [vp, _i64p, ctypes.c_int32]
+    lib.rrea_gpu_commit_survivors_resident.argtypes = [vp, _i64p]
+    lib.rrea_gpu_compact_resident.argtypes = [vp, ctypes.c_int32, _i64p]
+    lib.rrea_gpu_resident_count.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
     lib.rrea_gpu_kernel_launches.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
     lib.rrea_gpu_current_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
@@ -343,6 +347,25 @@ class RreaGpuContext:
         self._check(self.lib.rrea_gpu_fetch_survivors(self.handle, ctypes.c_void_p(out.ctypes.data) if n else None,
                                                       int(n), ctypes.byref(got)))
         return out[: got.value]
+
+    def commit_survivors_resident(self):
+        """Appends the last resident drain's survivors to the resident tiles;
+        returns the counts committed per species (electron, positron, photon)."""
+        out = np.zeros(3, dtype=np.int64)
+        self._check(self.lib.rrea_gpu_commit_survivors_resident(
+            self.handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return out
+
+    def compact_resident(self, species):
+        """Drops the invalid particles of a resident tile (order kept); returns its new size."""
+        n = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_compact_resident(self.handle, species, ctypes.byref(n)))
+        return n.value
+
+    def resident_count(self, species):
+        n = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_resident_count(self.handle, species, ctypes.byref(n)))
+        return n.value
 
     def pending_secondaries(self, discard=False):
         n = ctypes.c_int64()
