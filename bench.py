@@ -181,10 +181,28 @@ def cpu_populations(n, seed):
     return arr, pho, pos
 
 
+def commit_and_compact(tile, survivors, species):
+    """DrainAndCommitSecondaries' commit on a host tile: the species'
+    survivors become particles (oracle.commit_survivors), and the particles
+    that ended the step leave the tile."""
+    from oracle import oracle
+
+    keep = tile["id"] > 0
+    add = oracle.commit_survivors(survivors, species, int(np.abs(tile["id"]).max(initial=0)) + 1)
+    out = {}
+    for k, v in tile.items():
+        if k == "cpu":
+            extra = np.zeros(len(add["id"]), dtype=v.dtype)
+        else:
+            extra = add[k[5:] if k.startswith("prev_") else k]
+        out[k] = np.ascontiguousarray(np.concatenate([v[keep], extra.astype(v.dtype)]))
+    return out
+
+
 def cpu_oracle_rate(cfg, field, n, seed, steps=1):
     """Oracle particle-steps/s of the whole kinetic step (three phases, FIFO
-    drain, net-chord current, field update) on n electrons, the photon and
-    positron fractions, for `steps` steps (all threads)."""
+    drain and commit, net-chord current, field update) on n electrons, the
+    photon and positron fractions, for `steps` steps (all threads)."""
     from oracle import oracle
     from rrea_feedback_warpx_amrex_geant4_gb300 import DEFAULT_TABLES, workloads
 
@@ -204,6 +222,9 @@ def cpu_oracle_rate(cfg, field, n, seed, steps=1):
         op = oracle.positron_step(cfg, fld, s, DT_S, pos)
         pending = np.concatenate([oe["secondaries"], og["secondaries"], op["secondaries"]])
         od = oracle.drain(cfg, fld, s, DT_S, pending)
+        arr = commit_and_compact(arr, od["survivors"], 0)
+        pos = commit_and_compact(pos, od["survivors"], 1)
+        pho = commit_and_compact(pho, od["survivors"], 2)
         rows = np.concatenate([oracle.segment_rows(r) for r in (oe, op, od)])
         cur = oracle.deposit_segments(cfg, DT_S, rows)
         fld["er"], fld["ez"], fld["bt"] = oracle.advance_maxwell(cfg.nr, cfg.nz, dr, dz, DT_S, FIELD_SUBSTEPS,
@@ -243,7 +264,7 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * total_t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (scale-up case seed distribution)",
-        "config": {"workload": f"{CASE}: whole kinetic step (three phases, newborn FIFO, net-chord current, "
+        "config": {"workload": f"{CASE}: whole kinetic step (three phases, newborn FIFO and commit, net-chord current, "
                                f"field update), {population_text(args.cpu_sample)} per timed step",
                    "grid": "256x2048", "dt_s": DT_S, "field_substeps": FIELD_SUBSTEPS},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
@@ -276,7 +297,8 @@ def run_gb300(args, rank, world, local):
     n_g = int(n * PHOTON_FRACTION)
     n_p = max(1, int(n * POSITRON_FRACTION))
     cfg = workloads.make_config(gpu, CASE)
-    ctx = gpu.RreaGpuContext(cfg, n)
+    # room for the committed survivors: the populations grow from step to step
+    ctx = gpu.RreaGpuContext(cfg, n + n // 4)
     ctx.load_tables(DEFAULT_TABLES)
     field = workloads.make_field(CASE)
     ctx.set_field(**field)
@@ -302,10 +324,16 @@ def run_gb300(args, rank, world, local):
         tp, _, kmp = ctx.last_step_stats()
         ctx.drain_resident(step, DT_S)  # newborn residual legs of every secondary
         items, surv = ctx.last_drain_stats()
+        # DrainAndCommitSecondaries' commit: survivors become resident particles,
+        # and the particles that ended this step leave the tiles
+        committed = ctx.commit_survivors_resident()
+        for species in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON, gpu.SPECIES_PHOTON):
+            ctx.compact_resident(species)
         # Maxwell TM-RZ with this step's J, summed over the ranks' shards
         distributed.exchange_current_and_advance(ctx, dist, DT_S, FIELD_SUBSTEPS)
         return {"te": te, "tg": tg, "tp": tp, "kme": kme, "kmg": kmg, "kmp": kmp,
-                "secondaries": ne + ng + npos, "fifo_items": items, "survivors": surv}
+                "secondaries": ne + ng + npos, "fifo_items": items, "survivors": surv,
+                "committed": int(committed.sum())}
 
     step = 0
     for _ in range(args.warmup):
@@ -316,7 +344,8 @@ def run_gb300(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     total_ms = 0.0
-    acc = {k: 0 for k in ("te", "tg", "tp", "kme", "kmg", "kmp", "secondaries", "fifo_items", "survivors")}
+    acc = {k: 0 for k in ("te", "tg", "tp", "kme", "kmg", "kmp", "secondaries", "fifo_items", "survivors",
+                          "committed")}
     launches = 0
     for _ in range(args.steps):
         flush.zero_()  # L2 flush between timed steps (256 MiB write)
@@ -414,7 +443,7 @@ def run_gb300(args, rank, world, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (scale-up case seed distribution, seeded numpy PRNG)",
             "config": {"workload": f"{CASE}: whole kinetic step (electron, photon, positron phases, newborn "
-                                   f"FIFO, net-chord current, field update) over resident populations of "
+                                   f"FIFO and commit, net-chord current, field update) over resident populations of "
                                    f"{population_text(n)} per GPU (256x2048 cells over 200 m x 2 km, initial "
                                    f"uniform E_z = -500 kV/m), dt 0.5 ns",
                        "grid": "256x2048",
@@ -441,6 +470,7 @@ def run_gb300(args, rank, world, local):
                        "secondaries_per_step": acc["secondaries"] / args.steps,
                        "fifo_items_per_step": acc["fifo_items"] / args.steps,
                        "survivors_per_step": acc["survivors"] / args.steps,
+                       "committed_per_step": acc["committed"] / args.steps,
                        "transport_kernels_ms_per_step": (kernel_ms_e + kernel_ms_g + kernel_ms_p) / args.steps},
             "cpu_baseline": {"value": cpu_rate, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                              "sample": f"{population_text(cpu_n)} x {args.cpu_baseline_steps} steps of the same "

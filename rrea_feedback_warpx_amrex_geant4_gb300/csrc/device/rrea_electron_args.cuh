@@ -86,7 +86,9 @@ struct ElectronArgs {
 // Visits every particle index of [0, n) once.  With a work counter each warp
 // claims the next 32 indices when it is done with its previous ones, so a
 // slow particle does not hold up the ones a static assignment would have
-// queued behind it on the same thread.
+// queued behind it on the same thread.  The claims run from the end of the
+// tile: committed survivors, appended there, are mostly slow low-energy
+// particles, and starting with them keeps them out of the launch's tail.
 template <class F>
 __device__ __forceinline__ void for_each_particle(int64_t n, unsigned long long* work, F&& f)
 {
@@ -97,8 +99,8 @@ __device__ __forceinline__ void for_each_particle(int64_t n, unsigned long long*
             if (lane == 0) base = atomicAdd(work, 32ULL);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base >= static_cast<unsigned long long>(n)) break;
-            int64_t const ip = static_cast<int64_t>(base) + lane;
-            if (ip < n) f(ip);
+            int64_t const k = static_cast<int64_t>(base) + lane;
+            if (k < n) f(n - 1 - k);
         }
     } else {
         for (int64_t ip = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; ip < n;
