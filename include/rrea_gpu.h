@@ -457,6 +457,56 @@ rrea_gpu_status rrea_gpu_order_secondaries_noalloc(const uint32_t* d_counts, int
                                                    int64_t n_secondaries, rrea_gpu_secondary* d_ordered,
                                                    void* stream, char* message, size_t message_size);
 
+/*
+ * Seed schedule input adapter (RreaSeedSchedule, I/RreaSeedSchedule.H and
+ * S/RreaSeedSchedule.cpp): the CSV event list the overlay injects as native
+ * seeds.  Columns case_id, time_s, x_m, y_m, z_m, r_m, kinetic_energy_eV,
+ * ux, uy, uz, weight_real_electrons (required) and macro_index, species_id
+ * (optional: the CSV line number, electron).  Host-only calls except the
+ * injection; no GPU is needed to load, list or validate a schedule.
+ *   load:     the rows of case_id (all rows when empty or null), sorted by
+ *             (time_s, macro_index) (S/RreaSeedSchedule.cpp:75-144);
+ *             RREA_GPU_ERR_ARGUMENT on a missing file or column, a duplicate
+ *             column or a non-numeric cell (message via
+ *             rrea_gpu_seed_schedule_last_error).
+ *   validate: RreaSeedSchedule::ValidateProduction (:146-244) against the
+ *             certified charged energy range and the half-open RZ domain.
+ *   events:   copies the sorted events out (capacity >= size).
+ *   inject:   RreaWarpXCoupling::InjectScheduledSeeds
+ *             (O/RreaCouplingSources.cpp:96-215) on the resident tiles: events
+ *             from the schedule's cursor with time in [time_s, time_s + dt_s)
+ *             are appended to the resident electron or positron tile, earlier
+ *             (stale) events are skipped, the cursor advances past both; the
+ *             momentum is RreaNormalizeSeedMomentum (I/RreaSeedSchedule.H:55-71),
+ *             the weight weight_real_electrons, the captured state the
+ *             particle's own, ids continue the species' counter.
+ *             injected[2] (may be null): electrons, positrons added.
+ *             RREA_GPU_ERR_CAPACITY, with nothing appended, past the capacity.
+ */
+typedef struct rrea_gpu_seed_schedule rrea_gpu_seed_schedule;
+typedef struct {
+    int32_t macro_index;
+    int32_t species_id;   /* 1 electron, 2 positron */
+    double time_s;
+    double x_m, y_m, z_m, r_m;
+    double kinetic_energy_eV;
+    double ux, uy, uz;    /* direction hint (|u| < 1e6) or proper velocity (m/s) */
+    double weight;        /* weight_real_electrons */
+} rrea_gpu_seed_event;
+
+rrea_gpu_status rrea_gpu_seed_schedule_load(const char* path, const char* case_id, rrea_gpu_seed_schedule** out);
+rrea_gpu_status rrea_gpu_seed_schedule_free(rrea_gpu_seed_schedule* schedule);
+rrea_gpu_status rrea_gpu_seed_schedule_size(const rrea_gpu_seed_schedule* schedule, int64_t* n);
+rrea_gpu_status rrea_gpu_seed_schedule_events(const rrea_gpu_seed_schedule* schedule, rrea_gpu_seed_event* out,
+                                              int64_t capacity, int64_t* n);
+rrea_gpu_status rrea_gpu_seed_schedule_validate(const rrea_gpu_seed_schedule* schedule, double electron_min_energy_eV,
+                                                double electron_max_energy_eV, double radial_min_m,
+                                                double radial_max_m, double axial_min_m, double axial_max_m);
+/* The message of the last failed seed-schedule call on this thread. */
+void rrea_gpu_seed_schedule_last_error(char* buf, size_t size);
+rrea_gpu_status rrea_gpu_inject_seeds_resident(rrea_gpu_ctx* ctx, rrea_gpu_seed_schedule* schedule, double time_s,
+                                               double dt_s, int64_t* injected);
+
 #ifdef __cplusplus
 }
 #endif

@@ -540,6 +540,83 @@ int main(int argc, char** argv)
             write_f8("ref_altitude_profile_nodes", 2, nodes);
             write_f8("ref_altitude_profile", 2, rows);
         }
+        // ---- seed schedule: S/RreaSeedSchedule.cpp (Load, ValidateProduction)
+        // and I/RreaSeedSchedule.H (momentum normalisation, injection window)
+        // on a synthetic CSV kept beside the fixtures
+        {
+            std::string const csv = g_outdir + "/ref_seed_schedule_input.csv";
+            {
+                std::ofstream f(csv);
+                f << "case_id, macro_index,species_id,time_s,x_m,y_m,z_m,r_m,kinetic_energy_eV,ux,uy,uz,"
+                     "weight_real_electrons\n";
+                char line[1024];
+                for (int i = 0; i < 240; ++i) {
+                    char const* cid = (i % 11 == 5) ? "X9" : (i % 37 == 7 ? "BAD" : "C2");
+                    bool const quoted = (i % 13 == 3);
+                    double const rr = 1000.0 * std::sqrt(g.uni()), ph = 6.283185307179586 * g.uni();
+                    double const x = rr * std::cos(ph), y = rr * std::sin(ph), z = 8000.0 * g.uni();
+                    double r = std::hypot(x, y);
+                    if (std::string(cid) == "BAD") r *= 1.001;  // inconsistent radius
+                    // E^-1.5 on 1-100 MeV
+                    double const u0 = g.uni();
+                    double const k = 1.0e6 / std::pow(1.0 - u0 * (1.0 - std::pow(100.0, -0.5)), 2.0);
+                    double const ct = std::sqrt(g.uni()), st = std::sqrt(1.0 - ct * ct), az = 6.283185307179586 * g.uni();
+                    double dx = st * std::cos(az), dy = st * std::sin(az), dz = -ct;
+                    if (i % 5 == 2) {  // a proper velocity instead of a direction hint
+                        double const um = rrea::RreaElectronProperVelocityFromKineticEv(k);
+                        dx *= um; dy *= um; dz *= um;
+                    } else if (i % 7 == 4) {  // a hint of another magnitude
+                        dx *= 3.5; dy *= 3.5; dz *= 3.5;
+                    }
+                    double const t = (i % 17 == 0) ? 1.0e-6 : 2.0e-6 * g.uni();
+                    char macro[32] = "";
+                    if (i % 6 != 1) std::snprintf(macro, sizeof macro, "%d", 10000 + 3 * ((i * 7919) % 240));
+                    char spec[8] = "";
+                    if (i % 4 == 1) std::snprintf(spec, sizeof spec, "2");
+                    else if (i % 4 == 2) std::snprintf(spec, sizeof spec, "1");
+                    std::snprintf(line, sizeof line, "%s%s%s, %s ,%s,%.17g,%.17g,%.17g,%.17g,%.17g,%.17g,%.17g,%.17g,%.17g,%.17g\n",
+                                  quoted ? "\"" : "", cid, quoted ? "\"" : "", macro, spec, t, x, y, z, r, k, dx, dy,
+                                  dz, 1.0e3 + 1.0e5 * g.uni());
+                    f << line;
+                    if (i % 50 == 9) f << "   \n";  // blank lines are skipped
+                }
+            }
+            std::vector<double> rows, windows, checks;
+            rrea::RreaSeedSchedule all;
+            all.Load(csv, "");
+            checks.push_back(static_cast<double>(all.Size()));
+            rrea::RreaSeedSchedule sched;
+            sched.Load(csv, "C2");
+            double const win[3][2] = {{0.0, 5.0e-7}, {1.0e-6, 1.0005e-6}, {1.5e-6, 2.5e-6}};
+            for (std::size_t i = 0; i < sched.Size(); ++i) {
+                auto const& e = sched.Event(i);
+                auto const m = rrea::RreaNormalizeSeedMomentum(e.ux, e.uy, e.uz, e.kinetic_energy_eV);
+                rows.insert(rows.end(), {static_cast<double>(e.macro_index), static_cast<double>(e.species_id),
+                                         e.time_s, e.x_m, e.y_m, e.z_m, e.r_m, e.kinetic_energy_eV, e.ux, e.uy, e.uz,
+                                         e.weight_real_electrons, m.ux, m.uy, m.uz});
+                for (auto const& w : win) {
+                    auto const c = rrea::RreaSeedEventWindowClass(e.time_s, w[0], w[1]);
+                    windows.push_back(c == rrea::RreaSeedWindowClass::SkipStale ? -1.0
+                                      : c == rrea::RreaSeedWindowClass::Inject ? 0.0 : 1.0);
+                }
+            }
+            auto validates = [&](rrea::RreaSeedSchedule const& s) {
+                try {
+                    s.ValidateProduction(1.0e4, 1.0e9, 0.0, 1000.0, 0.0, 8000.0);
+                    return 1.0;
+                } catch (std::exception const&) {
+                    return 0.0;
+                }
+            };
+            checks.push_back(validates(sched));
+            rrea::RreaSeedSchedule bad;
+            bad.Load(csv, "BAD");
+            checks.push_back(static_cast<double>(bad.Size()));
+            checks.push_back(validates(bad));
+            write_f8("ref_seed_schedule_events", 15, rows);
+            write_f8("ref_seed_schedule_windows", 3, windows);
+            write_f8("ref_seed_schedule_checks", 1, checks);
+        }
         std::printf("golden fixtures written to %s\n", g_outdir.c_str());
     } catch (std::exception const& e) {
         std::fprintf(stderr, "ref_golden failed: %s\n", e.what());

@@ -7,6 +7,7 @@
 #include "../../include/rrea_gpu.h"
 
 #include "device/rrea_electron_args.cuh"
+#include "host/seed_schedule.hpp"
 #include "host/table_set.hpp"
 #include "rrea_kernels.h"
 
@@ -38,6 +39,14 @@ struct SpeciesTile {
     int32_t* cpu = nullptr;
     int64_t n = 0;
 };
+
+thread_local std::string g_seed_error;
+
+rrea_gpu_status seed_fail(int code, std::string const& msg)
+{
+    g_seed_error = msg;
+    return static_cast<rrea_gpu_status>(code);
+}
 
 // Dense slots for the transient roots (the RNG key and species of the live
 // particle whose streams a FIFO item draws from): an open-addressing table
@@ -94,6 +103,10 @@ private:
 };
 
 }  // namespace
+
+struct rrea_gpu_seed_schedule {
+    rrea_host::SeedSchedule s;
+};
 
 struct rrea_gpu_ctx {
     rrea_gpu_config cfg{};
@@ -1455,6 +1468,130 @@ rrea_gpu_status rrea_gpu_compact_resident(rrea_gpu_ctx* ctx, int32_t species, in
         st.n = last_off + last_flag;
     }
     if (n_live) *n_live = st.n;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_seed_schedule_load(const char* path, const char* case_id, rrea_gpu_seed_schedule** out)
+{
+    if (!path || !out) return seed_fail(RREA_GPU_ERR_ARGUMENT, "null path or output");
+    *out = nullptr;
+    auto* s = new (std::nothrow) rrea_gpu_seed_schedule();
+    if (!s) return seed_fail(RREA_GPU_ERR_ARGUMENT, "out of host memory");
+    try {
+        s->s.load(path, case_id ? case_id : "");
+    } catch (rrea_host::SeedScheduleError const& e) {
+        delete s;
+        return seed_fail(e.code, e.what());
+    } catch (std::exception const& e) {
+        delete s;
+        return seed_fail(RREA_GPU_ERR_ARGUMENT, e.what());
+    }
+    *out = s;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_seed_schedule_free(rrea_gpu_seed_schedule* schedule)
+{
+    delete schedule;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_seed_schedule_size(const rrea_gpu_seed_schedule* schedule, int64_t* n)
+{
+    if (!schedule || !n) return RREA_GPU_ERR_ARGUMENT;
+    *n = static_cast<int64_t>(schedule->s.events().size());
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_seed_schedule_events(const rrea_gpu_seed_schedule* schedule, rrea_gpu_seed_event* out,
+                                              int64_t capacity, int64_t* n)
+{
+    if (!schedule || capacity < 0) return RREA_GPU_ERR_ARGUMENT;
+    std::vector<rrea_gpu_seed_event> const& ev = schedule->s.events();
+    if (n) *n = static_cast<int64_t>(ev.size());
+    if (static_cast<int64_t>(ev.size()) > capacity) return seed_fail(RREA_GPU_ERR_CAPACITY, "event buffer too small");
+    if (!ev.empty()) {
+        if (!out) return RREA_GPU_ERR_ARGUMENT;
+        std::memcpy(out, ev.data(), ev.size() * sizeof(rrea_gpu_seed_event));
+    }
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_seed_schedule_validate(const rrea_gpu_seed_schedule* schedule, double e_min, double e_max,
+                                                double r_min, double r_max, double z_min, double z_max)
+{
+    if (!schedule) return RREA_GPU_ERR_ARGUMENT;
+    try {
+        schedule->s.validate(e_min, e_max, r_min, r_max, z_min, z_max);
+    } catch (rrea_host::SeedScheduleError const& e) {
+        return seed_fail(e.code, e.what());
+    }
+    return RREA_GPU_OK;
+}
+
+void rrea_gpu_seed_schedule_last_error(char* buf, size_t size)
+{
+    if (!buf || size == 0) return;
+    std::strncpy(buf, g_seed_error.c_str(), size - 1);
+    buf[size - 1] = '\0';
+}
+
+rrea_gpu_status rrea_gpu_inject_seeds_resident(rrea_gpu_ctx* ctx, rrea_gpu_seed_schedule* schedule, double time_s,
+                                               double dt_s, int64_t* injected)
+{
+    if (!ctx || !schedule) return RREA_GPU_ERR_ARGUMENT;
+    if (injected) injected[0] = injected[1] = 0;
+    rrea_host::SeedSchedule& sched = schedule->s;
+    std::vector<rrea_gpu_seed_event> const& events = sched.events();
+    if (!(dt_s > 0.0) || events.empty()) return RREA_GPU_OK;
+    // O/RreaCouplingSources.cpp:124-151: stale events are skipped, the window's
+    // events injected, the first later event stops the walk
+    double const end = time_s + dt_s;
+    std::vector<rrea_gpu_seed_event const*> pick[2];
+    int64_t c = sched.cursor;
+    for (; c < static_cast<int64_t>(events.size()); ++c) {
+        rrea_gpu_seed_event const& e = events[static_cast<size_t>(c)];
+        int const cls = rrea_host::seed_window_class(e.time_s, time_s, end);
+        if (cls < 0) continue;
+        if (cls > 0) break;
+        pick[e.species_id == rrea_host::kSeedPositron ? 1 : 0].push_back(&e);
+    }
+    int const tile_of[2] = {RREA_SPECIES_ELECTRON, RREA_SPECIES_POSITRON};
+    for (int k = 0; k < 2; ++k) {
+        if (ctx->tiles[tile_of[k]].n + static_cast<int64_t>(pick[k].size()) > ctx->capacity) {
+            return fail(ctx, RREA_GPU_ERR_CAPACITY, "injected seeds exceed the resident tile capacity");
+        }
+    }
+    for (int k = 0; k < 2; ++k) {
+        size_t const m = pick[k].size();
+        if (m == 0) continue;
+        SpeciesTile& st = ctx->tiles[tile_of[k]];
+        // columns as append_rrea_previous_position_attributes builds them
+        // (O/RreaCouplingSources.cpp:28-100): captured state = own state
+        std::vector<double> col(static_cast<size_t>(kTileDoubles) * m);
+        std::vector<int64_t> ids(m);
+        for (size_t i = 0; i < m; ++i) {
+            rrea_gpu_seed_event const& e = *pick[k][i];
+            double u[3];
+            rrea_host::normalize_seed_momentum(e.ux, e.uy, e.uz, e.kinetic_energy_eV, u);
+            double const r = std::hypot(e.x_m, e.y_m), th = std::atan2(e.y_m, e.x_m);
+            double const v[kTileDoubles] = {r, e.z_m, th, u[0], u[1], u[2], e.weight, r, e.z_m, th, u[0], u[1], u[2]};
+            for (int f = 0; f < kTileDoubles; ++f) col[static_cast<size_t>(f) * m + i] = v[f];
+            ids[i] = ctx->next_id[tile_of[k]] + static_cast<int64_t>(i);
+        }
+        for (int f = 0; f < kTileDoubles; ++f) {
+            RREA_CUDA(ctx, cudaMemcpyAsync(st.d[f] + st.n, col.data() + static_cast<size_t>(f) * m,
+                                           m * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        }
+        RREA_CUDA(ctx, cudaMemcpyAsync(st.id + st.n, ids.data(), m * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+        RREA_CUDA(ctx, cudaMemsetAsync(st.cpu + st.n, 0, m * sizeof(int32_t), ctx->stream));
+        RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        st.n += static_cast<int64_t>(m);
+        ctx->next_id[tile_of[k]] += static_cast<int64_t>(m);
+        if (injected) injected[k] = static_cast<int64_t>(m);
+    }
+    sched.cursor = c;
     return RREA_GPU_OK;
 }
 

@@ -55,6 +55,12 @@ class RreaGpuTile(ctypes.Structure):
 TILE_FIELDS = ("r", "z", "theta", "ux", "uy", "uz", "w",
                "prev_r", "prev_z", "prev_theta", "prev_ux", "prev_uy", "prev_uz")
 
+SEED_EVENT_DTYPE = np.dtype([  # rrea_gpu_seed_event
+    ("macro_index", "<i4"), ("species_id", "<i4"), ("time_s", "<f8"), ("x_m", "<f8"), ("y_m", "<f8"),
+    ("z_m", "<f8"), ("r_m", "<f8"), ("kinetic_energy_eV", "<f8"), ("ux", "<f8"), ("uy", "<f8"), ("uz", "<f8"),
+    ("weight", "<f8"),
+])
+
 SECONDARY_DTYPE = np.dtype([
     ("species", "<i4"), ("process", "<i4"), ("root_species", "<i4"), ("pad", "<i4"),
     ("parent_index", "<i8"), ("root_key", "<u8"), ("lineage", "<u8"),
@@ -78,6 +84,9 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_last_drain_stats", "rrea_gpu_kernel_launches", "rrea_gpu_current_device",
     "rrea_gpu_advance_field_from_current", "rrea_gpu_selftest_math", "rrea_gpu_set_density_profile",
     "rrea_gpu_commit_survivors_resident", "rrea_gpu_compact_resident", "rrea_gpu_resident_count",
+    "rrea_gpu_seed_schedule_load", "rrea_gpu_seed_schedule_free", "rrea_gpu_seed_schedule_size",
+    "rrea_gpu_seed_schedule_events", "rrea_gpu_seed_schedule_validate", "rrea_gpu_seed_schedule_last_error",
+    "rrea_gpu_inject_seeds_resident",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -133,6 +142,14 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_fetch_survivors.argtypes = [vp, vp, ctypes.c_int64, _i64p]
     lib.rrea_gpu_pending_secondaries.argtypes = [vp, _i64p, ctypes.c_int32]
     lib.rrea_gpu_commit_survivors_resident.argtypes = [vp, _i64p]
+    lib.rrea_gpu_seed_schedule_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)]
+    lib.rrea_gpu_seed_schedule_free.argtypes = [vp]
+    lib.rrea_gpu_seed_schedule_size.argtypes = [vp, _i64p]
+    lib.rrea_gpu_seed_schedule_events.argtypes = [vp, vp, ctypes.c_int64, _i64p]
+    lib.rrea_gpu_seed_schedule_validate.argtypes = [vp] + [ctypes.c_double] * 6
+    lib.rrea_gpu_seed_schedule_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    lib.rrea_gpu_seed_schedule_last_error.restype = None
+    lib.rrea_gpu_inject_seeds_resident.argtypes = [vp, vp, ctypes.c_double, ctypes.c_double, _i64p]
     lib.rrea_gpu_compact_resident.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_resident_count.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
@@ -193,6 +210,53 @@ def tile_struct(arrays):
     t.id = arrays["id"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
     t.cpu = arrays["cpu"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
     return t
+
+
+class SeedSchedule:
+    """The seed schedule CSV adapter (RreaSeedSchedule): load, list, validate.
+    Host-only; RreaGpuContext.inject_seeds appends its windows to the
+    resident tiles."""
+
+    def __init__(self, path, case_id=""):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        self._check(self.lib.rrea_gpu_seed_schedule_load(str(path).encode(), case_id.encode(), ctypes.byref(h)))
+        self.handle = h
+
+    def _check(self, status):
+        if status != 0:
+            buf = ctypes.create_string_buffer(1024)
+            self.lib.rrea_gpu_seed_schedule_last_error(buf, 1024)
+            raise RreaGpuError(status, buf.value.decode())
+
+    def __len__(self):
+        n = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_seed_schedule_size(self.handle, ctypes.byref(n)))
+        return n.value
+
+    def events(self):
+        out = np.zeros(len(self), dtype=SEED_EVENT_DTYPE)
+        n = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_seed_schedule_events(self.handle, ctypes.c_void_p(out.ctypes.data) if len(out)
+                                                           else None, len(out), ctypes.byref(n)))
+        return out
+
+    def validate(self, electron_min_energy_eV, electron_max_energy_eV, radial_min_m, radial_max_m, axial_min_m,
+                 axial_max_m):
+        self._check(self.lib.rrea_gpu_seed_schedule_validate(self.handle, electron_min_energy_eV,
+                                                             electron_max_energy_eV, radial_min_m, radial_max_m,
+                                                             axial_min_m, axial_max_m))
+
+    def close(self):
+        if self.handle:
+            self.lib.rrea_gpu_seed_schedule_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class RreaGpuContext:
@@ -361,6 +425,14 @@ class RreaGpuContext:
         n = ctypes.c_int64()
         self._check(self.lib.rrea_gpu_compact_resident(self.handle, species, ctypes.byref(n)))
         return n.value
+
+    def inject_seeds(self, schedule, time_s, dt_s):
+        """InjectScheduledSeeds on the resident tiles: the schedule's events in
+        [time_s, time_s + dt_s); returns (electrons, positrons) added."""
+        out = np.zeros(2, dtype=np.int64)
+        self._check(self.lib.rrea_gpu_inject_seeds_resident(self.handle, schedule.handle, float(time_s), float(dt_s),
+                                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return out
 
     def resident_count(self, species):
         n = ctypes.c_int64()

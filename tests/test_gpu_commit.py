@@ -127,3 +127,49 @@ def test_commit_beyond_capacity_changes_no_tile(mods):
     assert e.value.status == 8  # RREA_GPU_ERR_CAPACITY
     assert [ctx.resident_count(s) for s, _ in SPECIES] == sizes
     ctx.close()
+
+
+def test_scheduled_seeds_join_the_resident_tiles(mods):
+    """InjectScheduledSeeds on the resident tiles: the window's events are
+    appended per species with the reference's normalised momentum
+    (tests/golden/ref_seed_schedule_events.npy, computed by the reference);
+    stale events are skipped, later ones wait for their window."""
+    import os
+
+    from conftest import GOLDEN
+
+    gpu, workloads, oracle = mods
+    ref = np.load(os.path.join(GOLDEN, "ref_seed_schedule_events.npy"))
+    windows = np.load(os.path.join(GOLDEN, "ref_seed_schedule_windows.npy"))
+    sched = gpu.SeedSchedule(os.path.join(GOLDEN, "ref_seed_schedule_input.csv"), "C2")
+    cfg = workloads.make_config(gpu, "scaleup_c1")
+    ctx = gpu.RreaGpuContext(cfg, 4096)
+    ctx.load_tables(TABLES)
+    ctx.set_field(**workloads.make_field("scaleup_c1"))
+    e = workloads.make_electrons("scaleup_c1", 64, seed=90)
+    ctx.stage_electrons(e)
+    ctx.stage_positrons(workloads.make_electrons("scaleup_c1", 8, seed=91))
+    injected_total = np.zeros(2, dtype=np.int64)
+    # windows as the golden: [0, 5e-7), then (skipping) [1e-6, 1.0005e-6), then [1.5e-6, 2.5e-6)
+    for w, (t0, t1) in enumerate(((0.0, 5.0e-7), (1.0e-6, 1.0005e-6), (1.5e-6, 2.5e-6))):
+        n0 = [ctx.resident_count(0), ctx.resident_count(1)]
+        got = ctx.inject_seeds(sched, t0, t1 - t0)
+        sel = windows[:, w] == 0
+        want = ref[sel]
+        assert got[0] == int((want[:, 1] == 1).sum()) and got[1] == int((want[:, 1] == 2).sum()), w
+        injected_total += got
+        for k, species in ((0, 0), (1, 1)):
+            rows = want[want[:, 1] == k + 1]
+            t = _fetch(gpu, ctx, workloads, species)
+            new = {c: v[n0[k]:] for c, v in t.items()}
+            np.testing.assert_array_equal(new["z"], rows[:, 5])
+            np.testing.assert_array_equal(new["w"], rows[:, 11])
+            np.testing.assert_array_equal(new["ux"], rows[:, 12])
+            np.testing.assert_array_equal(new["uy"], rows[:, 13])
+            np.testing.assert_array_equal(new["uz"], rows[:, 14])
+            np.testing.assert_array_equal(new["r"], np.hypot(rows[:, 3], rows[:, 4]))
+            np.testing.assert_array_equal(new["theta"], np.arctan2(rows[:, 4], rows[:, 3]))
+            assert (np.diff(new["id"]) == 1).all() and (new["id"] > 0).all()
+    # events between the windows were stale when their window passed
+    assert injected_total.sum() == int((windows == 0).sum())
+    ctx.close()
