@@ -81,6 +81,9 @@ struct ElectronArgs {
     // over one chunk of a tile passes offset arrays and the chunk's start,
     // so parent indices and failure indices stay tile indices
     int64_t index_base;
+    // optional scheduling order of the tile indices (null: the end of the
+    // tile first); it changes which thread visits a particle, never a result
+    const uint32_t* __restrict__ order;
 };
 
 // Visits every particle index of [0, n) once.  With a work counter each warp
@@ -90,7 +93,8 @@ struct ElectronArgs {
 // tile: committed survivors, appended there, are mostly slow low-energy
 // particles, and starting with them keeps them out of the launch's tail.
 template <class F>
-__device__ __forceinline__ void for_each_particle(int64_t n, unsigned long long* work, F&& f)
+__device__ __forceinline__ void for_each_particle(int64_t n, unsigned long long* work, F&& f,
+                                                  const uint32_t* __restrict__ order = nullptr)
 {
     if (work) {
         int const lane = threadIdx.x & 31;
@@ -100,7 +104,7 @@ __device__ __forceinline__ void for_each_particle(int64_t n, unsigned long long*
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base >= static_cast<unsigned long long>(n)) break;
             int64_t const k = static_cast<int64_t>(base) + lane;
-            if (k < n) f(n - 1 - k);
+            if (k < n) f(order ? static_cast<int64_t>(__ldg(order + k)) : n - 1 - k);
         }
     } else {
         for (int64_t ip = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; ip < n;

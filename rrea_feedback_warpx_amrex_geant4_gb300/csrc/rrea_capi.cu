@@ -25,6 +25,8 @@
 namespace {
 
 constexpr int kTileDoubles = 13;
+// resident charged tiles at least this large are scheduled by momentum
+constexpr int64_t kScheduleMinParticles = 1 << 16;
 constexpr int kSpecies = 3;
 // Chunks of a drop-in phase call whose upload overlaps the compute of the
 // chunks before it, and the tile size from which that pays.
@@ -187,6 +189,7 @@ struct rrea_gpu_ctx {
     SpeciesTile spare;
     bool spare_ready = false;
     uint32_t* d_alive = nullptr;
+    uint32_t* d_cost_scratch = nullptr;  // histogram and cursors of the scheduling order
     uint64_t* d_child_lineage = nullptr;
     unsigned long long* d_invalid = nullptr;
     // roots of the initial FIFO items (16 B each) on the device and in pinned
@@ -379,6 +382,7 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         && dalloc(&ctx->d_diag_disp, n) == cudaSuccess && dalloc(&ctx->d_status, 1) == cudaSuccess
         && dalloc(&ctx->d_fail_index, 1) == cudaSuccess && dalloc(&ctx->d_transported, 1) == cudaSuccess
         && dalloc(&ctx->d_alive, n) == cudaSuccess && dalloc(&ctx->d_child_lineage, nsec) == cudaSuccess
+        && dalloc(&ctx->d_cost_scratch, static_cast<size_t>(rrea_launch::cost_order_scratch_elems())) == cudaSuccess
         && dalloc(&ctx->d_invalid, 1) == cudaSuccess && dalloc(&ctx->d_work, kPhaseChunks) == cudaSuccess
         && cudaEventCreate(&ctx->ev_start) == cudaSuccess && cudaEventCreate(&ctx->ev_stop) == cudaSuccess;
     if (!ok) return bail(RREA_GPU_ERR_CUDA);
@@ -438,6 +442,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
         dfree(ctx->spare.cpu);
     }
     dfree(ctx->d_alive);
+    dfree(ctx->d_cost_scratch);
     dfree(ctx->d_child_lineage);
     dfree(ctx->d_invalid);
     dfree(ctx->d_roots);
@@ -766,6 +771,13 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
         (host && species != RREA_SPECIES_PHOTON && a.n >= kPipelineMinParticles) ? kPhaseChunks : 1;
 #ifndef RREA_STATIC_SCHEDULE
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long) * chunks, ctx->stream));
+    // a resident charged tile is visited in its scheduling order (lowest
+    // |u| first): warps then hold particles of similar substep counts
+    if (!host && species != RREA_SPECIES_PHOTON && a.n >= kScheduleMinParticles) {
+        RREA_CUDA(ctx, rrea_launch::cost_order(a.ux, a.uy, a.uz, a.id, a.n, ctx->d_cost_scratch, ctx->d_alive,
+                                               ctx->num_sms * 4, ctx->stream));
+        a.order = ctx->d_alive;
+    }
 #endif
     RREA_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
     if (host && chunks == 1) {

@@ -102,6 +102,62 @@ __global__ void compact_tile_kernel(TileColumns src, int64_t n, const int64_t* _
     }
 }
 
+// Scheduling order of a charged tile: particles binned by |u|^2 in
+// quarter octaves (the exponent and top two mantissa bits of the double, an
+// integer key), lowest momentum first.  Slow low-energy particles (many
+// GS-limited substeps) then start first and share warps with particles of
+// a similar substep count; ended particles (id <= 0) go last.  The order
+// only schedules: every result is indexed by the particle's tile index.
+constexpr int kCostBins = 128;
+
+__device__ __forceinline__ int cost_bin(double ux, double uy, double uz, int64_t id)
+{
+    if (id <= 0) return kCostBins - 1;
+    unsigned long long const b = static_cast<unsigned long long>(__double_as_longlong(ux * ux + uy * uy + uz * uz));
+    // |u|^2 of 10 keV is 2^51.7 (m/s)^2 and of 20 MeV 2^66.9: bins from 2^48
+    int const key = static_cast<int>(b >> 50) - 4 * (1023 + 48);
+    return key < 0 ? 0 : (key > kCostBins - 2 ? kCostBins - 2 : key);
+}
+
+__global__ void cost_hist_kernel(const double* __restrict__ ux, const double* __restrict__ uy,
+                                 const double* __restrict__ uz, const int64_t* __restrict__ id, int64_t n,
+                                 uint32_t* __restrict__ hist)
+{
+    __shared__ uint32_t local[kCostBins];
+    for (int i = threadIdx.x; i < kCostBins; i += blockDim.x) local[i] = 0;
+    __syncthreads();
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        atomicAdd(&local[cost_bin(ux[i], uy[i], uz[i], id[i])], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kCostBins; i += blockDim.x) {
+        if (local[i]) atomicAdd(&hist[i], local[i]);
+    }
+}
+
+// hist[0, kCostBins) counts, cursor[kCostBins, 2 kCostBins) zeroed slots
+__global__ void cost_scatter_kernel(const double* __restrict__ ux, const double* __restrict__ uy,
+                                    const double* __restrict__ uz, const int64_t* __restrict__ id, int64_t n,
+                                    uint32_t* __restrict__ hist, uint32_t* __restrict__ order)
+{
+    __shared__ uint32_t start[kCostBins];
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int i = 0; i < kCostBins; ++i) {
+            start[i] = acc;
+            acc += hist[i];
+        }
+    }
+    __syncthreads();
+    uint32_t* cursor = hist + kCostBins;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int const bin = cost_bin(ux[i], uy[i], uz[i], id[i]);
+        order[start[bin] + atomicAdd(&cursor[bin], 1u)] = static_cast<uint32_t>(i);
+    }
+}
+
 unsigned grid_for(int64_t n, int threads)
 {
     int64_t const b = (n + threads - 1) / threads;
@@ -142,6 +198,21 @@ cudaError_t compact_tile(rrea_dev::TileColumns const& src, int64_t n, uint32_t* 
     if (e != cudaSuccess) return e;
     note_launch();
     rrea_dev::compact_tile_kernel<<<rrea_dev::grid_for(n, 256), 256, 0, stream>>>(src, n, offsets, dst);
+    return cudaGetLastError();
+}
+
+int cost_order_scratch_elems() { return 2 * rrea_dev::kCostBins; }
+
+cudaError_t cost_order(const double* ux, const double* uy, const double* uz, const int64_t* id, int64_t n,
+                       uint32_t* scratch, uint32_t* order, int blocks, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    cudaError_t const e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * 2 * rrea_dev::kCostBins, stream);
+    if (e != cudaSuccess) return e;
+    note_launch();
+    rrea_dev::cost_hist_kernel<<<blocks, 256, 0, stream>>>(ux, uy, uz, id, n, scratch);
+    note_launch();
+    rrea_dev::cost_scatter_kernel<<<blocks, 256, 0, stream>>>(ux, uy, uz, id, n, scratch, order);
     return cudaGetLastError();
 }
 

@@ -77,7 +77,7 @@ __device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
         if (A.diag_disposition) A.diag_disposition[ip] = disp;
         if (A.diag_subcycles) A.diag_subcycles[ip] = sub;
         if (A.diag_events) A.diag_events[ip] = ev;
-    });
+    }, A.order);
     // warp-aggregated count of transported particles
     unsigned int const warp_total = __reduce_add_sync(0xffffffffu, moved);
     if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(A.transported, static_cast<unsigned long long>(warp_total));

@@ -88,4 +88,10 @@ cudaError_t commit_scatter(const rrea_gpu_secondary* surv, int64_t n, int specie
 cudaError_t compact_tile(rrea_dev::TileColumns const& src, int64_t n, uint32_t* flags, int64_t* offsets,
                          int64_t* scan_scratch, rrea_dev::TileColumns const& dst, cudaStream_t stream);
 
+// Scheduling order of a charged tile (lowest |u| first, ended particles
+// last) into order[0, n); scratch holds cost_order_scratch_elems() words.
+int cost_order_scratch_elems();
+cudaError_t cost_order(const double* ux, const double* uy, const double* uz, const int64_t* id, int64_t n,
+                       uint32_t* scratch, uint32_t* order, int blocks, cudaStream_t stream);
+
 }  // namespace rrea_launch
