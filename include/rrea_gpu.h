@@ -264,7 +264,8 @@ rrea_gpu_status rrea_gpu_commit_survivors_resident(rrea_gpu_ctx* ctx, int64_t* c
  * null) receives the new tile size. */
 rrea_gpu_status rrea_gpu_compact_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t* n_live);
 
-/* Number of particles (valid or not) in a resident species tile. */
+/* Number of particles (valid or not) in a resident species tile.  NO COUNTERPART IN THE
+ * REFERENCE (WarpX containers know their own size). */
 rrea_gpu_status rrea_gpu_resident_count(rrea_gpu_ctx* ctx, int32_t species, int64_t* n);
 
 /*
