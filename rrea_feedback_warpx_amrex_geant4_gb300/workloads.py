@@ -34,7 +34,33 @@ CASES = {
     # hemisphere, uniform in a 5 m x 10 m disk; 500 kV/m; 256x2048 cells over
     # 200 m x 2 km
     "scaleup_c1": dict(r_hi=200.0, z_hi=2000.0, nr=256, nz=2048, field_v_per_m=5.0e5, seeds=100_000),
+    # profiled atmosphere: 512x4096 cells over r 0-1 km and altitudes 6-14 km
+    # (z = 0 at 6 km); density and ambient E_z from profiled_atmosphere()
+    "profiled_c2": dict(r_hi=1000.0, z_hi=8000.0, nr=512, nz=4096, field_v_per_m=0.0, seeds=0),
 }
+
+SEA_LEVEL_DENSITY = 1.225       # kg/m^3
+SCALE_HEIGHT_M = 7200.0
+THRESHOLD_V_PER_M = 2.84e5      # RREA threshold field at sea-level density
+
+
+def profiled_atmosphere(case="profiled_c2", altitude_at_z0_m=6000.0, peak_factor=1.3):
+    """The profiled-atmosphere workload: density 1.225 exp(-h / 7.2 km) kg/m^3
+    on 50 m altitude nodes over 6-14 km (for rrea_gpu_set_density_profile),
+    and an ambient E_z piecewise linear in altitude, 0 at 8 and 12 km and
+    peak_factor x the local runaway threshold (284 kV/m x n/n0) at 10 km,
+    negative so that it drives electrons toward +z.  Returns (altitudes,
+    densities, altitude of z = 0, field vectors for set_field)."""
+    p = CASES[case]
+    nr, nz = p["nr"], p["nz"]
+    alt = np.arange(6000.0, 14000.0 + 25.0, 50.0)
+    dens = SEA_LEVEL_DENSITY * np.exp(-alt / SCALE_HEIGHT_M)
+    h = altitude_at_z0_m + np.arange(nz + 1) * (p["z_hi"] / nz)
+    peak = peak_factor * THRESHOLD_V_PER_M * np.exp(-10000.0 / SCALE_HEIGHT_M)
+    ez = np.interp(h, [8000.0, 10000.0, 12000.0], [0.0, peak, 0.0], left=0.0, right=0.0)
+    field = dict(er=np.zeros((nr + 1) * nz), ez=np.zeros(nr * (nz + 1)), bt=np.zeros((nr + 1) * (nz + 1)),
+                 amb_er=np.zeros((nr + 1) * nz), amb_ez=np.ascontiguousarray(np.repeat(-ez, nr)))
+    return alt, dens, altitude_at_z0_m, field
 
 
 def make_config(gpu_module, case, low_energy_cutoff_eV=1.0e4, rng_seed=1, max_subcycles=8192):
