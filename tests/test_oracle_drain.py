@@ -92,3 +92,33 @@ def test_fifo_rejects_invalid_birth_payload(mods):
             oracle.drain(cfg, field, 0, 3.0e-8, bad)
         assert err.value.code == 1
     assert len(oracle.drain(cfg, field, 0, 3.0e-8, pending[:0])["survivors"]) == 0
+
+
+def test_commit_restatement_follows_the_overlay_rules():
+    """oracle.commit_survivors (the checker of the resident commit) follows
+    CommitLocalParticleBatch's rules (O/RreaCouplingSources.cpp:240-330):
+    weight <= 0 dropped, photons with E <= 0 dropped, e-/e+ proper velocity
+    along the direction, a zero direction giving (0, 0, u), photon momentum
+    E along the direction, ids in FIFO order."""
+    from oracle import oracle
+
+    recs = np.zeros(6, dtype=oracle.SECONDARY_DTYPE)
+    recs["species"] = [0, 0, 0, 2, 2, 1]
+    recs["weight"] = [1.0, 0.0, 2.0, 3.0, 4.0, 5.0]
+    recs["energy_eV"] = [1.0e6, 1.0e6, 2.0e6, 5.0e5, 0.0, 3.0e6]
+    recs["x"], recs["y"], recs["z"] = [3.0, 1, 0, 1, 1, -2.0], [4.0, 1, 2.0, 1, 1, 0.0], [5.0, 1, 6, 7, 8, 9]
+    recs["dir_x"], recs["dir_y"], recs["dir_z"] = [0.0, 1, 0, 0.6, 1, 0], [0.0, 0, 0, 0.8, 0, 0], [0.0, 0, 2.0, 0, 0, -1.0]
+    e = oracle.commit_survivors(recs, 0, 100)
+    np.testing.assert_array_equal(e["id"], [100, 101])
+    np.testing.assert_array_equal(e["w"], [1.0, 2.0])
+    np.testing.assert_allclose(e["r"], [5.0, 2.0])
+    np.testing.assert_allclose(e["theta"], [np.arctan2(4.0, 3.0), np.pi / 2])
+    u1 = oracle.C_M_PER_S * np.sqrt((1.0 + 1.0e6 / oracle.ME_C2_EV) ** 2 - 1.0)
+    u2 = oracle.C_M_PER_S * np.sqrt((1.0 + 2.0e6 / oracle.ME_C2_EV) ** 2 - 1.0)
+    np.testing.assert_allclose(np.stack([e["ux"], e["uy"], e["uz"]], axis=1), [[0.0, 0.0, u1], [0.0, 0.0, u2]])
+    g = oracle.commit_survivors(recs, 2, 7)
+    np.testing.assert_array_equal(g["id"], [7])
+    np.testing.assert_allclose([g["ux"][0], g["uy"][0], g["uz"][0]], [3.0e5, 4.0e5, 0.0])
+    p = oracle.commit_survivors(recs, 1, 1)
+    np.testing.assert_allclose(p["theta"], [np.pi])
+    assert p["uz"][0] < 0.0 and p["ux"][0] == 0.0
