@@ -67,3 +67,21 @@ def test_malformed_schedules(gpu, tmp_path, text, needle):
     assert needle in str(err.value)
     with pytest.raises(gpu.RreaGpuError):
         gpu.SeedSchedule(tmp_path / "missing.csv", "")
+
+
+def test_host_calls_refuse_bad_arguments(gpu):
+    """The host-only seed-schedule entry points return status codes for
+    null handles and short buffers (no GPU involved)."""
+    import ctypes
+
+    lib = gpu.load_library()
+    n = ctypes.c_int64()
+    assert lib.rrea_gpu_seed_schedule_size(None, ctypes.byref(n)) == 1
+    assert lib.rrea_gpu_seed_schedule_validate(None, 1.0e4, 1.0e9, 0.0, 1.0, 0.0, 1.0) == 1
+    assert lib.rrea_gpu_seed_schedule_free(None) == 0
+    out = ctypes.c_void_p()
+    assert lib.rrea_gpu_seed_schedule_load(None, b"", ctypes.byref(out)) == 1
+    s = gpu.SeedSchedule(CSV, "C2")
+    buf = np.zeros(3, dtype=gpu.SEED_EVENT_DTYPE)
+    assert lib.rrea_gpu_seed_schedule_events(s.handle, ctypes.c_void_p(buf.ctypes.data), 3, ctypes.byref(n)) == 8
+    assert n.value == len(s)
