@@ -264,6 +264,26 @@ rrea_gpu_status rrea_gpu_commit_survivors_resident(rrea_gpu_ctx* ctx, int64_t* c
  * null) receives the new tile size. */
 rrea_gpu_status rrea_gpu_compact_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t* n_live);
 
+/* Charge-exact stochastic thinning of order-1 CIC support groups, the
+ * per-support primitive of the population control's adaptive_resample_v1
+ * (RreaThinCicWeights and RreaCicResampleRemovalCapacity,
+ * I/RreaCicConservingResample.H:46-351).  Group g is rows
+ * [offsets[g], offsets[g+1]) (at most 64) of fraction_r, fraction_z (the
+ * order-1 CIC fractions in [0, 1]) and weight (updated in place: removed
+ * particles get weight 0; the four cell charges are kept to round-off and
+ * each weight keeps its expectation).  At most max_removals[g] particles
+ * are removed, with uniforms u_k = (mix64(keys[g] + k) >> 11 + 1/2) 2^-53
+ * (mix64 = RreaCicMix64).  Per group: removed, draws, valid (0 where the
+ * reference's primitive reports an invalid plan, weights then partly
+ * updated as there) and the removal capacity (live particles minus the rank
+ * of their CIC columns).  The global planning of the transaction (which
+ * supports thin and by how much) is not part of this call.  Host pointers;
+ * groups of more than 64 particles give RREA_GPU_ERR_ARGUMENT. */
+rrea_gpu_status rrea_gpu_thin_cic_groups(rrea_gpu_ctx* ctx, const double* fraction_r, const double* fraction_z,
+                                        double* weight, const int64_t* offsets, int64_t n_groups,
+                                        const int64_t* max_removals, const uint64_t* keys, int64_t* removed,
+                                        int64_t* draws, int32_t* valid, int64_t* capacity);
+
 /* Number of particles (valid or not) in a resident species tile.  NO COUNTERPART IN THE
  * REFERENCE (WarpX containers know their own size). */
 rrea_gpu_status rrea_gpu_resident_count(rrea_gpu_ctx* ctx, int32_t species, int64_t* n);

@@ -9,6 +9,7 @@
 #include "RreaParticleInteraction.H"
 #include "RreaRng.H"
 #include "rrea/RreaAltitudeProfile.H"
+#include "rrea/RreaCicConservingResample.H"
 #include "rrea/RreaInteractionTables.H"
 #include "rrea/RreaConstants.H"
 #include "rrea/RreaMaxwellTMRZ.H"
@@ -616,6 +617,51 @@ int main(int argc, char** argv)
             write_f8("ref_seed_schedule_events", 15, rows);
             write_f8("ref_seed_schedule_windows", 3, windows);
             write_f8("ref_seed_schedule_checks", 1, checks);
+        }
+        // ---- CIC-conserving thinning: I/RreaCicConservingResample.H
+        // (RreaThinCicWeights, RreaCicResampleRemovalCapacity) on seeded
+        // support groups, with the counter draw u_k = (mix(key + k) >> 11 + 0.5) 2^-53
+        {
+            std::vector<double> parts, groups;
+            for (int gi = 0; gi < 400; ++gi) {
+                int const n = 2 + static_cast<int>(g.next() % 11);
+                std::vector<rrea::RreaCicResampleParticle> ps(static_cast<std::size_t>(n));
+                for (int i = 0; i < n; ++i) {
+                    auto& q = ps[static_cast<std::size_t>(i)];
+                    uint64_t const kind = g.next() % 16;
+                    q.fraction_r = g.uni();
+                    q.fraction_z = g.uni();
+                    if (kind == 0 && i > 0) {  // same support point as the previous particle
+                        q.fraction_r = ps[static_cast<std::size_t>(i - 1)].fraction_r;
+                        q.fraction_z = ps[static_cast<std::size_t>(i - 1)].fraction_z;
+                    } else if (kind == 1) {
+                        q.fraction_r = (g.next() & 1) ? 1.0 : 0.0;
+                    } else if (kind == 2) {
+                        q.fraction_z = (g.next() & 1) ? 1.0 : 0.0;
+                    }
+                    q.weight = (kind == 3) ? 0.0 : 0.1 + 9.9 * g.uni();
+                }
+                std::size_t const capacity = rrea::RreaCicResampleRemovalCapacity(ps);
+                std::size_t const max_removals = (gi % 3 == 0) ? static_cast<std::size_t>(n)
+                                                                 : static_cast<std::size_t>(g.next() % (n + 1));
+                uint64_t const key = g.next();
+                std::vector<rrea::RreaCicResampleParticle> out = ps;
+                auto const res = rrea::RreaThinCicWeights(out, max_removals, [&](std::size_t k) {
+                    return (static_cast<double>(rrea::RreaCicMix64(key + k) >> 11) + 0.5) * 0x1.0p-53;
+                });
+                for (int i = 0; i < n; ++i) {
+                    auto const& a = ps[static_cast<std::size_t>(i)];
+                    parts.insert(parts.end(), {static_cast<double>(gi), a.fraction_r, a.fraction_z, a.weight,
+                                               out[static_cast<std::size_t>(i)].weight});
+                }
+                uint64_t const key_hi = key >> 32, key_lo = key & 0xffffffffULL;
+                groups.insert(groups.end(), {static_cast<double>(n), static_cast<double>(max_removals),
+                                             static_cast<double>(key_hi), static_cast<double>(key_lo),
+                                             static_cast<double>(res.removed), static_cast<double>(res.draws),
+                                             res.valid ? 1.0 : 0.0, static_cast<double>(capacity)});
+            }
+            write_f8("ref_cic_thin_particles", 5, parts);
+            write_f8("ref_cic_thin_groups", 8, groups);
         }
         std::printf("golden fixtures written to %s\n", g_outdir.c_str());
     } catch (std::exception const& e) {

@@ -23,6 +23,7 @@ SOURCES = [
     os.path.join(CSRC, "rrea_photon_kernels.cu"),
     os.path.join(CSRC, "rrea_noalloc.cu"),
     os.path.join(CSRC, "rrea_commit.cu"),
+    os.path.join(CSRC, "rrea_resample.cu"),
     os.path.join(CSRC, "rrea_newborn.cu"),
     os.path.join(CSRC, "rrea_deposit.cu"),
     os.path.join(CSRC, "rrea_field.cu"),

@@ -7,6 +7,7 @@
 #include "../../include/rrea_gpu.h"
 
 #include "device/rrea_electron_args.cuh"
+#include "device/rrea_resample.cuh"
 #include "host/seed_schedule.hpp"
 #include "host/table_set.hpp"
 #include "rrea_kernels.h"
@@ -1604,6 +1605,73 @@ rrea_gpu_status rrea_gpu_inject_seeds_resident(rrea_gpu_ctx* ctx, rrea_gpu_seed_
         if (injected) injected[k] = static_cast<int64_t>(m);
     }
     sched.cursor = c;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_thin_cic_groups(rrea_gpu_ctx* ctx, const double* fraction_r, const double* fraction_z,
+                                        double* weight, const int64_t* offsets, int64_t n_groups,
+                                        const int64_t* max_removals, const uint64_t* keys, int64_t* removed,
+                                        int64_t* draws, int32_t* valid, int64_t* capacity)
+{
+    if (!ctx || n_groups < 0 || (n_groups > 0 && (!fraction_r || !fraction_z || !weight || !offsets ||
+                                                  !max_removals || !keys || !removed || !draws || !valid ||
+                                                  !capacity))) {
+        return RREA_GPU_ERR_ARGUMENT;
+    }
+    if (n_groups == 0) return RREA_GPU_OK;
+    if (offsets[0] != 0) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "group offsets must start at 0");
+    for (int64_t g = 0; g < n_groups; ++g) {
+        int64_t const size = offsets[g + 1] - offsets[g];
+        if (size < 0 || size > rrea_dev::kCicMaxGroup) {
+            return fail(ctx, RREA_GPU_ERR_ARGUMENT, "a CIC group holds 0 to 64 particles");
+        }
+    }
+    int64_t const n = offsets[n_groups];
+    size_t const bn = static_cast<size_t>(n) * sizeof(double), bg = static_cast<size_t>(n_groups);
+    double *d_fr = nullptr, *d_fz = nullptr, *d_w = nullptr;
+    int64_t *d_off = nullptr, *d_max = nullptr, *d_rem = nullptr, *d_draw = nullptr, *d_cap = nullptr;
+    uint64_t* d_key = nullptr;
+    int32_t* d_valid = nullptr;
+    bool ok = dalloc(&d_fr, static_cast<size_t>(n) + 1) == cudaSuccess &&
+              dalloc(&d_fz, static_cast<size_t>(n) + 1) == cudaSuccess &&
+              dalloc(&d_w, static_cast<size_t>(n) + 1) == cudaSuccess && dalloc(&d_off, bg + 1) == cudaSuccess &&
+              dalloc(&d_max, bg) == cudaSuccess && dalloc(&d_key, bg) == cudaSuccess &&
+              dalloc(&d_rem, bg) == cudaSuccess && dalloc(&d_draw, bg) == cudaSuccess &&
+              dalloc(&d_valid, bg) == cudaSuccess && dalloc(&d_cap, bg) == cudaSuccess;
+    auto release = [&]() {
+        dfree(d_fr); dfree(d_fz); dfree(d_w); dfree(d_off); dfree(d_max); dfree(d_key);
+        dfree(d_rem); dfree(d_draw); dfree(d_valid); dfree(d_cap);
+    };
+    if (!ok) {
+        cudaGetLastError();
+        release();
+        return fail(ctx, RREA_GPU_ERR_CUDA, "thinning scratch allocation failed");
+    }
+    cudaError_t e = cudaSuccess;
+    auto up = [&](void* d, const void* h, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    };
+    auto down = [&](void* h, const void* d, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    };
+    up(d_fr, fraction_r, bn);
+    up(d_fz, fraction_z, bn);
+    up(d_w, weight, bn);
+    up(d_off, offsets, (bg + 1) * sizeof(int64_t));
+    up(d_max, max_removals, bg * sizeof(int64_t));
+    up(d_key, keys, bg * sizeof(uint64_t));
+    if (e == cudaSuccess) {
+        e = rrea_launch::cic_thin(d_fr, d_fz, d_w, d_off, n_groups, d_max, d_key, d_rem, d_draw, d_valid, d_cap,
+                                  ctx->stream);
+    }
+    down(weight, d_w, bn);
+    down(removed, d_rem, bg * sizeof(int64_t));
+    down(draws, d_draw, bg * sizeof(int64_t));
+    down(valid, d_valid, bg * sizeof(int32_t));
+    down(capacity, d_cap, bg * sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    release();
+    if (e != cudaSuccess) return fail(ctx, RREA_GPU_ERR_CUDA, std::string("thinning: ") + cudaGetErrorString(e));
     return RREA_GPU_OK;
 }
 

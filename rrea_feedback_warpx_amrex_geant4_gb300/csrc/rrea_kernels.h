@@ -88,6 +88,12 @@ cudaError_t commit_scatter(const rrea_gpu_secondary* surv, int64_t n, int specie
 cudaError_t compact_tile(rrea_dev::TileColumns const& src, int64_t n, uint32_t* flags, int64_t* offsets,
                          int64_t* scan_scratch, rrea_dev::TileColumns const& dst, cudaStream_t stream);
 
+// Charge-exact thinning of CIC support groups (rrea_resample.cu): group g is
+// rows [offsets[g], offsets[g+1]) of fr, fz, w (w updated in place).
+cudaError_t cic_thin(const double* fr, const double* fz, double* w, const int64_t* offsets, int64_t n_groups,
+                     const int64_t* max_removals, const uint64_t* keys, int64_t* removed, int64_t* draws,
+                     int32_t* valid, int64_t* capacity, cudaStream_t stream);
+
 // Scheduling order of a charged tile (lowest |u| first, ended particles
 // last) into order[0, n); scratch holds cost_order_scratch_elems() words.
 int cost_order_scratch_elems();

@@ -86,7 +86,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_commit_survivors_resident", "rrea_gpu_compact_resident", "rrea_gpu_resident_count",
     "rrea_gpu_seed_schedule_load", "rrea_gpu_seed_schedule_free", "rrea_gpu_seed_schedule_size",
     "rrea_gpu_seed_schedule_events", "rrea_gpu_seed_schedule_validate", "rrea_gpu_seed_schedule_last_error",
-    "rrea_gpu_inject_seeds_resident",
+    "rrea_gpu_inject_seeds_resident", "rrea_gpu_thin_cic_groups",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -150,6 +150,9 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_seed_schedule_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.rrea_gpu_seed_schedule_last_error.restype = None
     lib.rrea_gpu_inject_seeds_resident.argtypes = [vp, vp, ctypes.c_double, ctypes.c_double, _i64p]
+    lib.rrea_gpu_thin_cic_groups.argtypes = [vp, _D, _D, _D, _i64p, ctypes.c_int64, _i64p,
+                                             ctypes.POINTER(ctypes.c_uint64), _i64p, _i64p,
+                                             ctypes.POINTER(ctypes.c_int32), _i64p]
     lib.rrea_gpu_compact_resident.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_resident_count.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
@@ -433,6 +436,25 @@ class RreaGpuContext:
         self._check(self.lib.rrea_gpu_inject_seeds_resident(self.handle, schedule.handle, float(time_s), float(dt_s),
                                                             out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
         return out
+
+    def thin_cic_groups(self, fraction_r, fraction_z, weight, offsets, max_removals, keys):
+        """Charge-exact thinning of CIC support groups (rows offsets[g] to
+        offsets[g+1]); returns (weights, removed, draws, valid, capacity)."""
+        fr = np.ascontiguousarray(fraction_r, dtype=np.float64)
+        fz = np.ascontiguousarray(fraction_z, dtype=np.float64)
+        w = np.array(weight, dtype=np.float64)
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        g = off.shape[0] - 1
+        mx = np.ascontiguousarray(max_removals, dtype=np.int64)
+        k = np.ascontiguousarray(keys, dtype=np.uint64)
+        removed, draws, cap = (np.zeros(g, dtype=np.int64) for _ in range(3))
+        valid = np.zeros(g, dtype=np.int32)
+        i64 = ctypes.POINTER(ctypes.c_int64)
+        self._check(self.lib.rrea_gpu_thin_cic_groups(
+            self.handle, fr.ctypes.data_as(_D), fz.ctypes.data_as(_D), w.ctypes.data_as(_D), off.ctypes.data_as(i64),
+            g, mx.ctypes.data_as(i64), k.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), removed.ctypes.data_as(i64),
+            draws.ctypes.data_as(i64), valid.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cap.ctypes.data_as(i64)))
+        return w, removed, draws, valid, cap
 
     def resident_count(self, species):
         n = ctypes.c_int64()
