@@ -239,6 +239,26 @@ rrea_gpu_status rrea_gpu_advance_field_from_current(rrea_gpu_ctx* ctx, double dt
  * is the caller's to skip.  No context is needed for the projection.
  */
 rrea_gpu_status rrea_gpu_count_live(rrea_gpu_ctx* ctx, int32_t species, int64_t* live);
+
+/*
+ * Census of a resident species tile: the particle reductions of the
+ * overlay's reduced diagnostics (species_weight_statistics and
+ * electron_species_weight_above_energy, O/RreaCouplingDiagnostics.cpp:122-194,
+ * behind the N_kinetic_e_real, N_kinetic_e_ge_1MeV_real, N_photon_real and
+ * N_positron_real columns of rrea_reduced.csv) plus a weighted energy
+ * spectrum, reduced on the device.  Over the valid (id > 0) particles, with
+ * K = RreaKineticEnergyEvFromProperVelocity(u) for e-/e+
+ * (O/RreaParticleInteraction.H:1494-1505) and K = |u| for photons, out gets
+ *   [0] count  [1] largest weight  [2] sum w  [3] sum w^2  [4] sum w K [eV]
+ *   [5] weight with K < edges[0]  [6] weight with K >= edges[n_edges - 1]
+ *   [7 .. 7 + n_thresholds)              weight with K >= thresholds_eV[t]
+ *   [7 + n_thresholds .. + n_edges - 1)  weight with edges[b] <= K < edges[b+1]
+ * K is evaluated with round-to-nearest operations in this formula's order,
+ * so bin and threshold membership are exact; the sums are FP64 atomics.
+ * 2 <= n_edges <= 1025 (strictly increasing), 0 <= n_thresholds <= 16; host
+ * pointers. */
+rrea_gpu_status rrea_gpu_census_resident(rrea_gpu_ctx* ctx, int32_t species, const double* edges_eV, int32_t n_edges,
+                                         const double* thresholds_eV, int32_t n_thresholds, double* out);
 rrea_gpu_status rrea_gpu_population_projection(uint64_t current, uint64_t removals, uint64_t insertions,
                                                uint64_t ceiling, int32_t reject_equality, uint64_t* projected);
 
@@ -461,16 +481,20 @@ rrea_gpu_status rrea_gpu_stream(rrea_gpu_ctx* ctx, void** stream);
  * Returns RREA_GPU_ERR_CAPACITY (with a message) when n_parents exceeds
  * RREA_GPU_NOALLOC_MAX_PARENTS, RREA_GPU_ERR_ARGUMENT for negative sizes,
  * null or overlapping buffers, and RREA_GPU_ERR_INVALID_STATE when the
- * records are inconsistent with the counts (such records are skipped, no
- * out-of-range write happens).  The call blocks until the pass on `stream`
- * has finished.
+ * records are inconsistent with the counts, including two records with the
+ * same (parent_index, lineage) pair (such records are skipped, no
+ * out-of-range write happens; the output's content is then unspecified).
+ * The call blocks until the pass on `stream` has finished.
  *
- * The first call on each device looks up the scratch address once
- * (cudaGetSymbolAddress, with that device current); if stream capture is
- * used anywhere in the process, make that first call before capture starts.
- * All calls on one device share the one scratch array: calls that overlap in
- * time (from two host threads, or on two streams) race on it and must be
- * serialised by the caller.
+ * Every call looks up the scratch array's device address for the current
+ * device and context (cudaGetSymbolAddress, a host-side lookup), so the
+ * address stays right after cudaDeviceReset or under another context.  The
+ * first call on a device may load this library's device code there; if
+ * stream capture is used anywhere in the process, make one call before
+ * capture starts.  All calls on one device share the one scratch array,
+ * which keeps the last call's contents: calls that overlap in time (from two
+ * host threads, or on two streams) race on it and must be serialised by the
+ * caller.
  */
 #define RREA_GPU_NOALLOC_MAX_PARENTS (1 << 18)
 rrea_gpu_status rrea_gpu_order_secondaries_noalloc(const uint32_t* d_counts, int64_t n_parents,

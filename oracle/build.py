@@ -27,9 +27,16 @@ def build_oracle(force=False):
     return LIB
 
 
-def build_reference_golden(reference="/root/reference"):
+def reference_dir():
+    """The reference checkout: $RREA_REFERENCE_DIR, else a `reference`
+    directory beside the repository."""
+    return os.environ.get("RREA_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
+def build_reference_golden(reference=None):
     """Builds oracle/_ref/ref_golden from the reference's own sources when the
     reference checkout is present (never on the GPU host)."""
+    reference = reference or reference_dir()
     if not os.path.isdir(os.path.join(reference, "native_amrex_rrea")):
         return None
     subprocess.check_call(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={reference}"],

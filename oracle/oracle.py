@@ -292,6 +292,22 @@ def _collect(cfg, t):
             "disposition": disp, "cells": cells.reshape(5, cfg.nz, cfg.nr)}
 
 
+def default_config(**overrides):
+    """The library's default configuration (rrea_gpu_default_config, the
+    reference defaults of RreaParticleInteraction.H:1576-1596 with a 1 keV
+    tracking cut) built here without loading the GPU library, then
+    `overrides`."""
+    cfg = RreaGpuConfig(r_lo=0.0, r_hi=50.0, z_lo=0.0, z_hi=500.0, nr=32, nz=256, periodic_z=0,
+                        strict_transport_guards=1, density_ratio=1.0, low_energy_cutoff_eV=1.0e3,
+                        photon_cutoff_eV=5.0e4, max_optical_depth_per_substep=0.05, max_subcycles=256,
+                        max_gs_collisions_per_substep=32.0, gs_total_collision_cap=1024.0,
+                        max_field_impulse_fraction=0.1, field_impulse_floor_eV=1.0e4, rng_seed=0,
+                        debug_disable_hard_moller=0, reserved0=0)
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
 def as_config(cfg):
     """Copies any rrea_gpu_config-layout ctypes structure into the oracle's."""
     return RreaGpuConfig.from_buffer_copy(bytes(cfg))

@@ -1,0 +1,236 @@
+"""End-to-end avalanche runs through the resident C-ABI.
+
+One run is what the overlay's WarpX loop does to the RREA species over many
+steps (native_amrex_rrea/warpx_overlay/Source/Rrea/RreaParticleInteraction.cpp:12-62
+for the transport, RreaSecondaryCommit.cpp for the drain and commit), with
+every particle kept in HBM between steps:
+
+  per step: ResetNetChordStep, the electron, photon and positron phases on
+  the resident tiles (photons pushed straight on the device), the transient
+  FIFO of every secondary's residual leg, the commit of the survivors into
+  the tiles (new ids in FIFO order), the removal of the particles that ended
+  the step, and, with feedback on, the Maxwell TM-RZ update driven by the
+  step's net-chord current.
+
+Every `census_every` steps (and after the last) the tiles are reduced on the
+device (rrea_gpu_census_resident): counts, weights, the weight at or above
+100 keV and 1 MeV (the reduced diagnostics' N_kinetic_e_ge_100keV and
+N_kinetic_e_ge_1MeV_real probes, O/RreaCouplingDiagnostics.cpp:334-351) and
+the weighted e-/photon/e+ energy spectra.
+
+The multiplication factor of a run is the weight of electrons at or above
+1 MeV at the end over the seed weight (a runaway-electron count ratio).
+
+Run from the command line for a whole case:
+  python -m rrea_feedback_warpx_amrex_geant4_gb300.avalanche --case uniform_c0 --seeds 10000 --steps 4000
+"""
+import argparse
+import csv
+import json
+import os
+import time
+
+import numpy as np
+
+from . import DEFAULT_TABLES, gpu, workloads
+
+DT_S = 5.0e-10
+# 10 keV to 1 GeV, 20 bins per decade: the spectra the statistical checks compare
+SPECTRUM_EDGES_EV = np.logspace(4.0, 9.0, 101)
+# the reduced diagnostics' energy probes (100 keV, 1 MeV)
+THRESHOLDS_EV = np.array([1.0e5, 1.0e6])
+SPECIES_NAMES = ("electron", "positron", "photon")
+
+
+def c0_like_case(field_v_per_m=None, case="uniform_c0"):
+    """Geometry, air and field of the plain uniform-field case; a different
+    uniform field magnitude may be given."""
+    p = dict(workloads.CASES[case])
+    if field_v_per_m is not None:
+        p["field_v_per_m"] = float(field_v_per_m)
+    return p
+
+
+def make_context(case="uniform_c0", capacity=1 << 20, rng_seed=1, field_v_per_m=None, tables=DEFAULT_TABLES,
+                 blocks_per_sm=16):
+    """A context for `case` with the uniform ambient E_z of the case (or the
+    given magnitude) and a zero scattered field."""
+    cfg = workloads.make_config(gpu, case, rng_seed=rng_seed)
+    ctx = gpu.RreaGpuContext(cfg, capacity)
+    ctx.load_tables(tables)
+    field = workloads.make_field(case)
+    if field_v_per_m is not None:
+        field["amb_ez"][:] = -float(field_v_per_m)
+    ctx.set_field(**field)
+    ctx.set_launch(128, blocks_per_sm, diagnostics=False)
+    return ctx
+
+
+def census_row(ctx, step, edges=SPECTRUM_EDGES_EV, thresholds=THRESHOLDS_EV):
+    """One census of all three resident tiles."""
+    row = {"step": int(step), "time_s": step * DT_S}
+    spectra = {}
+    for sp, name in enumerate(SPECIES_NAMES):
+        c = ctx.census(sp, edges, thresholds)
+        row[f"{name}_count"] = c["count"]
+        row[f"{name}_weight"] = c["sum_w"]
+        row[f"{name}_energy_eV"] = c["sum_wk"]
+        row[f"{name}_ge_100keV"] = float(c["above"][0])
+        row[f"{name}_ge_1MeV"] = float(c["above"][1])
+        spectra[name] = c["hist"]
+    return row, spectra
+
+
+class AvalancheRun:
+    """A plain avalanche run on one GPU: seeds staged as the resident
+    electron tile, then `steps` whole kinetic steps."""
+
+    def __init__(self, ctx, electrons, photons=None, positrons=None, feedback=False, field_substeps=2):
+        self.ctx = ctx
+        self.feedback = feedback
+        self.field_substeps = field_substeps
+        empty = workloads.make_electrons("uniform_c0", 0)
+        ctx.stage_electrons(electrons)
+        ctx.stage_photons(photons if photons is not None else empty)
+        ctx.stage_positrons(positrons if positrons is not None else empty)
+        self.seed_weight = float(np.sum(electrons["w"][electrons["id"] > 0]))
+        self.step = 0
+
+    def advance(self, dt_s=DT_S):
+        """One whole kinetic step; returns the particle-steps it moved and
+        the drain's (FIFO items, survivors)."""
+        ctx = self.ctx
+        ctx.reset_current()
+        moved = 0
+        for sp, fn in ((gpu.SPECIES_ELECTRON, ctx.step_electrons_resident),
+                       (gpu.SPECIES_PHOTON, ctx.step_photons_resident),
+                       (gpu.SPECIES_POSITRON, ctx.step_positrons_resident)):
+            if ctx.resident_count(sp) == 0:
+                continue
+            fn(self.step, dt_s)
+            moved += ctx.last_step_stats()[0]
+        ctx.drain_resident(self.step, dt_s)
+        drained = ctx.last_drain_stats()
+        ctx.commit_survivors_resident()
+        for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON, gpu.SPECIES_PHOTON):
+            ctx.compact_resident(sp)
+        if self.feedback:
+            ctx.advance_field(dt_s, self.field_substeps)
+        self.step += 1
+        return moved, drained
+
+    def run(self, steps, census_every=100, dt_s=DT_S):
+        """Advances `steps` steps; returns a result dict with the census
+        history, the final spectra, the multiplication factor and the
+        device-side throughput."""
+        history = []
+        moved_total = 0
+        fifo_total = 0
+        row, _ = census_row(self.ctx, self.step)
+        history.append(row)
+        l0 = gpu.kernel_launches()
+        t0 = time.perf_counter()
+        for k in range(steps):
+            moved, drained = self.advance(dt_s)
+            moved_total += moved
+            fifo_total += drained[0]
+            if (k + 1) % census_every == 0 or k + 1 == steps:
+                row, spectra = census_row(self.ctx, self.step)
+                row["particle_steps"] = moved_total
+                history.append(row)
+        wall = time.perf_counter() - t0
+        launches = gpu.kernel_launches() - l0
+        final = history[-1]
+        return {
+            "history": history, "spectra": spectra, "edges_eV": SPECTRUM_EDGES_EV.tolist(),
+            "seed_weight": self.seed_weight,
+            "multiplication": final["electron_ge_1MeV"] / self.seed_weight if self.seed_weight > 0 else 0.0,
+            "particle_steps": moved_total, "fifo_items": fifo_total, "wall_s": wall,
+            "particle_steps_per_s": moved_total / wall if wall > 0 else 0.0,
+            "kernel_launches": launches, "steps": steps,
+        }
+
+
+def avalanche_length_m(history, lo_frac=0.3, hi_frac=0.6, dt_s=DT_S, key="electron_ge_1MeV"):
+    """Avalanche (e-folding) length of the runaway population along the
+    drift: the log-slope of N(>= 1 MeV) between the census rows at lo_frac
+    and hi_frac of the run, converted to distance at the speed of light
+    (runaway electrons move at ~c)."""
+    steps = np.array([h["step"] for h in history], dtype=np.float64)
+    n = np.array([h[key] for h in history], dtype=np.float64)
+    t_end = steps[-1]
+    sel = (steps >= lo_frac * t_end) & (steps <= hi_frac * t_end) & (n > 0)
+    if sel.sum() < 2:
+        return float("nan")
+    slope = np.polyfit(steps[sel] * dt_s * workloads.C_LIGHT, np.log(n[sel]), 1)[0]
+    return 1.0 / slope if slope > 0 else float("inf")
+
+
+def coleman_dwyer_length_m(field_v_per_m, density_kg_m3, threshold_kv_per_m=276.0, anchor_density=1.293):
+    """Coleman-Dwyer avalanche length lambda = 7300 kV / (E - E_th n/n0),
+    with the threshold scaled by the density over the 1.293 kg/m^3 anchor
+    (scripts/test_cd_science.py:341-382, scripts/rrea_profiled_atmosphere.py)."""
+    e_kv = field_v_per_m / 1000.0
+    return 7300.0 / (e_kv - threshold_kv_per_m * density_kg_m3 / anchor_density)
+
+
+REDUCED_COLUMNS = (  # our census fields under the reduced CSV's column names
+    ("step", "step"), ("time_s", "time_s"),
+    ("N_kinetic_e_real", "electron_weight"), ("N_kinetic_e_ge_1MeV_real", "electron_ge_1MeV"),
+    ("N_kinetic_e_ge_100keV_real", "electron_ge_100keV"), ("N_photon_real", "photon_weight"),
+    ("N_positron_real", "positron_weight"), ("N_positron_ge_100keV_real", "positron_ge_100keV"),
+)
+
+
+def write_reduced_csv(path, history):
+    """The census history as rrea_reduced.csv-style rows (the columns the
+    census provides, under the reduced diagnostics' names,
+    O/RreaCouplingDiagnostics.cpp:950-980)."""
+    with open(path, "w", newline="") as f:
+        w = csv.writer(f)
+        w.writerow([c for c, _ in REDUCED_COLUMNS])
+        for h in history:
+            w.writerow([h[k] for _, k in REDUCED_COLUMNS])
+
+
+def main():
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--case", default="uniform_c0", choices=["uniform_c0"])
+    p.add_argument("--seeds", type=int, default=10_000)
+    p.add_argument("--steps", type=int, default=4000)
+    p.add_argument("--rng-seed", type=int, default=1)
+    p.add_argument("--field", type=float, default=None, help="uniform |E_z| in V/m (default: the case's)")
+    p.add_argument("--capacity", type=int, default=1 << 24)
+    p.add_argument("--census-every", type=int, default=100)
+    p.add_argument("--json", default=None)
+    p.add_argument("--csv", default=None)
+    a = p.parse_args()
+    import torch
+
+    torch.cuda.set_device(0)
+    ctx = make_context(a.case, a.capacity, a.rng_seed, a.field)
+    seeds = workloads.make_electrons(a.case, a.seeds)
+    res = AvalancheRun(ctx, seeds).run(a.steps, census_every=a.census_every)
+    p_case = c0_like_case(a.field, a.case)
+    res["case"] = a.case
+    res["seeds"] = a.seeds
+    res["field_v_per_m"] = p_case["field_v_per_m"]
+    res["avalanche_length_m"] = avalanche_length_m(res["history"])
+    res["coleman_dwyer_length_m"] = [coleman_dwyer_length_m(p_case["field_v_per_m"], workloads.AIR_DENSITY, t)
+                                     for t in (276.0, 284.0)]
+    res["spectra"] = {k: v.tolist() for k, v in res["spectra"].items()}
+    if a.csv:
+        write_reduced_csv(a.csv, res["history"])
+    text = json.dumps(res)
+    if a.json:
+        os.makedirs(os.path.dirname(os.path.abspath(a.json)), exist_ok=True)
+        with open(a.json, "w") as f:
+            f.write(text)
+    print(json.dumps({k: res[k] for k in ("case", "seeds", "steps", "multiplication", "particle_steps", "wall_s",
+                                          "particle_steps_per_s", "kernel_launches", "avalanche_length_m",
+                                          "coleman_dwyer_length_m")}))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -171,42 +171,56 @@ void SeedSchedule::validate(double e_min, double e_max, double r_min, double r_m
     auto finite = [](double v) { return std::isfinite(v); };
     if (!finite(e_min) || !finite(e_max) || !(e_min > 0.0) || e_max < e_min || !finite(r_min) || !finite(r_max) ||
         !finite(z_min) || !finite(z_max) || !(r_max > r_min) || !(z_max > z_min)) {
-        fail(RREA_GPU_ERR_ARGUMENT, "seed validation received invalid energy/domain bounds");
+        fail(RREA_GPU_ERR_ARGUMENT, "seed validation bounds are not a finite positive energy range and a nonempty domain");
     }
     double const eps = std::numeric_limits<double>::epsilon();
     std::set<int> seen;
     for (rrea_gpu_seed_event const& e : m_events) {
-        auto bad = [&](char const* what) {
-            fail(RREA_GPU_ERR_ARGUMENT, "invalid seed macro_index=" + std::to_string(e.macro_index) + ": " + what);
+        // The first failing rule names the row; the rules run in the order
+        // the overlay's production validation applies them.
+        auto reject = [&](char const* rule) {
+            fail(RREA_GPU_ERR_ARGUMENT,
+                 "seed row with macro_index " + std::to_string(e.macro_index) + " rejected: " + rule);
         };
-        if (e.macro_index < 0) bad("macro_index must be nonnegative");
-        if (!seen.insert(e.macro_index).second) bad("macro_index must be unique within the case");
-        if (e.species_id != kSeedElectron && e.species_id != kSeedPositron) bad("species_id must be 1 or 2");
-        if (!finite(e.time_s) || e.time_s < 0.0) bad("time_s must be finite and nonnegative");
-        if (!finite(e.weight) || !(e.weight > 0.0)) bad("weight_real_electrons must be finite and positive");
-        if (!finite(e.x_m) || !finite(e.y_m) || !finite(e.r_m) || !finite(e.z_m)) bad("position must be finite");
+        bool const position_finite = finite(e.x_m) && finite(e.y_m) && finite(e.r_m) && finite(e.z_m);
         double const radius = std::hypot(e.x_m, e.y_m);
         double const r_tol = 128.0 * eps * std::max({1.0, radius, std::abs(e.r_m)});
-        if (std::abs(e.r_m - radius) > r_tol) bad("r_m is inconsistent with hypot(x_m, y_m)");
-        if (radius < r_min || !(radius < r_max) || e.z_m < z_min || !(e.z_m < z_max)) {
-            bad("initial position is outside the half-open RZ domain");
+        struct Rule {
+            bool broken;
+            char const* text;
+        };
+        Rule const identity[] = {
+            {e.macro_index < 0, "negative macro_index"},
+            {!seen.insert(e.macro_index).second, "macro_index repeats within the case"},
+            {e.species_id != kSeedElectron && e.species_id != kSeedPositron, "species_id is neither 1 (e-) nor 2 (e+)"},
+            {!finite(e.time_s) || e.time_s < 0.0, "time_s is negative or not finite"},
+            {!finite(e.weight) || !(e.weight > 0.0), "weight_real_electrons is not a finite positive number"},
+            {!position_finite, "a position column is not finite"},
+            {position_finite && std::abs(e.r_m - radius) > r_tol, "r_m does not equal the radius of (x_m, y_m)"},
+            {position_finite && (radius < r_min || !(radius < r_max) || e.z_m < z_min || !(e.z_m < z_max)),
+             "start point lies outside the RZ domain [r_min, r_max) x [z_min, z_max)"},
+            {!finite(e.kinetic_energy_eV) || e.kinetic_energy_eV < e_min || e.kinetic_energy_eV > e_max,
+             "kinetic_energy_eV lies outside the tables' charged energy range"},
+            {!finite(e.ux) || !finite(e.uy) || !finite(e.uz), "a momentum column is not finite"},
+        };
+        for (Rule const& rule : identity) {
+            if (rule.broken) reject(rule.text);
         }
-        if (!finite(e.kinetic_energy_eV) || e.kinetic_energy_eV < e_min || e.kinetic_energy_eV > e_max) {
-            bad("declared kinetic energy is outside the certified range");
-        }
-        if (!finite(e.ux) || !finite(e.uy) || !finite(e.uz)) bad("momentum components must be finite");
         double const norm = std::hypot(std::hypot(e.ux, e.uy), e.uz);
-        if (!finite(norm) || !(norm > 0.0)) bad("momentum vector must be nonzero and finite");
+        if (!finite(norm) || !(norm > 0.0)) reject("the momentum vector is zero or overflows");
         double k = e.kinetic_energy_eV;
         if (!(norm < kSeedDirectionHintMaxMPerS)) {
-            // kinetic energy of a proper velocity, cancellation-free
+            // a proper velocity, not a direction hint: its kinetic energy,
+            // written without the cancellation of gamma - 1
             double const q = norm / kC;
             double const gamma = std::hypot(1.0, q);
             k = kMeC2 * q * (q / (gamma + 1.0));
         }
-        if (!finite(k) || k < e_min || k > e_max) bad("effective kinetic energy is outside the certified range");
+        if (!finite(k) || k < e_min || k > e_max) reject("the energy of the given momentum lies outside the tables' range");
         double const k_tol = 256.0 * eps * std::max({1.0, k, e.kinetic_energy_eV});
-        if (std::abs(k - e.kinetic_energy_eV) > k_tol) bad("proper-velocity kinetic energy disagrees with kinetic_energy_eV");
+        if (std::abs(k - e.kinetic_energy_eV) > k_tol) {
+            reject("the energy of the given proper velocity does not match kinetic_energy_eV");
+        }
     }
 }
 

@@ -191,6 +191,7 @@ struct rrea_gpu_ctx {
     bool spare_ready = false;
     uint32_t* d_alive = nullptr;
     uint32_t* d_cost_scratch = nullptr;  // histogram and cursors of the scheduling order
+    double* d_census = nullptr;          // census sums, edges and thresholds (first census call)
     uint64_t* d_child_lineage = nullptr;
     unsigned long long* d_invalid = nullptr;
     // roots of the initial FIFO items (16 B each) on the device and in pinned
@@ -444,6 +445,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     }
     dfree(ctx->d_alive);
     dfree(ctx->d_cost_scratch);
+    dfree(ctx->d_census);
     dfree(ctx->d_child_lineage);
     dfree(ctx->d_invalid);
     dfree(ctx->d_roots);
@@ -1722,6 +1724,54 @@ rrea_gpu_status rrea_gpu_kernel_launches(uint64_t* count)
 {
     if (!count) return RREA_GPU_ERR_ARGUMENT;
     *count = rrea_launch::launches_noted();
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_census_resident(rrea_gpu_ctx* ctx, int32_t species, const double* edges_eV, int32_t n_edges,
+                                         const double* thresholds_eV, int32_t n_thresholds, double* out)
+{
+    constexpr int kMaxEdges = 1025, kMaxThresholds = 16;
+    constexpr int kSums = 5 + kMaxThresholds + kMaxEdges - 1;
+    if (!ctx || !out || species < 0 || species >= kSpecies) return RREA_GPU_ERR_ARGUMENT;
+    if (n_edges < 2 || n_edges > kMaxEdges || !edges_eV || n_thresholds < 0 || n_thresholds > kMaxThresholds
+        || (n_thresholds > 0 && !thresholds_eV)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "census needs 2..1025 edges and at most 16 thresholds");
+    }
+    for (int k = 0; k < n_edges; ++k) {
+        if (!std::isfinite(edges_eV[k]) || (k > 0 && !(edges_eV[k] > edges_eV[k - 1]))) {
+            return fail(ctx, RREA_GPU_ERR_ARGUMENT, "census edges must be finite and strictly increasing");
+        }
+    }
+    for (int k = 0; k < n_thresholds; ++k) {
+        if (std::isnan(thresholds_eV[k])) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "census threshold is NaN");
+    }
+    // sums | edges | thresholds | count and max-weight words
+    size_t const words = kSums + kMaxEdges + kMaxThresholds + 2;
+    if (!ctx->d_census) RREA_CUDA(ctx, dalloc(&ctx->d_census, words));
+    double* const sums = ctx->d_census;
+    double* const edges = sums + kSums;
+    double* const thr = edges + kMaxEdges;
+    auto* const words64 = reinterpret_cast<unsigned long long*>(thr + kMaxThresholds);
+    int const n_sums = 5 + n_thresholds + n_edges - 1;
+    RREA_CUDA(ctx, cudaMemsetAsync(sums, 0, sizeof(double) * n_sums, ctx->stream));
+    RREA_CUDA(ctx, cudaMemsetAsync(words64, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(edges, edges_eV, sizeof(double) * n_edges, cudaMemcpyHostToDevice, ctx->stream));
+    if (n_thresholds > 0) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(thr, thresholds_eV, sizeof(double) * n_thresholds, cudaMemcpyHostToDevice,
+                                       ctx->stream));
+    }
+    SpeciesTile const& st = ctx->tiles[species];
+    RREA_CUDA(ctx, rrea_launch::census(st.d[3], st.d[4], st.d[5], st.d[6], st.id, st.n, species == RREA_SPECIES_PHOTON,
+                                       edges, n_edges, thr, n_thresholds, sums, words64, words64 + 1,
+                                       ctx->num_sms * 8, ctx->stream));
+    unsigned long long w64[2] = {0, 0};
+    RREA_CUDA(ctx, cudaMemcpyAsync(out + 2, sums, sizeof(double) * n_sums, cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaMemcpyAsync(w64, words64, sizeof(w64), cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double max_w = 0.0;
+    std::memcpy(&max_w, &w64[1], sizeof(max_w));
+    out[0] = static_cast<double>(w64[0]);
+    out[1] = w64[0] ? max_w : 0.0;
     return RREA_GPU_OK;
 }
 

@@ -100,4 +100,15 @@ int cost_order_scratch_elems();
 cudaError_t cost_order(const double* ux, const double* uy, const double* uz, const int64_t* id, int64_t n,
                        uint32_t* scratch, uint32_t* order, int blocks, cudaStream_t stream);
 
+// Census of a species tile (rrea_census.cu): over the valid rows, the
+// weight sums (w, w^2, w K), under/overflow weight, weight at or above each
+// threshold and the weighted spectrum over [edges[0], edges[n_edges-1]) are
+// added into out (5 + n_thresholds + n_edges - 1 doubles), the particle count
+// into *count and the largest weight's bit pattern into *max_bits (all
+// zeroed by the caller).  n_edges <= 1025, n_thresholds <= 16.
+cudaError_t census(const double* ux, const double* uy, const double* uz, const double* w, const int64_t* id, int64_t n,
+                   bool photon, const double* edges, int n_edges, const double* thresholds, int n_thresholds,
+                   double* out, unsigned long long* count, unsigned long long* max_bits, int blocks,
+                   cudaStream_t stream);
+
 }  // namespace rrea_launch

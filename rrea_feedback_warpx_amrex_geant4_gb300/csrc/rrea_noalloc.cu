@@ -11,6 +11,14 @@
 // Offsets and block sums are written before they are read on every call,
 // so neither needs to start at zero.  The error word must be zero when the
 // scatter starts; each call clears it itself before launching.
+//
+// The scatter claims each output slot with a compare-and-swap on the
+// record's parent_index word, after a first pass has set that word to -1 in
+// every output slot (the output is the caller's buffer and needs no
+// initialisation).  A second record aimed at a claimed slot is a duplicated
+// (parent_index, lineage) pair: it is reported, never written.  With the
+// counts summing to n_secondaries, every record landing inside the output
+// and no slot claimed twice, every output slot is written exactly once.
 #include "../../include/rrea_gpu.h"
 
 #include "rrea_kernels.h"
@@ -19,7 +27,6 @@
 
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 namespace {
 
@@ -27,14 +34,17 @@ constexpr int64_t kMaxParents = RREA_GPU_NOALLOC_MAX_PARENTS;
 constexpr int64_t kScanBlock = 1024;
 constexpr int64_t kBlocks = (kMaxParents + kScanBlock - 1) / kScanBlock + 1;
 constexpr int64_t kScratchWords = kMaxParents + kBlocks + 8;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) int64_t g_order_scratch[kScratchWords];
 
-// Device address of g_order_scratch per device, looked up once per device
-// with that device current.
-std::mutex g_lookup_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
+// Marks every output slot unclaimed (parent_index = -1).
+__global__ void unclaim_slots_kernel(rrea_gpu_secondary* __restrict__ out, int64_t count)
+{
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        out[i].parent_index = -1;
+    }
+}
 
 // Scatter with the checks the internal pass does not need (its inputs are
 // produced by the transport kernel): every record must name a parent in
@@ -65,6 +75,11 @@ __global__ void scatter_checked_kernel(const rrea_gpu_secondary* __restrict__ in
         int64_t const dst = offsets[p] + static_cast<int64_t>(s.lineage);
         if (dst < 0 || dst >= count) {
             atomicCAS(err, 0ULL, 4ULL);
+            continue;
+        }
+        auto* const claim = reinterpret_cast<unsigned long long*>(&out[dst].parent_index);
+        if (atomicCAS(claim, ~0ULL, static_cast<unsigned long long>(p)) != ~0ULL) {
+            atomicCAS(err, 0ULL, 5ULL);
             continue;
         }
         out[dst] = s;
@@ -115,27 +130,17 @@ extern "C" rrea_gpu_status rrea_gpu_order_secondaries_noalloc(const uint32_t* d_
     }
     if (n_parents == 0) return RREA_GPU_OK;
 
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-        std::snprintf(text, sizeof(text), "cudaGetDevice: %s", e != cudaSuccess ? cudaGetErrorString(e) : "device id");
+    // The array's device address is looked up on every call, with the
+    // caller's device and context current: a cached address would go stale
+    // after cudaDeviceReset or under another context on the same device.
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_order_scratch);
+    if (e != cudaSuccess || !p) {
+        std::snprintf(text, sizeof(text), "cudaGetSymbolAddress: %s",
+                      e != cudaSuccess ? cudaGetErrorString(e) : "null address");
         return report(message, message_size, RREA_GPU_ERR_CUDA, text);
     }
-    int64_t* scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_lookup_mutex);
-        if (!g_scratch_ptr[dev]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_order_scratch);
-            if (e != cudaSuccess || !p) {
-                std::snprintf(text, sizeof(text), "cudaGetSymbolAddress: %s",
-                              e != cudaSuccess ? cudaGetErrorString(e) : "null address");
-                return report(message, message_size, RREA_GPU_ERR_CUDA, text);
-            }
-            g_scratch_ptr[dev] = p;
-        }
-        scratch = static_cast<int64_t*>(g_scratch_ptr[dev]);
-    }
+    int64_t* const scratch = static_cast<int64_t*>(p);
     int64_t* const offsets = scratch;
     int64_t* const block_sums = scratch + kMaxParents;
     auto* const err_word = reinterpret_cast<unsigned long long*>(scratch + kMaxParents + kBlocks);
@@ -143,11 +148,16 @@ extern "C" rrea_gpu_status rrea_gpu_order_secondaries_noalloc(const uint32_t* d_
 
     e = cudaMemsetAsync(err_word, 0, sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = rrea_launch::exclusive_scan_counts(d_counts, n_parents, offsets, block_sums, s);
+    int const threads = 256;
+    int64_t blocks = (n_secondaries + threads - 1) / threads;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 65535) blocks = 65535;
+    if (e == cudaSuccess && n_secondaries > 0) {
+        rrea_launch::note_launch();
+        unclaim_slots_kernel<<<static_cast<unsigned>(blocks), threads, 0, s>>>(d_ordered, n_secondaries);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) {
-        int const threads = 256;
-        int64_t blocks = (n_secondaries + threads - 1) / threads;
-        if (blocks < 1) blocks = 1;
-        if (blocks > 65535) blocks = 65535;
         rrea_launch::note_launch();
         scatter_checked_kernel<<<static_cast<unsigned>(blocks), threads, 0, s>>>(
             d_unordered, n_secondaries, d_counts, n_parents, offsets, d_ordered, err_word);
@@ -163,9 +173,10 @@ extern "C" rrea_gpu_status rrea_gpu_order_secondaries_noalloc(const uint32_t* d_
     if (flag != 0) {
         static char const* const why[] = {
             "", "per-parent counts do not sum to n_secondaries", "a record's parent_index is outside [0, n_parents)",
-            "a record's lineage is not below its parent's count", "a record's destination is outside the output"};
+            "a record's lineage is not below its parent's count", "a record's destination is outside the output",
+            "two records share one (parent_index, lineage) pair"};
         std::snprintf(text, sizeof(text), "inconsistent input: %s (offending records were skipped)",
-                      why[flag < 5 ? flag : 0]);
+                      why[flag < 6 ? flag : 0]);
         return report(message, message_size, RREA_GPU_ERR_INVALID_STATE, text);
     }
     return RREA_GPU_OK;

@@ -86,7 +86,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_commit_survivors_resident", "rrea_gpu_compact_resident", "rrea_gpu_resident_count",
     "rrea_gpu_seed_schedule_load", "rrea_gpu_seed_schedule_free", "rrea_gpu_seed_schedule_size",
     "rrea_gpu_seed_schedule_events", "rrea_gpu_seed_schedule_validate", "rrea_gpu_seed_schedule_last_error",
-    "rrea_gpu_inject_seeds_resident", "rrea_gpu_thin_cic_groups",
+    "rrea_gpu_inject_seeds_resident", "rrea_gpu_thin_cic_groups", "rrea_gpu_census_resident",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -154,6 +154,7 @@ def load_library(path=LIB_PATH):
                                              ctypes.POINTER(ctypes.c_uint64), _i64p, _i64p,
                                              ctypes.POINTER(ctypes.c_int32), _i64p]
     lib.rrea_gpu_compact_resident.argtypes = [vp, ctypes.c_int32, _i64p]
+    lib.rrea_gpu_census_resident.argtypes = [vp, ctypes.c_int32, _D, ctypes.c_int32, _D, ctypes.c_int32, _D]
     lib.rrea_gpu_resident_count.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
     lib.rrea_gpu_kernel_launches.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
@@ -456,6 +457,19 @@ class RreaGpuContext:
             draws.ctypes.data_as(i64), valid.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cap.ctypes.data_as(i64)))
         return w, removed, draws, valid, cap
 
+    def census(self, species, edges_eV, thresholds_eV=()):
+        """Census of a resident species tile (the reduced diagnostics'
+        particle reductions and a weighted energy spectrum over the bins
+        [edges[b], edges[b+1])); returns a dict of count, max_weight,
+        sum_w, sum_w2, sum_wk, under, over, above (per threshold), hist."""
+        edges = np.ascontiguousarray(edges_eV, dtype=np.float64)
+        thr = np.ascontiguousarray(thresholds_eV, dtype=np.float64)
+        out = np.zeros(7 + thr.size + edges.size - 1)
+        self._check(self.lib.rrea_gpu_census_resident(self.handle, int(species), edges.ctypes.data_as(_D), edges.size,
+                                                      thr.ctypes.data_as(_D) if thr.size else None, thr.size,
+                                                      out.ctypes.data_as(_D)))
+        return unpack_census(out, thr.size)
+
     def resident_count(self, species):
         n = ctypes.c_int64()
         self._check(self.lib.rrea_gpu_resident_count(self.handle, species, ctypes.byref(n)))
@@ -548,6 +562,13 @@ class RreaGpuContext:
         s = ctypes.c_void_p()
         self._check(self.lib.rrea_gpu_stream(self.handle, ctypes.byref(s)))
         return s.value
+
+
+def unpack_census(out, n_thresholds):
+    """Named fields of an rrea_gpu_census_resident output vector."""
+    return {"count": int(out[0]), "max_weight": float(out[1]), "sum_w": float(out[2]), "sum_w2": float(out[3]),
+            "sum_wk": float(out[4]), "under": float(out[5]), "over": float(out[6]),
+            "above": out[7:7 + n_thresholds].copy(), "hist": out[7 + n_thresholds:].copy()}
 
 
 def population_projection(current, removals, insertions, ceiling, reject_equality=False):

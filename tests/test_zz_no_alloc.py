@@ -80,3 +80,48 @@ def test_noalloc_flags_inconsistent_records(env):
     status, msg, out = _order(torch, gpu, counts, ref[::-1].copy(), 512)
     assert status == 0, msg
     assert out.tobytes() == ref.tobytes()
+
+
+def test_noalloc_at_its_maximum_parent_count(env):
+    """n_parents = RREA_GPU_NOALLOC_MAX_PARENTS exactly: the scan's last
+    block sums and the error word sit at the far end of the fixed array.
+    Counts mostly zero, a few thousand records; the expected order is a NumPy
+    reordering by (parent_index, lineage)."""
+    torch, gpu, workloads, ctx = env
+    n = gpu.NOALLOC_MAX_PARENTS
+    rng = np.random.default_rng(2718)
+    counts = np.zeros(n, dtype=np.int64)
+    parents = rng.choice(n, size=1500, replace=False)
+    parents[:2] = (0, n - 1)                             # both ends of the parent range
+    counts[parents] = rng.integers(1, 5, size=parents.size)
+    recs = np.zeros(int(counts.sum()), dtype=gpu.SECONDARY_DTYPE)
+    recs["parent_index"] = np.repeat(np.arange(n), counts)
+    starts = np.cumsum(counts) - counts
+    recs["lineage"] = np.arange(len(recs)) - np.repeat(starts, counts)
+    recs["energy_eV"] = rng.uniform(1.0, 2.0, len(recs))
+    recs["species"] = rng.integers(0, 3, len(recs))
+    expected = recs.copy()                               # already in (parent, lineage) order
+    for call in range(2):
+        perm = np.random.default_rng(call).permutation(len(recs))
+        status, msg, out = _order(torch, gpu, counts, recs[perm], n)
+        assert status == 0, msg
+        assert out.tobytes() == expected.tobytes()
+
+
+def test_noalloc_flags_a_duplicated_pair(env):
+    """One record duplicated in place of another: the counts still sum to
+    n_secondaries and every lineage is in range, yet one output slot would
+    stay unwritten.  The call reports it instead of returning OK."""
+    torch, gpu, workloads, ctx = env
+    arr = workloads.make_electrons("scaleup_c1", 512, seed=43)
+    ref = ctx.apply_electrons(arr, 1, 5.0e-10)
+    assert len(ref) > 2
+    counts = np.bincount(ref["parent_index"], minlength=512)
+    dup = ref.copy()
+    dup[1] = dup[0]                                      # record 1 lost, record 0 twice
+    status, msg, out = _order(torch, gpu, counts, dup, 512)
+    assert status == 9, msg                              # RREA_GPU_ERR_INVALID_STATE
+    assert "share" in msg
+    status, msg, out = _order(torch, gpu, counts, ref, 512)
+    assert status == 0, msg
+    assert out.tobytes() == ref.tobytes()
