@@ -27,7 +27,9 @@ one dt, its newborn residual legs included.  Synthetic seeds; no dataset.
               sample of the same workload
 
 --impl reference times the CPU restatement of the reference path (the
-WarpX/AMReX build itself cannot be built here) on the host cores.
+WarpX/AMReX build itself cannot be built here) on the host cores, on the same
+populations and the same evolution (warm-up steps untimed, then the timed
+steps), without loading the GPU library.
 """
 import argparse
 import json
@@ -59,10 +61,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--population", type=int, default=1 << 21)
-    p.add_argument("--cpu-sample", type=int, default=131072)
-    p.add_argument("--cpu-baseline-sample", type=int, default=1 << 19)
-    p.add_argument("--cpu-baseline-steps", type=int, default=4)
+    p.add_argument("--cpu-baseline-steps", type=int, default=3)
     p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--c0-steps", type=int, default=1000)
     p.add_argument("--threads", type=int, default=128)
     p.add_argument("--blocks-per-sm", type=int, default=16)
     return p.parse_args()
@@ -84,19 +85,26 @@ def read_peaks():
     return 6800.0, "fallback"
 
 
+TRAFFIC_RECORD = os.path.join(ROOT, "profiles", "electron_step_kernel_traffic.json")
+
+
 def read_traffic_per_particle_step():
-    """dram bytes per particle-step of the transport kernel from the committed
-    ncu summary (profiles/electron_step_kernel_scaleup_c1.md), if present."""
-    path = os.path.join(ROOT, "profiles", "electron_step_kernel_scaleup_c1.md")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        if line.strip().startswith("dram_bytes_per_particle_step:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+    """DRAM bytes (read + write) per particle-step of the electron transport
+    kernel, from the ncu capture recorded for THIS build: the record carries
+    the library's source digest, and a record of another build is not used
+    (returns (None, reason)).  ncu cannot run inside a timed bench, so the
+    counter comes from a capture of the same build on the same workload."""
+    from rrea_feedback_warpx_amrex_geant4_gb300 import build
+
+    if not os.path.exists(TRAFFIC_RECORD):
+        return None, "no ncu capture recorded"
+    with open(TRAFFIC_RECORD) as f:
+        rec = json.load(f)
+    digest = build.source_digest()
+    if rec.get("source_digest") != digest:
+        return None, f"the recorded capture is of build {rec.get('source_digest')}, not {digest}"
+    return float(rec["dram_bytes_per_particle_step"]), (f"ncu capture of this build ({digest}): "
+                                                        f"{rec.get('capture', '')}")
 
 
 class ClockSampler:
@@ -181,60 +189,61 @@ def cpu_populations(n, seed):
     return arr, pho, pos
 
 
-def commit_and_compact(tile, survivors, species):
-    """DrainAndCommitSecondaries' commit on a host tile: the species'
-    survivors become particles (oracle.commit_survivors), and the particles
-    that ended the step leave the tile."""
-    from oracle import oracle
+def gpu_arm_populations(n, rank=0):
+    """The resident populations both arms start from: n electrons from the
+    case's seed distribution, n/2 photons and n/16 positrons (seeded), with
+    photons at their start point (the resident photon step pushes them)."""
+    from rrea_feedback_warpx_amrex_geant4_gb300 import workloads
 
-    keep = tile["id"] > 0
-    add = oracle.commit_survivors(survivors, species, int(np.abs(tile["id"]).max(initial=0)) + 1)
-    out = {}
-    for k, v in tile.items():
-        if k == "cpu":
-            extra = np.zeros(len(add["id"]), dtype=v.dtype)
-        else:
-            extra = add[k[5:] if k.startswith("prev_") else k]
-        out[k] = np.ascontiguousarray(np.concatenate([v[keep], extra.astype(v.dtype)]))
-    return out
+    n_g = int(n * PHOTON_FRACTION)
+    n_p = max(1, int(n * POSITRON_FRACTION))
+    arr = workloads.make_electrons(CASE, n, seed=777 + rank)
+    pho = make_photons(n_g, seed=778 + rank)
+    for f in ("r", "z", "theta"):
+        pho[f][:] = pho["prev_" + f]
+    pos = workloads.make_electrons(CASE, n_p, seed=779 + rank)
+    return arr, pho, pos
 
 
-def cpu_oracle_rate(cfg, field, n, seed, steps=1):
-    """Oracle particle-steps/s of the whole kinetic step (three phases, FIFO
-    drain and commit, net-chord current, field update) on n electrons, the
-    photon and positron fractions, for `steps` steps (all threads)."""
-    from oracle import oracle
+def oracle_whole_steps(n, warmup, steps, rank=0):
+    """The oracle (CPU restatement, all host threads) running the bench's
+    whole kinetic step on the bench's populations: `warmup` untimed steps,
+    then `steps` timed ones, the populations evolving with commit and field
+    feedback exactly as on the GPU.  Returns (particle-steps, seconds, cores).
+    Loads no part of the GPU library."""
+    from oracle import avalanche as oav, oracle
     from rrea_feedback_warpx_amrex_geant4_gb300 import DEFAULT_TABLES, workloads
 
-    if not getattr(cpu_oracle_rate, "_loaded", False):
-        oracle.load_tables(DEFAULT_TABLES)
-        cpu_oracle_rate._loaded = True
-    arr, pho, pos = cpu_populations(n, seed)
-    fld = {k: np.array(v, dtype=np.float64) for k, v in field.items()}
-    dr = (cfg.r_hi - cfg.r_lo) / cfg.nr
-    dz = (cfg.z_hi - cfg.z_lo) / cfg.nz
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    oracle.load_tables(DEFAULT_TABLES)
+    cfg = workloads.make_config(oracle, CASE)
+    arr, pho, pos = gpu_arm_populations(n, rank)
+    run = oav.AvalancheRun(cfg, workloads.make_field(CASE), arr, photons=pho, positrons=pos, feedback=True,
+                           field_substeps=FIELD_SUBSTEPS)
+    for _ in range(warmup):
+        run.advance(DT_S)
     moved = 0
     t0 = time.perf_counter()
-    for s in range(steps):
-        moved += int((arr["id"] > 0).sum()) + int((pho["id"] > 0).sum()) + int((pos["id"] > 0).sum())
-        oe = oracle.electron_step(cfg, fld, s, DT_S, arr)
-        og = oracle.photon_step(cfg, s, DT_S, pho)
-        op = oracle.positron_step(cfg, fld, s, DT_S, pos)
-        pending = np.concatenate([oe["secondaries"], og["secondaries"], op["secondaries"]])
-        od = oracle.drain(cfg, fld, s, DT_S, pending)
-        arr = commit_and_compact(arr, od["survivors"], 0)
-        pos = commit_and_compact(pos, od["survivors"], 1)
-        pho = commit_and_compact(pho, od["survivors"], 2)
-        rows = np.concatenate([oracle.segment_rows(r) for r in (oe, op, od)])
-        cur = oracle.deposit_segments(cfg, DT_S, rows)
-        fld["er"], fld["ez"], fld["bt"] = oracle.advance_maxwell(cfg.nr, cfg.nz, dr, dz, DT_S, FIELD_SUBSTEPS,
-                                                                 fld["er"], fld["ez"], fld["bt"], cur["jr_phys"],
-                                                                 cur["jz_phys"])
-        for t in (arr, pho, pos):
-            workloads.capture_prev(t)
-        workloads.push_photons(pho, DT_S)
-    dt = time.perf_counter() - t0
-    return moved / dt, moved, dt
+    for _ in range(steps):
+        moved += run.advance(DT_S)
+    return moved, time.perf_counter() - t0, cores
+
+
+DATA = "synthetic (scale-up case seed distribution, seeded numpy PRNG)"
+
+
+def workload_config(n, world):
+    """The workload both arms time (the same populations, evolution and field)."""
+    return {"workload": f"{CASE}: whole kinetic step (electron, photon, positron phases, newborn FIFO and commit, "
+                        f"net-chord current, field update) over resident populations of {population_text(n)} per "
+                        f"GPU (256x2048 cells over 200 m x 2 km, initial uniform E_z = -500 kV/m), dt 0.5 ns",
+            "grid": "256x2048",
+            "population_per_gpu": {"electrons": n, "photons": int(n * PHOTON_FRACTION),
+                                   "positrons": max(1, int(n * POSITRON_FRACTION))},
+            "dt_s": DT_S, "field_substeps": FIELD_SUBSTEPS,
+            "l2": "flushed between timed steps (256 MiB write)",
+            "parallelism": f"dp{world} (independent particle shards)"}
 
 
 def population_text(n):
@@ -244,32 +253,19 @@ def population_text(n):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    from rrea_feedback_warpx_amrex_geant4_gb300 import gpu, workloads
-
-    cfg = workloads.make_config(gpu, CASE)
-    field = workloads.make_field(CASE)
-    cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    for w in range(args.warmup):
-        cpu_oracle_rate(cfg, field, 1024, seed=99 + w)
-    rates, total_moved, total_t = [], 0, 0.0
-    for s in range(args.steps):
-        r, moved, dt = cpu_oracle_rate(cfg, field, args.cpu_sample, seed=1000 + s)
-        rates.append(r)
-        total_moved += moved
-        total_t += dt
-    value = total_moved / total_t
+    n = args.population
+    moved, secs, cores = oracle_whole_steps(n, args.warmup, args.steps)
+    value = moved / secs
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * total_t / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (scale-up case seed distribution)",
-        "config": {"workload": f"{CASE}: whole kinetic step (three phases, newborn FIFO and commit, net-chord current, "
-                               f"field update), {population_text(args.cpu_sample)} per timed step",
-                   "grid": "256x2048", "dt_s": DT_S, "field_substeps": FIELD_SUBSTEPS},
+        "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": workload_config(n, world),
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{population_text(args.cpu_sample)} x {args.steps} steps (a fresh draw of the "
-                                   f"workload each step), OpenMP chunks of 64"},
+                         "sample": f"the whole workload: {population_text(n)} evolving over {args.warmup} untimed "
+                                   f"and {args.steps} timed steps ({moved} particle-steps in {secs:.1f} s), "
+                                   f"OpenMP chunks of 64, -O3"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -303,11 +299,7 @@ def run_gb300(args, rank, world, local):
     field = workloads.make_field(CASE)
     ctx.set_field(**field)
     ctx.set_launch(args.threads, args.blocks_per_sm, diagnostics=False)
-    arr = workloads.make_electrons(CASE, n, seed=777 + rank)
-    pho = make_photons(n_g, seed=778 + rank)
-    for f in ("r", "z", "theta"):
-        pho[f][:] = pho["prev_" + f]  # the resident photon step pushes by itself
-    pos = workloads.make_electrons(CASE, n_p, seed=779 + rank)
+    arr, pho, pos = gpu_arm_populations(n, rank)
     ctx.stage_electrons(arr)
     ctx.stage_photons(pho)
     ctx.stage_positrons(pos)
@@ -372,20 +364,25 @@ def run_gb300(args, rank, world, local):
     total_ms_max, moved_all = distributed.reduce_step_time(total_ms, moved, dist, "cuda")
     value = moved_all / (total_ms_max / 1000.0)
 
-    # ---- e2e through the drop-in C-ABI (host buffers, copies in the timed region)
+    # ---- e2e through the drop-in C-ABI (host buffers, copies in the timed
+    # region) on the populations the resident steps reached
     def pinned_tile(src):
         out = {}
         for k, v in src.items():
             out[k] = torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy()
         return out
 
-    pe = pinned_tile(workloads.make_electrons(CASE, n, seed=4242 + rank))
-    for f in ("r", "z", "theta", "ux", "uy", "uz"):
-        pe["prev_" + f] = pe[f]  # the captured state is the current state
-    pg = pinned_tile(make_photons(n_g, seed=4243 + rank))
-    pp = pinned_tile(workloads.make_electrons(CASE, n_p, seed=4244 + rank))
-    for f in ("r", "z", "theta", "ux", "uy", "uz"):
-        pp["prev_" + f] = pp[f]
+    def fetched(species, fetch):
+        m = ctx.resident_count(species)
+        t = {k: np.ascontiguousarray(v[:m]) for k, v in workloads.make_electrons(CASE, max(m, 1)).items()}
+        fetch(t)
+        for f in ("r", "z", "theta", "ux", "uy", "uz"):
+            t["prev_" + f][:] = t[f]  # the captured state is the current state
+        return pinned_tile(t)
+
+    pe = fetched(gpu.SPECIES_ELECTRON, ctx.fetch_electrons)
+    pg = fetched(gpu.SPECIES_PHOTON, ctx.fetch_photons)
+    pp = fetched(gpu.SPECIES_POSITRON, ctx.fetch_positrons)
     rec = gpu.SECONDARY_DTYPE.itemsize
 
     def e2e_step(step):
@@ -405,8 +402,6 @@ def run_gb300(args, rank, world, local):
     e2e_t = 0.0
     sec_bytes = 0
     surv_bytes = 0
-    e2e_step(step)  # warm
-    step += 1
     barrier()
     for _ in range(args.e2e_steps):
         # photons: the host captures the start and pushes (WarpX's part of the step)
@@ -421,36 +416,50 @@ def run_gb300(args, rank, world, local):
         sec_bytes += n_pending * rec
         surv_bytes += n_surv * rec
         step += 1
-    e2e_value = e2e_moved / e2e_t
+    e2e_value = e2e_moved / e2e_t if e2e_t > 0 else None
     k = max(args.e2e_steps, 1)
-    h2d = (n + n_g + n_p) * (13 * 8 + 8 + 4) + sec_bytes // k
-    d2h = (n + n_g + n_p) * (6 * 8 + 8) + sec_bytes // k + surv_bytes // k
+    tiles_n = len(pe["id"]) + len(pg["id"]) + len(pp["id"])
+    h2d = tiles_n * (13 * 8 + 8 + 4) + sec_bytes // k
+    d2h = tiles_n * (6 * 8 + 8) + sec_bytes // k + surv_bytes // k
+
+    # ---- the plain uniform-field case at its own small populations (1e4
+    # seeds, the first c0 steps of its 4000): launch- and latency-bound
+    c0 = None
+    if rank == 0 and args.c0_steps > 0:
+        from rrea_feedback_warpx_amrex_geant4_gb300 import avalanche
+
+        c0_ctx = avalanche.make_context("uniform_c0", 1 << 20, 1, blocks_per_sm=args.blocks_per_sm)
+        torch.cuda.synchronize()
+        res = avalanche.AvalancheRun(c0_ctx, workloads.make_electrons("uniform_c0", 10_000)).run(
+            args.c0_steps, census_every=args.c0_steps)
+        c0_ctx.close()
+        c0 = {"workload": f"uniform_c0: 10000 seeds at 7.2 MeV, E_z = -400 kV/m, 32x256 cells over 50 m x 500 m, "
+                          f"first {args.c0_steps} of its 4000 steps (the resident loop: three phases, drain, "
+                          f"commit, compaction; no field feedback)",
+              "value": res["particle_steps_per_s"], "unit": "particle-steps/s",
+              "ms_per_step": 1000.0 * res["wall_s"] / args.c0_steps,
+              "particle_steps": res["particle_steps"],
+              "launches_per_step": res["kernel_launches"] / args.c0_steps,
+              "final_electrons": res["history"][-1]["electron_count"],
+              "timing": "host wall clock around the steps (each step ends in a stream synchronisation)"}
 
     if rank == 0:
         peak, peak_kind = read_peaks()
         achieved = (moved_e * BYTES_PER_PARTICLE_STEP) / (kernel_ms_e / 1000.0) / 1.0e9 if kernel_ms_e > 0 else 0.0
         achieved_g = (moved_g * BYTES_PER_PARTICLE_STEP) / (kernel_ms_g / 1000.0) / 1.0e9 if kernel_ms_g > 0 else 0.0
         achieved_p = (moved_p * BYTES_PER_PARTICLE_STEP) / (kernel_ms_p / 1000.0) / 1.0e9 if kernel_ms_p > 0 else 0.0
-        traffic_pps = read_traffic_per_particle_step()
+        traffic_pps, traffic_source = read_traffic_per_particle_step()
         launches_per_step = launches / max(args.steps, 1)
         traffic = traffic_pps * (moved_e / max(args.steps, 1)) if traffic_pps else None
-        cores = os.cpu_count() or 1
-        cpu_n = args.cpu_baseline_sample
-        cpu_rate, cpu_moved, cpu_t = cpu_oracle_rate(cfg, field, cpu_n, seed=31337, steps=args.cpu_baseline_steps)
+        cpu_moved, cpu_t, cores = (oracle_whole_steps(n, 0, args.cpu_baseline_steps, rank)
+                                   if args.cpu_baseline_steps > 0 else (0, 0.0, os.cpu_count() or 1))
+        cpu_rate = cpu_moved / cpu_t if cpu_t > 0 else None
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (scale-up case seed distribution, seeded numpy PRNG)",
-            "config": {"workload": f"{CASE}: whole kinetic step (electron, photon, positron phases, newborn "
-                                   f"FIFO and commit, net-chord current, field update) over resident populations of "
-                                   f"{population_text(n)} per GPU (256x2048 cells over 200 m x 2 km, initial "
-                                   f"uniform E_z = -500 kV/m), dt 0.5 ns",
-                       "grid": "256x2048",
-                       "population_per_gpu": {"electrons": n, "photons": n_g, "positrons": n_p},
-                       "dt_s": DT_S, "field_substeps": FIELD_SUBSTEPS,
-                       "l2": "flushed between timed steps (256 MiB write)",
-                       "parallelism": f"dp{world} (independent particle shards)"},
+            "data": DATA,
+            "config": workload_config(n, world),
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
                     "path": "rrea_gpu_apply_electrons/_photons/_positrons (pinned host tiles -> HBM -> host), "
@@ -458,7 +467,7 @@ def run_gb300(args, rank, world, local):
                             "rrea_gpu_current_device + rrea_gpu_advance_field_from_current"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": traffic, "kernel": "electron_step_kernel",
+                         "traffic": traffic, "traffic_source": traffic_source, "kernel": "electron_step_kernel",
                          "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
                          "kernel_ms_per_step": kernel_ms_e / args.steps,
                          "photon_kernel": {"kernel": "photon_step_kernel", "achieved": achieved_g,
@@ -473,9 +482,10 @@ def run_gb300(args, rank, world, local):
                        "committed_per_step": acc["committed"] / args.steps,
                        "transport_kernels_ms_per_step": (kernel_ms_e + kernel_ms_g + kernel_ms_p) / args.steps},
             "cpu_baseline": {"value": cpu_rate, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{population_text(cpu_n)} x {args.cpu_baseline_steps} steps of the same "
-                                       f"whole kinetic step ({cpu_moved} particle-steps in {cpu_t:.1f} s), "
-                                       f"OpenMP chunks of 64"},
+                             "sample": f"{population_text(n)} (the GPU arm's starting populations) x "
+                                       f"{args.cpu_baseline_steps} steps of the same whole kinetic step "
+                                       f"({cpu_moved} particle-steps in {cpu_t:.1f} s), OpenMP chunks of 64, -O3"},
+            "small_population": c0,
             "gpu_launches": launches,
             "gpu_launches_per_step": launches_per_step,
             "clocks": clocks.summary(),

@@ -90,8 +90,10 @@ def census(tile, species, edges, thresholds):
 class AvalancheRun:
     """The oracle's whole-run loop over host tiles (electron seeds)."""
 
-    def __init__(self, cfg, field, electrons, photons=None, positrons=None):
+    def __init__(self, cfg, field, electrons, photons=None, positrons=None, feedback=False, field_substeps=2):
         self.cfg = cfg
+        self.feedback = feedback
+        self.field_substeps = field_substeps
         self.field = {k: np.array(v, dtype=np.float64) for k, v in field.items()}
         self.tiles = {0: {k: np.array(v) for k, v in electrons.items()},
                       1: positrons if positrons is not None else empty_tile(),
@@ -106,15 +108,27 @@ class AvalancheRun:
         cfg, fld, t = self.cfg, self.field, self.tiles
         moved = sum(int((t[s]["id"] > 0).sum()) for s in t)
         push_photons(t[2], dt_s)
-        parts = []
+        phases = []
         if len(t[0]["id"]):
-            parts.append(_oracle.electron_step(cfg, fld, self.step, dt_s, t[0])["secondaries"])
+            phases.append(_oracle.electron_step(cfg, fld, self.step, dt_s, t[0]))
         if len(t[2]["id"]):
-            parts.append(_oracle.photon_step(cfg, self.step, dt_s, t[2])["secondaries"])
+            phases.append(_oracle.photon_step(cfg, self.step, dt_s, t[2]))
         if len(t[1]["id"]):
-            parts.append(_oracle.positron_step(cfg, fld, self.step, dt_s, t[1])["secondaries"])
+            phases.append(_oracle.positron_step(cfg, fld, self.step, dt_s, t[1]))
+        parts = [r["secondaries"] for r in phases]
         pending = np.concatenate(parts) if parts else np.zeros(0, dtype=_oracle.SECONDARY_DTYPE)
-        surv = _oracle.drain(cfg, fld, self.step, dt_s, pending)["survivors"]
+        od = _oracle.drain(cfg, fld, self.step, dt_s, pending)
+        surv = od["survivors"]
+        if self.feedback:
+            # the step's net-chord current (charged phases and newborn legs)
+            # drives the Maxwell TM-RZ update of the scattered field
+            rows = np.concatenate([_oracle.segment_rows(r) for r in phases + [od]])
+            cur = _oracle.deposit_segments(cfg, dt_s, rows)
+            dr = (cfg.r_hi - cfg.r_lo) / cfg.nr
+            dz = (cfg.z_hi - cfg.z_lo) / cfg.nz
+            fld["er"], fld["ez"], fld["bt"] = _oracle.advance_maxwell(
+                cfg.nr, cfg.nz, dr, dz, dt_s, self.field_substeps, fld["er"], fld["ez"], fld["bt"],
+                cur["jr_phys"], cur["jz_phys"])
         for s in (0, 1, 2):
             t[s], added = commit_and_compact(t[s], surv, s, self.next_id[s])
             self.next_id[s] += added

@@ -20,7 +20,7 @@ def build_oracle(force=False):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps):
             return LIB
-    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
+    cmd = ["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
            "-I", ROOT] + SOURCES + ["-lz", "-o", LIB + ".tmp"]
     subprocess.check_call(cmd)
     os.replace(LIB + ".tmp", LIB)

@@ -80,6 +80,7 @@ def lib():
         _lib.oracle_photon_step.argtypes = [ctypes.POINTER(RreaGpuConfig), ctypes.c_int32, ctypes.c_double,
                                             ctypes.POINTER(RreaGpuTile)]
         _lib.oracle_counts.argtypes = [ctypes.POINTER(ctypes.c_int64)] * 3
+        _lib.oracle_elastic_branches.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]
         _lib.oracle_secondaries.argtypes = [ctypes.c_void_p]
         _lib.oracle_sources.argtypes = [d]
         _lib.oracle_segments.argtypes = [d]
@@ -148,6 +149,14 @@ def density_ratio_at_z(z_m, uniform_ratio):
     out = np.zeros_like(z)
     _check(lib().oracle_density_query(1, _dptr(z), z.shape[0], uniform_ratio, _dptr(out)))
     return out
+
+
+def elastic_branches(reset=True):
+    """Elastic angle draws since the last reset, by branch: dict of gs,
+    wentzel, isotropic, single."""
+    out = np.zeros(4, dtype=np.uint64)
+    lib().oracle_elastic_branches(out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), int(bool(reset)))
+    return dict(zip(("gs", "wentzel", "isotropic", "single"), (int(v) for v in out)))
 
 
 def primitive(which, inputs, out_cols):

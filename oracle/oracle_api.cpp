@@ -324,6 +324,15 @@ void oracle_survivors(rrea_gpu_secondary* out)
     }
 }
 
+// Elastic angle draws by branch (GS, Wentzel-VI, isotropic, single
+// scatter) since the last reset; reset != 0 clears them after reading.
+void oracle_elastic_branches(uint64_t* out4, int reset)
+{
+    for (int k = 0; k < 4; ++k) {
+        out4[k] = reset ? oracle::g_elastic_branch[k].exchange(0) : oracle::g_elastic_branch[k].load();
+    }
+}
+
 void oracle_counts(int64_t* n_sec, int64_t* n_src, int64_t* n_seg)
 {
     *n_sec = static_cast<int64_t>(g_out.secondaries.size());

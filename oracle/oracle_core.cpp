@@ -9,6 +9,8 @@
 
 namespace oracle {
 
+std::atomic<uint64_t> g_elastic_branch[4] = {};
+
 namespace {
 
 using rrea_host::TableSet;
@@ -437,13 +439,18 @@ struct Tables {
         if (!std::isfinite(n) || n < ix.gs_few_collision_threshold) {
             fail(RREA_GPU_ERR_INVALID_STATE, "GS path n below the multiple-scattering branch");
         }
-        if (n >= ix.gs_isotropic_above_n) return 2.0 * u - 1.0;
+        if (n >= ix.gs_isotropic_above_n) {
+            g_elastic_branch[2].fetch_add(1, std::memory_order_relaxed);
+            return 2.0 * u - 1.0;
+        }
+        g_elastic_branch[use_gs ? 0 : 1].fetch_add(1, std::memory_order_relaxed);
         return sample_gs_angle(a, e, n, u);
     }
     // :2546-2560
     double SampleSingleElasticCosTheta(int species, double e, double cdf_u) const
     {
         require_charged(e);
+        g_elastic_branch[3].fetch_add(1, std::memory_order_relaxed);
         double const eta = ScreeningEta(species, e);
         double const u = std::min(std::max(cdf_u, 0.0), 1.0 - 1.0e-15);
         return 1.0 - 2.0 * eta * u / (1.0 + eta - u);

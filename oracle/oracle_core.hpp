@@ -10,6 +10,7 @@
 //   I/ = native_amrex_rrea/include/rrea/
 #pragma once
 
+#include <atomic>
 #include "../rrea_feedback_warpx_amrex_geant4_gb300/csrc/host/table_set.hpp"
 #include "../include/rrea_gpu.h"
 
@@ -267,6 +268,11 @@ double DensityRatioAtZ(double uniform_ratio, double z_m);
 // The step's fallback ratio: the ratio at the domain's axial centre, else
 // the configured ratio, else 1 (O/RreaParticleInteraction.cpp:27-35).
 double StepDensityRatio(rrea_gpu_config const& cfg);
+
+// Elastic angle draws by branch since the last reset: GS inverse CDF
+// (E <= the Wentzel transition), Wentzel-VI inverse CDF, the isotropic branch
+// (n >= isotropic_above_path_n) and single screened-Rutherford scatters.
+extern std::atomic<uint64_t> g_elastic_branch[4];
 
 // Primitive-level evaluation for fixture comparisons (ids listed in oracle_core.cpp).
 int RunPrimitive(rrea_host::TableSet const& tables, int which, double const* in, int64_t n, double* out);

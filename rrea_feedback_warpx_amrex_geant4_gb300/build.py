@@ -47,6 +47,29 @@ def _deps():
     return out
 
 
+# the sources that define the charged and photon transport kernels
+KERNEL_SOURCES = ("rrea_kernels.cu", "rrea_kernels.h", "rrea_photon_kernels.cu")
+
+
+def source_digest():
+    """SHA-256 (first 16 hex digits) over the sources that define the
+    transport kernels (the device headers and their translation units) and
+    the build flag that changes their code: the identity of a kernel build,
+    so a counter measured on one build is never applied to another."""
+    import hashlib
+
+    files = [os.path.join(CSRC, f) for f in KERNEL_SOURCES]
+    dev = os.path.join(CSRC, "device")
+    files += [os.path.join(dev, f) for f in os.listdir(dev)]
+    h = hashlib.sha256()
+    for path in sorted(files):
+        h.update(os.path.relpath(path, ROOT).encode())
+        with open(path, "rb") as f:
+            h.update(f.read())
+    h.update(("fmad=" + os.environ.get("RREA_FMAD", "1")).encode())
+    return h.hexdigest()[:16]
+
+
 def build(force=False, verbose=False):
     if not force and os.path.exists(LIB):
         t = os.path.getmtime(LIB)
