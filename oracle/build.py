@@ -15,7 +15,8 @@ SOURCES = [
 
 
 def build_oracle(force=False):
-    deps = SOURCES + [os.path.join(HERE, "oracle_core.hpp")]
+    deps = SOURCES + [os.path.join(HERE, "oracle_core.hpp"), os.path.join(HERE, "interleave.hpp"),
+                          os.path.join(HERE, "interleave_scenarios.hpp")]
     if not force and os.path.exists(LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps):

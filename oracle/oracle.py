@@ -81,6 +81,8 @@ def lib():
                                             ctypes.POINTER(RreaGpuTile)]
         _lib.oracle_counts.argtypes = [ctypes.POINTER(ctypes.c_int64)] * 3
         _lib.oracle_elastic_branches.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]
+        _lib.oracle_interleave_trace.argtypes = [ctypes.c_int, ctypes.c_uint64, d, ctypes.c_int64,
+                                                 ctypes.POINTER(ctypes.c_int64)]
         _lib.oracle_secondaries.argtypes = [ctypes.c_void_p]
         _lib.oracle_sources.argtypes = [d]
         _lib.oracle_segments.argtypes = [d]
@@ -149,6 +151,18 @@ def density_ratio_at_z(z_m, uniform_ratio):
     out = np.zeros_like(z)
     _check(lib().oracle_density_query(1, _dptr(z), z.shape[0], uniform_ratio, _dptr(out)))
     return out
+
+
+def interleave_trace(kind, seed):
+    """Trace (records of code, a, b, c) of scripted scenario `seed` through
+    the oracle's event (kind 0) or substep (kind 1) skeleton."""
+    cap = 4096
+    out = np.zeros((cap, 4))
+    n = ctypes.c_int64()
+    lib().oracle_interleave_trace(int(kind), int(seed), _dptr(out), cap, ctypes.byref(n))
+    if n.value > cap:
+        raise RuntimeError("scenario trace longer than its buffer")
+    return out[: n.value]
 
 
 def elastic_branches(reset=True):

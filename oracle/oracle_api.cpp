@@ -1,6 +1,8 @@
 // ORACLE — test infrastructure only.  C entry points of the CPU restatement
 // for ctypes (oracle/oracle.py).  Never linked into the shipped library.
 #include "oracle_core.hpp"
+#include "interleave.hpp"
+#include "interleave_scenarios.hpp"
 
 #include <cstring>
 #include <memory>
@@ -22,6 +24,22 @@ int guard(std::exception const& e)
     return RREA_GPU_ERR_TABLES;
 }
 
+}  // namespace
+
+namespace {
+// The oracle's restated skeletons behind the scenario runner.
+struct OracleSkeleton {
+    template <class... P>
+    static void events(double b, double e, double& k, double cut, int channels, uint64_t max_ordinal, P&&... p)
+    {
+        oracle::RunChargedEventInterleave(b, e, k, cut, channels, max_ordinal, "scenario", std::forward<P>(p)...);
+    }
+    template <class... P>
+    static void substeps(uint64_t n, double& k, double cut, uint64_t& completed, bool& exited, P&&... p)
+    {
+        oracle::RunChargedSubstepInterleave(n, k, cut, completed, exited, std::forward<P>(p)...);
+    }
+};
 }  // namespace
 
 extern "C" {
@@ -321,6 +339,22 @@ void oracle_survivors(rrea_gpu_secondary* out)
         o.weight = s.w;
         o.energy_eV = s.energy;
         o.birth_fraction = s.birth;
+    }
+}
+
+
+// Trace of scripted scenario `seed` through the oracle's event (kind 0) or
+// substep (kind 1) skeleton: records of {code, a, b, c}; *n receives the
+// record count (the trace is truncated to `cap` records).
+void oracle_interleave_trace(int kind, uint64_t seed, double* out, int64_t cap, int64_t* n)
+{
+    namespace is = interleave_scenarios;
+    is::Trace const t = kind == 0 ? is::run_event_scenario<OracleSkeleton>(is::event_scenario(seed))
+                                  : is::run_substep_scenario<OracleSkeleton>(is::substep_scenario(seed));
+    int64_t const records = static_cast<int64_t>(t.rec.size() / 4);
+    *n = records;
+    for (int64_t i = 0; i < records && i < cap; ++i) {
+        for (int j = 0; j < 4; ++j) out[4 * i + j] = t.rec[static_cast<std::size_t>(4 * i + j)];
     }
 }
 

@@ -1,5 +1,6 @@
 // ORACLE — test infrastructure only (see oracle_core.hpp).
 #include "oracle_core.hpp"
+#include "interleave.hpp"
 
 #include <map>
 
@@ -10,6 +11,8 @@
 namespace oracle {
 
 std::atomic<uint64_t> g_elastic_branch[4] = {};
+
+void interleave_abort(int code, std::string const& message) { fail(code, message); }
 
 namespace {
 
@@ -1784,17 +1787,19 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
         };
 
         // RreaRunChargedSubstepInterleave (O/RreaChargedInterleave.H:693-732)
-        for (uint64_t sub = 0; sub < subcycles; ++sub) {
-            if (k < cutoff) break;
-            double sb = 0.0, se = 0.0;
-            // build_substep (:535-598)
-            {
+        double sb = 0.0, se = 0.0;
+        uint64_t cur_sub = 0;
+        RunChargedSubstepInterleave(
+            subcycles, k, cutoff, completed, exited,
+            // build_substep (:535-598): chord, intervals, field sub-range, leading half kick
+            [&](uint64_t sub, double& b, double& e) {
+                cur_sub = sub;
                 Path np;
-                if (!build_chord(sub_dt, np)) break;
+                if (!build_chord(sub_dt, np)) return false;
                 path = np;
                 if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
                     exited = path.exits;
-                    break;
+                    return false;
                 }
                 iv = build_intervals(path, density_ratio, density_ratio);
                 if (iv.empty()) fail(RREA_GPU_ERR_INVALID_STATE, "microchord with no material intervals");
@@ -1804,107 +1809,100 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
                 }
                 sb = path.in_begin;
                 se = path.in_end;
+                b = sb;
+                e = se;
                 sub_field = path_field_work(gather, path, -1.0, sb, se);
                 sub_dt_eff = sub_dt * (se - sb);
                 half_kick(sub_field, 0.5 * sub_dt_eff, -1.0, k, dx, dy, dz);
-                if (k < cutoff) { mark_stopped(sb); break; }
-            }
+                if (k < cutoff) {
+                    mark_stopped(sb);
+                    return false;
+                }
+                return true;
+            },
             // run_events: RreaRunChargedEventInterleave (:546-664)
-            {
+            [&](uint64_t sub, double b, double e) {
                 std::array<double, 3> stp{};
                 uint64_t rng_index = 0;
                 double ex = 0, ey = 0, ez = 0, er = 0;
-                double rem = sb;
-                uint64_t ordinal = 0;
-                while (rem < se && k >= cutoff) {
-                    if (ordinal >= kEventCap) fail(RREA_GPU_ERR_RNG_OVERFLOW, "electron event ordinal overflow");
-                    double const frozen = k;
-                    stp = competing(frozen);
-                    double const seg_dp = density_path(iv, path, rem, se);
-                    std::array<double, 3> const taus = {stp[0] * seg_dp, stp[1] * seg_dp, 0.0};
-                    if (!try_live_hazard_index(0, sub, ordinal, rng_index)) {
-                        fail(RREA_GPU_ERR_RNG_OVERFLOW, "electron repeated-hazard RNG index overflow");
-                    }
-                    ++events;
-                    uint64_t const od_ch = ordinal == 0 ? kElectronCompetingOpticalDepth : kElectronContinuationOpticalDepth;
-                    uint64_t const cc_ch = ordinal == 0 ? kElectronCompetingChannel : kElectronContinuationChannel;
-                    double const u1 = rng_uniform(seed, key, step_key, rng_index, od_ch);
-                    double const u2 = rng_uniform(seed, key, step_key, rng_index, cc_ch);
-                    Selection const sel = select_hazard(taus, 2, u1, u2);
-                    double ev_frac = 0.0;
-                    bool split_valid = false;
-                    if (sel.valid && sel.event) {
-                        ev_frac = fraction_at_density_path(iv, path, rem, se, sel.sampled / (stp[0] + stp[1]));
-                        split_valid = std::isfinite(rem) && std::isfinite(ev_frac) && std::isfinite(se) && (se > rem)
-                            && !(ev_frac < rem) && !(ev_frac > se);
-                    }
-                    if (!sel.valid) fail(RREA_GPU_ERR_INVALID_STATE, "electron competing-hazard selection invalid");
-                    if (!sel.event) {
-                        Limit const l = continuous(rem, se, frozen);
-                        if (l.reaches) mark_stopped(l.end);
-                        break;
-                    }
-                    if (!split_valid) fail(RREA_GPU_ERR_INVALID_STATE, "sampled event depth outside its subcycle");
-                    path.PointAtFull(ev_frac, ex, ey, ez);
-                    er = std::hypot(ex, ey);
-                    Limit const l = continuous(rem, ev_frac, frozen);
-                    if (l.reaches) { mark_stopped(l.end); break; }
-                    bool const open_ev = k >= cutoff && channel_open(sel.channel, k);
-                    if (!open_ev) {
-                        bool const open_fr = frozen >= cutoff && channel_open(sel.channel, frozen);
-                        if (!open_fr) fail(RREA_GPU_ERR_INVALID_STATE, "selected channel closed before its event depth");
-                        rem = ev_frac;
-                        ++ordinal;
-                        continue;
-                    }
-                    double const birth = elapsed_at(ev_frac);
-                    if (sel.channel == 0) {
-                        // RreaApplyHardMollerFinalState (O/RreaChargedFinalStates.H:164-225)
-                        double const kb = k;
-                        double sec = tables.SampleMollerSecondaryEnergy(
-                            kb, rng_uniform(seed, key, step_key, rng_index, kHardMollerEnergy));
-                        sec = std::max(hm_thr, std::min(sec, 0.5 * kb));
-                        double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
-                        moller_lab_directions(dx, dy, dz, kb, sec,
-                                              rng_uniform(seed, key, step_key, rng_index, kHardMollerAzimuth), pdx,
-                                              pdy, pdz, sdx, sdy, sdz);
-                        k = std::max(0.0, kb - sec);
-                        dx = pdx; dy = pdy; dz = pdz;
-                        current_process = 2;  // HardMoller
-                        add_secondary(0, ex, ey, ez, sdx, sdy, sdz, sec, birth);
-                        push_source(0, er, ez, weight, sec, sec);
-                    } else if (sel.channel == 1) {
-                        // RreaApplyBremsFinalState (O/RreaChargedFinalStates.H:329-394)
-                        double const kb = k;
-                        double const eu = rng_uniform(seed, key, step_key, rng_index, kBremsEnergy);
-                        double const sampled = tables.SampleBremsstrahlungPhotonEnergy(kb, eu);
-                        // RreaClassifyBremsEnergyDisposition (O/RreaParticleInteraction.H:1552-1574)
-                        double const eg = std::min(std::max(sampled, 0.0), std::max(kb, 0.0));
-                        double const after = std::max(0.0, std::max(kb, 0.0) - eg);
-                        bool const tracked = std::isfinite(photon_cut) && photon_cut >= 0.0 && eg >= photon_cut;
-                        double gx = dx, gy = dy, gz = dz;
-                        double const ct = tables.SampleBremsstrahlungCosTheta(
-                            kb, rng_uniform(seed, key, step_key, rng_index, kBremsAngle));
-                        cone_direction(dx, dy, dz, ct, rng_uniform(seed, key, step_key, rng_index, kBremsAzimuth), gx,
-                                       gy, gz);
-                        photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
-                        k = after;
-                        current_process = 4;  // Bremsstrahlung
-                        if (tracked) {
-                            add_secondary(2, ex, ey, ez, gx, gy, gz, eg, birth);
-                        } else if (eg > 0.0) {
-                            deposit_local(er, ez, weight, eg);
+                RunChargedEventInterleave(
+                    b, e, k, cutoff, 2, kEventCap, "electron",
+                    [&](double frozen, double rb, double re) {
+                        stp = competing(frozen);
+                        double const seg_dp = density_path(iv, path, rb, re);
+                        return std::array<double, 3>{stp[0] * seg_dp, stp[1] * seg_dp, 0.0};
+                    },
+                    [&](uint64_t ordinal) {
+                        if (!try_live_hazard_index(0, sub, ordinal, rng_index)) {
+                            fail(RREA_GPU_ERR_RNG_OVERFLOW, "electron repeated-hazard RNG index overflow");
                         }
-                    }
-                    if (k <= cutoff) { mark_stopped(ev_frac); break; }
-                    rem = ev_frac;
-                    ++ordinal;
-                }
-            }
-            if (terminated_mid) break;
-            // finish_interleaved_substep (:502-524)
-            {
-                bool stop = false;
+                        ++events;
+                        uint64_t const od_ch =
+                            ordinal == 0 ? kElectronCompetingOpticalDepth : kElectronContinuationOpticalDepth;
+                        uint64_t const cc_ch = ordinal == 0 ? kElectronCompetingChannel : kElectronContinuationChannel;
+                        double const u1 = rng_uniform(seed, key, step_key, rng_index, od_ch);
+                        double const u2 = rng_uniform(seed, key, step_key, rng_index, cc_ch);
+                        return std::pair<double, double>{u1, u2};
+                    },
+                    [&](double tau, double rb, double re) {
+                        return fraction_at_density_path(iv, path, rb, re, tau / (stp[0] + stp[1]));
+                    },
+                    [&](double rb, double re, double frozen) {
+                        Limit const l = continuous(rb, re, frozen);
+                        return SegmentLimit{l.reaches, l.end};
+                    },
+                    [&](double f) { mark_stopped(f); },
+                    [&](double f) {
+                        path.PointAtFull(f, ex, ey, ez);
+                        er = std::hypot(ex, ey);
+                    },
+                    [&](int ch, double en) { return channel_open(ch, en); },
+                    [&](int channel, double ev_frac) {
+                        double const birth = elapsed_at(ev_frac);
+                        if (channel == 0) {
+                            // RreaApplyHardMollerFinalState (O/RreaChargedFinalStates.H:164-225)
+                            double const kb = k;
+                            double sec = tables.SampleMollerSecondaryEnergy(
+                                kb, rng_uniform(seed, key, step_key, rng_index, kHardMollerEnergy));
+                            sec = std::max(hm_thr, std::min(sec, 0.5 * kb));
+                            double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
+                            moller_lab_directions(dx, dy, dz, kb, sec,
+                                                  rng_uniform(seed, key, step_key, rng_index, kHardMollerAzimuth),
+                                                  pdx, pdy, pdz, sdx, sdy, sdz);
+                            k = std::max(0.0, kb - sec);
+                            dx = pdx; dy = pdy; dz = pdz;
+                            current_process = 2;  // HardMoller
+                            add_secondary(0, ex, ey, ez, sdx, sdy, sdz, sec, birth);
+                            push_source(0, er, ez, weight, sec, sec);
+                        } else if (channel == 1) {
+                            // RreaApplyBremsFinalState (O/RreaChargedFinalStates.H:329-394)
+                            double const kb = k;
+                            double const eu = rng_uniform(seed, key, step_key, rng_index, kBremsEnergy);
+                            double const sampled = tables.SampleBremsstrahlungPhotonEnergy(kb, eu);
+                            // RreaClassifyBremsEnergyDisposition (O/RreaParticleInteraction.H:1552-1574)
+                            double const eg = std::min(std::max(sampled, 0.0), std::max(kb, 0.0));
+                            double const after = std::max(0.0, std::max(kb, 0.0) - eg);
+                            bool const tracked = std::isfinite(photon_cut) && photon_cut >= 0.0 && eg >= photon_cut;
+                            double gx = dx, gy = dy, gz = dz;
+                            double const ct = tables.SampleBremsstrahlungCosTheta(
+                                kb, rng_uniform(seed, key, step_key, rng_index, kBremsAngle));
+                            cone_direction(dx, dy, dz, ct, rng_uniform(seed, key, step_key, rng_index, kBremsAzimuth),
+                                           gx, gy, gz);
+                            photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
+                            k = after;
+                            current_process = 4;  // Bremsstrahlung
+                            if (tracked) {
+                                add_secondary(2, ex, ey, ez, gx, gy, gz, eg, birth);
+                            } else if (eg > 0.0) {
+                                deposit_local(er, ez, weight, eg);
+                            }
+                        }
+                        return true;
+                    });
+            },
+            [&] { return terminated_mid; },
+            // finish_interleaved_substep (:502-524): elastic scatter, trailing half kick
+            [&](uint64_t sub, double, double) {
                 if (k >= cutoff) {
                     // apply_gs_elastic_scatter (O/RreaTransportStep.H:371-423)
                     double const mfp = tables.ElasticMeanFreePath(0, k, 1.0);
@@ -1935,13 +1933,16 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
                     }
                 }
                 half_kick(sub_field, 0.5 * sub_dt_eff, -1.0, k, dx, dy, dz);
-                if (k < cutoff) { mark_stopped(se); stop = true; }
-                if (stop) break;
-            }
-            if (!advance_running(path, se, rlo, rhi, zlo, zhi, run_x, run_y, run_z)) { exited = true; break; }
-            if (path.exits) { exited = true; break; }
-            completed = sub + 1U;
-        }
+                if (k < cutoff) {
+                    mark_stopped(se);
+                    return true;
+                }
+                return false;
+            },
+            // RreaAdvanceRunningChargedPosition (O/RreaParticleInteraction.H:368-392)
+            [&](double e) { return advance_running(path, e, rlo, rhi, zlo, zhi, run_x, run_y, run_z); },
+            [&] { return path.exits; });
+        (void)cur_sub;
         out_events[sp] = events;
         if (exited) {
             escape = clipped_escape_policy(path, std::hypot(path.ex, path.ey), path.ez);
@@ -2312,130 +2313,124 @@ void ApplyPositronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
             return Limit{plan.end, plan.reaches, true};
         };
 
-        for (uint64_t sub = 0; sub < subcycles; ++sub) {
-            if (k < cutoff) break;
-            double sb = 0.0, se = 0.0;
-            {
+        // RreaRunChargedSubstepInterleave (O/RreaChargedInterleave.H:693-732)
+        double sb = 0.0, se = 0.0;
+        RunChargedSubstepInterleave(
+            subcycles, k, cutoff, completed, exited,
+            [&](uint64_t, double& b, double& e) {
                 Path np;
-                if (!build_chord(sub_dt, np)) break;
+                if (!build_chord(sub_dt, np)) return false;
                 path = np;
                 if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
                     exited = path.exits;
-                    break;
+                    return false;
                 }
                 iv = build_intervals(path, density_ratio, density_ratio);
                 if (iv.empty()) fail(RREA_GPU_ERR_INVALID_STATE, "positron microchord with no material intervals");
                 sb = path.in_begin;
                 se = path.in_end;
+                b = sb;
+                e = se;
                 sub_field = path_field_work(gather, path, 1.0, sb, se);
                 sub_dt_eff = sub_dt * (se - sb);
                 half_kick(sub_field, 0.5 * sub_dt_eff, 1.0, k, dx, dy, dz);
-                if (k < cutoff) { mark_stopped(sb); break; }
-            }
-            {
+                if (k < cutoff) {
+                    mark_stopped(sb);
+                    return false;
+                }
+                return true;
+            },
+            // RreaRunChargedEventInterleave (:546-664) with three channels
+            [&](uint64_t sub, double b, double e) {
                 std::array<double, 3> stp{};
                 uint64_t rng_index = 0;
                 double ex = 0, ey = 0, ez = 0, er = 0;
-                double rem = sb;
-                uint64_t ordinal = 0;
-                while (rem < se && k >= cutoff) {
-                    if (ordinal >= kEventCap) fail(RREA_GPU_ERR_RNG_OVERFLOW, "positron event ordinal overflow");
-                    double const frozen = k;
-                    stp = competing(frozen);
-                    double const total_stp = stp[0] + stp[1] + stp[2];
-                    double const seg_dp = density_path(iv, path, rem, se);
-                    std::array<double, 3> const taus = {stp[0] * seg_dp, stp[1] * seg_dp, stp[2] * seg_dp};
-                    if (!try_live_hazard_index(1, sub, ordinal, rng_index)) {
-                        fail(RREA_GPU_ERR_RNG_OVERFLOW, "positron repeated-hazard RNG index overflow");
-                    }
-                    ++events;
-                    uint64_t const od_ch =
-                        ordinal == 0 ? kPositronCompetingOpticalDepth : kPositronContinuationOpticalDepth;
-                    uint64_t const cc_ch = ordinal == 0 ? kPositronCompetingChannel : kPositronContinuationChannel;
-                    double const u1 = rng_uniform(seed, key, step_key, rng_index, od_ch);
-                    double const u2 = rng_uniform(seed, key, step_key, rng_index, cc_ch);
-                    Selection const sel = select_hazard(taus, 3, u1, u2);
-                    double ev_frac = 0.0;
-                    bool split_valid = false;
-                    if (sel.valid && sel.event) {
-                        ev_frac = fraction_at_density_path(iv, path, rem, se, sel.sampled / total_stp);
-                        split_valid = std::isfinite(rem) && std::isfinite(ev_frac) && std::isfinite(se) && (se > rem)
-                            && !(ev_frac < rem) && !(ev_frac > se);
-                    }
-                    if (!sel.valid) fail(RREA_GPU_ERR_INVALID_STATE, "positron competing-hazard selection invalid");
-                    if (!sel.event) {
-                        Limit const l = continuous(rem, se, frozen);
-                        if (l.reaches) mark_stopped(l.end);
-                        break;
-                    }
-                    if (!split_valid) fail(RREA_GPU_ERR_INVALID_STATE, "sampled event depth outside its subcycle");
-                    path.PointAtFull(ev_frac, ex, ey, ez);
-                    er = std::hypot(ex, ey);
-                    Limit const l = continuous(rem, ev_frac, frozen);
-                    if (l.reaches) { mark_stopped(l.end); break; }
-                    bool const open_ev = k >= cutoff && channel_open(sel.channel, k);
-                    if (!open_ev) {
-                        bool const open_fr = frozen >= cutoff && channel_open(sel.channel, frozen);
-                        if (!open_fr) fail(RREA_GPU_ERR_INVALID_STATE, "selected channel closed before its event depth");
-                        rem = ev_frac;
-                        ++ordinal;
-                        continue;
-                    }
-                    double const birth = elapsed_at(ev_frac);
-                    if (sel.channel == 0) {
-                        // RreaApplyBhabhaFinalState (O/RreaChargedFinalStates.H:238-288)
-                        double const kb = k;
-                        double const sec = std::min(
-                            tables.SamplePositronBhabhaSecondaryEnergy(
-                                kb, rng_uniform(seed, key, step_key, rng_index, kPositronBhabhaEnergy)),
-                            std::max(0.0, kb));
-                        if (sec > 0.0 && !(hm_thr > 0.0 && sec < hm_thr)) {
-                            double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
-                            moller_lab_directions(dx, dy, dz, kb, sec,
-                                                  rng_uniform(seed, key, step_key, rng_index, kPositronBhabhaAzimuth),
-                                                  pdx, pdy, pdz, sdx, sdy, sdz);
-                            k = std::max(0.0, kb - sec);
-                            dx = pdx; dy = pdy; dz = pdz;
-                            current_process = 3;  // HardBhabha
-                            add_secondary(0, ex, ey, ez, sdx, sdy, sdz, sec, birth);
-                            push_source(2, er, ez, weight, 0.0, sec);
+                RunChargedEventInterleave(
+                    b, e, k, cutoff, 3, kEventCap, "positron",
+                    [&](double frozen, double rb, double re) {
+                        stp = competing(frozen);
+                        double const seg_dp = density_path(iv, path, rb, re);
+                        return std::array<double, 3>{stp[0] * seg_dp, stp[1] * seg_dp, stp[2] * seg_dp};
+                    },
+                    [&](uint64_t ordinal) {
+                        if (!try_live_hazard_index(1, sub, ordinal, rng_index)) {
+                            fail(RREA_GPU_ERR_RNG_OVERFLOW, "positron repeated-hazard RNG index overflow");
                         }
-                    } else if (sel.channel == 1) {
-                        // RreaApplyBremsFinalState, positron CDF (O/RreaChargedFinalStates.H:329-394)
-                        double const kb = k;
-                        double const eu = rng_uniform(seed, key, step_key, rng_index, kPositronBremsEnergy);
-                        double const sampled = tables.SamplePositronBremsstrahlungPhotonEnergy(kb, eu);
-                        double const eg = std::min(std::max(sampled, 0.0), std::max(kb, 0.0));
-                        double const after = std::max(0.0, std::max(kb, 0.0) - eg);
-                        bool const tracked = std::isfinite(photon_cut) && photon_cut >= 0.0 && eg >= photon_cut;
-                        double gx = dx, gy = dy, gz = dz;
-                        double const ct = tables.SampleBremsstrahlungCosTheta(
-                            kb, rng_uniform(seed, key, step_key, rng_index, kPositronBremsAngle));
-                        cone_direction(dx, dy, dz, ct,
-                                       rng_uniform(seed, key, step_key, rng_index, kPositronBremsAzimuth), gx, gy, gz);
-                        photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
-                        k = after;
-                        current_process = 4;  // Bremsstrahlung
-                        if (tracked) {
-                            add_secondary(2, ex, ey, ez, gx, gy, gz, eg, birth);
-                        } else if (eg > 0.0) {
-                            deposit_local(er, ez, weight, eg);
+                        ++events;
+                        uint64_t const od_ch =
+                            ordinal == 0 ? kPositronCompetingOpticalDepth : kPositronContinuationOpticalDepth;
+                        uint64_t const cc_ch = ordinal == 0 ? kPositronCompetingChannel : kPositronContinuationChannel;
+                        double const u1 = rng_uniform(seed, key, step_key, rng_index, od_ch);
+                        double const u2 = rng_uniform(seed, key, step_key, rng_index, cc_ch);
+                        return std::pair<double, double>{u1, u2};
+                    },
+                    [&](double tau, double rb, double re) {
+                        return fraction_at_density_path(iv, path, rb, re, tau / (stp[0] + stp[1] + stp[2]));
+                    },
+                    [&](double rb, double re, double frozen) {
+                        Limit const l = continuous(rb, re, frozen);
+                        return SegmentLimit{l.reaches, l.end};
+                    },
+                    [&](double f) { mark_stopped(f); },
+                    [&](double f) {
+                        path.PointAtFull(f, ex, ey, ez);
+                        er = std::hypot(ex, ey);
+                    },
+                    [&](int ch, double en) { return channel_open(ch, en); },
+                    [&](int channel, double ev_frac) {
+                        double const birth = elapsed_at(ev_frac);
+                        if (channel == 0) {
+                            // RreaApplyBhabhaFinalState (O/RreaChargedFinalStates.H:238-288)
+                            double const kb = k;
+                            double const sec = std::min(
+                                tables.SamplePositronBhabhaSecondaryEnergy(
+                                    kb, rng_uniform(seed, key, step_key, rng_index, kPositronBhabhaEnergy)),
+                                std::max(0.0, kb));
+                            if (sec > 0.0 && !(hm_thr > 0.0 && sec < hm_thr)) {
+                                double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
+                                moller_lab_directions(dx, dy, dz, kb, sec,
+                                                      rng_uniform(seed, key, step_key, rng_index, kPositronBhabhaAzimuth),
+                                                      pdx, pdy, pdz, sdx, sdy, sdz);
+                                k = std::max(0.0, kb - sec);
+                                dx = pdx; dy = pdy; dz = pdz;
+                                current_process = 3;  // HardBhabha
+                                add_secondary(0, ex, ey, ez, sdx, sdy, sdz, sec, birth);
+                                push_source(2, er, ez, weight, 0.0, sec);
+                            }
+                        } else if (channel == 1) {
+                            // RreaApplyBremsFinalState, positron CDF (O/RreaChargedFinalStates.H:329-394)
+                            double const kb = k;
+                            double const eu = rng_uniform(seed, key, step_key, rng_index, kPositronBremsEnergy);
+                            double const sampled = tables.SamplePositronBremsstrahlungPhotonEnergy(kb, eu);
+                            double const eg = std::min(std::max(sampled, 0.0), std::max(kb, 0.0));
+                            double const after = std::max(0.0, std::max(kb, 0.0) - eg);
+                            bool const tracked = std::isfinite(photon_cut) && photon_cut >= 0.0 && eg >= photon_cut;
+                            double gx = dx, gy = dy, gz = dz;
+                            double const ct = tables.SampleBremsstrahlungCosTheta(
+                                kb, rng_uniform(seed, key, step_key, rng_index, kPositronBremsAngle));
+                            cone_direction(dx, dy, dz, ct,
+                                           rng_uniform(seed, key, step_key, rng_index, kPositronBremsAzimuth), gx, gy, gz);
+                            photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
+                            k = after;
+                            current_process = 4;  // Bremsstrahlung
+                            if (tracked) {
+                                add_secondary(2, ex, ey, ez, gx, gy, gz, eg, birth);
+                            } else if (eg > 0.0) {
+                                deposit_local(er, ez, weight, eg);
+                            }
+                        } else {
+                            // in-flight annihilation (:700-727): the parent is consumed
+                            annihilate(ex, ey, ez, er, weight, k, false, rng_index, birth);
+                            push_segment(0, {r_particle, z_particle, er, ez, weight, 0.0, 0.0}, 4u, 0u);
+                            annihilated = true;
+                            return false;
                         }
-                    } else {
-                        // in-flight annihilation (:700-727)
-                        annihilate(ex, ey, ez, er, weight, k, false, rng_index, birth);
-                        push_segment(0, {r_particle, z_particle, er, ez, weight, 0.0, 0.0}, 4u, 0u);
-                        annihilated = true;
-                        break;
-                    }
-                    if (k <= cutoff) { mark_stopped(ev_frac); break; }
-                    rem = ev_frac;
-                    ++ordinal;
-                }
-            }
-            if (stopped || annihilated) break;
+                        return true;
+                    });
+            },
+            [&] { return stopped || annihilated; },
             // finish_interleaved_substep (:478-499)
-            {
+            [&](uint64_t sub, double, double) {
                 if (k >= cutoff) {
                     double const mfp = tables.ElasticMeanFreePath(1, k, 1.0);
                     double const gs_n = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0) * density_path(iv, path, sb, se);
@@ -2465,12 +2460,14 @@ void ApplyPositronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
                     }
                 }
                 half_kick(sub_field, 0.5 * sub_dt_eff, 1.0, k, dx, dy, dz);
-                if (k < cutoff) { mark_stopped(se); break; }
-            }
-            if (!advance_running(path, se, rlo, rhi, zlo, zhi, run_x, run_y, run_z)) { exited = true; break; }
-            if (path.exits) { exited = true; break; }
-            completed = sub + 1U;
-        }
+                if (k < cutoff) {
+                    mark_stopped(se);
+                    return true;
+                }
+                return false;
+            },
+            [&](double e) { return advance_running(path, e, rlo, rhi, zlo, zhi, run_x, run_y, run_z); },
+            [&] { return path.exits; });
         out.events[sp] = events;
         if (exited) {
             escape = clipped_escape_policy(path, std::hypot(path.ex, path.ey), path.ez);
@@ -2847,22 +2844,26 @@ bool advance_charged_newborn(NewbornContext const& c, Secondary& p, NewbornEffec
         return std::isfinite(out.full) && out.in_begin == 0.0;
     };
 
-    for (uint64_t sub = 0; sub < substeps; ++sub) {
-        if (k < cut) break;
-        double sb = 0.0, se = 0.0;
-        {
+    // RreaRunChargedSubstepInterleave (O/RreaChargedInterleave.H:693-732), as
+    // the reference's newborn advance runs it (O/RreaNewbornAdvance.cpp:440-640)
+    double sb = 0.0, se = 0.0;
+    RunChargedSubstepInterleave(
+        substeps, k, cut, completed, exited,
+        [&](uint64_t, double& b, double& e) {
             Path np;
-            if (!build_chord(np)) break;
+            if (!build_chord(np)) return false;
             path = np;
             if (!(path.full > 0.0) || !(path.in_length > 0.0)) {
                 exited = path.exits;
                 final_fraction = 0.0;
-                break;
+                return false;
             }
             iv = build_intervals(path, rho, rho);
             if (iv.empty()) fail(RREA_GPU_ERR_INVALID_STATE, "transient microchord has no material intervals");
             sb = path.in_begin;
             se = path.in_end;
+            b = sb;
+            e = se;
             final_fraction = se;
             sub_field = path_field_work(c.gather, path, q, sb, se);
             sub_dt_eff = sub_dt * (se - sb);
@@ -2870,171 +2871,145 @@ bool advance_charged_newborn(NewbornContext const& c, Secondary& p, NewbornEffec
             if (k < cut) {
                 final_fraction = sb;
                 terminal_at_point = true;
-                break;
+                return false;
             }
             require_certified();
-        }
-        {
-            double rem = sb;
-            uint64_t ordinal = 0;
-            while (rem < se && k >= cut) {
-                if (ordinal >= kEventCap) fail(RREA_GPU_ERR_RNG_OVERFLOW, "newborn event ordinal overflow");
-                double const frozen = k;
-                std::array<double, 3> const st = competing(frozen);
-                double const total_stp = st[0] + st[1] + st[2];
-                double const seg_dp = density_path(iv, path, rem, se);
-                std::array<double, 3> const taus = {st[0] * seg_dp, st[1] * seg_dp, st[2] * seg_dp};
-                uint64_t const idx = pack_newborn(p, sub, ordinal, 0);
-                double const u1 = rng_uniform(seed, key, step_key, idx, kNewbornCompetingOpticalDepth);
-                double const u2 = rng_uniform(seed, key, step_key, idx, kNewbornCompetingChannel);
-                Selection const sel = select_hazard(taus, pos ? 3 : 2, u1, u2);
-                double ev = 0.0;
-                bool split_valid = false;
-                if (sel.valid && sel.event) {
-                    ev = fraction_at_density_path(iv, path, rem, se, sel.sampled / total_stp);
-                    split_valid = std::isfinite(rem) && std::isfinite(ev) && std::isfinite(se) && (se > rem)
-                        && !(ev < rem) && !(ev > se);
-                }
-                if (!sel.valid) fail(RREA_GPU_ERR_INVALID_STATE, "newborn competing-hazard selection invalid");
-                if (!sel.event) {
-                    Limit const l = continuous(rem, se, frozen);
-                    if (l.reaches) {
-                        final_fraction = l.end;
-                        terminal_at_point = true;
-                    }
-                    break;
-                }
-                if (!split_valid) fail(RREA_GPU_ERR_INVALID_STATE, "newborn event depth outside its substep");
-                double ex2, ey2, ez2;
-                path.PointAtFull(ev, ex2, ey2, ez2);
-                double const er2 = std::hypot(ex2, ey2);
-                ez2 = path.WrapZ(ez2);
-                double const ev_elapsed = elapsed_at(ev);
-                Limit const l = continuous(rem, ev, frozen);
-                if (l.reaches) {
-                    final_fraction = l.end;
+            return true;
+        },
+        [&](uint64_t sub, double b, double e) {
+            double ex2 = 0, ey2 = 0, ez2 = 0, er2 = 0, ev_elapsed = 1.0;
+            uint64_t idx = 0;
+            std::array<double, 3> st{};
+            RunChargedEventInterleave(
+                b, e, k, cut, pos ? 3 : 2, kEventCap, pos ? "newborn positron" : "newborn electron",
+                [&](double frozen, double rb, double re) {
+                    st = competing(frozen);
+                    double const seg_dp = density_path(iv, path, rb, re);
+                    return std::array<double, 3>{st[0] * seg_dp, st[1] * seg_dp, st[2] * seg_dp};
+                },
+                [&](uint64_t ordinal) {
+                    idx = pack_newborn(p, sub, ordinal, 0);
+                    double const u1 = rng_uniform(seed, key, step_key, idx, kNewbornCompetingOpticalDepth);
+                    double const u2 = rng_uniform(seed, key, step_key, idx, kNewbornCompetingChannel);
+                    return std::pair<double, double>{u1, u2};
+                },
+                [&](double tau, double rb, double re) {
+                    return fraction_at_density_path(iv, path, rb, re, tau / (st[0] + st[1] + st[2]));
+                },
+                [&](double rb, double re, double frozen) {
+                    Limit const l = continuous(rb, re, frozen);
+                    return SegmentLimit{l.reaches, l.end};
+                },
+                [&](double f) {
+                    final_fraction = f;
                     terminal_at_point = true;
-                    break;
-                }
-                bool const open_ev = k >= cut && channel_open(sel.channel, k);
-                if (!open_ev) {
-                    bool const open_fr = frozen >= cut && channel_open(sel.channel, frozen);
-                    if (!open_fr) fail(RREA_GPU_ERR_INVALID_STATE, "selected channel closed before its event depth");
-                    rem = ev;
-                    ++ordinal;
-                    continue;
-                }
-                auto R = [&](uint64_t ch) { return rng_uniform(seed, key, step_key, idx, ch); };
-                if (sel.channel == 0 && !pos) {
-                    double const kb = k;
-                    double sec = tables.SampleMollerSecondaryEnergy(kb, R(kHardMollerEnergy));
-                    sec = std::max(thr, std::min(sec, 0.5 * kb));
-                    double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
-                    moller_lab_directions(dx, dy, dz, kb, sec, R(kHardMollerAzimuth), pdx, pdy, pdz, sdx, sdy, sdz);
-                    k = std::max(0.0, kb - sec);
-                    dx = pdx; dy = pdy; dz = pdz;
-                    current_process = 2;
-                    add_child(0, ex2, ey2, ez2, sdx, sdy, sdz, sec, ev_elapsed);
-                    push_source(0, er2, ez2, w, sec, sec);
-                } else if (sel.channel == 0) {
-                    double const kb = k;
-                    double const sec =
-                        std::min(tables.SamplePositronBhabhaSecondaryEnergy(kb, R(kPositronBhabhaEnergy)),
-                                 std::max(0.0, kb));
-                    if (sec > 0.0 && !(thr > 0.0 && sec < thr)) {
-                        double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
-                        moller_lab_directions(dx, dy, dz, kb, sec, R(kPositronBhabhaAzimuth), pdx, pdy, pdz, sdx,
-                                              sdy, sdz);
-                        k = std::max(0.0, kb - sec);
-                        dx = pdx; dy = pdy; dz = pdz;
-                        current_process = 3;
-                        add_child(0, ex2, ey2, ez2, sdx, sdy, sdz, sec, ev_elapsed);
-                        push_source(2, er2, ez2, w, 0.0, sec);
-                    }
-                } else if (sel.channel == 1) {
-                    double const kb = k;
-                    double const sampled = pos
-                        ? tables.SamplePositronBremsstrahlungPhotonEnergy(kb, R(kPositronBremsEnergy))
-                        : tables.SampleBremsstrahlungPhotonEnergy(kb, R(kBremsEnergy));
-                    double const eg = std::min(std::max(sampled, 0.0), std::max(kb, 0.0));
-                    double const after = std::max(0.0, std::max(kb, 0.0) - eg);
-                    bool const tracked = std::isfinite(photon_cut) && photon_cut >= 0.0 && eg >= photon_cut;
-                    double gx = dx, gy = dy, gz = dz;
-                    double const ct = tables.SampleBremsstrahlungCosTheta(kb, R(pos ? kPositronBremsAngle : kBremsAngle));
-                    cone_direction(dx, dy, dz, ct, R(pos ? kPositronBremsAzimuth : kBremsAzimuth), gx, gy, gz);
-                    photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
-                    k = after;
-                    current_process = 4;
-                    if (tracked) add_child(2, ex2, ey2, ez2, gx, gy, gz, eg, ev_elapsed);
-                    else if (eg > 0.0) deposit_local(er2, ez2, w, eg);
-                } else {
-                    annihilate(ex2, ey2, ez2, er2, k, false, idx, ev_elapsed);
-                    push_segment(er2, ez2);
-                    terminal_interaction = true;
-                    final_fraction = ev;
-                    break;
-                }
-                if (k <= cut) {
-                    final_fraction = ev;
-                    terminal_at_point = true;
-                    break;
-                }
-                rem = ev;
-                ++ordinal;
-            }
-        }
-        if (terminal_interaction || terminal_at_point) break;
-        {
-            if (k >= cut) {
-                double const mfp = tables.ElasticMeanFreePath(sp, k, 1.0);
-                double const gs_n = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0) * density_path(iv, path, sb, se);
-                if (gs_n > 0.0) {
-                    auto gkey = [&](uint64_t ch, uint64_t inner) {
-                        return rng_uniform(seed, key, step_key, pack_newborn(p, sub, 0, inner), ch);
-                    };
-                    auto deflect = [&](double ct, double uphi) {
-                        double nx, ny, nz;
-                        cone_direction(dx, dy, dz, ct, uphi, nx, ny, nz);
-                        dx = nx; dy = ny; dz = nz;
-                    };
-                    double const few = c.ts.index().gs_few_collision_threshold;
-                    if (gs_n < few) {
-                        int const cap = static_cast<int>(std::ceil(3.0 * few));
-                        if (cap >= 255) fail(RREA_GPU_ERR_INVALID_STATE, "GS few-collision cap too large");
-                        int const cnt =
-                            poisson_capped(gs_n, gkey(pos ? kNewbornPositronGsFewCount : kNewbornElectronGsFewCount, 0),
-                                           cap);
-                        for (int qq = 0; qq < cnt; ++qq) {
-                            uint64_t const inner = static_cast<uint64_t>(qq + 1);
-                            double const ct = tables.SampleSingleElasticCosTheta(
-                                sp, k, gkey(pos ? kNewbornPositronGsFewScatter : kNewbornElectronGsFewScatter, inner));
-                            deflect(ct, gkey(pos ? kNewbornPositronGsFewAzimuth : kNewbornElectronGsFewAzimuth, inner));
-                        }
+                },
+                [&](double f) {
+                    path.PointAtFull(f, ex2, ey2, ez2);
+                    er2 = std::hypot(ex2, ey2);
+                    ez2 = path.WrapZ(ez2);
+                    ev_elapsed = elapsed_at(f);
+                },
+                [&](int ch, double en) { return channel_open(ch, en); },
+                [&](int channel, double ev) {
+                        auto R = [&](uint64_t ch) { return rng_uniform(seed, key, step_key, idx, ch); };
+                        if (channel == 0 && !pos) {
+                            double const kb = k;
+                            double sec = tables.SampleMollerSecondaryEnergy(kb, R(kHardMollerEnergy));
+                            sec = std::max(thr, std::min(sec, 0.5 * kb));
+                            double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
+                            moller_lab_directions(dx, dy, dz, kb, sec, R(kHardMollerAzimuth), pdx, pdy, pdz, sdx, sdy, sdz);
+                            k = std::max(0.0, kb - sec);
+                            dx = pdx; dy = pdy; dz = pdz;
+                            current_process = 2;
+                            add_child(0, ex2, ey2, ez2, sdx, sdy, sdz, sec, ev_elapsed);
+                            push_source(0, er2, ez2, w, sec, sec);
+                        } else if (channel == 0) {
+                            double const kb = k;
+                            double const sec =
+                                std::min(tables.SamplePositronBhabhaSecondaryEnergy(kb, R(kPositronBhabhaEnergy)),
+                                         std::max(0.0, kb));
+                            if (sec > 0.0 && !(thr > 0.0 && sec < thr)) {
+                                double pdx = dx, pdy = dy, pdz = dz, sdx = dx, sdy = dy, sdz = dz;
+                                moller_lab_directions(dx, dy, dz, kb, sec, R(kPositronBhabhaAzimuth), pdx, pdy, pdz, sdx,
+                                                      sdy, sdz);
+                                k = std::max(0.0, kb - sec);
+                                dx = pdx; dy = pdy; dz = pdz;
+                                current_process = 3;
+                                add_child(0, ex2, ey2, ez2, sdx, sdy, sdz, sec, ev_elapsed);
+                                push_source(2, er2, ez2, w, 0.0, sec);
+                            }
+                        } else if (channel == 1) {
+                            double const kb = k;
+                            double const sampled = pos
+                                ? tables.SamplePositronBremsstrahlungPhotonEnergy(kb, R(kPositronBremsEnergy))
+                                : tables.SampleBremsstrahlungPhotonEnergy(kb, R(kBremsEnergy));
+                            double const eg = std::min(std::max(sampled, 0.0), std::max(kb, 0.0));
+                            double const after = std::max(0.0, std::max(kb, 0.0) - eg);
+                            bool const tracked = std::isfinite(photon_cut) && photon_cut >= 0.0 && eg >= photon_cut;
+                            double gx = dx, gy = dy, gz = dz;
+                            double const ct = tables.SampleBremsstrahlungCosTheta(kb, R(pos ? kPositronBremsAngle : kBremsAngle));
+                            cone_direction(dx, dy, dz, ct, R(pos ? kPositronBremsAzimuth : kBremsAzimuth), gx, gy, gz);
+                            photon_recoil(kb, eg, gx, gy, gz, dx, dy, dz);
+                            k = after;
+                            current_process = 4;
+                            if (tracked) add_child(2, ex2, ey2, ez2, gx, gy, gz, eg, ev_elapsed);
+                            else if (eg > 0.0) deposit_local(er2, ez2, w, eg);
                     } else {
-                        double const ct = tables.SampleGsCosTheta(
-                            sp, k, gs_n, gkey(pos ? kNewbornPositronGsAngle : kNewbornElectronGsAngle, 0));
-                        deflect(ct, gkey(pos ? kNewbornPositronGsAzimuth : kNewbornElectronGsAzimuth, 0));
+                        annihilate(ex2, ey2, ez2, er2, k, false, idx, ev_elapsed);
+                        push_segment(er2, ez2);
+                        terminal_interaction = true;
+                        final_fraction = ev;
+                        return false;
+                    }
+                    return true;
+                });
+        },
+        [&] { return terminal_interaction || terminal_at_point; },
+        [&](uint64_t sub, double, double) {
+                if (k >= cut) {
+                    double const mfp = tables.ElasticMeanFreePath(sp, k, 1.0);
+                    double const gs_n = frozen_rate(mfp > 0.0 ? 1.0 / mfp : 0.0) * density_path(iv, path, sb, se);
+                    if (gs_n > 0.0) {
+                        auto gkey = [&](uint64_t ch, uint64_t inner) {
+                            return rng_uniform(seed, key, step_key, pack_newborn(p, sub, 0, inner), ch);
+                        };
+                        auto deflect = [&](double ct, double uphi) {
+                            double nx, ny, nz;
+                            cone_direction(dx, dy, dz, ct, uphi, nx, ny, nz);
+                            dx = nx; dy = ny; dz = nz;
+                        };
+                        double const few = c.ts.index().gs_few_collision_threshold;
+                        if (gs_n < few) {
+                            int const cap = static_cast<int>(std::ceil(3.0 * few));
+                            if (cap >= 255) fail(RREA_GPU_ERR_INVALID_STATE, "GS few-collision cap too large");
+                            int const cnt =
+                                poisson_capped(gs_n, gkey(pos ? kNewbornPositronGsFewCount : kNewbornElectronGsFewCount, 0),
+                                               cap);
+                            for (int qq = 0; qq < cnt; ++qq) {
+                                uint64_t const inner = static_cast<uint64_t>(qq + 1);
+                                double const ct = tables.SampleSingleElasticCosTheta(
+                                    sp, k, gkey(pos ? kNewbornPositronGsFewScatter : kNewbornElectronGsFewScatter, inner));
+                                deflect(ct, gkey(pos ? kNewbornPositronGsFewAzimuth : kNewbornElectronGsFewAzimuth, inner));
+                            }
+                        } else {
+                            double const ct = tables.SampleGsCosTheta(
+                                sp, k, gs_n, gkey(pos ? kNewbornPositronGsAngle : kNewbornElectronGsAngle, 0));
+                            deflect(ct, gkey(pos ? kNewbornPositronGsAzimuth : kNewbornElectronGsAzimuth, 0));
+                        }
                     }
                 }
-            }
             half_kick(sub_field, 0.5 * sub_dt_eff, q, k, dx, dy, dz);
             if (k < cut) {
                 final_fraction = se;
                 terminal_at_point = true;
-                break;
+                return true;
             }
             require_certified();
-        }
-        if (!advance_running(path, se, rlo, rhi, zlo, zhi, run_x, run_y, run_z)) {
-            exited = true;
-            break;
-        }
-        if (path.exits) {
-            exited = true;
-            break;
-        }
-        completed = sub + 1U;
-    }
+            return false;
+        },
+        [&](double e) { return advance_running(path, e, rlo, rhi, zlo, zhi, run_x, run_y, run_z); },
+        [&] { return path.exits; });
     if (terminal_interaction) return false;
     double fx_, fy_, fz_;
     if (!newborn_final_point(path, final_fraction, cfg, fx_, fy_, fz_)) {

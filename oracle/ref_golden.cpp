@@ -6,6 +6,7 @@
 // restatement (oracle/oracle_core.cpp) and the device kernels to the
 // reference's arithmetic.  Test infrastructure only.
 #include "RreaChargedInterleave.H"
+#include "interleave_scenarios.hpp"
 #include "RreaParticleInteraction.H"
 #include "RreaRng.H"
 #include "rrea/RreaAltitudeProfile.H"
@@ -90,6 +91,21 @@ std::vector<double> charged_energies(Gen& g, rrea::RreaInteractionTables const& 
     for (int i = 0; i < n_random; ++i) e.push_back(g.logu(1.0e3, 1.0e10));
     return e;
 }
+
+// The reference's own charged-loop skeletons behind the scenario runner.
+struct RefSkeleton {
+    template <class... P>
+    static void events(double b, double e, double& k, double cut, int channels, uint64_t max_ordinal, P&&... p)
+    {
+        rrea::warpx::RreaRunChargedEventInterleave(b, e, k, cut, channels, max_ordinal, "scenario",
+                                                   std::forward<P>(p)...);
+    }
+    template <class... P>
+    static void substeps(uint64_t n, double& k, double cut, uint64_t& completed, bool& exited, P&&... p)
+    {
+        rrea::warpx::RreaRunChargedSubstepInterleave(n, k, cut, completed, exited, std::forward<P>(p)...);
+    }
+};
 
 }  // namespace
 
@@ -662,6 +678,26 @@ int main(int argc, char** argv)
             }
             write_f8("ref_cic_thin_particles", 5, parts);
             write_f8("ref_cic_thin_groups", 8, groups);
+        }
+        // ---- charged-loop skeletons: O/RreaChargedInterleave.H:546-732 driven by
+        // scripted policies (oracle/interleave_scenarios.hpp)
+        {
+            namespace is = interleave_scenarios;
+            std::vector<double> ev, sub;
+            for (uint64_t seed = 0; seed < 400; ++seed) {
+                is::Trace const t = is::run_event_scenario<RefSkeleton>(is::event_scenario(seed));
+                for (std::size_t i = 0; i < t.rec.size(); i += 4) {
+                    ev.insert(ev.end(), {static_cast<double>(seed), t.rec[i], t.rec[i + 1], t.rec[i + 2], t.rec[i + 3]});
+                }
+            }
+            for (uint64_t seed = 0; seed < 300; ++seed) {
+                is::Trace const t = is::run_substep_scenario<RefSkeleton>(is::substep_scenario(seed));
+                for (std::size_t i = 0; i < t.rec.size(); i += 4) {
+                    sub.insert(sub.end(), {static_cast<double>(seed), t.rec[i], t.rec[i + 1], t.rec[i + 2], t.rec[i + 3]});
+                }
+            }
+            write_f8("ref_interleave_events", 5, ev);
+            write_f8("ref_interleave_substeps", 5, sub);
         }
         std::printf("golden fixtures written to %s\n", g_outdir.c_str());
     } catch (std::exception const& e) {
