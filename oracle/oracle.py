@@ -81,6 +81,7 @@ def lib():
                                             ctypes.POINTER(RreaGpuTile)]
         _lib.oracle_counts.argtypes = [ctypes.POINTER(ctypes.c_int64)] * 3
         _lib.oracle_elastic_branches.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]
+        _lib.oracle_photon_flow.argtypes = [d, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]
         _lib.oracle_interleave_trace.argtypes = [ctypes.c_int, ctypes.c_uint64, d, ctypes.c_int64,
                                                  ctypes.POINTER(ctypes.c_int64)]
         _lib.oracle_secondaries.argtypes = [ctypes.c_void_p]
@@ -163,6 +164,15 @@ def interleave_trace(kind, seed):
     if n.value > cap:
         raise RuntimeError("scenario trace longer than its buffer")
     return out[: n.value]
+
+
+def photon_flow_valid(rows):
+    """The photon energy-flow ledger check on rows of (kind, weight,
+    incident, x1, x2, x3, has_recoil, local); returns a bool per row."""
+    rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 8)
+    ok = np.zeros(rows.shape[0], dtype=np.int32)
+    lib().oracle_photon_flow(_dptr(rows), rows.shape[0], ok.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    return ok.astype(bool)
 
 
 def elastic_branches(reset=True):

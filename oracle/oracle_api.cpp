@@ -358,6 +358,16 @@ void oracle_interleave_trace(int kind, uint64_t seed, double* out, int64_t cap, 
     }
 }
 
+// The photon energy-flow check on n rows of {kind, w, incident, x1, x2, x3,
+// has_recoil, local}; ok[i] = 1 where the row passes.
+void oracle_photon_flow(double const* rows, int64_t n, int32_t* ok)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        double const* r = rows + 8 * i;
+        ok[i] = oracle::PhotonFlowValid(static_cast<int>(r[0]), r[1], r[2], r[3], r[4], r[5], r[6] != 0.0, r[7]) ? 1 : 0;
+    }
+}
+
 // Elastic angle draws by branch (GS, Wentzel-VI, isotropic, single
 // scatter) since the last reset; reset != 0 clears them after reading.
 void oracle_elastic_branches(uint64_t* out4, int reset)

@@ -14,6 +14,29 @@ std::atomic<uint64_t> g_elastic_branch[4] = {};
 
 void interleave_abort(int code, std::string const& message) { fail(code, message); }
 
+// Photon energy-flow ledger checks of DrainAndCommitSecondaries
+// (O/RreaSecondaryCommit.cpp:55-160) on one Compton (kind 0), photoelectric
+// (kind 1) or pair (kind 2) interaction: a finite, non-negative payload whose
+// parts add up to the incident energy, and a booked local flow equal to the
+// split RreaComptonPhotonEnergyFlow / RreaPhotoelectricPhotonEnergyFlow /
+// RreaPairPhotonEnergyFlow (O/RreaParticleInteraction.H:1015-1090) recomputes
+// from the recorded energies, within 64 eps of the incident energy.
+//   Compton: x1 = recoil, x2 = scattered; photoelectric: x1 = electron,
+//   x2 = binding; pair: x1 = electron, x2 = positron, x3 = recoil.
+bool PhotonFlowValid(int kind, double w, double inc, double x1, double x2, double x3, bool has_recoil, double local)
+{
+    double const eps64 = 64.0 * std::numeric_limits<double>::epsilon();
+    auto matches = [&](double actual, double expected) {
+        return std::isfinite(actual) && actual >= 0.0 && std::abs(actual - expected) <= eps64 * std::max(inc, 1.0);
+    };
+    if (!(std::isfinite(w) && std::isfinite(inc) && w > 0.0 && inc > 0.0)) return false;
+    if (!(std::isfinite(x1) && std::isfinite(x2) && x1 >= 0.0 && x2 >= 0.0)) return false;
+    if (kind == 0 || kind == 1) return matches(x1 + x2, inc);
+    if (!(std::isfinite(x3) && x3 >= 0.0)) return false;
+    double const expected = std::max(inc - 2.0 * kMeC2 - x1 - x2 - (has_recoil ? x3 : 0.0), 0.0);
+    return matches(std::max(local, 0.0), expected);
+}
+
 namespace {
 
 using rrea_host::TableSet;
@@ -3147,6 +3170,9 @@ bool advance_photon_newborn(NewbornContext const& c, Secondary& p, NewbornEffect
                 push_source(0, pr, pz, w, cs.recoil, 0.0);
                 deposit_local(pr, pz, w, cs.recoil);
             }
+            if (!PhotonFlowValid(0, w, inc, cs.recoil, cs.scattered, 0.0, false, 0.0)) {
+                fail(RREA_GPU_ERR_INVALID_STATE, "newborn Compton photon energy flow does not close");
+            }
             energy = cs.scattered;
             if (energy < photon_cut) {
                 deposit_local(pr, pz, w, energy);
@@ -3182,6 +3208,9 @@ bool advance_photon_newborn(NewbornContext const& c, Secondary& p, NewbornEffect
                 deposit_local(pr, pz, w, ee);
             }
             if (bind > 0.0) deposit_local(pr, pz, w, bind);
+            if (!PhotonFlowValid(1, w, energy, ee, std::max(bind, 0.0), 0.0, false, 0.0)) {
+                fail(RREA_GPU_ERR_INVALID_STATE, "newborn photoelectric photon energy flow does not close");
+            }
             return false;
         }
         bool const triplet = channel == 3;
@@ -3215,6 +3244,9 @@ bool advance_photon_newborn(NewbornContext const& c, Secondary& p, NewbornEffect
             if (ps.e_recoil < cut) deposit_local(pr, pz, w, ps.e_recoil);
         }
         if (ps.local > 0.0) deposit_local(pr, pz, w, ps.local);
+        if (!PhotonFlowValid(2, w, energy, ps.e_electron, ps.e_positron, ps.e_recoil, ps.recoil, ps.local)) {
+            fail(RREA_GPU_ERR_INVALID_STATE, "newborn pair photon energy flow does not close");
+        }
         return false;
     }
 }
@@ -3466,6 +3498,9 @@ void ApplyPhotonTransport(TableSet const& ts, rrea_gpu_config const& cfg, int st
                     push_source(0, pr, pz, weight, cs.recoil, 0.0);
                     deposit_local_at(pr, pz, weight, cs.recoil);
                 }
+                if (!PhotonFlowValid(0, weight, inc, cs.recoil, cs.scattered, 0.0, false, 0.0)) {
+                    fail(RREA_GPU_ERR_INVALID_STATE, "Compton photon energy flow does not close");
+                }
                 energy = cs.scattered;
                 if (energy < photon_cut) {
                     deposit_local_at(pr, pz, weight, energy);
@@ -3503,6 +3538,9 @@ void ApplyPhotonTransport(TableSet const& ts, rrea_gpu_config const& cfg, int st
                     deposit_local_at(pr, pz, weight, ee);
                 }
                 if (bind > 0.0) deposit_local_at(pr, pz, weight, bind);
+                if (!PhotonFlowValid(1, weight, energy, ee, std::max(bind, 0.0), 0.0, false, 0.0)) {
+                    fail(RREA_GPU_ERR_INVALID_STATE, "photoelectric photon energy flow does not close");
+                }
                 tile.id[ip] = -tile.id[ip];
                 disp = 2;
             } else {
@@ -3549,6 +3587,9 @@ void ApplyPhotonTransport(TableSet const& ts, rrea_gpu_config const& cfg, int st
                     if (ps.e_recoil < cutoff) deposit_local_at(pr, pz, weight, ps.e_recoil);
                 }
                 if (ps.local > 0.0) deposit_local_at(pr, pz, weight, ps.local);
+                if (!PhotonFlowValid(2, weight, energy, ps.e_electron, ps.e_positron, ps.e_recoil, ps.recoil, ps.local)) {
+                    fail(RREA_GPU_ERR_INVALID_STATE, "pair photon energy flow does not close");
+                }
                 tile.id[ip] = -tile.id[ip];
                 disp = 2;
             }

@@ -274,6 +274,9 @@ double StepDensityRatio(rrea_gpu_config const& cfg);
 // (n >= isotropic_above_path_n) and single screened-Rutherford scatters.
 extern std::atomic<uint64_t> g_elastic_branch[4];
 
+// Photon energy-flow ledger check of one interaction (oracle_core.cpp).
+bool PhotonFlowValid(int kind, double w, double inc, double x1, double x2, double x3, bool has_recoil, double local);
+
 // Primitive-level evaluation for fixture comparisons (ids listed in oracle_core.cpp).
 int RunPrimitive(rrea_host::TableSet const& tables, int which, double const* in, int64_t n, double* out);
 

@@ -1,6 +1,11 @@
 """Builds the GB300 kinetic-step library in-tree:
 rrea_feedback_warpx_amrex_geant4_gb300/lib/librrea_gpu.so (sm_103a only).
 
+Parity-study variants (RREA_LIBM=1: CUDA's log/exp in place of the
+table-driven ones; RREA_FMAD=0, below) build into the path RREA_GPU_LIB
+names, with their own object directory, and the bindings load from there
+when RREA_GPU_LIB is set; the default build is the product.
+
 FP64 FMA contraction is on (--fmad=true): GB300's FP64 pipe issues a fused
 multiply-add for the price of a multiply, a measured 9 % of the electron
 kernel.  RREA_FMAD=0 builds with --fmad=false, whose products and sums round
@@ -15,7 +20,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
-LIB = os.path.join(LIBDIR, "librrea_gpu.so")
+LIB = os.environ.get("RREA_GPU_LIB") or os.path.join(LIBDIR, "librrea_gpu.so")
 
 SOURCES = [
     os.path.join(CSRC, "rrea_capi.cu"),
@@ -67,6 +72,7 @@ def source_digest():
         with open(path, "rb") as f:
             h.update(f.read())
     h.update(("fmad=" + os.environ.get("RREA_FMAD", "1")).encode())
+    h.update(("libm=" + os.environ.get("RREA_LIBM", "0")).encode())
     return h.hexdigest()[:16]
 
 
@@ -75,13 +81,16 @@ def build(force=False, verbose=False):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in _deps()):
             return LIB
-    os.makedirs(LIBDIR, exist_ok=True)
-    objdir = os.path.join(PKG, "_build")
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    variant = f"fmad{os.environ.get('RREA_FMAD', '1')}_libm{os.environ.get('RREA_LIBM', '0')}"
+    objdir = os.path.join(PKG, "_build" if variant == "fmad1_libm0" else "_build_" + variant)
     os.makedirs(objdir, exist_ok=True)
     nvcc = _nvcc()
     fmad = "false" if os.environ.get("RREA_FMAD", "1") == "0" else "true"
     common = ["-std=c++17", "-O3", "-lineinfo", f"--fmad={fmad}", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I", CSRC, "-I", os.path.join(ROOT, "include")] + ARCH
+    if os.environ.get("RREA_LIBM", "0") == "1":
+        common += ["-DRREA_CUDA_LIBM"]
     if verbose:
         common += ["-Xptxas", "-v"]
     objs = []

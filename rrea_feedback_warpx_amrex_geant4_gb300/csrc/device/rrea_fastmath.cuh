@@ -29,6 +29,11 @@ constexpr double kLn2Lo = 2.31904681384629955842e-17;   // RN(ln 2 - kLn2Hi)
 
 __device__ __forceinline__ double flog(const double* __restrict__ arena, double x)
 {
+#ifdef RREA_CUDA_LIBM
+    // parity-study build: CUDA's logarithm everywhere
+    (void)arena;
+    return log(x);
+#endif
     long long const bits = __double_as_longlong(x);
     // normal, positive and finite: sign clear, biased exponent in [1, 2046]
     if (bits < 0x0010000000000000LL || bits >= 0x7ff0000000000000LL) return log(x);
@@ -61,6 +66,11 @@ constexpr double kLn2by128Lo = 1.81175532331742157843e-19;  // RN(ln 2 / 128 - k
 
 __device__ __forceinline__ double fexp(const double* __restrict__ arena, double x)
 {
+#ifdef RREA_CUDA_LIBM
+    // parity-study build: CUDA's exponential everywhere
+    (void)arena;
+    return exp(x);
+#endif
     if (!(fabs(x) < 700.0)) return exp(x);
     double const kf = rint(x * kInvLn2x128);
     int const k = static_cast<int>(kf);

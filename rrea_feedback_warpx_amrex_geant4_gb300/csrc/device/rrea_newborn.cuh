@@ -660,6 +660,10 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
                 deposit_source(C, A.cells, 0, pr, pz, w, cs.recoil, 0.0);
                 deposit_local(pr, pz, cs.recoil);
             }
+            if (!compton_flow_valid(w, inc, cs.recoil, cs.scattered)) {
+                err.set(RREA_GPU_ERR_INVALID_STATE);
+                return -1;
+            }
             energy = cs.scattered;
             {
                 // closure of the Compton group
@@ -713,6 +717,10 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
                 deposit_local(pr, pz, ee);
             }
             if (gt0(bind)) deposit_local(pr, pz, bind);
+            if (!photoelectric_flow_valid(w, energy, ee, fmax(bind, 0.0))) {
+                err.set(RREA_GPU_ERR_INVALID_STATE);
+                return -1;
+            }
             GroupClosure gc;  // closure of the Photoelectric group
             gc.begin(0.0, 0.0, w, energy, 0.0, false);
             if (ee >= cut) gc.secondary(-1.0, kMeC2, w, ee);
@@ -758,7 +766,8 @@ __device__ int advance_photon_newborn(StepConstants const& C, ElectronArgs const
             if (ps.e_recoil < cut) deposit_local(pr, pz, ps.e_recoil);
         }
         if (gt0(ps.local)) deposit_local(pr, pz, ps.local);
-        if (!pair_closure_valid(ps, w, energy, cut, photon_cut, w_air)) {
+        if (!pair_flow_valid(w, energy, ps.e_electron, ps.e_positron, ps.e_recoil, ps.recoil, ps.local)
+            || !pair_closure_valid(ps, w, energy, cut, photon_cut, w_air)) {
             err.set(RREA_GPU_ERR_INVALID_STATE);
             return -1;
         }

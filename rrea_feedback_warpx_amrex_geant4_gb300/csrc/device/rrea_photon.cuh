@@ -293,6 +293,53 @@ __device__ __forceinline__ double* pair_largest(PairState& st)
     if (st.e_recoil > *l) l = &st.e_recoil;
     return l;
 }
+// Photon energy-flow ledger checks of the commit (O/RreaSecondaryCommit.cpp:55-160):
+// every Compton, photoelectric and pair record must carry a finite,
+// non-negative payload whose parts add up to the incident photon energy
+// within 64 eps of it, and whose split into charged (kinetic + created rest
+// mass) and local (recoil, binding, sub-cutoff) flows
+// (RreaComptonPhotonEnergyFlow, RreaPhotoelectricPhotonEnergyFlow,
+// RreaPairPhotonEnergyFlow, O/RreaParticleInteraction.H:1015-1090) matches
+// the split recomputed from the recorded energies.  A mismatch fails the
+// step closed, as the reference's transaction validation does.
+__device__ __forceinline__ bool photon_flow_matches(double actual, double expected, double scale)
+{
+    return finite_bits(actual) && ge0(actual) && fabs(actual - expected) <= 64.0 * kEps * fmax(scale, 1.0);
+}
+
+__device__ __forceinline__ bool photon_payload_ok(double w, double inc)
+{
+    return finite_bits(w) && finite_bits(inc) && gt0(w) && gt0(inc);
+}
+
+// Compton: recoil electron + scattered photon = incident.
+__device__ __forceinline__ bool compton_flow_valid(double w, double inc, double recoil, double scattered)
+{
+    return photon_payload_ok(w, inc) && finite_bits(recoil) && ge0(recoil) && finite_bits(scattered)
+        && ge0(scattered) && photon_flow_matches(recoil + scattered, inc, inc);
+}
+
+// Photoelectric: photoelectron + binding = incident.
+__device__ __forceinline__ bool photoelectric_flow_valid(double w, double inc, double electron, double binding)
+{
+    return photon_payload_ok(w, inc) && finite_bits(electron) && ge0(electron) && finite_bits(binding)
+        && ge0(binding) && photon_flow_matches(electron + binding, inc, inc);
+}
+
+// Pair: the local flow the final state booked equals the incident energy
+// left after the two rest masses and the kinetic energies (the triplet
+// recoil's included), floored at zero.
+__device__ __forceinline__ bool pair_flow_valid(double w, double inc, double electron, double positron,
+                                                double recoil, bool has_recoil, double local)
+{
+    if (!(photon_payload_ok(w, inc) && finite_bits(electron) && finite_bits(positron) && finite_bits(recoil)
+          && ge0(electron) && ge0(positron) && ge0(recoil))) {
+        return false;
+    }
+    double const expected = fmax(inc - 2.0 * kMeC2 - electron - positron - (has_recoil ? recoil : 0.0), 0.0);
+    return photon_flow_matches(fmax(local, 0.0), expected, inc);
+}
+
 // Closure of the PairNuclear / PairTriplet group (O/RreaPhotonFinalStates.H:278-364):
 // a sub-cutoff positron annihilates at rest into two m_e c^2 photons beside a
 // positive ion, inside the same group.
@@ -611,6 +658,10 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
                 deposit_source(C, A.cells, 0, pr, pz, weight, cs.recoil, 0.0);
                 deposit_local_at(pr, pz, weight, cs.recoil);
             }
+            if (!compton_flow_valid(weight, inc, cs.recoil, cs.scattered)) {
+                err.set(RREA_GPU_ERR_INVALID_STATE);
+                return -1;
+            }
             energy = cs.scattered;
             {
                 // closure of the Compton group (O/RreaPhotonFinalStates.H:92-142)
@@ -676,6 +727,10 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
                 deposit_local_at(pr, pz, weight, ee);
             }
             if (gt0(bind)) deposit_local_at(pr, pz, weight, bind);
+            if (!photoelectric_flow_valid(weight, energy, ee, fmax(bind, 0.0))) {
+                err.set(RREA_GPU_ERR_INVALID_STATE);
+                return -1;
+            }
             {
                 // closure of the Photoelectric group (O/RreaPhotonFinalStates.H:181-223)
                 GroupClosure gc;
@@ -743,7 +798,8 @@ __device__ __forceinline__ int transport_photon(StepConstants const& C, Electron
             if (ps.e_recoil < cutoff) deposit_local_at(pr, pz, weight, ps.e_recoil);
         }
         if (gt0(ps.local)) deposit_local_at(pr, pz, weight, ps.local);
-        if (!pair_closure_valid(ps, weight, energy, cutoff, photon_cut, w_air)) {
+        if (!pair_flow_valid(weight, energy, ps.e_electron, ps.e_positron, ps.e_recoil, ps.recoil, ps.local)
+            || !pair_closure_valid(ps, weight, energy, cutoff, photon_cut, w_air)) {
             err.set(RREA_GPU_ERR_INVALID_STATE);
             return -1;
         }

@@ -15,7 +15,8 @@ import numpy as np
 
 from . import DEFAULT_TABLES, PACKAGE_DIR
 
-LIB_PATH = os.path.join(PACKAGE_DIR, "lib", "librrea_gpu.so")
+# RREA_GPU_LIB selects a parity-study build of the library (see build.py)
+LIB_PATH = os.environ.get("RREA_GPU_LIB") or os.path.join(PACKAGE_DIR, "lib", "librrea_gpu.so")
 
 STATUS_NAMES = {
     0: "OK", 1: "ERR_ARGUMENT", 2: "ERR_TABLES", 3: "ERR_CUDA", 4: "ERR_RANGE", 5: "ERR_GEOMETRY",
