@@ -47,7 +47,8 @@ def _tile(workloads, n, k_lo, k_hi, seed):
 
 def _run(mods, cfg, arr, dt, species, parent_energy):
     gpu, workloads, oracle, compare = mods
-    ctx = gpu.RreaGpuContext(cfg, len(arr["id"]))
+    # room for the secondaries of long steps (about five per particle at 100 ns)
+    ctx = gpu.RreaGpuContext(cfg, 8 * len(arr["id"]))
     ctx.load_tables(TABLES)
     field = workloads.make_field(CASE)
     ctx.set_field(**field)
