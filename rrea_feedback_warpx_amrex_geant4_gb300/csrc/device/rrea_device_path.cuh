@@ -287,7 +287,11 @@ __device__ __forceinline__ void cone_direction(double ax, double ay, double az, 
     normalize(b1x, b1y, b1z);
     double const b2x = dy * b1z - dz * b1y, b2y = dz * b1x - dx * b1z, b2z = dx * b1y - dy * b1x;
     cos_t = fmin(1.0, fmax(-1.0, cos_t));
-    double const sin_t = sqrt(max0(1.0 - cos_t * cos_t));
+    // cos^2 is rounded on its own before the subtraction, as the reference's
+    // x86-64 build rounds it: a fused 1 - cos^2 differs by up to an ulp of 1,
+    // which a small-angle deflection (cos near 1, the Wentzel-VI energies)
+    // amplifies by 1/sin^2 in sin and then in every later direction.
+    double const sin_t = sqrt(max0(1.0 - __dmul_rn(cos_t, cos_t)));
     double const phi = kTwoPi * u_phi;
     double sp, cp;
     sincos(phi, &sp, &cp);
