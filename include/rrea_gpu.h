@@ -241,6 +241,20 @@ rrea_gpu_status rrea_gpu_advance_field_from_current(rrea_gpu_ctx* ctx, double dt
 rrea_gpu_status rrea_gpu_count_live(rrea_gpu_ctx* ctx, int32_t species, int64_t* live);
 
 /*
+ * Charge of the resident charged particles on the cell-centred grid
+ * (RreaWarpXCoupling::DepositParticleChargeToRreaGrid,
+ * O/RreaWarpXCoupling.cpp:376-389, in the cell-centred CIC convention of
+ * DepositChargeCIC, I/RreaSegmentDepositionRZ.H:68-92): every valid electron
+ * deposits -w and every valid positron +w with bilinear weights from the
+ * four nearest cell centres, the support folded evenly at the axis and
+ * clamped at r_hi and both z edges.  rho receives nr*nz values (index
+ * i + nr*j) in elementary charges per cell; the charge density in C/m^3 is
+ * rho * 1.602176634e-19 / (pi (r_{i+1}^2 - r_i^2) dz).  WarpX's own
+ * DepositCharge is in the absent WarpX sources: this is the reference's
+ * header convention.  Host pointer. */
+rrea_gpu_status rrea_gpu_deposit_charge_resident(rrea_gpu_ctx* ctx, double* rho);
+
+/*
  * Census of a resident species tile: the particle reductions of the
  * overlay's reduced diagnostics (species_weight_statistics and
  * electron_species_weight_above_energy, O/RreaCouplingDiagnostics.cpp:122-194,

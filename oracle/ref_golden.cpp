@@ -679,6 +679,31 @@ int main(int argc, char** argv)
             write_f8("ref_cic_thin_particles", 5, parts);
             write_f8("ref_cic_thin_groups", 8, groups);
         }
+        // ---- particle charge: DepositChargeCIC (I/RreaSegmentDepositionRZ.H:68-92), the
+        //      cell-centred CIC with the axis fold and edge clamps, on a 12 x 20 grid
+        {
+            rrea::SegmentGridRZ grid;
+            grid.nr = 12;
+            grid.nz = 20;
+            grid.dr = 0.5;
+            grid.dz = 2.5;
+            grid.r_lo = 0.0;
+            grid.z_lo = 10.0;
+            grid.resize();
+            std::vector<double> parts;
+            for (int i = 0; i < 3000; ++i) {
+                double const r = (i % 7 == 0) ? 0.6 * grid.dr * g.uni() : 1.02 * grid.nr * grid.dr * g.uni();
+                double const z = grid.z_lo + (1.04 * g.uni() - 0.02) * grid.nz * grid.dz;
+                double const qw = (g.uni() < 0.3 ? 1.0 : -1.0) * (0.25 + 4.0 * g.uni());
+                rrea::DepositChargeCIC(grid, qw, r, z);
+                parts.insert(parts.end(), {r, z, qw});
+            }
+            write_f8("ref_cic_charge_particles", 3, parts);
+            write_f8("ref_cic_charge_rho", 1, grid.rho);
+            write_f8("ref_cic_charge_grid", 6, {static_cast<double>(grid.nr), static_cast<double>(grid.nz), grid.dr,
+                                                 grid.dz, grid.r_lo, grid.z_lo});
+        }
+
         // ---- charged-loop skeletons: O/RreaChargedInterleave.H:546-732 driven by
         // scripted policies (oracle/interleave_scenarios.hpp)
         {

@@ -192,6 +192,7 @@ struct rrea_gpu_ctx {
     uint32_t* d_alive = nullptr;
     uint32_t* d_cost_scratch = nullptr;  // histogram and cursors of the scheduling order
     double* d_census = nullptr;          // census sums, edges and thresholds (first census call)
+    double* d_rho_cells = nullptr;       // particle charge grid nr*nz (first deposit call)
     uint64_t* d_child_lineage = nullptr;
     unsigned long long* d_invalid = nullptr;
     // roots of the initial FIFO items (16 B each) on the device and in pinned
@@ -446,6 +447,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     dfree(ctx->d_alive);
     dfree(ctx->d_cost_scratch);
     dfree(ctx->d_census);
+    dfree(ctx->d_rho_cells);
     dfree(ctx->d_child_lineage);
     dfree(ctx->d_invalid);
     dfree(ctx->d_roots);
@@ -1772,6 +1774,27 @@ rrea_gpu_status rrea_gpu_census_resident(rrea_gpu_ctx* ctx, int32_t species, con
     std::memcpy(&max_w, &w64[1], sizeof(max_w));
     out[0] = static_cast<double>(w64[0]);
     out[1] = w64[0] ? max_w : 0.0;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_deposit_charge_resident(rrea_gpu_ctx* ctx, double* rho)
+{
+    if (!ctx || !rho) return RREA_GPU_ERR_ARGUMENT;
+    rrea_gpu_config const& c = ctx->cfg;
+    size_t const cells = static_cast<size_t>(c.nr) * c.nz;
+    if (!ctx->d_rho_cells) RREA_CUDA(ctx, dalloc(&ctx->d_rho_cells, cells));
+    RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_rho_cells, 0, cells * sizeof(double), ctx->stream));
+    double const dr = (c.r_hi - c.r_lo) / c.nr, dz = (c.z_hi - c.z_lo) / c.nz;
+    int const species[2] = {RREA_SPECIES_ELECTRON, RREA_SPECIES_POSITRON};
+    double const charge[2] = {-1.0, 1.0};
+    for (int k = 0; k < 2; ++k) {
+        SpeciesTile const& st = ctx->tiles[species[k]];
+        RREA_CUDA(ctx, rrea_launch::particle_charge(st.d[0], st.d[1], st.d[6], st.id, st.n, charge[k], c.nr, c.nz,
+                                                    c.r_lo, c.z_lo, dr, dz, ctx->d_rho_cells, ctx->num_sms * 8,
+                                                    ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaMemcpyAsync(rho, ctx->d_rho_cells, cells * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RREA_GPU_OK;
 }
 

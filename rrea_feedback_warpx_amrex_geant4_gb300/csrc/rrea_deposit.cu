@@ -283,6 +283,40 @@ __global__ void netchord_deposit_kernel(const SegmentRec* __restrict__ seg, int6
     }
 }
 
+// DepositChargeCIC (I/RreaSegmentDepositionRZ.H:68-92) of every valid
+// particle of a tile, charge q * w, onto the cell-centred nr x nz grid: the
+// convention of the overlay's DepositParticleChargeToRreaGrid
+// (O/RreaWarpXCoupling.cpp:376-389).
+__global__ void particle_charge_kernel(const double* __restrict__ r, const double* __restrict__ z,
+                                       const double* __restrict__ w, const int64_t* __restrict__ id, int64_t n,
+                                       double q, int nr, int nz, double r_lo, double z_lo, double dr, double dz,
+                                       double* __restrict__ rho)
+{
+    for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < n;
+         p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (!(id[p] > 0)) continue;
+        double const qw = q * w[p];
+        double const xr = (r[p] - r_lo) / dr - 0.5;
+        double const xz = (z[p] - z_lo) / dz - 0.5;
+        int const i0 = static_cast<int>(floor(xr));
+        int const j0 = static_cast<int>(floor(xz));
+        double const fr = xr - i0, fz = xz - j0;
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                int i = i0 + a, j = j0 + b;
+                if (i < 0) i = -1 - i;
+                if (i >= nr) i = nr - 1;
+                if (j < 0) j = 0;
+                if (j >= nz) j = nz - 1;
+                warp_add(rho, static_cast<size_t>(i) + static_cast<size_t>(nr) * j, kGridRho,
+                         qw * (a == 0 ? 1.0 - fr : fr) * (b == 0 ? 1.0 - fz : fz));
+            }
+        }
+    }
+}
+
 __global__ void netchord_convert_kernel(NetGrid g, double* __restrict__ jr_phys, double* __restrict__ jz_phys)
 {
     double constexpr pi = 3.14159265358979323846;
@@ -320,6 +354,19 @@ cudaError_t netchord_deposit(rrea_dev::SegmentRec const* seg, int64_t n, rrea_de
     if (n <= 0) return cudaSuccess;
     note_launch();
     rrea_dev::netchord_deposit_kernel<<<blocks, 256, 0, stream>>>(seg, n, g, dt, status, fail_index);
+    return cudaGetLastError();
+}
+
+cudaError_t particle_charge(const double* r, const double* z, const double* w, const int64_t* id, int64_t n, double q,
+                            int nr, int nz, double r_lo, double z_lo, double dr, double dz, double* rho, int blocks,
+                            cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    int64_t const want = (n + 255) / 256;
+    if (want < blocks) blocks = static_cast<int>(want);
+    note_launch();
+    rrea_dev::particle_charge_kernel<<<blocks > 0 ? blocks : 1, 256, 0, stream>>>(r, z, w, id, n, q, nr, nz, r_lo, z_lo,
+                                                                                  dr, dz, rho);
     return cudaGetLastError();
 }
 

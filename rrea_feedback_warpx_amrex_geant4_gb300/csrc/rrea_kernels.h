@@ -43,6 +43,10 @@ cudaError_t photon_step(rrea_dev::ElectronArgs const& args, int blocks, int thre
 cudaError_t netchord_deposit(rrea_dev::SegmentRec const* seg, int64_t n, rrea_dev::NetGrid const& g, double dt,
                              int* status, long long* fail_index, int blocks, cudaStream_t stream);
 cudaError_t netchord_convert(rrea_dev::NetGrid const& g, double* jr_phys, double* jz_phys, cudaStream_t stream);
+// Cell-centred CIC charge q * w of a tile's valid particles (rrea_deposit.cu).
+cudaError_t particle_charge(const double* r, const double* z, const double* w, const int64_t* id, int64_t n, double q,
+                            int nr, int nz, double r_lo, double z_lo, double dr, double dz, double* rho, int blocks,
+                            cudaStream_t stream);
 // Maxwell TM-RZ step with a fixed face current (rrea_field.cu).
 cudaError_t maxwell_step(int nr, int nz, double dr, double dz, double dt, int substeps, double* er, double* ez,
                          double* bt, const double* jr, const double* jz, cudaStream_t stream);

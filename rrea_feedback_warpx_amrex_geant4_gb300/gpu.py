@@ -88,6 +88,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_seed_schedule_load", "rrea_gpu_seed_schedule_free", "rrea_gpu_seed_schedule_size",
     "rrea_gpu_seed_schedule_events", "rrea_gpu_seed_schedule_validate", "rrea_gpu_seed_schedule_last_error",
     "rrea_gpu_inject_seeds_resident", "rrea_gpu_thin_cic_groups", "rrea_gpu_census_resident",
+    "rrea_gpu_deposit_charge_resident",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -155,6 +156,7 @@ def load_library(path=LIB_PATH):
                                              ctypes.POINTER(ctypes.c_uint64), _i64p, _i64p,
                                              ctypes.POINTER(ctypes.c_int32), _i64p]
     lib.rrea_gpu_compact_resident.argtypes = [vp, ctypes.c_int32, _i64p]
+    lib.rrea_gpu_deposit_charge_resident.argtypes = [vp, _D]
     lib.rrea_gpu_census_resident.argtypes = [vp, ctypes.c_int32, _D, ctypes.c_int32, _D, ctypes.c_int32, _D]
     lib.rrea_gpu_resident_count.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
@@ -457,6 +459,14 @@ class RreaGpuContext:
             g, mx.ctypes.data_as(i64), k.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), removed.ctypes.data_as(i64),
             draws.ctypes.data_as(i64), valid.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cap.ctypes.data_as(i64)))
         return w, removed, draws, valid, cap
+
+    def deposit_charge(self):
+        """Cell-centred CIC charge of the resident electrons (-w) and
+        positrons (+w), elementary charges per cell, shape (nz, nr)."""
+        c = self.config
+        out = np.zeros(c.nr * c.nz)
+        self._check(self.lib.rrea_gpu_deposit_charge_resident(self.handle, out.ctypes.data_as(_D)))
+        return out.reshape(c.nz, c.nr)
 
     def census(self, species, edges_eV, thresholds_eV=()):
         """Census of a resident species tile (the reduced diagnostics'

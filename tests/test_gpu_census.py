@@ -74,3 +74,38 @@ def test_census_refuses_bad_edges(env):
         ctx.census(0, np.logspace(0, 1, 1100))
     with pytest.raises(gpu.RreaGpuError):
         ctx.census(0, [1.0, 2.0], np.ones(17))
+
+
+def test_particle_charge_matches_restatement(env):
+    """rrea_gpu_deposit_charge_resident against the oracle's
+    DepositChargeCIC restatement (itself pinned bit-exact to the reference
+    header): electrons -w and positrons +w on the 32 x 256 grid, particles
+    near the axis and at the domain's edges included, invalid ones skipped.
+    Atomics: within 1e-12 of the grid's largest cell; total charge kept."""
+    gpu, workloads, avalanche, oav, ctx = env
+    from oracle import oracle
+    cfg = ctx.config
+    rng = np.random.default_rng(5)
+    tiles = []
+    for species, stage in ((0, ctx.stage_electrons), (1, ctx.stage_positrons)):
+        n = 40_000
+        t = workloads.make_electrons("uniform_c0", n)
+        t["r"][:] = cfg.r_hi * rng.uniform(0.0, 1.0, n) ** 2          # crowded near the axis
+        t["z"][:] = cfg.z_hi * rng.uniform(0.0, 1.0, n)
+        t["w"][:] = rng.uniform(0.5, 3.0, n)
+        t["id"][rng.uniform(size=n) < 0.05] *= -1
+        for f in ("r", "z"):
+            t["prev_" + f][:] = t[f]
+        stage(t)
+        tiles.append((species, t))
+    got = ctx.deposit_charge().ravel()
+    dr, dz = (cfg.r_hi - cfg.r_lo) / cfg.nr, (cfg.z_hi - cfg.z_lo) / cfg.nz
+    want = np.zeros(cfg.nr * cfg.nz)
+    for species, t in tiles:
+        v = t["id"] > 0
+        q = -1.0 if species == 0 else 1.0
+        want += oracle.deposit_charge_cic(cfg.nr, cfg.nz, dr, dz, cfg.r_lo, cfg.z_lo, t["r"][v], t["z"][v],
+                                          q * t["w"][v])
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * np.abs(want).max())
+    total = sum((-1.0 if s == 0 else 1.0) * t["w"][t["id"] > 0].sum() for s, t in tiles)
+    assert abs(got.sum() - total) <= 1e-10 * sum(t["w"].sum() for _, t in tiles)
