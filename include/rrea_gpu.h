@@ -318,6 +318,48 @@ rrea_gpu_status rrea_gpu_thin_cic_groups(rrea_gpu_ctx* ctx, const double* fracti
                                         const int64_t* max_removals, const uint64_t* keys, int64_t* removed,
                                         int64_t* draws, int32_t* valid, int64_t* capacity);
 
+/*
+ * Adaptive population control (rrea.population_ceiling_policy =
+ * adaptive_resample_v1) of the resident electron or positron population.
+ *
+ * population_thin_resident is the global thinning plan of
+ * RreaWarpXCoupling::PreflightAndApplySecondaryPopulationControl
+ * (O/RreaCouplingPopulation.cpp:175-640) on one rank: when the live
+ * particles of `species` plus its staged candidates exceed 1.25 x target,
+ * min(members - target, removal capacity) particles leave by charge-exact
+ * thinning of their order-1 CIC supports (RreaPlanGlobalCicThinning,
+ * I/RreaCicConservingResample.H:489-640), support by support in sorted
+ * order, with the species' RreaAdaptiveResampleCicUniform stream
+ * (rng_seed, group id ^ salt, step).  A live particle thinned to weight 0 is
+ * invalidated (negated id: rrea_gpu_compact_resident removes it); a
+ * candidate keeps its record with its new weight (weight 0: dropped at the
+ * commit).  The candidates are the last resident drain's survivors when
+ * `candidates` is NULL (call between rrea_gpu_drain_resident and
+ * rrea_gpu_commit_survivors_resident), else the n_candidates host records,
+ * whose weights are updated in place.  stats (may be NULL) receives 8
+ * values: members, live members, candidate members, supports, removal
+ * capacity, geometric floor, nominal request, removed.  Nothing is applied
+ * when a support's plan is rejected or the plans remove less than the
+ * nominal request (RREA_GPU_ERR_INVALID_STATE, where the reference aborts),
+ * or when a particle lies beyond 32767 cells of the grid
+ * (RREA_GPU_ERR_GEOMETRY).  Live stable ids are the packed id/cpu word
+ * (id << 24 | cpu): AMReX's own packing is in the absent AMReX sources.
+ *
+ * population_split_resident is the split refill of
+ * AdaptiveResampleOneSpecies (:686-767): when 0 < live < target/2 and the
+ * floor is positive, every valid particle with weight >= 2 x floor halves
+ * its weight and an identical clone (captured state = own state, cpu word
+ * kept) joins the tile end in tile order with the next species ids
+ * (RreaAdaptiveResampleSplitOutcome, O/RreaRng.H:163-175).  added (may be
+ * NULL) receives the clone count; RREA_GPU_ERR_CAPACITY, with nothing
+ * changed, when the clones do not fit.
+ */
+rrea_gpu_status rrea_gpu_population_thin_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t target, int32_t step,
+                                                 uint64_t salt, rrea_gpu_secondary* candidates, int64_t n_candidates,
+                                                 int64_t* stats);
+rrea_gpu_status rrea_gpu_population_split_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t target,
+                                                  double split_min_weight, int64_t* added);
+
 /* Number of particles (valid or not) in a resident species tile.  NO COUNTERPART IN THE
  * REFERENCE (WarpX containers know their own size). */
 rrea_gpu_status rrea_gpu_resident_count(rrea_gpu_ctx* ctx, int32_t species, int64_t* n);

@@ -704,6 +704,159 @@ int main(int argc, char** argv)
                                                  grid.dz, grid.r_lo, grid.z_lo});
         }
 
+        // ---- adaptive_resample_v1 global thinning on one rank: the plan of
+        //      O/RreaCouplingPopulation.cpp:175-640 (records, sort, support capacity,
+        //      greedy requests) around the reference's own RreaPlanGlobalCicThinning,
+        //      RreaCicResampleRemovalCapacity and RreaAdaptiveResampleCicUniform
+        for (int pc_case = 0; pc_case < 2; ++pc_case) {
+            int const nr = 10, nz = 12;
+            double const dr = 1.0, dz = 2.0, r_lo = 0.0, z_lo = 0.0;
+            bool const positron = pc_case == 1;
+            int const n_live = pc_case == 0 ? 4000 : 3200;
+            int const n_cand = pc_case == 0 ? 800 : 800;
+            long const target = pc_case == 0 ? 1500 : 3000;
+            std::uint64_t const seed = 77, salt = pc_case == 0 ? 0 : 12345;
+            std::uint64_t const step = 9 + pc_case;
+            std::vector<double> live, cand;  // the inputs as the device receives them
+            struct Rec {
+                int sr, sz, phase;
+                bool candidate;
+                std::uint64_t high, low;
+                double fr, fz, w;
+                int member;
+            };
+            std::vector<Rec> recs;
+            auto record = [&](double r, double z, double ux, double uy, double uz, double th, double w, bool c,
+                              std::uint64_t high, std::uint64_t low, int member) {
+                double const rc = (r - r_lo) / dr + 0.0 - 0.5;
+                double const zc = (z - z_lo) / dz + 0.0 - 0.5;
+                double const i0 = std::floor(rc), j0 = std::floor(zc);
+                double const co = std::cos(th), si = std::sin(th);
+                double const ur = ux * co + uy * si, ut = -ux * si + uy * co;
+                double const mag = std::sqrt(ux * ux + uy * uy + uz * uz);
+                int ex = mag > 0.0 && std::isfinite(mag) ? std::ilogb(mag) : -1024;
+                ex = std::max(-1024, std::min(1023, ex));
+                recs.push_back(Rec{static_cast<int>(i0), static_cast<int>(j0),
+                                   (ex + 1024) * 8 + (ur >= 0.0 ? 1 : 0) + (ut >= 0.0 ? 2 : 0) + (uz >= 0.0 ? 4 : 0),
+                                   c, high, low, rc - i0, zc - j0, w, member});
+            };
+            for (int i = 0; i < n_live; ++i) {
+                // clustered: a third of the particles in three cells
+                double const r = (i % 3 == 0) ? (0.5 + (i % 9) / 3) * dr + 0.4 * g.uni() : nr * dr * g.uni();
+                double const z = (i % 3 == 0) ? 5.0 * dz + 0.7 * dz * g.uni() : nz * dz * g.uni();
+                double const th = 6.283185307179586 * g.uni() - 3.141592653589793;
+                double const k = g.logu(1.0e4, 1.0e8);
+                double const u = rrea::RreaElectronProperVelocityFromKineticEv(k);
+                double const mu = 2.0 * g.uni() - 1.0, ph = 6.283185307179586 * g.uni();
+                double const sn = std::sqrt(1.0 - mu * mu);
+                double const ux = u * sn * std::cos(ph), uy = u * sn * std::sin(ph), uz = u * mu;
+                double const w = 0.5 + 1.5 * g.uni();
+                std::int64_t const id = 1 + i;
+                std::int32_t const cpu = i % 5;
+                live.insert(live.end(), {r, z, th, ux, uy, uz, w, static_cast<double>(id), static_cast<double>(cpu)});
+                record(r, z, ux, uy, uz, th, w, false, 0,
+                       (static_cast<std::uint64_t>(id) << 24) | static_cast<std::uint32_t>(cpu), i);
+            }
+            for (int i = 0; i < n_cand; ++i) {
+                double const rr = (i % 2 == 0) ? (0.6 + (i % 6) / 2) * dr + 0.3 * g.uni() : nr * dr * g.uni();
+                double const th = 6.283185307179586 * g.uni() - 3.141592653589793;
+                double const x = rr * std::cos(th), y = rr * std::sin(th);
+                double const z = (i % 2 == 0) ? 5.0 * dz + 0.9 * dz * g.uni() : nz * dz * g.uni();
+                double const k = g.logu(1.0e4, 3.0e7);
+                double const mu = 2.0 * g.uni() - 1.0, ph = 6.283185307179586 * g.uni();
+                double const sn = std::sqrt(1.0 - mu * mu);
+                double const dx = sn * std::cos(ph), dy = sn * std::sin(ph), dzr = mu;
+                double const w = 0.5 + 1.5 * g.uni();
+                std::uint64_t const root = g.next() >> 8;
+                std::uint64_t const lineage = static_cast<std::uint64_t>(i % 37);
+                int const root_species = i % 3;
+                cand.insert(cand.end(), {x, y, z, dx, dy, dzr, k, w, static_cast<double>(root >> 32),
+                                         static_cast<double>(root & 0xffffffffULL), static_cast<double>(lineage),
+                                         static_cast<double>(root_species)});
+                double const u = rrea::RreaElectronProperVelocityFromKineticEv(k);
+                record(std::hypot(x, y), z, u * dx, u * dy, u * dzr, std::atan2(y, x), w, true, root,
+                       (lineage << 2) | static_cast<std::uint64_t>(root_species), n_live + i);
+            }
+            std::sort(recs.begin(), recs.end(), [](Rec const& a, Rec const& b) {
+                if (a.sr != b.sr) return a.sr < b.sr;
+                if (a.sz != b.sz) return a.sz < b.sz;
+                if (a.phase != b.phase) return a.phase < b.phase;
+                if (a.candidate != b.candidate) return a.candidate < b.candidate;
+                if (a.high != b.high) return a.high < b.high;
+                return a.low < b.low;
+            });
+            std::uint64_t const stream_key = positron ? 0x706f736974726f6eULL : 0x656c656374726f6eULL;
+            auto const rng_species = positron ? rrea::warpx::RreaAdaptiveResampleSpecies::Positron
+                                              : rrea::warpx::RreaAdaptiveResampleSpecies::Electron;
+            std::vector<std::pair<std::size_t, std::size_t>> supports;
+            std::vector<std::size_t> caps;
+            std::size_t total_cap = 0;
+            for (std::size_t b = 0; b < recs.size();) {
+                std::size_t e = b + 1;
+                while (e < recs.size() && recs[e].sr == recs[b].sr && recs[e].sz == recs[b].sz) ++e;
+                std::vector<rrea::RreaCicResampleParticle> sup;
+                for (std::size_t i = b; i < e; ++i) sup.push_back({recs[i].fr, recs[i].fz, recs[i].w});
+                std::size_t const cap = rrea::RreaCicResampleRemovalCapacity(sup);
+                supports.push_back({b, e});
+                caps.push_back(cap);
+                total_cap += cap;
+                b = e;
+            }
+            long const members = static_cast<long>(recs.size());
+            long const nominal = members > target + target / 4
+                ? std::min<long>(members - target, static_cast<long>(total_cap)) : 0;
+            std::vector<double> new_w(recs.size());
+            for (auto const& r : recs) new_w[static_cast<std::size_t>(r.member)] = r.w;
+            long remaining = nominal, removed = 0;
+            for (std::size_t sidx = 0; sidx < supports.size(); ++sidx) {
+                long const request = std::min<long>(remaining, static_cast<long>(caps[sidx]));
+                remaining -= request;
+                if (request == 0) continue;
+                std::vector<rrea::RreaGlobalCicParticle> sup;
+                for (std::size_t i = supports[sidx].first; i < supports[sidx].second; ++i) {
+                    rrea::RreaGlobalCicParticle q;
+                    q.support_r = recs[i].sr;
+                    q.support_z = recs[i].sz;
+                    q.phase = recs[i].phase;
+                    q.source_rank = 0;
+                    q.stable_id = recs[i].low;
+                    q.fraction_r = recs[i].fr;
+                    q.fraction_z = recs[i].fz;
+                    q.weight = recs[i].w;
+                    q.candidate = recs[i].candidate;
+                    q.stable_id_high = recs[i].high;
+                    sup.push_back(q);
+                }
+                auto const plan = rrea::RreaPlanGlobalCicThinning<double>(
+                    sup, sup.size() - static_cast<std::size_t>(request), 1, stream_key,
+                    [&](std::uint64_t group_id, std::size_t reduction) {
+                        return rrea::warpx::RreaAdaptiveResampleCicUniform(seed, group_id ^ salt, step, reduction,
+                                                                           rng_species);
+                    });
+                if (!plan.valid()) throw std::runtime_error("population golden: support plan rejected");
+                removed += static_cast<long>(plan.removed);
+                for (auto const& u : plan.updates) {
+                    for (std::size_t i = supports[sidx].first; i < supports[sidx].second; ++i) {
+                        if (recs[i].candidate == u.candidate && recs[i].low == u.stable_id &&
+                            recs[i].high == u.stable_id_high) {
+                            new_w[static_cast<std::size_t>(recs[i].member)] = u.stored_weight;
+                        }
+                    }
+                }
+            }
+            std::string const tag = pc_case == 0 ? "ref_population_electron" : "ref_population_positron";
+            write_f8(tag + "_live", 9, live);
+            write_f8(tag + "_candidates", 12, cand);
+            write_f8(tag + "_weights", 1, new_w);
+            write_f8(tag + "_plan", 8, {static_cast<double>(members), static_cast<double>(n_live),
+                                        static_cast<double>(n_cand), static_cast<double>(supports.size()),
+                                        static_cast<double>(total_cap), static_cast<double>(nominal),
+                                        static_cast<double>(removed), static_cast<double>(target)});
+            write_f8(tag + "_setup", 10, {static_cast<double>(nr), static_cast<double>(nz), dr, dz, r_lo, z_lo,
+                                          static_cast<double>(seed), static_cast<double>(salt),
+                                          static_cast<double>(step), positron ? 1.0 : 0.0});
+        }
+
         // ---- charged-loop skeletons: O/RreaChargedInterleave.H:546-732 driven by
         // scripted policies (oracle/interleave_scenarios.hpp)
         {

@@ -85,10 +85,19 @@ class AvalancheRun:
     """A plain avalanche run on one GPU: seeds staged as the resident
     electron tile, then `steps` whole kinetic steps."""
 
-    def __init__(self, ctx, electrons, photons=None, positrons=None, feedback=False, field_substeps=2):
+    def __init__(self, ctx, electrons, photons=None, positrons=None, feedback=False, field_substeps=2,
+                 population_target=None, split_min_weight=0.0, control_interval=1, controller_salt=0):
         self.ctx = ctx
         self.feedback = feedback
         self.field_substeps = field_substeps
+        # adaptive_resample_v1: e- and e+ macro targets, the split floor, the
+        # control interval in steps and the controller's RNG salt
+        self.population_target = population_target
+        self.split_min_weight = split_min_weight
+        self.control_interval = control_interval
+        self.controller_salt = controller_salt
+        self.thinned = 0
+        self.split = 0
         empty = workloads.make_electrons("uniform_c0", 0)
         ctx.stage_electrons(electrons)
         ctx.stage_photons(photons if photons is not None else empty)
@@ -111,9 +120,20 @@ class AvalancheRun:
             moved += ctx.last_step_stats()[0]
         ctx.drain_resident(self.step, dt_s)
         drained = ctx.last_drain_stats()
+        control = bool(self.population_target) and self.step % self.control_interval == 0
+        if control:
+            # global thinning over the live particles and the staged survivors,
+            # inside the commit transaction (PreflightAndApplySecondaryPopulationControl)
+            for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON):
+                self.thinned += ctx.population_thin(sp, self.population_target, self.step,
+                                                    self.controller_salt)["removed"]
         ctx.commit_survivors_resident()
         for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON, gpu.SPECIES_PHOTON):
             ctx.compact_resident(sp)
+        if control and self.split_min_weight > 0.0:
+            # split refill at the step boundary (ApplyAdaptivePopulationControl)
+            for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON):
+                self.split += ctx.population_split(sp, self.population_target, self.split_min_weight)
         if self.feedback:
             ctx.advance_field(dt_s, self.field_substeps)
         self.step += 1
@@ -148,6 +168,7 @@ class AvalancheRun:
             "particle_steps": moved_total, "fifo_items": fifo_total, "wall_s": wall,
             "particle_steps_per_s": moved_total / wall if wall > 0 else 0.0,
             "kernel_launches": launches, "steps": steps,
+            "population_thinned": self.thinned, "population_split": self.split,
         }
 
 
@@ -202,6 +223,9 @@ def main():
     p.add_argument("--field", type=float, default=None, help="uniform |E_z| in V/m (default: the case's)")
     p.add_argument("--capacity", type=int, default=1 << 24)
     p.add_argument("--census-every", type=int, default=100)
+    p.add_argument("--population-target", type=int, default=0,
+                   help="adaptive_resample_v1 e-/e+ macro target (0: no population control)")
+    p.add_argument("--split-min-weight", type=float, default=0.0)
     p.add_argument("--json", default=None)
     p.add_argument("--csv", default=None)
     a = p.parse_args()
@@ -210,7 +234,8 @@ def main():
     torch.cuda.set_device(0)
     ctx = make_context(a.case, a.capacity, a.rng_seed, a.field)
     seeds = workloads.make_electrons(a.case, a.seeds)
-    res = AvalancheRun(ctx, seeds).run(a.steps, census_every=a.census_every)
+    res = AvalancheRun(ctx, seeds, population_target=a.population_target or None,
+                       split_min_weight=a.split_min_weight).run(a.steps, census_every=a.census_every)
     p_case = c0_like_case(a.field, a.case)
     res["case"] = a.case
     res["seeds"] = a.seeds
@@ -228,7 +253,7 @@ def main():
             f.write(text)
     print(json.dumps({k: res[k] for k in ("case", "seeds", "steps", "multiplication", "particle_steps", "wall_s",
                                           "particle_steps_per_s", "kernel_launches", "avalanche_length_m",
-                                          "coleman_dwyer_length_m")}))
+                                          "coleman_dwyer_length_m", "population_thinned", "population_split")}))
     ctx.close()
 
 

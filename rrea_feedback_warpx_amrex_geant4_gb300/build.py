@@ -33,6 +33,7 @@ SOURCES = [
     os.path.join(CSRC, "rrea_deposit.cu"),
     os.path.join(CSRC, "rrea_field.cu"),
     os.path.join(CSRC, "rrea_census.cu"),
+    os.path.join(CSRC, "rrea_population.cu"),
     os.path.join(CSRC, "host", "table_set.cpp"),
     os.path.join(CSRC, "host", "seed_schedule.cpp"),
 ]

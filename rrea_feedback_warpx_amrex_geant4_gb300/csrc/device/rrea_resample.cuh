@@ -251,4 +251,160 @@ __device__ inline CicThinResult cic_thin(const double* fr, const double* fz, dou
     return res;
 }
 
+// RreaThinCicWeights over a support of any size in global memory, with the
+// uniform of draw k from draw(k).  The reference's active list is the live
+// particles in index order and a draw only changes its first five entries,
+// so the list is kept as a window of those (at most) five followed by the
+// untouched particles from `cursor` on: the window is compacted after each
+// draw and refilled in index order, which is the reference's erase of the
+// zeroed entries, at O(1) per draw instead of O(n).
+template <class Draw>
+__device__ inline CicThinResult cic_thin_window(const double* fr, const double* fz, double* w, int64_t n,
+                                                int64_t max_removals, Draw const& draw)
+{
+    CicThinResult res{0, 0, true};
+    int64_t n_active = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (!isfinite(fr[i]) || !isfinite(fz[i]) || fr[i] < 0.0 || fr[i] > 1.0 || fz[i] < 0.0 || fz[i] > 1.0 ||
+            !isfinite(w[i]) || w[i] < 0.0) {
+            res.valid = false;
+            return res;
+        }
+        if (w[i] > 0.0) ++n_active;
+    }
+    int64_t win[5];
+    int nw = 0;
+    int64_t cursor = 0;
+    auto refill = [&]() {
+        while (nw < 5 && cursor < n) {
+            if (w[cursor] > 0.0) win[nw++] = cursor;
+            ++cursor;
+        }
+    };
+    refill();
+    constexpr double kEps = 2.220446049250313080847263336181640625e-16;
+    while (res.removed < max_removals && n_active >= 2) {
+        int const m = nw;  // min(5, n_active): the window is full whenever five are live
+        CicColumn cols[5];
+        for (int c = 0; c < m; ++c) cols[c] = cic_column(fr[win[c]], fz[win[c]]);
+        dd dir[5];
+        if (!cic_null_direction(cols, m, dir)) {
+            if (n_active > m) res.valid = false;
+            return res;
+        }
+        dd a_plus = dd_from(__longlong_as_double(0x7ff0000000000000LL));
+        dd a_minus = a_plus;
+        int hit_plus = m, hit_minus = m;
+        for (int c = 0; c < m; ++c) {
+            dd const wc = dd_from(w[win[c]]);
+            if (dd_lt_d(dir[c], 0.0)) {
+                dd const b = dd_div(wc, dd_neg(dir[c]));
+                if (dd_lt(b, a_plus)) {
+                    a_plus = b;
+                    hit_plus = c;
+                }
+            } else if (dd_gt_d(dir[c], 0.0)) {
+                dd const b = dd_div(wc, dir[c]);
+                if (dd_lt(b, a_minus)) {
+                    a_minus = b;
+                    hit_minus = c;
+                }
+            }
+        }
+        if (!isfinite(a_plus.hi) || !isfinite(a_minus.hi) || a_plus.hi < 0.0 || a_minus.hi < 0.0 ||
+            hit_plus == m || hit_minus == m) {
+            res.valid = false;
+            return res;
+        }
+        double const u = draw(static_cast<uint64_t>(res.draws));
+        if (!(u > 0.0) || !(u < 1.0)) {
+            res.valid = false;
+            return res;
+        }
+        ++res.draws;
+        dd const p_plus = dd_div(a_minus, dd_add(a_plus, a_minus));
+        bool const take_plus = dd_lt(dd_from(u), p_plus);
+        dd const alpha = take_plus ? a_plus : dd_neg(a_minus);
+        int const zero = take_plus ? hit_plus : hit_minus;
+        for (int c = 0; c < m; ++c) {
+            double const w0 = w[win[c]];
+            dd upd = dd_add(dd_from(w0), dd_mul(alpha, dir[c]));
+            if (c == zero) upd = dd_from(0.0);
+            double const slack = 512.0 * kEps * static_cast<double>(m) * fmax(1.0, fabs(w0));
+            if (dd_lt_d(upd, 0.0) && !dd_gt_d(dd_neg(upd), slack)) upd = dd_from(0.0);
+            if (dd_lt_d(upd, 0.0) || !isfinite(upd.hi)) {
+                res.valid = false;
+                return res;
+            }
+            w[win[c]] = upd.hi > 0.0 ? upd.hi + upd.lo : 0.0;
+        }
+        int kept = 0;
+        for (int c = 0; c < nw; ++c) {
+            if (w[win[c]] != 0.0) win[kept++] = win[c];
+        }
+        int const removed_now = nw - kept;
+        nw = kept;
+        if (removed_now == 0) {
+            res.valid = false;
+            return res;
+        }
+        n_active -= removed_now;
+        res.removed += removed_now;
+        refill();
+    }
+    return res;
+}
+
+// Rank of the CIC columns of a support of any size (at most four, found
+// among its first independent columns; :162-205).
+__device__ inline int cic_constraint_rank_any(const double* fr, const double* fz, const double* w, int64_t n)
+{
+    dd basis[4][4];
+    int rank = 0;
+    for (int64_t i = 0; i < n && rank < 4; ++i) {
+        if (!(w[i] > 0.0)) continue;
+        CicColumn col = cic_column(fr[i], fz[i]);
+        dd* v = col.v;
+        for (int r = 0; r < rank; ++r) {
+            int p = 0;
+            while (p < 4 && !dd_gt_d(dd_absv(basis[r][p]), kCicTolerance)) ++p;
+            if (p == 4) continue;
+            dd const f = dd_div(v[p], basis[r][p]);
+            for (int j = p; j < 4; ++j) v[j] = dd_sub(v[j], dd_mul(f, basis[r][j]));
+        }
+        int p = 0;
+        while (p < 4 && !dd_gt_d(dd_absv(v[p]), kCicTolerance)) ++p;
+        if (p == 4) continue;
+        dd const pv = v[p];
+        for (int j = 0; j < 4; ++j) basis[rank][j] = j < p ? dd_from(0.0) : dd_div(v[j], pv);
+        ++rank;
+    }
+    return rank;
+}
+
+// RreaRoundAndVerifyCicWeights (:424-468) with FP64 storage: the four cell
+// moments of the thinned weights agree with those of the original weights
+// within 512 ulps x support size x max(1, |moment|).
+__device__ inline bool cic_moments_kept(const double* fr, const double* fz, const double* w0, const double* w1,
+                                        int64_t n)
+{
+    dd before[4] = {dd_from(0.0), dd_from(0.0), dd_from(0.0), dd_from(0.0)};
+    dd after[4] = {dd_from(0.0), dd_from(0.0), dd_from(0.0), dd_from(0.0)};
+    for (int64_t i = 0; i < n; ++i) {
+        CicColumn const c = cic_column(fr[i], fz[i]);
+        for (int k = 0; k < 4; ++k) {
+            before[k] = dd_add(before[k], dd_mul(dd_from(w0[i]), c.v[k]));
+            after[k] = dd_add(after[k], dd_mul(dd_from(w1[i]), c.v[k]));
+        }
+    }
+    constexpr double kEps = 2.220446049250313080847263336181640625e-16;
+    for (int k = 0; k < 4; ++k) {
+        double const scale = fmax(1.0, fabs(before[k].hi));
+        double const tol = 512.0 * kEps * static_cast<double>(n) * scale;
+        dd const diff = dd_absv(dd_sub(after[k], before[k]));
+        if (dd_gt_d(diff, tol)) return false;
+    }
+    return true;
+}
+
 }  // namespace rrea_dev

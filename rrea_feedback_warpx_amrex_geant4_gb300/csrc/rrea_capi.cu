@@ -193,6 +193,9 @@ struct rrea_gpu_ctx {
     uint32_t* d_cost_scratch = nullptr;  // histogram and cursors of the scheduling order
     double* d_census = nullptr;          // census sums, edges and thresholds (first census call)
     double* d_rho_cells = nullptr;       // particle charge grid nr*nz (first deposit call)
+    rrea_launch::PopulationWork* pop_work = nullptr;  // population-control plan scratch (first use)
+    rrea_gpu_secondary* d_pc_cand = nullptr;          // host candidates of a population-control call
+    int64_t pc_cand_cap = 0;
     uint64_t* d_child_lineage = nullptr;
     unsigned long long* d_invalid = nullptr;
     // roots of the initial FIFO items (16 B each) on the device and in pinned
@@ -448,6 +451,8 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     dfree(ctx->d_cost_scratch);
     dfree(ctx->d_census);
     dfree(ctx->d_rho_cells);
+    rrea_launch::population_work_free(ctx->pop_work);
+    dfree(ctx->d_pc_cand);
     dfree(ctx->d_child_lineage);
     dfree(ctx->d_invalid);
     dfree(ctx->d_roots);
@@ -1795,6 +1800,99 @@ rrea_gpu_status rrea_gpu_deposit_charge_resident(rrea_gpu_ctx* ctx, double* rho)
     }
     RREA_CUDA(ctx, cudaMemcpyAsync(rho, ctx->d_rho_cells, cells * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_population_thin_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t target, int32_t step,
+                                                 uint64_t salt, rrea_gpu_secondary* candidates, int64_t n_candidates,
+                                                 int64_t* stats)
+{
+    if (!ctx || (species != RREA_SPECIES_ELECTRON && species != RREA_SPECIES_POSITRON) || target < 0 ||
+        n_candidates < 0 || (n_candidates > 0 && !candidates)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "population control takes e- or e+, a target >= 0 and a candidate array");
+    }
+    rrea_gpu_config const& c = ctx->cfg;
+    rrea_gpu_secondary* d_cand = ctx->d_surv;
+    int64_t n_cand = ctx->n_surv;
+    if (candidates) {
+        if (n_candidates > ctx->pc_cand_cap) {
+            dfree(ctx->d_pc_cand);
+            ctx->d_pc_cand = nullptr;
+            ctx->pc_cand_cap = 0;
+            RREA_CUDA(ctx, dalloc(&ctx->d_pc_cand, static_cast<size_t>(n_candidates)));
+            ctx->pc_cand_cap = n_candidates;
+        }
+        d_cand = ctx->d_pc_cand;
+        n_cand = n_candidates;
+        if (n_cand > 0) {
+            RREA_CUDA(ctx, cudaMemcpyAsync(d_cand, candidates, static_cast<size_t>(n_cand) * sizeof(rrea_gpu_secondary),
+                                           cudaMemcpyHostToDevice, ctx->stream));
+        }
+    }
+    SpeciesTile& st = ctx->tiles[species];
+    rrea_launch::PopulationInput in{};
+    in.r = st.d[0]; in.z = st.d[1]; in.theta = st.d[2]; in.ux = st.d[3]; in.uy = st.d[4]; in.uz = st.d[5];
+    in.w = st.d[6];
+    in.id = st.id;
+    in.cpu = st.cpu;
+    in.n_tile = st.n;
+    in.cand = d_cand;
+    in.n_cand = n_cand;
+    in.species = species;
+    in.periodic_z = c.periodic_z;
+    in.r_lo = c.r_lo;
+    in.z_lo = c.z_lo;
+    in.z_hi = c.z_hi;
+    in.dr = (c.r_hi - c.r_lo) / c.nr;
+    in.dz = (c.z_hi - c.z_lo) / c.nz;
+    in.target = target;
+    in.rng_seed = c.rng_seed;
+    in.salt = salt;
+    in.step = step;
+    rrea_launch::PopulationStats ps{};
+    RREA_CUDA(ctx, rrea_launch::population_thin(in, ctx->pop_work, ps, ctx->num_sms * 8, ctx->stream));
+    if (stats) {
+        int64_t const v[8] = {ps.members, ps.live, ps.candidates, ps.supports, ps.capacity, ps.floor, ps.requested,
+                              ps.removed};
+        for (int k = 0; k < 8; ++k) stats[k] = v[k];
+    }
+    if (ps.status != 0) {
+        return fail(ctx, static_cast<rrea_gpu_status>(ps.status),
+                    ps.status == RREA_GPU_ERR_GEOMETRY
+                        ? "population control found a particle outside the supported grid"
+                        : "population control plan rejected (invalid support plan or insufficient progress); "
+                          "nothing was applied");
+    }
+    if (candidates && n_cand > 0) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(candidates, d_cand, static_cast<size_t>(n_cand) * sizeof(rrea_gpu_secondary),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_population_split_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t target,
+                                                  double split_min_weight, int64_t* added)
+{
+    if (!ctx || (species != RREA_SPECIES_ELECTRON && species != RREA_SPECIES_POSITRON) || target < 0 ||
+        !std::isfinite(split_min_weight)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "split refill takes e- or e+, a target >= 0 and a finite floor");
+    }
+    if (added) *added = 0;
+    int64_t live = 0;
+    rrea_gpu_status const s = rrea_gpu_count_live(ctx, species, &live);
+    if (s != RREA_GPU_OK) return s;
+    // RreaAdaptiveResampleAction (O/RreaRng.H:139-153): split strictly below half the target
+    if (!(live > 0 && live < target / 2 && split_min_weight > 0.0)) return RREA_GPU_OK;
+    SpeciesTile& st = ctx->tiles[species];
+    int64_t n_added = 0;
+    RREA_CUDA(ctx, rrea_launch::population_split(columns(st), st.n, split_min_weight, ctx->pop_work,
+                                                 ctx->next_id[species], ctx->capacity - st.n, &n_added, ctx->stream));
+    if (n_added < 0) return fail(ctx, RREA_GPU_ERR_CAPACITY, "split clones exceed the resident tile capacity");
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    st.n += n_added;
+    ctx->next_id[species] += n_added;
+    if (added) *added = n_added;
     return RREA_GPU_OK;
 }
 

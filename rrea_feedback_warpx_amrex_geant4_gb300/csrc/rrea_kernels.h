@@ -115,4 +115,41 @@ cudaError_t census(const double* ux, const double* uy, const double* uz, const d
                    double* out, unsigned long long* count, unsigned long long* max_bits, int blocks,
                    cudaStream_t stream);
 
+// Adaptive population control of one charged species (rrea_population.cu):
+// the live tile rows and the staged candidates of the transaction.
+struct PopulationInput {
+    const double *r, *z, *theta, *ux, *uy, *uz;
+    double* w;
+    int64_t* id;
+    const int32_t* cpu;
+    int64_t n_tile;
+    rrea_gpu_secondary* cand;
+    int64_t n_cand;
+    int species;
+    int periodic_z;
+    double r_lo, z_lo, z_hi, dr, dz;
+    int64_t target;
+    uint64_t rng_seed, salt;
+    int64_t step;
+};
+// members, live and candidate members, supports, removal capacity and the
+// geometric floor, the nominal request, particles removed; status is an
+// rrea_gpu_status (0: plan applied or nothing due)
+struct PopulationStats {
+    int64_t members, live, candidates, supports, capacity, floor, requested, removed;
+    int status;
+};
+struct PopulationWork;
+void population_work_free(PopulationWork* work);
+// Global CIC thinning plan and its application (nothing is applied unless
+// status is 0).
+cudaError_t population_thin(PopulationInput const& in, PopulationWork*& work, PopulationStats& stats, int blocks,
+                            cudaStream_t stream);
+// Split refill of the tile's first n rows: weight halved for every valid
+// particle at or above twice min_w, clones appended at rows n.. with ids
+// from first_id in tile order; *added < 0 when the clones exceed `room`
+// (nothing changed).
+cudaError_t population_split(rrea_dev::TileColumns const& t, int64_t n, double min_w, PopulationWork*& work,
+                             int64_t first_id, int64_t room, int64_t* added, cudaStream_t stream);
+
 }  // namespace rrea_launch

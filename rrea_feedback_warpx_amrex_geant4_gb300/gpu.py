@@ -88,7 +88,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_seed_schedule_load", "rrea_gpu_seed_schedule_free", "rrea_gpu_seed_schedule_size",
     "rrea_gpu_seed_schedule_events", "rrea_gpu_seed_schedule_validate", "rrea_gpu_seed_schedule_last_error",
     "rrea_gpu_inject_seeds_resident", "rrea_gpu_thin_cic_groups", "rrea_gpu_census_resident",
-    "rrea_gpu_deposit_charge_resident",
+    "rrea_gpu_deposit_charge_resident", "rrea_gpu_population_thin_resident", "rrea_gpu_population_split_resident",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -157,6 +157,9 @@ def load_library(path=LIB_PATH):
                                              ctypes.POINTER(ctypes.c_int32), _i64p]
     lib.rrea_gpu_compact_resident.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_deposit_charge_resident.argtypes = [vp, _D]
+    lib.rrea_gpu_population_thin_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                                      ctypes.c_uint64, vp, ctypes.c_int64, _i64p]
+    lib.rrea_gpu_population_split_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_double, _i64p]
     lib.rrea_gpu_census_resident.argtypes = [vp, ctypes.c_int32, _D, ctypes.c_int32, _D, ctypes.c_int32, _D]
     lib.rrea_gpu_resident_count.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
@@ -459,6 +462,30 @@ class RreaGpuContext:
             g, mx.ctypes.data_as(i64), k.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), removed.ctypes.data_as(i64),
             draws.ctypes.data_as(i64), valid.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cap.ctypes.data_as(i64)))
         return w, removed, draws, valid, cap
+
+    POPULATION_STATS = ("members", "live", "candidates", "supports", "capacity", "floor", "requested", "removed")
+
+    def population_thin(self, species, target, step, salt=0, candidates=None):
+        """Global CIC thinning plan of adaptive_resample_v1 over the resident
+        tile of `species` and its candidates (the last drain's survivors, or
+        a SECONDARY_DTYPE array updated in place); returns the plan's stats."""
+        stats = np.zeros(8, dtype=np.int64)
+        if candidates is None:
+            ptr, n = None, 0
+        else:
+            assert candidates.dtype == SECONDARY_DTYPE and candidates.flags.c_contiguous
+            ptr, n = ctypes.c_void_p(candidates.ctypes.data) if len(candidates) else None, len(candidates)
+        self._check(self.lib.rrea_gpu_population_thin_resident(
+            self.handle, int(species), int(target), int(step), int(salt), ptr, n,
+            stats.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return dict(zip(self.POPULATION_STATS, (int(v) for v in stats)))
+
+    def population_split(self, species, target, split_min_weight):
+        """Split refill of the resident tile; returns the clones added."""
+        added = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_population_split_resident(self.handle, int(species), int(target),
+                                                                float(split_min_weight), ctypes.byref(added)))
+        return added.value
 
     def deposit_charge(self):
         """Cell-centred CIC charge of the resident electrons (-w) and
