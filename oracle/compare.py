@@ -2,12 +2,10 @@
 
 Parity comparison of one GPU species phase (electron, positron or photon) against the
 oracle on the same input tile.  Discrete results (dispositions, substep and hazard-draw counts,
-validity, secondary keys) must match exactly; FP64 state within 1e-12
-relative (positions with a 1e-12 x domain-size floor), with a bounded tail
-(TAIL_FRACTION of the particles, never beyond TAIL_RTOL); cell-source grids,
-which the GPU accumulates with atomics in nondeterministic order, within
-1.6e-11 of each grid's largest cell, except the few cells the tail particles
-deposit into, which stay within 1.6e-9.
+validity, secondary keys) must match exactly; every FP64 state entry within
+1e-12 relative (positions with a 1e-12 x domain-size floor); cell-source
+grids, which the GPU accumulates with atomics in nondeterministic order,
+within 1e-12 of each grid's largest cell.
 """
 import numpy as np
 
@@ -15,14 +13,6 @@ from . import oracle as _oracle
 from rrea_feedback_warpx_amrex_geant4_gb300.workloads import copy_tile
 
 RTOL = 1.0e-12
-# Continuous state after many substeps: a one-ulp difference between the
-# device libm and glibc in a small-angle cos(theta) is amplified by
-# 1/sin(theta) in the reference's own deflection formula
-# (sin = sqrt(1 - cos^2)), so a few particles per thousand may sit above
-# RTOL.  At most TAIL_FRACTION of the compared particles (at least one) may
-# exceed RTOL, and none may exceed TAIL_RTOL.
-TAIL_FRACTION = 1.0e-3
-TAIL_RTOL = 1.0e-10
 
 
 def _close(a, b, rtol, atol):
@@ -31,30 +21,23 @@ def _close(a, b, rtol, atol):
     return np.abs(a - b) <= atol + rtol * np.maximum(np.abs(a), np.abs(b))
 
 
-def _tail_ok(a, b, atol):
-    """True when all entries are within TAIL_RTOL and only the allowed tail
-    exceeds RTOL; returns (ok, n_over_rtol)."""
+def entries_ok(a, b, atol):
+    """True when every entry is within RTOL (relative, with the absolute
+    floor atol); returns (ok, n_over_rtol)."""
     strict = _close(a, b, RTOL, atol)
-    loose = _close(a, b, TAIL_RTOL, np.asarray(atol, dtype=np.float64) * (TAIL_RTOL / RTOL))
     n_over = int((~strict).sum())
-    allowed = max(1, int(TAIL_FRACTION * strict.size))
-    return bool(loose.all() and n_over <= allowed), n_over
+    return n_over == 0, n_over
 
 
 def cells_ok(g, o):
-    """Cell grid check: every cell within 16 RTOL of the grid's largest cell,
-    except at most four cells per tail particle allowance (the order-1
-    stencil of a deposit spans four cells), which must stay within
-    16 TAIL_RTOL.  Returns (ok, n_over_strict)."""
+    """Cell grid check: every cell within RTOL of the grid's largest cell.
+    Returns (ok, n_over)."""
     g = np.asarray(g, dtype=np.float64)
     o = np.asarray(o, dtype=np.float64)
     scale = max(np.abs(o).max(), 1e-300)
-    strict = _close(g, o, 0.0, RTOL * scale * 16)
-    loose = _close(g, o, 0.0, TAIL_RTOL * scale * 16)
+    strict = _close(g, o, 0.0, RTOL * scale)
     n_over = int((~strict).sum())
-    nonzero = int(((g != 0.0) | (o != 0.0)).sum())
-    allowed = 4 * max(1, int(TAIL_FRACTION * nonzero))
-    return bool(loose.all() and n_over <= allowed), n_over
+    return n_over == 0, n_over
 
 
 def _worst(a, b, atol):
@@ -121,14 +104,14 @@ def compare(cfg, gpu, orc, domain_scale, parent_energy=None):
     alive = (o_arr["id"] > 0) & (o["disposition"] == 0)
     atol_pos = RTOL * domain_scale
     for name, atol in (("z", atol_pos), ("r", atol_pos)):
-        ok, n_over = _tail_ok(g_arr[name][alive], o_arr[name][alive], atol)
+        ok, n_over = entries_ok(g_arr[name][alive], o_arr[name][alive], atol)
         if not ok:
             w = _worst(g_arr[name][alive], o_arr[name][alive], atol)
             problems.append(f"{name} differs for {n_over} survivors (worst {w:.2e})")
     gx, gy = g_arr["r"] * np.cos(g_arr["theta"]), g_arr["r"] * np.sin(g_arr["theta"])
     ox, oy = o_arr["r"] * np.cos(o_arr["theta"]), o_arr["r"] * np.sin(o_arr["theta"])
     for name, a, b in (("x", gx, ox), ("y", gy, oy)):
-        ok, n_over = _tail_ok(a[alive], b[alive], atol_pos * 4)
+        ok, n_over = entries_ok(a[alive], b[alive], atol_pos * 4)
         if not ok:
             w = _worst(a[alive], b[alive], atol_pos * 4)
             problems.append(f"{name} differs for {n_over} survivors (worst {w:.2e})")
@@ -136,7 +119,7 @@ def compare(cfg, gpu, orc, domain_scale, parent_energy=None):
     moved = o["disposition"] <= 1
     moved &= o["disposition"] >= 0
     for name in ("ux", "uy", "uz"):
-        ok, n_over = _tail_ok(g_arr[name][moved], o_arr[name][moved], RTOL * umag[moved])
+        ok, n_over = entries_ok(g_arr[name][moved], o_arr[name][moved], RTOL * umag[moved])
         if not ok:
             strict = _close(g_arr[name][moved], o_arr[name][moved], RTOL, RTOL * umag[moved])
             w = _worst(g_arr[name][moved], o_arr[name][moved], RTOL * umag[moved])
@@ -161,7 +144,7 @@ def compare(cfg, gpu, orc, domain_scale, parent_energy=None):
         for key, atol in (("x", atol_pos), ("y", atol_pos), ("z", atol_pos), ("dir_x", atol_dir),
                           ("dir_y", atol_dir), ("dir_z", atol_dir), ("weight", 0.0), ("energy_eV", atol_e),
                           ("birth_fraction", RTOL)):
-            ok, n_over = _tail_ok(g_sec[key], os_[key], atol)
+            ok, n_over = entries_ok(g_sec[key], os_[key], atol)
             if not ok:
                 w = _worst(g_sec[key], os_[key], atol)
                 problems.append(f"secondary {key} differs for {n_over} (worst {w:.2e})")

@@ -1,0 +1,2 @@
+#pragma once
+#include "amrex_single_box.hpp"

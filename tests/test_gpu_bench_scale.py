@@ -9,11 +9,9 @@ net-chord current.  The oracle runs the same step on the same staged tiles.
 
 Exact: tile sizes, ids and their order after commit and compaction (so
 every disposition, secondary count and FIFO survivor agreed), weights.
-FP64 state: within 1e-12 relative (positions: of the domain size), with the
-bounded tail of oracle/compare.py (at most 0.1 % of the particles, none
-beyond 1e-10); the tail counts are printed.  Field after the update:
-within 1e-10 of each vector's largest entry (the current comes from
-positions that agree to the same tail)."""
+FP64 state: every entry within 1e-12 relative (positions: of the domain
+size).  Field after the update: within 1e-12 of each vector's largest
+entry."""
 import os
 import sys
 
@@ -89,10 +87,10 @@ def test_one_bench_step_matches_oracle(mods):
         umag = np.sqrt(want["ux"] ** 2 + want["uy"] ** 2 + want["uz"] ** 2)
         for f in ("r", "z", "ux", "uy", "uz"):
             atol = compare.RTOL * (scale if f in ("r", "z") else umag)
-            ok, n_over = compare._tail_ok(have[f], want[f], atol)
+            ok, n_over = compare.entries_ok(have[f], want[f], atol)
             report.append(f"{NAMES[s]}.{f}: {n_over} of {len(want[f])} above 1e-12")
             assert ok, f"{NAMES[s]} {f}: {n_over} outside the tolerance"
     print("; ".join(report))
     for name, a, b in zip(("er", "ez", "bt"), field_after, (run.field["er"], run.field["ez"], run.field["bt"])):
         big = max(np.abs(b).max(), 1e-300)
-        np.testing.assert_allclose(a, b, rtol=0, atol=1e-10 * big, err_msg=name)
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-12 * big, err_msg=name)

@@ -108,4 +108,4 @@ def test_particle_charge_matches_restatement(env):
                                           q * t["w"][v])
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * np.abs(want).max())
     total = sum((-1.0 if s == 0 else 1.0) * t["w"][t["id"] > 0].sum() for s, t in tiles)
-    assert abs(got.sum() - total) <= 1e-10 * sum(t["w"].sum() for _, t in tiles)
+    assert abs(got.sum() - total) <= 1e-12 * sum(t["w"].sum() for _, t in tiles)

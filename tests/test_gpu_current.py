@@ -2,7 +2,7 @@
 on the GPU vs the oracle's replay of the same step's segments, through the
 C-ABI (rrea_gpu_download_current_index / rrea_gpu_download_current).
 
-Tolerance: every padded grid within 1e-9 of its largest entry (the GPU sums
+Tolerance: every padded grid within 1e-12 of its largest entry (the GPU sums
 with atomics in arbitrary order, and the segment endpoints are the transport
 results, equal to the oracle's within 1e-12 relative).  The continuity
 identity drho + dt div J = 0 is checked on the GPU output alone, to 1e-12 of
@@ -48,10 +48,10 @@ def _run(mods, case, n, species, arr, dt=5.0e-10, step=0):
 def _assert_grids(gi, phys, ref):
     for key in ("rho", "jr", "jz"):
         scale = max(np.abs(ref[key]).max(), 1e-300)
-        np.testing.assert_allclose(gi[key], ref[key], rtol=0, atol=1e-9 * scale, err_msg=key)
+        np.testing.assert_allclose(gi[key], ref[key], rtol=0, atol=1e-12 * scale, err_msg=key)
     for got, key in zip(phys, ("jr_phys", "jz_phys")):
         scale = max(np.abs(ref[key]).max(), 1e-300)
-        np.testing.assert_allclose(got, ref[key], rtol=0, atol=1e-9 * scale, err_msg=key)
+        np.testing.assert_allclose(got, ref[key], rtol=0, atol=1e-12 * scale, err_msg=key)
 
 
 @pytest.mark.parametrize("species", ["electron", "positron"])

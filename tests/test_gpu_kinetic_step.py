@@ -10,9 +10,9 @@ pending records with its drain survivors appended as new particles, and the
 field the GPU left on the device (downloaded bit for bit for the oracle).
 
 Tolerances as in the per-phase tests: each phase through the shared phase
-comparison (discrete outcomes exact, FP64 state within 1e-12 with the
-bounded tail); survivor keys bit-exact;
-the net-chord current within 1e-9 of its largest entry (atomics); the field
+comparison (discrete outcomes exact, FP64 state within 1e-12); survivor keys
+bit-exact; the net-chord current within 1e-12 of its largest entry (atomics
+sum the signed index fluxes in nondeterministic order); the field
 update within 1e-12 of each vector's largest entry given the GPU's current."""
 import numpy as np
 import pytest
@@ -99,7 +99,7 @@ def test_three_kinetic_steps_match_oracle(mods):
         gi = ctx.current_index()
         for key in ("rho", "jr", "jz"):
             scale = max(np.abs(cur[key]).max(), 1e-300)
-            np.testing.assert_allclose(gi[key], cur[key], rtol=0, atol=1e-9 * scale, err_msg=f"{key} step {step}")
+            np.testing.assert_allclose(gi[key], cur[key], rtol=0, atol=1e-12 * scale, err_msg=f"{key} step {step}")
         jr, jz = ctx.current()
         before = ctx.field()
         ctx.advance_field(DT_S, SUBSTEPS)

@@ -10,11 +10,8 @@ start from bit-identical input.
 Tolerances: survivor count, order and keys (species, process, root species,
 parent index, root key, lineage) bit-exact; birth fraction exactly 1; FP64
 payload within 1e-12 (positions with a 1e-12 x domain floor, energies
-relative; at most 0.1% of survivors may reach 1e-10, where a small-angle
-deflection amplifies a one-ulp libm difference); cell sources within
-1.6e-11 of each grid's largest cell (the few cells of tail particles within
-1.6e-9) and the net-chord current within 1e-9 of its largest entry (both
-summed with atomics in arbitrary order)."""
+relative); cell sources and the net-chord current within 1e-12 of each
+grid's largest entry (both summed with atomics in arbitrary order)."""
 import numpy as np
 import pytest
 
@@ -65,7 +62,7 @@ def _compare_survivors(compare, cfg, got, ref):
     for key, atol in (("x", compare.RTOL * scale), ("y", compare.RTOL * scale), ("z", compare.RTOL * scale),
                       ("dir_x", compare.RTOL), ("dir_y", compare.RTOL), ("dir_z", compare.RTOL),
                       ("energy_eV", compare.RTOL * np.abs(ref["energy_eV"]))):
-        ok, n_over = compare._tail_ok(got[key], ref[key], atol)
+        ok, n_over = compare.entries_ok(got[key], ref[key], atol)
         assert ok, f"survivor {key} differs for {n_over} (worst {compare._worst(got[key], ref[key], atol):.2e})"
 
 
@@ -80,7 +77,7 @@ def _compare_current(oracle, cfg, ctx, dt_s, o):
     gi = ctx.current_index()
     for key in ("rho", "jr", "jz"):
         scale = max(np.abs(ref[key]).max(), 1e-300)
-        np.testing.assert_allclose(gi[key], ref[key], rtol=0, atol=1e-9 * scale, err_msg=key)
+        np.testing.assert_allclose(gi[key], ref[key], rtol=0, atol=1e-12 * scale, err_msg=key)
 
 
 @pytest.mark.parametrize("case,n,dt_s,capacity,periodic", [

@@ -2,13 +2,12 @@
 C-ABI drop-in entry point rrea_gpu_apply_photons.
 
 Tolerances: dispositions, hazard-draw counts, validity and secondary keys
-(species, process, parent, lineage, root key) bit-exact; FP64 state within
-1e-12 relative (positions with a 1e-12 x domain floor; at most 0.1% of
-particles may reach 1e-10, where a small-angle deflection amplifies a
-one-ulp libm difference); secondary energies
+(species, process, parent, lineage, root key) bit-exact; every FP64 state
+entry within 1e-12 relative (positions with a 1e-12 x domain floor);
+secondary energies
 and directions within 1e-12 of the parent photon's energy scale (they are
 differences of parent-scale quantities); atomically accumulated cell
-sources within 1.6e-11 of each grid's largest cell."""
+sources within 1e-12 of each grid's largest cell."""
 import numpy as np
 import pytest
 

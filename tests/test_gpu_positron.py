@@ -2,12 +2,11 @@
 drop-in entry point rrea_gpu_apply_positrons.
 
 Tolerances: dispositions, substep and hazard-draw counts, validity and
-secondary keys bit-exact; FP64 state within 1e-12 relative (positions with
-a 1e-12 x domain floor; at most 0.1% of particles may reach 1e-10, where a
-small-angle deflection amplifies a one-ulp libm difference); secondary
+secondary keys bit-exact; every FP64 state entry within 1e-12 relative
+(positions with a 1e-12 x domain floor); secondary
 energies and directions within 1e-12 of the parent's total energy scale (K + 2 m c^2: the in-flight annihilation
 photon direction is a momentum difference at that scale); atomically
-accumulated cell sources within 1.6e-11 of each grid's largest cell."""
+accumulated cell sources within 1e-12 of each grid's largest cell."""
 import numpy as np
 import pytest
 

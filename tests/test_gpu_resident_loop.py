@@ -7,7 +7,7 @@ restatement of the overlay's particle creation.
 The oracle starts every step from the GPU's fetched tiles (lockstep), so a
 one-ulp difference of one step cannot grow into a different history in the
 next.  Tolerances: tile sizes, ids and their order, and weights exact; FP64
-state within 1e-12 relative with the bounded tail of the phase tests."""
+state within 1e-12 relative, as in the phase tests."""
 import numpy as np
 import pytest
 
@@ -94,7 +94,7 @@ def test_two_resident_steps_with_commit_match_oracle(mods):
             umag = np.sqrt(want["ux"] ** 2 + want["uy"] ** 2 + want["uz"] ** 2)
             for f in ("r", "z", "ux", "uy", "uz"):
                 scale = np.abs(want[f]) + 1.0 if f in ("r", "z") else umag
-                ok, n_over = compare._tail_ok(got[f], want[f], compare.RTOL * scale)
+                ok, n_over = compare.entries_ok(got[f], want[f], compare.RTOL * scale)
                 assert ok, f"step {step} {NAMES[s]} {f}: {n_over} outside tolerance"
         committed_total += int(committed.sum())
     assert committed_total > 0, "no survivors were committed: the workload does not exercise the commit"
