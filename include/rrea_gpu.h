@@ -608,6 +608,154 @@ void rrea_gpu_seed_schedule_last_error(char* buf, size_t size);
 rrea_gpu_status rrea_gpu_inject_seeds_resident(rrea_gpu_ctx* ctx, rrea_gpu_seed_schedule* schedule, double time_s,
                                                double dt_s, int64_t* injected);
 
+/*
+ * ---- Low-energy carrier fluid -------------------------------------------
+ * The three carrier densities of LowEnergyFluidState (S/LowEnergyFluidState.cpp,
+ * S/LowEnergyFluidFaceTransport.cpp) held on the context's cell grid
+ * (nr x nz, index i + nr*j), with their ionization source rates, the
+ * conservative fluid charge, the diagnostic conductivity, and the
+ * caller-evaluated closure fields.  Carrier ordinals: 0 positive ion,
+ * 1 negative ion, 2 low-energy electron (the face-flux component order).
+ */
+enum {
+    RREA_GPU_MOBILITY_ABSOLUTE = 0,       /* "absolute" */
+    RREA_GPU_MOBILITY_EN_TABLE_FLUX = 1,  /* electrons: "en_table_flux_v1" */
+    RREA_GPU_MOBILITY_REDUCED_STP = 2     /* ions: "reduced_stp_density_scaled" */
+};
+enum { RREA_GPU_ATTACHMENT_CONSTANT = 0, RREA_GPU_ATTACHMENT_EN_TABLE = 1 /* "en_table_attachment_v1" */ };
+
+/* LowEnergyFluidConfig (I/LowEnergyFluidState.H:80-124) and the material
+ * substep controls of RreaAmrexAdvanceConfig (I/RreaAmrexAdvance.H:51-58).
+ * rrea_gpu_default_fluid_config() fills the reference defaults. */
+typedef struct {
+    double electron_mobility_m2_per_vs;                  /* 0.1 */
+    double positive_ion_mobility_m2_per_vs;              /* 2e-4 */
+    double negative_ion_mobility_m2_per_vs;              /* 2e-4 */
+    double positive_ion_reduced_mobility_stp_m2_per_vs;  /* 0 */
+    double negative_ion_reduced_mobility_stp_m2_per_vs;  /* 0 */
+    double ion_mobility_density_ratio_floor;             /* 0 */
+    double ion_drift_cfl;                                /* 0.5 */
+    double transport_density_ratio;                      /* 1: Loschmidt-relative, where no ratio field is bound */
+    double attachment_frequency_s;                       /* 2e6 */
+    double electron_ion_recombination_coefficient_m3_per_s; /* 0 */
+    double ion_ion_recombination_coefficient_m3_per_s;      /* 0 */
+    double detachment_frequency_s;                          /* 0 */
+    int32_t ion_drift_enable;                            /* 0 */
+    int32_t electron_drift_enable;                       /* 1 */
+    int32_t electron_mobility_model;                     /* RREA_GPU_MOBILITY_ABSOLUTE */
+    int32_t ion_mobility_model;                          /* RREA_GPU_MOBILITY_ABSOLUTE */
+    int32_t attachment_model;                            /* RREA_GPU_ATTACHMENT_CONSTANT */
+    int32_t material_min_substeps;                       /* 2 */
+    int32_t material_max_substeps;                       /* 64 */
+    int32_t reserved0;
+    double material_conduction_target;                   /* 0.08 */
+    double material_conduction_guard;                    /* 0.1 */
+    double material_diffusion_target;                    /* 0.8 */
+    double material_diffusion_guard;                     /* 1.0 */
+    double material_reaction_target;                     /* 0.08 */
+    double material_reaction_guard;                      /* 0.1 */
+} rrea_gpu_fluid_config;
+
+void rrea_gpu_default_fluid_config(rrea_gpu_fluid_config* cfg);
+
+/* Allocates the fluid state on the context's grid, all zero, and binds the
+ * configuration (validated as ValidateCarrierTransportConfig,
+ * S/LowEnergyFluidFaceTransport.cpp:87-163, plus the model names and
+ * nonnegative finite recombination coefficients).  Calling it again rebinds
+ * the configuration and keeps the state. */
+rrea_gpu_status rrea_gpu_fluid_configure(rrea_gpu_ctx* ctx, const rrea_gpu_fluid_config* cfg);
+
+/* Loads the dry-air electron closure table (LowEnergyElectronClosure::Load,
+ * S/RreaInteractionTables.cpp:3267-3404: exact schema-3 header, strictly
+ * increasing E/N nodes, positive coefficients, the derivation identities
+ * within 1e-9) onto the device. */
+rrea_gpu_status rrea_gpu_fluid_load_closure(rrea_gpu_ctx* ctx, const char* csv_path);
+
+/* Host <-> device copies of the state (each pointer may be NULL to skip it).
+ * set_state writes the carrier densities and the conservative charge;
+ * get_state also reads the conductivity and the Maxwell time. */
+rrea_gpu_status rrea_gpu_fluid_set_state(rrea_gpu_ctx* ctx, const double* n_pos, const double* n_neg,
+                                         const double* n_e, const double* rho_fluid);
+rrea_gpu_status rrea_gpu_fluid_get_state(rrea_gpu_ctx* ctx, double* n_pos, double* n_neg, double* n_e,
+                                         double* rho_fluid, double* sigma, double* tau_m);
+/* Source rates [m^-3 s^-1]: low-energy electrons, positive ions, direct
+ * negative ions. */
+rrea_gpu_status rrea_gpu_fluid_set_source_rates(rrea_gpu_ctx* ctx, const double* s_e, const double* s_pos,
+                                                const double* s_neg);
+rrea_gpu_status rrea_gpu_fluid_get_source_rates(rrea_gpu_ctx* ctx, double* s_e, double* s_pos, double* s_neg);
+/* The Loschmidt-relative density ratio of every cell (the mobility and
+ * closure density; NULL unbinds it and the scalar transport ratio applies). */
+rrea_gpu_status rrea_gpu_fluid_set_density_ratio(rrea_gpu_ctx* ctx, const double* chi);
+/* Caller-evaluated closure fields: electron mobility, attachment frequency
+ * and the RZ diffusion tensor (3 x nr*nz: Drr, Drz, Dzz); NULL skips one. */
+rrea_gpu_status rrea_gpu_fluid_set_closure_fields(rrea_gpu_ctx* ctx, const double* mu_e, const double* nu_att,
+                                                  const double* diffusion3);
+rrea_gpu_status rrea_gpu_fluid_get_closure_fields(rrea_gpu_ctx* ctx, double* mu_e, double* nu_att,
+                                                  double* diffusion3);
+
+/* The kinetic cell sources 0..2 accumulated since rrea_gpu_reset_sources,
+ * normalised by cell volume and dt (RreaEventAccumulator::NormalizeAndSync,
+ * S/RreaEventAccumulator.cpp:280-331) and copied into the fluid source rates
+ * (O/RreaWarpXCoupling.cpp:689-706). */
+rrea_gpu_status rrea_gpu_fluid_take_sources(rrea_gpu_ctx* ctx, double dt_s);
+
+/* Local chemistry over dt (UpdateFromIonizationSource,
+ * S/LowEnergyFluidState.cpp:105-308): exact attachment with the constant or
+ * table frequency, detachment, electron-ion then ion-ion pair loss, the
+ * conservative charge advanced by the source charge.  Fails closed with
+ * RREA_GPU_ERR_INVALID_STATE when the normalised charge residual exceeds
+ * 512 eps (or is not finite); *residual (may be NULL) receives it. */
+rrea_gpu_status rrea_gpu_fluid_react(rrea_gpu_ctx* ctx, double dt_s, int32_t clear_sources, double* residual);
+/* MaxReactionFrequency (S/LowEnergyFluidState.cpp:310-343). */
+rrea_gpu_status rrea_gpu_fluid_max_reaction_frequency(rrea_gpu_ctx* ctx, double* out);
+/* ComputeConductivity and ComputeFluidChargeDensity
+ * (S/LowEnergyFluidState.cpp:345-455). */
+rrea_gpu_status rrea_gpu_fluid_conductivity(rrea_gpu_ctx* ctx);
+rrea_gpu_status rrea_gpu_fluid_charge_density(rrea_gpu_ctx* ctx);
+
+/* BuildElectronClosureCellFields (S/LowEnergyFluidFaceTransport.cpp:1034-1243)
+ * from cell fields er_cell/ez_cell (nr*nz; NULL for both: the cell averages
+ * of the context's total field), writing the mobility, attachment and
+ * diffusion fields.  diag (may be NULL) receives 8 doubles: min E/N, max
+ * E/N [Td], held-below, above-range and invalid cell counts, electron count,
+ * held-below electron count, electron source rate [1/s]. */
+rrea_gpu_status rrea_gpu_fluid_evaluate_closure(rrea_gpu_ctx* ctx, const double* er_cell, const double* ez_cell,
+                                                double* diag);
+
+/* One explicit carrier-transport update over dt with the face field
+ * efr ((nr+1)*nz) / efz (nr*(nz+1)) from the host (both NULL: the context's
+ * total Yee field, scattered plus ambient): PrepareExplicitCarrierTransport,
+ * BuildExplicitFaceTransport and ApplyExplicitCarrierTransport
+ * (S/LowEnergyFluidFaceTransport.cpp:165-954).  flux_r (3*(nr+1)*nz) and
+ * flux_z (3*nr*(nz+1)), species-major, receive the limited number fluxes
+ * (may be NULL).  diag (may be NULL) receives 14 doubles: max face
+ * conductivity, max explicit diffusion number, unlimited max outgoing CFL,
+ * min outflow scale, limited outflow fraction, limited electron-number
+ * fraction, max outgoing CFL, max drift speed, CFL dt, positive-ion centre
+ * r and z, negative-ion centre r and z, mobility-weighted density ratio at
+ * the positive-ion centre.  Fails closed (RREA_GPU_ERR_INVALID_STATE) on a
+ * non-PSD tensor, a diffusion number >= 1, an outgoing CFL above
+ * ion_drift_cfl, or a negative or non-finite density. */
+rrea_gpu_status rrea_gpu_fluid_transport(rrea_gpu_ctx* ctx, double dt_s, const double* efr, const double* efz,
+                                         double* flux_r, double* flux_z, double* diag);
+
+/*
+ * The coupled fluid + Maxwell step of one outer dt (RreaAmrexAdvance::
+ * AdvanceOneStep, S/RreaAmrexAdvance.cpp:593-838): closure fields at the
+ * step start (table models), the stiffness probe choosing the shared
+ * material substeps, then per substep a half reaction, transport with the
+ * limited face flux, the total face current (fluid + the step's kinetic
+ * net-chord current), B / Silver-Mueller / E, the closure fields on the new
+ * field, and the second half reaction; the B restagger, the final
+ * conductivity, and the source rates cleared.  diag (may be NULL) receives
+ * 8 doubles: substeps, full conduction, diffusion and reaction numbers of
+ * the probe, max reaction number, max dt sigma_face / eps0, max diffusion
+ * number, max reaction charge residual.  Guards fail closed
+ * (RREA_GPU_ERR_INVALID_STATE) at the end of the step.  Requires a
+ * non-periodic z and the Yee CFL, like rrea_gpu_advance_field.
+ */
+rrea_gpu_status rrea_gpu_advance_field_coupled(rrea_gpu_ctx* ctx, double dt_s, double* diag);
+
 #ifdef __cplusplus
 }
 #endif

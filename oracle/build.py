@@ -10,13 +10,15 @@ LIB = os.path.join(HERE, "liboracle.so")
 SOURCES = [
     os.path.join(HERE, "oracle_core.cpp"),
     os.path.join(HERE, "oracle_api.cpp"),
+    os.path.join(HERE, "fluid.cpp"),
+    os.path.join(ROOT, "rrea_feedback_warpx_amrex_geant4_gb300", "csrc", "host", "closure_table.cpp"),
     os.path.join(ROOT, "rrea_feedback_warpx_amrex_geant4_gb300", "csrc", "host", "table_set.cpp"),
 ]
 
 
 def build_oracle(force=False):
     deps = SOURCES + [os.path.join(HERE, "oracle_core.hpp"), os.path.join(HERE, "interleave.hpp"),
-                          os.path.join(HERE, "interleave_scenarios.hpp")]
+                          os.path.join(HERE, "interleave_scenarios.hpp"), os.path.join(HERE, "fluid.hpp")]
     if not force and os.path.exists(LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps):
@@ -40,8 +42,8 @@ def build_reference_golden(reference=None):
     reference = reference or reference_dir()
     if not os.path.isdir(os.path.join(reference, "native_amrex_rrea")):
         return None
-    subprocess.check_call(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={reference}"],
-                          cwd=ROOT)
+    subprocess.check_call(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={reference}",
+                           "oracle/_ref/ref_golden", "oracle/_ref/ref_golden_fluid"], cwd=ROOT)
     return os.path.join(HERE, "_ref", "ref_golden")
 
 

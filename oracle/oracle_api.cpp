@@ -3,6 +3,7 @@
 #include "oracle_core.hpp"
 #include "interleave.hpp"
 #include "interleave_scenarios.hpp"
+#include "fluid.hpp"
 
 #include <cstring>
 #include <memory>
@@ -14,6 +15,7 @@ std::unique_ptr<rrea_host::TableSet> g_tables;
 oracle::StepOutputs g_out;
 oracle::CellSources g_cells;
 std::string g_error;
+std::unique_ptr<rrea_host::ClosureTable> g_closure;
 
 int guard(std::exception const& e)
 {
@@ -444,6 +446,145 @@ void oracle_cell_sources(double* out5)
     std::size_t const n = static_cast<std::size_t>(g_cells.nr) * g_cells.nz;
     for (int f = 0; f < 5; ++f) {
         for (std::size_t i = 0; i < n; ++i) out5[f * n + i] = g_cells.f[f].empty() ? 0.0 : g_cells.f[f][i];
+    }
+}
+
+// ---- carrier fluid (oracle/fluid.cpp)
+int oracle_fluid_react(rrea_gpu_fluid_config const* cfg, int64_t n, double dt, double* ne, double* np, double* nn,
+                       double* se, double* sp, double* sn, double* rho, double const* nu, int clear, double* residual)
+{
+    try {
+        *residual = oracle_fluid::react(*cfg, static_cast<std::size_t>(n), dt, ne, np, nn, se, sp, sn, rho, nu, clear != 0);
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+int oracle_fluid_max_reaction_frequency(rrea_gpu_fluid_config const* cfg, int64_t n, double const* ne,
+                                        double const* np, double const* nn, double const* nu, double* out)
+{
+    try {
+        *out = oracle_fluid::max_reaction_frequency(*cfg, static_cast<std::size_t>(n), ne, np, nn, nu);
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+int oracle_fluid_conductivity(rrea_gpu_fluid_config const* cfg, int64_t n, double const* ne, double const* np,
+                              double const* nn, double const* chi, double const* mu, double* sigma, double* tau)
+{
+    try {
+        oracle_fluid::conductivity(*cfg, static_cast<std::size_t>(n), ne, np, nn, chi, mu, sigma, tau);
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+void oracle_fluid_charge_density(int64_t n, double const* ne, double const* np, double const* nn, double* rho)
+{
+    oracle_fluid::charge_density(static_cast<std::size_t>(n), ne, np, nn, rho);
+}
+
+int oracle_fluid_load_closure(char const* path)
+{
+    try {
+        g_closure = std::make_unique<rrea_host::ClosureTable>(rrea_host::load_closure_table(path));
+        return 0;
+    } catch (std::exception const& e) {
+        g_error = e.what();
+        return RREA_GPU_ERR_TABLES;
+    }
+}
+
+int oracle_fluid_closure_fields(int nr, int nz, double r_lo, double z_lo, double dr, double dz, double scalar_chi,
+                                double const* er, double const* ez, double const* chi, double const* ne,
+                                double const* src, double* mu, double* nu, double* diff3, double* diag8)
+{
+    try {
+        if (!g_closure) oracle::fail(RREA_GPU_ERR_NOT_READY, "no closure table loaded");
+        oracle_fluid::ClosureDiag d;
+        oracle_fluid::closure_fields(*g_closure, oracle_fluid::Grid{nr, nz, r_lo, z_lo, dr, dz, false}, scalar_chi, er,
+                                     ez, chi, ne, src, mu, nu, diff3, d);
+        double const v[8] = {d.min_en, d.max_en, d.held_below, d.above_range, d.invalid, d.electron_count,
+                             d.held_below_count, d.source_rate};
+        std::memcpy(diag8, v, sizeof(v));
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+int oracle_fluid_transport(rrea_gpu_fluid_config const* cfg, int nr, int nz, double r_lo, double z_lo, double dr,
+                           double dz, int periodic_z, double dt, double* n_pos, double* n_neg, double* n_e, double* rho,
+                           double const* chi, double const* mu, double const* diff3, double const* efr,
+                           double const* efz, double* flux_r, double* flux_z, double* raw_r, double* raw_z,
+                           double* diag14)
+{
+    try {
+        oracle_fluid::TransportDiag d;
+        double* const dens[3] = {n_pos, n_neg, n_e};
+        oracle_fluid::transport(*cfg, oracle_fluid::Grid{nr, nz, r_lo, z_lo, dr, dz, periodic_z != 0}, dt, dens, rho,
+                                chi, mu, diff3, efr, efz, flux_r, flux_z, raw_r, raw_z, d);
+        double const v[14] = {d.max_face_conductivity, d.max_diffusion_number, d.unlimited_max_outgoing_cfl,
+                              d.min_outflow_scale, d.limited_outflow_fraction, d.limited_electron_number_fraction,
+                              d.max_outgoing_cfl, d.max_drift_speed, d.cfl_dt, d.pos_center_r, d.pos_center_z,
+                              d.neg_center_r, d.neg_center_z, d.density_ratio_at_pos_center};
+        std::memcpy(diag14, v, sizeof(v));
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
+    }
+}
+
+int oracle_fluid_coupled_step(rrea_gpu_fluid_config const* cfg, int nr, int nz, double z_lo, double dr, double dz,
+                              double dt, double* er, double* ez, double* bt, double const* amb_er, double const* amb_ez,
+                              double const* jr_kin, double const* jz_kin, double* ne, double* np, double* nn, double* rho,
+                              double* se, double* sp, double* sn, double const* chi, double* mu, double* nu,
+                              double* diff3, double* sigma, double* diag8)
+{
+    try {
+        std::size_t const n = static_cast<std::size_t>(nr) * nz;
+        std::size_t const nfr = static_cast<std::size_t>(nr + 1) * nz, nfz = static_cast<std::size_t>(nr) * (nz + 1);
+        oracle::MaxwellField f;
+        f.nr = nr;
+        f.nz = nz;
+        f.dr = dr;
+        f.dz = dz;
+        f.er.assign(er, er + nfr);
+        f.ez.assign(ez, ez + nfz);
+        f.bt.assign(bt, bt + static_cast<std::size_t>(nr + 1) * (nz + 1));
+        oracle_fluid::State st;
+        st.ne.assign(ne, ne + n);
+        st.np.assign(np, np + n);
+        st.nn.assign(nn, nn + n);
+        st.rho.assign(rho, rho + n);
+        st.se.assign(se, se + n);
+        st.sp.assign(sp, sp + n);
+        st.sn.assign(sn, sn + n);
+        oracle_fluid::CoupledDiag d;
+        oracle_fluid::coupled_step(*cfg, g_closure.get(), oracle_fluid::Grid{nr, nz, 0.0, z_lo, dr, dz, false}, dt, f,
+                                   std::vector<double>(amb_er, amb_er + nfr), std::vector<double>(amb_ez, amb_ez + nfz),
+                                   std::vector<double>(jr_kin, jr_kin + nfr), std::vector<double>(jz_kin, jz_kin + nfz),
+                                   st, chi, d);
+        std::copy(f.er.begin(), f.er.end(), er);
+        std::copy(f.ez.begin(), f.ez.end(), ez);
+        std::copy(f.bt.begin(), f.bt.end(), bt);
+        for (auto [dst, src] : {std::pair{ne, &st.ne}, {np, &st.np}, {nn, &st.nn}, {rho, &st.rho}, {se, &st.se},
+                                {sp, &st.sp}, {sn, &st.sn}, {sigma, &st.sigma}}) {
+            std::copy(src->begin(), src->end(), dst);
+        }
+        if (mu && !st.mu.empty()) std::copy(st.mu.begin(), st.mu.end(), mu);
+        if (nu && !st.nu.empty()) std::copy(st.nu.begin(), st.nu.end(), nu);
+        if (diff3 && !st.diff3.empty()) std::copy(st.diff3.begin(), st.diff3.end(), diff3);
+        double const v[8] = {static_cast<double>(d.substeps), d.full_conduction, d.full_diffusion, d.full_reaction,
+                             d.max_reaction_number, d.max_dt_sigma, d.max_diffusion_number, d.max_residual};
+        std::memcpy(diag8, v, sizeof(v));
+        return 0;
+    } catch (std::exception const& e) {
+        return guard(e);
     }
 }
 

@@ -4032,8 +4032,10 @@ inline std::size_t ez_at(MaxwellField const& f, int i, int j)
     return static_cast<std::size_t>(i) + static_cast<std::size_t>(f.nr) * j;
 }
 
+}  // namespace
+
 // :143-154, dBtheta/dt = dEz/dr - dEr/dz at interior corners
-void advance_b(MaxwellField& f, double dt)
+void MaxwellAdvanceB(MaxwellField& f, double dt)
 {
     for (int j = 1; j < f.nz; ++j) {
         for (int i = 1; i < f.nr; ++i) {
@@ -4043,7 +4045,7 @@ void advance_b(MaxwellField& f, double dt)
     }
 }
 // :156-175, first-order Silver-Mueller on the outer r and both z faces
-void silver_mueller(MaxwellField& f)
+void MaxwellSilverMueller(MaxwellField& f)
 {
     for (int j = 0; j <= f.nz; ++j) f.bt[er_at(f, f.nr, j)] = -f.ez[ez_at(f, f.nr - 1, j)] / kC;
     for (int i = 1; i <= f.nr; ++i) {
@@ -4053,7 +4055,7 @@ void silver_mueller(MaxwellField& f)
     for (int j = 0; j <= f.nz; ++j) f.bt[er_at(f, 0, j)] = 0.0;
 }
 // :177-214 with no conductivity and no ambient term
-void advance_e(MaxwellField& f, double dt, std::vector<double> const& jr, std::vector<double> const& jz)
+void MaxwellAdvanceE(MaxwellField& f, double dt, std::vector<double> const& jr, std::vector<double> const& jz)
 {
     double const c2dt = dt / (kEps0 * kMu0);
     for (int j = 0; j < f.nz; ++j) {
@@ -4077,8 +4079,6 @@ void advance_e(MaxwellField& f, double dt, std::vector<double> const& jr, std::v
     }
 }
 
-}  // namespace
-
 void AdvanceMaxwell(MaxwellField& f, double dt_s, int substeps, std::vector<double> const& jr,
                     std::vector<double> const& jz)
 {
@@ -4087,14 +4087,14 @@ void AdvanceMaxwell(MaxwellField& f, double dt_s, int substeps, std::vector<doub
     if (!std::isfinite(cfl) || !(cfl < 1.0)) fail(RREA_GPU_ERR_ARGUMENT, "Maxwell TM violates the Yee CFL condition");
     double const dts = dt_s / static_cast<double>(substeps);
     double const restagger = 0.5 * (dt_s - dts);
-    advance_b(f, restagger);
+    MaxwellAdvanceB(f, restagger);
     for (int k = 0; k < substeps; ++k) {
-        advance_b(f, dts);
-        silver_mueller(f);
-        advance_e(f, dts, jr, jz);
+        MaxwellAdvanceB(f, dts);
+        MaxwellSilverMueller(f);
+        MaxwellAdvanceE(f, dts, jr, jz);
     }
-    advance_b(f, -restagger);
-    silver_mueller(f);
+    MaxwellAdvanceB(f, -restagger);
+    MaxwellSilverMueller(f);
 }
 
 // O/RreaCouplingSources.cpp:435-512 + S/RreaEventAccumulator.cpp:129-164, 386-502

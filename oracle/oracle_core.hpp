@@ -246,6 +246,12 @@ struct MaxwellField {
 // Throws on a CFL violation.
 void AdvanceMaxwell(MaxwellField& f, double dt_s, int substeps, std::vector<double> const& jr,
                     std::vector<double> const& jz);
+// Its three leapfrog pieces (I/RreaMaxwellTMRZ.H:143-214): B at the interior
+// corners, first-order Silver-Mueller on the open faces, E with the face
+// current and no conductivity.
+void MaxwellAdvanceB(MaxwellField& f, double dt);
+void MaxwellSilverMueller(MaxwellField& f);
+void MaxwellAdvanceE(MaxwellField& f, double dt, std::vector<double> const& jr, std::vector<double> const& jz);
 
 // Transport density ratio at an axial position, TransportDensityRatioAtZ
 // (O/RreaWarpXCoupling.cpp:79-95): the configured uniform ratio, or, with an

@@ -2,6 +2,8 @@
 // interfaces each function follows).
 #include "seed_schedule.hpp"
 
+#include "csv_text.hpp"
+
 #include <algorithm>
 #include <cctype>
 #include <cmath>
@@ -20,41 +22,8 @@ constexpr double kC = 299792458.0;      // I/RreaConstants.H:10
 
 [[noreturn]] void fail(int code, std::string const& msg) { throw SeedScheduleError(code, msg); }
 
-// The CSV text convention of the reference's tables, profiles and schedules
-// (I/RreaCsvTextUtil.H): cells are whitespace-trimmed, commas inside quotes
-// are protected, a doubled quote inside quotes is one literal quote.
-std::string trim(std::string const& s)
-{
-    std::size_t b = 0, e = s.size();
-    while (b < e && std::isspace(static_cast<unsigned char>(s[b]))) ++b;
-    while (e > b && std::isspace(static_cast<unsigned char>(s[e - 1]))) --e;
-    return s.substr(b, e - b);
-}
-
-std::vector<std::string> split_cells(std::string const& line)
-{
-    std::vector<std::string> cells;
-    std::string cell;
-    bool quoted = false;
-    for (std::size_t i = 0; i < line.size(); ++i) {
-        char const c = line[i];
-        if (c == '"') {
-            if (quoted && i + 1 < line.size() && line[i + 1] == '"') {
-                cell.push_back('"');
-                ++i;
-            } else {
-                quoted = !quoted;
-            }
-        } else if (c == ',' && !quoted) {
-            cells.push_back(trim(cell));
-            cell.clear();
-        } else {
-            cell.push_back(c);
-        }
-    }
-    cells.push_back(trim(cell));
-    return cells;
-}
+using csv::split_cells;
+using csv::trim;
 
 // A whole cell must parse as one number (S/RreaSeedSchedule.cpp:28-39).
 template <typename T>
