@@ -34,9 +34,14 @@ SOURCES = [
     os.path.join(CSRC, "rrea_field.cu"),
     os.path.join(CSRC, "rrea_census.cu"),
     os.path.join(CSRC, "rrea_population.cu"),
+    os.path.join(CSRC, "rrea_fluid.cu"),
     os.path.join(CSRC, "host", "table_set.cpp"),
     os.path.join(CSRC, "host", "seed_schedule.cpp"),
+    os.path.join(CSRC, "host", "closure_table.cpp"),
 ]
+# Sources compiled without FMA contraction whatever the variant: the carrier
+# fluid rounds every product and sum like the reference's host build.
+NO_FMAD = ("rrea_fluid.cu",)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -88,7 +93,7 @@ def build(force=False, verbose=False):
     os.makedirs(objdir, exist_ok=True)
     nvcc = _nvcc()
     fmad = "false" if os.environ.get("RREA_FMAD", "1") == "0" else "true"
-    common = ["-std=c++17", "-O3", "-lineinfo", f"--fmad={fmad}", "-Xcompiler", "-fPIC,-ffp-contract=off",
+    common = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I", CSRC, "-I", os.path.join(ROOT, "include")] + ARCH
     if os.environ.get("RREA_LIBM", "0") == "1":
         common += ["-DRREA_CUDA_LIBM"]
@@ -99,6 +104,7 @@ def build(force=False, verbose=False):
     for src in SOURCES:
         obj = os.path.join(objdir, os.path.basename(src) + ".o")
         cmd = [nvcc, "-c", src, "-o", obj] + common
+        cmd += ["--fmad=false" if os.path.basename(src) in NO_FMAD else f"--fmad={fmad}"]
         if src.endswith(".cpp"):
             cmd = [nvcc, "-x", "cu", "-c", src, "-o", obj] + common
         procs.append((subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT), cmd))

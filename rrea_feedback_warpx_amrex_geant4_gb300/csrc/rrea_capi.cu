@@ -8,6 +8,7 @@
 
 #include "device/rrea_electron_args.cuh"
 #include "device/rrea_resample.cuh"
+#include "host/closure_table.hpp"
 #include "host/seed_schedule.hpp"
 #include "host/table_set.hpp"
 #include "rrea_kernels.h"
@@ -195,6 +196,7 @@ struct rrea_gpu_ctx {
     double* d_rho_cells = nullptr;       // particle charge grid nr*nz (first deposit call)
     rrea_launch::PopulationWork* pop_work = nullptr;  // population-control plan scratch (first use)
     rrea_gpu_secondary* d_pc_cand = nullptr;          // host candidates of a population-control call
+    rrea_launch::FluidState* fluid = nullptr;         // low-energy carrier fluid (rrea_gpu_fluid_configure)
     int64_t pc_cand_cap = 0;
     uint64_t* d_child_lineage = nullptr;
     unsigned long long* d_invalid = nullptr;
@@ -405,6 +407,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     if (!ctx) return RREA_GPU_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     dfree(ctx->d_arena);
+    rrea_launch::fluid_free(ctx->fluid);
     dfree(ctx->d_er);
     dfree(ctx->d_ez);
     dfree(ctx->d_bt);
@@ -2040,6 +2043,344 @@ rrea_gpu_status rrea_gpu_stream(rrea_gpu_ctx* ctx, void** stream)
     if (!ctx || !stream) return RREA_GPU_ERR_ARGUMENT;
     *stream = ctx->stream;
     return RREA_GPU_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Low-energy carrier fluid (rrea_fluid.cu)
+// ===========================================================================
+namespace {
+
+rrea_gpu_status fluid_ready(rrea_gpu_ctx* ctx)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->fluid) return fail(ctx, RREA_GPU_ERR_NOT_READY, "the carrier fluid is not configured");
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status fluid_checked(rrea_gpu_ctx* ctx, bool ok)
+{
+    return ok ? RREA_GPU_OK : fail(ctx, RREA_GPU_ERR_INVALID_STATE, rrea_launch::fluid_error(*ctx->fluid));
+}
+
+rrea_gpu_status fluid_copy(rrea_gpu_ctx* ctx, int field, const double* host, int64_t count)
+{
+    if (!host) return RREA_GPU_OK;
+    RREA_CUDA(ctx, cudaMemcpyAsync(rrea_launch::fluid_field(*ctx->fluid, field), host, sizeof(double) * count,
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status fluid_fetch(rrea_gpu_ctx* ctx, int field, double* host, int64_t count)
+{
+    if (!host) return RREA_GPU_OK;
+    RREA_CUDA(ctx, cudaMemcpyAsync(host, rrea_launch::fluid_field(*ctx->fluid, field), sizeof(double) * count,
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    return RREA_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rrea_gpu_default_fluid_config(rrea_gpu_fluid_config* c)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    // LowEnergyFluidConfig (I/LowEnergyFluidState.H:80-124)
+    c->electron_mobility_m2_per_vs = 0.1;
+    c->positive_ion_mobility_m2_per_vs = 2.0e-4;
+    c->negative_ion_mobility_m2_per_vs = 2.0e-4;
+    c->ion_drift_cfl = 0.5;
+    c->transport_density_ratio = 1.0;
+    c->attachment_frequency_s = 2.0e6;
+    c->electron_drift_enable = 1;
+    // RreaAmrexAdvanceConfig (I/RreaAmrexAdvance.H:51-58)
+    c->material_min_substeps = 2;
+    c->material_max_substeps = 64;
+    c->material_conduction_target = 0.08;
+    c->material_conduction_guard = 0.1;
+    c->material_diffusion_target = 0.8;
+    c->material_diffusion_guard = 1.0;
+    c->material_reaction_target = 0.08;
+    c->material_reaction_guard = 0.1;
+}
+
+rrea_gpu_status rrea_gpu_fluid_configure(rrea_gpu_ctx* ctx, const rrea_gpu_fluid_config* cfg)
+{
+    if (!ctx || !cfg) return RREA_GPU_ERR_ARGUMENT;
+    if (!(cfg->material_min_substeps >= 1) || !(cfg->material_max_substeps >= cfg->material_min_substeps)
+        || !(cfg->material_conduction_target > 0.0) || !(cfg->material_diffusion_target > 0.0)
+        || !(cfg->material_reaction_target > 0.0)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "invalid material substep controls");
+    }
+    if (!ctx->fluid) {
+        rrea_gpu_config const& c = ctx->cfg;
+        rrea_launch::FluidGrid const g{c.nr, c.nz, c.r_lo, c.z_lo, (c.r_hi - c.r_lo) / c.nr, (c.z_hi - c.z_lo) / c.nz,
+                                       c.periodic_z};
+        RREA_CUDA(ctx, rrea_launch::fluid_create(g, std::max(1, ctx->num_sms * 4), ctx->fluid));
+    }
+    rrea_gpu_fluid_config const previous = rrea_launch::fluid_config(*ctx->fluid);
+    rrea_launch::fluid_set_config(*ctx->fluid, *cfg);
+    if (!rrea_launch::fluid_validate(*ctx->fluid, true)) {
+        std::string const why = rrea_launch::fluid_error(*ctx->fluid);
+        rrea_launch::fluid_set_config(*ctx->fluid, previous);
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, why);
+    }
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_load_closure(rrea_gpu_ctx* ctx, const char* csv_path)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    if (!csv_path) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "no closure table path");
+    try {
+        rrea_host::ClosureTable const t = rrea_host::load_closure_table(csv_path);
+        std::vector<double> cols;
+        for (auto const* v : {&t.en_td, &t.log_en_td, &t.k0, &t.log_k0, &t.nu2, &t.nu3, &t.log_nu3, &t.dl, &t.log_dl,
+                              &t.dt, &t.log_dt}) {
+            cols.insert(cols.end(), v->begin(), v->end());
+        }
+        RREA_CUDA(ctx, rrea_launch::fluid_load_closure(*ctx->fluid, cols, static_cast<int>(t.size())));
+    } catch (std::exception const& e) {
+        return fail(ctx, RREA_GPU_ERR_TABLES, e.what());
+    }
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_set_state(rrea_gpu_ctx* ctx, const double* n_pos, const double* n_neg, const double* n_e,
+                                         const double* rho_fluid)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    int64_t const n = rrea_launch::fluid_cells(*ctx->fluid);
+    for (auto [f, p] : {std::pair{1, n_pos}, {2, n_neg}, {0, n_e}, {3, rho_fluid}}) {
+        if (rrea_gpu_status const s = fluid_copy(ctx, f, p, n)) return s;
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_get_state(rrea_gpu_ctx* ctx, double* n_pos, double* n_neg, double* n_e,
+                                         double* rho_fluid, double* sigma, double* tau_m)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    int64_t const n = rrea_launch::fluid_cells(*ctx->fluid);
+    for (auto [f, p] : {std::pair{1, n_pos}, {2, n_neg}, {0, n_e}, {3, rho_fluid}, {4, sigma}, {5, tau_m}}) {
+        if (rrea_gpu_status const s = fluid_fetch(ctx, f, p, n)) return s;
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_set_source_rates(rrea_gpu_ctx* ctx, const double* s_e, const double* s_pos,
+                                                const double* s_neg)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    int64_t const n = rrea_launch::fluid_cells(*ctx->fluid);
+    for (auto [f, p] : {std::pair{6, s_e}, {7, s_pos}, {8, s_neg}}) {
+        if (rrea_gpu_status const s = fluid_copy(ctx, f, p, n)) return s;
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_get_source_rates(rrea_gpu_ctx* ctx, double* s_e, double* s_pos, double* s_neg)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    int64_t const n = rrea_launch::fluid_cells(*ctx->fluid);
+    for (auto [f, p] : {std::pair{6, s_e}, {7, s_pos}, {8, s_neg}}) {
+        if (rrea_gpu_status const s = fluid_fetch(ctx, f, p, n)) return s;
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_set_density_ratio(rrea_gpu_ctx* ctx, const double* chi)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    int64_t const n = rrea_launch::fluid_cells(*ctx->fluid);
+    if (chi) {
+        for (int64_t k = 0; k < n; ++k) {
+            if (!std::isfinite(chi[k]) || !(chi[k] > 0.0)) {
+                return fail(ctx, RREA_GPU_ERR_ARGUMENT, "density ratios must be finite and positive");
+            }
+        }
+        if (rrea_gpu_status const s = fluid_copy(ctx, 9, chi, n)) return s;
+        RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    rrea_launch::fluid_bind_chi(*ctx->fluid, chi != nullptr);
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_set_closure_fields(rrea_gpu_ctx* ctx, const double* mu_e, const double* nu_att,
+                                                  const double* diffusion3)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    int64_t const n = rrea_launch::fluid_cells(*ctx->fluid);
+    for (auto [f, p, c] : {std::tuple{10, mu_e, n}, {11, nu_att, n}, {12, diffusion3, 3 * n}}) {
+        if (rrea_gpu_status const s = fluid_copy(ctx, f, p, c)) return s;
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_get_closure_fields(rrea_gpu_ctx* ctx, double* mu_e, double* nu_att, double* diffusion3)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    int64_t const n = rrea_launch::fluid_cells(*ctx->fluid);
+    for (auto [f, p, c] : {std::tuple{10, mu_e, n}, {11, nu_att, n}, {12, diffusion3, 3 * n}}) {
+        if (rrea_gpu_status const s = fluid_fetch(ctx, f, p, c)) return s;
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_take_sources(rrea_gpu_ctx* ctx, double dt_s)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    if (!(dt_s > 0.0) || !std::isfinite(dt_s)) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "source normalisation needs dt > 0");
+    RREA_CUDA(ctx, rrea_launch::fluid_take_sources(*ctx->fluid, ctx->d_cells, dt_s, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_react(rrea_gpu_ctx* ctx, double dt_s, int32_t clear_sources, double* residual)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    if (!std::isfinite(dt_s) || dt_s < 0.0) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "the fluid needs dt >= 0");
+    if (!rrea_launch::fluid_validate(*ctx->fluid, false)) return fluid_checked(ctx, false);
+    double r = 0.0;
+    bool ok = false;
+    RREA_CUDA(ctx, rrea_launch::fluid_react(*ctx->fluid, dt_s, clear_sources != 0, r, ok, ctx->stream));
+    if (residual) *residual = r;
+    return fluid_checked(ctx, ok);
+}
+
+rrea_gpu_status rrea_gpu_fluid_max_reaction_frequency(rrea_gpu_ctx* ctx, double* out)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    if (!out) return RREA_GPU_ERR_ARGUMENT;
+    RREA_CUDA(ctx, rrea_launch::fluid_max_reaction_frequency(*ctx->fluid, *out, ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_conductivity(rrea_gpu_ctx* ctx)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    RREA_CUDA(ctx, rrea_launch::fluid_conductivity(*ctx->fluid, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_charge_density(rrea_gpu_ctx* ctx)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    RREA_CUDA(ctx, rrea_launch::fluid_charge_density(*ctx->fluid, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_fluid_evaluate_closure(rrea_gpu_ctx* ctx, const double* er_cell, const double* ez_cell,
+                                                double* diag)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    if (!rrea_launch::fluid_has_closure(*ctx->fluid)) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no closure table loaded");
+    if ((er_cell == nullptr) != (ez_cell == nullptr)) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "give both cell fields or neither");
+    int64_t const n = rrea_launch::fluid_cells(*ctx->fluid);
+    const double* er = ctx->d_cell_er;
+    const double* ez = ctx->d_cell_ez;
+    if (er_cell) {
+        // the face-current buffers hold the host cell fields for this call
+        double* scratch_r = rrea_launch::fluid_field(*ctx->fluid, 13);
+        double* scratch_z = rrea_launch::fluid_field(*ctx->fluid, 14);
+        RREA_CUDA(ctx, cudaMemcpyAsync(scratch_r, er_cell, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(scratch_z, ez_cell, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        er = scratch_r;
+        ez = scratch_z;
+    } else if (!ctx->field_set) {
+        return fail(ctx, RREA_GPU_ERR_NOT_READY, "no field has been set");
+    }
+    double d[8];
+    bool ok = false;
+    RREA_CUDA(ctx, rrea_launch::fluid_closure(*ctx->fluid, er, ez, d, ok, ctx->stream));
+    if (diag) std::memcpy(diag, d, sizeof(d));
+    return fluid_checked(ctx, ok);
+}
+
+rrea_gpu_status rrea_gpu_fluid_transport(rrea_gpu_ctx* ctx, double dt_s, const double* efr, const double* efz,
+                                         double* flux_r, double* flux_z, double* diag)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    if (!std::isfinite(dt_s) || dt_s <= 0.0) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "explicit carrier transport requires finite, positive dt");
+    }
+    if ((efr == nullptr) != (efz == nullptr)) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "give both face fields or neither");
+    if (!rrea_launch::fluid_validate(*ctx->fluid, true)) return fluid_checked(ctx, false);
+    rrea_gpu_config const& c = ctx->cfg;
+    int64_t const nfr = static_cast<int64_t>(c.nr + 1) * c.nz, nfz = static_cast<int64_t>(c.nr) * (c.nz + 1);
+    const double *er = ctx->d_er, *ez = ctx->d_ez, *er_add = ctx->d_amb_er, *ez_add = ctx->d_amb_ez;
+    if (efr) {
+        double* scratch_r = rrea_launch::fluid_field(*ctx->fluid, 13);
+        double* scratch_z = rrea_launch::fluid_field(*ctx->fluid, 14);
+        RREA_CUDA(ctx, cudaMemcpyAsync(scratch_r, efr, sizeof(double) * nfr, cudaMemcpyHostToDevice, ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(scratch_z, efz, sizeof(double) * nfz, cudaMemcpyHostToDevice, ctx->stream));
+        er = scratch_r;
+        ez = scratch_z;
+        er_add = ez_add = nullptr;
+    } else if (!ctx->field_set) {
+        return fail(ctx, RREA_GPU_ERR_NOT_READY, "no field has been set");
+    }
+    double d[14];
+    bool ok = false;
+    RREA_CUDA(ctx, rrea_launch::fluid_transport(*ctx->fluid, dt_s, er, er_add, ez, ez_add, d, ok, ctx->stream));
+    if (flux_r) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(flux_r, rrea_launch::fluid_flux(*ctx->fluid, 0), sizeof(double) * 3 * nfr,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (flux_z) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(flux_z, rrea_launch::fluid_flux(*ctx->fluid, 1), sizeof(double) * 3 * nfz,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (diag) std::memcpy(diag, d, sizeof(d));
+    return fluid_checked(ctx, ok);
+}
+
+rrea_gpu_status rrea_gpu_advance_field_coupled(rrea_gpu_ctx* ctx, double dt_s, double* diag)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    if (!ctx->field_set) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no field has been set");
+    rrea_gpu_config const& c = ctx->cfg;
+    if (c.periodic_z || !ctx->netchord) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "the coupled field step needs a non-periodic z");
+    }
+    double const dr = (c.r_hi - c.r_lo) / c.nr, dz = (c.z_hi - c.z_lo) / c.nz;
+    if (!std::isfinite(dt_s) || !(dt_s > 0.0)) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "the field step needs dt > 0");
+    double const cfl = 299792458.0 * dt_s * std::sqrt(1.0 / (dr * dr) + 1.0 / (dz * dz));
+    if (!std::isfinite(cfl) || !(cfl < 1.0)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "Maxwell TM violates the two-dimensional Yee CFL condition");
+    }
+    if (!rrea_launch::fluid_validate(*ctx->fluid, true)) return fluid_checked(ctx, false);
+    rrea_gpu_fluid_config const& fc = rrea_launch::fluid_config(*ctx->fluid);
+    bool const tables = (fc.electron_drift_enable && fc.electron_mobility_model == RREA_GPU_MOBILITY_EN_TABLE_FLUX)
+        || fc.attachment_model == RREA_GPU_ATTACHMENT_EN_TABLE;
+    if (tables && !rrea_launch::fluid_has_closure(*ctx->fluid)) {
+        return fail(ctx, RREA_GPU_ERR_NOT_READY, "en_table fluid models require a loaded electron closure");
+    }
+    // the step's kinetic face current (ConvertPaddedIndexCurrentToPhysicalRZ)
+    RREA_CUDA(ctx, rrea_launch::netchord_convert(ctx->net, ctx->d_jr_phys, ctx->d_jz_phys, ctx->stream));
+    rrea_launch::CoupledField const f{c.nr,          c.nz,          dr,           dz,
+                                      ctx->d_er,     ctx->d_ez,     ctx->d_bt,    ctx->d_amb_er,
+                                      ctx->d_amb_ez, ctx->d_cell_er, ctx->d_cell_ez, ctx->d_jr_phys,
+                                      ctx->d_jz_phys};
+    double d[8];
+    bool ok = false;
+    RREA_CUDA(ctx, rrea_launch::fluid_coupled_step(*ctx->fluid, f, dt_s, d, ok, ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->has_b = true;
+    if (diag) std::memcpy(diag, d, sizeof(d));
+    return fluid_checked(ctx, ok);
 }
 
 }  // extern "C"

@@ -103,6 +103,35 @@ int blocks_for(int64_t n)
 
 namespace rrea_launch {
 
+cudaError_t maxwell_advance_b(int nr, int nz, double dr, double dz, double dt, const double* er, const double* ez,
+                              double* bt, cudaStream_t stream)
+{
+    if (nr > 1 && nz > 1) {
+        note_launch();
+        rrea_dev::advance_b_kernel<<<rrea_dev::blocks_for(static_cast<int64_t>(nr - 1) * (nz - 1)), 256, 0, stream>>>(
+            nr, nz, dr, dz, dt, er, ez, bt);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t maxwell_silver_mueller(int nr, int nz, const double* er, const double* ez, double* bt, cudaStream_t stream)
+{
+    note_launch();
+    rrea_dev::silver_mueller_kernel<<<rrea_dev::blocks_for(static_cast<int64_t>(nr + 1) * (nz + 1)), 256, 0, stream>>>(
+        nr, nz, er, ez, bt);
+    return cudaGetLastError();
+}
+
+cudaError_t maxwell_advance_e(int nr, int nz, double dr, double dz, double dt, const double* bt, const double* jr,
+                              const double* jz, double* er, double* ez, cudaStream_t stream)
+{
+    note_launch();
+    rrea_dev::advance_e_kernel<<<rrea_dev::blocks_for(static_cast<int64_t>(nr + 1) * nz
+                                                      + static_cast<int64_t>(nr) * (nz + 1)),
+                                 256, 0, stream>>>(nr, nz, dr, dz, dt, bt, jr, jz, er, ez);
+    return cudaGetLastError();
+}
+
 cudaError_t maxwell_step(int nr, int nz, double dr, double dz, double dt, int substeps, double* er, double* ez,
                          double* bt, const double* jr, const double* jz, cudaStream_t stream)
 {

@@ -5,6 +5,9 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+#include <vector>
+
 namespace rrea_dev {
 struct ElectronArgs;
 struct SegmentRec;
@@ -151,5 +154,56 @@ cudaError_t population_thin(PopulationInput const& in, PopulationWork*& work, Po
 // (nothing changed).
 cudaError_t population_split(rrea_dev::TileColumns const& t, int64_t n, double min_w, PopulationWork*& work,
                              int64_t first_id, int64_t room, int64_t* added, cudaStream_t stream);
+
+// Maxwell leapfrog pieces (I/RreaMaxwellTMRZ.H:143-214) for the coupled step.
+cudaError_t maxwell_advance_b(int nr, int nz, double dr, double dz, double dt, const double* er, const double* ez,
+                              double* bt, cudaStream_t stream);
+cudaError_t maxwell_silver_mueller(int nr, int nz, const double* er, const double* ez, double* bt, cudaStream_t stream);
+cudaError_t maxwell_advance_e(int nr, int nz, double dr, double dz, double dt, const double* bt, const double* jr,
+                              const double* jz, double* er, double* ez, cudaStream_t stream);
+
+// Low-energy carrier fluid (rrea_fluid.cu).  A failed fail-closed check
+// returns cudaSuccess with ok = false and the message in fluid_error().
+struct FluidGrid {
+    int nr, nz;
+    double r_lo, z_lo, dr, dz;
+    int periodic_z;
+};
+struct FluidState;
+// The device field of the coupled step: scattered er/ez/bt, ambient faces,
+// the cell averages the closure and the gather read, the kinetic current.
+struct CoupledField {
+    int nr, nz;
+    double dr, dz;
+    double *er, *ez, *bt;
+    const double *amb_er, *amb_ez;
+    double *cell_er, *cell_ez;
+    const double *jr_kin, *jz_kin;
+};
+cudaError_t fluid_create(FluidGrid const& g, int blocks, FluidState*& out);
+void fluid_free(FluidState* s);
+void fluid_set_config(FluidState& s, rrea_gpu_fluid_config const& c);
+rrea_gpu_fluid_config const& fluid_config(FluidState const& s);
+std::string const& fluid_error(FluidState const& s);
+bool fluid_validate(FluidState& s, bool require_cfl);
+cudaError_t fluid_load_closure(FluidState& s, std::vector<double> const& columns, int nodes);
+bool fluid_has_closure(FluidState const& s);
+// 0 ne, 1 np, 2 nn, 3 rho, 4 sigma, 5 tau, 6 se, 7 sp, 8 sn, 9 chi, 10 mu, 11 nu, 12 diffusion (3n),
+// 13/14 the face-current buffers (radial/axial)
+double* fluid_field(FluidState& s, int field);
+void fluid_bind_chi(FluidState& s, bool bound);
+int64_t fluid_cells(FluidState const& s);
+const double* fluid_flux(FluidState const& s, int dir);
+cudaError_t fluid_take_sources(FluidState& s, const double* cells5, double dt, cudaStream_t stream);
+cudaError_t fluid_react(FluidState& s, double dt, bool clear, double& residual, bool& ok, cudaStream_t stream);
+cudaError_t fluid_max_reaction_frequency(FluidState& s, double& out, cudaStream_t stream);
+cudaError_t fluid_conductivity(FluidState& s, cudaStream_t stream);
+cudaError_t fluid_charge_density(FluidState& s, cudaStream_t stream);
+cudaError_t fluid_closure(FluidState& s, const double* er_cell, const double* ez_cell, double diag8[8], bool& ok,
+                          cudaStream_t stream);
+cudaError_t fluid_transport(FluidState& s, double dt, const double* efr, const double* efr_add, const double* efz,
+                            const double* efz_add, double diag14[14], bool& ok, cudaStream_t stream);
+cudaError_t fluid_coupled_step(FluidState& s, CoupledField const& f, double dt, double diag8[8], bool& ok,
+                               cudaStream_t stream);
 
 }  // namespace rrea_launch

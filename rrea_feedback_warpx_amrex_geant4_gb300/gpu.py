@@ -44,6 +44,34 @@ class RreaGpuConfig(ctypes.Structure):
     ]
 
 
+class RreaFluidConfig(ctypes.Structure):
+    """Mirror of rrea_gpu_fluid_config (include/rrea_gpu.h)."""
+
+    _fields_ = [(name, ctypes.c_double) for name in (
+        "electron_mobility_m2_per_vs", "positive_ion_mobility_m2_per_vs", "negative_ion_mobility_m2_per_vs",
+        "positive_ion_reduced_mobility_stp_m2_per_vs", "negative_ion_reduced_mobility_stp_m2_per_vs",
+        "ion_mobility_density_ratio_floor", "ion_drift_cfl", "transport_density_ratio", "attachment_frequency_s",
+        "electron_ion_recombination_coefficient_m3_per_s", "ion_ion_recombination_coefficient_m3_per_s",
+        "detachment_frequency_s")] + [(name, ctypes.c_int32) for name in (
+        "ion_drift_enable", "electron_drift_enable", "electron_mobility_model", "ion_mobility_model",
+        "attachment_model", "material_min_substeps", "material_max_substeps", "reserved0")] + [
+        (name, ctypes.c_double) for name in (
+            "material_conduction_target", "material_conduction_guard", "material_diffusion_target",
+            "material_diffusion_guard", "material_reaction_target", "material_reaction_guard")]
+
+
+MOBILITY_ABSOLUTE, MOBILITY_EN_TABLE_FLUX, MOBILITY_REDUCED_STP = 0, 1, 2   # RREA_GPU_MOBILITY_*
+ATTACHMENT_CONSTANT, ATTACHMENT_EN_TABLE = 0, 1                             # RREA_GPU_ATTACHMENT_*
+FLUID_TRANSPORT_DIAG = ("max_face_conductivity", "max_diffusion_number", "unlimited_max_outgoing_cfl",
+                        "min_outflow_scale", "limited_outflow_fraction", "limited_electron_number_fraction",
+                        "max_outgoing_cfl", "max_drift_speed", "cfl_dt", "pos_center_r", "pos_center_z",
+                        "neg_center_r", "neg_center_z", "density_ratio_at_pos_center")
+FLUID_COUPLED_DIAG = ("substeps", "full_conduction", "full_diffusion", "full_reaction", "max_reaction_number",
+                      "max_dt_sigma", "max_diffusion_number", "max_residual")
+FLUID_CLOSURE_DIAG = ("min_en_td", "max_en_td", "held_below", "above_range", "invalid", "electron_count",
+                      "held_below_electron_count", "electron_source_rate")
+
+
 class RreaGpuTile(ctypes.Structure):
     """rrea_gpu_tile (include/rrea_gpu.h)."""
 
@@ -89,6 +117,12 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_seed_schedule_events", "rrea_gpu_seed_schedule_validate", "rrea_gpu_seed_schedule_last_error",
     "rrea_gpu_inject_seeds_resident", "rrea_gpu_thin_cic_groups", "rrea_gpu_census_resident",
     "rrea_gpu_deposit_charge_resident", "rrea_gpu_population_thin_resident", "rrea_gpu_population_split_resident",
+    "rrea_gpu_default_fluid_config", "rrea_gpu_fluid_configure", "rrea_gpu_fluid_load_closure",
+    "rrea_gpu_fluid_set_state", "rrea_gpu_fluid_get_state", "rrea_gpu_fluid_set_source_rates",
+    "rrea_gpu_fluid_get_source_rates", "rrea_gpu_fluid_set_density_ratio", "rrea_gpu_fluid_set_closure_fields",
+    "rrea_gpu_fluid_get_closure_fields", "rrea_gpu_fluid_take_sources", "rrea_gpu_fluid_react",
+    "rrea_gpu_fluid_max_reaction_frequency", "rrea_gpu_fluid_conductivity", "rrea_gpu_fluid_charge_density",
+    "rrea_gpu_fluid_evaluate_closure", "rrea_gpu_fluid_transport", "rrea_gpu_advance_field_coupled",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -184,9 +218,30 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_stream.argtypes = [vp, ctypes.POINTER(vp)]
     lib.rrea_gpu_last_step_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                              ctypes.POINTER(ctypes.c_double)]
+    _fc = ctypes.POINTER(RreaFluidConfig)
+    lib.rrea_gpu_default_fluid_config.argtypes = [_fc]
+    lib.rrea_gpu_default_fluid_config.restype = None
+    lib.rrea_gpu_fluid_configure.argtypes = [vp, _fc]
+    lib.rrea_gpu_fluid_load_closure.argtypes = [vp, ctypes.c_char_p]
+    lib.rrea_gpu_fluid_set_state.argtypes = [vp, _D, _D, _D, _D]
+    lib.rrea_gpu_fluid_get_state.argtypes = [vp, _D, _D, _D, _D, _D, _D]
+    lib.rrea_gpu_fluid_set_source_rates.argtypes = [vp, _D, _D, _D]
+    lib.rrea_gpu_fluid_get_source_rates.argtypes = [vp, _D, _D, _D]
+    lib.rrea_gpu_fluid_set_density_ratio.argtypes = [vp, _D]
+    lib.rrea_gpu_fluid_set_closure_fields.argtypes = [vp, _D, _D, _D]
+    lib.rrea_gpu_fluid_get_closure_fields.argtypes = [vp, _D, _D, _D]
+    lib.rrea_gpu_fluid_take_sources.argtypes = [vp, ctypes.c_double]
+    lib.rrea_gpu_fluid_react.argtypes = [vp, ctypes.c_double, ctypes.c_int32, _D]
+    lib.rrea_gpu_fluid_max_reaction_frequency.argtypes = [vp, _D]
+    lib.rrea_gpu_fluid_conductivity.argtypes = [vp]
+    lib.rrea_gpu_fluid_charge_density.argtypes = [vp]
+    lib.rrea_gpu_fluid_evaluate_closure.argtypes = [vp, _D, _D, _D]
+    lib.rrea_gpu_fluid_transport.argtypes = [vp, ctypes.c_double, _D, _D, _D, _D, _D]
+    lib.rrea_gpu_advance_field_coupled.argtypes = [vp, ctypes.c_double, _D]
     for name in EXPORTED_SYMBOLS:
         fn = getattr(lib, name)
-        if fn.restype is not None and name not in ("rrea_gpu_default_config", "rrea_gpu_last_error"):
+        if fn.restype is not None and name not in ("rrea_gpu_default_config", "rrea_gpu_last_error",
+                                                   "rrea_gpu_default_fluid_config"):
             fn.restype = ctypes.c_int
     _lib = lib
     return lib
@@ -207,6 +262,26 @@ def default_config(**overrides):
     for k, v in overrides.items():
         setattr(cfg, k, v)
     return cfg
+
+
+def default_fluid_config(**overrides):
+    """rrea_gpu_default_fluid_config (the reference's LowEnergyFluidConfig and
+    material substep defaults), then `overrides`."""
+    cfg = RreaFluidConfig()
+    load_library().rrea_gpu_default_fluid_config(ctypes.byref(cfg))
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def _opt(a, n=None):
+    """A contiguous float64 copy of `a` (or None) and its pointer."""
+    if a is None:
+        return None, None
+    arr = np.ascontiguousarray(np.ravel(a), dtype=np.float64).copy()
+    if n is not None and arr.size != n:
+        raise ValueError(f"expected {n} values, got {arr.size}")
+    return arr, arr.ctypes.data_as(_D)
 
 
 def tile_struct(arrays):
@@ -494,6 +569,106 @@ class RreaGpuContext:
         out = np.zeros(c.nr * c.nz)
         self._check(self.lib.rrea_gpu_deposit_charge_resident(self.handle, out.ctypes.data_as(_D)))
         return out.reshape(c.nz, c.nr)
+
+    # ---- low-energy carrier fluid ------------------------------------------
+    def fluid_configure(self, fluid_config=None, **overrides):
+        """Allocates (first call) and configures the carrier fluid."""
+        cfg = fluid_config if fluid_config is not None else default_fluid_config()
+        for k, v in overrides.items():
+            setattr(cfg, k, v)
+        self._check(self.lib.rrea_gpu_fluid_configure(self.handle, ctypes.byref(cfg)))
+        self.fluid_config = cfg
+        return cfg
+
+    def fluid_load_closure(self, path):
+        self._check(self.lib.rrea_gpu_fluid_load_closure(self.handle, str(path).encode()))
+
+    def _cells(self):
+        return self.config.nr * self.config.nz
+
+    def fluid_set_state(self, n_pos=None, n_neg=None, n_e=None, rho=None):
+        n = self._cells()
+        keep = [_opt(a, n) for a in (n_pos, n_neg, n_e, rho)]
+        self._check(self.lib.rrea_gpu_fluid_set_state(self.handle, *[p for _, p in keep]))
+
+    def fluid_state(self):
+        """Dict of n_pos, n_neg, n_e, rho, sigma, tau (cells i + nr*j)."""
+        n = self._cells()
+        out = {k: np.zeros(n) for k in ("n_pos", "n_neg", "n_e", "rho", "sigma", "tau")}
+        self._check(self.lib.rrea_gpu_fluid_get_state(self.handle, *[out[k].ctypes.data_as(_D) for k in out]))
+        return out
+
+    def fluid_set_source_rates(self, s_e=None, s_pos=None, s_neg=None):
+        n = self._cells()
+        keep = [_opt(a, n) for a in (s_e, s_pos, s_neg)]
+        self._check(self.lib.rrea_gpu_fluid_set_source_rates(self.handle, *[p for _, p in keep]))
+
+    def fluid_source_rates(self):
+        n = self._cells()
+        out = {k: np.zeros(n) for k in ("s_e", "s_pos", "s_neg")}
+        self._check(self.lib.rrea_gpu_fluid_get_source_rates(self.handle, *[out[k].ctypes.data_as(_D) for k in out]))
+        return out
+
+    def fluid_set_density_ratio(self, chi=None):
+        arr, p = _opt(chi, self._cells())
+        self._check(self.lib.rrea_gpu_fluid_set_density_ratio(self.handle, p))
+
+    def fluid_set_closure_fields(self, mu=None, nu=None, diffusion=None):
+        n = self._cells()
+        keep = [_opt(mu, n), _opt(nu, n), _opt(diffusion, 3 * n)]
+        self._check(self.lib.rrea_gpu_fluid_set_closure_fields(self.handle, *[p for _, p in keep]))
+
+    def fluid_closure_fields(self):
+        n = self._cells()
+        mu, nu, d3 = np.zeros(n), np.zeros(n), np.zeros(3 * n)
+        self._check(self.lib.rrea_gpu_fluid_get_closure_fields(self.handle, mu.ctypes.data_as(_D), nu.ctypes.data_as(_D),
+                                                               d3.ctypes.data_as(_D)))
+        return mu, nu, d3.reshape(3, n)
+
+    def fluid_take_sources(self, dt_s):
+        self._check(self.lib.rrea_gpu_fluid_take_sources(self.handle, dt_s))
+
+    def fluid_react(self, dt_s, clear_sources=True):
+        r = ctypes.c_double(0.0)
+        self._check(self.lib.rrea_gpu_fluid_react(self.handle, dt_s, int(bool(clear_sources)), ctypes.byref(r)))
+        return r.value
+
+    def fluid_max_reaction_frequency(self):
+        r = ctypes.c_double(0.0)
+        self._check(self.lib.rrea_gpu_fluid_max_reaction_frequency(self.handle, ctypes.byref(r)))
+        return r.value
+
+    def fluid_conductivity(self):
+        self._check(self.lib.rrea_gpu_fluid_conductivity(self.handle))
+
+    def fluid_charge_density(self):
+        self._check(self.lib.rrea_gpu_fluid_charge_density(self.handle))
+
+    def fluid_evaluate_closure(self, er_cell=None, ez_cell=None):
+        n = self._cells()
+        a, pa = _opt(er_cell, n)
+        b, pb = _opt(ez_cell, n)
+        d = np.zeros(8)
+        self._check(self.lib.rrea_gpu_fluid_evaluate_closure(self.handle, pa, pb, d.ctypes.data_as(_D)))
+        return dict(zip(FLUID_CLOSURE_DIAG, d))
+
+    def fluid_transport(self, dt_s, efr=None, efz=None):
+        """One explicit carrier-transport update; returns (flux_r (3, faces),
+        flux_z (3, faces), diagnostics dict)."""
+        c = self.config
+        nfr, nfz = (c.nr + 1) * c.nz, c.nr * (c.nz + 1)
+        a, pa = _opt(efr, nfr)
+        b, pb = _opt(efz, nfz)
+        fr, fz, d = np.zeros(3 * nfr), np.zeros(3 * nfz), np.zeros(14)
+        self._check(self.lib.rrea_gpu_fluid_transport(self.handle, dt_s, pa, pb, fr.ctypes.data_as(_D),
+                                                      fz.ctypes.data_as(_D), d.ctypes.data_as(_D)))
+        return fr.reshape(3, nfr), fz.reshape(3, nfz), dict(zip(FLUID_TRANSPORT_DIAG, d))
+
+    def advance_field_coupled(self, dt_s):
+        """The coupled fluid + Maxwell step; returns its diagnostics dict."""
+        d = np.zeros(8)
+        self._check(self.lib.rrea_gpu_advance_field_coupled(self.handle, dt_s, d.ctypes.data_as(_D)))
+        return dict(zip(FLUID_COUPLED_DIAG, d))
 
     def census(self, species, edges_eV, thresholds_eV=()):
         """Census of a resident species tile (the reduced diagnostics'
