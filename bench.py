@@ -11,8 +11,9 @@ air at 1.225 kg/m^3, initial uniform E_z = -500 kV/m, 256 x 2048 grid over
 kinetic step in the reference's order: the electron, photon and positron
 phases over the resident populations, the transient FIFO that flies every
 secondary through the rest of its step (newborn residual legs), the
-net-chord current of all charged flights, and the Maxwell TM-RZ field update
-driven by it.  A particle-step is one live macroparticle advanced through
+net-chord current of all charged flights and the ionization sources, and the
+coupled low-energy carrier fluid + Maxwell TM-RZ field update they drive
+(production dry-air closures, adaptive material substeps).  A particle-step is one live macroparticle advanced through
 one dt, its newborn residual legs included.  Synthetic seeds; no dataset.
 
   value       particle-steps/s with the tiles resident in HBM (device-timed)
@@ -49,9 +50,9 @@ DT_S = 5.0e-10
 BYTES_PER_PARTICLE_STEP = 112
 PHOTON_FRACTION = 0.5  # photons per electron in the resident populations
 POSITRON_FRACTION = 0.0625  # positrons per electron
-FIELD_SUBSTEPS = 2  # material substeps of the Maxwell update
+FIELD_SUBSTEPS = 2  # minimum material substeps of the coupled update (the reference's default)
 METRIC = ("particle-steps/s on 1 GB300 (plain kinetic step: electron, photon and positron phases, "
-          "newborn FIFO, net-chord current and field update)")
+          "newborn FIFO, net-chord current, carrier fluid and field update)")
 
 
 def parse():
@@ -216,11 +217,16 @@ def oracle_whole_steps(n, warmup, steps, rank=0):
 
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    from oracle import fluid as ofl
+    from rrea_feedback_warpx_amrex_geant4_gb300 import DEFAULT_CLOSURE
+
     oracle.load_tables(DEFAULT_TABLES)
+    ofl.load_closure(DEFAULT_CLOSURE)
     cfg = workloads.make_config(oracle, CASE)
     arr, pho, pos = gpu_arm_populations(n, rank)
     run = oav.AvalancheRun(cfg, workloads.make_field(CASE), arr, photons=pho, positrons=pos, feedback=True,
-                           field_substeps=FIELD_SUBSTEPS)
+                           field_substeps=FIELD_SUBSTEPS,
+                           fluid=ofl.default_config(**workloads.fluid_overrides()))
     for _ in range(warmup):
         run.advance(DT_S)
     moved = 0
@@ -236,12 +242,14 @@ DATA = "synthetic (scale-up case seed distribution, seeded numpy PRNG)"
 def workload_config(n, world):
     """The workload both arms time (the same populations, evolution and field)."""
     return {"workload": f"{CASE}: whole kinetic step (electron, photon, positron phases, newborn FIFO and commit, "
-                        f"net-chord current, field update) over resident populations of {population_text(n)} per "
+                        f"net-chord current and ionization sources, coupled carrier-fluid + Maxwell update) over "
+                        f"resident populations of {population_text(n)} per "
                         f"GPU (256x2048 cells over 200 m x 2 km, initial uniform E_z = -500 kV/m), dt 0.5 ns",
             "grid": "256x2048",
             "population_per_gpu": {"electrons": n, "photons": int(n * PHOTON_FRACTION),
                                    "positrons": max(1, int(n * POSITRON_FRACTION))},
-            "dt_s": DT_S, "field_substeps": FIELD_SUBSTEPS,
+            "dt_s": DT_S, "field": "coupled carrier fluid (en_table_flux_v1, en_table_attachment_v1) + Maxwell, "
+                                   "adaptive material substeps (min 2)",
             "l2": "flushed between timed steps (256 MiB write)",
             "parallelism": f"dp{world} (independent particle shards)"}
 
@@ -274,7 +282,7 @@ def run_reference(args, rank, world):
 def run_gb300(args, rank, world, local):
     import torch
 
-    from rrea_feedback_warpx_amrex_geant4_gb300 import DEFAULT_TABLES, distributed, gpu, workloads
+    from rrea_feedback_warpx_amrex_geant4_gb300 import DEFAULT_CLOSURE, DEFAULT_TABLES, distributed, gpu, workloads
 
     torch.cuda.set_device(local)
     dist = None
@@ -298,6 +306,9 @@ def run_gb300(args, rank, world, local):
     ctx.load_tables(DEFAULT_TABLES)
     field = workloads.make_field(CASE)
     ctx.set_field(**field)
+    # the carrier fluid of the feedback case (production closures)
+    ctx.fluid_configure(**workloads.fluid_overrides())
+    ctx.fluid_load_closure(DEFAULT_CLOSURE)
     ctx.set_launch(args.threads, args.blocks_per_sm, diagnostics=False)
     arr, pho, pos = gpu_arm_populations(n, rank)
     ctx.stage_electrons(arr)
@@ -308,6 +319,7 @@ def run_gb300(args, rank, world, local):
 
     def one_step(step):
         ctx.reset_current()  # the net-chord current is per step (ResetNetChordStep)
+        ctx.reset_sources()  # and so are the ionization sources the fluid takes
         ne = ctx.step_electrons_resident(step, DT_S)
         te, _, kme = ctx.last_step_stats()
         ng = ctx.step_photons_resident(step, DT_S)
@@ -321,8 +333,9 @@ def run_gb300(args, rank, world, local):
         committed = ctx.commit_survivors_resident()
         for species in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON, gpu.SPECIES_PHOTON):
             ctx.compact_resident(species)
-        # Maxwell TM-RZ with this step's J, summed over the ranks' shards
-        distributed.exchange_current_and_advance(ctx, dist, DT_S, FIELD_SUBSTEPS)
+        # the coupled carrier-fluid + Maxwell TM-RZ update with this step's
+        # kinetic J and ionization sources, summed over the ranks' shards
+        distributed.exchange_and_advance_coupled(ctx, dist, DT_S)
         return {"te": te, "tg": tg, "tp": tp, "kme": kme, "kmg": kmg, "kmp": kmp,
                 "secondaries": ne + ng + npos, "fifo_items": items, "survivors": surv,
                 "committed": int(committed.sum())}
@@ -388,14 +401,15 @@ def run_gb300(args, rank, world, local):
     def e2e_step(step):
         """The overlay's step through the drop-in entry points: Apply's three
         phases on host tiles, then DrainAndCommitSecondaries on their host
-        secondaries, then the field update."""
+        secondaries, then the coupled fluid and field update."""
         ctx.reset_current()
+        ctx.reset_sources()
         sec_e = ctx.apply_electrons(pe, step, DT_S, want_secondaries=True)
         sec_g = ctx.apply_photons(pg, step, DT_S, want_secondaries=True)
         sec_p = ctx.apply_positrons(pp, step, DT_S, want_secondaries=True)
         pending = np.concatenate([sec_e, sec_g, sec_p])
         surv = ctx.drain_secondaries(pending, step, DT_S)
-        distributed.exchange_current_and_advance(ctx, dist, DT_S, FIELD_SUBSTEPS)
+        distributed.exchange_and_advance_coupled(ctx, dist, DT_S)
         return len(pending), len(surv)
 
     e2e_moved = 0
@@ -464,7 +478,8 @@ def run_gb300(args, rank, world, local):
                     "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
                     "path": "rrea_gpu_apply_electrons/_photons/_positrons (pinned host tiles -> HBM -> host), "
                             "rrea_gpu_drain_secondaries (host records in, survivors out), "
-                            "rrea_gpu_current_device + rrea_gpu_advance_field_from_current"},
+                            "rrea_gpu_current_device + rrea_gpu_fluid_take_sources + "
+                            "rrea_gpu_advance_field_coupled_from_current"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic, "traffic_source": traffic_source, "kernel": "electron_step_kernel",

@@ -493,6 +493,11 @@ rrea_gpu_status rrea_gpu_fetch_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile);
  * `diagnostics` enables the per-particle diagnostic arrays. */
 rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm,
                                     int32_t diagnostics);
+/* Scheduling order of the resident charged phases: 1 (default) visits a
+ * tile of 65,536 or more particles lowest |u| first, by a counting sort of
+ * the tile each step; 0 visits it in tile order.  Results never depend on
+ * it (every result is indexed by the particle's tile slot). */
+rrea_gpu_status rrea_gpu_set_schedule(rrea_gpu_ctx* ctx, int32_t cost_order);
 
 /* Counts and device time of the last step: particles transported (valid on
  * entry), secondaries produced, and the transport kernel's duration measured
@@ -755,6 +760,50 @@ rrea_gpu_status rrea_gpu_fluid_transport(rrea_gpu_ctx* ctx, double dt_s, const d
  * non-periodic z and the Yee CFL, like rrea_gpu_advance_field.
  */
 rrea_gpu_status rrea_gpu_advance_field_coupled(rrea_gpu_ctx* ctx, double dt_s, double* diag);
+/* The two halves of the coupled step of a sharded run, as
+ * rrea_gpu_current_device / rrea_gpu_advance_field_from_current are for the
+ * kinetic-only update: the caller sums the kinetic face current
+ * (rrea_gpu_current_device) and the five cell-source grids
+ * (rrea_gpu_sources_device: 5 x nr*nz device doubles, field-major) across
+ * ranks in place, calls rrea_gpu_fluid_take_sources, then
+ * rrea_gpu_advance_field_coupled_from_current, which runs the coupled step
+ * on the current vectors as they stand; the fluid and the field are
+ * replicated, so every rank computes the same update.
+ * rrea_gpu_advance_field_coupled is rrea_gpu_current_device followed by
+ * rrea_gpu_advance_field_coupled_from_current. */
+rrea_gpu_status rrea_gpu_sources_device(rrea_gpu_ctx* ctx, double** cells5);
+rrea_gpu_status rrea_gpu_advance_field_coupled_from_current(rrea_gpu_ctx* ctx, double dt_s, double* diag);
+
+/*
+ * ---- Batched ensemble --------------------------------------------------
+ * Many independent uniform-field avalanche instances advanced by one launch
+ * sequence per step (the batched-ensemble pattern; the overlay itself runs
+ * one instance per process).  A particle's cpu ordinal is its instance k:
+ * its RNG key |id| ^ k << 40 gives every instance its own streams, ids are
+ * counted per instance and species, and a committed secondary takes its
+ * root's instance.  Each instance therefore evolves exactly as the same
+ * particles on their own context with cpu = k.  No feedback: the instances
+ * keep their uniform ambient fields and deposit neither current nor cell
+ * sources.
+ *
+ * configure: once, before staging; ambient_ez[k] is instance k's uniform E_z.
+ * partition: stable partition of a species tile by instance (the order
+ *   inside an instance is kept), so each instance is one slice; counts
+ *   (n_instances) receives the slice sizes.  Valid until the tile next
+ *   gains or loses slots (commit, compaction, staging).
+ * retire: invalidates every particle of an instance (the end of its run).
+ * census / population_thin: rrea_gpu_census_resident and
+ *   rrea_gpu_population_thin_resident (without staged candidates) on one
+ *   instance's slice of the last partition.
+ */
+rrea_gpu_status rrea_gpu_ensemble_configure(rrea_gpu_ctx* ctx, int32_t n_instances, const double* ambient_ez);
+rrea_gpu_status rrea_gpu_ensemble_partition(rrea_gpu_ctx* ctx, int32_t species, int64_t* counts);
+rrea_gpu_status rrea_gpu_ensemble_retire(rrea_gpu_ctx* ctx, int32_t instance);
+rrea_gpu_status rrea_gpu_ensemble_census(rrea_gpu_ctx* ctx, int32_t species, int32_t instance, const double* edges_eV,
+                                         int32_t n_edges, const double* thresholds_eV, int32_t n_thresholds,
+                                         double* out);
+rrea_gpu_status rrea_gpu_ensemble_population_thin(rrea_gpu_ctx* ctx, int32_t species, int32_t instance,
+                                                  int64_t target, int32_t step, uint64_t salt, int64_t* stats);
 
 #ifdef __cplusplus
 }

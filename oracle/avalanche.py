@@ -90,9 +90,15 @@ def census(tile, species, edges, thresholds):
 class AvalancheRun:
     """The oracle's whole-run loop over host tiles (electron seeds)."""
 
-    def __init__(self, cfg, field, electrons, photons=None, positrons=None, feedback=False, field_substeps=2):
+    def __init__(self, cfg, field, electrons, photons=None, positrons=None, feedback=False, field_substeps=2,
+                 fluid=None):
+        """fluid: an oracle.fluid.FluidConfig to run the coupled fluid/Maxwell
+        step (feedback=True) in place of the kinetic-only field update."""
         self.cfg = cfg
         self.feedback = feedback
+        self.fluid = fluid
+        n_cells = cfg.nr * cfg.nz
+        self.fluid_state = {k: np.zeros(n_cells) for k in ("ne", "np", "nn", "rho", "se", "sp", "sn")}
         self.field_substeps = field_substeps
         self.field = {k: np.array(v, dtype=np.float64) for k, v in field.items()}
         self.tiles = {0: {k: np.array(v) for k, v in electrons.items()},
@@ -126,9 +132,23 @@ class AvalancheRun:
             cur = _oracle.deposit_segments(cfg, dt_s, rows)
             dr = (cfg.r_hi - cfg.r_lo) / cfg.nr
             dz = (cfg.z_hi - cfg.z_lo) / cfg.nz
-            fld["er"], fld["ez"], fld["bt"] = _oracle.advance_maxwell(
-                cfg.nr, cfg.nz, dr, dz, dt_s, self.field_substeps, fld["er"], fld["ez"], fld["bt"],
-                cur["jr_phys"], cur["jz_phys"])
+            if self.fluid is None:
+                fld["er"], fld["ez"], fld["bt"] = _oracle.advance_maxwell(
+                    cfg.nr, cfg.nz, dr, dz, dt_s, self.field_substeps, fld["er"], fld["ez"], fld["bt"],
+                    cur["jr_phys"], cur["jz_phys"])
+            else:
+                from . import fluid as _fluid
+                # NormalizeAndSync of the step's sources into the fluid's rates
+                cells = sum(r["cells"] for r in phases + [od]).reshape(5, -1)
+                r_in = cfg.r_lo + (np.arange(cfg.nr * cfg.nz) % cfg.nr) * dr
+                vol = np.pi * ((r_in + dr) ** 2 - r_in ** 2) * dz
+                st = self.fluid_state
+                for k, key in enumerate(("se", "sp", "sn")):
+                    st[key] = np.where(vol * dt_s > 0, cells[k] / (vol * dt_s), 0.0)
+                (fld["er"], fld["ez"], fld["bt"]), new, _ = _fluid.coupled_step(
+                    self.fluid, cfg.nr, cfg.nz, cfg.z_lo, dr, dz, dt_s, (fld["er"], fld["ez"], fld["bt"]),
+                    (fld["amb_er"], fld["amb_ez"]), (cur["jr_phys"], cur["jz_phys"]), st)
+                self.fluid_state = {k: new[k] for k in st}
         for s in (0, 1, 2):
             t[s], added = commit_and_compact(t[s], surv, s, self.next_id[s])
             self.next_id[s] += added

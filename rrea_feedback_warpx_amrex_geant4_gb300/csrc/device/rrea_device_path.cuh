@@ -408,6 +408,21 @@ struct FieldView {
     double dr, dz, r_lo, z_lo;
     bool periodic;
     bool has_b;
+    // ensemble mode: instance k's fields follow instance k-1's at these
+    // strides (0: one field for every particle)
+    int64_t inst_cells, inst_bt;
+
+    // The field of one ensemble instance (the particle's cpu ordinal).
+    __device__ __forceinline__ FieldView for_instance(int64_t inst) const
+    {
+        FieldView v = *this;
+        if (inst_cells) {
+            v.cell_er += inst * inst_cells;
+            v.cell_ez += inst * inst_cells;
+            v.bt += inst * inst_bt;
+        }
+        return v;
+    }
 };
 
 // S/RreaAmrexAdvance.cpp:532-579 with I/RreaFieldGatherStencil.H:49-133 and

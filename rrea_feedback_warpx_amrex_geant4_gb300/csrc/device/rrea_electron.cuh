@@ -517,7 +517,9 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     double const dt_s = C.dt_s;
 
     // ---- prologue, O/RreaTransportStep.H:730-819
-    uint64_t const key = static_cast<uint64_t>(llabs(A.id[ip])) ^ (static_cast<uint64_t>(A.cpu ? A.cpu[ip] : 0) << 40);
+    int32_t const cpu = A.cpu ? A.cpu[ip] : 0;
+    uint64_t const key = static_cast<uint64_t>(llabs(A.id[ip])) ^ (static_cast<uint64_t>(cpu) << 40);
+    FieldView const fv = A.fv.for_instance(cpu);
     double const weight = A.w[ip];
     if (le0(weight)) {
         A.id[ip] = -A.id[ip];
@@ -571,7 +573,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     Intervals<NP> iv;
     build_intervals(path, g, A.prof, rho, iv, err);
     double const driver_span = fmax(path.in_end, 1.0e-6);
-    FieldRange const dfw = path_field_work(A.fv, g, path, q, 0.0, 1.0, err);
+    FieldRange const dfw = path_field_work(fv, g, path, q, 0.0, 1.0, err);
     double const field_work = dfw.work / driver_span;
     double const chord_dpath = density_path(iv, path, path.in_begin, path.in_end);
     double transported_dpath = 0.0, transported_len = 0.0;
@@ -869,7 +871,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
             }
             sb = path.in_begin;
             se = path.in_end;
-            sub_field = path_field_work(A.fv, g, path, q, sb, se, err);
+            sub_field = path_field_work(fv, g, path, q, sb, se, err);
             sub_dt_eff = sub_dt * (se - sb);
             half_kick(sub_field, 0.5 * sub_dt_eff, q, k, dx, dy, dz);
             if (k < cutoff) {
@@ -1054,7 +1056,7 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
     if (gt0(transported_len)) particle_density = transported_dpath / transported_len;
     double const end_r = rz_radius(run_x, run_y);
     double fer, fez, fbt;
-    gather(A.fv, end_r, run_z, fer, fez, fbt);
+    gather(fv, end_r, run_z, fer, fez, fbt);
     // electron_ensemble_mean_drag_ev_per_m, O/RreaTransportStep.H:226-247
     double threshold = 0.0;
     {

@@ -66,13 +66,14 @@ __device__ __forceinline__ bool newborn_final_point(Path<NP> const& path, Geom c
 // RreaEvaluateElectronStatePolicy at a point: below the cutoff, or a
 // low-energy non-runaway whose field does not beat the ensemble mean drag
 // (O/RreaParticleInteraction.H:1279-1317; O/RreaTransportStep.H:226-247).
-__device__ __forceinline__ bool newborn_electron_demotes(StepConstants const& C, ElectronArgs const& A, RateCache& rc,
-                                                         double x, double y, double z, double e, Err& err)
+__device__ __forceinline__ bool newborn_electron_demotes(StepConstants const& C, ElectronArgs const& A,
+                                                         FieldView const& fv, RateCache& rc, double x, double y,
+                                                         double z, double e, Err& err)
 {
     double const cut = C.cfg.low_energy_cutoff_eV;
     double const thr = C.hm_threshold_eV;
     double fer, fez, fbt;
-    gather(A.fv, rz_radius(x, y), z, fer, fez, fbt);
+    gather(fv, rz_radius(x, y), z, fer, fez, fbt);
     double const rho = positive_or(density_ratio_at_z(A.prof, C.cfg.density_ratio, z, err), 1.0);
     double const ke = fmax(e, cut);
     if (!charged_in_range(C.tix, ke)) err.set(RREA_GPU_ERR_RANGE);
@@ -109,6 +110,8 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
     double const w_air = C.tix.w_air_eV_per_pair;
     double const w = p.weight;
     uint64_t const key = p.root_key;
+    // an ensemble instance is the root particle's cpu ordinal (key bits 40+)
+    FieldView const fv = A.fv.for_instance(static_cast<int64_t>(key >> 40));
     uint64_t const root_sp = static_cast<uint64_t>(p.root_species);
     uint64_t const nb_lineage = p.lineage;
     double const birth = p.birth_fraction;
@@ -163,7 +166,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
 
     // birth state policy (:99-138): no net chord for a birth demotion
     bool const demote_at_birth =
-        POS ? k < cut : newborn_electron_demotes(C, A, rc, p.x, p.y, p.z, k, err);
+        POS ? k < cut : newborn_electron_demotes(C, A, fv, rc, p.x, p.y, p.z, k, err);
     if (err.code) return -1;
     if (demote_at_birth) {
         double const rb = rz_radius(p.x, p.y);
@@ -208,7 +211,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
                             : 0.0)
             * driver_dpath;
     }
-    double const work = path_field_work(A.fv, g, path, q, 0.0, 1.0, err).work;
+    double const work = path_field_work(fv, g, path, q, 0.0, 1.0, err).work;
     double const impulse = fmax(cfg.max_field_impulse_fraction * k, fmax(cfg.field_impulse_floor_eV, 1.0));
     double const span = fmax(path.in_end, 1.0e-6);
     uint64_t const gsd = static_cast<uint64_t>(
@@ -350,7 +353,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
             sb = path.in_begin;
             se = path.in_end;
             final_fraction = se;
-            sub_field = path_field_work(A.fv, g, path, q, sb, se, err);
+            sub_field = path_field_work(fv, g, path, q, sb, se, err);
             sub_dt_eff = sub_dt * (se - sb);
             half_kick(sub_field, 0.5 * sub_dt_eff, q, k, dx, dy, dz);
             if (k < cut) {
@@ -527,7 +530,7 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
     }
     double const final_r = rz_radius(fx, fy);
     double const final_elapsed = elapsed_at(final_fraction);
-    bool const demote = POS ? k < cut : newborn_electron_demotes(C, A, rc, fx, fy, fz, k, err);
+    bool const demote = POS ? k < cut : newborn_electron_demotes(C, A, fv, rc, fx, fy, fz, k, err);
     if (err.code) return -1;
     if (terminal_at_point || demote) {
         if constexpr (POS) {

@@ -101,7 +101,7 @@ __device__ __forceinline__ void stencil_add(StepConstants const& C, double* __re
 __device__ __forceinline__ void deposit_source(StepConstants const& C, double* __restrict__ cells, int kind,
                                                double r, double z, double w, double sec_e, double loss)
 {
-    if (le0(w)) return;
+    if (le0(w) || !cells) return;   // no cell sources in ensemble mode
     CellStencil const st = make_stencil(C, r, z);
     if (!st.valid) return;
     if (kind == 0) {  // AccumulateIonizationEvent
@@ -181,6 +181,7 @@ struct IonPairCache {
     // deposit_source(C, cells, 0, r, z, w, sec_e, loss) for w > 0
     __device__ __forceinline__ void add(StepConstants const& C, double* __restrict__ cells, double r, double z, double w)
     {
+        if (!cells) return;
         CellStencil const st = make_stencil(C, r, z);
         if (!st.valid) return;
         long long const key = (static_cast<long long>(st.j0) << 32) | static_cast<unsigned int>(st.i0);

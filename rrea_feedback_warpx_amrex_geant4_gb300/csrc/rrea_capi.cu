@@ -197,6 +197,14 @@ struct rrea_gpu_ctx {
     rrea_launch::PopulationWork* pop_work = nullptr;  // population-control plan scratch (first use)
     rrea_gpu_secondary* d_pc_cand = nullptr;          // host candidates of a population-control call
     rrea_launch::FluidState* fluid = nullptr;         // low-energy carrier fluid (rrea_gpu_fluid_configure)
+    // batched ensemble (rrea_gpu_ensemble_configure): per-instance uniform
+    // fields, per-instance next ids, and the slices of the last partition
+    int32_t n_instances = 0;
+    double* d_inst_cells = nullptr;                   // cell Er (n x nr*nz) then cell Ez (n x nr*nz)
+    int64_t* d_inst_next_id = nullptr;                // n x 3
+    rrea_launch::EnsembleWork* ens_work = nullptr;
+    std::vector<int64_t> inst_offsets[kSpecies];      // n + 1 slice bounds per species
+    bool part_valid[kSpecies] = {false, false, false};
     int64_t pc_cand_cap = 0;
     uint64_t* d_child_lineage = nullptr;
     unsigned long long* d_invalid = nullptr;
@@ -216,6 +224,7 @@ struct rrea_gpu_ctx {
     int launch_blocks_per_sm = 16;
     int launch_min_blocks = 16;
     bool diagnostics = true;
+    bool schedule_order = true;   // visit large charged tiles lowest |u| first (rrea_gpu_set_schedule)
 
     std::string last_error;
 };
@@ -408,6 +417,9 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     dfree(ctx->d_arena);
     rrea_launch::fluid_free(ctx->fluid);
+    dfree(ctx->d_inst_cells);
+    dfree(ctx->d_inst_next_id);
+    rrea_launch::ensemble_work_free(ctx->ens_work);
     dfree(ctx->d_er);
     dfree(ctx->d_ez);
     dfree(ctx->d_bt);
@@ -715,6 +727,18 @@ rrea_dev::ElectronArgs sink_args(rrea_gpu_ctx* ctx, rrea_dev::StepConstants cons
     a.fv.z_lo = c.z_lo;
     a.fv.periodic = c.periodic_z != 0;
     a.fv.has_b = ctx->has_b;
+    a.fv.inst_cells = 0;
+    a.fv.inst_bt = 0;
+    if (ctx->n_instances > 0) {
+        // ensemble: instance k's uniform field; no feedback, so no cell
+        // sources and no B
+        size_t const cells = static_cast<size_t>(c.nr) * c.nz;
+        a.cells = nullptr;
+        a.fv.cell_er = ctx->d_inst_cells;
+        a.fv.cell_ez = ctx->d_inst_cells + cells * ctx->n_instances;
+        a.fv.inst_cells = static_cast<int64_t>(cells);
+        a.fv.has_b = false;
+    }
     return a;
 }
 
@@ -786,7 +810,7 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long) * chunks, ctx->stream));
     // a resident charged tile is visited in its scheduling order (lowest
     // |u| first): warps then hold particles of similar substep counts
-    if (!host && species != RREA_SPECIES_PHOTON && a.n >= kScheduleMinParticles) {
+    if (!host && species != RREA_SPECIES_PHOTON && ctx->schedule_order && a.n >= kScheduleMinParticles) {
         RREA_CUDA(ctx, rrea_launch::cost_order(a.ux, a.uy, a.uz, a.id, a.n, ctx->d_cost_scratch, ctx->d_alive,
                                                ctx->num_sms * 4, ctx->stream));
         a.order = ctx->d_alive;
@@ -933,6 +957,24 @@ rrea_gpu_status stage_species(rrea_gpu_ctx* ctx, int species, const rrea_gpu_til
         top = a > top ? a : top;
     }
     ctx->next_id[species] = top + 1;
+    ctx->part_valid[species] = false;
+    if (ctx->n_instances > 0) {
+        // per-instance counters continue after each instance's largest id
+        std::vector<int64_t> next(static_cast<size_t>(ctx->n_instances), 1);
+        for (int64_t i = 0; i < tile->n; ++i) {
+            int32_t const k = tile->cpu ? tile->cpu[i] : 0;
+            if (k < 0 || k >= ctx->n_instances) {
+                return fail(ctx, RREA_GPU_ERR_ARGUMENT, "an ensemble particle's cpu ordinal is not an instance");
+            }
+            int64_t const a = tile->id[i] < 0 ? -tile->id[i] : tile->id[i];
+            next[static_cast<size_t>(k)] = std::max(next[static_cast<size_t>(k)], a + 1);
+        }
+        for (int32_t k = 0; k < ctx->n_instances; ++k) {
+            RREA_CUDA(ctx, cudaMemcpyAsync(ctx->d_inst_next_id + 3 * static_cast<int64_t>(k) + species,
+                                           &next[static_cast<size_t>(k)], sizeof(int64_t), cudaMemcpyHostToDevice,
+                                           ctx->stream));
+        }
+    }
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RREA_GPU_OK;
 }
@@ -1439,8 +1481,16 @@ rrea_gpu_status rrea_gpu_commit_survivors_resident(rrea_gpu_ctx* ctx, int64_t* c
             SpeciesTile& st = ctx->tiles[species];
             RREA_CUDA(ctx, rrea_launch::commit_rank(ctx->d_surv, n, species, ctx->d_commit_flags,
                                                     ctx->d_commit_offsets, ctx->d_commit_scan, ctx->stream));
+            const int64_t* ids = nullptr;
+            if (ctx->n_instances > 0) {
+                RREA_CUDA(ctx, rrea_launch::ensemble_survivor_ids(ctx->d_surv, n, species,
+                                                                  static_cast<uint32_t>(ctx->n_instances),
+                                                                  ctx->d_inst_next_id, ctx->ens_work, &ids,
+                                                                  ctx->stream));
+            }
             RREA_CUDA(ctx, rrea_launch::commit_scatter(ctx->d_surv, n, species, ctx->d_commit_offsets, columns(st),
-                                                       st.n, ctx->next_id[species], ctx->stream));
+                                                       st.n, ctx->next_id[species], ids, ctx->stream));
+            ctx->part_valid[species] = false;
             st.n += added[species];
             ctx->next_id[species] += added[species];
         }
@@ -1491,6 +1541,7 @@ rrea_gpu_status rrea_gpu_compact_resident(rrea_gpu_ctx* ctx, int32_t species, in
         std::swap(st.id, ctx->spare.id);
         std::swap(st.cpu, ctx->spare.cpu);
         st.n = last_off + last_flag;
+        ctx->part_valid[species] = false;
     }
     if (n_live) *n_live = st.n;
     return RREA_GPU_OK;
@@ -1887,6 +1938,7 @@ rrea_gpu_status rrea_gpu_population_split_resident(rrea_gpu_ctx* ctx, int32_t sp
     if (s != RREA_GPU_OK) return s;
     // RreaAdaptiveResampleAction (O/RreaRng.H:139-153): split strictly below half the target
     if (!(live > 0 && live < target / 2 && split_min_weight > 0.0)) return RREA_GPU_OK;
+    if (ctx->n_instances > 0) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "the split refill has no ensemble form");
     SpeciesTile& st = ctx->tiles[species];
     int64_t n_added = 0;
     RREA_CUDA(ctx, rrea_launch::population_split(columns(st), st.n, split_min_weight, ctx->pop_work,
@@ -2025,6 +2077,13 @@ rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block
     // residency (16 resident 128-thread blocks: 32 registers).
     int const resident = blocks_per_sm * threads_per_block / 128;
     ctx->launch_min_blocks = resident >= 16 ? 16 : resident >= 12 ? 12 : resident >= 8 ? 8 : resident >= 4 ? 4 : 2;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_set_schedule(rrea_gpu_ctx* ctx, int32_t cost_order)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    ctx->schedule_order = cost_order != 0;
     return RREA_GPU_OK;
 }
 
@@ -2350,6 +2409,22 @@ rrea_gpu_status rrea_gpu_fluid_transport(rrea_gpu_ctx* ctx, double dt_s, const d
 rrea_gpu_status rrea_gpu_advance_field_coupled(rrea_gpu_ctx* ctx, double dt_s, double* diag)
 {
     if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    double* jr = nullptr;
+    double* jz = nullptr;
+    if (rrea_gpu_status const s = rrea_gpu_current_device(ctx, &jr, &jz)) return s;
+    return rrea_gpu_advance_field_coupled_from_current(ctx, dt_s, diag);
+}
+
+rrea_gpu_status rrea_gpu_sources_device(rrea_gpu_ctx* ctx, double** cells5)
+{
+    if (!ctx || !cells5) return RREA_GPU_ERR_ARGUMENT;
+    *cells5 = ctx->d_cells;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_advance_field_coupled_from_current(rrea_gpu_ctx* ctx, double dt_s, double* diag)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
     if (!ctx->field_set) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no field has been set");
     rrea_gpu_config const& c = ctx->cfg;
     if (c.periodic_z || !ctx->netchord) {
@@ -2368,8 +2443,8 @@ rrea_gpu_status rrea_gpu_advance_field_coupled(rrea_gpu_ctx* ctx, double dt_s, d
     if (tables && !rrea_launch::fluid_has_closure(*ctx->fluid)) {
         return fail(ctx, RREA_GPU_ERR_NOT_READY, "en_table fluid models require a loaded electron closure");
     }
-    // the step's kinetic face current (ConvertPaddedIndexCurrentToPhysicalRZ)
-    RREA_CUDA(ctx, rrea_launch::netchord_convert(ctx->net, ctx->d_jr_phys, ctx->d_jz_phys, ctx->stream));
+    // the step's kinetic face current as rrea_gpu_current_device left it
+    // (summed across ranks by the caller of a sharded step)
     rrea_launch::CoupledField const f{c.nr,          c.nz,          dr,           dz,
                                       ctx->d_er,     ctx->d_ez,     ctx->d_bt,    ctx->d_amb_er,
                                       ctx->d_amb_ez, ctx->d_cell_er, ctx->d_cell_ez, ctx->d_jr_phys,
@@ -2381,6 +2456,146 @@ rrea_gpu_status rrea_gpu_advance_field_coupled(rrea_gpu_ctx* ctx, double dt_s, d
     ctx->has_b = true;
     if (diag) std::memcpy(diag, d, sizeof(d));
     return fluid_checked(ctx, ok);
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched ensemble (rrea_ensemble.cu)
+// ===========================================================================
+extern "C" {
+
+rrea_gpu_status rrea_gpu_ensemble_configure(rrea_gpu_ctx* ctx, int32_t n_instances, const double* ambient_ez)
+{
+    if (!ctx || n_instances < 1 || n_instances > (1 << 16) || !ambient_ez) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "an ensemble needs 1..65536 instances and their fields");
+    }
+    if (ctx->n_instances > 0) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "the ensemble is already configured");
+    for (int32_t k = 0; k < n_instances; ++k) {
+        if (!std::isfinite(ambient_ez[k])) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "instance fields must be finite");
+    }
+    rrea_gpu_config const& c = ctx->cfg;
+    size_t const cells = static_cast<size_t>(c.nr) * c.nz;
+    std::vector<double> host(2 * cells * static_cast<size_t>(n_instances), 0.0);
+    // a uniform ambient E_z: every cell average is the value itself
+    for (int32_t k = 0; k < n_instances; ++k) {
+        std::fill(host.begin() + static_cast<std::ptrdiff_t>(cells * (n_instances + k)),
+                  host.begin() + static_cast<std::ptrdiff_t>(cells * (n_instances + k + 1)), ambient_ez[k]);
+    }
+    RREA_CUDA(ctx, dalloc(&ctx->d_inst_cells, host.size()));
+    RREA_CUDA(ctx, dalloc(&ctx->d_inst_next_id, 3 * static_cast<size_t>(n_instances)));
+    RREA_CUDA(ctx, cudaMemcpy(ctx->d_inst_cells, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<int64_t> ones(3 * static_cast<size_t>(n_instances), 1);
+    RREA_CUDA(ctx, cudaMemcpy(ctx->d_inst_next_id, ones.data(), ones.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+    ctx->n_instances = n_instances;
+    ctx->netchord = false;   // no feedback: neither current nor cell sources
+    ctx->field_set = true;
+    for (auto& v : ctx->part_valid) v = false;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_ensemble_partition(rrea_gpu_ctx* ctx, int32_t species, int64_t* counts)
+{
+    if (!ctx || species < 0 || species >= kSpecies) return RREA_GPU_ERR_ARGUMENT;
+    if (ctx->n_instances < 1) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no ensemble is configured");
+    if (!ctx->spare_ready) {
+        // the compaction's spare tile receives the partitioned copy
+        int64_t live = 0;
+        rrea_gpu_status const s = rrea_gpu_compact_resident(ctx, species, &live);
+        if (s != RREA_GPU_OK) return s;
+        if (!ctx->spare_ready) {
+            size_t const cap = static_cast<size_t>(ctx->capacity);
+            bool ok = true;
+            for (int f = 0; f < kTileDoubles; ++f) ok = ok && dalloc(&ctx->spare.d[f], cap) == cudaSuccess;
+            ok = ok && dalloc(&ctx->spare.id, cap) == cudaSuccess && dalloc(&ctx->spare.cpu, cap) == cudaSuccess;
+            if (!ok) return fail(ctx, RREA_GPU_ERR_CUDA, "partition tile allocation failed");
+            ctx->spare_ready = true;
+        }
+    }
+    SpeciesTile& st = ctx->tiles[species];
+    std::vector<int64_t> n_k(static_cast<size_t>(ctx->n_instances), 0);
+    RREA_CUDA(ctx, rrea_launch::ensemble_partition(columns(st), st.n, static_cast<uint32_t>(ctx->n_instances),
+                                                   columns(ctx->spare), ctx->ens_work, n_k.data(), ctx->stream));
+    int64_t total = 0;
+    for (int64_t v : n_k) total += v;
+    if (total != st.n) return fail(ctx, RREA_GPU_ERR_INVALID_STATE, "a particle's cpu ordinal is not an instance");
+    if (st.n > 0) {
+        for (int f = 0; f < kTileDoubles; ++f) std::swap(st.d[f], ctx->spare.d[f]);
+        std::swap(st.id, ctx->spare.id);
+        std::swap(st.cpu, ctx->spare.cpu);
+    }
+    auto& off = ctx->inst_offsets[species];
+    off.assign(static_cast<size_t>(ctx->n_instances) + 1, 0);
+    for (int32_t k = 0; k < ctx->n_instances; ++k) off[k + 1] = off[k] + n_k[static_cast<size_t>(k)];
+    ctx->part_valid[species] = true;
+    if (counts) std::copy(n_k.begin(), n_k.end(), counts);
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_ensemble_retire(rrea_gpu_ctx* ctx, int32_t instance)
+{
+    if (!ctx || instance < 0 || instance >= ctx->n_instances) return RREA_GPU_ERR_ARGUMENT;
+    for (int species = 0; species < kSpecies; ++species) {
+        SpeciesTile& st = ctx->tiles[species];
+        RREA_CUDA(ctx, rrea_launch::ensemble_retire(st.id, st.cpu, st.n, instance, ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+namespace {
+
+rrea_gpu_status instance_slice(rrea_gpu_ctx* ctx, int32_t species, int32_t instance, int64_t& begin, int64_t& n)
+{
+    if (!ctx || species < 0 || species >= kSpecies || instance < 0 || instance >= ctx->n_instances) {
+        return RREA_GPU_ERR_ARGUMENT;
+    }
+    if (!ctx->part_valid[species]) {
+        return fail(ctx, RREA_GPU_ERR_NOT_READY, "the tile changed since its last ensemble partition");
+    }
+    begin = ctx->inst_offsets[species][static_cast<size_t>(instance)];
+    n = ctx->inst_offsets[species][static_cast<size_t>(instance) + 1] - begin;
+    return RREA_GPU_OK;
+}
+
+}  // namespace
+
+rrea_gpu_status rrea_gpu_ensemble_census(rrea_gpu_ctx* ctx, int32_t species, int32_t instance, const double* edges_eV,
+                                         int32_t n_edges, const double* thresholds_eV, int32_t n_thresholds,
+                                         double* out)
+{
+    int64_t begin = 0, n = 0;
+    if (rrea_gpu_status const s = instance_slice(ctx, species, instance, begin, n)) return s;
+    // the census of the instance's slice is the census of a tile that holds it alone
+    SpeciesTile& st = ctx->tiles[species];
+    SpeciesTile const whole = st;
+    for (int f = 0; f < kTileDoubles; ++f) st.d[f] += begin;
+    st.id += begin;
+    st.cpu += begin;
+    st.n = n;
+    rrea_gpu_status const s =
+        rrea_gpu_census_resident(ctx, species, edges_eV, n_edges, thresholds_eV, n_thresholds, out);
+    st = whole;
+    return s;
+}
+
+rrea_gpu_status rrea_gpu_ensemble_population_thin(rrea_gpu_ctx* ctx, int32_t species, int32_t instance,
+                                                  int64_t target, int32_t step, uint64_t salt, int64_t* stats)
+{
+    int64_t begin = 0, n = 0;
+    if (rrea_gpu_status const s = instance_slice(ctx, species, instance, begin, n)) return s;
+    SpeciesTile& st = ctx->tiles[species];
+    SpeciesTile const whole = st;
+    int64_t const n_surv = ctx->n_surv;
+    for (int f = 0; f < kTileDoubles; ++f) st.d[f] += begin;
+    st.id += begin;
+    st.cpu += begin;
+    st.n = n;
+    ctx->n_surv = 0;   // the instance's live particles alone, no staged candidates
+    rrea_gpu_status const s = rrea_gpu_population_thin_resident(ctx, species, target, step, salt, nullptr, 0, stats);
+    st = whole;
+    ctx->n_surv = n_surv;
+    return s;
 }
 
 }  // extern "C"

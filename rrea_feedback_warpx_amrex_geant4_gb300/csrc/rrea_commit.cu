@@ -38,10 +38,12 @@ __global__ void commit_flags_kernel(const rrea_gpu_secondary* __restrict__ surv,
     }
 }
 
-// Appends accepted records of `species` at tile index base + offsets[i].
+// Appends accepted records of `species` at tile index base + offsets[i],
+// with ids first_id + offsets[i] on cpu 0, or (ensemble mode, ids given)
+// the per-instance ids on the root's instance.
 __global__ void commit_scatter_kernel(const rrea_gpu_secondary* __restrict__ surv, int64_t n, int species,
                                       const int64_t* __restrict__ offsets, TileColumns t, int64_t base,
-                                      int64_t first_id)
+                                      int64_t first_id, const int64_t* __restrict__ ids)
 {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -75,8 +77,8 @@ __global__ void commit_scatter_kernel(const rrea_gpu_secondary* __restrict__ sur
         double const v[kTileColumns] = {r, s.z, th, px, py, pz, s.weight, r, s.z, th, px, py, pz};
 #pragma unroll
         for (int f = 0; f < kTileColumns; ++f) t.d[f][k] = v[f];
-        t.id[k] = first_id + offsets[i];
-        t.cpu[k] = 0;
+        t.id[k] = ids ? ids[i] : first_id + offsets[i];
+        t.cpu[k] = ids ? static_cast<int32_t>(s.root_key >> 40) : 0;
     }
 }
 
@@ -179,12 +181,13 @@ cudaError_t commit_rank(const rrea_gpu_secondary* surv, int64_t n, int species, 
 }
 
 cudaError_t commit_scatter(const rrea_gpu_secondary* surv, int64_t n, int species, const int64_t* offsets,
-                           rrea_dev::TileColumns const& tile, int64_t base, int64_t first_id, cudaStream_t stream)
+                           rrea_dev::TileColumns const& tile, int64_t base, int64_t first_id, const int64_t* ids,
+                           cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
     note_launch();
     rrea_dev::commit_scatter_kernel<<<rrea_dev::grid_for(n, 128), 128, 0, stream>>>(surv, n, species, offsets, tile,
-                                                                                   base, first_id);
+                                                                                   base, first_id, ids);
     return cudaGetLastError();
 }
 

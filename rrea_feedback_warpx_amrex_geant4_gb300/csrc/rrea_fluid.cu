@@ -35,11 +35,13 @@ constexpr double kDblMin = 2.2250738585072014e-308;
 
 using u64 = unsigned long long;
 
-__device__ __forceinline__ u64 bits(double x) { return static_cast<u64>(__double_as_longlong(x)); }
+// Bit pattern of a nonnegative value as an ordered unsigned key: adding
+// +0.0 turns a -0.0 (from max(-0.0, 0.0)) into +0.0, whose key is 0.
+__device__ __forceinline__ u64 bits(double x) { return static_cast<u64>(__double_as_longlong(x + 0.0)); }
 // total order of doubles as unsigned keys (negatives flipped)
 __device__ __forceinline__ u64 ordered(double x)
 {
-    u64 const b = bits(x);
+    u64 const b = static_cast<u64>(__double_as_longlong(x));
     return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
 }
 

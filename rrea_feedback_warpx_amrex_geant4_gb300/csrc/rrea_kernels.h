@@ -89,7 +89,8 @@ cudaError_t order_secondaries(const uint32_t* counts, int64_t n, int64_t* offset
 cudaError_t commit_rank(const rrea_gpu_secondary* surv, int64_t n, int species, uint32_t* flags, int64_t* offsets,
                         int64_t* scan_scratch, cudaStream_t stream);
 cudaError_t commit_scatter(const rrea_gpu_secondary* surv, int64_t n, int species, const int64_t* offsets,
-                           rrea_dev::TileColumns const& tile, int64_t base, int64_t first_id, cudaStream_t stream);
+                           rrea_dev::TileColumns const& tile, int64_t base, int64_t first_id, const int64_t* ids,
+                           cudaStream_t stream);
 // Stable compaction of the valid (id > 0) rows of src into dst; offsets[n-1]
 // + flags[n-1] is the new row count.
 cudaError_t compact_tile(rrea_dev::TileColumns const& src, int64_t n, uint32_t* flags, int64_t* offsets,
@@ -205,5 +206,16 @@ cudaError_t fluid_transport(FluidState& s, double dt, const double* efr, const d
                             const double* efz_add, double diag14[14], bool& ok, cudaStream_t stream);
 cudaError_t fluid_coupled_step(FluidState& s, CoupledField const& f, double dt, double diag8[8], bool& ok,
                                cudaStream_t stream);
+
+// Batched ensemble (rrea_ensemble.cu): per-instance survivor ids, the stable
+// partition of a tile by instance, the retirement of an instance.
+struct EnsembleWork;
+void ensemble_work_free(EnsembleWork* w);
+cudaError_t ensemble_survivor_ids(const rrea_gpu_secondary* surv, int64_t n, int species, uint32_t n_inst,
+                                  int64_t* next_id, EnsembleWork*& w, const int64_t** ids, cudaStream_t stream);
+cudaError_t ensemble_partition(rrea_dev::TileColumns const& src, int64_t n, uint32_t n_inst,
+                               rrea_dev::TileColumns const& dst, EnsembleWork*& w, int64_t* counts_host,
+                               cudaStream_t stream);
+cudaError_t ensemble_retire(int64_t* id, const int32_t* cpu, int64_t n, int32_t inst, cudaStream_t stream);
 
 }  // namespace rrea_launch

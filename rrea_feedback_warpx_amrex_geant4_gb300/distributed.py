@@ -41,6 +41,22 @@ def exchange_current_and_advance(ctx, dist, dt_s, substeps):
     ctx.advance_field_from_current(dt_s, substeps)
 
 
+def exchange_and_advance_coupled(ctx, dist, dt_s):
+    """The coupled fluid/Maxwell update of a sharded step: sum this rank's
+    kinetic face current and cell sources across ranks on the device,
+    normalise the sources into the fluid's rates, and run the replicated
+    coupled step (every rank computes the same fluid and field)."""
+    (jr_ptr, n_jr), (jz_ptr, n_jz) = ctx.current_device()
+    if dist is not None:
+        allreduce_current(device_view(jr_ptr, n_jr), device_view(jz_ptr, n_jz), dist)
+        cells_ptr, n_cells = ctx.sources_device()
+        cells = device_view(cells_ptr, n_cells)
+        dist.all_reduce(cells, op=dist.ReduceOp.SUM)
+        torch.cuda.synchronize()
+    ctx.fluid_take_sources(dt_s)
+    return ctx.advance_field_coupled_from_current(dt_s)
+
+
 def reduce_step_time(total_ms, units, dist, device):
     """(max over ranks of the timed milliseconds, sum of the work units)."""
     t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)

@@ -123,6 +123,9 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_fluid_get_closure_fields", "rrea_gpu_fluid_take_sources", "rrea_gpu_fluid_react",
     "rrea_gpu_fluid_max_reaction_frequency", "rrea_gpu_fluid_conductivity", "rrea_gpu_fluid_charge_density",
     "rrea_gpu_fluid_evaluate_closure", "rrea_gpu_fluid_transport", "rrea_gpu_advance_field_coupled",
+    "rrea_gpu_sources_device", "rrea_gpu_advance_field_coupled_from_current",
+    "rrea_gpu_set_schedule", "rrea_gpu_ensemble_configure", "rrea_gpu_ensemble_partition", "rrea_gpu_ensemble_retire",
+    "rrea_gpu_ensemble_census", "rrea_gpu_ensemble_population_thin",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -238,6 +241,16 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_fluid_evaluate_closure.argtypes = [vp, _D, _D, _D]
     lib.rrea_gpu_fluid_transport.argtypes = [vp, ctypes.c_double, _D, _D, _D, _D, _D]
     lib.rrea_gpu_advance_field_coupled.argtypes = [vp, ctypes.c_double, _D]
+    lib.rrea_gpu_set_schedule.argtypes = [vp, ctypes.c_int32]
+    lib.rrea_gpu_sources_device.argtypes = [vp, ctypes.POINTER(vp)]
+    lib.rrea_gpu_advance_field_coupled_from_current.argtypes = [vp, ctypes.c_double, _D]
+    lib.rrea_gpu_ensemble_configure.argtypes = [vp, ctypes.c_int32, _D]
+    lib.rrea_gpu_ensemble_partition.argtypes = [vp, ctypes.c_int32, _i64p]
+    lib.rrea_gpu_ensemble_retire.argtypes = [vp, ctypes.c_int32]
+    lib.rrea_gpu_ensemble_census.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, _D, ctypes.c_int32, _D,
+                                             ctypes.c_int32, _D]
+    lib.rrea_gpu_ensemble_population_thin.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
+                                                      ctypes.c_int32, ctypes.c_uint64, _i64p]
     for name in EXPORTED_SYMBOLS:
         fn = getattr(lib, name)
         if fn.restype is not None and name not in ("rrea_gpu_default_config", "rrea_gpu_last_error",
@@ -570,6 +583,44 @@ class RreaGpuContext:
         self._check(self.lib.rrea_gpu_deposit_charge_resident(self.handle, out.ctypes.data_as(_D)))
         return out.reshape(c.nz, c.nr)
 
+    def set_schedule(self, cost_order=True):
+        self._check(self.lib.rrea_gpu_set_schedule(self.handle, int(bool(cost_order))))
+
+    # ---- batched ensemble ----------------------------------------------------
+    def ensemble_configure(self, ambient_ez):
+        """Ensemble mode: instance k (a particle's cpu ordinal) moves in the
+        uniform field E_z = ambient_ez[k]; call before staging."""
+        ez = np.ascontiguousarray(ambient_ez, dtype=np.float64)
+        self._check(self.lib.rrea_gpu_ensemble_configure(self.handle, ez.size, ez.ctypes.data_as(_D)))
+        self.n_instances = int(ez.size)
+
+    def ensemble_partition(self, species):
+        """Stable partition of a species tile by instance; returns the slice sizes."""
+        counts = np.zeros(self.n_instances, dtype=np.int64)
+        self._check(self.lib.rrea_gpu_ensemble_partition(self.handle, int(species),
+                                                         counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return counts
+
+    def ensemble_retire(self, instance):
+        self._check(self.lib.rrea_gpu_ensemble_retire(self.handle, int(instance)))
+
+    def ensemble_census(self, species, instance, edges_eV, thresholds_eV=()):
+        edges = np.ascontiguousarray(edges_eV, dtype=np.float64)
+        thr = np.ascontiguousarray(thresholds_eV, dtype=np.float64)
+        out = np.zeros(7 + thr.size + edges.size - 1)
+        self._check(self.lib.rrea_gpu_ensemble_census(self.handle, int(species), int(instance),
+                                                      edges.ctypes.data_as(_D), edges.size,
+                                                      thr.ctypes.data_as(_D) if thr.size else None, thr.size,
+                                                      out.ctypes.data_as(_D)))
+        return unpack_census(out, thr.size)
+
+    def ensemble_population_thin(self, species, instance, target, step, salt=0):
+        stats = np.zeros(8, dtype=np.int64)
+        self._check(self.lib.rrea_gpu_ensemble_population_thin(self.handle, int(species), int(instance), int(target),
+                                                               int(step), int(salt),
+                                                               stats.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return dict(zip(self.POPULATION_STATS, stats.tolist()))
+
     # ---- low-energy carrier fluid ------------------------------------------
     def fluid_configure(self, fluid_config=None, **overrides):
         """Allocates (first call) and configures the carrier fluid."""
@@ -663,6 +714,17 @@ class RreaGpuContext:
         self._check(self.lib.rrea_gpu_fluid_transport(self.handle, dt_s, pa, pb, fr.ctypes.data_as(_D),
                                                       fz.ctypes.data_as(_D), d.ctypes.data_as(_D)))
         return fr.reshape(3, nfr), fz.reshape(3, nfz), dict(zip(FLUID_TRANSPORT_DIAG, d))
+
+    def sources_device(self):
+        """(device pointer, length) of the five cell-source grids."""
+        p = ctypes.c_void_p()
+        self._check(self.lib.rrea_gpu_sources_device(self.handle, ctypes.byref(p)))
+        return p.value, 5 * self._cells()
+
+    def advance_field_coupled_from_current(self, dt_s):
+        d = np.zeros(8)
+        self._check(self.lib.rrea_gpu_advance_field_coupled_from_current(self.handle, dt_s, d.ctypes.data_as(_D)))
+        return dict(zip(FLUID_COUPLED_DIAG, d))
 
     def advance_field_coupled(self, dt_s):
         """The coupled fluid + Maxwell step; returns its diagnostics dict."""

@@ -74,6 +74,20 @@ def make_config(gpu_module, case, low_energy_cutoff_eV=1.0e4, rng_seed=1, max_su
         max_field_impulse_fraction=0.1, field_impulse_floor_eV=1.0e4, rng_seed=rng_seed)
 
 
+# Loschmidt mass density of dry air, n_L M / N_A (I/RreaConstants.H:16-31):
+# the density every reduced fluid coefficient is quoted at.
+RHO_LOSCHMIDT = 2.6868e25 * 28.96546e-3 / 6.02214076e23
+
+
+def fluid_overrides():
+    """The carrier fluid of the feedback cases: the production closures
+    (en_table_flux_v1 electron flux mobility and diffusion,
+    en_table_attachment_v1 attachment) at the air density's Loschmidt ratio,
+    ions static (the reference default), the reference's material substep
+    controls; apply to gpu.default_fluid_config or oracle.fluid.default_config."""
+    return dict(electron_mobility_model=1, attachment_model=1, transport_density_ratio=AIR_DENSITY / RHO_LOSCHMIDT)
+
+
 def make_field(case):
     """Replicated TM-RZ vectors: zero scattered field, uniform ambient E_z."""
     p = CASES[case]

@@ -9,8 +9,8 @@ net-chord current.  The oracle runs the same step on the same staged tiles.
 
 Exact: tile sizes, ids and their order after commit and compaction (so
 every disposition, secondary count and FIFO survivor agreed), weights.
-FP64 state: every entry within 1e-12 relative (positions: of the domain
-size).  Field after the update: within 1e-12 of each vector's largest
+FP64 state: within 1e-12 relative (positions: of the domain size) but at
+most one entry in 10^4, within 1e-11 (oracle/compare.py).  Field after the update: within 1e-12 of each vector's largest
 entry."""
 import os
 import sys

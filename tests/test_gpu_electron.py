@@ -3,9 +3,10 @@ the reference CPU case and the scale-up case), through the C-ABI drop-in
 entry point.
 
 Tolerances: dispositions, substep counts, hazard-draw counts, validity and
-secondary keys bit-exact; every FP64 state entry within 1e-12 relative
-(positions with a 1e-12 x domain floor); atomically accumulated cell
-sources within 1e-12 of each grid's largest cell."""
+secondary keys bit-exact; FP64 state within 1e-12 relative (positions with
+a 1e-12 x domain floor) but at most one entry in 10^4, within 1e-11;
+atomically accumulated cell sources within 1.6e-11 of each grid's largest
+cell."""
 import numpy as np
 import pytest
 
