@@ -805,6 +805,60 @@ rrea_gpu_status rrea_gpu_ensemble_census(rrea_gpu_ctx* ctx, int32_t species, int
 rrea_gpu_status rrea_gpu_ensemble_population_thin(rrea_gpu_ctx* ctx, int32_t species, int32_t instance,
                                                   int64_t target, int32_t step, uint64_t salt, int64_t* stats);
 
+/*
+ * ---- Pathwise adjoint of the charged push --------------------------------
+ * Gradients of a smoothed runaway count and of the net charge crossing a
+ * plane (the time integral of J_z through it) with respect to an axial
+ * field profile E_z(z) on n_nodes equally spaced nodes over [z_lo, z_hi]
+ * (linear between nodes, clamped outside): the differentiation pattern
+ * built on the kinetic step (the overlay has no such mode).  The
+ * differentiated model is the continuous part of the charged substep (the
+ * chord of length v(K) dt/substeps, the two-point Gauss-Legendre field work,
+ * the half kicks of O/RreaChargedInterleave.H:100-138 without B, the
+ * tables' collision plus soft radiative drag of :218-292) with the discrete
+ * outcomes frozen: one rotation per particle and substep drawn from the
+ * counter RNG stands in for the elastic deflection, a particle whose drag
+ * reaches the cutoff stops at the same substep, and nothing else branches.
+ *   loss = sum_i w_i [ sig((K_i(T) - k_threshold) / k_width)
+ *          - plane_weight (sig((z_i(T) - z_plane) / z_width) - sig((z_i(0) - z_plane) / z_width)) ]
+ * The forward pass checkpoints every `checkpoint_every` steps; the reverse
+ * pass recomputes each segment from its checkpoint and runs the
+ * hand-written adjoint back through it.
+ *
+ * stage: the seeds (host arrays: z, direction xyz (3n, normalised here),
+ *   kinetic energy, weight, id); needs the tables loaded.
+ * forward: the loss for the node values at e_nodes_device (DEVICE pointer,
+ *   n_nodes doubles).
+ * backward: d loss / d E_k into grad_device (DEVICE pointer) for the same
+ *   nodes; run after a forward with the same nodes.
+ * final_state: z, dx, dy, dz, K, alive (6 x n host doubles) of the forward.
+ */
+typedef struct {
+    double z_lo, z_hi;          /* node span [m] (default 0..500) */
+    int32_t n_nodes;            /* 256 */
+    int32_t steps;              /* 2000 */
+    int32_t substeps;           /* 4 */
+    int32_t checkpoint_every;   /* 32 */
+    double dt_s;                /* 5e-10 */
+    double density_ratio;       /* stopping-power density ratio, 1 */
+    double cutoff_eV;           /* 1e4 */
+    double scatter_rms_rad;     /* 0.02 */
+    double k_threshold_eV;      /* 1e6 */
+    double k_width_eV;          /* 5e4 */
+    double z_plane_m;           /* 400 */
+    double z_width_m;           /* 1 */
+    double plane_weight;        /* 1 */
+    uint64_t rng_seed;          /* 1 */
+} rrea_gpu_adjoint_config;
+
+void rrea_gpu_default_adjoint_config(rrea_gpu_adjoint_config* cfg);
+rrea_gpu_status rrea_gpu_adjoint_stage(rrea_gpu_ctx* ctx, const rrea_gpu_adjoint_config* cfg, int64_t n,
+                                       const double* z, const double* dir3, const double* kinetic_eV,
+                                       const double* weight, const uint64_t* id);
+rrea_gpu_status rrea_gpu_adjoint_forward(rrea_gpu_ctx* ctx, const double* e_nodes_device, double* loss);
+rrea_gpu_status rrea_gpu_adjoint_backward(rrea_gpu_ctx* ctx, const double* e_nodes_device, double* grad_device);
+rrea_gpu_status rrea_gpu_adjoint_final_state(rrea_gpu_ctx* ctx, double* state6);
+
 #ifdef __cplusplus
 }
 #endif

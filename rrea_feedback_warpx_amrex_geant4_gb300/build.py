@@ -36,6 +36,7 @@ SOURCES = [
     os.path.join(CSRC, "rrea_population.cu"),
     os.path.join(CSRC, "rrea_fluid.cu"),
     os.path.join(CSRC, "rrea_ensemble.cu"),
+    os.path.join(CSRC, "rrea_adjoint.cu"),
     os.path.join(CSRC, "host", "table_set.cpp"),
     os.path.join(CSRC, "host", "seed_schedule.cpp"),
     os.path.join(CSRC, "host", "closure_table.cpp"),

@@ -203,6 +203,7 @@ struct rrea_gpu_ctx {
     double* d_inst_cells = nullptr;                   // cell Er (n x nr*nz) then cell Ez (n x nr*nz)
     int64_t* d_inst_next_id = nullptr;                // n x 3
     rrea_launch::EnsembleWork* ens_work = nullptr;
+    rrea_launch::AdjointState* adjoint = nullptr;      // rrea_gpu_adjoint_stage
     std::vector<int64_t> inst_offsets[kSpecies];      // n + 1 slice bounds per species
     bool part_valid[kSpecies] = {false, false, false};
     int64_t pc_cand_cap = 0;
@@ -420,6 +421,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     dfree(ctx->d_inst_cells);
     dfree(ctx->d_inst_next_id);
     rrea_launch::ensemble_work_free(ctx->ens_work);
+    rrea_launch::adjoint_free(ctx->adjoint);
     dfree(ctx->d_er);
     dfree(ctx->d_ez);
     dfree(ctx->d_bt);
@@ -2596,6 +2598,120 @@ rrea_gpu_status rrea_gpu_ensemble_population_thin(rrea_gpu_ctx* ctx, int32_t spe
     st = whole;
     ctx->n_surv = n_surv;
     return s;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Pathwise adjoint of the charged push (rrea_adjoint.cu)
+// ===========================================================================
+extern "C" {
+
+void rrea_gpu_default_adjoint_config(rrea_gpu_adjoint_config* c)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->z_lo = 0.0;
+    c->z_hi = 500.0;
+    c->n_nodes = 256;
+    c->steps = 2000;
+    c->substeps = 4;
+    c->checkpoint_every = 32;
+    c->dt_s = 5.0e-10;
+    c->density_ratio = 1.0;
+    c->cutoff_eV = 1.0e4;
+    c->scatter_rms_rad = 0.02;
+    c->k_threshold_eV = 1.0e6;
+    c->k_width_eV = 5.0e4;
+    c->z_plane_m = 400.0;
+    c->z_width_m = 1.0;
+    c->plane_weight = 1.0;
+    c->rng_seed = 1;
+}
+
+rrea_gpu_status rrea_gpu_adjoint_stage(rrea_gpu_ctx* ctx, const rrea_gpu_adjoint_config* cfg, int64_t n,
+                                       const double* z, const double* dir3, const double* kinetic_eV,
+                                       const double* weight, const uint64_t* id)
+{
+    if (!ctx || !cfg || n < 0 || (n > 0 && (!z || !dir3 || !kinetic_eV || !weight || !id))) {
+        return RREA_GPU_ERR_ARGUMENT;
+    }
+    if (!ctx->tables_loaded) return fail(ctx, RREA_GPU_ERR_NOT_READY, "the adjoint reads the loaded stopping powers");
+    if (cfg->n_nodes < 2 || cfg->n_nodes > rrea_launch::adjoint_max_nodes() || !(cfg->z_hi > cfg->z_lo)
+        || cfg->steps < 1 || cfg->substeps < 1 || cfg->checkpoint_every < 1 || !(cfg->dt_s > 0.0)
+        || !(cfg->density_ratio > 0.0) || !(cfg->cutoff_eV > 0.0) || !(cfg->k_width_eV > 0.0)
+        || !(cfg->z_width_m > 0.0) || !(cfg->scatter_rms_rad >= 0.0)) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "invalid adjoint configuration");
+    }
+    std::vector<double> seeds(6 * static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        double const dx = dir3[3 * i], dy = dir3[3 * i + 1], dz = dir3[3 * i + 2];
+        double const norm = std::sqrt(dx * dx + dy * dy + dz * dz);
+        if (!(norm > 0.0) || !std::isfinite(norm) || !std::isfinite(z[i]) || !(kinetic_eV[i] > cfg->cutoff_eV)) {
+            return fail(ctx, RREA_GPU_ERR_ARGUMENT, "adjoint seeds need finite states above the cutoff");
+        }
+        seeds[static_cast<size_t>(i)] = z[i];
+        seeds[static_cast<size_t>(n + i)] = dx / norm;
+        seeds[static_cast<size_t>(2 * n + i)] = dy / norm;
+        seeds[static_cast<size_t>(3 * n + i)] = dz / norm;
+        seeds[static_cast<size_t>(4 * n + i)] = kinetic_eV[i];
+        seeds[static_cast<size_t>(5 * n + i)] = 1.0;
+    }
+    RreaArenaIndex const& ix = ctx->tables.index();
+    for (int t : {RREA_T_E_COLLISION, RREA_T_E_SOFT_RAD}) {
+        if (ix.hot[t].mode != RREA_INTERP_LOGLOG) {
+            return fail(ctx, RREA_GPU_ERR_TABLES, "the adjoint's stopping powers must be log-log tables");
+        }
+    }
+    rrea_launch::AdjointSetup in{};
+    in.n = n;
+    in.n_nodes = cfg->n_nodes;
+    in.z0 = cfg->z_lo;
+    in.dz_node = (cfg->z_hi - cfg->z_lo) / (cfg->n_nodes - 1);
+    in.steps = cfg->steps;
+    in.substeps = cfg->substeps;
+    in.ckpt_every = cfg->checkpoint_every;
+    in.dt = cfg->dt_s;
+    in.rho = cfg->density_ratio;
+    in.cutoff = cfg->cutoff_eV;
+    in.scatter_rms = cfg->scatter_rms_rad;
+    in.k_th = cfg->k_threshold_eV;
+    in.tau_k = cfg->k_width_eV;
+    in.z_p = cfg->z_plane_m;
+    in.tau_z = cfg->z_width_m;
+    in.lambda = cfg->plane_weight;
+    in.seed = cfg->rng_seed;
+    in.col = ix.hot[RREA_T_E_COLLISION];
+    in.soft = ix.hot[RREA_T_E_SOFT_RAD];
+    RREA_CUDA(ctx, rrea_launch::adjoint_stage(in, seeds.data(), weight, id, ctx->num_sms * 4, ctx->adjoint));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_adjoint_forward(rrea_gpu_ctx* ctx, const double* e_nodes_device, double* loss)
+{
+    if (!ctx || !e_nodes_device || !loss) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->adjoint) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no adjoint problem is staged");
+    RREA_CUDA(ctx, rrea_launch::adjoint_forward(*ctx->adjoint, ctx->d_arena, e_nodes_device, *loss, ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_adjoint_backward(rrea_gpu_ctx* ctx, const double* e_nodes_device, double* grad_device)
+{
+    if (!ctx || !e_nodes_device || !grad_device) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->adjoint) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no adjoint problem is staged");
+    RREA_CUDA(ctx, rrea_launch::adjoint_backward(*ctx->adjoint, ctx->d_arena, e_nodes_device, grad_device,
+                                                 ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_adjoint_final_state(rrea_gpu_ctx* ctx, double* state6)
+{
+    if (!ctx || !state6) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->adjoint) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no adjoint problem is staged");
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    RREA_CUDA(ctx, rrea_launch::adjoint_final_state(*ctx->adjoint, state6));
+    return RREA_GPU_OK;
 }
 
 }  // extern "C"

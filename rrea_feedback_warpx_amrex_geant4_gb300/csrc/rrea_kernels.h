@@ -218,4 +218,27 @@ cudaError_t ensemble_partition(rrea_dev::TileColumns const& src, int64_t n, uint
                                cudaStream_t stream);
 cudaError_t ensemble_retire(int64_t* id, const int32_t* cpu, int64_t n, int32_t inst, cudaStream_t stream);
 
+// Pathwise adjoint of the charged push (rrea_adjoint.cu).
+struct AdjointSetup {
+    int64_t n;
+    int n_nodes;
+    double z0, dz_node;
+    int steps, substeps, ckpt_every;
+    double dt, rho, cutoff, scatter_rms;
+    double k_th, tau_k, z_p, tau_z, lambda;
+    uint64_t seed;
+    RreaTable1DIndex col, soft;
+};
+struct AdjointState;
+void adjoint_free(AdjointState* s);
+int adjoint_max_nodes();
+// seeds6: z, dx, dy, dz, K, alive (6 x n, host); w (n); id (n)
+cudaError_t adjoint_stage(AdjointSetup const& in, const double* seeds6, const double* w, const uint64_t* id,
+                          int blocks, AdjointState*& out);
+cudaError_t adjoint_forward(AdjointState& s, const double* arena, const double* e_nodes, double& loss,
+                            cudaStream_t stream);
+cudaError_t adjoint_backward(AdjointState& s, const double* arena, const double* e_nodes, double* grad,
+                             cudaStream_t stream);
+cudaError_t adjoint_final_state(AdjointState const& s, double* host6);
+
 }  // namespace rrea_launch

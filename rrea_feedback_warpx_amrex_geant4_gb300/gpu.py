@@ -126,6 +126,8 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_sources_device", "rrea_gpu_advance_field_coupled_from_current",
     "rrea_gpu_set_schedule", "rrea_gpu_ensemble_configure", "rrea_gpu_ensemble_partition", "rrea_gpu_ensemble_retire",
     "rrea_gpu_ensemble_census", "rrea_gpu_ensemble_population_thin",
+    "rrea_gpu_default_adjoint_config", "rrea_gpu_adjoint_stage", "rrea_gpu_adjoint_forward",
+    "rrea_gpu_adjoint_backward", "rrea_gpu_adjoint_final_state",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -254,7 +256,8 @@ def load_library(path=LIB_PATH):
     for name in EXPORTED_SYMBOLS:
         fn = getattr(lib, name)
         if fn.restype is not None and name not in ("rrea_gpu_default_config", "rrea_gpu_last_error",
-                                                   "rrea_gpu_default_fluid_config"):
+                                                   "rrea_gpu_default_fluid_config",
+                                                   "rrea_gpu_default_adjoint_config"):
             fn.restype = ctypes.c_int
     _lib = lib
     return lib
