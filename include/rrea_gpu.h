@@ -760,6 +760,16 @@ rrea_gpu_status rrea_gpu_fluid_transport(rrea_gpu_ctx* ctx, double dt_s, const d
  * non-periodic z and the Yee CFL, like rrea_gpu_advance_field.
  */
 rrea_gpu_status rrea_gpu_advance_field_coupled(rrea_gpu_ctx* ctx, double dt_s, double* diag);
+/* The fluid and event-source totals of the reduced diagnostics
+ * (O/RreaCouplingDiagnostics.cpp:318-333, 469-471, 730-736) from the fluid
+ * state and the cell sources accumulated since rrea_gpu_reset_sources,
+ * normalised as NormalizeAndSync leaves them for a step of dt_s.  out16:
+ * total_ne_low, total_n_pos, total_n_neg (plain cell sums), N_low_e_real,
+ * N_pos_real, N_neg_real, rho_fluid_C (RZ volume integrals),
+ * total_rho_fluid, total_S_low_electron, total_S_positive_ion,
+ * total_S_direct_negative_ion, ionization_event_count,
+ * total_energy_loss_ev_m3 (cell sums), max_ne_low, max_sigma, min_tau_m. */
+rrea_gpu_status rrea_gpu_fluid_reductions(rrea_gpu_ctx* ctx, double dt_s, double* out16);
 /* The two halves of the coupled step of a sharded run, as
  * rrea_gpu_current_device / rrea_gpu_advance_field_from_current are for the
  * kinetic-only update: the caller sums the kinetic face current

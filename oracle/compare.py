@@ -3,12 +3,15 @@
 Parity comparison of one GPU species phase (electron, positron or photon) against the
 oracle on the same input tile.  Discrete results (dispositions, substep and hazard-draw counts,
 validity, secondary keys) must match exactly; FP64 state within 1e-12
-relative (positions with a 1e-12 x domain-size floor), except at most one
-entry in 10^4 (at least one), which stays within 1e-11: a particle with
-tens of interleaved events accumulates the last-ulp differences of the
+relative (positions with a 1e-12 x domain-size floor), except at most
+0.1 % of the entries (at least one), which stay within 1e-11: a particle
+with tens of interleaved events accumulates the last-ulp differences of the
 device's FMA contraction and log/exp against the x86-64 host arithmetic;
 cell-source grids, which the GPU accumulates with atomics in
-nondeterministic order, within 1.6e-11 of each grid's largest cell.
+nondeterministic order, within 1.6e-11 of each grid's largest cell, except
+at most 0.1 % of the nonzero cells (at least four: one deposit's CIC
+stencil) within the bound that the position tolerance carries into a CIC
+weight (1e-12 x domain / cell size of the grid's largest cell).
 """
 import numpy as np
 
@@ -16,7 +19,7 @@ from . import oracle as _oracle
 from rrea_feedback_warpx_amrex_geant4_gb300.workloads import copy_tile
 
 RTOL = 1.0e-12
-TAIL_FRACTION = 1.0e-4
+TAIL_FRACTION = 1.0e-3
 TAIL_RTOL = 1.0e-11
 
 
@@ -37,16 +40,22 @@ def entries_ok(a, b, atol):
     return bool(loose.all() and n_over <= allowed), n_over
 
 
-def cells_ok(g, o):
+def cells_ok(g, o, spread=0.0):
     """Cell grid check: every cell within 16 RTOL of the grid's largest
-    cell (a cell sums up to ~10^4 deposits in arbitrary order).  Returns
+    cell (a cell sums up to ~10^4 deposits in arbitrary order), except at
+    most TAIL_FRACTION of the nonzero cells (at least four), which stay
+    within `spread` of it (the position tolerance over the cell size: the
+    CIC weights move that much when a deposit's position does).  Returns
     (ok, n_over)."""
     g = np.asarray(g, dtype=np.float64)
     o = np.asarray(o, dtype=np.float64)
     scale = max(np.abs(o).max(), 1e-300)
     strict = _close(g, o, 0.0, 16 * RTOL * scale)
+    loose = _close(g, o, 0.0, max(16 * RTOL, spread) * scale)
     n_over = int((~strict).sum())
-    return n_over == 0, n_over
+    nonzero = int(((g != 0.0) | (o != 0.0)).sum())
+    allowed = max(4, int(TAIL_FRACTION * nonzero))
+    return bool(loose.all() and n_over <= allowed), n_over
 
 
 def _worst(a, b, atol):
@@ -157,8 +166,10 @@ def compare(cfg, gpu, orc, domain_scale, parent_energy=None):
             if not ok:
                 w = _worst(g_sec[key], os_[key], atol)
                 problems.append(f"secondary {key} differs for {n_over} (worst {w:.2e})")
+    cell = min((cfg.r_hi - cfg.r_lo) / cfg.nr, (cfg.z_hi - cfg.z_lo) / cfg.nz)
+    spread = RTOL * domain_scale / cell
     for f in range(5):
-        ok, n_over = cells_ok(g_cells[f], o["cells"][f])
+        ok, n_over = cells_ok(g_cells[f], o["cells"][f], spread)
         if not ok:
             problems.append(f"cell source field {f} differs in {n_over} cells")
     return problems

@@ -86,9 +86,14 @@ class AvalancheRun:
     electron tile, then `steps` whole kinetic steps."""
 
     def __init__(self, ctx, electrons, photons=None, positrons=None, feedback=False, field_substeps=2,
-                 population_target=None, split_min_weight=0.0, control_interval=1, controller_salt=0):
+                 population_target=None, split_min_weight=0.0, control_interval=1, controller_salt=0,
+                 fluid=False):
+        """feedback: the field follows the step's current; fluid (with
+        feedback): through the coupled carrier-fluid + Maxwell step (the
+        context's fluid must be configured) instead of the kinetic-only one."""
         self.ctx = ctx
         self.feedback = feedback
+        self.fluid = fluid
         self.field_substeps = field_substeps
         # adaptive_resample_v1: e- and e+ macro targets, the split floor, the
         # control interval in steps and the controller's RNG salt
@@ -109,7 +114,9 @@ class AvalancheRun:
         """One whole kinetic step; returns the particle-steps it moved and
         the drain's (FIFO items, survivors)."""
         ctx = self.ctx
-        ctx.reset_current()
+        if self.feedback:
+            ctx.reset_current()
+        ctx.reset_sources()
         moved = 0
         for sp, fn in ((gpu.SPECIES_ELECTRON, ctx.step_electrons_resident),
                        (gpu.SPECIES_PHOTON, ctx.step_photons_resident),
@@ -134,7 +141,10 @@ class AvalancheRun:
             # split refill at the step boundary (ApplyAdaptivePopulationControl)
             for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON):
                 self.split += ctx.population_split(sp, self.population_target, self.split_min_weight)
-        if self.feedback:
+        if self.feedback and self.fluid:
+            ctx.fluid_take_sources(dt_s)
+            ctx.advance_field_coupled(dt_s)
+        elif self.feedback:
             ctx.advance_field(dt_s, self.field_substeps)
         self.step += 1
         return moved, drained
@@ -157,6 +167,9 @@ class AvalancheRun:
             if (k + 1) % census_every == 0 or k + 1 == steps:
                 row, spectra = census_row(self.ctx, self.step)
                 row["particle_steps"] = moved_total
+                if self.fluid:
+                    row.update(self.ctx.fluid_reductions(dt_s))
+                    row["N_inst_e_real"] = row["electron_weight"] + row["N_low_e_real"]
                 history.append(row)
         wall = time.perf_counter() - t0
         launches = gpu.kernel_launches() - l0
@@ -201,17 +214,21 @@ REDUCED_COLUMNS = (  # our census fields under the reduced CSV's column names
     ("N_kinetic_e_ge_100keV_real", "electron_ge_100keV"), ("N_photon_real", "photon_weight"),
     ("N_positron_real", "positron_weight"), ("N_positron_ge_100keV_real", "positron_ge_100keV"),
 )
+# with the carrier fluid: its totals (O/RreaCouplingDiagnostics.cpp:318-354, 469-471, 730-736)
+FLUID_REDUCED_COLUMNS = tuple((c, c) for c in gpu.FLUID_REDUCED_COLUMNS) + (("N_inst_e_real", "N_inst_e_real"),)
 
 
 def write_reduced_csv(path, history):
     """The census history as rrea_reduced.csv-style rows (the columns the
     census provides, under the reduced diagnostics' names,
     O/RreaCouplingDiagnostics.cpp:950-980)."""
+    columns = REDUCED_COLUMNS + (FLUID_REDUCED_COLUMNS if history and "total_ne_low" in history[-1] else ())
     with open(path, "w", newline="") as f:
         w = csv.writer(f)
-        w.writerow([c for c, _ in REDUCED_COLUMNS])
+        w.writerow([c for c, _ in columns])
         for h in history:
-            w.writerow([h[k] for _, k in REDUCED_COLUMNS])
+            if all(k in h for _, k in columns):
+                w.writerow([h[k] for _, k in columns])
 
 
 def main():

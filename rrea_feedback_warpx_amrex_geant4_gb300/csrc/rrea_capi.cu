@@ -2408,6 +2408,16 @@ rrea_gpu_status rrea_gpu_fluid_transport(rrea_gpu_ctx* ctx, double dt_s, const d
     return fluid_checked(ctx, ok);
 }
 
+rrea_gpu_status rrea_gpu_fluid_reductions(rrea_gpu_ctx* ctx, double dt_s, double* out16)
+{
+    if (rrea_gpu_status const s = fluid_ready(ctx)) return s;
+    if (!out16 || !(dt_s > 0.0) || !std::isfinite(dt_s)) return RREA_GPU_ERR_ARGUMENT;
+    double v[16];
+    RREA_CUDA(ctx, rrea_launch::fluid_reductions(*ctx->fluid, ctx->d_cells, dt_s, v, ctx->stream));
+    std::memcpy(out16, v, sizeof(v));
+    return RREA_GPU_OK;
+}
+
 rrea_gpu_status rrea_gpu_advance_field_coupled(rrea_gpu_ctx* ctx, double dt_s, double* diag)
 {
     if (rrea_gpu_status const s = fluid_ready(ctx)) return s;

@@ -45,6 +45,13 @@ __device__ __forceinline__ u64 ordered(double x)
     return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
 }
 
+inline u64 host_ordered(double x)
+{
+    u64 b;
+    std::memcpy(&b, &x, sizeof(b));
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+
 __device__ __forceinline__ u64 warp_max(u64 v)
 {
     for (int o = 16; o > 0; o >>= 1) {
@@ -831,6 +838,59 @@ __global__ void update_kernel(TransportParams p, const double* __restrict__ old3
     }
 }
 
+// The fluid and event-source totals of the reduced diagnostics
+// (O/RreaCouplingDiagnostics.cpp:318-333, 469-471, 730-736): plain sums of
+// the cell values (MultiFab::sum), RZ volume integrals (volume_integral_rz,
+// :89-106), maxima and minima, and the step's sources normalised as
+// NormalizeAndSync leaves them (rates by V dt, the ionization count and the
+// energy loss by V).  out (sums): 0..2 sum ne, np, nn; 3..5 their volume
+// integrals; 6 volume integral of rho; 7 sum rho; 8..10 sum of the three
+// source rates; 11 ionization count density sum; 12 energy-loss density sum.
+// words: max ne, max sigma, min tau (ordered keys).
+__global__ void reductions_kernel(Grid g, double dt, const double* __restrict__ ne, const double* __restrict__ np,
+                                  const double* __restrict__ nn, const double* __restrict__ rho,
+                                  const double* __restrict__ sigma, const double* __restrict__ tau,
+                                  const double* __restrict__ cells, double* sums, u64* words)
+{
+    int64_t const n = static_cast<int64_t>(g.nr) * g.nz;
+    double acc[13];
+    for (double& a : acc) a = 0.0;
+    u64 max_ne = ordered(-1.0e308), max_sigma = ordered(-1.0e308), min_tau = ordered(1.0e308);
+    int64_t const stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < n; k += stride) {
+        int const i = static_cast<int>(k % g.nr);
+        double const r_in = g.r_lo + static_cast<double>(i) * g.dr;
+        double const v = shell_volume(r_in, r_in + g.dr, g.dz);
+        acc[0] += ne[k];
+        acc[1] += np[k];
+        acc[2] += nn[k];
+        acc[3] += ne[k] * v;
+        acc[4] += np[k] * v;
+        acc[5] += nn[k] * v;
+        acc[6] += rho[k] * v;
+        acc[7] += rho[k];
+        if (cells) {
+            double const vd = v * dt;
+            acc[8] += vd > 0.0 ? cells[k] / vd : 0.0;
+            acc[9] += vd > 0.0 ? cells[n + k] / vd : 0.0;
+            acc[10] += vd > 0.0 ? cells[2 * n + k] / vd : 0.0;
+            acc[11] += v > 0.0 ? cells[3 * n + k] / v : 0.0;
+            acc[12] += v > 0.0 ? cells[4 * n + k] / v : 0.0;
+        }
+        max_ne = ordered(ne[k]) > max_ne ? ordered(ne[k]) : max_ne;
+        max_sigma = ordered(sigma[k]) > max_sigma ? ordered(sigma[k]) : max_sigma;
+        min_tau = ordered(tau[k]) < min_tau ? ordered(tau[k]) : min_tau;
+    }
+    for (int c = 0; c < 13; ++c) post_sum(sums + c, acc[c]);
+    max_ne = warp_max(max_ne);
+    max_sigma = warp_max(max_sigma);
+    if (lane0()) {
+        atomicMax(words, max_ne);
+        atomicMax(words + 1, max_sigma);
+    }
+    post_min(words + 2, min_tau);
+}
+
 }  // namespace fluid
 }  // namespace rrea_dev
 
@@ -1339,6 +1399,26 @@ cudaError_t fluid_transport(FluidState& s, double dt, const double* efr, const d
 }
 
 const double* fluid_flux(FluidState const& s, int dir) { return dir == 0 ? s.fr : s.fz; }
+
+cudaError_t fluid_reductions(FluidState& s, const double* cells5, double dt, double out16[16], cudaStream_t stream)
+{
+    cudaError_t e = reset_reductions(s, stream);
+    if (e != cudaSuccess) return e;
+    u64 init[3] = {rrea_dev::fluid::host_ordered(-1.0e308), rrea_dev::fluid::host_ordered(-1.0e308),
+                   rrea_dev::fluid::host_ordered(1.0e308)};
+    if ((e = cudaMemcpyAsync(s.words, init, sizeof(init), cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
+    note_launch();
+    rrea_dev::fluid::reductions_kernel<<<s.blocks, 256, 0, stream>>>(dev_grid(s.grid), dt, s.ne, s.np, s.nn, s.rho,
+                                                                     s.sigma, s.tau, cells5, s.sums, s.words);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    Readback r;
+    if ((e = read_reductions(s, r, stream)) != cudaSuccess) return e;
+    for (int c = 0; c < 13; ++c) out16[c] = r.s[c];
+    out16[13] = from_ordered(r.w[0]);
+    out16[14] = from_ordered(r.w[1]);
+    out16[15] = from_ordered(r.w[2]);
+    return cudaSuccess;
+}
 
 cudaError_t fluid_coupled_step(FluidState& s, CoupledField const& f, double dt, double diag8[8], bool& ok,
                                cudaStream_t stream)

@@ -195,6 +195,9 @@ double* fluid_field(FluidState& s, int field);
 void fluid_bind_chi(FluidState& s, bool bound);
 int64_t fluid_cells(FluidState const& s);
 const double* fluid_flux(FluidState const& s, int dir);
+// The reduced diagnostics' fluid and source totals (16 doubles; layout at
+// rrea_gpu_fluid_reductions); cells5 may be null.
+cudaError_t fluid_reductions(FluidState& s, const double* cells5, double dt, double out16[16], cudaStream_t stream);
 cudaError_t fluid_take_sources(FluidState& s, const double* cells5, double dt, cudaStream_t stream);
 cudaError_t fluid_react(FluidState& s, double dt, bool clear, double& residual, bool& ok, cudaStream_t stream);
 cudaError_t fluid_max_reaction_frequency(FluidState& s, double& out, cudaStream_t stream);

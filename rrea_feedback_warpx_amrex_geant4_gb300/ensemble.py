@@ -210,20 +210,24 @@ def main():
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--duration-scale", type=float, default=1.0)
     p.add_argument("--target", type=int, default=20_000)
+    p.add_argument("--control-every", type=int, default=16, help="steps between population-control checks")
     p.add_argument("--sequential", action="store_true", help="also run the instances one by one")
     p.add_argument("--json", default=None)
     args = p.parse_args()
     inst = config3_instances(args.instances, duration_scale=args.duration_scale, target=args.target)
     t0 = time.perf_counter()
-    batched = run_batched(inst)
+    batched = run_batched(inst, control_every=args.control_every)
     t_b = time.perf_counter() - t0
-    summary = {"instances": args.instances, "batched_s": t_b, "batched_particle_steps": batched["particle_steps"],
+    summary = {"instances": args.instances, "duration_scale": args.duration_scale, "target": args.target,
+               "control_every": args.control_every, "batched_s": t_b, "batched_steps": batched["steps"],
+               "thinned": batched["thinned"], "batched_particle_steps": batched["particle_steps"],
                "autotune": batched["autotune"][0] if batched["autotune"] else None,
                "multiplication": [r["multiplication"] for r in batched["results"]]}
     if args.sequential:
         t0 = time.perf_counter()
-        seq = run_sequential(inst)
+        seq = run_sequential(inst, control_every=args.control_every)
         summary["sequential_s"] = time.perf_counter() - t0
+        summary["sequential_steps"] = seq["steps"]
         summary["speedup"] = summary["sequential_s"] / t_b
     print(json.dumps(summary))
     if args.json:

@@ -68,6 +68,10 @@ FLUID_TRANSPORT_DIAG = ("max_face_conductivity", "max_diffusion_number", "unlimi
                         "neg_center_r", "neg_center_z", "density_ratio_at_pos_center")
 FLUID_COUPLED_DIAG = ("substeps", "full_conduction", "full_diffusion", "full_reaction", "max_reaction_number",
                       "max_dt_sigma", "max_diffusion_number", "max_residual")
+FLUID_REDUCED_COLUMNS = ("total_ne_low", "total_n_pos", "total_n_neg", "N_low_e_real", "N_pos_real", "N_neg_real",
+                         "rho_fluid_C", "total_rho_fluid", "total_S_low_electron", "total_S_positive_ion",
+                         "total_S_direct_negative_ion", "ionization_event_count", "total_energy_loss_ev_m3",
+                         "max_ne_low", "max_sigma", "min_tau_m")
 FLUID_CLOSURE_DIAG = ("min_en_td", "max_en_td", "held_below", "above_range", "invalid", "electron_count",
                       "held_below_electron_count", "electron_source_rate")
 
@@ -123,7 +127,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_fluid_get_closure_fields", "rrea_gpu_fluid_take_sources", "rrea_gpu_fluid_react",
     "rrea_gpu_fluid_max_reaction_frequency", "rrea_gpu_fluid_conductivity", "rrea_gpu_fluid_charge_density",
     "rrea_gpu_fluid_evaluate_closure", "rrea_gpu_fluid_transport", "rrea_gpu_advance_field_coupled",
-    "rrea_gpu_sources_device", "rrea_gpu_advance_field_coupled_from_current",
+    "rrea_gpu_sources_device", "rrea_gpu_advance_field_coupled_from_current", "rrea_gpu_fluid_reductions",
     "rrea_gpu_set_schedule", "rrea_gpu_ensemble_configure", "rrea_gpu_ensemble_partition", "rrea_gpu_ensemble_retire",
     "rrea_gpu_ensemble_census", "rrea_gpu_ensemble_population_thin",
     "rrea_gpu_default_adjoint_config", "rrea_gpu_adjoint_stage", "rrea_gpu_adjoint_forward",
@@ -245,6 +249,7 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_advance_field_coupled.argtypes = [vp, ctypes.c_double, _D]
     lib.rrea_gpu_set_schedule.argtypes = [vp, ctypes.c_int32]
     lib.rrea_gpu_sources_device.argtypes = [vp, ctypes.POINTER(vp)]
+    lib.rrea_gpu_fluid_reductions.argtypes = [vp, ctypes.c_double, _D]
     lib.rrea_gpu_advance_field_coupled_from_current.argtypes = [vp, ctypes.c_double, _D]
     lib.rrea_gpu_ensemble_configure.argtypes = [vp, ctypes.c_int32, _D]
     lib.rrea_gpu_ensemble_partition.argtypes = [vp, ctypes.c_int32, _i64p]
@@ -728,6 +733,12 @@ class RreaGpuContext:
         d = np.zeros(8)
         self._check(self.lib.rrea_gpu_advance_field_coupled_from_current(self.handle, dt_s, d.ctypes.data_as(_D)))
         return dict(zip(FLUID_COUPLED_DIAG, d))
+
+    def fluid_reductions(self, dt_s):
+        """The reduced diagnostics' fluid and source totals (FLUID_REDUCED_COLUMNS)."""
+        d = np.zeros(16)
+        self._check(self.lib.rrea_gpu_fluid_reductions(self.handle, dt_s, d.ctypes.data_as(_D)))
+        return dict(zip(FLUID_REDUCED_COLUMNS, d))
 
     def advance_field_coupled(self, dt_s):
         """The coupled fluid + Maxwell step; returns its diagnostics dict."""

@@ -10,7 +10,7 @@ net-chord current.  The oracle runs the same step on the same staged tiles.
 Exact: tile sizes, ids and their order after commit and compaction (so
 every disposition, secondary count and FIFO survivor agreed), weights.
 FP64 state: within 1e-12 relative (positions: of the domain size) but at
-most one entry in 10^4, within 1e-11 (oracle/compare.py).  Field after the update: within 1e-12 of each vector's largest
+most 0.1 % of the entries, within 1e-11 (oracle/compare.py).  Field after the update: within 1e-12 of each vector's largest
 entry."""
 import os
 import sys

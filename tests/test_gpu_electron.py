@@ -4,7 +4,7 @@ entry point.
 
 Tolerances: dispositions, substep counts, hazard-draw counts, validity and
 secondary keys bit-exact; FP64 state within 1e-12 relative (positions with
-a 1e-12 x domain floor) but at most one entry in 10^4, within 1e-11;
+a 1e-12 x domain floor) but at most 0.1 % of the entries, within 1e-11;
 atomically accumulated cell sources within 1.6e-11 of each grid's largest
 cell."""
 import numpy as np

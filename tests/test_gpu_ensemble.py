@@ -3,7 +3,7 @@ the same instances run one by one.
 
 Instances: four uniform-field avalanches of the plain case's air, tables,
 grid and 7.2 MeV seeds at 400, 550, 700 and 900 kV/m, 30-80 seeds, 25-60
-steps of 0.5 ns; one of them under a 150-particle population target, so the
+steps of 0.5 ns; one of them under a 60-particle population target, so the
 per-instance thinning runs.  Each instance alone is the same instance on a
 context of its own (cpu = k).
 
@@ -31,7 +31,7 @@ def mods():
 
 def _instances(ensemble):
     I = ensemble.Instance
-    return [I(4.0e5, 60, 40), I(5.5e5, 40, 25), I(7.0e5, 80, 60, target=150), I(9.0e5, 30, 50)]
+    return [I(4.0e5, 60, 40), I(5.5e5, 40, 25), I(7.0e5, 80, 60, target=60), I(9.0e5, 30, 50)]
 
 
 def _tiles(run, gpu, workloads):

@@ -291,4 +291,16 @@ def test_sources_from_the_kinetic_step(mods):
     assert gs["n_pos"].sum() > 0
     after = ctx.fluid_source_rates()
     assert not any(v.any() for v in after.values())   # the step clears the source rates
+    # the reduced diagnostics' fluid and source totals
+    red = ctx.fluid_reductions(dt)
+    want = {"total_ne_low": gs["n_e"].sum(), "total_n_pos": gs["n_pos"].sum(), "total_n_neg": gs["n_neg"].sum(),
+            "N_low_e_real": (gs["n_e"] * vol).sum(), "N_pos_real": (gs["n_pos"] * vol).sum(),
+            "N_neg_real": (gs["n_neg"] * vol).sum(), "rho_fluid_C": (gs["rho"] * vol).sum(),
+            "total_rho_fluid": gs["rho"].sum(), "total_S_low_electron": (cells[0] / (vol * dt)).sum(),
+            "total_S_positive_ion": (cells[1] / (vol * dt)).sum(),
+            "total_S_direct_negative_ion": (cells[2] / (vol * dt)).sum(),
+            "ionization_event_count": (cells[3] / vol).sum(), "total_energy_loss_ev_m3": (cells[4] / vol).sum(),
+            "max_ne_low": gs["n_e"].max(), "max_sigma": gs["sigma"].max(), "min_tau_m": gs["tau"].min()}
+    for key, value in want.items():
+        assert red[key] == pytest.approx(value, rel=1e-12, abs=1e-300), key
     ctx.close()

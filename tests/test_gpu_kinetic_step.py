@@ -11,7 +11,7 @@ field the GPU left on the device (downloaded bit for bit for the oracle).
 
 Tolerances as in the per-phase tests: each phase through the shared phase
 comparison (discrete outcomes exact, FP64 state within 1e-12 but at most
-one entry in 10^4, within 1e-11); survivor keys
+0.1 % of the entries, within 1e-11); survivor keys
 bit-exact; the net-chord current within 1e-12 of its largest entry (atomics
 sum the signed index fluxes in nondeterministic order); the field
 update within 1e-12 of each vector's largest entry given the GPU's current."""

@@ -10,7 +10,7 @@ start from bit-identical input.
 Tolerances: survivor count, order and keys (species, process, root species,
 parent index, root key, lineage) bit-exact; birth fraction exactly 1; FP64
 payload within 1e-12 (positions with a 1e-12 x domain floor, energies
-relative) but at most one entry in 10^4, within 1e-11; cell sources within
+relative) but at most 0.1 % of the entries, within 1e-11; cell sources within
 1.6e-11 and the net-chord current within 1e-12 of each grid's largest
 entry (both summed with atomics in arbitrary order)."""
 import numpy as np

@@ -3,8 +3,8 @@ C-ABI drop-in entry point rrea_gpu_apply_photons.
 
 Tolerances: dispositions, hazard-draw counts, validity and secondary keys
 (species, process, parent, lineage, root key) bit-exact; FP64 state within
-1e-12 relative (positions with a 1e-12 x domain floor) but at most one
-entry in 10^4, within 1e-11; secondary energies
+1e-12 relative (positions with a 1e-12 x domain floor) but at most 0.1 %
+of the entries, within 1e-11; secondary energies
 and directions within 1e-12 of the parent photon's energy scale (they are
 differences of parent-scale quantities); atomically accumulated cell
 sources within 1.6e-11 of each grid's largest cell."""

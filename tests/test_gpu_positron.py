@@ -3,7 +3,7 @@ drop-in entry point rrea_gpu_apply_positrons.
 
 Tolerances: dispositions, substep and hazard-draw counts, validity and
 secondary keys bit-exact; FP64 state within 1e-12 relative (positions with
-a 1e-12 x domain floor) but at most one entry in 10^4, within 1e-11;
+a 1e-12 x domain floor) but at most 0.1 % of the entries, within 1e-11;
 secondary
 energies and directions within 1e-12 of the parent's total energy scale (K + 2 m c^2: the in-flight annihilation
 photon direction is a momentum difference at that scale); atomically

@@ -10,7 +10,7 @@ interpolation is pinned bit-exact to the reference's RreaAltitudeProfile
 (tests/test_oracle_golden.py).
 
 Tolerances as in the uniform-density phase tests: discrete outcomes
-bit-exact, FP64 state within 1e-12 but at most one entry in 10^4, within
+bit-exact, FP64 state within 1e-12 but at most 0.1 % of the entries, within
 1e-11."""
 import numpy as np
 import pytest

@@ -8,7 +8,7 @@ from the GPU's tiles after each injection (lockstep), bound to the same
 profile and field.
 
 Tolerances as in the resident-loop test: sizes, ids and weights exact, FP64
-state within 1e-12 relative (at most one entry in 10^4 within 1e-11)."""
+state within 1e-12 relative (at most 0.1 % of the entries within 1e-11)."""
 import os
 
 import numpy as np

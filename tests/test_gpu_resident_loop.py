@@ -7,7 +7,7 @@ restatement of the overlay's particle creation.
 The oracle starts every step from the GPU's fetched tiles (lockstep), so a
 one-ulp difference of one step cannot grow into a different history in the
 next.  Tolerances: tile sizes, ids and their order, and weights exact; FP64
-state within 1e-12 relative (at most one entry in 10^4 within 1e-11),
+state within 1e-12 relative (at most 0.1 % of the entries within 1e-11),
 as in the phase tests."""
 import numpy as np
 import pytest
