@@ -805,6 +805,13 @@ rrea_gpu_status rrea_gpu_advance_field_coupled_from_current(rrea_gpu_ctx* ctx, d
  * census / population_thin: rrea_gpu_census_resident and
  *   rrea_gpu_population_thin_resident (without staged candidates) on one
  *   instance's slice of the last partition.
+ * population_thin_all: the population control of every instance in one
+ *   pass, no partition needed: instance k, due when its valid particles
+ *   exceed 1.25 targets[k] (host, n_instances; 0 = no control), is thinned
+ *   exactly as population_thin(species, k, targets[k], step, salt) would
+ *   thin its slice.  removed_per_instance (host, n_instances) receives the
+ *   removals; stats the totals in population_thin's layout.  A rejected or
+ *   short plan of any instance applies nothing.
  */
 rrea_gpu_status rrea_gpu_ensemble_configure(rrea_gpu_ctx* ctx, int32_t n_instances, const double* ambient_ez);
 rrea_gpu_status rrea_gpu_ensemble_partition(rrea_gpu_ctx* ctx, int32_t species, int64_t* counts);
@@ -814,6 +821,9 @@ rrea_gpu_status rrea_gpu_ensemble_census(rrea_gpu_ctx* ctx, int32_t species, int
                                          double* out);
 rrea_gpu_status rrea_gpu_ensemble_population_thin(rrea_gpu_ctx* ctx, int32_t species, int32_t instance,
                                                   int64_t target, int32_t step, uint64_t salt, int64_t* stats);
+rrea_gpu_status rrea_gpu_ensemble_population_thin_all(rrea_gpu_ctx* ctx, int32_t species, const int64_t* targets,
+                                                      int32_t step, uint64_t salt, int64_t* removed_per_instance,
+                                                      int64_t* stats);
 
 /*
  * ---- Pathwise adjoint of the charged push --------------------------------

@@ -2610,6 +2610,56 @@ rrea_gpu_status rrea_gpu_ensemble_population_thin(rrea_gpu_ctx* ctx, int32_t spe
     return s;
 }
 
+rrea_gpu_status rrea_gpu_ensemble_population_thin_all(rrea_gpu_ctx* ctx, int32_t species, const int64_t* targets,
+                                                      int32_t step, uint64_t salt, int64_t* removed_per_instance,
+                                                      int64_t* stats)
+{
+    if (!ctx || (species != RREA_SPECIES_ELECTRON && species != RREA_SPECIES_POSITRON) || !targets ||
+        !removed_per_instance) {
+        return RREA_GPU_ERR_ARGUMENT;
+    }
+    if (ctx->n_instances <= 0) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no ensemble is configured");
+    for (int32_t k = 0; k < ctx->n_instances; ++k) {
+        if (targets[k] < 0) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "population targets must be >= 0");
+    }
+    rrea_gpu_config const& c = ctx->cfg;
+    SpeciesTile& st = ctx->tiles[species];
+    rrea_launch::PopulationInput in{};
+    in.r = st.d[0]; in.z = st.d[1]; in.theta = st.d[2]; in.ux = st.d[3]; in.uy = st.d[4]; in.uz = st.d[5];
+    in.w = st.d[6];
+    in.id = st.id;
+    in.cpu = st.cpu;
+    in.n_tile = st.n;
+    in.species = species;
+    in.periodic_z = c.periodic_z;
+    in.r_lo = c.r_lo;
+    in.z_lo = c.z_lo;
+    in.z_hi = c.z_hi;
+    in.dr = (c.r_hi - c.r_lo) / c.nr;
+    in.dz = (c.z_hi - c.z_lo) / c.nz;
+    in.rng_seed = c.rng_seed;
+    in.salt = salt;
+    in.step = step;
+    in.targets = targets;
+    in.n_inst = ctx->n_instances;
+    rrea_launch::PopulationStats ps{};
+    RREA_CUDA(ctx, rrea_launch::population_thin_instances(in, ctx->pop_work, ps, removed_per_instance, ctx->stream));
+    if (stats) {
+        int64_t const v[8] = {ps.members, ps.live, ps.candidates, ps.supports, ps.capacity, ps.floor, ps.requested,
+                              ps.removed};
+        for (int k = 0; k < 8; ++k) stats[k] = v[k];
+    }
+    if (ps.status != 0) {
+        return fail(ctx, static_cast<rrea_gpu_status>(ps.status),
+                    ps.status == RREA_GPU_ERR_GEOMETRY
+                        ? "population control found a particle outside the supported grid"
+                        : "population control plan rejected (invalid support plan or insufficient progress); "
+                          "nothing was applied");
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
 }  // extern "C"
 
 // ===========================================================================

@@ -135,6 +135,11 @@ struct PopulationInput {
     int64_t target;
     uint64_t rng_seed, salt;
     int64_t step;
+    // ensemble (population_thin_instances): a plan per instance, the
+    // instance being a live row's cpu ordinal, with targets[k] (host memory)
+    // per instance
+    const int64_t* targets;
+    int32_t n_inst;
 };
 // members, live and candidate members, supports, removal capacity and the
 // geometric floor, the nominal request, particles removed; status is an
@@ -149,6 +154,10 @@ void population_work_free(PopulationWork* work);
 // status is 0).
 cudaError_t population_thin(PopulationInput const& in, PopulationWork*& work, PopulationStats& stats, int blocks,
                             cudaStream_t stream);
+// The per-instance plans of an ensemble in one pass (in.n_inst > 0); the
+// stats are totals and removed_per_instance (host, n_inst) the removals.
+cudaError_t population_thin_instances(PopulationInput const& in, PopulationWork*& work, PopulationStats& stats,
+                                      int64_t* removed_per_instance, cudaStream_t stream);
 // Split refill of the tile's first n rows: weight halved for every valid
 // particle at or above twice min_w, clones appended at rows n.. with ids
 // from first_id in tile order; *added < 0 when the clones exceed `room`

@@ -89,7 +89,7 @@ __global__ void records_kernel(rrea_launch::PopulationInput in, const int64_t* _
                                int64_t n_live, int64_t n_members, uint64_t* __restrict__ k1,
                                uint64_t* __restrict__ k2, uint64_t* __restrict__ k3, uint32_t* __restrict__ perm,
                                double* __restrict__ fr, double* __restrict__ fz, double* __restrict__ w,
-                               int* __restrict__ status)
+                               int* __restrict__ status, uint64_t* __restrict__ k0 = nullptr)
 {
     double constexpr me_c2 = 510998.95000;  // I/RreaConstants.H:9
     double constexpr c_light = 299792458.0;  // I/RreaConstants.H:10
@@ -97,7 +97,7 @@ __global__ void records_kernel(rrea_launch::PopulationInput in, const int64_t* _
          m += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         int64_t const src = members[m];
         double r, z, th, ux, uy, uz, wt;
-        uint64_t high, low;
+        uint64_t high, low, inst;
         uint32_t cand;
         if (m < n_live) {
             r = in.r[src];
@@ -110,6 +110,7 @@ __global__ void records_kernel(rrea_launch::PopulationInput in, const int64_t* _
             high = 0;
             // the particle's packed id/cpu word (40-bit id above the 24-bit cpu)
             low = (static_cast<uint64_t>(in.id[src]) << 24) | static_cast<uint32_t>(in.cpu ? in.cpu[src] & 0xffffff : 0);
+            inst = in.cpu ? static_cast<uint64_t>(static_cast<uint32_t>(in.cpu[src])) : 0;
             cand = 0;
         } else {
             rrea_gpu_secondary const s = in.cand[src];
@@ -124,6 +125,7 @@ __global__ void records_kernel(rrea_launch::PopulationInput in, const int64_t* _
             wt = s.weight;
             high = s.root_key;
             low = (s.lineage << 2) | static_cast<uint64_t>(static_cast<uint32_t>(s.root_species));
+            inst = s.root_key >> 40;
             cand = 1;
         }
         if (in.periodic_z) {
@@ -155,6 +157,7 @@ __global__ void records_kernel(rrea_launch::PopulationInput in, const int64_t* _
                 (static_cast<uint64_t>(phase) << 1) | cand;
         k2[m] = high;
         k3[m] = low;
+        if (k0) k0[m] = inst;
         perm[m] = static_cast<uint32_t>(m);
         fr[m] = rc - i0;
         fz[m] = zc - j0;
@@ -307,6 +310,147 @@ __global__ void split_scatter_kernel(TileColumns t, int64_t n, const uint32_t* _
     }
 }
 
+// ---- ensemble: the plans of every instance in one pass -----------------
+// Valid live rows per instance (the instance is the cpu ordinal); a
+// shared-memory histogram per block when the instances fit.
+__global__ void instance_members_kernel(const int64_t* __restrict__ id, const int32_t* __restrict__ cpu, int64_t n,
+                                        uint32_t n_inst, bool shared_hist,
+                                        unsigned long long* __restrict__ counts)
+{
+    extern __shared__ unsigned long long hist[];
+    if (shared_hist) {
+        for (uint32_t k = threadIdx.x; k < n_inst; k += blockDim.x) hist[k] = 0;
+        __syncthreads();
+    }
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        uint32_t const k = static_cast<uint32_t>(cpu[i]);
+        if (id[i] <= 0 || k >= n_inst) continue;
+        atomicAdd(shared_hist ? hist + k : counts + k, 1ULL);
+    }
+    if (shared_hist) {
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < n_inst; k += blockDim.x) {
+            if (hist[k]) atomicAdd(counts + k, hist[k]);
+        }
+    }
+}
+
+// Members: valid live rows of the instances due for thinning.
+__global__ void flags_due_kernel(const int64_t* __restrict__ id, const int32_t* __restrict__ cpu, int64_t n,
+                                 const int64_t* __restrict__ due_target, uint32_t n_inst, uint32_t* __restrict__ flags)
+{
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        uint32_t const k = static_cast<uint32_t>(cpu[i]);
+        flags[i] = (id[i] > 0 && k < n_inst && due_target[k] >= 0) ? 1u : 0u;
+    }
+}
+
+// Sorted copies of the records and the heads of the (instance, support) groups.
+__global__ void heads_instances_kernel(const uint32_t* __restrict__ perm, int64_t n, const uint64_t* __restrict__ k0s,
+                                       const uint64_t* __restrict__ k1s, const uint64_t* __restrict__ k2,
+                                       const uint64_t* __restrict__ k3, const double* __restrict__ fr,
+                                       const double* __restrict__ fz, const double* __restrict__ w,
+                                       double* __restrict__ sfr, double* __restrict__ sfz, double* __restrict__ sw,
+                                       double* __restrict__ sw0, uint64_t* __restrict__ k2s,
+                                       uint64_t* __restrict__ k3s, uint32_t* __restrict__ heads)
+{
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        uint32_t const m = perm[i];
+        sfr[i] = fr[m];
+        sfz[i] = fz[m];
+        sw[i] = w[m];
+        sw0[i] = w[m];
+        k2s[i] = k2[m];
+        k3s[i] = k3[m];
+        heads[i] = (i == 0 || k0s[i] != k0s[i - 1] || (k1s[i] >> 32) != (k1s[i - 1] >> 32)) ? 1u : 0u;
+    }
+}
+
+// Each group's instance, the instances' capacity totals and the capacity
+// prefix at each instance's first group.
+__global__ void group_instances_kernel(const int64_t* __restrict__ begin, int64_t groups,
+                                       const uint64_t* __restrict__ k0s, const int64_t* __restrict__ capacity,
+                                       const int64_t* __restrict__ cap_prefix, uint32_t* __restrict__ ginst,
+                                       unsigned long long* __restrict__ cap_per_inst, int64_t* __restrict__ inst_base)
+{
+    for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < groups;
+         g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        uint64_t const k = k0s[begin[g]];
+        ginst[g] = static_cast<uint32_t>(k);
+        atomicAdd(cap_per_inst + k, static_cast<unsigned long long>(capacity[g]));
+        if (g == 0 || k0s[begin[g - 1]] != k) inst_base[k] = cap_prefix[g];
+    }
+}
+
+// The request of each due instance (RreaAdaptiveResampleAction): its
+// excess over the target, at most its removal capacity.
+__global__ void nominal_kernel(const unsigned long long* __restrict__ members, const unsigned long long* __restrict__ cap,
+                               const int64_t* __restrict__ due_target, uint32_t n_inst, int64_t* __restrict__ nominal)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_inst; k += gridDim.x * blockDim.x) {
+        int64_t const n = static_cast<int64_t>(members[k]), t = due_target[k];
+        int64_t const c = static_cast<int64_t>(cap[k]);
+        nominal[k] = t >= 0 ? (n - t < c ? n - t : c) : 0;
+    }
+}
+
+// group_thin_kernel with the request taken from the group's instance.
+__global__ void group_thin_instances_kernel(rrea_launch::PopulationInput in, const int64_t* __restrict__ begin,
+                                            int64_t groups, int64_t n, const uint64_t* __restrict__ k1s,
+                                            const uint64_t* __restrict__ k2s, const uint64_t* __restrict__ k3s,
+                                            const double* __restrict__ sfr, const double* __restrict__ sfz,
+                                            double* __restrict__ sw, const double* __restrict__ sw0,
+                                            const int64_t* __restrict__ capacity,
+                                            const int64_t* __restrict__ cap_prefix, const uint32_t* __restrict__ ginst,
+                                            const int64_t* __restrict__ inst_base, const int64_t* __restrict__ nominal,
+                                            unsigned long long* __restrict__ removed_per_inst, int* __restrict__ status)
+{
+    uint64_t const stream_key = in.species == RREA_SPECIES_POSITRON ? kStreamPositron : kStreamElectron;
+    uint64_t const channel = in.species == RREA_SPECIES_POSITRON ? kChResamplePositron : kChResampleElectron;
+    for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < groups;
+         g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        uint32_t const k = ginst[g];
+        int64_t const left = nominal[k] - (cap_prefix[g] - inst_base[k]);
+        int64_t const request = left <= 0 ? 0 : (left < capacity[g] ? left : capacity[g]);
+        if (request == 0) continue;
+        int64_t const b = begin[g];
+        int64_t const e = g + 1 < groups ? begin[g + 1] : n;
+        uint64_t const key1 = k1s[b];
+        int const sr = static_cast<int>(key1 >> 48) - kSupportBias;
+        int const sz = static_cast<int>((key1 >> 32) & 0xffffu) - kSupportBias;
+        uint64_t const id = cic_mix64(support_key(sr, sz, stream_key) ^ cic_mix64(k2s[b]) ^ cic_mix64(k3s[b]) ^
+                                      (key1 & 1u));
+        ResampleDraw draw;
+        draw.rng.init(in.rng_seed, id ^ in.salt, static_cast<uint64_t>(in.step));
+        draw.channel = channel;
+        CicThinResult const r = cic_thin_window(sfr + b, sfz + b, sw + b, e - b, request, draw);
+        if (!r.valid || r.removed == 0 || !cic_moments_kept(sfr + b, sfz + b, sw0 + b, sw + b, e - b)) {
+            atomicCAS(status, 0, RREA_GPU_ERR_INVALID_STATE);
+            continue;
+        }
+        atomicAdd(removed_per_inst + k, static_cast<unsigned long long>(r.removed));
+    }
+}
+
+// apply_kernel for the members of instances with a request.
+__global__ void apply_instances_kernel(rrea_launch::PopulationInput in, const uint32_t* __restrict__ perm,
+                                       const int64_t* __restrict__ members, int64_t n,
+                                       const double* __restrict__ sw, const uint64_t* __restrict__ k0s,
+                                       const int64_t* __restrict__ nominal)
+{
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (nominal[k0s[i]] <= 0) continue;
+        int64_t const src = members[perm[i]];
+        double const wn = sw[i];
+        in.w[src] = wn;
+        if (!(wn > 0.0)) in.id[src] = -in.id[src];
+    }
+}
+
 int blocks_for(int64_t n)
 {
     int64_t b = (n + 255) / 256;
@@ -348,6 +492,11 @@ struct PopulationWork {
     size_t cub_bytes = 0;
     int* status = nullptr;
     unsigned long long* removed = nullptr;
+    // ensemble plans: instance keys, per-instance words, group instances
+    uint64_t* k0 = nullptr;
+    int64_t* inst_words = nullptr;
+    uint32_t* ginst = nullptr;
+    int64_t inst_cap = 0, group_cap = 0;
 };
 
 namespace {
@@ -356,7 +505,7 @@ void release(PopulationWork& p)
 {
     void* ptrs[] = {p.flags, p.offsets, p.scan_scratch, p.members, p.k1, p.k2, p.k3, p.ka, p.kb, p.k2s, p.k3s,
                     p.perm_a, p.perm_b, p.fr, p.fz, p.w, p.sfr, p.sfz, p.sw, p.sw0, p.begin, p.capacity,
-                    p.cap_prefix, p.cub_temp, p.status, p.removed};
+                    p.cap_prefix, p.cub_temp, p.status, p.removed, p.k0, p.inst_words, p.ginst};
     for (void* q : ptrs) {
         if (q) cudaFree(q);
     }
@@ -385,6 +534,7 @@ cudaError_t ensure(PopulationWork& p, int64_t n)
     g(&p.k1, cap);
     g(&p.k2, cap);
     g(&p.k3, cap);
+    g(&p.k0, cap);
     g(&p.ka, cap);
     g(&p.kb, cap);
     g(&p.k2s, cap);
@@ -424,14 +574,14 @@ cudaError_t ensure(PopulationWork& p, int64_t n)
 
 // stable sort of (key, perm) pairs of n records by key
 cudaError_t sort_by(PopulationWork& p, uint64_t const* keys_in_member_order, uint32_t*& perm, uint32_t*& perm_spare,
-                    int64_t n, cudaStream_t s)
+                    int64_t n, cudaStream_t s, int end_bit = 64)
 {
     note_launch();
     rrea_dev::gather_u64_kernel<<<rrea_dev::blocks_for(n), 256, 0, s>>>(keys_in_member_order, perm, n, p.ka);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     size_t bytes = p.cub_bytes;
-    e = cub::DeviceRadixSort::SortPairs(p.cub_temp, bytes, p.ka, p.kb, perm, perm_spare, static_cast<int>(n), 0, 64,
+    e = cub::DeviceRadixSort::SortPairs(p.cub_temp, bytes, p.ka, p.kb, perm, perm_spare, static_cast<int>(n), 0, end_bit,
                                         s);
     std::swap(perm, perm_spare);
     return e;
@@ -565,6 +715,173 @@ cudaError_t population_thin(PopulationInput const& in, PopulationWork*& work, Po
     }
     note_launch();
     apply_kernel<<<blocks_for(n), 256, 0, s>>>(in, perm, p.members, counts[0], n, p.sw);
+    return cudaGetLastError();
+}
+
+cudaError_t population_thin_instances(PopulationInput const& in, PopulationWork*& work, PopulationStats& st,
+                                      int64_t* removed_per_instance, cudaStream_t s)
+{
+    using namespace rrea_dev;
+    st = PopulationStats{};
+    uint32_t const n_inst = static_cast<uint32_t>(in.n_inst);
+    for (uint32_t k = 0; k < n_inst; ++k) removed_per_instance[k] = 0;
+    if (n_inst == 0 || in.n_tile == 0) return cudaSuccess;
+    if (!in.cpu || in.n_cand != 0 || in.n_tile > INT32_MAX) {
+        st.status = in.n_tile > INT32_MAX ? RREA_GPU_ERR_CAPACITY : RREA_GPU_ERR_ARGUMENT;
+        return cudaSuccess;
+    }
+    if (!work) work = new PopulationWork{};
+    PopulationWork& p = *work;
+    cudaError_t e = ensure(p, in.n_tile);
+    if (e != cudaSuccess) return e;
+    // per-instance words: members, due target (-1: not due), capacity,
+    // capacity base, request, removals; the group instances
+    if (p.inst_cap < static_cast<int64_t>(n_inst) || p.group_cap < p.cap) {
+        if (p.inst_words) cudaFree(p.inst_words);
+        if (p.ginst) cudaFree(p.ginst);
+        p.inst_words = nullptr;
+        p.ginst = nullptr;
+        p.inst_cap = p.group_cap = 0;
+        if ((e = cudaMalloc(&p.inst_words, sizeof(int64_t) * 6 * static_cast<size_t>(n_inst))) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&p.ginst, sizeof(uint32_t) * static_cast<size_t>(p.cap))) != cudaSuccess) return e;
+        p.inst_cap = n_inst;
+        p.group_cap = p.cap;
+    }
+    auto* const members_k = reinterpret_cast<unsigned long long*>(p.inst_words);
+    int64_t* const due_k = p.inst_words + n_inst;
+    auto* const cap_k = reinterpret_cast<unsigned long long*>(p.inst_words + 2 * n_inst);
+    int64_t* const base_k = p.inst_words + 3 * n_inst;
+    int64_t* const nominal_k = p.inst_words + 4 * n_inst;
+    auto* const removed_k = reinterpret_cast<unsigned long long*>(p.inst_words + 5 * n_inst);
+    if ((e = cudaMemsetAsync(p.inst_words, 0, sizeof(int64_t) * 6 * n_inst, s)) != cudaSuccess) return e;
+    bool const shared_hist = n_inst <= 4096;
+    note_launch();
+    instance_members_kernel<<<blocks_for(in.n_tile), 256, shared_hist ? sizeof(unsigned long long) * n_inst : 0, s>>>(
+        in.id, in.cpu, in.n_tile, n_inst, shared_hist, members_k);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // RreaAdaptiveResampleAction per instance: due strictly above 1.25 x target
+    std::vector<int64_t> members(n_inst), due(n_inst, -1);
+    if ((e = cudaMemcpyAsync(members.data(), members_k, sizeof(int64_t) * n_inst, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s))) {
+        return e;
+    }
+    bool any = false;
+    for (uint32_t k = 0; k < n_inst; ++k) {
+        int64_t const t = in.targets[k];
+        st.live += members[k];
+        if (t > 0 && members[k] > t + t / 4) {
+            due[k] = t;
+            any = true;
+        }
+    }
+    if (!any) return cudaSuccess;
+    if ((e = cudaMemcpyAsync(due_k, due.data(), sizeof(int64_t) * n_inst, cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+        return e;
+    }
+    note_launch();
+    flags_due_kernel<<<blocks_for(in.n_tile), 256, 0, s>>>(in.id, in.cpu, in.n_tile, due_k, n_inst, p.flags);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = exclusive_scan_counts(p.flags, in.n_tile, p.offsets, p.scan_scratch, s)) != cudaSuccess) return e;
+    note_launch();
+    scatter_members_kernel<<<blocks_for(in.n_tile), 256, 0, s>>>(p.flags, p.offsets, in.n_tile, 0, p.members);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    int64_t last_off = 0;
+    uint32_t last_flag = 0;
+    if ((e = cudaMemcpyAsync(&last_off, p.offsets + in.n_tile - 1, sizeof(last_off), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemcpyAsync(&last_flag, p.flags + in.n_tile - 1, sizeof(last_flag), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemsetAsync(p.status, 0, sizeof(int), s)) || (e = cudaStreamSynchronize(s))) {
+        return e;
+    }
+    int64_t const n = last_off + last_flag;
+    st.members = n;
+    note_launch();
+    records_kernel<<<blocks_for(n), 256, 0, s>>>(in, p.members, n, n, p.k1, p.k2, p.k3, p.perm_a, p.fr, p.fz, p.w,
+                                                 p.status, p.k0);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // (instance, support, phase, candidate, identity high, identity low):
+    // four stable passes, least significant first; the instance pass sorts
+    // only the bits an instance number has
+    int inst_bits = 1;
+    while (inst_bits < 32 && (1u << inst_bits) < n_inst) ++inst_bits;
+    uint32_t* perm = p.perm_a;
+    uint32_t* spare = p.perm_b;
+    if ((e = sort_by(p, p.k3, perm, spare, n, s)) != cudaSuccess) return e;
+    if ((e = sort_by(p, p.k2, perm, spare, n, s)) != cudaSuccess) return e;
+    if ((e = sort_by(p, p.k1, perm, spare, n, s)) != cudaSuccess) return e;
+    if ((e = sort_by(p, p.k0, perm, spare, n, s, inst_bits)) != cudaSuccess) return e;
+    // p.kb holds the sorted instances; the sorted k1 into p.ka
+    note_launch();
+    gather_u64_kernel<<<blocks_for(n), 256, 0, s>>>(p.k1, perm, n, p.ka);
+    note_launch();
+    heads_instances_kernel<<<blocks_for(n), 256, 0, s>>>(perm, n, p.kb, p.ka, p.k2, p.k3, p.fr, p.fz, p.w, p.sfr,
+                                                         p.sfz, p.sw, p.sw0, p.k2s, p.k3s, p.flags);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = exclusive_scan_counts(p.flags, n, p.offsets, p.scan_scratch, s)) != cudaSuccess) return e;
+    note_launch();
+    group_begin_kernel<<<blocks_for(n), 256, 0, s>>>(p.flags, p.offsets, n, p.begin);
+    int status = 0;
+    if ((e = cudaGetLastError()) ||
+        (e = cudaMemcpyAsync(&last_off, p.offsets + n - 1, sizeof(last_off), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemcpyAsync(&last_flag, p.flags + n - 1, sizeof(last_flag), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemcpyAsync(&status, p.status, sizeof(status), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s))) {
+        return e;
+    }
+    if (status != 0) {
+        st.status = status;
+        return cudaSuccess;
+    }
+    int64_t const groups = last_off + last_flag;
+    st.supports = groups;
+    note_launch();
+    group_capacity_kernel<<<blocks_for(groups), 256, 0, s>>>(p.begin, groups, n, p.sfr, p.sfz, p.sw, p.capacity);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    size_t bytes = p.cub_bytes;
+    if ((e = cub::DeviceScan::ExclusiveSum(p.cub_temp, bytes, p.capacity, p.cap_prefix, static_cast<int>(groups), s))) {
+        return e;
+    }
+    note_launch();
+    group_instances_kernel<<<blocks_for(groups), 256, 0, s>>>(p.begin, groups, p.kb, p.capacity, p.cap_prefix,
+                                                              p.ginst, cap_k, base_k);
+    note_launch();
+    nominal_kernel<<<blocks_for(n_inst), 256, 0, s>>>(members_k, cap_k, due_k, n_inst, nominal_k);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    std::vector<int64_t> cap(n_inst), nominal(n_inst);
+    if ((e = cudaMemcpyAsync(cap.data(), cap_k, sizeof(int64_t) * n_inst, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemcpyAsync(nominal.data(), nominal_k, sizeof(int64_t) * n_inst, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s))) {
+        return e;
+    }
+    for (uint32_t k = 0; k < n_inst; ++k) {
+        st.capacity += cap[k];
+        st.requested += nominal[k] > 0 ? nominal[k] : 0;
+    }
+    st.floor = n - st.capacity;
+    if (st.requested <= 0) return cudaSuccess;
+    note_launch();
+    group_thin_instances_kernel<<<blocks_for(groups), 64, 0, s>>>(in, p.begin, groups, n, p.ka, p.k2s, p.k3s, p.sfr,
+                                                                  p.sfz, p.sw, p.sw0, p.capacity, p.cap_prefix,
+                                                                  p.ginst, base_k, nominal_k, removed_k, p.status);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    std::vector<int64_t> removed(n_inst);
+    if ((e = cudaMemcpyAsync(removed.data(), removed_k, sizeof(int64_t) * n_inst, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemcpyAsync(&status, p.status, sizeof(status), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s))) {
+        return e;
+    }
+    bool short_plan = false;
+    for (uint32_t k = 0; k < n_inst; ++k) {
+        st.removed += removed[k];
+        short_plan = short_plan || removed[k] < nominal[k];
+    }
+    if (status != 0 || short_plan) {
+        // as population_thin: a rejected or short plan applies nothing
+        st.status = status != 0 ? status : RREA_GPU_ERR_INVALID_STATE;
+        return cudaSuccess;
+    }
+    for (uint32_t k = 0; k < n_inst; ++k) removed_per_instance[k] = removed[k];
+    note_launch();
+    apply_instances_kernel<<<blocks_for(n), 256, 0, s>>>(in, perm, p.members, n, p.sw, p.kb, nominal_k);
     return cudaGetLastError();
 }
 

@@ -78,12 +78,13 @@ class EnsembleRun:
 
     SPECIES = (gpu.SPECIES_ELECTRON, gpu.SPECIES_PHOTON, gpu.SPECIES_POSITRON)
 
-    def __init__(self, instances, capacity=1 << 22, rng_seed=1, only=None, control_every=1,
+    def __init__(self, instances, capacity=1 << 22, rng_seed=1, only=None, control_every=1, one_pass=True,
                  tables=DEFAULT_TABLES, edges=avalanche.SPECTRUM_EDGES_EV, thresholds=avalanche.THRESHOLDS_EV):
         self.instances = list(instances)
         self.active = sorted(range(len(self.instances)) if only is None else only)
         self.edges, self.thresholds = edges, thresholds
         self.control_every = control_every
+        self.one_pass = one_pass
         cfg = workloads.make_config(gpu, CASE, rng_seed=rng_seed)
         self.ctx = ctx = gpu.RreaGpuContext(cfg, capacity)
         ctx.load_tables(tables)
@@ -128,19 +129,35 @@ class EnsembleRun:
         self.step += 1
         ending = [k for k in self.active if self.instances[k].steps == self.step]
         controlled = [k for k in self.active if self.instances[k].target > 0 and k not in ending]
-        if ending or (controlled and self.step % self.control_every == 0):
-            counts = {sp: ctx.ensemble_partition(sp) for sp in self.SPECIES}
-            if self.step % self.control_every == 0:
-                for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON):
-                    for k in controlled:
-                        t = self.instances[k].target
-                        if counts[sp][k] > t + t // 4:
-                            self.thinned += ctx.ensemble_population_thin(sp, k, t, self.step)["removed"]
+        if controlled and self.step % self.control_every == 0:
+            self._control(controlled)
+        if ending:
+            for sp in self.SPECIES:
+                ctx.ensemble_partition(sp)
             for k in ending:
                 self.results[k] = self._census(k)
                 ctx.ensemble_retire(k)
                 self.active.remove(k)
         return per_particle_ms
+
+    def _control(self, controlled):
+        """Population control of the listed instances: one plan over all of
+        them per species, or (one_pass=False) one per instance slice."""
+        ctx = self.ctx
+        if self.one_pass:
+            targets = np.zeros(len(self.instances), dtype=np.int64)
+            for k in controlled:
+                targets[k] = self.instances[k].target
+            for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON):
+                removed, _ = ctx.ensemble_population_thin_all(sp, targets, self.step)
+                self.thinned += int(removed.sum())
+            return
+        for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON):
+            counts = ctx.ensemble_partition(sp)
+            for k in controlled:
+                t = self.instances[k].target
+                if counts[k] > t + t // 4:
+                    self.thinned += ctx.ensemble_population_thin(sp, k, t, self.step)["removed"]
 
     def _census(self, k):
         ctx = self.ctx

@@ -129,7 +129,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_fluid_evaluate_closure", "rrea_gpu_fluid_transport", "rrea_gpu_advance_field_coupled",
     "rrea_gpu_sources_device", "rrea_gpu_advance_field_coupled_from_current", "rrea_gpu_fluid_reductions",
     "rrea_gpu_set_schedule", "rrea_gpu_ensemble_configure", "rrea_gpu_ensemble_partition", "rrea_gpu_ensemble_retire",
-    "rrea_gpu_ensemble_census", "rrea_gpu_ensemble_population_thin",
+    "rrea_gpu_ensemble_census", "rrea_gpu_ensemble_population_thin", "rrea_gpu_ensemble_population_thin_all",
     "rrea_gpu_default_adjoint_config", "rrea_gpu_adjoint_stage", "rrea_gpu_adjoint_forward",
     "rrea_gpu_adjoint_backward", "rrea_gpu_adjoint_final_state",
 )
@@ -258,6 +258,8 @@ def load_library(path=LIB_PATH):
                                              ctypes.c_int32, _D]
     lib.rrea_gpu_ensemble_population_thin.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
                                                       ctypes.c_int32, ctypes.c_uint64, _i64p]
+    lib.rrea_gpu_ensemble_population_thin_all.argtypes = [vp, ctypes.c_int32, _i64p, ctypes.c_int32,
+                                                          ctypes.c_uint64, _i64p, _i64p]
     for name in EXPORTED_SYMBOLS:
         fn = getattr(lib, name)
         if fn.restype is not None and name not in ("rrea_gpu_default_config", "rrea_gpu_last_error",
@@ -628,6 +630,20 @@ class RreaGpuContext:
                                                                int(step), int(salt),
                                                                stats.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
         return dict(zip(self.POPULATION_STATS, stats.tolist()))
+
+    def ensemble_population_thin_all(self, species, targets, step, salt=0):
+        """Population control of every instance in one pass (targets per
+        instance, 0 = none); returns (removed per instance, total stats)."""
+        t = np.ascontiguousarray(targets, dtype=np.int64)
+        if t.size != self.n_instances:
+            raise ValueError("one target per instance")
+        removed = np.zeros(self.n_instances, dtype=np.int64)
+        stats = np.zeros(8, dtype=np.int64)
+        P = ctypes.POINTER(ctypes.c_int64)
+        self._check(self.lib.rrea_gpu_ensemble_population_thin_all(self.handle, int(species), t.ctypes.data_as(P),
+                                                                   int(step), int(salt), removed.ctypes.data_as(P),
+                                                                   stats.ctypes.data_as(P)))
+        return removed, dict(zip(self.POPULATION_STATS, stats.tolist()))
 
     # ---- low-energy carrier fluid ------------------------------------------
     def fluid_configure(self, fluid_config=None, **overrides):

@@ -12,7 +12,9 @@ context of its own (cpu = k).
     weights, in the same order;
   * each instance's census at its end (counts exactly, weight sums and
     spectra within 1e-12: the census sums with atomics) and its thinning
-    totals match;
+    totals match, the batched run thinning every instance in one plan per
+    species (rrea_gpu_ensemble_population_thin_all) and the instance alone
+    thinning its slice (rrea_gpu_ensemble_population_thin);
   * the autotuner's launch shapes and scheduling orders change no result."""
 import numpy as np
 import pytest
@@ -88,11 +90,33 @@ def test_census_at_each_end_matches_the_instances_alone(mods):
     gpu, workloads, ensemble = mods
     inst = _instances(ensemble)
     batched = ensemble.run_batched(inst, capacity=1 << 18, autotune=False, tables=TABLES)
-    seq = ensemble.run_sequential(inst, capacity=1 << 18, tables=TABLES)
+    seq = ensemble.run_sequential(inst, capacity=1 << 18, tables=TABLES, one_pass=False)
     _compare(batched["results"], seq["results"])
     assert batched["thinned"] == seq["thinned"] > 0
     assert batched["steps"] == max(i.steps for i in inst)
     assert batched["particle_steps"] == seq["particle_steps"]
+
+
+def test_one_pass_control_is_the_slice_control(mods):
+    """Both control paths on the same batched state: tiles equal bit for bit
+    after 30 steps with control every 5 steps."""
+    gpu, workloads, ensemble = mods
+    inst = _instances(ensemble)
+    inst[0].target = 70
+    tiles = []
+    for one_pass in (True, False):
+        run = ensemble.EnsembleRun(inst, capacity=1 << 18, tables=TABLES, control_every=5, one_pass=one_pass)
+        for _ in range(30):
+            run.advance()
+        tiles.append((_tiles(run, gpu, workloads), run.thinned))
+        run.close()
+    (a, ta), (b, tb) = tiles
+    assert ta == tb > 0
+    for k in range(len(inst)):
+        for sp in a:
+            x, y = _instance_rows(a[sp], k), _instance_rows(b[sp], k)
+            for key in x:
+                np.testing.assert_array_equal(x[key], y[key], err_msg=f"instance {k} species {sp} {key}")
 
 
 def test_autotune_changes_no_result(mods):
