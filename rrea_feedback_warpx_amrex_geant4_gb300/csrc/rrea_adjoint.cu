@@ -103,10 +103,17 @@ __device__ __forceinline__ double drag_power(Params const& p, const double* __re
         if (!bracket_hot(arena, *h, k, b, err)) continue;
         double const v = eval_hot(arena, *h, b, err);
         total += v;
-        if (b.kind == 3 && v > 0.0) {
+        if (b.kind != 3) continue;   // constant beyond the grid (a node itself has measure zero)
+        // d/dK in the table's mode: log-log between positive nodes, linear
+        // in the log-energy fraction otherwise (the zero-threshold rule)
+        const double* y = arena + h->y;
+        double const ylo = __ldg(y + b.hi - 1), yhi = __ldg(y + b.hi);
+        double const ilx = __ldg(arena + h->ilx + b.hi);
+        if (h->mode == RREA_INTERP_LOGLOG || (ylo > 0.0 && yhi > 0.0)) {
             const double* ly = arena + h->ly;
-            double const slope_log = (__ldg(ly + b.hi) - __ldg(ly + b.hi - 1)) * __ldg(arena + h->ilx + b.hi);
-            dk += v * slope_log / k;
+            dk += v * (__ldg(ly + b.hi) - __ldg(ly + b.hi - 1)) * ilx / k;
+        } else {
+            dk += (yhi - ylo) * ilx / k;
         }
     }
     dk *= p.rho;

@@ -2719,7 +2719,7 @@ rrea_gpu_status rrea_gpu_adjoint_stage(rrea_gpu_ctx* ctx, const rrea_gpu_adjoint
     }
     RreaArenaIndex const& ix = ctx->tables.index();
     for (int t : {RREA_T_E_COLLISION, RREA_T_E_SOFT_RAD}) {
-        if (ix.hot[t].mode != RREA_INTERP_LOGLOG) {
+        if (ix.hot[t].mode != RREA_INTERP_LOGLOG && ix.hot[t].mode != RREA_INTERP_LOGLOG_ZERO_THRESHOLD) {
             return fail(ctx, RREA_GPU_ERR_TABLES, "the adjoint's stopping powers must be log-log tables");
         }
     }

@@ -794,6 +794,7 @@ cudaError_t population_thin_instances(PopulationInput const& in, PopulationWork*
     }
     int64_t const n = last_off + last_flag;
     st.members = n;
+    if (n == 0) return cudaSuccess;
     note_launch();
     records_kernel<<<blocks_for(n), 256, 0, s>>>(in, p.members, n, n, p.k1, p.k2, p.k3, p.perm_a, p.fr, p.fz, p.w,
                                                  p.status, p.k0);

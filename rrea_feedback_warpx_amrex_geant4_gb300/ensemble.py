@@ -44,9 +44,10 @@ class Instance:
     target: int = 0        # per-species population target of the thinning (0: none)
 
 
-def config3_instances(n=64, seed=7, duration_scale=1.0, target=20_000):
+def config3_instances(n=64, seed=7, duration_scale=1.0, target=0):
     """The batched configuration: n instances; durations scaled by
-    duration_scale (1 = 0.5-4 us)."""
+    duration_scale (1 = 0.5-4 us); target > 0 adds a per-instance population
+    control (the configuration itself has none)."""
     e = np.linspace(3.0e5, 1.0e6, n)
     rng = np.random.default_rng(seed)
     seeds = np.exp(rng.uniform(np.log(1.0e3), np.log(1.0e5), n)).astype(np.int64)
@@ -226,7 +227,7 @@ def main():
     p = argparse.ArgumentParser(description="batched ensemble of uniform-field avalanches")
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--duration-scale", type=float, default=1.0)
-    p.add_argument("--target", type=int, default=20_000)
+    p.add_argument("--target", type=int, default=0, help="per-instance population target (0: no control)")
     p.add_argument("--control-every", type=int, default=16, help="steps between population-control checks")
     p.add_argument("--sequential", action="store_true", help="also run the instances one by one")
     p.add_argument("--json", default=None)
