@@ -203,9 +203,9 @@ rrea_gpu_status rrea_gpu_download_current_index(rrea_gpu_ctx* ctx, double* rho, 
  * RreaMaxwellTMRZ.H:147-228): the accumulated net-chord current is converted
  * to physical Jr/Jz and drives `substeps` equal leapfrog substeps of the
  * scattered TM field (B restaggered by (dt - dt_sub)/2 before and after,
- * first-order Silver-Mueller on the open faces).  The carrier-fluid current
- * and conductivity are not included (no fluid model in this library).  The
- * cell fields the transport gathers are refreshed afterwards.  Refuses a
+ * first-order Silver-Mueller on the open faces).  The kinetic current alone:
+ * with the carrier fluid, rrea_gpu_advance_field_coupled runs the step with
+ * the fluid's current and conductivity instead.  The cell fields the transport gathers are refreshed afterwards.  Refuses a
  * step violating c dt sqrt(dr^-2 + dz^-2) < 1, and periodic z.
  */
 rrea_gpu_status rrea_gpu_advance_field(rrea_gpu_ctx* ctx, double dt_s, int32_t substeps);
