@@ -109,6 +109,29 @@ rrea_gpu_status rrea_gpu_set_density_profile(rrea_gpu_ctx* ctx, const double* al
                                              double altitude_msl_at_z0_m,
                                              double reference_density_kg_m3);
 
+/*
+ * Plane-crossing diagnostic (rrea.cd_plane_z_m; RreaPlaneFluxState and
+ * RreaPlaneFluxAccumulator, I/RreaPlaneFlux.H; the crossings of
+ * defer_cd_electron_plane_crossings, O/RreaTransportStep.H:249-332, taken
+ * by the electron phase and the electrons' newborn legs).  Every electron
+ * continuous-loss segment adds its weight to each plane it crosses
+ * (upward z0 < plane <= z1, downward z1 < plane <= z0), per direction, in
+ * three selections: all tracked, local runaway (|E| at the crossing above
+ * the ensemble mean drag at the crossing energy), and >= 1 MeV; the local
+ * runaways also add w r and w r^2.  The accumulators are cumulative on the
+ * device (atomics), 10 per plane in RreaPlaneFluxAccumulator::Flatten's
+ * order: all up/down, local-runaway up/down, >= 1 MeV up/down, w r up/down,
+ * w r^2 up/down.
+ *
+ * set_planes: n_planes strictly increasing finite z (0 turns it off; not in
+ * ensemble mode); the accumulators start at zero.  plane_flux copies them
+ * out (10 n_planes doubles).  restore_plane_flux sets them (RestoreFlat:
+ * finite and nonnegative), NULL zeroes them.
+ */
+rrea_gpu_status rrea_gpu_set_planes(rrea_gpu_ctx* ctx, const double* plane_z, int32_t n_planes);
+rrea_gpu_status rrea_gpu_plane_flux(rrea_gpu_ctx* ctx, double* values);
+rrea_gpu_status rrea_gpu_restore_plane_flux(rrea_gpu_ctx* ctx, const double* values);
+
 /* Sets the Maxwell (scattered) field and the static ambient field on the
  * replicated TM-RZ vectors (I/RreaMaxwellTMRZ.H:61-85): er (nr+1)*nz,
  * ez nr*(nz+1), btheta (nr+1)*(nz+1); amb_er/amb_ez as er/ez.  Host pointers. */
@@ -848,9 +871,13 @@ rrea_gpu_status rrea_gpu_ensemble_population_thin_all(rrea_gpu_ctx* ctx, int32_t
  * stage: the seeds (host arrays: z, direction xyz (3n, normalised here),
  *   kinetic energy, weight, id); needs the tables loaded.
  * forward: the loss for the node values at e_nodes_device (DEVICE pointer,
- *   n_nodes doubles).
- * backward: d loss / d E_k into grad_device (DEVICE pointer) for the same
- *   nodes; run after a forward with the same nodes.
+ *   n_nodes doubles); records where every particle ended (stopped in the
+ *   drag, or below the cutoff after a kick).
+ * forward_frozen: the same with every particle ending exactly where the
+ *   last forward ended it, whatever the new nodes: the frozen-topology loss
+ *   that backward differentiates (finite differences compare against it).
+ * backward: d loss / d E_k into grad_device (DEVICE pointer) for the nodes
+ *   of the last forward (run after it, with the same nodes).
  * final_state: z, dx, dy, dz, K, alive (6 x n host doubles) of the forward.
  */
 typedef struct {
@@ -876,6 +903,7 @@ rrea_gpu_status rrea_gpu_adjoint_stage(rrea_gpu_ctx* ctx, const rrea_gpu_adjoint
                                        const double* z, const double* dir3, const double* kinetic_eV,
                                        const double* weight, const uint64_t* id);
 rrea_gpu_status rrea_gpu_adjoint_forward(rrea_gpu_ctx* ctx, const double* e_nodes_device, double* loss);
+rrea_gpu_status rrea_gpu_adjoint_forward_frozen(rrea_gpu_ctx* ctx, const double* e_nodes_device, double* loss);
 rrea_gpu_status rrea_gpu_adjoint_backward(rrea_gpu_ctx* ctx, const double* e_nodes_device, double* grad_device);
 rrea_gpu_status rrea_gpu_adjoint_final_state(rrea_gpu_ctx* ctx, double* state6);
 

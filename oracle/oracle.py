@@ -92,6 +92,13 @@ def lib():
         _lib.oracle_cell_sources.argtypes = [d]
         _lib.oracle_set_density_profile.argtypes = [d, d, ctypes.c_int64, ctypes.c_double, ctypes.c_double]
         _lib.oracle_density_query.argtypes = [ctypes.c_int, d, ctypes.c_int64, ctypes.c_double, d]
+        _lib.oracle_set_planes.argtypes = [d, ctypes.c_int64]
+        _lib.oracle_plane_flux.argtypes = [d]
+        _lib.oracle_plane_enumerate.argtypes = [d, ctypes.c_int64, d, ctypes.c_int64, ctypes.c_int64, d,
+                                                ctypes.POINTER(ctypes.c_int64)]
+        _lib.oracle_plane_enumerate.restype = None
+        _lib.oracle_plane_accumulate.argtypes = [d, ctypes.c_int64, ctypes.c_int64, d, ctypes.POINTER(ctypes.c_int32)]
+        _lib.oracle_plane_accumulate.restype = None
     return _lib
 
 
@@ -121,6 +128,48 @@ def load_tables(path):
         return
     _check(lib().oracle_load_tables(path.encode()))
     _loaded_path = path
+
+
+_planes = 0
+
+
+def set_planes(plane_z_m=()):
+    """The plane-crossing diagnostic's planes (empty: off)."""
+    global _planes
+    z = np.ascontiguousarray(plane_z_m, dtype=np.float64)
+    _check(lib().oracle_set_planes(z.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), z.size))
+    _planes = int(z.size)
+
+
+def plane_flux():
+    """The last step's (or drain's) crossings accumulated from zero: (n_planes, 10)."""
+    out = np.zeros((_planes, 10))
+    _check(lib().oracle_plane_flux(out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return out
+
+
+def plane_enumerate(segments, planes, cap=64):
+    """RreaForEachNonperiodicPlaneCrossing over rows (z0, z1): a list of
+    (plane, fraction, direction) arrays, None where the geometry is invalid."""
+    seg = np.ascontiguousarray(segments, dtype=np.float64).reshape(-1, 2)
+    pl = np.ascontiguousarray(planes, dtype=np.float64)
+    out = np.zeros((len(seg), cap, 3))
+    counts = np.zeros(len(seg), dtype=np.int64)
+    lib().oracle_plane_enumerate(seg.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(seg), pl.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), pl.size, cap,
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    return [None if c < 0 else out[i, :c] for i, c in enumerate(counts)]
+
+
+def plane_accumulate(rows, n_planes):
+    """Crossing rows (plane, direction, weight, r, local, mev) added one by
+    one (an invalid one is refused and changes nothing): (ok flags, bins)."""
+    r = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 6)
+    out = np.zeros((n_planes, 10))
+    ok = np.zeros(len(r), dtype=np.int32)
+    lib().oracle_plane_accumulate(r.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(r), n_planes,
+                                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  ok.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    return ok, out
 
 
 def set_density_profile(altitude_m=None, density_kg_m3=None, altitude_msl_at_z0_m=0.0,

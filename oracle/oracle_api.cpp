@@ -5,6 +5,7 @@
 #include "interleave_scenarios.hpp"
 #include "fluid.hpp"
 
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -439,6 +440,64 @@ void oracle_diagnostics(uint64_t* subcycles, uint64_t* events, int32_t* disposit
         events[i] = g_out.events[i];
         disposition[i] = g_out.disposition[i];
     }
+}
+
+int oracle_set_planes(double const* z, int64_t n)
+{
+    std::vector<double> planes(z, z + n);
+    for (int64_t i = 0; i < n; ++i) {
+        if (!std::isfinite(z[i]) || (i > 0 && !(z[i] > z[i - 1]))) return RREA_GPU_ERR_ARGUMENT;
+    }
+    oracle::SetPlanes(std::move(planes));
+    return 0;
+}
+
+// The last step's (or drain's) plane crossings accumulated from zero, 10 per plane.
+int oracle_plane_flux(double* out)
+{
+    std::vector<double> bins(oracle::Planes().size() * 10U, 0.0);
+    if (!oracle::AccumulatePlaneCrossings(g_out.crossings, bins)) return RREA_GPU_ERR_INVALID_STATE;
+    std::memcpy(out, bins.data(), bins.size() * sizeof(double));
+    return 0;
+}
+
+// Crossing enumeration of segments (z0, z1) over the given planes: per
+// segment up to `cap` (plane, fraction, direction) triples; counts[i] the
+// number (-1 on invalid geometry).
+void oracle_plane_enumerate(double const* segs, int64_t n, double const* planes, int64_t n_planes, int64_t cap,
+                            double* out, int64_t* counts)
+{
+    std::vector<double> pl(planes, planes + n_planes);
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t c = 0;
+        bool const ok = oracle::ForEachPlaneCrossing(segs[2 * i], segs[2 * i + 1], pl,
+                                                     [&](std::size_t p, double f, int d) {
+                                                         if (c < cap) {
+                                                             out[(i * cap + c) * 3 + 0] = static_cast<double>(p);
+                                                             out[(i * cap + c) * 3 + 1] = f;
+                                                             out[(i * cap + c) * 3 + 2] = d;
+                                                         }
+                                                         ++c;
+                                                     });
+        counts[i] = ok ? c : -1;
+    }
+}
+
+// Crossings (plane, direction, weight, r, local, mev) added one by one as
+// RreaPlaneFluxAccumulator::AddCrossing adds them: an invalid one changes
+// nothing and gets ok = 0.  out: n_planes x 10 values.
+void oracle_plane_accumulate(double const* rows, int64_t n, int64_t n_planes, double* out, int32_t* ok)
+{
+    std::vector<double> bins(static_cast<std::size_t>(n_planes) * 10U, 0.0);
+    for (int64_t i = 0; i < n; ++i) {
+        double const* r = rows + 6 * i;
+        std::vector<oracle::PlaneCrossing> one{oracle::PlaneCrossing{static_cast<int>(r[0]), static_cast<int>(r[1]),
+                                                                     r[2], r[3], r[4] != 0.0, r[5] != 0.0}};
+        std::vector<double> trial = bins;
+        ok[i] = oracle::AccumulatePlaneCrossings(one, trial) ? 1 : 0;
+        if (ok[i]) bins.swap(trial);
+    }
+    std::memcpy(out, bins.data(), bins.size() * sizeof(double));
 }
 
 void oracle_cell_sources(double* out5)

@@ -1536,6 +1536,77 @@ AnnihilationState sample_annihilation(Tables const& t, double k, double d_energy
 // Electron phase: O/RreaElectronTransport.cpp:9-902 (+ O/RreaTransportStep.H
 // prologue/escape/writeback :720-905)
 // ======================================================================
+namespace {
+std::vector<double> g_planes;
+}  // namespace
+
+void SetPlanes(std::vector<double> planes) { g_planes = std::move(planes); }
+std::vector<double> const& Planes() { return g_planes; }
+
+bool AccumulatePlaneCrossings(std::vector<PlaneCrossing> const& crossings, std::vector<double>& bins)
+{
+    for (PlaneCrossing const& c : crossings) {
+        std::size_t const base = static_cast<std::size_t>(c.plane) * 10U;
+        if (c.plane < 0 || base + 10U > bins.size() || (c.direction != 1 && c.direction != -1)
+            || !std::isfinite(c.weight) || !(c.weight >= 0.0) || !std::isfinite(c.r) || !(c.r >= 0.0)) {
+            return false;
+        }
+        std::size_t const d = c.direction > 0 ? 0U : 1U;
+        bins[base + d] += c.weight;
+        if (c.local_runaway) bins[base + 2U + d] += c.weight;
+        if (c.at_least_one_mev) bins[base + 4U + d] += c.weight;
+        if (c.local_runaway) {
+            bins[base + 6U + d] += c.weight * c.r;
+            bins[base + 8U + d] += c.weight * c.r * c.r;
+        }
+    }
+    return true;
+}
+
+namespace {
+
+// defer_cd_electron_plane_crossings (O/RreaTransportStep.H:249-332) for one
+// electron continuous segment [b, eff].
+void defer_plane_crossings(Tables const& tables, rrea_gpu_config const& cfg, Gather const& gather, Path const& path,
+                           std::vector<Interval> const& iv, double b, double eff, double weight, double k_before,
+                           double stopping_energy, double drag, bool hm_enabled, std::vector<PlaneCrossing>& out)
+{
+    if (g_planes.empty() || !(eff > b)) return;
+    double bx, by, bz, ex, ey, ez;
+    path.PointAtFull(b, bx, by, bz);
+    path.PointAtFull(eff, ex, ey, ez);
+    // electron_realized_continuous_loss_ev_per_m at the frozen energy, STP
+    double const fixed_stp = tables.ElectronCollisionLoss(stopping_energy, 1.0)
+        + tables.ElectronSoftRadiativeDrag(stopping_energy, 1.0);
+    double const cut = cfg.low_energy_cutoff_eV;
+    bool const valid = ForEachPlaneCrossing(bz, ez, g_planes, [&](std::size_t i, double sf, int direction) {
+        double const f = b + sf * (eff - b);
+        double x, y, z;
+        path.PointAtFull(f, x, y, z);
+        double const r = std::hypot(x, y);
+        double const raw = fixed_stp * density_path(iv, path, b, f);
+        double const kc = std::max(0.0, k_before - std::min(drag, raw));
+        bool local = false;
+        if (kc >= cut) {
+            double const rho = positive_or(DensityRatioAtZ(cfg.density_ratio, z), 1.0);
+            double fer, fez, fbt;
+            gather.at(r, z, fer, fez, fbt);
+            double mean_drag = 0.0;
+            if (kc > 0.0 && rho > 0.0) {
+                double const hard = hm_enabled ? tables.ElectronHardMollerEnergyLoss(kc, rho) : 0.0;
+                mean_drag = (tables.ElectronCollisionLoss(kc, rho) + tables.ElectronSoftRadiativeDrag(kc, rho)) + hard
+                    + tables.ElectronTrackedBremsEnergyLoss(kc, rho);
+            }
+            double const magnitude = std::hypot(fer, fez);
+            local = std::isfinite(magnitude) && std::isfinite(mean_drag) && mean_drag >= 0.0 && magnitude > mean_drag;
+        }
+        out.push_back(PlaneCrossing{static_cast<int>(i), direction, weight, r, local, kc >= 1.0e6});
+    });
+    if (!valid) fail(RREA_GPU_ERR_GEOMETRY, "plane crossing enumeration received invalid geometry");
+}
+
+}  // namespace
+
 void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, FieldGrid const& field, int step,
                             double dt_s, ChargedTile& tile, StepOutputs& out)
 {
@@ -1804,6 +1875,8 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
                     push_source(0, std::hypot(x, y), z, pw, 0.5 * cutoff, w_air);
                 }
             }
+            defer_plane_crossings(tables, cfg, gather, path, iv, b, plan.end, weight, k, stop_e, plan.drag, hm_enabled,
+                                  cout.crossings);
             k = std::max(0.0, k - plan.drag);
             if (plan.reaches) k = cutoff;
             return Limit{plan.end, plan.reaches, true};
@@ -2024,6 +2097,7 @@ void ApplyElectronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
         out.secondaries.insert(out.secondaries.end(), c.secondaries.begin(), c.secondaries.end());
         out.sources.insert(out.sources.end(), c.sources.begin(), c.sources.end());
         out.segments.insert(out.segments.end(), c.segments.begin(), c.segments.end());
+        out.crossings.insert(out.crossings.end(), c.crossings.begin(), c.crossings.end());
     }
 }
 
@@ -2543,6 +2617,7 @@ void ApplyPositronTransport(TableSet const& ts, rrea_gpu_config const& cfg, Fiel
         out.secondaries.insert(out.secondaries.end(), c.secondaries.begin(), c.secondaries.end());
         out.sources.insert(out.sources.end(), c.sources.begin(), c.sources.end());
         out.segments.insert(out.segments.end(), c.segments.begin(), c.segments.end());
+        out.crossings.insert(out.crossings.end(), c.crossings.begin(), c.crossings.end());
     }
 }
 
@@ -2557,6 +2632,7 @@ struct NewbornEffects {
     std::vector<Secondary> children;  // root and lineage are assigned at the FIFO merge
     std::vector<Source> sources;
     std::vector<Segment> segments;
+    std::vector<PlaneCrossing> crossings;
 };
 
 struct NewbornContext {
@@ -2847,6 +2923,10 @@ bool advance_charged_newborn(NewbornContext const& c, Secondary& p, NewbornEffec
                 }
                 push_source(0, sr, sz, pw, pos ? 0.0 : 0.5 * cut, w_air);
             }
+        }
+        if (!pos) {
+            defer_plane_crossings(tables, cfg, c.gather, path, iv, b, plan.end, w, k, stop_e, plan.drag, hm_enabled,
+                                  fx.crossings);
         }
         k = std::max(0.0, k - plan.drag);
         if (plan.reaches) k = cut;
@@ -3318,6 +3398,7 @@ void DrainSecondaries(TableSet const& ts, rrea_gpu_config const& cfg, FieldGrid 
                 work.push_back(ch);
             }
             out.sources.insert(out.sources.end(), fx[i].sources.begin(), fx[i].sources.end());
+            out.crossings.insert(out.crossings.end(), fx[i].crossings.begin(), fx[i].crossings.end());
             out.segments.insert(out.segments.end(), fx[i].segments.begin(), fx[i].segments.end());
             if (alive[i]) {
                 Secondary s = work[cursor + i];

@@ -133,10 +133,19 @@ struct Segment {
     int64_t parent_index;
 };
 
+// One deferred plane crossing (RreaPlaneFluxCrossing, I/RreaPlaneFlux.H:48-55).
+struct PlaneCrossing {
+    int plane;
+    int direction;  // +1 up, -1 down
+    double weight, r;
+    bool local_runaway, at_least_one_mev;
+};
+
 struct StepOutputs {
     std::vector<Secondary> secondaries;
     std::vector<Source> sources;
     std::vector<Segment> segments;
+    std::vector<PlaneCrossing> crossings;
     // per-particle diagnostics for parity: substeps used, events drawn
     std::vector<uint64_t> subcycles;
     std::vector<uint64_t> events;
@@ -146,6 +155,7 @@ struct StepOutputs {
         secondaries.clear();
         sources.clear();
         segments.clear();
+        crossings.clear();
         subcycles.clear();
         events.clear();
         disposition.clear();
@@ -285,6 +295,40 @@ bool PhotonFlowValid(int kind, double w, double inc, double x1, double x2, doubl
 
 // Primitive-level evaluation for fixture comparisons (ids listed in oracle_core.cpp).
 int RunPrimitive(rrea_host::TableSet const& tables, int which, double const* in, int64_t n, double* out);
+
+// The plane-crossing diagnostic's planes (empty: off); strictly increasing.
+void SetPlanes(std::vector<double> planes);
+std::vector<double> const& Planes();
+
+// RreaForEachNonperiodicPlaneCrossing (I/RreaPlaneFlux.H:79-118): calls
+// cb(plane index, segment fraction, direction) for every plane in (z0, z1]
+// (upward) or (z1, z0] (downward), in crossing order; false on a non-finite
+// end or planes that are not strictly increasing.
+template <class F>
+bool ForEachPlaneCrossing(double z0, double z1, std::vector<double> const& planes, F&& cb)
+{
+    if (!std::isfinite(z0) || !std::isfinite(z1)) return false;
+    for (std::size_t i = 0; i < planes.size(); ++i) {
+        if (!std::isfinite(planes[i]) || (i > 0 && !(planes[i] > planes[i - 1]))) return false;
+    }
+    if (z1 == z0) return true;
+    double const inverse_span = 1.0 / (z1 - z0);
+    std::size_t const first =
+        static_cast<std::size_t>(std::upper_bound(planes.begin(), planes.end(), std::min(z0, z1)) - planes.begin());
+    std::size_t const last =
+        static_cast<std::size_t>(std::upper_bound(planes.begin(), planes.end(), std::max(z0, z1)) - planes.begin());
+    if (z1 > z0) {
+        for (std::size_t i = first; i < last; ++i) cb(i, (planes[i] - z0) * inverse_span, 1);
+    } else {
+        for (std::size_t j = last; j > first; --j) cb(j - 1, (planes[j - 1] - z0) * inverse_span, -1);
+    }
+    return true;
+}
+
+// RreaPlaneFluxAccumulator::AddCrossing (I/RreaPlaneFlux.H:193-283) over the
+// crossings in order, into 10 values per plane in Flatten's order; false
+// (bins unchanged from the failing crossing on) on an invalid crossing.
+bool AccumulatePlaneCrossings(std::vector<PlaneCrossing> const& crossings, std::vector<double>& bins);
 
 // O/RreaCouplingSources.cpp:435-512 + S/RreaEventAccumulator.cpp:386-502
 void DepositSources(rrea_gpu_config const& cfg, std::vector<Source> const& sources,

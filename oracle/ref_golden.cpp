@@ -14,6 +14,7 @@
 #include "rrea/RreaInteractionTables.H"
 #include "rrea/RreaConstants.H"
 #include "rrea/RreaMaxwellTMRZ.H"
+#include "rrea/RreaPlaneFlux.H"
 #include "rrea/RreaSeedSchedule.H"
 #include "rrea/RreaSegmentDepositionRZ.H"
 #include "rrea/RreaTransportPath.H"
@@ -23,6 +24,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <limits>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -702,6 +704,57 @@ int main(int argc, char** argv)
             write_f8("ref_cic_charge_rho", 1, grid.rho);
             write_f8("ref_cic_charge_grid", 6, {static_cast<double>(grid.nr), static_cast<double>(grid.nz), grid.dr,
                                                  grid.dz, grid.r_lo, grid.z_lo});
+        }
+
+        // ---- plane-crossing diagnostic (I/RreaPlaneFlux.H): the crossing
+        //      enumeration of RreaForEachNonperiodicPlaneCrossing over seeded
+        //      segments (ends on planes, reversals, zero length, a non-finite
+        //      end) and RreaPlaneFluxAccumulator::AddCrossing / Flatten over a
+        //      crossing batch that ends with invalid crossings
+        {
+            Gen g(20261204ULL);   // its own stream: the vectors after this block keep theirs
+            std::vector<amrex::Real> const planes{-3.0, 0.0, 1.5, 2.0, 4.25, 10.0, 10.5, 30.0};
+            std::vector<double> segs, rows;
+            for (int i = 0; i < 600; ++i) {
+                double z0 = -8.0 + 44.0 * g.uni();
+                double z1 = z0 + (g.uni() < 0.5 ? -1.0 : 1.0) * 25.0 * g.uni() * g.uni();
+                uint64_t const kind = g.next() % 10;
+                if (kind == 0) z0 = planes[g.next() % planes.size()];
+                if (kind == 1) z1 = planes[g.next() % planes.size()];
+                if (kind == 2) z1 = z0;
+                if (kind == 3 && i % 7 == 0) z1 = std::numeric_limits<double>::infinity();
+                int count = 0;
+                bool const ok = rrea::RreaForEachNonperiodicPlaneCrossing(
+                    z0, z1, planes, [&](std::size_t p, amrex::Real, amrex::Real f, int d) {
+                        rows.insert(rows.end(), {static_cast<double>(i), static_cast<double>(p), f,
+                                                 static_cast<double>(d)});
+                        ++count;
+                    });
+                segs.insert(segs.end(), {z0, z1, ok ? static_cast<double>(count) : -1.0});
+            }
+            write_f8("ref_plane_segments", 3, segs);
+            write_f8("ref_plane_crossings", 4, rows);
+            write_f8("ref_plane_planes", 1, std::vector<double>(planes.begin(), planes.end()));
+            rrea::RreaPlaneFluxAccumulator acc(planes.size());
+            std::vector<double> batch, status;
+            for (int i = 0; i < 400; ++i) {
+                double const p = static_cast<double>(g.next() % planes.size());
+                double const d = (g.next() & 1) ? 1.0 : -1.0;
+                double w = 0.1 + 5.0 * g.uni();
+                double r = 40.0 * g.uni();
+                if (i == 397) w = -1.0;                   // invalid weight
+                if (i == 398) r = std::nan("");           // invalid radius
+                double const local = (g.next() % 3 == 0) ? 1.0 : 0.0;
+                double const mev = (g.next() % 2 == 0) ? 1.0 : 0.0;
+                batch.insert(batch.end(), {p, d, w, r, local, mev});
+                bool const ok = acc.AddCrossing(static_cast<std::size_t>(p), static_cast<int>(d), w, r, local != 0.0,
+                                                mev != 0.0);
+                status.push_back(ok ? 1.0 : 0.0);
+            }
+            write_f8("ref_plane_batch", 6, batch);
+            write_f8("ref_plane_batch_ok", 1, status);
+            auto const flat = acc.Flatten();
+            write_f8("ref_plane_flux", 10, std::vector<double>(flat.begin(), flat.end()));
         }
 
         // ---- adaptive_resample_v1 global thinning on one rank: the plan of

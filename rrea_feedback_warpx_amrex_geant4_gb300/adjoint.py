@@ -49,10 +49,11 @@ def _lib():
         lib.rrea_gpu_adjoint_stage.argtypes = [vp, ctypes.POINTER(AdjointConfig), ctypes.c_int64, d, d, d, d,
                                                ctypes.POINTER(ctypes.c_uint64)]
         lib.rrea_gpu_adjoint_forward.argtypes = [vp, vp, d]
+        lib.rrea_gpu_adjoint_forward_frozen.argtypes = [vp, vp, d]
         lib.rrea_gpu_adjoint_backward.argtypes = [vp, vp, vp]
         lib.rrea_gpu_adjoint_final_state.argtypes = [vp, d]
-        for name in ("rrea_gpu_adjoint_stage", "rrea_gpu_adjoint_forward", "rrea_gpu_adjoint_backward",
-                     "rrea_gpu_adjoint_final_state"):
+        for name in ("rrea_gpu_adjoint_stage", "rrea_gpu_adjoint_forward", "rrea_gpu_adjoint_forward_frozen",
+                     "rrea_gpu_adjoint_backward", "rrea_gpu_adjoint_final_state"):
             getattr(lib, name).restype = ctypes.c_int
         _bound = True
     return lib
@@ -112,13 +113,15 @@ class PushAdjoint:
         if self.own:
             self.ctx.close()
 
-    def forward(self, e_nodes):
-        """Loss for a CUDA float64 tensor of node values."""
+    def forward(self, e_nodes, frozen=False):
+        """Loss for a CUDA float64 tensor of node values.  frozen=True ends
+        every particle where the last plain forward ended it (the topology
+        the adjoint differentiates); a plain forward records the ends."""
         import torch
         torch.cuda.synchronize()
         loss = ctypes.c_double()
-        self.ctx._check(self.lib.rrea_gpu_adjoint_forward(self.ctx.handle, ctypes.c_void_p(e_nodes.data_ptr()),
-                                                          ctypes.byref(loss)))
+        fn = self.lib.rrea_gpu_adjoint_forward_frozen if frozen else self.lib.rrea_gpu_adjoint_forward
+        self.ctx._check(fn(self.ctx.handle, ctypes.c_void_p(e_nodes.data_ptr()), ctypes.byref(loss)))
         return loss.value
 
     def backward(self, e_nodes):
@@ -160,15 +163,16 @@ def field_loss_function():
 
 def central_differences(problem, e_nodes, nodes, h=1.0):
     """Central finite differences of the loss at the listed nodes with the
-    same frozen streams (common random numbers), step h [V/m]."""
-    import torch
+    same streams (common random numbers) and the topology frozen at the
+    nodes' run (every particle ends where it ended there), step h [V/m]."""
     out = []
+    problem.forward(e_nodes)          # records the ends
     for k in nodes:
         e = e_nodes.clone()
         e[k] += h
-        up = problem.forward(e)
+        up = problem.forward(e, frozen=True)
         e[k] -= 2.0 * h
-        down = problem.forward(e)
+        down = problem.forward(e, frozen=True)
         out.append((up - down) / (2.0 * h))
         del e
     problem.forward(e_nodes)

@@ -149,10 +149,12 @@ class AvalancheRun:
         self.step += 1
         return moved, drained
 
-    def run(self, steps, census_every=100, dt_s=DT_S):
+    def run(self, steps, census_every=100, dt_s=DT_S, plane_csv=None):
         """Advances `steps` steps; returns a result dict with the census
         history, the final spectra, the multiplication factor and the
-        device-side throughput."""
+        device-side throughput.  plane_csv (a PlaneFluxCsv over the planes
+        set on the context) writes the plane rows on its cadence and once
+        more, forced, after the last step."""
         history = []
         moved_total = 0
         fifo_total = 0
@@ -164,6 +166,8 @@ class AvalancheRun:
             moved, drained = self.advance(dt_s)
             moved_total += moved
             fifo_total += drained[0]
+            if plane_csv is not None:
+                plane_csv.maybe_write(self.ctx, self.step, self.step * dt_s, force=k + 1 == steps)
             if (k + 1) % census_every == 0 or k + 1 == steps:
                 row, spectra = census_row(self.ctx, self.step)
                 row["particle_steps"] = moved_total
@@ -231,6 +235,121 @@ def write_reduced_csv(path, history):
                 w.writerow([h[k] for _, k in columns])
 
 
+class PlaneFluxCsv:
+    """rrea_cd_plane_flux.csv of RreaWarpXCoupling::MaybeWriteCdPlaneFlux
+    (O/RreaCouplingPlaneWriter.cpp:31-207) with the write cadence of
+    RreaPlaneFluxState (I/RreaPlaneFlux.H:288-436): at the first step at or
+    past each multiple of interval_s (within 32 ulps of the time), or when
+    forced, one row per plane with the device's cumulative crossing
+    accumulators (rrea_gpu_plane_flux) and the area-weighted mean of the
+    cell-centred E_z over the core disc r <= core_radius_m at the plane (the
+    plane between its bracketing cell-centre rows, clamped at the edges),
+    beside the same mean of the ambient E_z and their relative difference."""
+
+    HEADER = ("format_version", "write_index", "step", "time_s", "plane_index", "altitude_m",
+              *gpu.RreaGpuContext.PLANE_VALUES,
+              "core_total_ez_v_per_m", "core_ambient_ez_v_per_m", "core_field_perturbation_fraction")
+
+    def __init__(self, path, planes, interval_s, core_radius_m, ambient_ez, altitude_at_z0_m=0.0):
+        planes = np.asarray(planes, dtype=np.float64)
+        if (planes.size == 0 or not np.all(np.isfinite(planes)) or np.any(np.diff(planes) <= 0.0)
+                or not np.isfinite(interval_s) or not interval_s > 0.0
+                or not np.isfinite(core_radius_m) or not core_radius_m > 0.0):
+            raise ValueError("plane diagnostics need finite increasing planes, a positive output interval "
+                             "and a positive core radius")
+        self.path, self.planes = path, planes
+        self.interval_s, self.core_radius_m = float(interval_s), float(core_radius_m)
+        self.ambient_ez = np.asarray(ambient_ez, dtype=np.float64)   # the ambient face vector (nr x (nz+1))
+        self.altitude_at_z0_m = float(altitude_at_z0_m)
+        self.next_time_s = self.interval_s
+        self.writes = 0
+        self.last_step, self.last_time_s = -1, -np.inf
+
+    def _tolerance(self, time_s):
+        return 32.0 * np.finfo(np.float64).eps * max(1.0, abs(time_s), abs(self.next_time_s))
+
+    def due(self, step, time_s, force=False):
+        if step < 0 or not np.isfinite(time_s):
+            return False
+        if step == self.last_step and time_s == self.last_time_s:
+            return False
+        return force or time_s + self._tolerance(time_s) >= self.next_time_s
+
+    def mark_written(self, step, time_s):
+        if not self.due(step, time_s, True):
+            raise ValueError("invalid or duplicate plane write")
+        tol = self._tolerance(time_s)
+        self.writes += 1
+        self.last_step, self.last_time_s = step, time_s
+        if time_s + tol >= self.next_time_s:
+            # a forced write before the boundary keeps the schedule; an accepted
+            # one moves past the boundary it was accepted at
+            nxt = np.longdouble(self.next_time_s)
+            intervals = np.floor((np.longdouble(time_s + tol) - nxt) / np.longdouble(self.interval_s)) + 1
+            self.next_time_s = float(nxt + max(np.longdouble(1), intervals) * np.longdouble(self.interval_s))
+
+    def core_means(self, cfg, scattered_ez):
+        """Per plane: (total, ambient) area-weighted core means of E_z."""
+        nr, nz = cfg.nr, cfg.nz
+        dr, dz = (cfg.r_hi - cfg.r_lo) / nr, (cfg.z_hi - cfg.z_lo) / nz
+        faces = (np.asarray(scattered_ez) + self.ambient_ez).reshape(nz + 1, nr)
+        cell = 0.5 * (faces[:-1] + faces[1:])
+        amb_faces = self.ambient_ez.reshape(nz + 1, nr)
+        out = []
+        for z in self.planes:
+            x = (z - cfg.z_lo) / dz - 0.5        # RreaCellCenteredGatherIndexCoordinate
+            if x <= 0.0:
+                rows = [(0, 1.0)]
+            elif x >= nz - 1:
+                rows = [(nz - 1, 1.0)]
+            else:
+                lo = int(np.floor(x))
+                rows = [(lo, 1.0 - (x - lo)), (lo + 1, x - lo)]
+            total = ambient = area = 0.0
+            # the ambient at the plane itself: linear between its bracketing E_z faces
+            fz = min(max((z - cfg.z_lo) / dz, 0.0), float(nz))
+            f0 = min(int(np.floor(fz)), nz - 1)
+            amb_at_plane = amb_faces[f0] + (fz - f0) * (amb_faces[f0 + 1] - amb_faces[f0])
+            for j, coefficient in rows:
+                if not coefficient > 0.0:
+                    continue
+                for i in range(nr):
+                    r_lo = max(0.0, cfg.r_lo + i * dr)
+                    r_hi = min(self.core_radius_m, cfg.r_lo + (i + 1) * dr)
+                    a = r_hi * r_hi - r_lo * r_lo if r_hi > r_lo else 0.0   # RreaCoreAnnulusArea
+                    if not a > 0.0:
+                        continue
+                    wgt = coefficient * a
+                    total += wgt * cell[j, i]
+                    ambient += wgt * amb_at_plane[i]
+                    area += wgt
+            if not area > 0.0:
+                raise ValueError("plane core field average has zero area")
+            out.append((total / area, ambient / area))
+        return out
+
+    def maybe_write(self, ctx, step, time_s, force=False):
+        if not self.due(step, time_s, force):
+            return False
+        flux = ctx.plane_flux()
+        _, ez, _ = ctx.field()
+        means = self.core_means(ctx.config, ez)
+        fresh = self.writes == 0
+        if fresh and os.path.exists(self.path) and os.path.getsize(self.path) > 0:
+            raise ValueError("a fresh plane stream refuses to overwrite a non-empty CSV")
+        with open(self.path, "w" if fresh else "a", newline="") as f:
+            w = csv.writer(f)
+            if fresh:
+                w.writerow(self.HEADER)
+            for p, z in enumerate(self.planes):
+                total, ambient = means[p]
+                perturbation = abs(total - ambient) / max(abs(ambient), 1.0e-30)
+                w.writerow([1, self.writes, step, repr(float(time_s)), p, repr(self.altitude_at_z0_m + z)]
+                           + [repr(float(v)) for v in flux[p]] + [repr(total), repr(ambient), repr(perturbation)])
+        self.mark_written(step, time_s)
+        return True
+
+
 def main():
     p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     p.add_argument("--case", default="uniform_c0", choices=["uniform_c0"])
@@ -245,14 +364,27 @@ def main():
     p.add_argument("--split-min-weight", type=float, default=0.0)
     p.add_argument("--json", default=None)
     p.add_argument("--csv", default=None)
+    p.add_argument("--planes", default=None, help="comma-separated plane z [m] of the crossing diagnostic")
+    p.add_argument("--plane-interval", type=float, default=1.0e-7, help="plane CSV output interval [s]")
+    p.add_argument("--plane-core-radius", type=float, default=5.0, help="core radius of the plane field mean [m]")
+    p.add_argument("--plane-csv", default="rrea_cd_plane_flux.csv")
     a = p.parse_args()
     import torch
 
     torch.cuda.set_device(0)
     ctx = make_context(a.case, a.capacity, a.rng_seed, a.field)
     seeds = workloads.make_electrons(a.case, a.seeds)
+    planes = None
+    if a.planes:
+        z = [float(v) for v in a.planes.split(",")]
+        ctx.set_planes(z)
+        amb = workloads.make_field(a.case)["amb_ez"]
+        if a.field is not None:
+            amb[:] = -float(a.field)
+        planes = PlaneFluxCsv(a.plane_csv, z, a.plane_interval, a.plane_core_radius, amb)
     res = AvalancheRun(ctx, seeds, population_target=a.population_target or None,
-                       split_min_weight=a.split_min_weight).run(a.steps, census_every=a.census_every)
+                       split_min_weight=a.split_min_weight).run(a.steps, census_every=a.census_every,
+                                                                plane_csv=planes)
     p_case = c0_like_case(a.field, a.case)
     res["case"] = a.case
     res["seeds"] = a.seeds

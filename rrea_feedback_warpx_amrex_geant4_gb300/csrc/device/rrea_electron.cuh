@@ -132,6 +132,99 @@ __device__ __forceinline__ double hard_moller_energy_loss(StepConstants const& C
     return mean * inv * dr;
 }
 
+// electron_ensemble_mean_drag_ev_per_m (O/RreaTransportStep.H:226-247): the
+// realized continuous loss plus the mean losses of the discrete hard-Moller
+// and tracked-brems channels.
+__device__ __forceinline__ double ensemble_mean_drag(StepConstants const& C, const double* __restrict__ arena,
+                                                     double e, double rho, Err& err)
+{
+    if (!(e > 0.0) || !(rho > 0.0)) return 0.0;
+    RateCache rc;
+    double const col = rate_value(C, arena, rc, e, kRateCollision, err);
+    double const soft = rate_value(C, arena, rc, e, kRateSoft, err);
+    double const hard = C.hm_enabled ? hard_moller_energy_loss(C, arena, e, rho, err) : 0.0;
+    double tracked = 0.0;
+    double const inv = rate_value(C, arena, rc, e, kRateBrems, err) * rho;
+    if (gt0(inv)) tracked = inv * mean_conditional(arena, C.tix.cdf[RREA_C_BREMS_E], e, err);
+    return (col * rho + soft * rho) + hard + tracked;
+}
+
+// defer_cd_electron_plane_crossings (O/RreaTransportStep.H:249-332) for one
+// continuous segment [b, eff] of an electron's chord, with the crossing rule
+// of RreaForEachNonperiodicPlaneCrossing (I/RreaPlaneFlux.H:79-118: upward
+// z0 < plane <= z1, downward z1 < plane <= z0) and the accumulation of
+// RreaPlaneFluxAccumulator::AddCrossing (:193-283) as device atomics.  The
+// energy at a crossing is the segment's start energy less the fixed-energy
+// stopping over the density path to the crossing, capped by the segment's
+// drag; a crossing is a local runaway when its energy is at or above the
+// cutoff and |E| there beats the ensemble mean drag.  Rare (planes only),
+// so out of line with its arguments by value; returns a status code.
+template <int NP>
+__device__ __noinline__ int plane_crossings(StepConstants const& C, ElectronArgs const& A, FieldView const fv,
+                                            Path<NP> const path, Geom const g, Intervals<NP> const iv, double b,
+                                            double eff, double weight, double k_before, double fixed_stp,
+                                            double drag)
+{
+    double x0, y0, z0, x1, y1, z1;
+    point_at_full(path, g, b, x0, y0, z0);
+    point_at_full(path, g, eff, x1, y1, z1);
+    if (!isfinite(z0) || !isfinite(z1)) return RREA_GPU_ERR_GEOMETRY;
+    if (z1 == z0) return 0;
+    int const n = A.n_planes;
+    const double* __restrict__ pz = A.plane_z;
+    double const lo = fmin(z0, z1), hi = fmax(z0, z1);
+    // [upper_bound(lo), upper_bound(hi)): the planes in (lo, hi]
+    int first = 0, last = 0;
+    {
+        int a = 0, c = n;
+        while (a < c) {
+            int const m = (a + c) >> 1;
+            if (__ldg(pz + m) <= lo) a = m + 1;
+            else c = m;
+        }
+        first = a;
+        c = n;
+        while (a < c) {
+            int const m = (a + c) >> 1;
+            if (__ldg(pz + m) <= hi) a = m + 1;
+            else c = m;
+        }
+        last = a;
+    }
+    double const inverse_span = 1.0 / (z1 - z0);
+    int const d = z1 > z0 ? 0 : 1;
+    double const cut = C.cfg.low_energy_cutoff_eV;
+    for (int i = first; i < last; ++i) {
+        double const fraction = b + (__ldg(pz + i) - z0) * inverse_span * (eff - b);
+        double x, y, z;
+        point_at_full(path, g, fraction, x, y, z);
+        double const r = hypot(x, y);
+        double const raw = fixed_stp * density_path(iv, path, b, fraction);
+        double const kc = fmax(0.0, k_before - fmin(drag, raw));
+        bool local = false;
+        if (kc >= cut) {
+            Err err;
+            double const rho = positive_or(density_ratio_at_z(A.prof, C.cfg.density_ratio, z, err), 1.0);
+            double fer, fez, fbt;
+            gather(fv, r, z, fer, fez, fbt);
+            double const mean_drag = ensemble_mean_drag(C, A.arena, kc, rho, err);
+            if (err.code) return err.code;
+            double const magnitude = hypot(fer, fez);
+            local = isfinite(magnitude) && isfinite(mean_drag) && mean_drag >= 0.0 && magnitude > mean_drag;
+        }
+        if (!isfinite(weight) || !(weight >= 0.0) || !isfinite(r) || !(r >= 0.0)) return RREA_GPU_ERR_INVALID_STATE;
+        double* const bin = A.plane_bins + kPlaneValues * i;
+        atomicAdd(bin + d, weight);
+        if (local) {
+            atomicAdd(bin + 2 + d, weight);
+            atomicAdd(bin + 6 + d, weight * r);
+            atomicAdd(bin + 8 + d, weight * r * r);
+        }
+        if (kc >= 1.0e6) atomicAdd(bin + 4 + d, weight);
+    }
+    return 0;
+}
+
 // S/RreaInteractionTables.cpp:2477-2493
 __device__ __forceinline__ double elastic_inverse_stp(StepConstants const& C, const double* __restrict__ arena,
                                                       double e, Err& err,
@@ -812,6 +905,13 @@ __device__ __forceinline__ int transport_charged(StepConstants const& C, Electro
                 point_at_full(path, g, 0.5 * (bb + ee), x, y, z);
                 // deposit_source(kind 0, sec POS ? 0 : cutoff/2, loss w_air) through the cache
                 ion_pairs.add(C, A.cells, rz_radius(x, y), z, pw);
+            }
+        }
+        if constexpr (!POS) {
+            if (A.n_planes > 0) {
+                if (int const code = plane_crossings<NP>(C, A, fv, path, g, iv, b, eff, weight, k, total, drag)) {
+                    err.set(code);
+                }
             }
         }
         k = max0(k - drag);

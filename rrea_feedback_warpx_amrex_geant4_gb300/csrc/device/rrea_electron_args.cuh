@@ -84,7 +84,19 @@ struct ElectronArgs {
     // optional scheduling order of the tile indices (null: the end of the
     // tile first); it changes which thread visits a particle, never a result
     const uint32_t* __restrict__ order;
+    // plane-crossing diagnostic of the electrons' continuous segments:
+    // n_planes strictly increasing plane z and kPlaneValues accumulators per
+    // plane (n_planes = 0: off)
+    int32_t n_planes;
+    const double* __restrict__ plane_z;
+    double* __restrict__ plane_bins;
 };
+
+// Accumulators per plane, in the reference's flattened order
+// (RreaPlaneFluxAccumulator::Flatten, I/RreaPlaneFlux.H:161-176): up and down
+// weight of all tracked, local-runaway and >= 1 MeV crossings, then the
+// local-runaway crossings' up and down sums of w r and of w r^2.
+constexpr int kPlaneValues = 10;
 
 // Visits every particle index of [0, n) once.  With a work counter each warp
 // claims the next 32 indices when it is done with its previous ones, so a

@@ -297,6 +297,13 @@ __device__ int advance_charged_newborn(StepConstants const& C, ElectronArgs cons
                 }
             }
         }
+        if constexpr (!POS) {
+            if (A.n_planes > 0) {
+                if (int const code = plane_crossings<NP>(C, A, fv, path, g, iv, b, eff, w, k, total, drag)) {
+                    err.set(code);
+                }
+            }
+        }
         k = max0(k - drag);
         if (reaches) k = cut;
         end_out = eff;

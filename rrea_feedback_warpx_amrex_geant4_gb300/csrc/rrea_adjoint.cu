@@ -55,6 +55,13 @@ struct Params {
     double k_th, tau_k, z_p, tau_z, lambda;
     uint64_t seed;
     RreaTable1DIndex col, soft;
+    // each particle's end: (global substep << 1) | kind (0 stopped in the
+    // drag, 1 below the cutoff after the second kick), -1 for none.  A
+    // recording forward writes it; a replaying one (and the reverse pass)
+    // ends every particle exactly there, so a perturbed profile keeps the
+    // topology of the recorded run.
+    int32_t* ends;
+    int replay;
 };
 
 struct State {
@@ -168,9 +175,15 @@ __device__ __forceinline__ void rotate(double const n[3], double c, double s, do
     v[2] = r[2];
 }
 
-// One substep forward.
+__device__ __forceinline__ int32_t end_code(Params const& p, int step, int sub, int kind)
+{
+    return ((step * p.substeps + sub) << 1) | kind;
+}
+
+// One substep forward; `end` is the particle's end record (see Params).
 __device__ __forceinline__ void substep(Params const& p, const double* __restrict__ e,
-                                        const double* __restrict__ arena, uint64_t id, int step, int sub, State& st)
+                                        const double* __restrict__ arena, uint64_t id, int step, int sub, State& st,
+                                        int32_t& end)
 {
     if (!st.alive) return;
     double const q = -1.0;
@@ -193,10 +206,12 @@ __device__ __forceinline__ void substep(Params const& p, const double* __restric
     // drag
     double ds;
     double const loss = drag_power(p, arena, k1, ds) * L;
-    if (!(k1 - loss > p.cutoff)) {
+    bool const stop = p.replay ? end == end_code(p, step, sub, 0) : !(k1 - loss > p.cutoff);
+    if (stop) {
         st.z = z1;
         st.k = p.cutoff;
         st.alive = 0;
+        if (!p.replay) end = end_code(p, step, sub, 0);
         return;
     }
     double const k2 = k1 - loss;
@@ -218,7 +233,11 @@ __device__ __forceinline__ void substep(Params const& p, const double* __restric
     st.dx = d[0];
     st.dy = d[1];
     st.dz = d[2];
-    if (!(k3 > p.cutoff)) st.alive = 0;
+    bool const below = p.replay ? end == end_code(p, step, sub, 1) : !(k3 > p.cutoff);
+    if (below) {
+        st.alive = 0;
+        if (!p.replay) end = end_code(p, step, sub, 1);
+    }
 }
 
 struct Adj {
@@ -229,7 +248,7 @@ struct Adj {
 // output adjoint and becomes the input adjoint; node gradients go to g.
 __device__ __forceinline__ void substep_adjoint(Params const& p, const double* __restrict__ e,
                                                 const double* __restrict__ arena, uint64_t id, int step, int sub,
-                                                State const& in, Adj& a, double* g)
+                                                State const& in, int32_t end, Adj& a, double* g)
 {
     if (!in.alive) return;   // frozen: nothing moved
     double const q = -1.0;
@@ -251,7 +270,7 @@ __device__ __forceinline__ void substep_adjoint(Params const& p, const double* _
     double dsp;
     double const sp = drag_power(p, arena, k1, dsp);
     double const loss = sp * L;
-    if (!(k1 - loss > p.cutoff)) {
+    if (end == end_code(p, step, sub, 0)) {
         // stopped in the drag: z1 = z + L d_z, K the constant cutoff, d as it came
         a = Adj{a.z, a.dx, a.dy, a.dz + a.z * L, a.z * in.dz * p.h * dspeed(in.k)};
         return;
@@ -334,10 +353,12 @@ __global__ void forward_kernel(Params p, const double* __restrict__ e, const dou
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         State st = load(seeds, p.n, i);
         double const z_init = st.z;
+        int32_t end = p.replay ? p.ends[i] : -1;
         for (int t = 0; t < p.steps; ++t) {
             if (t % p.ckpt_every == 0) store(ckpt + static_cast<int64_t>(t / p.ckpt_every) * 6 * p.n, p.n, i, st);
-            for (int q = 0; q < p.substeps; ++q) substep(p, e, arena, id[i], t, q, st);
+            for (int q = 0; q < p.substeps; ++q) substep(p, e, arena, id[i], t, q, st, end);
         }
+        if (!p.replay) p.ends[i] = end;
         store(final_state, p.n, i, st);
         acc += w[i] * (sig((st.k - p.k_th) / p.tau_k)
                        - p.lambda * (sig((st.z - p.z_p) / p.tau_z) - sig((z_init - p.z_p) / p.tau_z)));
@@ -360,17 +381,18 @@ __global__ void reverse_segment_kernel(Params p, const double* __restrict__ e, c
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < p.n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         State st = load(ckpt, p.n, i);
+        int32_t end = p.ends[i];
         for (int t = t0; t < t1; ++t) {
             for (int q = 0; q < p.substeps; ++q) {
                 store(tape + (static_cast<int64_t>(t - t0) * p.substeps + q) * 6 * p.n, p.n, i, st);
-                substep(p, e, arena, id[i], t, q, st);
+                substep(p, e, arena, id[i], t, q, st, end);
             }
         }
         Adj a{adj[i], adj[p.n + i], adj[2 * p.n + i], adj[3 * p.n + i], adj[4 * p.n + i]};
         for (int64_t k = entries - 1; k >= 0; --k) {
             int const t = t0 + static_cast<int>(k / p.substeps), q = static_cast<int>(k % p.substeps);
             State const in = load(tape + k * 6 * p.n, p.n, i);
-            substep_adjoint(p, e, arena, id[i], t, q, in, a, g);
+            substep_adjoint(p, e, arena, id[i], t, q, in, end, a, g);
         }
         adj[i] = a.z;
         adj[p.n + i] = a.dx;
@@ -415,6 +437,8 @@ struct AdjointState {
     double* tape = nullptr;    // C x substeps x 6 x n
     double* adj = nullptr;     // 5 x n
     double* loss = nullptr;
+    int32_t* ends = nullptr;   // n end records (Params::ends)
+    bool recorded = false;     // a recording forward has run
     int blocks = 1;
 };
 
@@ -423,7 +447,7 @@ void adjoint_free(AdjointState* s)
     if (!s) return;
     for (void* ptr : {static_cast<void*>(s->seeds), static_cast<void*>(s->w), static_cast<void*>(s->id),
                       static_cast<void*>(s->ckpt), static_cast<void*>(s->final_state), static_cast<void*>(s->tape),
-                      static_cast<void*>(s->adj), static_cast<void*>(s->loss)}) {
+                      static_cast<void*>(s->adj), static_cast<void*>(s->loss), static_cast<void*>(s->ends)}) {
         if (ptr) cudaFree(ptr);
     }
     delete s;
@@ -470,6 +494,9 @@ cudaError_t adjoint_stage(AdjointSetup const& in, const double* seeds6, const do
     alloc(&s->tape, static_cast<int64_t>(in.ckpt_every) * in.substeps * 6 * n);
     alloc(&s->adj, 5 * n);
     alloc(&s->loss, 1);
+    alloc(&s->ends, n);
+    p.ends = s->ends;
+    p.replay = 0;
     if (e == cudaSuccess && n > 0) {
         e = cudaMemcpy(s->seeds, seeds6, sizeof(double) * 6 * n, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(s->w, w, sizeof(double) * n, cudaMemcpyHostToDevice);
@@ -483,24 +510,30 @@ cudaError_t adjoint_stage(AdjointSetup const& in, const double* seeds6, const do
     return cudaSuccess;
 }
 
-cudaError_t adjoint_forward(AdjointState& s, const double* arena, const double* e_nodes, double& loss,
+cudaError_t adjoint_forward(AdjointState& s, const double* arena, const double* e_nodes, bool replay, double& loss,
                             cudaStream_t stream)
 {
     cudaError_t e = cudaMemsetAsync(s.loss, 0, sizeof(double), stream);
     if (e != cudaSuccess) return e;
+    rrea_dev::adj::Params p = s.p;
+    p.replay = replay ? 1 : 0;
     note_launch();
-    rrea_dev::adj::forward_kernel<<<s.blocks, 128, 0, stream>>>(s.p, e_nodes, arena, s.seeds, s.w, s.id, s.ckpt,
+    rrea_dev::adj::forward_kernel<<<s.blocks, 128, 0, stream>>>(p, e_nodes, arena, s.seeds, s.w, s.id, s.ckpt,
                                                                s.final_state, s.loss);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (!replay) s.recorded = true;
     e = cudaMemcpyAsync(&loss, s.loss, sizeof(double), cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     return e;
 }
 
+bool adjoint_recorded(AdjointState const& s) { return s.recorded; }
+
 cudaError_t adjoint_backward(AdjointState& s, const double* arena, const double* e_nodes, double* grad,
                              cudaStream_t stream)
 {
-    rrea_dev::adj::Params const& p = s.p;
+    rrea_dev::adj::Params p = s.p;
+    p.replay = 1;   // the reverse pass follows the recorded ends
     cudaError_t e = cudaMemsetAsync(grad, 0, sizeof(double) * p.n_nodes, stream);
     if (e != cudaSuccess) return e;
     note_launch();

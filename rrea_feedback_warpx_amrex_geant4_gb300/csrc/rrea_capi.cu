@@ -143,6 +143,10 @@ struct rrea_gpu_ctx {
     double profile_alt0 = 0.0, profile_ref = 0.0;
     double profile_step_ratio = 1.0;  // the ratio at the domain's axial centre
 
+    // plane-crossing diagnostic: plane z, then kPlaneValues accumulators per plane
+    double* d_planes = nullptr;
+    int32_t n_planes = 0;
+
     // one resident SoA tile per species (RREA_SPECIES_ELECTRON/POSITRON/PHOTON)
     SpeciesTile tiles[kSpecies];
 
@@ -435,6 +439,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
         dfree(st.cpu);
     }
     dfree(ctx->d_profile);
+    dfree(ctx->d_planes);
     dfree(ctx->d_sec_unordered);
     dfree(ctx->d_sec_ordered);
     dfree(ctx->d_sec_count);
@@ -626,6 +631,68 @@ rrea_gpu_status rrea_gpu_set_density_profile(rrea_gpu_ctx* ctx, const double* al
     return RREA_GPU_OK;
 }
 
+rrea_gpu_status rrea_gpu_set_planes(rrea_gpu_ctx* ctx, const double* plane_z, int32_t n_planes)
+{
+    if (!ctx || n_planes < 0 || (n_planes > 0 && !plane_z)) return RREA_GPU_ERR_ARGUMENT;
+    if (n_planes > 0 && ctx->n_instances > 0) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "the plane diagnostic is not available in ensemble mode");
+    }
+    // RreaPlaneLocationsAreStrictlyIncreasingFinite (I/RreaPlaneFlux.H:62-77)
+    for (int32_t i = 0; i < n_planes; ++i) {
+        if (!std::isfinite(plane_z[i]) || (i > 0 && !(plane_z[i] > plane_z[i - 1]))) {
+            return fail(ctx, RREA_GPU_ERR_ARGUMENT, "plane z must be finite and strictly increasing");
+        }
+    }
+    double* d = nullptr;
+    if (n_planes > 0) {
+        size_t const words = static_cast<size_t>(n_planes) * (1 + rrea_dev::kPlaneValues);
+        if (cudaMalloc(&d, words * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, RREA_GPU_ERR_CUDA, "plane diagnostic allocation failed");
+        }
+        RREA_CUDA(ctx, cudaMemcpyAsync(d, plane_z, static_cast<size_t>(n_planes) * sizeof(double),
+                                       cudaMemcpyHostToDevice, ctx->stream));
+        RREA_CUDA(ctx, cudaMemsetAsync(d + n_planes, 0, (words - n_planes) * sizeof(double), ctx->stream));
+        RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    dfree(ctx->d_planes);
+    ctx->d_planes = d;
+    ctx->n_planes = n_planes;
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_plane_flux(rrea_gpu_ctx* ctx, double* values)
+{
+    if (!ctx || (ctx->n_planes > 0 && !values)) return RREA_GPU_ERR_ARGUMENT;
+    if (ctx->n_planes == 0) return RREA_GPU_OK;
+    size_t const n = static_cast<size_t>(ctx->n_planes) * rrea_dev::kPlaneValues;
+    RREA_CUDA(ctx, cudaMemcpyAsync(values, ctx->d_planes + ctx->n_planes, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_restore_plane_flux(rrea_gpu_ctx* ctx, const double* values)
+{
+    if (!ctx) return RREA_GPU_ERR_ARGUMENT;
+    if (ctx->n_planes == 0) return RREA_GPU_OK;
+    size_t const n = static_cast<size_t>(ctx->n_planes) * rrea_dev::kPlaneValues;
+    double* const bins = ctx->d_planes + ctx->n_planes;
+    if (!values) {
+        RREA_CUDA(ctx, cudaMemsetAsync(bins, 0, n * sizeof(double), ctx->stream));
+    } else {
+        // RreaPlaneFluxAccumulator::RestoreFlat (I/RreaPlaneFlux.H:178-202)
+        for (size_t i = 0; i < n; ++i) {
+            if (!std::isfinite(values[i]) || values[i] < 0.0) {
+                return fail(ctx, RREA_GPU_ERR_ARGUMENT, "plane accumulators must be finite and nonnegative");
+            }
+        }
+        RREA_CUDA(ctx, cudaMemcpyAsync(bins, values, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
 }  // extern "C"
 
 namespace {
@@ -740,6 +807,12 @@ rrea_dev::ElectronArgs sink_args(rrea_gpu_ctx* ctx, rrea_dev::StepConstants cons
         a.fv.cell_ez = ctx->d_inst_cells + cells * ctx->n_instances;
         a.fv.inst_cells = static_cast<int64_t>(cells);
         a.fv.has_b = false;
+    }
+    // the instances of an ensemble would share the planes' accumulators
+    if (ctx->n_planes > 0 && ctx->n_instances == 0) {
+        a.n_planes = ctx->n_planes;
+        a.plane_z = ctx->d_planes;
+        a.plane_bins = ctx->d_planes + ctx->n_planes;
     }
     return a;
 }
@@ -2751,14 +2824,28 @@ rrea_gpu_status rrea_gpu_adjoint_forward(rrea_gpu_ctx* ctx, const double* e_node
 {
     if (!ctx || !e_nodes_device || !loss) return RREA_GPU_ERR_ARGUMENT;
     if (!ctx->adjoint) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no adjoint problem is staged");
-    RREA_CUDA(ctx, rrea_launch::adjoint_forward(*ctx->adjoint, ctx->d_arena, e_nodes_device, *loss, ctx->stream));
+    RREA_CUDA(ctx, rrea_launch::adjoint_forward(*ctx->adjoint, ctx->d_arena, e_nodes_device, false, *loss,
+                                                ctx->stream));
+    return RREA_GPU_OK;
+}
+
+rrea_gpu_status rrea_gpu_adjoint_forward_frozen(rrea_gpu_ctx* ctx, const double* e_nodes_device, double* loss)
+{
+    if (!ctx || !e_nodes_device || !loss) return RREA_GPU_ERR_ARGUMENT;
+    if (!ctx->adjoint || !rrea_launch::adjoint_recorded(*ctx->adjoint)) {
+        return fail(ctx, RREA_GPU_ERR_NOT_READY, "no recording adjoint forward has run");
+    }
+    RREA_CUDA(ctx, rrea_launch::adjoint_forward(*ctx->adjoint, ctx->d_arena, e_nodes_device, true, *loss,
+                                                ctx->stream));
     return RREA_GPU_OK;
 }
 
 rrea_gpu_status rrea_gpu_adjoint_backward(rrea_gpu_ctx* ctx, const double* e_nodes_device, double* grad_device)
 {
     if (!ctx || !e_nodes_device || !grad_device) return RREA_GPU_ERR_ARGUMENT;
-    if (!ctx->adjoint) return fail(ctx, RREA_GPU_ERR_NOT_READY, "no adjoint problem is staged");
+    if (!ctx->adjoint || !rrea_launch::adjoint_recorded(*ctx->adjoint)) {
+        return fail(ctx, RREA_GPU_ERR_NOT_READY, "the reverse pass follows a recording forward");
+    }
     RREA_CUDA(ctx, rrea_launch::adjoint_backward(*ctx->adjoint, ctx->d_arena, e_nodes_device, grad_device,
                                                  ctx->stream));
     RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -247,8 +247,11 @@ int adjoint_max_nodes();
 // seeds6: z, dx, dy, dz, K, alive (6 x n, host); w (n); id (n)
 cudaError_t adjoint_stage(AdjointSetup const& in, const double* seeds6, const double* w, const uint64_t* id,
                           int blocks, AdjointState*& out);
-cudaError_t adjoint_forward(AdjointState& s, const double* arena, const double* e_nodes, double& loss,
+// replay = false records every particle's end; replay = true ends every
+// particle where the last recording forward ended it (frozen topology)
+cudaError_t adjoint_forward(AdjointState& s, const double* arena, const double* e_nodes, bool replay, double& loss,
                             cudaStream_t stream);
+bool adjoint_recorded(AdjointState const& s);
 cudaError_t adjoint_backward(AdjointState& s, const double* arena, const double* e_nodes, double* grad,
                              cudaStream_t stream);
 cudaError_t adjoint_final_state(AdjointState const& s, double* host6);

@@ -131,7 +131,9 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_set_schedule", "rrea_gpu_ensemble_configure", "rrea_gpu_ensemble_partition", "rrea_gpu_ensemble_retire",
     "rrea_gpu_ensemble_census", "rrea_gpu_ensemble_population_thin", "rrea_gpu_ensemble_population_thin_all",
     "rrea_gpu_default_adjoint_config", "rrea_gpu_adjoint_stage", "rrea_gpu_adjoint_forward",
-    "rrea_gpu_adjoint_backward", "rrea_gpu_adjoint_final_state",
+    "rrea_gpu_adjoint_forward_frozen",
+    "rrea_gpu_adjoint_backward", "rrea_gpu_adjoint_final_state", "rrea_gpu_set_planes", "rrea_gpu_plane_flux",
+    "rrea_gpu_restore_plane_flux",
 )
 NOALLOC_MAX_PARENTS = 1 << 18  # RREA_GPU_NOALLOC_MAX_PARENTS
 SPECIES_ELECTRON, SPECIES_POSITRON, SPECIES_PHOTON = 0, 1, 2  # RREA_SPECIES_*
@@ -248,6 +250,9 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_fluid_transport.argtypes = [vp, ctypes.c_double, _D, _D, _D, _D, _D]
     lib.rrea_gpu_advance_field_coupled.argtypes = [vp, ctypes.c_double, _D]
     lib.rrea_gpu_set_schedule.argtypes = [vp, ctypes.c_int32]
+    lib.rrea_gpu_set_planes.argtypes = [vp, _D, ctypes.c_int32]
+    lib.rrea_gpu_plane_flux.argtypes = [vp, _D]
+    lib.rrea_gpu_restore_plane_flux.argtypes = [vp, _D]
     lib.rrea_gpu_sources_device.argtypes = [vp, ctypes.POINTER(vp)]
     lib.rrea_gpu_fluid_reductions.argtypes = [vp, ctypes.c_double, _D]
     lib.rrea_gpu_advance_field_coupled_from_current.argtypes = [vp, ctypes.c_double, _D]
@@ -404,6 +409,34 @@ class RreaGpuContext:
     def set_field(self, er, ez, bt, amb_er, amb_ez):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (er, ez, bt, amb_er, amb_ez)]
         self._check(self.lib.rrea_gpu_set_field(self.handle, *[a.ctypes.data_as(_D) for a in arrs]))
+
+    PLANE_VALUES = ("all_tracked_up_weight", "all_tracked_down_weight", "local_runaway_up_weight",
+                    "local_runaway_down_weight", "e_ge_1mev_up_weight", "e_ge_1mev_down_weight",
+                    "local_runaway_up_r_weighted_m", "local_runaway_down_r_weighted_m",
+                    "local_runaway_up_r2_weighted_m2", "local_runaway_down_r2_weighted_m2")
+
+    def set_planes(self, plane_z_m=()):
+        """Turns on the plane-crossing diagnostic at the given strictly
+        increasing z (an empty list turns it off); accumulators start at 0."""
+        z = np.ascontiguousarray(plane_z_m, dtype=np.float64)
+        self._check(self.lib.rrea_gpu_set_planes(self.handle, z.ctypes.data_as(_D) if z.size else None, z.size))
+        self.n_planes = int(z.size)
+
+    def plane_flux(self):
+        """The cumulative accumulators, (n_planes, 10) in PLANE_VALUES order."""
+        out = np.zeros((getattr(self, "n_planes", 0), len(self.PLANE_VALUES)))
+        if out.size:
+            self._check(self.lib.rrea_gpu_plane_flux(self.handle, out.ctypes.data_as(_D)))
+        return out
+
+    def restore_plane_flux(self, values=None):
+        if values is None:
+            self._check(self.lib.rrea_gpu_restore_plane_flux(self.handle, None))
+            return
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        if v.size != getattr(self, "n_planes", 0) * len(self.PLANE_VALUES):
+            raise ValueError("10 values per plane")
+        self._check(self.lib.rrea_gpu_restore_plane_flux(self.handle, v.ctypes.data_as(_D)))
 
     def set_density_profile(self, altitude_m=None, density_kg_m3=None, altitude_msl_at_z0_m=0.0,
                             reference_density_kg_m3=0.0):

@@ -10,9 +10,12 @@ perturbation), 96 steps of 0.5 ns in 2 substeps, checkpoints every 32 steps;
 the runaway threshold at 8 MeV (50 keV wide) and the crossing plane at 12 m
 (1 m wide), where both loss terms move.
 
-  * gradient: within 1e-5 relative of central differences (h = 1 V/m) on
+  * gradient: within 1e-5 relative of central differences (h = 1 V/m,
+    common random numbers, every particle ending where it ended in the
+    unperturbed run: the frozen topology the adjoint differentiates) on
     every node the particles reach with a gradient above 1e-3 of the
     largest, and exactly zero on the nodes none reaches;
+  * the frozen forward at the unperturbed nodes is the plain forward;
   * forward: final K and z within 1e-11 relative of the numpy restatement
     (the device's exp/log/sin/cos against numpy's);
   * autograd: torch's backward through the Function returns the adjoint;
@@ -61,6 +64,14 @@ def test_gradient_matches_central_differences(problem):
     np.testing.assert_allclose(g[reached], fd, rtol=1e-5, atol=1e-7 * big)
     far = np.arange(40, 256)        # beyond 80 m: no particle gets there in 48 ns
     assert np.all(g[far] == 0.0)
+
+
+def test_frozen_forward_replays_the_recorded_run(problem):
+    adjoint, prob, e, seeds, cfg = problem
+    plain = prob.forward(e)
+    state = prob.final_state()
+    assert prob.forward(e, frozen=True) == plain
+    np.testing.assert_array_equal(prob.final_state(), state)
 
 
 def test_forward_matches_restatement(problem):
