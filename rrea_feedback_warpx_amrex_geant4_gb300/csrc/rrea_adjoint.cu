@@ -346,7 +346,7 @@ __device__ __forceinline__ void store(double* __restrict__ s, int64_t n, int64_t
 __global__ void forward_kernel(Params p, const double* __restrict__ e, const double* __restrict__ arena,
                                const double* __restrict__ seeds, const double* __restrict__ w,
                                const uint64_t* __restrict__ id, double* __restrict__ ckpt,
-                               double* __restrict__ final_state, double* loss)
+                               double* __restrict__ final_state, double* __restrict__ partials)
 {
     double acc = 0.0;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < p.n;
@@ -363,8 +363,34 @@ __global__ void forward_kernel(Params p, const double* __restrict__ e, const dou
         acc += w[i] * (sig((st.k - p.k_th) / p.tau_k)
                        - p.lambda * (sig((st.z - p.z_p) / p.tau_z) - sig((z_init - p.z_p) / p.tau_z)));
     }
+    // the loss is summed in a fixed order (warp tree, the warps of a block
+    // in turn, then the blocks in turn by sum_partials_kernel), so the same
+    // nodes give the same loss to the bit and finite differences of the loss
+    // carry only its rounding
+    __shared__ double warp_sums[32];
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(loss, acc);
+    if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int k = 0; k < static_cast<int>(blockDim.x >> 5); ++k) b += warp_sums[k];
+        partials[blockIdx.x] = b;
+    }
+}
+
+// The block partials summed in order with Neumaier's compensation, so the
+// loss is the correctly rounded sum of the partials to within an ulp or two
+// and a difference of two losses carries only their final roundings.
+__global__ void sum_partials_kernel(const double* __restrict__ partials, int count, double* loss)
+{
+    double s = 0.0, c = 0.0;
+    for (int k = 0; k < count; ++k) {
+        double const x = partials[k];
+        double const t = s + x;
+        c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+        s = t;
+    }
+    *loss = s + c;
 }
 
 // Reverse pass over one checkpoint segment [t0, t1): recompute onto the tape
@@ -437,6 +463,7 @@ struct AdjointState {
     double* tape = nullptr;    // C x substeps x 6 x n
     double* adj = nullptr;     // 5 x n
     double* loss = nullptr;
+    double* partials = nullptr;   // one loss partial per forward block
     int32_t* ends = nullptr;   // n end records (Params::ends)
     bool recorded = false;     // a recording forward has run
     int blocks = 1;
@@ -447,7 +474,8 @@ void adjoint_free(AdjointState* s)
     if (!s) return;
     for (void* ptr : {static_cast<void*>(s->seeds), static_cast<void*>(s->w), static_cast<void*>(s->id),
                       static_cast<void*>(s->ckpt), static_cast<void*>(s->final_state), static_cast<void*>(s->tape),
-                      static_cast<void*>(s->adj), static_cast<void*>(s->loss), static_cast<void*>(s->ends)}) {
+                      static_cast<void*>(s->adj), static_cast<void*>(s->loss), static_cast<void*>(s->partials),
+                      static_cast<void*>(s->ends)}) {
         if (ptr) cudaFree(ptr);
     }
     delete s;
@@ -494,6 +522,7 @@ cudaError_t adjoint_stage(AdjointSetup const& in, const double* seeds6, const do
     alloc(&s->tape, static_cast<int64_t>(in.ckpt_every) * in.substeps * 6 * n);
     alloc(&s->adj, 5 * n);
     alloc(&s->loss, 1);
+    alloc(&s->partials, blocks);
     alloc(&s->ends, n);
     p.ends = s->ends;
     p.replay = 0;
@@ -513,13 +542,15 @@ cudaError_t adjoint_stage(AdjointSetup const& in, const double* seeds6, const do
 cudaError_t adjoint_forward(AdjointState& s, const double* arena, const double* e_nodes, bool replay, double& loss,
                             cudaStream_t stream)
 {
-    cudaError_t e = cudaMemsetAsync(s.loss, 0, sizeof(double), stream);
-    if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
     rrea_dev::adj::Params p = s.p;
     p.replay = replay ? 1 : 0;
     note_launch();
     rrea_dev::adj::forward_kernel<<<s.blocks, 128, 0, stream>>>(p, e_nodes, arena, s.seeds, s.w, s.id, s.ckpt,
-                                                               s.final_state, s.loss);
+                                                               s.final_state, s.partials);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    note_launch();
+    rrea_dev::adj::sum_partials_kernel<<<1, 1, 0, stream>>>(s.partials, s.blocks, s.loss);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (!replay) s.recorded = true;
     e = cudaMemcpyAsync(&loss, s.loss, sizeof(double), cudaMemcpyDeviceToHost, stream);

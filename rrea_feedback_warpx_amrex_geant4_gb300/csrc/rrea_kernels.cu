@@ -84,13 +84,13 @@ __device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
 }
 
 template <int MinBlocks, int NP>
-__global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(ElectronArgs A)
+__global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(const __grid_constant__ ElectronArgs A)
 {
     charged_step_body<NP, false>(A);
 }
 
 template <int MinBlocks, int NP>
-__global__ void __launch_bounds__(128, MinBlocks) positron_step_kernel(ElectronArgs A)
+__global__ void __launch_bounds__(128, MinBlocks) positron_step_kernel(const __grid_constant__ ElectronArgs A)
 {
     charged_step_body<NP, true>(A);
 }

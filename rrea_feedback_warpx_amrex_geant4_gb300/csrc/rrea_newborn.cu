@@ -20,7 +20,7 @@ namespace {
 // SPECIES 1 positron, 2 photon, 0 every other species id (the reference
 // advances anything that is not a photon or a positron as an electron).
 template <int NP, int SPECIES>
-__global__ void __launch_bounds__(128, RREA_NEWBORN_MIN_BLOCKS) newborn_kernel(ElectronArgs A, rrea_gpu_secondary* __restrict__ items,
+__global__ void __launch_bounds__(128, RREA_NEWBORN_MIN_BLOCKS) newborn_kernel(const __grid_constant__ ElectronArgs A, rrea_gpu_secondary* __restrict__ items,
                                                       int64_t n, uint32_t* __restrict__ alive)
 {
     StepConstants const& C = c_step;

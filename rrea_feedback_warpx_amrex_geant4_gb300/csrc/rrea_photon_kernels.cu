@@ -12,7 +12,7 @@ namespace rrea_dev {
 __constant__ StepConstants c_step_photon;
 
 template <int NP>
-__global__ void __launch_bounds__(128, 2) photon_step_kernel(ElectronArgs A)
+__global__ void __launch_bounds__(128, 2) photon_step_kernel(const __grid_constant__ ElectronArgs A)
 {
     StepConstants const& C = c_step_photon;
     unsigned int moved = 0;
