@@ -177,3 +177,51 @@ def central_differences(problem, e_nodes, nodes, h=1.0):
         del e
     problem.forward(e_nodes)
     return np.array(out)
+
+
+def measure(n=1_000_000, repeats=2, **overrides):
+    """Seconds per gradient of the batched adjoint configuration (config4
+    profile and seeds, the default adjoint config: 2000 steps of 0.5 ns in 4
+    substeps, checkpoints every 32 steps): one recording forward plus the
+    reverse pass, timed after one untimed gradient; returns a dict."""
+    import time
+
+    import torch
+
+    cfg = default_config(**overrides)
+    prob = PushAdjoint(cfg, config4_seeds(n))
+    try:
+        e = torch.tensor(config4_profile(n_nodes=cfg.n_nodes, z_hi=cfg.z_hi), dtype=torch.float64, device="cuda")
+        prob.forward(e)
+        prob.backward(e)
+        torch.cuda.synchronize()
+        t_f = t_b = 0.0
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            loss = prob.forward(e)
+            t1 = time.perf_counter()
+            g = prob.backward(e)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            t_f += t1 - t0
+            t_b += t2 - t1
+        t_f /= repeats
+        t_b /= repeats
+        return {"electrons": n, "steps": cfg.steps, "substeps": cfg.substeps, "checkpoint_every": cfg.checkpoint_every,
+                "nodes": cfg.n_nodes, "loss": loss, "grad_norm": float(torch.linalg.vector_norm(g)),
+                "forward_s": t_f, "reverse_s": t_b, "s_per_grad": t_f + t_b, "reverse_over_forward": t_b / t_f,
+                "particle_substeps_per_s_forward": n * cfg.steps * cfg.substeps / t_f}
+    finally:
+        prob.close()
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    p = argparse.ArgumentParser(description="seconds per gradient of the batched adjoint configuration")
+    p.add_argument("--electrons", type=int, default=1_000_000)
+    p.add_argument("--steps", type=int, default=2000)
+    p.add_argument("--repeats", type=int, default=2)
+    a = p.parse_args()
+    print(json.dumps(measure(a.electrons, a.repeats, steps=a.steps)))

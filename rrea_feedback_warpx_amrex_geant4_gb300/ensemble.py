@@ -192,11 +192,16 @@ class EnsembleRun:
         return best, timings
 
     def run(self, autotune=False):
+        """Advances every instance to its end; `stepping_s` is the wall time
+        of the steps (the autotuner's steps included, set-up excluded: every
+        step ends in a stream synchronisation)."""
+        t0 = time.perf_counter()
         tuned = self.autotune() if autotune else None
         while self.active:
             self.advance()
         return {"results": [self.results[k] for k in sorted(self.results)], "steps": self.step,
-                "particle_steps": self.particle_steps, "thinned": self.thinned, "autotune": tuned}
+                "particle_steps": self.particle_steps, "thinned": self.thinned, "autotune": tuned,
+                "stepping_s": time.perf_counter() - t0}
 
 
 def run_batched(instances, capacity=1 << 22, autotune=True, **kw):
@@ -209,7 +214,7 @@ def run_batched(instances, capacity=1 << 22, autotune=True, **kw):
 
 def run_sequential(instances, capacity=1 << 20, **kw):
     """Every instance alone on its own context (cpu = k)."""
-    out, steps, particle_steps, thinned = [], 0, 0, 0
+    out, steps, particle_steps, thinned, stepping = [], 0, 0, 0, 0.0
     for k in range(len(instances)):
         run = EnsembleRun(instances, capacity=capacity, only=[k], **kw)
         try:
@@ -220,7 +225,9 @@ def run_sequential(instances, capacity=1 << 20, **kw):
         steps += res["steps"]
         particle_steps += res["particle_steps"]
         thinned += res["thinned"]
-    return {"results": out, "steps": steps, "particle_steps": particle_steps, "thinned": thinned}
+        stepping += res["stepping_s"]
+    return {"results": out, "steps": steps, "particle_steps": particle_steps, "thinned": thinned,
+            "stepping_s": stepping}
 
 
 def main():
@@ -237,7 +244,8 @@ def main():
     batched = run_batched(inst, control_every=args.control_every)
     t_b = time.perf_counter() - t0
     summary = {"instances": args.instances, "duration_scale": args.duration_scale, "target": args.target,
-               "control_every": args.control_every, "batched_s": t_b, "batched_steps": batched["steps"],
+               "control_every": args.control_every, "batched_s": t_b,
+               "batched_stepping_s": batched["stepping_s"], "batched_steps": batched["steps"],
                "thinned": batched["thinned"], "batched_particle_steps": batched["particle_steps"],
                "autotune": batched["autotune"][0] if batched["autotune"] else None,
                "multiplication": [r["multiplication"] for r in batched["results"]]}
@@ -245,8 +253,12 @@ def main():
         t0 = time.perf_counter()
         seq = run_sequential(inst, control_every=args.control_every)
         summary["sequential_s"] = time.perf_counter() - t0
+        summary["sequential_stepping_s"] = seq["stepping_s"]
         summary["sequential_steps"] = seq["steps"]
+        summary["sequential_particle_steps"] = seq["particle_steps"]
         summary["speedup"] = summary["sequential_s"] / t_b
+        # the steps alone: 64 context set-ups and table loads left out
+        summary["speedup_stepping"] = seq["stepping_s"] / batched["stepping_s"]
     print(json.dumps(summary))
     if args.json:
         with open(args.json, "w") as f:
