@@ -26,6 +26,11 @@ one dt, its newborn residual legs included.  Synthetic seeds; no dataset.
               r,z,theta,ux,uy,uz,w,id, write r,z,theta,ux,uy,uz)
   cpu_baseline the oracle (CPU restatement, all host threads) on a bounded
               sample of the same workload
+  batched     the batched pattern: 64 independent uniform-field instances
+              advanced by one set of launches per step against the same 64
+              run one after another (stepping wall time, results identical)
+  adjoint     seconds per pathwise field gradient of the adjoint pattern
+              (1e6 electrons, 2000 steps, checkpoints every 32 steps)
 
 --impl reference times the CPU restatement of the reference path (the
 WarpX/AMReX build itself cannot be built here) on the host cores, on the same
@@ -65,6 +70,9 @@ def parse():
     p.add_argument("--cpu-baseline-steps", type=int, default=3)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--c0-steps", type=int, default=1000)
+    p.add_argument("--ensemble-scale", type=float, default=0.05,
+                   help="duration scale of the batched 64-instance ensemble line (0: skip it)")
+    p.add_argument("--adjoint-steps", type=int, default=2000, help="steps of the adjoint line (0: skip it)")
     p.add_argument("--threads", type=int, default=128)
     p.add_argument("--blocks-per-sm", type=int, default=16)
     return p.parse_args()
@@ -457,6 +465,44 @@ def run_gb300(args, rank, world, local):
               "final_electrons": res["history"][-1]["electron_count"],
               "timing": "host wall clock around the steps (each step ends in a stream synchronisation)"}
 
+    # ---- the batched pattern: 64 independent uniform-field instances in one
+    # set of launches per step against the same 64 run one after another
+    # (identical per-instance results, so the statistics match exactly)
+    batched = None
+    if rank == 0 and world == 1 and args.ensemble_scale > 0:
+        from rrea_feedback_warpx_amrex_geant4_gb300 import ensemble
+
+        inst = ensemble.config3_instances(64, duration_scale=args.ensemble_scale)
+        b = ensemble.run_batched(inst, control_every=16)
+        q = ensemble.run_sequential(inst, control_every=16)
+        same = all(x["multiplication"] == y["multiplication"] and x["electron_count"] == y["electron_count"]
+                   for x, y in zip(b["results"], q["results"]))
+        batched = {"workload": f"64 uniform-field instances (E_z 300-1000 kV/m, 1e3-1e5 seeds at 7.2 MeV, 32x256 "
+                               f"cells each), durations 0.5-4 us scaled by {args.ensemble_scale} "
+                               f"({min(i.steps for i in inst)}-{max(i.steps for i in inst)} steps)",
+                   "batched_s": b["stepping_s"], "sequential_s": q["stepping_s"],
+                   "speedup": q["stepping_s"] / b["stepping_s"],
+                   "batched_particle_steps_per_s": b["particle_steps"] / b["stepping_s"],
+                   "sequential_particle_steps_per_s": q["particle_steps"] / q["stepping_s"],
+                   "particle_steps": b["particle_steps"], "identical_results": same,
+                   "launch_shape": b["autotune"][0] if b["autotune"] else None,
+                   "timing": "host wall clock of the steps (set-up and table loads excluded; every step ends in a "
+                             "stream synchronisation)"}
+
+    # ---- the adjoint pattern: seconds per pathwise field gradient
+    adjoint_line = None
+    if rank == 0 and world == 1 and args.adjoint_steps > 0:
+        from rrea_feedback_warpx_amrex_geant4_gb300 import adjoint
+
+        a = adjoint.measure(1_000_000, repeats=1, steps=args.adjoint_steps)
+        adjoint_line = {"workload": f"1e6 seed electrons at 7.2 MeV, E_z(z) on 256 nodes over 0-500 m (450 kV/m "
+                                    f"plus a 20 kV/m, 20 m correlated perturbation), {a['steps']} steps of 0.5 ns "
+                                    f"in {a['substeps']} substeps, checkpoints every {a['checkpoint_every']} steps, "
+                                    f"FP64",
+                        "s_per_grad": a["s_per_grad"], "forward_s": a["forward_s"], "reverse_s": a["reverse_s"],
+                        "reverse_over_forward": a["reverse_over_forward"], "unit": "s/grad",
+                        "higher_is_better": False}
+
     if rank == 0:
         peak, peak_kind = read_peaks()
         achieved = (moved_e * BYTES_PER_PARTICLE_STEP) / (kernel_ms_e / 1000.0) / 1.0e9 if kernel_ms_e > 0 else 0.0
@@ -501,6 +547,8 @@ def run_gb300(args, rank, world, local):
                                        f"{args.cpu_baseline_steps} steps of the same whole kinetic step "
                                        f"({cpu_moved} particle-steps in {cpu_t:.1f} s), OpenMP chunks of 64, -O3"},
             "small_population": c0,
+            "batched": batched,
+            "adjoint": adjoint_line,
             "gpu_launches": launches,
             "gpu_launches_per_step": launches_per_step,
             "clocks": clocks.summary(),

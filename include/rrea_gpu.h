@@ -512,8 +512,11 @@ rrea_gpu_status rrea_gpu_fetch_photons(rrea_gpu_ctx* ctx, rrea_gpu_tile* tile);
  * multiple of 32) and resident 128-thread blocks per SM (1 to 64; the
  * electron kernel variant follows the residency: 2, 4, 8, 12 or 16 blocks
  * with 255, 128, 64, 40 or 32 registers per thread; default 16, the full
- * 64 warps per SM).  The grid is one resident wave with a grid-stride loop.
- * `diagnostics` enables the per-particle diagnostic arrays. */
+ * 64 warps per SM; the positron kernel has the 2, 4, 8 and 16 variants).
+ * A charged tile too small to fill that residency in one wave runs the
+ * variant with the most registers that still holds it (results do not
+ * depend on the variant).  The grid is one resident wave with a grid-stride
+ * loop.  `diagnostics` enables the per-particle diagnostic arrays. */
 rrea_gpu_status rrea_gpu_set_launch(rrea_gpu_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm,
                                     int32_t diagnostics);
 /* Scheduling order of the resident charged phases: 1 (default) visits a

@@ -1,10 +1,11 @@
 """Builds the GB300 kinetic-step library in-tree:
 rrea_feedback_warpx_amrex_geant4_gb300/lib/librrea_gpu.so (sm_103a only).
 
-Parity-study variants (RREA_LIBM=1: CUDA's log/exp in place of the
-table-driven ones; RREA_FMAD=0, below) build into the path RREA_GPU_LIB
-names, with their own object directory, and the bindings load from there
-when RREA_GPU_LIB is set; the default build is the product.
+Parity-study and tuning variants (RREA_LIBM=1: CUDA's log/exp in place of
+the table-driven ones; RREA_FMAD=0, below; RREA_DEFINES=NAME=VALUE,...:
+compile-time settings such as RREA_NEWBORN_MIN_BLOCKS) build into the path
+RREA_GPU_LIB names, with their own object directory, and the bindings load
+from there when RREA_GPU_LIB is set; the default build is the product.
 
 FP64 FMA contraction is on (--fmad=true): GB300's FP64 pipe issues a fused
 multiply-add for the price of a multiply, a measured 9 % of the electron
@@ -26,6 +27,7 @@ SOURCES = [
     os.path.join(CSRC, "rrea_capi.cu"),
     os.path.join(CSRC, "rrea_kernels.cu"),
     os.path.join(CSRC, "rrea_photon_kernels.cu"),
+    os.path.join(CSRC, "rrea_positron_kernels.cu"),
     os.path.join(CSRC, "rrea_noalloc.cu"),
     os.path.join(CSRC, "rrea_commit.cu"),
     os.path.join(CSRC, "rrea_resample.cu"),
@@ -61,7 +63,7 @@ def _deps():
 
 
 # the sources that define the charged and photon transport kernels
-KERNEL_SOURCES = ("rrea_kernels.cu", "rrea_kernels.h", "rrea_photon_kernels.cu")
+KERNEL_SOURCES = ("rrea_kernels.cu", "rrea_kernels.h", "rrea_photon_kernels.cu", "rrea_positron_kernels.cu")
 
 
 def source_digest():
@@ -81,6 +83,7 @@ def source_digest():
             h.update(f.read())
     h.update(("fmad=" + os.environ.get("RREA_FMAD", "1")).encode())
     h.update(("libm=" + os.environ.get("RREA_LIBM", "0")).encode())
+    h.update(("defines=" + os.environ.get("RREA_DEFINES", "")).encode())
     return h.hexdigest()[:16]
 
 
@@ -90,7 +93,10 @@ def build(force=False, verbose=False):
         if all(os.path.getmtime(d) <= t for d in _deps()):
             return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    defines = [d for d in os.environ.get("RREA_DEFINES", "").split(",") if d]
     variant = f"fmad{os.environ.get('RREA_FMAD', '1')}_libm{os.environ.get('RREA_LIBM', '0')}"
+    if defines:
+        variant += "_" + "_".join(d.replace("=", "") for d in defines)
     objdir = os.path.join(PKG, "_build" if variant == "fmad1_libm0" else "_build_" + variant)
     os.makedirs(objdir, exist_ok=True)
     nvcc = _nvcc()
@@ -99,6 +105,7 @@ def build(force=False, verbose=False):
               "-I", CSRC, "-I", os.path.join(ROOT, "include")] + ARCH
     if os.environ.get("RREA_LIBM", "0") == "1":
         common += ["-DRREA_CUDA_LIBM"]
+    common += ["-D" + d for d in defines]
     if verbose:
         common += ["-Xptxas", "-v"]
     objs = []

@@ -29,8 +29,10 @@
 //
 // Forward: one thread per particle, the state checkpointed every C steps.
 // Reverse: per checkpoint segment, last to first, the forward is recomputed
-// from the checkpoint onto a tape of substep inputs, then the adjoint runs
-// back through it; the node gradient is accumulated per block in shared
+// from the checkpoint onto a tape of substep inputs (with each substep's
+// stopping power, its derivative and the frozen rotation, so the adjoint
+// evaluates neither tables nor the RNG again), then the adjoint runs back
+// through it; the node gradient is accumulated per block in shared
 // memory and added to the output once per block and node.
 #include "rrea_kernels.h"
 
@@ -180,10 +182,17 @@ __device__ __forceinline__ int32_t end_code(Params const& p, int step, int sub, 
     return ((step * p.substeps + sub) << 1) | kind;
 }
 
+// Values of one substep that the reverse pass reads back instead of
+// evaluating them again: the stopping power and its K-derivative at K1, and
+// the frozen rotation (axis, cos, sin).  kAux columns of n per tape entry.
+constexpr int kAux = 7;
+
 // One substep forward; `end` is the particle's end record (see Params).
+// With `aux` (column stride n, particle i) the drag and rotation go to the
+// tape beside the substep's input state.
 __device__ __forceinline__ void substep(Params const& p, const double* __restrict__ e,
                                         const double* __restrict__ arena, uint64_t id, int step, int sub, State& st,
-                                        int32_t& end)
+                                        int32_t& end, double* __restrict__ aux = nullptr, int64_t i = 0)
 {
     if (!st.alive) return;
     double const q = -1.0;
@@ -205,7 +214,12 @@ __device__ __forceinline__ void substep(Params const& p, const double* __restric
     double const z1 = st.z + L * st.dz;
     // drag
     double ds;
-    double const loss = drag_power(p, arena, k1, ds) * L;
+    double const sp = drag_power(p, arena, k1, ds);
+    double const loss = sp * L;
+    if (aux) {
+        aux[i] = sp;
+        aux[p.n + i] = ds;
+    }
     bool const stop = p.replay ? end == end_code(p, step, sub, 0) : !(k1 - loss > p.cutoff);
     if (stop) {
         st.z = z1;
@@ -227,6 +241,13 @@ __device__ __forceinline__ void substep(Params const& p, const double* __restric
     double const k3 = k2 + 0.5 * w;
     double n[3], c, sn;
     rotation(p, id, step, sub, n, c, sn);
+    if (aux) {
+        aux[2 * p.n + i] = n[0];
+        aux[3 * p.n + i] = n[1];
+        aux[4 * p.n + i] = n[2];
+        aux[5 * p.n + i] = c;
+        aux[6 * p.n + i] = sn;
+    }
     rotate(n, c, sn, d);
     st.z = z1;
     st.k = k3;
@@ -244,10 +265,11 @@ struct Adj {
     double z, dx, dy, dz, k;
 };
 
-// One substep backward: `in` is the substep's input state; `a` holds the
-// output adjoint and becomes the input adjoint; node gradients go to g.
+// One substep backward: `in` is the substep's input state and `aux` its
+// tape values (column stride n, particle i); `a` holds the output adjoint
+// and becomes the input adjoint; node gradients go to g.
 __device__ __forceinline__ void substep_adjoint(Params const& p, const double* __restrict__ e,
-                                                const double* __restrict__ arena, uint64_t id, int step, int sub,
+                                                const double* __restrict__ aux, int64_t i, int step, int sub,
                                                 State const& in, int32_t end, Adj& a, double* g)
 {
     if (!in.alive) return;   // frozen: nothing moved
@@ -267,8 +289,7 @@ __device__ __forceinline__ void substep_adjoint(Params const& p, const double* _
     double const nm1 = sqrt(m1[0] * m1[0] + m1[1] * m1[1] + m1[2] * m1[2]);
     double const d1[3] = {m1[0] / nm1, m1[1] / nm1, m1[2] / nm1};
     double const k1 = in.k + 0.5 * w;
-    double dsp;
-    double const sp = drag_power(p, arena, k1, dsp);
+    double const sp = aux[i], dsp = aux[p.n + i];
     double const loss = sp * L;
     if (end == end_code(p, step, sub, 0)) {
         // stopped in the drag: z1 = z + L d_z, K the constant cutoff, d as it came
@@ -284,8 +305,8 @@ __device__ __forceinline__ void substep_adjoint(Params const& p, const double* _
     double const nm2 = sqrt(m2[0] * m2[0] + m2[1] * m2[1] + m2[2] * m2[2]);
     double const d2[3] = {m2[0] / nm2, m2[1] / nm2, m2[2] / nm2};
     // scatter: d3 = R d2 -> d2_bar = R^T d3_bar
-    double n[3], c, sn;
-    rotation(p, id, step, sub, n, c, sn);
+    double const n[3] = {aux[2 * p.n + i], aux[3 * p.n + i], aux[4 * p.n + i]};
+    double const c = aux[5 * p.n + i], sn = aux[6 * p.n + i];
     double d2_bar[3] = {a.dx, a.dy, a.dz};
     rotate(n, c, -sn, d2_bar);
     // kick 2: d2 = m2 / |m2|, K3 = K2 + W/2
@@ -397,8 +418,8 @@ __global__ void sum_partials_kernel(const double* __restrict__ partials, int cou
 // (substep inputs, 6 x n per entry), then run the adjoint back through it.
 __global__ void reverse_segment_kernel(Params p, const double* __restrict__ e, const double* __restrict__ arena,
                                        const uint64_t* __restrict__ id, const double* __restrict__ ckpt, int t0,
-                                       int t1, double* __restrict__ tape, double* __restrict__ adj,
-                                       double* __restrict__ grad)
+                                       int t1, double* __restrict__ tape, double* __restrict__ aux,
+                                       double* __restrict__ adj, double* __restrict__ grad)
 {
     extern __shared__ double g[];
     for (int k = threadIdx.x; k < p.n_nodes; k += blockDim.x) g[k] = 0.0;
@@ -410,15 +431,16 @@ __global__ void reverse_segment_kernel(Params p, const double* __restrict__ e, c
         int32_t end = p.ends[i];
         for (int t = t0; t < t1; ++t) {
             for (int q = 0; q < p.substeps; ++q) {
-                store(tape + (static_cast<int64_t>(t - t0) * p.substeps + q) * 6 * p.n, p.n, i, st);
-                substep(p, e, arena, id[i], t, q, st, end);
+                int64_t const k = static_cast<int64_t>(t - t0) * p.substeps + q;
+                store(tape + k * 6 * p.n, p.n, i, st);
+                substep(p, e, arena, id[i], t, q, st, end, aux + k * kAux * p.n, i);
             }
         }
         Adj a{adj[i], adj[p.n + i], adj[2 * p.n + i], adj[3 * p.n + i], adj[4 * p.n + i]};
         for (int64_t k = entries - 1; k >= 0; --k) {
             int const t = t0 + static_cast<int>(k / p.substeps), q = static_cast<int>(k % p.substeps);
             State const in = load(tape + k * 6 * p.n, p.n, i);
-            substep_adjoint(p, e, arena, id[i], t, q, in, end, a, g);
+            substep_adjoint(p, e, aux + k * kAux * p.n, i, t, q, in, end, a, g);
         }
         adj[i] = a.z;
         adj[p.n + i] = a.dx;
@@ -461,6 +483,7 @@ struct AdjointState {
     double* ckpt = nullptr;    // n_ckpt x 6 x n
     double* final_state = nullptr;
     double* tape = nullptr;    // C x substeps x 6 x n
+    double* aux = nullptr;     // C x substeps x kAux x n
     double* adj = nullptr;     // 5 x n
     double* loss = nullptr;
     double* partials = nullptr;   // one loss partial per forward block
@@ -474,6 +497,7 @@ void adjoint_free(AdjointState* s)
     if (!s) return;
     for (void* ptr : {static_cast<void*>(s->seeds), static_cast<void*>(s->w), static_cast<void*>(s->id),
                       static_cast<void*>(s->ckpt), static_cast<void*>(s->final_state), static_cast<void*>(s->tape),
+                      static_cast<void*>(s->aux),
                       static_cast<void*>(s->adj), static_cast<void*>(s->loss), static_cast<void*>(s->partials),
                       static_cast<void*>(s->ends)}) {
         if (ptr) cudaFree(ptr);
@@ -520,6 +544,7 @@ cudaError_t adjoint_stage(AdjointSetup const& in, const double* seeds6, const do
     alloc(&s->ckpt, n_ckpt * 6 * n);
     alloc(&s->final_state, 6 * n);
     alloc(&s->tape, static_cast<int64_t>(in.ckpt_every) * in.substeps * 6 * n);
+    alloc(&s->aux, static_cast<int64_t>(in.ckpt_every) * in.substeps * rrea_dev::adj::kAux * n);
     alloc(&s->adj, 5 * n);
     alloc(&s->loss, 1);
     alloc(&s->partials, blocks);
@@ -576,7 +601,7 @@ cudaError_t adjoint_backward(AdjointState& s, const double* arena, const double*
         int const t1 = t0 + p.ckpt_every < p.steps ? t0 + p.ckpt_every : p.steps;
         note_launch();
         rrea_dev::adj::reverse_segment_kernel<<<s.blocks, 128, shmem, stream>>>(
-            p, e_nodes, arena, s.id, s.ckpt + static_cast<int64_t>(c) * 6 * p.n, t0, t1, s.tape, s.adj, grad);
+            p, e_nodes, arena, s.id, s.ckpt + static_cast<int64_t>(c) * 6 * p.n, t0, t1, s.tape, s.aux, s.adj, grad);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;

@@ -857,6 +857,7 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     rrea_dev::StepConstants const sc = step_constants(ctx, step, dt_s);
     RREA_CUDA(ctx, rrea_launch::set_step_constants(sc, ctx->stream));
     if (species == RREA_SPECIES_PHOTON) RREA_CUDA(ctx, rrea_launch::photon_constants(sc, ctx->stream));
+    if (species == RREA_SPECIES_POSITRON) RREA_CUDA(ctx, rrea_launch::positron_constants(sc, ctx->stream));
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_sec_count, 0, sizeof(unsigned long long), ctx->stream));
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_transported, 0, sizeof(unsigned long long), ctx->stream));
@@ -881,6 +882,18 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     // kernel is short and loses more to the tails than it gains.
     int const chunks =
         (host && species != RREA_SPECIES_PHOTON && a.n >= kPipelineMinParticles) ? kPhaseChunks : 1;
+    // Register variant of the charged kernels: the configured residency, or,
+    // for a tile too small to fill it, the variant with the most registers
+    // per thread that still holds the whole tile in one resident wave (a
+    // positron tile of 131 k particles fills 27 of 64 warps per SM: the
+    // 64-register variant instead of the 32-register one).  Every variant runs
+    // the same arithmetic; only spills and occupancy differ.
+    int min_blocks = ctx->launch_min_blocks;
+    if (chunks == 1) {
+        int64_t const warps_per_sm = ((a.n + 31) / 32 + ctx->num_sms - 1) / ctx->num_sms;
+        int const fit = warps_per_sm <= 8 ? 2 : warps_per_sm <= 16 ? 4 : warps_per_sm <= 32 ? 8 : 16;
+        if (fit < min_blocks) min_blocks = fit;
+    }
 #ifndef RREA_STATIC_SCHEDULE
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long) * chunks, ctx->stream));
     // a resident charged tile is visited in its scheduling order (lowest
@@ -932,11 +945,11 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
             RREA_CUDA(ctx, rrea_launch::photon_step(b, blocks > 0 ? blocks : 1, ctx->launch_threads, c.periodic_z != 0,
                                                     cs));
         } else if (species == RREA_SPECIES_POSITRON) {
-            RREA_CUDA(ctx, rrea_launch::positron_step(b, blocks > 0 ? blocks : 1, ctx->launch_threads,
+            RREA_CUDA(ctx, rrea_launch::positron_step(b, blocks > 0 ? blocks : 1, ctx->launch_threads, min_blocks,
                                                       c.periodic_z != 0, cs));
         } else {
-            RREA_CUDA(ctx, rrea_launch::electron_step(b, blocks > 0 ? blocks : 1, ctx->launch_threads,
-                                                      ctx->launch_min_blocks, c.periodic_z != 0, cs));
+            RREA_CUDA(ctx, rrea_launch::electron_step(b, blocks > 0 ? blocks : 1, ctx->launch_threads, min_blocks,
+                                                      c.periodic_z != 0, cs));
         }
         if (chunks > 1) RREA_CUDA(ctx, cudaEventRecord(ctx->chunk_done[k], cs));
     }

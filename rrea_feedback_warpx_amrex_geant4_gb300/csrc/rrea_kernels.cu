@@ -2,15 +2,15 @@
 //
 //   field_prep_kernel     cell-centred total field (Maxwell + ambient face
 //                         averages), once per step
-//   electron_step_kernel  one thread per electron, full outer step
-//   positron_step_kernel  one thread per positron, full outer step
+//   electron_step_kernel  one thread per electron, full outer step (the
+//                         positron kernel lives in rrea_positron_kernels.cu)
 //   scan / scatter        orders the appended secondaries into the reference's
 //                         deterministic order (parent index, then lineage)
 #include "rrea_kernels.h"
 
 #include <atomic>
 
-#include "device/rrea_electron.cuh"
+#include "device/rrea_charged_kernel.cuh"
 
 #include <cuda_runtime.h>
 
@@ -36,63 +36,6 @@ __global__ void field_prep_kernel(int nr, int nz, const double* __restrict__ er,
         double const zh = ez[zhi] + amb_ez[zhi];
         cell_ez[c] = 0.5 * (zl + zh);
     }
-}
-
-// MinBlocks trades registers for resident warps: 2 -> up to 255 registers
-// (8 warps/SM), 4 -> 128 (16), 8 -> 64 (32), 12 -> 40 (48), 16 -> 32 (64).
-// The transport loop is latency-bound (instruction fetch and dependent
-// FP64 chains), so full residency wins despite the spills it forces.
-// NP is the chord piece capacity: 1 for absorbing z faces, 4 for periodic z.
-// Grid-stride body shared by the electron and positron kernels.
-template <int NP, bool POS>
-__device__ __forceinline__ void charged_step_body(ElectronArgs const& A)
-{
-    StepConstants const& C = c_step;
-    // one ion-pair slot per thread (the kernels launch at most 128 threads per block)
-    __shared__ IonPairSlot ion_slots[128];
-    IonPairSlot* const my_slot = ion_slots + threadIdx.x;
-    unsigned int moved = 0;
-    for_each_particle(A.n, A.work, [&](int64_t ip) {
-        if (!(A.id[ip] > 0)) {
-            if (A.segments) A.segments[ip].kind = 0;
-            if (A.sec_per_parent) A.sec_per_parent[ip] = 0;
-            if (A.diag_disposition) A.diag_disposition[ip] = -1;
-            if (A.diag_subcycles) A.diag_subcycles[ip] = 0;
-            if (A.diag_events) A.diag_events[ip] = 0;
-            return;
-        }
-        Err err;
-        uint64_t sub = 0, ev = 0;
-        uint32_t lineage = 0;
-        ++moved;
-        if (A.segments) A.segments[ip].kind = 0;
-        IonPairCache ion_pairs;
-        ion_pairs.init(my_slot, POS ? 0.0 : 0.5 * C.cfg.low_energy_cutoff_eV, C.tix.w_air_eV_per_pair);
-        int const disp = transport_charged<NP, POS>(C, A, ip, sub, ev, lineage, ion_pairs, err);
-        ion_pairs.flush(C, A.cells);
-        // Every record this particle appended carries a lineage below this
-        // count, so the ordering scan/scatter stays in bounds on every path.
-        if (A.sec_per_parent) A.sec_per_parent[ip] = lineage;
-        if (err.code) record_failure(A, err.code, ip);
-        if (A.diag_disposition) A.diag_disposition[ip] = disp;
-        if (A.diag_subcycles) A.diag_subcycles[ip] = sub;
-        if (A.diag_events) A.diag_events[ip] = ev;
-    }, A.order);
-    // warp-aggregated count of transported particles
-    unsigned int const warp_total = __reduce_add_sync(0xffffffffu, moved);
-    if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(A.transported, static_cast<unsigned long long>(warp_total));
-}
-
-template <int MinBlocks, int NP>
-__global__ void __launch_bounds__(128, MinBlocks) electron_step_kernel(const __grid_constant__ ElectronArgs A)
-{
-    charged_step_body<NP, false>(A);
-}
-
-template <int MinBlocks, int NP>
-__global__ void __launch_bounds__(128, MinBlocks) positron_step_kernel(const __grid_constant__ ElectronArgs A)
-{
-    charged_step_body<NP, true>(A);
 }
 
 // The table-driven log (which 0) or exp (which 1) next to the CUDA
@@ -239,18 +182,6 @@ cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int th
     case 12: rrea_dev::electron_step_kernel<12, 1><<<blocks, threads, 0, stream>>>(args); break;
     case 16: rrea_dev::electron_step_kernel<16, 1><<<blocks, threads, 0, stream>>>(args); break;
     default: rrea_dev::electron_step_kernel<2, 1><<<blocks, threads, 0, stream>>>(args); break;
-    }
-    return cudaGetLastError();
-}
-
-cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, bool periodic,
-                          cudaStream_t stream)
-{
-    note_launch();
-    if (periodic) {
-        rrea_dev::positron_step_kernel<16, RREA_ARENA_MAX_PIECES><<<blocks, threads, 0, stream>>>(args);
-    } else {
-        rrea_dev::positron_step_kernel<16, 1><<<blocks, threads, 0, stream>>>(args);
     }
     return cudaGetLastError();
 }

@@ -35,7 +35,11 @@ cudaError_t field_prep(int nr, int nz, const double* er, const double* ez, const
                        double* cell_er, double* cell_ez, cudaStream_t stream);
 cudaError_t electron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, int min_blocks, bool periodic,
                           cudaStream_t stream);
-cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, bool periodic,
+// Positron phase (rrea_positron_kernels.cu): its own constant bank, set
+// once per phase before its launches; min_blocks picks the register variant
+// as for electrons (2, 4, 8 or 16 resident 128-thread blocks per SM).
+cudaError_t positron_constants(rrea_dev::StepConstants const& sc, cudaStream_t stream);
+cudaError_t positron_step(rrea_dev::ElectronArgs const& args, int blocks, int threads, int min_blocks, bool periodic,
                           cudaStream_t stream);
 // Photon phase (rrea_photon_kernels.cu): its own constant bank, set once
 // per phase before its launches.

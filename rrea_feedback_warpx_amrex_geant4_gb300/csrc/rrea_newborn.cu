@@ -12,9 +12,11 @@ namespace {
 
 // Resident blocks of 128 threads per SM the newborn kernels are compiled
 // for.  A drain holds few items, each a long dependent chain, so the goal is
-// one wave with the fewest spills, not full residency.
+// one wave with the fewest spills, not full residency (4 blocks, 128
+// registers, measured within noise of 8 blocks, 64 registers, on the bench
+// step).
 #ifndef RREA_NEWBORN_MIN_BLOCKS
-#define RREA_NEWBORN_MIN_BLOCKS 8
+#define RREA_NEWBORN_MIN_BLOCKS 4
 #endif
 
 // SPECIES 1 positron, 2 photon, 0 every other species id (the reference

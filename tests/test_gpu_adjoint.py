@@ -26,7 +26,7 @@ the runaway threshold at 8 MeV (50 keV wide) and the crossing plane at 12 m
   * forward: final K and z within 1e-11 relative of the numpy restatement
     (the device's exp/log/sin/cos against numpy's);
   * autograd: torch's backward through the Function returns the adjoint;
-  * cost: the reverse pass (recomputation included) within 4x the forward."""
+  * cost: the reverse pass (recomputation included) within 3x the forward."""
 import time
 
 import numpy as np
@@ -114,7 +114,7 @@ def test_autograd_function_and_cost(problem):
         prob.backward(e)
     t_bwd = (time.perf_counter() - t0) / 3
     print(f"forward {1e3 * t_fwd:.2f} ms, reverse {1e3 * t_bwd:.2f} ms ({t_bwd / t_fwd:.2f}x)")
-    assert t_bwd <= 4.0 * t_fwd
+    assert t_bwd <= 3.0 * t_fwd
 
 
 # ---- numpy restatement of the differentiated model (test oracle) ------------
