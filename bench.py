@@ -69,6 +69,7 @@ def parse():
     p.add_argument("--population", type=int, default=1 << 21)
     p.add_argument("--cpu-baseline-steps", type=int, default=3)
     p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-warmup", type=int, default=1, help="untimed drop-in steps before the timed e2e steps")
     p.add_argument("--c0-steps", type=int, default=1000)
     p.add_argument("--ensemble-scale", type=float, default=0.05,
                    help="duration scale of the batched 64-instance ensemble line (0: skip it)")
@@ -406,18 +407,31 @@ def run_gb300(args, rank, world, local):
     pp = fetched(gpu.SPECIES_POSITRON, ctx.fetch_positrons)
     rec = gpu.SECONDARY_DTYPE.itemsize
 
+    e2e_calls = {}
+
+    e2e_kernels = {}
+
+    def timed(name, fn, *a, **kw):
+        t = time.perf_counter()
+        out = fn(*a, **kw)
+        e2e_calls[name] = e2e_calls.get(name, 0.0) + time.perf_counter() - t
+        if name.startswith("apply_"):
+            # the phase's device time, uploads of a chunked tile included
+            e2e_kernels[name] = e2e_kernels.get(name, 0.0) + ctx.last_step_stats()[2] / 1000.0
+        return out
+
     def e2e_step(step):
         """The overlay's step through the drop-in entry points: Apply's three
         phases on host tiles, then DrainAndCommitSecondaries on their host
         secondaries, then the coupled fluid and field update."""
         ctx.reset_current()
         ctx.reset_sources()
-        sec_e = ctx.apply_electrons(pe, step, DT_S, want_secondaries=True)
-        sec_g = ctx.apply_photons(pg, step, DT_S, want_secondaries=True)
-        sec_p = ctx.apply_positrons(pp, step, DT_S, want_secondaries=True)
+        sec_e = timed("apply_electrons", ctx.apply_electrons, pe, step, DT_S, want_secondaries=True)
+        sec_g = timed("apply_photons", ctx.apply_photons, pg, step, DT_S, want_secondaries=True)
+        sec_p = timed("apply_positrons", ctx.apply_positrons, pp, step, DT_S, want_secondaries=True)
         pending = np.concatenate([sec_e, sec_g, sec_p])
-        surv = ctx.drain_secondaries(pending, step, DT_S)
-        distributed.exchange_and_advance_coupled(ctx, dist, DT_S)
+        surv = timed("drain_secondaries", ctx.drain_secondaries, pending, step, DT_S)
+        timed("field_update", distributed.exchange_and_advance_coupled, ctx, dist, DT_S)
         return len(pending), len(surv)
 
     e2e_moved = 0
@@ -425,7 +439,7 @@ def run_gb300(args, rank, world, local):
     sec_bytes = 0
     surv_bytes = 0
     barrier()
-    for _ in range(args.e2e_steps):
+    for i in range(args.e2e_warmup + args.e2e_steps):
         # photons: the host captures the start and pushes (WarpX's part of the step)
         for f in ("r", "z", "theta", "ux", "uy", "uz"):
             np.copyto(pg["prev_" + f], pg[f])
@@ -433,11 +447,15 @@ def run_gb300(args, rank, world, local):
         live = int((pe["id"] > 0).sum()) + int((pg["id"] > 0).sum()) + int((pp["id"] > 0).sum())
         t0 = time.perf_counter()
         n_pending, n_surv = e2e_step(step)
+        step += 1
+        if i < args.e2e_warmup:
+            e2e_calls.clear()
+            e2e_kernels.clear()
+            continue  # first use of the drop-in path's buffers, untimed
         e2e_t += time.perf_counter() - t0
         e2e_moved += live
         sec_bytes += n_pending * rec
         surv_bytes += n_surv * rec
-        step += 1
     e2e_value = e2e_moved / e2e_t if e2e_t > 0 else None
     k = max(args.e2e_steps, 1)
     tiles_n = len(pe["id"]) + len(pg["id"]) + len(pp["id"])
@@ -521,7 +539,11 @@ def run_gb300(args, rank, world, local):
             "data": DATA,
             "config": workload_config(n, world),
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
+                    "d2h_bytes_per_step": d2h, "steps": args.e2e_steps, "warmup": args.e2e_warmup,
+                    "ms_per_step": 1000.0 * e2e_t / max(args.e2e_steps, 1),
+                    "calls_ms_per_step": {k: 1000.0 * v / max(args.e2e_steps, 1) for k, v in e2e_calls.items()},
+                    "phase_device_ms_per_step": {k: 1000.0 * v / max(args.e2e_steps, 1)
+                                                 for k, v in e2e_kernels.items()},
                     "path": "rrea_gpu_apply_electrons/_photons/_positrons (pinned host tiles -> HBM -> host), "
                             "rrea_gpu_drain_secondaries (host records in, survivors out), "
                             "rrea_gpu_current_device + rrea_gpu_fluid_take_sources + "

@@ -33,7 +33,10 @@ constexpr int kSpecies = 3;
 // Chunks of a drop-in phase call whose upload overlaps the compute of the
 // chunks before it, and the tile size from which that pays.
 constexpr int kPhaseChunks = 4;
-constexpr int64_t kPipelineMinParticles = 1 << 18;
+#ifndef RREA_PIPELINE_MIN_PARTICLES
+#define RREA_PIPELINE_MIN_PARTICLES (1LL << 18)
+#endif
+constexpr int64_t kPipelineMinParticles = RREA_PIPELINE_MIN_PARTICLES;
 
 // Device SoA of one species: r, z, theta, ux, uy, uz, w, prev_r, prev_z,
 // prev_theta, prev_ux, prev_uy, prev_uz, then id and cpu.
@@ -64,14 +67,11 @@ public:
     {
         size_t cap = 16;
         while (cap < 2 * expected) cap <<= 1;
-        if (cap > keys_.size()) {
-            keys_.assign(cap, 0);
-            species_.assign(cap, 0);
-            slots_.assign(cap, 0);
-            stamp_.assign(cap, 0);
+        if (cap > entries_.size()) {
+            entries_.assign(cap, Entry{});
             epoch_ = 0;
         }
-        mask_ = keys_.size() - 1;
+        mask_ = entries_.size() - 1;
         ++epoch_;
     }
     // slot of (key, species); `fresh` is the slot a new root receives
@@ -82,26 +82,28 @@ public:
         h *= 0xff51afd7ed558ccdULL;
         h ^= h >> 33;
         for (size_t i = static_cast<size_t>(h) & mask_;; i = (i + 1) & mask_) {
-            if (stamp_[i] != epoch_) {
-                keys_[i] = key;
-                species_[i] = species;
-                slots_[i] = fresh;
-                stamp_[i] = epoch_;
+            Entry& e = entries_[i];
+            if (e.stamp != epoch_) {
+                e = Entry{key, epoch_, species, fresh};
                 inserted = true;
                 return fresh;
             }
-            if (keys_[i] == key && species_[i] == species) {
+            if (e.key == key && e.species == species) {
                 inserted = false;
-                return slots_[i];
+                return e.slot;
             }
         }
     }
 
 private:
-    std::vector<uint64_t> keys_;
-    std::vector<int32_t> species_;
-    std::vector<uint32_t> slots_;
-    std::vector<uint64_t> stamp_;
+    // one 24-byte entry per bucket: a probe touches one cache line
+    struct Entry {
+        uint64_t key = 0;
+        uint64_t stamp = 0;  // epoch of the drain that filled it; older = empty
+        int32_t species = 0;
+        uint32_t slot = 0;
+    };
+    std::vector<Entry> entries_;
     uint64_t epoch_ = 0;
     size_t mask_ = 0;
 };
@@ -120,6 +122,7 @@ struct rrea_gpu_ctx {
     // side streams and events that let the drain's species kernels overlap
     cudaStream_t side[2] = {nullptr, nullptr};
     cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t roots_ev = nullptr;  // the initial FIFO items' roots have reached the host
     cudaEvent_t join_ev[2] = {nullptr, nullptr};
     int num_sms = 0;
 
@@ -351,6 +354,7 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         }
     }
     if (cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bail(RREA_GPU_ERR_CUDA);
+    if (cudaEventCreateWithFlags(&ctx->roots_ev, cudaEventDisableTiming) != cudaSuccess) return bail(RREA_GPU_ERR_CUDA);
     for (int k = 0; k < kPhaseChunks; ++k) {
         if (cudaEventCreateWithFlags(&ctx->chunk_up[k], cudaEventDisableTiming) != cudaSuccess
             || cudaEventCreateWithFlags(&ctx->chunk_done[k], cudaEventDisableTiming) != cudaSuccess) {
@@ -491,6 +495,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
         if (ctx->join_ev[k]) cudaEventDestroy(ctx->join_ev[k]);
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->roots_ev) cudaEventDestroy(ctx->roots_ev);
     for (int k = 0; k < kPhaseChunks; ++k) {
         if (ctx->chunk_up[k]) cudaEventDestroy(ctx->chunk_up[k]);
         if (ctx->chunk_done[k]) cudaEventDestroy(ctx->chunk_done[k]);
@@ -896,19 +901,22 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
     }
 #ifndef RREA_STATIC_SCHEDULE
     RREA_CUDA(ctx, cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long) * chunks, ctx->stream));
-    // a resident charged tile is visited in its scheduling order (lowest
-    // |u| first): warps then hold particles of similar substep counts
-    if (!host && species != RREA_SPECIES_PHOTON && ctx->schedule_order && a.n >= kScheduleMinParticles) {
-        RREA_CUDA(ctx, rrea_launch::cost_order(a.ux, a.uy, a.uz, a.id, a.n, ctx->d_cost_scratch, ctx->d_alive,
-                                               ctx->num_sms * 4, ctx->stream));
-        a.order = ctx->d_alive;
-    }
 #endif
     RREA_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
     if (host && chunks == 1) {
         rrea_gpu_status const s = upload_range(ctx, st, host, 0, a.n, ctx->stream);
         if (s != RREA_GPU_OK) return s;
     }
+#ifndef RREA_STATIC_SCHEDULE
+    // a charged tile on the device in one piece is visited in its
+    // scheduling order (lowest |u| first): warps then hold particles of
+    // similar substep counts
+    if (chunks == 1 && species != RREA_SPECIES_PHOTON && ctx->schedule_order && a.n >= kScheduleMinParticles) {
+        RREA_CUDA(ctx, rrea_launch::cost_order(a.ux, a.uy, a.uz, a.id, a.n, ctx->d_cost_scratch, ctx->d_alive,
+                                               ctx->num_sms * 4, ctx->stream));
+        a.order = ctx->d_alive;
+    }
+#endif
     if (chunks > 1) {
         RREA_CUDA(ctx, cudaStreamWaitEvent(ctx->side[0], ctx->ev_start, 0));
         RREA_CUDA(ctx, cudaStreamWaitEvent(ctx->side[1], ctx->ev_start, 0));
@@ -1188,27 +1196,33 @@ rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t
     // free lineage of slot s
     std::vector<uint32_t> slot(static_cast<size_t>(n_initial));
     std::vector<uint64_t> next;
-    {
-        if (n_initial > ctx->roots_cap) {
-            RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            dfree(ctx->d_roots);
-            if (ctx->h_roots) cudaFreeHost(ctx->h_roots);
-            ctx->d_roots = nullptr;
-            ctx->h_roots = nullptr;
-            ctx->roots_cap = 0;
-            int64_t const cap = std::max<int64_t>(n_initial, 2 * ctx->roots_cap);
-            RREA_CUDA(ctx, dalloc(&ctx->d_roots, static_cast<size_t>(2 * cap)));
-            RREA_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&ctx->h_roots),
-                                          static_cast<size_t>(2 * cap) * sizeof(unsigned long long)));
-            ctx->roots_cap = cap;
-        }
-        if (n_initial > 0) {
-            RREA_CUDA(ctx, rrea_launch::gather_roots(ctx->d_fifo, n_initial, ctx->d_roots, ctx->stream));
-            RREA_CUDA(ctx, cudaMemcpyAsync(ctx->h_roots, ctx->d_roots,
-                                           static_cast<size_t>(2 * n_initial) * sizeof(unsigned long long),
-                                           cudaMemcpyDeviceToHost, ctx->stream));
-            RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        }
+    if (n_initial > ctx->roots_cap) {
+        RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        int64_t const cap = std::max<int64_t>(n_initial, 2 * ctx->roots_cap);
+        dfree(ctx->d_roots);
+        if (ctx->h_roots) cudaFreeHost(ctx->h_roots);
+        ctx->d_roots = nullptr;
+        ctx->h_roots = nullptr;
+        ctx->roots_cap = 0;
+        RREA_CUDA(ctx, dalloc(&ctx->d_roots, static_cast<size_t>(2 * cap)));
+        RREA_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&ctx->h_roots),
+                                      static_cast<size_t>(2 * cap) * sizeof(unsigned long long)));
+        ctx->roots_cap = cap;
+    }
+    if (n_initial > 0) {
+        RREA_CUDA(ctx, rrea_launch::gather_roots(ctx->d_fifo, n_initial, ctx->d_roots, ctx->stream));
+        RREA_CUDA(ctx, cudaMemcpyAsync(ctx->h_roots, ctx->d_roots,
+                                       static_cast<size_t>(2 * n_initial) * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+        RREA_CUDA(ctx, cudaEventRecord(ctx->roots_ev, ctx->stream));
+    }
+    // The root table is built on the host while the first chunk's newborn
+    // kernels run: only the lineages of that chunk's children need it.
+    bool roots_built = false;
+    auto build_roots = [&]() -> rrea_gpu_status {
+        roots_built = true;
+        if (n_initial <= 0) return RREA_GPU_OK;
+        RREA_CUDA(ctx, cudaEventSynchronize(ctx->roots_ev));
         unsigned long long const* roots = ctx->h_roots;
         RootSlots& table = ctx->root_slots;
         table.reset(static_cast<size_t>(n_initial));
@@ -1228,7 +1242,8 @@ rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t
             slot[static_cast<size_t>(i)] = s;
             next[s] = std::max<uint64_t>(next[s], lin + 1U);
         }
-    }
+        return RREA_GPU_OK;
+    };
     std::vector<uint32_t> counts;
     std::vector<uint64_t> lineage;
     int64_t cursor = 0, tail = n_initial;
@@ -1267,6 +1282,10 @@ rrea_gpu_status drain_fifo(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t
         counts.resize(static_cast<size_t>(chunk));
         RREA_CUDA(ctx, cudaMemcpyAsync(counts.data(), ctx->d_sec_per_parent, static_cast<size_t>(chunk) * sizeof(uint32_t),
                                        cudaMemcpyDeviceToHost, ctx->stream));
+        if (!roots_built) {
+            s = build_roots();
+            if (s != RREA_GPU_OK) return s;
+        }
         RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (status != 0) {
             return fail(ctx, static_cast<rrea_gpu_status>(status),

@@ -379,6 +379,9 @@ class RreaGpuContext:
         self.lib = load_library()
         self.config = config
         self.capacity = int(capacity)
+        # the drop-in phases' secondaries land here (reused: its pages are
+        # mapped once, not on every call); callers get a copy of the filled part
+        self._sec_buf = None
         handle = ctypes.c_void_p()
         self._check(self.lib.rrea_gpu_create(ctypes.byref(config), self.capacity, ctypes.byref(handle)), None)
         self.handle = handle
@@ -461,12 +464,15 @@ class RreaGpuContext:
     def _apply(self, fn, arrays, step, dt_s, time_s, want_secondaries):
         t = tile_struct(arrays)
         n_sec = ctypes.c_int64()
-        cap = 2 * self.capacity + 4096
-        buf = np.zeros(cap if want_secondaries else 0, dtype=SECONDARY_DTYPE)
-        ptr = ctypes.c_void_p(buf.ctypes.data) if want_secondaries else None
+        cap = 2 * self.capacity + 4096 if want_secondaries else 0
+        ptr = None
+        if want_secondaries:
+            if self._sec_buf is None or len(self._sec_buf) < cap:
+                self._sec_buf = np.empty(cap, dtype=SECONDARY_DTYPE)
+            ptr = ctypes.c_void_p(self._sec_buf.ctypes.data)
         self._check(fn(self.handle, ctypes.byref(t), int(step), float(time_s), float(dt_s), ptr, cap,
                        ctypes.byref(n_sec)))
-        return buf[: n_sec.value] if want_secondaries else n_sec.value
+        return self._sec_buf[: n_sec.value].copy() if want_secondaries else n_sec.value
 
     def apply_electrons(self, arrays, step, dt_s, time_s=0.0, want_secondaries=True):
         """Drop-in electron phase on host arrays (modified in place).
