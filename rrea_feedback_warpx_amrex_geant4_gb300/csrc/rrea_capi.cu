@@ -198,7 +198,7 @@ struct rrea_gpu_ctx {
     SpeciesTile spare;
     bool spare_ready = false;
     uint32_t* d_alive = nullptr;
-    uint32_t* d_cost_scratch = nullptr;  // histogram and cursors of the scheduling order
+    uint32_t* d_cost_scratch = nullptr;  // histogram and cursors of the scheduling order, one per chunk
     double* d_census = nullptr;          // census sums, edges and thresholds (first census call)
     double* d_rho_cells = nullptr;       // particle charge grid nr*nz (first deposit call)
     rrea_launch::PopulationWork* pop_work = nullptr;  // population-control plan scratch (first use)
@@ -408,7 +408,8 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
         && dalloc(&ctx->d_diag_disp, n) == cudaSuccess && dalloc(&ctx->d_status, 1) == cudaSuccess
         && dalloc(&ctx->d_fail_index, 1) == cudaSuccess && dalloc(&ctx->d_transported, 1) == cudaSuccess
         && dalloc(&ctx->d_alive, n) == cudaSuccess && dalloc(&ctx->d_child_lineage, nsec) == cudaSuccess
-        && dalloc(&ctx->d_cost_scratch, static_cast<size_t>(rrea_launch::cost_order_scratch_elems())) == cudaSuccess
+        && dalloc(&ctx->d_cost_scratch,
+                  static_cast<size_t>(kPhaseChunks) * rrea_launch::cost_order_scratch_elems()) == cudaSuccess
         && dalloc(&ctx->d_invalid, 1) == cudaSuccess && dalloc(&ctx->d_work, kPhaseChunks) == cudaSuccess
         && cudaEventCreate(&ctx->ev_start) == cudaSuccess && cudaEventCreate(&ctx->ev_stop) == cudaSuccess;
     if (!ok) return bail(RREA_GPU_ERR_CUDA);
@@ -945,6 +946,14 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
         if (b.diag_disposition) b.diag_disposition += off;
 #ifndef RREA_STATIC_SCHEDULE
         b.work = ctx->d_work + k;
+        // a chunk of a drop-in tile is visited in its own scheduling order
+        // (chunk-local indices at d_alive + off), built once the chunk has landed
+        if (chunks > 1 && species != RREA_SPECIES_PHOTON && ctx->schedule_order && len >= kScheduleMinParticles) {
+            RREA_CUDA(ctx, rrea_launch::cost_order(b.ux, b.uy, b.uz, b.id, len,
+                                                   ctx->d_cost_scratch + k * rrea_launch::cost_order_scratch_elems(),
+                                                   ctx->d_alive + off, ctx->num_sms * 4, cs));
+            b.order = ctx->d_alive + off;
+        }
 #endif
         int64_t const want = (len + ctx->launch_threads - 1) / ctx->launch_threads;
         int64_t const cap = static_cast<int64_t>(ctx->num_sms) * ctx->launch_blocks_per_sm * (128 / ctx->launch_threads);
