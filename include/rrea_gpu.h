@@ -383,6 +383,31 @@ rrea_gpu_status rrea_gpu_population_thin_resident(rrea_gpu_ctx* ctx, int32_t spe
 rrea_gpu_status rrea_gpu_population_split_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t target,
                                                   double split_min_weight, int64_t* added);
 
+/*
+ * Weight-doubling merge above the cap, for a resident species tile.  NO
+ * COUNTERPART IN THE REFERENCE: above its cap the overlay either aborts
+ * (strict_abort_v1, O/RreaCouplingPopulation.cpp:100-146) or thins
+ * (adaptive_resample_v1, above); the scale-up and profiled-atmosphere
+ * cases ask for a merge that doubles weights instead, validated
+ * statistically.
+ *
+ * When the tile holds more than `target` valid particles, they are grouped
+ * by (cell-centred grid cell of the position, the quarter octave of |u|^2,
+ * the sign of u_z) and, inside a group, consecutive particles in tile order
+ * pair up.  R = min(live - target, pairs) pairs merge, spread evenly over
+ * the pairs in group order (pair j when floor((j+1) R / P) > floor(j R / P)).
+ * A merging pair (a, b) keeps a with probability w_a / (w_a + w_b), else b,
+ * with a counter-hash uniform of (rng_seed, species, step, the two stream
+ * keys |id| ^ cpu << 40); the kept particle carries w_a + w_b and the other
+ * is invalidated (negated id: rrea_gpu_compact_resident removes it).  Every
+ * weighted sum keeps its expectation, each cell's weight is kept exactly
+ * (up to the rounding of w_a + w_b), and the same call gives the same result
+ * on the same tile.  stats (may be NULL) receives 5 values: live particles,
+ * groups, pairs, requested merges, merged pairs.  Not in ensemble mode.
+ */
+rrea_gpu_status rrea_gpu_population_merge_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t target, int32_t step,
+                                                  int64_t* stats);
+
 /* Number of particles (valid or not) in a resident species tile.  NO COUNTERPART IN THE
  * REFERENCE (WarpX containers know their own size). */
 rrea_gpu_status rrea_gpu_resident_count(rrea_gpu_ctx* ctx, int32_t species, int64_t* n);

@@ -87,10 +87,12 @@ class AvalancheRun:
 
     def __init__(self, ctx, electrons, photons=None, positrons=None, feedback=False, field_substeps=2,
                  population_target=None, split_min_weight=0.0, control_interval=1, controller_salt=0,
-                 fluid=False):
+                 fluid=False, merge_cap=None):
         """feedback: the field follows the step's current; fluid (with
         feedback): through the coupled carrier-fluid + Maxwell step (the
-        context's fluid must be configured) instead of the kinetic-only one."""
+        context's fluid must be configured) instead of the kinetic-only one;
+        merge_cap: the weight-doubling merge of every species tile above
+        that many live particles after each commit."""
         self.ctx = ctx
         self.feedback = feedback
         self.fluid = fluid
@@ -103,6 +105,8 @@ class AvalancheRun:
         self.controller_salt = controller_salt
         self.thinned = 0
         self.split = 0
+        self.merge_cap = merge_cap
+        self.merged = 0
         empty = workloads.make_electrons("uniform_c0", 0)
         ctx.stage_electrons(electrons)
         ctx.stage_photons(photons if photons is not None else empty)
@@ -135,6 +139,10 @@ class AvalancheRun:
                 self.thinned += ctx.population_thin(sp, self.population_target, self.step,
                                                     self.controller_salt)["removed"]
         ctx.commit_survivors_resident()
+        if self.merge_cap:
+            # weight-doubling merge above the cap (merged partners leave at the compaction)
+            for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON, gpu.SPECIES_PHOTON):
+                self.merged += ctx.population_merge(sp, self.merge_cap, self.step)["merged"]
         for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON, gpu.SPECIES_PHOTON):
             ctx.compact_resident(sp)
         if control and self.split_min_weight > 0.0:
@@ -185,7 +193,7 @@ class AvalancheRun:
             "particle_steps": moved_total, "fifo_items": fifo_total, "wall_s": wall,
             "particle_steps_per_s": moved_total / wall if wall > 0 else 0.0,
             "kernel_launches": launches, "steps": steps,
-            "population_thinned": self.thinned, "population_split": self.split,
+            "population_thinned": self.thinned, "population_split": self.split, "population_merged": self.merged,
         }
 
 
@@ -362,6 +370,8 @@ def main():
     p.add_argument("--population-target", type=int, default=0,
                    help="adaptive_resample_v1 e-/e+ macro target (0: no population control)")
     p.add_argument("--split-min-weight", type=float, default=0.0)
+    p.add_argument("--merge-cap", type=int, default=0,
+                   help="weight-doubling merge of each species above this many live particles (0: off)")
     p.add_argument("--json", default=None)
     p.add_argument("--csv", default=None)
     p.add_argument("--planes", default=None, help="comma-separated plane z [m] of the crossing diagnostic")
@@ -383,7 +393,7 @@ def main():
             amb[:] = -float(a.field)
         planes = PlaneFluxCsv(a.plane_csv, z, a.plane_interval, a.plane_core_radius, amb)
     res = AvalancheRun(ctx, seeds, population_target=a.population_target or None,
-                       split_min_weight=a.split_min_weight).run(a.steps, census_every=a.census_every,
+                       split_min_weight=a.split_min_weight, merge_cap=a.merge_cap or None).run(a.steps, census_every=a.census_every,
                                                                 plane_csv=planes)
     p_case = c0_like_case(a.field, a.case)
     res["case"] = a.case
@@ -402,7 +412,8 @@ def main():
             f.write(text)
     print(json.dumps({k: res[k] for k in ("case", "seeds", "steps", "multiplication", "particle_steps", "wall_s",
                                           "particle_steps_per_s", "kernel_launches", "avalanche_length_m",
-                                          "coleman_dwyer_length_m", "population_thinned", "population_split")}))
+                                          "coleman_dwyer_length_m", "population_thinned", "population_split",
+                                          "population_merged")}))
     ctx.close()
 
 

@@ -2067,6 +2067,45 @@ rrea_gpu_status rrea_gpu_population_split_resident(rrea_gpu_ctx* ctx, int32_t sp
     return RREA_GPU_OK;
 }
 
+rrea_gpu_status rrea_gpu_population_merge_resident(rrea_gpu_ctx* ctx, int32_t species, int64_t target, int32_t step,
+                                                  int64_t* stats)
+{
+    if (!ctx || species < 0 || species >= kSpecies || target < 0) {
+        return fail(ctx, RREA_GPU_ERR_ARGUMENT, "merge takes a species and a target >= 0");
+    }
+    if (ctx->n_instances > 0) return fail(ctx, RREA_GPU_ERR_ARGUMENT, "the merge has no ensemble form");
+    rrea_gpu_config const& c = ctx->cfg;
+    SpeciesTile& st = ctx->tiles[species];
+    rrea_launch::MergeInput in{};
+    in.r = st.d[0];
+    in.z = st.d[1];
+    in.ux = st.d[3];
+    in.uy = st.d[4];
+    in.uz = st.d[5];
+    in.w = st.d[6];
+    in.id = st.id;
+    in.cpu = st.cpu;
+    in.n_tile = st.n;
+    in.species = species;
+    in.nr = c.nr;
+    in.nz = c.nz;
+    in.r_lo = c.r_lo;
+    in.z_lo = c.z_lo;
+    in.dr = (c.r_hi - c.r_lo) / c.nr;
+    in.dz = (c.z_hi - c.z_lo) / c.nz;
+    in.target = target;
+    in.rng_seed = c.rng_seed;
+    in.step = step;
+    rrea_launch::MergeStats ms{};
+    RREA_CUDA(ctx, rrea_launch::population_merge(in, ctx->pop_work, ms, ctx->stream));
+    if (ms.status != 0) return fail(ctx, static_cast<rrea_gpu_status>(ms.status), "merge plan exceeds its index range");
+    if (stats) {
+        int64_t const v[5] = {ms.live, ms.groups, ms.pairs, ms.requested, ms.merged};
+        std::copy(v, v + 5, stats);
+    }
+    return RREA_GPU_OK;
+}
+
 rrea_gpu_status rrea_gpu_count_live(rrea_gpu_ctx* ctx, int32_t species, int64_t* live)
 {
     if (!ctx || !live || species < 0 || species >= kSpecies) return RREA_GPU_ERR_ARGUMENT;

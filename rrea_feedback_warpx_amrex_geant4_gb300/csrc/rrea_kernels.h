@@ -154,6 +154,27 @@ struct PopulationStats {
 };
 struct PopulationWork;
 void population_work_free(PopulationWork* work);
+// Weight-doubling merge of a resident tile above `target` live particles
+// (rrea_population.cu): pairs inside (cell, |u| octave, u_z sign) groups,
+// R = min(live - target, pairs) of them merged, evenly spread.
+struct MergeInput {
+    const double *r, *z, *ux, *uy, *uz;
+    double* w;
+    int64_t* id;
+    const int32_t* cpu;
+    int64_t n_tile;
+    int species;
+    int64_t nr, nz;
+    double r_lo, z_lo, dr, dz;
+    int64_t target;
+    uint64_t rng_seed;
+    int64_t step;
+};
+struct MergeStats {
+    int64_t live, groups, pairs, requested, merged;
+    int status;
+};
+cudaError_t population_merge(MergeInput const& in, PopulationWork*& work, MergeStats& stats, cudaStream_t stream);
 // Global CIC thinning plan and its application (nothing is applied unless
 // status is 0).
 cudaError_t population_thin(PopulationInput const& in, PopulationWork*& work, PopulationStats& stats, int blocks,

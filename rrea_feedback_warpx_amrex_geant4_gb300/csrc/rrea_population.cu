@@ -457,6 +457,102 @@ int blocks_for(int64_t n)
     return static_cast<int>(b < 1 ? 1 : (b > 65535 ? 65535 : b));
 }
 
+// ---------------------------------------------------------------------------
+// Weight-doubling merge above the cap (a policy of this library: the
+// reference has strict_abort_v1 and adaptive_resample_v1 only).  Live
+// particles are grouped by (cell, |u| quarter octave, sign of u_z); inside a
+// group, in tile order, consecutive members pair up; an evenly spread subset
+// of the pairs merges, each pair into one particle that carries both weights,
+// which member survives being drawn with probability proportional to its
+// weight.  Any weighted sum of the particles keeps its expectation, and the
+// weight of every cell is kept exactly (up to the rounding of w_a + w_b).
+
+// group key: bits 34..57 the cell row z, 14..33 the cell column r, 1..13 the
+// |u|^2 quarter octave (its double's exponent and two leading mantissa
+// bits), bit 0 the sign of u_z
+__global__ void merge_keys_kernel(rrea_launch::MergeInput in, const int64_t* __restrict__ members, int64_t n,
+                                  uint64_t* __restrict__ keys, uint32_t* __restrict__ perm)
+{
+    for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < n;
+         k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t const i = members[k];
+        double const fr = (in.r[i] - in.r_lo) / in.dr;
+        double const fz = (in.z[i] - in.z_lo) / in.dz;
+        int64_t ir = fr >= 0.0 ? static_cast<int64_t>(fr) : 0;
+        int64_t iz = fz >= 0.0 ? static_cast<int64_t>(fz) : 0;
+        ir = ir < in.nr ? ir : in.nr - 1;
+        iz = iz < in.nz ? iz : in.nz - 1;
+        double const ux = in.ux[i], uy = in.uy[i], uz = in.uz[i];
+        // |u|^2 rounded product by product and sum by sum (no contraction),
+        // so the key is reproducible off the device
+        double const u2 = __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)), __dmul_rn(uz, uz));
+        uint64_t const bin = (static_cast<uint64_t>(__double_as_longlong(u2)) >> 50) & 0x1fffULL;
+        keys[k] = (static_cast<uint64_t>(iz) << 34) | (static_cast<uint64_t>(ir) << 14) | (bin << 1)
+            | (__double_as_longlong(uz) < 0 ? 1ULL : 0ULL);
+        perm[k] = static_cast<uint32_t>(k);
+    }
+}
+
+__global__ void merge_heads_kernel(const uint64_t* __restrict__ sorted_keys, int64_t n, uint32_t* __restrict__ heads)
+{
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        heads[i] = (i == 0 || sorted_keys[i] != sorted_keys[i - 1]) ? 1u : 0u;
+    }
+}
+
+// a pair starts at every even rank of a group that has a next member
+__global__ void merge_pairs_kernel(const uint64_t* __restrict__ sorted_keys, const uint32_t* __restrict__ heads,
+                                   const int64_t* __restrict__ group_of, const int64_t* __restrict__ begin, int64_t n,
+                                   uint32_t* __restrict__ pair_head)
+{
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t const g = group_of[i] + heads[i] - 1;
+        int64_t const rank = i - begin[g];
+        pair_head[i] = ((rank & 1) == 0 && i + 1 < n && sorted_keys[i + 1] == sorted_keys[i]) ? 1u : 0u;
+    }
+}
+
+// The uniform of one pair: counter hashing of (seed, species, step, the two
+// particles' stream keys |id| ^ cpu << 40) with splitmix64.
+__device__ __forceinline__ double merge_uniform(uint64_t seed, int species, int64_t step, uint64_t ka, uint64_t kb)
+{
+    uint64_t h = splitmix64(seed ^ 0x6d65726765ULL ^ (static_cast<uint64_t>(species) << 56));
+    h = splitmix64(h ^ static_cast<uint64_t>(step));
+    h = splitmix64(h ^ ka);
+    h = splitmix64(h ^ kb);
+    return (static_cast<double>(h >> 11) + 0.5) * 0x1.0p-53;
+}
+
+// pair j (in sorted order) merges when floor((j + 1) R / P) > floor(j R / P):
+// R of the P pairs, spread evenly over the groups
+__global__ void merge_apply_kernel(rrea_launch::MergeInput in, const int64_t* __restrict__ members, const uint32_t* __restrict__ perm,
+                                   const uint32_t* __restrict__ pair_head, const int64_t* __restrict__ pair_ordinal,
+                                   int64_t n, uint64_t pairs, uint64_t merges, unsigned long long* __restrict__ merged)
+{
+    unsigned int done = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (!pair_head[i]) continue;
+        uint64_t const j = static_cast<uint64_t>(pair_ordinal[i]);
+        if ((j + 1) * merges / pairs == j * merges / pairs) continue;
+        int64_t const a = members[perm[i]], b = members[perm[i + 1]];
+        double const wa = in.w[a], wb = in.w[b];
+        uint64_t const ka = static_cast<uint64_t>(llabs(in.id[a])) ^ (static_cast<uint64_t>(in.cpu ? in.cpu[a] : 0) << 40);
+        uint64_t const kb = static_cast<uint64_t>(llabs(in.id[b])) ^ (static_cast<uint64_t>(in.cpu ? in.cpu[b] : 0) << 40);
+        double const u = merge_uniform(in.rng_seed, in.species, in.step, ka, kb);
+        double const sum = wa + wb;
+        bool const keep_a = u * sum < wa;
+        int64_t const keep = keep_a ? a : b, drop = keep_a ? b : a;
+        in.w[keep] = sum;
+        in.id[drop] = -in.id[drop];
+        ++done;
+    }
+    unsigned int const warp_total = __reduce_add_sync(0xffffffffu, done);
+    if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(merged, static_cast<unsigned long long>(warp_total));
+}
+
 }  // namespace
 }  // namespace rrea_dev
 
@@ -917,6 +1013,84 @@ cudaError_t population_split(rrea_dev::TileColumns const& t, int64_t n, double m
     split_scatter_kernel<<<blocks_for(n), 256, 0, s>>>(t, n, p.flags, p.offsets, first_id);
     *added = clones;
     return cudaGetLastError();
+}
+
+cudaError_t population_merge(MergeInput const& in, PopulationWork*& work, MergeStats& st, cudaStream_t s)
+{
+    using namespace rrea_dev;
+    st = MergeStats{};
+    if (in.n_tile <= 0) return cudaSuccess;
+    if (in.n_tile > INT32_MAX) {
+        st.status = RREA_GPU_ERR_CAPACITY;
+        return cudaSuccess;
+    }
+    if (!work) work = new PopulationWork{};
+    PopulationWork& p = *work;
+    cudaError_t e = ensure(p, in.n_tile);
+    if (e != cudaSuccess) return e;
+    int64_t const nt = in.n_tile;
+    note_launch();
+    flags_live_kernel<<<blocks_for(nt), 256, 0, s>>>(in.id, nt, p.flags);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = exclusive_scan_counts(p.flags, nt, p.offsets, p.scan_scratch, s)) != cudaSuccess) return e;
+    note_launch();
+    scatter_members_kernel<<<blocks_for(nt), 256, 0, s>>>(p.flags, p.offsets, nt, 0, p.members);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    int64_t last_off = 0;
+    uint32_t last_flag = 0;
+    if ((e = cudaMemcpyAsync(&last_off, p.offsets + nt - 1, sizeof(last_off), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemcpyAsync(&last_flag, p.flags + nt - 1, sizeof(last_flag), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s))) {
+        return e;
+    }
+    int64_t const n = last_off + last_flag;
+    st.live = n;
+    if (n <= in.target || n < 2) return cudaSuccess;
+    note_launch();
+    merge_keys_kernel<<<blocks_for(n), 256, 0, s>>>(in, p.members, n, p.k1, p.perm_a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    uint32_t* perm = p.perm_a;
+    uint32_t* spare = p.perm_b;
+    if ((e = sort_by(p, p.k1, perm, spare, n, s, 58)) != cudaSuccess) return e;
+    // p.kb: the keys in sorted order; groups and their first members
+    note_launch();
+    merge_heads_kernel<<<blocks_for(n), 256, 0, s>>>(p.kb, n, p.flags);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = exclusive_scan_counts(p.flags, n, p.offsets, p.scan_scratch, s)) != cudaSuccess) return e;
+    note_launch();
+    group_begin_kernel<<<blocks_for(n), 256, 0, s>>>(p.flags, p.offsets, n, p.begin);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    uint32_t* const pair_head = reinterpret_cast<uint32_t*>(p.k2);
+    note_launch();
+    merge_pairs_kernel<<<blocks_for(n), 256, 0, s>>>(p.kb, p.flags, p.offsets, p.begin, n, pair_head);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = exclusive_scan_counts(pair_head, n, p.cap_prefix, p.scan_scratch, s)) != cudaSuccess) return e;
+    int64_t groups_off = 0, pairs_off = 0;
+    uint32_t groups_flag = 0, pairs_flag = 0;
+    if ((e = cudaMemcpyAsync(&groups_off, p.offsets + n - 1, sizeof(groups_off), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemcpyAsync(&groups_flag, p.flags + n - 1, sizeof(groups_flag), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemcpyAsync(&pairs_off, p.cap_prefix + n - 1, sizeof(pairs_off), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemcpyAsync(&pairs_flag, pair_head + n - 1, sizeof(pairs_flag), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s))) {
+        return e;
+    }
+    st.groups = groups_off + groups_flag;
+    st.pairs = pairs_off + pairs_flag;
+    st.requested = std::min<int64_t>(n - in.target, st.pairs);
+    if (st.requested <= 0) return cudaSuccess;
+    if ((e = cudaMemsetAsync(p.removed, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
+    note_launch();
+    merge_apply_kernel<<<blocks_for(n), 256, 0, s>>>(in, p.members, perm, pair_head, p.cap_prefix, n,
+                                                     static_cast<uint64_t>(st.pairs),
+                                                     static_cast<uint64_t>(st.requested), p.removed);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    unsigned long long merged = 0;
+    if ((e = cudaMemcpyAsync(&merged, p.removed, sizeof(merged), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s))) {
+        return e;
+    }
+    st.merged = static_cast<int64_t>(merged);
+    return cudaSuccess;
 }
 
 }  // namespace rrea_launch

@@ -121,6 +121,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_seed_schedule_events", "rrea_gpu_seed_schedule_validate", "rrea_gpu_seed_schedule_last_error",
     "rrea_gpu_inject_seeds_resident", "rrea_gpu_thin_cic_groups", "rrea_gpu_census_resident",
     "rrea_gpu_deposit_charge_resident", "rrea_gpu_population_thin_resident", "rrea_gpu_population_split_resident",
+    "rrea_gpu_population_merge_resident",
     "rrea_gpu_default_fluid_config", "rrea_gpu_fluid_configure", "rrea_gpu_fluid_load_closure",
     "rrea_gpu_fluid_set_state", "rrea_gpu_fluid_get_state", "rrea_gpu_fluid_set_source_rates",
     "rrea_gpu_fluid_get_source_rates", "rrea_gpu_fluid_set_density_ratio", "rrea_gpu_fluid_set_closure_fields",
@@ -205,6 +206,7 @@ def load_library(path=LIB_PATH):
     lib.rrea_gpu_population_thin_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
                                                       ctypes.c_uint64, vp, ctypes.c_int64, _i64p]
     lib.rrea_gpu_population_split_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_double, _i64p]
+    lib.rrea_gpu_population_merge_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _i64p]
     lib.rrea_gpu_census_resident.argtypes = [vp, ctypes.c_int32, _D, ctypes.c_int32, _D, ctypes.c_int32, _D]
     lib.rrea_gpu_resident_count.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
@@ -623,6 +625,17 @@ class RreaGpuContext:
         self._check(self.lib.rrea_gpu_population_split_resident(self.handle, int(species), int(target),
                                                                 float(split_min_weight), ctypes.byref(added)))
         return added.value
+
+    MERGE_STATS = ("live", "groups", "pairs", "requested", "merged")
+
+    def population_merge(self, species, target, step):
+        """Weight-doubling merge of the resident tile above `target` valid
+        particles (merged particles are invalidated; compact_resident removes
+        them); returns the MERGE_STATS as a dict."""
+        stats = np.zeros(len(self.MERGE_STATS), dtype=np.int64)
+        self._check(self.lib.rrea_gpu_population_merge_resident(
+            self.handle, int(species), int(target), int(step), stats.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return dict(zip(self.MERGE_STATS, (int(v) for v in stats)))
 
     def deposit_charge(self):
         """Cell-centred CIC charge of the resident electrons (-w) and
