@@ -360,7 +360,10 @@ class PlaneFluxCsv:
 
 def main():
     p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    p.add_argument("--case", default="uniform_c0", choices=["uniform_c0"])
+    p.add_argument("--case", default="uniform_c0", choices=["uniform_c0", "scaleup_c1"])
+    p.add_argument("--feedback", action="store_true", help="the field follows the step's current")
+    p.add_argument("--fluid", action="store_true",
+                   help="with --feedback: the coupled carrier fluid (production closures) and Maxwell update")
     p.add_argument("--seeds", type=int, default=10_000)
     p.add_argument("--steps", type=int, default=4000)
     p.add_argument("--rng-seed", type=int, default=1)
@@ -383,6 +386,10 @@ def main():
 
     torch.cuda.set_device(0)
     ctx = make_context(a.case, a.capacity, a.rng_seed, a.field)
+    if a.feedback and a.fluid:
+        from . import DEFAULT_CLOSURE
+        ctx.fluid_configure(**workloads.fluid_overrides())
+        ctx.fluid_load_closure(DEFAULT_CLOSURE)
     seeds = workloads.make_electrons(a.case, a.seeds)
     planes = None
     if a.planes:
@@ -393,7 +400,8 @@ def main():
             amb[:] = -float(a.field)
         planes = PlaneFluxCsv(a.plane_csv, z, a.plane_interval, a.plane_core_radius, amb)
     res = AvalancheRun(ctx, seeds, population_target=a.population_target or None,
-                       split_min_weight=a.split_min_weight, merge_cap=a.merge_cap or None).run(a.steps, census_every=a.census_every,
+                       split_min_weight=a.split_min_weight, merge_cap=a.merge_cap or None,
+                       feedback=a.feedback, fluid=a.feedback and a.fluid).run(a.steps, census_every=a.census_every,
                                                                 plane_csv=planes)
     p_case = c0_like_case(a.field, a.case)
     res["case"] = a.case
