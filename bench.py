@@ -98,6 +98,20 @@ def read_peaks():
 TRAFFIC_RECORD = os.path.join(ROOT, "profiles", "electron_step_kernel_traffic.json")
 
 
+def read_fp64_pipe_pct():
+    """The electron kernel's FP64-pipe utilisation from the same record
+    (None when the record is absent, of another build, or lacks it)."""
+    from rrea_feedback_warpx_amrex_geant4_gb300 import build
+
+    if not os.path.exists(TRAFFIC_RECORD):
+        return None
+    with open(TRAFFIC_RECORD) as f:
+        rec = json.load(f)
+    if rec.get("source_digest") != build.source_digest():
+        return None
+    return rec.get("fp64_pipe_pct")
+
+
 def read_traffic_per_particle_step():
     """DRAM bytes (read + write) per particle-step of the electron transport
     kernel, from the ncu capture recorded for THIS build: the record carries
@@ -551,6 +565,7 @@ def run_gb300(args, rank, world, local):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic, "traffic_source": traffic_source, "kernel": "electron_step_kernel",
+                         "fp64_pipe_pct_of_peak": read_fp64_pipe_pct(),
                          "algorithmic_bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
                          "kernel_ms_per_step": kernel_ms_e / args.steps,
                          "photon_kernel": {"kernel": "photon_step_kernel", "achieved": achieved_g,

@@ -5,10 +5,11 @@ counter behind the bench line's roofline.traffic.
           electron population: K log-uniform 1-20 MeV in the -E hemisphere,
           5 m x 10 m disk, E_z = -500 kV/m, 256 x 2048 cells) and runs
           `launches` resident electron phases of 0.5 ns.  Meant to run under
-              ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+              ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum,
+                  sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active
                   --print-units base --clock-control none
                   -k regex:electron_step_kernel -s 1 -c 1 --csv --log-file <csv>
-          (one pass: nothing is saved or restored around the launch).
+          (a pass or two on this one launch of 1 M electrons).
   record  reads that CSV and writes profiles/electron_step_kernel_traffic.json:
           (read + write bytes) / n per particle-step (every staged electron is
           live in the captured launch), with the library's source digest, so
@@ -27,6 +28,8 @@ DT_S = 5.0e-10
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 RECORD = os.path.join(ROOT, "profiles", "electron_step_kernel_traffic.json")
 METRICS = ("dram__bytes_read.sum", "dram__bytes_write.sum", "gpu__time_duration.sum")
+# recorded when the capture has it (the FP64 pipe is the kernel's real bound)
+FP64_PIPE = "sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active"
 
 
 def run(n, launches, threads=128, blocks_per_sm=16):
@@ -60,7 +63,7 @@ def read_capture(path):
         if "electron_step_kernel" not in row.get("Kernel Name", ""):
             continue
         name = row.get("Metric Name")
-        if name in METRICS:
+        if name in METRICS or name == FP64_PIPE:
             values[name] = float(row["Metric Value"].replace(",", ""))
     missing = [m for m in METRICS if m not in values]
     if missing:
@@ -75,7 +78,8 @@ def record(path, n, out=RECORD, command=""):
            "electrons": n, "dram_bytes_read": v["dram__bytes_read.sum"],
            "dram_bytes_write": v["dram__bytes_write.sum"], "duration_ns": v["gpu__time_duration.sum"],
            "dram_bytes_per_particle_step": traffic / n,
-           "capture": f"one electron phase of {n} scale-up electrons under ncu (one pass), {command}".strip()}
+           "fp64_pipe_pct": v.get(FP64_PIPE),
+           "capture": f"one electron phase of {n} scale-up electrons under ncu, {command}".strip()}
     with open(out, "w") as f:
         json.dump(rec, f, indent=1)
         f.write("\n")
