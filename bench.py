@@ -26,6 +26,9 @@ one dt, its newborn residual legs included.  Synthetic seeds; no dataset.
               r,z,theta,ux,uy,uz,w,id, write r,z,theta,ux,uy,uz)
   cpu_baseline the oracle (CPU restatement, all host threads) on a bounded
               sample of the same workload
+  profiled_atmosphere  the largest case's geometry (512x4096 cells, 6-14 km,
+              density profile, altitude-dependent E_z) with an entering
+              column of 2e6 e- and 5e5 e+ and the coupled fluid update
   batched     the batched pattern: 64 independent uniform-field instances
               advanced by one set of launches per step against the same 64
               run one after another (stepping wall time, results identical)
@@ -74,6 +77,8 @@ def parse():
     p.add_argument("--ensemble-scale", type=float, default=0.05,
                    help="duration scale of the batched 64-instance ensemble line (0: skip it)")
     p.add_argument("--adjoint-steps", type=int, default=2000, help="steps of the adjoint line (0: skip it)")
+    p.add_argument("--profiled-steps", type=int, default=8,
+                   help="timed steps of the profiled-atmosphere line (0: skip it)")
     p.add_argument("--threads", type=int, default=128)
     p.add_argument("--blocks-per-sm", type=int, default=16)
     return p.parse_args()
@@ -302,6 +307,91 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def profiled_column(n_e, n_p, seed=2026):
+    """The profiled case's entering column: e- and e+ at 12 km altitude
+    (z = 6 km above the 6 km floor) over r <= 1 km, K from E^-1.5 on
+    1-100 MeV, moving down with zenith angle density ~ cos^2."""
+    from rrea_feedback_warpx_amrex_geant4_gb300 import workloads
+
+    def tile(n, s):
+        rng = np.random.default_rng(s)
+        a = 1.0 - 1.5
+        k = (1.0e6 ** a + rng.uniform(0.0, 1.0, n) * (1.0e8 ** a - 1.0e6 ** a)) ** (1.0 / a)
+        mu = rng.uniform(0.0, 1.0, n) ** (1.0 / 3.0)
+        phi = rng.uniform(0.0, 2.0 * np.pi, n)
+        sn = np.sqrt(1.0 - mu * mu)
+        u = workloads.proper_velocity(k)
+        t = workloads.make_electrons("profiled_c2", n, seed=s)
+        t["r"][:] = 1000.0 * np.sqrt(rng.uniform(0.0, 1.0, n))
+        t["theta"][:] = rng.uniform(-np.pi, np.pi, n)
+        t["z"][:] = 6000.0 - 10.0 * rng.uniform(0.0, 1.0, n)
+        t["ux"][:] = u * sn * np.cos(phi)
+        t["uy"][:] = u * sn * np.sin(phi)
+        t["uz"][:] = -u * mu
+        workloads.capture_prev(t)
+        return t
+
+    return tile(n_e, seed), tile(n_p, seed + 1)
+
+
+def profiled_line(args, gpu, workloads, distributed, tables, closure):
+    import torch
+
+    n_e, n_p = 2_000_000, 500_000
+    cfg = workloads.make_config(gpu, "profiled_c2")
+    ctx = gpu.RreaGpuContext(cfg, 4_000_000)
+    try:
+        ctx.load_tables(tables)
+        alt, dens, alt0, field = workloads.profiled_atmosphere()
+        ctx.set_field(**field)
+        ctx.set_density_profile(alt, dens, alt0, workloads.TABLE_DENSITY)
+        ctx.fluid_configure(**workloads.fluid_overrides())
+        ctx.fluid_load_closure(closure)
+        ctx.set_launch(args.threads, args.blocks_per_sm, diagnostics=False)
+        e, pos = profiled_column(n_e, n_p)
+        ctx.stage_electrons(e)
+        ctx.stage_positrons(pos)
+        ctx.stage_photons(workloads.make_electrons("profiled_c2", 0))
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        moved = 0
+        total_ms = 0.0
+        for k in range(args.warmup + args.profiled_steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            ctx.reset_current()
+            ctx.reset_sources()
+            step_moved = 0
+            for sp, fn in ((gpu.SPECIES_ELECTRON, ctx.step_electrons_resident),
+                           (gpu.SPECIES_PHOTON, ctx.step_photons_resident),
+                           (gpu.SPECIES_POSITRON, ctx.step_positrons_resident)):
+                if ctx.resident_count(sp) == 0:
+                    continue
+                fn(k, DT_S)
+                step_moved += ctx.last_step_stats()[0]
+            ctx.drain_resident(k, DT_S)
+            ctx.commit_survivors_resident()
+            for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_POSITRON, gpu.SPECIES_PHOTON):
+                ctx.compact_resident(sp)
+            distributed.exchange_and_advance_coupled(ctx, None, DT_S)
+            e1.record(stream)
+            e1.synchronize()
+            if k >= args.warmup:
+                total_ms += e0.elapsed_time(e1)
+                moved += step_moved
+        counts = [ctx.resident_count(sp) for sp in (gpu.SPECIES_ELECTRON, gpu.SPECIES_PHOTON, gpu.SPECIES_POSITRON)]
+    finally:
+        ctx.close()
+    return {"workload": "profiled atmosphere: 512x4096 cells over r 0-1 km, altitudes 6-14 km, density 1.225 "
+                        "exp(-h/7.2 km) as the transport's altitude profile, E_z 1.3 x threshold at 10 km; "
+                        f"{n_e} e- and {n_p} e+ entering at 12 km (K ~ E^-1.5 on 1-100 MeV, zenith ~ cos^2); "
+                        "three phases, drain, commit, compaction and the coupled carrier fluid + Maxwell update",
+            "value": moved / (total_ms / 1000.0), "unit": "particle-steps/s",
+            "ms_per_step": total_ms / args.profiled_steps, "steps": args.profiled_steps, "warmup": args.warmup,
+            "final_counts": {"electrons": counts[0], "photons": counts[1], "positrons": counts[2]}}
+
+
 def run_gb300(args, rank, world, local):
     import torch
 
@@ -497,6 +587,19 @@ def run_gb300(args, rank, world, local):
               "final_electrons": res["history"][-1]["electron_count"],
               "timing": "host wall clock around the steps (each step ends in a stream synchronisation)"}
 
+    # ---- the profiled atmosphere (the largest case's geometry): 512x4096
+    # cells over r 0-1 km and altitudes 6-14 km, density 1.225 exp(-h/7.2 km)
+    # bound as the transport's altitude profile, E_z peaking at 1.3 x the
+    # local threshold at 10 km, a column of 2e6 e- and 5e5 e+ entering at
+    # 12 km over r <= 1 km (K ~ E^-1.5 on 1-100 MeV, zenith ~ cos^2), with
+    # the coupled carrier fluid and field update
+    profiled = None
+    if rank == 0 and world == 1 and args.profiled_steps > 0:
+        try:
+            profiled = profiled_line(args, gpu, workloads, distributed, DEFAULT_TABLES, DEFAULT_CLOSURE)
+        except gpu.RreaGpuError as exc:  # reported in the line, the headline stands
+            profiled = {"error": str(exc)}
+
     # ---- the batched pattern: 64 independent uniform-field instances in one
     # set of launches per step against the same 64 run one after another
     # (identical per-instance results, so the statistics match exactly)
@@ -584,6 +687,7 @@ def run_gb300(args, rank, world, local):
                                        f"{args.cpu_baseline_steps} steps of the same whole kinetic step "
                                        f"({cpu_moved} particle-steps in {cpu_t:.1f} s), OpenMP chunks of 64, -O3"},
             "small_population": c0,
+            "profiled_atmosphere": profiled,
             "batched": batched,
             "adjoint": adjoint_line,
             "gpu_launches": launches,
