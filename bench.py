@@ -513,30 +513,22 @@ def run_gb300(args, rank, world, local):
 
     e2e_calls = {}
 
-    e2e_kernels = {}
-
     def timed(name, fn, *a, **kw):
         t = time.perf_counter()
         out = fn(*a, **kw)
         e2e_calls[name] = e2e_calls.get(name, 0.0) + time.perf_counter() - t
-        if name.startswith("apply_"):
-            # the phase's device time, uploads of a chunked tile included
-            e2e_kernels[name] = e2e_kernels.get(name, 0.0) + ctx.last_step_stats()[2] / 1000.0
         return out
 
     def e2e_step(step):
-        """The overlay's step through the drop-in entry points: Apply's three
-        phases on host tiles, then DrainAndCommitSecondaries on their host
-        secondaries, then the coupled fluid and field update."""
+        """The overlay's step through the drop-in entry point: Apply in one
+        call (the three phases on host tiles and DrainAndCommitSecondaries'
+        transient FIFO, survivors back to the host), then the coupled fluid
+        and field update."""
         ctx.reset_current()
         ctx.reset_sources()
-        sec_e = timed("apply_electrons", ctx.apply_electrons, pe, step, DT_S, want_secondaries=True)
-        sec_g = timed("apply_photons", ctx.apply_photons, pg, step, DT_S, want_secondaries=True)
-        sec_p = timed("apply_positrons", ctx.apply_positrons, pp, step, DT_S, want_secondaries=True)
-        pending = np.concatenate([sec_e, sec_g, sec_p])
-        surv = timed("drain_secondaries", ctx.drain_secondaries, pending, step, DT_S)
+        surv = timed("apply_step", ctx.apply_step, pe, pg, pp, step, DT_S)
         timed("field_update", distributed.exchange_and_advance_coupled, ctx, dist, DT_S)
-        return len(pending), len(surv)
+        return 0, len(surv)
 
     e2e_moved = 0
     e2e_t = 0.0
@@ -554,7 +546,6 @@ def run_gb300(args, rank, world, local):
         step += 1
         if i < args.e2e_warmup:
             e2e_calls.clear()
-            e2e_kernels.clear()
             continue  # first use of the drop-in path's buffers, untimed
         e2e_t += time.perf_counter() - t0
         e2e_moved += live
@@ -659,10 +650,9 @@ def run_gb300(args, rank, world, local):
                     "d2h_bytes_per_step": d2h, "steps": args.e2e_steps, "warmup": args.e2e_warmup,
                     "ms_per_step": 1000.0 * e2e_t / max(args.e2e_steps, 1),
                     "calls_ms_per_step": {k: 1000.0 * v / max(args.e2e_steps, 1) for k, v in e2e_calls.items()},
-                    "phase_device_ms_per_step": {k: 1000.0 * v / max(args.e2e_steps, 1)
-                                                 for k, v in e2e_kernels.items()},
-                    "path": "rrea_gpu_apply_electrons/_photons/_positrons (pinned host tiles -> HBM -> host), "
-                            "rrea_gpu_drain_secondaries (host records in, survivors out), "
+
+                    "path": "rrea_gpu_apply_step (pinned host tiles -> HBM; the three phases and the transient "
+                            "FIFO on the device; tiles and FIFO-ordered survivors back to the host), "
                             "rrea_gpu_current_device + rrea_gpu_fluid_take_sources + "
                             "rrea_gpu_advance_field_coupled_from_current"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

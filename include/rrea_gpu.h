@@ -434,6 +434,24 @@ rrea_gpu_status rrea_gpu_resident_count(rrea_gpu_ctx* ctx, int32_t species, int6
  *   pending_secondaries: size of the resident queue; discard != 0 empties it.
  *   last_drain_stats:  FIFO items advanced and survivors of the last drain.
  */
+/*
+ * The whole of RreaParticleInteraction::Apply in one call
+ * (O/RreaParticleInteraction.cpp:12-62: the electron, photon and positron
+ * phases, then DrainAndCommitSecondaries, O/RreaSecondaryCommit.cpp:9-638,
+ * up to the survivors' AddNParticles): each host tile goes up, its phase
+ * runs as rrea_gpu_apply_* does, the phases' secondaries queue on the device
+ * in phase order and the transient FIFO drains them there (as
+ * rrea_gpu_drain_secondaries would over the concatenated secondaries), then
+ * the tiles come back and the survivors land in `survivors` in FIFO order.
+ * A NULL tile skips its species.  The caller's tiles and survivor buffer
+ * change only when every phase and the drain succeeded (fail closed); a
+ * survivor count above survivor_capacity is RREA_GPU_ERR_CAPACITY with
+ * *n_survivors set.  Results equal the per-phase calls followed by
+ * drain_secondaries; no secondary crosses to the host.
+ */
+rrea_gpu_status rrea_gpu_apply_step(rrea_gpu_ctx* ctx, rrea_gpu_tile* electrons, rrea_gpu_tile* photons,
+                                    rrea_gpu_tile* positrons, int32_t step, double time_s, double dt_s,
+                                    rrea_gpu_secondary* survivors, int64_t survivor_capacity, int64_t* n_survivors);
 rrea_gpu_status rrea_gpu_drain_secondaries(rrea_gpu_ctx* ctx, const rrea_gpu_secondary* pending,
                                            int64_t n_pending, int32_t step, double dt_s,
                                            rrea_gpu_secondary* survivors, int64_t survivor_capacity,

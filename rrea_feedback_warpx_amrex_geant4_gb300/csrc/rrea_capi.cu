@@ -1525,6 +1525,56 @@ rrea_gpu_status rrea_gpu_drain_secondaries(rrea_gpu_ctx* ctx, const rrea_gpu_sec
     return RREA_GPU_OK;
 }
 
+rrea_gpu_status rrea_gpu_apply_step(rrea_gpu_ctx* ctx, rrea_gpu_tile* electrons, rrea_gpu_tile* photons,
+                                    rrea_gpu_tile* positrons, int32_t step, double time_s, double dt_s,
+                                    rrea_gpu_secondary* survivors, int64_t survivor_capacity, int64_t* n_survivors)
+{
+    (void)time_s;
+    if (!ctx || survivor_capacity < 0 || (survivor_capacity > 0 && !survivors)) return RREA_GPU_ERR_ARGUMENT;
+    // Apply's phase order (O/RreaParticleInteraction.cpp:12-62)
+    struct Phase {
+        int species;
+        rrea_gpu_tile* tile;
+    } const phases[3] = {{RREA_SPECIES_ELECTRON, electrons}, {RREA_SPECIES_PHOTON, photons},
+                         {RREA_SPECIES_POSITRON, positrons}};
+    for (Phase const& ph : phases) {
+        if (!ph.tile) continue;
+        if (ph.tile->n < 0) return RREA_GPU_ERR_ARGUMENT;
+        rrea_gpu_status const s = check_tile(ctx, ph.tile);
+        if (s != RREA_GPU_OK) return s;
+    }
+    // the phases' secondaries queue on the device in phase order, and the
+    // transient FIFO drains them there: no secondary crosses to the host
+    ctx->fifo_pending = 0;
+    for (Phase const& ph : phases) {
+        if (!ph.tile) continue;
+        rrea_gpu_status s = launch_phase(ctx, ph.species, step, dt_s, /*aliased=*/false, ph.tile);
+        if (s == RREA_GPU_OK) s = queue_secondaries(ctx);
+        if (s != RREA_GPU_OK) {
+            ctx->fifo_pending = 0;
+            return s;
+        }
+    }
+    int64_t const n = ctx->fifo_pending;
+    ctx->fifo_pending = 0;
+    rrea_gpu_status s = drain_fifo(ctx, step, dt_s, n);
+    if (s != RREA_GPU_OK) return s;
+    if (n_survivors) *n_survivors = ctx->n_surv;
+    if (ctx->n_surv > survivor_capacity) return fail(ctx, RREA_GPU_ERR_CAPACITY, "caller survivor buffer too small");
+    // every guard passed: only now do the caller's tiles change
+    for (Phase const& ph : phases) {
+        if (!ph.tile) continue;
+        s = unstage_tile(ctx, ph.species, ph.tile);
+        if (s != RREA_GPU_OK) return s;
+    }
+    if (ctx->n_surv > 0) {
+        RREA_CUDA(ctx, cudaMemcpyAsync(survivors, ctx->d_surv, static_cast<size_t>(ctx->n_surv) * sizeof(rrea_gpu_secondary),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    RREA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RREA_GPU_OK;
+}
+
 rrea_gpu_status rrea_gpu_drain_resident(rrea_gpu_ctx* ctx, int32_t step, double dt_s, int64_t* n_survivors)
 {
     if (!ctx) return RREA_GPU_ERR_ARGUMENT;

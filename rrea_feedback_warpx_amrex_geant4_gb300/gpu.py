@@ -121,7 +121,7 @@ EXPORTED_SYMBOLS = (
     "rrea_gpu_seed_schedule_events", "rrea_gpu_seed_schedule_validate", "rrea_gpu_seed_schedule_last_error",
     "rrea_gpu_inject_seeds_resident", "rrea_gpu_thin_cic_groups", "rrea_gpu_census_resident",
     "rrea_gpu_deposit_charge_resident", "rrea_gpu_population_thin_resident", "rrea_gpu_population_split_resident",
-    "rrea_gpu_population_merge_resident",
+    "rrea_gpu_population_merge_resident", "rrea_gpu_apply_step",
     "rrea_gpu_default_fluid_config", "rrea_gpu_fluid_configure", "rrea_gpu_fluid_load_closure",
     "rrea_gpu_fluid_set_state", "rrea_gpu_fluid_get_state", "rrea_gpu_fluid_set_source_rates",
     "rrea_gpu_fluid_get_source_rates", "rrea_gpu_fluid_set_density_ratio", "rrea_gpu_fluid_set_closure_fields",
@@ -207,6 +207,8 @@ def load_library(path=LIB_PATH):
                                                       ctypes.c_uint64, vp, ctypes.c_int64, _i64p]
     lib.rrea_gpu_population_split_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_double, _i64p]
     lib.rrea_gpu_population_merge_resident.argtypes = [vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _i64p]
+    lib.rrea_gpu_apply_step.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                        ctypes.c_double, ctypes.c_double, vp, ctypes.c_int64, _i64p]
     lib.rrea_gpu_census_resident.argtypes = [vp, ctypes.c_int32, _D, ctypes.c_int32, _D, ctypes.c_int32, _D]
     lib.rrea_gpu_resident_count.argtypes = [vp, ctypes.c_int32, _i64p]
     lib.rrea_gpu_last_drain_stats.argtypes = [vp, _i64p, _i64p]
@@ -384,6 +386,7 @@ class RreaGpuContext:
         # the drop-in phases' secondaries land here (reused: its pages are
         # mapped once, not on every call); callers get a copy of the filled part
         self._sec_buf = None
+        self._surv_buf = None
         handle = ctypes.c_void_p()
         self._check(self.lib.rrea_gpu_create(ctypes.byref(config), self.capacity, ctypes.byref(handle)), None)
         self.handle = handle
@@ -480,6 +483,21 @@ class RreaGpuContext:
         """Drop-in electron phase on host arrays (modified in place).
         Returns the ordered secondaries as a structured array."""
         return self._apply(self.lib.rrea_gpu_apply_electrons, arrays, step, dt_s, time_s, want_secondaries)
+
+    def apply_step(self, electrons, photons, positrons, step, dt_s, time_s=0.0):
+        """Apply in one call: the three phases on host tiles (modified in
+        place; None skips a species) and the transient FIFO of their
+        secondaries on the device.  Returns the survivors in FIFO order."""
+        tiles = [tile_struct(a) if a is not None else None for a in (electrons, photons, positrons)]
+        refs = [ctypes.byref(t) if t is not None else None for t in tiles]
+        cap = 2 * self.capacity + 4096
+        if self._surv_buf is None or len(self._surv_buf) < cap:
+            self._surv_buf = np.empty(cap, dtype=SECONDARY_DTYPE)
+        n = ctypes.c_int64()
+        self._check(self.lib.rrea_gpu_apply_step(self.handle, refs[0], refs[1], refs[2], int(step), float(time_s),
+                                                 float(dt_s), ctypes.c_void_p(self._surv_buf.ctypes.data), cap,
+                                                 ctypes.byref(n)))
+        return self._surv_buf[: n.value].copy()
 
     def apply_positrons(self, arrays, step, dt_s, time_s=0.0, want_secondaries=True):
         """Drop-in positron phase on host arrays (modified in place)."""
