@@ -100,3 +100,17 @@ def test_library_leaves_no_internal_symbol_undefined(gpu):
     out = subprocess.run([nm, "-D", "--undefined-only", gpu.LIB_PATH], capture_output=True, text=True, check=True)
     internal = [line for line in out.stdout.splitlines() if "rrea" in line]
     assert not internal, internal
+
+
+def test_one_call_apply_and_merge_refuse_bad_arguments(gpu):
+    """rrea_gpu_apply_step and rrea_gpu_population_merge_resident check their
+    arguments before any device work: a null context (or a negative survivor
+    capacity) is RREA_GPU_ERR_ARGUMENT, on a box without a GPU too."""
+    lib = gpu.load_library()
+    n = ctypes.c_int64()
+    stats = (ctypes.c_int64 * 5)()
+    arg = 1  # RREA_GPU_ERR_ARGUMENT
+    assert lib.rrea_gpu_apply_step(None, None, None, None, 0, 0.0, 5e-10, None, 0, ctypes.byref(n)) == arg
+    assert lib.rrea_gpu_apply_step(None, None, None, None, 0, 0.0, 5e-10, None, -1, ctypes.byref(n)) == arg
+    assert lib.rrea_gpu_population_merge_resident(None, 0, 10, 0, stats) == arg
+    assert lib.rrea_gpu_population_merge_resident(None, 0, -1, 0, stats) == arg
