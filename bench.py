@@ -26,6 +26,8 @@ one dt, its newborn residual legs included.  Synthetic seeds; no dataset.
               r,z,theta,ux,uy,uz,w,id, write r,z,theta,ux,uy,uz)
   cpu_baseline the oracle (CPU restatement, all host threads) on a bounded
               sample of the same workload
+  scaleup_run the scale-up case run from its seeds with field feedback and
+              the merge cap (800 steps, host wall clock)
   profiled_atmosphere  the largest case's geometry (512x4096 cells, 6-14 km,
               density profile, altitude-dependent E_z) with an entering
               column of 2e6 e- and 5e5 e+ and the coupled fluid update
@@ -77,6 +79,8 @@ def parse():
     p.add_argument("--ensemble-scale", type=float, default=0.05,
                    help="duration scale of the batched 64-instance ensemble line (0: skip it)")
     p.add_argument("--adjoint-steps", type=int, default=2000, help="steps of the adjoint line (0: skip it)")
+    p.add_argument("--c1-run-steps", type=int, default=800,
+                   help="steps of the scale-up avalanche run line (0: skip it)")
     p.add_argument("--profiled-steps", type=int, default=8,
                    help="timed steps of the profiled-atmosphere line (0: skip it)")
     p.add_argument("--threads", type=int, default=128)
@@ -578,6 +582,38 @@ def run_gb300(args, rank, world, local):
               "final_electrons": res["history"][-1]["electron_count"],
               "timing": "host wall clock around the steps (each step ends in a stream synchronisation)"}
 
+    # ---- the scale-up case run from its seeds: 1e5 electrons (K log-uniform
+    # 1-20 MeV), field feedback through the coupled carrier fluid, every step
+    # committed, each species capped at 1e6 macroparticles by the
+    # weight-doubling merge
+    c1_run = None
+    if rank == 0 and world == 1 and args.c1_run_steps > 0:
+        from rrea_feedback_warpx_amrex_geant4_gb300 import avalanche
+
+        try:
+            run_ctx = avalanche.make_context(CASE, 3_000_000, 1, blocks_per_sm=args.blocks_per_sm)
+            try:
+                run_ctx.fluid_configure(**workloads.fluid_overrides())
+                run_ctx.fluid_load_closure(DEFAULT_CLOSURE)
+                res = avalanche.AvalancheRun(run_ctx, workloads.make_electrons(CASE, 100_000), feedback=True,
+                                             fluid=True, merge_cap=1_000_000).run(args.c1_run_steps,
+                                                                                 census_every=args.c1_run_steps)
+            finally:
+                run_ctx.close()
+            last = res["history"][-1]
+            c1_run = {"workload": f"scale-up case from its 1e5 seeds (K log-uniform 1-20 MeV), field feedback through the "
+                                  f"coupled carrier fluid, {args.c1_run_steps} steps of 0.5 ns, every step committed, each "
+                                  f"species capped at 1e6 macroparticles by the weight-doubling merge",
+                      "value": res["particle_steps_per_s"], "unit": "particle-steps/s",
+                      "ms_per_step": 1000.0 * res["wall_s"] / args.c1_run_steps,
+                      "particle_steps": res["particle_steps"], "merged": res["population_merged"],
+                      "multiplication": res["multiplication"],
+                      "final": {"electrons": last["electron_count"], "electron_weight": last["electron_weight"],
+                                "photons": last["photon_count"], "positrons": last["positron_count"]},
+                      "timing": "host wall clock around the steps (each step ends in a stream synchronisation)"}
+        except gpu.RreaGpuError as exc:  # reported in the line, the headline stands
+            c1_run = {"error": str(exc)}
+
     # ---- the profiled atmosphere (the largest case's geometry): 512x4096
     # cells over r 0-1 km and altitudes 6-14 km, density 1.225 exp(-h/7.2 km)
     # bound as the transport's altitude profile, E_z peaking at 1.3 x the
@@ -677,6 +713,7 @@ def run_gb300(args, rank, world, local):
                                        f"{args.cpu_baseline_steps} steps of the same whole kinetic step "
                                        f"({cpu_moved} particle-steps in {cpu_t:.1f} s), OpenMP chunks of 64, -O3"},
             "small_population": c0,
+            "scaleup_run": c1_run,
             "profiled_atmosphere": profiled,
             "batched": batched,
             "adjoint": adjoint_line,
