@@ -634,7 +634,7 @@ def run_gb300(args, rank, world, local):
     if rank == 0 and world == 1 and args.ensemble_scale > 0:
         from rrea_feedback_warpx_amrex_geant4_gb300 import ensemble
 
-        inst = ensemble.config3_instances(64, duration_scale=args.ensemble_scale)
+        inst = ensemble.batched_instances(64, duration_scale=args.ensemble_scale)
         b = ensemble.run_batched(inst, control_every=16)
         q = ensemble.run_sequential(inst, control_every=16)
         same = all(x["multiplication"] == y["multiplication"] and x["electron_count"] == y["electron_count"]

@@ -15,7 +15,7 @@ the cutoff stop at the same substep), and the loss
 (a smoothed runaway count plus the smoothed net charge that crossed the
 plane z_p, which is the time integral of J_z through it).
 
-`config4_profile` draws the batched adjoint configuration's field: E_z on
+`adjoint_field_profile` draws the adjoint configuration's field: E_z on
 256 nodes over 0-500 m, 450 kV/m plus a Gaussian-correlated perturbation
 (sigma 20 kV/m, correlation length 20 m), seeded, pointing along -z."""
 import ctypes
@@ -67,7 +67,7 @@ def default_config(**overrides):
     return c
 
 
-def config4_profile(n_nodes=256, z_hi=500.0, base=4.5e5, sigma=2.0e4, length=20.0, seed=4):
+def adjoint_field_profile(n_nodes=256, z_hi=500.0, base=4.5e5, sigma=2.0e4, length=20.0, seed=4):
     """E_z on the nodes: -(base + a seeded Gaussian-correlated perturbation)."""
     z = np.linspace(0.0, z_hi, n_nodes)
     cov = sigma * sigma * np.exp(-0.5 * ((z[:, None] - z[None, :]) / length) ** 2)
@@ -76,7 +76,7 @@ def config4_profile(n_nodes=256, z_hi=500.0, base=4.5e5, sigma=2.0e4, length=20.
     return -(base + chol @ rng.standard_normal(n_nodes))
 
 
-def config4_seeds(n, seed=11):
+def adjoint_seeds(n, seed=11):
     """The plain case's seeds (7.2 MeV along +z from the origin)."""
     t = workloads.make_electrons("uniform_c0", n, seed=seed)
     k = np.full(n, 7.2e6)
@@ -180,18 +180,19 @@ def central_differences(problem, e_nodes, nodes, h=1.0):
 
 
 def measure(n=1_000_000, repeats=2, **overrides):
-    """Seconds per gradient of the batched adjoint configuration (config4
-    profile and seeds, the default adjoint config: 2000 steps of 0.5 ns in 4
-    substeps, checkpoints every 32 steps): one recording forward plus the
-    reverse pass, timed after one untimed gradient; returns a dict."""
+    """Seconds per gradient of the adjoint configuration (the perturbed
+    field profile and the 7.2 MeV seeds, the default adjoint config: 2000
+    steps of 0.5 ns in 4 substeps, checkpoints every 32 steps): one recording
+    forward plus the reverse pass, timed after one untimed gradient; returns
+    a dict."""
     import time
 
     import torch
 
     cfg = default_config(**overrides)
-    prob = PushAdjoint(cfg, config4_seeds(n))
+    prob = PushAdjoint(cfg, adjoint_seeds(n))
     try:
-        e = torch.tensor(config4_profile(n_nodes=cfg.n_nodes, z_hi=cfg.z_hi), dtype=torch.float64, device="cuda")
+        e = torch.tensor(adjoint_field_profile(n_nodes=cfg.n_nodes, z_hi=cfg.z_hi), dtype=torch.float64, device="cuda")
         prob.forward(e)
         prob.backward(e)
         torch.cuda.synchronize()
@@ -219,7 +220,7 @@ if __name__ == "__main__":
     import argparse
     import json
 
-    p = argparse.ArgumentParser(description="seconds per gradient of the batched adjoint configuration")
+    p = argparse.ArgumentParser(description="seconds per gradient of the adjoint configuration")
     p.add_argument("--electrons", type=int, default=1_000_000)
     p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--repeats", type=int, default=2)

@@ -18,7 +18,7 @@ blocks per SM, i.e. block shape and particles per thread) and the
 scheduling order of the charged tiles (the per-step sort by |u|) are picked
 by `autotune`, which times live steps: no result depends on them.
 
-Instances of BASELINE's batched configuration come from `config3_instances`:
+Instances of the batched configuration come from `batched_instances`:
 E_z evenly spaced 300-1000 kV/m, seed counts log-uniform 1e3-1e5 (seeded),
 durations mapped linearly in 1/(E - 280 kV/m) onto 0.5-4 us, the air,
 tables, grid and seeds of the plain uniform-field case."""
@@ -44,7 +44,7 @@ class Instance:
     target: int = 0        # per-species population target of the thinning (0: none)
 
 
-def config3_instances(n=64, seed=7, duration_scale=1.0, target=0):
+def batched_instances(n=64, seed=7, duration_scale=1.0, target=0):
     """The batched configuration: n instances; durations scaled by
     duration_scale (1 = 0.5-4 us); target > 0 adds a per-instance population
     control (the configuration itself has none)."""
@@ -239,7 +239,7 @@ def main():
     p.add_argument("--sequential", action="store_true", help="also run the instances one by one")
     p.add_argument("--json", default=None)
     args = p.parse_args()
-    inst = config3_instances(args.instances, duration_scale=args.duration_scale, target=args.target)
+    inst = batched_instances(args.instances, duration_scale=args.duration_scale, target=args.target)
     t0 = time.perf_counter()
     batched = run_batched(inst, control_every=args.control_every)
     t_b = time.perf_counter() - t0

@@ -7,9 +7,9 @@ onto 0.5-4 us) and the adjoint's field profile (256 nodes over 0-500 m,
 import numpy as np
 
 
-def test_config3_instances():
+def test_batched_instances():
     from rrea_feedback_warpx_amrex_geant4_gb300 import ensemble
-    inst = ensemble.config3_instances(64)
+    inst = ensemble.batched_instances(64)
     e = np.array([i.field_v_per_m for i in inst])
     np.testing.assert_allclose(np.diff(e), (1.0e6 - 3.0e5) / 63)
     seeds = np.array([i.n_seeds for i in inst])
@@ -17,7 +17,7 @@ def test_config3_instances():
     steps = np.array([i.steps for i in inst])
     assert steps.max() == 8000 and steps.min() == 1000          # 4 us and 0.5 us at 0.5 ns
     assert np.all(np.diff(steps) <= 0)                          # shorter runs in stronger fields
-    assert ensemble.config3_instances(64, seed=7)[5].n_seeds == inst[5].n_seeds
+    assert ensemble.batched_instances(64, seed=7)[5].n_seeds == inst[5].n_seeds
 
 
 def test_ensemble_seed_tile_marks_instances():
@@ -30,13 +30,13 @@ def test_ensemble_seed_tile_marks_instances():
     np.testing.assert_array_equal(only["cpu"], [1, 1])
 
 
-def test_config4_profile():
+def test_adjoint_field_profile():
     from rrea_feedback_warpx_amrex_geant4_gb300 import adjoint
-    e = adjoint.config4_profile()
+    e = adjoint.adjoint_field_profile()
     assert e.shape == (256,)
     assert np.all(e < 0)                                        # along -z
     dev = -e - 4.5e5
     assert 5e3 < dev.std() < 4e4
     # neighbouring nodes (1.96 m apart) are strongly correlated at 20 m
     assert np.corrcoef(dev[:-1], dev[1:])[0, 1] > 0.9
-    np.testing.assert_array_equal(adjoint.config4_profile(), e)   # seeded
+    np.testing.assert_array_equal(adjoint.adjoint_field_profile(), e)   # seeded

@@ -4,7 +4,7 @@ differences with common random numbers, and its forward against a numpy
 restatement of the same model.
 
 Problem: 3000 electrons of 0.3-20 MeV (a tenth of them against the field,
-so some stop at the cutoff) in the batched adjoint configuration's field
+so some stop at the cutoff) in the adjoint configuration's field
 profile (256 nodes over 0-500 m, 450 kV/m plus a correlated 20 kV/m
 perturbation), 96 steps of 0.5 ns in 2 substeps, checkpoints every 32 steps;
 the runaway threshold at 8 MeV (50 keV wide) and the crossing plane at 12 m
@@ -54,7 +54,7 @@ def problem():
     cfg = adjoint.default_config(steps=96, substeps=2, checkpoint_every=32, k_threshold_eV=8.0e6,
                                  z_plane_m=12.0, density_ratio=1.225 / 1.20479)
     prob = adjoint.PushAdjoint(cfg, seeds, tables=TABLES)
-    e = torch.tensor(adjoint.config4_profile(), dtype=torch.float64, device="cuda")
+    e = torch.tensor(adjoint.adjoint_field_profile(), dtype=torch.float64, device="cuda")
     yield adjoint, prob, e, seeds, cfg
     prob.close()
 
