@@ -73,7 +73,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--population", type=int, default=1 << 21)
     p.add_argument("--cpu-baseline-steps", type=int, default=3)
-    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--e2e-warmup", type=int, default=1, help="untimed drop-in steps before the timed e2e steps")
     p.add_argument("--c0-steps", type=int, default=1000)
     p.add_argument("--ensemble-scale", type=float, default=0.05,
