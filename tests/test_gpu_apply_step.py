@@ -11,7 +11,9 @@ Case: scale-up tiles of 4096 electrons, 2048 photons (50 keV-20 MeV) and
     holds the same items in the same order;
   * cell sources within 16e-12 of each grid's largest cell (FP64 atomics in
     arbitrary order), net-chord currents within 1e-12 of their largest face;
-  * a NULL tile skips its species."""
+  * a NULL tile skips its species;
+  * a survivor buffer too small is RREA_GPU_ERR_CAPACITY and leaves the
+    caller's tiles and buffer untouched (fail closed)."""
 import numpy as np
 import pytest
 
@@ -95,3 +97,29 @@ def test_apply_step_skips_null_tiles(mods):
     finally:
         a.close()
         b.close()
+
+
+def test_apply_step_fails_closed_on_a_short_survivor_buffer(mods):
+    """A survivor buffer too small for the step's survivors is
+    RREA_GPU_ERR_CAPACITY with the count reported, and the caller's tiles
+    stay as they were (nothing is written back before every stage passed)."""
+    import ctypes
+    gpu, workloads = mods
+    e, g, p = _inputs(workloads)
+    ctx = _context(gpu, workloads)
+    try:
+        eb, gb, pb = (workloads.copy_tile(t) for t in (e, g, p))
+        tiles = [gpu.tile_struct(t) for t in (eb, gb, pb)]
+        buf = np.zeros(4, dtype=gpu.SECONDARY_DTYPE)
+        n = ctypes.c_int64()
+        st = ctx.lib.rrea_gpu_apply_step(ctx.handle, ctypes.byref(tiles[0]), ctypes.byref(tiles[1]),
+                                         ctypes.byref(tiles[2]), STEP, 0.0, DT, ctypes.c_void_p(buf.ctypes.data), 4,
+                                         ctypes.byref(n))
+        assert st == 8  # RREA_GPU_ERR_CAPACITY
+        assert n.value > 4
+        for name, x, y in (("electrons", e, eb), ("photons", g, gb), ("positrons", p, pb)):
+            for key in x:
+                np.testing.assert_array_equal(x[key], y[key], err_msg=f"{name} {key}")
+        assert not buf.tobytes().strip(b"\0")
+    finally:
+        ctx.close()
