@@ -123,6 +123,11 @@ struct rrea_gpu_ctx {
     cudaStream_t side[2] = {nullptr, nullptr};
     cudaEvent_t fork_ev = nullptr;
     cudaEvent_t roots_ev = nullptr;  // the initial FIFO items' roots have reached the host
+    // rrea_gpu_apply_step: host tiles of later phases uploaded on side[0]
+    // behind a chunked electron tile's uploads, while its kernels run
+    rrea_gpu_tile const* prefetch[kSpecies] = {nullptr, nullptr, nullptr};
+    bool prefetched[kSpecies] = {false, false, false};
+    cudaEvent_t prefetch_ev = nullptr;
     cudaEvent_t join_ev[2] = {nullptr, nullptr};
     int num_sms = 0;
 
@@ -355,6 +360,9 @@ rrea_gpu_status rrea_gpu_create(const rrea_gpu_config* cfg, int64_t capacity, rr
     }
     if (cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bail(RREA_GPU_ERR_CUDA);
     if (cudaEventCreateWithFlags(&ctx->roots_ev, cudaEventDisableTiming) != cudaSuccess) return bail(RREA_GPU_ERR_CUDA);
+    if (cudaEventCreateWithFlags(&ctx->prefetch_ev, cudaEventDisableTiming) != cudaSuccess) {
+        return bail(RREA_GPU_ERR_CUDA);
+    }
     for (int k = 0; k < kPhaseChunks; ++k) {
         if (cudaEventCreateWithFlags(&ctx->chunk_up[k], cudaEventDisableTiming) != cudaSuccess
             || cudaEventCreateWithFlags(&ctx->chunk_done[k], cudaEventDisableTiming) != cudaSuccess) {
@@ -497,6 +505,7 @@ rrea_gpu_status rrea_gpu_destroy(rrea_gpu_ctx* ctx)
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
     if (ctx->roots_ev) cudaEventDestroy(ctx->roots_ev);
+    if (ctx->prefetch_ev) cudaEventDestroy(ctx->prefetch_ev);
     for (int k = 0; k < kPhaseChunks; ++k) {
         if (ctx->chunk_up[k]) cudaEventDestroy(ctx->chunk_up[k]);
         if (ctx->chunk_done[k]) cudaEventDestroy(ctx->chunk_done[k]);
@@ -905,8 +914,14 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
 #endif
     RREA_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
     if (host && chunks == 1) {
-        rrea_gpu_status const s = upload_range(ctx, st, host, 0, a.n, ctx->stream);
-        if (s != RREA_GPU_OK) return s;
+        if (ctx->prefetched[species]) {
+            // already uploaded behind the electron tile (rrea_gpu_apply_step)
+            ctx->prefetched[species] = false;
+            RREA_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->prefetch_ev, 0));
+        } else {
+            rrea_gpu_status const s = upload_range(ctx, st, host, 0, a.n, ctx->stream);
+            if (s != RREA_GPU_OK) return s;
+        }
     }
 #ifndef RREA_STATIC_SCHEDULE
     // a charged tile on the device in one piece is visited in its
@@ -971,6 +986,18 @@ rrea_gpu_status launch_phase(rrea_gpu_ctx* ctx, int species, int32_t step, doubl
         if (chunks > 1) RREA_CUDA(ctx, cudaEventRecord(ctx->chunk_done[k], cs));
     }
     if (chunks > 1) {
+        // later phases' tiles go up behind this tile's chunks, under its kernels
+        bool any = false;
+        for (int sp = 0; sp < kSpecies; ++sp) {
+            rrea_gpu_tile const* t = ctx->prefetch[sp];
+            if (!t || sp == species) continue;
+            ctx->prefetch[sp] = nullptr;
+            rrea_gpu_status const s = upload_range(ctx, ctx->tiles[sp], t, 0, t->n, ctx->side[0]);
+            if (s != RREA_GPU_OK) return s;
+            ctx->prefetched[sp] = true;
+            any = true;
+        }
+        if (any) RREA_CUDA(ctx, cudaEventRecord(ctx->prefetch_ev, ctx->side[0]));
         RREA_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->chunk_done[chunks - 1], 0));
         RREA_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->chunk_done[chunks - 2], 0));
     }
@@ -1546,15 +1573,34 @@ rrea_gpu_status rrea_gpu_apply_step(rrea_gpu_ctx* ctx, rrea_gpu_tile* electrons,
     // the phases' secondaries queue on the device in phase order, and the
     // transient FIFO drains them there: no secondary crosses to the host
     ctx->fifo_pending = 0;
+    // photon and positron tiles that go up in one piece are uploaded under a
+    // chunked electron phase's kernels
+    if (electrons && electrons->n >= kPipelineMinParticles) {
+        for (Phase const& ph : phases) {
+            if (ph.tile && ph.species != RREA_SPECIES_ELECTRON && ph.tile->n > 0
+                && (ph.species == RREA_SPECIES_PHOTON || ph.tile->n < kPipelineMinParticles)) {
+                ctx->prefetch[ph.species] = ph.tile;
+            }
+        }
+    }
+    auto clear_prefetch = [&]() {
+        for (int sp = 0; sp < kSpecies; ++sp) {
+            ctx->prefetch[sp] = nullptr;
+            ctx->prefetched[sp] = false;
+        }
+    };
     for (Phase const& ph : phases) {
         if (!ph.tile) continue;
         rrea_gpu_status s = launch_phase(ctx, ph.species, step, dt_s, /*aliased=*/false, ph.tile);
         if (s == RREA_GPU_OK) s = queue_secondaries(ctx);
         if (s != RREA_GPU_OK) {
             ctx->fifo_pending = 0;
+            clear_prefetch();
+            cudaStreamSynchronize(ctx->side[0]);
             return s;
         }
     }
+    clear_prefetch();
     int64_t const n = ctx->fifo_pending;
     ctx->fifo_pending = 0;
     rrea_gpu_status s = drain_fifo(ctx, step, dt_s, n);
